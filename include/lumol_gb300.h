@@ -1,0 +1,219 @@
+/*
+ * lumol_gb300.h -- C ABI of the GB300 force / energy / integration engine for Lumol.
+ *
+ * One engine handle owns the device state of one or more independent systems
+ * (a "batch"; a Lumol `System` is a batch of one).  All host arrays are owned
+ * by the caller and copied in and out; device memory belongs to the handle
+ * until lg_destroy.  Every function returns LG_OK (0) or an LG_ERR_* status;
+ * lg_last_error() gives the message.  A handle is not re-entrant: callers
+ * serialise access to it (Lumol's SharedEwald does the same with a RwLock,
+ * lumol-core/src/energy/global/ewald.rs:847-875).  Distinct handles may be used
+ * from different threads.
+ *
+ * Units are Lumol's internal units (lumol-core/src/units.rs:4-16): Angstrom,
+ * femtosecond, unified atomic mass, Kelvin, and 1e-4 kJ/mol for energy.
+ *
+ * Arrays of vectors are 3*n doubles, x y z per atom, the layout of
+ * `&[Vector3D]` (lumol-core/src/types/vectors.rs:59).  A virial is 9 doubles,
+ * row-major, the layout of `Matrix3` (lumol-core/src/types/matrix.rs:73).
+ */
+#ifndef LUMOL_GB300_H
+#define LUMOL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LG_ABI_VERSION 1
+
+/* ---- status codes --------------------------------------------------------- */
+enum {
+    LG_OK = 0,
+    LG_ERR_ARGUMENT = 1,  /* invalid argument; the reference panics in the same cases */
+    LG_ERR_CUDA = 2,      /* a CUDA runtime call failed */
+    LG_ERR_STATE = 3,     /* call out of order (e.g. compute before set_cell) */
+    LG_ERR_CAPACITY = 4,  /* a device list overflowed and could not be regrown */
+    LG_ERR_NONFINITE = 5, /* a non-finite energy was produced (compute.rs:125) */
+    LG_ERR_NO_DEVICE = 6  /* no CUDA device is visible: there is no CPU fallback */
+};
+
+/* ---- enumerations mirroring the reference --------------------------------- */
+/* Pair potentials (lumol-core/src/energy/functions.rs). */
+enum {
+    LG_PAIR_ABSENT = 0,     /* no PairInteraction for this kind pair */
+    LG_PAIR_NULL = 1,       /* NullPotential (functions.rs:29-50) */
+    LG_PAIR_LJ = 2,         /* LennardJones {sigma, epsilon} (functions.rs:71-107) */
+    LG_PAIR_BUCKINGHAM = 3, /* Buckingham {a, c, rho} (functions.rs:276-319) */
+    LG_PAIR_HARMONIC = 4    /* Harmonic {k, x0} (functions.rs:127-160) */
+};
+
+/* PairRestriction (lumol-core/src/energy/restrictions.rs:13-33). */
+enum {
+    LG_RESTRICT_NONE = 0,
+    LG_RESTRICT_INTRA = 1,
+    LG_RESTRICT_INTER = 2,
+    LG_RESTRICT_EXCLUDE12 = 3,
+    LG_RESTRICT_EXCLUDE13 = 4,
+    LG_RESTRICT_EXCLUDE14 = 5,
+    LG_RESTRICT_SCALE14 = 6
+};
+
+/* Coulombic potentials (energy/global/ewald.rs, energy/global/wolf.rs). */
+enum { LG_COULOMB_NONE = 0, LG_COULOMB_EWALD = 1, LG_COULOMB_WOLF = 2 };
+
+/* Arithmetic of the force path. */
+enum {
+    LG_PRECISION_FP64 = 0,  /* reference arithmetic in FP64, pair sets bit-exact */
+    LG_PRECISION_MIXED = 1  /* FP32 pair / Ewald arithmetic with compensated per-atom
+                               force sums; FP64 energies, virials, rho(k) and x/v state */
+};
+
+/* Energy / force / virial terms (bit mask). */
+enum {
+    LG_TERM_PAIRS = 1,          /* EnergyEvaluator::pairs (sys/energy.rs:47-59) */
+    LG_TERM_TAIL = 2,           /* EnergyEvaluator::pairs_tail (sys/energy.rs:63-79) */
+    LG_TERM_BONDS = 4,          /* bonds (sys/energy.rs:90-100) */
+    LG_TERM_ANGLES = 8,         /* angles (sys/energy.rs:110-120) */
+    LG_TERM_COUL_REAL = 16,     /* Ewald real space, or the whole Wolf sum */
+    LG_TERM_COUL_SELF = 32,     /* Ewald self energy (ewald.rs:619-626) */
+    LG_TERM_COUL_KSPACE = 64,   /* Ewald k-space (ewald.rs:677-733) */
+    LG_TERM_ALL = 127
+};
+
+/* Quantities (bit mask). */
+enum { LG_WANT_FORCES = 1, LG_WANT_ENERGY = 2, LG_WANT_VIRIAL = 4 };
+
+/* ---- descriptors ---------------------------------------------------------- */
+/* One PairInteraction (lumol-core/src/energy/pairs.rs:57-95). */
+typedef struct {
+    int32_t type;         /* LG_PAIR_* */
+    int32_t shifted;      /* 1: PairInteraction::shifted (energy shifted, force not) */
+    int32_t restriction;  /* LG_RESTRICT_* */
+    int32_t tail;         /* 1: enable_tail_corrections */
+    double p0, p1, p2;    /* LJ: sigma, epsilon; Buckingham: a, c, rho; Harmonic: k, x0 */
+    double cutoff;
+    double scale14;       /* factor of LG_RESTRICT_SCALE14 */
+} lg_pair;
+
+/* A bond or angle potential (Harmonic or Null). */
+typedef struct {
+    int32_t type;  /* LG_PAIR_ABSENT, LG_PAIR_NULL or LG_PAIR_HARMONIC */
+    int32_t pad;
+    double k, x0;
+} lg_bonded;
+
+/* Ewald::new(cutoff, kmax, alpha) (ewald.rs:278-305) or Wolf::new(cutoff) (wolf.rs:68-84). */
+typedef struct {
+    int32_t kind;         /* LG_COULOMB_* */
+    int32_t restriction;  /* CoulombicPotential::set_restriction (global/mod.rs:197-202) */
+    int32_t kmax;         /* Ewald only, > 0 */
+    int32_t pad;
+    double cutoff;
+    double alpha;         /* Ewald only; <= 0 selects the default PI / cutoff */
+    double scale14;
+} lg_coulomb;
+
+/* Engine options. */
+typedef struct {
+    int32_t device;      /* CUDA device ordinal */
+    int32_t precision;   /* LG_PRECISION_* */
+    double skin;         /* Verlet-list skin in Angstrom (0: default 1.0) */
+} lg_options;
+
+typedef struct lg_engine lg_engine;
+
+/* ---- lifetime --------------------------------------------------------------- */
+int lg_version(void);
+/* Message of the last failure on `engine` (or of the last failed lg_create when NULL). */
+const char* lg_last_error(const lg_engine* engine);
+
+/* Creates an engine with `n_systems` independent systems (1 for a Lumol System). */
+int lg_create(const lg_options* options, int32_t n_systems, lg_engine** engine);
+void lg_destroy(lg_engine* engine);
+
+/* ---- system description (per system index `s`) ----------------------------- */
+/* UnitCell::ortho / cubic (cells.rs:51-66): `matrix` is the 3x3 cell, row-major;
+ * only orthorhombic cells are accepted.  Replaces setting `System::cell`. */
+int lg_set_cell(lg_engine* e, int32_t s, const double matrix[9]);
+
+/* Particles of system `s` (Configuration, sys/config/configuration.rs:42-51):
+ * kinds index the pair table, molecules give each atom's molecule index
+ * (atoms of a molecule are contiguous, as in Lumol). */
+int lg_set_particles(lg_engine* e, int32_t s, int64_t n, const int32_t* kinds,
+                     const double* charges, const double* masses, const int32_t* molecules);
+
+/* Bonds (i, j) and angles (i, j, k) of system `s` with their potentials
+ * (Molecule::bonds/angles with System::bond_potential / angle_potential,
+ * sys/system.rs:185-204).  Bond paths for restrictions are derived from the
+ * bonds as Bonding::rebuild does (sys/config/bonding.rs:78-186). */
+int lg_set_bonds(lg_engine* e, int32_t s, int64_t n_bonds, const int32_t* bonds,
+                 const lg_bonded* potentials);
+int lg_set_angles(lg_engine* e, int32_t s, int64_t n_angles, const int32_t* angles,
+                  const lg_bonded* potentials);
+
+/* Pair table of system `s`: n_kinds^2 entries, symmetric, replacing
+ * System::set_pair_potential (sys/system.rs:122-131).  Fails like the
+ * reference when a cutoff exceeds half the smallest cell length. */
+int lg_set_pairs(lg_engine* e, int32_t s, int32_t n_kinds, const lg_pair* table);
+
+/* Coulomb potential of system `s`, replacing System::set_coulomb_potential
+ * (sys/system.rs:159-170) with SharedEwald or Wolf. */
+int lg_set_coulomb(lg_engine* e, int32_t s, const lg_coulomb* coulomb);
+
+/* ---- forces, energy, virial ---------------------------------------------- */
+/* Computes the requested quantities of system `s` at `positions` (3n, host).
+ * forces (3n, host) are ACCUMULATED into, as GlobalPotential::forces does
+ * (global/mod.rs:84-105); energy and virial are written.  Any output may be
+ * NULL when not requested.  Replaces Forces / PotentialEnergy / AtomicVirial
+ * (sys/compute.rs:30-255) and the GlobalPotential methods of Ewald / Wolf. */
+int lg_compute(lg_engine* e, int32_t s, const double* positions, uint32_t terms, uint32_t want,
+               double* forces, double* energy, double virial[9]);
+
+/* Same for every system of the engine, on device pointers: d_positions and
+ * d_forces hold 3*N_total doubles (systems in index order, forces overwritten),
+ * d_energy n_systems doubles and d_virial 9*n_systems doubles.  `stream` is a
+ * cudaStream_t (NULL: the engine's stream). */
+int lg_compute_device(lg_engine* e, const double* d_positions, uint32_t terms, uint32_t want,
+                      double* d_forces, double* d_energy, double* d_virial, void* stream);
+
+/* Pair set of family 0 (pair potentials: r < cutoff, not excluded) or 1
+ * (real-space Coulomb: r <= cutoff, q_i q_j != 0) at `positions`, as the
+ * device kernels see it.  Writes up to `capacity` (i, j), i < j, and the count. */
+int lg_pairset(lg_engine* e, int32_t s, const double* positions, int32_t family,
+               int32_t* pairs, int64_t capacity, int64_t* count);
+
+/* ---- molecular dynamics ------------------------------------------------------ */
+/* VelocityVerlet::new + setup (lumol-sim/src/md/integrators.rs:22-42): sets the
+ * timestep and zeroes the accelerations.  thermostat_tau > 0 adds a
+ * BerendsenThermostat(temperature, tau) (md/thermostats.rs:91-121) applied after
+ * every step, as MolecularDynamics::propagate does (md/molecular_dynamics.rs:66-76). */
+int lg_md_setup(lg_engine* e, int32_t s, double dt, double thermostat_temperature,
+                double thermostat_tau);
+/* Uploads / downloads positions and velocities (3n each) of system `s`. */
+int lg_md_set_state(lg_engine* e, int32_t s, const double* positions, const double* velocities);
+int lg_md_get_state(lg_engine* e, int32_t s, double* positions, double* velocities);
+/* Runs `nsteps` steps of every system with device-resident state. */
+int lg_md_run(lg_engine* e, int64_t nsteps);
+/* Integrator::integrate for a single-system engine (integrators.rs:44-69): copies
+ * host positions / velocities in, runs `nsteps` steps, copies them back. */
+int lg_md_integrate(lg_engine* e, double* positions, double* velocities, int64_t nsteps);
+
+/* ---- Monte Carlo ------------------------------------------------------------- */
+/* EnergyCache::init (sys/cache.rs:75-98) at `positions` for system `s`. */
+int lg_mc_init(lg_engine* e, int32_t s, const double* positions, double* energy);
+/* EnergyCache::move_molecule_cost (sys/cache.rs:145-220) with the Coulomb
+ * GlobalCache cost (ewald.rs:572-613, 758-839; wolf.rs:121-165). */
+int lg_mc_move_molecule_cost(lg_engine* e, int32_t s, int64_t molecule,
+                             const double* new_positions, double* cost);
+/* EnergyCache::update (sys/cache.rs:118-127) after the move was applied:
+ * `positions` are the molecule's positions after Translate::apply's
+ * center-of-mass wrap (lumol-sim/src/mc/moves/translate.rs:114-125). */
+int lg_mc_update(lg_engine* e, int32_t s, const double* molecule_positions, double* energy);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1193 @@
+// capi.cu -- the engine object behind the C ABI of include/lumol_gb300.h.
+//
+// The host side keeps the description of every system (particles, topology,
+// pair table, Coulomb potential, cell) as Lumol's System holds it, lowers it
+// into the flat device layout of kernels.h on first use after a change, and
+// drives the kernels.  Host arithmetic that feeds results (potential shifts,
+// Ewald k-vector factors, tail corrections, self energy) restates the
+// reference operation by operation; the file is compiled with
+// -ffp-contract=off so the host compiler does not fuse it either.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/lumol_gb300.h"
+#include "kernels.h"
+
+using namespace lg;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+template <class T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    ~DBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    cudaError_t alloc(size_t count) {
+        release();
+        if (count == 0) count = 1;
+        cudaError_t e = cudaMalloc((void**)&p, count * sizeof(T));
+        if (e == cudaSuccess) n = count;
+        return e;
+    }
+};
+
+struct HostSystem {
+    bool has_cell = false;
+    double L[3] = {0, 0, 0};
+    int64_t n = 0;
+    std::vector<int32_t> kinds, mols;
+    std::vector<double> charges, masses;
+    std::vector<int32_t> bonds;
+    std::vector<lg_bonded> bond_pots;
+    std::vector<int32_t> angles;
+    std::vector<lg_bonded> angle_pots;
+    int32_t nk = 0;
+    std::vector<lg_pair> pairs;
+    lg_coulomb coul{};
+    // molecular dynamics
+    double dt = 0.0, T0 = 0.0, tau = 0.0;
+    bool md_ready = false;
+    // derived
+    double tail_energy = 0.0, tail_virial = 0.0, ewald_self = 0.0;
+    double alpha = 0.0;
+};
+
+// ---- host restatement of the reference's scalar functions -----------------
+double powi6(double x) {
+    double x2 = x * x;
+    double x4 = x2 * x2;
+    return x2 * x4;
+}
+// Potential::energy (functions.rs:85-88, 287-292, 135-139)
+double pot_energy(const lg_pair& p, double r) {
+    switch (p.type) {
+        case LG_PAIR_LJ: {
+            double s6 = powi6(p.p0 / r);
+            return 4.0 * p.p1 * (s6 * s6 - s6);
+        }
+        case LG_PAIR_BUCKINGHAM: {
+            double r3 = r * r * r;
+            double r6 = r3 * r3;
+            double e = std::exp(-r / p.p2);
+            return p.p0 * e - p.p1 / r6;
+        }
+        case LG_PAIR_HARMONIC: {
+            double dx = r - p.p1;
+            return 0.5 * p.p0 * dx * dx;
+        }
+        default:
+            return 0.0;
+    }
+}
+// PairPotential::tail_energy / tail_virial (functions.rs:97-111, 303-318)
+double pot_tail_energy(const lg_pair& p, double rc) {
+    if (p.type == LG_PAIR_LJ) {
+        double s3 = p.p0 * p.p0 * p.p0;
+        double rc3 = rc * rc * rc;
+        double s9 = s3 * s3 * s3;
+        double rc9 = rc3 * rc3 * rc3;
+        return 4.0 / 3.0 * p.p1 * s3 * (1.0 / 3.0 * s9 / rc9 - s3 / rc3);
+    }
+    if (p.type == LG_PAIR_BUCKINGHAM) {
+        double rc2 = rc * rc;
+        double rc3 = rc2 * rc;
+        double e = std::exp(-rc / p.p2);
+        double factor = rc2 - 2.0 * rc * p.p2 + 2.0 * p.p2 * p.p2;
+        return p.p0 * p.p2 * e * factor - p.p1 / (3.0 * rc3);
+    }
+    return 0.0;
+}
+double pot_tail_virial(const lg_pair& p, double rc) {
+    if (p.type == LG_PAIR_LJ) {
+        double s3 = p.p0 * p.p0 * p.p0;
+        double rc3 = rc * rc * rc;
+        double s9 = s3 * s3 * s3;
+        double rc9 = rc3 * rc3 * rc3;
+        return 8.0 * p.p1 * s3 * (2.0 / 3.0 * s9 / rc9 - s3 / rc3);
+    }
+    if (p.type == LG_PAIR_BUCKINGHAM) {
+        double rc2 = rc * rc;
+        double rc3 = rc2 * rc;
+        double e = std::exp(-rc / p.p2);
+        double factor = rc3 + 3.0 * rc2 * p.p2 + 6.0 * rc * p.p2 * p.p2 + 6.0 * p.p2 * p.p2 * p.p2;
+        return p.p0 * e * factor - 20.0 * p.p1 / rc3 + 8.0;
+    }
+    return 0.0;
+}
+
+// Matrix3::inverse of diag(a, b, c) (types/matrix.rs:212-227), diagonal only
+void ortho_inverse_diag(const double L[3], double out[3]) {
+    double a = L[0], b = L[1], c = L[2];
+    double m[3][3] = {{a, 0.0, 0.0}, {0.0, b, 0.0}, {0.0, 0.0, c}};
+    double det = m[0][0] * (m[1][1] * m[2][2] - m[2][1] * m[1][2]) -
+                 m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) +
+                 m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+    double id = 1.0 / det;
+    out[0] = (m[1][1] * m[2][2] - m[2][1] * m[1][2]) * id;
+    out[1] = (m[0][0] * m[2][2] - m[0][2] * m[2][0]) * id;
+    out[2] = (m[0][0] * m[1][1] - m[1][0] * m[0][1]) * id;
+}
+
+// Ewald::prepare + compute_ewald_factors_triclinic (ewald.rs:130-183, 353-379)
+void ewald_factors(const double L[3], double alpha, int kmax, int sys, std::vector<KVecDev>& out) {
+    double inv[3];
+    ortho_inverse_diag(L, inv);
+    double s[3] = {(2.0 * PI) * inv[0], (2.0 * PI) * inv[1], (2.0 * PI) * inv[2]};
+    // k_vector([1, 1, 1]).max() * kmax; off-diagonal products are zero
+    double mx = std::max(std::max(s[0], s[1]), s[2]) * (double)kmax;
+    double kmax2 = 1.0001 * mx * mx;
+    double alpha_sq_inv_fourth = 0.25 / (alpha * alpha);
+    double four_pi_v = 4.0 * PI / (L[0] * L[1] * L[2]);
+    auto push = [&](int ikx, int iky, int ikz) {
+        double k[3] = {s[0] * (double)ikx, s[1] * (double)iky, s[2] * (double)ikz};
+        double k2 = k[0] * k[0] + k[1] * k[1] + k[2] * k[2];
+        if (k2 > kmax2) return;
+        KVecDev f;
+        std::memset(&f, 0, sizeof(f));
+        f.ikx = ikx;
+        f.iky = iky;
+        f.ikz = ikz;
+        f.sys = sys;
+        f.energy = four_pi_v * std::exp(-k2 * alpha_sq_inv_fourth) / k2;
+        for (int d = 0; d < 3; d++) f.field[d] = (2.0 * f.energy) * k[d];
+        double vf = -2.0 * (1.0 / k2 + alpha_sq_inv_fourth);
+        const int ia[6] = {0, 0, 0, 1, 1, 2}, ib[6] = {0, 1, 2, 1, 2, 2};
+        for (int c = 0; c < 6; c++) {
+            double v = (ia[c] == ib[c] ? 1.0 : 0.0) + vf * (k[ia[c]] * k[ib[c]]);
+            f.virial[c] = f.energy * v;
+        }
+        out.push_back(f);
+    };
+    for (int ikx = 1; ikx < kmax; ikx++)
+        for (int iky = -kmax; iky < kmax; iky++)
+            for (int ikz = -kmax; ikz < kmax; ikz++) push(ikx, iky, ikz);
+    for (int iky = 1; iky < kmax; iky++)
+        for (int ikz = -kmax; ikz < kmax; ikz++) push(0, iky, ikz);
+    for (int ikz = 1; ikz < kmax; ikz++) push(0, 0, ikz);
+}
+
+}  // namespace
+
+struct lg_engine {
+    lg_options opt{};
+    int nsys = 0;
+    std::vector<HostSystem> sys;
+    std::string err;
+    cudaStream_t stream = nullptr;
+    bool dirty = true;
+    std::vector<int64_t> begin;  // atom offsets (nsys + 1)
+    double skin = 1.0;
+
+    Batch b;
+    // device storage
+    DBuf<double4_32a> posq, vel, acc, pos_build;
+    DBuf<double> force, pos3, vel3, red, host_const, lambda, ke, out, fpart, kred, mc_part;
+    DBuf<int> kind, mol, sysid, spec_off, spec_j, bt_off, bt_role, nbr, nnb, atom_cell, cell_count, cell_start,
+        cell_atoms;
+    DBuf<int8_t> spec_path;
+    DBuf<int4> bt;
+    DBuf<double2> bt_par, eikr, rho;
+    DBuf<float4> wpos;
+    DBuf<SysDev> sysdev;
+    DBuf<PairDev> ptab;
+    DBuf<KVecDev> kvec;
+    DBuf<uint32_t> status;
+    DBuf<int> pairs_out;
+    DBuf<unsigned long long> pairs_count;
+    uint32_t* h_status = nullptr;  // pinned
+    double* h_out = nullptr;       // pinned, nsys * RED_STRIDE
+    std::vector<SysDev> h_sysdev;
+    std::vector<int> h_kvec_sys;
+
+    // MD graph
+    cudaGraphExec_t graph = nullptr;
+    int graph_steps = 0;
+    bool graph_thermo = false;
+
+    // MC (single molecule moves)
+    DBuf<double> mc_newpos;
+    DBuf<double2> mc_eikr, mc_drho;
+    double mc_energy = 0.0;
+    double mc_pending_cost = 0.0;
+    bool mc_pending = false;
+    int mc_sys = -1;
+    int64_t mc_mol_begin = 0, mc_mol_size = 0;
+
+    ~lg_engine() {
+        if (graph) cudaGraphExecDestroy(graph);
+        if (h_status) cudaFreeHost(h_status);
+        if (h_out) cudaFreeHost(h_out);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+int fail(lg_engine* e, int code, const std::string& msg) {
+    if (e) e->err = msg;
+    else g_create_error = msg;
+    return code;
+}
+
+#define CUDA_TRY(e, call)                                                                          \
+    do {                                                                                           \
+        cudaError_t _err = (call);                                                                 \
+        if (_err != cudaSuccess)                                                                   \
+            return fail((e), LG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_err)); \
+    } while (0)
+
+bool valid_sys(lg_engine* e, int32_t s) { return e && s >= 0 && s < e->nsys; }
+
+void invalidate(lg_engine* e) {
+    e->dirty = true;
+    if (e->graph) {
+        cudaGraphExecDestroy(e->graph);
+        e->graph = nullptr;
+    }
+}
+
+double max_cutoff(const HostSystem& h) {
+    double rc = 0.0;
+    for (const lg_pair& p : h.pairs)
+        if (p.type != LG_PAIR_ABSENT) rc = std::max(rc, p.cutoff);
+    if (h.coul.kind != LG_COULOMB_NONE) rc = std::max(rc, h.coul.cutoff);
+    return rc;
+}
+
+// Bond paths from the bond graph: the shortest path, when it has at most three
+// bonds, is the BondPath Bonding::rebuild_connections records for the pair
+// (bonds give ONE, angle ends TWO, dihedral ends THREE; bonding.rs:159-186).
+void bond_paths(const HostSystem& h, int64_t base, std::vector<std::vector<std::pair<int, int8_t>>>& spec) {
+    std::vector<std::vector<int>> adj(h.n);
+    for (size_t b = 0; b + 1 < h.bonds.size(); b += 2) {
+        int i = h.bonds[b], j = h.bonds[b + 1];
+        adj[i].push_back(j);
+        adj[j].push_back(i);
+    }
+    for (int64_t i = 0; i < h.n; i++) {
+        if (adj[i].empty()) continue;
+        std::vector<std::pair<int, int>> frontier{{(int)i, 0}};
+        std::vector<int> seen{(int)i};
+        for (size_t f = 0; f < frontier.size(); f++) {
+            auto [a, depth] = frontier[f];
+            if (depth == 3) continue;
+            for (int nb : adj[a]) {
+                if (std::find(seen.begin(), seen.end(), nb) != seen.end()) continue;
+                seen.push_back(nb);
+                frontier.push_back({nb, depth + 1});
+                spec[base + i].push_back({(int)(base + nb), (int8_t)(depth + 2)});
+            }
+        }
+    }
+}
+
+int commit(lg_engine* e) {
+    if (!e->dirty) return LG_OK;
+    int nsys = e->nsys;
+    e->begin.assign(nsys + 1, 0);
+    for (int s = 0; s < nsys; s++) {
+        const HostSystem& h = e->sys[s];
+        if (!h.has_cell) return fail(e, LG_ERR_STATE, "system " + std::to_string(s) + " has no cell");
+        if (h.nk == 0 && h.n > 0)
+            return fail(e, LG_ERR_STATE, "system " + std::to_string(s) + " has no pair table");
+        e->begin[s + 1] = e->begin[s] + h.n;
+    }
+    int64_t n = e->begin[nsys];
+    if (n > (int64_t)0x7fffffff / 64) return fail(e, LG_ERR_ARGUMENT, "too many atoms");
+
+    std::vector<double4_32a> h_posq(n), h_vel(n);
+    std::vector<int> h_kind(n), h_mol(n), h_sysid(n);
+    std::vector<PairDev> h_ptab;
+    std::vector<KVecDev> h_kvec;
+    std::vector<std::vector<std::pair<int, int8_t>>> spec(n);
+    struct Term {
+        int4 t;
+        int role;
+        double2 par;
+    };
+    std::vector<std::vector<Term>> terms(n);
+    e->h_sysdev.assign(nsys, SysDev{});
+    std::vector<double> h_const((size_t)nsys * RED_STRIDE, 0.0);
+    int mol_base = 0, cell_total = 0, kdim = 1;
+    double max_expected = 0.0;
+    int64_t max_n = 1;
+
+    for (int s = 0; s < nsys; s++) {
+        HostSystem& h = e->sys[s];
+        SysDev& d = e->h_sysdev[s];
+        std::memset(&d, 0, sizeof(d));
+        int64_t base = e->begin[s];
+        max_n = std::max(max_n, h.n);
+        int max_mol = -1;
+        for (int64_t i = 0; i < h.n; i++) {
+            h_posq[base + i] = make_double4_32a(0.0, 0.0, 0.0, h.charges[i]);
+            h_vel[base + i] = make_double4_32a(0.0, 0.0, 0.0, h.masses[i]);
+            h_kind[base + i] = h.kinds[i];
+            h_mol[base + i] = mol_base + h.mols[i];
+            h_sysid[base + i] = s;
+            max_mol = std::max(max_mol, h.mols[i]);
+        }
+        mol_base += max_mol + 1;
+        bond_paths(h, base, spec);
+        for (size_t b = 0; b * 2 < h.bonds.size(); b++) {
+            const lg_bonded& p = h.bond_pots[b];
+            if (p.type == LG_PAIR_ABSENT) continue;
+            double k = p.type == LG_PAIR_NULL ? NAN : p.k;
+            int i = (int)(base + h.bonds[2 * b]), j = (int)(base + h.bonds[2 * b + 1]);
+            int a = std::min(i, j), c = std::max(i, j);  // Bond::new orders i < j (connect.rs:21-26)
+            int4 t = make_int4(0, a, c, -1);
+            terms[a].push_back({t, 0, make_double2(k, p.x0)});
+            terms[c].push_back({t, 1, make_double2(k, p.x0)});
+        }
+        for (size_t a = 0; a * 3 < h.angles.size(); a++) {
+            const lg_bonded& p = h.angle_pots[a];
+            if (p.type == LG_PAIR_ABSENT) continue;
+            double k = p.type == LG_PAIR_NULL ? NAN : p.k;
+            int i = (int)(base + h.angles[3 * a]), j = (int)(base + h.angles[3 * a + 1]),
+                m = (int)(base + h.angles[3 * a + 2]);
+            int lo = std::min(i, m), hi = std::max(i, m);  // Angle::new (connect.rs:54-65)
+            int4 t = make_int4(1, lo, j, hi);
+            terms[lo].push_back({t, 0, make_double2(k, p.x0)});
+            terms[j].push_back({t, 1, make_double2(k, p.x0)});
+            terms[hi].push_back({t, 2, make_double2(k, p.x0)});
+        }
+
+        // pair table
+        d.ptab = (int)h_ptab.size();
+        d.nk = h.nk;
+        bool needs_path = false;
+        for (const lg_pair& p : h.pairs) {
+            PairDev q;
+            std::memset(&q, 0, sizeof(q));
+            q.type = p.type;
+            q.shifted = p.shifted;
+            q.restriction = p.restriction;
+            q.tail = p.tail;
+            q.p0 = p.p0;
+            q.p1 = p.p1;
+            q.p2 = p.p2;
+            q.cutoff = p.cutoff;
+            q.shift = p.shifted ? pot_energy(p, p.cutoff) : 0.0;  // pairs.rs:86-95
+            q.scale14 = p.scale14;
+            q.cutoff2_f = (float)(p.cutoff * p.cutoff);
+            if (p.type != LG_PAIR_ABSENT && p.restriction > LG_RESTRICT_INTER) needs_path = true;
+            h_ptab.push_back(q);
+        }
+        if (h.coul.kind != LG_COULOMB_NONE && h.coul.restriction > LG_RESTRICT_INTER) needs_path = true;
+        d.needs_path = needs_path;
+
+        // cell and neighbour list geometry
+        for (int k = 0; k < 3; k++) {
+            d.L[k] = h.L[k];
+            d.invL[k] = 1.0 / h.L[k];
+            d.Lf[k] = (float)h.L[k];
+            d.invLf[k] = (float)(1.0 / h.L[k]);
+        }
+        double rc = max_cutoff(h);
+        d.rlist = rc + e->skin;
+        d.half_skin2 = 0.25 * e->skin * e->skin;
+        double margin = 1e-5 * std::max(std::max(h.L[0], h.L[1]), h.L[2]) + 1e-4;
+        d.rlist2_f = (float)((d.rlist + margin) * (d.rlist + margin));
+        int cells = 1;
+        for (int k = 0; k < 3; k++) {
+            int nc = (int)std::floor(h.L[k] / (d.rlist + margin));
+            nc = std::max(1, std::min(nc, 64));
+            d.ncell[k] = nc;
+            cells *= nc;
+        }
+        d.cell_begin = cell_total;
+        cell_total += cells;
+        double volume = h.L[0] * h.L[1] * h.L[2];
+        if (h.n > 0) {
+            double expected = (double)h.n / volume * 4.0 / 3.0 * PI * d.rlist * d.rlist * d.rlist;
+            max_expected = std::max(max_expected, expected);
+        }
+
+        // Coulomb
+        d.coul = h.coul.kind;
+        d.coul_restr = h.coul.restriction;
+        d.coul_rc = h.coul.cutoff;
+        d.coul_scale14 = h.coul.scale14;
+        d.coul_rc2_f = (float)(h.coul.cutoff * h.coul.cutoff);
+        h.ewald_self = 0.0;
+        if (h.coul.kind == LG_COULOMB_EWALD) {
+            h.alpha = h.coul.alpha > 0.0 ? h.coul.alpha : PI / h.coul.cutoff;  // ewald.rs:278-279
+            d.alpha = h.alpha;
+            d.kmax = h.coul.kmax;
+            kdim = std::max(kdim, h.coul.kmax + 1);
+            double inv[3];
+            ortho_inverse_diag(h.L, inv);
+            for (int k = 0; k < 3; k++) d.k1[k] = (2.0 * PI) * inv[k];
+            d.kbegin = (int)h_kvec.size();
+            ewald_factors(h.L, h.alpha, h.coul.kmax, s, h_kvec);
+            d.kend = (int)h_kvec.size();
+            // Ewald::self_energy (ewald.rs:619-626)
+            double q2 = 0.0;
+            for (double q : h.charges) q2 += q * q;
+            h.ewald_self = -h.alpha / std::sqrt(PI) * q2 / FOUR_PI_EPSILON_0;
+        } else if (h.coul.kind == LG_COULOMB_WOLF) {
+            // Wolf::new (wolf.rs:68-84)
+            double cutoff = h.coul.cutoff;
+            double alpha = PI / cutoff;
+            double ac = alpha * cutoff;
+            double ac2 = ac * ac;
+            d.alpha = alpha;
+            d.wolf_ec = std::erfc(ac) / cutoff;
+            d.wolf_fc = std::erfc(ac) / (cutoff * cutoff) + FRAC_2_SQRT_PI * alpha * std::exp(-ac2) / cutoff;
+        }
+        d.kbegin = h.coul.kind == LG_COULOMB_EWALD ? d.kbegin : (int)h_kvec.size();
+        d.kend = h.coul.kind == LG_COULOMB_EWALD ? d.kend : (int)h_kvec.size();
+
+        // Tail corrections (sys/energy.rs:63-79, compute.rs:219-229), kinds in index order
+        std::vector<int64_t> counts(h.nk, 0);
+        for (int32_t k : h.kinds) counts[k]++;
+        double te = 0.0, tv = 0.0;
+        for (int a = 0; a < h.nk; a++) {
+            if (!counts[a]) continue;
+            for (int c = 0; c < h.nk; c++) {
+                if (!counts[c]) continue;
+                double two_pi_density = 2.0 * PI * (double)counts[a] * (double)counts[c] / volume;
+                const lg_pair& p = h.pairs[(size_t)a * h.nk + c];
+                if (p.type == LG_PAIR_ABSENT || !p.tail) continue;
+                te += two_pi_density * pot_tail_energy(p, p.cutoff);
+                tv += two_pi_density * (pot_tail_virial(p, p.cutoff) * (1.0 / 3.0));
+            }
+        }
+        h.tail_energy = te;
+        h.tail_virial = tv;
+        double* hc = &h_const[(size_t)s * RED_STRIDE];
+        hc[0] = te;
+        hc[1] = tv;
+        hc[2] = h.ewald_self;
+
+        d.begin = (int)base;
+        d.end = (int)(base + h.n);
+        d.dt = h.dt;
+        d.thermo_T = h.T0;
+        d.thermo_tau = h.tau;
+        d.dof = (double)(3 * h.n);
+    }
+
+    // per-atom CSR tables
+    std::vector<int> h_spec_off(n + 1, 0), h_spec_j;
+    std::vector<int8_t> h_spec_path;
+    for (int64_t i = 0; i < n; i++) {
+        h_spec_off[i] = (int)h_spec_j.size();
+        for (auto& pr : spec[i]) {
+            h_spec_j.push_back(pr.first);
+            h_spec_path.push_back(pr.second);
+        }
+    }
+    h_spec_off[n] = (int)h_spec_j.size();
+    std::vector<int> h_bt_off(n + 1, 0), h_bt_role;
+    std::vector<int4> h_bt;
+    std::vector<double2> h_bt_par;
+    for (int64_t i = 0; i < n; i++) {
+        h_bt_off[i] = (int)h_bt.size();
+        for (auto& t : terms[i]) {
+            h_bt.push_back(t.t);
+            h_bt_role.push_back(t.role);
+            h_bt_par.push_back(t.par);
+        }
+    }
+    h_bt_off[n] = (int)h_bt.size();
+
+    // neighbour capacity: 1.6x the mean count plus a margin, never above the largest system
+    int maxnb = (int)std::ceil(1.6 * max_expected + 64.0);
+    maxnb = std::min(maxnb, (int)max_n);
+    maxnb = std::max(32, (maxnb + 31) / 32 * 32);
+    if (e->b.maxnb > maxnb && e->b.n == n) maxnb = e->b.maxnb;  // keep a capacity that was regrown
+
+    // allocate
+    CUDA_TRY(e, e->posq.alloc(n));
+    CUDA_TRY(e, e->vel.alloc(n));
+    CUDA_TRY(e, e->acc.alloc(n));
+    CUDA_TRY(e, e->pos_build.alloc(n));
+    CUDA_TRY(e, e->force.alloc(3 * n));
+    CUDA_TRY(e, e->pos3.alloc(3 * n));
+    CUDA_TRY(e, e->vel3.alloc(3 * n));
+    CUDA_TRY(e, e->red.alloc((size_t)n * RED_STRIDE));
+    CUDA_TRY(e, e->host_const.alloc((size_t)nsys * RED_STRIDE));
+    CUDA_TRY(e, e->lambda.alloc(nsys));
+    CUDA_TRY(e, e->ke.alloc(n));
+    CUDA_TRY(e, e->out.alloc((size_t)nsys * RED_STRIDE));
+    CUDA_TRY(e, e->kind.alloc(n));
+    CUDA_TRY(e, e->mol.alloc(n));
+    CUDA_TRY(e, e->sysid.alloc(n));
+    CUDA_TRY(e, e->spec_off.alloc(n + 1));
+    CUDA_TRY(e, e->spec_j.alloc(h_spec_j.size()));
+    CUDA_TRY(e, e->spec_path.alloc(h_spec_path.size()));
+    CUDA_TRY(e, e->bt_off.alloc(n + 1));
+    CUDA_TRY(e, e->bt.alloc(h_bt.size()));
+    CUDA_TRY(e, e->bt_role.alloc(h_bt_role.size()));
+    CUDA_TRY(e, e->bt_par.alloc(h_bt_par.size()));
+    CUDA_TRY(e, e->nbr.alloc((size_t)n * maxnb));
+    CUDA_TRY(e, e->nnb.alloc(n));
+    CUDA_TRY(e, e->atom_cell.alloc(n));
+    CUDA_TRY(e, e->cell_count.alloc(cell_total));
+    CUDA_TRY(e, e->cell_start.alloc(cell_total + 1));
+    CUDA_TRY(e, e->cell_atoms.alloc(n));
+    CUDA_TRY(e, e->wpos.alloc(n));
+    CUDA_TRY(e, e->sysdev.alloc(nsys));
+    CUDA_TRY(e, e->ptab.alloc(h_ptab.size()));
+    CUDA_TRY(e, e->status.alloc(1));
+    int nkv = (int)h_kvec.size();
+    int kchunk = 32;
+    int nkchunks = 0;
+    for (int s = 0; s < nsys; s++) {
+        int nk_s = e->h_sysdev[s].kend - e->h_sysdev[s].kbegin;
+        nkchunks = std::max(nkchunks, (nk_s + kchunk - 1) / kchunk);
+    }
+    CUDA_TRY(e, e->kvec.alloc(nkv));
+    CUDA_TRY(e, e->eikr.alloc(nkv ? (size_t)kdim * 3 * n : 1));
+    CUDA_TRY(e, e->rho.alloc(nkv));
+    CUDA_TRY(e, e->kred.alloc((size_t)nkv * 7));
+    CUDA_TRY(e, e->fpart.alloc(nkv ? (size_t)nkchunks * 3 * n : 1));
+
+    cudaStream_t st = e->stream;
+    CUDA_TRY(e, cudaMemcpyAsync(e->posq.p, h_posq.data(), n * sizeof(double4_32a), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(e, cudaMemcpyAsync(e->vel.p, h_vel.data(), n * sizeof(double4_32a), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(e, cudaMemsetAsync(e->acc.p, 0, n * sizeof(double4_32a), st));
+    CUDA_TRY(e, cudaMemsetAsync(e->pos_build.p, 0, n * sizeof(double4_32a), st));
+    CUDA_TRY(e, cudaMemcpyAsync(e->kind.p, h_kind.data(), n * sizeof(int), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(e, cudaMemcpyAsync(e->mol.p, h_mol.data(), n * sizeof(int), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(e, cudaMemcpyAsync(e->sysid.p, h_sysid.data(), n * sizeof(int), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(e, cudaMemcpyAsync(e->spec_off.p, h_spec_off.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
+    if (!h_spec_j.empty()) {
+        CUDA_TRY(e, cudaMemcpyAsync(e->spec_j.p, h_spec_j.data(), h_spec_j.size() * sizeof(int),
+                                    cudaMemcpyHostToDevice, st));
+        CUDA_TRY(e, cudaMemcpyAsync(e->spec_path.p, h_spec_path.data(), h_spec_path.size(),
+                                    cudaMemcpyHostToDevice, st));
+    }
+    CUDA_TRY(e, cudaMemcpyAsync(e->bt_off.p, h_bt_off.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
+    if (!h_bt.empty()) {
+        CUDA_TRY(e, cudaMemcpyAsync(e->bt.p, h_bt.data(), h_bt.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(e, cudaMemcpyAsync(e->bt_role.p, h_bt_role.data(), h_bt_role.size() * sizeof(int),
+                                    cudaMemcpyHostToDevice, st));
+        CUDA_TRY(e, cudaMemcpyAsync(e->bt_par.p, h_bt_par.data(), h_bt_par.size() * sizeof(double2),
+                                    cudaMemcpyHostToDevice, st));
+    }
+    CUDA_TRY(e, cudaMemsetAsync(e->cell_count.p, 0, cell_total * sizeof(int), st));
+    CUDA_TRY(e, cudaMemsetAsync(e->nnb.p, 0, n * sizeof(int), st));
+    CUDA_TRY(e, cudaMemcpyAsync(e->sysdev.p, e->h_sysdev.data(), nsys * sizeof(SysDev), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(e, cudaMemcpyAsync(e->ptab.p, h_ptab.data(), h_ptab.size() * sizeof(PairDev), cudaMemcpyHostToDevice, st));
+    if (nkv)
+        CUDA_TRY(e, cudaMemcpyAsync(e->kvec.p, h_kvec.data(), nkv * sizeof(KVecDev), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(e, cudaMemcpyAsync(e->host_const.p, h_const.data(), h_const.size() * sizeof(double),
+                                cudaMemcpyHostToDevice, st));
+    uint32_t st_init = ST_REBUILD;
+    CUDA_TRY(e, cudaMemcpyAsync(e->status.p, &st_init, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(e, cudaStreamSynchronize(st));
+
+    if (e->h_out) cudaFreeHost(e->h_out);
+    e->h_out = nullptr;
+    CUDA_TRY(e, cudaMallocHost((void**)&e->h_out, (size_t)nsys * RED_STRIDE * sizeof(double)));
+
+    Batch& b = e->b;
+    b = Batch{};
+    b.n = (int)n;
+    b.nsys = nsys;
+    b.precision = e->opt.precision;
+    b.posq = e->posq.p;
+    b.vel = e->vel.p;
+    b.acc = e->acc.p;
+    b.force = e->force.p;
+    b.kind = e->kind.p;
+    b.mol = e->mol.p;
+    b.sysid = e->sysid.p;
+    b.sys = e->sysdev.p;
+    b.ptab = e->ptab.p;
+    b.spec_off = e->spec_off.p;
+    b.spec_j = e->spec_j.p;
+    b.spec_path = e->spec_path.p;
+    b.bt_off = h_bt.empty() ? nullptr : e->bt_off.p;
+    b.bt = e->bt.p;
+    b.bt_role = e->bt_role.p;
+    b.bt_par = e->bt_par.p;
+    b.maxnb = maxnb;
+    b.ncells = cell_total;
+    b.nbr = e->nbr.p;
+    b.nnb = e->nnb.p;
+    b.atom_cell = e->atom_cell.p;
+    b.cell_count = e->cell_count.p;
+    b.cell_start = e->cell_start.p;
+    b.cell_atoms = e->cell_atoms.p;
+    b.wpos = e->wpos.p;
+    b.pos_build = e->pos_build.p;
+    b.status = e->status.p;
+    b.nkvec = nkv;
+    b.kdim = kdim;
+    b.kchunk = kchunk;
+    b.nkchunks = nkchunks;
+    b.kvec = e->kvec.p;
+    b.eikr = e->eikr.p;
+    b.rho = e->rho.p;
+    b.fpart = e->fpart.p;
+    b.kred = e->kred.p;
+    b.red = e->red.p;
+    b.host_const = e->host_const.p;
+    b.lambda = e->lambda.p;
+    b.ke = e->ke.p;
+    e->dirty = false;
+    return LG_OK;
+}
+
+// Regrows the neighbour list after an overflow.
+int regrow(lg_engine* e) {
+    int maxnb = e->b.maxnb * 3 / 2;
+    maxnb = (maxnb + 31) / 32 * 32;
+    CUDA_TRY(e, e->nbr.alloc((size_t)e->b.n * maxnb));
+    e->b.maxnb = maxnb;
+    e->b.nbr = e->nbr.p;
+    uint32_t st_init = ST_REBUILD;
+    CUDA_TRY(e, cudaMemcpyAsync(e->status.p, &st_init, sizeof(uint32_t), cudaMemcpyHostToDevice, e->stream));
+    if (e->graph) {
+        cudaGraphExecDestroy(e->graph);
+        e->graph = nullptr;
+    }
+    return LG_OK;
+}
+
+int read_status(lg_engine* e, uint32_t* out) {
+    CUDA_TRY(e, cudaMemcpyAsync(e->h_status, e->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->stream));
+    CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+    *out = *e->h_status;
+    return LG_OK;
+}
+
+int clear_status_bits(lg_engine* e, uint32_t bits) {
+    uint32_t v = *e->h_status & ~bits;
+    *e->h_status = v;
+    CUDA_TRY(e, cudaMemcpyAsync(e->status.p, e->h_status, sizeof(uint32_t), cudaMemcpyHostToDevice, e->stream));
+    return LG_OK;
+}
+
+// Forces (and energies / virials) of the whole batch at the positions in posq.
+void enqueue_forces(lg_engine* e, uint32_t terms, bool ev, cudaStream_t st) {
+    const Batch& b = e->b;
+    launch_nlist_build(b, st);
+    if (terms & (LG_TERM_PAIRS | LG_TERM_COUL_REAL)) launch_pair_forces(b, terms, ev, st);
+    if (terms & (LG_TERM_BONDS | LG_TERM_ANGLES)) launch_bonded(b, terms, ev, st);
+    if ((terms & LG_TERM_COUL_KSPACE) && b.nkvec) launch_kspace(b, true, ev, st);
+}
+
+int compute_batch(lg_engine* e, uint32_t terms, uint32_t want, double* d_force_out, double* d_out) {
+    bool ev = (want & (LG_WANT_ENERGY | LG_WANT_VIRIAL)) != 0;
+    cudaStream_t st = e->stream;
+    for (int attempt = 0; attempt < 4; attempt++) {
+        launch_check_displacement(e->b, st);
+        CUDA_TRY(e, cudaMemsetAsync(e->force.p, 0, 3 * (size_t)e->b.n * sizeof(double), st));
+        if (ev) CUDA_TRY(e, cudaMemsetAsync(e->red.p, 0, (size_t)e->b.n * RED_STRIDE * sizeof(double), st));
+        enqueue_forces(e, terms, ev, st);
+        if (ev) launch_reduce(e->b, terms, (terms & LG_TERM_COUL_KSPACE) && e->b.nkvec, e->out.p, st);
+        CUDA_TRY(e, cudaGetLastError());
+        uint32_t status;
+        int rc = read_status(e, &status);
+        if (rc) return rc;
+        if (status & ST_OVERFLOW) {
+            rc = clear_status_bits(e, ST_OVERFLOW);
+            if (rc) return rc;
+            rc = regrow(e);
+            if (rc) return rc;
+            continue;
+        }
+        if (status & ST_NONFINITE) {
+            clear_status_bits(e, ST_NONFINITE);
+            return fail(e, LG_ERR_NONFINITE, "Potential energy is infinite!");
+        }
+        if (d_force_out)
+            CUDA_TRY(e, cudaMemcpyAsync(d_force_out, e->force.p, 3 * (size_t)e->b.n * sizeof(double),
+                                        cudaMemcpyDeviceToDevice, st));
+        (void)d_out;
+        return LG_OK;
+    }
+    return fail(e, LG_ERR_CAPACITY, "neighbour list overflow persisted after regrowing");
+}
+
+int check_pair_cutoffs(lg_engine* e, const HostSystem& h) {
+    if (!h.has_cell) return LG_OK;
+    double half = 0.5 * std::min(std::min(h.L[0], h.L[1]), h.L[2]);
+    for (const lg_pair& p : h.pairs)
+        if (p.type != LG_PAIR_ABSENT && half < p.cutoff)
+            return fail(e, LG_ERR_ARGUMENT,
+                        "Can not add a potential with a cutoff bigger than half of the smallest cell length. "
+                        "Try increasing the cell size or decreasing the cutoff.");
+    if (h.coul.kind != LG_COULOMB_NONE && half < h.coul.cutoff)
+        return fail(e, LG_ERR_ARGUMENT,
+                    "Can not add a potential with a cutoff bigger than half of the smallest cell length. "
+                    "Try increasing the cell size or decreasing the cutoff.");
+    return LG_OK;
+}
+
+}  // namespace
+
+// ============================================================================
+// C ABI
+// ============================================================================
+extern "C" {
+
+int lg_version(void) { return LG_ABI_VERSION; }
+
+const char* lg_last_error(const lg_engine* e) { return e ? e->err.c_str() : g_create_error.c_str(); }
+
+int lg_create(const lg_options* options, int32_t n_systems, lg_engine** out) {
+    if (!out) return fail(nullptr, LG_ERR_ARGUMENT, "null engine pointer");
+    *out = nullptr;
+    if (n_systems <= 0) return fail(nullptr, LG_ERR_ARGUMENT, "n_systems must be positive");
+    lg_options opt{0, LG_PRECISION_FP64, 1.0};
+    if (options) opt = *options;
+    if (opt.precision != LG_PRECISION_FP64 && opt.precision != LG_PRECISION_MIXED)
+        return fail(nullptr, LG_ERR_ARGUMENT, "unknown precision");
+    if (opt.skin <= 0.0) opt.skin = 1.0;
+    int count = 0;
+    cudaError_t ce = cudaGetDeviceCount(&count);
+    if (ce != cudaSuccess || count == 0)
+        return fail(nullptr, LG_ERR_NO_DEVICE,
+                    std::string("no CUDA device is visible (") + cudaGetErrorString(ce) +
+                        "); the engine has no CPU fallback");
+    if (opt.device < 0 || opt.device >= count) return fail(nullptr, LG_ERR_ARGUMENT, "invalid device ordinal");
+    ce = cudaSetDevice(opt.device);
+    if (ce != cudaSuccess) return fail(nullptr, LG_ERR_CUDA, cudaGetErrorString(ce));
+    lg_engine* e = new lg_engine();
+    e->opt = opt;
+    e->skin = opt.skin;
+    e->nsys = n_systems;
+    e->sys.resize(n_systems);
+    ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
+    if (ce == cudaSuccess) ce = cudaMallocHost((void**)&e->h_status, sizeof(uint32_t));
+    if (ce != cudaSuccess) {
+        delete e;
+        return fail(nullptr, LG_ERR_CUDA, cudaGetErrorString(ce));
+    }
+    *out = e;
+    return LG_OK;
+}
+
+void lg_destroy(lg_engine* e) {
+    if (!e) return;
+    cudaSetDevice(e->opt.device);
+    cudaStreamSynchronize(e->stream);
+    delete e;
+}
+
+int lg_set_cell(lg_engine* e, int32_t s, const double m[9]) {
+    if (!valid_sys(e, s) || !m) return fail(e, LG_ERR_ARGUMENT, "invalid system index or cell");
+    for (int a = 0; a < 3; a++)
+        for (int c = 0; c < 3; c++)
+            if (a != c && m[3 * a + c] != 0.0)
+                return fail(e, LG_ERR_ARGUMENT, "only orthorhombic cells are supported");
+    if (!(m[0] > 0.0 && m[4] > 0.0 && m[8] > 0.0)) return fail(e, LG_ERR_ARGUMENT, "Cell lengths must be positive");
+    HostSystem& h = e->sys[s];
+    h.L[0] = m[0];
+    h.L[1] = m[4];
+    h.L[2] = m[8];
+    h.has_cell = true;
+    invalidate(e);
+    return check_pair_cutoffs(e, h);
+}
+
+int lg_set_particles(lg_engine* e, int32_t s, int64_t n, const int32_t* kinds, const double* charges,
+                     const double* masses, const int32_t* molecules) {
+    if (!valid_sys(e, s) || n < 0 || (n > 0 && (!kinds || !charges || !masses || !molecules)))
+        return fail(e, LG_ERR_ARGUMENT, "invalid particles");
+    HostSystem& h = e->sys[s];
+    h.n = n;
+    h.kinds.assign(kinds, kinds + n);
+    h.charges.assign(charges, charges + n);
+    h.masses.assign(masses, masses + n);
+    h.mols.assign(molecules, molecules + n);
+    for (int64_t i = 0; i < n; i++) {
+        if (h.kinds[i] < 0) return fail(e, LG_ERR_ARGUMENT, "negative kind");
+        if (h.mols[i] < 0) return fail(e, LG_ERR_ARGUMENT, "negative molecule index");
+        if (!(h.masses[i] > 0.0)) return fail(e, LG_ERR_ARGUMENT, "masses must be positive");
+        if (i > 0 && h.mols[i] != h.mols[i - 1] && h.mols[i] != h.mols[i - 1] + 1)
+            return fail(e, LG_ERR_ARGUMENT, "molecules must be numbered contiguously in atom order");
+    }
+    h.md_ready = false;
+    invalidate(e);
+    return LG_OK;
+}
+
+int lg_set_bonds(lg_engine* e, int32_t s, int64_t nb, const int32_t* bonds, const lg_bonded* pots) {
+    if (!valid_sys(e, s) || nb < 0 || (nb > 0 && (!bonds || !pots))) return fail(e, LG_ERR_ARGUMENT, "invalid bonds");
+    HostSystem& h = e->sys[s];
+    for (int64_t b = 0; b < 2 * nb; b++)
+        if (bonds[b] < 0 || bonds[b] >= h.n) return fail(e, LG_ERR_ARGUMENT, "bond index out of range");
+    for (int64_t b = 0; b < nb; b++) {
+        if (bonds[2 * b] == bonds[2 * b + 1]) return fail(e, LG_ERR_ARGUMENT, "a bond needs two particles");
+        if (h.mols[bonds[2 * b]] != h.mols[bonds[2 * b + 1]])
+            return fail(e, LG_ERR_ARGUMENT, "bonded particles must be in the same molecule");
+    }
+    h.bonds.assign(bonds, bonds + 2 * nb);
+    h.bond_pots.assign(pots, pots + nb);
+    invalidate(e);
+    return LG_OK;
+}
+
+int lg_set_angles(lg_engine* e, int32_t s, int64_t na, const int32_t* angles, const lg_bonded* pots) {
+    if (!valid_sys(e, s) || na < 0 || (na > 0 && (!angles || !pots)))
+        return fail(e, LG_ERR_ARGUMENT, "invalid angles");
+    HostSystem& h = e->sys[s];
+    for (int64_t a = 0; a < 3 * na; a++)
+        if (angles[a] < 0 || angles[a] >= h.n) return fail(e, LG_ERR_ARGUMENT, "angle index out of range");
+    h.angles.assign(angles, angles + 3 * na);
+    h.angle_pots.assign(pots, pots + na);
+    invalidate(e);
+    return LG_OK;
+}
+
+int lg_set_pairs(lg_engine* e, int32_t s, int32_t nk, const lg_pair* table) {
+    if (!valid_sys(e, s) || nk <= 0 || !table) return fail(e, LG_ERR_ARGUMENT, "invalid pair table");
+    HostSystem& h = e->sys[s];
+    for (int32_t k : h.kinds)
+        if (k >= nk) return fail(e, LG_ERR_ARGUMENT, "a particle kind is outside the pair table");
+    for (int a = 0; a < nk; a++)
+        for (int c = 0; c < nk; c++) {
+            const lg_pair& p = table[a * nk + c];
+            const lg_pair& q = table[c * nk + a];
+            if (p.type != q.type || p.cutoff != q.cutoff || p.p0 != q.p0 || p.p1 != q.p1 || p.p2 != q.p2 ||
+                p.restriction != q.restriction || p.shifted != q.shifted || p.tail != q.tail)
+                return fail(e, LG_ERR_ARGUMENT, "the pair table must be symmetric");
+            if (p.type < LG_PAIR_ABSENT || p.type > LG_PAIR_HARMONIC)
+                return fail(e, LG_ERR_ARGUMENT, "unknown pair potential");
+            if (p.type != LG_PAIR_ABSENT && !(p.cutoff >= 0.0))
+                return fail(e, LG_ERR_ARGUMENT, "invalid pair cutoff");
+        }
+    h.nk = nk;
+    h.pairs.assign(table, table + (size_t)nk * nk);
+    invalidate(e);
+    return check_pair_cutoffs(e, h);
+}
+
+int lg_set_coulomb(lg_engine* e, int32_t s, const lg_coulomb* c) {
+    if (!valid_sys(e, s) || !c) return fail(e, LG_ERR_ARGUMENT, "invalid coulomb descriptor");
+    if (c->kind == LG_COULOMB_EWALD) {
+        // Ewald::new panics (ewald.rs:281-287)
+        if (c->cutoff < 0.0) return fail(e, LG_ERR_ARGUMENT, "the cutoff can not be negative in Ewald");
+        if (c->alpha < 0.0) return fail(e, LG_ERR_ARGUMENT, "alpha can not be negative in Ewald");
+        if (c->kmax <= 0) return fail(e, LG_ERR_ARGUMENT, "kmax can not be 0 in Ewald");
+        if (c->restriction == LG_RESTRICT_SCALE14)
+            return fail(e, LG_ERR_ARGUMENT, "Scaling restriction scheme using Ewald are not implemented");
+    } else if (c->kind == LG_COULOMB_WOLF) {
+        if (!(c->cutoff > 0.0)) return fail(e, LG_ERR_ARGUMENT, "Got a negative cutoff in Wolf summation");
+    } else if (c->kind != LG_COULOMB_NONE) {
+        return fail(e, LG_ERR_ARGUMENT, "unknown coulomb potential");
+    }
+    HostSystem& h = e->sys[s];
+    h.coul = *c;
+    invalidate(e);
+    return check_pair_cutoffs(e, h);
+}
+
+int lg_compute(lg_engine* e, int32_t s, const double* positions, uint32_t terms, uint32_t want, double* forces,
+               double* energy, double virial[9]) {
+    if (!valid_sys(e, s) || !positions) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    int rc = commit(e);
+    if (rc) return rc;
+    const HostSystem& h = e->sys[s];
+    int64_t base = e->begin[s];
+    cudaStream_t st = e->stream;
+    if (h.n) {
+        CUDA_TRY(e, cudaMemcpyAsync(e->pos3.p + 3 * base, positions, 3 * h.n * sizeof(double),
+                                    cudaMemcpyHostToDevice, st));
+        launch_pack_positions(e->b, e->pos3.p, st);
+    }
+    bool ev = (want & (LG_WANT_ENERGY | LG_WANT_VIRIAL)) != 0;
+    rc = compute_batch(e, terms, want, nullptr, nullptr);
+    if (rc) return rc;
+    std::vector<double> f;
+    if ((want & LG_WANT_FORCES) && forces && h.n) {
+        f.resize(3 * h.n);
+        CUDA_TRY(e, cudaMemcpyAsync(f.data(), e->force.p + 3 * base, 3 * h.n * sizeof(double),
+                                    cudaMemcpyDeviceToHost, st));
+    }
+    if (ev)
+        CUDA_TRY(e, cudaMemcpyAsync(e->h_out, e->out.p + (size_t)s * RED_STRIDE, RED_STRIDE * sizeof(double),
+                                    cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(e, cudaStreamSynchronize(st));
+    if ((want & LG_WANT_FORCES) && forces)
+        for (int64_t i = 0; i < 3 * h.n; i++) forces[i] += f[i];
+    if ((want & LG_WANT_ENERGY) && energy) *energy = e->h_out[0];
+    if ((want & LG_WANT_VIRIAL) && virial)
+        for (int c = 0; c < 9; c++) virial[c] = e->h_out[1 + c];
+    return LG_OK;
+}
+
+int lg_compute_device(lg_engine* e, const double* d_positions, uint32_t terms, uint32_t want, double* d_forces,
+                      double* d_energy, double* d_virial, void* stream) {
+    if (!e || !d_positions) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    int rc = commit(e);
+    if (rc) return rc;
+    cudaStream_t user = stream ? (cudaStream_t)stream : e->stream;
+    cudaStream_t st = e->stream;
+    if (user != st) {
+        cudaEvent_t ev;
+        CUDA_TRY(e, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        cudaEventRecord(ev, user);
+        cudaStreamWaitEvent(st, ev, 0);
+        cudaEventDestroy(ev);
+    }
+    launch_pack_positions(e->b, d_positions, st);
+    rc = compute_batch(e, terms, want, (want & LG_WANT_FORCES) ? d_forces : nullptr, nullptr);
+    if (rc) return rc;
+    bool ev = (want & (LG_WANT_ENERGY | LG_WANT_VIRIAL)) != 0;
+    if (ev) {
+        for (int s = 0; s < e->nsys; s++) {
+            if (d_energy && (want & LG_WANT_ENERGY))
+                CUDA_TRY(e, cudaMemcpyAsync(d_energy + s, e->out.p + (size_t)s * RED_STRIDE, sizeof(double),
+                                            cudaMemcpyDeviceToDevice, st));
+            if (d_virial && (want & LG_WANT_VIRIAL))
+                CUDA_TRY(e, cudaMemcpyAsync(d_virial + 9 * s, e->out.p + (size_t)s * RED_STRIDE + 1,
+                                            9 * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        }
+    }
+    if (user != st) {
+        cudaEvent_t ev2;
+        CUDA_TRY(e, cudaEventCreateWithFlags(&ev2, cudaEventDisableTiming));
+        cudaEventRecord(ev2, st);
+        cudaStreamWaitEvent(user, ev2, 0);
+        cudaEventDestroy(ev2);
+    }
+    return LG_OK;
+}
+
+int lg_pairset(lg_engine* e, int32_t s, const double* positions, int32_t family, int32_t* pairs, int64_t capacity,
+               int64_t* count) {
+    if (!valid_sys(e, s) || !positions || !count || (family != 0 && family != 1) || capacity < 0)
+        return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    int rc = commit(e);
+    if (rc) return rc;
+    const HostSystem& h = e->sys[s];
+    int64_t base = e->begin[s];
+    cudaStream_t st = e->stream;
+    if (h.n) {
+        CUDA_TRY(e, cudaMemcpyAsync(e->pos3.p + 3 * base, positions, 3 * h.n * sizeof(double),
+                                    cudaMemcpyHostToDevice, st));
+        launch_pack_positions(e->b, e->pos3.p, st);
+    }
+    // make sure the list is current (and large enough) for these positions
+    rc = compute_batch(e, LG_TERM_PAIRS | LG_TERM_COUL_REAL, LG_WANT_FORCES, nullptr, nullptr);
+    if (rc) return rc;
+    size_t cap = (size_t)std::max<int64_t>(capacity, 1);
+    CUDA_TRY(e, e->pairs_out.alloc(2 * cap));
+    CUDA_TRY(e, e->pairs_count.alloc(1));
+    CUDA_TRY(e, cudaMemsetAsync(e->pairs_count.p, 0, sizeof(unsigned long long), st));
+    launch_pairset(e->b, family, (int)base, (int)(base + h.n), e->pairs_out.p, capacity, e->pairs_count.p, st);
+    CUDA_TRY(e, cudaGetLastError());
+    unsigned long long total = 0;
+    CUDA_TRY(e, cudaMemcpyAsync(&total, e->pairs_count.p, sizeof(total), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(e, cudaStreamSynchronize(st));
+    size_t got = std::min<size_t>(total, (size_t)capacity);
+    if (got && pairs) {
+        std::vector<int32_t> tmp(2 * got);
+        CUDA_TRY(e, cudaMemcpy(tmp.data(), e->pairs_out.p, 2 * got * sizeof(int32_t), cudaMemcpyDeviceToHost));
+        std::vector<std::pair<int32_t, int32_t>> v(got);
+        for (size_t k = 0; k < got; k++) v[k] = {tmp[2 * k], tmp[2 * k + 1]};
+        std::sort(v.begin(), v.end());
+        for (size_t k = 0; k < got; k++) {
+            pairs[2 * k] = v[k].first;
+            pairs[2 * k + 1] = v[k].second;
+        }
+    }
+    *count = (int64_t)total;
+    return LG_OK;
+}
+
+// ---- molecular dynamics -----------------------------------------------------
+int lg_md_setup(lg_engine* e, int32_t s, double dt, double T0, double tau) {
+    if (!valid_sys(e, s) || !(dt > 0.0)) return fail(e, LG_ERR_ARGUMENT, "invalid timestep");
+    if (tau > 0.0) {
+        // BerendsenThermostat::new (thermostats.rs:102-109)
+        if (T0 < 0.0) return fail(e, LG_ERR_ARGUMENT, "The temperature must be positive in thermostats.");
+        if (tau < 1.0) return fail(e, LG_ERR_ARGUMENT, "The timestep must be larger than 1 in berendsen thermostat.");
+    }
+    HostSystem& h = e->sys[s];
+    h.dt = dt;
+    h.T0 = T0;
+    h.tau = tau > 0.0 ? tau : 0.0;
+    h.md_ready = true;
+    if (!e->dirty) {
+        SysDev& d = e->h_sysdev[s];
+        d.dt = h.dt;
+        d.thermo_T = h.T0;
+        d.thermo_tau = h.tau;
+        CUDA_TRY(e, cudaSetDevice(e->opt.device));
+        CUDA_TRY(e, cudaMemcpyAsync(e->sysdev.p + s, &d, sizeof(SysDev), cudaMemcpyHostToDevice, e->stream));
+        // VelocityVerlet::setup: accelerations := 0 (integrators.rs:40-42)
+        CUDA_TRY(e, cudaMemsetAsync(e->acc.p + e->begin[s], 0, h.n * sizeof(double4_32a), e->stream));
+        CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+        if (e->graph) {
+            cudaGraphExecDestroy(e->graph);
+            e->graph = nullptr;
+        }
+    }
+    return LG_OK;
+}
+
+int lg_md_set_state(lg_engine* e, int32_t s, const double* positions, const double* velocities) {
+    if (!valid_sys(e, s) || !positions || !velocities) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    bool was_dirty = e->dirty;
+    int rc = commit(e);
+    if (rc) return rc;
+    const HostSystem& h = e->sys[s];
+    int64_t base = e->begin[s];
+    cudaStream_t st = e->stream;
+    if (h.n == 0) return LG_OK;
+    CUDA_TRY(e, cudaMemcpyAsync(e->pos3.p + 3 * base, positions, 3 * h.n * sizeof(double), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(e, cudaMemcpyAsync(e->vel3.p + 3 * base, velocities, 3 * h.n * sizeof(double), cudaMemcpyHostToDevice, st));
+    // pack only this system's atoms: the other systems keep their state
+    Batch sub = e->b;
+    sub.n = (int)h.n;
+    sub.posq = e->posq.p + base;
+    sub.vel = e->vel.p + base;
+    launch_pack_positions(sub, e->pos3.p + 3 * base, st);
+    launch_pack_velocities(sub, e->vel3.p + 3 * base, st);
+    if (was_dirty) CUDA_TRY(e, cudaMemsetAsync(e->acc.p, 0, e->b.n * sizeof(double4_32a), st));
+    CUDA_TRY(e, cudaGetLastError());
+    CUDA_TRY(e, cudaStreamSynchronize(st));
+    return LG_OK;
+}
+
+int lg_md_get_state(lg_engine* e, int32_t s, double* positions, double* velocities) {
+    if (!valid_sys(e, s)) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    if (e->dirty) return fail(e, LG_ERR_STATE, "no device state: call lg_md_set_state first");
+    CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    const HostSystem& h = e->sys[s];
+    int64_t base = e->begin[s];
+    cudaStream_t st = e->stream;
+    if (h.n == 0) return LG_OK;
+    Batch sub = e->b;
+    sub.n = (int)h.n;
+    sub.posq = e->posq.p + base;
+    sub.vel = e->vel.p + base;
+    launch_unpack_positions(sub, e->pos3.p + 3 * base, st);
+    launch_unpack_velocities(sub, e->vel3.p + 3 * base, st);
+    if (positions)
+        CUDA_TRY(e, cudaMemcpyAsync(positions, e->pos3.p + 3 * base, 3 * h.n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (velocities)
+        CUDA_TRY(e, cudaMemcpyAsync(velocities, e->vel3.p + 3 * base, 3 * h.n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(e, cudaStreamSynchronize(st));
+    return LG_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+void enqueue_md_step(lg_engine* e, bool thermo, cudaStream_t st) {
+    launch_vv_first(e->b, st);
+    enqueue_forces(e, LG_TERM_ALL, false, st);
+    launch_vv_second(e->b, thermo, st);
+    if (thermo) launch_thermostat(e->b, st);
+}
+
+int build_md_graph(lg_engine* e, int steps, bool thermo) {
+    if (e->graph) {
+        cudaGraphExecDestroy(e->graph);
+        e->graph = nullptr;
+    }
+    cudaGraph_t g;
+    CUDA_TRY(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < steps; k++) enqueue_md_step(e, thermo, e->stream);
+    CUDA_TRY(e, cudaStreamEndCapture(e->stream, &g));
+    cudaError_t ce = cudaGraphInstantiate(&e->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) return fail(e, LG_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ce));
+    e->graph_steps = steps;
+    e->graph_thermo = thermo;
+    return LG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lg_md_run(lg_engine* e, int64_t nsteps) {
+    if (!e || nsteps < 0) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    if (e->dirty) return fail(e, LG_ERR_STATE, "no device state: call lg_md_set_state first");
+    bool thermo = false;
+    for (int s = 0; s < e->nsys; s++) {
+        if (!e->sys[s].md_ready) return fail(e, LG_ERR_STATE, "lg_md_setup was not called for every system");
+        if (e->sys[s].tau > 0.0) thermo = true;
+    }
+    const int chunk = 16;
+    cudaStream_t st = e->stream;
+    int64_t done = 0;
+    int retries = 0;
+    // checkpoint buffers: a chunk whose list overflowed is replayed after regrowing
+    DBuf<double4_32a> cp_pos, cp_vel, cp_acc;
+    CUDA_TRY(e, cp_pos.alloc(e->b.n));
+    CUDA_TRY(e, cp_vel.alloc(e->b.n));
+    CUDA_TRY(e, cp_acc.alloc(e->b.n));
+    while (done < nsteps) {
+        int steps = (int)std::min<int64_t>(chunk, nsteps - done);
+        if (!e->graph || e->graph_steps != steps || e->graph_thermo != thermo) {
+            int rc = build_md_graph(e, steps, thermo);
+            if (rc) return rc;
+        }
+        size_t bytes = e->b.n * sizeof(double4_32a);
+        CUDA_TRY(e, cudaMemcpyAsync(cp_pos.p, e->posq.p, bytes, cudaMemcpyDeviceToDevice, st));
+        CUDA_TRY(e, cudaMemcpyAsync(cp_vel.p, e->vel.p, bytes, cudaMemcpyDeviceToDevice, st));
+        CUDA_TRY(e, cudaMemcpyAsync(cp_acc.p, e->acc.p, bytes, cudaMemcpyDeviceToDevice, st));
+        CUDA_TRY(e, cudaGraphLaunch(e->graph, st));
+        uint32_t status;
+        int rc = read_status(e, &status);
+        if (rc) return rc;
+        if (status & ST_OVERFLOW) {
+            if (++retries > 4) return fail(e, LG_ERR_CAPACITY, "neighbour list overflow persisted after regrowing");
+            CUDA_TRY(e, cudaMemcpyAsync(e->posq.p, cp_pos.p, bytes, cudaMemcpyDeviceToDevice, st));
+            CUDA_TRY(e, cudaMemcpyAsync(e->vel.p, cp_vel.p, bytes, cudaMemcpyDeviceToDevice, st));
+            CUDA_TRY(e, cudaMemcpyAsync(e->acc.p, cp_acc.p, bytes, cudaMemcpyDeviceToDevice, st));
+            rc = clear_status_bits(e, ST_OVERFLOW);
+            if (rc) return rc;
+            rc = regrow(e);
+            if (rc) return rc;
+            continue;
+        }
+        done += steps;
+    }
+    return LG_OK;
+}
+
+int lg_md_integrate(lg_engine* e, double* positions, double* velocities, int64_t nsteps) {
+    if (!e || e->nsys != 1) return fail(e, LG_ERR_ARGUMENT, "lg_md_integrate needs a single-system engine");
+    int rc = lg_md_set_state(e, 0, positions, velocities);
+    if (rc) return rc;
+    rc = lg_md_run(e, nsteps);
+    if (rc) return rc;
+    return lg_md_get_state(e, 0, positions, velocities);
+}
+
+// ---- Monte Carlo ---------------------------------------------------------------
+int lg_mc_init(lg_engine* e, int32_t s, const double* positions, double* energy) {
+    (void)e; (void)s; (void)positions; (void)energy;
+    return fail(e, LG_ERR_STATE, "Monte Carlo entry points are not available in this build");
+}
+int lg_mc_move_molecule_cost(lg_engine* e, int32_t s, int64_t molecule, const double* new_positions, double* cost) {
+    (void)s; (void)molecule; (void)new_positions; (void)cost;
+    return fail(e, LG_ERR_STATE, "Monte Carlo entry points are not available in this build");
+}
+int lg_mc_update(lg_engine* e, int32_t s, const double* molecule_positions, double* energy) {
+    (void)s; (void)molecule_positions; (void)energy;
+    return fail(e, LG_ERR_STATE, "Monte Carlo entry points are not available in this build");
+}
+
+}  // extern "C"

@@ -1,0 +1,211 @@
+// device_common.cuh -- data layout shared by the host engine and the kernels,
+// and the device restatement of the reference's per-pair arithmetic.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace lg {
+
+constexpr double PI = 3.14159265358979323846;
+constexpr double FRAC_2_SQRT_PI = 1.12837916709551257390;
+// lumol-core/src/consts.rs:9,15
+constexpr double K_BOLTZMANN = 8.31446284161522e-7;
+constexpr double FOUR_PI_EPSILON_0 = 7.197589831304046;
+
+// Pair potential table entry: one PairInteraction (energy/pairs.rs:57-95).
+struct PairDev {
+    int32_t type;         // LG_PAIR_*
+    int32_t shifted;
+    int32_t restriction;  // LG_RESTRICT_*
+    int32_t tail;
+    double p0, p1, p2;    // LJ: sigma, epsilon; Buckingham: a, c, rho; Harmonic: k, x0
+    double cutoff;
+    double shift;         // potential.energy(cutoff) when shifted (pairs.rs:86-95)
+    double scale14;
+    float cutoff2_f;      // mixed path: cutoff^2 in FP32
+    float pad_f;
+};
+
+// Per-system descriptor (one Lumol System).
+struct SysDev {
+    double L[3];          // orthorhombic cell lengths (UnitCell::a/b/c)
+    double invL[3];       // 1 / L (fast path of the exact minimum image)
+    double rlist;         // neighbour-list radius = max cutoff + skin
+    double half_skin2;    // (skin / 2)^2: rebuild threshold on displacement
+    int32_t begin, end;   // atom range [begin, end) in the batch arrays
+    int32_t ptab, nk;     // offset of the pair table and number of kinds
+    int32_t coul;         // LG_COULOMB_*
+    int32_t coul_restr;   // LG_RESTRICT_*
+    double coul_rc;       // Coulomb cutoff
+    double alpha;         // Ewald alpha, or Wolf alpha = PI / cutoff
+    double wolf_ec, wolf_fc;  // Wolf energy / force constants (wolf.rs:68-84)
+    double coul_scale14;
+    int32_t kbegin, kend; // Ewald k-vectors [kbegin, kend) in the batch k arrays
+    int32_t kmax;
+    int32_t ncell[3];     // neighbour cells per dimension
+    int32_t cell_begin;   // offset of this system's cells in the batch cell arrays
+    int32_t needs_path;   // 1 when a restriction needs bond paths (Exclude*/Scale14)
+    double k1[3];         // 2 PI * inv(cell)[d][d]: k-vector of index 1 per axis (cells.rs:224-226)
+    // molecular dynamics
+    double dt;
+    double thermo_T, thermo_tau;  // Berendsen (tau <= 0: none)
+    double dof;                   // 3 N (DegreesOfFreedom::Particles)
+    float Lf[3], invLf[3];        // FP32 copies for the list build and the mixed path
+    float rlist2_f;               // (rlist + margin)^2 in FP32
+    float coul_rc2_f;
+};
+
+// One Ewald k-vector with its factors (ewald.rs:102-116).
+struct KVecDev {
+    int32_t ikx, iky, ikz, sys;
+    double energy;      // 4 pi / V exp(-k^2 / (4 alpha^2)) / k^2
+    double field[3];    // 2 energy k
+    double virial[6];   // energy (1 - 2 (1/k^2 + 1/(4 alpha^2)) k k^T), symmetric xx xy xz yy yz zz
+};
+
+// Status word bits (device -> host).
+enum : uint32_t {
+    ST_REBUILD = 1u,        // neighbour list must be rebuilt
+    ST_OVERFLOW = 2u,       // neighbour list capacity exceeded
+    ST_NONFINITE = 4u,      // non-finite energy
+    ST_SPECIAL_OVF = 8u,    // bond-path table overflow
+};
+
+// Number of energy slots per system in the reduction output:
+// [pairs, coulomb real (Ewald real or Wolf), bonds, angles, kspace] then virial 9.
+enum { E_PAIRS = 0, E_COUL = 1, E_BONDS = 2, E_ANGLES = 3, E_KSPACE = 4, N_ESLOT = 5 };
+enum { RED_STRIDE = N_ESLOT + 9 };
+
+// ---------------------------------------------------------------------------
+// Exact minimum image (cells.rs:284-301, orthorhombic branch):
+//   d -= round(d / L) * L
+// with a true division, round half away from zero, and no contraction.  The
+// fast path multiplies by 1/L; the result of round() can only differ from the
+// reference when d/L is within a few ulps of a half-integer, in which case the
+// true division is taken.  The multiply and subtract are rounded separately.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double exact_image(double d, double L, double invL) {
+    double t = __dmul_rn(d, invL);
+    double rt = round(t);
+    if (fabs(__dsub_rn(t, rt)) > 0.4999999999 || fabs(t) > 1.0e5) rt = round(__ddiv_rn(d, L));
+    return __dsub_rn(d, __dmul_rn(rt, L));
+}
+
+// Vector3D::norm2 then f64::sqrt (types/vectors.rs:102-117), unfused.
+__device__ __forceinline__ double exact_norm(double x, double y, double z) {
+    double r2 = __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
+    return __dsqrt_rn(r2);
+}
+
+// Configuration::nearest_image(i, j) = image(r_i - r_j) (configuration.rs:399-403)
+__device__ __forceinline__ void exact_nearest_image(const SysDev& s, double xi, double yi, double zi,
+                                                    double xj, double yj, double zj, double& dx,
+                                                    double& dy, double& dz) {
+    dx = exact_image(__dsub_rn(xi, xj), s.L[0], s.invL[0]);
+    dy = exact_image(__dsub_rn(yi, yj), s.L[1], s.invL[1]);
+    dz = exact_image(__dsub_rn(zi, zj), s.L[2], s.invL[2]);
+}
+
+// PairRestriction::information (restrictions.rs:85-115).  path: 0 none
+// (different molecules), 2 one bond, 3 two bonds, 4 three bonds, 5 far.
+__device__ __forceinline__ bool restriction_excluded(int restriction, int path) {
+    bool same = path != 0;
+    switch (restriction) {
+        case 1: return !same;                               // IntraMolecular
+        case 2: return same;                                // InterMolecular
+        case 3: return path == 2;                           // Exclude12
+        case 4: case 6: return path == 2 || path == 3;      // Exclude13, Scale14
+        case 5: return path == 2 || path == 3 || path == 4; // Exclude14
+        default: return false;                              // None
+    }
+}
+__device__ __forceinline__ double restriction_scaling(int restriction, int path, double s14) {
+    return (restriction == 6 && path == 4) ? s14 : 1.0;
+}
+
+// f64::powi(x, 6) as LLVM expands it: x^2 * (x^2)^2
+__device__ __forceinline__ double powi6(double x) {
+    double x2 = x * x;
+    return x2 * (x2 * x2);
+}
+
+// Potential::energy / force of the pair potentials (functions.rs:85-143, 287-299).
+// inv_r = 1 / r.
+__device__ __forceinline__ void pair_energy_force(const PairDev& p, double r, double inv_r,
+                                                  double& e, double& f) {
+    switch (p.type) {
+        case 2: {  // LennardJones
+            double s6 = powi6(p.p0 * inv_r);
+            e = 4.0 * p.p1 * (s6 * s6 - s6);
+            f = -24.0 * p.p1 * (s6 - 2.0 * (s6 * s6)) * inv_r;
+            break;
+        }
+        case 3: {  // Buckingham
+            double ir3 = inv_r * inv_r * inv_r;
+            double ex = exp(-r / p.p2);
+            e = p.p0 * ex - p.p1 * (ir3 * ir3);
+            f = p.p0 / p.p2 * ex - 6.0 * p.p1 * (ir3 * ir3 * inv_r);
+            break;
+        }
+        case 4: {  // Harmonic
+            double dx = r - p.p1;
+            e = 0.5 * p.p0 * dx * dx;
+            f = p.p0 * (p.p1 - r);
+            break;
+        }
+        default:
+            e = 0.0;
+            f = 0.0;
+    }
+    if (p.shifted) e -= p.shift;
+}
+
+// Ewald real-space pair term (ewald.rs:383-428): energy and force / r.
+__device__ __forceinline__ void ewald_real_pair(double alpha, bool excluded, double qiqj, double r,
+                                                double inv_r, double& e, double& f_over_r) {
+    double ar = alpha * r;
+    double pref = qiqj * (1.0 / FOUR_PI_EPSILON_0);
+    double g = alpha * FRAC_2_SQRT_PI * exp(-ar * ar);
+    if (excluded) {
+        double erfv = erf(ar);
+        e = -pref * erfv * inv_r;
+        f_over_r = pref * inv_r * inv_r * (g - erfv * inv_r);
+    } else {
+        double erfcv = erfc(ar);
+        e = pref * erfcv * inv_r;
+        f_over_r = pref * inv_r * inv_r * (g + erfcv * inv_r);
+    }
+}
+
+// Wolf pair term (wolf.rs:90-117): energy and force / r.
+__device__ __forceinline__ void wolf_pair(const SysDev& s, double qiqj, double r, double inv_r,
+                                          double& e, double& f_over_r) {
+    double ar = s.alpha * r;
+    double erfcv = erfc(ar);
+    e = qiqj * (erfcv * inv_r - s.wolf_ec) * (1.0 / FOUR_PI_EPSILON_0);
+    double factor = erfcv * inv_r * inv_r + s.alpha * FRAC_2_SQRT_PI * exp(-ar * ar) * inv_r;
+    f_over_r = qiqj * (factor - s.wolf_fc) * inv_r * (1.0 / FOUR_PI_EPSILON_0);
+}
+
+// Bond path lookup in the per-atom table of same-molecule pairs closer than
+// four bonds.  Returns 0 (different molecules), 2, 3, 4 or 5 (far).
+__device__ __forceinline__ int bond_path(int i, int j, int mol_i, int mol_j, const int* spec_off,
+                                         const int* spec_j, const int8_t* spec_path) {
+    if (mol_i != mol_j) return 0;
+    for (int k = spec_off[i]; k < spec_off[i + 1]; k++)
+        if (spec_j[k] == j) return spec_path[k];
+    return 5;
+}
+
+// Warp-level sum of a double.
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_sum_f(float v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+}  // namespace lg

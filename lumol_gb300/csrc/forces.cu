@@ -1,0 +1,529 @@
+// forces.cu -- FP64 force / energy / virial kernels of the plain path.
+//
+// Pair potentials (sys/compute.rs:30-59, sys/energy.rs:32-59, compute.rs:198-231)
+// and real-space Coulomb (ewald.rs:383-530, wolf.rs:90-282) run in one pass over
+// the full neighbour list, one warp per atom i: the lanes walk i's neighbours,
+// apply the reference's exact cutoff tests, and the per-atom force is a warp
+// sum.  No force is scattered, so every atom's force is summed in a fixed order
+// and results do not depend on the rest of the batch.  Energies and virials are
+// counted once per pair (j > i) into per-atom slots that a per-system reduction
+// adds up in a fixed order.
+#include "kernels.h"
+
+namespace lg {
+
+// The reference's decision whether pair (i, j) contributes, for one family,
+// shared by the force kernel and the pair-set export so both see the same set.
+struct PairDecision {
+    bool pair_in;      // pair potential contributes (r < cutoff, not excluded)
+    bool coul_in;      // real-space Coulomb contributes
+    bool coul_excl;    // Ewald excluded-pair correction (-erf term)
+    double pair_scale; // restriction scaling of the pair potential
+    double coul_scale; // restriction scaling of Wolf
+};
+
+__device__ __forceinline__ PairDecision decide_pair(const SysDev& s, const PairDev& p, uint32_t terms,
+                                                    int i, int j, int mi, int mj, double qi, double qj,
+                                                    double r, const int* spec_off, const int* spec_j,
+                                                    const int8_t* spec_path) {
+    PairDecision d{false, false, false, 1.0, 1.0};
+    int path = -1;
+    if ((terms & 1u) && p.type != 0 && !(r >= p.cutoff)) {  // pairs.rs:185-218
+        if (p.restriction != 0) {
+            path = (p.restriction <= 2) ? (mi != mj ? 0 : 5)
+                                        : bond_path(i, j, mi, mj, spec_off, spec_j, spec_path);
+            if (!restriction_excluded(p.restriction, path)) {
+                d.pair_in = true;
+                d.pair_scale = restriction_scaling(p.restriction, path, p.scale14);
+            }
+        } else {
+            d.pair_in = true;
+        }
+    }
+    if ((terms & 16u) && s.coul != 0 && qi != 0.0 && qj != 0.0 && !(r > s.coul_rc)) {
+        bool excl = false;
+        if (s.coul_restr != 0) {
+            if (path < 0 || (s.coul_restr > 2 && path == 5 && mi == mj))
+                path = (s.coul_restr <= 2) ? (mi != mj ? 0 : 5)
+                                           : bond_path(i, j, mi, mj, spec_off, spec_j, spec_path);
+            excl = restriction_excluded(s.coul_restr, path);
+            d.coul_scale = restriction_scaling(s.coul_restr, path, s.coul_scale14);
+        }
+        if (s.coul == 1) {  // Ewald: excluded pairs get the -erf correction (ewald.rs:390-397)
+            d.coul_in = true;
+            d.coul_excl = excl;
+        } else {  // Wolf: excluded pairs are skipped (wolf.rs:186-189)
+            d.coul_in = !excl;
+        }
+    }
+    return d;
+}
+
+template <bool EV>
+__global__ void __launch_bounds__(256) pair_fp64_kernel(
+    int n, const double4_32a* __restrict__ posq, const int* __restrict__ kind, const int* __restrict__ mol,
+    const int* __restrict__ sysid, const SysDev* __restrict__ sys, const PairDev* __restrict__ ptab,
+    const int* __restrict__ nbr, const int* __restrict__ nnb, int maxnb, const int* __restrict__ spec_off,
+    const int* __restrict__ spec_j, const int8_t* __restrict__ spec_path, uint32_t terms,
+    double* __restrict__ force, double* __restrict__ red) {
+    int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (i >= n) return;
+    const SysDev& s = sys[sysid[i]];
+    double4_32a pi = posq[i];
+    int ki = kind[i], mi = mol[i];
+    const PairDev* prow = ptab + s.ptab + ki * s.nk;
+    double fx = 0.0, fy = 0.0, fz = 0.0;
+    double ep = 0.0, ec = 0.0;
+    double wxx = 0.0, wxy = 0.0, wxz = 0.0, wyy = 0.0, wyz = 0.0, wzz = 0.0;
+    int cnt = nnb[i];
+    const int* list = nbr + (size_t)i * maxnb;
+    for (int k = lane; k < cnt; k += 32) {
+        int j = list[k];
+        double4_32a pj = posq[j];
+        double dx, dy, dz;
+        exact_nearest_image(s, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z, dx, dy, dz);
+        double r = exact_norm(dx, dy, dz);
+        const PairDev& p = prow[kind[j]];
+        PairDecision dec = decide_pair(s, p, terms, i, j, mi, mol[j], pi.w, pj.w, r, spec_off, spec_j,
+                                       spec_path);
+        if (!(dec.pair_in || dec.coul_in)) continue;
+        double inv_r = 1.0 / r;
+        double f_over_r = 0.0;
+        bool count = EV && (j > i);
+        if (dec.pair_in) {
+            double e, f;
+            pair_energy_force(p, r, inv_r, e, f);
+            f_over_r += dec.pair_scale * f * inv_r;
+            if (count) ep += dec.pair_scale * e;
+        }
+        if (dec.coul_in) {
+            double e, fr;
+            if (s.coul == 1) {
+                ewald_real_pair(s.alpha, dec.coul_excl, pi.w * pj.w, r, inv_r, e, fr);
+            } else {
+                wolf_pair(s, pi.w * pj.w, r, inv_r, e, fr);
+                e *= dec.coul_scale;
+                fr *= dec.coul_scale;
+            }
+            f_over_r += fr;
+            if (count) ec += e;
+        }
+        double gx = f_over_r * dx, gy = f_over_r * dy, gz = f_over_r * dz;
+        fx += gx;
+        fy += gy;
+        fz += gz;
+        if (count) {
+            wxx += gx * dx;
+            wxy += gx * dy;
+            wxz += gx * dz;
+            wyy += gy * dy;
+            wyz += gy * dz;
+            wzz += gz * dz;
+        }
+    }
+    fx = warp_sum(fx);
+    fy = warp_sum(fy);
+    fz = warp_sum(fz);
+    if (EV) {
+        ep = warp_sum(ep);
+        ec = warp_sum(ec);
+        wxx = warp_sum(wxx);
+        wxy = warp_sum(wxy);
+        wxz = warp_sum(wxz);
+        wyy = warp_sum(wyy);
+        wyz = warp_sum(wyz);
+        wzz = warp_sum(wzz);
+    }
+    if (lane == 0) {
+        force[3 * i] += fx;
+        force[3 * i + 1] += fy;
+        force[3 * i + 2] += fz;
+        if (EV) {
+            // Wolf self energy, subtracted once per charged atom (wolf.rs:205)
+            if ((terms & 16u) && s.coul == 2 && pi.w != 0.0)
+                ec -= pi.w * pi.w * 0.5 * (s.wolf_ec + s.alpha * FRAC_2_SQRT_PI) / FOUR_PI_EPSILON_0;
+            double* rr = red + (size_t)i * RED_STRIDE;
+            rr[E_PAIRS] += ep;
+            rr[E_COUL] += ec;
+            double* w = rr + N_ESLOT;
+            w[0] += wxx; w[1] += wxy; w[2] += wxz;
+            w[3] += wxy; w[4] += wyy; w[5] += wyz;
+            w[6] += wxz; w[7] += wyz; w[8] += wzz;
+        }
+    }
+}
+
+void launch_pair_forces(const Batch& b, uint32_t terms, bool ev, cudaStream_t st) {
+    if (b.n == 0) return;
+    int tb = 256;
+    long long threads = (long long)b.n * 32;
+    unsigned grid = (unsigned)((threads + tb - 1) / tb);
+    if (ev)
+        pair_fp64_kernel<true><<<grid, tb, 0, st>>>(b.n, b.posq, b.kind, b.mol, b.sysid, b.sys, b.ptab,
+                                                    b.nbr, b.nnb, b.maxnb, b.spec_off, b.spec_j,
+                                                    b.spec_path, terms, b.force, b.red);
+    else
+        pair_fp64_kernel<false><<<grid, tb, 0, st>>>(b.n, b.posq, b.kind, b.mol, b.sysid, b.sys, b.ptab,
+                                                     b.nbr, b.nnb, b.maxnb, b.spec_off, b.spec_j,
+                                                     b.spec_path, terms, b.force, b.red);
+}
+
+// ---------------------------------------------------------------------------
+// Bonds and angles, gathered per atom (compute.rs:62-84, 233-241;
+// energy.rs:90-120; UnitCell::angle_and_derivatives, cells.rs:335-362).
+// ---------------------------------------------------------------------------
+template <bool EV>
+__global__ void bonded_kernel(int n, const double4_32a* __restrict__ posq, const int* __restrict__ sysid,
+                              const SysDev* __restrict__ sys, const int* __restrict__ bt_off,
+                              const int4* __restrict__ bt, const int* __restrict__ bt_role,
+                              const double2* __restrict__ bt_par, uint32_t terms,
+                              double* __restrict__ force, double* __restrict__ red) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const SysDev& s = sys[sysid[i]];
+    double fx = 0.0, fy = 0.0, fz = 0.0, eb = 0.0, ea = 0.0;
+    double w[6] = {0, 0, 0, 0, 0, 0};
+    for (int t = bt_off[i]; t < bt_off[i + 1]; t++) {
+        int4 term = bt[t];
+        int role = bt_role[t];
+        double2 par = bt_par[t];  // (k, x0); k is NaN for a NullPotential
+        bool null_pot = isnan(par.x);
+        if (term.x == 0) {
+            if (!(terms & 4u)) continue;
+            double4_32a pa = posq[term.y], pb = posq[term.z];
+            double dx, dy, dz;
+            exact_nearest_image(s, pa.x, pa.y, pa.z, pb.x, pb.y, pb.z, dx, dy, dz);
+            double r = exact_norm(dx, dy, dz);
+            double f = null_pot ? 0.0 : par.x * (par.y - r);
+            double gx = f * (dx / r), gy = f * (dy / r), gz = f * (dz / r);
+            double sgn = role == 0 ? 1.0 : -1.0;
+            fx += sgn * gx;
+            fy += sgn * gy;
+            fz += sgn * gz;
+            if (EV && role == 0) {
+                double dr = r - par.y;
+                eb += null_pot ? 0.0 : 0.5 * par.x * dr * dr;
+                w[0] += gx * dx; w[1] += gx * dy; w[2] += gx * dz;
+                w[3] += gy * dy; w[4] += gy * dz; w[5] += gz * dz;
+            }
+        } else {
+            if (!(terms & 8u)) continue;
+            double4_32a p1 = posq[term.y], p2 = posq[term.z], p3 = posq[term.w];
+            double ax, ay, az, bx, by, bz;
+            exact_nearest_image(s, p1.x, p1.y, p1.z, p2.x, p2.y, p2.z, ax, ay, az);  // r12
+            exact_nearest_image(s, p3.x, p3.y, p3.z, p2.x, p2.y, p2.z, bx, by, bz);  // r23
+            double n12 = exact_norm(ax, ay, az), n23 = exact_norm(bx, by, bz);
+            double ux = ax / n12, uy = ay / n12, uz = az / n12;
+            double vx = bx / n23, vy = by / n23, vz = bz / n23;
+            double cs = ux * vx + uy * vy + uz * vz;
+            double sin_inv = 1.0 / sqrt(1.0 - cs * cs);
+            double theta = acos(cs);
+            double f = null_pot ? 0.0 : par.x * (par.y - theta);
+            double gx, gy, gz;
+            double d1x = sin_inv * (cs * ux - vx) / n12, d1y = sin_inv * (cs * uy - vy) / n12,
+                   d1z = sin_inv * (cs * uz - vz) / n12;
+            double d3x = sin_inv * (cs * vx - ux) / n23, d3y = sin_inv * (cs * vy - uy) / n23,
+                   d3z = sin_inv * (cs * vz - uz) / n23;
+            if (role == 0) {
+                gx = d1x; gy = d1y; gz = d1z;
+            } else if (role == 2) {
+                gx = d3x; gy = d3y; gz = d3z;
+            } else {
+                gx = -(d1x + d3x); gy = -(d1y + d3y); gz = -(d1z + d3z);
+            }
+            fx += f * gx;
+            fy += f * gy;
+            fz += f * gz;
+            if (EV && role == 0 && !null_pot) {
+                // EnergyEvaluator::angles uses UnitCell::angle (cells.rs:322-330)
+                double th = acos((ax * bx + ay * by + az * bz) / (n12 * n23));
+                double dt = th - par.y;
+                ea += 0.5 * par.x * dt * dt;
+            }
+        }
+    }
+    force[3 * i] += fx;
+    force[3 * i + 1] += fy;
+    force[3 * i + 2] += fz;
+    if (EV) {
+        double* rr = red + (size_t)i * RED_STRIDE;
+        rr[E_BONDS] += eb;
+        rr[E_ANGLES] += ea;
+        double* v = rr + N_ESLOT;
+        v[0] += w[0]; v[1] += w[1]; v[2] += w[2];
+        v[3] += w[1]; v[4] += w[3]; v[5] += w[4];
+        v[6] += w[2]; v[7] += w[4]; v[8] += w[5];
+    }
+}
+
+void launch_bonded(const Batch& b, uint32_t terms, bool ev, cudaStream_t st) {
+    if (b.n == 0 || !b.bt_off) return;
+    int tb = 128;
+    unsigned grid = (b.n + tb - 1) / tb;
+    if (ev)
+        bonded_kernel<true><<<grid, tb, 0, st>>>(b.n, b.posq, b.sysid, b.sys, b.bt_off, b.bt, b.bt_role,
+                                                 b.bt_par, terms, b.force, b.red);
+    else
+        bonded_kernel<false><<<grid, tb, 0, st>>>(b.n, b.posq, b.sysid, b.sys, b.bt_off, b.bt, b.bt_role,
+                                                  b.bt_par, terms, b.force, b.red);
+}
+
+// ---------------------------------------------------------------------------
+// Ewald k-space (ewald.rs:633-733)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// Ewald::eik_dot_r, per-atom part: e^{i k.r} for k = 0..kmax along each axis,
+// k = 1 from polar(1, k1 . r) and the others by the same recursion.
+__global__ void eikr_kernel(int n, int kdim, const double4_32a* __restrict__ posq,
+                            const int* __restrict__ sysid, const SysDev* __restrict__ sys,
+                            double2* __restrict__ eikr) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 3 * n) return;
+    int axis = t / n, i = t - axis * n;
+    const SysDev& s = sys[sysid[i]];
+    if (s.coul != 1) return;
+    double4_32a p = posq[i];
+    double x = axis == 0 ? p.x : (axis == 1 ? p.y : p.z);
+    double phi = s.k1[axis] * x;
+    double sn, cs;
+    sincos(phi, &sn, &cs);
+    double2 e1 = make_double2(cs, sn);
+    eikr[(size_t)(0 * 3 + axis) * n + i] = make_double2(1.0, 0.0);
+    eikr[(size_t)(1 * 3 + axis) * n + i] = e1;
+    double2 e = e1;
+    for (int kk = 2; kk <= s.kmax; kk++) {
+        e = cmul(e, e1);
+        eikr[(size_t)(kk * 3 + axis) * n + i] = e;
+    }
+}
+
+__device__ __forceinline__ double2 eikr_at(const double2* __restrict__ eikr, int n, int kk, int axis, int i) {
+    if (kk >= 0) return eikr[(size_t)(kk * 3 + axis) * n + i];
+    double2 v = eikr[(size_t)((-kk) * 3 + axis) * n + i];
+    return make_double2(v.x, -v.y);
+}
+
+// rho(k) = sum_i q_i e^{i k.r_i}: one block per k-vector, fixed-order tree sum.
+template <bool EV>
+__global__ void __launch_bounds__(256) rho_kernel(int n, const double4_32a* __restrict__ posq,
+                                                  const SysDev* __restrict__ sys,
+                                                  const KVecDev* __restrict__ kvec,
+                                                  const double2* __restrict__ eikr,
+                                                  double2* __restrict__ rho, double* __restrict__ kred) {
+    __shared__ double sre[256], sim[256];
+    int k = blockIdx.x;
+    KVecDev kv = kvec[k];
+    const SysDev& s = sys[kv.sys];
+    double re = 0.0, im = 0.0;
+    for (int i = s.begin + threadIdx.x; i < s.end; i += blockDim.x) {
+        double2 phi = cmul(cmul(eikr_at(eikr, n, kv.ikx, 0, i), eikr_at(eikr, n, kv.iky, 1, i)),
+                           eikr_at(eikr, n, kv.ikz, 2, i));
+        double q = posq[i].w;
+        re += q * phi.x;
+        im += q * phi.y;
+    }
+    sre[threadIdx.x] = re;
+    sim[threadIdx.x] = im;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            sre[threadIdx.x] += sre[threadIdx.x + o];
+            sim[threadIdx.x] += sim[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double2 r = make_double2(sre[0], sim[0]);
+        rho[k] = r;
+        if (EV) {
+            double nrm = r.x * r.x + r.y * r.y;
+            double* out = kred + (size_t)k * 7;
+            out[0] = kv.energy * nrm;
+            for (int c = 0; c < 6; c++) out[1 + c] = nrm * kv.virial[c];
+        }
+    }
+}
+
+// field_i = sum_k Im(e^{i k.r_i} conj(rho_k)) field_k over one chunk of k-vectors.
+__global__ void __launch_bounds__(128) field_kernel(int n, int kchunk, const int* __restrict__ sysid,
+                                                    const SysDev* __restrict__ sys,
+                                                    const KVecDev* __restrict__ kvec,
+                                                    const double2* __restrict__ eikr,
+                                                    const double2* __restrict__ rho,
+                                                    double* __restrict__ fpart) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int c = blockIdx.y;
+    if (i >= n) return;
+    const SysDev& s = sys[sysid[i]];
+    double fx = 0.0, fy = 0.0, fz = 0.0;
+    if (s.coul == 1) {
+        int k0 = s.kbegin + c * kchunk;
+        int k1 = min(k0 + kchunk, s.kend);
+        for (int k = k0; k < k1; k++) {
+            const KVecDev& kv = kvec[k];
+            double2 e = cmul(cmul(eikr_at(eikr, n, kv.ikx, 0, i), eikr_at(eikr, n, kv.iky, 1, i)),
+                             eikr_at(eikr, n, kv.ikz, 2, i));
+            double2 r = rho[k];
+            double imag = e.x * (-r.y) + e.y * r.x;
+            fx += imag * kv.field[0];
+            fy += imag * kv.field[1];
+            fz += imag * kv.field[2];
+        }
+    }
+    double* out = fpart + (size_t)c * 3 * n + 3 * (size_t)i;
+    out[0] = fx;
+    out[1] = fy;
+    out[2] = fz;
+}
+
+// force_i += q_i field_i / (4 pi eps0) (ewald.rs:716-719)
+__global__ void field_reduce_kernel(int n, int nchunks, const double4_32a* __restrict__ posq,
+                                    const int* __restrict__ sysid, const SysDev* __restrict__ sys,
+                                    const double* __restrict__ fpart, double* __restrict__ force) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (sys[sysid[i]].coul != 1) return;
+    double f[3] = {0.0, 0.0, 0.0};
+    for (int c = 0; c < nchunks; c++)
+        for (int d = 0; d < 3; d++) f[d] += fpart[(size_t)c * 3 * n + 3 * (size_t)i + d];
+    double q = posq[i].w;
+    for (int d = 0; d < 3; d++) force[3 * i + d] += q * f[d] / FOUR_PI_EPSILON_0;
+}
+
+void launch_kspace(const Batch& b, bool forces, bool ev, cudaStream_t st) {
+    if (b.nkvec == 0 || b.n == 0) return;
+    int tb = 256;
+    eikr_kernel<<<(3 * b.n + tb - 1) / tb, tb, 0, st>>>(b.n, b.kdim, b.posq, b.sysid, b.sys, b.eikr);
+    if (ev)
+        rho_kernel<true><<<b.nkvec, 256, 0, st>>>(b.n, b.posq, b.sys, b.kvec, b.eikr, b.rho, b.kred);
+    else
+        rho_kernel<false><<<b.nkvec, 256, 0, st>>>(b.n, b.posq, b.sys, b.kvec, b.eikr, b.rho, b.kred);
+    if (forces) {
+        dim3 grid((b.n + 127) / 128, b.nkchunks);
+        field_kernel<<<grid, 128, 0, st>>>(b.n, b.kchunk, b.sysid, b.sys, b.kvec, b.eikr, b.rho, b.fpart);
+        field_reduce_kernel<<<(b.n + 127) / 128, 128, 0, st>>>(b.n, b.nkchunks, b.posq, b.sysid, b.sys,
+                                                               b.fpart, b.force);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Per-system reduction of energies and virials, in a fixed order.
+// out[s * RED_STRIDE]: energy of the requested terms, then the virial (9).
+// host_const[s * RED_STRIDE]: tail energy, tail virial (trace / 3), Ewald self energy.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) reduce_kernel(const SysDev* __restrict__ sys,
+                                                     const double* __restrict__ red,
+                                                     const double* __restrict__ kred,
+                                                     const double* __restrict__ host_const,
+                                                     uint32_t terms, int use_kspace,
+                                                     double* __restrict__ out, uint32_t* status) {
+    __shared__ double sh[RED_STRIDE][256];
+    int s_idx = blockIdx.x;
+    const SysDev& s = sys[s_idx];
+    double acc[RED_STRIDE];
+    for (int c = 0; c < RED_STRIDE; c++) acc[c] = 0.0;
+    for (int i = s.begin + threadIdx.x; i < s.end; i += blockDim.x) {
+        const double* rr = red + (size_t)i * RED_STRIDE;
+        for (int c = 0; c < RED_STRIDE; c++) acc[c] += rr[c];
+    }
+    if (use_kspace && s.coul == 1) {
+        for (int k = s.kbegin + threadIdx.x; k < s.kend; k += blockDim.x) {
+            const double* kk = kred + (size_t)k * 7;
+            acc[E_KSPACE] += kk[0];
+            const double* v = kk + 1;  // xx xy xz yy yz zz
+            acc[N_ESLOT + 0] += v[0] / FOUR_PI_EPSILON_0;
+            acc[N_ESLOT + 1] += v[1] / FOUR_PI_EPSILON_0;
+            acc[N_ESLOT + 2] += v[2] / FOUR_PI_EPSILON_0;
+            acc[N_ESLOT + 3] += v[1] / FOUR_PI_EPSILON_0;
+            acc[N_ESLOT + 4] += v[3] / FOUR_PI_EPSILON_0;
+            acc[N_ESLOT + 5] += v[4] / FOUR_PI_EPSILON_0;
+            acc[N_ESLOT + 6] += v[2] / FOUR_PI_EPSILON_0;
+            acc[N_ESLOT + 7] += v[4] / FOUR_PI_EPSILON_0;
+            acc[N_ESLOT + 8] += v[5] / FOUR_PI_EPSILON_0;
+        }
+    }
+    for (int c = 0; c < RED_STRIDE; c++) sh[c][threadIdx.x] = acc[c];
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o)
+            for (int c = 0; c < RED_STRIDE; c++) sh[c][threadIdx.x] += sh[c][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double* hc = host_const + (size_t)s_idx * RED_STRIDE;
+        double e = 0.0;
+        if (terms & 1u) e += sh[E_PAIRS][0];
+        if (terms & 2u) e += hc[0];
+        if (terms & 4u) e += sh[E_BONDS][0];
+        if (terms & 8u) e += sh[E_ANGLES][0];
+        if (terms & 16u) e += sh[E_COUL][0];
+        if ((terms & 32u) && s.coul == 1) e += hc[2];
+        if ((terms & 64u) && s.coul == 1) e += sh[E_KSPACE][0] / FOUR_PI_EPSILON_0;
+        double* o = out + (size_t)s_idx * RED_STRIDE;
+        o[0] = e;
+        for (int c = 0; c < 9; c++) o[1 + c] = sh[N_ESLOT + c][0];
+        if (terms & 2u) {
+            o[1] += hc[1];
+            o[5] += hc[1];
+            o[9] += hc[1];
+        }
+    }
+}
+
+void launch_reduce(const Batch& b, uint32_t terms, bool kspace, double* out, cudaStream_t st) {
+    reduce_kernel<<<b.nsys, 256, 0, st>>>(b.sys, b.red, b.kred, b.host_const, terms, kspace ? 1 : 0, out,
+                                          b.status);
+}
+
+// ---------------------------------------------------------------------------
+// Pair-set export: the (i, j), i < j, that the force kernel counts, decided by
+// the same decide_pair().  Order is arbitrary; the host sorts.
+// ---------------------------------------------------------------------------
+__global__ void pairset_kernel(int n, int family, int a_begin, int a_end, const double4_32a* __restrict__ posq,
+                               const int* __restrict__ kind, const int* __restrict__ mol,
+                               const int* __restrict__ sysid, const SysDev* __restrict__ sys,
+                               const PairDev* __restrict__ ptab, const int* __restrict__ nbr,
+                               const int* __restrict__ nnb, int maxnb, const int* __restrict__ spec_off,
+                               const int* __restrict__ spec_j, const int8_t* __restrict__ spec_path,
+                               int* __restrict__ out, long long cap, unsigned long long* count) {
+    int i = a_begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a_end) return;
+    const SysDev& s = sys[sysid[i]];
+    double4_32a pi = posq[i];
+    int ki = kind[i], mi = mol[i];
+    uint32_t terms = family == 0 ? 1u : 16u;
+    for (int k = 0; k < nnb[i]; k++) {
+        int j = nbr[(size_t)i * maxnb + k];
+        if (j <= i) continue;
+        double4_32a pj = posq[j];
+        double dx, dy, dz;
+        exact_nearest_image(s, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z, dx, dy, dz);
+        double r = exact_norm(dx, dy, dz);
+        const PairDev& p = ptab[s.ptab + ki * s.nk + kind[j]];
+        PairDecision d = decide_pair(s, p, terms, i, j, mi, mol[j], pi.w, pj.w, r, spec_off, spec_j, spec_path);
+        bool in = family == 0 ? d.pair_in : d.coul_in;
+        if (in) {
+            unsigned long long slot = atomicAdd(count, 1ull);
+            if ((long long)slot < cap) {
+                out[2 * slot] = i - s.begin;
+                out[2 * slot + 1] = j - s.begin;
+            }
+        }
+    }
+}
+
+void launch_pairset(const Batch& b, int family, int a_begin, int a_end, int* out, long long cap,
+                    unsigned long long* count, cudaStream_t st) {
+    int tb = 128;
+    int na = a_end - a_begin;
+    if (na <= 0) return;
+    pairset_kernel<<<(na + tb - 1) / tb, tb, 0, st>>>(b.n, family, a_begin, a_end, b.posq, b.kind, b.mol,
+                                                      b.sysid, b.sys, b.ptab, b.nbr, b.nnb, b.maxnb,
+                                                      b.spec_off, b.spec_j, b.spec_path, out, cap, count);
+}
+
+}  // namespace lg

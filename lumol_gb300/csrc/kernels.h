@@ -1,0 +1,83 @@
+// kernels.h -- device buffers of one engine (a batch of systems) and the
+// launch functions of every kernel.
+#pragma once
+
+#include "device_common.cuh"
+
+namespace lg {
+
+// Raw device pointers of a batch.  Atoms of all systems are concatenated in
+// system order; per-atom arrays have n entries.
+struct Batch {
+    int n = 0;           // atoms in the batch
+    int nsys = 0;        // systems
+    int precision = 0;   // LG_PRECISION_*
+    // state
+    double4_32a* posq = nullptr;      // x, y, z (unwrapped, FP64) and charge
+    double4_32a* vel = nullptr;       // vx, vy, vz and mass
+    double4_32a* acc = nullptr;       // accelerations (VelocityVerlet::accelerations)
+    double* force = nullptr;      // 3n, Vector3D layout
+    int* kind = nullptr;          // kind index within the system's pair table
+    int* mol = nullptr;           // global molecule index
+    int* sysid = nullptr;         // system of each atom
+    SysDev* sys = nullptr;
+    PairDev* ptab = nullptr;
+    // bond paths: same-molecule partners closer than four bonds
+    int* spec_off = nullptr;      // n + 1
+    int* spec_j = nullptr;
+    int8_t* spec_path = nullptr;
+    // bonded terms gathered per atom
+    int* bt_off = nullptr;        // n + 1
+    int4* bt = nullptr;           // (type: 0 bond 1 angle, a, b, c) ; role implied by position
+    int* bt_role = nullptr;
+    double2* bt_par = nullptr;    // (k, x0)
+    // neighbour list
+    int maxnb = 0;
+    int ncells = 0;
+    int* nbr = nullptr;           // n * maxnb
+    int* nnb = nullptr;           // n
+    int* atom_cell = nullptr;
+    int* cell_count = nullptr;    // ncells
+    int* cell_start = nullptr;    // ncells + 1
+    int* cell_atoms = nullptr;    // n
+    float4* wpos = nullptr;       // wrapped FP32 positions at build, charge
+    double4_32a* pos_build = nullptr; // positions at the last build
+    uint32_t* status = nullptr;   // ST_* bits
+    // Ewald k-space
+    int nkvec = 0;
+    int kdim = 0;                 // max kmax + 1 (eikr stores k = 0..kmax per axis)
+    int kchunk = 32;              // k-vectors per chunk of the field kernel
+    int nkchunks = 0;
+    KVecDev* kvec = nullptr;
+    double2* eikr = nullptr;      // [(kk * 3 + axis) * n + i]
+    double2* rho = nullptr;       // nkvec
+    double* fpart = nullptr;      // [chunk][3 n] partial k-space fields
+    double* kred = nullptr;       // [k][7]: energy, virial xx xy xz yy yz zz
+    // reductions
+    double* red = nullptr;        // [n][RED_STRIDE] per-atom partial energies / virials
+    double* host_const = nullptr; // [nsys][RED_STRIDE]: tail energy/virial, Ewald self energy
+    double* lambda = nullptr;     // nsys Berendsen factors
+    double* ke = nullptr;         // n kinetic energies
+};
+
+// nlist.cu
+void launch_nlist_build(const Batch& b, cudaStream_t st);
+// forces.cu
+void launch_pair_forces(const Batch& b, uint32_t terms, bool ev, cudaStream_t st);
+void launch_bonded(const Batch& b, uint32_t terms, bool ev, cudaStream_t st);
+void launch_kspace(const Batch& b, bool forces, bool ev, cudaStream_t st);
+void launch_reduce(const Batch& b, uint32_t terms, bool kspace, double* out, cudaStream_t st);
+void launch_pairset(const Batch& b, int family, int s_begin, int s_end, int* out, long long cap,
+                    unsigned long long* count, cudaStream_t st);
+// md.cu
+void launch_pack_positions(const Batch& b, const double* pos3, cudaStream_t st);
+void launch_unpack_positions(const Batch& b, double* pos3, cudaStream_t st);
+void launch_pack_velocities(const Batch& b, const double* vel3, cudaStream_t st);
+void launch_unpack_velocities(const Batch& b, double* vel3, cudaStream_t st);
+void launch_vv_first(const Batch& b, cudaStream_t st);
+void launch_vv_second(const Batch& b, bool thermostat, cudaStream_t st);
+void launch_thermostat(const Batch& b, cudaStream_t st);
+void launch_request_rebuild(const Batch& b, cudaStream_t st);
+void launch_check_displacement(const Batch& b, cudaStream_t st);
+
+}  // namespace lg

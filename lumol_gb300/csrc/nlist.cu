@@ -1,0 +1,202 @@
+// nlist.cu -- device cell list and Verlet list.
+//
+// The reference has no neighbour list: every loop is O(N^2) over i < j
+// (lumol-core/src/sys/compute.rs:37-55) with the cutoff test inside the pair
+// functions (energy/pairs.rs:185-243, ewald.rs:387-428, wolf.rs:90-117).  The
+// list built here is a SUPERSET of those pairs: it holds every j whose minimum
+// image lies within rlist = max cutoff + skin (tested in FP32 on wrapped
+// copies, with a margin larger than the FP32 error), and the force kernels then
+// apply the reference's exact FP64 cutoff test on the unwrapped positions.  The
+// list stays valid while no atom moved more than skin / 2 since the build.
+//
+// All kernels are launched every step (so one step can be captured in a CUDA
+// graph) and return at once unless the status word asks for a rebuild.
+#include "kernels.h"
+
+namespace lg {
+
+// Atom pass: cell index of each atom from its wrapped position
+// (UnitCell::wrap_vector, cells.rs:263-282), FP32 wrapped copy, reference
+// position for the displacement test.
+__global__ void nl_bin_kernel(int n, const double4_32a* __restrict__ posq, const int* __restrict__ sysid,
+                              const SysDev* __restrict__ sys, const uint32_t* __restrict__ status,
+                              int* __restrict__ atom_cell, int* __restrict__ cell_count,
+                              float4* __restrict__ wpos, double4_32a* __restrict__ pos_build) {
+    if (!(*status & ST_REBUILD)) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const SysDev& s = sys[sysid[i]];
+    double4_32a p = posq[i];
+    double w[3] = {p.x, p.y, p.z};
+    int c[3];
+    for (int d = 0; d < 3; d++) {
+        w[d] -= floor(w[d] / s.L[d]) * s.L[d];
+        int cd = (int)(w[d] * s.invL[d] * (double)s.ncell[d]);
+        c[d] = min(max(cd, 0), s.ncell[d] - 1);
+    }
+    int cell = s.cell_begin + (c[2] * s.ncell[1] + c[1]) * s.ncell[0] + c[0];
+    atom_cell[i] = cell;
+    atomicAdd(&cell_count[cell], 1);
+    wpos[i] = make_float4((float)w[0], (float)w[1], (float)w[2], (float)p.w);
+    pos_build[i] = p;
+}
+
+// Exclusive scan of the cell counts (single block).  Also zeroes the fill
+// counters used by the scatter pass.
+__global__ void nl_scan_kernel(int ncells, const uint32_t* __restrict__ status,
+                               int* __restrict__ cell_count, int* __restrict__ cell_start) {
+    if (!(*status & ST_REBUILD)) return;
+    __shared__ int partial[1024];
+    int t = threadIdx.x;
+    int per = (ncells + blockDim.x - 1) / blockDim.x;
+    int lo = min(t * per, ncells), hi = min(lo + per, ncells);
+    int sum = 0;
+    for (int c = lo; c < hi; c++) sum += cell_count[c];
+    partial[t] = sum;
+    __syncthreads();
+    // Hillis-Steele inclusive scan over the per-thread sums
+    for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+        int v = t >= o ? partial[t - o] : 0;
+        __syncthreads();
+        partial[t] += v;
+        __syncthreads();
+    }
+    int run = partial[t] - sum;
+    for (int c = lo; c < hi; c++) {
+        cell_start[c] = run;
+        run += cell_count[c];
+        cell_count[c] = 0;
+    }
+    if (t == blockDim.x - 1) cell_start[ncells] = partial[t];
+}
+
+__global__ void nl_scatter_kernel(int n, const uint32_t* __restrict__ status,
+                                  const int* __restrict__ atom_cell, int* __restrict__ cell_count,
+                                  const int* __restrict__ cell_start, int* __restrict__ cell_atoms) {
+    if (!(*status & ST_REBUILD)) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int c = atom_cell[i];
+    int slot = atomicAdd(&cell_count[c], 1);
+    cell_atoms[cell_start[c] + slot] = i;
+}
+
+// Sort each cell's atoms by index so that the list order (and so the order of
+// the force sums) does not depend on the atomics above.
+__global__ void nl_sort_kernel(int ncells, const uint32_t* __restrict__ status,
+                               const int* __restrict__ cell_start, int* __restrict__ cell_atoms,
+                               int* __restrict__ cell_count) {
+    if (!(*status & ST_REBUILD)) return;
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncells) return;
+    cell_count[c] = 0;  // ready for the next binning pass
+    int lo = cell_start[c], hi = cell_start[c + 1];
+    for (int a = lo + 1; a < hi; a++) {
+        int v = cell_atoms[a];
+        int b = a - 1;
+        while (b >= lo && cell_atoms[b] > v) {
+            cell_atoms[b + 1] = cell_atoms[b];
+            b--;
+        }
+        cell_atoms[b + 1] = v;
+    }
+}
+
+// Stencil cells of one dimension: c-1, c, c+1 (periodic) when there are at
+// least three cells, else every cell once, so that no cell is visited twice.
+__device__ __forceinline__ int stencil_cells(int c, int nc, int* out) {
+    if (nc >= 3) {
+        out[0] = (c + nc - 1) % nc;
+        out[1] = c;
+        out[2] = (c + 1) % nc;
+        return 3;
+    }
+    for (int k = 0; k < nc; k++) out[k] = k;
+    return nc;
+}
+
+// Warp per atom: scan the stencil, keep j != i whose FP32 minimum-image
+// distance is below rlist (plus margin).  Full list: each pair appears in the
+// lists of both atoms.
+__global__ void nl_build_kernel(int n, const uint32_t* status,
+                                const int* __restrict__ sysid, const SysDev* __restrict__ sys,
+                                const float4* __restrict__ wpos, const int* __restrict__ atom_cell,
+                                const int* __restrict__ cell_start, const int* __restrict__ cell_atoms,
+                                int maxnb, int* __restrict__ nbr, int* __restrict__ nnb,
+                                uint32_t* status_out) {
+    if (!(*status & ST_REBUILD)) return;
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (warp >= n) return;
+    int i = warp;
+    const SysDev& s = sys[sysid[i]];
+    float4 pi = wpos[i];
+    int local = atom_cell[i] - s.cell_begin;
+    int cx = local % s.ncell[0];
+    int cy = (local / s.ncell[0]) % s.ncell[1];
+    int cz = local / (s.ncell[0] * s.ncell[1]);
+    int sx[3], sy[3], sz[3];
+    int nx = stencil_cells(cx, s.ncell[0], sx);
+    int ny = stencil_cells(cy, s.ncell[1], sy);
+    int nz = stencil_cells(cz, s.ncell[2], sz);
+    float Lx = s.Lf[0], Ly = s.Lf[1], Lz = s.Lf[2];
+    float ix = s.invLf[0], iy = s.invLf[1], iz = s.invLf[2];
+    float rl2 = s.rlist2_f;
+    int count = 0;
+    int* out = nbr + (size_t)i * maxnb;
+    for (int a = 0; a < nz; a++)
+        for (int b = 0; b < ny; b++)
+            for (int c = 0; c < nx; c++) {
+                int cell = s.cell_begin + (sz[a] * s.ncell[1] + sy[b]) * s.ncell[0] + sx[c];
+                int lo = cell_start[cell], hi = cell_start[cell + 1];
+                for (int base = lo; base < hi; base += 32) {
+                    int idx = base + lane;
+                    bool keep = false;
+                    int j = -1;
+                    if (idx < hi) {
+                        j = cell_atoms[idx];
+                        float4 pj = wpos[j];
+                        float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+                        dx -= rintf(dx * ix) * Lx;
+                        dy -= rintf(dy * iy) * Ly;
+                        dz -= rintf(dz * iz) * Lz;
+                        float r2 = dx * dx + dy * dy + dz * dz;
+                        keep = (j != i) && (r2 < rl2);
+                    }
+                    unsigned mask = __ballot_sync(0xffffffffu, keep);
+                    if (keep) {
+                        int pos = count + __popc(mask & ((1u << lane) - 1u));
+                        if (pos < maxnb) out[pos] = j;
+                    }
+                    count += __popc(mask);
+                }
+            }
+    if (lane == 0) {
+        nnb[i] = min(count, maxnb);
+        if (count > maxnb) atomicOr(status_out, ST_OVERFLOW);
+    }
+}
+
+// Clears the rebuild request once the list is in place.
+__global__ void nl_done_kernel(uint32_t* status) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *status &= ~ST_REBUILD;
+}
+
+void launch_nlist_build(const Batch& b, cudaStream_t st) {
+    int n = b.n;
+    int tb = 256;
+    nl_bin_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, b.posq, b.sysid, b.sys, b.status, b.atom_cell,
+                                                  b.cell_count, b.wpos, b.pos_build);
+    nl_scan_kernel<<<1, 1024, 0, st>>>(b.ncells, b.status, b.cell_count, b.cell_start);
+    nl_scatter_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, b.status, b.atom_cell, b.cell_count,
+                                                      b.cell_start, b.cell_atoms);
+    nl_sort_kernel<<<(b.ncells + tb - 1) / tb, tb, 0, st>>>(b.ncells, b.status, b.cell_start, b.cell_atoms,
+                                                          b.cell_count);
+    long long threads = (long long)n * 32;
+    nl_build_kernel<<<(unsigned)((threads + tb - 1) / tb), tb, 0, st>>>(
+        n, b.status, b.sysid, b.sys, b.wpos, b.atom_cell, b.cell_start, b.cell_atoms, b.maxnb, b.nbr,
+        b.nnb, b.status);
+    nl_done_kernel<<<1, 32, 0, st>>>(b.status);
+}
+
+}  // namespace lg

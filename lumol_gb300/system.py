@@ -1,0 +1,555 @@
+"""Host-side mirror of Lumol's System / potential / integrator interface.
+
+The classes keep the names, arguments and error behaviour of lumol-core and
+lumol-sim, so that a simulation written against Lumol maps onto them line by
+line; every computation runs on the GPU through the C ABI of
+include/lumol_gb300.h (see `_capi.py`).  There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _capi as C
+from .units import ATOMIC_MASSES
+
+
+# ---------------------------------------------------------------------------
+# Restrictions (lumol-core/src/energy/restrictions.rs:13-33)
+# ---------------------------------------------------------------------------
+class PairRestriction:
+    NONE = 0
+    INTRA_MOLECULAR = 1
+    INTER_MOLECULAR = 2
+    EXCLUDE12 = 3
+    EXCLUDE13 = 4
+    EXCLUDE14 = 5
+
+    @staticmethod
+    def scale14(factor: float) -> tuple:
+        return (6, float(factor))
+
+
+def _restriction(r) -> tuple[int, float]:
+    if isinstance(r, tuple):
+        return int(r[0]), float(r[1])
+    return int(r), 1.0
+
+
+# ---------------------------------------------------------------------------
+# Potentials (lumol-core/src/energy/functions.rs)
+# ---------------------------------------------------------------------------
+@dataclass(frozen=True)
+class NullPotential:
+    """NullPotential (functions.rs:29-50)."""
+
+    def _params(self):
+        return C.LG_PAIR_NULL, (0.0, 0.0, 0.0)
+
+
+@dataclass(frozen=True)
+class LennardJones:
+    """LennardJones {sigma, epsilon} (functions.rs:71-107)."""
+    sigma: float
+    epsilon: float
+
+    def _params(self):
+        return C.LG_PAIR_LJ, (self.sigma, self.epsilon, 0.0)
+
+
+@dataclass(frozen=True)
+class Buckingham:
+    """Buckingham {a, c, rho}: A exp(-r / rho) - C / r^6 (functions.rs:276-319)."""
+    a: float
+    c: float
+    rho: float
+
+    def _params(self):
+        return C.LG_PAIR_BUCKINGHAM, (self.a, self.c, self.rho)
+
+
+@dataclass(frozen=True)
+class Harmonic:
+    """Harmonic {k, x0}: k / 2 (x - x0)^2 (functions.rs:127-160)."""
+    k: float
+    x0: float
+
+    def _params(self):
+        return C.LG_PAIR_HARMONIC, (self.k, self.x0, 0.0)
+
+
+class PairInteraction:
+    """PairInteraction (lumol-core/src/energy/pairs.rs:22-296)."""
+
+    def __init__(self, potential, cutoff: float):
+        self.potential = potential
+        self.cutoff = float(cutoff)
+        self.shifted_energy = False
+        self.tail = False
+        self.restriction = PairRestriction.NONE
+
+    @classmethod
+    def shifted(cls, potential, cutoff: float) -> "PairInteraction":
+        p = cls(potential, cutoff)
+        p.shifted_energy = True
+        return p
+
+    def enable_tail_corrections(self) -> None:
+        self.tail = True
+
+    def set_restriction(self, restriction) -> None:
+        self.restriction = restriction
+
+    def _lower(self) -> C.LgPair:
+        kind, (p0, p1, p2) = self.potential._params()
+        r, s14 = _restriction(self.restriction)
+        return C.LgPair(kind, int(self.shifted_energy), r, int(self.tail), p0, p1, p2, self.cutoff, s14)
+
+
+class Ewald:
+    """Ewald::new(cutoff, kmax, alpha) (energy/global/ewald.rs:278-305), used
+    as SharedEwald behind System::set_coulomb_potential."""
+
+    def __init__(self, cutoff: float, kmax: int, alpha: float | None = None):
+        import math
+        a = math.pi / cutoff if alpha is None else alpha
+        if cutoff < 0.0:
+            raise ValueError("the cutoff can not be negative in Ewald")
+        if a < 0.0:
+            raise ValueError("alpha can not be negative in Ewald")
+        if kmax == 0:
+            raise ValueError("kmax can not be 0 in Ewald")
+        self.cutoff = float(cutoff)
+        self.kmax = int(kmax)
+        self.alpha = float(a)
+        self.restriction = PairRestriction.NONE
+
+    def set_restriction(self, restriction) -> None:
+        self.restriction = restriction
+
+    def _lower(self) -> C.LgCoulomb:
+        r, s14 = _restriction(self.restriction)
+        return C.LgCoulomb(C.LG_COULOMB_EWALD, r, self.kmax, 0, self.cutoff, self.alpha, s14)
+
+
+class Wolf:
+    """Wolf::new(cutoff) (energy/global/wolf.rs:68-84)."""
+
+    def __init__(self, cutoff: float):
+        if not cutoff > 0.0:
+            raise ValueError("Got a negative cutoff in Wolf summation")
+        self.cutoff = float(cutoff)
+        self.restriction = PairRestriction.NONE
+
+    def set_restriction(self, restriction) -> None:
+        self.restriction = restriction
+
+    def _lower(self) -> C.LgCoulomb:
+        r, s14 = _restriction(self.restriction)
+        return C.LgCoulomb(C.LG_COULOMB_WOLF, r, 0, 0, self.cutoff, 0.0, s14)
+
+
+@dataclass
+class UnitCell:
+    """Orthorhombic UnitCell (lumol-core/src/sys/config/cells.rs:51-66)."""
+    lengths: tuple
+
+    @classmethod
+    def cubic(cls, length: float) -> "UnitCell":
+        if not length > 0.0:
+            raise ValueError("Cell lengths must be positive")
+        return cls((float(length),) * 3)
+
+    @classmethod
+    def ortho(cls, a: float, b: float, c: float) -> "UnitCell":
+        if not (a > 0.0 and b > 0.0 and c > 0.0):
+            raise ValueError("Cell lengths must be positive")
+        return cls((float(a), float(b), float(c)))
+
+    def volume(self) -> float:
+        a, b, c = self.lengths
+        return a * b * c
+
+    def matrix(self) -> np.ndarray:
+        return np.diag(np.array(self.lengths, dtype=np.float64))
+
+
+# ---------------------------------------------------------------------------
+# Engine handle
+# ---------------------------------------------------------------------------
+class Engine:
+    """Owns one lg_engine handle (a batch of `n_systems` systems)."""
+
+    def __init__(self, n_systems: int = 1, precision: str = "fp64", skin: float = 1.0, device: int = 0):
+        lib = C.load()
+        prec = {"fp64": C.LG_PRECISION_FP64, "mixed": C.LG_PRECISION_MIXED}[precision]
+        opt = C.LgOptions(device, prec, skin)
+        handle = ctypes.c_void_p()
+        C.check(lib.lg_create(ctypes.byref(opt), n_systems, ctypes.byref(handle)))
+        self.lib = lib
+        self.handle = handle
+        self.n_systems = n_systems
+        self.precision = precision
+
+    def call(self, name: str, *args) -> None:
+        C.check(getattr(self.lib, name)(self.handle, *args), self.handle)
+
+    def close(self) -> None:
+        if self.handle:
+            self.lib.lg_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, s: int, system: "System") -> None:
+        """Lowers the description of `system` into system slot `s`."""
+        system._lower_into(self, s)
+
+
+# ---------------------------------------------------------------------------
+# System
+# ---------------------------------------------------------------------------
+def _angles_from_bonds(bonds: list[tuple[int, int]]) -> list[tuple[int, int, int]]:
+    """Angles of a bond set as Bonding::rebuild finds them (bonding.rs:78-110):
+    every pair of bonds sharing a particle, (i, j, k) with i < k."""
+    angles = set()
+    for b1 in bonds:
+        for b2 in bonds:
+            if b1 == b2:
+                continue
+            if b1[0] == b2[1]:
+                a = (b2[0], b2[1], b1[1])
+            elif b1[1] == b2[0]:
+                a = (b1[0], b1[1], b2[1])
+            elif b1[1] == b2[1]:
+                a = (b1[0], b1[1], b2[0])
+            elif b1[0] == b2[0]:
+                a = (b1[1], b1[0], b2[1])
+            else:
+                continue
+            angles.add((min(a[0], a[2]), a[1], max(a[0], a[2])))
+    return sorted(angles)
+
+
+class System:
+    """Configuration + Interactions (lumol-core/src/sys/system.rs), evaluated on
+    the GPU.  Particles of a molecule are contiguous, as in Lumol."""
+
+    def __init__(self, cell: UnitCell, precision: str = "fp64", skin: float = 1.0):
+        self.cell = cell
+        self.precision = precision
+        self.skin = skin
+        self.names: list[str] = []
+        self._kinds: dict[str, int] = {}
+        self._pos: list = []
+        self._charges: list[float] = []
+        self._masses: list[float] = []
+        self._mols: list[int] = []
+        self._bonds: list[tuple[int, int]] = []
+        self.velocities: np.ndarray | None = None
+        self.pairs: dict[tuple[str, str], PairInteraction] = {}
+        self.bond_potentials: dict[tuple[str, str], object] = {}
+        self.angle_potentials: dict[tuple[str, str, str], object] = {}
+        self.coulomb = None
+        self.step = 0
+        self._engine: Engine | None = None
+        self._positions = None
+        self._version = 0
+        self._uploaded = -1
+
+    # ---- building ---------------------------------------------------------
+    def _kind(self, name: str) -> int:
+        if name not in self._kinds:
+            self._kinds[name] = len(self._kinds)
+        return self._kinds[name]
+
+    def add_molecule(self, names, positions, bonds=(), charges=None, masses=None) -> int:
+        """Adds one molecule; `bonds` index its particles from 0.  Returns the
+        molecule index."""
+        positions = np.asarray(positions, dtype=np.float64).reshape(-1, 3)
+        names = list(names)
+        start = len(self.names)
+        mol = (self._mols[-1] + 1) if self._mols else 0
+        for a, name in enumerate(names):
+            self._kind(name)
+            self.names.append(name)
+            self._charges.append(0.0 if charges is None else float(charges[a]))
+            self._masses.append(ATOMIC_MASSES.get(name, 0.0) if masses is None else float(masses[a]))
+            self._mols.append(mol)
+        self._pos.append(positions)
+        for i, j in bonds:
+            self._bonds.append((start + min(i, j), start + max(i, j)))
+        self._positions = None
+        self._touch()
+        return mol
+
+    def add_particle(self, name: str, position, charge: float = 0.0, mass: float | None = None) -> None:
+        self.add_molecule([name], [position], charges=[charge], masses=None if mass is None else [mass])
+
+    def add_particles(self, names, positions, charges=None, masses=None) -> None:
+        """Adds many single-particle molecules at once."""
+        positions = np.asarray(positions, dtype=np.float64).reshape(-1, 3)
+        n = len(names)
+        mol0 = (self._mols[-1] + 1) if self._mols else 0
+        for a, name in enumerate(names):
+            self._kind(name)
+        self.names.extend(names)
+        self._charges.extend([0.0] * n if charges is None else [float(q) for q in charges])
+        self._masses.extend([ATOMIC_MASSES.get(nm, 0.0) for nm in names] if masses is None
+                            else [float(m) for m in masses])
+        self._mols.extend(range(mol0, mol0 + n))
+        self._pos.append(positions)
+        self._positions = None
+        self._touch()
+
+    def _touch(self) -> None:
+        self._version += 1
+
+    # ---- accessors ----------------------------------------------------------
+    @property
+    def size(self) -> int:
+        return len(self.names)
+
+    @property
+    def positions(self) -> np.ndarray:
+        if self._positions is None:
+            self._positions = (np.ascontiguousarray(np.concatenate(self._pos, axis=0))
+                               if self._pos else np.zeros((0, 3)))
+            self._pos = [self._positions]
+        return self._positions
+
+    @positions.setter
+    def positions(self, value) -> None:
+        value = np.ascontiguousarray(value, dtype=np.float64).reshape(-1, 3)
+        assert value.shape == (self.size, 3)
+        self._positions = value
+        self._pos = [value]
+
+    @property
+    def charges(self) -> np.ndarray:
+        return np.array(self._charges, dtype=np.float64)
+
+    def set_charge(self, i: int, q: float) -> None:
+        self._charges[i] = float(q)
+        self._touch()
+
+    @property
+    def masses(self) -> np.ndarray:
+        return np.array(self._masses, dtype=np.float64)
+
+    @property
+    def kinds(self) -> np.ndarray:
+        return np.array([self._kinds[nm] for nm in self.names], dtype=np.int32)
+
+    @property
+    def molecules(self) -> np.ndarray:
+        return np.array(self._mols, dtype=np.int32)
+
+    @property
+    def bonds(self) -> list[tuple[int, int]]:
+        return sorted(set(self._bonds))
+
+    def angles(self) -> list[tuple[int, int, int]]:
+        return _angles_from_bonds(self.bonds)
+
+    def molecule_range(self, molid: int) -> tuple[int, int]:
+        mols = self.molecules
+        idx = np.nonzero(mols == molid)[0]
+        return int(idx[0]), int(idx[-1]) + 1
+
+    def volume(self) -> float:
+        return self.cell.volume()
+
+    # ---- interactions -------------------------------------------------------
+    def set_pair_potential(self, pair: tuple[str, str], interaction: PairInteraction) -> None:
+        """System::set_pair_potential (sys/system.rs:122-131)."""
+        if any(0.5 * d < interaction.cutoff for d in self.cell.lengths):
+            raise ValueError(
+                "Can not add a potential with a cutoff bigger than half of the smallest cell length. "
+                "Try increasing the cell size or decreasing the cutoff."
+            )
+        self._kind(pair[0])
+        self._kind(pair[1])
+        self.pairs[tuple(sorted(pair))] = interaction
+        self._touch()
+
+    def set_bond_potential(self, pair: tuple[str, str], potential) -> None:
+        self.bond_potentials[tuple(sorted(pair))] = potential
+        self._touch()
+
+    def set_angle_potential(self, angle: tuple[str, str, str], potential) -> None:
+        a, b, c = angle
+        self.angle_potentials[(min(a, c), b, max(a, c))] = potential
+        self._touch()
+
+    def set_coulomb_potential(self, potential) -> None:
+        """System::set_coulomb_potential (sys/system.rs:159-170)."""
+        if any(0.5 * d < potential.cutoff for d in self.cell.lengths):
+            raise ValueError(
+                "Can not add a potential with a cutoff bigger than half of the smallest cell length. "
+                "Try increasing the cell size or decreasing the cutoff."
+            )
+        self.coulomb = potential
+        self._touch()
+
+    # ---- lowering ---------------------------------------------------------------
+    def pair_table(self) -> list:
+        names = sorted(self._kinds, key=self._kinds.get)
+        nk = len(names)
+        table = (C.LgPair * (nk * nk))()
+        for a, na in enumerate(names):
+            for b, nb in enumerate(names):
+                inter = self.pairs.get(tuple(sorted((na, nb))))
+                table[a * nk + b] = inter._lower() if inter else C.LgPair()
+        return nk, table
+
+    def _bonded(self, pot) -> C.LgBonded:
+        if pot is None:
+            return C.LgBonded(C.LG_PAIR_ABSENT, 0, 0.0, 0.0)
+        kind, (k, x0, _) = pot._params()
+        return C.LgBonded(kind, 0, k, x0)
+
+    def _lower_into(self, eng: Engine, s: int) -> None:
+        n = self.size
+        eng.call("lg_set_cell", s, C.dptr(np.ascontiguousarray(self.cell.matrix().ravel())))
+        kinds = self.kinds
+        charges = self.charges
+        masses = self.masses
+        mols = self.molecules
+        eng.call("lg_set_particles", s, n, C.iptr(kinds), C.dptr(charges), C.dptr(masses), C.iptr(mols))
+        nk, table = self.pair_table()
+        eng.call("lg_set_pairs", s, nk, table)
+        bonds = self.bonds
+        barr = np.array(bonds, dtype=np.int32).reshape(-1)
+        bpots = (C.LgBonded * max(len(bonds), 1))()
+        for b, (i, j) in enumerate(bonds):
+            bpots[b] = self._bonded(self.bond_potentials.get(tuple(sorted((self.names[i], self.names[j])))))
+        eng.call("lg_set_bonds", s, len(bonds), C.iptr(barr), bpots)
+        angles = self.angles()
+        aarr = np.array(angles, dtype=np.int32).reshape(-1)
+        apots = (C.LgBonded * max(len(angles), 1))()
+        for a, (i, j, k) in enumerate(angles):
+            ni, nj, nk_ = self.names[i], self.names[j], self.names[k]
+            apots[a] = self._bonded(self.angle_potentials.get((min(ni, nk_), nj, max(ni, nk_))))
+        eng.call("lg_set_angles", s, len(angles), C.iptr(aarr), apots)
+        coul = self.coulomb._lower() if self.coulomb is not None else C.LgCoulomb()
+        eng.call("lg_set_coulomb", s, ctypes.byref(coul))
+
+    def engine(self) -> Engine:
+        if self._engine is None:
+            self._engine = Engine(1, self.precision, self.skin)
+        if self._uploaded != self._version:
+            self._lower_into(self._engine, 0)
+            self._uploaded = self._version
+        return self._engine
+
+    # ---- computations -------------------------------------------------------------
+    def compute(self, terms: int = C.LG_TERM_ALL, want: int = 7):
+        """Forces, energy and virial of the requested terms in one GPU pass."""
+        eng = self.engine()
+        pos = np.ascontiguousarray(self.positions, dtype=np.float64)
+        forces = np.zeros((self.size, 3))
+        energy = ctypes.c_double(0.0)
+        virial = np.zeros(9)
+        eng.call("lg_compute", 0, C.dptr(pos), terms, want, C.dptr(forces), ctypes.byref(energy),
+                 C.dptr(virial))
+        return forces, energy.value, virial.reshape(3, 3)
+
+    def forces(self) -> np.ndarray:
+        """System::forces (sys/system.rs:316-318)."""
+        return self.compute(C.LG_TERM_ALL, C.LG_WANT_FORCES)[0]
+
+    def potential_energy(self) -> float:
+        """System::potential_energy (sys/system.rs:263-265)."""
+        return self.compute(C.LG_TERM_ALL, C.LG_WANT_ENERGY)[1]
+
+    def virial(self) -> np.ndarray:
+        """System::virial with the atomic definition (sys/compute.rs:198-254)."""
+        return self.compute(C.LG_TERM_ALL, C.LG_WANT_VIRIAL)[2]
+
+    def energy_term(self, terms: int) -> float:
+        return self.compute(terms, C.LG_WANT_ENERGY)[1]
+
+    def pair_set(self, family: int = 0) -> np.ndarray:
+        """(i, j) pairs, i < j, that the device counts for a family
+        (0: pair potentials, 1: real-space Coulomb), sorted."""
+        eng = self.engine()
+        pos = np.ascontiguousarray(self.positions, dtype=np.float64)
+        count = ctypes.c_int64(0)
+        cap = 1 << 16
+        while True:
+            out = np.zeros(2 * cap, dtype=np.int32)
+            eng.call("lg_pairset", 0, C.dptr(pos), family, C.iptr(out), cap, ctypes.byref(count))
+            if count.value <= cap:
+                return out[: 2 * count.value].reshape(-1, 2)
+            cap = int(count.value)
+
+    def kinetic_energy(self) -> float:
+        v = self.velocities
+        return float(sum(0.5 * m * float(np.dot(vi, vi)) for m, vi in zip(self._masses, v)))
+
+    def temperature(self) -> float:
+        from .units import K_BOLTZMANN
+        return 2.0 * self.kinetic_energy() / (3 * self.size * K_BOLTZMANN)
+
+
+# ---------------------------------------------------------------------------
+# Molecular dynamics (lumol-sim/src/md)
+# ---------------------------------------------------------------------------
+@dataclass
+class VelocityVerlet:
+    """VelocityVerlet::new(timestep) (md/integrators.rs:22-70)."""
+    timestep: float
+
+
+@dataclass
+class BerendsenThermostat:
+    """BerendsenThermostat::new(temperature, tau) (md/thermostats.rs:91-121)."""
+    temperature: float
+    tau: float
+
+    def __post_init__(self):
+        if self.temperature < 0.0:
+            raise ValueError("The temperature must be positive in thermostats.")
+        if self.tau < 1.0:
+            raise ValueError("The timestep must be larger than 1 in berendsen thermostat.")
+
+
+@dataclass
+class MolecularDynamics:
+    """MolecularDynamics propagator (md/molecular_dynamics.rs:11-83): integrate,
+    then thermostat, every step, with the state resident on the GPU."""
+    integrator: VelocityVerlet
+    thermostat: BerendsenThermostat | None = None
+    _ready: bool = field(default=False, repr=False)
+
+    def setup(self, system: System) -> None:
+        """Propagator::setup -> VelocityVerlet::setup: accelerations := 0."""
+        eng = system.engine()
+        T0, tau = (self.thermostat.temperature, self.thermostat.tau) if self.thermostat else (0.0, 0.0)
+        eng.call("lg_md_setup", 0, self.integrator.timestep, T0, tau)
+        if system.velocities is None:
+            system.velocities = np.zeros((system.size, 3))
+        pos = np.ascontiguousarray(system.positions)
+        vel = np.ascontiguousarray(system.velocities, dtype=np.float64)
+        eng.call("lg_md_set_state", 0, C.dptr(pos), C.dptr(vel))
+        self._ready = True
+
+    def run(self, system: System, nsteps: int) -> None:
+        """`nsteps` calls of Propagator::propagate, then the state is read back."""
+        if not self._ready:
+            self.setup(system)
+        eng = system.engine()
+        eng.call("lg_md_run", int(nsteps))
+        pos = np.zeros((system.size, 3))
+        vel = np.zeros((system.size, 3))
+        eng.call("lg_md_get_state", 0, C.dptr(pos), C.dptr(vel))
+        system.positions = pos
+        system.velocities = vel
+        system.step += int(nsteps)

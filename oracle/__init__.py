@@ -1,0 +1,265 @@
+"""CPU oracle of the parity tests -- TEST INFRASTRUCTURE ONLY.
+
+A ctypes wrapper around `lumol_oracle.cpp`, a C++17 restatement of
+lumol-core's CPU arithmetic (see the header of that file for the files it
+follows).  Only the tests, `__graft_entry__.smoke()` and bench.py's CPU
+baseline use it, as the checker; the engine never imports it.
+
+Parity pin: tests/test_oracle_reference.py checks this oracle against the
+reference's own unit-test literals and its NIST LJ / SPC/E data.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "lumol_oracle.cpp")
+LIB = os.path.join(HERE, "_build", "liblumol_oracle.so")
+
+TERM_PAIRS, TERM_TAIL, TERM_BONDS, TERM_ANGLES = 1, 2, 4, 8
+TERM_COUL_REAL, TERM_COUL_SELF, TERM_COUL_KSPACE, TERM_ALL = 16, 32, 64, 127
+
+
+def build(force: bool = False) -> str:
+    """Compiles the oracle with g++ (-ffp-contract=off: Rust never fuses a*b+c)."""
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    hdr = os.path.join(HERE, "lumol_oracle.h")
+    if (not force and os.path.exists(LIB)
+            and os.path.getmtime(LIB) >= max(os.path.getmtime(SRC), os.path.getmtime(hdr))):
+        return LIB
+    tmp = LIB + ".tmp"
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
+           "-fopenmp", "-o", tmp, SRC]
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    if proc.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + proc.stdout + proc.stderr)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+class OrcPair(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_int32), ("shifted", ctypes.c_int32), ("restriction", ctypes.c_int32),
+                ("tail", ctypes.c_int32), ("p0", ctypes.c_double), ("p1", ctypes.c_double),
+                ("p2", ctypes.c_double), ("cutoff", ctypes.c_double), ("scale14", ctypes.c_double)]
+
+
+class OrcBonded(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_int32), ("pad", ctypes.c_int32), ("k", ctypes.c_double), ("x0", ctypes.c_double)]
+
+
+class OrcCoulomb(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("restriction", ctypes.c_int32), ("kmax", ctypes.c_int32),
+                ("pad", ctypes.c_int32), ("cutoff", ctypes.c_double), ("alpha", ctypes.c_double),
+                ("scale14", ctypes.c_double)]
+
+
+class OrcDesc(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64), ("positions", ctypes.c_void_p), ("kinds", ctypes.c_void_p),
+                ("charges", ctypes.c_void_p), ("masses", ctypes.c_void_p), ("molecules", ctypes.c_void_p),
+                ("n_bonds", ctypes.c_int64), ("bonds", ctypes.c_void_p), ("n_kinds", ctypes.c_int32),
+                ("pairs", ctypes.POINTER(OrcPair)), ("bond_pots", ctypes.POINTER(OrcBonded)),
+                ("angle_pots", ctypes.POINTER(OrcBonded)), ("coulomb", OrcCoulomb),
+                ("cell", ctypes.c_double * 3)]
+
+
+_lib = None
+
+
+def load() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        lib = ctypes.CDLL(LIB)
+        P, D, V = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p
+        lib.orc_create.restype = P
+        lib.orc_create.argtypes = [ctypes.POINTER(OrcDesc)]
+        lib.orc_destroy.argtypes = [P]
+        lib.orc_num_threads.restype = ctypes.c_int
+        lib.orc_set_threads.argtypes = [ctypes.c_int]
+        lib.orc_set_positions.argtypes = [P, V]
+        lib.orc_get_positions.argtypes = [P, V]
+        lib.orc_n_angles.restype = ctypes.c_int64
+        lib.orc_n_angles.argtypes = [P]
+        lib.orc_angles.argtypes = [P, V]
+        lib.orc_energy.restype = ctypes.c_double
+        lib.orc_energy.argtypes = [P, ctypes.c_int]
+        lib.orc_forces.argtypes = [P, ctypes.c_int, V]
+        lib.orc_virial.argtypes = [P, ctypes.c_int, V]
+        lib.orc_pairset.restype = ctypes.c_int64
+        lib.orc_pairset.argtypes = [P, ctypes.c_int, V, ctypes.c_int64]
+        lib.orc_velocity_verlet.argtypes = [P, V, V, V, ctypes.c_double, ctypes.c_int64, ctypes.c_double,
+                                            ctypes.c_double]
+        lib.orc_temperature.restype = ctypes.c_double
+        lib.orc_temperature.argtypes = [P, V]
+        lib.orc_kinetic_energy.restype = ctypes.c_double
+        lib.orc_kinetic_energy.argtypes = [P, V]
+        lib.orc_cache_init.argtypes = [P]
+        lib.orc_cache_energy.restype = ctypes.c_double
+        lib.orc_cache_energy.argtypes = [P]
+        lib.orc_move_molecule_cost.restype = ctypes.c_double
+        lib.orc_move_molecule_cost.argtypes = [P, ctypes.c_int64, V]
+        lib.orc_cache_update.argtypes = [P]
+        lib.orc_pair_eval.argtypes = [ctypes.POINTER(OrcPair), ctypes.c_double, D, D, D, D]
+        _lib = lib
+    return _lib
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+class Oracle:
+    """Oracle restatement of one Lumol System.
+
+    `spec` is any object with the attributes of a lumol_gb300.System
+    (positions, kinds, charges, masses, molecules, bonds, names, pairs,
+    bond_potentials, angle_potentials, coulomb, cell, _kinds)."""
+
+    def __init__(self, spec):
+        lib = load()
+        self.lib = lib
+        names = sorted(spec._kinds, key=spec._kinds.get)
+        nk = len(names)
+        self.n = spec.size
+        self._keep = []
+
+        def keep(a):
+            a = np.ascontiguousarray(a)
+            self._keep.append(a)
+            return a
+
+        pos = keep(np.asarray(spec.positions, dtype=np.float64))
+        kinds = keep(np.asarray(spec.kinds, dtype=np.int32))
+        charges = keep(np.asarray(spec.charges, dtype=np.float64))
+        masses = keep(np.asarray(spec.masses, dtype=np.float64))
+        mols = keep(np.asarray(spec.molecules, dtype=np.int32))
+        bonds = keep(np.array(spec.bonds, dtype=np.int32).reshape(-1))
+        pairs = (OrcPair * (nk * nk))()
+        bpots = (OrcBonded * (nk * nk))()
+        apots = (OrcBonded * (nk * nk * nk))()
+        for a, na in enumerate(names):
+            for b, nb in enumerate(names):
+                inter = spec.pairs.get(tuple(sorted((na, nb))))
+                if inter is not None:
+                    kind, (p0, p1, p2) = inter.potential._params()
+                    r = inter.restriction
+                    rr, s14 = (r[0], r[1]) if isinstance(r, tuple) else (r, 1.0)
+                    pairs[a * nk + b] = OrcPair(kind, int(inter.shifted_energy), rr, int(inter.tail),
+                                                p0, p1, p2, inter.cutoff, s14)
+                bp = spec.bond_potentials.get(tuple(sorted((na, nb))))
+                if bp is not None:
+                    kind, (k, x0, _) = bp._params()
+                    bpots[a * nk + b] = OrcBonded(kind, 0, k, x0)
+                for c, nc in enumerate(names):
+                    ap = spec.angle_potentials.get((min(na, nc), nb, max(na, nc)))
+                    if ap is not None:
+                        kind, (k, x0, _) = ap._params()
+                        apots[(a * nk + b) * nk + c] = OrcBonded(kind, 0, k, x0)
+        coul = OrcCoulomb()
+        if spec.coulomb is not None:
+            c = spec.coulomb
+            r = c.restriction
+            rr, s14 = (r[0], r[1]) if isinstance(r, tuple) else (r, 1.0)
+            if hasattr(c, "kmax"):
+                coul = OrcCoulomb(1, rr, c.kmax, 0, c.cutoff, c.alpha, s14)
+            else:
+                coul = OrcCoulomb(2, rr, 0, 0, c.cutoff, 0.0, s14)
+        desc = OrcDesc()
+        desc.n = self.n
+        desc.positions = _ptr(pos)
+        desc.kinds = _ptr(kinds)
+        desc.charges = _ptr(charges)
+        desc.masses = _ptr(masses)
+        desc.molecules = _ptr(mols)
+        desc.n_bonds = len(bonds) // 2
+        desc.bonds = _ptr(bonds) if len(bonds) else None
+        desc.n_kinds = nk
+        desc.pairs = pairs
+        desc.bond_pots = bpots
+        desc.angle_pots = apots
+        desc.coulomb = coul
+        desc.cell = (ctypes.c_double * 3)(*spec.cell.lengths)
+        self.h = lib.orc_create(ctypes.byref(desc))
+        self.masses = masses
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.lib.orc_destroy(self.h)
+        except Exception:
+            pass
+
+    def set_positions(self, pos) -> None:
+        pos = np.ascontiguousarray(pos, dtype=np.float64)
+        self.lib.orc_set_positions(self.h, _ptr(pos))
+
+    def energy(self, terms: int = TERM_ALL) -> float:
+        return self.lib.orc_energy(self.h, terms)
+
+    def forces(self, terms: int = TERM_ALL) -> np.ndarray:
+        f = np.zeros((self.n, 3))
+        self.lib.orc_forces(self.h, terms, _ptr(f))
+        return f
+
+    def virial(self, terms: int = TERM_ALL) -> np.ndarray:
+        v = np.zeros(9)
+        self.lib.orc_virial(self.h, terms, _ptr(v))
+        return v.reshape(3, 3)
+
+    def pairset(self, family: int) -> np.ndarray:
+        count = self.lib.orc_pairset(self.h, family, None, 0)
+        out = np.zeros(2 * max(count, 1), dtype=np.int32)
+        self.lib.orc_pairset(self.h, family, _ptr(out), count)
+        return out[: 2 * count].reshape(-1, 2)
+
+    def angles(self) -> np.ndarray:
+        n = self.lib.orc_n_angles(self.h)
+        out = np.zeros(3 * max(n, 1), dtype=np.int32)
+        self.lib.orc_angles(self.h, _ptr(out))
+        return out[: 3 * n].reshape(-1, 3)
+
+    def velocity_verlet(self, pos, vel, acc, dt, nsteps, temperature=0.0, tau=0.0):
+        pos = np.ascontiguousarray(pos, dtype=np.float64).copy()
+        vel = np.ascontiguousarray(vel, dtype=np.float64).copy()
+        acc = np.ascontiguousarray(acc, dtype=np.float64).copy()
+        self.lib.orc_velocity_verlet(self.h, _ptr(pos), _ptr(vel), _ptr(acc), dt, nsteps, temperature, tau)
+        return pos, vel, acc
+
+    def temperature(self, vel) -> float:
+        vel = np.ascontiguousarray(vel, dtype=np.float64)
+        return self.lib.orc_temperature(self.h, _ptr(vel))
+
+    def cache_init(self) -> None:
+        self.lib.orc_cache_init(self.h)
+
+    def cache_energy(self) -> float:
+        return self.lib.orc_cache_energy(self.h)
+
+    def move_molecule_cost(self, molid: int, newpos) -> float:
+        newpos = np.ascontiguousarray(newpos, dtype=np.float64)
+        return self.lib.orc_move_molecule_cost(self.h, molid, _ptr(newpos))
+
+    def cache_update(self) -> None:
+        self.lib.orc_cache_update(self.h)
+
+
+def pair_eval(potential_type: int, params, cutoff: float, r: float, shifted: bool = False,
+              tail: bool = False):
+    """(energy, force, tail_energy, tail_virial) of one PairInteraction at r."""
+    p0, p1, p2 = (list(params) + [0.0, 0.0, 0.0])[:3]
+    pair = OrcPair(potential_type, int(shifted), 0, int(tail), p0, p1, p2, cutoff, 1.0)
+    out = [ctypes.c_double() for _ in range(4)]
+    load().orc_pair_eval(ctypes.byref(pair), r, *[ctypes.byref(o) for o in out])
+    return tuple(o.value for o in out)
+
+
+def set_threads(n: int) -> None:
+    load().orc_set_threads(n)
+
+
+def num_threads() -> int:
+    return load().orc_num_threads()

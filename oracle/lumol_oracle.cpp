@@ -1,0 +1,1366 @@
+// lumol_oracle.cpp -- CPU oracle for the lumol-gb300 parity tests.
+//
+// TEST INFRASTRUCTURE ONLY: a C++17 restatement of lumol-core's CPU arithmetic,
+// used as the checker for the GPU engine.  It is never linked into, loaded by or
+// called from the product.
+//
+// Every function keeps the reference's operation order, and the file is built
+// with -ffp-contract=off because Rust never contracts a*b+c into an FMA.  The
+// O(N^2) loops are parallelised over i with OpenMP and per-thread force buffers,
+// the same structure as rayon + ThreadLocalVec (lumol-core/src/utils/thread_vec.rs).
+// Summation order across threads is therefore not fixed, exactly as in the
+// reference (rayon's sum is not ordered either).
+
+#include "lumol_oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <set>
+#include <tuple>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+constexpr double PI = 3.14159265358979323846;
+constexpr double FRAC_2_SQRT_PI = 1.12837916709551257390;
+// lumol-core/src/consts.rs:9,15
+constexpr double K_BOLTZMANN = 8.31446284161522e-7;
+constexpr double FOUR_PI_EPSILON_0 = 7.197589831304046;
+
+struct V3 {
+    double v[3];
+    double& operator[](int k) { return v[k]; }
+    double operator[](int k) const { return v[k]; }
+};
+struct M3 {
+    double m[3][3];
+};
+
+inline V3 vzero() { return V3{{0.0, 0.0, 0.0}}; }
+inline V3 vsub(const V3& a, const V3& b) { return V3{{a[0] - b[0], a[1] - b[1], a[2] - b[2]}}; }
+inline V3 vadd(const V3& a, const V3& b) { return V3{{a[0] + b[0], a[1] + b[1], a[2] + b[2]}}; }
+inline V3 vscale(double s, const V3& a) { return V3{{s * a[0], s * a[1], s * a[2]}}; }
+inline V3 vdiv(const V3& a, double s) { return V3{{a[0] / s, a[1] / s, a[2] / s}}; }
+// types/vectors.rs: dot = x*x' + y*y' + z*z' evaluated left to right
+inline double vdot(const V3& a, const V3& b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+inline double vnorm2(const V3& a) { return vdot(a, a); }
+inline double vnorm(const V3& a) { return std::sqrt(vnorm2(a)); }
+inline V3 vnormalized(const V3& a) { return vdiv(a, vnorm(a)); }
+inline M3 mzero() {
+    M3 r;
+    std::memset(&r, 0, sizeof(r));
+    return r;
+}
+// types/vectors.rs:150-156
+inline M3 tensorial(const V3& a, const V3& b) {
+    M3 r;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) r.m[i][j] = a[i] * b[j];
+    return r;
+}
+inline void madd(M3& a, const M3& b) {
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) a.m[i][j] += b.m[i][j];
+}
+inline M3 mscale(double s, const M3& a) {
+    M3 r;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) r.m[i][j] = s * a.m[i][j];
+    return r;
+}
+
+struct Complex {
+    double re, im;
+};
+// types/complex.rs:40-63, 152-154
+inline Complex cmul(const Complex& a, const Complex& b) {
+    return Complex{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+inline Complex cconj(const Complex& a) { return Complex{a.re, -a.im}; }
+inline double cnorm2(const Complex& a) { return a.re * a.re + a.im * a.im; }
+
+// ---------------------------------------------------------------------------
+// UnitCell, orthorhombic (lumol-core/src/sys/config/cells.rs)
+// ---------------------------------------------------------------------------
+struct Cell {
+    double a, b, c;
+    M3 inv;  // Matrix3::inverse of diag(a, b, c), types/matrix.rs:212-227
+
+    void init(double la, double lb, double lc) {
+        a = la;
+        b = lb;
+        c = lc;
+        double m[3][3] = {{a, 0.0, 0.0}, {0.0, b, 0.0}, {0.0, 0.0, c}};
+        double det = m[0][0] * (m[1][1] * m[2][2] - m[2][1] * m[1][2]) -
+                     m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) +
+                     m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+        double id = 1.0 / det;
+        inv.m[0][0] = (m[1][1] * m[2][2] - m[2][1] * m[1][2]) * id;
+        inv.m[0][1] = (m[0][2] * m[2][1] - m[0][1] * m[2][2]) * id;
+        inv.m[0][2] = (m[0][1] * m[1][2] - m[0][2] * m[1][1]) * id;
+        inv.m[1][0] = (m[1][2] * m[2][0] - m[1][0] * m[2][2]) * id;
+        inv.m[1][1] = (m[0][0] * m[2][2] - m[0][2] * m[2][0]) * id;
+        inv.m[1][2] = (m[1][0] * m[0][2] - m[0][0] * m[1][2]) * id;
+        inv.m[2][0] = (m[1][0] * m[2][1] - m[2][0] * m[1][1]) * id;
+        inv.m[2][1] = (m[2][0] * m[0][1] - m[0][0] * m[2][1]) * id;
+        inv.m[2][2] = (m[0][0] * m[1][1] - m[1][0] * m[0][1]) * id;
+    }
+    // cells.rs:185-200
+    double volume() const { return a * b * c; }
+    // cells.rs:284-301, orthorhombic branch
+    void vector_image(V3& v) const {
+        v[0] -= std::round(v[0] / a) * a;
+        v[1] -= std::round(v[1] / b) * b;
+        v[2] -= std::round(v[2] / c) * c;
+    }
+    // cells.rs:263-282
+    void wrap_vector(V3& v) const {
+        v[0] -= std::floor(v[0] / a) * a;
+        v[1] -= std::floor(v[1] / b) * b;
+        v[2] -= std::floor(v[2] / c) * c;
+    }
+    // cells.rs:224-226: 2 PI * inv * index
+    V3 k_vector(double i0, double i1, double i2) const {
+        M3 s = mscale(2.0 * PI, inv);
+        return V3{{s.m[0][0] * i0 + s.m[0][1] * i1 + s.m[0][2] * i2,
+                   s.m[1][0] * i0 + s.m[1][1] * i1 + s.m[1][2] * i2,
+                   s.m[2][0] * i0 + s.m[2][1] * i1 + s.m[2][2] * i2}};
+    }
+    // cells.rs:316-320
+    double distance(const V3& u, const V3& v) const {
+        V3 d = vsub(v, u);
+        vector_image(d);
+        return vnorm(d);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Potentials (lumol-core/src/energy/functions.rs)
+// ---------------------------------------------------------------------------
+
+// f64::powi(x, 6) as lowered by LLVM (repeated squaring): x^2 * (x^2)^2
+inline double powi6(double x) {
+    double x2 = x * x;
+    double x4 = x2 * x2;
+    return x2 * x4;
+}
+
+struct PairPot {
+    orc_pair d;
+    double shift = 0.0;
+
+    // Potential::energy
+    double pot_energy(double r) const {
+        switch (d.type) {
+            case ORC_PAIR_LJ: {  // functions.rs:85-88
+                double s6 = powi6(d.p0 / r);
+                return 4.0 * d.p1 * (s6 * s6 - s6);
+            }
+            case ORC_PAIR_BUCKINGHAM: {  // functions.rs:287-292
+                double r3 = r * r * r;
+                double r6 = r3 * r3;
+                double e = std::exp(-r / d.p2);
+                return d.p0 * e - d.p1 / r6;
+            }
+            case ORC_PAIR_HARMONIC: {  // functions.rs:135-139
+                double dx = r - d.p1;
+                return 0.5 * d.p0 * dx * dx;
+            }
+            default:
+                return 0.0;
+        }
+    }
+    // Potential::force
+    double pot_force(double r) const {
+        switch (d.type) {
+            case ORC_PAIR_LJ: {  // functions.rs:90-93
+                double s6 = powi6(d.p0 / r);
+                return -24.0 * d.p1 * (s6 - 2.0 * (s6 * s6)) / r;
+            }
+            case ORC_PAIR_BUCKINGHAM: {  // functions.rs:294-299
+                double r3 = r * r * r;
+                double r7 = r3 * r3 * r;
+                double e = std::exp(-r / d.p2);
+                return d.p0 / d.p2 * e - 6.0 * d.p1 / r7;
+            }
+            case ORC_PAIR_HARMONIC:  // functions.rs:141-143
+                return d.p0 * (d.p1 - r);
+            default:
+                return 0.0;
+        }
+    }
+    double pot_tail_energy(double rc) const {
+        switch (d.type) {
+            case ORC_PAIR_LJ: {  // functions.rs:97-103
+                double s3 = d.p0 * d.p0 * d.p0;
+                double rc3 = rc * rc * rc;
+                double s9 = s3 * s3 * s3;
+                double rc9 = rc3 * rc3 * rc3;
+                return 4.0 / 3.0 * d.p1 * s3 * (1.0 / 3.0 * s9 / rc9 - s3 / rc3);
+            }
+            case ORC_PAIR_BUCKINGHAM: {  // functions.rs:303-309
+                double rc2 = rc * rc;
+                double rc3 = rc2 * rc;
+                double e = std::exp(-rc / d.p2);
+                double factor = rc2 - 2.0 * rc * d.p2 + 2.0 * d.p2 * d.p2;
+                return d.p0 * d.p2 * e * factor - d.p1 / (3.0 * rc3);
+            }
+            default:
+                return 0.0;
+        }
+    }
+    double pot_tail_virial(double rc) const {
+        switch (d.type) {
+            case ORC_PAIR_LJ: {  // functions.rs:105-111
+                double s3 = d.p0 * d.p0 * d.p0;
+                double rc3 = rc * rc * rc;
+                double s9 = s3 * s3 * s3;
+                double rc9 = rc3 * rc3 * rc3;
+                return 8.0 * d.p1 * s3 * (2.0 / 3.0 * s9 / rc9 - s3 / rc3);
+            }
+            case ORC_PAIR_BUCKINGHAM: {  // functions.rs:311-318, including the "+ 8.0"
+                double rc2 = rc * rc;
+                double rc3 = rc2 * rc;
+                double e = std::exp(-rc / d.p2);
+                double factor = rc3 + 3.0 * rc2 * d.p2 + 6.0 * rc * d.p2 * d.p2 +
+                                6.0 * d.p2 * d.p2 * d.p2;
+                return d.p0 * e * factor - 20.0 * d.p1 / rc3 + 8.0;
+            }
+            default:
+                return 0.0;
+        }
+    }
+
+    // PairInteraction (energy/pairs.rs:185-296)
+    double energy(double r) const {
+        if (r >= d.cutoff) return 0.0;
+        double e = pot_energy(r);
+        return d.shifted ? e - shift : e;
+    }
+    double force(double r) const {
+        if (r >= d.cutoff) return 0.0;
+        return pot_force(r);
+    }
+    // PairPotential::virial default (energy/mod.rs:137-142) behind the cutoff test
+    M3 virial(const V3& r) const {
+        if (vnorm(r) >= d.cutoff) return mzero();
+        double fact = pot_force(vnorm(r));
+        V3 rn = vnormalized(r);
+        V3 f = vscale(fact, rn);
+        return tensorial(f, r);
+    }
+    double tail_energy() const { return d.tail ? pot_tail_energy(d.cutoff) : 0.0; }
+    double tail_virial_scalar() const { return d.tail ? pot_tail_virial(d.cutoff) : 0.0; }
+};
+
+struct Bonded {
+    orc_bonded d;
+    bool present() const { return d.type != 0; }
+    double energy(double x) const {
+        if (d.type != ORC_PAIR_HARMONIC) return 0.0;
+        double dx = x - d.x0;
+        return 0.5 * d.k * dx * dx;
+    }
+    double force(double x) const {
+        if (d.type != ORC_PAIR_HARMONIC) return 0.0;
+        return d.k * (d.x0 - x);
+    }
+};
+
+// BondPath (energy/restrictions.rs:37-50)
+enum BondPath { PATH_NONE, PATH_SAME, PATH_ONE, PATH_TWO, PATH_THREE, PATH_FAR };
+
+struct RestrictionInfo {
+    bool excluded;
+    double scaling;
+};
+
+// PairRestriction::information (energy/restrictions.rs:85-115)
+RestrictionInfo information(int restriction, double scale14, BondPath path) {
+    bool same = path != PATH_NONE;
+    bool excluded = false;
+    switch (restriction) {
+        case ORC_RESTRICT_NONE: excluded = false; break;
+        case ORC_RESTRICT_INTER: excluded = same; break;
+        case ORC_RESTRICT_INTRA: excluded = !same; break;
+        case ORC_RESTRICT_EXCLUDE12: excluded = path == PATH_ONE; break;
+        case ORC_RESTRICT_EXCLUDE13:
+        case ORC_RESTRICT_SCALE14: excluded = path == PATH_ONE || path == PATH_TWO; break;
+        case ORC_RESTRICT_EXCLUDE14:
+            excluded = path == PATH_ONE || path == PATH_TWO || path == PATH_THREE;
+            break;
+    }
+    double scaling = 1.0;
+    if (restriction == ORC_RESTRICT_SCALE14 && path == PATH_THREE) scaling = scale14;
+    return RestrictionInfo{excluded, scaling};
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// The system
+// ---------------------------------------------------------------------------
+struct orc_system {
+    int64_t n = 0;
+    std::vector<V3> pos;
+    std::vector<int32_t> kind;
+    std::vector<double> charge, mass;
+    std::vector<int32_t> mol;
+    std::vector<std::pair<int64_t, int64_t>> mol_range;  // [start, end) per molecule
+    int32_t nk = 0;
+    std::vector<PairPot> pairs;
+    std::vector<Bonded> bond_pots, angle_pots;
+    std::vector<std::pair<int32_t, int32_t>> bonds;          // i < j
+    std::vector<std::tuple<int32_t, int32_t, int32_t>> angles;  // i < k
+    std::vector<std::tuple<int32_t, int32_t, int32_t, int32_t>> dihedrals;
+    // bond distances flags per molecule, indexed by (i - start, j - start)
+    std::vector<std::vector<uint8_t>> distances;
+    Cell cell;
+    orc_coulomb coul;
+    double ewald_alpha = 0.0;
+
+    // Ewald state (energy/global/ewald.rs:187-196)
+    struct KFactor {
+        int ikx, iky, ikz;
+        double energy;
+        V3 field;
+        M3 virial;
+    };
+    std::vector<KFactor> factors;
+    double kmax2 = 0.0;
+    int kmax = 0;
+    std::vector<Complex> eikr;  // [(k + kmax)][axis][atom]
+    std::vector<Complex> rho;
+    bool factors_ready = false;
+
+    // Wolf constants (wolf.rs:68-84)
+    double wolf_alpha = 0.0, wolf_ec = 0.0, wolf_fc = 0.0;
+
+    // EnergyCache (sys/cache.rs:22-42)
+    std::vector<double> pairs_cache;
+    double c_pairs = 0, c_tail = 0, c_bonds = 0, c_angles = 0, c_coulomb = 0;
+    bool has_pending = false;
+    int64_t pending_mol = -1;
+    std::vector<double> pending_new_pairs;  // rows of the moved molecule: [local i][j]
+    double pending_pairs_delta = 0, pending_coulomb_delta = 0;
+    std::vector<Complex> pending_delta_rho;
+
+    const PairPot* pair(int64_t i, int64_t j) const {
+        const PairPot& p = pairs[(size_t)kind[i] * nk + kind[j]];
+        return p.d.type == ORC_PAIR_ABSENT ? nullptr : &p;
+    }
+
+    // Configuration::nearest_image (configuration.rs:399-403)
+    V3 nearest_image(int64_t i, int64_t j) const {
+        V3 d = vsub(pos[i], pos[j]);
+        cell.vector_image(d);
+        return d;
+    }
+    double distance(int64_t i, int64_t j) const { return cell.distance(pos[i], pos[j]); }
+
+    // Configuration::bond_path (configuration.rs:124-145)
+    BondPath bond_path(int64_t i, int64_t j) const {
+        if (mol[i] != mol[j]) return PATH_NONE;
+        if (i == j) return PATH_SAME;
+        int64_t m = mol[i];
+        int64_t start = mol_range[m].first, size = mol_range[m].second - start;
+        uint8_t flags = distances[m][(size_t)(i - start) * size + (j - start)];
+        if (flags & 1) return PATH_ONE;
+        if (flags & 2) return PATH_TWO;
+        if (flags & 4) return PATH_THREE;
+        return PATH_FAR;
+    }
+
+    ~orc_system() = default;
+};
+
+namespace {
+
+// Bonding::rebuild (sys/config/bonding.rs:78-157) restated per molecule
+void rebuild_bonding(orc_system* s) {
+    std::set<std::pair<int32_t, int32_t>> bonds(s->bonds.begin(), s->bonds.end());
+    std::set<std::tuple<int32_t, int32_t, int32_t>> angles;
+    std::set<std::tuple<int32_t, int32_t, int32_t, int32_t>> dihedrals;
+    auto make_angle = [](int32_t a, int32_t b, int32_t c) {
+        return std::make_tuple(std::min(a, c), b, std::max(a, c));
+    };
+    auto make_dihedral = [](int32_t a, int32_t b, int32_t c, int32_t d) {
+        if (std::max(a, b) < std::max(c, d)) return std::make_tuple(a, b, c, d);
+        return std::make_tuple(d, c, b, a);
+    };
+    for (auto& b1 : bonds) {
+        for (auto& b2 : bonds) {
+            if (b1 == b2) continue;
+            std::tuple<int32_t, int32_t, int32_t> angle;
+            if (b1.first == b2.second) angle = make_angle(b2.first, b2.second, b1.second);
+            else if (b1.second == b2.first) angle = make_angle(b1.first, b1.second, b2.second);
+            else if (b1.second == b2.second) angle = make_angle(b1.first, b1.second, b2.first);
+            else if (b1.first == b2.first) angle = make_angle(b1.second, b1.first, b2.second);
+            else continue;
+            angles.insert(angle);
+            int32_t ai = std::get<0>(angle), aj = std::get<1>(angle), ak = std::get<2>(angle);
+            for (auto& b3 : bonds) {
+                if (b2 == b3) continue;
+                if (ak == b3.first && aj != b3.second)
+                    dihedrals.insert(make_dihedral(ai, aj, ak, b3.second));
+                else if (ak == b3.second && aj != b3.first)
+                    dihedrals.insert(make_dihedral(ai, aj, ak, b3.first));
+                else if (ai == b3.second && aj != b3.first)
+                    dihedrals.insert(make_dihedral(b3.first, ai, aj, ak));
+                else if (ai == b3.first && aj != b3.second)
+                    dihedrals.insert(make_dihedral(b3.second, ai, aj, ak));
+            }
+        }
+    }
+    s->angles.assign(angles.begin(), angles.end());
+    s->dihedrals.assign(dihedrals.begin(), dihedrals.end());
+
+    // rebuild_connections (bonding.rs:159-186)
+    s->distances.assign(s->mol_range.size(), {});
+    for (size_t m = 0; m < s->mol_range.size(); m++) {
+        int64_t size = s->mol_range[m].second - s->mol_range[m].first;
+        s->distances[m].assign((size_t)(size * size), 0);
+    }
+    auto add = [&](int32_t i, int32_t j, uint8_t term) {
+        int64_t m = s->mol[i];
+        int64_t start = s->mol_range[m].first, size = s->mol_range[m].second - start;
+        s->distances[m][(size_t)(i - start) * size + (j - start)] |= term;
+    };
+    for (auto& b : s->bonds) {
+        add(b.first, b.second, 1);
+        add(b.second, b.first, 1);
+    }
+    for (auto& a : s->angles) {
+        add(std::get<0>(a), std::get<2>(a), 2);
+        add(std::get<2>(a), std::get<0>(a), 2);
+    }
+    for (auto& d : s->dihedrals) {
+        add(std::get<0>(d), std::get<3>(d), 4);
+        add(std::get<3>(d), std::get<0>(d), 4);
+    }
+}
+
+int nthreads() {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+int thread_id() {
+#ifdef _OPENMP
+    return omp_get_thread_num();
+#else
+    return 0;
+#endif
+}
+
+// ---------------------------------------------------------------------------
+// Pair potentials: sys/compute.rs:30-59, sys/energy.rs:32-79, compute.rs:198-231
+// ---------------------------------------------------------------------------
+double pair_energy_ij(const orc_system* s, BondPath path, double r, int64_t i, int64_t j) {
+    const PairPot* p = s->pair(i, j);
+    if (!p) return 0.0;
+    RestrictionInfo info = information(p->d.restriction, p->d.scale14, path);
+    if (info.excluded) return 0.0;
+    return info.scaling * p->energy(r);
+}
+
+double pairs_energy(const orc_system* s) {
+    double total = 0.0;
+    int64_t n = s->n;
+#pragma omp parallel for schedule(dynamic, 16) reduction(+ : total)
+    for (int64_t i = 0; i < n; i++) {
+        double local = 0.0;
+        for (int64_t j = i + 1; j < n; j++) {
+            double r = vnorm(s->nearest_image(i, j));
+            BondPath path = s->bond_path(i, j);
+            local += pair_energy_ij(s, path, r, i, j);
+        }
+        total += local;
+    }
+    return total;
+}
+
+double pairs_tail(const orc_system* s) {
+    double energy = 0.0;
+    double volume = s->cell.volume();
+    std::vector<int64_t> counts(s->nk, 0);
+    for (int64_t i = 0; i < s->n; i++) counts[s->kind[i]]++;
+    for (int a = 0; a < s->nk; a++) {
+        if (!counts[a]) continue;
+        for (int b = 0; b < s->nk; b++) {
+            if (!counts[b]) continue;
+            double two_pi_density = 2.0 * PI * (double)counts[a] * (double)counts[b] / volume;
+            const PairPot& p = s->pairs[(size_t)a * s->nk + b];
+            if (p.d.type != ORC_PAIR_ABSENT) energy += two_pi_density * p.tail_energy();
+        }
+    }
+    return energy;
+}
+
+M3 pairs_tail_virial(const orc_system* s) {
+    M3 virial = mzero();
+    double volume = s->cell.volume();
+    std::vector<int64_t> counts(s->nk, 0);
+    for (int64_t i = 0; i < s->n; i++) counts[s->kind[i]]++;
+    for (int a = 0; a < s->nk; a++) {
+        if (!counts[a]) continue;
+        for (int b = 0; b < s->nk; b++) {
+            if (!counts[b]) continue;
+            double two_pi_density = 2.0 * PI * (double)counts[a] * (double)counts[b] / volume;
+            const PairPot& p = s->pairs[(size_t)a * s->nk + b];
+            if (p.d.type == ORC_PAIR_ABSENT) continue;
+            // PairInteraction::tail_virial: tail_virial(rc) * (Matrix3::one() / 3.0)
+            M3 t = mzero();
+            if (p.d.tail) {
+                double w = p.tail_virial_scalar();
+                for (int k = 0; k < 3; k++)
+                    for (int l = 0; l < 3; l++) t.m[k][l] = w * ((k == l ? 1.0 : 0.0) / 3.0);
+            }
+            madd(virial, mscale(two_pi_density, t));
+        }
+    }
+    return virial;
+}
+
+void reduce_thread_forces(const std::vector<std::vector<V3>>& tl, int64_t n, double* out) {
+    for (auto& buf : tl)
+        for (int64_t i = 0; i < n; i++)
+            for (int k = 0; k < 3; k++) out[3 * i + k] += buf[i][k];
+}
+
+void pairs_forces(const orc_system* s, double* out) {
+    int64_t n = s->n;
+    std::vector<std::vector<V3>> tl(nthreads(), std::vector<V3>(n, vzero()));
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t i = 0; i < n; i++) {
+        auto& forces = tl[thread_id()];
+        V3 force_i = vzero();
+        for (int64_t j = i + 1; j < n; j++) {
+            BondPath path = s->bond_path(i, j);
+            V3 d = s->nearest_image(i, j);
+            V3 dn = vnormalized(d);
+            double r = vnorm(d);
+            const PairPot* p = s->pair(i, j);
+            if (p) {
+                RestrictionInfo info = information(p->d.restriction, p->d.scale14, path);
+                if (!info.excluded) {
+                    V3 f = vscale(info.scaling * p->force(r), dn);
+                    force_i = vadd(force_i, f);
+                    forces[j] = vsub(forces[j], f);
+                }
+            }
+        }
+        forces[i] = vadd(forces[i], force_i);
+    }
+    reduce_thread_forces(tl, n, out);
+}
+
+M3 pairs_virial(const orc_system* s) {
+    int64_t n = s->n;
+    std::vector<M3> partial(nthreads(), mzero());
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t i = 0; i < n; i++) {
+        M3 local = mzero();
+        for (int64_t j = i + 1; j < n; j++) {
+            BondPath path = s->bond_path(i, j);
+            const PairPot* p = s->pair(i, j);
+            if (p) {
+                RestrictionInfo info = information(p->d.restriction, p->d.scale14, path);
+                if (!info.excluded) {
+                    V3 d = s->nearest_image(i, j);
+                    madd(local, mscale(info.scaling, p->virial(d)));
+                }
+            }
+        }
+        madd(partial[thread_id()], local);
+    }
+    M3 total = mzero();
+    for (auto& m : partial) madd(total, m);
+    return total;
+}
+
+// ---------------------------------------------------------------------------
+// Bonds and angles: compute.rs:62-84, 233-241; energy.rs:90-120; cells.rs:322-362
+// ---------------------------------------------------------------------------
+const Bonded* bond_pot(const orc_system* s, int32_t i, int32_t j) {
+    const Bonded& b = s->bond_pots[(size_t)s->kind[i] * s->nk + s->kind[j]];
+    return b.present() ? &b : nullptr;
+}
+const Bonded* angle_pot(const orc_system* s, int32_t i, int32_t j, int32_t k) {
+    size_t nk = s->nk;
+    const Bonded& b = s->angle_pots[((size_t)s->kind[i] * nk + s->kind[j]) * nk + s->kind[k]];
+    return b.present() ? &b : nullptr;
+}
+
+double bonds_energy(const orc_system* s) {
+    double e = 0.0;
+    for (auto& b : s->bonds) {
+        double r = vnorm(s->nearest_image(b.first, b.second));
+        const Bonded* p = bond_pot(s, b.first, b.second);
+        if (p) e += p->energy(r);
+    }
+    return e;
+}
+
+// UnitCell::angle (cells.rs:322-330)
+double cell_angle(const orc_system* s, int32_t i, int32_t j, int32_t k) {
+    V3 r12 = vsub(s->pos[i], s->pos[j]);
+    s->cell.vector_image(r12);
+    V3 r23 = vsub(s->pos[k], s->pos[j]);
+    s->cell.vector_image(r23);
+    return std::acos(vdot(r12, r23) / (vnorm(r12) * vnorm(r23)));
+}
+
+double angles_energy(const orc_system* s) {
+    double e = 0.0;
+    for (auto& a : s->angles) {
+        int32_t i = std::get<0>(a), j = std::get<1>(a), k = std::get<2>(a);
+        double theta = cell_angle(s, i, j, k);
+        const Bonded* p = angle_pot(s, i, j, k);
+        if (p) e += p->energy(theta);
+    }
+    return e;
+}
+
+void bonded_forces(const orc_system* s, int terms, double* out) {
+    if (terms & ORC_TERM_BONDS) {
+        for (auto& b : s->bonds) {
+            V3 d = s->nearest_image(b.first, b.second);
+            V3 dn = vnormalized(d);
+            double r = vnorm(d);
+            const Bonded* p = bond_pot(s, b.first, b.second);
+            if (p) {
+                V3 f = vscale(p->force(r), dn);
+                for (int k = 0; k < 3; k++) {
+                    out[3 * b.first + k] += f[k];
+                    out[3 * b.second + k] -= f[k];
+                }
+            }
+        }
+    }
+    if (terms & ORC_TERM_ANGLES) {
+        for (auto& a : s->angles) {
+            int32_t i = std::get<0>(a), j = std::get<1>(a), k = std::get<2>(a);
+            // UnitCell::angle_and_derivatives (cells.rs:335-362)
+            V3 r12 = vsub(s->pos[i], s->pos[j]);
+            s->cell.vector_image(r12);
+            V3 r23 = vsub(s->pos[k], s->pos[j]);
+            s->cell.vector_image(r23);
+            double r12_norm = vnorm(r12), r23_norm = vnorm(r23);
+            V3 r12n = vdiv(r12, r12_norm), r23n = vdiv(r23, r23_norm);
+            double cos = vdot(r12n, r23n);
+            double sin_inv = 1.0 / std::sqrt(1.0 - cos * cos);
+            V3 d1 = vdiv(vscale(sin_inv, vsub(vscale(cos, r12n), r23n)), r12_norm);
+            V3 d3 = vdiv(vscale(sin_inv, vsub(vscale(cos, r23n), r12n)), r23_norm);
+            V3 sum = vadd(d1, d3);
+            V3 d2 = V3{{-sum[0], -sum[1], -sum[2]}};
+            double theta = std::acos(cos);
+            const Bonded* p = angle_pot(s, i, j, k);
+            if (p) {
+                double f = p->force(theta);
+                for (int c = 0; c < 3; c++) {
+                    out[3 * i + c] += f * d1[c];
+                    out[3 * j + c] += f * d2[c];
+                    out[3 * k + c] += f * d3[c];
+                }
+            }
+        }
+    }
+}
+
+M3 bonds_virial(const orc_system* s) {
+    M3 virial = mzero();
+    for (auto& b : s->bonds) {
+        V3 r = s->nearest_image(b.first, b.second);
+        const Bonded* p = bond_pot(s, b.first, b.second);
+        if (p) {
+            // BondPotential::virial (energy/mod.rs:188-193)
+            double fact = p->force(vnorm(r));
+            V3 f = vscale(fact, vnormalized(r));
+            madd(virial, tensorial(f, r));
+        }
+    }
+    return virial;
+}
+
+// ---------------------------------------------------------------------------
+// Ewald (energy/global/ewald.rs)
+// ---------------------------------------------------------------------------
+RestrictionInfo coul_info(const orc_system* s, int64_t i, int64_t j) {
+    return information(s->coul.restriction, s->coul.scale14, s->bond_path(i, j));
+}
+
+// Ewald::prepare + compute_ewald_factors_triclinic (ewald.rs:130-183, 353-379)
+void ewald_prepare(orc_system* s) {
+    if (s->factors_ready) return;
+    s->factors_ready = true;
+    V3 k111 = s->cell.k_vector(1.0, 1.0, 1.0);
+    double max = std::max(std::max(k111[0], k111[1]), k111[2]) * (double)s->kmax;
+    s->kmax2 = 1.0001 * max * max;
+
+    double alpha = s->ewald_alpha;
+    double alpha_sq_inv_fourth = 0.25 / (alpha * alpha);
+    double four_pi_v = 4.0 * PI / s->cell.volume();
+    s->factors.clear();
+    auto push = [&](V3 k, double k2, int ikx, int iky, int ikz) {
+        orc_system::KFactor f;
+        f.ikx = ikx;
+        f.iky = iky;
+        f.ikz = ikz;
+        f.energy = four_pi_v * std::exp(-k2 * alpha_sq_inv_fourth) / k2;
+        f.field = vscale(2.0 * f.energy, k);
+        double virial_factor = -2.0 * (1.0 / k2 + alpha_sq_inv_fourth);
+        M3 kk = tensorial(k, k);
+        M3 v;
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++)
+                v.m[a][b] = (a == b ? 1.0 : 0.0) + virial_factor * kk.m[a][b];
+        f.virial = mscale(f.energy, v);
+        s->factors.push_back(f);
+    };
+    int kmax = s->kmax;
+    for (int ikx = 1; ikx < kmax; ikx++)
+        for (int iky = -kmax; iky < kmax; iky++)
+            for (int ikz = -kmax; ikz < kmax; ikz++) {
+                V3 k = s->cell.k_vector(ikx, iky, ikz);
+                double k2 = vnorm2(k);
+                if (k2 > s->kmax2) continue;
+                push(k, k2, ikx, iky, ikz);
+            }
+    for (int iky = 1; iky < kmax; iky++)
+        for (int ikz = -kmax; ikz < kmax; ikz++) {
+            V3 k = s->cell.k_vector(0.0, iky, ikz);
+            double k2 = vnorm2(k);
+            if (k2 > s->kmax2) continue;
+            push(k, k2, 0, iky, ikz);
+        }
+    for (int ikz = 1; ikz < kmax; ikz++) {
+        V3 k = s->cell.k_vector(0.0, 0.0, ikz);
+        double k2 = vnorm2(k);
+        if (k2 > s->kmax2) continue;
+        push(k, k2, 0, 0, ikz);
+    }
+}
+
+inline Complex& eikr_at(orc_system* s, int k, int axis, int64_t i) {
+    return s->eikr[((size_t)(k + s->kmax) * 3 + axis) * s->n + i];
+}
+
+// Ewald::eik_dot_r (ewald.rs:633-674)
+void eik_dot_r(orc_system* s) {
+    int64_t n = s->n;
+    int kmax = s->kmax;
+    s->eikr.assign((size_t)(2 * kmax + 1) * 3 * n, Complex{0.0, 0.0});
+    for (int spatial = 0; spatial < 3; spatial++) {
+        double idx[3] = {0.0, 0.0, 0.0};
+        idx[spatial] = 1.0;
+        V3 k = s->cell.k_vector(idx[0], idx[1], idx[2]);
+        for (int64_t i = 0; i < n; i++) {
+            double phi = vdot(k, s->pos[i]);
+            eikr_at(s, 0, spatial, i) = Complex{1.0, 0.0};
+            eikr_at(s, 1, spatial, i) = Complex{1.0 * std::cos(phi), 1.0 * std::sin(phi)};
+            eikr_at(s, -1, spatial, i) = cconj(eikr_at(s, 1, spatial, i));
+        }
+    }
+    for (int spatial = 0; spatial < 3; spatial++)
+        for (int k = 2; k <= kmax; k++)
+            for (int64_t i = 0; i < n; i++) {
+                eikr_at(s, k, spatial, i) = cmul(eikr_at(s, k - 1, spatial, i), eikr_at(s, 1, spatial, i));
+                eikr_at(s, -k, spatial, i) = cconj(eikr_at(s, k, spatial, i));
+            }
+    s->rho.assign(s->factors.size(), Complex{0.0, 0.0});
+    size_t nk = s->factors.size();
+#pragma omp parallel for schedule(dynamic, 8)
+    for (size_t f = 0; f < nk; f++) {
+        const auto& kf = s->factors[f];
+        Complex partial{0.0, 0.0};
+        for (int64_t i = 0; i < n; i++) {
+            Complex phi = cmul(cmul(eikr_at(s, kf.ikx, 0, i), eikr_at(s, kf.iky, 1, i)),
+                               eikr_at(s, kf.ikz, 2, i));
+            partial.re += s->charge[i] * phi.re;
+            partial.im += s->charge[i] * phi.im;
+        }
+        s->rho[f] = partial;
+    }
+}
+
+// ewald.rs:383-398
+double ewald_real_energy_pair(const orc_system* s, RestrictionInfo info, double qiqj, double r) {
+    if (r > s->coul.cutoff) return 0.0;
+    double alpha = s->ewald_alpha;
+    if (info.excluded) return -qiqj / FOUR_PI_EPSILON_0 * std::erf(alpha * r) / r;
+    return qiqj / FOUR_PI_EPSILON_0 * std::erfc(alpha * r) / r;
+}
+
+// ewald.rs:402-428
+double ewald_real_force_pair(const orc_system* s, RestrictionInfo info, double qiqj, double r) {
+    if (r > s->coul.cutoff) return 0.0;
+    double alpha = s->ewald_alpha;
+    if (info.excluded)
+        return qiqj / (FOUR_PI_EPSILON_0 * r * r) *
+               (alpha * FRAC_2_SQRT_PI * std::exp(-alpha * alpha * r * r) - std::erf(alpha * r) / r);
+    return qiqj / (FOUR_PI_EPSILON_0 * r * r) *
+           (alpha * FRAC_2_SQRT_PI * std::exp(-alpha * alpha * r * r) + std::erfc(alpha * r) / r);
+}
+
+// Wolf (wolf.rs:90-117)
+double wolf_energy_pair(const orc_system* s, double qiqj, double r) {
+    if (r > s->coul.cutoff) return 0.0;
+    return qiqj * (std::erfc(s->wolf_alpha * r) / r - s->wolf_ec) / FOUR_PI_EPSILON_0;
+}
+double wolf_energy_self(const orc_system* s, double qi) {
+    return qi * qi * 0.5 * (s->wolf_ec + s->wolf_alpha * FRAC_2_SQRT_PI) / FOUR_PI_EPSILON_0;
+}
+double wolf_force_pair(const orc_system* s, double qiqj, double r) {
+    if (r > s->coul.cutoff) return 0.0;
+    double rij2 = r * r;
+    double alpha_rij = s->wolf_alpha * r;
+    double exp_alpha_rij = std::exp(-alpha_rij * alpha_rij);
+    double factor = std::erfc(alpha_rij) / rij2 + s->wolf_alpha * FRAC_2_SQRT_PI * exp_alpha_rij / r;
+    return qiqj * (factor - s->wolf_fc) / (r * FOUR_PI_EPSILON_0);
+}
+
+// Ewald real_space_energy (ewald.rs:431-457), Wolf energy (wolf.rs:177-207)
+double coulomb_real_energy(const orc_system* s) {
+    int64_t n = s->n;
+    double total = 0.0;
+    bool ewald = s->coul.kind == ORC_COULOMB_EWALD;
+#pragma omp parallel for schedule(dynamic, 16) reduction(+ : total)
+    for (int64_t i = 0; i < n; i++) {
+        double qi = s->charge[i];
+        if (qi == 0.0) continue;
+        double local = 0.0;
+        for (int64_t j = i + 1; j < n; j++) {
+            double qj = s->charge[j];
+            if (qj == 0.0) continue;
+            RestrictionInfo info = coul_info(s, i, j);
+            if (ewald) {
+                double r = s->distance(i, j);
+                local += ewald_real_energy_pair(s, info, qi * qj, r);
+            } else {
+                if (info.excluded) continue;
+                double r = s->distance(i, j);
+                local += info.scaling * wolf_energy_pair(s, qi * qj, r);
+            }
+        }
+        if (!ewald) local = local - wolf_energy_self(s, qi);
+        total += local;
+    }
+    return total;
+}
+
+// ewald.rs:461-500, wolf.rs:209-249
+void coulomb_real_forces(const orc_system* s, double* out) {
+    int64_t n = s->n;
+    bool ewald = s->coul.kind == ORC_COULOMB_EWALD;
+    std::vector<std::vector<V3>> tl(nthreads(), std::vector<V3>(n, vzero()));
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t i = 0; i < n; i++) {
+        auto& forces = tl[thread_id()];
+        double qi = s->charge[i];
+        if (qi == 0.0) continue;
+        V3 force_i = vzero();
+        for (int64_t j = i + 1; j < n; j++) {
+            double qj = s->charge[j];
+            if (qj == 0.0) continue;
+            RestrictionInfo info = coul_info(s, i, j);
+            V3 rij = s->nearest_image(i, j);
+            V3 f;
+            if (ewald) {
+                f = vscale(ewald_real_force_pair(s, info, qi * qj, vnorm(rij)), rij);
+            } else {
+                if (info.excluded) continue;
+                f = vscale(info.scaling * wolf_force_pair(s, qi * qj, vnorm(rij)), rij);
+            }
+            force_i = vadd(force_i, f);
+            forces[j] = vsub(forces[j], f);
+        }
+        forces[i] = vadd(forces[i], force_i);
+    }
+    reduce_thread_forces(tl, n, out);
+}
+
+// ewald.rs:502-530, wolf.rs:251-282
+M3 coulomb_real_virial(const orc_system* s) {
+    int64_t n = s->n;
+    bool ewald = s->coul.kind == ORC_COULOMB_EWALD;
+    std::vector<M3> partial(nthreads(), mzero());
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t i = 0; i < n; i++) {
+        double qi = s->charge[i];
+        if (qi == 0.0) continue;
+        M3 local = mzero();
+        for (int64_t j = i + 1; j < n; j++) {
+            double qj = s->charge[j];
+            if (qj == 0.0) continue;
+            RestrictionInfo info = coul_info(s, i, j);
+            V3 rij = s->nearest_image(i, j);
+            V3 f;
+            if (ewald) {
+                f = vscale(ewald_real_force_pair(s, info, qi * qj, vnorm(rij)), rij);
+            } else {
+                if (info.excluded) continue;
+                f = vscale(info.scaling * wolf_force_pair(s, qi * qj, vnorm(rij)), rij);
+            }
+            madd(local, tensorial(f, rij));
+        }
+        madd(partial[thread_id()], local);
+    }
+    M3 total = mzero();
+    for (auto& m : partial) madd(total, m);
+    return total;
+}
+
+// ewald.rs:619-626
+double ewald_self_energy(const orc_system* s) {
+    double q2 = 0.0;
+    for (int64_t i = 0; i < s->n; i++) q2 += s->charge[i] * s->charge[i];
+    return -s->ewald_alpha / std::sqrt(PI) * q2 / FOUR_PI_EPSILON_0;
+}
+
+// ewald.rs:677-688
+double ewald_kspace_energy(orc_system* s) {
+    eik_dot_r(s);
+    double e = 0.0;
+    for (size_t f = 0; f < s->factors.size(); f++) e += s->factors[f].energy * cnorm2(s->rho[f]);
+    return e / FOUR_PI_EPSILON_0;
+}
+
+// ewald.rs:690-720
+void ewald_kspace_forces(orc_system* s, double* out) {
+    eik_dot_r(s);
+    int64_t n = s->n;
+    size_t nk = s->factors.size();
+    std::vector<std::vector<V3>> tl(nthreads(), std::vector<V3>(n, vzero()));
+#pragma omp parallel for schedule(dynamic, 4)
+    for (size_t f = 0; f < nk; f++) {
+        auto& field = tl[thread_id()];
+        const auto& kf = s->factors[f];
+        Complex rc = cconj(s->rho[f]);
+        for (int64_t i = 0; i < n; i++) {
+            Complex e = cmul(cmul(eikr_at(s, kf.ikx, 0, i), eikr_at(s, kf.iky, 1, i)),
+                             eikr_at(s, kf.ikz, 2, i));
+            Complex partial = cmul(e, rc);
+            field[i] = vadd(field[i], vscale(partial.im, kf.field));
+        }
+    }
+    std::vector<double> fieldsum(3 * n, 0.0);
+    reduce_thread_forces(tl, n, fieldsum.data());
+    for (int64_t i = 0; i < n; i++) {
+        for (int k = 0; k < 3; k++) out[3 * i + k] += s->charge[i] * fieldsum[3 * i + k] / FOUR_PI_EPSILON_0;
+    }
+}
+
+// ewald.rs:723-733
+M3 ewald_kspace_virial(orc_system* s) {
+    eik_dot_r(s);
+    M3 v = mzero();
+    for (size_t f = 0; f < s->factors.size(); f++) madd(v, mscale(cnorm2(s->rho[f]), s->factors[f].virial));
+    M3 r;
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++) r.m[a][b] = v.m[a][b] / FOUR_PI_EPSILON_0;
+    return r;
+}
+
+double coulomb_energy_terms(orc_system* s, int terms) {
+    double e = 0.0;
+    if (s->coul.kind == ORC_COULOMB_NONE) return 0.0;
+    if (s->coul.kind == ORC_COULOMB_EWALD) ewald_prepare(s);
+    if (terms & ORC_TERM_COUL_REAL) e += coulomb_real_energy(s);
+    if (s->coul.kind == ORC_COULOMB_EWALD) {
+        if (terms & ORC_TERM_COUL_SELF) e += ewald_self_energy(s);
+        if (terms & ORC_TERM_COUL_KSPACE) e += ewald_kspace_energy(s);
+    }
+    return e;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C API
+// ---------------------------------------------------------------------------
+extern "C" {
+
+orc_system* orc_create(const orc_desc* d) {
+    orc_system* s = new orc_system();
+    s->n = d->n;
+    s->pos.resize(d->n);
+    for (int64_t i = 0; i < d->n; i++)
+        for (int k = 0; k < 3; k++) s->pos[i][k] = d->positions[3 * i + k];
+    s->kind.assign(d->kinds, d->kinds + d->n);
+    s->charge.assign(d->charges, d->charges + d->n);
+    s->mass.assign(d->masses, d->masses + d->n);
+    s->mol.assign(d->molecules, d->molecules + d->n);
+    int32_t nmol = 0;
+    for (int64_t i = 0; i < d->n; i++) nmol = std::max(nmol, s->mol[i] + 1);
+    s->mol_range.assign(nmol, {INT64_MAX, 0});
+    for (int64_t i = 0; i < d->n; i++) {
+        auto& r = s->mol_range[s->mol[i]];
+        r.first = std::min(r.first, i);
+        r.second = std::max(r.second, i + 1);
+    }
+    s->nk = d->n_kinds;
+    s->pairs.resize((size_t)s->nk * s->nk);
+    for (size_t p = 0; p < s->pairs.size(); p++) {
+        s->pairs[p].d = d->pairs[p];
+        // PairInteraction::shifted: shift = potential.energy(cutoff) (pairs.rs:86-95)
+        if (d->pairs[p].shifted) s->pairs[p].shift = s->pairs[p].pot_energy(d->pairs[p].cutoff);
+    }
+    s->bond_pots.resize((size_t)s->nk * s->nk);
+    for (size_t p = 0; p < s->bond_pots.size(); p++) s->bond_pots[p].d = d->bond_pots ? d->bond_pots[p] : orc_bonded{0, 0, 0, 0};
+    s->angle_pots.resize((size_t)s->nk * s->nk * s->nk);
+    for (size_t p = 0; p < s->angle_pots.size(); p++) s->angle_pots[p].d = d->angle_pots ? d->angle_pots[p] : orc_bonded{0, 0, 0, 0};
+    for (int64_t b = 0; b < d->n_bonds; b++) {
+        int32_t i = d->bonds[2 * b], j = d->bonds[2 * b + 1];
+        s->bonds.push_back({std::min(i, j), std::max(i, j)});
+    }
+    std::sort(s->bonds.begin(), s->bonds.end());
+    s->bonds.erase(std::unique(s->bonds.begin(), s->bonds.end()), s->bonds.end());
+    rebuild_bonding(s);
+    s->cell.init(d->cell[0], d->cell[1], d->cell[2]);
+    s->coul = d->coulomb;
+    s->kmax = d->coulomb.kmax;
+    if (s->coul.kind == ORC_COULOMB_EWALD) {
+        // Ewald::new: alpha defaults to PI / cutoff (ewald.rs:278-279)
+        s->ewald_alpha = d->coulomb.alpha > 0.0 ? d->coulomb.alpha : PI / d->coulomb.cutoff;
+    } else if (s->coul.kind == ORC_COULOMB_WOLF) {
+        double cutoff = d->coulomb.cutoff;
+        double alpha = PI / cutoff;
+        double ac = alpha * cutoff;
+        double ac2 = ac * ac;
+        s->wolf_alpha = alpha;
+        s->wolf_ec = std::erfc(ac) / cutoff;
+        s->wolf_fc = std::erfc(ac) / (cutoff * cutoff) + FRAC_2_SQRT_PI * alpha * std::exp(-ac2) / cutoff;
+    }
+    return s;
+}
+
+void orc_destroy(orc_system* s) { delete s; }
+
+int orc_num_threads(void) { return nthreads(); }
+void orc_set_threads(int n) {
+#ifdef _OPENMP
+    omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
+void orc_set_positions(orc_system* s, const double* p) {
+    for (int64_t i = 0; i < s->n; i++)
+        for (int k = 0; k < 3; k++) s->pos[i][k] = p[3 * i + k];
+}
+void orc_get_positions(const orc_system* s, double* p) {
+    for (int64_t i = 0; i < s->n; i++)
+        for (int k = 0; k < 3; k++) p[3 * i + k] = s->pos[i][k];
+}
+
+int64_t orc_n_angles(const orc_system* s) { return (int64_t)s->angles.size(); }
+void orc_angles(const orc_system* s, int32_t* out) {
+    for (size_t a = 0; a < s->angles.size(); a++) {
+        out[3 * a] = std::get<0>(s->angles[a]);
+        out[3 * a + 1] = std::get<1>(s->angles[a]);
+        out[3 * a + 2] = std::get<2>(s->angles[a]);
+    }
+}
+
+// PotentialEnergy::compute (compute.rs:111-128), per term
+double orc_energy(orc_system* s, int terms) {
+    double e = 0.0;
+    if (terms & ORC_TERM_PAIRS) e += pairs_energy(s);
+    if (terms & ORC_TERM_TAIL) e += pairs_tail(s);
+    if (terms & ORC_TERM_BONDS) e += bonds_energy(s);
+    if (terms & ORC_TERM_ANGLES) e += angles_energy(s);
+    e += coulomb_energy_terms(s, terms);
+    return e;
+}
+
+// Forces::compute (compute.rs:30-108), per term
+void orc_forces(orc_system* s, int terms, double* out) {
+    if (terms & ORC_TERM_PAIRS) pairs_forces(s, out);
+    bonded_forces(s, terms, out);
+    if (s->coul.kind != ORC_COULOMB_NONE) {
+        if (s->coul.kind == ORC_COULOMB_EWALD) ewald_prepare(s);
+        if (terms & ORC_TERM_COUL_REAL) coulomb_real_forces(s, out);
+        if (s->coul.kind == ORC_COULOMB_EWALD && (terms & ORC_TERM_COUL_KSPACE)) ewald_kspace_forces(s, out);
+    }
+}
+
+// AtomicVirial::compute (compute.rs:198-254), per term
+void orc_virial(orc_system* s, int terms, double* out) {
+    M3 v = mzero();
+    if (terms & ORC_TERM_PAIRS) madd(v, pairs_virial(s));
+    if (terms & ORC_TERM_TAIL) madd(v, pairs_tail_virial(s));
+    if (terms & ORC_TERM_BONDS) madd(v, bonds_virial(s));
+    if (s->coul.kind != ORC_COULOMB_NONE) {
+        if (s->coul.kind == ORC_COULOMB_EWALD) ewald_prepare(s);
+        if (terms & ORC_TERM_COUL_REAL) madd(v, coulomb_real_virial(s));
+        if (s->coul.kind == ORC_COULOMB_EWALD && (terms & ORC_TERM_COUL_KSPACE)) madd(v, ewald_kspace_virial(s));
+    }
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++) out[3 * a + b] = v.m[a][b];
+}
+
+int64_t orc_pairset(orc_system* s, int family, int32_t* out, int64_t cap) {
+    int64_t count = 0;
+    for (int64_t i = 0; i < s->n; i++) {
+        for (int64_t j = i + 1; j < s->n; j++) {
+            bool in = false;
+            if (family == 0) {
+                // the pair contributes iff the potential exists, is not excluded and r < cutoff
+                const PairPot* p = s->pair(i, j);
+                if (!p) continue;
+                RestrictionInfo info = information(p->d.restriction, p->d.scale14, s->bond_path(i, j));
+                if (info.excluded) continue;
+                double r = vnorm(s->nearest_image(i, j));
+                in = !(r >= p->d.cutoff);
+            } else {
+                if (s->coul.kind == ORC_COULOMB_NONE) continue;
+                if (s->charge[i] == 0.0 || s->charge[j] == 0.0) continue;
+                RestrictionInfo info = coul_info(s, i, j);
+                if (s->coul.kind == ORC_COULOMB_WOLF && info.excluded) continue;
+                double r = vnorm(s->nearest_image(i, j));
+                in = !(r > s->coul.cutoff);
+            }
+            if (in) {
+                if (count < cap) {
+                    out[2 * count] = (int32_t)i;
+                    out[2 * count + 1] = (int32_t)j;
+                }
+                count++;
+            }
+        }
+    }
+    return count;
+}
+
+// KineticEnergy (compute.rs:133-144)
+double orc_kinetic_energy(const orc_system* s, const double* v) {
+    double e = 0.0;
+    for (int64_t i = 0; i < s->n; i++) {
+        V3 vi{{v[3 * i], v[3 * i + 1], v[3 * i + 2]}};
+        e += 0.5 * s->mass[i] * vnorm2(vi);
+    }
+    return e;
+}
+
+// Temperature (compute.rs:164-172) with DegreesOfFreedom::Particles (system.rs:249-255)
+double orc_temperature(const orc_system* s, const double* v) {
+    double k = orc_kinetic_energy(s, v);
+    double dof = (double)(3 * s->n);
+    return 2.0 * k / (dof * K_BOLTZMANN);
+}
+
+void orc_velocity_verlet(orc_system* s, double* x, double* v, double* a, double dt, int64_t nsteps,
+                         double T0, double tau) {
+    int64_t n = s->n;
+    std::vector<double> f(3 * n);
+    for (int64_t step = 0; step < nsteps; step++) {
+        // integrators.rs:48-53
+        for (int64_t i = 0; i < 3 * n; i++) {
+            v[i] += 0.5 * dt * a[i];
+            x[i] += v[i] * dt;
+        }
+        orc_set_positions(s, x);
+        std::fill(f.begin(), f.end(), 0.0);
+        orc_forces(s, ORC_TERM_ALL, f.data());
+        // integrators.rs:55-68
+        for (int64_t i = 0; i < n; i++)
+            for (int k = 0; k < 3; k++) a[3 * i + k] = f[3 * i + k] / s->mass[i];
+        for (int64_t i = 0; i < 3 * n; i++) v[i] += 0.5 * dt * a[i];
+        // BerendsenThermostat::apply (thermostats.rs:112-121)
+        if (tau > 0.0) {
+            double T = orc_temperature(s, v);
+            double factor = std::sqrt(1.0 + (T0 / T - 1.0) / tau);
+            for (int64_t i = 0; i < 3 * n; i++) v[i] *= factor;
+        }
+    }
+}
+
+void orc_pair_eval(const orc_pair* d, double r, double* energy, double* force, double* tail_energy,
+                   double* tail_virial) {
+    PairPot p;
+    p.d = *d;
+    if (d->shifted) p.shift = p.pot_energy(d->cutoff);
+    *energy = p.energy(r);
+    *force = p.force(r);
+    *tail_energy = p.tail_energy();
+    *tail_virial = p.tail_virial_scalar();
+}
+
+// EnergyCache::init (cache.rs:75-98)
+void orc_cache_init(orc_system* s) {
+    int64_t n = s->n;
+    s->pairs_cache.assign((size_t)(n * n), 0.0);
+    s->c_pairs = 0.0;
+    for (int64_t i = 0; i < n; i++)
+        for (int64_t j = i + 1; j < n; j++) {
+            double r = vnorm(s->nearest_image(i, j));
+            double e = pair_energy_ij(s, s->bond_path(i, j), r, i, j);
+            s->pairs_cache[(size_t)(i * n + j)] = e;
+            s->pairs_cache[(size_t)(j * n + i)] = e;
+            s->c_pairs += e;
+        }
+    s->c_tail = pairs_tail(s);
+    s->c_bonds = bonds_energy(s);
+    s->c_angles = angles_energy(s);
+    s->c_coulomb = coulomb_energy_terms(s, ORC_TERM_ALL);
+    s->has_pending = false;
+}
+
+// EnergyCache::energy (cache.rs:100-114)
+double orc_cache_energy(const orc_system* s) {
+    double e = 0.0;
+    e += s->c_pairs;
+    e += s->c_tail;
+    e += s->c_bonds;
+    e += s->c_angles;
+    e += s->c_coulomb;
+    return e;
+}
+
+// EnergyCache::move_molecule_cost (cache.rs:145-220) with the Coulomb
+// GlobalCache costs of Ewald (ewald.rs:572-613, 758-839) and Wolf (wolf.rs:121-165)
+double orc_move_molecule_cost(orc_system* s, int64_t molid, const double* newp) {
+    int64_t n = s->n;
+    int64_t start = s->mol_range[molid].first, end = s->mol_range[molid].second;
+    int64_t msize = end - start;
+    std::vector<V3> newpos(msize);
+    for (int64_t a = 0; a < msize; a++)
+        for (int k = 0; k < 3; k++) newpos[a][k] = newp[3 * a + k];
+
+    s->pending_new_pairs.assign((size_t)(msize * n), 0.0);
+    double pairs_delta = 0.0;
+    for (int64_t a = 0; a < msize; a++) {
+        int64_t part_i = start + a;
+        for (int64_t part_j = 0; part_j < n; part_j++) {
+            if (part_j >= start && part_j < end) continue;
+            double r = s->cell.distance(s->pos[part_j], newpos[a]);
+            double e = pair_energy_ij(s, s->bond_path(part_i, part_j), r, part_i, part_j);
+            pairs_delta += e;
+            s->pending_new_pairs[(size_t)(a * n + part_j)] += e;
+            pairs_delta -= s->pairs_cache[(size_t)(part_i * n + part_j)];
+        }
+    }
+
+    double coulomb_delta = 0.0;
+    s->pending_delta_rho.clear();
+    if (s->coul.kind != ORC_COULOMB_NONE) {
+        double old_e = 0.0, new_e = 0.0;
+        bool ewald = s->coul.kind == ORC_COULOMB_EWALD;
+        for (int64_t a = 0; a < msize; a++) {
+            int64_t part_i = start + a;
+            double qi = s->charge[part_i];
+            if (qi == 0.0) continue;
+            for (int64_t part_j = 0; part_j < n; part_j++) {
+                if (part_j >= start && part_j < end) continue;
+                double qj = s->charge[part_j];
+                if (qj == 0.0) continue;
+                RestrictionInfo info = coul_info(s, part_i, part_j);
+                if (ewald) {
+                    double old_r = s->distance(part_i, part_j);
+                    double new_r = s->cell.distance(newpos[a], s->pos[part_j]);
+                    old_e += ewald_real_energy_pair(s, info, qi * qj, old_r);
+                    new_e += ewald_real_energy_pair(s, info, qi * qj, new_r);
+                } else {
+                    if (info.excluded) continue;
+                    double old_r = s->distance(part_i, part_j);
+                    double new_r = s->cell.distance(newpos[a], s->pos[part_j]);
+                    old_e += info.scaling * wolf_energy_pair(s, qi * qj, old_r);
+                    new_e += info.scaling * wolf_energy_pair(s, qi * qj, new_r);
+                }
+            }
+        }
+        coulomb_delta = new_e - old_e;
+        if (ewald) {
+            ewald_prepare(s);
+            // k_space_move_molecule_cost: uses the rho / eikr of the last eik_dot_r call
+            if (s->rho.size() != s->factors.size()) eik_dot_r(s);
+            double old_k = 0.0;
+            for (size_t f = 0; f < s->factors.size(); f++) old_k += s->factors[f].energy * cnorm2(s->rho[f]);
+            old_k /= FOUR_PI_EPSILON_0;
+            // delta_rho_move_rigid_molecules (ewald.rs:758-805)
+            int kmax = s->kmax;
+            std::vector<Complex> ne((size_t)(2 * kmax + 1) * 3 * msize);
+            auto at = [&](int k, int axis, int64_t a) -> Complex& {
+                return ne[((size_t)(k + kmax) * 3 + axis) * msize + a];
+            };
+            for (int spatial = 0; spatial < 3; spatial++) {
+                double idx[3] = {0.0, 0.0, 0.0};
+                idx[spatial] = 1.0;
+                V3 k = s->cell.k_vector(idx[0], idx[1], idx[2]);
+                for (int64_t a = 0; a < msize; a++) {
+                    double phi = vdot(k, newpos[a]);
+                    at(0, spatial, a) = Complex{1.0, 0.0};
+                    at(1, spatial, a) = Complex{1.0 * std::cos(phi), 1.0 * std::sin(phi)};
+                    at(-1, spatial, a) = cconj(at(1, spatial, a));
+                }
+            }
+            for (int spatial = 0; spatial < 3; spatial++)
+                for (int k = 2; k <= kmax; k++)
+                    for (int64_t a = 0; a < msize; a++) {
+                        at(k, spatial, a) = cmul(at(k - 1, spatial, a), at(1, spatial, a));
+                        at(-k, spatial, a) = cconj(at(k, spatial, a));
+                    }
+            s->pending_delta_rho.assign(s->factors.size(), Complex{0.0, 0.0});
+            for (size_t f = 0; f < s->factors.size(); f++) {
+                const auto& kf = s->factors[f];
+                Complex partial{0.0, 0.0};
+                for (int64_t a = 0; a < msize; a++) {
+                    int64_t part_i = start + a;
+                    Complex old_phi = cmul(cmul(eikr_at(s, kf.ikx, 0, part_i), eikr_at(s, kf.iky, 1, part_i)),
+                                           eikr_at(s, kf.ikz, 2, part_i));
+                    Complex new_phi = cmul(cmul(at(kf.ikx, 0, a), at(kf.iky, 1, a)), at(kf.ikz, 2, a));
+                    double q = s->charge[part_i];
+                    partial.re += q * (new_phi.re - old_phi.re);
+                    partial.im += q * (new_phi.im - old_phi.im);
+                }
+                s->pending_delta_rho[f] = partial;
+            }
+            double new_k = 0.0;
+            for (size_t f = 0; f < s->factors.size(); f++) {
+                Complex r{s->rho[f].re + s->pending_delta_rho[f].re, s->rho[f].im + s->pending_delta_rho[f].im};
+                new_k += s->factors[f].energy * cnorm2(r);
+            }
+            new_k /= FOUR_PI_EPSILON_0;
+            coulomb_delta += new_k - old_k;
+        }
+    }
+
+    s->pending_mol = molid;
+    s->pending_pairs_delta = pairs_delta;
+    s->pending_coulomb_delta = coulomb_delta;
+    s->has_pending = true;
+    return pairs_delta + coulomb_delta;
+}
+
+// EnergyCache::update (cache.rs:118-127) running the closure of cache.rs:190-218
+void orc_cache_update(orc_system* s) {
+    if (!s->has_pending) return;
+    int64_t n = s->n;
+    int64_t start = s->mol_range[s->pending_mol].first, end = s->mol_range[s->pending_mol].second;
+    s->c_pairs += s->pending_pairs_delta;
+    s->c_coulomb += s->pending_coulomb_delta;
+    for (int64_t i = start; i < end; i++)
+        for (int64_t j = 0; j < n; j++) {
+            if (j >= start && j < end) continue;
+            double e = s->pending_new_pairs[(size_t)((i - start) * n + j)];
+            s->pairs_cache[(size_t)(i * n + j)] = e;
+            s->pairs_cache[(size_t)(j * n + i)] = e;
+        }
+    // SharedEwald::update: rho += delta (ewald.rs:826-830, 947-955)
+    for (size_t f = 0; f < s->pending_delta_rho.size() && f < s->rho.size(); f++) {
+        s->rho[f].re += s->pending_delta_rho[f].re;
+        s->rho[f].im += s->pending_delta_rho[f].im;
+    }
+    s->has_pending = false;
+}
+
+}  // extern "C"

@@ -1,0 +1,152 @@
+/*
+ * lumol_oracle.h -- CPU oracle for the lumol-gb300 parity tests.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain C++17 restatement of lumol-core's
+ * CPU arithmetic for the force / energy / virial / integration path.  It is the
+ * checker the GPU engine is compared against; the product never links, loads or
+ * calls it.  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+ * leg may use it.
+ *
+ * Parity pin: the restatement is checked against the reference's own unit-test
+ * literals (energy/functions.rs, energy/pairs.rs, sys/energy.rs,
+ * energy/global/ewald.rs, energy/global/wolf.rs) and against the NIST LJ and
+ * SPC/E reference data shipped with the reference (tests/nist-lj.rs,
+ * tests/nist-spce.rs).  erf/erfc come from the C library, the reference takes
+ * them from the `special` 0.10 crate (lumol-core/src/math.rs:10-18), so values
+ * that depend on erfc are pinned only to the tolerance of those tests.
+ */
+#ifndef LUMOL_ORACLE_H
+#define LUMOL_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Pair potential kinds (lumol-core/src/energy/functions.rs). */
+enum {
+    ORC_PAIR_ABSENT = 0,     /* no PairInteraction registered for the kind pair */
+    ORC_PAIR_NULL = 1,       /* NullPotential */
+    ORC_PAIR_LJ = 2,         /* LennardJones {sigma, epsilon} */
+    ORC_PAIR_BUCKINGHAM = 3, /* Buckingham {a, c, rho} */
+    ORC_PAIR_HARMONIC = 4    /* Harmonic {k, x0} */
+};
+
+/* PairRestriction (lumol-core/src/energy/restrictions.rs:13-33). */
+enum {
+    ORC_RESTRICT_NONE = 0,
+    ORC_RESTRICT_INTRA = 1,
+    ORC_RESTRICT_INTER = 2,
+    ORC_RESTRICT_EXCLUDE12 = 3,
+    ORC_RESTRICT_EXCLUDE13 = 4,
+    ORC_RESTRICT_EXCLUDE14 = 5,
+    ORC_RESTRICT_SCALE14 = 6
+};
+
+enum { ORC_COULOMB_NONE = 0, ORC_COULOMB_EWALD = 1, ORC_COULOMB_WOLF = 2 };
+
+/* Energy / force / virial terms, combinable as a bit mask. */
+enum {
+    ORC_TERM_PAIRS = 1,
+    ORC_TERM_TAIL = 2,
+    ORC_TERM_BONDS = 4,
+    ORC_TERM_ANGLES = 8,
+    ORC_TERM_COUL_REAL = 16,  /* Ewald real space, or the whole Wolf sum */
+    ORC_TERM_COUL_SELF = 32,  /* Ewald self energy (Wolf self is part of COUL_REAL) */
+    ORC_TERM_COUL_KSPACE = 64,
+    ORC_TERM_ALL = 127
+};
+
+/* PairInteraction (lumol-core/src/energy/pairs.rs:57-95). */
+typedef struct {
+    int32_t type;        /* ORC_PAIR_* */
+    int32_t shifted;     /* PairInteraction::shifted */
+    int32_t restriction; /* ORC_RESTRICT_* */
+    int32_t tail;        /* enable_tail_corrections */
+    double p0, p1, p2;   /* LJ: sigma, epsilon; Buckingham: a, c, rho; Harmonic: k, x0 */
+    double cutoff;
+    double scale14;      /* Scale14 factor */
+} orc_pair;
+
+/* Bond / angle potential (Harmonic or absent). */
+typedef struct {
+    int32_t type;        /* 0: absent, ORC_PAIR_HARMONIC, ORC_PAIR_NULL */
+    int32_t pad;
+    double k, x0;
+} orc_bonded;
+
+typedef struct {
+    int32_t kind;        /* ORC_COULOMB_* */
+    int32_t restriction; /* ORC_RESTRICT_* */
+    int32_t kmax;        /* Ewald */
+    int32_t pad;
+    double cutoff;
+    double alpha;        /* Ewald alpha; <= 0 means PI / cutoff (ewald.rs:278-279) */
+    double scale14;
+} orc_coulomb;
+
+typedef struct {
+    int64_t n;
+    const double* positions;  /* 3n, unwrapped */
+    const int32_t* kinds;     /* n, kind index 0..n_kinds-1 */
+    const double* charges;    /* n */
+    const double* masses;     /* n */
+    const int32_t* molecules; /* n, molecule index; atoms of a molecule are contiguous */
+    int64_t n_bonds;
+    const int32_t* bonds;     /* 2 * n_bonds */
+    int32_t n_kinds;
+    const orc_pair* pairs;         /* n_kinds^2, symmetric */
+    const orc_bonded* bond_pots;   /* n_kinds^2, symmetric */
+    const orc_bonded* angle_pots;  /* n_kinds^3, symmetric in first/last */
+    orc_coulomb coulomb;
+    double cell[3];           /* orthorhombic cell lengths */
+} orc_desc;
+
+typedef struct orc_system orc_system;
+
+orc_system* orc_create(const orc_desc* desc);
+void orc_destroy(orc_system* s);
+int orc_num_threads(void);
+void orc_set_threads(int n);
+
+void orc_set_positions(orc_system* s, const double* positions);
+void orc_get_positions(const orc_system* s, double* positions);
+int64_t orc_n_angles(const orc_system* s);
+void orc_angles(const orc_system* s, int32_t* out); /* 3 * n_angles, sorted */
+
+/* Energies (internal units).  `terms` is a mask of ORC_TERM_*. */
+double orc_energy(orc_system* s, int terms);
+/* forces (3n) are ACCUMULATED into `forces`. */
+void orc_forces(orc_system* s, int terms, double* forces);
+void orc_virial(orc_system* s, int terms, double* virial9);
+
+/* Pair set of a family: 0 = pair potentials (r < cutoff and not excluded),
+ * 1 = real-space Coulomb (r <= cutoff, q_i q_j != 0).  Returns the count and
+ * writes up to `cap` (i, j) with i < j into out. */
+int64_t orc_pairset(orc_system* s, int family, int32_t* out, int64_t cap);
+
+/* Velocity-Verlet (lumol-sim/src/md/integrators.rs:22-70), with an optional
+ * Berendsen thermostat (md/thermostats.rs:112-121) when tau > 0.
+ * positions / velocities / accelerations: 3n in/out. */
+void orc_velocity_verlet(orc_system* s, double* positions, double* velocities,
+                         double* accelerations, double dt, int64_t nsteps,
+                         double thermostat_temperature, double thermostat_tau);
+double orc_temperature(const orc_system* s, const double* velocities);
+double orc_kinetic_energy(const orc_system* s, const double* velocities);
+
+/* One PairInteraction evaluated at distance r: energy, force, tail energy,
+ * tail virial (energy/pairs.rs:185-296). */
+void orc_pair_eval(const orc_pair* p, double r, double* energy, double* force,
+                   double* tail_energy, double* tail_virial);
+
+/* EnergyCache (lumol-core/src/sys/cache.rs). */
+void orc_cache_init(orc_system* s);
+double orc_cache_energy(const orc_system* s);
+double orc_move_molecule_cost(orc_system* s, int64_t molecule, const double* new_positions);
+void orc_cache_update(orc_system* s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
