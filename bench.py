@@ -1,0 +1,373 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 engine on Lumol's MD hot path.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload nacl_ewald|argon|water] [--precision fp64|mixed]
+
+A step is one Velocity-Verlet MD step (integrate: half kick, drift, forces,
+half kick) of the workload, with the state resident on the GPU.  `value` is
+atom-steps/s of the whole job (all ranks), timed with CUDA events on the
+engine's stream; the L2 cache is flushed (256 MiB write) before every timed
+step because the workloads fit in L2.  `e2e` is the same metric through the
+public C ABI call Lumol's Integrator would make (lg_md_integrate), with the
+positions and velocities copied from pinned host memory and back every step.
+
+`--impl reference` times the reference algorithm on the host cores: the CPU
+oracle (a C++ restatement of lumol-core's O(N^2) loops, OpenMP over all
+cores), on the same workload and metric.  With torchrun (N > 1) every rank
+runs an independent replica (the path has no exchange between systems);
+rank 0 prints the line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "atom-steps/s"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--warmup", type=int, default=10)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--workload", default="nacl_ewald", choices=["nacl_ewald", "argon", "water"])
+    p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def make_system(name: str, precision: str):
+    from lumol_gb300 import workloads
+    if name == "nacl_ewald":
+        return workloads.nacl_crystal(precision=precision), 1.0, (
+            "NaCl rock salt 5x5x5 (1000 ions, L=28.2 A), LJ rc=9 A, Ewald rc=9 A alpha=0.35 kmax=7, "
+            "NVE Velocity-Verlet dt=1 fs")
+    if name == "argon":
+        return workloads.argon_fcc(precision=precision), 1.0, (
+            "Argon FCC 5x5x5 (500 atoms, L=28.8 A), shifted LJ rc=10 A, NVE Velocity-Verlet dt=1 fs")
+    return workloads.water_box(precision=precision), 0.5, (
+        "SPC/E-geometry flexible water 12^3 (5184 atoms, L=37.3 A), Ewald alpha=0.3 kmax=8 rc=10 A, "
+        "harmonic bonds/angles, Velocity-Verlet dt=0.5 fs")
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, value: float) -> float:
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(world, value: float) -> float:
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.file, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        self.proc.wait()
+        self.file.flush()
+        self.file.seek(0)
+        rows = [r.split(",") for r in self.file.read().splitlines() if r.strip()]
+        os.unlink(self.file.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for name, flag in zip(names, r[5:9]):
+                if flag.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_work(system):
+    """Algorithmic flops per launch of the pair kernel, counted per unordered
+    in-cutoff pair as the reference loops do (geometry 21, LJ body + epilogue
+    36, real-space Coulomb body + epilogue 35), and per (k, atom) of the Ewald
+    field (21) and rho (16) kernels."""
+    import numpy as np
+    p0 = system.pair_set(0)
+    p1 = system.pair_set(1)
+    key = lambda a: a[:, 0].astype(np.int64) * system.size + a[:, 1]
+    union = np.union1d(key(p0), key(p1)).size if len(p0) or len(p1) else 0
+    pair_flops = 21 * union + 36 * len(p0) + 35 * len(p1)
+    nk = 0
+    if system.coulomb is not None and hasattr(system.coulomb, "kmax"):
+        nk = count_kvectors(system.cell.lengths, system.coulomb.kmax)
+    return {"pairs_lj": int(len(p0)), "pairs_coulomb": int(len(p1)), "pair_flops": int(pair_flops),
+            "kvectors": nk, "field_flops": 21 * nk * system.size, "rho_flops": 16 * nk * system.size}
+
+
+def count_kvectors(lengths, kmax):
+    """Size of the k-vector list of Ewald::prepare (ewald.rs:130-183, 353-379)."""
+    k1 = [2.0 * math.pi / L for L in lengths]
+    mx = max(k1) * kmax
+    kmax2 = 1.0001 * mx * mx
+    n = 0
+    ranges = [((1, kmax), (-kmax, kmax), (-kmax, kmax)), ((0, 1), (1, kmax), (-kmax, kmax)),
+              ((0, 1), (0, 1), (1, kmax))]
+    for rx, ry, rz in ranges:
+        for a in range(*rx):
+            for b in range(*ry):
+                for c in range(*rz):
+                    k2 = (k1[0] * a) ** 2 + (k1[1] * b) ** 2 + (k1[2] * c) ** 2
+                    if k2 <= kmax2:
+                        n += 1
+    return n
+
+
+def traffic_from_profiles(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        parts = line.split()
+        if len(parts) >= 2 and parts[0] == kernel:
+            try:
+                return float(parts[1])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_baseline(system, dt, seconds: float = 12.0):
+    """The oracle's Velocity-Verlet on the host cores, on a bounded sample of
+    steps of the same workload."""
+    import numpy as np
+    import oracle
+    orc = oracle.Oracle(system)
+    threads = oracle.num_threads()
+    x, v = system.positions.copy(), system.velocities.copy()
+    a = np.zeros_like(x)
+    x, v, a = orc.velocity_verlet(x, v, a, dt, 1)  # warm-up step
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        x, v, a = orc.velocity_verlet(x, v, a, dt, 1)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el > seconds or steps >= 2000:
+            break
+    return {"value": system.size * steps / el, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"{steps} Velocity-Verlet steps of the same {system.size}-atom system "
+                      f"(O(N^2) forces, C++ restatement of lumol-core, OpenMP {threads} threads)"}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    import numpy as np
+    import oracle
+    oracle.build()
+    system, dt, desc = make_system(args.workload, "fp64")
+    orc = oracle.Oracle(system)
+    threads = oracle.num_threads()
+    x, v = system.positions.copy(), system.velocities.copy()
+    a = np.zeros_like(x)
+    for _ in range(args.warmup):
+        x, v, a = orc.velocity_verlet(x, v, a, dt, 1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        x, v, a = orc.velocity_verlet(x, v, a, dt, 1)
+    el = time.perf_counter() - t0
+    value = system.size * args.steps / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded lattice + Maxwell-Boltzmann velocities)",
+        "config": {"workload": desc, "atoms": system.size, "precision": "fp64"},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} timed Velocity-Verlet steps after {args.warmup} warm-up steps; "
+                                   "C++ restatement of lumol-core's O(N^2) CPU path (the Rust reference has "
+                                   "no toolchain here)"},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    from lumol_gb300 import build as engine_build
+    if not os.path.exists(engine_build.LIB):
+        engine_build.build()
+    import lumol_gb300 as lg
+    from lumol_gb300 import _capi as C
+
+    torch.cuda.set_device(local)
+    system, dt, desc = make_system(args.workload, args.precision)
+    md = lg.MolecularDynamics(lg.VelocityVerlet(dt))
+    md.setup(system)
+    eng = system.engine()
+    stream_ptr = ctypes.c_void_p()
+    eng.call("lg_get_stream", ctypes.byref(stream_ptr))
+    stream = torch.cuda.ExternalStream(stream_ptr.value)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    for _ in range(max(args.warmup, 3)):
+        eng.call("lg_md_run", 1)
+    torch.cuda.synchronize()
+
+    n0 = ctypes.c_uint64()
+    eng.call("lg_launch_count", ctypes.byref(n0))
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    for k in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        starts[k].record(stream)
+        eng.call("lg_md_run", 1)
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    n1 = ctypes.c_uint64()
+    eng.call("lg_launch_count", ctypes.byref(n1))
+    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    ms_max = max_over_ranks(world, ms)
+    atoms_total = sum_over_ranks(world, float(system.size))
+    value = atoms_total * args.steps / (ms_max * 1e-3)
+
+    # end to end through the public call, pinned host buffers
+    pos = torch.empty((system.size, 3), dtype=torch.float64, pin_memory=True)
+    vel = torch.empty((system.size, 3), dtype=torch.float64, pin_memory=True)
+    eng.call("lg_md_get_state", 0, C.dptr(pos.numpy()), C.dptr(vel.numpy()))
+    for _ in range(3):
+        eng.call("lg_md_integrate", C.dptr(pos.numpy()), C.dptr(vel.numpy()), 1)
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        eng.call("lg_md_integrate", C.dptr(pos.numpy()), C.dptr(vel.numpy()), 1)
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(world, time.perf_counter() - t0)
+    e2e_value = atoms_total * args.steps / e2e_s
+    bytes_state = 2 * 3 * 8 * system.size
+
+    # roofline of the dominant kernel, timed live with CUDA events
+    kt = (ctypes.c_double * C.LG_KT_COUNT)() if hasattr(C, "LG_KT_COUNT") else (ctypes.c_double * 8)()
+    eng.call("lg_kernel_times", 20, kt)
+    times = {name: kt[i] for i, name in enumerate(C.LG_KT_NAMES)}
+    work = algorithmic_work(system)
+    fp64_peak = ctypes.c_double()
+    C.check(lg_lib_fma(C, 1, fp64_peak))
+    candidates = {"pair": work["pair_flops"], "field": work["field_flops"], "rho": work["rho_flops"]}
+    dominant = max(candidates, key=lambda k: times.get(k, 0.0))
+    achieved = candidates[dominant] / (times[dominant] * 1e-3) / 1e12
+    kernel_names = {"pair": "pair_fp64_kernel", "field": "field_kernel", "rho": "rho_kernel"}
+    roofline = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak.value, "unit": "TFLOP/s",
+                "frac": achieved / fp64_peak.value, "traffic": traffic_from_profiles(kernel_names[dominant]),
+                "kernel": kernel_names[dominant], "kernel_ms": times[dominant],
+                "peak_source": "FP64 DFMA throughput measured live by lg_fma_peak (no FP64 figure in "
+                               "MEASURED_PEAKS.json; this path does not use tensor cores)",
+                "kernel_ms_by_group": times, "work": work}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(system, dt)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+            "data": "synthetic (seeded lattice + Maxwell-Boltzmann velocities)",
+            "config": {"workload": desc, "atoms": system.size, "precision": args.precision,
+                       "parallelism": f"replicas x{world}" if world > 1 else "single system",
+                       "l2": "flushed before every timed step (256 MiB write)"},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": bytes_state,
+                    "d2h_bytes_per_step": bytes_state},
+            "gpu_launches": int(n1.value - n0.value),
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def lg_lib_fma(C, fp64, out):
+    import ctypes
+    return C.load().lg_fma_peak(fp64, ctypes.byref(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -213,6 +213,30 @@ int lg_mc_move_molecule_cost(lg_engine* e, int32_t s, int64_t molecule,
  * center-of-mass wrap (lumol-sim/src/mc/moves/translate.rs:114-125). */
 int lg_mc_update(lg_engine* e, int32_t s, const double* molecule_positions, double* energy);
 
+/* ---- diagnostics (no counterpart in the reference) ----------------------------- */
+/* Kernel groups timed by lg_kernel_times, in output order. */
+enum {
+    LG_KT_NLIST = 0,   /* cell binning + Verlet list build (forced rebuild) */
+    LG_KT_PAIR = 1,    /* pair potentials + real-space Coulomb */
+    LG_KT_BONDED = 2,  /* bonds and angles */
+    LG_KT_EIKR = 3,    /* Ewald e^{ik.r} per atom */
+    LG_KT_RHO = 4,     /* Ewald structure factors rho(k) */
+    LG_KT_FIELD = 5,   /* Ewald k-space field and forces */
+    LG_KT_VV = 6,      /* the two Velocity-Verlet half steps */
+    LG_KT_STEP = 7,    /* one whole MD step, launched without a graph */
+    LG_KT_COUNT = 8
+};
+/* The engine's CUDA stream (a cudaStream_t), to time its work with events. */
+int lg_get_stream(lg_engine* e, void** stream);
+/* Average device time (ms) of each kernel group over `reps` launches, timed
+ * with CUDA events on the engine's stream at the current device state. */
+int lg_kernel_times(lg_engine* e, int32_t reps, double ms[LG_KT_COUNT]);
+/* Number of kernels this engine has launched (graph replays included). */
+int lg_launch_count(lg_engine* e, uint64_t* count);
+/* Measured FMA throughput of the FP64 (fp64 = 1) or FP32 pipe of the current
+ * device, in TFLOP/s (2 flops per FMA). */
+int lg_fma_peak(int32_t fp64, double* tflops);
+
 #ifdef __cplusplus
 }
 #endif

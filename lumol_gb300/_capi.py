@@ -98,7 +98,13 @@ SIGNATURES = {
     "lg_mc_init": (ctypes.c_int, [_P, ctypes.c_int32, _D, _D]),
     "lg_mc_move_molecule_cost": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int64, _D, _D]),
     "lg_mc_update": (ctypes.c_int, [_P, ctypes.c_int32, _D, _D]),
+    "lg_get_stream": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
+    "lg_kernel_times": (ctypes.c_int, [_P, ctypes.c_int32, _D]),
+    "lg_launch_count": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64)]),
+    "lg_fma_peak": (ctypes.c_int, [ctypes.c_int32, _D]),
 }
+
+LG_KT_NAMES = ["nlist", "pair", "bonded", "eikr", "rho", "field", "vv", "step"]
 
 _lib = None
 

@@ -212,6 +212,10 @@ struct lg_engine {
     std::vector<SysDev> h_sysdev;
     std::vector<int> h_kvec_sys;
 
+    // kernels launched so far (graph replays counted by their kernel nodes)
+    uint64_t launches = 0;
+    size_t graph_kernels = 0;
+
     // MD graph
     cudaGraphExec_t graph = nullptr;
     int graph_steps = 0;
@@ -678,10 +682,21 @@ int clear_status_bits(lg_engine* e, uint32_t bits) {
 // Forces (and energies / virials) of the whole batch at the positions in posq.
 void enqueue_forces(lg_engine* e, uint32_t terms, bool ev, cudaStream_t st) {
     const Batch& b = e->b;
+    if (b.n == 0) return;
     launch_nlist_build(b, st);
-    if (terms & (LG_TERM_PAIRS | LG_TERM_COUL_REAL)) launch_pair_forces(b, terms, ev, st);
-    if (terms & (LG_TERM_BONDS | LG_TERM_ANGLES)) launch_bonded(b, terms, ev, st);
-    if ((terms & LG_TERM_COUL_KSPACE) && b.nkvec) launch_kspace(b, true, ev, st);
+    e->launches += 6;
+    if (terms & (LG_TERM_PAIRS | LG_TERM_COUL_REAL)) {
+        launch_pair_forces(b, terms, ev, st);
+        e->launches += 1;
+    }
+    if ((terms & (LG_TERM_BONDS | LG_TERM_ANGLES)) && b.bt_off) {
+        launch_bonded(b, terms, ev, st);
+        e->launches += 1;
+    }
+    if ((terms & LG_TERM_COUL_KSPACE) && b.nkvec) {
+        launch_kspace(b, true, ev, st);
+        e->launches += 4;
+    }
 }
 
 int compute_batch(lg_engine* e, uint32_t terms, uint32_t want, double* d_force_out, double* d_out) {
@@ -689,10 +704,14 @@ int compute_batch(lg_engine* e, uint32_t terms, uint32_t want, double* d_force_o
     cudaStream_t st = e->stream;
     for (int attempt = 0; attempt < 4; attempt++) {
         launch_check_displacement(e->b, st);
+        e->launches += e->b.n ? 1 : 0;
         CUDA_TRY(e, cudaMemsetAsync(e->force.p, 0, 3 * (size_t)e->b.n * sizeof(double), st));
         if (ev) CUDA_TRY(e, cudaMemsetAsync(e->red.p, 0, (size_t)e->b.n * RED_STRIDE * sizeof(double), st));
         enqueue_forces(e, terms, ev, st);
-        if (ev) launch_reduce(e->b, terms, (terms & LG_TERM_COUL_KSPACE) && e->b.nkvec, e->out.p, st);
+        if (ev) {
+            launch_reduce(e->b, terms, (terms & LG_TERM_COUL_KSPACE) && e->b.nkvec, e->out.p, st);
+            e->launches += 1;
+        }
         CUDA_TRY(e, cudaGetLastError());
         uint32_t status;
         int rc = read_status(e, &status);
@@ -1096,6 +1115,7 @@ void enqueue_md_step(lg_engine* e, bool thermo, cudaStream_t st) {
     enqueue_forces(e, LG_TERM_ALL, false, st);
     launch_vv_second(e->b, thermo, st);
     if (thermo) launch_thermostat(e->b, st);
+    e->launches += 2 + (thermo ? 2 : 0);
 }
 
 int build_md_graph(lg_engine* e, int steps, bool thermo) {
@@ -1104,9 +1124,14 @@ int build_md_graph(lg_engine* e, int steps, bool thermo) {
         e->graph = nullptr;
     }
     cudaGraph_t g;
+    uint64_t before = e->launches;
     CUDA_TRY(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < steps; k++) enqueue_md_step(e, thermo, e->stream);
+    e->launches = before;  // captured launches run (and are counted) at replay
     CUDA_TRY(e, cudaStreamEndCapture(e->stream, &g));
+    size_t nodes = 0;
+    cudaGraphGetNodes(g, nullptr, &nodes);
+    e->graph_kernels = nodes;
     cudaError_t ce = cudaGraphInstantiate(&e->graph, g, 0);
     cudaGraphDestroy(g);
     if (ce != cudaSuccess) return fail(e, LG_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ce));
@@ -1148,6 +1173,7 @@ int lg_md_run(lg_engine* e, int64_t nsteps) {
         CUDA_TRY(e, cudaMemcpyAsync(cp_vel.p, e->vel.p, bytes, cudaMemcpyDeviceToDevice, st));
         CUDA_TRY(e, cudaMemcpyAsync(cp_acc.p, e->acc.p, bytes, cudaMemcpyDeviceToDevice, st));
         CUDA_TRY(e, cudaGraphLaunch(e->graph, st));
+        e->launches += e->graph_kernels;
         uint32_t status;
         int rc = read_status(e, &status);
         if (rc) return rc;
@@ -1174,6 +1200,87 @@ int lg_md_integrate(lg_engine* e, double* positions, double* velocities, int64_t
     rc = lg_md_run(e, nsteps);
     if (rc) return rc;
     return lg_md_get_state(e, 0, positions, velocities);
+}
+
+// ---- diagnostics ---------------------------------------------------------------
+int lg_get_stream(lg_engine* e, void** stream) {
+    if (!e || !stream) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    *stream = (void*)e->stream;
+    return LG_OK;
+}
+
+int lg_launch_count(lg_engine* e, uint64_t* count) {
+    if (!e || !count) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    *count = e->launches;
+    return LG_OK;
+}
+
+int lg_fma_peak(int32_t fp64, double* tflops) {
+    if (!tflops) return fail(nullptr, LG_ERR_ARGUMENT, "invalid arguments");
+    int rc = measure_fma_peak(fp64 ? 1 : 0, tflops);
+    return rc ? fail(nullptr, LG_ERR_CUDA, "FMA probe failed") : LG_OK;
+}
+
+int lg_kernel_times(lg_engine* e, int32_t reps, double* ms) {
+    if (!e || !ms || reps <= 0) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    if (e->dirty) return fail(e, LG_ERR_STATE, "no device state");
+    CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    cudaStream_t st = e->stream;
+    const Batch& b = e->b;
+    cudaEvent_t e0, e1;
+    CUDA_TRY(e, cudaEventCreate(&e0));
+    CUDA_TRY(e, cudaEventCreate(&e1));
+    bool thermo = false;
+    for (int s = 0; s < e->nsys; s++) thermo = thermo || e->sys[s].tau > 0.0;
+    // save the state: timing must not advance the trajectory
+    DBuf<double4_32a> sp, sv, sa;
+    CUDA_TRY(e, sp.alloc(b.n));
+    CUDA_TRY(e, sv.alloc(b.n));
+    CUDA_TRY(e, sa.alloc(b.n));
+    size_t bytes = (size_t)b.n * sizeof(double4_32a);
+    CUDA_TRY(e, cudaMemcpyAsync(sp.p, e->posq.p, bytes, cudaMemcpyDeviceToDevice, st));
+    CUDA_TRY(e, cudaMemcpyAsync(sv.p, e->vel.p, bytes, cudaMemcpyDeviceToDevice, st));
+    CUDA_TRY(e, cudaMemcpyAsync(sa.p, e->acc.p, bytes, cudaMemcpyDeviceToDevice, st));
+    for (int g = 0; g < LG_KT_COUNT; g++) {
+        float total = 0.f;
+        for (int r = 0; r < reps; r++) {
+            if (g == LG_KT_NLIST) launch_request_rebuild(b, st);
+            CUDA_TRY(e, cudaEventRecord(e0, st));
+            switch (g) {
+                case LG_KT_NLIST: launch_nlist_build(b, st); break;
+                case LG_KT_PAIR: launch_pair_forces(b, LG_TERM_ALL, false, st); break;
+                case LG_KT_BONDED: launch_bonded(b, LG_TERM_ALL, false, st); break;
+                case LG_KT_EIKR: launch_kspace_part(b, 0, false, st); break;
+                case LG_KT_RHO: launch_kspace_part(b, 1, false, st); break;
+                case LG_KT_FIELD: launch_kspace_part(b, 2, false, st); break;
+                case LG_KT_VV:
+                    launch_vv_first(b, st);
+                    launch_vv_second(b, thermo, st);
+                    break;
+                case LG_KT_STEP: enqueue_md_step(e, thermo, st); break;
+            }
+            CUDA_TRY(e, cudaEventRecord(e1, st));
+            CUDA_TRY(e, cudaEventSynchronize(e1));
+            float t = 0.f;
+            CUDA_TRY(e, cudaEventElapsedTime(&t, e0, e1));
+            total += t;
+            if (g == LG_KT_VV || g == LG_KT_STEP) {
+                CUDA_TRY(e, cudaMemcpyAsync(e->posq.p, sp.p, bytes, cudaMemcpyDeviceToDevice, st));
+                CUDA_TRY(e, cudaMemcpyAsync(e->vel.p, sv.p, bytes, cudaMemcpyDeviceToDevice, st));
+                CUDA_TRY(e, cudaMemcpyAsync(e->acc.p, sa.p, bytes, cudaMemcpyDeviceToDevice, st));
+            }
+        }
+        ms[g] = total / reps;
+    }
+    CUDA_TRY(e, cudaGetLastError());
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    // the forces buffer was overwritten by the timing runs: recompute it at the saved state
+    launch_request_rebuild(b, st);
+    CUDA_TRY(e, cudaMemsetAsync(e->force.p, 0, 3 * (size_t)b.n * sizeof(double), st));
+    enqueue_forces(e, LG_TERM_ALL, false, st);
+    CUDA_TRY(e, cudaStreamSynchronize(st));
+    return LG_OK;
 }
 
 // ---- Monte Carlo ---------------------------------------------------------------

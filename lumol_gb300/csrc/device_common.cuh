@@ -27,6 +27,20 @@ struct PairDev {
     float pad_f;
 };
 
+// FP32 pair table entry of the mixed path.
+//   LJ: a = 4 eps sigma^12, b = 4 eps sigma^6;  Buckingham: a = A, b = C, c = 1 / rho;
+//   Harmonic: a = k, b = x0.  shift: energy shift of a shifted interaction.
+struct PairDevF {
+    int32_t type, restriction, pad0, pad1;
+    float a, b, c, rc2, shift, scale14, pad2, pad3;
+};
+
+// FP32 k-vector of the mixed Ewald field kernel.
+struct KVecF {
+    int32_t ikx, iky, ikz, sys;
+    float fx, fy, fz, energy;
+};
+
 // Per-system descriptor (one Lumol System).
 struct SysDev {
     double L[3];          // orthorhombic cell lengths (UnitCell::a/b/c)
@@ -52,6 +66,7 @@ struct SysDev {
     double thermo_T, thermo_tau;  // Berendsen (tau <= 0: none)
     double dof;                   // 3 N (DegreesOfFreedom::Particles)
     float Lf[3], invLf[3];        // FP32 copies for the list build and the mixed path
+    float Llo[3];                 // L - (double)Lf: low word of the cell lengths
     float rlist2_f;               // (rlist + margin)^2 in FP32
     float coul_rc2_f;
 };

@@ -59,26 +59,36 @@ __device__ __forceinline__ PairDecision decide_pair(const SysDev& s, const PairD
     return d;
 }
 
-template <bool EV>
+template <int TPA>
+__device__ __forceinline__ double group_sum(double v) {
+#pragma unroll
+    for (int o = TPA / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// TPA threads per atom (1..32, autotuned) walk atom i's neighbour list.
+template <int TPA, bool EV>
 __global__ void __launch_bounds__(256) pair_fp64_kernel(
     int n, const double4_32a* __restrict__ posq, const int* __restrict__ kind, const int* __restrict__ mol,
     const int* __restrict__ sysid, const SysDev* __restrict__ sys, const PairDev* __restrict__ ptab,
     const int* __restrict__ nbr, const int* __restrict__ nnb, int maxnb, const int* __restrict__ spec_off,
     const int* __restrict__ spec_j, const int8_t* __restrict__ spec_path, uint32_t terms,
     double* __restrict__ force, double* __restrict__ red) {
-    int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int lane = threadIdx.x & 31;
-    if (i >= n) return;
-    const SysDev& s = sys[sysid[i]];
-    double4_32a pi = posq[i];
-    int ki = kind[i], mi = mol[i];
+    int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = gt / TPA;
+    int sub = gt % TPA;
+    bool active = i < n;
+    int ii = active ? i : n - 1;
+    const SysDev& s = sys[sysid[ii]];
+    double4_32a pi = posq[ii];
+    int ki = kind[ii], mi = mol[ii];
     const PairDev* prow = ptab + s.ptab + ki * s.nk;
     double fx = 0.0, fy = 0.0, fz = 0.0;
     double ep = 0.0, ec = 0.0;
     double wxx = 0.0, wxy = 0.0, wxz = 0.0, wyy = 0.0, wyz = 0.0, wzz = 0.0;
-    int cnt = nnb[i];
-    const int* list = nbr + (size_t)i * maxnb;
-    for (int k = lane; k < cnt; k += 32) {
+    int cnt = active ? nnb[ii] : 0;
+    const int* list = nbr + (size_t)ii * maxnb;
+    for (int k = sub; k < cnt; k += TPA) {
         int j = list[k];
         double4_32a pj = posq[j];
         double dx, dy, dz;
@@ -122,20 +132,20 @@ __global__ void __launch_bounds__(256) pair_fp64_kernel(
             wzz += gz * dz;
         }
     }
-    fx = warp_sum(fx);
-    fy = warp_sum(fy);
-    fz = warp_sum(fz);
+    fx = group_sum<TPA>(fx);
+    fy = group_sum<TPA>(fy);
+    fz = group_sum<TPA>(fz);
     if (EV) {
-        ep = warp_sum(ep);
-        ec = warp_sum(ec);
-        wxx = warp_sum(wxx);
-        wxy = warp_sum(wxy);
-        wxz = warp_sum(wxz);
-        wyy = warp_sum(wyy);
-        wyz = warp_sum(wyz);
-        wzz = warp_sum(wzz);
+        ep = group_sum<TPA>(ep);
+        ec = group_sum<TPA>(ec);
+        wxx = group_sum<TPA>(wxx);
+        wxy = group_sum<TPA>(wxy);
+        wxz = group_sum<TPA>(wxz);
+        wyy = group_sum<TPA>(wyy);
+        wyz = group_sum<TPA>(wyz);
+        wzz = group_sum<TPA>(wzz);
     }
-    if (lane == 0) {
+    if (active && sub == 0) {
         force[3 * i] += fx;
         force[3 * i + 1] += fy;
         force[3 * i + 2] += fz;
@@ -154,19 +164,35 @@ __global__ void __launch_bounds__(256) pair_fp64_kernel(
     }
 }
 
-void launch_pair_forces(const Batch& b, uint32_t terms, bool ev, cudaStream_t st) {
-    if (b.n == 0) return;
+template <int TPA>
+void launch_pair_fp64_tpa(const Batch& b, uint32_t terms, bool ev, cudaStream_t st) {
     int tb = 256;
-    long long threads = (long long)b.n * 32;
+    long long threads = (long long)b.n * TPA;
     unsigned grid = (unsigned)((threads + tb - 1) / tb);
     if (ev)
-        pair_fp64_kernel<true><<<grid, tb, 0, st>>>(b.n, b.posq, b.kind, b.mol, b.sysid, b.sys, b.ptab,
-                                                    b.nbr, b.nnb, b.maxnb, b.spec_off, b.spec_j,
-                                                    b.spec_path, terms, b.force, b.red);
+        pair_fp64_kernel<TPA, true><<<grid, tb, 0, st>>>(b.n, b.posq, b.kind, b.mol, b.sysid, b.sys, b.ptab,
+                                                         b.nbr, b.nnb, b.maxnb, b.spec_off, b.spec_j,
+                                                         b.spec_path, terms, b.force, b.red);
     else
-        pair_fp64_kernel<false><<<grid, tb, 0, st>>>(b.n, b.posq, b.kind, b.mol, b.sysid, b.sys, b.ptab,
-                                                     b.nbr, b.nnb, b.maxnb, b.spec_off, b.spec_j,
-                                                     b.spec_path, terms, b.force, b.red);
+        pair_fp64_kernel<TPA, false><<<grid, tb, 0, st>>>(b.n, b.posq, b.kind, b.mol, b.sysid, b.sys, b.ptab,
+                                                          b.nbr, b.nnb, b.maxnb, b.spec_off, b.spec_j,
+                                                          b.spec_path, terms, b.force, b.red);
+}
+
+void launch_pair_forces(const Batch& b, uint32_t terms, bool ev, cudaStream_t st) {
+    if (b.n == 0) return;
+    if (b.precision == 1) {
+        launch_pair_mixed(b, terms, ev, st);
+        return;
+    }
+    switch (b.tpa) {
+        case 1: launch_pair_fp64_tpa<1>(b, terms, ev, st); break;
+        case 2: launch_pair_fp64_tpa<2>(b, terms, ev, st); break;
+        case 4: launch_pair_fp64_tpa<4>(b, terms, ev, st); break;
+        case 8: launch_pair_fp64_tpa<8>(b, terms, ev, st); break;
+        case 16: launch_pair_fp64_tpa<16>(b, terms, ev, st); break;
+        default: launch_pair_fp64_tpa<32>(b, terms, ev, st); break;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -396,6 +422,12 @@ __global__ void field_reduce_kernel(int n, int nchunks, const double4_32a* __res
 
 void launch_kspace(const Batch& b, bool forces, bool ev, cudaStream_t st) {
     if (b.nkvec == 0 || b.n == 0) return;
+    if (b.precision == 1) {
+        launch_kspace_mixed_part(b, 0, ev, st);
+        launch_kspace_mixed_part(b, 1, ev, st);
+        if (forces) launch_kspace_mixed_part(b, 2, ev, st);
+        return;
+    }
     int tb = 256;
     eikr_kernel<<<(3 * b.n + tb - 1) / tb, tb, 0, st>>>(b.n, b.kdim, b.posq, b.sysid, b.sys, b.eikr);
     if (ev)
@@ -408,6 +440,32 @@ void launch_kspace(const Batch& b, bool forces, bool ev, cudaStream_t st) {
         field_reduce_kernel<<<(b.n + 127) / 128, 128, 0, st>>>(b.n, b.nkchunks, b.posq, b.sysid, b.sys,
                                                                b.fpart, b.force);
     }
+}
+
+// One piece of launch_kspace: 0 eikr, 1 rho, 2 field + force.
+void launch_kspace_part(const Batch& b, int part, bool ev, cudaStream_t st) {
+    if (b.nkvec == 0 || b.n == 0) return;
+    if (b.precision == 1) {
+        launch_kspace_mixed_part(b, part, ev, st);
+        return;
+    }
+    if (part == 0) {
+        eikr_kernel<<<(3 * b.n + 255) / 256, 256, 0, st>>>(b.n, b.kdim, b.posq, b.sysid, b.sys, b.eikr);
+    } else if (part == 1) {
+        if (ev)
+            rho_kernel<true><<<b.nkvec, 256, 0, st>>>(b.n, b.posq, b.sys, b.kvec, b.eikr, b.rho, b.kred);
+        else
+            rho_kernel<false><<<b.nkvec, 256, 0, st>>>(b.n, b.posq, b.sys, b.kvec, b.eikr, b.rho, b.kred);
+    } else {
+        dim3 grid((b.n + 127) / 128, b.nkchunks);
+        field_kernel<<<grid, 128, 0, st>>>(b.n, b.kchunk, b.sysid, b.sys, b.kvec, b.eikr, b.rho, b.fpart);
+        launch_field_reduce(b, st);
+    }
+}
+
+void launch_field_reduce(const Batch& b, cudaStream_t st) {
+    field_reduce_kernel<<<(b.n + 127) / 128, 128, 0, st>>>(b.n, b.nkchunks, b.posq, b.sysid, b.sys, b.fpart,
+                                                           b.force);
 }
 
 // ---------------------------------------------------------------------------
@@ -475,6 +533,7 @@ __global__ void __launch_bounds__(256) reduce_kernel(const SysDev* __restrict__ 
 }
 
 void launch_reduce(const Batch& b, uint32_t terms, bool kspace, double* out, cudaStream_t st) {
+    if (b.nsys == 0) return;
     reduce_kernel<<<b.nsys, 256, 0, st>>>(b.sys, b.red, b.kred, b.host_const, terms, kspace ? 1 : 0, out,
                                           b.status);
 }

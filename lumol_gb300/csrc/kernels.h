@@ -58,6 +58,14 @@ struct Batch {
     double* host_const = nullptr; // [nsys][RED_STRIDE]: tail energy/virial, Ewald self energy
     double* lambda = nullptr;     // nsys Berendsen factors
     double* ke = nullptr;         // n kinetic energies
+    // mixed precision
+    int tpa = 32;                 // threads per atom of the pair kernels (autotuned)
+    float4* pos_hi = nullptr;     // wrapped positions, high FP32 word, charge
+    float4* pos_lo = nullptr;     // low FP32 word
+    PairDevF* ptabf = nullptr;
+    KVecF* kvecf = nullptr;
+    float2* eikrf = nullptr;
+    float2* rhof = nullptr;
 };
 
 // nlist.cu
@@ -66,6 +74,12 @@ void launch_nlist_build(const Batch& b, cudaStream_t st);
 void launch_pair_forces(const Batch& b, uint32_t terms, bool ev, cudaStream_t st);
 void launch_bonded(const Batch& b, uint32_t terms, bool ev, cudaStream_t st);
 void launch_kspace(const Batch& b, bool forces, bool ev, cudaStream_t st);
+void launch_kspace_part(const Batch& b, int part, bool ev, cudaStream_t st);
+void launch_field_reduce(const Batch& b, cudaStream_t st);
+// mixed.cu
+void launch_pair_mixed(const Batch& b, uint32_t terms, bool ev, cudaStream_t st);
+void launch_split_positions(const Batch& b, cudaStream_t st);
+void launch_kspace_mixed_part(const Batch& b, int part, bool ev, cudaStream_t st);
 void launch_reduce(const Batch& b, uint32_t terms, bool kspace, double* out, cudaStream_t st);
 void launch_pairset(const Batch& b, int family, int s_begin, int s_end, int* out, long long cap,
                     unsigned long long* count, cudaStream_t st);
@@ -79,5 +93,8 @@ void launch_vv_second(const Batch& b, bool thermostat, cudaStream_t st);
 void launch_thermostat(const Batch& b, cudaStream_t st);
 void launch_request_rebuild(const Batch& b, cudaStream_t st);
 void launch_check_displacement(const Batch& b, cudaStream_t st);
+
+// diag.cu
+int measure_fma_peak(int fp64, double* tflops);
 
 }  // namespace lg

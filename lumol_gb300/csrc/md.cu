@@ -183,6 +183,7 @@ void launch_vv_second(const Batch& b, bool thermostat, cudaStream_t st) {
                                                           thermostat ? 1 : 0);
 }
 void launch_thermostat(const Batch& b, cudaStream_t st) {
+    if (b.n == 0) return;
     thermostat_reduce_kernel<<<b.nsys, 256, 0, st>>>(b.sys, b.ke, b.lambda);
     thermostat_scale_kernel<<<(b.n + 255) / 256, 256, 0, st>>>(b.n, b.sysid, b.lambda, b.vel);
 }

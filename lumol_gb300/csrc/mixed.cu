@@ -1,0 +1,401 @@
+// mixed.cu -- the mixed-precision force path.
+//
+// Pair potentials and Ewald real space / Wolf are evaluated in FP32; every
+// atom's force is summed with error-free TwoSum steps (a compensated FP32
+// sum, converted to FP64 once per atom); energies and virials are accumulated
+// in FP64; the Ewald structure factors rho(k) are accumulated in FP64; the
+// integrator keeps FP64 positions and velocities.
+//
+// Positions reach the kernels as two FP32 words per coordinate, hi + lo = the
+// wrapped FP64 position to about 48 bits, and the cell length likewise, so
+// the minimum-image difference of two atoms carries only the FP32 rounding of
+// the difference itself (relative 6e-8), not the FP32 rounding of absolute
+// positions (which would be an absolute ulp(L) error).
+//
+// Threads per atom (TPA = 1..32) is a template parameter chosen per workload
+// by the autotuner: the TPA lanes of a group walk one atom's neighbour list
+// and combine their compensated partial sums with shuffles.
+#include "kernels.h"
+
+namespace lg {
+
+__device__ __forceinline__ void two_sum_acc(float& s, float& c, float x) {
+    float t = s + x;
+    float bp = t - s;
+    float err = (s - (t - bp)) + (x - bp);
+    s = t;
+    c += err;
+}
+
+template <int TPA>
+__device__ __forceinline__ double group_sum_comp(float s, float c) {
+#pragma unroll
+    for (int o = TPA / 2; o > 0; o >>= 1) {
+        float so = __shfl_xor_sync(0xffffffffu, s, o);
+        float co = __shfl_xor_sync(0xffffffffu, c, o);
+        two_sum_acc(s, c, so);
+        c += co;
+    }
+    return (double)s + (double)c;
+}
+
+template <int TPA>
+__device__ __forceinline__ double group_sum_d(double v) {
+#pragma unroll
+    for (int o = TPA / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Minimum image of hi/lo coordinates in FP32 (the image shift uses L = Lhi + Llo).
+__device__ __forceinline__ float mixed_image(float hi_i, float lo_i, float hi_j, float lo_j, float Lhi, float Llo,
+                                             float invL) {
+    float d = (hi_i - hi_j) + (lo_i - lo_j);
+    float nimg = rintf(d * invL);
+    d = fmaf(-nimg, Lhi, d);
+    d = fmaf(-nimg, Llo, d);
+    return d;
+}
+
+// Pair potential in FP32: returns energy, writes force / r.
+__device__ __forceinline__ float pair_mixed(const PairDevF& p, float r2, float inv_r2, float inv_r, float& fr) {
+    switch (p.type) {
+        case 2: {  // LJ: c12 / r^12 - c6 / r^6
+            float ir6 = inv_r2 * inv_r2 * inv_r2;
+            float e = ir6 * (p.a * ir6 - p.b);
+            fr = ir6 * (12.0f * p.a * ir6 - 6.0f * p.b) * inv_r2;
+            return e - p.shift;
+        }
+        case 3: {  // Buckingham: A exp(-r / rho) - C / r^6
+            float r = r2 * inv_r;
+            float ex = p.a * __expf(-r * p.c);
+            float ir6 = inv_r2 * inv_r2 * inv_r2;
+            fr = ex * p.c * inv_r - 6.0f * p.b * ir6 * inv_r2;
+            return ex - p.b * ir6 - p.shift;
+        }
+        case 4: {  // Harmonic k / 2 (r - x0)^2
+            float r = r2 * inv_r;
+            float dx = r - p.b;
+            fr = -p.a * dx * inv_r;
+            return 0.5f * p.a * dx * dx - p.shift;
+        }
+        default:
+            fr = 0.0f;
+            return 0.0f;
+    }
+}
+
+template <int TPA, bool EV>
+__global__ void __launch_bounds__(256) pair_mixed_kernel(
+    int n, const float4* __restrict__ phi, const float4* __restrict__ plo, const int* __restrict__ kind,
+    const int* __restrict__ mol, const int* __restrict__ sysid, const SysDev* __restrict__ sys,
+    const PairDevF* __restrict__ ptab, const int* __restrict__ nbr, const int* __restrict__ nnb, int maxnb,
+    const int* __restrict__ spec_off, const int* __restrict__ spec_j, const int8_t* __restrict__ spec_path,
+    uint32_t terms, double* __restrict__ force, double* __restrict__ red) {
+    int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = gt / TPA;
+    int sub = gt % TPA;
+    bool active = i < n;
+    int ii = active ? i : n - 1;
+    const SysDev& s = sys[sysid[ii]];
+    float4 hi = phi[ii], lo = plo[ii];
+    int ki = kind[ii], mi = mol[ii];
+    const PairDevF* prow = ptab + s.ptab + ki * s.nk;
+    float Lh0 = s.Lf[0], Lh1 = s.Lf[1], Lh2 = s.Lf[2];
+    float Ll0 = s.Llo[0], Ll1 = s.Llo[1], Ll2 = s.Llo[2];
+    float iL0 = s.invLf[0], iL1 = s.invLf[1], iL2 = s.invLf[2];
+    bool coul = (terms & 16u) && s.coul != 0 && hi.w != 0.0f;
+    bool pairs = (terms & 1u) != 0;
+    float coul_rc2 = s.coul_rc2_f;
+    float alpha = (float)s.alpha;
+    float pref = hi.w * (float)(1.0 / FOUR_PI_EPSILON_0);
+    float fxs = 0.f, fxc = 0.f, fys = 0.f, fyc = 0.f, fzs = 0.f, fzc = 0.f;
+    double ep = 0.0, ec = 0.0;
+    double w0 = 0, w1 = 0, w2 = 0, w3 = 0, w4 = 0, w5 = 0;
+    int cnt = active ? nnb[ii] : 0;
+    const int* list = nbr + (size_t)ii * maxnb;
+    for (int k = sub; k < cnt; k += TPA) {
+        int j = list[k];
+        float4 hj = phi[j], lj = plo[j];
+        float dx = mixed_image(hi.x, lo.x, hj.x, lj.x, Lh0, Ll0, iL0);
+        float dy = mixed_image(hi.y, lo.y, hj.y, lj.y, Lh1, Ll1, iL1);
+        float dz = mixed_image(hi.z, lo.z, hj.z, lj.z, Lh2, Ll2, iL2);
+        float r2 = dx * dx + dy * dy + dz * dz;
+        const PairDevF& p = prow[kind[j]];
+        bool pin = pairs && p.type != 0 && r2 < p.rc2;
+        bool cin = coul && hj.w != 0.0f && r2 <= coul_rc2;
+        if (!(pin || cin)) continue;
+        int path = -1;
+        int mj = mol[j];
+        float sc = 1.0f;
+        if (pin && p.restriction != 0) {
+            path = p.restriction <= 2 ? (mi != mj ? 0 : 5) : bond_path(i, j, mi, mj, spec_off, spec_j, spec_path);
+            if (restriction_excluded(p.restriction, path)) pin = false;
+            else sc = p.restriction == 6 && path == 4 ? p.scale14 : 1.0f;
+        }
+        float inv_r = rsqrtf(r2);
+        float inv_r2 = inv_r * inv_r;
+        float fr = 0.0f;
+        float e_pair = 0.0f, e_coul = 0.0f;
+        if (pin) {
+            float f;
+            e_pair = sc * pair_mixed(p, r2, inv_r2, inv_r, f);
+            fr = sc * f;
+        }
+        if (cin) {
+            bool excl = false;
+            float csc = 1.0f;
+            if (s.coul_restr != 0) {
+                if (path < 0 || (s.coul_restr > 2 && path == 5))
+                    path = s.coul_restr <= 2 ? (mi != mj ? 0 : 5)
+                                             : bond_path(i, j, mi, mj, spec_off, spec_j, spec_path);
+                excl = restriction_excluded(s.coul_restr, path);
+                if (s.coul_restr == 6 && path == 4) csc = (float)s.coul_scale14;
+            }
+            float qq = pref * hj.w;
+            float r = r2 * inv_r;
+            float ar = alpha * r;
+            if (s.coul == 1) {
+                float g = alpha * (float)FRAC_2_SQRT_PI * __expf(-ar * ar);
+                if (excl) {
+                    float ef = erff(ar);
+                    e_coul = -qq * ef * inv_r;
+                    fr += qq * inv_r2 * (g - ef * inv_r);
+                } else {
+                    float ec_ = erfcf(ar);
+                    e_coul = qq * ec_ * inv_r;
+                    fr += qq * inv_r2 * (g + ec_ * inv_r);
+                }
+            } else if (!excl) {
+                float ec_ = erfcf(ar);
+                e_coul = csc * qq * (ec_ * inv_r - (float)s.wolf_ec);
+                float factor = ec_ * inv_r2 + alpha * (float)FRAC_2_SQRT_PI * __expf(-ar * ar) * inv_r;
+                fr += csc * qq * (factor - (float)s.wolf_fc) * inv_r;
+            }
+        }
+        float gx = fr * dx, gy = fr * dy, gz = fr * dz;
+        two_sum_acc(fxs, fxc, gx);
+        two_sum_acc(fys, fyc, gy);
+        two_sum_acc(fzs, fzc, gz);
+        if (EV && j > i) {
+            ep += (double)e_pair;
+            ec += (double)e_coul;
+            w0 += (double)(gx * dx);
+            w1 += (double)(gx * dy);
+            w2 += (double)(gx * dz);
+            w3 += (double)(gy * dy);
+            w4 += (double)(gy * dz);
+            w5 += (double)(gz * dz);
+        }
+    }
+    double fx = group_sum_comp<TPA>(fxs, fxc);
+    double fy = group_sum_comp<TPA>(fys, fyc);
+    double fz = group_sum_comp<TPA>(fzs, fzc);
+    if (EV) {
+        ep = group_sum_d<TPA>(ep);
+        ec = group_sum_d<TPA>(ec);
+        w0 = group_sum_d<TPA>(w0);
+        w1 = group_sum_d<TPA>(w1);
+        w2 = group_sum_d<TPA>(w2);
+        w3 = group_sum_d<TPA>(w3);
+        w4 = group_sum_d<TPA>(w4);
+        w5 = group_sum_d<TPA>(w5);
+    }
+    if (active && sub == 0) {
+        force[3 * i] += fx;
+        force[3 * i + 1] += fy;
+        force[3 * i + 2] += fz;
+        if (EV) {
+            if ((terms & 16u) && s.coul == 2 && hi.w != 0.0f) {
+                double q = (double)hi.w;
+                ec -= q * q * 0.5 * (s.wolf_ec + s.alpha * FRAC_2_SQRT_PI) / FOUR_PI_EPSILON_0;
+            }
+            double* rr = red + (size_t)i * RED_STRIDE;
+            rr[E_PAIRS] += ep;
+            rr[E_COUL] += ec;
+            double* w = rr + N_ESLOT;
+            w[0] += w0; w[1] += w1; w[2] += w2;
+            w[3] += w1; w[4] += w3; w[5] += w4;
+            w[6] += w2; w[7] += w4; w[8] += w5;
+        }
+    }
+}
+
+template <int TPA>
+void launch_pair_mixed_tpa(const Batch& b, uint32_t terms, bool ev, cudaStream_t st) {
+    int tb = 256;
+    long long threads = (long long)b.n * TPA;
+    unsigned grid = (unsigned)((threads + tb - 1) / tb);
+    if (ev)
+        pair_mixed_kernel<TPA, true><<<grid, tb, 0, st>>>(b.n, b.pos_hi, b.pos_lo, b.kind, b.mol, b.sysid, b.sys,
+                                                          b.ptabf, b.nbr, b.nnb, b.maxnb, b.spec_off, b.spec_j,
+                                                          b.spec_path, terms, b.force, b.red);
+    else
+        pair_mixed_kernel<TPA, false><<<grid, tb, 0, st>>>(b.n, b.pos_hi, b.pos_lo, b.kind, b.mol, b.sysid, b.sys,
+                                                           b.ptabf, b.nbr, b.nnb, b.maxnb, b.spec_off, b.spec_j,
+                                                           b.spec_path, terms, b.force, b.red);
+}
+
+void launch_pair_mixed(const Batch& b, uint32_t terms, bool ev, cudaStream_t st) {
+    if (b.n == 0) return;
+    switch (b.tpa) {
+        case 1: launch_pair_mixed_tpa<1>(b, terms, ev, st); break;
+        case 2: launch_pair_mixed_tpa<2>(b, terms, ev, st); break;
+        case 4: launch_pair_mixed_tpa<4>(b, terms, ev, st); break;
+        case 8: launch_pair_mixed_tpa<8>(b, terms, ev, st); break;
+        case 16: launch_pair_mixed_tpa<16>(b, terms, ev, st); break;
+        default: launch_pair_mixed_tpa<32>(b, terms, ev, st); break;
+    }
+}
+
+// FP32 hi / lo split of the wrapped FP64 positions (UnitCell::wrap_vector).
+__global__ void split_positions_kernel(int n, const double4_32a* __restrict__ posq, const int* __restrict__ sysid,
+                                       const SysDev* __restrict__ sys, float4* __restrict__ phi,
+                                       float4* __restrict__ plo) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const SysDev& s = sys[sysid[i]];
+    double4_32a p = posq[i];
+    double w[3] = {p.x, p.y, p.z};
+    float h[3], l[3];
+    for (int d = 0; d < 3; d++) {
+        double x = w[d] - floor(w[d] * s.invL[d]) * s.L[d];
+        h[d] = (float)x;
+        l[d] = (float)(x - (double)h[d]);
+    }
+    phi[i] = make_float4(h[0], h[1], h[2], (float)p.w);
+    plo[i] = make_float4(l[0], l[1], l[2], 0.0f);
+}
+
+void launch_split_positions(const Batch& b, cudaStream_t st) {
+    if (b.n && b.pos_hi)
+        split_positions_kernel<<<(b.n + 255) / 256, 256, 0, st>>>(b.n, b.posq, b.sysid, b.sys, b.pos_hi, b.pos_lo);
+}
+
+// ---------------------------------------------------------------------------
+// Mixed Ewald k-space: FP32 e^{ik.r} with the phase reduced in FP64, FP64
+// rho(k) accumulation, FP32 field per chunk of k-vectors.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+__global__ void eikr_mixed_kernel(int n, const double4_32a* __restrict__ posq, const int* __restrict__ sysid,
+                                  const SysDev* __restrict__ sys, float2* __restrict__ eikr) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 3 * n) return;
+    int axis = t / n, i = t - axis * n;
+    const SysDev& s = sys[sysid[i]];
+    if (s.coul != 1) return;
+    double4_32a p = posq[i];
+    double x = axis == 0 ? p.x : (axis == 1 ? p.y : p.z);
+    double phase = s.k1[axis] * x;
+    phase -= 2.0 * PI * rint(phase * (0.5 / PI));
+    float sn, cs;
+    sincosf((float)phase, &sn, &cs);
+    float2 e1 = make_float2(cs, sn);
+    eikr[(size_t)(0 * 3 + axis) * n + i] = make_float2(1.0f, 0.0f);
+    eikr[(size_t)(1 * 3 + axis) * n + i] = e1;
+    float2 e = e1;
+    for (int kk = 2; kk <= s.kmax; kk++) {
+        e = cmulf(e, e1);
+        eikr[(size_t)(kk * 3 + axis) * n + i] = e;
+    }
+}
+
+__device__ __forceinline__ float2 eikrf_at(const float2* __restrict__ eikr, int n, int kk, int axis, int i) {
+    if (kk >= 0) return eikr[(size_t)(kk * 3 + axis) * n + i];
+    float2 v = eikr[(size_t)((-kk) * 3 + axis) * n + i];
+    return make_float2(v.x, -v.y);
+}
+
+template <bool EV>
+__global__ void __launch_bounds__(256) rho_mixed_kernel(int n, const double4_32a* __restrict__ posq,
+                                                        const SysDev* __restrict__ sys,
+                                                        const KVecDev* __restrict__ kvec,
+                                                        const float2* __restrict__ eikr, double2* __restrict__ rho,
+                                                        float2* __restrict__ rhof, double* __restrict__ kred) {
+    __shared__ double sre[256], sim[256];
+    int k = blockIdx.x;
+    KVecDev kv = kvec[k];
+    const SysDev& s = sys[kv.sys];
+    double re = 0.0, im = 0.0;
+    for (int i = s.begin + threadIdx.x; i < s.end; i += blockDim.x) {
+        float2 ph = cmulf(cmulf(eikrf_at(eikr, n, kv.ikx, 0, i), eikrf_at(eikr, n, kv.iky, 1, i)),
+                          eikrf_at(eikr, n, kv.ikz, 2, i));
+        double q = posq[i].w;
+        re += q * (double)ph.x;
+        im += q * (double)ph.y;
+    }
+    sre[threadIdx.x] = re;
+    sim[threadIdx.x] = im;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            sre[threadIdx.x] += sre[threadIdx.x + o];
+            sim[threadIdx.x] += sim[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double2 r = make_double2(sre[0], sim[0]);
+        rho[k] = r;
+        rhof[k] = make_float2((float)r.x, (float)r.y);
+        if (EV) {
+            double nrm = r.x * r.x + r.y * r.y;
+            double* out = kred + (size_t)k * 7;
+            out[0] = kv.energy * nrm;
+            for (int c = 0; c < 6; c++) out[1 + c] = nrm * kv.virial[c];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) field_mixed_kernel(int n, int kchunk, const int* __restrict__ sysid,
+                                                          const SysDev* __restrict__ sys,
+                                                          const KVecF* __restrict__ kvecf,
+                                                          const float2* __restrict__ eikr,
+                                                          const float2* __restrict__ rhof,
+                                                          double* __restrict__ fpart) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int c = blockIdx.y;
+    if (i >= n) return;
+    const SysDev& s = sys[sysid[i]];
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    if (s.coul == 1) {
+        int k0 = s.kbegin + c * kchunk;
+        int k1 = min(k0 + kchunk, s.kend);
+        for (int k = k0; k < k1; k++) {
+            KVecF kv = kvecf[k];
+            float2 e = cmulf(cmulf(eikrf_at(eikr, n, kv.ikx, 0, i), eikrf_at(eikr, n, kv.iky, 1, i)),
+                             eikrf_at(eikr, n, kv.ikz, 2, i));
+            float2 r = rhof[k];
+            float imag = e.y * r.x - e.x * r.y;
+            fx = fmaf(imag, kv.fx, fx);
+            fy = fmaf(imag, kv.fy, fy);
+            fz = fmaf(imag, kv.fz, fz);
+        }
+    }
+    double* out = fpart + (size_t)c * 3 * n + 3 * (size_t)i;
+    out[0] = fx;
+    out[1] = fy;
+    out[2] = fz;
+}
+
+void launch_kspace_mixed_part(const Batch& b, int part, bool ev, cudaStream_t st) {
+    if (b.nkvec == 0 || b.n == 0) return;
+    if (part == 0) {
+        eikr_mixed_kernel<<<(3 * b.n + 255) / 256, 256, 0, st>>>(b.n, b.posq, b.sysid, b.sys, b.eikrf);
+    } else if (part == 1) {
+        if (ev)
+            rho_mixed_kernel<true><<<b.nkvec, 256, 0, st>>>(b.n, b.posq, b.sys, b.kvec, b.eikrf, b.rho, b.rhof,
+                                                            b.kred);
+        else
+            rho_mixed_kernel<false><<<b.nkvec, 256, 0, st>>>(b.n, b.posq, b.sys, b.kvec, b.eikrf, b.rho, b.rhof,
+                                                             b.kred);
+    } else {
+        dim3 grid((b.n + 127) / 128, b.nkchunks);
+        field_mixed_kernel<<<grid, 128, 0, st>>>(b.n, b.kchunk, b.sysid, b.sys, b.kvecf, b.eikrf, b.rhof, b.fpart);
+        launch_field_reduce(b, st);
+    }
+}
+
+}  // namespace lg

@@ -184,6 +184,7 @@ __global__ void nl_done_kernel(uint32_t* status) {
 
 void launch_nlist_build(const Batch& b, cudaStream_t st) {
     int n = b.n;
+    if (n == 0) return;
     int tb = 256;
     nl_bin_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, b.posq, b.sysid, b.sys, b.status, b.atom_cell,
                                                   b.cell_count, b.wpos, b.pos_build);

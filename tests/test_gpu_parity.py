@@ -1,0 +1,189 @@
+"""Parity of the FP64 GPU path with the CPU oracle, through the C ABI.
+
+Bar: pair sets bit-for-bit; energies, virials and forces within 1e-10
+relative (forces as the RMS of the difference over the RMS of the oracle's
+forces; virials relative to their largest entry)."""
+import numpy as np
+import pytest
+
+import lumol_gb300 as lg
+import oracle
+import systems
+from lumol_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+TERMS = [lg.LG_TERM_ALL, lg.LG_TERM_PAIRS, lg.LG_TERM_TAIL, lg.LG_TERM_BONDS, lg.LG_TERM_ANGLES,
+         lg.LG_TERM_COUL_REAL, lg.LG_TERM_COUL_SELF, lg.LG_TERM_COUL_KSPACE]
+
+
+def _rel(a, b, scale):
+    return abs(a - b) / max(abs(scale), 1e-300)
+
+
+def assert_parity(system, terms_list=TERMS, tol=TOL):
+    orc = oracle.Oracle(system)
+    e_all = abs(orc.energy())
+    for terms in terms_list:
+        f, e, w = system.compute(terms)
+        fo, eo, wo = orc.forces(terms), orc.energy(terms), orc.virial(terms)
+        escale = max(abs(eo), 1e-12 * e_all, 1e-300)
+        assert _rel(e, eo, escale) <= tol, (terms, e, eo)
+        wscale = max(np.abs(wo).max(), 1e-300)
+        assert np.abs(w - wo).max() / wscale <= tol or np.abs(wo).max() < 1e-14, (terms, w, wo)
+        frms = np.sqrt(np.mean(fo * fo))
+        if frms > 0:
+            err = np.sqrt(np.mean((f - fo) ** 2)) / frms
+            assert err <= tol, (terms, err)
+        else:
+            assert np.abs(f).max() == 0.0
+
+
+def jitter(system, amount, seed):
+    rng = np.random.default_rng(seed)
+    system.positions = system.positions + rng.uniform(-amount, amount, size=system.positions.shape)
+    return system
+
+
+def test_argon_fcc_lj_shifted():
+    s = jitter(workloads.argon_fcc(), 0.3, 1)
+    assert_parity(s)
+
+
+def test_nacl_ewald():
+    s = workloads.nacl_crystal()
+    assert_parity(s)
+
+
+def test_nacl_wolf():
+    s = workloads.nacl_crystal(coulomb="wolf")
+    assert_parity(s)
+
+
+def test_small_water_ewald_bonds_angles_exclusions():
+    s = workloads.water_box(n_side=7, length=21.76)
+    s = jitter(s, 0.05, 2)
+    assert_parity(s)
+
+
+def test_reference_unit_systems():
+    s = systems.nacl_pair()
+    s.set_coulomb_potential(lg.Ewald(8.0, 10))
+    assert_parity(s)
+    s = systems.ewald_water()
+    ew = lg.Ewald(8.0, 10)
+    ew.set_restriction(lg.PairRestriction.INTER_MOLECULAR)
+    s.set_coulomb_potential(ew)
+    assert_parity(s)
+    assert_parity(systems.evaluator_system(), [lg.LG_TERM_PAIRS, lg.LG_TERM_TAIL, lg.LG_TERM_BONDS,
+                                               lg.LG_TERM_ANGLES])
+
+
+@pytest.mark.parametrize("buckingham", [False, True])
+def test_two_kind_fluid_unwrapped(buckingham):
+    s = systems.random_lj_fluid(700, 0.02, 5, 9.0, buckingham=buckingham)
+    assert_parity(s, [lg.LG_TERM_ALL, lg.LG_TERM_PAIRS, lg.LG_TERM_TAIL])
+
+
+@pytest.mark.parametrize("restriction", [lg.PairRestriction.EXCLUDE12, lg.PairRestriction.EXCLUDE13,
+                                         lg.PairRestriction.EXCLUDE14, lg.PairRestriction.scale14(0.5),
+                                         lg.PairRestriction.INTRA_MOLECULAR])
+def test_chain_restrictions_wolf(restriction):
+    s = systems.chains(27, 24.0, 7, restriction, coulomb=lg.Wolf(8.0))
+    assert_parity(s)
+
+
+@pytest.mark.parametrize("restriction", [lg.PairRestriction.EXCLUDE13, lg.PairRestriction.INTER_MOLECULAR])
+def test_chain_restrictions_ewald(restriction):
+    s = systems.chains(27, 24.0, 8, restriction, coulomb=lg.Ewald(8.0, 6, 0.4))
+    assert_parity(s)
+
+
+# ---- pair sets, bit for bit ----------------------------------------------------------
+def _pairset_equal(system):
+    orc = oracle.Oracle(system)
+    for family in (0, 1):
+        gpu = system.pair_set(family)
+        ref = orc.pairset(family)
+        assert gpu.shape == ref.shape and np.array_equal(gpu, ref), family
+
+
+def test_pairset_nacl_and_water():
+    _pairset_equal(workloads.nacl_crystal())
+    _pairset_equal(jitter(workloads.water_box(n_side=7, length=21.76), 0.05, 3))
+
+
+def test_pairset_atoms_exactly_at_cutoff():
+    """Pairs at r == cutoff: excluded for pair potentials (r >= rc), kept by
+    Ewald (r > rc is the test); and half-box separations for the image."""
+    s = lg.System(lg.UnitCell.cubic(20.0))
+    pos = [[0.0, 0.0, 0.0], [9.0, 0.0, 0.0], [0.0, 9.0, 0.0], [10.0, 10.0, 10.0], [3.0, 3.0, 3.0],
+           [3.0, 3.0, 12.0], [-7.0, 3.0, 3.0], [1.5, 0.25, 19.0]]
+    s.add_particles(["Na", "Cl"] * 4, pos, charges=[1.0, -1.0] * 4)
+    for a, b in [("Na", "Na"), ("Na", "Cl"), ("Cl", "Cl")]:
+        s.set_pair_potential((a, b), lg.PairInteraction(lg.LennardJones(2.5, 0.1), 9.0))
+    s.set_coulomb_potential(lg.Ewald(9.0, 4, 0.3))
+    _pairset_equal(s)
+    assert_parity(s, [lg.LG_TERM_ALL])
+
+
+def test_pairset_random_unwrapped_fluid():
+    _pairset_equal(systems.random_lj_fluid(1500, 0.025, 11, 9.5))
+
+
+# ---- molecular dynamics ----------------------------------------------------------------------
+def test_velocity_verlet_trajectory_matches_oracle():
+    s = jitter(workloads.argon_fcc(), 0.2, 4)
+    orc = oracle.Oracle(s)
+    x0, v0 = s.positions.copy(), s.velocities.copy()
+    md = lg.MolecularDynamics(lg.VelocityVerlet(1.0))
+    md.setup(s)
+    md.run(s, 40)
+    xo, vo, _ = orc.velocity_verlet(x0, v0, np.zeros_like(x0), 1.0, 40)
+    assert np.abs(s.positions - xo).max() < 1e-9
+    assert np.abs(s.velocities - vo).max() / np.abs(vo).max() < 1e-8
+
+
+def test_velocity_verlet_ewald_berendsen():
+    s = workloads.nacl_crystal(cells=3, cutoff=8.0, kmax=5)
+    orc = oracle.Oracle(s)
+    x0, v0 = s.positions.copy(), s.velocities.copy()
+    md = lg.MolecularDynamics(lg.VelocityVerlet(1.0), lg.BerendsenThermostat(250.0, 100.0))
+    md.setup(s)
+    md.run(s, 25)
+    xo, vo, _ = orc.velocity_verlet(x0, v0, np.zeros_like(x0), 1.0, 25, 250.0, 100.0)
+    assert np.abs(s.positions - xo).max() < 1e-9
+    assert np.abs(s.velocities - vo).max() / np.abs(vo).max() < 1e-8
+
+
+def test_md_energy_conservation_nve():
+    """NVE drift bound of tests/md-nacl.rs (Ewald 5e-3 relative over the run)."""
+    s = workloads.nacl_crystal(cells=3, cutoff=8.0, kmax=5, temperature=300.0)
+    md = lg.MolecularDynamics(lg.VelocityVerlet(1.0))
+    md.setup(s)
+
+    def total():
+        return s.potential_energy() + s.kinetic_energy()
+
+    e0 = total()
+    for _ in range(10):
+        md.run(s, 50)
+    assert abs((total() - e0) / e0) < 5e-3
+
+
+# ---- errors mirror the reference's panics ------------------------------------------------------
+def test_cutoff_above_half_cell_is_rejected():
+    s = lg.System(lg.UnitCell.cubic(10.0))
+    with pytest.raises(ValueError):
+        s.set_pair_potential(("A", "A"), lg.PairInteraction(lg.LennardJones(1.0, 1.0), 6.0))
+    eng = lg.Engine(1)
+    import ctypes
+    from lumol_gb300 import _capi as C
+    eng.call("lg_set_cell", 0, C.dptr(np.diag([10.0, 10.0, 10.0]).ravel().copy()))
+    table = (C.LgPair * 1)(C.LgPair(C.LG_PAIR_LJ, 0, 0, 0, 1.0, 1.0, 0.0, 6.0, 1.0))
+    with pytest.raises(lg.EngineError):
+        eng.call("lg_set_pairs", 0, 1, table)
+    bad = C.LgCoulomb(C.LG_COULOMB_EWALD, 0, 0, 0, 3.0, 0.3, 1.0)
+    with pytest.raises(lg.EngineError, match="kmax can not be 0"):
+        eng.call("lg_set_coulomb", 0, ctypes.byref(bad))
