@@ -200,7 +200,10 @@ struct lg_engine {
     DBuf<int8_t> spec_path;
     DBuf<int4> bt;
     DBuf<double2> bt_par, eikr, rho;
-    DBuf<float4> wpos;
+    DBuf<float4> wpos, pos_hi, pos_lo;
+    DBuf<PairDevF> ptabf;
+    DBuf<KVecF> kvecf;
+    DBuf<float2> eikrf, rhof;
     DBuf<SysDev> sysdev;
     DBuf<PairDev> ptab;
     DBuf<KVecDev> kvec;
@@ -315,6 +318,7 @@ int commit(lg_engine* e) {
     std::vector<double4_32a> h_posq(n), h_vel(n);
     std::vector<int> h_kind(n), h_mol(n), h_sysid(n);
     std::vector<PairDev> h_ptab;
+    std::vector<PairDevF> h_ptabf;
     std::vector<KVecDev> h_kvec;
     std::vector<std::vector<std::pair<int, int8_t>>> spec(n);
     struct Term {
@@ -389,6 +393,26 @@ int commit(lg_engine* e) {
             q.cutoff2_f = (float)(p.cutoff * p.cutoff);
             if (p.type != LG_PAIR_ABSENT && p.restriction > LG_RESTRICT_INTER) needs_path = true;
             h_ptab.push_back(q);
+            PairDevF qf;
+            std::memset(&qf, 0, sizeof(qf));
+            qf.type = p.type;
+            qf.restriction = p.restriction;
+            if (p.type == LG_PAIR_LJ) {
+                double s6 = std::pow(p.p0, 6.0);
+                qf.a = (float)(4.0 * p.p1 * s6 * s6);
+                qf.b = (float)(4.0 * p.p1 * s6);
+            } else if (p.type == LG_PAIR_BUCKINGHAM) {
+                qf.a = (float)p.p0;
+                qf.b = (float)p.p1;
+                qf.c = (float)(1.0 / p.p2);
+            } else if (p.type == LG_PAIR_HARMONIC) {
+                qf.a = (float)p.p0;
+                qf.b = (float)p.p1;
+            }
+            qf.rc2 = (float)(p.cutoff * p.cutoff);
+            qf.shift = (float)q.shift;
+            qf.scale14 = (float)p.scale14;
+            h_ptabf.push_back(qf);
         }
         if (h.coul.kind != LG_COULOMB_NONE && h.coul.restriction > LG_RESTRICT_INTER) needs_path = true;
         d.needs_path = needs_path;
@@ -399,6 +423,7 @@ int commit(lg_engine* e) {
             d.invL[k] = 1.0 / h.L[k];
             d.Lf[k] = (float)h.L[k];
             d.invLf[k] = (float)(1.0 / h.L[k]);
+            d.Llo[k] = (float)(h.L[k] - (double)d.Lf[k]);
         }
         double rc = max_cutoff(h);
         d.rlist = rc + e->skin;
@@ -555,6 +580,19 @@ int commit(lg_engine* e) {
         int nk_s = e->h_sysdev[s].kend - e->h_sysdev[s].kbegin;
         nkchunks = std::max(nkchunks, (nk_s + kchunk - 1) / kchunk);
     }
+    bool mixed = e->opt.precision == LG_PRECISION_MIXED;
+    std::vector<KVecF> h_kvecf(nkv);
+    for (int k = 0; k < nkv; k++) {
+        const KVecDev& v = h_kvec[k];
+        h_kvecf[k] = KVecF{v.ikx, v.iky, v.ikz, v.sys, (float)v.field[0], (float)v.field[1], (float)v.field[2],
+                           (float)v.energy};
+    }
+    CUDA_TRY(e, e->ptabf.alloc(h_ptabf.size()));
+    CUDA_TRY(e, e->pos_hi.alloc(mixed ? n : 1));
+    CUDA_TRY(e, e->pos_lo.alloc(mixed ? n : 1));
+    CUDA_TRY(e, e->kvecf.alloc(nkv));
+    CUDA_TRY(e, e->eikrf.alloc(mixed && nkv ? (size_t)kdim * 3 * n : 1));
+    CUDA_TRY(e, e->rhof.alloc(nkv));
     CUDA_TRY(e, e->kvec.alloc(nkv));
     CUDA_TRY(e, e->eikr.alloc(nkv ? (size_t)kdim * 3 * n : 1));
     CUDA_TRY(e, e->rho.alloc(nkv));
@@ -588,6 +626,10 @@ int commit(lg_engine* e) {
     CUDA_TRY(e, cudaMemsetAsync(e->nnb.p, 0, n * sizeof(int), st));
     CUDA_TRY(e, cudaMemcpyAsync(e->sysdev.p, e->h_sysdev.data(), nsys * sizeof(SysDev), cudaMemcpyHostToDevice, st));
     CUDA_TRY(e, cudaMemcpyAsync(e->ptab.p, h_ptab.data(), h_ptab.size() * sizeof(PairDev), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(e, cudaMemcpyAsync(e->ptabf.p, h_ptabf.data(), h_ptabf.size() * sizeof(PairDevF), cudaMemcpyHostToDevice,
+                                st));
+    if (nkv)
+        CUDA_TRY(e, cudaMemcpyAsync(e->kvecf.p, h_kvecf.data(), nkv * sizeof(KVecF), cudaMemcpyHostToDevice, st));
     if (nkv)
         CUDA_TRY(e, cudaMemcpyAsync(e->kvec.p, h_kvec.data(), nkv * sizeof(KVecDev), cudaMemcpyHostToDevice, st));
     CUDA_TRY(e, cudaMemcpyAsync(e->host_const.p, h_const.data(), h_const.size() * sizeof(double),
@@ -645,6 +687,13 @@ int commit(lg_engine* e) {
     b.host_const = e->host_const.p;
     b.lambda = e->lambda.p;
     b.ke = e->ke.p;
+    b.tpa = mixed ? 8 : 32;
+    b.pos_hi = mixed ? e->pos_hi.p : nullptr;
+    b.pos_lo = mixed ? e->pos_lo.p : nullptr;
+    b.ptabf = e->ptabf.p;
+    b.kvecf = e->kvecf.p;
+    b.eikrf = e->eikrf.p;
+    b.rhof = e->rhof.p;
     e->dirty = false;
     return LG_OK;
 }
@@ -683,6 +732,10 @@ int clear_status_bits(lg_engine* e, uint32_t bits) {
 void enqueue_forces(lg_engine* e, uint32_t terms, bool ev, cudaStream_t st) {
     const Batch& b = e->b;
     if (b.n == 0) return;
+    if (b.precision == LG_PRECISION_MIXED) {
+        launch_split_positions(b, st);
+        e->launches += 1;
+    }
     launch_nlist_build(b, st);
     e->launches += 6;
     if (terms & (LG_TERM_PAIRS | LG_TERM_COUL_REAL)) {
