@@ -237,6 +237,28 @@ int lg_launch_count(lg_engine* e, uint64_t* count);
  * device, in TFLOP/s (2 flops per FMA). */
 int lg_fma_peak(int32_t fp64, double* tflops);
 
+/* ---- Ewald k-space without device allocation ----------------------------------- */
+/* No counterpart in the reference.  For callers that cannot call cudaMalloc --
+ * code running inside a host framework whose device memory belongs to its own
+ * pool allocator, and per-step or per-move loops where cudaMalloc / cudaFree
+ * would synchronise the device -- this computes what
+ * lg_compute(LG_TERM_COUL_KSPACE) computes for one orthorhombic system, on
+ * device pointers the caller owns, and allocates nothing: its scratch is one
+ * fixed __device__ array of about 2 MB that every GPU loading the library holds
+ * until exit.  Limits: n <= LG_NOALLOC_MAX_ATOMS, 1 <= kmax <= LG_NOALLOC_MAX_KMAX;
+ * larger sizes are rejected with LG_ERR_ARGUMENT (message in lg_last_error(NULL)).
+ * d_positions: 3n, d_charges: n; d_forces (3n) is ACCUMULATED into; d_energy (1)
+ * and d_virial (9) are written (either may be NULL).  `stream` is a
+ * cudaStream_t (NULL: the default stream).  Calls share the scratch array:
+ * calls whose work overlaps on the GPU race.  The first call on a device sets
+ * the scratch address up for that device and should come before any stream
+ * capture. */
+#define LG_NOALLOC_MAX_ATOMS 4096
+#define LG_NOALLOC_MAX_KMAX 8
+int lg_ewald_kspace_noalloc(const double* d_positions, const double* d_charges, int64_t n,
+                            const double cell_lengths[3], double alpha, int32_t kmax,
+                            double* d_forces, double* d_energy, double* d_virial, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -102,6 +102,8 @@ SIGNATURES = {
     "lg_kernel_times": (ctypes.c_int, [_P, ctypes.c_int32, _D]),
     "lg_launch_count": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64)]),
     "lg_fma_peak": (ctypes.c_int, [ctypes.c_int32, _D]),
+    "lg_ewald_kspace_noalloc": (ctypes.c_int, [_P, _P, ctypes.c_int64, _D, ctypes.c_double, ctypes.c_int32,
+                                               _P, _P, _P, _P]),
 }
 
 LG_KT_NAMES = ["nlist", "pair", "bonded", "eikr", "rho", "field", "vv", "step"]

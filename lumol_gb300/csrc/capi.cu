@@ -181,6 +181,10 @@ void ewald_factors(const double L[3], double alpha, int kmax, int sys, std::vect
 
 }  // namespace
 
+namespace lg {
+void set_global_error(const std::string& msg) { g_create_error = msg; }
+}  // namespace lg
+
 struct lg_engine {
     lg_options opt{};
     int nsys = 0;

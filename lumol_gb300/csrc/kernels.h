@@ -2,6 +2,8 @@
 // launch functions of every kernel.
 #pragma once
 
+#include <string>
+
 #include "device_common.cuh"
 
 namespace lg {
@@ -96,5 +98,7 @@ void launch_check_displacement(const Batch& b, cudaStream_t st);
 
 // diag.cu
 int measure_fma_peak(int fp64, double* tflops);
+// capi.cu: the message lg_last_error(NULL) returns
+void set_global_error(const std::string& msg);
 
 }  // namespace lg
