@@ -7,8 +7,9 @@
 A step is one Velocity-Verlet MD step (integrate: half kick, drift, forces,
 half kick) of the workload, with the state resident on the GPU.  `value` is
 atom-steps/s of the whole job (all ranks), timed with CUDA events on the
-engine's stream; the L2 cache is flushed (256 MiB write) before every timed
-step because the workloads fit in L2.  `e2e` is the same metric through the
+engine's stream, one timed iteration being one lg_md_run call of `--chunk`
+MD steps (the engine's own chunk length); the L2 cache is flushed (256 MiB
+write) before every timed iteration because the workloads fit in L2.  `e2e` is the same metric through the
 public C ABI call Lumol's Integrator would make (lg_md_integrate), with the
 positions and velocities copied from pinned host memory and back every step.
 
@@ -45,22 +46,30 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--workload", default="nacl_ewald", choices=["nacl_ewald", "argon", "water"])
     p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    p.add_argument("--cells", type=int, default=0, help="lattice cells per side (0: the workload's size)")
+    p.add_argument("--chunk", type=int, default=16, help="MD steps per timed iteration (one lg_md_run call)")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-roofline", action="store_true")
     return p.parse_args()
 
 
-def make_system(name: str, precision: str):
+def make_system(name: str, precision: str, cells: int = 0):
     from lumol_gb300 import workloads
     if name == "nacl_ewald":
-        return workloads.nacl_crystal(precision=precision), 1.0, (
-            "NaCl rock salt 5x5x5 (1000 ions, L=28.2 A), LJ rc=9 A, Ewald rc=9 A alpha=0.35 kmax=7, "
-            "NVE Velocity-Verlet dt=1 fs")
+        c = cells or 5
+        s = workloads.nacl_crystal(cells=c, precision=precision)
+        return s, 1.0, (f"NaCl rock salt {c}x{c}x{c} ({s.size} ions, L={5.64 * c:.1f} A), LJ rc=9 A, "
+                        "Ewald rc=9 A alpha=0.35 kmax=7, NVE Velocity-Verlet dt=1 fs")
     if name == "argon":
-        return workloads.argon_fcc(precision=precision), 1.0, (
-            "Argon FCC 5x5x5 (500 atoms, L=28.8 A), shifted LJ rc=10 A, NVE Velocity-Verlet dt=1 fs")
-    return workloads.water_box(precision=precision), 0.5, (
-        "SPC/E-geometry flexible water 12^3 (5184 atoms, L=37.3 A), Ewald alpha=0.3 kmax=8 rc=10 A, "
-        "harmonic bonds/angles, Velocity-Verlet dt=0.5 fs")
+        c = cells or 5
+        s = workloads.argon_fcc(cells=c, precision=precision)
+        return s, 1.0, (f"Argon FCC {c}x{c}x{c} ({s.size} atoms, L={5.76 * c:.1f} A), shifted LJ rc=10 A, "
+                        "NVE Velocity-Verlet dt=1 fs")
+    c = cells or 12
+    s = workloads.water_box(n_side=c, length=37.3 * c / 12, precision=precision)
+    return s, 0.5, (f"SPC/E-geometry flexible water {c}^3 ({s.size} atoms, L={37.3 * c / 12:.1f} A), Ewald "
+                    "alpha=0.3 kmax=8 rc=10 A, harmonic bonds/angles, Velocity-Verlet dt=0.5 fs")
 
 
 def dist_setup():
@@ -223,7 +232,7 @@ def run_reference(args, world, rank):
     import numpy as np
     import oracle
     oracle.build()
-    system, dt, desc = make_system(args.workload, "fp64")
+    system, dt, desc = make_system(args.workload, "fp64", args.cells)
     orc = oracle.Oracle(system)
     threads = oracle.num_threads()
     x, v = system.positions.copy(), system.velocities.copy()
@@ -268,7 +277,7 @@ def main():
     from lumol_gb300 import _capi as C
 
     torch.cuda.set_device(local)
-    system, dt, desc = make_system(args.workload, args.precision)
+    system, dt, desc = make_system(args.workload, args.precision, args.cells)
     md = lg.MolecularDynamics(lg.VelocityVerlet(dt))
     md.setup(system)
     eng = system.engine()
@@ -277,23 +286,30 @@ def main():
     stream = torch.cuda.ExternalStream(stream_ptr.value)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
 
+    chunk = max(1, min(args.chunk, args.steps))
+    iters = (args.steps + chunk - 1) // chunk
     for _ in range(max(args.warmup, 3)):
-        eng.call("lg_md_run", 1)
+        eng.call("lg_md_run", chunk)
+    if args.steps % chunk:
+        eng.call("lg_md_run", args.steps % chunk)  # instantiate the remainder's graph outside the timing
     torch.cuda.synchronize()
 
     n0 = ctypes.c_uint64()
     eng.call("lg_launch_count", ctypes.byref(n0))
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(iters)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(iters)]
     barrier(world)
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
-    for k in range(args.steps):
+    done = 0
+    for k in range(iters):
+        steps_k = min(chunk, args.steps - done)
         flush.zero_()
         torch.cuda.synchronize()
         starts[k].record(stream)
-        eng.call("lg_md_run", 1)
+        eng.call("lg_md_run", steps_k)
         ends[k].record(stream)
+        done += steps_k
     torch.cuda.synchronize()
     barrier(world)
     clk = clocks.stop()
@@ -305,38 +321,12 @@ def main():
     value = atoms_total * args.steps / (ms_max * 1e-3)
 
     # end to end through the public call, pinned host buffers
-    pos = torch.empty((system.size, 3), dtype=torch.float64, pin_memory=True)
-    vel = torch.empty((system.size, 3), dtype=torch.float64, pin_memory=True)
-    eng.call("lg_md_get_state", 0, C.dptr(pos.numpy()), C.dptr(vel.numpy()))
-    for _ in range(3):
-        eng.call("lg_md_integrate", C.dptr(pos.numpy()), C.dptr(vel.numpy()), 1)
-    torch.cuda.synchronize()
-    barrier(world)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        eng.call("lg_md_integrate", C.dptr(pos.numpy()), C.dptr(vel.numpy()), 1)
-    torch.cuda.synchronize()
-    e2e_s = max_over_ranks(world, time.perf_counter() - t0)
-    e2e_value = atoms_total * args.steps / e2e_s
+    e2e = None
     bytes_state = 2 * 3 * 8 * system.size
+    if not args.no_e2e:
+        e2e = run_e2e(args, world, eng, C, torch, system, atoms_total, bytes_state)
 
-    # roofline of the dominant kernel, timed live with CUDA events
-    kt = (ctypes.c_double * C.LG_KT_COUNT)() if hasattr(C, "LG_KT_COUNT") else (ctypes.c_double * 8)()
-    eng.call("lg_kernel_times", 20, kt)
-    times = {name: kt[i] for i, name in enumerate(C.LG_KT_NAMES)}
-    work = algorithmic_work(system)
-    fp64_peak = ctypes.c_double()
-    C.check(lg_lib_fma(C, 1, fp64_peak))
-    candidates = {"pair": work["pair_flops"], "field": work["field_flops"], "rho": work["rho_flops"]}
-    dominant = max(candidates, key=lambda k: times.get(k, 0.0))
-    achieved = candidates[dominant] / (times[dominant] * 1e-3) / 1e12
-    kernel_names = {"pair": "pair_fp64_kernel", "field": "field_kernel", "rho": "rho_kernel"}
-    roofline = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak.value, "unit": "TFLOP/s",
-                "frac": achieved / fp64_peak.value, "traffic": traffic_from_profiles(kernel_names[dominant]),
-                "kernel": kernel_names[dominant], "kernel_ms": times[dominant],
-                "peak_source": "FP64 DFMA throughput measured live by lg_fma_peak (no FP64 figure in "
-                               "MEASURED_PEAKS.json; this path does not use tensor cores)",
-                "kernel_ms_by_group": times, "work": work}
+    roofline = None if args.no_roofline else measure_roofline(args, eng, C, system)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -350,11 +340,11 @@ def main():
             "data": "synthetic (seeded lattice + Maxwell-Boltzmann velocities)",
             "config": {"workload": desc, "atoms": system.size, "precision": args.precision,
                        "parallelism": f"replicas x{world}" if world > 1 else "single system",
-                       "l2": "flushed before every timed step (256 MiB write)"},
+                       "timed_iteration": f"lg_md_run of {chunk} MD steps",
+                       "l2": "flushed before every timed iteration (256 MiB write)"},
             "roofline": roofline,
             "cpu_baseline": cpu,
-            "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": bytes_state,
-                    "d2h_bytes_per_step": bytes_state},
+            "e2e": e2e,
             "gpu_launches": int(n1.value - n0.value),
             "clocks": clk,
         }
@@ -364,9 +354,52 @@ def main():
         dist.destroy_process_group()
 
 
-def lg_lib_fma(C, fp64, out):
+def run_e2e(args, world, eng, C, torch, system, atoms_total, bytes_state):
+    """The same metric through lg_md_integrate (Integrator::integrate), one MD
+    step per call, positions and velocities copied from pinned host memory and
+    back every step; host wall clock."""
+    pos = torch.empty((system.size, 3), dtype=torch.float64, pin_memory=True)
+    vel = torch.empty((system.size, 3), dtype=torch.float64, pin_memory=True)
+    eng.call("lg_md_get_state", 0, C.dptr(pos.numpy()), C.dptr(vel.numpy()))
+    for _ in range(3):
+        eng.call("lg_md_integrate", C.dptr(pos.numpy()), C.dptr(vel.numpy()), 1)
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        eng.call("lg_md_integrate", C.dptr(pos.numpy()), C.dptr(vel.numpy()), 1)
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(world, time.perf_counter() - t0)
+    return {"value": atoms_total * args.steps / e2e_s, "unit": METRIC, "h2d_bytes_per_step": bytes_state,
+            "d2h_bytes_per_step": bytes_state}
+
+
+def measure_roofline(args, eng, C, system):
+    """Dominant force kernel: algorithmic FLOP/s (per-unit work x units per
+    launch / CUDA-event time of one launch) against the measured FMA peak of
+    the pipe it runs on (FP64 for the plain path, FP32 for the mixed one)."""
     import ctypes
-    return C.load().lg_fma_peak(fp64, ctypes.byref(out))
+    kt = (ctypes.c_double * 8)()
+    eng.call("lg_kernel_times", 20, kt)
+    times = {name: kt[i] for i, name in enumerate(C.LG_KT_NAMES)}
+    work = algorithmic_work(system)
+    fp64 = args.precision == "fp64"
+    peak = ctypes.c_double()
+    C.check(C.load().lg_fma_peak(1 if fp64 else 0, ctypes.byref(peak)))
+    candidates = {"pair": work["pair_flops"], "field": work["field_flops"], "rho": work["rho_flops"]}
+    dominant = max(candidates, key=lambda k: times.get(k, 0.0))
+    achieved = candidates[dominant] / (times[dominant] * 1e-3) / 1e12
+    names = {"pair": "pair_fp64_kernel" if fp64 else "pair_mixed_kernel",
+             "field": "field_kernel" if fp64 else "field_mixed_kernel",
+             "rho": "rho_kernel" if fp64 else "rho_mixed_kernel"}
+    pipe = "FP64" if fp64 else "FP32"
+    return {"bound": "fp64" if fp64 else "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
+            "frac": achieved / peak.value, "traffic": traffic_from_profiles(names[dominant]),
+            "kernel": names[dominant], "kernel_ms": times[dominant],
+            "peak_source": f"{pipe} FMA throughput measured live by lg_fma_peak (MEASURED_PEAKS.json has no "
+                           f"{pipe} figure; this path does not use tensor cores)",
+            "kernel_ms_by_group": times, "work": work}
+
 
 
 if __name__ == "__main__":

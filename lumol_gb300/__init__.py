@@ -16,10 +16,12 @@ from .system import (
     Harmonic,
     LennardJones,
     MolecularDynamics,
+    MonteCarlo,
     NullPotential,
     PairInteraction,
     PairRestriction,
     System,
+    Translate,
     UnitCell,
     VelocityVerlet,
     Wolf,
@@ -37,7 +39,7 @@ from ._capi import (
 
 __all__ = [
     "units", "EngineError", "BerendsenThermostat", "Buckingham", "Engine", "Ewald", "Harmonic",
-    "LennardJones", "MolecularDynamics", "NullPotential", "PairInteraction", "PairRestriction",
+    "LennardJones", "MolecularDynamics", "MonteCarlo", "Translate", "NullPotential", "PairInteraction", "PairRestriction",
     "System", "UnitCell", "VelocityVerlet", "Wolf",
     "LG_TERM_ALL", "LG_TERM_ANGLES", "LG_TERM_BONDS", "LG_TERM_COUL_KSPACE", "LG_TERM_COUL_REAL",
     "LG_TERM_COUL_SELF", "LG_TERM_PAIRS", "LG_TERM_TAIL",

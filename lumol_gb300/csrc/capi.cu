@@ -12,7 +12,11 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstddef>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -24,6 +28,12 @@ using namespace lg;
 namespace {
 
 thread_local std::string g_create_error;
+constexpr int MIN_KCHUNK = 8;
+
+// Tuned launch parameters per workload shape: (device, precision, atoms,
+// list capacity, k-vectors) -> (threads per atom, k-vectors per field chunk).
+std::mutex g_tune_mutex;
+std::map<std::tuple<int, int, int, int, int>, std::pair<int, int>> g_tune_cache;
 
 template <class T>
 struct DBuf {
@@ -61,6 +71,7 @@ struct HostSystem {
     double dt = 0.0, T0 = 0.0, tau = 0.0;
     bool md_ready = false;
     // derived
+    std::vector<int64_t> mol_begin;  // first atom of each molecule (local index), plus the end
     double tail_energy = 0.0, tail_virial = 0.0, ewald_self = 0.0;
     double alpha = 0.0;
 };
@@ -219,17 +230,19 @@ struct lg_engine {
     std::vector<SysDev> h_sysdev;
     std::vector<int> h_kvec_sys;
 
+    bool tuned = false;
+    int max_nk = 0;
     // kernels launched so far (graph replays counted by their kernel nodes)
     uint64_t launches = 0;
     size_t graph_kernels = 0;
 
-    // MD graph
-    cudaGraphExec_t graph = nullptr;
-    int graph_steps = 0;
+    // MD graphs, one per chunk length
+    std::map<int, cudaGraphExec_t> graphs;
+    std::map<int, size_t> graph_nodes;
     bool graph_thermo = false;
 
     // MC (single molecule moves)
-    DBuf<double> mc_newpos;
+    DBuf<double> mc_newpos, mc_partial, mc_dk, mc_out;
     DBuf<double2> mc_eikr, mc_drho;
     double mc_energy = 0.0;
     double mc_pending_cost = 0.0;
@@ -237,8 +250,14 @@ struct lg_engine {
     int mc_sys = -1;
     int64_t mc_mol_begin = 0, mc_mol_size = 0;
 
+    void drop_graphs() {
+        for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+        graphs.clear();
+        graph_nodes.clear();
+    }
+
     ~lg_engine() {
-        if (graph) cudaGraphExecDestroy(graph);
+        drop_graphs();
         if (h_status) cudaFreeHost(h_status);
         if (h_out) cudaFreeHost(h_out);
         if (stream) cudaStreamDestroy(stream);
@@ -264,10 +283,7 @@ bool valid_sys(lg_engine* e, int32_t s) { return e && s >= 0 && s < e->nsys; }
 
 void invalidate(lg_engine* e) {
     e->dirty = true;
-    if (e->graph) {
-        cudaGraphExecDestroy(e->graph);
-        e->graph = nullptr;
-    }
+    e->drop_graphs();
 }
 
 double max_cutoff(const HostSystem& h) {
@@ -353,6 +369,8 @@ int commit(lg_engine* e) {
             max_mol = std::max(max_mol, h.mols[i]);
         }
         mol_base += max_mol + 1;
+        h.mol_begin.assign(max_mol + 2, h.n);
+        for (int64_t i = h.n - 1; i >= 0; i--) h.mol_begin[h.mols[i]] = i;
         bond_paths(h, base, spec);
         for (size_t b = 0; b * 2 < h.bonds.size(); b++) {
             const lg_bonded& p = h.bond_pots[b];
@@ -579,11 +597,12 @@ int commit(lg_engine* e) {
     CUDA_TRY(e, e->status.alloc(1));
     int nkv = (int)h_kvec.size();
     int kchunk = 32;
-    int nkchunks = 0;
-    for (int s = 0; s < nsys; s++) {
-        int nk_s = e->h_sysdev[s].kend - e->h_sysdev[s].kbegin;
-        nkchunks = std::max(nkchunks, (nk_s + kchunk - 1) / kchunk);
-    }
+    int nkchunks = 0, max_chunks = 0;
+    int max_nk = 0;
+    for (int s = 0; s < nsys; s++) max_nk = std::max(max_nk, e->h_sysdev[s].kend - e->h_sysdev[s].kbegin);
+    nkchunks = (max_nk + kchunk - 1) / kchunk;
+    max_chunks = (max_nk + MIN_KCHUNK - 1) / MIN_KCHUNK;  // room for the smallest chunk the tuner tries
+    e->max_nk = max_nk;
     bool mixed = e->opt.precision == LG_PRECISION_MIXED;
     std::vector<KVecF> h_kvecf(nkv);
     for (int k = 0; k < nkv; k++) {
@@ -601,7 +620,7 @@ int commit(lg_engine* e) {
     CUDA_TRY(e, e->eikr.alloc(nkv ? (size_t)kdim * 3 * n : 1));
     CUDA_TRY(e, e->rho.alloc(nkv));
     CUDA_TRY(e, e->kred.alloc((size_t)nkv * 7));
-    CUDA_TRY(e, e->fpart.alloc(nkv ? (size_t)nkchunks * 3 * n : 1));
+    CUDA_TRY(e, e->fpart.alloc(nkv ? (size_t)max_chunks * 3 * n : 1));
 
     cudaStream_t st = e->stream;
     CUDA_TRY(e, cudaMemcpyAsync(e->posq.p, h_posq.data(), n * sizeof(double4_32a), cudaMemcpyHostToDevice, st));
@@ -699,6 +718,7 @@ int commit(lg_engine* e) {
     b.eikrf = e->eikrf.p;
     b.rhof = e->rhof.p;
     e->dirty = false;
+    e->tuned = false;
     return LG_OK;
 }
 
@@ -711,10 +731,7 @@ int regrow(lg_engine* e) {
     e->b.nbr = e->nbr.p;
     uint32_t st_init = ST_REBUILD;
     CUDA_TRY(e, cudaMemcpyAsync(e->status.p, &st_init, sizeof(uint32_t), cudaMemcpyHostToDevice, e->stream));
-    if (e->graph) {
-        cudaGraphExecDestroy(e->graph);
-        e->graph = nullptr;
-    }
+    e->drop_graphs();
     return LG_OK;
 }
 
@@ -1108,10 +1125,7 @@ int lg_md_setup(lg_engine* e, int32_t s, double dt, double T0, double tau) {
         // VelocityVerlet::setup: accelerations := 0 (integrators.rs:40-42)
         CUDA_TRY(e, cudaMemsetAsync(e->acc.p + e->begin[s], 0, h.n * sizeof(double4_32a), e->stream));
         CUDA_TRY(e, cudaStreamSynchronize(e->stream));
-        if (e->graph) {
-            cudaGraphExecDestroy(e->graph);
-            e->graph = nullptr;
-        }
+        e->drop_graphs();
     }
     return LG_OK;
 }
@@ -1167,6 +1181,89 @@ int lg_md_get_state(lg_engine* e, int32_t s, double* positions, double* velociti
 
 namespace {
 
+// The autotuner: times the pair kernel at every threads-per-atom width and the
+// Ewald field kernel at several chunk lengths on the current batch and list,
+// keeps the fastest, and caches the choice for this workload shape.
+int autotune(lg_engine* e) {
+    if (e->tuned || e->b.n == 0) return LG_OK;
+    Batch& b = e->b;
+    auto key = std::make_tuple(e->opt.device, b.precision, b.n, b.maxnb, b.nkvec);
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            b.tpa = it->second.first;
+            b.kchunk = it->second.second;
+            b.nkchunks = (e->max_nk + b.kchunk - 1) / b.kchunk;
+            e->tuned = true;
+            return LG_OK;
+        }
+    }
+    cudaStream_t st = e->stream;
+    cudaEvent_t e0, e1;
+    CUDA_TRY(e, cudaEventCreate(&e0));
+    CUDA_TRY(e, cudaEventCreate(&e1));
+    // a current list for the timing
+    launch_check_displacement(b, st);
+    if (b.precision == LG_PRECISION_MIXED) launch_split_positions(b, st);
+    launch_nlist_build(b, st);
+    auto time_it = [&](auto&& launch) -> float {
+        launch();  // warm
+        float best = 1e30f;
+        for (int r = 0; r < 3; r++) {
+            cudaEventRecord(e0, st);
+            launch();
+            cudaEventRecord(e1, st);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            best = std::min(best, ms);
+        }
+        return best;
+    };
+    const int tpas[6] = {1, 2, 4, 8, 16, 32};
+    int best_tpa = b.tpa;
+    float best_t = 1e30f;
+    for (int t : tpas) {
+        b.tpa = t;
+        float ms = time_it([&] { launch_pair_forces(b, LG_TERM_ALL, false, st); });
+        if (ms < best_t) {
+            best_t = ms;
+            best_tpa = t;
+        }
+    }
+    b.tpa = best_tpa;
+    if (b.nkvec) {
+        launch_kspace_part(b, 0, false, st);
+        launch_kspace_part(b, 1, false, st);
+        const int chunks[4] = {MIN_KCHUNK, 16, 32, 64};
+        int best_c = b.kchunk;
+        best_t = 1e30f;
+        for (int kc : chunks) {
+            b.kchunk = kc;
+            b.nkchunks = (e->max_nk + kc - 1) / kc;
+            float ms = time_it([&] { launch_kspace_part(b, 2, false, st); });
+            if (ms < best_t) {
+                best_t = ms;
+                best_c = kc;
+            }
+        }
+        b.kchunk = best_c;
+        b.nkchunks = (e->max_nk + best_c - 1) / best_c;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    CUDA_TRY(e, cudaGetLastError());
+    CUDA_TRY(e, cudaStreamSynchronize(st));
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        g_tune_cache[key] = {b.tpa, b.kchunk};
+    }
+    e->tuned = true;
+    e->drop_graphs();
+    return LG_OK;
+}
+
 void enqueue_md_step(lg_engine* e, bool thermo, cudaStream_t st) {
     launch_vv_first(e->b, st);
     enqueue_forces(e, LG_TERM_ALL, false, st);
@@ -1176,10 +1273,7 @@ void enqueue_md_step(lg_engine* e, bool thermo, cudaStream_t st) {
 }
 
 int build_md_graph(lg_engine* e, int steps, bool thermo) {
-    if (e->graph) {
-        cudaGraphExecDestroy(e->graph);
-        e->graph = nullptr;
-    }
+    if (e->graph_thermo != thermo) e->drop_graphs();
     cudaGraph_t g;
     uint64_t before = e->launches;
     CUDA_TRY(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
@@ -1188,11 +1282,12 @@ int build_md_graph(lg_engine* e, int steps, bool thermo) {
     CUDA_TRY(e, cudaStreamEndCapture(e->stream, &g));
     size_t nodes = 0;
     cudaGraphGetNodes(g, nullptr, &nodes);
-    e->graph_kernels = nodes;
-    cudaError_t ce = cudaGraphInstantiate(&e->graph, g, 0);
+    cudaGraphExec_t exec = nullptr;
+    cudaError_t ce = cudaGraphInstantiate(&exec, g, 0);
     cudaGraphDestroy(g);
     if (ce != cudaSuccess) return fail(e, LG_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ce));
-    e->graph_steps = steps;
+    e->graphs[steps] = exec;
+    e->graph_nodes[steps] = nodes;
     e->graph_thermo = thermo;
     return LG_OK;
 }
@@ -1214,6 +1309,10 @@ int lg_md_run(lg_engine* e, int64_t nsteps) {
     cudaStream_t st = e->stream;
     int64_t done = 0;
     int retries = 0;
+    if (!e->tuned) {
+        int rc = autotune(e);
+        if (rc) return rc;
+    }
     // checkpoint buffers: a chunk whose list overflowed is replayed after regrowing
     DBuf<double4_32a> cp_pos, cp_vel, cp_acc;
     CUDA_TRY(e, cp_pos.alloc(e->b.n));
@@ -1221,7 +1320,7 @@ int lg_md_run(lg_engine* e, int64_t nsteps) {
     CUDA_TRY(e, cp_acc.alloc(e->b.n));
     while (done < nsteps) {
         int steps = (int)std::min<int64_t>(chunk, nsteps - done);
-        if (!e->graph || e->graph_steps != steps || e->graph_thermo != thermo) {
+        if (e->graph_thermo != thermo || !e->graphs.count(steps)) {
             int rc = build_md_graph(e, steps, thermo);
             if (rc) return rc;
         }
@@ -1229,8 +1328,8 @@ int lg_md_run(lg_engine* e, int64_t nsteps) {
         CUDA_TRY(e, cudaMemcpyAsync(cp_pos.p, e->posq.p, bytes, cudaMemcpyDeviceToDevice, st));
         CUDA_TRY(e, cudaMemcpyAsync(cp_vel.p, e->vel.p, bytes, cudaMemcpyDeviceToDevice, st));
         CUDA_TRY(e, cudaMemcpyAsync(cp_acc.p, e->acc.p, bytes, cudaMemcpyDeviceToDevice, st));
-        CUDA_TRY(e, cudaGraphLaunch(e->graph, st));
-        e->launches += e->graph_kernels;
+        CUDA_TRY(e, cudaGraphLaunch(e->graphs[steps], st));
+        e->launches += e->graph_nodes[steps];
         uint32_t status;
         int rc = read_status(e, &status);
         if (rc) return rc;
@@ -1342,16 +1441,96 @@ int lg_kernel_times(lg_engine* e, int32_t reps, double* ms) {
 
 // ---- Monte Carlo ---------------------------------------------------------------
 int lg_mc_init(lg_engine* e, int32_t s, const double* positions, double* energy) {
-    (void)e; (void)s; (void)positions; (void)energy;
-    return fail(e, LG_ERR_STATE, "Monte Carlo entry points are not available in this build");
+    if (!valid_sys(e, s) || !positions) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    int rc = commit(e);
+    if (rc) return rc;
+    const HostSystem& h = e->sys[s];
+    int64_t base = e->begin[s];
+    cudaStream_t st = e->stream;
+    if (h.n) {
+        CUDA_TRY(e, cudaMemcpyAsync(e->pos3.p + 3 * base, positions, 3 * h.n * sizeof(double),
+                                    cudaMemcpyHostToDevice, st));
+        Batch sub = e->b;
+        sub.n = (int)h.n;
+        sub.posq = e->posq.p + base;
+        launch_pack_positions(sub, e->pos3.p + 3 * base, st);
+    }
+    rc = compute_batch(e, LG_TERM_ALL, LG_WANT_ENERGY, nullptr, nullptr);
+    if (rc) return rc;
+    // FP64 e^{ik.r} and rho(k) at these positions: the state the move costs update
+    Batch fb = e->b;
+    fb.precision = LG_PRECISION_FP64;
+    launch_kspace_part(fb, 0, false, st);
+    launch_kspace_part(fb, 1, false, st);
+    CUDA_TRY(e, cudaMemcpyAsync(e->h_out, e->out.p + (size_t)s * RED_STRIDE, sizeof(double), cudaMemcpyDeviceToHost,
+                                st));
+    CUDA_TRY(e, cudaStreamSynchronize(st));
+    CUDA_TRY(e, cudaGetLastError());
+    e->mc_energy = e->h_out[0];
+    e->mc_sys = s;
+    e->mc_pending = false;
+    if (energy) *energy = e->mc_energy;
+    return LG_OK;
 }
+
 int lg_mc_move_molecule_cost(lg_engine* e, int32_t s, int64_t molecule, const double* new_positions, double* cost) {
-    (void)s; (void)molecule; (void)new_positions; (void)cost;
-    return fail(e, LG_ERR_STATE, "Monte Carlo entry points are not available in this build");
+    if (!valid_sys(e, s) || !new_positions || !cost) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    if (e->dirty || e->mc_sys != s) return fail(e, LG_ERR_STATE, "lg_mc_init was not called for this system");
+    const HostSystem& h = e->sys[s];
+    if (molecule < 0 || molecule + 1 >= (int64_t)h.mol_begin.size())
+        return fail(e, LG_ERR_ARGUMENT, "molecule index out of range");
+    CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    int64_t mb = h.mol_begin[molecule], me = h.mol_begin[molecule + 1];
+    int msize = (int)(me - mb);
+    const SysDev& sd = e->h_sysdev[s];
+    cudaStream_t st = e->stream;
+    size_t need_pos = (size_t)std::max(msize, 1) * 3;
+    if (e->mc_newpos.n < need_pos) CUDA_TRY(e, e->mc_newpos.alloc(need_pos));
+    int nblocks = (int)((h.n + 255) / 256);
+    if (e->mc_partial.n < (size_t)std::max(2 * nblocks, 2)) CUDA_TRY(e, e->mc_partial.alloc(std::max(2 * nblocks, 2)));
+    int nk = sd.coul == LG_COULOMB_EWALD ? sd.kend - sd.kbegin : 0;
+    if (e->mc_dk.n < (size_t)std::max(nk, 1)) CUDA_TRY(e, e->mc_dk.alloc(std::max(nk, 1)));
+    if (e->mc_drho.n < (size_t)std::max(nk, 1)) CUDA_TRY(e, e->mc_drho.alloc(std::max(nk, 1)));
+    size_t need_eikr = (size_t)(sd.kmax + 1) * 3 * std::max(msize, 1);
+    if (e->mc_eikr.n < need_eikr) CUDA_TRY(e, e->mc_eikr.alloc(need_eikr));
+    if (e->mc_out.n < 3) CUDA_TRY(e, e->mc_out.alloc(3));
+    CUDA_TRY(e, cudaMemcpyAsync(e->mc_newpos.p, new_positions, 3 * msize * sizeof(double), cudaMemcpyHostToDevice,
+                                st));
+    launch_mc_cost(e->b, s, sd, (int)(e->begin[s] + mb), msize, e->mc_newpos.p, e->mc_eikr.p, e->mc_drho.p,
+                   e->mc_partial.p, e->mc_dk.p, e->mc_out.p, st);
+    e->launches += 2 + (nk > 0 ? 2 : 0);
+    double out[3];
+    CUDA_TRY(e, cudaMemcpyAsync(out, e->mc_out.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(e, cudaStreamSynchronize(st));
+    CUDA_TRY(e, cudaGetLastError());
+    e->mc_pending_cost = out[0] + out[1] + out[2];
+    e->mc_pending = true;
+    e->mc_mol_begin = e->begin[s] + mb;
+    e->mc_mol_size = msize;
+    *cost = e->mc_pending_cost;
+    return LG_OK;
 }
+
 int lg_mc_update(lg_engine* e, int32_t s, const double* molecule_positions, double* energy) {
-    (void)s; (void)molecule_positions; (void)energy;
-    return fail(e, LG_ERR_STATE, "Monte Carlo entry points are not available in this build");
+    if (!valid_sys(e, s) || !molecule_positions) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    if (!e->mc_pending || e->mc_sys != s)
+        return fail(e, LG_ERR_STATE, "called EnergyCache::update without call a `*_cost` function first");
+    CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    cudaStream_t st = e->stream;
+    int msize = (int)e->mc_mol_size;
+    const SysDev& sd = e->h_sysdev[s];
+    CUDA_TRY(e, cudaMemcpyAsync(e->mc_newpos.p, molecule_positions, 3 * msize * sizeof(double),
+                                cudaMemcpyHostToDevice, st));
+    const double* d_k1 = (const double*)((const char*)(e->sysdev.p + s) + offsetof(SysDev, k1));
+    launch_mc_accept(e->b, sd, (int)e->mc_mol_begin, msize, e->mc_newpos.p, d_k1, e->mc_drho.p, st);
+    e->launches += 2;
+    CUDA_TRY(e, cudaStreamSynchronize(st));
+    CUDA_TRY(e, cudaGetLastError());
+    e->mc_energy += e->mc_pending_cost;
+    e->mc_pending = false;
+    if (energy) *energy = e->mc_energy;
+    return LG_OK;
 }
 
 }  // extern "C"

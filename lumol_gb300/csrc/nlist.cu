@@ -82,23 +82,39 @@ __global__ void nl_scatter_kernel(int n, const uint32_t* __restrict__ status,
 }
 
 // Sort each cell's atoms by index so that the list order (and so the order of
-// the force sums) does not depend on the atomics above.
-__global__ void nl_sort_kernel(int ncells, const uint32_t* __restrict__ status,
-                               const int* __restrict__ cell_start, int* __restrict__ cell_atoms,
-                               int* __restrict__ cell_count) {
+// the force sums) does not depend on the atomics above: one block per cell,
+// each atom's slot is its rank among the cell's atoms (indices are distinct).
+constexpr int SORT_SMEM = 2048;
+
+__global__ void __launch_bounds__(128) nl_sort_kernel(int ncells, const uint32_t* __restrict__ status,
+                                                      const int* __restrict__ cell_start,
+                                                      int* __restrict__ cell_atoms, int* __restrict__ cell_count) {
     if (!(*status & ST_REBUILD)) return;
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncells) return;
-    cell_count[c] = 0;  // ready for the next binning pass
+    __shared__ int buf[SORT_SMEM];
+    int c = blockIdx.x;
+    if (threadIdx.x == 0) cell_count[c] = 0;  // ready for the next binning pass
     int lo = cell_start[c], hi = cell_start[c + 1];
-    for (int a = lo + 1; a < hi; a++) {
-        int v = cell_atoms[a];
-        int b = a - 1;
-        while (b >= lo && cell_atoms[b] > v) {
-            cell_atoms[b + 1] = cell_atoms[b];
-            b--;
+    int m = hi - lo;
+    if (m <= 1) return;
+    if (m <= SORT_SMEM) {
+        for (int a = threadIdx.x; a < m; a += blockDim.x) buf[a] = cell_atoms[lo + a];
+        __syncthreads();
+        for (int a = threadIdx.x; a < m; a += blockDim.x) {
+            int v = buf[a], rank = 0;
+            for (int b = 0; b < m; b++) rank += buf[b] < v;
+            cell_atoms[lo + rank] = v;
         }
-        cell_atoms[b + 1] = v;
+    } else if (threadIdx.x == 0) {
+        // very crowded cell: serial insertion sort in place
+        for (int a = lo + 1; a < hi; a++) {
+            int v = cell_atoms[a];
+            int b = a - 1;
+            while (b >= lo && cell_atoms[b] > v) {
+                cell_atoms[b + 1] = cell_atoms[b];
+                b--;
+            }
+            cell_atoms[b + 1] = v;
+        }
     }
 }
 
@@ -191,8 +207,7 @@ void launch_nlist_build(const Batch& b, cudaStream_t st) {
     nl_scan_kernel<<<1, 1024, 0, st>>>(b.ncells, b.status, b.cell_count, b.cell_start);
     nl_scatter_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, b.status, b.atom_cell, b.cell_count,
                                                       b.cell_start, b.cell_atoms);
-    nl_sort_kernel<<<(b.ncells + tb - 1) / tb, tb, 0, st>>>(b.ncells, b.status, b.cell_start, b.cell_atoms,
-                                                          b.cell_count);
+    nl_sort_kernel<<<b.ncells, 128, 0, st>>>(b.ncells, b.status, b.cell_start, b.cell_atoms, b.cell_count);
     long long threads = (long long)n * 32;
     nl_build_kernel<<<(unsigned)((threads + tb - 1) / tb), tb, 0, st>>>(
         n, b.status, b.sysid, b.sys, b.wpos, b.atom_cell, b.cell_start, b.cell_atoms, b.maxnb, b.nbr,

@@ -490,6 +490,53 @@ class System:
                 return out[: 2 * count.value].reshape(-1, 2)
             cap = int(count.value)
 
+    # ---- Monte Carlo (EnergyCache, sys/cache.rs) -----------------------------------------
+    def mc_init(self) -> float:
+        """EnergyCache::init (cache.rs:75-98): returns the cached total energy."""
+        eng = self.engine()
+        pos = np.ascontiguousarray(self.positions, dtype=np.float64)
+        energy = ctypes.c_double(0.0)
+        eng.call("lg_mc_init", 0, C.dptr(pos), ctypes.byref(energy))
+        return energy.value
+
+    def move_molecule_cost(self, molid: int, new_positions) -> float:
+        """EnergyCache::move_molecule_cost (cache.rs:145-220): energy change of
+        moving molecule `molid` to `new_positions`."""
+        newpos = np.ascontiguousarray(new_positions, dtype=np.float64)
+        cost = ctypes.c_double(0.0)
+        self.engine().call("lg_mc_move_molecule_cost", 0, molid, C.dptr(newpos), ctypes.byref(cost))
+        return cost.value
+
+    def mc_update(self, molid: int, molecule_positions) -> float:
+        """EnergyCache::update (cache.rs:118-127) after the move was applied;
+        returns the new cached energy."""
+        newpos = np.ascontiguousarray(molecule_positions, dtype=np.float64)
+        energy = ctypes.c_double(0.0)
+        self.engine().call("lg_mc_update", 0, C.dptr(newpos), ctypes.byref(energy))
+        lo, hi = self.molecule_range(molid)
+        pos = self.positions.copy()
+        pos[lo:hi] = newpos.reshape(-1, 3)
+        self.positions = pos
+        return energy.value
+
+    def wrap_molecule(self, molid: int, positions) -> np.ndarray:
+        """Molecule::wrap (sys/config/molecules.rs:287-296): shift the molecule so
+        that its centre of mass lies in the cell (UnitCell::wrap_vector)."""
+        lo, hi = self.molecule_range(molid)
+        m = self.masses[lo:hi]
+        positions = np.asarray(positions, dtype=np.float64).reshape(-1, 3)
+        total = 0.0
+        com = np.zeros(3)
+        for a in range(hi - lo):
+            total += m[a]
+            com = com + m[a] * positions[a]
+        com = com / total
+        wrapped = com.copy()
+        for d in range(3):
+            L = self.cell.lengths[d]
+            wrapped[d] -= np.floor(wrapped[d] / L) * L
+        return positions + (wrapped - com)
+
     def kinetic_energy(self) -> float:
         v = self.velocities
         return float(sum(0.5 * m * float(np.dot(vi, vi)) for m, vi in zip(self._masses, v)))
@@ -553,3 +600,46 @@ class MolecularDynamics:
         system.positions = pos
         system.velocities = vel
         system.step += int(nsteps)
+
+
+# ---------------------------------------------------------------------------
+# Monte Carlo (lumol-sim/src/mc)
+# ---------------------------------------------------------------------------
+class Translate:
+    """Translate move (mc/moves/translate.rs:20-125): a uniform displacement in
+    [-delta / sqrt(3), delta / sqrt(3)) per axis of one random molecule."""
+
+    def __init__(self, delta: float):
+        if not delta > 0.0:
+            raise ValueError("delta must be positive in Translate move")
+        self.delta = delta / np.sqrt(3.0)
+
+
+class MonteCarlo:
+    """Metropolis propagator (mc/monte_carlo.rs:289-329) with Translate moves;
+    the move costs run on the GPU.  The random stream is numpy's, seeded (the
+    reference's xorshift stream is not reproduced)."""
+
+    def __init__(self, temperature: float, move: Translate, seed: int = 0):
+        from .units import K_BOLTZMANN
+        self.beta = 1.0 / (K_BOLTZMANN * temperature)
+        self.move = move
+        self.rng = np.random.default_rng(seed)
+        self.accepted = 0
+        self.attempted = 0
+        self.energy = None
+
+    def setup(self, system: System) -> None:
+        self.energy = system.mc_init()
+
+    def propagate(self, system: System) -> None:
+        nmol = int(system.molecules[-1]) + 1
+        molid = int(self.rng.integers(nmol))
+        lo, hi = system.molecule_range(molid)
+        delta = self.rng.uniform(-self.move.delta, self.move.delta, size=3)
+        newpos = system.positions[lo:hi] + delta
+        cost = self.beta * system.move_molecule_cost(molid, newpos)
+        self.attempted += 1
+        if cost <= 0.0 or self.rng.random() < np.exp(-cost):
+            self.energy = system.mc_update(molid, system.wrap_molecule(molid, newpos))
+            self.accepted += 1

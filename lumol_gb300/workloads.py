@@ -140,3 +140,48 @@ def water_box(n_side: int = 12, length: float = 37.3, seed: int = 0, precision: 
     system.set_coulomb_potential(ewald)
     system.velocities = boltzmann_velocities(system, temperature, seed + 1)
     return system
+
+
+def lj_replica(n: int, reduced_density: float, temperature: float, seed: int, precision: str = "fp64",
+               sigma: float = 3.405, epsilon_kj: float = 0.996) -> System:
+    """One argon-type replica: `n` atoms on a jittered simple-cubic lattice at
+    reduced density rho* = rho sigma^3, LJ of the argon workload with
+    rc = 2.5 sigma (plain cutoff), Maxwell-Boltzmann velocities at `temperature`."""
+    rng = np.random.default_rng(seed)
+    length = (n * sigma ** 3 / reduced_density) ** (1.0 / 3.0)
+    side = int(math.ceil(n ** (1.0 / 3.0)))
+    spacing = length / side
+    grid = np.array([[i, j, k] for i in range(side) for j in range(side) for k in range(side)], dtype=float)
+    grid = grid[rng.permutation(len(grid))[:n]]
+    pos = (grid + 0.5) * spacing + rng.uniform(-0.1, 0.1, size=(n, 3)) * spacing
+    system = System(UnitCell.cubic(length), precision=precision)
+    system.add_particles(["Ar"] * n, pos, masses=[39.948] * n)
+    lj = LennardJones(sigma=sigma, epsilon=from_(epsilon_kj, "kJ/mol"))
+    system.set_pair_potential(("Ar", "Ar"), PairInteraction(lj, 2.5 * sigma))
+    system.velocities = boltzmann_velocities(system, temperature, seed + 7)
+    return system
+
+
+def lj_replica_parameters(count: int = 256, seed: int = 2024, sigma: float = 3.405):
+    """Seeded draws of the batched-replica workload: N ~ U{64..4096}, rho* ~
+    U(0.3, 0.9), T ~ U(90, 300) K.  Draws whose box would be shorter than twice
+    the cutoff (N < 125 rho*, where Lumol refuses the cutoff, sys/system.rs:122-131)
+    are drawn again; the number of redraws is returned."""
+    rng = np.random.default_rng(seed)
+    params, redraws = [], 0
+    while len(params) < count:
+        n = int(rng.integers(64, 4097))
+        rho = float(rng.uniform(0.3, 0.9))
+        t = float(rng.uniform(90.0, 300.0))
+        length = (n * sigma ** 3 / rho) ** (1.0 / 3.0)
+        if 0.5 * length < 2.5 * sigma:
+            redraws += 1
+            continue
+        params.append((n, rho, t))
+    return params, redraws
+
+
+def lj_replicas(count: int = 256, seed: int = 2024, precision: str = "fp64"):
+    params, redraws = lj_replica_parameters(count, seed)
+    systems = [lj_replica(n, rho, t, seed + 1000 + i, precision) for i, (n, rho, t) in enumerate(params)]
+    return systems, params, redraws

@@ -1,0 +1,54 @@
+"""Monte Carlo move costs on the GPU against the oracle's EnergyCache
+(sys/cache.rs:145-220) with Ewald / Wolf GlobalCache costs."""
+import numpy as np
+import pytest
+
+import lumol_gb300 as lg
+import oracle
+import systems
+from lumol_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("coulomb", ["none", "ewald", "wolf"])
+def test_move_costs_match_oracle(coulomb):
+    s = systems.chains(27, 24.0, 3, lg.PairRestriction.INTER_MOLECULAR,
+                       coulomb={"none": None, "ewald": lg.Ewald(9.0, 5, 0.35), "wolf": lg.Wolf(9.0)}[coulomb])
+    orc = oracle.Oracle(s)
+    orc.cache_init()
+    e0 = s.mc_init()
+    assert abs(e0 - orc.cache_energy()) <= 1e-10 * abs(e0)
+    rng = np.random.default_rng(5)
+    # distinct molecules: the reference keeps its e^{ik.r} table stale for a molecule
+    # that moved before (ewald.rs:826-830), the engine refreshes it
+    for molid in (3, 11, 20, 7):
+        lo, hi = s.molecule_range(molid)
+        newpos = s.positions[lo:hi] + rng.uniform(-0.5, 0.5, size=3)
+        cost = s.move_molecule_cost(molid, newpos)
+        cost_ref = orc.move_molecule_cost(molid, newpos)
+        assert abs(cost - cost_ref) <= 1e-10 * abs(e0), (cost, cost_ref)
+        wrapped = s.wrap_molecule(molid, newpos)
+        e_gpu = s.mc_update(molid, wrapped)
+        pos = s.positions.copy()
+        orc.set_positions(pos)
+        orc.cache_update()
+        assert abs(e_gpu - orc.cache_energy()) <= 1e-9 * abs(e0)
+
+
+def test_cached_energy_equals_fresh_energy_after_many_moves():
+    s = workloads.nacl_crystal(cells=3, cutoff=8.0, kmax=5)
+    mc = lg.MonteCarlo(300.0, lg.Translate(0.3), seed=1)
+    mc.setup(s)
+    for _ in range(300):
+        mc.propagate(s)
+    fresh = s.potential_energy()
+    assert mc.accepted > 0
+    assert abs(mc.energy - fresh) <= 1e-9 * abs(fresh)
+
+
+def test_update_without_cost_is_an_error():
+    s = workloads.nacl_crystal(cells=3, cutoff=8.0, kmax=5)
+    s.mc_init()
+    with pytest.raises(lg.EngineError, match="without call a"):
+        s.mc_update(0, s.positions[0:1])
