@@ -44,7 +44,8 @@ def parse():
     p.add_argument("--steps", type=int, default=200)
     p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default="nacl_ewald", choices=["nacl_ewald", "argon", "water"])
+    p.add_argument("--workload", default="lj_batch", choices=["lj_batch", "nacl_ewald", "argon", "water"])
+    p.add_argument("--replicas", type=int, default=256, help="lj_batch: replicas (half MD, half MC)")
     p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     p.add_argument("--cells", type=int, default=0, help="lattice cells per side (0: the workload's size)")
     p.add_argument("--chunk", type=int, default=16, help="MD steps per timed iteration (one lg_md_run call)")
@@ -232,6 +233,17 @@ def run_reference(args, world, rank):
     import numpy as np
     import oracle
     oracle.build()
+    if args.workload == "lj_batch":
+        md_sys, md_p, mc_sys, mc_p, desc = batch_workload(args, "fp64")
+        base = batch_cpu_baseline(md_sys, mc_sys, mc_p, seconds=max(5.0, 0.05 * args.steps))
+        line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": METRIC, "n_gpus": 0,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded replicas)", "config": {"workload": desc, "precision": "fp64"},
+                "cpu_baseline": base,
+                "e2e": {"value": base["value"], "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
     system, dt, desc = make_system(args.workload, "fp64", args.cells)
     orc = oracle.Oracle(system)
     threads = oracle.num_threads()
@@ -259,11 +271,207 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def batch_workload(args, precision):
+    """The batched-replica workload: seeded argon-type replicas, even indices
+    run NVT MD (Velocity-Verlet dt = 1 fs, Berendsen tau = 100 steps), odd
+    indices NVT Monte Carlo (Translate, delta = 0.3 A)."""
+    from lumol_gb300 import workloads
+    params, redraws = workloads.lj_replica_parameters(args.replicas)
+    md_p = [(i, p) for i, p in enumerate(params) if i % 2 == 0]
+    mc_p = [(i, p) for i, p in enumerate(params) if i % 2 == 1]
+    md = [workloads.lj_replica(n, rho, t, 1000 + i, precision) for i, (n, rho, t) in md_p]
+    mc = [workloads.lj_replica(n, rho, t, 1000 + i, precision) for i, (n, rho, t) in mc_p]
+    desc = (f"{len(params)} argon-type LJ replicas (N ~ U{{64..4096}}, rho* ~ U(0.3,0.9), T ~ U(90,300) K, "
+            f"seeded; {redraws} draw(s) with L < 2 rc redrawn), rc = 2.5 sigma; {len(md)} NVT MD "
+            f"(VV dt=1 fs, Berendsen tau=100 fs) + {len(mc)} NVT MC (Translate delta=0.3 A); "
+            f"one batched step = one Lumol step of every replica (MD: N atom-steps, MC: 1 move)")
+    return md, md_p, mc, mc_p, desc
+
+
+def main_batch(args, world, rank, local):
+    import concurrent.futures
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    from lumol_gb300 import _capi as C
+    from lumol_gb300.batch import Batch
+
+    torch.cuda.set_device(local)
+    md_sys, md_p, mc_sys, mc_p, desc = batch_workload(args, args.precision)
+    md = Batch(md_sys, precision=args.precision)
+    md.md_setup([1.0] * len(md_sys), [(t, 100.0) for _, (n, rho, t) in md_p])
+    mc = Batch(mc_sys, precision=args.precision)
+    mc.md_setup([1.0] * len(mc_sys))
+    for s, (i, (n, rho, t)) in enumerate(mc_p):
+        mc.mc_setup(s, t, 0.3, 5000 + i)
+    md_atoms = md.atoms
+    mc_chains = len(mc_sys)
+
+    def stream_of(batch):
+        ptr = ctypes.c_void_p()
+        batch.engine.call("lg_get_stream", ctypes.byref(ptr))
+        return torch.cuda.ExternalStream(ptr.value)
+
+    s_md, s_mc = stream_of(md), stream_of(mc)
+    chunk = max(1, min(args.chunk, args.steps))
+    iters = (args.steps + chunk - 1) // chunk
+    pool = concurrent.futures.ThreadPoolExecutor(max_workers=2)
+
+    def one_iteration(steps_k):
+        f1 = pool.submit(md.md_run, steps_k)
+        f2 = pool.submit(mc.mc_run, steps_k)
+        f1.result()
+        f2.result()
+
+    for _ in range(max(args.warmup, 3)):
+        one_iteration(chunk)
+    if args.steps % chunk:
+        one_iteration(args.steps % chunk)
+    torch.cuda.synchronize()
+    n0a, n0b = ctypes.c_uint64(), ctypes.c_uint64()
+    md.engine.call("lg_launch_count", ctypes.byref(n0a))
+    mc.engine.call("lg_launch_count", ctypes.byref(n0b))
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(iters)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(iters)]
+    mc_done = [torch.cuda.Event() for _ in range(iters)]
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    done = 0
+    for k in range(iters):
+        steps_k = min(chunk, args.steps - done)
+        starts[k].record(s_md)
+        s_mc.wait_event(starts[k])
+        one_iteration(steps_k)
+        mc_done[k].record(s_mc)
+        s_md.wait_event(mc_done[k])
+        ends[k].record(s_md)
+        done += steps_k
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    n1a, n1b = ctypes.c_uint64(), ctypes.c_uint64()
+    md.engine.call("lg_launch_count", ctypes.byref(n1a))
+    mc.engine.call("lg_launch_count", ctypes.byref(n1b))
+    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    ms_max = max_over_ranks(world, ms)
+    work = (md_atoms + mc_chains) * args.steps
+    value = sum_over_ranks(world, float(work)) / (ms_max * 1e-3)
+
+    # MC chains alone, over many moves: moves/s of the MC half
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    mc.mc_run(2048)
+    torch.cuda.synchronize()
+    mc_rate = mc_chains * 2048 / (time.perf_counter() - t0)
+
+    # end to end: every step, all MD replicas' positions and velocities go
+    # host -> device and back through the public calls (pinned buffers)
+    e2e = None
+    if not args.no_e2e:
+        n_all = md_atoms
+        pos = torch.empty((n_all, 3), dtype=torch.float64, pin_memory=True)
+        vel = torch.empty((n_all, 3), dtype=torch.float64, pin_memory=True)
+        md.engine.call("lg_md_get_state_all", C.dptr(pos.numpy()), C.dptr(vel.numpy()), None)
+        steps_e2e = min(args.steps, 32)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps_e2e):
+            md.engine.call("lg_md_set_state_all", C.dptr(pos.numpy()), C.dptr(vel.numpy()), None)
+            md.engine.call("lg_md_run", 1)
+            md.engine.call("lg_md_get_state_all", C.dptr(pos.numpy()), C.dptr(vel.numpy()), None)
+        torch.cuda.synchronize()
+        el = max_over_ranks(world, time.perf_counter() - t0)
+        e2e = {"value": sum_over_ranks(world, float(n_all)) * steps_e2e / el, "unit": METRIC,
+               "h2d_bytes_per_step": 2 * 3 * 8 * n_all, "d2h_bytes_per_step": 2 * 3 * 8 * n_all,
+               "scope": "MD half (the MC chains' state stays on the device)"}
+
+    roofline = None if args.no_roofline else batch_roofline(args, md, C)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = batch_cpu_baseline(md_sys, mc_sys, mc_p)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+            "data": "synthetic (seeded replicas, lattice + jitter, Maxwell-Boltzmann velocities)",
+            "config": {"workload": desc, "atoms": md_atoms + mc.atoms, "md_atoms": md_atoms,
+                       "mc_chains": mc_chains, "precision": args.precision,
+                       "parallelism": f"replicas x{world}" if world > 1 else "one GPU, two engine streams",
+                       "timed_iteration": f"{chunk} batched steps (lg_md_run || lg_mc_run)",
+                       "l2": "inputs larger than L2 (neighbour lists of all replicas), no flush"},
+            "mc_moves_per_s": mc_rate,
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": int(n1a.value - n0a.value + n1b.value - n0b.value),
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def batch_roofline(args, md, C):
+    """Pair kernel of the MD half: algorithmic FLOP/s (21 geometry + 36 LJ per
+    unordered in-cutoff pair, counted with lg_pairset over every replica) over
+    its CUDA-event time, against the measured FMA peak of its pipe."""
+    import ctypes
+    kt = (ctypes.c_double * 8)()
+    md.engine.call("lg_kernel_times", 10, kt)
+    times = {name: kt[i] for i, name in enumerate(C.LG_KT_NAMES)}
+    pairs = 0
+    for s, system in enumerate(md.systems):
+        pos, _ = md.state(s)
+        count = ctypes.c_int64()
+        md.engine.call("lg_pairset", s, C.dptr(pos), 0, None, 0, ctypes.byref(count))
+        pairs += count.value
+    flops = 57 * pairs
+    fp64 = args.precision == "fp64"
+    peak = ctypes.c_double()
+    C.check(C.load().lg_fma_peak(1 if fp64 else 0, ctypes.byref(peak)))
+    achieved = flops / (times["pair"] * 1e-3) / 1e12
+    kernel = "pair_fp64_kernel" if fp64 else "pair_mixed_kernel"
+    return {"bound": "fp64" if fp64 else "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
+            "frac": achieved / peak.value, "traffic": traffic_from_profiles(kernel + "_lj_batch"),
+            "kernel": kernel, "kernel_ms": times["pair"],
+            "peak_source": ("FP64" if fp64 else "FP32") + " FMA throughput measured live by lg_fma_peak "
+                           "(MEASURED_PEAKS.json has no such figure; no tensor cores on this path)",
+            "kernel_ms_by_group": times, "work": {"pairs_lj": pairs, "pair_flops": flops}}
+
+
+def batch_cpu_baseline(md_sys, mc_sys, mc_p, seconds: float = 15.0):
+    """The oracle on the host cores over a bounded sample of the same replicas:
+    MD steps of MD replicas (O(N^2) forces) in round robin until `seconds`."""
+    import numpy as np
+    import oracle
+    threads = oracle.num_threads()
+    orcs = [oracle.Oracle(s) for s in md_sys]
+    state = [(s.positions.copy(), s.velocities.copy(), np.zeros((s.size, 3))) for s in md_sys]
+    atom_steps, steps, k = 0, 0, 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        x, v, a = state[k]
+        state[k] = orcs[k].velocity_verlet(x, v, a, 1.0, 1)
+        atom_steps += md_sys[k].size
+        steps += 1
+        k = (k + 1) % len(md_sys)
+    el = time.perf_counter() - t0
+    return {"value": atom_steps / el, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"{steps} Velocity-Verlet steps over the first {min(steps, len(md_sys))} MD replicas in "
+                      f"round robin (O(N^2) C++ restatement of lumol-core, OpenMP {threads} threads)"}
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
+        return
+    if args.workload == "lj_batch":
+        main_batch(args, world, rank, local)
         return
     import ctypes
 

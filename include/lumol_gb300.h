@@ -121,6 +121,10 @@ typedef struct {
     int32_t device;      /* CUDA device ordinal */
     int32_t precision;   /* LG_PRECISION_* */
     double skin;         /* Verlet-list skin in Angstrom (0: default 1.0) */
+    int32_t threads_per_atom;  /* 1, 2, 4, 8, 16 or 32 threads per atom in the pair kernels;
+                                  0: chosen by the autotuner.  A fixed value makes every
+                                  system's results independent of the rest of the batch. */
+    int32_t reserved;
 } lg_options;
 
 typedef struct lg_engine lg_engine;
@@ -195,6 +199,13 @@ int lg_md_setup(lg_engine* e, int32_t s, double dt, double thermostat_temperatur
 /* Uploads / downloads positions and velocities (3n each) of system `s`. */
 int lg_md_set_state(lg_engine* e, int32_t s, const double* positions, const double* velocities);
 int lg_md_get_state(lg_engine* e, int32_t s, double* positions, double* velocities);
+/* Uploads / downloads the state of every system at once: 3 * N_total doubles
+ * each, systems in index order.  `accelerations` (VelocityVerlet's, the
+ * a(t) the next half kick uses) may be NULL; on upload NULL keeps the device
+ * accelerations (zero after a description change). */
+int lg_md_set_state_all(lg_engine* e, const double* positions, const double* velocities,
+                        const double* accelerations);
+int lg_md_get_state_all(lg_engine* e, double* positions, double* velocities, double* accelerations);
 /* Runs `nsteps` steps of every system with device-resident state. */
 int lg_md_run(lg_engine* e, int64_t nsteps);
 /* Integrator::integrate for a single-system engine (integrators.rs:44-69): copies
@@ -212,6 +223,21 @@ int lg_mc_move_molecule_cost(lg_engine* e, int32_t s, int64_t molecule,
  * `positions` are the molecule's positions after Translate::apply's
  * center-of-mass wrap (lumol-sim/src/mc/moves/translate.rs:114-125). */
 int lg_mc_update(lg_engine* e, int32_t s, const double* molecule_positions, double* energy);
+
+/* Batched Monte Carlo: every system given lg_mc_setup runs its own Metropolis
+ * chain of single-particle Translate moves on the device (MonteCarlo::propagate,
+ * lumol-sim/src/mc/monte_carlo.rs:289-329, with Translate::new(delta),
+ * mc/moves/translate.rs:41-125: a uniform displacement in [-delta/sqrt(3),
+ * delta/sqrt(3)) per axis, Metropolis acceptance, centre-of-mass wrap), the
+ * cost being EnergyCache::move_molecule_cost (sys/cache.rs:145-220).  Systems
+ * with pair potentials and one-particle molecules only; delta <= skin / 2.
+ * The random stream is the engine's own (SplitMix64 seeded by `seed`), not the
+ * reference's xorshift stream. */
+int lg_mc_setup(lg_engine* e, int32_t s, double temperature, double delta, uint64_t seed);
+/* Runs `moves` attempted moves in every chain. */
+int lg_mc_run(lg_engine* e, int64_t moves);
+/* Cached energy, accepted and attempted moves of chain `s`. */
+int lg_mc_stats(lg_engine* e, int32_t s, double* energy, int64_t* accepted, int64_t* attempted);
 
 /* ---- diagnostics (no counterpart in the reference) ----------------------------- */
 /* Kernel groups timed by lg_kernel_times, in output order. */

@@ -68,7 +68,8 @@ class LgCoulomb(ctypes.Structure):
 
 
 class LgOptions(ctypes.Structure):
-    _fields_ = [("device", ctypes.c_int32), ("precision", ctypes.c_int32), ("skin", ctypes.c_double)]
+    _fields_ = [("device", ctypes.c_int32), ("precision", ctypes.c_int32), ("skin", ctypes.c_double),
+                ("threads_per_atom", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 # name -> (restype, argtypes)
@@ -93,11 +94,16 @@ SIGNATURES = {
     "lg_md_setup": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double]),
     "lg_md_set_state": (ctypes.c_int, [_P, ctypes.c_int32, _D, _D]),
     "lg_md_get_state": (ctypes.c_int, [_P, ctypes.c_int32, _D, _D]),
+    "lg_md_set_state_all": (ctypes.c_int, [_P, _D, _D, _D]),
+    "lg_md_get_state_all": (ctypes.c_int, [_P, _D, _D, _D]),
     "lg_md_run": (ctypes.c_int, [_P, ctypes.c_int64]),
     "lg_md_integrate": (ctypes.c_int, [_P, _D, _D, ctypes.c_int64]),
     "lg_mc_init": (ctypes.c_int, [_P, ctypes.c_int32, _D, _D]),
     "lg_mc_move_molecule_cost": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int64, _D, _D]),
     "lg_mc_update": (ctypes.c_int, [_P, ctypes.c_int32, _D, _D]),
+    "lg_mc_setup": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_uint64]),
+    "lg_mc_run": (ctypes.c_int, [_P, ctypes.c_int64]),
+    "lg_mc_stats": (ctypes.c_int, [_P, ctypes.c_int32, _D, _I64, _I64]),
     "lg_get_stream": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
     "lg_kernel_times": (ctypes.c_int, [_P, ctypes.c_int32, _D]),
     "lg_launch_count": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64)]),

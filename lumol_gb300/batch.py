@@ -16,9 +16,10 @@ class Batch:
     Each system keeps its own cell, pair table, Coulomb potential, timestep
     and thermostat; atoms are concatenated in system order on the device."""
 
-    def __init__(self, systems: list[System], precision: str = "fp64", skin: float = 1.0):
+    def __init__(self, systems: list[System], precision: str = "fp64", skin: float = 1.0,
+                 threads_per_atom: int = 0):
         self.systems = systems
-        self.engine = Engine(len(systems), precision, skin)
+        self.engine = Engine(len(systems), precision, skin, threads_per_atom=threads_per_atom)
         for s, system in enumerate(systems):
             system._lower_into(self.engine, s)
         self.offsets = np.cumsum([0] + [s.size for s in systems])
@@ -46,3 +47,47 @@ class Batch:
         pos, vel = np.zeros((n, 3)), np.zeros((n, 3))
         self.engine.call("lg_md_get_state", s, C.dptr(pos), C.dptr(vel))
         return pos, vel
+
+    # ---- batched Monte Carlo chains ---------------------------------------------------
+    def mc_setup(self, s: int, temperature: float, delta: float, seed: int) -> None:
+        """MonteCarlo(temperature) with Translate(delta) moves for system `s`."""
+        self.engine.call("lg_mc_setup", s, float(temperature), float(delta), int(seed) & (2 ** 64 - 1))
+
+    def mc_run(self, moves: int) -> None:
+        """`moves` attempted moves in every chain."""
+        self.engine.call("lg_mc_run", int(moves))
+
+    def mc_stats(self, s: int):
+        energy = ctypes.c_double()
+        acc, att = ctypes.c_int64(), ctypes.c_int64()
+        self.engine.call("lg_mc_stats", s, ctypes.byref(energy), ctypes.byref(acc), ctypes.byref(att))
+        return energy.value, acc.value, att.value
+
+    def energy(self, s: int) -> float:
+        """Potential energy of system `s` at its current device positions."""
+        pos, _ = self.state(s)
+        system = self.systems[s]
+        out = ctypes.c_double()
+        forces = np.zeros((system.size, 3))
+        virial = np.zeros(9)
+        self.engine.call("lg_compute", s, C.dptr(np.ascontiguousarray(pos)), C.LG_TERM_ALL, C.LG_WANT_ENERGY,
+                         C.dptr(forces), ctypes.byref(out), C.dptr(virial))
+        return out.value
+
+
+class SplitMix64:
+    """Host copy of the chains' random stream (SplitMix64), for tests that replay
+    a chain's moves."""
+
+    def __init__(self, seed: int):
+        self.state = (int(seed) * 0x9E3779B97F4A7C15 + 0x632BE59BD9B4E019) & (2 ** 64 - 1)
+
+    def next(self) -> int:
+        self.state = (self.state + 0x9E3779B97F4A7C15) & (2 ** 64 - 1)
+        z = self.state
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & (2 ** 64 - 1)
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & (2 ** 64 - 1)
+        return z ^ (z >> 31)
+
+    def uniform(self) -> float:
+        return (self.next() >> 11) * (1.0 / 9007199254740992.0)

@@ -222,7 +222,7 @@ struct lg_engine {
     DBuf<SysDev> sysdev;
     DBuf<PairDev> ptab;
     DBuf<KVecDev> kvec;
-    DBuf<uint32_t> status;
+    DBuf<uint32_t> status, sys_rebuild;
     DBuf<int> pairs_out;
     DBuf<unsigned long long> pairs_count;
     uint32_t* h_status = nullptr;  // pinned
@@ -240,6 +240,11 @@ struct lg_engine {
     std::map<int, cudaGraphExec_t> graphs;
     std::map<int, size_t> graph_nodes;
     bool graph_thermo = false;
+
+    // batched Monte Carlo chains
+    DBuf<McState> mc_chains;
+    std::vector<McState> h_mc;
+    bool mc_energies_ready = false;
 
     // MC (single molecule moves)
     DBuf<double> mc_newpos, mc_partial, mc_dk, mc_out;
@@ -595,6 +600,7 @@ int commit(lg_engine* e) {
     CUDA_TRY(e, e->sysdev.alloc(nsys));
     CUDA_TRY(e, e->ptab.alloc(h_ptab.size()));
     CUDA_TRY(e, e->status.alloc(1));
+    CUDA_TRY(e, e->sys_rebuild.alloc(nsys));
     int nkv = (int)h_kvec.size();
     int kchunk = 32;
     int nkchunks = 0, max_chunks = 0;
@@ -659,6 +665,9 @@ int commit(lg_engine* e) {
                                 cudaMemcpyHostToDevice, st));
     uint32_t st_init = ST_REBUILD;
     CUDA_TRY(e, cudaMemcpyAsync(e->status.p, &st_init, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    std::vector<uint32_t> all_rebuild(nsys, 1u);
+    CUDA_TRY(e, cudaMemcpyAsync(e->sys_rebuild.p, all_rebuild.data(), nsys * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                st));
     CUDA_TRY(e, cudaStreamSynchronize(st));
 
     if (e->h_out) cudaFreeHost(e->h_out);
@@ -697,6 +706,7 @@ int commit(lg_engine* e) {
     b.wpos = e->wpos.p;
     b.pos_build = e->pos_build.p;
     b.status = e->status.p;
+    b.sys_rebuild = e->sys_rebuild.p;
     b.nkvec = nkv;
     b.kdim = kdim;
     b.kchunk = kchunk;
@@ -710,7 +720,11 @@ int commit(lg_engine* e) {
     b.host_const = e->host_const.p;
     b.lambda = e->lambda.p;
     b.ke = e->ke.p;
-    b.tpa = mixed ? 8 : 32;
+    if (e->h_mc.size() != (size_t)nsys) e->h_mc.assign(nsys, McState{});
+    CUDA_TRY(e, e->mc_chains.alloc(nsys));
+    CUDA_TRY(e, cudaMemcpy(e->mc_chains.p, e->h_mc.data(), nsys * sizeof(McState), cudaMemcpyHostToDevice));
+    e->mc_energies_ready = false;
+    b.tpa = e->opt.threads_per_atom ? e->opt.threads_per_atom : (mixed ? 8 : 32);
     b.pos_hi = mixed ? e->pos_hi.p : nullptr;
     b.pos_lo = mixed ? e->pos_lo.p : nullptr;
     b.ptabf = e->ptabf.p;
@@ -729,8 +743,7 @@ int regrow(lg_engine* e) {
     CUDA_TRY(e, e->nbr.alloc((size_t)e->b.n * maxnb));
     e->b.maxnb = maxnb;
     e->b.nbr = e->nbr.p;
-    uint32_t st_init = ST_REBUILD;
-    CUDA_TRY(e, cudaMemcpyAsync(e->status.p, &st_init, sizeof(uint32_t), cudaMemcpyHostToDevice, e->stream));
+    launch_request_rebuild(e->b, e->stream);
     e->drop_graphs();
     return LG_OK;
 }
@@ -810,6 +823,23 @@ int compute_batch(lg_engine* e, uint32_t terms, uint32_t want, double* d_force_o
     return fail(e, LG_ERR_CAPACITY, "neighbour list overflow persisted after regrowing");
 }
 
+// Copies the host positions of system s into its slice of the device state;
+// the other systems keep theirs.
+int upload_positions(lg_engine* e, int32_t s, const double* positions) {
+    const HostSystem& h = e->sys[s];
+    if (h.n == 0) return LG_OK;
+    int64_t base = e->begin[s];
+    cudaStream_t st = e->stream;
+    CUDA_TRY(e, cudaMemcpyAsync(e->pos3.p + 3 * base, positions, 3 * h.n * sizeof(double), cudaMemcpyHostToDevice,
+                                st));
+    Batch sub = e->b;
+    sub.n = (int)h.n;
+    sub.posq = e->posq.p + base;
+    launch_pack_positions(sub, e->pos3.p + 3 * base, st);
+    e->launches += 1;
+    return LG_OK;
+}
+
 int check_pair_cutoffs(lg_engine* e, const HostSystem& h) {
     if (!h.has_cell) return LG_OK;
     double half = 0.5 * std::min(std::min(h.L[0], h.L[1]), h.L[2]);
@@ -840,8 +870,11 @@ int lg_create(const lg_options* options, int32_t n_systems, lg_engine** out) {
     if (!out) return fail(nullptr, LG_ERR_ARGUMENT, "null engine pointer");
     *out = nullptr;
     if (n_systems <= 0) return fail(nullptr, LG_ERR_ARGUMENT, "n_systems must be positive");
-    lg_options opt{0, LG_PRECISION_FP64, 1.0};
+    lg_options opt{0, LG_PRECISION_FP64, 1.0, 0, 0};
     if (options) opt = *options;
+    int t = opt.threads_per_atom;
+    if (t != 0 && t != 1 && t != 2 && t != 4 && t != 8 && t != 16 && t != 32)
+        return fail(nullptr, LG_ERR_ARGUMENT, "threads_per_atom must be 0, 1, 2, 4, 8, 16 or 32");
     if (opt.precision != LG_PRECISION_FP64 && opt.precision != LG_PRECISION_MIXED)
         return fail(nullptr, LG_ERR_ARGUMENT, "unknown precision");
     if (opt.skin <= 0.0) opt.skin = 1.0;
@@ -994,11 +1027,8 @@ int lg_compute(lg_engine* e, int32_t s, const double* positions, uint32_t terms,
     const HostSystem& h = e->sys[s];
     int64_t base = e->begin[s];
     cudaStream_t st = e->stream;
-    if (h.n) {
-        CUDA_TRY(e, cudaMemcpyAsync(e->pos3.p + 3 * base, positions, 3 * h.n * sizeof(double),
-                                    cudaMemcpyHostToDevice, st));
-        launch_pack_positions(e->b, e->pos3.p, st);
-    }
+    rc = upload_positions(e, s, positions);
+    if (rc) return rc;
     bool ev = (want & (LG_WANT_ENERGY | LG_WANT_VIRIAL)) != 0;
     rc = compute_batch(e, terms, want, nullptr, nullptr);
     if (rc) return rc;
@@ -1069,11 +1099,8 @@ int lg_pairset(lg_engine* e, int32_t s, const double* positions, int32_t family,
     const HostSystem& h = e->sys[s];
     int64_t base = e->begin[s];
     cudaStream_t st = e->stream;
-    if (h.n) {
-        CUDA_TRY(e, cudaMemcpyAsync(e->pos3.p + 3 * base, positions, 3 * h.n * sizeof(double),
-                                    cudaMemcpyHostToDevice, st));
-        launch_pack_positions(e->b, e->pos3.p, st);
-    }
+    rc = upload_positions(e, s, positions);
+    if (rc) return rc;
     // make sure the list is current (and large enough) for these positions
     rc = compute_batch(e, LG_TERM_PAIRS | LG_TERM_COUL_REAL, LG_WANT_FORCES, nullptr, nullptr);
     if (rc) return rc;
@@ -1186,6 +1213,10 @@ namespace {
 // keeps the fastest, and caches the choice for this workload shape.
 int autotune(lg_engine* e) {
     if (e->tuned || e->b.n == 0) return LG_OK;
+    if (e->opt.threads_per_atom) {  // fixed by the caller
+        e->tuned = true;
+        return LG_OK;
+    }
     Batch& b = e->b;
     auto key = std::make_tuple(e->opt.device, b.precision, b.n, b.maxnb, b.nkvec);
     {
@@ -1349,6 +1380,56 @@ int lg_md_run(lg_engine* e, int64_t nsteps) {
     return LG_OK;
 }
 
+int lg_md_set_state_all(lg_engine* e, const double* positions, const double* velocities,
+                        const double* accelerations) {
+    if (!e || !positions || !velocities) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    bool was_dirty = e->dirty;
+    int rc = commit(e);
+    if (rc) return rc;
+    cudaStream_t st = e->stream;
+    size_t n = (size_t)e->b.n;
+    if (n == 0) return LG_OK;
+    CUDA_TRY(e, cudaMemcpyAsync(e->pos3.p, positions, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(e, cudaMemcpyAsync(e->vel3.p, velocities, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st));
+    launch_pack_positions(e->b, e->pos3.p, st);
+    launch_pack_velocities(e->b, e->vel3.p, st);
+    e->launches += 2;
+    if (accelerations) {
+        CUDA_TRY(e, cudaMemcpyAsync(e->force.p, accelerations, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st));
+        launch_pack_vectors(e->b.n, e->force.p, e->acc.p, st);
+        e->launches += 1;
+    } else if (was_dirty) {
+        CUDA_TRY(e, cudaMemsetAsync(e->acc.p, 0, n * sizeof(double4_32a), st));
+    }
+    CUDA_TRY(e, cudaGetLastError());
+    CUDA_TRY(e, cudaStreamSynchronize(st));
+    return LG_OK;
+}
+
+int lg_md_get_state_all(lg_engine* e, double* positions, double* velocities, double* accelerations) {
+    if (!e) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    if (e->dirty) return fail(e, LG_ERR_STATE, "no device state: call lg_md_set_state first");
+    CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    cudaStream_t st = e->stream;
+    size_t n = (size_t)e->b.n;
+    if (n == 0) return LG_OK;
+    launch_unpack_positions(e->b, e->pos3.p, st);
+    launch_unpack_velocities(e->b, e->vel3.p, st);
+    e->launches += 2;
+    if (positions)
+        CUDA_TRY(e, cudaMemcpyAsync(positions, e->pos3.p, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (velocities)
+        CUDA_TRY(e, cudaMemcpyAsync(velocities, e->vel3.p, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (accelerations) {
+        launch_unpack_vectors(e->b.n, e->acc.p, e->force.p, st);
+        e->launches += 1;
+        CUDA_TRY(e, cudaMemcpyAsync(accelerations, e->force.p, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    }
+    CUDA_TRY(e, cudaStreamSynchronize(st));
+    return LG_OK;
+}
+
 int lg_md_integrate(lg_engine* e, double* positions, double* velocities, int64_t nsteps) {
     if (!e || e->nsys != 1) return fail(e, LG_ERR_ARGUMENT, "lg_md_integrate needs a single-system engine");
     int rc = lg_md_set_state(e, 0, positions, velocities);
@@ -1445,17 +1526,9 @@ int lg_mc_init(lg_engine* e, int32_t s, const double* positions, double* energy)
     CUDA_TRY(e, cudaSetDevice(e->opt.device));
     int rc = commit(e);
     if (rc) return rc;
-    const HostSystem& h = e->sys[s];
-    int64_t base = e->begin[s];
     cudaStream_t st = e->stream;
-    if (h.n) {
-        CUDA_TRY(e, cudaMemcpyAsync(e->pos3.p + 3 * base, positions, 3 * h.n * sizeof(double),
-                                    cudaMemcpyHostToDevice, st));
-        Batch sub = e->b;
-        sub.n = (int)h.n;
-        sub.posq = e->posq.p + base;
-        launch_pack_positions(sub, e->pos3.p + 3 * base, st);
-    }
+    rc = upload_positions(e, s, positions);
+    if (rc) return rc;
     rc = compute_batch(e, LG_TERM_ALL, LG_WANT_ENERGY, nullptr, nullptr);
     if (rc) return rc;
     // FP64 e^{ik.r} and rho(k) at these positions: the state the move costs update
@@ -1530,6 +1603,116 @@ int lg_mc_update(lg_engine* e, int32_t s, const double* molecule_positions, doub
     e->mc_energy += e->mc_pending_cost;
     e->mc_pending = false;
     if (energy) *energy = e->mc_energy;
+    return LG_OK;
+}
+
+int lg_mc_setup(lg_engine* e, int32_t s, double temperature, double delta, uint64_t seed) {
+    if (!valid_sys(e, s)) return fail(e, LG_ERR_ARGUMENT, "invalid system index");
+    // MonteCarlo::new (mc/monte_carlo.rs) and Translate::new (translate.rs:41-52)
+    if (!(temperature > 0.0)) return fail(e, LG_ERR_ARGUMENT, "the temperature must be positive in Monte Carlo");
+    if (!(delta > 0.0)) return fail(e, LG_ERR_ARGUMENT, "delta must be positive in Translate move");
+    const HostSystem& h = e->sys[s];
+    if (h.coul.kind != LG_COULOMB_NONE)
+        return fail(e, LG_ERR_ARGUMENT,
+                    "batched Monte Carlo chains evaluate pair potentials only; use lg_mc_move_molecule_cost "
+                    "for systems with Coulomb interactions");
+    for (size_t i = 1; i < h.mols.size(); i++)
+        if (h.mols[i] == h.mols[i - 1])
+            return fail(e, LG_ERR_ARGUMENT, "batched Monte Carlo chains move single-particle molecules only");
+    double half = delta / std::sqrt(3.0);
+    if (std::sqrt(3.0) * half > 0.5 * e->skin)
+        return fail(e, LG_ERR_ARGUMENT, "the Translate amplitude must not exceed half the neighbour-list skin");
+    if (e->h_mc.size() != (size_t)e->nsys) e->h_mc.assign(e->nsys, McState{});
+    McState& m = e->h_mc[s];
+    m.beta = 1.0 / (K_BOLTZMANN * temperature);
+    m.delta = half;
+    m.rng = seed * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull;
+    m.enabled = 1;
+    m.moves_left = 0;
+    m.need_rebuild = 0;
+    m.accepted = m.attempted = 0;
+    if (!e->dirty) {
+        CUDA_TRY(e, cudaSetDevice(e->opt.device));
+        CUDA_TRY(e, cudaMemcpy(e->mc_chains.p + s, &m, sizeof(McState), cudaMemcpyHostToDevice));
+    }
+    return LG_OK;
+}
+
+int lg_mc_run(lg_engine* e, int64_t moves) {
+    if (!e || moves < 0) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    if (e->dirty) return fail(e, LG_ERR_STATE, "no device state: call lg_md_set_state first");
+    CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    cudaStream_t st = e->stream;
+    int nsys = e->nsys;
+    CUDA_TRY(e, cudaMemcpy(e->h_mc.data(), e->mc_chains.p, nsys * sizeof(McState), cudaMemcpyDeviceToHost));
+    if (!e->mc_energies_ready) {
+        // EnergyCache::init: the chains start from the full energy of every system
+        int rc = compute_batch(e, LG_TERM_ALL, LG_WANT_ENERGY, nullptr, nullptr);
+        if (rc) return rc;
+        std::vector<double> out((size_t)nsys * RED_STRIDE);
+        CUDA_TRY(e, cudaMemcpy(out.data(), e->out.p, out.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        for (int s = 0; s < nsys; s++) e->h_mc[s].energy = out[(size_t)s * RED_STRIDE];
+        e->mc_energies_ready = true;
+    }
+    bool any = false;
+    bool fp64 = e->opt.precision == LG_PRECISION_FP64;
+    for (int s = 0; s < nsys; s++)
+        if (e->h_mc[s].enabled) {
+            e->h_mc[s].moves_left = moves;
+            e->h_mc[s].need_rebuild = 0;
+            any = true;
+        }
+    if (!any) return fail(e, LG_ERR_STATE, "lg_mc_setup was not called for any system");
+    CUDA_TRY(e, cudaMemcpyAsync(e->mc_chains.p, e->h_mc.data(), nsys * sizeof(McState), cudaMemcpyHostToDevice, st));
+    // the list must be current for the positions the chains start from
+    launch_check_displacement(e->b, st);
+    launch_nlist_build(e->b, st);
+    e->launches += 7;
+    for (int64_t launch = 0; launch < moves + 64; launch++) {
+        launch_mc_chains(e->b, e->mc_chains.p, fp64, st);
+        e->launches += 1;
+        CUDA_TRY(e, cudaMemcpyAsync(e->h_mc.data(), e->mc_chains.p, nsys * sizeof(McState), cudaMemcpyDeviceToHost,
+                                    st));
+        CUDA_TRY(e, cudaStreamSynchronize(st));
+        CUDA_TRY(e, cudaGetLastError());
+        bool rebuild = false, pending = false;
+        for (int s = 0; s < nsys; s++) {
+            if (!e->h_mc[s].enabled) continue;
+            rebuild = rebuild || e->h_mc[s].need_rebuild;
+            pending = pending || e->h_mc[s].moves_left > 0;
+        }
+        if (!pending) return LG_OK;
+        if (rebuild) {
+            for (int s = 0; s < nsys; s++) e->h_mc[s].need_rebuild = 0;
+            CUDA_TRY(e, cudaMemcpyAsync(e->mc_chains.p, e->h_mc.data(), nsys * sizeof(McState),
+                                        cudaMemcpyHostToDevice, st));
+            launch_request_rebuild(e->b, st);
+            launch_nlist_build(e->b, st);
+            e->launches += 7;
+            uint32_t status;
+            int rc = read_status(e, &status);
+            if (rc) return rc;
+            if (status & ST_OVERFLOW) {
+                rc = clear_status_bits(e, ST_OVERFLOW);
+                if (rc) return rc;
+                rc = regrow(e);
+                if (rc) return rc;
+                launch_nlist_build(e->b, st);
+            }
+        }
+    }
+    return fail(e, LG_ERR_STATE, "Monte Carlo chains did not finish");
+}
+
+int lg_mc_stats(lg_engine* e, int32_t s, double* energy, int64_t* accepted, int64_t* attempted) {
+    if (!valid_sys(e, s)) return fail(e, LG_ERR_ARGUMENT, "invalid system index");
+    if (e->dirty) return fail(e, LG_ERR_STATE, "no device state");
+    CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    McState m;
+    CUDA_TRY(e, cudaMemcpy(&m, e->mc_chains.p + s, sizeof(McState), cudaMemcpyDeviceToHost));
+    if (energy) *energy = m.energy;
+    if (accepted) *accepted = m.accepted;
+    if (attempted) *attempted = m.attempted;
     return LG_OK;
 }
 

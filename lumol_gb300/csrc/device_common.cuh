@@ -79,6 +79,18 @@ struct KVecDev {
     double virial[6];   // energy (1 - 2 (1/k^2 + 1/(4 alpha^2)) k k^T), symmetric xx xy xz yy yz zz
 };
 
+// Metropolis chain of one system (batched Monte Carlo).
+struct McState {
+    double beta;          // 1 / (kB T)
+    double delta;         // Translate: delta / sqrt(3), the half width per axis
+    double energy;        // EnergyCache energy, updated by the accepted moves
+    uint64_t rng;         // SplitMix64 state
+    long long moves_left;
+    long long accepted, attempted;
+    int32_t enabled;
+    int32_t need_rebuild;
+};
+
 // Status word bits (device -> host).
 enum : uint32_t {
     ST_REBUILD = 1u,        // neighbour list must be rebuilt

@@ -45,6 +45,7 @@ struct Batch {
     float4* wpos = nullptr;       // wrapped FP32 positions at build, charge
     double4_32a* pos_build = nullptr; // positions at the last build
     uint32_t* status = nullptr;   // ST_* bits
+    uint32_t* sys_rebuild = nullptr;  // nsys: 1 when that system's list must be rebuilt
     // Ewald k-space
     int nkvec = 0;
     int kdim = 0;                 // max kmax + 1 (eikr stores k = 0..kmax per axis)
@@ -87,6 +88,8 @@ void launch_pairset(const Batch& b, int family, int s_begin, int s_end, int* out
                     unsigned long long* count, cudaStream_t st);
 // md.cu
 void launch_pack_positions(const Batch& b, const double* pos3, cudaStream_t st);
+void launch_pack_vectors(int n, const double* src3, double4_32a* dst, cudaStream_t st);
+void launch_unpack_vectors(int n, const double4_32a* src, double* dst3, cudaStream_t st);
 void launch_unpack_positions(const Batch& b, double* pos3, cudaStream_t st);
 void launch_pack_velocities(const Batch& b, const double* vel3, cudaStream_t st);
 void launch_unpack_velocities(const Batch& b, double* vel3, cudaStream_t st);
@@ -102,6 +105,7 @@ void launch_mc_cost(const Batch& b, int s, const SysDev& sd, int mbeg, int msize
                     cudaStream_t st);
 void launch_mc_accept(const Batch& b, const SysDev& sd, int mbeg, int msize, const double* d_newpos,
                       const double* d_k1, const double2* d_drho, cudaStream_t st);
+void launch_mc_chains(const Batch& b, McState* mc, bool fp64, cudaStream_t st);
 // diag.cu
 int measure_fma_peak(int fp64, double* tflops);
 // capi.cu: the message lg_last_error(NULL) returns

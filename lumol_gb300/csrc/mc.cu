@@ -227,4 +227,161 @@ void launch_mc_accept(const Batch& b, const SysDev& sd, int mbeg, int msize, con
                                                                         b.posq, b.eikr, nk > 0 ? 1 : 0);
 }
 
+// ---------------------------------------------------------------------------
+// Batched Monte Carlo: every system of the batch runs its own Metropolis chain
+// of Translate moves (lumol-sim/src/mc/moves/translate.rs:85-125,
+// mc/monte_carlo.rs:289-329), one warp per system.  A move's energy change is
+// the EnergyCache cost (sys/cache.rs:145-220) of a one-atom molecule, summed
+// over the atom's Verlet-list neighbours: the list holds every atom within the
+// cutoff of both the old and the new position as long as no atom, the moved
+// one included, is farther than skin/2 from where the list was built.  A move
+// that would break this stops the chain before it is attempted; the host
+// rebuilds the lists and relaunches the remaining moves.
+// ---------------------------------------------------------------------------
+
+// SplitMix64 (Steele, Lea & Flood, "Fast splittable pseudorandom number
+// generators", OOPSLA 2014): one 64-bit state per chain.
+__device__ __forceinline__ uint64_t splitmix64(uint64_t& state) {
+    uint64_t z = (state += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+__device__ __forceinline__ double uniform01(uint64_t& state) {
+    return (double)(splitmix64(state) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+template <bool FP64>
+__device__ __forceinline__ double mc_pair_energy(const SysDev& s, const PairDev& p, const PairDevF& pf, double dx,
+                                                 double dy, double dz) {
+    if (FP64) {
+        double r = exact_norm(dx, dy, dz);
+        if (r >= p.cutoff) return 0.0;
+        double e, f;
+        pair_energy_force(p, r, 1.0 / r, e, f);
+        return e;
+    } else {
+        float fx = (float)dx, fy = (float)dy, fz = (float)dz;
+        float r2 = fx * fx + fy * fy + fz * fz;
+        if (!(r2 < pf.rc2)) return 0.0;
+        float ir2 = 1.0f / r2;
+        float ir6 = ir2 * ir2 * ir2;
+        if (pf.type == 2) return (double)(ir6 * (pf.a * ir6 - pf.b) - pf.shift);
+        float inv_r = rsqrtf(r2);
+        float fr;
+        float ef;
+        switch (pf.type) {
+            case 3: ef = pf.a * __expf(-r2 * inv_r * pf.c) - pf.b * ir6 - pf.shift; break;
+            case 4: {
+                float dr = r2 * inv_r - pf.b;
+                ef = 0.5f * pf.a * dr * dr - pf.shift;
+                break;
+            }
+            default: ef = 0.0f;
+        }
+        (void)fr;
+        return (double)ef;
+    }
+}
+
+template <bool FP64>
+__global__ void __launch_bounds__(128) mc_chain_kernel(Batch b, McState* __restrict__ mc) {
+    int s = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    int lane = threadIdx.x & 31;
+    if (s >= b.nsys) return;
+    McState st = mc[s];
+    if (!st.enabled || st.moves_left <= 0 || st.need_rebuild) return;
+    const SysDev& sd = b.sys[s];
+    int natoms = sd.end - sd.begin;
+    if (natoms <= 0) return;
+    uint64_t rng = st.rng;
+    int64_t left = st.moves_left;
+    double energy = st.energy;
+    long long accepted = st.accepted, attempted = st.attempted;
+    bool rebuild = false;
+    while (left > 0) {
+        // the move: a random atom (select_molecule) and a displacement in [-delta, delta) per axis
+        uint64_t saved = rng;
+        int i = sd.begin + min((int)(uniform01(rng) * natoms), natoms - 1);
+        double ddx = -st.delta + 2.0 * st.delta * uniform01(rng);
+        double ddy = -st.delta + 2.0 * st.delta * uniform01(rng);
+        double ddz = -st.delta + 2.0 * st.delta * uniform01(rng);
+        double u_accept = uniform01(rng);
+        double4_32a old = b.posq[i];
+        double nx = old.x + ddx, ny = old.y + ddy, nz = old.z + ddz;
+        double4_32a bp = b.pos_build[i];
+        double ex = nx - bp.x, ey = ny - bp.y, ez = nz - bp.z;
+        ex -= rint(ex * sd.invL[0]) * sd.L[0];
+        ey -= rint(ey * sd.invL[1]) * sd.L[1];
+        ez -= rint(ez * sd.invL[2]) * sd.L[2];
+        if (!(ex * ex + ey * ey + ez * ez <= sd.half_skin2)) {
+            rng = saved;  // not attempted: retried after the list rebuild
+            rebuild = true;
+            break;
+        }
+        int ki = b.kind[i];
+        const PairDev* prow = b.ptab + sd.ptab + ki * sd.nk;
+        const PairDevF* prowf = b.ptabf + sd.ptab + ki * sd.nk;
+        double de = 0.0;
+        int cnt = b.nnb[i];
+        const int* list = b.nbr + (size_t)i * b.maxnb;
+        for (int k = lane; k < cnt; k += 32) {
+            int j = list[k];
+            double4_32a pj = b.posq[j];
+            int kj = b.kind[j];
+            const PairDev& p = prow[kj];
+            if (p.type == 0 || restriction_excluded(p.restriction, 0)) continue;
+            if (FP64) {
+                double ox, oy, oz, wx, wy, wz;
+                // Configuration::distance(i, j), UnitCell::distance(r_j, new_i)
+                exact_nearest_image(sd, pj.x, pj.y, pj.z, old.x, old.y, old.z, ox, oy, oz);
+                exact_nearest_image(sd, nx, ny, nz, pj.x, pj.y, pj.z, wx, wy, wz);
+                de += mc_pair_energy<true>(sd, p, prowf[kj], wx, wy, wz) -
+                      mc_pair_energy<true>(sd, p, prowf[kj], ox, oy, oz);
+            } else {
+                // FP32 minimum image of FP64 differences
+                float o3[3] = {(float)(old.x - pj.x), (float)(old.y - pj.y), (float)(old.z - pj.z)};
+                float w3[3] = {(float)(nx - pj.x), (float)(ny - pj.y), (float)(nz - pj.z)};
+                for (int d = 0; d < 3; d++) {
+                    o3[d] -= sd.Lf[d] * rintf(o3[d] * sd.invLf[d]);
+                    w3[d] -= sd.Lf[d] * rintf(w3[d] * sd.invLf[d]);
+                }
+                de += mc_pair_energy<false>(sd, p, prowf[kj], w3[0], w3[1], w3[2]) -
+                      mc_pair_energy<false>(sd, p, prowf[kj], o3[0], o3[1], o3[2]);
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) de += __shfl_xor_sync(0xffffffffu, de, o);
+        attempted++;
+        double cost = st.beta * de;
+        bool accept = cost <= 0.0 || u_accept < exp(-cost);
+        if (accept) {
+            // Translate::apply: new position, then Molecule::wrap (UnitCell::wrap_vector)
+            if (lane == 0) {
+                double w[3] = {nx, ny, nz};
+                for (int d = 0; d < 3; d++) w[d] -= floor(w[d] / sd.L[d]) * sd.L[d];
+                b.posq[i] = make_double4_32a(w[0], w[1], w[2], old.w);
+            }
+            energy += de;
+            accepted++;
+        }
+        __syncwarp();
+        left--;
+    }
+    if (lane == 0) {
+        mc[s].rng = rng;
+        mc[s].moves_left = left;
+        mc[s].energy = energy;
+        mc[s].accepted = accepted;
+        mc[s].attempted = attempted;
+        mc[s].need_rebuild = rebuild ? 1 : 0;
+    }
+}
+
+void launch_mc_chains(const Batch& b, McState* mc, bool fp64, cudaStream_t st) {
+    int warps_per_block = 4;
+    int grid = (b.nsys + warps_per_block - 1) / warps_per_block;
+    if (fp64) mc_chain_kernel<true><<<grid, 32 * warps_per_block, 0, st>>>(b, mc);
+    else mc_chain_kernel<false><<<grid, 32 * warps_per_block, 0, st>>>(b, mc);
+}
+
 }  // namespace lg

@@ -45,6 +45,18 @@ __global__ void unpack_velocities_kernel(int n, const double4_32a* __restrict__ 
     vel3[3 * i + 2] = v.z;
 }
 
+__global__ void pack_vectors_kernel(int n, const double* __restrict__ src3, double4_32a* __restrict__ dst) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    dst[i] = make_double4_32a(src3[3 * i], src3[3 * i + 1], src3[3 * i + 2], 0.0);
+}
+void launch_pack_vectors(int n, const double* src3, double4_32a* dst, cudaStream_t st) {
+    if (n) pack_vectors_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, src3, dst);
+}
+void launch_unpack_vectors(int n, const double4_32a* src, double* dst3, cudaStream_t st) {
+    if (n) unpack_velocities_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, src, dst3);
+}
+
 void launch_pack_positions(const Batch& b, const double* pos3, cudaStream_t st) {
     if (b.n) pack_positions_kernel<<<(b.n + 255) / 256, 256, 0, st>>>(b.n, pos3, b.posq);
 }
@@ -64,10 +76,11 @@ void launch_unpack_velocities(const Batch& b, double* vel3, cudaStream_t st) {
 __global__ void vv_first_kernel(int n, const int* __restrict__ sysid, const SysDev* __restrict__ sys,
                                 double4_32a* __restrict__ posq, double4_32a* __restrict__ vel,
                                 const double4_32a* __restrict__ acc, const double4_32a* __restrict__ pos_build,
-                                double* __restrict__ force, uint32_t* status) {
+                                double* __restrict__ force, uint32_t* status, uint32_t* sys_rebuild) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const SysDev& s = sys[sysid[i]];
+    int si = sysid[i];
+    const SysDev& s = sys[si];
     // products and sums rounded separately, as the reference (no FMA)
     double hdt = __dmul_rn(0.5, s.dt);
     double4_32a v = vel[i], a = acc[i], p = posq[i];
@@ -87,7 +100,10 @@ __global__ void vv_first_kernel(int n, const int* __restrict__ sysid, const SysD
     dx -= rint(dx * s.invL[0]) * s.L[0];
     dy -= rint(dy * s.invL[1]) * s.L[1];
     dz -= rint(dz * s.invL[2]) * s.L[2];
-    if (dx * dx + dy * dy + dz * dz > s.half_skin2) atomicOr(status, ST_REBUILD);
+    if (dx * dx + dy * dy + dz * dz > s.half_skin2) {
+        sys_rebuild[si] = 1u;
+        atomicOr(status, ST_REBUILD);
+    }
 }
 
 // a = F / m; v += 0.5 dt a (integrators.rs:55-68); kinetic energy per atom
@@ -150,32 +166,38 @@ __global__ void thermostat_scale_kernel(int n, const int* __restrict__ sysid, co
 // Displacement test alone, for positions set from the host.
 __global__ void check_displacement_kernel(int n, const int* __restrict__ sysid, const SysDev* __restrict__ sys,
                                           const double4_32a* __restrict__ posq,
-                                          const double4_32a* __restrict__ pos_build, uint32_t* status) {
+                                          const double4_32a* __restrict__ pos_build, uint32_t* status,
+                                          uint32_t* sys_rebuild) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const SysDev& s = sys[sysid[i]];
+    int si = sysid[i];
+    const SysDev& s = sys[si];
     double4_32a p = posq[i], b = pos_build[i];
     double dx = p.x - b.x, dy = p.y - b.y, dz = p.z - b.z;
     dx -= rint(dx * s.invL[0]) * s.L[0];
     dy -= rint(dy * s.invL[1]) * s.L[1];
     dz -= rint(dz * s.invL[2]) * s.L[2];
-    if (!(dx * dx + dy * dy + dz * dz <= s.half_skin2)) atomicOr(status, ST_REBUILD);
+    if (!(dx * dx + dy * dy + dz * dz <= s.half_skin2)) {
+        sys_rebuild[si] = 1u;
+        atomicOr(status, ST_REBUILD);
+    }
 }
 
 void launch_check_displacement(const Batch& b, cudaStream_t st) {
     if (b.n)
         check_displacement_kernel<<<(b.n + 255) / 256, 256, 0, st>>>(b.n, b.sysid, b.sys, b.posq, b.pos_build,
-                                                                   b.status);
+                                                                   b.status, b.sys_rebuild);
 }
 
-__global__ void request_rebuild_kernel(uint32_t* status) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) *status |= ST_REBUILD;
+__global__ void request_rebuild_kernel(int nsys, uint32_t* status, uint32_t* sys_rebuild) {
+    for (int s = threadIdx.x; s < nsys; s += blockDim.x) sys_rebuild[s] = 1u;
+    if (threadIdx.x == 0) atomicOr(status, ST_REBUILD);
 }
 
 void launch_vv_first(const Batch& b, cudaStream_t st) {
     if (b.n)
         vv_first_kernel<<<(b.n + 255) / 256, 256, 0, st>>>(b.n, b.sysid, b.sys, b.posq, b.vel, b.acc,
-                                                         b.pos_build, b.force, b.status);
+                                                         b.pos_build, b.force, b.status, b.sys_rebuild);
 }
 void launch_vv_second(const Batch& b, bool thermostat, cudaStream_t st) {
     if (b.n)
@@ -187,6 +209,8 @@ void launch_thermostat(const Batch& b, cudaStream_t st) {
     thermostat_reduce_kernel<<<b.nsys, 256, 0, st>>>(b.sys, b.ke, b.lambda);
     thermostat_scale_kernel<<<(b.n + 255) / 256, 256, 0, st>>>(b.n, b.sysid, b.lambda, b.vel);
 }
-void launch_request_rebuild(const Batch& b, cudaStream_t st) { request_rebuild_kernel<<<1, 32, 0, st>>>(b.status); }
+void launch_request_rebuild(const Batch& b, cudaStream_t st) {
+    request_rebuild_kernel<<<1, 256, 0, st>>>(b.nsys, b.status, b.sys_rebuild);
+}
 
 }  // namespace lg

@@ -10,7 +10,10 @@
 // list stays valid while no atom moved more than skin / 2 since the build.
 //
 // All kernels are launched every step (so one step can be captured in a CUDA
-// graph) and return at once unless the status word asks for a rebuild.
+// graph) and return at once unless the status word asks for a rebuild.  The
+// decision is per system: only the systems with an atom that moved more than
+// skin / 2 rebuild, so a system's list (and the order of its force sums) never
+// depends on the other systems of the batch.
 #include "kernels.h"
 
 namespace lg {
@@ -20,11 +23,12 @@ namespace lg {
 // position for the displacement test.
 __global__ void nl_bin_kernel(int n, const double4_32a* __restrict__ posq, const int* __restrict__ sysid,
                               const SysDev* __restrict__ sys, const uint32_t* __restrict__ status,
-                              int* __restrict__ atom_cell, int* __restrict__ cell_count,
-                              float4* __restrict__ wpos, double4_32a* __restrict__ pos_build) {
+                              const uint32_t* __restrict__ sys_rebuild, int* __restrict__ atom_cell,
+                              int* __restrict__ cell_count, float4* __restrict__ wpos,
+                              double4_32a* __restrict__ pos_build) {
     if (!(*status & ST_REBUILD)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || !sys_rebuild[sysid[i]]) return;
     const SysDev& s = sys[sysid[i]];
     double4_32a p = posq[i];
     double w[3] = {p.x, p.y, p.z};
@@ -70,12 +74,13 @@ __global__ void nl_scan_kernel(int ncells, const uint32_t* __restrict__ status,
     if (t == blockDim.x - 1) cell_start[ncells] = partial[t];
 }
 
-__global__ void nl_scatter_kernel(int n, const uint32_t* __restrict__ status,
-                                  const int* __restrict__ atom_cell, int* __restrict__ cell_count,
-                                  const int* __restrict__ cell_start, int* __restrict__ cell_atoms) {
+__global__ void nl_scatter_kernel(int n, const uint32_t* __restrict__ status, const int* __restrict__ sysid,
+                                  const uint32_t* __restrict__ sys_rebuild, const int* __restrict__ atom_cell,
+                                  int* __restrict__ cell_count, const int* __restrict__ cell_start,
+                                  int* __restrict__ cell_atoms) {
     if (!(*status & ST_REBUILD)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || !sys_rebuild[sysid[i]]) return;
     int c = atom_cell[i];
     int slot = atomicAdd(&cell_count[c], 1);
     cell_atoms[cell_start[c] + slot] = i;
@@ -134,7 +139,7 @@ __device__ __forceinline__ int stencil_cells(int c, int nc, int* out) {
 // Warp per atom: scan the stencil, keep j != i whose FP32 minimum-image
 // distance is below rlist (plus margin).  Full list: each pair appears in the
 // lists of both atoms.
-__global__ void nl_build_kernel(int n, const uint32_t* status,
+__global__ void nl_build_kernel(int n, const uint32_t* status, const uint32_t* __restrict__ sys_rebuild,
                                 const int* __restrict__ sysid, const SysDev* __restrict__ sys,
                                 const float4* __restrict__ wpos, const int* __restrict__ atom_cell,
                                 const int* __restrict__ cell_start, const int* __restrict__ cell_atoms,
@@ -145,6 +150,7 @@ __global__ void nl_build_kernel(int n, const uint32_t* status,
     int lane = threadIdx.x & 31;
     if (warp >= n) return;
     int i = warp;
+    if (!sys_rebuild[sysid[i]]) return;  // this system keeps its list
     const SysDev& s = sys[sysid[i]];
     float4 pi = wpos[i];
     int local = atom_cell[i] - s.cell_begin;
@@ -193,26 +199,29 @@ __global__ void nl_build_kernel(int n, const uint32_t* status,
     }
 }
 
-// Clears the rebuild request once the list is in place.
-__global__ void nl_done_kernel(uint32_t* status) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) *status &= ~ST_REBUILD;
+// Clears the rebuild requests once the lists are in place.
+__global__ void nl_done_kernel(int nsys, uint32_t* status, uint32_t* sys_rebuild) {
+    if (!(*status & ST_REBUILD)) return;
+    for (int s = threadIdx.x; s < nsys; s += blockDim.x) sys_rebuild[s] = 0;
+    __syncthreads();
+    if (threadIdx.x == 0) *status &= ~ST_REBUILD;
 }
 
 void launch_nlist_build(const Batch& b, cudaStream_t st) {
     int n = b.n;
     if (n == 0) return;
     int tb = 256;
-    nl_bin_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, b.posq, b.sysid, b.sys, b.status, b.atom_cell,
-                                                  b.cell_count, b.wpos, b.pos_build);
+    nl_bin_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, b.posq, b.sysid, b.sys, b.status, b.sys_rebuild,
+                                                  b.atom_cell, b.cell_count, b.wpos, b.pos_build);
     nl_scan_kernel<<<1, 1024, 0, st>>>(b.ncells, b.status, b.cell_count, b.cell_start);
-    nl_scatter_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, b.status, b.atom_cell, b.cell_count,
-                                                      b.cell_start, b.cell_atoms);
+    nl_scatter_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, b.status, b.sysid, b.sys_rebuild, b.atom_cell,
+                                                      b.cell_count, b.cell_start, b.cell_atoms);
     nl_sort_kernel<<<b.ncells, 128, 0, st>>>(b.ncells, b.status, b.cell_start, b.cell_atoms, b.cell_count);
     long long threads = (long long)n * 32;
     nl_build_kernel<<<(unsigned)((threads + tb - 1) / tb), tb, 0, st>>>(
-        n, b.status, b.sysid, b.sys, b.wpos, b.atom_cell, b.cell_start, b.cell_atoms, b.maxnb, b.nbr,
-        b.nnb, b.status);
-    nl_done_kernel<<<1, 32, 0, st>>>(b.status);
+        n, b.status, b.sys_rebuild, b.sysid, b.sys, b.wpos, b.atom_cell, b.cell_start, b.cell_atoms, b.maxnb,
+        b.nbr, b.nnb, b.status);
+    nl_done_kernel<<<1, 256, 0, st>>>(b.nsys, b.status, b.sys_rebuild);
 }
 
 }  // namespace lg

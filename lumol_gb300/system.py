@@ -182,10 +182,11 @@ class UnitCell:
 class Engine:
     """Owns one lg_engine handle (a batch of `n_systems` systems)."""
 
-    def __init__(self, n_systems: int = 1, precision: str = "fp64", skin: float = 1.0, device: int = 0):
+    def __init__(self, n_systems: int = 1, precision: str = "fp64", skin: float = 1.0, device: int = 0,
+                 threads_per_atom: int = 0):
         lib = C.load()
         prec = {"fp64": C.LG_PRECISION_FP64, "mixed": C.LG_PRECISION_MIXED}[precision]
-        opt = C.LgOptions(device, prec, skin)
+        opt = C.LgOptions(device, prec, skin, threads_per_atom, 0)
         handle = ctypes.c_void_p()
         C.check(lib.lg_create(ctypes.byref(opt), n_systems, ctypes.byref(handle)))
         self.lib = lib

@@ -185,3 +185,50 @@ def lj_replicas(count: int = 256, seed: int = 2024, precision: str = "fp64"):
     params, redraws = lj_replica_parameters(count, seed)
     systems = [lj_replica(n, rho, t, seed + 1000 + i, precision) for i, (n, rho, t) in enumerate(params)]
     return systems, params, redraws
+
+
+def lj_fluid_like_argon(n: int, seed: int, precision: str = "fp64") -> System:
+    """LJ fluid like the argon workload: `n` atoms at its density (500 / 28.8^3),
+    jittered simple-cubic placement, shifted LJ, rc = 10 A."""
+    density = 500.0 / 28.8 ** 3
+    sigma = 3.405
+    system = lj_replica(n, density * sigma ** 3, 300.0, seed, precision)
+    lj = LennardJones(sigma=sigma, epsilon=from_(0.996, "kJ/mol"))
+    system.pairs.clear()
+    system.set_pair_potential(("Ar", "Ar"), PairInteraction.shifted(lj, 10.0))
+    return system
+
+
+def serving_requests(count: int = 48, rate: float = 40.0, seed: int = 77, precision: str = "mixed",
+                     scale: float = 1.0):
+    """Seeded request stream of the serving workload: Poisson arrivals at `rate`
+    per second; 60 % LJ fluids like the argon workload (200-20000 atoms), 25 %
+    NaCl Ewald crystals like the NaCl workload (3^3..10^3 conventional cells,
+    216-8000 ions; rc = min(9 A, L/2)), 15 % water boxes like the water workload
+    (300-3000 molecules); 500-5000 MD steps each.  `scale` < 1 shrinks sizes and
+    step counts for tests."""
+    from .serving import Request
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for rid in range(count):
+        t += float(rng.exponential(1.0 / rate))
+        u = float(rng.random())
+        steps = max(10, int(rng.integers(500, 5001) * scale))
+        if u < 0.60:
+            n = max(170, int(rng.integers(200, 20001) * scale))
+            system, kind, dt = lj_fluid_like_argon(n, 3000 + rid, precision), "lj", 1.0
+        elif u < 0.85:
+            c = int(rng.integers(3, 11)) if scale >= 1.0 else int(rng.integers(3, 5))
+            length = 5.64 * c
+            rc = min(9.0, 0.5 * length * (1.0 - 1e-9))
+            system, kind, dt = nacl_crystal(cells=c, cutoff=rc, precision=precision, seed=3000 + rid), "nacl", 1.0
+        else:
+            m = max(300, int(rng.integers(300, 3001) * scale))
+            side = int(math.ceil(m ** (1.0 / 3.0)))
+            length = 37.3 * (m / 1728.0) ** (1.0 / 3.0)
+            system = water_box(n_side=side, length=length * side / m ** (1.0 / 3.0), precision=precision,
+                               seed=3000 + rid)
+            kind, dt = "water", 0.5
+        out.append(Request(rid=rid, system=system, nsteps=steps, timestep=dt, arrival=t, kind=kind))
+    return out

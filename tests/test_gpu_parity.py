@@ -187,3 +187,32 @@ def test_cutoff_above_half_cell_is_rejected():
     bad = C.LgCoulomb(C.LG_COULOMB_EWALD, 0, 0, 0, 3.0, 0.3, 1.0)
     with pytest.raises(lg.EngineError, match="kmax can not be 0"):
         eng.call("lg_set_coulomb", 0, ctypes.byref(bad))
+
+
+def test_batch_of_systems_matches_each_alone():
+    """Systems of one engine are independent: each one's energy, forces and
+    virial equal the oracle's for that system, and computing one system leaves
+    the others' device state alone."""
+    from lumol_gb300.batch import Batch
+    systems = [jitter(workloads.argon_fcc(cells=4), 0.2, 1), workloads.nacl_crystal(cells=3, cutoff=8.0, kmax=5),
+               jitter(workloads.water_box(n_side=7, length=21.76), 0.05, 2)]
+    batch = Batch(systems)
+    batch.md_setup([1.0, 1.0, 0.5])
+    batch.md_run(10)
+    states = [batch.state(s) for s in range(3)]
+    for s, system in enumerate(systems):
+        system.positions = states[s][0]
+        orc = oracle.Oracle(system)
+        import ctypes
+        from lumol_gb300 import _capi as C
+        forces = np.zeros((system.size, 3))
+        energy = ctypes.c_double()
+        virial = np.zeros(9)
+        batch.engine.call("lg_compute", s, C.dptr(np.ascontiguousarray(system.positions)), lg.LG_TERM_ALL, 7,
+                          C.dptr(forces), ctypes.byref(energy), C.dptr(virial))
+        assert abs(energy.value - orc.energy()) <= TOL * abs(orc.energy())
+        fo = orc.forces()
+        assert np.sqrt(np.mean((forces - fo) ** 2)) / np.sqrt(np.mean(fo ** 2)) <= TOL
+    for s in range(3):
+        pos, vel = batch.state(s)
+        assert np.array_equal(pos, states[s][0]) and np.array_equal(vel, states[s][1])
