@@ -44,7 +44,9 @@ def parse():
     p.add_argument("--steps", type=int, default=200)
     p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default="lj_batch", choices=["lj_batch", "nacl_ewald", "argon", "water"])
+    p.add_argument("--workload", default="lj_batch", choices=["lj_batch", "serving", "nacl_ewald", "argon", "water"])
+    p.add_argument("--requests", type=int, default=48, help="serving: number of requests")
+    p.add_argument("--rate", type=float, default=40.0, help="serving: Poisson arrival rate (1/s)")
     p.add_argument("--replicas", type=int, default=256, help="lj_batch: replicas (half MD, half MC)")
     p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     p.add_argument("--cells", type=int, default=0, help="lattice cells per side (0: the workload's size)")
@@ -414,6 +416,54 @@ def main_batch(args, world, rank, local):
         dist.destroy_process_group()
 
 
+def main_serving(args, world, rank, local):
+    """The serving stream: Poisson arrivals of LJ / NaCl+Ewald / water MD
+    requests served by the continuous-batching server; throughput over the
+    wall-clock span of the stream and p50 / p99 completion latency."""
+    import torch
+
+    from lumol_gb300 import workloads
+    from lumol_gb300.serving import Server, latency_percentiles
+
+    torch.cuda.set_device(local)
+    requests = workloads.serving_requests(count=args.requests, rate=args.rate, seed=77 + rank,
+                                          precision=args.precision)
+    warm = workloads.serving_requests(count=4, rate=1000.0, seed=1, precision=args.precision, scale=0.02)
+    server = Server(precision=args.precision, chunk=args.chunk * 4, max_lanes=4)
+    server.run(warm)
+    server.close()
+    server = Server(precision=args.precision, chunk=args.chunk * 4, max_lanes=4)
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    t0 = time.perf_counter()
+    done = server.run(requests)
+    torch.cuda.synchronize()
+    span = max_over_ranks(world, time.perf_counter() - t0)
+    clk = clocks.stop()
+    server.close()
+    atom_steps = sum(r.system.size * r.nsteps for r in done)
+    value = sum_over_ranks(world, float(atom_steps)) / span
+    p50, p99 = latency_percentiles(done)
+    kinds = {k: sum(1 for r in done if r.kind == k) for k in ("lj", "nacl", "water")}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": len(done),
+            "warmup": 4, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+            "data": "synthetic (seeded Poisson request stream)",
+            "config": {"workload": f"serving stream of {len(done)} MD requests at {args.rate}/s: "
+                                   f"60% LJ (200-20000 atoms), 25% NaCl+Ewald (216-8000 ions), 15% water "
+                                   f"(300-3000 molecules), 500-5000 steps each", "kinds": kinds,
+                       "precision": args.precision, "timing": "host wall clock over the stream (latency metric)",
+                       "lanes_max": server.stats.max_lanes, "lane_rebuilds": server.stats.lane_rebuilds,
+                       "rounds": server.stats.rounds},
+            "latency_s": {"p50": p50, "p99": p99},
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+
+
 def batch_roofline(args, md, C):
     """Pair kernel of the MD half: algorithmic FLOP/s (21 geometry + 36 LJ per
     unordered in-cutoff pair, counted with lg_pairset over every replica) over
@@ -472,6 +522,9 @@ def main():
         return
     if args.workload == "lj_batch":
         main_batch(args, world, rank, local)
+        return
+    if args.workload == "serving":
+        main_serving(args, world, rank, local)
         return
     import ctypes
 

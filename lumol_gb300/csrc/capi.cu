@@ -215,7 +215,8 @@ struct lg_engine {
     DBuf<int8_t> spec_path;
     DBuf<int4> bt;
     DBuf<double2> bt_par, eikr, rho;
-    DBuf<float4> wpos, pos_hi, pos_lo;
+    DBuf<float4> wpos;
+    DBuf<uint4> posfx;
     DBuf<PairDevF> ptabf;
     DBuf<KVecF> kvecf;
     DBuf<float2> eikrf, rhof;
@@ -450,7 +451,7 @@ int commit(lg_engine* e) {
             d.invL[k] = 1.0 / h.L[k];
             d.Lf[k] = (float)h.L[k];
             d.invLf[k] = (float)(1.0 / h.L[k]);
-            d.Llo[k] = (float)(h.L[k] - (double)d.Lf[k]);
+            d.Lq[k] = (float)(h.L[k] / 4294967296.0);
         }
         double rc = max_cutoff(h);
         d.rlist = rc + e->skin;
@@ -617,8 +618,7 @@ int commit(lg_engine* e) {
                            (float)v.energy};
     }
     CUDA_TRY(e, e->ptabf.alloc(h_ptabf.size()));
-    CUDA_TRY(e, e->pos_hi.alloc(mixed ? n : 1));
-    CUDA_TRY(e, e->pos_lo.alloc(mixed ? n : 1));
+    CUDA_TRY(e, e->posfx.alloc(mixed ? n : 1));
     CUDA_TRY(e, e->kvecf.alloc(nkv));
     CUDA_TRY(e, e->eikrf.alloc(mixed && nkv ? (size_t)kdim * 3 * n : 1));
     CUDA_TRY(e, e->rhof.alloc(nkv));
@@ -725,8 +725,7 @@ int commit(lg_engine* e) {
     CUDA_TRY(e, cudaMemcpy(e->mc_chains.p, e->h_mc.data(), nsys * sizeof(McState), cudaMemcpyHostToDevice));
     e->mc_energies_ready = false;
     b.tpa = e->opt.threads_per_atom ? e->opt.threads_per_atom : (mixed ? 8 : 32);
-    b.pos_hi = mixed ? e->pos_hi.p : nullptr;
-    b.pos_lo = mixed ? e->pos_lo.p : nullptr;
+    b.posfx = mixed ? e->posfx.p : nullptr;
     b.ptabf = e->ptabf.p;
     b.kvecf = e->kvecf.p;
     b.eikrf = e->eikrf.p;

@@ -66,7 +66,7 @@ struct SysDev {
     double thermo_T, thermo_tau;  // Berendsen (tau <= 0: none)
     double dof;                   // 3 N (DegreesOfFreedom::Particles)
     float Lf[3], invLf[3];        // FP32 copies for the list build and the mixed path
-    float Llo[3];                 // L - (double)Lf: low word of the cell lengths
+    float Lq[3];                  // L / 2^32: the length of one fixed-point unit
     float rlist2_f;               // (rlist + margin)^2 in FP32
     float coul_rc2_f;
 };

@@ -63,8 +63,7 @@ struct Batch {
     double* ke = nullptr;         // n kinetic energies
     // mixed precision
     int tpa = 32;                 // threads per atom of the pair kernels (autotuned)
-    float4* pos_hi = nullptr;     // wrapped positions, high FP32 word, charge
-    float4* pos_lo = nullptr;     // low FP32 word
+    uint4* posfx = nullptr;       // wrapped positions as 32-bit fractions of L, charge bits
     PairDevF* ptabf = nullptr;
     KVecF* kvecf = nullptr;
     float2* eikrf = nullptr;

@@ -6,11 +6,13 @@
 // in FP64; the Ewald structure factors rho(k) are accumulated in FP64; the
 // integrator keeps FP64 positions and velocities.
 //
-// Positions reach the kernels as two FP32 words per coordinate, hi + lo = the
-// wrapped FP64 position to about 48 bits, and the cell length likewise, so
-// the minimum-image difference of two atoms carries only the FP32 rounding of
-// the difference itself (relative 6e-8), not the FP32 rounding of absolute
-// positions (which would be an absolute ulp(L) error).
+// Positions reach the kernels as 32-bit fixed-point fractions of the cell
+// length (u = floor(frac(x / L) * 2^32)), 16 bytes per atom with the charge:
+// the difference of two coordinates, taken as a signed 32-bit integer, wraps
+// around exactly like the minimum image of an orthorhombic cell, and its
+// resolution (L / 2^32, 1.6e-8 A at L = 70 A) is far below the FP32 rounding
+// of the distance itself, so d = int32(u_i - u_j) * L / 2^32 carries a
+// relative error of about 6e-8 with no absolute ulp(L) term.
 //
 // Threads per atom (TPA = 1..32) is a template parameter chosen per workload
 // by the autotuner: the TPA lanes of a group walk one atom's neighbour list
@@ -46,14 +48,9 @@ __device__ __forceinline__ double group_sum_d(double v) {
     return v;
 }
 
-// Minimum image of hi/lo coordinates in FP32 (the image shift uses L = Lhi + Llo).
-__device__ __forceinline__ float mixed_image(float hi_i, float lo_i, float hi_j, float lo_j, float Lhi, float Llo,
-                                             float invL) {
-    float d = (hi_i - hi_j) + (lo_i - lo_j);
-    float nimg = rintf(d * invL);
-    d = fmaf(-nimg, Lhi, d);
-    d = fmaf(-nimg, Llo, d);
-    return d;
+// Minimum image of two fixed-point coordinates: signed wrap-around difference.
+__device__ __forceinline__ float fixed_image(uint32_t ui, uint32_t uj, float scale) {
+    return (float)(int32_t)(ui - uj) * scale;
 }
 
 // Pair potential in FP32: returns energy, writes force / r.
@@ -86,7 +83,7 @@ __device__ __forceinline__ float pair_mixed(const PairDevF& p, float r2, float i
 
 template <int TPA, bool EV>
 __global__ void __launch_bounds__(256) pair_mixed_kernel(
-    int n, const float4* __restrict__ phi, const float4* __restrict__ plo, const int* __restrict__ kind,
+    int n, const uint4* __restrict__ pfx, const int* __restrict__ kind,
     const int* __restrict__ mol, const int* __restrict__ sysid, const SysDev* __restrict__ sys,
     const PairDevF* __restrict__ ptab, const int* __restrict__ nbr, const int* __restrict__ nnb, int maxnb,
     const int* __restrict__ spec_off, const int* __restrict__ spec_j, const int8_t* __restrict__ spec_path,
@@ -97,17 +94,16 @@ __global__ void __launch_bounds__(256) pair_mixed_kernel(
     bool active = i < n;
     int ii = active ? i : n - 1;
     const SysDev& s = sys[sysid[ii]];
-    float4 hi = phi[ii], lo = plo[ii];
+    uint4 pi = pfx[ii];
+    float qi = __uint_as_float(pi.w);
     int ki = kind[ii], mi = mol[ii];
     const PairDevF* prow = ptab + s.ptab + ki * s.nk;
-    float Lh0 = s.Lf[0], Lh1 = s.Lf[1], Lh2 = s.Lf[2];
-    float Ll0 = s.Llo[0], Ll1 = s.Llo[1], Ll2 = s.Llo[2];
-    float iL0 = s.invLf[0], iL1 = s.invLf[1], iL2 = s.invLf[2];
-    bool coul = (terms & 16u) && s.coul != 0 && hi.w != 0.0f;
+    float sc0 = s.Lq[0], sc1 = s.Lq[1], sc2 = s.Lq[2];
+    bool coul = (terms & 16u) && s.coul != 0 && qi != 0.0f;
     bool pairs = (terms & 1u) != 0;
     float coul_rc2 = s.coul_rc2_f;
     float alpha = (float)s.alpha;
-    float pref = hi.w * (float)(1.0 / FOUR_PI_EPSILON_0);
+    float pref = qi * (float)(1.0 / FOUR_PI_EPSILON_0);
     float fxs = 0.f, fxc = 0.f, fys = 0.f, fyc = 0.f, fzs = 0.f, fzc = 0.f;
     double ep = 0.0, ec = 0.0;
     double w0 = 0, w1 = 0, w2 = 0, w3 = 0, w4 = 0, w5 = 0;
@@ -115,14 +111,15 @@ __global__ void __launch_bounds__(256) pair_mixed_kernel(
     const int* list = nbr + (size_t)ii * maxnb;
     for (int k = sub; k < cnt; k += TPA) {
         int j = list[k];
-        float4 hj = phi[j], lj = plo[j];
-        float dx = mixed_image(hi.x, lo.x, hj.x, lj.x, Lh0, Ll0, iL0);
-        float dy = mixed_image(hi.y, lo.y, hj.y, lj.y, Lh1, Ll1, iL1);
-        float dz = mixed_image(hi.z, lo.z, hj.z, lj.z, Lh2, Ll2, iL2);
+        uint4 pj = pfx[j];
+        float qj = __uint_as_float(pj.w);
+        float dx = fixed_image(pi.x, pj.x, sc0);
+        float dy = fixed_image(pi.y, pj.y, sc1);
+        float dz = fixed_image(pi.z, pj.z, sc2);
         float r2 = dx * dx + dy * dy + dz * dz;
         const PairDevF& p = prow[kind[j]];
         bool pin = pairs && p.type != 0 && r2 < p.rc2;
-        bool cin = coul && hj.w != 0.0f && r2 <= coul_rc2;
+        bool cin = coul && qj != 0.0f && r2 <= coul_rc2;
         if (!(pin || cin)) continue;
         int path = -1;
         int mj = mol[j];
@@ -151,7 +148,7 @@ __global__ void __launch_bounds__(256) pair_mixed_kernel(
                 excl = restriction_excluded(s.coul_restr, path);
                 if (s.coul_restr == 6 && path == 4) csc = (float)s.coul_scale14;
             }
-            float qq = pref * hj.w;
+            float qq = pref * qj;
             float r = r2 * inv_r;
             float ar = alpha * r;
             if (s.coul == 1) {
@@ -205,8 +202,8 @@ __global__ void __launch_bounds__(256) pair_mixed_kernel(
         force[3 * i + 1] += fy;
         force[3 * i + 2] += fz;
         if (EV) {
-            if ((terms & 16u) && s.coul == 2 && hi.w != 0.0f) {
-                double q = (double)hi.w;
+            if ((terms & 16u) && s.coul == 2 && qi != 0.0f) {
+                double q = (double)qi;
                 ec -= q * q * 0.5 * (s.wolf_ec + s.alpha * FRAC_2_SQRT_PI) / FOUR_PI_EPSILON_0;
             }
             double* rr = red + (size_t)i * RED_STRIDE;
@@ -226,11 +223,11 @@ void launch_pair_mixed_tpa(const Batch& b, uint32_t terms, bool ev, cudaStream_t
     long long threads = (long long)b.n * TPA;
     unsigned grid = (unsigned)((threads + tb - 1) / tb);
     if (ev)
-        pair_mixed_kernel<TPA, true><<<grid, tb, 0, st>>>(b.n, b.pos_hi, b.pos_lo, b.kind, b.mol, b.sysid, b.sys,
+        pair_mixed_kernel<TPA, true><<<grid, tb, 0, st>>>(b.n, b.posfx, b.kind, b.mol, b.sysid, b.sys,
                                                           b.ptabf, b.nbr, b.nnb, b.maxnb, b.spec_off, b.spec_j,
                                                           b.spec_path, terms, b.force, b.red);
     else
-        pair_mixed_kernel<TPA, false><<<grid, tb, 0, st>>>(b.n, b.pos_hi, b.pos_lo, b.kind, b.mol, b.sysid, b.sys,
+        pair_mixed_kernel<TPA, false><<<grid, tb, 0, st>>>(b.n, b.posfx, b.kind, b.mol, b.sysid, b.sys,
                                                            b.ptabf, b.nbr, b.nnb, b.maxnb, b.spec_off, b.spec_j,
                                                            b.spec_path, terms, b.force, b.red);
 }
@@ -247,28 +244,28 @@ void launch_pair_mixed(const Batch& b, uint32_t terms, bool ev, cudaStream_t st)
     }
 }
 
-// FP32 hi / lo split of the wrapped FP64 positions (UnitCell::wrap_vector).
-__global__ void split_positions_kernel(int n, const double4_32a* __restrict__ posq, const int* __restrict__ sysid,
-                                       const SysDev* __restrict__ sys, float4* __restrict__ phi,
-                                       float4* __restrict__ plo) {
+// Fixed-point copy of the wrapped FP64 positions (UnitCell::wrap_vector):
+// u = floor(frac(x / L) * 2^32), and the charge's FP32 bits.
+__global__ void fixed_positions_kernel(int n, const double4_32a* __restrict__ posq, const int* __restrict__ sysid,
+                                       const SysDev* __restrict__ sys, uint4* __restrict__ pfx) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const SysDev& s = sys[sysid[i]];
     double4_32a p = posq[i];
     double w[3] = {p.x, p.y, p.z};
-    float h[3], l[3];
+    uint32_t u[3];
     for (int d = 0; d < 3; d++) {
-        double x = w[d] - floor(w[d] * s.invL[d]) * s.L[d];
-        h[d] = (float)x;
-        l[d] = (float)(x - (double)h[d]);
+        double f = w[d] * s.invL[d];
+        f -= floor(f);
+        unsigned long long q = (unsigned long long)(f * 4294967296.0);
+        u[d] = (uint32_t)(q & 0xffffffffull);
     }
-    phi[i] = make_float4(h[0], h[1], h[2], (float)p.w);
-    plo[i] = make_float4(l[0], l[1], l[2], 0.0f);
+    pfx[i] = make_uint4(u[0], u[1], u[2], __float_as_uint((float)p.w));
 }
 
 void launch_split_positions(const Batch& b, cudaStream_t st) {
-    if (b.n && b.pos_hi)
-        split_positions_kernel<<<(b.n + 255) / 256, 256, 0, st>>>(b.n, b.posq, b.sysid, b.sys, b.pos_hi, b.pos_lo);
+    if (b.n && b.posfx)
+        fixed_positions_kernel<<<(b.n + 255) / 256, 256, 0, st>>>(b.n, b.posq, b.sysid, b.sys, b.posfx);
 }
 
 // ---------------------------------------------------------------------------

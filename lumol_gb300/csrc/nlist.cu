@@ -136,20 +136,26 @@ __device__ __forceinline__ int stencil_cells(int c, int nc, int* out) {
     return nc;
 }
 
-// Warp per atom: scan the stencil, keep j != i whose FP32 minimum-image
-// distance is below rlist (plus margin).  Full list: each pair appears in the
-// lists of both atoms.
-__global__ void nl_build_kernel(int n, const uint32_t* status, const uint32_t* __restrict__ sys_rebuild,
-                                const int* __restrict__ sysid, const SysDev* __restrict__ sys,
-                                const float4* __restrict__ wpos, const int* __restrict__ atom_cell,
-                                const int* __restrict__ cell_start, const int* __restrict__ cell_atoms,
-                                int maxnb, int* __restrict__ nbr, int* __restrict__ nnb,
-                                uint32_t* status_out) {
+// Warp per atom: keep j != i whose FP32 minimum-image distance is below
+// rlist (plus margin).  The stencil cells are flattened into one range of
+// candidates (per-warp prefix sums of the cell populations in shared memory),
+// so all 32 lanes test candidates even when cells hold a few atoms; candidates
+// keep the cell-then-index order.  Full list: each pair appears in the lists
+// of both atoms.
+constexpr int NL_WARPS = 8;
+
+__global__ void __launch_bounds__(32 * NL_WARPS) nl_build_kernel(
+    int n, const uint32_t* status, const uint32_t* __restrict__ sys_rebuild, const int* __restrict__ sysid,
+    const SysDev* __restrict__ sys, const float4* __restrict__ wpos, const int* __restrict__ atom_cell,
+    const int* __restrict__ cell_start, const int* __restrict__ cell_atoms, int maxnb, int* __restrict__ nbr,
+    int* __restrict__ nnb, uint32_t* status_out) {
+    __shared__ int s_lo[NL_WARPS][28];
+    __shared__ int s_pre[NL_WARPS][28];
     if (!(*status & ST_REBUILD)) return;
-    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int wib = threadIdx.x >> 5;
+    int i = blockIdx.x * NL_WARPS + wib;
     int lane = threadIdx.x & 31;
-    if (warp >= n) return;
-    int i = warp;
+    if (i >= n) return;
     if (!sys_rebuild[sysid[i]]) return;  // this system keeps its list
     const SysDev& s = sys[sysid[i]];
     float4 pi = wpos[i];
@@ -161,38 +167,60 @@ __global__ void nl_build_kernel(int n, const uint32_t* status, const uint32_t* _
     int nx = stencil_cells(cx, s.ncell[0], sx);
     int ny = stencil_cells(cy, s.ncell[1], sy);
     int nz = stencil_cells(cz, s.ncell[2], sz);
+    int ncand = nx * ny * nz;
+    // lane c < ncand owns stencil cell c (z, y, x order)
+    int cnt = 0, lo = 0;
+    if (lane < ncand) {
+        int a = lane / (nx * ny), b = (lane / nx) % ny, c = lane % nx;
+        int cell = s.cell_begin + (sz[a] * s.ncell[1] + sy[b]) * s.ncell[0] + sx[c];
+        lo = cell_start[cell];
+        cnt = cell_start[cell + 1] - lo;
+    }
+    int incl = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+        int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    int total = __shfl_sync(0xffffffffu, incl, 31);
+    if (lane < ncand) {
+        s_lo[wib][lane] = lo;
+        s_pre[wib][lane] = incl - cnt;
+    }
+    if (lane == 0) s_pre[wib][ncand] = total;
+    __syncwarp();
     float Lx = s.Lf[0], Ly = s.Lf[1], Lz = s.Lf[2];
     float ix = s.invLf[0], iy = s.invLf[1], iz = s.invLf[2];
     float rl2 = s.rlist2_f;
     int count = 0;
     int* out = nbr + (size_t)i * maxnb;
-    for (int a = 0; a < nz; a++)
-        for (int b = 0; b < ny; b++)
-            for (int c = 0; c < nx; c++) {
-                int cell = s.cell_begin + (sz[a] * s.ncell[1] + sy[b]) * s.ncell[0] + sx[c];
-                int lo = cell_start[cell], hi = cell_start[cell + 1];
-                for (int base = lo; base < hi; base += 32) {
-                    int idx = base + lane;
-                    bool keep = false;
-                    int j = -1;
-                    if (idx < hi) {
-                        j = cell_atoms[idx];
-                        float4 pj = wpos[j];
-                        float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-                        dx -= rintf(dx * ix) * Lx;
-                        dy -= rintf(dy * iy) * Ly;
-                        dz -= rintf(dz * iz) * Lz;
-                        float r2 = dx * dx + dy * dy + dz * dz;
-                        keep = (j != i) && (r2 < rl2);
-                    }
-                    unsigned mask = __ballot_sync(0xffffffffu, keep);
-                    if (keep) {
-                        int pos = count + __popc(mask & ((1u << lane) - 1u));
-                        if (pos < maxnb) out[pos] = j;
-                    }
-                    count += __popc(mask);
-                }
+    for (int base = 0; base < total; base += 32) {
+        int t = base + lane;
+        bool keep = false;
+        int j = -1;
+        if (t < total) {
+            // the stencil cell holding candidate t: last c with pre[c] <= t
+            int a = 0, b = ncand - 1;
+            while (a < b) {
+                int mid = (a + b + 1) >> 1;
+                if (s_pre[wib][mid] <= t) a = mid;
+                else b = mid - 1;
             }
+            j = cell_atoms[s_lo[wib][a] + (t - s_pre[wib][a])];
+            float4 pj = wpos[j];
+            float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+            dx -= rintf(dx * ix) * Lx;
+            dy -= rintf(dy * iy) * Ly;
+            dz -= rintf(dz * iz) * Lz;
+            float r2 = dx * dx + dy * dy + dz * dz;
+            keep = (j != i) && (r2 < rl2);
+        }
+        unsigned mask = __ballot_sync(0xffffffffu, keep);
+        if (keep) {
+            int pos = count + __popc(mask & ((1u << lane) - 1u));
+            if (pos < maxnb) out[pos] = j;
+        }
+        count += __popc(mask);
+    }
     if (lane == 0) {
         nnb[i] = min(count, maxnb);
         if (count > maxnb) atomicOr(status_out, ST_OVERFLOW);
@@ -217,8 +245,7 @@ void launch_nlist_build(const Batch& b, cudaStream_t st) {
     nl_scatter_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, b.status, b.sysid, b.sys_rebuild, b.atom_cell,
                                                       b.cell_count, b.cell_start, b.cell_atoms);
     nl_sort_kernel<<<b.ncells, 128, 0, st>>>(b.ncells, b.status, b.cell_start, b.cell_atoms, b.cell_count);
-    long long threads = (long long)n * 32;
-    nl_build_kernel<<<(unsigned)((threads + tb - 1) / tb), tb, 0, st>>>(
+    nl_build_kernel<<<(unsigned)((n + NL_WARPS - 1) / NL_WARPS), 32 * NL_WARPS, 0, st>>>(
         n, b.status, b.sys_rebuild, b.sysid, b.sys, b.wpos, b.atom_cell, b.cell_start, b.cell_atoms, b.maxnb,
         b.nbr, b.nnb, b.status);
     nl_done_kernel<<<1, 256, 0, st>>>(b.nsys, b.status, b.sys_rebuild);

@@ -218,23 +218,19 @@ class Engine:
 # ---------------------------------------------------------------------------
 def _angles_from_bonds(bonds: list[tuple[int, int]]) -> list[tuple[int, int, int]]:
     """Angles of a bond set as Bonding::rebuild finds them (bonding.rs:78-110):
-    every pair of bonds sharing a particle, (i, j, k) with i < k."""
+    every pair of distinct bonds sharing a particle j gives the angle (i, j, k)
+    with i < k."""
+    partners: dict[int, list[int]] = {}
+    for a, b in bonds:
+        partners.setdefault(a, []).append(b)
+        partners.setdefault(b, []).append(a)
     angles = set()
-    for b1 in bonds:
-        for b2 in bonds:
-            if b1 == b2:
-                continue
-            if b1[0] == b2[1]:
-                a = (b2[0], b2[1], b1[1])
-            elif b1[1] == b2[0]:
-                a = (b1[0], b1[1], b2[1])
-            elif b1[1] == b2[1]:
-                a = (b1[0], b1[1], b2[0])
-            elif b1[0] == b2[0]:
-                a = (b1[1], b1[0], b2[1])
-            else:
-                continue
-            angles.add((min(a[0], a[2]), a[1], max(a[0], a[2])))
+    for j, ends in partners.items():
+        for x in range(len(ends)):
+            for y in range(x + 1, len(ends)):
+                i, k = ends[x], ends[y]
+                if i != k:
+                    angles.add((min(i, k), j, max(i, k)))
     return sorted(angles)
 
 
@@ -357,7 +353,11 @@ class System:
         return sorted(set(self._bonds))
 
     def angles(self) -> list[tuple[int, int, int]]:
-        return _angles_from_bonds(self.bonds)
+        key = len(self._bonds)
+        if getattr(self, "_angles_key", None) != key:
+            self._angles_cache = _angles_from_bonds(self.bonds)
+            self._angles_key = key
+        return self._angles_cache
 
     def molecule_range(self, molid: int) -> tuple[int, int]:
         mols = self.molecules

@@ -39,10 +39,12 @@ def test_served_results_equal_alone_results():
 
 def test_admission_waits_for_memory():
     requests = workloads.serving_requests(count=6, rate=1000.0, seed=9, precision="mixed", scale=0.03)
+    for r in requests:
+        r.arrival = 0.0  # all at once: they contend for the budget
     from lumol_gb300.serving import footprint_bytes
     biggest = max(footprint_bytes(r.system, "mixed") for r in requests)
-    # a budget that holds about two requests at a time
-    server = Server(precision="mixed", chunk=20, max_lanes=4, memory_budget=2 * biggest + (1 << 20),
+    # a budget that holds the biggest request but not all of them at once
+    server = Server(precision="mixed", chunk=20, max_lanes=4, memory_budget=int(1.5 * biggest),
                     reserve_bytes=0, threads_per_atom=8)
     done = server.run(requests)
     server.close()
