@@ -211,7 +211,8 @@ struct lg_engine {
     DBuf<double4_32a> posq, vel, acc, pos_build;
     DBuf<double> force, pos3, vel3, red, host_const, lambda, ke, out, fpart, kred, mc_part;
     DBuf<int> kind, mol, sysid, spec_off, spec_j, bt_off, bt_role, nbr, nnb, atom_cell, cell_count, cell_start,
-        cell_atoms;
+        cell_atoms, cell_sys, perm;
+    DBuf<int2> km;
     DBuf<int8_t> spec_path;
     DBuf<int4> bt;
     DBuf<double2> bt_par, eikr, rho;
@@ -595,8 +596,9 @@ int commit(lg_engine* e) {
     CUDA_TRY(e, e->nnb.alloc(n));
     CUDA_TRY(e, e->atom_cell.alloc(n));
     CUDA_TRY(e, e->cell_count.alloc(cell_total));
-    CUDA_TRY(e, e->cell_start.alloc(cell_total + 1));
+    CUDA_TRY(e, e->cell_start.alloc(cell_total + nsys));  // one end sentinel per system
     CUDA_TRY(e, e->cell_atoms.alloc(n));
+    CUDA_TRY(e, e->cell_sys.alloc(cell_total));
     CUDA_TRY(e, e->wpos.alloc(n));
     CUDA_TRY(e, e->sysdev.alloc(nsys));
     CUDA_TRY(e, e->ptab.alloc(h_ptab.size()));
@@ -619,6 +621,8 @@ int commit(lg_engine* e) {
     }
     CUDA_TRY(e, e->ptabf.alloc(h_ptabf.size()));
     CUDA_TRY(e, e->posfx.alloc(mixed ? n : 1));
+    CUDA_TRY(e, e->perm.alloc(mixed ? n : 1));
+    CUDA_TRY(e, e->km.alloc(mixed ? n : 1));
     CUDA_TRY(e, e->kvecf.alloc(nkv));
     CUDA_TRY(e, e->eikrf.alloc(mixed && nkv ? (size_t)kdim * 3 * n : 1));
     CUDA_TRY(e, e->rhof.alloc(nkv));
@@ -652,6 +656,19 @@ int commit(lg_engine* e) {
                                     cudaMemcpyHostToDevice, st));
     }
     CUDA_TRY(e, cudaMemsetAsync(e->cell_count.p, 0, cell_total * sizeof(int), st));
+    // the cell order starts as the identity (every system rebuilds before its first use)
+    std::vector<int> h_iota(n), h_cell_sys(cell_total);
+    for (int64_t i = 0; i < (int64_t)n; i++) h_iota[i] = (int)i;
+    for (int s = 0; s < nsys; s++) {
+        const SysDev& d = e->h_sysdev[s];
+        int nc = d.ncell[0] * d.ncell[1] * d.ncell[2];
+        for (int c = 0; c < nc; c++) h_cell_sys[d.cell_begin + c] = s;
+    }
+    CUDA_TRY(e, cudaMemcpyAsync(e->cell_atoms.p, h_iota.data(), n * sizeof(int), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(e, cudaMemcpyAsync(e->cell_sys.p, h_cell_sys.data(), cell_total * sizeof(int), cudaMemcpyHostToDevice,
+                                st));
+    if (mixed)
+        CUDA_TRY(e, cudaMemcpyAsync(e->perm.p, h_iota.data(), n * sizeof(int), cudaMemcpyHostToDevice, st));
     CUDA_TRY(e, cudaMemsetAsync(e->nnb.p, 0, n * sizeof(int), st));
     CUDA_TRY(e, cudaMemcpyAsync(e->sysdev.p, e->h_sysdev.data(), nsys * sizeof(SysDev), cudaMemcpyHostToDevice, st));
     CUDA_TRY(e, cudaMemcpyAsync(e->ptab.p, h_ptab.data(), h_ptab.size() * sizeof(PairDev), cudaMemcpyHostToDevice, st));
@@ -703,6 +720,9 @@ int commit(lg_engine* e) {
     b.cell_count = e->cell_count.p;
     b.cell_start = e->cell_start.p;
     b.cell_atoms = e->cell_atoms.p;
+    b.cell_sys = e->cell_sys.p;
+    b.perm = mixed ? e->perm.p : nullptr;
+    b.km = mixed ? e->km.p : nullptr;
     b.wpos = e->wpos.p;
     b.pos_build = e->pos_build.p;
     b.status = e->status.p;
@@ -761,16 +781,19 @@ int clear_status_bits(lg_engine* e, uint32_t bits) {
     return LG_OK;
 }
 
+// Kernels launch_nlist_build enqueues.
+int nlist_launches(const Batch& b) { return b.n ? (b.perm ? 7 : 6) : 0; }
+
 // Forces (and energies / virials) of the whole batch at the positions in posq.
 void enqueue_forces(lg_engine* e, uint32_t terms, bool ev, cudaStream_t st) {
     const Batch& b = e->b;
     if (b.n == 0) return;
-    if (b.precision == LG_PRECISION_MIXED) {
+    launch_nlist_build(b, st);
+    e->launches += nlist_launches(b);
+    if (b.precision == LG_PRECISION_MIXED) {  // fixed-point copy in the order of the current list
         launch_split_positions(b, st);
         e->launches += 1;
     }
-    launch_nlist_build(b, st);
-    e->launches += 6;
     if (terms & (LG_TERM_PAIRS | LG_TERM_COUL_REAL)) {
         launch_pair_forces(b, terms, ev, st);
         e->launches += 1;
@@ -1235,8 +1258,8 @@ int autotune(lg_engine* e) {
     CUDA_TRY(e, cudaEventCreate(&e1));
     // a current list for the timing
     launch_check_displacement(b, st);
-    if (b.precision == LG_PRECISION_MIXED) launch_split_positions(b, st);
     launch_nlist_build(b, st);
+    if (b.precision == LG_PRECISION_MIXED) launch_split_positions(b, st);
     auto time_it = [&](auto&& launch) -> float {
         launch();  // warm
         float best = 1e30f;
@@ -1666,7 +1689,7 @@ int lg_mc_run(lg_engine* e, int64_t moves) {
     // the list must be current for the positions the chains start from
     launch_check_displacement(e->b, st);
     launch_nlist_build(e->b, st);
-    e->launches += 7;
+    e->launches += 1 + nlist_launches(e->b);
     for (int64_t launch = 0; launch < moves + 64; launch++) {
         launch_mc_chains(e->b, e->mc_chains.p, fp64, st);
         e->launches += 1;
@@ -1682,12 +1705,23 @@ int lg_mc_run(lg_engine* e, int64_t moves) {
         }
         if (!pending) return LG_OK;
         if (rebuild) {
-            for (int s = 0; s < nsys; s++) e->h_mc[s].need_rebuild = 0;
+            // rebuild the lists of the stopped chains' systems only
+            std::vector<uint32_t> flags(nsys, 0u);
+            for (int s = 0; s < nsys; s++) {
+                flags[s] = e->h_mc[s].need_rebuild ? 1u : 0u;
+                e->h_mc[s].need_rebuild = 0;
+            }
             CUDA_TRY(e, cudaMemcpyAsync(e->mc_chains.p, e->h_mc.data(), nsys * sizeof(McState),
                                         cudaMemcpyHostToDevice, st));
-            launch_request_rebuild(e->b, st);
+            CUDA_TRY(e, cudaMemcpyAsync(e->sys_rebuild.p, flags.data(), nsys * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                        st));
+            uint32_t rebuild_bit = ST_REBUILD;
+            CUDA_TRY(e, cudaMemcpyAsync(e->h_status, e->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+            CUDA_TRY(e, cudaStreamSynchronize(st));
+            *e->h_status |= rebuild_bit;
+            CUDA_TRY(e, cudaMemcpyAsync(e->status.p, e->h_status, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
             launch_nlist_build(e->b, st);
-            e->launches += 7;
+            e->launches += nlist_launches(e->b);
             uint32_t status;
             int rc = read_status(e, &status);
             if (rc) return rc;

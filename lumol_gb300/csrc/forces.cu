@@ -548,6 +548,7 @@ __global__ void pairset_kernel(int n, int family, int a_begin, int a_end, const 
                                const PairDev* __restrict__ ptab, const int* __restrict__ nbr,
                                const int* __restrict__ nnb, int maxnb, const int* __restrict__ spec_off,
                                const int* __restrict__ spec_j, const int8_t* __restrict__ spec_path,
+                               const int* __restrict__ perm, const int* __restrict__ cell_atoms,
                                int* __restrict__ out, long long cap, unsigned long long* count) {
     int i = a_begin + blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a_end) return;
@@ -555,8 +556,11 @@ __global__ void pairset_kernel(int n, int family, int a_begin, int a_end, const 
     double4_32a pi = posq[i];
     int ki = kind[i], mi = mol[i];
     uint32_t terms = family == 0 ? 1u : 16u;
-    for (int k = 0; k < nnb[i]; k++) {
-        int j = nbr[(size_t)i * maxnb + k];
+    // a cell-sorted list (mixed engines) holds sorted positions: map back to atoms
+    int row = perm ? perm[i] : i;
+    for (int k = 0; k < nnb[row]; k++) {
+        int j = nbr[(size_t)row * maxnb + k];
+        if (perm) j = cell_atoms[j];
         if (j <= i) continue;
         double4_32a pj = posq[j];
         double dx, dy, dz;
@@ -582,7 +586,8 @@ void launch_pairset(const Batch& b, int family, int a_begin, int a_end, int* out
     if (na <= 0) return;
     pairset_kernel<<<(na + tb - 1) / tb, tb, 0, st>>>(b.n, family, a_begin, a_end, b.posq, b.kind, b.mol,
                                                       b.sysid, b.sys, b.ptab, b.nbr, b.nnb, b.maxnb,
-                                                      b.spec_off, b.spec_j, b.spec_path, out, cap, count);
+                                                      b.spec_off, b.spec_j, b.spec_path, b.perm, b.cell_atoms,
+                                                      out, cap, count);
 }
 
 }  // namespace lg

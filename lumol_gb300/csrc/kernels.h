@@ -40,8 +40,11 @@ struct Batch {
     int* nnb = nullptr;           // n
     int* atom_cell = nullptr;
     int* cell_count = nullptr;    // ncells
-    int* cell_start = nullptr;    // ncells + 1
-    int* cell_atoms = nullptr;    // n
+    int* cell_start = nullptr;    // ncells + nsys: per system, its cells then an end sentinel
+    int* cell_sys = nullptr;      // ncells: system of each cell
+    int* perm = nullptr;          // n: cell-sorted position of each atom (mixed path; null for FP64)
+    int2* km = nullptr;           // n: (kind, molecule) in cell-sorted order (mixed path)
+    int* cell_atoms = nullptr;    // n: atoms in cell order, per system at [begin, end)
     float4* wpos = nullptr;       // wrapped FP32 positions at build, charge
     double4_32a* pos_build = nullptr; // positions at the last build
     uint32_t* status = nullptr;   // ST_* bits

@@ -323,10 +323,12 @@ __global__ void __launch_bounds__(128) mc_chain_kernel(Batch b, McState* __restr
         const PairDev* prow = b.ptab + sd.ptab + ki * sd.nk;
         const PairDevF* prowf = b.ptabf + sd.ptab + ki * sd.nk;
         double de = 0.0;
-        int cnt = b.nnb[i];
-        const int* list = b.nbr + (size_t)i * b.maxnb;
+        // a cell-sorted list (mixed engines) holds sorted positions: map back to atoms
+        int row = b.perm ? b.perm[i] : i;
+        int cnt = b.nnb[row];
+        const int* list = b.nbr + (size_t)row * b.maxnb;
         for (int k = lane; k < cnt; k += 32) {
-            int j = list[k];
+            int j = b.perm ? b.cell_atoms[list[k]] : list[k];
             double4_32a pj = b.posq[j];
             int kj = b.kind[j];
             const PairDev& p = prow[kj];

@@ -73,6 +73,16 @@ void launch_unpack_velocities(const Batch& b, double* vel3, cudaStream_t st) {
 // v += 0.5 dt a; x += v dt (integrators.rs:48-53), then the displacement
 // since the last list build against skin / 2.  Also clears the force buffer
 // that the force kernels accumulate into.
+// Marks system si for a list rebuild.  The flag store is idempotent; the
+// status word gets one atomic per warp, not one per moved atom.
+__device__ __forceinline__ void flag_rebuild(bool moved, int si, uint32_t* status, uint32_t* sys_rebuild) {
+    unsigned mask = __ballot_sync(__activemask(), moved);
+    if (moved) {
+        sys_rebuild[si] = 1u;
+        if ((threadIdx.x & 31) == __ffs(mask) - 1) atomicOr(status, ST_REBUILD);
+    }
+}
+
 __global__ void vv_first_kernel(int n, const int* __restrict__ sysid, const SysDev* __restrict__ sys,
                                 double4_32a* __restrict__ posq, double4_32a* __restrict__ vel,
                                 const double4_32a* __restrict__ acc, const double4_32a* __restrict__ pos_build,
@@ -95,29 +105,35 @@ __global__ void vv_first_kernel(int n, const int* __restrict__ sysid, const SysD
     force[3 * i] = 0.0;
     force[3 * i + 1] = 0.0;
     force[3 * i + 2] = 0.0;
+    // displacement since the list build, in FP32 against a threshold 1 % below
+    // (skin / 2)^2: the FP32 rounding only ever triggers a rebuild early
     double4_32a b = pos_build[i];
-    double dx = p.x - b.x, dy = p.y - b.y, dz = p.z - b.z;
-    dx -= rint(dx * s.invL[0]) * s.L[0];
-    dy -= rint(dy * s.invL[1]) * s.L[1];
-    dz -= rint(dz * s.invL[2]) * s.L[2];
-    if (dx * dx + dy * dy + dz * dz > s.half_skin2) {
-        sys_rebuild[si] = 1u;
-        atomicOr(status, ST_REBUILD);
-    }
+    float dx = (float)(p.x - b.x), dy = (float)(p.y - b.y), dz = (float)(p.z - b.z);
+    dx -= rintf(dx * s.invLf[0]) * s.Lf[0];
+    dy -= rintf(dy * s.invLf[1]) * s.Lf[1];
+    dz -= rintf(dz * s.invLf[2]) * s.Lf[2];
+    flag_rebuild(dx * dx + dy * dy + dz * dz > 0.99f * (float)s.half_skin2, si, status, sys_rebuild);
 }
 
 // a = F / m; v += 0.5 dt a (integrators.rs:55-68); kinetic energy per atom
 // for the thermostat (compute.rs:133-144).
 __global__ void vv_second_kernel(int n, const int* __restrict__ sysid, const SysDev* __restrict__ sys,
                                  const double* __restrict__ force, double4_32a* __restrict__ vel,
-                                 double4_32a* __restrict__ acc, double* __restrict__ ke, int thermostat) {
+                                 double4_32a* __restrict__ acc, double* __restrict__ ke, int thermostat,
+                                 int exact_division) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const SysDev& s = sys[sysid[i]];
     double hdt = __dmul_rn(0.5, s.dt);
     double4_32a v = vel[i];
     double m = v.w;
-    double4_32a a = make_double4_32a(force[3 * i] / m, force[3 * i + 1] / m, force[3 * i + 2] / m, 0.0);
+    double4_32a a;
+    if (exact_division) {  // the reference's force / mass
+        a = make_double4_32a(force[3 * i] / m, force[3 * i + 1] / m, force[3 * i + 2] / m, 0.0);
+    } else {  // mixed path: one reciprocal per atom
+        double im = 1.0 / m;
+        a = make_double4_32a(force[3 * i] * im, force[3 * i + 1] * im, force[3 * i + 2] * im, 0.0);
+    }
     v.x = __dadd_rn(v.x, __dmul_rn(hdt, a.x));
     v.y = __dadd_rn(v.y, __dmul_rn(hdt, a.y));
     v.z = __dadd_rn(v.z, __dmul_rn(hdt, a.z));
@@ -177,10 +193,7 @@ __global__ void check_displacement_kernel(int n, const int* __restrict__ sysid, 
     dx -= rint(dx * s.invL[0]) * s.L[0];
     dy -= rint(dy * s.invL[1]) * s.L[1];
     dz -= rint(dz * s.invL[2]) * s.L[2];
-    if (!(dx * dx + dy * dy + dz * dz <= s.half_skin2)) {
-        sys_rebuild[si] = 1u;
-        atomicOr(status, ST_REBUILD);
-    }
+    flag_rebuild(!(dx * dx + dy * dy + dz * dz <= s.half_skin2), si, status, sys_rebuild);
 }
 
 void launch_check_displacement(const Batch& b, cudaStream_t st) {
@@ -202,7 +215,7 @@ void launch_vv_first(const Batch& b, cudaStream_t st) {
 void launch_vv_second(const Batch& b, bool thermostat, cudaStream_t st) {
     if (b.n)
         vv_second_kernel<<<(b.n + 255) / 256, 256, 0, st>>>(b.n, b.sysid, b.sys, b.force, b.vel, b.acc, b.ke,
-                                                          thermostat ? 1 : 0);
+                                                          thermostat ? 1 : 0, b.precision == 0 ? 1 : 0);
 }
 void launch_thermostat(const Batch& b, cudaStream_t st) {
     if (b.n == 0) return;

@@ -17,6 +17,11 @@
 // Threads per atom (TPA = 1..32) is a template parameter chosen per workload
 // by the autotuner: the TPA lanes of a group walk one atom's neighbour list
 // and combine their compensated partial sums with shuffles.
+//
+// The kernels walk each system's atoms in the cell-sorted order of the last
+// list build (rows, list entries, fixed-point positions and (kind, molecule)
+// are all in that order), so the neighbours of consecutive atoms share cache
+// lines; forces are written back to each atom's own index.
 #include "kernels.h"
 
 namespace lg {
@@ -83,20 +88,23 @@ __device__ __forceinline__ float pair_mixed(const PairDevF& p, float r2, float i
 
 template <int TPA, bool EV>
 __global__ void __launch_bounds__(256) pair_mixed_kernel(
-    int n, const uint4* __restrict__ pfx, const int* __restrict__ kind,
-    const int* __restrict__ mol, const int* __restrict__ sysid, const SysDev* __restrict__ sys,
+    int n, const uint4* __restrict__ pfx, const int2* __restrict__ km, const int* __restrict__ order,
+    const int* __restrict__ sysid, const SysDev* __restrict__ sys,
     const PairDevF* __restrict__ ptab, const int* __restrict__ nbr, const int* __restrict__ nnb, int maxnb,
     const int* __restrict__ spec_off, const int* __restrict__ spec_j, const int8_t* __restrict__ spec_path,
     uint32_t terms, double* __restrict__ force, double* __restrict__ red) {
+    // t walks the cell-sorted order; i is the atom's own index (forces, bond paths)
     int gt = blockIdx.x * blockDim.x + threadIdx.x;
-    int i = gt / TPA;
+    int t = gt / TPA;
     int sub = gt % TPA;
-    bool active = i < n;
-    int ii = active ? i : n - 1;
-    const SysDev& s = sys[sysid[ii]];
-    uint4 pi = pfx[ii];
+    bool active = t < n;
+    int tt = active ? t : n - 1;
+    int i = order[tt];
+    const SysDev& s = sys[sysid[tt]];
+    uint4 pi = pfx[tt];
     float qi = __uint_as_float(pi.w);
-    int ki = kind[ii], mi = mol[ii];
+    int2 kmi = km[tt];
+    int ki = kmi.x, mi = kmi.y;
     const PairDevF* prow = ptab + s.ptab + ki * s.nk;
     float sc0 = s.Lq[0], sc1 = s.Lq[1], sc2 = s.Lq[2];
     bool coul = (terms & 16u) && s.coul != 0 && qi != 0.0f;
@@ -107,25 +115,27 @@ __global__ void __launch_bounds__(256) pair_mixed_kernel(
     float fxs = 0.f, fxc = 0.f, fys = 0.f, fyc = 0.f, fzs = 0.f, fzc = 0.f;
     double ep = 0.0, ec = 0.0;
     double w0 = 0, w1 = 0, w2 = 0, w3 = 0, w4 = 0, w5 = 0;
-    int cnt = active ? nnb[ii] : 0;
-    const int* list = nbr + (size_t)ii * maxnb;
+    int cnt = active ? nnb[tt] : 0;
+    const int* list = nbr + (size_t)tt * maxnb;
     for (int k = sub; k < cnt; k += TPA) {
-        int j = list[k];
-        uint4 pj = pfx[j];
+        int js = list[k];  // sorted position of the neighbour
+        uint4 pj = pfx[js];
         float qj = __uint_as_float(pj.w);
         float dx = fixed_image(pi.x, pj.x, sc0);
         float dy = fixed_image(pi.y, pj.y, sc1);
         float dz = fixed_image(pi.z, pj.z, sc2);
         float r2 = dx * dx + dy * dy + dz * dz;
-        const PairDevF& p = prow[kind[j]];
+        int2 kmj = km[js];
+        const PairDevF& p = prow[kmj.x];
         bool pin = pairs && p.type != 0 && r2 < p.rc2;
         bool cin = coul && qj != 0.0f && r2 <= coul_rc2;
         if (!(pin || cin)) continue;
         int path = -1;
-        int mj = mol[j];
+        int mj = kmj.y;
         float sc = 1.0f;
         if (pin && p.restriction != 0) {
-            path = p.restriction <= 2 ? (mi != mj ? 0 : 5) : bond_path(i, j, mi, mj, spec_off, spec_j, spec_path);
+            path = p.restriction <= 2 ? (mi != mj ? 0 : 5)
+                                      : bond_path(i, order[js], mi, mj, spec_off, spec_j, spec_path);
             if (restriction_excluded(p.restriction, path)) pin = false;
             else sc = p.restriction == 6 && path == 4 ? p.scale14 : 1.0f;
         }
@@ -144,7 +154,7 @@ __global__ void __launch_bounds__(256) pair_mixed_kernel(
             if (s.coul_restr != 0) {
                 if (path < 0 || (s.coul_restr > 2 && path == 5))
                     path = s.coul_restr <= 2 ? (mi != mj ? 0 : 5)
-                                             : bond_path(i, j, mi, mj, spec_off, spec_j, spec_path);
+                                             : bond_path(i, order[js], mi, mj, spec_off, spec_j, spec_path);
                 excl = restriction_excluded(s.coul_restr, path);
                 if (s.coul_restr == 6 && path == 4) csc = (float)s.coul_scale14;
             }
@@ -173,7 +183,7 @@ __global__ void __launch_bounds__(256) pair_mixed_kernel(
         two_sum_acc(fxs, fxc, gx);
         two_sum_acc(fys, fyc, gy);
         two_sum_acc(fzs, fzc, gz);
-        if (EV && j > i) {
+        if (EV && js > tt) {  // each unordered pair once (the list is symmetric)
             ep += (double)e_pair;
             ec += (double)e_coul;
             w0 += (double)(gx * dx);
@@ -223,11 +233,11 @@ void launch_pair_mixed_tpa(const Batch& b, uint32_t terms, bool ev, cudaStream_t
     long long threads = (long long)b.n * TPA;
     unsigned grid = (unsigned)((threads + tb - 1) / tb);
     if (ev)
-        pair_mixed_kernel<TPA, true><<<grid, tb, 0, st>>>(b.n, b.posfx, b.kind, b.mol, b.sysid, b.sys,
+        pair_mixed_kernel<TPA, true><<<grid, tb, 0, st>>>(b.n, b.posfx, b.km, b.cell_atoms, b.sysid, b.sys,
                                                           b.ptabf, b.nbr, b.nnb, b.maxnb, b.spec_off, b.spec_j,
                                                           b.spec_path, terms, b.force, b.red);
     else
-        pair_mixed_kernel<TPA, false><<<grid, tb, 0, st>>>(b.n, b.posfx, b.kind, b.mol, b.sysid, b.sys,
+        pair_mixed_kernel<TPA, false><<<grid, tb, 0, st>>>(b.n, b.posfx, b.km, b.cell_atoms, b.sysid, b.sys,
                                                            b.ptabf, b.nbr, b.nnb, b.maxnb, b.spec_off, b.spec_j,
                                                            b.spec_path, terms, b.force, b.red);
 }
@@ -247,11 +257,12 @@ void launch_pair_mixed(const Batch& b, uint32_t terms, bool ev, cudaStream_t st)
 // Fixed-point copy of the wrapped FP64 positions (UnitCell::wrap_vector):
 // u = floor(frac(x / L) * 2^32), and the charge's FP32 bits.
 __global__ void fixed_positions_kernel(int n, const double4_32a* __restrict__ posq, const int* __restrict__ sysid,
-                                       const SysDev* __restrict__ sys, uint4* __restrict__ pfx) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const SysDev& s = sys[sysid[i]];
-    double4_32a p = posq[i];
+                                       const SysDev* __restrict__ sys, const int* __restrict__ order,
+                                       uint4* __restrict__ pfx) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;  // cell-sorted position
+    if (t >= n) return;
+    const SysDev& s = sys[sysid[t]];
+    double4_32a p = posq[order[t]];
     double w[3] = {p.x, p.y, p.z};
     uint32_t u[3];
     for (int d = 0; d < 3; d++) {
@@ -260,12 +271,13 @@ __global__ void fixed_positions_kernel(int n, const double4_32a* __restrict__ po
         unsigned long long q = (unsigned long long)(f * 4294967296.0);
         u[d] = (uint32_t)(q & 0xffffffffull);
     }
-    pfx[i] = make_uint4(u[0], u[1], u[2], __float_as_uint((float)p.w));
+    pfx[t] = make_uint4(u[0], u[1], u[2], __float_as_uint((float)p.w));
 }
 
 void launch_split_positions(const Batch& b, cudaStream_t st) {
     if (b.n && b.posfx)
-        fixed_positions_kernel<<<(b.n + 255) / 256, 256, 0, st>>>(b.n, b.posq, b.sysid, b.sys, b.posfx);
+        fixed_positions_kernel<<<(b.n + 255) / 256, 256, 0, st>>>(b.n, b.posq, b.sysid, b.sys, b.cell_atoms,
+                                                                  b.posfx);
 }
 
 // ---------------------------------------------------------------------------

@@ -45,33 +45,42 @@ __global__ void nl_bin_kernel(int n, const double4_32a* __restrict__ posq, const
     pos_build[i] = p;
 }
 
-// Exclusive scan of the cell counts (single block).  Also zeroes the fill
-// counters used by the scatter pass.
-__global__ void nl_scan_kernel(int ncells, const uint32_t* __restrict__ status,
-                               int* __restrict__ cell_count, int* __restrict__ cell_start) {
+// Exclusive scan of the cell counts of one system (one block per rebuilding
+// system).  A system's cells hold its atoms at [begin, end) of cell_atoms, and
+// its start array has one slot per cell plus an end sentinel, at
+// cell_start[cell + system index].  Also zeroes the counts for the scatter.
+__global__ void __launch_bounds__(1024) nl_scan_kernel(int nsys, const uint32_t* __restrict__ status,
+                                                       const uint32_t* __restrict__ sys_rebuild,
+                                                       const SysDev* __restrict__ sys, int* __restrict__ cell_count,
+                                                       int* __restrict__ cell_start) {
     if (!(*status & ST_REBUILD)) return;
+    int s = blockIdx.x;
+    if (!sys_rebuild[s]) return;
     __shared__ int partial[1024];
+    const SysDev& d = sys[s];
+    int ncells = d.ncell[0] * d.ncell[1] * d.ncell[2];
+    int* count = cell_count + d.cell_begin;
+    int* start = cell_start + d.cell_begin + s;
     int t = threadIdx.x;
     int per = (ncells + blockDim.x - 1) / blockDim.x;
     int lo = min(t * per, ncells), hi = min(lo + per, ncells);
     int sum = 0;
-    for (int c = lo; c < hi; c++) sum += cell_count[c];
+    for (int c = lo; c < hi; c++) sum += count[c];
     partial[t] = sum;
     __syncthreads();
-    // Hillis-Steele inclusive scan over the per-thread sums
     for (int o = 1; o < (int)blockDim.x; o <<= 1) {
         int v = t >= o ? partial[t - o] : 0;
         __syncthreads();
         partial[t] += v;
         __syncthreads();
     }
-    int run = partial[t] - sum;
+    int run = d.begin + partial[t] - sum;
     for (int c = lo; c < hi; c++) {
-        cell_start[c] = run;
-        run += cell_count[c];
-        cell_count[c] = 0;
+        start[c] = run;
+        run += count[c];
+        count[c] = 0;
     }
-    if (t == blockDim.x - 1) cell_start[ncells] = partial[t];
+    if (t == blockDim.x - 1) start[ncells] = d.begin + partial[t];
 }
 
 __global__ void nl_scatter_kernel(int n, const uint32_t* __restrict__ status, const int* __restrict__ sysid,
@@ -80,10 +89,12 @@ __global__ void nl_scatter_kernel(int n, const uint32_t* __restrict__ status, co
                                   int* __restrict__ cell_atoms) {
     if (!(*status & ST_REBUILD)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || !sys_rebuild[sysid[i]]) return;
+    if (i >= n) return;
+    int s = sysid[i];
+    if (!sys_rebuild[s]) return;
     int c = atom_cell[i];
     int slot = atomicAdd(&cell_count[c], 1);
-    cell_atoms[cell_start[c] + slot] = i;
+    cell_atoms[cell_start[c + s] + slot] = i;
 }
 
 // Sort each cell's atoms by index so that the list order (and so the order of
@@ -92,13 +103,17 @@ __global__ void nl_scatter_kernel(int n, const uint32_t* __restrict__ status, co
 constexpr int SORT_SMEM = 2048;
 
 __global__ void __launch_bounds__(128) nl_sort_kernel(int ncells, const uint32_t* __restrict__ status,
+                                                      const uint32_t* __restrict__ sys_rebuild,
+                                                      const int* __restrict__ cell_sys,
                                                       const int* __restrict__ cell_start,
                                                       int* __restrict__ cell_atoms, int* __restrict__ cell_count) {
     if (!(*status & ST_REBUILD)) return;
     __shared__ int buf[SORT_SMEM];
     int c = blockIdx.x;
+    int s = cell_sys[c];
     if (threadIdx.x == 0) cell_count[c] = 0;  // ready for the next binning pass
-    int lo = cell_start[c], hi = cell_start[c + 1];
+    if (!sys_rebuild[s]) return;
+    int lo = cell_start[c + s], hi = cell_start[c + s + 1];
     int m = hi - lo;
     if (m <= 1) return;
     if (m <= SORT_SMEM) {
@@ -121,6 +136,20 @@ __global__ void __launch_bounds__(128) nl_sort_kernel(int ncells, const uint32_t
             cell_atoms[b + 1] = v;
         }
     }
+}
+
+// Position of every atom in the cell-sorted order (perm) and the sorted copies
+// of kind and molecule the mixed kernels read.  Systems that did not rebuild
+// keep their order, so rewriting their entries changes nothing.
+__global__ void nl_perm_kernel(int n, const uint32_t* __restrict__ status, const int* __restrict__ cell_atoms,
+                               const int* __restrict__ kind, const int* __restrict__ mol, int* __restrict__ perm,
+                               int2* __restrict__ km) {
+    if (!(*status & ST_REBUILD)) return;
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    int i = cell_atoms[t];
+    perm[i] = t;
+    km[t] = make_int2(kind[i], mol[i]);
 }
 
 // Stencil cells of one dimension: c-1, c, c+1 (periodic) when there are at
@@ -147,17 +176,19 @@ constexpr int NL_WARPS = 8;
 __global__ void __launch_bounds__(32 * NL_WARPS) nl_build_kernel(
     int n, const uint32_t* status, const uint32_t* __restrict__ sys_rebuild, const int* __restrict__ sysid,
     const SysDev* __restrict__ sys, const float4* __restrict__ wpos, const int* __restrict__ atom_cell,
-    const int* __restrict__ cell_start, const int* __restrict__ cell_atoms, int maxnb, int* __restrict__ nbr,
-    int* __restrict__ nnb, uint32_t* status_out) {
+    const int* __restrict__ cell_start, const int* __restrict__ cell_atoms, const int* __restrict__ perm,
+    int maxnb, int* __restrict__ nbr, int* __restrict__ nnb, uint32_t* status_out) {
     __shared__ int s_lo[NL_WARPS][28];
     __shared__ int s_pre[NL_WARPS][28];
     if (!(*status & ST_REBUILD)) return;
     int wib = threadIdx.x >> 5;
-    int i = blockIdx.x * NL_WARPS + wib;
+    int w = blockIdx.x * NL_WARPS + wib;
     int lane = threadIdx.x & 31;
-    if (i >= n) return;
-    if (!sys_rebuild[sysid[i]]) return;  // this system keeps its list
-    const SysDev& s = sys[sysid[i]];
+    if (w >= n) return;
+    int i = cell_atoms[w];  // warps walk the atoms cell by cell: neighbouring warps share a stencil
+    int si = sysid[i];
+    if (!sys_rebuild[si]) return;  // this system keeps its list
+    const SysDev& s = sys[si];
     float4 pi = wpos[i];
     int local = atom_cell[i] - s.cell_begin;
     int cx = local % s.ncell[0];
@@ -173,8 +204,8 @@ __global__ void __launch_bounds__(32 * NL_WARPS) nl_build_kernel(
     if (lane < ncand) {
         int a = lane / (nx * ny), b = (lane / nx) % ny, c = lane % nx;
         int cell = s.cell_begin + (sz[a] * s.ncell[1] + sy[b]) * s.ncell[0] + sx[c];
-        lo = cell_start[cell];
-        cnt = cell_start[cell + 1] - lo;
+        lo = cell_start[cell + si];
+        cnt = cell_start[cell + si + 1] - lo;
     }
     int incl = cnt;
     for (int o = 1; o < 32; o <<= 1) {
@@ -192,11 +223,13 @@ __global__ void __launch_bounds__(32 * NL_WARPS) nl_build_kernel(
     float ix = s.invLf[0], iy = s.invLf[1], iz = s.invLf[2];
     float rl2 = s.rlist2_f;
     int count = 0;
-    int* out = nbr + (size_t)i * maxnb;
+    // with a cell-sorted order (mixed path) the row and its entries are sorted positions
+    int row = perm ? perm[i] : i;
+    int* out = nbr + (size_t)row * maxnb;
     for (int base = 0; base < total; base += 32) {
         int t = base + lane;
         bool keep = false;
-        int j = -1;
+        int j = -1, jout = -1;
         if (t < total) {
             // the stencil cell holding candidate t: last c with pre[c] <= t
             int a = 0, b = ncand - 1;
@@ -205,7 +238,9 @@ __global__ void __launch_bounds__(32 * NL_WARPS) nl_build_kernel(
                 if (s_pre[wib][mid] <= t) a = mid;
                 else b = mid - 1;
             }
-            j = cell_atoms[s_lo[wib][a] + (t - s_pre[wib][a])];
+            int slot = s_lo[wib][a] + (t - s_pre[wib][a]);
+            j = cell_atoms[slot];
+            jout = perm ? slot : j;
             float4 pj = wpos[j];
             float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             dx -= rintf(dx * ix) * Lx;
@@ -217,12 +252,12 @@ __global__ void __launch_bounds__(32 * NL_WARPS) nl_build_kernel(
         unsigned mask = __ballot_sync(0xffffffffu, keep);
         if (keep) {
             int pos = count + __popc(mask & ((1u << lane) - 1u));
-            if (pos < maxnb) out[pos] = j;
+            if (pos < maxnb) out[pos] = jout;
         }
         count += __popc(mask);
     }
     if (lane == 0) {
-        nnb[i] = min(count, maxnb);
+        nnb[row] = min(count, maxnb);
         if (count > maxnb) atomicOr(status_out, ST_OVERFLOW);
     }
 }
@@ -241,13 +276,16 @@ void launch_nlist_build(const Batch& b, cudaStream_t st) {
     int tb = 256;
     nl_bin_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, b.posq, b.sysid, b.sys, b.status, b.sys_rebuild,
                                                   b.atom_cell, b.cell_count, b.wpos, b.pos_build);
-    nl_scan_kernel<<<1, 1024, 0, st>>>(b.ncells, b.status, b.cell_count, b.cell_start);
+    nl_scan_kernel<<<b.nsys, 1024, 0, st>>>(b.nsys, b.status, b.sys_rebuild, b.sys, b.cell_count, b.cell_start);
     nl_scatter_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, b.status, b.sysid, b.sys_rebuild, b.atom_cell,
                                                       b.cell_count, b.cell_start, b.cell_atoms);
-    nl_sort_kernel<<<b.ncells, 128, 0, st>>>(b.ncells, b.status, b.cell_start, b.cell_atoms, b.cell_count);
+    nl_sort_kernel<<<b.ncells, 128, 0, st>>>(b.ncells, b.status, b.sys_rebuild, b.cell_sys, b.cell_start,
+                                             b.cell_atoms, b.cell_count);
+    if (b.perm)
+        nl_perm_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, b.status, b.cell_atoms, b.kind, b.mol, b.perm, b.km);
     nl_build_kernel<<<(unsigned)((n + NL_WARPS - 1) / NL_WARPS), 32 * NL_WARPS, 0, st>>>(
-        n, b.status, b.sys_rebuild, b.sysid, b.sys, b.wpos, b.atom_cell, b.cell_start, b.cell_atoms, b.maxnb,
-        b.nbr, b.nnb, b.status);
+        n, b.status, b.sys_rebuild, b.sysid, b.sys, b.wpos, b.atom_cell, b.cell_start, b.cell_atoms, b.perm,
+        b.maxnb, b.nbr, b.nnb, b.status);
     nl_done_kernel<<<1, 256, 0, st>>>(b.nsys, b.status, b.sys_rebuild);
 }
 
