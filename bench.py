@@ -1,17 +1,27 @@
 #!/usr/bin/env python
-"""Benchmark of the GB300 engine on Lumol's MD hot path.
+"""Benchmark of the GB300 engine on Lumol's MD / MC hot path.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload nacl_ewald|argon|water] [--precision fp64|mixed]
+                    [--workload lj_batch|serving|nacl_ewald|argon|water] [--precision mixed|fp64]
 
-A step is one Velocity-Verlet MD step (integrate: half kick, drift, forces,
-half kick) of the workload, with the state resident on the GPU.  `value` is
-atom-steps/s of the whole job (all ranks), timed with CUDA events on the
-engine's stream, one timed iteration being one lg_md_run call of `--chunk`
-MD steps (the engine's own chunk length); the L2 cache is flushed (256 MiB
-write) before every timed iteration because the workloads fit in L2.  `e2e` is the same metric through the
-public C ABI call Lumol's Integrator would make (lg_md_integrate), with the
-positions and velocities copied from pinned host memory and back every step.
+Default workload (lj_batch): 256 seeded argon-type LJ replicas of uneven size
+(64..4096 atoms), half running NVT Velocity-Verlet MD in one engine, half
+running NVT Monte Carlo Translate chains in another; one batched step is one
+Lumol step of every replica (an MD step of each MD replica, one move of each
+chain), and `value` is atom-steps/s (MD atoms + MC chains per step) of the
+whole job, timed with CUDA events on the engines' streams.  With the mixed
+path (default) the line also carries the plain FP64 path's value on the same
+workload (`fp64_plain`, with the ratio) and the mixed path's error against
+FP64 (`accuracy`: relative force RMS, energy and virial errors, NVE drift of
+both paths).
+
+The single-system workloads (nacl_ewald, argon, water) time one lg_md_run
+call of `--chunk` MD steps per iteration, with the L2 cache flushed (256 MiB
+write) before every timed iteration because those workloads fit in L2.  The
+serving workload replays a seeded Poisson stream of mixed MD requests through
+the continuous-batching server and reports throughput and p50 / p99 latency.
+`e2e` is the same metric through the public C ABI with the state copied from
+pinned host memory and back every step.
 
 `--impl reference` times the reference algorithm on the host cores: the CPU
 oracle (a C++ restatement of lumol-core's O(N^2) loops, OpenMP over all
@@ -48,12 +58,14 @@ def parse():
     p.add_argument("--requests", type=int, default=48, help="serving: number of requests")
     p.add_argument("--rate", type=float, default=40.0, help="serving: Poisson arrival rate (1/s)")
     p.add_argument("--replicas", type=int, default=256, help="lj_batch: replicas (half MD, half MC)")
-    p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    p.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     p.add_argument("--cells", type=int, default=0, help="lattice cells per side (0: the workload's size)")
     p.add_argument("--chunk", type=int, default=16, help="MD steps per timed iteration (one lg_md_run call)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-roofline", action="store_true")
+    p.add_argument("--no-accuracy", action="store_true", help="skip the mixed-vs-FP64 error report")
+    p.add_argument("--no-fp64-leg", action="store_true", help="lj_batch: skip timing the plain FP64 path")
     return p.parse_args()
 
 
@@ -284,32 +296,31 @@ def batch_workload(args, precision):
     md = [workloads.lj_replica(n, rho, t, 1000 + i, precision) for i, (n, rho, t) in md_p]
     mc = [workloads.lj_replica(n, rho, t, 1000 + i, precision) for i, (n, rho, t) in mc_p]
     desc = (f"{len(params)} argon-type LJ replicas (N ~ U{{64..4096}}, rho* ~ U(0.3,0.9), T ~ U(90,300) K, "
-            f"seeded; {redraws} draw(s) with L < 2 rc redrawn), rc = 2.5 sigma; {len(md)} NVT MD "
+            f"seeded; {redraws} draw(s) with L < 2 rc redrawn), shifted LJ rc = 2.5 sigma; {len(md)} NVT MD "
             f"(VV dt=1 fs, Berendsen tau=100 fs) + {len(mc)} NVT MC (Translate delta=0.3 A); "
             f"one batched step = one Lumol step of every replica (MD: N atom-steps, MC: 1 move)")
     return md, md_p, mc, mc_p, desc
 
 
-def main_batch(args, world, rank, local):
+def timed_batch(args, world, local, precision: str, steps: int, warmup: int):
+    """Builds the batched-replica workload at `precision` and times `steps`
+    batched steps (MD half and MC half concurrently, on the two engines' own
+    streams) with CUDA events; returns the figures and the live engines."""
     import concurrent.futures
     import ctypes
 
-    import numpy as np
     import torch
 
-    from lumol_gb300 import _capi as C
     from lumol_gb300.batch import Batch
 
-    torch.cuda.set_device(local)
-    md_sys, md_p, mc_sys, mc_p, desc = batch_workload(args, args.precision)
-    md = Batch(md_sys, precision=args.precision)
+    md_sys, md_p, mc_sys, mc_p, desc = batch_workload(args, precision)
+    md = Batch(md_sys, precision=precision)
     md.md_setup([1.0] * len(md_sys), [(t, 100.0) for _, (n, rho, t) in md_p])
-    mc = Batch(mc_sys, precision=args.precision)
+    # a 2 A skin for the chains: fewer list rebuilds for single-particle moves of up to 0.3 A
+    mc = Batch(mc_sys, precision=precision, skin=2.0)
     mc.md_setup([1.0] * len(mc_sys))
     for s, (i, (n, rho, t)) in enumerate(mc_p):
         mc.mc_setup(s, t, 0.3, 5000 + i)
-    md_atoms = md.atoms
-    mc_chains = len(mc_sys)
 
     def stream_of(batch):
         ptr = ctypes.c_void_p()
@@ -317,8 +328,8 @@ def main_batch(args, world, rank, local):
         return torch.cuda.ExternalStream(ptr.value)
 
     s_md, s_mc = stream_of(md), stream_of(mc)
-    chunk = max(1, min(args.chunk, args.steps))
-    iters = (args.steps + chunk - 1) // chunk
+    chunk = max(1, min(args.chunk, steps))
+    iters = (steps + chunk - 1) // chunk
     pool = concurrent.futures.ThreadPoolExecutor(max_workers=2)
 
     def one_iteration(steps_k):
@@ -327,10 +338,10 @@ def main_batch(args, world, rank, local):
         f1.result()
         f2.result()
 
-    for _ in range(max(args.warmup, 3)):
+    for _ in range(max(warmup, 3)):
         one_iteration(chunk)
-    if args.steps % chunk:
-        one_iteration(args.steps % chunk)
+    if steps % chunk:
+        one_iteration(steps % chunk)
     torch.cuda.synchronize()
     n0a, n0b = ctypes.c_uint64(), ctypes.c_uint64()
     md.engine.call("lg_launch_count", ctypes.byref(n0a))
@@ -343,7 +354,7 @@ def main_batch(args, world, rank, local):
     clocks = ClockSampler(local)
     done = 0
     for k in range(iters):
-        steps_k = min(chunk, args.steps - done)
+        steps_k = min(chunk, steps - done)
         starts[k].record(s_md)
         s_mc.wait_event(starts[k])
         one_iteration(steps_k)
@@ -357,17 +368,34 @@ def main_batch(args, world, rank, local):
     n1a, n1b = ctypes.c_uint64(), ctypes.c_uint64()
     md.engine.call("lg_launch_count", ctypes.byref(n1a))
     mc.engine.call("lg_launch_count", ctypes.byref(n1b))
+    pool.shutdown()
     ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
     ms_max = max_over_ranks(world, ms)
-    work = (md_atoms + mc_chains) * args.steps
+    work = (md.atoms + len(mc_sys)) * steps
     value = sum_over_ranks(world, float(work)) / (ms_max * 1e-3)
+    return {"value": value, "ms_max": ms_max, "chunk": chunk, "clocks": clk, "desc": desc,
+            "launches": int(n1a.value - n0a.value + n1b.value - n0b.value), "md": md, "mc": mc,
+            "md_sys": md_sys, "md_p": md_p, "mc_sys": mc_sys, "mc_p": mc_p}
+
+
+def main_batch(args, world, rank, local):
+    import time as _time
+
+    import torch
+
+    from lumol_gb300 import _capi as C
+
+    torch.cuda.set_device(local)
+    leg = timed_batch(args, world, local, args.precision, args.steps, args.warmup)
+    md, mc = leg["md"], leg["mc"]
+    md_atoms, mc_chains = md.atoms, len(leg["mc_sys"])
 
     # MC chains alone, over many moves: moves/s of the MC half
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
+    t0 = _time.perf_counter()
     mc.mc_run(2048)
     torch.cuda.synchronize()
-    mc_rate = mc_chains * 2048 / (time.perf_counter() - t0)
+    mc_rate = mc_chains * 2048 / (_time.perf_counter() - t0)
 
     # end to end: every step, all MD replicas' positions and velocities go
     # host -> device and back through the public calls (pinned buffers)
@@ -379,36 +407,60 @@ def main_batch(args, world, rank, local):
         md.engine.call("lg_md_get_state_all", C.dptr(pos.numpy()), C.dptr(vel.numpy()), None)
         steps_e2e = min(args.steps, 32)
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
+        t0 = _time.perf_counter()
         for _ in range(steps_e2e):
             md.engine.call("lg_md_set_state_all", C.dptr(pos.numpy()), C.dptr(vel.numpy()), None)
             md.engine.call("lg_md_run", 1)
             md.engine.call("lg_md_get_state_all", C.dptr(pos.numpy()), C.dptr(vel.numpy()), None)
         torch.cuda.synchronize()
-        el = max_over_ranks(world, time.perf_counter() - t0)
+        el = max_over_ranks(world, _time.perf_counter() - t0)
         e2e = {"value": sum_over_ranks(world, float(n_all)) * steps_e2e / el, "unit": METRIC,
                "h2d_bytes_per_step": 2 * 3 * 8 * n_all, "d2h_bytes_per_step": 2 * 3 * 8 * n_all,
                "scope": "MD half (the MC chains' state stays on the device)"}
 
     roofline = None if args.no_roofline else batch_roofline(args, md, C)
+    md.engine.close()
+    mc.engine.close()
+
+    # the plain FP64 path on the same workload: the mixed-vs-FP64 ratio of the metric
+    fp64_leg = None
+    if args.precision == "mixed" and not args.no_fp64_leg:
+        steps64 = min(args.steps, 64)
+        leg64 = timed_batch(args, world, local, "fp64", steps64, 3)
+        leg64["md"].engine.close()
+        leg64["mc"].engine.close()
+        fp64_leg = {"value": leg64["value"], "unit": METRIC, "steps": steps64,
+                    "ms_per_step": leg64["ms_max"] / steps64, "mixed_over_fp64": leg["value"] / leg64["value"]}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = batch_cpu_baseline(md_sys, mc_sys, mc_p)
+        cpu = batch_cpu_baseline(leg["md_sys"], leg["mc_sys"], leg["mc_p"])
+    acc = None
+    if rank == 0 and args.precision == "mixed" and not args.no_accuracy:
+        from lumol_gb300 import workloads
+        sub = leg["md_p"][:8]
+        pairs = [(workloads.lj_replica(n, rho, t, 1000 + i, "fp64"),
+                  workloads.lj_replica(n, rho, t, 1000 + i, "mixed")) for i, (n, rho, t) in sub]
+        acc = accuracy_report(pairs, [1.0] * len(pairs), 2000,
+                              f"the first {len(pairs)} MD replicas ({sum(p[0].size for p in pairs)} atoms), "
+                              "starting positions; NVE dt = 1 fs")
     if rank == 0:
         line = {
-            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "metric": METRIC, "value": leg["value"], "unit": METRIC, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": leg["ms_max"] / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
             "data": "synthetic (seeded replicas, lattice + jitter, Maxwell-Boltzmann velocities)",
-            "config": {"workload": desc, "atoms": md_atoms + mc.atoms, "md_atoms": md_atoms,
+            "config": {"workload": leg["desc"], "atoms": md_atoms + mc.atoms, "md_atoms": md_atoms,
                        "mc_chains": mc_chains, "precision": args.precision,
                        "parallelism": f"replicas x{world}" if world > 1 else "one GPU, two engine streams",
-                       "timed_iteration": f"{chunk} batched steps (lg_md_run || lg_mc_run)",
+                       "timed_iteration": f"{leg['chunk']} batched steps (lg_md_run || lg_mc_run)",
                        "l2": "inputs larger than L2 (neighbour lists of all replicas), no flush"},
+            "fp64_plain": fp64_leg,
+            "accuracy": acc,
             "mc_moves_per_s": mc_rate,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-            "gpu_launches": int(n1a.value - n0a.value + n1b.value - n0b.value),
-            "clocks": clk,
+            "gpu_launches": leg["launches"],
+            "clocks": leg["clocks"],
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -490,6 +542,48 @@ def batch_roofline(args, md, C):
             "peak_source": ("FP64" if fp64 else "FP32") + " FMA throughput measured live by lg_fma_peak "
                            "(MEASURED_PEAKS.json has no such figure; no tensor cores on this path)",
             "kernel_ms_by_group": times, "work": {"pairs_lj": pairs, "pair_flops": flops}}
+
+
+def accuracy_report(pairs, timesteps, nve_steps: int, label: str):
+    """Error of the mixed path against the plain FP64 path, stated per
+    workload: for each (FP64, mixed) pair of the same seeded system, the
+    relative force RMS sqrt(sum|F_mixed - F_fp64|^2 / sum|F_fp64|^2), the
+    relative potential-energy error, the virial error relative to its largest
+    entry, all at the starting positions; then both paths run `nve_steps`
+    Velocity-Verlet steps without thermostat and the total-energy drift
+    |E(end) - E(0)| / |E(0)| is reported for each.  Maxima over the pairs."""
+    import numpy as np
+
+    from lumol_gb300 import units
+    from lumol_gb300.batch import Batch
+
+    out = {"vs": "plain FP64 GPU path on the same seeded systems", "systems": label,
+           "force_rms_rel": 0.0, "energy_rel": 0.0, "virial_rel": 0.0, "nve_steps": nve_steps}
+    for sd, sm in pairs:
+        fd, ed, wd = sd.compute()
+        fm, em, wm = sm.compute()
+        out["force_rms_rel"] = max(out["force_rms_rel"], float(np.sqrt(np.sum((fm - fd) ** 2) / np.sum(fd ** 2))))
+        out["energy_rel"] = max(out["energy_rel"], abs(em - ed) / abs(ed))
+        out["virial_rel"] = max(out["virial_rel"], float(np.max(np.abs(wm - wd)) / np.max(np.abs(wd))))
+    for name, idx in (("fp64", 0), ("mixed", 1)):
+        systems = [p[idx] for p in pairs]
+        b = Batch(systems, precision=name)
+        b.md_setup(timesteps)
+        e0 = []
+        for s, system in enumerate(systems):
+            _, v = b.state(s)
+            e0.append(b.energy(s) + 0.5 * float(np.sum(system.masses[:, None] * v * v)))
+        b.md_run(nve_steps)
+        drift, per_atom = 0.0, 0.0
+        for s, system in enumerate(systems):
+            _, v = b.state(s)
+            e1 = b.energy(s) + 0.5 * float(np.sum(system.masses[:, None] * v * v))
+            drift = max(drift, abs(e1 - e0[s]) / abs(e0[s]))
+            per_atom = max(per_atom, units.to(abs(e1 - e0[s]), "kJ/mol") / system.size)
+        b.engine.close()
+        out[f"nve_drift_rel_{name}"] = drift
+        out[f"nve_drift_kJmol_per_atom_{name}"] = per_atom
+    return out
 
 
 def batch_cpu_baseline(md_sys, mc_sys, mc_p, seconds: float = 15.0):
@@ -592,6 +686,11 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(system, dt)
+    acc = None
+    if rank == 0 and args.precision == "mixed" and not args.no_accuracy:
+        pair = (make_system(args.workload, "fp64", args.cells)[0], make_system(args.workload, "mixed", args.cells)[0])
+        nve = {"nacl_ewald": 2000, "water": 5000}.get(args.workload, 1000)
+        acc = accuracy_report([pair], [dt], nve, f"the benchmarked system, starting positions; NVE dt = {dt} fs")
 
     if rank == 0:
         line = {
@@ -606,6 +705,7 @@ def main():
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "accuracy": acc,
             "gpu_launches": int(n1.value - n0.value),
             "clocks": clk,
         }

@@ -209,15 +209,18 @@ struct lg_engine {
     Batch b;
     // device storage
     DBuf<double4_32a> posq, vel, acc, pos_build;
-    DBuf<double> force, pos3, vel3, red, host_const, lambda, ke, out, fpart, kred, mc_part;
+    DBuf<double> force, pos3, vel3, red, host_const, kepart, out, fpart, kred, mc_part;
+    DBuf<int2> tiles;
+    DBuf<double4_32a> cp_pos, cp_vel, cp_acc;  // MD checkpoint: a chunk whose list overflowed is replayed
     DBuf<int> kind, mol, sysid, spec_off, spec_j, bt_off, bt_role, nbr, nnb, atom_cell, cell_count, cell_start,
-        cell_atoms, cell_sys, perm;
+        cell_atoms, plan, perm;
     DBuf<int2> km;
     DBuf<int8_t> spec_path;
     DBuf<int4> bt;
     DBuf<double2> bt_par, eikr, rho;
     DBuf<float4> wpos;
-    DBuf<uint4> posfx;
+    DBuf<uint4> posfx, pfx_build;
+    DBuf<double> inv_mass;
     DBuf<PairDevF> ptabf;
     DBuf<KVecF> kvecf;
     DBuf<float2> eikrf, rhof;
@@ -357,6 +360,7 @@ int commit(lg_engine* e) {
     e->h_sysdev.assign(nsys, SysDev{});
     std::vector<double> h_const((size_t)nsys * RED_STRIDE, 0.0);
     int mol_base = 0, cell_total = 0, kdim = 1;
+    std::vector<int2> h_tiles;
     double max_expected = 0.0;
     int64_t max_n = 1;
 
@@ -453,6 +457,7 @@ int commit(lg_engine* e) {
             d.Lf[k] = (float)h.L[k];
             d.invLf[k] = (float)(1.0 / h.L[k]);
             d.Lq[k] = (float)(h.L[k] / 4294967296.0);
+            d.fxscale[k] = d.invL[k] * 4294967296.0;
         }
         double rc = max_cutoff(h);
         d.rlist = rc + e->skin;
@@ -468,6 +473,9 @@ int commit(lg_engine* e) {
         }
         d.cell_begin = cell_total;
         cell_total += cells;
+        d.tile_begin = (int)h_tiles.size();
+        for (int64_t a = 0; a < h.n; a += VV_TILE) h_tiles.push_back(make_int2(s, (int)(base + a)));
+        d.tile_end = (int)h_tiles.size();
         double volume = h.L[0] * h.L[1] * h.L[2];
         if (h.n > 0) {
             double expected = (double)h.n / volume * 4.0 / 3.0 * PI * d.rlist * d.rlist * d.rlist;
@@ -534,6 +542,7 @@ int commit(lg_engine* e) {
         d.begin = (int)base;
         d.end = (int)(base + h.n);
         d.dt = h.dt;
+        d.hdt = 0.5 * h.dt;
         d.thermo_T = h.T0;
         d.thermo_tau = h.tau;
         d.dof = (double)(3 * h.n);
@@ -579,8 +588,11 @@ int commit(lg_engine* e) {
     CUDA_TRY(e, e->vel3.alloc(3 * n));
     CUDA_TRY(e, e->red.alloc((size_t)n * RED_STRIDE));
     CUDA_TRY(e, e->host_const.alloc((size_t)nsys * RED_STRIDE));
-    CUDA_TRY(e, e->lambda.alloc(nsys));
-    CUDA_TRY(e, e->ke.alloc(n));
+    CUDA_TRY(e, e->tiles.alloc(std::max<size_t>(h_tiles.size(), 1)));
+    CUDA_TRY(e, e->kepart.alloc(std::max<size_t>(h_tiles.size(), 1)));
+    CUDA_TRY(e, e->cp_pos.alloc(n));
+    CUDA_TRY(e, e->cp_vel.alloc(n));
+    CUDA_TRY(e, e->cp_acc.alloc(n));
     CUDA_TRY(e, e->out.alloc((size_t)nsys * RED_STRIDE));
     CUDA_TRY(e, e->kind.alloc(n));
     CUDA_TRY(e, e->mol.alloc(n));
@@ -598,7 +610,7 @@ int commit(lg_engine* e) {
     CUDA_TRY(e, e->cell_count.alloc(cell_total));
     CUDA_TRY(e, e->cell_start.alloc(cell_total + nsys));  // one end sentinel per system
     CUDA_TRY(e, e->cell_atoms.alloc(n));
-    CUDA_TRY(e, e->cell_sys.alloc(cell_total));
+    CUDA_TRY(e, e->plan.alloc(3 + 3 * (size_t)nsys));
     CUDA_TRY(e, e->wpos.alloc(n));
     CUDA_TRY(e, e->sysdev.alloc(nsys));
     CUDA_TRY(e, e->ptab.alloc(h_ptab.size()));
@@ -622,6 +634,8 @@ int commit(lg_engine* e) {
     CUDA_TRY(e, e->ptabf.alloc(h_ptabf.size()));
     CUDA_TRY(e, e->posfx.alloc(mixed ? n : 1));
     CUDA_TRY(e, e->perm.alloc(mixed ? n : 1));
+    CUDA_TRY(e, e->pfx_build.alloc(mixed ? n : 1));
+    CUDA_TRY(e, e->inv_mass.alloc(mixed ? n : 1));
     CUDA_TRY(e, e->km.alloc(mixed ? n : 1));
     CUDA_TRY(e, e->kvecf.alloc(nkv));
     CUDA_TRY(e, e->eikrf.alloc(mixed && nkv ? (size_t)kdim * 3 * n : 1));
@@ -657,20 +671,25 @@ int commit(lg_engine* e) {
     }
     CUDA_TRY(e, cudaMemsetAsync(e->cell_count.p, 0, cell_total * sizeof(int), st));
     // the cell order starts as the identity (every system rebuilds before its first use)
-    std::vector<int> h_iota(n), h_cell_sys(cell_total);
+    std::vector<int> h_iota(n);
     for (int64_t i = 0; i < (int64_t)n; i++) h_iota[i] = (int)i;
-    for (int s = 0; s < nsys; s++) {
-        const SysDev& d = e->h_sysdev[s];
-        int nc = d.ncell[0] * d.ncell[1] * d.ncell[2];
-        for (int c = 0; c < nc; c++) h_cell_sys[d.cell_begin + c] = s;
-    }
     CUDA_TRY(e, cudaMemcpyAsync(e->cell_atoms.p, h_iota.data(), n * sizeof(int), cudaMemcpyHostToDevice, st));
-    CUDA_TRY(e, cudaMemcpyAsync(e->cell_sys.p, h_cell_sys.data(), cell_total * sizeof(int), cudaMemcpyHostToDevice,
-                                st));
-    if (mixed)
+    CUDA_TRY(e, cudaMemsetAsync(e->plan.p, 0, (3 + 3 * (size_t)nsys) * sizeof(int), st));
+    std::vector<double> h_inv_mass;
+    if (mixed) {
         CUDA_TRY(e, cudaMemcpyAsync(e->perm.p, h_iota.data(), n * sizeof(int), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(e, cudaMemsetAsync(e->pfx_build.p, 0, n * sizeof(uint4), st));
+        h_inv_mass.resize(n);
+        for (int64_t i = 0; i < (int64_t)n; i++) h_inv_mass[i] = 1.0 / h_vel[i].w;
+        CUDA_TRY(e, cudaMemcpyAsync(e->inv_mass.p, h_inv_mass.data(), n * sizeof(double), cudaMemcpyHostToDevice,
+                                    st));
+    }
     CUDA_TRY(e, cudaMemsetAsync(e->nnb.p, 0, n * sizeof(int), st));
     CUDA_TRY(e, cudaMemcpyAsync(e->sysdev.p, e->h_sysdev.data(), nsys * sizeof(SysDev), cudaMemcpyHostToDevice, st));
+    if (!h_tiles.empty())
+        CUDA_TRY(e, cudaMemcpyAsync(e->tiles.p, h_tiles.data(), h_tiles.size() * sizeof(int2), cudaMemcpyHostToDevice,
+                                    st));
+    CUDA_TRY(e, cudaMemsetAsync(e->kepart.p, 0, std::max<size_t>(h_tiles.size(), 1) * sizeof(double), st));
     CUDA_TRY(e, cudaMemcpyAsync(e->ptab.p, h_ptab.data(), h_ptab.size() * sizeof(PairDev), cudaMemcpyHostToDevice, st));
     CUDA_TRY(e, cudaMemcpyAsync(e->ptabf.p, h_ptabf.data(), h_ptabf.size() * sizeof(PairDevF), cudaMemcpyHostToDevice,
                                 st));
@@ -720,7 +739,8 @@ int commit(lg_engine* e) {
     b.cell_count = e->cell_count.p;
     b.cell_start = e->cell_start.p;
     b.cell_atoms = e->cell_atoms.p;
-    b.cell_sys = e->cell_sys.p;
+    b.plan = e->plan.p;
+    CUDA_TRY(e, cudaDeviceGetAttribute(&b.sms, cudaDevAttrMultiProcessorCount, e->opt.device));
     b.perm = mixed ? e->perm.p : nullptr;
     b.km = mixed ? e->km.p : nullptr;
     b.wpos = e->wpos.p;
@@ -738,15 +758,22 @@ int commit(lg_engine* e) {
     b.kred = e->kred.p;
     b.red = e->red.p;
     b.host_const = e->host_const.p;
-    b.lambda = e->lambda.p;
-    b.ke = e->ke.p;
+    b.ntiles = (int)h_tiles.size();
+    b.tiles = e->tiles.p;
+    b.kepart = e->kepart.p;
     if (e->h_mc.size() != (size_t)nsys) e->h_mc.assign(nsys, McState{});
     CUDA_TRY(e, e->mc_chains.alloc(nsys));
     CUDA_TRY(e, cudaMemcpy(e->mc_chains.p, e->h_mc.data(), nsys * sizeof(McState), cudaMemcpyHostToDevice));
     e->mc_energies_ready = false;
     b.tpa = e->opt.threads_per_atom ? e->opt.threads_per_atom : (mixed ? 8 : 32);
     b.posfx = mixed ? e->posfx.p : nullptr;
+    b.pfx_build = mixed ? e->pfx_build.p : nullptr;
+    b.inv_mass = mixed ? e->inv_mass.p : nullptr;
     b.ptabf = e->ptabf.p;
+    // the pairs-only variant of the mixed pair kernel when nothing needs restrictions or Coulomb
+    b.pair_general = 0;
+    for (const PairDevF& q : h_ptabf) b.pair_general |= (q.type != 0 && q.restriction != 0) ? 1 : 0;
+    for (int s = 0; s < nsys; s++) b.pair_general |= e->h_sysdev[s].coul != 0 ? 1 : 0;
     b.kvecf = e->kvecf.p;
     b.eikrf = e->eikrf.p;
     b.rhof = e->rhof.p;
@@ -782,21 +809,26 @@ int clear_status_bits(lg_engine* e, uint32_t bits) {
 }
 
 // Kernels launch_nlist_build enqueues.
-int nlist_launches(const Batch& b) { return b.n ? (b.perm ? 7 : 6) : 0; }
+int nlist_launches(const Batch& b) { return b.n ? (b.perm ? 8 : 7) : 0; }
 
 // Forces (and energies / virials) of the whole batch at the positions in posq.
-void enqueue_forces(lg_engine* e, uint32_t terms, bool ev, cudaStream_t st) {
+// The pair kernel assigns the forces, the other force kernels add to them.
+// In an MD step vv_first has already written the mixed path's fixed-point
+// positions (fixed_written).
+void enqueue_forces(lg_engine* e, uint32_t terms, bool ev, cudaStream_t st, bool fixed_written = false) {
     const Batch& b = e->b;
     if (b.n == 0) return;
     launch_nlist_build(b, st);
     e->launches += nlist_launches(b);
-    if (b.precision == LG_PRECISION_MIXED) {  // fixed-point copy in the order of the current list
+    if (b.precision == LG_PRECISION_MIXED && !fixed_written) {  // fixed-point copy in the order of the list
         launch_split_positions(b, st);
         e->launches += 1;
     }
     if (terms & (LG_TERM_PAIRS | LG_TERM_COUL_REAL)) {
         launch_pair_forces(b, terms, ev, st);
         e->launches += 1;
+    } else {
+        cudaMemsetAsync(e->force.p, 0, 3 * (size_t)b.n * sizeof(double), st);
     }
     if ((terms & (LG_TERM_BONDS | LG_TERM_ANGLES)) && b.bt_off) {
         launch_bonded(b, terms, ev, st);
@@ -814,7 +846,6 @@ int compute_batch(lg_engine* e, uint32_t terms, uint32_t want, double* d_force_o
     for (int attempt = 0; attempt < 4; attempt++) {
         launch_check_displacement(e->b, st);
         e->launches += e->b.n ? 1 : 0;
-        CUDA_TRY(e, cudaMemsetAsync(e->force.p, 0, 3 * (size_t)e->b.n * sizeof(double), st));
         if (ev) CUDA_TRY(e, cudaMemsetAsync(e->red.p, 0, (size_t)e->b.n * RED_STRIDE * sizeof(double), st));
         enqueue_forces(e, terms, ev, st);
         if (ev) {
@@ -1167,6 +1198,7 @@ int lg_md_setup(lg_engine* e, int32_t s, double dt, double T0, double tau) {
     if (!e->dirty) {
         SysDev& d = e->h_sysdev[s];
         d.dt = h.dt;
+        d.hdt = 0.5 * h.dt;
         d.thermo_T = h.T0;
         d.thermo_tau = h.tau;
         CUDA_TRY(e, cudaSetDevice(e->opt.device));
@@ -1317,12 +1349,14 @@ int autotune(lg_engine* e) {
     return LG_OK;
 }
 
-void enqueue_md_step(lg_engine* e, bool thermo, cudaStream_t st) {
-    launch_vv_first(e->b, st);
-    enqueue_forces(e, LG_TERM_ALL, false, st);
+// One Velocity-Verlet step.  With a thermostat, the Berendsen scaling of the
+// previous step is applied by this step's vv_first (apply_previous), and the
+// last step of a run is followed by launch_thermostat_finalize.
+void enqueue_md_step(lg_engine* e, bool thermo, bool apply_previous, cudaStream_t st) {
+    launch_vv_first(e->b, thermo && apply_previous, st);
+    enqueue_forces(e, LG_TERM_ALL, false, st, true);
     launch_vv_second(e->b, thermo, st);
-    if (thermo) launch_thermostat(e->b, st);
-    e->launches += 2 + (thermo ? 2 : 0);
+    e->launches += e->b.ntiles ? 2 : 0;
 }
 
 int build_md_graph(lg_engine* e, int steps, bool thermo) {
@@ -1330,7 +1364,8 @@ int build_md_graph(lg_engine* e, int steps, bool thermo) {
     cudaGraph_t g;
     uint64_t before = e->launches;
     CUDA_TRY(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-    for (int k = 0; k < steps; k++) enqueue_md_step(e, thermo, e->stream);
+    for (int k = 0; k < steps; k++) enqueue_md_step(e, thermo, k > 0, e->stream);
+    if (thermo) launch_thermostat_finalize(e->b, e->stream);
     e->launches = before;  // captured launches run (and are counted) at replay
     CUDA_TRY(e, cudaStreamEndCapture(e->stream, &g));
     size_t nodes = 0;
@@ -1366,11 +1401,9 @@ int lg_md_run(lg_engine* e, int64_t nsteps) {
         int rc = autotune(e);
         if (rc) return rc;
     }
-    // checkpoint buffers: a chunk whose list overflowed is replayed after regrowing
-    DBuf<double4_32a> cp_pos, cp_vel, cp_acc;
-    CUDA_TRY(e, cp_pos.alloc(e->b.n));
-    CUDA_TRY(e, cp_vel.alloc(e->b.n));
-    CUDA_TRY(e, cp_acc.alloc(e->b.n));
+    DBuf<double4_32a>& cp_pos = e->cp_pos;
+    DBuf<double4_32a>& cp_vel = e->cp_vel;
+    DBuf<double4_32a>& cp_acc = e->cp_acc;
     while (done < nsteps) {
         int steps = (int)std::min<int64_t>(chunk, nsteps - done);
         if (e->graph_thermo != thermo || !e->graphs.count(steps)) {
@@ -1512,11 +1545,11 @@ int lg_kernel_times(lg_engine* e, int32_t reps, double* ms) {
                 case LG_KT_EIKR: launch_kspace_part(b, 0, false, st); break;
                 case LG_KT_RHO: launch_kspace_part(b, 1, false, st); break;
                 case LG_KT_FIELD: launch_kspace_part(b, 2, false, st); break;
-                case LG_KT_VV:
-                    launch_vv_first(b, st);
+                case LG_KT_VV:  // (the tile kinetic energies may not be current: no scaling here)
+                    launch_vv_first(b, false, st);
                     launch_vv_second(b, thermo, st);
                     break;
-                case LG_KT_STEP: enqueue_md_step(e, thermo, st); break;
+                case LG_KT_STEP: enqueue_md_step(e, thermo, false, st); break;
             }
             CUDA_TRY(e, cudaEventRecord(e1, st));
             CUDA_TRY(e, cudaEventSynchronize(e1));
@@ -1536,7 +1569,6 @@ int lg_kernel_times(lg_engine* e, int32_t reps, double* ms) {
     cudaEventDestroy(e1);
     // the forces buffer was overwritten by the timing runs: recompute it at the saved state
     launch_request_rebuild(b, st);
-    CUDA_TRY(e, cudaMemsetAsync(e->force.p, 0, 3 * (size_t)b.n * sizeof(double), st));
     enqueue_forces(e, LG_TERM_ALL, false, st);
     CUDA_TRY(e, cudaStreamSynchronize(st));
     return LG_OK;

@@ -30,7 +30,7 @@ struct PairDev {
 // FP32 pair table entry of the mixed path.
 //   LJ: a = 4 eps sigma^12, b = 4 eps sigma^6;  Buckingham: a = A, b = C, c = 1 / rho;
 //   Harmonic: a = k, b = x0.  shift: energy shift of a shifted interaction.
-struct PairDevF {
+struct alignas(16) PairDevF {
     int32_t type, restriction, pad0, pad1;
     float a, b, c, rc2, shift, scale14, pad2, pad3;
 };
@@ -63,13 +63,30 @@ struct SysDev {
     double k1[3];         // 2 PI * inv(cell)[d][d]: k-vector of index 1 per axis (cells.rs:224-226)
     // molecular dynamics
     double dt;
+    double hdt;                   // 0.5 dt (exact)
+    double fxscale[3];            // 2^32 / L: fixed-point units per length (mixed path)
     double thermo_T, thermo_tau;  // Berendsen (tau <= 0: none)
     double dof;                   // 3 N (DegreesOfFreedom::Particles)
+    int32_t tile_begin, tile_end; // this system's tiles of the per-atom MD kernels
     float Lf[3], invLf[3];        // FP32 copies for the list build and the mixed path
     float Lq[3];                  // L / 2^32: the length of one fixed-point unit
     float rlist2_f;               // (rlist + margin)^2 in FP32
     float coul_rc2_f;
 };
+
+// Fixed-point copy of a wrapped position for the mixed path: per axis
+// u = floor(frac(x / L) * 2^32) (UnitCell::wrap_vector, cells.rs:263-282, as a
+// fraction of the cell), and the charge's FP32 bits.
+// floor(x 2^32 / L) taken modulo 2^32 is that fraction (two's complement
+// wrap-around does the frac), so each axis costs one FP64 multiply and one
+// conversion.
+__device__ __forceinline__ uint32_t fixed_coordinate(double x, double scale) {
+    return (uint32_t)(unsigned long long)__double2ll_rd(x * scale);
+}
+__device__ __forceinline__ uint4 fixed_position(const SysDev& s, double4_32a p) {
+    return make_uint4(fixed_coordinate(p.x, s.fxscale[0]), fixed_coordinate(p.y, s.fxscale[1]),
+                      fixed_coordinate(p.z, s.fxscale[2]), __float_as_uint((float)p.w));
+}
 
 // One Ewald k-vector with its factors (ewald.rs:102-116).
 struct KVecDev {

@@ -145,10 +145,10 @@ __global__ void __launch_bounds__(256) pair_fp64_kernel(
         wyz = group_sum<TPA>(wyz);
         wzz = group_sum<TPA>(wzz);
     }
-    if (active && sub == 0) {
-        force[3 * i] += fx;
-        force[3 * i + 1] += fy;
-        force[3 * i + 2] += fz;
+    if (active && sub == 0) {  // the first force kernel of a step: assigns
+        force[3 * i] = fx;
+        force[3 * i + 1] = fy;
+        force[3 * i + 2] = fz;
         if (EV) {
             // Wolf self energy, subtracted once per charged atom (wolf.rs:205)
             if ((terms & 16u) && s.coul == 2 && pi.w != 0.0)

@@ -41,7 +41,8 @@ struct Batch {
     int* atom_cell = nullptr;
     int* cell_count = nullptr;    // ncells
     int* cell_start = nullptr;    // ncells + nsys: per system, its cells then an end sentinel
-    int* cell_sys = nullptr;      // ncells: system of each cell
+    int* plan = nullptr;          // 3 + 3 nsys: the systems that rebuild and their atom / cell prefix sums
+    int sms = 152;                // multiprocessors of the device (grid sizes of the list-build kernels)
     int* perm = nullptr;          // n: cell-sorted position of each atom (mixed path; null for FP64)
     int2* km = nullptr;           // n: (kind, molecule) in cell-sorted order (mixed path)
     int* cell_atoms = nullptr;    // n: atoms in cell order, per system at [begin, end)
@@ -62,11 +63,16 @@ struct Batch {
     // reductions
     double* red = nullptr;        // [n][RED_STRIDE] per-atom partial energies / virials
     double* host_const = nullptr; // [nsys][RED_STRIDE]: tail energy/virial, Ewald self energy
-    double* lambda = nullptr;     // nsys Berendsen factors
-    double* ke = nullptr;         // n kinetic energies
+    // per-atom MD kernels run on tiles of VV_TILE atoms that never straddle two systems
+    int ntiles = 0;
+    int2* tiles = nullptr;        // ntiles: (system, first atom)
+    double* kepart = nullptr;     // ntiles: kinetic energy of each tile after the last vv_second
     // mixed precision
     int tpa = 32;                 // threads per atom of the pair kernels (autotuned)
-    uint4* posfx = nullptr;       // wrapped positions as 32-bit fractions of L, charge bits
+    int pair_general = 1;         // 0: pair potentials only, no restriction and no Coulomb in the batch
+    uint4* posfx = nullptr;       // wrapped positions as 32-bit fractions of L, charge bits (cell order)
+    uint4* pfx_build = nullptr;   // n: fixed-point positions at the last list build (atom order, mixed path)
+    double* inv_mass = nullptr;   // n: 1 / m (mixed path)
     PairDevF* ptabf = nullptr;
     KVecF* kvecf = nullptr;
     float2* eikrf = nullptr;
@@ -95,9 +101,10 @@ void launch_unpack_vectors(int n, const double4_32a* src, double* dst3, cudaStre
 void launch_unpack_positions(const Batch& b, double* pos3, cudaStream_t st);
 void launch_pack_velocities(const Batch& b, const double* vel3, cudaStream_t st);
 void launch_unpack_velocities(const Batch& b, double* vel3, cudaStream_t st);
-void launch_vv_first(const Batch& b, cudaStream_t st);
+constexpr int VV_TILE = 256;
+void launch_vv_first(const Batch& b, bool apply_thermostat, cudaStream_t st);
 void launch_vv_second(const Batch& b, bool thermostat, cudaStream_t st);
-void launch_thermostat(const Batch& b, cudaStream_t st);
+void launch_thermostat_finalize(const Batch& b, cudaStream_t st);
 void launch_request_rebuild(const Batch& b, cudaStream_t st);
 void launch_check_displacement(const Batch& b, cudaStream_t st);
 

@@ -1,11 +1,13 @@
 // md.cu -- Velocity-Verlet (lumol-sim/src/md/integrators.rs:22-70) and the
 // Berendsen thermostat (md/thermostats.rs:91-121) on device-resident state.
 //
-// One step is: vv_first (half kick + drift + neighbour-list displacement test),
-// the force kernels, vv_second (a = F / m, half kick, kinetic energy), and,
-// with a thermostat, a per-system reduction of the temperature followed by the
-// velocity scaling.  All launches have fixed shapes, so a step is captured once
-// in a CUDA graph and replayed.
+// One step is: vv_first (the previous step's Berendsen scaling, half kick,
+// drift, the mixed path's fixed-point positions, neighbour-list displacement
+// test), the force kernels, vv_second (a = F / m, half kick, per-tile kinetic
+// energy).  The per-atom kernels run on tiles of VV_TILE atoms of one system,
+// so per-system quantities (the thermostat factor) need no atomics and are
+// summed in a fixed order.  All launches have fixed shapes, so a run of steps
+// is captured once in a CUDA graph and replayed.
 #include "kernels.h"
 
 namespace lg {
@@ -83,95 +85,151 @@ __device__ __forceinline__ void flag_rebuild(bool moved, int si, uint32_t* statu
     }
 }
 
-__global__ void vv_first_kernel(int n, const int* __restrict__ sysid, const SysDev* __restrict__ sys,
-                                double4_32a* __restrict__ posq, double4_32a* __restrict__ vel,
-                                const double4_32a* __restrict__ acc, const double4_32a* __restrict__ pos_build,
-                                double* __restrict__ force, uint32_t* status, uint32_t* sys_rebuild) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int si = sysid[i];
-    const SysDev& s = sys[si];
-    // products and sums rounded separately, as the reference (no FMA)
-    double hdt = __dmul_rn(0.5, s.dt);
-    double4_32a v = vel[i], a = acc[i], p = posq[i];
-    v.x = __dadd_rn(v.x, __dmul_rn(hdt, a.x));
-    v.y = __dadd_rn(v.y, __dmul_rn(hdt, a.y));
-    v.z = __dadd_rn(v.z, __dmul_rn(hdt, a.z));
-    p.x = __dadd_rn(p.x, __dmul_rn(v.x, s.dt));
-    p.y = __dadd_rn(p.y, __dmul_rn(v.y, s.dt));
-    p.z = __dadd_rn(p.z, __dmul_rn(v.z, s.dt));
-    vel[i] = v;
-    posq[i] = p;
-    force[3 * i] = 0.0;
-    force[3 * i + 1] = 0.0;
-    force[3 * i + 2] = 0.0;
-    // displacement since the list build, in FP32 against a threshold 1 % below
-    // (skin / 2)^2: the FP32 rounding only ever triggers a rebuild early
-    double4_32a b = pos_build[i];
-    float dx = (float)(p.x - b.x), dy = (float)(p.y - b.y), dz = (float)(p.z - b.z);
-    dx -= rintf(dx * s.invLf[0]) * s.Lf[0];
-    dy -= rintf(dy * s.invLf[1]) * s.Lf[1];
-    dz -= rintf(dz * s.invLf[2]) * s.Lf[2];
-    flag_rebuild(dx * dx + dy * dy + dz * dz > 0.99f * (float)s.half_skin2, si, status, sys_rebuild);
+// Berendsen factor sqrt(1 + (T0 / T - 1) / tau) of one system
+// (md/thermostats.rs:113-120), T = 2 K / (dof kB) (compute.rs:133-144) from the
+// tile kinetic energies of the last vv_second, summed in tile order, so every
+// block of the system computes the same factor.
+__device__ __forceinline__ double berendsen_lambda(const SysDev& s, const double* __restrict__ kepart) {
+    if (!(s.thermo_tau > 0.0)) return 1.0;
+    double k = 0.0;
+    for (int t = s.tile_begin; t < s.tile_end; t++) k += kepart[t];
+    double T = 2.0 * k / (s.dof * K_BOLTZMANN);
+    return sqrt(1.0 + (s.thermo_T / T - 1.0) / s.thermo_tau);
 }
 
-// a = F / m; v += 0.5 dt a (integrators.rs:55-68); kinetic energy per atom
-// for the thermostat (compute.rs:133-144).
-__global__ void vv_second_kernel(int n, const int* __restrict__ sysid, const SysDev* __restrict__ sys,
-                                 const double* __restrict__ force, double4_32a* __restrict__ vel,
-                                 double4_32a* __restrict__ acc, double* __restrict__ ke, int thermostat,
-                                 int exact_division) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const SysDev& s = sys[sysid[i]];
-    double hdt = __dmul_rn(0.5, s.dt);
-    double4_32a v = vel[i];
-    double m = v.w;
-    double4_32a a;
-    if (exact_division) {  // the reference's force / mass
-        a = make_double4_32a(force[3 * i] / m, force[3 * i + 1] / m, force[3 * i + 2] / m, 0.0);
-    } else {  // mixed path: one reciprocal per atom
-        double im = 1.0 / m;
-        a = make_double4_32a(force[3 * i] * im, force[3 * i + 1] * im, force[3 * i + 2] * im, 0.0);
-    }
-    v.x = __dadd_rn(v.x, __dmul_rn(hdt, a.x));
-    v.y = __dadd_rn(v.y, __dmul_rn(hdt, a.y));
-    v.z = __dadd_rn(v.z, __dmul_rn(hdt, a.z));
-    acc[i] = a;
-    vel[i] = v;
-    if (thermostat) ke[i] = 0.5 * m * (v.x * v.x + v.y * v.y + v.z * v.z);
-}
-
-// Per-system temperature T = 2 K / (dof kB) and Berendsen factor
-// sqrt(1 + (T0 / T - 1) / tau), fixed-order tree sum.
-__global__ void __launch_bounds__(256) thermostat_reduce_kernel(const SysDev* __restrict__ sys,
-                                                                const double* __restrict__ ke,
-                                                                double* __restrict__ lambda) {
-    __shared__ double sh[256];
-    const SysDev& s = sys[blockIdx.x];
-    double acc = 0.0;
-    for (int i = s.begin + threadIdx.x; i < s.end; i += blockDim.x) acc += ke[i];
-    sh[threadIdx.x] = acc;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+// The Berendsen scaling of step k is applied at the start of step k + 1 (the
+// same products, in the same order, as scaling right after step k), and by
+// thermostat_finalize at the end of a run, which saves two launches a step.
+// vv_first: [v *= lambda]; v += 0.5 dt a; x += v dt (integrators.rs:45-53);
+// the neighbour-list displacement test.  Zeroing the forces is left to the
+// pair kernel, which assigns.
+//
+// Plain path (MIXED = false): products and sums rounded separately, as the
+// reference (no FMA); the displacement test in FP32 on FP64 differences.
+// Mixed path: the same FP64 state updated with fused multiply-adds (FP64
+// operations are scarce on this GPU: about 1.7 per SM and clock), the
+// fixed-point copy written at the atom's current cell-order slot, and the
+// displacement test on fixed-point differences against the copy taken at the
+// last build (no FP64 operation).
+template <bool MIXED>
+__global__ void __launch_bounds__(VV_TILE) vv_first_kernel(
+    const int2* __restrict__ tiles, const SysDev* __restrict__ sys, double4_32a* __restrict__ posq,
+    double4_32a* __restrict__ vel, const double4_32a* __restrict__ acc, const double4_32a* __restrict__ pos_build,
+    const uint4* __restrict__ pfx_build, const double* __restrict__ kepart, int apply_thermostat,
+    const int* __restrict__ perm, uint4* __restrict__ posfx, uint32_t* status, uint32_t* sys_rebuild) {
+    int2 tile = tiles[blockIdx.x];
+    const SysDev& s = sys[tile.x];
+    __shared__ double s_lambda;
+    if (apply_thermostat) {
+        if (threadIdx.x == 0) s_lambda = berendsen_lambda(s, kepart);
         __syncthreads();
     }
-    if (threadIdx.x == 0) {
-        double f = 1.0;
-        if (s.thermo_tau > 0.0) {
-            double T = 2.0 * sh[0] / (s.dof * K_BOLTZMANN);
-            f = sqrt(1.0 + (s.thermo_T / T - 1.0) / s.thermo_tau);
+    int i = tile.y + threadIdx.x;
+    if (i >= s.end) return;
+    double hdt = s.hdt, dt = s.dt;
+    double4_32a v = vel[i], a = acc[i], p = posq[i];
+    if (apply_thermostat) {
+        double f = s_lambda;
+        v.x *= f;
+        v.y *= f;
+        v.z *= f;
+    }
+    float dx, dy, dz;
+    if (MIXED) {
+        v.x = fma(hdt, a.x, v.x);
+        v.y = fma(hdt, a.y, v.y);
+        v.z = fma(hdt, a.z, v.z);
+        p.x = fma(v.x, dt, p.x);
+        p.y = fma(v.y, dt, p.y);
+        p.z = fma(v.z, dt, p.z);
+        uint4 u = fixed_position(s, p);
+        posfx[perm[i]] = u;  // a rebuild this step rewrites it in the new order
+        uint4 ub = pfx_build[i];
+        dx = (float)(int32_t)(u.x - ub.x) * s.Lq[0];
+        dy = (float)(int32_t)(u.y - ub.y) * s.Lq[1];
+        dz = (float)(int32_t)(u.z - ub.z) * s.Lq[2];
+    } else {
+        v.x = __dadd_rn(v.x, __dmul_rn(hdt, a.x));
+        v.y = __dadd_rn(v.y, __dmul_rn(hdt, a.y));
+        v.z = __dadd_rn(v.z, __dmul_rn(hdt, a.z));
+        p.x = __dadd_rn(p.x, __dmul_rn(v.x, dt));
+        p.y = __dadd_rn(p.y, __dmul_rn(v.y, dt));
+        p.z = __dadd_rn(p.z, __dmul_rn(v.z, dt));
+        double4_32a b = pos_build[i];
+        dx = (float)(p.x - b.x);
+        dy = (float)(p.y - b.y);
+        dz = (float)(p.z - b.z);
+        dx -= rintf(dx * s.invLf[0]) * s.Lf[0];
+        dy -= rintf(dy * s.invLf[1]) * s.Lf[1];
+        dz -= rintf(dz * s.invLf[2]) * s.Lf[2];
+    }
+    vel[i] = v;
+    posq[i] = p;
+    // against a threshold 1 % below (skin / 2)^2: the FP32 rounding only ever
+    // triggers a rebuild early
+    flag_rebuild(dx * dx + dy * dy + dz * dz > 0.99f * (float)s.half_skin2, tile.x, status, sys_rebuild);
+}
+
+// a = F / m; v += 0.5 dt a (integrators.rs:55-68); with a thermostat, the
+// kinetic energy of the tile (fixed-order tree sum) for the next step's factor.
+// Plain path: the reference's division and unfused products; mixed path:
+// 1 / m precomputed and fused multiply-adds.
+template <bool MIXED>
+__global__ void __launch_bounds__(VV_TILE) vv_second_kernel(
+    const int2* __restrict__ tiles, const SysDev* __restrict__ sys, const double* __restrict__ force,
+    const double* __restrict__ inv_mass, double4_32a* __restrict__ vel, double4_32a* __restrict__ acc,
+    double* __restrict__ kepart, int thermostat) {
+    int2 tile = tiles[blockIdx.x];
+    const SysDev& s = sys[tile.x];
+    int i = tile.y + threadIdx.x;
+    double ke = 0.0;
+    if (i < s.end) {
+        double hdt = s.hdt;
+        double4_32a v = vel[i];
+        double m = v.w;
+        double4_32a a;
+        if (MIXED) {
+            double im = inv_mass[i];
+            a = make_double4_32a(force[3 * i] * im, force[3 * i + 1] * im, force[3 * i + 2] * im, 0.0);
+            v.x = fma(hdt, a.x, v.x);
+            v.y = fma(hdt, a.y, v.y);
+            v.z = fma(hdt, a.z, v.z);
+            if (thermostat) ke = 0.5 * m * fma(v.x, v.x, fma(v.y, v.y, v.z * v.z));
+        } else {  // the reference's force / mass
+            a = make_double4_32a(force[3 * i] / m, force[3 * i + 1] / m, force[3 * i + 2] / m, 0.0);
+            v.x = __dadd_rn(v.x, __dmul_rn(hdt, a.x));
+            v.y = __dadd_rn(v.y, __dmul_rn(hdt, a.y));
+            v.z = __dadd_rn(v.z, __dmul_rn(hdt, a.z));
+            if (thermostat) ke = 0.5 * m * (v.x * v.x + v.y * v.y + v.z * v.z);
         }
-        lambda[blockIdx.x] = f;
+        acc[i] = a;
+        vel[i] = v;
+    }
+    if (thermostat) {
+        __shared__ double sh[VV_TILE];
+        sh[threadIdx.x] = ke;
+        __syncthreads();
+        for (int o = VV_TILE / 2; o > 0; o >>= 1) {
+            if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) kepart[blockIdx.x] = sh[0];
     }
 }
 
-__global__ void thermostat_scale_kernel(int n, const int* __restrict__ sysid, const double* __restrict__ lambda,
-                                        double4_32a* __restrict__ vel) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    double f = lambda[sysid[i]];
+// The pending Berendsen scaling at the end of a run.
+__global__ void __launch_bounds__(VV_TILE) thermostat_finalize_kernel(const int2* __restrict__ tiles,
+                                                                     const SysDev* __restrict__ sys,
+                                                                     const double* __restrict__ kepart,
+                                                                     double4_32a* __restrict__ vel) {
+    int2 tile = tiles[blockIdx.x];
+    const SysDev& s = sys[tile.x];
+    __shared__ double s_lambda;
+    if (threadIdx.x == 0) s_lambda = berendsen_lambda(s, kepart);
+    __syncthreads();
+    int i = tile.y + threadIdx.x;
+    if (i >= s.end) return;
+    double f = s_lambda;
     double4_32a v = vel[i];
     v.x *= f;
     v.y *= f;
@@ -207,20 +265,30 @@ __global__ void request_rebuild_kernel(int nsys, uint32_t* status, uint32_t* sys
     if (threadIdx.x == 0) atomicOr(status, ST_REBUILD);
 }
 
-void launch_vv_first(const Batch& b, cudaStream_t st) {
-    if (b.n)
-        vv_first_kernel<<<(b.n + 255) / 256, 256, 0, st>>>(b.n, b.sysid, b.sys, b.posq, b.vel, b.acc,
-                                                         b.pos_build, b.force, b.status, b.sys_rebuild);
+void launch_vv_first(const Batch& b, bool apply_thermostat, cudaStream_t st) {
+    if (!b.ntiles) return;
+    int th = apply_thermostat ? 1 : 0;
+    if (b.posfx)
+        vv_first_kernel<true><<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.posq, b.vel, b.acc, b.pos_build,
+                                                            b.pfx_build, b.kepart, th, b.perm, b.posfx, b.status,
+                                                            b.sys_rebuild);
+    else
+        vv_first_kernel<false><<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.posq, b.vel, b.acc, b.pos_build,
+                                                             nullptr, b.kepart, th, nullptr, nullptr, b.status,
+                                                             b.sys_rebuild);
 }
 void launch_vv_second(const Batch& b, bool thermostat, cudaStream_t st) {
-    if (b.n)
-        vv_second_kernel<<<(b.n + 255) / 256, 256, 0, st>>>(b.n, b.sysid, b.sys, b.force, b.vel, b.acc, b.ke,
-                                                          thermostat ? 1 : 0, b.precision == 0 ? 1 : 0);
+    if (!b.ntiles) return;
+    int th = thermostat ? 1 : 0;
+    if (b.precision == 1)
+        vv_second_kernel<true><<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.force, b.inv_mass, b.vel, b.acc,
+                                                             b.kepart, th);
+    else
+        vv_second_kernel<false><<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.force, nullptr, b.vel, b.acc,
+                                                              b.kepart, th);
 }
-void launch_thermostat(const Batch& b, cudaStream_t st) {
-    if (b.n == 0) return;
-    thermostat_reduce_kernel<<<b.nsys, 256, 0, st>>>(b.sys, b.ke, b.lambda);
-    thermostat_scale_kernel<<<(b.n + 255) / 256, 256, 0, st>>>(b.n, b.sysid, b.lambda, b.vel);
+void launch_thermostat_finalize(const Batch& b, cudaStream_t st) {
+    if (b.ntiles) thermostat_finalize_kernel<<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.kepart, b.vel);
 }
 void launch_request_rebuild(const Batch& b, cudaStream_t st) {
     request_rebuild_kernel<<<1, 256, 0, st>>>(b.nsys, b.status, b.sys_rebuild);

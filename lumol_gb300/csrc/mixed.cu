@@ -35,18 +35,6 @@ __device__ __forceinline__ void two_sum_acc(float& s, float& c, float x) {
 }
 
 template <int TPA>
-__device__ __forceinline__ double group_sum_comp(float s, float c) {
-#pragma unroll
-    for (int o = TPA / 2; o > 0; o >>= 1) {
-        float so = __shfl_xor_sync(0xffffffffu, s, o);
-        float co = __shfl_xor_sync(0xffffffffu, c, o);
-        two_sum_acc(s, c, so);
-        c += co;
-    }
-    return (double)s + (double)c;
-}
-
-template <int TPA>
 __device__ __forceinline__ double group_sum_d(double v) {
 #pragma unroll
     for (int o = TPA / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -86,63 +74,56 @@ __device__ __forceinline__ float pair_mixed(const PairDevF& p, float r2, float i
     }
 }
 
-template <int TPA, bool EV>
-__global__ void __launch_bounds__(256) pair_mixed_kernel(
-    int n, const uint4* __restrict__ pfx, const int2* __restrict__ km, const int* __restrict__ order,
-    const int* __restrict__ sysid, const SysDev* __restrict__ sys,
-    const PairDevF* __restrict__ ptab, const int* __restrict__ nbr, const int* __restrict__ nnb, int maxnb,
-    const int* __restrict__ spec_off, const int* __restrict__ spec_j, const int8_t* __restrict__ spec_path,
-    uint32_t terms, double* __restrict__ force, double* __restrict__ red) {
-    // t walks the cell-sorted order; i is the atom's own index (forces, bond paths)
-    int gt = blockIdx.x * blockDim.x + threadIdx.x;
-    int t = gt / TPA;
-    int sub = gt % TPA;
-    bool active = t < n;
-    int tt = active ? t : n - 1;
-    int i = order[tt];
-    const SysDev& s = sys[sysid[tt]];
-    uint4 pi = pfx[tt];
-    float qi = __uint_as_float(pi.w);
-    int2 kmi = km[tt];
-    int ki = kmi.x, mi = kmi.y;
-    const PairDevF* prow = ptab + s.ptab + ki * s.nk;
-    float sc0 = s.Lq[0], sc1 = s.Lq[1], sc2 = s.Lq[2];
-    bool coul = (terms & 16u) && s.coul != 0 && qi != 0.0f;
-    bool pairs = (terms & 1u) != 0;
-    float coul_rc2 = s.coul_rc2_f;
-    float alpha = (float)s.alpha;
-    float pref = qi * (float)(1.0 / FOUR_PI_EPSILON_0);
+// Accumulators of one lane of a pair-kernel group.
+struct MixedAcc {
     float fxs = 0.f, fxc = 0.f, fys = 0.f, fyc = 0.f, fzs = 0.f, fzc = 0.f;
     double ep = 0.0, ec = 0.0;
     double w0 = 0, w1 = 0, w2 = 0, w3 = 0, w4 = 0, w5 = 0;
-    int cnt = active ? nnb[tt] : 0;
-    const int* list = nbr + (size_t)tt * maxnb;
-    for (int k = sub; k < cnt; k += TPA) {
-        int js = list[k];  // sorted position of the neighbour
-        uint4 pj = pfx[js];
-        float qj = __uint_as_float(pj.w);
-        float dx = fixed_image(pi.x, pj.x, sc0);
-        float dy = fixed_image(pi.y, pj.y, sc1);
-        float dz = fixed_image(pi.z, pj.z, sc2);
-        float r2 = dx * dx + dy * dy + dz * dz;
-        int2 kmj = km[js];
-        const PairDevF& p = prow[kmj.x];
-        bool pin = pairs && p.type != 0 && r2 < p.rc2;
-        bool cin = coul && qj != 0.0f && r2 <= coul_rc2;
-        if (!(pin || cin)) continue;
+};
+
+// One neighbour-list entry of atom i (sorted position tt): pair potential and
+// (GENERAL) restrictions and real-space Coulomb, added to the lane's sums.
+template <bool EV, bool GENERAL>
+__device__ __forceinline__ void mixed_entry(
+    MixedAcc& A, const SysDev& s, const PairDevF* __restrict__ prow, uint4 pi, float qi, int mi, int i, int tt,
+    int js, uint4 pj, int2 kmj, const int* __restrict__ order, const int* __restrict__ spec_off,
+    const int* __restrict__ spec_j, const int8_t* __restrict__ spec_path, bool pairs, bool coul, float coul_rc2,
+    float alpha, float pref) {
+    float qj = __uint_as_float(pj.w);
+    float dx = fixed_image(pi.x, pj.x, s.Lq[0]);
+    float dy = fixed_image(pi.y, pj.y, s.Lq[1]);
+    float dz = fixed_image(pi.z, pj.z, s.Lq[2]);
+    float r2 = dx * dx + dy * dy + dz * dz;
+    // the parameters as two 16-byte loads: (type, restriction, -, -) and (a, b, c, rc2)
+    const PairDevF* pp = prow + kmj.x;
+    int4 ph = __ldg(reinterpret_cast<const int4*>(pp));
+    float4 pq = __ldg(reinterpret_cast<const float4*>(pp) + 1);
+    bool pin = pairs && ph.x != 0 && r2 < pq.w;
+    bool cin = GENERAL && coul && qj != 0.0f && r2 <= coul_rc2;
+    if (!(pin || cin)) return;
+    float inv_r = rsqrtf(r2);
+    float inv_r2 = inv_r * inv_r;
+    float fr = 0.0f;
+    float e_pair = 0.0f, e_coul = 0.0f;
+    if (!GENERAL) {
+        float shift = EV ? __ldg(&pp->shift) : 0.0f;
+        if (ph.x == 2) {  // LJ: c12 / r^12 - c6 / r^6
+            float ir6 = inv_r2 * inv_r2 * inv_r2;
+            fr = ir6 * (12.0f * pq.x * ir6 - 6.0f * pq.y) * inv_r2;
+            if (EV) e_pair = ir6 * (pq.x * ir6 - pq.y) - shift;
+        } else {
+            e_pair = pair_mixed(*pp, r2, inv_r2, inv_r, fr);
+        }
+    } else {
         int path = -1;
         int mj = kmj.y;
         float sc = 1.0f;
-        if (pin && p.restriction != 0) {
-            path = p.restriction <= 2 ? (mi != mj ? 0 : 5)
-                                      : bond_path(i, order[js], mi, mj, spec_off, spec_j, spec_path);
-            if (restriction_excluded(p.restriction, path)) pin = false;
-            else sc = p.restriction == 6 && path == 4 ? p.scale14 : 1.0f;
+        const PairDevF& p = *pp;
+        if (pin && ph.y != 0) {
+            path = ph.y <= 2 ? (mi != mj ? 0 : 5) : bond_path(i, order[js], mi, mj, spec_off, spec_j, spec_path);
+            if (restriction_excluded(ph.y, path)) pin = false;
+            else sc = ph.y == 6 && path == 4 ? p.scale14 : 1.0f;
         }
-        float inv_r = rsqrtf(r2);
-        float inv_r2 = inv_r * inv_r;
-        float fr = 0.0f;
-        float e_pair = 0.0f, e_coul = 0.0f;
         if (pin) {
             float f;
             e_pair = sc * pair_mixed(p, r2, inv_r2, inv_r, f);
@@ -179,67 +160,129 @@ __global__ void __launch_bounds__(256) pair_mixed_kernel(
                 fr += csc * qq * (factor - (float)s.wolf_fc) * inv_r;
             }
         }
-        float gx = fr * dx, gy = fr * dy, gz = fr * dz;
-        two_sum_acc(fxs, fxc, gx);
-        two_sum_acc(fys, fyc, gy);
-        two_sum_acc(fzs, fzc, gz);
-        if (EV && js > tt) {  // each unordered pair once (the list is symmetric)
-            ep += (double)e_pair;
-            ec += (double)e_coul;
-            w0 += (double)(gx * dx);
-            w1 += (double)(gx * dy);
-            w2 += (double)(gx * dz);
-            w3 += (double)(gy * dy);
-            w4 += (double)(gy * dz);
-            w5 += (double)(gz * dz);
-        }
     }
-    double fx = group_sum_comp<TPA>(fxs, fxc);
-    double fy = group_sum_comp<TPA>(fys, fyc);
-    double fz = group_sum_comp<TPA>(fzs, fzc);
+    float gx = fr * dx, gy = fr * dy, gz = fr * dz;
+    two_sum_acc(A.fxs, A.fxc, gx);
+    two_sum_acc(A.fys, A.fyc, gy);
+    two_sum_acc(A.fzs, A.fzc, gz);
+    if (EV && js > tt) {  // each unordered pair once (the list is symmetric)
+        A.ep += (double)e_pair;
+        A.ec += (double)e_coul;
+        A.w0 += (double)(gx * dx);
+        A.w1 += (double)(gx * dy);
+        A.w2 += (double)(gx * dz);
+        A.w3 += (double)(gy * dy);
+        A.w4 += (double)(gy * dz);
+        A.w5 += (double)(gz * dz);
+    }
+}
+
+template <int TPA, bool EV, bool GENERAL>
+__global__ void __launch_bounds__(256) pair_mixed_kernel(
+    int n, const uint4* __restrict__ pfx, const int2* __restrict__ km, const int* __restrict__ order,
+    const int* __restrict__ sysid, const SysDev* __restrict__ sys,
+    const PairDevF* __restrict__ ptab, const int* __restrict__ nbr, const int* __restrict__ nnb, int maxnb,
+    const int* __restrict__ spec_off, const int* __restrict__ spec_j, const int8_t* __restrict__ spec_path,
+    uint32_t terms, double* __restrict__ force, double* __restrict__ red) {
+    // t walks the cell-sorted order; i is the atom's own index (forces, bond paths)
+    int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    int t = gt / TPA;
+    int sub = gt % TPA;
+    bool active = t < n;
+    int tt = active ? t : n - 1;
+    int i = order[tt];
+    const SysDev& s = sys[sysid[tt]];
+    uint4 pi = pfx[tt];
+    float qi = __uint_as_float(pi.w);
+    int2 kmi = km[tt];
+    const PairDevF* prow = ptab + s.ptab + kmi.x * s.nk;
+    bool coul = GENERAL && (terms & 16u) && s.coul != 0 && qi != 0.0f;
+    bool pairs = (terms & 1u) != 0;
+    float coul_rc2 = GENERAL ? s.coul_rc2_f : 0.0f;
+    float alpha = GENERAL ? (float)s.alpha : 0.0f;
+    float pref = qi * (float)(1.0 / FOUR_PI_EPSILON_0);
+    MixedAcc A;
+    int cnt = active ? nnb[tt] : 0;
+    const int* list = nbr + (size_t)tt * maxnb;
+    // two entries per lane per iteration: their loads are in flight together
+    int k = sub;
+    for (; k + TPA < cnt; k += 2 * TPA) {
+        int js0 = list[k], js1 = list[k + TPA];
+        uint4 pj0 = pfx[js0], pj1 = pfx[js1];
+        int2 km0 = km[js0], km1 = km[js1];
+        mixed_entry<EV, GENERAL>(A, s, prow, pi, qi, kmi.y, i, tt, js0, pj0, km0, order, spec_off, spec_j, spec_path,
+                                 pairs, coul, coul_rc2, alpha, pref);
+        mixed_entry<EV, GENERAL>(A, s, prow, pi, qi, kmi.y, i, tt, js1, pj1, km1, order, spec_off, spec_j, spec_path,
+                                 pairs, coul, coul_rc2, alpha, pref);
+    }
+    if (k < cnt) {
+        int js = list[k];
+        mixed_entry<EV, GENERAL>(A, s, prow, pi, qi, kmi.y, i, tt, js, pfx[js], km[js], order, spec_off, spec_j,
+                                 spec_path, pairs, coul, coul_rc2, alpha, pref);
+    }
+    // combine the group's compensated sums (FP32 shuffles); one lane converts to FP64
+#pragma unroll
+    for (int o = TPA / 2; o > 0; o >>= 1) {
+        float sx = __shfl_xor_sync(0xffffffffu, A.fxs, o), cx = __shfl_xor_sync(0xffffffffu, A.fxc, o);
+        float sy = __shfl_xor_sync(0xffffffffu, A.fys, o), cy = __shfl_xor_sync(0xffffffffu, A.fyc, o);
+        float sz = __shfl_xor_sync(0xffffffffu, A.fzs, o), cz = __shfl_xor_sync(0xffffffffu, A.fzc, o);
+        two_sum_acc(A.fxs, A.fxc, sx);
+        A.fxc += cx;
+        two_sum_acc(A.fys, A.fyc, sy);
+        A.fyc += cy;
+        two_sum_acc(A.fzs, A.fzc, sz);
+        A.fzc += cz;
+    }
     if (EV) {
-        ep = group_sum_d<TPA>(ep);
-        ec = group_sum_d<TPA>(ec);
-        w0 = group_sum_d<TPA>(w0);
-        w1 = group_sum_d<TPA>(w1);
-        w2 = group_sum_d<TPA>(w2);
-        w3 = group_sum_d<TPA>(w3);
-        w4 = group_sum_d<TPA>(w4);
-        w5 = group_sum_d<TPA>(w5);
+        A.ep = group_sum_d<TPA>(A.ep);
+        A.ec = group_sum_d<TPA>(A.ec);
+        A.w0 = group_sum_d<TPA>(A.w0);
+        A.w1 = group_sum_d<TPA>(A.w1);
+        A.w2 = group_sum_d<TPA>(A.w2);
+        A.w3 = group_sum_d<TPA>(A.w3);
+        A.w4 = group_sum_d<TPA>(A.w4);
+        A.w5 = group_sum_d<TPA>(A.w5);
     }
-    if (active && sub == 0) {
-        force[3 * i] += fx;
-        force[3 * i + 1] += fy;
-        force[3 * i + 2] += fz;
+    if (active && sub == 0) {  // the first force kernel of a step: assigns
+        force[3 * i] = (double)A.fxs + (double)A.fxc;
+        force[3 * i + 1] = (double)A.fys + (double)A.fyc;
+        force[3 * i + 2] = (double)A.fzs + (double)A.fzc;
         if (EV) {
-            if ((terms & 16u) && s.coul == 2 && qi != 0.0f) {
+            double ec = A.ec;
+            if (GENERAL && (terms & 16u) && s.coul == 2 && qi != 0.0f) {
                 double q = (double)qi;
                 ec -= q * q * 0.5 * (s.wolf_ec + s.alpha * FRAC_2_SQRT_PI) / FOUR_PI_EPSILON_0;
             }
             double* rr = red + (size_t)i * RED_STRIDE;
-            rr[E_PAIRS] += ep;
+            rr[E_PAIRS] += A.ep;
             rr[E_COUL] += ec;
             double* w = rr + N_ESLOT;
-            w[0] += w0; w[1] += w1; w[2] += w2;
-            w[3] += w1; w[4] += w3; w[5] += w4;
-            w[6] += w2; w[7] += w4; w[8] += w5;
+            w[0] += A.w0; w[1] += A.w1; w[2] += A.w2;
+            w[3] += A.w1; w[4] += A.w3; w[5] += A.w4;
+            w[6] += A.w2; w[7] += A.w4; w[8] += A.w5;
         }
     }
 }
 
-template <int TPA>
-void launch_pair_mixed_tpa(const Batch& b, uint32_t terms, bool ev, cudaStream_t st) {
+template <int TPA, bool GENERAL>
+void launch_pair_mixed_variant(const Batch& b, uint32_t terms, bool ev, cudaStream_t st) {
     int tb = 256;
     long long threads = (long long)b.n * TPA;
     unsigned grid = (unsigned)((threads + tb - 1) / tb);
     if (ev)
-        pair_mixed_kernel<TPA, true><<<grid, tb, 0, st>>>(b.n, b.posfx, b.km, b.cell_atoms, b.sysid, b.sys,
-                                                          b.ptabf, b.nbr, b.nnb, b.maxnb, b.spec_off, b.spec_j,
-                                                          b.spec_path, terms, b.force, b.red);
+        pair_mixed_kernel<TPA, true, GENERAL><<<grid, tb, 0, st>>>(
+            b.n, b.posfx, b.km, b.cell_atoms, b.sysid, b.sys, b.ptabf, b.nbr, b.nnb, b.maxnb, b.spec_off, b.spec_j,
+            b.spec_path, terms, b.force, b.red);
     else
-        pair_mixed_kernel<TPA, false><<<grid, tb, 0, st>>>(b.n, b.posfx, b.km, b.cell_atoms, b.sysid, b.sys,
-                                                           b.ptabf, b.nbr, b.nnb, b.maxnb, b.spec_off, b.spec_j,
-                                                           b.spec_path, terms, b.force, b.red);
+        pair_mixed_kernel<TPA, false, GENERAL><<<grid, tb, 0, st>>>(
+            b.n, b.posfx, b.km, b.cell_atoms, b.sysid, b.sys, b.ptabf, b.nbr, b.nnb, b.maxnb, b.spec_off, b.spec_j,
+            b.spec_path, terms, b.force, b.red);
+}
+
+template <int TPA>
+void launch_pair_mixed_tpa(const Batch& b, uint32_t terms, bool ev, cudaStream_t st) {
+    if (b.pair_general) launch_pair_mixed_variant<TPA, true>(b, terms, ev, st);
+    else launch_pair_mixed_variant<TPA, false>(b, terms, ev, st);
 }
 
 void launch_pair_mixed(const Batch& b, uint32_t terms, bool ev, cudaStream_t st) {
@@ -254,24 +297,13 @@ void launch_pair_mixed(const Batch& b, uint32_t terms, bool ev, cudaStream_t st)
     }
 }
 
-// Fixed-point copy of the wrapped FP64 positions (UnitCell::wrap_vector):
-// u = floor(frac(x / L) * 2^32), and the charge's FP32 bits.
+// Fixed-point copy of the wrapped FP64 positions in the cell-sorted order.
 __global__ void fixed_positions_kernel(int n, const double4_32a* __restrict__ posq, const int* __restrict__ sysid,
                                        const SysDev* __restrict__ sys, const int* __restrict__ order,
                                        uint4* __restrict__ pfx) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;  // cell-sorted position
     if (t >= n) return;
-    const SysDev& s = sys[sysid[t]];
-    double4_32a p = posq[order[t]];
-    double w[3] = {p.x, p.y, p.z};
-    uint32_t u[3];
-    for (int d = 0; d < 3; d++) {
-        double f = w[d] * s.invL[d];
-        f -= floor(f);
-        unsigned long long q = (unsigned long long)(f * 4294967296.0);
-        u[d] = (uint32_t)(q & 0xffffffffull);
-    }
-    pfx[t] = make_uint4(u[0], u[1], u[2], __float_as_uint((float)p.w));
+    pfx[t] = fixed_position(sys[sysid[t]], posq[order[t]]);
 }
 
 void launch_split_positions(const Batch& b, cudaStream_t st) {

@@ -18,31 +18,113 @@
 
 namespace lg {
 
+// Rebuild plan: the systems whose list is rebuilt at this build, with prefix
+// sums of their atom and cell counts, so that every later kernel walks only
+// their atoms and cells (a step in which one system of a large batch rebuilds
+// costs that system's work, not the batch's).  Layout of `plan`: R, then the R
+// system indices (room for nsys), then R + 1 atom prefix sums, then R + 1 cell
+// prefix sums (each with room for nsys + 1).
+struct PlanView {
+    int R;
+    const int* sys;
+    const int* apre;
+    const int* cpre;
+};
+
+__device__ __forceinline__ PlanView plan_view(const int* plan, int nsys) {
+    return PlanView{plan[0], plan + 1, plan + 1 + nsys, plan + 2 + 2 * nsys};
+}
+
+// index r of the planned system holding virtual index v: the last r with pre[r] <= v
+__device__ __forceinline__ int plan_find(const int* pre, int R, int v) {
+    int a = 0, b = R - 1;
+    while (a < b) {
+        int mid = (a + b + 1) >> 1;
+        if (pre[mid] <= v) a = mid;
+        else b = mid - 1;
+    }
+    return a;
+}
+
+__global__ void __launch_bounds__(1024) nl_plan_kernel(int nsys, const uint32_t* __restrict__ status,
+                                                       const uint32_t* __restrict__ sys_rebuild,
+                                                       const SysDev* __restrict__ sys, int* __restrict__ plan) {
+    if (!(*status & ST_REBUILD)) return;
+    __shared__ int s_r[1024], s_a[1024], s_c[1024];
+    int t = threadIdx.x;
+    int per = (nsys + blockDim.x - 1) / blockDim.x;
+    int lo = min(t * per, nsys), hi = min(lo + per, nsys);
+    int r = 0, a = 0, c = 0;
+    for (int s = lo; s < hi; s++)
+        if (sys_rebuild[s]) {
+            const SysDev& d = sys[s];
+            r += 1;
+            a += d.end - d.begin;
+            c += d.ncell[0] * d.ncell[1] * d.ncell[2];
+        }
+    s_r[t] = r;
+    s_a[t] = a;
+    s_c[t] = c;
+    __syncthreads();
+    for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+        int vr = t >= o ? s_r[t - o] : 0;
+        int va = t >= o ? s_a[t - o] : 0;
+        int vc = t >= o ? s_c[t - o] : 0;
+        __syncthreads();
+        s_r[t] += vr;
+        s_a[t] += va;
+        s_c[t] += vc;
+        __syncthreads();
+    }
+    int* sl = plan + 1;
+    int* apre = plan + 1 + nsys;
+    int* cpre = plan + 2 + 2 * nsys;
+    int rr = s_r[t] - r, aa = s_a[t] - a, cc = s_c[t] - c;
+    for (int s = lo; s < hi; s++)
+        if (sys_rebuild[s]) {
+            const SysDev& d = sys[s];
+            sl[rr] = s;
+            apre[rr] = aa;
+            cpre[rr] = cc;
+            rr += 1;
+            aa += d.end - d.begin;
+            cc += d.ncell[0] * d.ncell[1] * d.ncell[2];
+        }
+    if (t == (int)blockDim.x - 1) {
+        plan[0] = s_r[t];
+        apre[s_r[t]] = s_a[t];
+        cpre[s_r[t]] = s_c[t];
+    }
+}
+
 // Atom pass: cell index of each atom from its wrapped position
 // (UnitCell::wrap_vector, cells.rs:263-282), FP32 wrapped copy, reference
 // position for the displacement test.
-__global__ void nl_bin_kernel(int n, const double4_32a* __restrict__ posq, const int* __restrict__ sysid,
+__global__ void nl_bin_kernel(int nsys, const int* __restrict__ plan, const double4_32a* __restrict__ posq,
                               const SysDev* __restrict__ sys, const uint32_t* __restrict__ status,
-                              const uint32_t* __restrict__ sys_rebuild, int* __restrict__ atom_cell,
-                              int* __restrict__ cell_count, float4* __restrict__ wpos,
+                              int* __restrict__ atom_cell, int* __restrict__ cell_count, float4* __restrict__ wpos,
                               double4_32a* __restrict__ pos_build) {
     if (!(*status & ST_REBUILD)) return;
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || !sys_rebuild[sysid[i]]) return;
-    const SysDev& s = sys[sysid[i]];
-    double4_32a p = posq[i];
-    double w[3] = {p.x, p.y, p.z};
-    int c[3];
-    for (int d = 0; d < 3; d++) {
-        w[d] -= floor(w[d] / s.L[d]) * s.L[d];
-        int cd = (int)(w[d] * s.invL[d] * (double)s.ncell[d]);
-        c[d] = min(max(cd, 0), s.ncell[d] - 1);
+    PlanView pv = plan_view(plan, nsys);
+    int A = pv.apre[pv.R];
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < A; v += gridDim.x * blockDim.x) {
+        int r = plan_find(pv.apre, pv.R, v);
+        const SysDev& s = sys[pv.sys[r]];
+        int i = s.begin + (v - pv.apre[r]);
+        double4_32a p = posq[i];
+        double w[3] = {p.x, p.y, p.z};
+        int c[3];
+        for (int d = 0; d < 3; d++) {
+            w[d] -= floor(w[d] / s.L[d]) * s.L[d];
+            int cd = (int)(w[d] * s.invL[d] * (double)s.ncell[d]);
+            c[d] = min(max(cd, 0), s.ncell[d] - 1);
+        }
+        int cell = s.cell_begin + (c[2] * s.ncell[1] + c[1]) * s.ncell[0] + c[0];
+        atom_cell[i] = cell;
+        atomicAdd(&cell_count[cell], 1);
+        wpos[i] = make_float4((float)w[0], (float)w[1], (float)w[2], (float)p.w);
+        pos_build[i] = p;
     }
-    int cell = s.cell_begin + (c[2] * s.ncell[1] + c[1]) * s.ncell[0] + c[0];
-    atom_cell[i] = cell;
-    atomicAdd(&cell_count[cell], 1);
-    wpos[i] = make_float4((float)w[0], (float)w[1], (float)w[2], (float)p.w);
-    pos_build[i] = p;
 }
 
 // Exclusive scan of the cell counts of one system (one block per rebuilding
@@ -50,106 +132,128 @@ __global__ void nl_bin_kernel(int n, const double4_32a* __restrict__ posq, const
 // its start array has one slot per cell plus an end sentinel, at
 // cell_start[cell + system index].  Also zeroes the counts for the scatter.
 __global__ void __launch_bounds__(1024) nl_scan_kernel(int nsys, const uint32_t* __restrict__ status,
-                                                       const uint32_t* __restrict__ sys_rebuild,
+                                                       const int* __restrict__ plan,
                                                        const SysDev* __restrict__ sys, int* __restrict__ cell_count,
                                                        int* __restrict__ cell_start) {
     if (!(*status & ST_REBUILD)) return;
-    int s = blockIdx.x;
-    if (!sys_rebuild[s]) return;
+    PlanView pv = plan_view(plan, nsys);
     __shared__ int partial[1024];
-    const SysDev& d = sys[s];
-    int ncells = d.ncell[0] * d.ncell[1] * d.ncell[2];
-    int* count = cell_count + d.cell_begin;
-    int* start = cell_start + d.cell_begin + s;
-    int t = threadIdx.x;
-    int per = (ncells + blockDim.x - 1) / blockDim.x;
-    int lo = min(t * per, ncells), hi = min(lo + per, ncells);
-    int sum = 0;
-    for (int c = lo; c < hi; c++) sum += count[c];
-    partial[t] = sum;
-    __syncthreads();
-    for (int o = 1; o < (int)blockDim.x; o <<= 1) {
-        int v = t >= o ? partial[t - o] : 0;
+    for (int r = blockIdx.x; r < pv.R; r += gridDim.x) {
+        int s = pv.sys[r];
+        const SysDev& d = sys[s];
+        int ncells = d.ncell[0] * d.ncell[1] * d.ncell[2];
+        int* count = cell_count + d.cell_begin;
+        int* start = cell_start + d.cell_begin + s;
+        int t = threadIdx.x;
+        int per = (ncells + blockDim.x - 1) / blockDim.x;
+        int lo = min(t * per, ncells), hi = min(lo + per, ncells);
+        int sum = 0;
+        for (int c = lo; c < hi; c++) sum += count[c];
+        __syncthreads();  // the previous system's readers of partial are done
+        partial[t] = sum;
         __syncthreads();
-        partial[t] += v;
-        __syncthreads();
+        for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+            int v = t >= o ? partial[t - o] : 0;
+            __syncthreads();
+            partial[t] += v;
+            __syncthreads();
+        }
+        int run = d.begin + partial[t] - sum;
+        for (int c = lo; c < hi; c++) {
+            start[c] = run;
+            run += count[c];
+            count[c] = 0;
+        }
+        if (t == (int)blockDim.x - 1) start[ncells] = d.begin + partial[t];
     }
-    int run = d.begin + partial[t] - sum;
-    for (int c = lo; c < hi; c++) {
-        start[c] = run;
-        run += count[c];
-        count[c] = 0;
-    }
-    if (t == blockDim.x - 1) start[ncells] = d.begin + partial[t];
 }
 
-__global__ void nl_scatter_kernel(int n, const uint32_t* __restrict__ status, const int* __restrict__ sysid,
-                                  const uint32_t* __restrict__ sys_rebuild, const int* __restrict__ atom_cell,
+__global__ void nl_scatter_kernel(int nsys, const int* __restrict__ plan, const uint32_t* __restrict__ status,
+                                  const SysDev* __restrict__ sys, const int* __restrict__ atom_cell,
                                   int* __restrict__ cell_count, const int* __restrict__ cell_start,
                                   int* __restrict__ cell_atoms) {
     if (!(*status & ST_REBUILD)) return;
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int s = sysid[i];
-    if (!sys_rebuild[s]) return;
-    int c = atom_cell[i];
-    int slot = atomicAdd(&cell_count[c], 1);
-    cell_atoms[cell_start[c + s] + slot] = i;
+    PlanView pv = plan_view(plan, nsys);
+    int A = pv.apre[pv.R];
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < A; v += gridDim.x * blockDim.x) {
+        int r = plan_find(pv.apre, pv.R, v);
+        int s = pv.sys[r];
+        int i = sys[s].begin + (v - pv.apre[r]);
+        int c = atom_cell[i];
+        int slot = atomicAdd(&cell_count[c], 1);
+        cell_atoms[cell_start[c + s] + slot] = i;
+    }
 }
 
 // Sort each cell's atoms by index so that the list order (and so the order of
-// the force sums) does not depend on the atomics above: one block per cell,
-// each atom's slot is its rank among the cell's atoms (indices are distinct).
+// the force sums) does not depend on the atomics above: blocks walk the planned
+// cells, each atom's slot is its rank among the cell's atoms (indices are
+// distinct).  Leaves the counts at zero for the next build.
 constexpr int SORT_SMEM = 2048;
 
-__global__ void __launch_bounds__(128) nl_sort_kernel(int ncells, const uint32_t* __restrict__ status,
-                                                      const uint32_t* __restrict__ sys_rebuild,
-                                                      const int* __restrict__ cell_sys,
+__global__ void __launch_bounds__(128) nl_sort_kernel(int nsys, const int* __restrict__ plan,
+                                                      const uint32_t* __restrict__ status,
+                                                      const SysDev* __restrict__ sys,
                                                       const int* __restrict__ cell_start,
                                                       int* __restrict__ cell_atoms, int* __restrict__ cell_count) {
     if (!(*status & ST_REBUILD)) return;
     __shared__ int buf[SORT_SMEM];
-    int c = blockIdx.x;
-    int s = cell_sys[c];
-    if (threadIdx.x == 0) cell_count[c] = 0;  // ready for the next binning pass
-    if (!sys_rebuild[s]) return;
-    int lo = cell_start[c + s], hi = cell_start[c + s + 1];
-    int m = hi - lo;
-    if (m <= 1) return;
-    if (m <= SORT_SMEM) {
-        for (int a = threadIdx.x; a < m; a += blockDim.x) buf[a] = cell_atoms[lo + a];
-        __syncthreads();
-        for (int a = threadIdx.x; a < m; a += blockDim.x) {
-            int v = buf[a], rank = 0;
-            for (int b = 0; b < m; b++) rank += buf[b] < v;
-            cell_atoms[lo + rank] = v;
-        }
-    } else if (threadIdx.x == 0) {
-        // very crowded cell: serial insertion sort in place
-        for (int a = lo + 1; a < hi; a++) {
-            int v = cell_atoms[a];
-            int b = a - 1;
-            while (b >= lo && cell_atoms[b] > v) {
-                cell_atoms[b + 1] = cell_atoms[b];
-                b--;
+    PlanView pv = plan_view(plan, nsys);
+    int C = pv.cpre[pv.R];
+    for (int vc = blockIdx.x; vc < C; vc += gridDim.x) {
+        int r = plan_find(pv.cpre, pv.R, vc);
+        int s = pv.sys[r];
+        int c = sys[s].cell_begin + (vc - pv.cpre[r]);
+        if (threadIdx.x == 0) cell_count[c] = 0;
+        int lo = cell_start[c + s], hi = cell_start[c + s + 1];
+        int m = hi - lo;
+        if (m <= 1) continue;
+        if (m <= SORT_SMEM) {
+            __syncthreads();  // the previous cell's readers of buf are done
+            for (int a = threadIdx.x; a < m; a += blockDim.x) buf[a] = cell_atoms[lo + a];
+            __syncthreads();
+            for (int a = threadIdx.x; a < m; a += blockDim.x) {
+                int v = buf[a], rank = 0;
+                for (int b = 0; b < m; b++) rank += buf[b] < v;
+                cell_atoms[lo + rank] = v;
             }
-            cell_atoms[b + 1] = v;
+        } else if (threadIdx.x == 0) {
+            // very crowded cell: serial insertion sort in place
+            for (int a = lo + 1; a < hi; a++) {
+                int v = cell_atoms[a];
+                int b = a - 1;
+                while (b >= lo && cell_atoms[b] > v) {
+                    cell_atoms[b + 1] = cell_atoms[b];
+                    b--;
+                }
+                cell_atoms[b + 1] = v;
+            }
         }
     }
 }
 
 // Position of every atom in the cell-sorted order (perm) and the sorted copies
-// of kind and molecule the mixed kernels read.  Systems that did not rebuild
-// keep their order, so rewriting their entries changes nothing.
-__global__ void nl_perm_kernel(int n, const uint32_t* __restrict__ status, const int* __restrict__ cell_atoms,
-                               const int* __restrict__ kind, const int* __restrict__ mol, int* __restrict__ perm,
-                               int2* __restrict__ km) {
+// of kind, molecule and fixed-point position the mixed kernels read, for the
+// planned systems.
+__global__ void nl_perm_kernel(int nsys, const int* __restrict__ plan, const uint32_t* __restrict__ status,
+                               const SysDev* __restrict__ sys, const int* __restrict__ cell_atoms,
+                               const int* __restrict__ kind, const int* __restrict__ mol,
+                               const double4_32a* __restrict__ posq, int* __restrict__ perm, int2* __restrict__ km,
+                               uint4* __restrict__ posfx, uint4* __restrict__ pfx_build) {
     if (!(*status & ST_REBUILD)) return;
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    int i = cell_atoms[t];
-    perm[i] = t;
-    km[t] = make_int2(kind[i], mol[i]);
+    PlanView pv = plan_view(plan, nsys);
+    int A = pv.apre[pv.R];
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < A; v += gridDim.x * blockDim.x) {
+        int r = plan_find(pv.apre, pv.R, v);
+        const SysDev& s = sys[pv.sys[r]];
+        int t = s.begin + (v - pv.apre[r]);
+        int i = cell_atoms[t];
+        perm[i] = t;
+        km[t] = make_int2(kind[i], mol[i]);
+        uint4 u = fixed_position(s, posq[i]);
+        posfx[t] = u;
+        pfx_build[i] = u;  // reference point of the displacement test
+    }
 }
 
 // Stencil cells of one dimension: c-1, c, c+1 (periodic) when there are at
@@ -166,99 +270,103 @@ __device__ __forceinline__ int stencil_cells(int c, int nc, int* out) {
 }
 
 // Warp per atom: keep j != i whose FP32 minimum-image distance is below
-// rlist (plus margin).  The stencil cells are flattened into one range of
-// candidates (per-warp prefix sums of the cell populations in shared memory),
-// so all 32 lanes test candidates even when cells hold a few atoms; candidates
-// keep the cell-then-index order.  Full list: each pair appears in the lists
-// of both atoms.
+// rlist (plus margin).  Warps walk the planned systems' atoms in cell order
+// (neighbouring warps share a stencil).  The stencil cells are flattened into
+// one range of candidates (per-warp prefix sums of the cell populations in
+// shared memory), so all 32 lanes test candidates even when cells hold a few
+// atoms; candidates keep the cell-then-index order.  Full list: each pair
+// appears in the lists of both atoms.
 constexpr int NL_WARPS = 8;
 
 __global__ void __launch_bounds__(32 * NL_WARPS) nl_build_kernel(
-    int n, const uint32_t* status, const uint32_t* __restrict__ sys_rebuild, const int* __restrict__ sysid,
-    const SysDev* __restrict__ sys, const float4* __restrict__ wpos, const int* __restrict__ atom_cell,
-    const int* __restrict__ cell_start, const int* __restrict__ cell_atoms, const int* __restrict__ perm,
-    int maxnb, int* __restrict__ nbr, int* __restrict__ nnb, uint32_t* status_out) {
+    int nsys, const int* __restrict__ plan, const uint32_t* status, const SysDev* __restrict__ sys,
+    const float4* __restrict__ wpos, const int* __restrict__ atom_cell, const int* __restrict__ cell_start,
+    const int* __restrict__ cell_atoms, const int* __restrict__ perm, int maxnb, int* __restrict__ nbr,
+    int* __restrict__ nnb, uint32_t* status_out) {
     __shared__ int s_lo[NL_WARPS][28];
     __shared__ int s_pre[NL_WARPS][28];
     if (!(*status & ST_REBUILD)) return;
+    PlanView pv = plan_view(plan, nsys);
+    int A = pv.apre[pv.R];
     int wib = threadIdx.x >> 5;
-    int w = blockIdx.x * NL_WARPS + wib;
     int lane = threadIdx.x & 31;
-    if (w >= n) return;
-    int i = cell_atoms[w];  // warps walk the atoms cell by cell: neighbouring warps share a stencil
-    int si = sysid[i];
-    if (!sys_rebuild[si]) return;  // this system keeps its list
-    const SysDev& s = sys[si];
-    float4 pi = wpos[i];
-    int local = atom_cell[i] - s.cell_begin;
-    int cx = local % s.ncell[0];
-    int cy = (local / s.ncell[0]) % s.ncell[1];
-    int cz = local / (s.ncell[0] * s.ncell[1]);
-    int sx[3], sy[3], sz[3];
-    int nx = stencil_cells(cx, s.ncell[0], sx);
-    int ny = stencil_cells(cy, s.ncell[1], sy);
-    int nz = stencil_cells(cz, s.ncell[2], sz);
-    int ncand = nx * ny * nz;
-    // lane c < ncand owns stencil cell c (z, y, x order)
-    int cnt = 0, lo = 0;
-    if (lane < ncand) {
-        int a = lane / (nx * ny), b = (lane / nx) % ny, c = lane % nx;
-        int cell = s.cell_begin + (sz[a] * s.ncell[1] + sy[b]) * s.ncell[0] + sx[c];
-        lo = cell_start[cell + si];
-        cnt = cell_start[cell + si + 1] - lo;
-    }
-    int incl = cnt;
-    for (int o = 1; o < 32; o <<= 1) {
-        int v = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += v;
-    }
-    int total = __shfl_sync(0xffffffffu, incl, 31);
-    if (lane < ncand) {
-        s_lo[wib][lane] = lo;
-        s_pre[wib][lane] = incl - cnt;
-    }
-    if (lane == 0) s_pre[wib][ncand] = total;
-    __syncwarp();
-    float Lx = s.Lf[0], Ly = s.Lf[1], Lz = s.Lf[2];
-    float ix = s.invLf[0], iy = s.invLf[1], iz = s.invLf[2];
-    float rl2 = s.rlist2_f;
-    int count = 0;
-    // with a cell-sorted order (mixed path) the row and its entries are sorted positions
-    int row = perm ? perm[i] : i;
-    int* out = nbr + (size_t)row * maxnb;
-    for (int base = 0; base < total; base += 32) {
-        int t = base + lane;
-        bool keep = false;
-        int j = -1, jout = -1;
-        if (t < total) {
-            // the stencil cell holding candidate t: last c with pre[c] <= t
-            int a = 0, b = ncand - 1;
-            while (a < b) {
-                int mid = (a + b + 1) >> 1;
-                if (s_pre[wib][mid] <= t) a = mid;
-                else b = mid - 1;
+    for (int w = blockIdx.x * NL_WARPS + wib; w < A; w += gridDim.x * NL_WARPS) {
+        int r = plan_find(pv.apre, pv.R, w);
+        int si = pv.sys[r];
+        const SysDev& s = sys[si];
+        int i = cell_atoms[s.begin + (w - pv.apre[r])];
+        float4 pi = wpos[i];
+        int local = atom_cell[i] - s.cell_begin;
+        int cx = local % s.ncell[0];
+        int cy = (local / s.ncell[0]) % s.ncell[1];
+        int cz = local / (s.ncell[0] * s.ncell[1]);
+        int sx[3], sy[3], sz[3];
+        int nx = stencil_cells(cx, s.ncell[0], sx);
+        int ny = stencil_cells(cy, s.ncell[1], sy);
+        int nz = stencil_cells(cz, s.ncell[2], sz);
+        int ncand = nx * ny * nz;
+        // lane c < ncand owns stencil cell c (z, y, x order)
+        int cnt = 0, lo = 0;
+        if (lane < ncand) {
+            int a = lane / (nx * ny), b = (lane / nx) % ny, c = lane % nx;
+            int cell = s.cell_begin + (sz[a] * s.ncell[1] + sy[b]) * s.ncell[0] + sx[c];
+            lo = cell_start[cell + si];
+            cnt = cell_start[cell + si + 1] - lo;
+        }
+        int incl = cnt;
+        for (int o = 1; o < 32; o <<= 1) {
+            int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        int total = __shfl_sync(0xffffffffu, incl, 31);
+        __syncwarp();  // the previous atom's readers of s_lo / s_pre are done
+        if (lane < ncand) {
+            s_lo[wib][lane] = lo;
+            s_pre[wib][lane] = incl - cnt;
+        }
+        if (lane == 0) s_pre[wib][ncand] = total;
+        __syncwarp();
+        float Lx = s.Lf[0], Ly = s.Lf[1], Lz = s.Lf[2];
+        float ix = s.invLf[0], iy = s.invLf[1], iz = s.invLf[2];
+        float rl2 = s.rlist2_f;
+        int count = 0;
+        // with a cell-sorted order (mixed path) the row and its entries are sorted positions
+        int row = perm ? perm[i] : i;
+        int* out = nbr + (size_t)row * maxnb;
+        for (int base = 0; base < total; base += 32) {
+            int t = base + lane;
+            bool keep = false;
+            int j = -1, jout = -1;
+            if (t < total) {
+                // the stencil cell holding candidate t: last c with pre[c] <= t
+                int a = 0, b = ncand - 1;
+                while (a < b) {
+                    int mid = (a + b + 1) >> 1;
+                    if (s_pre[wib][mid] <= t) a = mid;
+                    else b = mid - 1;
+                }
+                int slot = s_lo[wib][a] + (t - s_pre[wib][a]);
+                j = cell_atoms[slot];
+                jout = perm ? slot : j;
+                float4 pj = wpos[j];
+                float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+                dx -= rintf(dx * ix) * Lx;
+                dy -= rintf(dy * iy) * Ly;
+                dz -= rintf(dz * iz) * Lz;
+                float r2 = dx * dx + dy * dy + dz * dz;
+                keep = (j != i) && (r2 < rl2);
             }
-            int slot = s_lo[wib][a] + (t - s_pre[wib][a]);
-            j = cell_atoms[slot];
-            jout = perm ? slot : j;
-            float4 pj = wpos[j];
-            float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-            dx -= rintf(dx * ix) * Lx;
-            dy -= rintf(dy * iy) * Ly;
-            dz -= rintf(dz * iz) * Lz;
-            float r2 = dx * dx + dy * dy + dz * dz;
-            keep = (j != i) && (r2 < rl2);
+            unsigned mask = __ballot_sync(0xffffffffu, keep);
+            if (keep) {
+                int pos = count + __popc(mask & ((1u << lane) - 1u));
+                if (pos < maxnb) out[pos] = jout;
+            }
+            count += __popc(mask);
         }
-        unsigned mask = __ballot_sync(0xffffffffu, keep);
-        if (keep) {
-            int pos = count + __popc(mask & ((1u << lane) - 1u));
-            if (pos < maxnb) out[pos] = jout;
+        if (lane == 0) {
+            nnb[row] = min(count, maxnb);
+            if (count > maxnb) atomicOr(status_out, ST_OVERFLOW);
         }
-        count += __popc(mask);
-    }
-    if (lane == 0) {
-        nnb[row] = min(count, maxnb);
-        if (count > maxnb) atomicOr(status_out, ST_OVERFLOW);
     }
 }
 
@@ -274,18 +382,26 @@ void launch_nlist_build(const Batch& b, cudaStream_t st) {
     int n = b.n;
     if (n == 0) return;
     int tb = 256;
-    nl_bin_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, b.posq, b.sysid, b.sys, b.status, b.sys_rebuild,
-                                                  b.atom_cell, b.cell_count, b.wpos, b.pos_build);
-    nl_scan_kernel<<<b.nsys, 1024, 0, st>>>(b.nsys, b.status, b.sys_rebuild, b.sys, b.cell_count, b.cell_start);
-    nl_scatter_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, b.status, b.sysid, b.sys_rebuild, b.atom_cell,
-                                                      b.cell_count, b.cell_start, b.cell_atoms);
-    nl_sort_kernel<<<b.ncells, 128, 0, st>>>(b.ncells, b.status, b.sys_rebuild, b.cell_sys, b.cell_start,
-                                             b.cell_atoms, b.cell_count);
+    // grid-stride kernels: enough blocks to fill the device at a full rebuild,
+    // few enough that a step with a small (or no) rebuild costs little
+    unsigned atoms_grid = (unsigned)std::min((n + tb - 1) / tb, 4 * b.sms);
+    unsigned cells_grid = (unsigned)std::min(b.ncells, 16 * b.sms);
+    unsigned build_grid = (unsigned)std::min((n + NL_WARPS - 1) / NL_WARPS, 8 * b.sms);
+    unsigned scan_grid = (unsigned)std::min(b.nsys, 2 * b.sms);
+    nl_plan_kernel<<<1, 1024, 0, st>>>(b.nsys, b.status, b.sys_rebuild, b.sys, b.plan);
+    nl_bin_kernel<<<atoms_grid, tb, 0, st>>>(b.nsys, b.plan, b.posq, b.sys, b.status, b.atom_cell, b.cell_count,
+                                             b.wpos, b.pos_build);
+    nl_scan_kernel<<<scan_grid, 1024, 0, st>>>(b.nsys, b.status, b.plan, b.sys, b.cell_count, b.cell_start);
+    nl_scatter_kernel<<<atoms_grid, tb, 0, st>>>(b.nsys, b.plan, b.status, b.sys, b.atom_cell, b.cell_count,
+                                                 b.cell_start, b.cell_atoms);
+    nl_sort_kernel<<<cells_grid, 128, 0, st>>>(b.nsys, b.plan, b.status, b.sys, b.cell_start, b.cell_atoms,
+                                               b.cell_count);
     if (b.perm)
-        nl_perm_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(n, b.status, b.cell_atoms, b.kind, b.mol, b.perm, b.km);
-    nl_build_kernel<<<(unsigned)((n + NL_WARPS - 1) / NL_WARPS), 32 * NL_WARPS, 0, st>>>(
-        n, b.status, b.sys_rebuild, b.sysid, b.sys, b.wpos, b.atom_cell, b.cell_start, b.cell_atoms, b.perm,
-        b.maxnb, b.nbr, b.nnb, b.status);
+        nl_perm_kernel<<<atoms_grid, tb, 0, st>>>(b.nsys, b.plan, b.status, b.sys, b.cell_atoms, b.kind, b.mol,
+                                                  b.posq, b.perm, b.km, b.posfx, b.pfx_build);
+    nl_build_kernel<<<build_grid, 32 * NL_WARPS, 0, st>>>(b.nsys, b.plan, b.status, b.sys, b.wpos, b.atom_cell,
+                                                          b.cell_start, b.cell_atoms, b.perm, b.maxnb, b.nbr, b.nnb,
+                                                          b.status);
     nl_done_kernel<<<1, 256, 0, st>>>(b.nsys, b.status, b.sys_rebuild);
 }
 

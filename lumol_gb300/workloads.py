@@ -145,8 +145,9 @@ def water_box(n_side: int = 12, length: float = 37.3, seed: int = 0, precision: 
 def lj_replica(n: int, reduced_density: float, temperature: float, seed: int, precision: str = "fp64",
                sigma: float = 3.405, epsilon_kj: float = 0.996) -> System:
     """One argon-type replica: `n` atoms on a jittered simple-cubic lattice at
-    reduced density rho* = rho sigma^3, LJ of the argon workload with
-    rc = 2.5 sigma (plain cutoff), Maxwell-Boltzmann velocities at `temperature`."""
+    reduced density rho* = rho sigma^3, the argon workload's LJ parameters and
+    energy-shifted cutoff (PairInteraction::shifted) at rc = 2.5 sigma,
+    Maxwell-Boltzmann velocities at `temperature`."""
     rng = np.random.default_rng(seed)
     length = (n * sigma ** 3 / reduced_density) ** (1.0 / 3.0)
     side = int(math.ceil(n ** (1.0 / 3.0)))
@@ -157,7 +158,7 @@ def lj_replica(n: int, reduced_density: float, temperature: float, seed: int, pr
     system = System(UnitCell.cubic(length), precision=precision)
     system.add_particles(["Ar"] * n, pos, masses=[39.948] * n)
     lj = LennardJones(sigma=sigma, epsilon=from_(epsilon_kj, "kJ/mol"))
-    system.set_pair_potential(("Ar", "Ar"), PairInteraction(lj, 2.5 * sigma))
+    system.set_pair_potential(("Ar", "Ar"), PairInteraction.shifted(lj, 2.5 * sigma))
     system.velocities = boltzmann_velocities(system, temperature, seed + 7)
     return system
 

@@ -157,6 +157,22 @@ def test_velocity_verlet_ewald_berendsen():
     assert np.abs(s.velocities - vo).max() / np.abs(vo).max() < 1e-8
 
 
+def test_berendsen_across_run_boundaries():
+    """The thermostat's scaling is carried into the next step inside a run and
+    applied at the end of every run: runs of 1, 3 and 21 steps give the
+    oracle's 25-step trajectory."""
+    s = workloads.nacl_crystal(cells=3, cutoff=8.0, kmax=5)
+    orc = oracle.Oracle(s)
+    x0, v0 = s.positions.copy(), s.velocities.copy()
+    md = lg.MolecularDynamics(lg.VelocityVerlet(1.0), lg.BerendsenThermostat(200.0, 10.0))
+    md.setup(s)
+    for k in (1, 3, 21):
+        md.run(s, k)
+    xo, vo, _ = orc.velocity_verlet(x0, v0, np.zeros_like(x0), 1.0, 25, 200.0, 10.0)
+    assert np.abs(s.positions - xo).max() < 1e-9
+    assert np.abs(s.velocities - vo).max() / np.abs(vo).max() < 1e-8
+
+
 def test_md_energy_conservation_nve():
     """NVE drift bound of tests/md-nacl.rs (Ewald 5e-3 relative over the run)."""
     s = workloads.nacl_crystal(cells=3, cutoff=8.0, kmax=5, temperature=300.0)
