@@ -537,7 +537,7 @@ def batch_roofline(args, md, C):
     achieved = flops / (times["pair"] * 1e-3) / 1e12
     kernel = "pair_fp64_kernel" if fp64 else "pair_mixed_kernel"
     return {"bound": "fp64" if fp64 else "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
-            "frac": achieved / peak.value, "traffic": traffic_from_profiles(kernel + "_lj_batch"),
+            "frac": achieved / peak.value, "traffic": traffic_from_profiles(kernel + "_lj_batch256" + ("_sorted" if not fp64 else "")),
             "kernel": kernel, "kernel_ms": times["pair"],
             "peak_source": ("FP64" if fp64 else "FP32") + " FMA throughput measured live by lg_fma_peak "
                            "(MEASURED_PEAKS.json has no such figure; no tensor cores on this path)",
