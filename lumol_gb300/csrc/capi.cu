@@ -221,6 +221,8 @@ struct lg_engine {
     DBuf<float4> wpos;
     DBuf<uint4> posfx, pfx_build;
     DBuf<double> inv_mass;
+    DBuf<int> nlo, rev;
+    DBuf<double4_32a> pf;
     DBuf<PairDevF> ptabf;
     DBuf<KVecF> kvecf;
     DBuf<float2> eikrf, rhof;
@@ -424,6 +426,11 @@ int commit(lg_engine* e) {
             q.shift = p.shifted ? pot_energy(p, p.cutoff) : 0.0;  // pairs.rs:86-95
             q.scale14 = p.scale14;
             q.cutoff2_f = (float)(p.cutoff * p.cutoff);
+            if (p.type == LG_PAIR_LJ) {
+                double s2 = p.p0 * p.p0, s6 = s2 * s2 * s2;
+                q.c6 = 4.0 * p.p1 * s6;
+                q.c12 = 4.0 * p.p1 * s6 * s6;
+            }
             if (p.type != LG_PAIR_ABSENT && p.restriction > LG_RESTRICT_INTER) needs_path = true;
             h_ptab.push_back(q);
             PairDevF qf;
@@ -632,7 +639,10 @@ int commit(lg_engine* e) {
                            (float)v.energy};
     }
     CUDA_TRY(e, e->ptabf.alloc(h_ptabf.size()));
-    CUDA_TRY(e, e->posfx.alloc(mixed ? n : 1));
+    CUDA_TRY(e, e->posfx.alloc(n));  // fixed-point copy: the mixed path's positions, the plain path's classification
+    CUDA_TRY(e, e->nlo.alloc(mixed ? 1 : n));
+    CUDA_TRY(e, e->rev.alloc(mixed ? 1 : (size_t)n * maxnb));
+    CUDA_TRY(e, e->pf.alloc(mixed ? 1 : (size_t)n * maxnb));
     CUDA_TRY(e, e->perm.alloc(mixed ? n : 1));
     CUDA_TRY(e, e->pfx_build.alloc(mixed ? n : 1));
     CUDA_TRY(e, e->inv_mass.alloc(mixed ? n : 1));
@@ -685,6 +695,7 @@ int commit(lg_engine* e) {
                                     st));
     }
     CUDA_TRY(e, cudaMemsetAsync(e->nnb.p, 0, n * sizeof(int), st));
+    if (!mixed) CUDA_TRY(e, cudaMemsetAsync(e->nlo.p, 0, n * sizeof(int), st));
     CUDA_TRY(e, cudaMemcpyAsync(e->sysdev.p, e->h_sysdev.data(), nsys * sizeof(SysDev), cudaMemcpyHostToDevice, st));
     if (!h_tiles.empty())
         CUDA_TRY(e, cudaMemcpyAsync(e->tiles.p, h_tiles.data(), h_tiles.size() * sizeof(int2), cudaMemcpyHostToDevice,
@@ -766,7 +777,10 @@ int commit(lg_engine* e) {
     CUDA_TRY(e, cudaMemcpy(e->mc_chains.p, e->h_mc.data(), nsys * sizeof(McState), cudaMemcpyHostToDevice));
     e->mc_energies_ready = false;
     b.tpa = e->opt.threads_per_atom ? e->opt.threads_per_atom : (mixed ? 8 : 32);
-    b.posfx = mixed ? e->posfx.p : nullptr;
+    b.posfx = e->posfx.p;
+    b.nlo = mixed ? nullptr : e->nlo.p;
+    b.rev = mixed ? nullptr : e->rev.p;
+    b.pf = mixed ? nullptr : e->pf.p;
     b.pfx_build = mixed ? e->pfx_build.p : nullptr;
     b.inv_mass = mixed ? e->inv_mass.p : nullptr;
     b.ptabf = e->ptabf.p;
@@ -789,6 +803,12 @@ int regrow(lg_engine* e) {
     CUDA_TRY(e, e->nbr.alloc((size_t)e->b.n * maxnb));
     e->b.maxnb = maxnb;
     e->b.nbr = e->nbr.p;
+    if (e->b.pf) {
+        CUDA_TRY(e, e->rev.alloc((size_t)e->b.n * maxnb));
+        CUDA_TRY(e, e->pf.alloc((size_t)e->b.n * maxnb));
+        e->b.rev = e->rev.p;
+        e->b.pf = e->pf.p;
+    }
     launch_request_rebuild(e->b, e->stream);
     e->drop_graphs();
     return LG_OK;
@@ -809,7 +829,7 @@ int clear_status_bits(lg_engine* e, uint32_t bits) {
 }
 
 // Kernels launch_nlist_build enqueues.
-int nlist_launches(const Batch& b) { return b.n ? (b.perm ? 8 : 7) : 0; }
+int nlist_launches(const Batch& b) { return b.n ? (b.perm ? 8 : 9) : 0; }
 
 // Forces (and energies / virials) of the whole batch at the positions in posq.
 // The pair kernel assigns the forces, the other force kernels add to them.
@@ -820,13 +840,13 @@ void enqueue_forces(lg_engine* e, uint32_t terms, bool ev, cudaStream_t st, bool
     if (b.n == 0) return;
     launch_nlist_build(b, st);
     e->launches += nlist_launches(b);
-    if (b.precision == LG_PRECISION_MIXED && !fixed_written) {  // fixed-point copy in the order of the list
+    if (!fixed_written) {  // fixed-point copy (mixed: in the order of the list)
         launch_split_positions(b, st);
         e->launches += 1;
     }
     if (terms & (LG_TERM_PAIRS | LG_TERM_COUL_REAL)) {
         launch_pair_forces(b, terms, ev, st);
-        e->launches += 1;
+        e->launches += b.precision == LG_PRECISION_MIXED ? 1 : 2;
     } else {
         cudaMemsetAsync(e->force.p, 0, 3 * (size_t)b.n * sizeof(double), st);
     }
@@ -1291,7 +1311,7 @@ int autotune(lg_engine* e) {
     // a current list for the timing
     launch_check_displacement(b, st);
     launch_nlist_build(b, st);
-    if (b.precision == LG_PRECISION_MIXED) launch_split_positions(b, st);
+    launch_split_positions(b, st);
     auto time_it = [&](auto&& launch) -> float {
         launch();  // warm
         float best = 1e30f;

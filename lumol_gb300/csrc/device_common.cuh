@@ -25,6 +25,7 @@ struct PairDev {
     double scale14;
     float cutoff2_f;      // mixed path: cutoff^2 in FP32
     float pad_f;
+    double c12, c6;       // LJ: 4 eps sigma^12, 4 eps sigma^6 (plain path, interior pairs)
 };
 
 // FP32 pair table entry of the mixed path.
@@ -83,9 +84,16 @@ struct SysDev {
 __device__ __forceinline__ uint32_t fixed_coordinate(double x, double scale) {
     return (uint32_t)(unsigned long long)__double2ll_rd(x * scale);
 }
+// The charge's FP32 copy is never zero for a non-zero charge (a charge below
+// the FP32 range keeps the smallest normal value), so "q != 0" tests agree
+// with the FP64 charges.
+__device__ __forceinline__ float charge_f32(double q) {
+    float f = (float)q;
+    return (f == 0.0f && q != 0.0) ? (q < 0.0 ? -1.17549435e-38f : 1.17549435e-38f) : f;
+}
 __device__ __forceinline__ uint4 fixed_position(const SysDev& s, double4_32a p) {
     return make_uint4(fixed_coordinate(p.x, s.fxscale[0]), fixed_coordinate(p.y, s.fxscale[1]),
-                      fixed_coordinate(p.z, s.fxscale[2]), __float_as_uint((float)p.w));
+                      fixed_coordinate(p.z, s.fxscale[2]), __float_as_uint(charge_f32(p.w)));
 }
 
 // One Ewald k-vector with its factors (ewald.rs:102-116).

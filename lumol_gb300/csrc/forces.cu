@@ -1,13 +1,13 @@
 // forces.cu -- FP64 force / energy / virial kernels of the plain path.
 //
 // Pair potentials (sys/compute.rs:30-59, sys/energy.rs:32-59, compute.rs:198-231)
-// and real-space Coulomb (ewald.rs:383-530, wolf.rs:90-282) run in one pass over
-// the full neighbour list, one warp per atom i: the lanes walk i's neighbours,
-// apply the reference's exact cutoff tests, and the per-atom force is a warp
-// sum.  No force is scattered, so every atom's force is summed in a fixed order
-// and results do not depend on the rest of the batch.  Energies and virials are
-// counted once per pair (j > i) into per-atom slots that a per-system reduction
-// adds up in a fixed order.
+// and real-space Coulomb (ewald.rs:383-530, wolf.rs:90-282) run over the
+// neighbour list in two passes: each pair is evaluated once (row i, j > i) and
+// its force stored, then every atom gathers the forces of its j < i pairs.  No
+// force is scattered with atomics, so every atom's force is summed in a fixed
+// order and results do not depend on the rest of the batch.  Energies and
+// virials go to per-atom slots that a per-system reduction adds up in a fixed
+// order.
 #include "kernels.h"
 
 namespace lg {
@@ -22,13 +22,15 @@ struct PairDecision {
     double coul_scale; // restriction scaling of Wolf
 };
 
-__device__ __forceinline__ PairDecision decide_pair(const SysDev& s, const PairDev& p, uint32_t terms,
-                                                    int i, int j, int mi, int mj, double qi, double qj,
-                                                    double r, const int* spec_off, const int* spec_j,
-                                                    const int8_t* spec_path) {
+// Restrictions (restrictions.rs:85-115) of a pair whose cutoff tests are
+// already decided: pin = the pair potential is within its cutoff, cin = the
+// real-space Coulomb term is within its cutoff (both charges non-zero).
+__device__ __forceinline__ PairDecision restrict_pair(const SysDev& s, const PairDev& p, bool pin, bool cin,
+                                                      int i, int j, int mi, int mj, const int* spec_off,
+                                                      const int* spec_j, const int8_t* spec_path) {
     PairDecision d{false, false, false, 1.0, 1.0};
     int path = -1;
-    if ((terms & 1u) && p.type != 0 && !(r >= p.cutoff)) {  // pairs.rs:185-218
+    if (pin) {  // pairs.rs:185-218
         if (p.restriction != 0) {
             path = (p.restriction <= 2) ? (mi != mj ? 0 : 5)
                                         : bond_path(i, j, mi, mj, spec_off, spec_j, spec_path);
@@ -40,7 +42,7 @@ __device__ __forceinline__ PairDecision decide_pair(const SysDev& s, const PairD
             d.pair_in = true;
         }
     }
-    if ((terms & 16u) && s.coul != 0 && qi != 0.0 && qj != 0.0 && !(r > s.coul_rc)) {
+    if (cin) {
         bool excl = false;
         if (s.coul_restr != 0) {
             if (path < 0 || (s.coul_restr > 2 && path == 5 && mi == mj))
@@ -59,6 +61,18 @@ __device__ __forceinline__ PairDecision decide_pair(const SysDev& s, const PairD
     return d;
 }
 
+// The reference's decision with its own cutoff tests on the exact distance r
+// (pairs: r >= cutoff is out, pairs.rs:185-218; Coulomb: r > cutoff is out,
+// ewald.rs:387-428, wolf.rs:90-117).
+__device__ __forceinline__ PairDecision decide_pair(const SysDev& s, const PairDev& p, uint32_t terms,
+                                                    int i, int j, int mi, int mj, double qi, double qj,
+                                                    double r, const int* spec_off, const int* spec_j,
+                                                    const int8_t* spec_path) {
+    bool pin = (terms & 1u) && p.type != 0 && !(r >= p.cutoff);
+    bool cin = (terms & 16u) && s.coul != 0 && qi != 0.0 && qj != 0.0 && !(r > s.coul_rc);
+    return restrict_pair(s, p, pin, cin, i, j, mi, mj, spec_off, spec_j, spec_path);
+}
+
 template <int TPA>
 __device__ __forceinline__ double group_sum(double v) {
 #pragma unroll
@@ -66,14 +80,36 @@ __device__ __forceinline__ double group_sum(double v) {
     return v;
 }
 
-// TPA threads per atom (1..32, autotuned) walk atom i's neighbour list.
-template <int TPA, bool EV>
-__global__ void __launch_bounds__(256) pair_fp64_kernel(
-    int n, const double4_32a* __restrict__ posq, const int* __restrict__ kind, const int* __restrict__ mol,
-    const int* __restrict__ sysid, const SysDev* __restrict__ sys, const PairDev* __restrict__ ptab,
-    const int* __restrict__ nbr, const int* __restrict__ nnb, int maxnb, const int* __restrict__ spec_off,
-    const int* __restrict__ spec_j, const int8_t* __restrict__ spec_path, uint32_t terms,
-    double* __restrict__ force, double* __restrict__ red) {
+// Relative half-width of the band around a cutoff^2 inside which the FP32
+// classification of a pair defers to the reference's exact geometry.  The
+// FP32 distance from the fixed-point copies carries a relative error below
+// 1e-6, so a pair outside the band is on the same side of the cutoff in FP32
+// as in the reference's FP64 test.
+constexpr float CUT_BAND = 4.0e-5f;
+
+// Minimum image of an interior pair (|d| well below L / 2, so the nearest
+// integer of d / L is never in doubt).
+__device__ __forceinline__ double fast_image(double d, double L, double invL) {
+    return fma(-rint(d * invL), L, d);
+}
+
+// Half-list pair kernel of the plain path: TPA threads per atom (1..32,
+// autotuned) walk the j > i tail of atom i's sorted row.  Each entry is first
+// classified in FP32 on the fixed-point copies: clearly outside every cutoff
+// (skipped, no FP64 work), clearly inside (FP64 arithmetic without the exact
+// geometry's fallbacks; LJ from 1 / r^2 without a square root), or near a
+// cutoff (the reference's exact geometry and cutoff test, so the pair set is
+// the reference's bit for bit).  The pair force is added to atom i's sum and
+// stored for atom j, which reads it back in pair_gather_kernel; energies and
+// virials count each pair once.  All sums run in a fixed order.
+template <int TPA, bool EV, bool GENERAL>
+__global__ void __launch_bounds__(256) pair_half_kernel(
+    int n, const double4_32a* __restrict__ posq, const uint4* __restrict__ pfx, const int* __restrict__ kind,
+    const int* __restrict__ mol, const int* __restrict__ sysid, const SysDev* __restrict__ sys,
+    const PairDev* __restrict__ ptab, const int* __restrict__ nbr, const int* __restrict__ nnb,
+    const int* __restrict__ nlo, int maxnb, const int* __restrict__ spec_off, const int* __restrict__ spec_j,
+    const int8_t* __restrict__ spec_path, uint32_t terms, double* __restrict__ force,
+    double4_32a* __restrict__ pf, double* __restrict__ red) {
     int gt = blockIdx.x * blockDim.x + threadIdx.x;
     int i = gt / TPA;
     int sub = gt % TPA;
@@ -81,56 +117,97 @@ __global__ void __launch_bounds__(256) pair_fp64_kernel(
     int ii = active ? i : n - 1;
     const SysDev& s = sys[sysid[ii]];
     double4_32a pi = posq[ii];
+    uint4 ui = pfx[ii];
     int ki = kind[ii], mi = mol[ii];
     const PairDev* prow = ptab + s.ptab + ki * s.nk;
+    bool pairs = (terms & 1u) != 0;
+    bool coul_i = GENERAL && (terms & 16u) && s.coul != 0 && pi.w != 0.0;
+    float crc2 = s.coul_rc2_f;
     double fx = 0.0, fy = 0.0, fz = 0.0;
     double ep = 0.0, ec = 0.0;
     double wxx = 0.0, wxy = 0.0, wxz = 0.0, wyy = 0.0, wyz = 0.0, wzz = 0.0;
     int cnt = active ? nnb[ii] : 0;
+    int k0 = active ? nlo[ii] : 0;
     const int* list = nbr + (size_t)ii * maxnb;
-    for (int k = sub; k < cnt; k += TPA) {
+    double4_32a* out = pf + (size_t)ii * maxnb;
+    for (int k = k0 + sub; k < cnt; k += TPA) {
         int j = list[k];
-        double4_32a pj = posq[j];
-        double dx, dy, dz;
-        exact_nearest_image(s, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z, dx, dy, dz);
-        double r = exact_norm(dx, dy, dz);
+        uint4 uj = pfx[j];
+        float dxf = (float)(int32_t)(ui.x - uj.x) * s.Lq[0];
+        float dyf = (float)(int32_t)(ui.y - uj.y) * s.Lq[1];
+        float dzf = (float)(int32_t)(ui.z - uj.z) * s.Lq[2];
+        float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
         const PairDev& p = prow[kind[j]];
-        PairDecision dec = decide_pair(s, p, terms, i, j, mi, mol[j], pi.w, pj.w, r, spec_off, spec_j,
-                                       spec_path);
-        if (!(dec.pair_in || dec.coul_in)) continue;
-        double inv_r = 1.0 / r;
-        double f_over_r = 0.0;
-        bool count = EV && (j > i);
-        if (dec.pair_in) {
-            double e, f;
-            pair_energy_force(p, r, inv_r, e, f);
-            f_over_r += dec.pair_scale * f * inv_r;
-            if (count) ep += dec.pair_scale * e;
-        }
-        if (dec.coul_in) {
-            double e, fr;
-            if (s.coul == 1) {
-                ewald_real_pair(s.alpha, dec.coul_excl, pi.w * pj.w, r, inv_r, e, fr);
+        bool pc = pairs && p.type != 0;
+        bool cc = coul_i && __uint_as_float(uj.w) != 0.0f;
+        float prc2 = p.cutoff2_f;
+        bool band = (pc && fabsf(r2f - prc2) <= CUT_BAND * prc2) || (cc && fabsf(r2f - crc2) <= CUT_BAND * crc2);
+        bool pin = pc && r2f < prc2;
+        bool cin = cc && r2f < crc2;
+        double gx = 0.0, gy = 0.0, gz = 0.0;
+        if (band || pin || cin) {
+            double4_32a pj = posq[j];
+            double dx, dy, dz, r = 0.0, r2 = 0.0;
+            PairDecision dec;
+            if (band) {
+                exact_nearest_image(s, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z, dx, dy, dz);
+                r = exact_norm(dx, dy, dz);
+                dec = decide_pair(s, p, terms, i, j, mi, mol[j], pi.w, pj.w, r, spec_off, spec_j, spec_path);
             } else {
-                wolf_pair(s, pi.w * pj.w, r, inv_r, e, fr);
-                e *= dec.coul_scale;
-                fr *= dec.coul_scale;
+                dx = fast_image(pi.x - pj.x, s.L[0], s.invL[0]);
+                dy = fast_image(pi.y - pj.y, s.L[1], s.invL[1]);
+                dz = fast_image(pi.z - pj.z, s.L[2], s.invL[2]);
+                r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+                if (GENERAL) dec = restrict_pair(s, p, pin, cin, i, j, mi, mol[j], spec_off, spec_j, spec_path);
+                else dec = PairDecision{pin, false, false, 1.0, 1.0};
             }
-            f_over_r += fr;
-            if (count) ec += e;
+            double f_over_r = 0.0, e_p = 0.0, e_c = 0.0;
+            if (!band && dec.pair_in && p.type == 2 && !dec.coul_in) {
+                // interior LJ: c12 / r^12 - c6 / r^6 from 1 / r^2
+                double inv_r2 = __drcp_rn(r2);
+                double ir6 = inv_r2 * inv_r2 * inv_r2;
+                f_over_r = dec.pair_scale * (ir6 * (12.0 * p.c12 * ir6 - 6.0 * p.c6) * inv_r2);
+                if (EV) e_p = dec.pair_scale * (ir6 * (p.c12 * ir6 - p.c6) - p.shift);
+            } else if (dec.pair_in || dec.coul_in) {
+                if (!band) r = sqrt(r2);
+                double inv_r = 1.0 / r;
+                if (dec.pair_in) {
+                    double e, f;
+                    pair_energy_force(p, r, inv_r, e, f);
+                    f_over_r += dec.pair_scale * f * inv_r;
+                    e_p = dec.pair_scale * e;
+                }
+                if (GENERAL && dec.coul_in) {
+                    double e, fr;
+                    if (s.coul == 1) {
+                        ewald_real_pair(s.alpha, dec.coul_excl, pi.w * pj.w, r, inv_r, e, fr);
+                    } else {
+                        wolf_pair(s, pi.w * pj.w, r, inv_r, e, fr);
+                        e *= dec.coul_scale;
+                        fr *= dec.coul_scale;
+                    }
+                    f_over_r += fr;
+                    e_c = e;
+                }
+            }
+            gx = f_over_r * dx;
+            gy = f_over_r * dy;
+            gz = f_over_r * dz;
+            fx += gx;
+            fy += gy;
+            fz += gz;
+            if (EV) {
+                ep += e_p;
+                ec += e_c;
+                wxx += gx * dx;
+                wxy += gx * dy;
+                wxz += gx * dz;
+                wyy += gy * dy;
+                wyz += gy * dz;
+                wzz += gz * dz;
+            }
         }
-        double gx = f_over_r * dx, gy = f_over_r * dy, gz = f_over_r * dz;
-        fx += gx;
-        fy += gy;
-        fz += gz;
-        if (count) {
-            wxx += gx * dx;
-            wxy += gx * dy;
-            wxz += gx * dz;
-            wyy += gy * dy;
-            wyz += gy * dz;
-            wzz += gz * dz;
-        }
+        out[k] = make_double4_32a(gx, gy, gz, 0.0);  // the force on i; j reads it back negated
     }
     fx = group_sum<TPA>(fx);
     fy = group_sum<TPA>(fy);
@@ -164,19 +241,58 @@ __global__ void __launch_bounds__(256) pair_fp64_kernel(
     }
 }
 
+// The j < i head of each row: minus the stored forces of pairs (j, i), read
+// through the reverse index, added to the atom's force in row order.
+template <int TPA>
+__global__ void __launch_bounds__(256) pair_gather_kernel(int n, const int* __restrict__ nbr,
+                                                          const int* __restrict__ nlo, const int* __restrict__ rev,
+                                                          int maxnb, const double4_32a* __restrict__ pf,
+                                                          double* __restrict__ force) {
+    int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = gt / TPA;
+    int sub = gt % TPA;
+    bool active = i < n;
+    int ii = active ? i : n - 1;
+    int head = active ? nlo[ii] : 0;
+    const int* list = nbr + (size_t)ii * maxnb;
+    const int* rrow = rev + (size_t)ii * maxnb;
+    double fx = 0.0, fy = 0.0, fz = 0.0;
+    for (int k = sub; k < head; k += TPA) {
+        double4_32a f = pf[(size_t)list[k] * maxnb + rrow[k]];
+        fx -= f.x;
+        fy -= f.y;
+        fz -= f.z;
+    }
+    fx = group_sum<TPA>(fx);
+    fy = group_sum<TPA>(fy);
+    fz = group_sum<TPA>(fz);
+    if (active && sub == 0) {
+        force[3 * i] += fx;
+        force[3 * i + 1] += fy;
+        force[3 * i + 2] += fz;
+    }
+}
+
+template <int TPA, bool EV, bool GENERAL>
+void launch_pair_half(const Batch& b, uint32_t terms, unsigned grid, cudaStream_t st) {
+    pair_half_kernel<TPA, EV, GENERAL><<<grid, 256, 0, st>>>(b.n, b.posq, b.posfx, b.kind, b.mol, b.sysid, b.sys,
+                                                             b.ptab, b.nbr, b.nnb, b.nlo, b.maxnb, b.spec_off,
+                                                             b.spec_j, b.spec_path, terms, b.force, b.pf, b.red);
+}
+
 template <int TPA>
 void launch_pair_fp64_tpa(const Batch& b, uint32_t terms, bool ev, cudaStream_t st) {
-    int tb = 256;
     long long threads = (long long)b.n * TPA;
-    unsigned grid = (unsigned)((threads + tb - 1) / tb);
-    if (ev)
-        pair_fp64_kernel<TPA, true><<<grid, tb, 0, st>>>(b.n, b.posq, b.kind, b.mol, b.sysid, b.sys, b.ptab,
-                                                         b.nbr, b.nnb, b.maxnb, b.spec_off, b.spec_j,
-                                                         b.spec_path, terms, b.force, b.red);
-    else
-        pair_fp64_kernel<TPA, false><<<grid, tb, 0, st>>>(b.n, b.posq, b.kind, b.mol, b.sysid, b.sys, b.ptab,
-                                                          b.nbr, b.nnb, b.maxnb, b.spec_off, b.spec_j,
-                                                          b.spec_path, terms, b.force, b.red);
+    unsigned grid = (unsigned)((threads + 255) / 256);
+    // the pairs-only variant when nothing in the batch needs restrictions or Coulomb
+    if (b.pair_general) {
+        if (ev) launch_pair_half<TPA, true, true>(b, terms, grid, st);
+        else launch_pair_half<TPA, false, true>(b, terms, grid, st);
+    } else {
+        if (ev) launch_pair_half<TPA, true, false>(b, terms, grid, st);
+        else launch_pair_half<TPA, false, false>(b, terms, grid, st);
+    }
+    pair_gather_kernel<TPA><<<grid, 256, 0, st>>>(b.n, b.nbr, b.nlo, b.rev, b.maxnb, b.pf, b.force);
 }
 
 void launch_pair_forces(const Batch& b, uint32_t terms, bool ev, cudaStream_t st) {

@@ -72,6 +72,12 @@ struct Batch {
     int pair_general = 1;         // 0: pair potentials only, no restriction and no Coulomb in the batch
     uint4* posfx = nullptr;       // wrapped positions as 32-bit fractions of L, charge bits (cell order)
     uint4* pfx_build = nullptr;   // n: fixed-point positions at the last list build (atom order, mixed path)
+    // plain path: half-list evaluation.  Rows are sorted by neighbour index;
+    // row i's pairs with j > i are evaluated once and their forces stored, the
+    // j < i entries read them back through the reverse index.
+    int* nlo = nullptr;           // n: entries j < i at the head of each row
+    int* rev = nullptr;           // n * maxnb: for j < i, the slot of i in row j
+    double4_32a* pf = nullptr;    // n * maxnb: force on i from pair (i, j > i)
     double* inv_mass = nullptr;   // n: 1 / m (mixed path)
     PairDevF* ptabf = nullptr;
     KVecF* kvecf = nullptr;

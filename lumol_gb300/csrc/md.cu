@@ -162,6 +162,7 @@ __global__ void __launch_bounds__(VV_TILE) vv_first_kernel(
         dx -= rintf(dx * s.invLf[0]) * s.Lf[0];
         dy -= rintf(dy * s.invLf[1]) * s.Lf[1];
         dz -= rintf(dz * s.invLf[2]) * s.Lf[2];
+        if (posfx) posfx[i] = fixed_position(s, p);  // atom order: the half-list kernel's FP32 classification
     }
     vel[i] = v;
     posq[i] = p;
@@ -268,13 +269,13 @@ __global__ void request_rebuild_kernel(int nsys, uint32_t* status, uint32_t* sys
 void launch_vv_first(const Batch& b, bool apply_thermostat, cudaStream_t st) {
     if (!b.ntiles) return;
     int th = apply_thermostat ? 1 : 0;
-    if (b.posfx)
+    if (b.precision == 1)
         vv_first_kernel<true><<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.posq, b.vel, b.acc, b.pos_build,
                                                             b.pfx_build, b.kepart, th, b.perm, b.posfx, b.status,
                                                             b.sys_rebuild);
     else
         vv_first_kernel<false><<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.posq, b.vel, b.acc, b.pos_build,
-                                                             nullptr, b.kepart, th, nullptr, nullptr, b.status,
+                                                             nullptr, b.kepart, th, nullptr, b.posfx, b.status,
                                                              b.sys_rebuild);
 }
 void launch_vv_second(const Batch& b, bool thermostat, cudaStream_t st) {

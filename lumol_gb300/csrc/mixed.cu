@@ -297,19 +297,21 @@ void launch_pair_mixed(const Batch& b, uint32_t terms, bool ev, cudaStream_t st)
     }
 }
 
-// Fixed-point copy of the wrapped FP64 positions in the cell-sorted order.
+// Fixed-point copy of the wrapped FP64 positions, in the cell-sorted order of
+// the mixed path or in atom order (plain path: the FP32 classification of the
+// half-list kernel).
 __global__ void fixed_positions_kernel(int n, const double4_32a* __restrict__ posq, const int* __restrict__ sysid,
                                        const SysDev* __restrict__ sys, const int* __restrict__ order,
                                        uint4* __restrict__ pfx) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;  // cell-sorted position
+    int t = blockIdx.x * blockDim.x + threadIdx.x;  // cell-sorted position (atom index without an order)
     if (t >= n) return;
-    pfx[t] = fixed_position(sys[sysid[t]], posq[order[t]]);
+    pfx[t] = fixed_position(sys[sysid[t]], posq[order ? order[t] : t]);
 }
 
 void launch_split_positions(const Batch& b, cudaStream_t st) {
     if (b.n && b.posfx)
-        fixed_positions_kernel<<<(b.n + 255) / 256, 256, 0, st>>>(b.n, b.posq, b.sysid, b.sys, b.cell_atoms,
-                                                                  b.posfx);
+        fixed_positions_kernel<<<(b.n + 255) / 256, 256, 0, st>>>(b.n, b.posq, b.sysid, b.sys,
+                                                                  b.perm ? b.cell_atoms : nullptr, b.posfx);
 }
 
 // ---------------------------------------------------------------------------

@@ -370,6 +370,88 @@ __global__ void __launch_bounds__(32 * NL_WARPS) nl_build_kernel(
     }
 }
 
+// Plain path, after the build: sort each rebuilt row by neighbour index (warp
+// per row, rank sort in shared memory) and count its j < i head (nlo).  The
+// order of a row's entries only changes the order of the force sums.
+constexpr int ROW_SMEM = 512;
+
+__global__ void __launch_bounds__(32 * NL_WARPS) nl_rowsort_kernel(int nsys, const int* __restrict__ plan,
+                                                                   const uint32_t* __restrict__ status,
+                                                                   const SysDev* __restrict__ sys, int maxnb,
+                                                                   int* __restrict__ nbr,
+                                                                   const int* __restrict__ nnb,
+                                                                   int* __restrict__ nlo) {
+    __shared__ int buf[NL_WARPS][ROW_SMEM];
+    if (!(*status & ST_REBUILD)) return;
+    PlanView pv = plan_view(plan, nsys);
+    int A = pv.apre[pv.R];
+    int wib = threadIdx.x >> 5;
+    int lane = threadIdx.x & 31;
+    for (int w = blockIdx.x * NL_WARPS + wib; w < A; w += gridDim.x * NL_WARPS) {
+        int r = plan_find(pv.apre, pv.R, w);
+        int i = sys[pv.sys[r]].begin + (w - pv.apre[r]);
+        int* row = nbr + (size_t)i * maxnb;
+        int cnt = nnb[i];
+        int below = 0;
+        __syncwarp();
+        if (cnt <= ROW_SMEM) {
+            for (int a = lane; a < cnt; a += 32) buf[wib][a] = row[a];
+            __syncwarp();
+            for (int a = lane; a < cnt; a += 32) {
+                int v = buf[wib][a], rank = 0;
+                for (int b = 0; b < cnt; b++) rank += buf[wib][b] < v;
+                row[rank] = v;
+                below += v < i;
+            }
+        } else if (lane == 0) {
+            // very long row: serial insertion sort in place
+            for (int a = 1; a < cnt; a++) {
+                int v = row[a];
+                int b = a - 1;
+                while (b >= 0 && row[b] > v) {
+                    row[b + 1] = row[b];
+                    b--;
+                }
+                row[b + 1] = v;
+            }
+            for (int a = 0; a < cnt; a++) below += row[a] < i;
+        }
+        for (int o = 16; o > 0; o >>= 1) below += __shfl_xor_sync(0xffffffffu, below, o);
+        if (lane == 0) nlo[i] = below;
+    }
+}
+
+// Reverse index of every j < i entry: the slot of i in row j (binary search
+// in j's sorted j' > j tail; the list is symmetric).  A row cut short by an
+// overflow has no slot for some partners: those get an in-range slot and the
+// overflow status makes the caller rebuild and recompute.
+__global__ void nl_rev_kernel(int nsys, const int* __restrict__ plan, const uint32_t* __restrict__ status,
+                              const SysDev* __restrict__ sys, int maxnb, const int* __restrict__ nbr,
+                              const int* __restrict__ nnb, const int* __restrict__ nlo, int* __restrict__ rev) {
+    if (!(*status & ST_REBUILD)) return;
+    PlanView pv = plan_view(plan, nsys);
+    int A = pv.apre[pv.R];
+    int wib = threadIdx.x >> 5;
+    int lane = threadIdx.x & 31;
+    for (int w = blockIdx.x * NL_WARPS + wib; w < A; w += gridDim.x * NL_WARPS) {
+        int r = plan_find(pv.apre, pv.R, w);
+        int i = sys[pv.sys[r]].begin + (w - pv.apre[r]);
+        const int* row = nbr + (size_t)i * maxnb;
+        int head = nlo[i];
+        for (int k = lane; k < head; k += 32) {
+            int j = row[k];
+            const int* rj = nbr + (size_t)j * maxnb;
+            int a = nlo[j], b = nnb[j];  // first slot with rj[slot] >= i
+            while (a < b) {
+                int mid = (a + b) >> 1;
+                if (rj[mid] < i) a = mid + 1;
+                else b = mid;
+            }
+            rev[(size_t)i * maxnb + k] = min(a, maxnb - 1);
+        }
+    }
+}
+
 // Clears the rebuild requests once the lists are in place.
 __global__ void nl_done_kernel(int nsys, uint32_t* status, uint32_t* sys_rebuild) {
     if (!(*status & ST_REBUILD)) return;
@@ -402,6 +484,12 @@ void launch_nlist_build(const Batch& b, cudaStream_t st) {
     nl_build_kernel<<<build_grid, 32 * NL_WARPS, 0, st>>>(b.nsys, b.plan, b.status, b.sys, b.wpos, b.atom_cell,
                                                           b.cell_start, b.cell_atoms, b.perm, b.maxnb, b.nbr, b.nnb,
                                                           b.status);
+    if (b.pf) {
+        nl_rowsort_kernel<<<build_grid, 32 * NL_WARPS, 0, st>>>(b.nsys, b.plan, b.status, b.sys, b.maxnb, b.nbr,
+                                                                b.nnb, b.nlo);
+        nl_rev_kernel<<<build_grid, 32 * NL_WARPS, 0, st>>>(b.nsys, b.plan, b.status, b.sys, b.maxnb, b.nbr, b.nnb,
+                                                            b.nlo, b.rev);
+    }
     nl_done_kernel<<<1, 256, 0, st>>>(b.nsys, b.status, b.sys_rebuild);
 }
 
