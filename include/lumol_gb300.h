@@ -124,8 +124,21 @@ typedef struct {
     int32_t threads_per_atom;  /* 1, 2, 4, 8, 16 or 32 threads per atom in the pair kernels;
                                   0: chosen by the autotuner.  A fixed value makes every
                                   system's results independent of the rest of the batch. */
-    int32_t reserved;
+    int32_t flags;       /* LG_OPT_* bits */
 } lg_options;
+
+/* lg_options.flags.  Batches of mixed-precision systems with pair potentials
+   only (no bonds, restrictions or Coulomb) run MD in one persistent launch per
+   lg_md_run chunk, one thread-block cluster per group of systems; this flag
+   keeps them on the per-step kernels instead. */
+#define LG_OPT_NO_PERSISTENT 1
+/* The persistent kernel gathers neighbour positions from global memory
+   instead of staging them in shared memory. */
+#define LG_OPT_NO_STAGING 2
+/* Bits 4-7 of lg_options.flags fix the cluster size of the persistent kernel
+   (the value is log2(size) + 1, so 1, 2, 3, 4 select 1, 2, 4, 8 blocks);
+   0 lets the planner choose. */
+#define LG_OPT_CLUSTER_SHIFT 4
 
 typedef struct lg_engine lg_engine;
 
@@ -259,6 +272,10 @@ int lg_get_stream(lg_engine* e, void** stream);
 int lg_kernel_times(lg_engine* e, int32_t reps, double ms[LG_KT_COUNT]);
 /* Number of kernels this engine has launched (graph replays included). */
 int lg_launch_count(lg_engine* e, uint64_t* count);
+/* The persistent kernel's plan for the current batch: cluster size and number
+ * of groups (0 and 0 while MD runs on the per-step kernels or before the first
+ * lg_md_run). */
+int lg_md_plan(lg_engine* e, int32_t* cluster, int32_t* groups);
 /* Measured FMA throughput of the FP64 (fp64 = 1) or FP32 pipe of the current
  * device, in TFLOP/s (2 flops per FMA). */
 int lg_fma_peak(int32_t fp64, double* tflops);

@@ -22,6 +22,9 @@ LG_ERR_NO_DEVICE = 6
 LG_PAIR_ABSENT, LG_PAIR_NULL, LG_PAIR_LJ, LG_PAIR_BUCKINGHAM, LG_PAIR_HARMONIC = range(5)
 LG_COULOMB_NONE, LG_COULOMB_EWALD, LG_COULOMB_WOLF = range(3)
 LG_PRECISION_FP64, LG_PRECISION_MIXED = 0, 1
+LG_OPT_NO_PERSISTENT = 1
+LG_OPT_NO_STAGING = 2
+LG_OPT_CLUSTER_SHIFT = 4
 
 LG_TERM_PAIRS = 1
 LG_TERM_TAIL = 2
@@ -69,7 +72,7 @@ class LgCoulomb(ctypes.Structure):
 
 class LgOptions(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("precision", ctypes.c_int32), ("skin", ctypes.c_double),
-                ("threads_per_atom", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("threads_per_atom", ctypes.c_int32), ("flags", ctypes.c_int32)]
 
 
 # name -> (restype, argtypes)
@@ -107,6 +110,7 @@ SIGNATURES = {
     "lg_get_stream": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
     "lg_kernel_times": (ctypes.c_int, [_P, ctypes.c_int32, _D]),
     "lg_launch_count": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64)]),
+    "lg_md_plan": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
     "lg_fma_peak": (ctypes.c_int, [ctypes.c_int32, _D]),
     "lg_ewald_kspace_noalloc": (ctypes.c_int, [_P, _P, ctypes.c_int64, _D, ctypes.c_double, ctypes.c_int32,
                                                _P, _P, _P, _P]),

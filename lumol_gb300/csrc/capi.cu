@@ -220,7 +220,7 @@ struct lg_engine {
     DBuf<double2> bt_par, eikr, rho;
     DBuf<float4> wpos;
     DBuf<uint4> posfx, pfx_build;
-    DBuf<double> inv_mass;
+    DBuf<float> inv_mass;
     DBuf<int> nlo, rev;
     DBuf<double4_32a> pf;
     DBuf<PairDevF> ptabf;
@@ -242,6 +242,16 @@ struct lg_engine {
     // kernels launched so far (graph replays counted by their kernel nodes)
     uint64_t launches = 0;
     size_t graph_kernels = 0;
+
+    // persistent batched MD (mixed batches of pair-potential systems)
+    int pk_cluster = 0;  // cluster size of the plan; 0: not planned, -1: not eligible
+    int pk_groups = 0;
+    int pk_stage = 0;    // atoms each block stages in shared memory (0: gathers from global memory)
+    DBuf<int> pk_group_off, pk_group_sys, pk_group_flag;
+    DBuf<double> pk_lambda, pk_ke;
+    // one graph per (steps, thermostat): checkpoint copies, flag reset, the launch
+    // (a graph replay avoids the per-launch cost of a cluster launch)
+    std::map<int, cudaGraphExec_t> pk_graphs;
 
     // MD graphs, one per chunk length
     std::map<int, cudaGraphExec_t> graphs;
@@ -266,6 +276,8 @@ struct lg_engine {
         for (auto& g : graphs) cudaGraphExecDestroy(g.second);
         graphs.clear();
         graph_nodes.clear();
+        for (auto& g : pk_graphs) cudaGraphExecDestroy(g.second);
+        pk_graphs.clear();
     }
 
     ~lg_engine() {
@@ -469,12 +481,14 @@ int commit(lg_engine* e) {
         double rc = max_cutoff(h);
         d.rlist = rc + e->skin;
         d.half_skin2 = 0.25 * e->skin * e->skin;
+        d.rebuild2_f = 0.99f * (float)d.half_skin2;
         double margin = 1e-5 * std::max(std::max(h.L[0], h.L[1]), h.L[2]) + 1e-4;
         d.rlist2_f = (float)((d.rlist + margin) * (d.rlist + margin));
+        // cells at least half the list radius wide: the list builds look two cells around
         int cells = 1;
         for (int k = 0; k < 3; k++) {
-            int nc = (int)std::floor(h.L[k] / (d.rlist + margin));
-            nc = std::max(1, std::min(nc, 64));
+            int nc = (int)std::floor(h.L[k] / (0.5 * (d.rlist + margin)));
+            nc = std::max(1, std::min(nc, 128));
             d.ncell[k] = nc;
             cells *= nc;
         }
@@ -685,13 +699,13 @@ int commit(lg_engine* e) {
     for (int64_t i = 0; i < (int64_t)n; i++) h_iota[i] = (int)i;
     CUDA_TRY(e, cudaMemcpyAsync(e->cell_atoms.p, h_iota.data(), n * sizeof(int), cudaMemcpyHostToDevice, st));
     CUDA_TRY(e, cudaMemsetAsync(e->plan.p, 0, (3 + 3 * (size_t)nsys) * sizeof(int), st));
-    std::vector<double> h_inv_mass;
+    std::vector<float> h_inv_mass;
     if (mixed) {
         CUDA_TRY(e, cudaMemcpyAsync(e->perm.p, h_iota.data(), n * sizeof(int), cudaMemcpyHostToDevice, st));
         CUDA_TRY(e, cudaMemsetAsync(e->pfx_build.p, 0, n * sizeof(uint4), st));
         h_inv_mass.resize(n);
-        for (int64_t i = 0; i < (int64_t)n; i++) h_inv_mass[i] = 1.0 / h_vel[i].w;
-        CUDA_TRY(e, cudaMemcpyAsync(e->inv_mass.p, h_inv_mass.data(), n * sizeof(double), cudaMemcpyHostToDevice,
+        for (int64_t i = 0; i < (int64_t)n; i++) h_inv_mass[i] = (float)(1.0 / h_vel[i].w);
+        CUDA_TRY(e, cudaMemcpyAsync(e->inv_mass.p, h_inv_mass.data(), n * sizeof(float), cudaMemcpyHostToDevice,
                                     st));
     }
     CUDA_TRY(e, cudaMemsetAsync(e->nnb.p, 0, n * sizeof(int), st));
@@ -793,6 +807,7 @@ int commit(lg_engine* e) {
     b.rhof = e->rhof.p;
     e->dirty = false;
     e->tuned = false;
+    e->pk_cluster = 0;
     return LG_OK;
 }
 
@@ -1379,6 +1394,148 @@ void enqueue_md_step(lg_engine* e, bool thermo, bool apply_previous, cudaStream_
     e->launches += e->b.ntiles ? 2 : 0;
 }
 
+// ---- persistent batched MD -------------------------------------------------------
+bool persist_eligible(const lg_engine* e) {
+    const Batch& b = e->b;
+    return !(e->opt.flags & LG_OPT_NO_PERSISTENT) && b.precision == LG_PRECISION_MIXED && !b.pair_general &&
+           !b.bt_off && b.nkvec == 0 && b.n > 0;
+}
+
+// Packs the systems into groups of about equal work (atoms times the expected
+// neighbour count; longest first, each to the least loaded group) for each
+// cluster size the device can hold, and keeps the size whose largest group
+// per block is smallest.  A system's arithmetic does not depend on its group.
+int persist_plan(lg_engine* e) {
+    e->pk_cluster = -1;
+    const Batch& b = e->b;
+    int nsys = e->nsys;
+    // work of a system: its neighbour-list entries (measured when the lists
+    // exist, else estimated from the density) plus a per-atom share
+    std::vector<int> h_nnb(b.n);
+    CUDA_TRY(e, cudaMemcpy(h_nnb.data(), e->nnb.p, (size_t)b.n * sizeof(int), cudaMemcpyDeviceToHost));
+    std::vector<double> work(nsys);
+    for (int s = 0; s < nsys; s++) {
+        const HostSystem& h = e->sys[s];
+        double V = h.L[0] * h.L[1] * h.L[2];
+        double rl = e->h_sysdev[s].rlist;
+        double entries = 0.0;
+        for (int64_t i = e->begin[s]; i < e->begin[s + 1]; i++) entries += h_nnb[i];
+        if (entries == 0.0) entries = (double)h.n * (double)h.n / V * 4.0 / 3.0 * PI * rl * rl * rl;
+        work[s] = entries + 8.0 * (double)h.n;
+    }
+    std::vector<int> order(nsys);
+    for (int s = 0; s < nsys; s++) order[s] = s;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return work[x] > work[y]; });
+    double best_t = 0.0;
+    int best_c = 0;
+    std::vector<std::vector<int>> best_bins;
+    int forced = (e->opt.flags >> LG_OPT_CLUSTER_SHIFT) & 0xf;
+    for (int C : {1, 2, 4, 8}) {
+        if (forced && C != (1 << (forced - 1))) continue;
+        int gmax = persist_max_clusters(b.tpa, C, PK_STAGE_MAX);
+        if (gmax <= 0) continue;
+        int G = std::max(std::min(gmax, nsys), (nsys + PK_MAXG - 1) / PK_MAXG);
+        std::vector<std::vector<int>> bins(G);
+        std::vector<double> load(G, 0.0);
+        for (int s : order) {
+            int pick = -1;
+            for (int g = 0; g < G; g++)
+                if ((int)bins[g].size() < PK_MAXG && (pick < 0 || load[g] < load[pick])) pick = g;
+            bins[pick].push_back(s);
+            load[pick] += work[s];
+        }
+        double waves = std::ceil((double)G / (double)gmax);
+        double t = *std::max_element(load.begin(), load.end()) / C * waves;
+        if (best_c == 0 || t < 0.97 * best_t) {
+            best_t = t;
+            best_c = C;
+            best_bins = bins;
+        }
+    }
+    if (best_c == 0) return LG_OK;  // no cluster fits: the per-step kernels run
+    std::vector<int> off(1, 0), sys;
+    for (auto& bin : best_bins) {
+        if (bin.empty()) continue;
+        std::sort(bin.begin(), bin.end());
+        sys.insert(sys.end(), bin.begin(), bin.end());
+        off.push_back((int)sys.size());
+    }
+    int G = (int)off.size() - 1;
+    // the largest group's atoms, staged in shared memory when they fit
+    int stage = 0;
+    for (int g = 0; g < G; g++) {
+        int atoms = 0;
+        for (int k = off[g]; k < off[g + 1]; k++) atoms += (int)e->sys[sys[k]].n;
+        stage = std::max(stage, atoms);
+    }
+    e->pk_stage = (stage <= PK_STAGE_MAX && !(e->opt.flags & LG_OPT_NO_STAGING)) ? stage : 0;
+    cudaStream_t st = e->stream;
+    CUDA_TRY(e, e->pk_group_off.alloc(off.size()));
+    CUDA_TRY(e, e->pk_group_sys.alloc(sys.size()));
+    CUDA_TRY(e, e->pk_group_flag.alloc(G));
+    CUDA_TRY(e, e->pk_lambda.alloc(nsys));
+    CUDA_TRY(e, e->pk_ke.alloc(b.n));
+    CUDA_TRY(e, cudaMemcpyAsync(e->pk_group_off.p, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(e, cudaMemcpyAsync(e->pk_group_sys.p, sys.data(), sys.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(e, cudaStreamSynchronize(st));
+    e->pk_groups = G;
+    e->pk_cluster = best_c;
+    return LG_OK;
+}
+
+// lg_md_run on the persistent kernel: one launch per chunk, with the same
+// checkpoint / regrow / replay on a list overflow as the per-step path.
+int md_run_persistent(lg_engine* e, int64_t nsteps, bool thermo) {
+    const int chunk = 32;
+    cudaStream_t st = e->stream;
+    int64_t done = 0;
+    int retries = 0;
+    size_t bytes = e->b.n * sizeof(double4_32a);
+    while (done < nsteps) {
+        int steps = (int)std::min<int64_t>(chunk, nsteps - done);
+        int key = 2 * steps + (thermo ? 1 : 0);
+        auto it = e->pk_graphs.find(key);
+        if (it == e->pk_graphs.end()) {
+            cudaGraph_t g;
+            CUDA_TRY(e, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            cudaMemcpyAsync(e->cp_pos.p, e->posq.p, bytes, cudaMemcpyDeviceToDevice, st);
+            cudaMemcpyAsync(e->cp_vel.p, e->vel.p, bytes, cudaMemcpyDeviceToDevice, st);
+            cudaMemcpyAsync(e->cp_acc.p, e->acc.p, bytes, cudaMemcpyDeviceToDevice, st);
+            cudaMemsetAsync(e->pk_group_flag.p, 0, e->pk_groups * sizeof(int), st);
+            PkArgs a{e->pk_groups, e->pk_group_off.p, e->pk_group_sys.p, e->pk_group_flag.p, e->pk_lambda.p,
+                     e->pk_ke.p, steps, thermo ? 1 : 0, e->pk_stage};
+            cudaError_t le = launch_md_persist(e->b, a, e->pk_cluster, st);
+            cudaError_t ce = cudaStreamEndCapture(st, &g);
+            if (le != cudaSuccess) return fail(e, LG_ERR_CUDA, std::string("persistent launch: ") + cudaGetErrorString(le));
+            if (ce != cudaSuccess) return fail(e, LG_ERR_CUDA, std::string("stream capture: ") + cudaGetErrorString(ce));
+            cudaGraphExec_t exec = nullptr;
+            ce = cudaGraphInstantiate(&exec, g, 0);
+            cudaGraphDestroy(g);
+            if (ce != cudaSuccess)
+                return fail(e, LG_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ce));
+            it = e->pk_graphs.emplace(key, exec).first;
+        }
+        CUDA_TRY(e, cudaGraphLaunch(it->second, st));
+        e->launches += 1;
+        uint32_t status;
+        int rc = read_status(e, &status);
+        if (rc) return rc;
+        if (status & ST_OVERFLOW) {
+            if (++retries > 4) return fail(e, LG_ERR_CAPACITY, "neighbour list overflow persisted after regrowing");
+            CUDA_TRY(e, cudaMemcpyAsync(e->posq.p, e->cp_pos.p, bytes, cudaMemcpyDeviceToDevice, st));
+            CUDA_TRY(e, cudaMemcpyAsync(e->vel.p, e->cp_vel.p, bytes, cudaMemcpyDeviceToDevice, st));
+            CUDA_TRY(e, cudaMemcpyAsync(e->acc.p, e->cp_acc.p, bytes, cudaMemcpyDeviceToDevice, st));
+            rc = clear_status_bits(e, ST_OVERFLOW);
+            if (rc) return rc;
+            rc = regrow(e);
+            if (rc) return rc;
+            continue;
+        }
+        done += steps;
+    }
+    return LG_OK;
+}
+
 int build_md_graph(lg_engine* e, int steps, bool thermo) {
     if (e->graph_thermo != thermo) e->drop_graphs();
     cudaGraph_t g;
@@ -1420,6 +1577,15 @@ int lg_md_run(lg_engine* e, int64_t nsteps) {
     if (!e->tuned) {
         int rc = autotune(e);
         if (rc) return rc;
+    }
+    // the persistent kernel for runs of several steps: a launch pays for the
+    // slowest group's list rebuild, which short runs do not amortize
+    if (persist_eligible(e) && nsteps >= 8) {
+        if (e->pk_cluster == 0) {
+            int rc = persist_plan(e);
+            if (rc) return rc;
+        }
+        if (e->pk_cluster > 0) return md_run_persistent(e, nsteps, thermo);
     }
     DBuf<double4_32a>& cp_pos = e->cp_pos;
     DBuf<double4_32a>& cp_vel = e->cp_vel;
@@ -1518,6 +1684,13 @@ int lg_md_integrate(lg_engine* e, double* positions, double* velocities, int64_t
 int lg_get_stream(lg_engine* e, void** stream) {
     if (!e || !stream) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
     *stream = (void*)e->stream;
+    return LG_OK;
+}
+
+int lg_md_plan(lg_engine* e, int32_t* cluster, int32_t* groups) {
+    if (!e || !cluster || !groups) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    *cluster = e->pk_cluster > 0 ? e->pk_cluster : 0;
+    *groups = e->pk_cluster > 0 ? e->pk_groups : 0;
     return LG_OK;
 }
 

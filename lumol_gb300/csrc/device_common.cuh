@@ -72,6 +72,7 @@ struct SysDev {
     float Lf[3], invLf[3];        // FP32 copies for the list build and the mixed path
     float Lq[3];                  // L / 2^32: the length of one fixed-point unit
     float rlist2_f;               // (rlist + margin)^2 in FP32
+    float rebuild2_f;             // 0.99 (skin / 2)^2: FP32 displacement threshold (errs towards rebuilding)
     float coul_rc2_f;
 };
 
@@ -94,6 +95,121 @@ __device__ __forceinline__ float charge_f32(double q) {
 __device__ __forceinline__ uint4 fixed_position(const SysDev& s, double4_32a p) {
     return make_uint4(fixed_coordinate(p.x, s.fxscale[0]), fixed_coordinate(p.y, s.fxscale[1]),
                       fixed_coordinate(p.z, s.fxscale[2]), __float_as_uint(charge_f32(p.w)));
+}
+
+// Squared minimum-image distance of two fixed-point positions in FP32, every
+// operation rounded on its own, so the list builds of the per-step and the
+// persistent kernels decide every candidate alike.
+__device__ __forceinline__ float fixed_dist2(uint4 a, uint4 b, const float* Lq) {
+    float dx = __fmul_rn((float)(int32_t)(a.x - b.x), Lq[0]);
+    float dy = __fmul_rn((float)(int32_t)(a.y - b.y), Lq[1]);
+    float dz = __fmul_rn((float)(int32_t)(a.z - b.z), Lq[2]);
+    return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
+
+// Cell of a fixed-point position: u / 2^32 is the wrapped fraction of the
+// cell length, so floor(fraction * ncell) is (u * ncell) >> 32.
+__device__ __forceinline__ int fixed_cell(const SysDev& s, uint4 u) {
+    int cx = (int)(((unsigned long long)u.x * (unsigned)s.ncell[0]) >> 32);
+    int cy = (int)(((unsigned long long)u.y * (unsigned)s.ncell[1]) >> 32);
+    int cz = (int)(((unsigned long long)u.z * (unsigned)s.ncell[2]) >> 32);
+    return s.cell_begin + (cz * s.ncell[1] + cy) * s.ncell[0] + cx;
+}
+
+// Candidate cells of a list build.  Cells are at least half the list radius
+// wide, so every atom within the list radius of an atom in cell (cx, cy, cz)
+// lies within two cells of it per dimension (all cells of a dimension with
+// fewer than five, each once).  The candidates come as runs of cells that are
+// contiguous in memory (one x-row segment each; the periodic wrap splits a
+// segment in two): run k = (iz * ny + iy) * 2 + part, at most 5 * 5 * 2 runs.
+constexpr int NL_RUNS = 64;
+
+__device__ __forceinline__ int stencil_span(int nc) { return nc >= 5 ? 5 : nc; }
+__device__ __forceinline__ int stencil_at(int c, int nc, int k) { return nc >= 5 ? (c + k - 2 + nc) % nc : k; }
+
+// Cells [lo, hi] (system-local indices, hi < lo: empty) of run k.
+__device__ __forceinline__ void stencil_run(const SysDev& s, int cx, int cy, int cz, int k, int& lo, int& hi) {
+    int ny = stencil_span(s.ncell[1]);
+    int iz = k / (2 * ny), iy = (k / 2) % ny, part = k & 1;
+    int z = stencil_at(cz, s.ncell[2], iz), y = stencil_at(cy, s.ncell[1], iy);
+    int nx = s.ncell[0];
+    int xlo, xhi;
+    if (nx < 5) {
+        xlo = part == 0 ? 0 : 1;
+        xhi = part == 0 ? nx - 1 : 0;
+    } else if (cx - 2 < 0) {  // wraps below: [cx - 2 + nx, nx - 1], then [0, cx + 2]
+        xlo = part == 0 ? cx - 2 + nx : 0;
+        xhi = part == 0 ? nx - 1 : cx + 2;
+    } else if (cx + 2 >= nx) {  // wraps above: [cx - 2, nx - 1], then [0, cx + 2 - nx]
+        xlo = part == 0 ? cx - 2 : 0;
+        xhi = part == 0 ? nx - 1 : cx + 2 - nx;
+    } else {
+        xlo = part == 0 ? cx - 2 : 1;
+        xhi = part == 0 ? cx + 2 : 0;
+    }
+    int row = (z * s.ncell[1] + y) * nx;
+    lo = row + xlo;
+    hi = row + xhi;
+}
+
+__device__ __forceinline__ int stencil_runs(const SysDev& s) {
+    return stencil_span(s.ncell[2]) * stencil_span(s.ncell[1]) * 2;
+}
+
+// One warp's candidate table for an atom in system cell `local` (system-local
+// index) of system si: s_lo[k] = first slot of run k, s_pre[k] = candidates
+// before run k, s_pre[nruns] = total.  Returns (nruns, total).
+__device__ __forceinline__ int2 stencil_table(const SysDev& s, int si, int local, const int* __restrict__ cell_start,
+                                              int lane, int* s_lo, int* s_pre) {
+    int cx = local % s.ncell[0];
+    int cy = (local / s.ncell[0]) % s.ncell[1];
+    int cz = local / (s.ncell[0] * s.ncell[1]);
+    int nruns = stencil_runs(s);
+    int cnt[2], lo[2];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        int k = lane + 32 * h;
+        cnt[h] = 0;
+        lo[h] = 0;
+        if (k < nruns) {
+            int c0, c1;
+            stencil_run(s, cx, cy, cz, k, c0, c1);
+            if (c1 >= c0) {
+                lo[h] = cell_start[s.cell_begin + c0 + si];
+                cnt[h] = cell_start[s.cell_begin + c1 + 1 + si] - lo[h];
+            }
+        }
+    }
+    int base = 0, total = 0;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        int incl = cnt[h];
+        for (int o = 1; o < 32; o <<= 1) {
+            int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        int sum = __shfl_sync(0xffffffffu, incl, 31);
+        int k = lane + 32 * h;
+        if (k < nruns) {
+            s_lo[k] = lo[h];
+            s_pre[k] = base + incl - cnt[h];
+        }
+        base += sum;
+        total = base;
+    }
+    if (lane == 0) s_pre[nruns] = total;
+    return make_int2(nruns, total);
+}
+
+// Slot of candidate q: the run holding it is the last k with s_pre[k] <= q.
+__device__ __forceinline__ int stencil_slot(const int* s_lo, const int* s_pre, int nruns, int q) {
+    int a = 0, b = nruns - 1;
+    while (a < b) {
+        int mid = (a + b + 1) >> 1;
+        if (s_pre[mid] <= q) a = mid;
+        else b = mid - 1;
+    }
+    return s_lo[a] + (q - s_pre[a]);
 }
 
 // One Ewald k-vector with its factors (ewald.rs:102-116).

@@ -78,12 +78,30 @@ struct Batch {
     int* nlo = nullptr;           // n: entries j < i at the head of each row
     int* rev = nullptr;           // n * maxnb: for j < i, the slot of i in row j
     double4_32a* pf = nullptr;    // n * maxnb: force on i from pair (i, j > i)
-    double* inv_mass = nullptr;   // n: 1 / m (mixed path)
+    float* inv_mass = nullptr;    // n: 1 / m in FP32 (mixed path)
     PairDevF* ptabf = nullptr;
     KVecF* kvecf = nullptr;
     float2* eikrf = nullptr;
     float2* rhof = nullptr;
 };
+
+// persist.cu: batched MD of pairs-only systems, one persistent launch per run of steps
+constexpr int PK_MAXG = 64;       // systems per group
+struct PkArgs {
+    int ngroups;
+    const int* group_off;         // ngroups + 1: each group's range in group_sys
+    const int* group_sys;         // system indices, group by group
+    int* group_flag;              // ngroups: a list overflow stopped the group (zero before a launch)
+    double* lambda;               // nsys: Berendsen factor of the last step
+    double* ke;                   // n: kinetic energy of each atom after the last step
+    int nsteps;
+    int thermo;                   // some system has a thermostat
+    int stage;                    // > 0: every block stages this many atoms' positions in shared memory
+};
+constexpr int PK_STAGE_MAX = 9216;  // atoms a group may stage (20 bytes each)
+cudaError_t launch_md_persist(const Batch& b, const PkArgs& a, int cluster, cudaStream_t st);
+int persist_max_clusters(int tpa, int cluster, int stage_atoms);
+size_t persist_smem_bytes(int stage_atoms);
 
 // nlist.cu
 void launch_nlist_build(const Batch& b, cudaStream_t st);

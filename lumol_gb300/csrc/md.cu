@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(VV_TILE) vv_first_kernel(
         v.y *= f;
         v.z *= f;
     }
-    float dx, dy, dz;
+    float r2;
     if (MIXED) {
         v.x = fma(hdt, a.x, v.x);
         v.y = fma(hdt, a.y, v.y);
@@ -144,10 +144,7 @@ __global__ void __launch_bounds__(VV_TILE) vv_first_kernel(
         p.z = fma(v.z, dt, p.z);
         uint4 u = fixed_position(s, p);
         posfx[perm[i]] = u;  // a rebuild this step rewrites it in the new order
-        uint4 ub = pfx_build[i];
-        dx = (float)(int32_t)(u.x - ub.x) * s.Lq[0];
-        dy = (float)(int32_t)(u.y - ub.y) * s.Lq[1];
-        dz = (float)(int32_t)(u.z - ub.z) * s.Lq[2];
+        r2 = fixed_dist2(u, pfx_build[i], s.Lq);  // as the persistent kernel
     } else {
         v.x = __dadd_rn(v.x, __dmul_rn(hdt, a.x));
         v.y = __dadd_rn(v.y, __dmul_rn(hdt, a.y));
@@ -156,29 +153,31 @@ __global__ void __launch_bounds__(VV_TILE) vv_first_kernel(
         p.y = __dadd_rn(p.y, __dmul_rn(v.y, dt));
         p.z = __dadd_rn(p.z, __dmul_rn(v.z, dt));
         double4_32a b = pos_build[i];
-        dx = (float)(p.x - b.x);
-        dy = (float)(p.y - b.y);
-        dz = (float)(p.z - b.z);
+        float dx = (float)(p.x - b.x);
+        float dy = (float)(p.y - b.y);
+        float dz = (float)(p.z - b.z);
         dx -= rintf(dx * s.invLf[0]) * s.Lf[0];
         dy -= rintf(dy * s.invLf[1]) * s.Lf[1];
         dz -= rintf(dz * s.invLf[2]) * s.Lf[2];
+        r2 = dx * dx + dy * dy + dz * dz;
         if (posfx) posfx[i] = fixed_position(s, p);  // atom order: the half-list kernel's FP32 classification
     }
     vel[i] = v;
     posq[i] = p;
     // against a threshold 1 % below (skin / 2)^2: the FP32 rounding only ever
     // triggers a rebuild early
-    flag_rebuild(dx * dx + dy * dy + dz * dz > 0.99f * (float)s.half_skin2, tile.x, status, sys_rebuild);
+    flag_rebuild(r2 > s.rebuild2_f, tile.x, status, sys_rebuild);
 }
 
 // a = F / m; v += 0.5 dt a (integrators.rs:55-68); with a thermostat, the
 // kinetic energy of the tile (fixed-order tree sum) for the next step's factor.
 // Plain path: the reference's division and unfused products; mixed path:
-// 1 / m precomputed and fused multiply-adds.
+// a = F * (1 / m) in FP32 (the force is an FP32 value) and fused multiply-adds
+// on the FP64 velocity.
 template <bool MIXED>
 __global__ void __launch_bounds__(VV_TILE) vv_second_kernel(
     const int2* __restrict__ tiles, const SysDev* __restrict__ sys, const double* __restrict__ force,
-    const double* __restrict__ inv_mass, double4_32a* __restrict__ vel, double4_32a* __restrict__ acc,
+    const float* __restrict__ inv_mass, double4_32a* __restrict__ vel, double4_32a* __restrict__ acc,
     double* __restrict__ kepart, int thermostat) {
     int2 tile = tiles[blockIdx.x];
     const SysDev& s = sys[tile.x];
@@ -189,9 +188,10 @@ __global__ void __launch_bounds__(VV_TILE) vv_second_kernel(
         double4_32a v = vel[i];
         double m = v.w;
         double4_32a a;
-        if (MIXED) {
-            double im = inv_mass[i];
-            a = make_double4_32a(force[3 * i] * im, force[3 * i + 1] * im, force[3 * i + 2] * im, 0.0);
+        if (MIXED) {  // the force is an FP32 value (the compensated sum, rounded once): a = F / m in FP32
+            float im = inv_mass[i];
+            a = make_double4_32a((double)((float)force[3 * i] * im), (double)((float)force[3 * i + 1] * im),
+                                 (double)((float)force[3 * i + 2] * im), 0.0);
             v.x = fma(hdt, a.x, v.x);
             v.y = fma(hdt, a.y, v.y);
             v.z = fma(hdt, a.z, v.z);

@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(1024) nl_plan_kernel(int nsys, const uint32_t*
 __global__ void nl_bin_kernel(int nsys, const int* __restrict__ plan, const double4_32a* __restrict__ posq,
                               const SysDev* __restrict__ sys, const uint32_t* __restrict__ status,
                               int* __restrict__ atom_cell, int* __restrict__ cell_count, float4* __restrict__ wpos,
-                              double4_32a* __restrict__ pos_build) {
+                              double4_32a* __restrict__ pos_build, int fixed) {
     if (!(*status & ST_REBUILD)) return;
     PlanView pv = plan_view(plan, nsys);
     int A = pv.apre[pv.R];
@@ -112,6 +112,13 @@ __global__ void nl_bin_kernel(int nsys, const int* __restrict__ plan, const doub
         const SysDev& s = sys[pv.sys[r]];
         int i = s.begin + (v - pv.apre[r]);
         double4_32a p = posq[i];
+        pos_build[i] = p;
+        if (fixed) {  // mixed path: cells and the list test from the fixed-point copies
+            int cell = fixed_cell(s, fixed_position(s, p));
+            atom_cell[i] = cell;
+            atomicAdd(&cell_count[cell], 1);
+            continue;
+        }
         double w[3] = {p.x, p.y, p.z};
         int c[3];
         for (int d = 0; d < 3; d++) {
@@ -123,7 +130,6 @@ __global__ void nl_bin_kernel(int nsys, const int* __restrict__ plan, const doub
         atom_cell[i] = cell;
         atomicAdd(&cell_count[cell], 1);
         wpos[i] = make_float4((float)w[0], (float)w[1], (float)w[2], (float)p.w);
-        pos_build[i] = p;
     }
 }
 
@@ -256,35 +262,23 @@ __global__ void nl_perm_kernel(int nsys, const int* __restrict__ plan, const uin
     }
 }
 
-// Stencil cells of one dimension: c-1, c, c+1 (periodic) when there are at
-// least three cells, else every cell once, so that no cell is visited twice.
-__device__ __forceinline__ int stencil_cells(int c, int nc, int* out) {
-    if (nc >= 3) {
-        out[0] = (c + nc - 1) % nc;
-        out[1] = c;
-        out[2] = (c + 1) % nc;
-        return 3;
-    }
-    for (int k = 0; k < nc; k++) out[k] = k;
-    return nc;
-}
-
 // Warp per atom: keep j != i whose FP32 minimum-image distance is below
 // rlist (plus margin).  Warps walk the planned systems' atoms in cell order
-// (neighbouring warps share a stencil).  The stencil cells are flattened into
-// one range of candidates (per-warp prefix sums of the cell populations in
-// shared memory), so all 32 lanes test candidates even when cells hold a few
-// atoms; candidates keep the cell-then-index order.  Full list: each pair
-// appears in the lists of both atoms.
+// (neighbouring warps share a stencil).  The candidate cells (two cells around
+// the atom's per dimension, cells being at least half the list radius wide)
+// come as runs of cells contiguous in memory, flattened into one range of
+// candidates (per-warp prefix sums in shared memory), so all 32 lanes test
+// candidates; candidates keep the run-then-cell-then-index order.  Full list:
+// each pair appears in the lists of both atoms.
 constexpr int NL_WARPS = 8;
 
 __global__ void __launch_bounds__(32 * NL_WARPS) nl_build_kernel(
     int nsys, const int* __restrict__ plan, const uint32_t* status, const SysDev* __restrict__ sys,
     const float4* __restrict__ wpos, const int* __restrict__ atom_cell, const int* __restrict__ cell_start,
-    const int* __restrict__ cell_atoms, const int* __restrict__ perm, int maxnb, int* __restrict__ nbr,
-    int* __restrict__ nnb, uint32_t* status_out) {
-    __shared__ int s_lo[NL_WARPS][28];
-    __shared__ int s_pre[NL_WARPS][28];
+    const int* __restrict__ cell_atoms, const int* __restrict__ perm, const uint4* __restrict__ posfx, int maxnb,
+    int* __restrict__ nbr, int* __restrict__ nnb, uint32_t* status_out) {
+    __shared__ int s_lo[NL_WARPS][NL_RUNS];
+    __shared__ int s_pre[NL_WARPS][NL_RUNS + 1];
     if (!(*status & ST_REBUILD)) return;
     PlanView pv = plan_view(plan, nsys);
     int A = pv.apre[pv.R];
@@ -295,36 +289,12 @@ __global__ void __launch_bounds__(32 * NL_WARPS) nl_build_kernel(
         int si = pv.sys[r];
         const SysDev& s = sys[si];
         int i = cell_atoms[s.begin + (w - pv.apre[r])];
-        float4 pi = wpos[i];
-        int local = atom_cell[i] - s.cell_begin;
-        int cx = local % s.ncell[0];
-        int cy = (local / s.ncell[0]) % s.ncell[1];
-        int cz = local / (s.ncell[0] * s.ncell[1]);
-        int sx[3], sy[3], sz[3];
-        int nx = stencil_cells(cx, s.ncell[0], sx);
-        int ny = stencil_cells(cy, s.ncell[1], sy);
-        int nz = stencil_cells(cz, s.ncell[2], sz);
-        int ncand = nx * ny * nz;
-        // lane c < ncand owns stencil cell c (z, y, x order)
-        int cnt = 0, lo = 0;
-        if (lane < ncand) {
-            int a = lane / (nx * ny), b = (lane / nx) % ny, c = lane % nx;
-            int cell = s.cell_begin + (sz[a] * s.ncell[1] + sy[b]) * s.ncell[0] + sx[c];
-            lo = cell_start[cell + si];
-            cnt = cell_start[cell + si + 1] - lo;
-        }
-        int incl = cnt;
-        for (int o = 1; o < 32; o <<= 1) {
-            int v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += v;
-        }
-        int total = __shfl_sync(0xffffffffu, incl, 31);
+        // mixed path (perm): the fixed-point copies in the new cell order (written by nl_perm)
+        float4 pi = perm ? make_float4(0.f, 0.f, 0.f, 0.f) : wpos[i];
+        uint4 ui = perm ? posfx[perm[i]] : make_uint4(0u, 0u, 0u, 0u);
         __syncwarp();  // the previous atom's readers of s_lo / s_pre are done
-        if (lane < ncand) {
-            s_lo[wib][lane] = lo;
-            s_pre[wib][lane] = incl - cnt;
-        }
-        if (lane == 0) s_pre[wib][ncand] = total;
+        int2 nt = stencil_table(s, si, atom_cell[i] - s.cell_begin, cell_start, lane, s_lo[wib], s_pre[wib]);
+        int nruns = nt.x, total = nt.y;
         __syncwarp();
         float Lx = s.Lf[0], Ly = s.Lf[1], Lz = s.Lf[2];
         float ix = s.invLf[0], iy = s.invLf[1], iz = s.invLf[2];
@@ -338,23 +308,21 @@ __global__ void __launch_bounds__(32 * NL_WARPS) nl_build_kernel(
             bool keep = false;
             int j = -1, jout = -1;
             if (t < total) {
-                // the stencil cell holding candidate t: last c with pre[c] <= t
-                int a = 0, b = ncand - 1;
-                while (a < b) {
-                    int mid = (a + b + 1) >> 1;
-                    if (s_pre[wib][mid] <= t) a = mid;
-                    else b = mid - 1;
+                int slot = stencil_slot(s_lo[wib], s_pre[wib], nruns, t);
+                if (perm) {  // the same test as the persistent kernel's list build
+                    jout = slot;
+                    keep = slot != row && fixed_dist2(ui, posfx[slot], s.Lq) < rl2;
+                } else {
+                    j = cell_atoms[slot];
+                    jout = j;
+                    float4 pj = wpos[j];
+                    float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+                    dx -= rintf(dx * ix) * Lx;
+                    dy -= rintf(dy * iy) * Ly;
+                    dz -= rintf(dz * iz) * Lz;
+                    float r2 = dx * dx + dy * dy + dz * dz;
+                    keep = (j != i) && (r2 < rl2);
                 }
-                int slot = s_lo[wib][a] + (t - s_pre[wib][a]);
-                j = cell_atoms[slot];
-                jout = perm ? slot : j;
-                float4 pj = wpos[j];
-                float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-                dx -= rintf(dx * ix) * Lx;
-                dy -= rintf(dy * iy) * Ly;
-                dz -= rintf(dz * iz) * Lz;
-                float r2 = dx * dx + dy * dy + dz * dz;
-                keep = (j != i) && (r2 < rl2);
             }
             unsigned mask = __ballot_sync(0xffffffffu, keep);
             if (keep) {
@@ -472,7 +440,7 @@ void launch_nlist_build(const Batch& b, cudaStream_t st) {
     unsigned scan_grid = (unsigned)std::min(b.nsys, 2 * b.sms);
     nl_plan_kernel<<<1, 1024, 0, st>>>(b.nsys, b.status, b.sys_rebuild, b.sys, b.plan);
     nl_bin_kernel<<<atoms_grid, tb, 0, st>>>(b.nsys, b.plan, b.posq, b.sys, b.status, b.atom_cell, b.cell_count,
-                                             b.wpos, b.pos_build);
+                                             b.wpos, b.pos_build, b.perm ? 1 : 0);
     nl_scan_kernel<<<scan_grid, 1024, 0, st>>>(b.nsys, b.status, b.plan, b.sys, b.cell_count, b.cell_start);
     nl_scatter_kernel<<<atoms_grid, tb, 0, st>>>(b.nsys, b.plan, b.status, b.sys, b.atom_cell, b.cell_count,
                                                  b.cell_start, b.cell_atoms);
@@ -482,8 +450,8 @@ void launch_nlist_build(const Batch& b, cudaStream_t st) {
         nl_perm_kernel<<<atoms_grid, tb, 0, st>>>(b.nsys, b.plan, b.status, b.sys, b.cell_atoms, b.kind, b.mol,
                                                   b.posq, b.perm, b.km, b.posfx, b.pfx_build);
     nl_build_kernel<<<build_grid, 32 * NL_WARPS, 0, st>>>(b.nsys, b.plan, b.status, b.sys, b.wpos, b.atom_cell,
-                                                          b.cell_start, b.cell_atoms, b.perm, b.maxnb, b.nbr, b.nnb,
-                                                          b.status);
+                                                          b.cell_start, b.cell_atoms, b.perm, b.posfx, b.maxnb,
+                                                          b.nbr, b.nnb, b.status);
     if (b.pf) {
         nl_rowsort_kernel<<<build_grid, 32 * NL_WARPS, 0, st>>>(b.nsys, b.plan, b.status, b.sys, b.maxnb, b.nbr,
                                                                 b.nnb, b.nlo);

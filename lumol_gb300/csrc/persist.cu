@@ -1,0 +1,517 @@
+// persist.cu -- batched MD of pair-potential systems in one persistent launch.
+//
+// Independent replicas (Lumol systems with pair potentials only: no bonds, no
+// restrictions, no Coulomb) are packed into groups of about equal work, and
+// one thread-block cluster owns a group for a whole run of steps.  A step of
+// a group is a sequence of phases over its atoms, separated by cluster
+// barriers: the first Velocity-Verlet half (integrators.rs:45-53) with the
+// previous step's Berendsen factor (thermostats.rs:113-120), the neighbour
+// list rebuild of the group's systems that moved more than skin / 2, the
+// forces (the mixed path's compensated FP32 pair sums) fused with the second
+// half (integrators.rs:55-68) and the kinetic energies, then the Berendsen
+// factor of each system.  Groups never wait for one another, so a rebuild in
+// one replica delays only its own cluster, and a step costs no kernel launch.
+//
+// The arithmetic is the per-step mixed path's (same list, same order of the
+// force sums, same fixed-point positions); results agree with it to rounding
+// (the thermostat's kinetic energy is summed per system instead of per tile).
+#include <cooperative_groups.h>
+
+#include "kernels.h"
+#include "mixed_common.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace lg {
+
+constexpr int PK_THREADS = 1024;
+constexpr int PK_WARPS = PK_THREADS / 32;
+constexpr int PK_SORT = 128;  // per-warp buffer of the cell sort
+
+// last r in [0, R) with pre[r] <= v
+__device__ __forceinline__ int pk_find(const int* pre, int R, int v) {
+    int a = 0, b = R - 1;
+    while (a < b) {
+        int mid = (a + b + 1) >> 1;
+        if (pre[mid] <= v) a = mid;
+        else b = mid - 1;
+    }
+    return a;
+}
+
+// Cluster-wide barrier.  barrier.cluster.arrive has release and
+// barrier.cluster.wait acquire semantics at cluster scope, so every global
+// write made before the barrier is visible to every block of the cluster
+// after it.
+__device__ __forceinline__ void pk_sync(cg::cluster_group& cluster) { cluster.sync(); }
+
+// Every block of a cluster runs the same sequence of cluster barriers: the
+// loop over steps, the rebuild branch (decided from flags that are only
+// written before a barrier and cleared after the rebuild's last barrier) and
+// the early exit on a list overflow (a per-group flag read after a barrier)
+// are the same in every block.
+template <int TPA>
+__global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkArgs a) {
+    cg::cluster_group cluster = cg::this_cluster();
+    const int C = (int)cluster.num_blocks();
+    const int rank = (int)cluster.block_rank();
+    const int g = blockIdx.x / C;
+    if (g >= a.ngroups) return;  // every block of this cluster
+
+    __shared__ int s_sys[PK_MAXG];
+    __shared__ int s_apre[PK_MAXG + 1];
+    __shared__ int s_tpre[PK_MAXG + 1];  // tile prefix over the group's systems
+    __shared__ int s_rsys[PK_MAXG];      // systems rebuilt at this step
+    __shared__ int s_rapre[PK_MAXG + 1];
+    __shared__ int s_rcpre[PK_MAXG + 1];
+    __shared__ int s_R;
+    __shared__ int s_part[PK_THREADS];
+    __shared__ int s_lo[PK_WARPS][NL_RUNS], s_pre[PK_WARPS][NL_RUNS + 1];
+    __shared__ int s_buf[PK_WARPS][PK_SORT];
+    extern __shared__ uint4 s_dyn[];  // staged positions (a.stage atoms), then their kinds
+    uint4* s_pos = s_dyn;
+    int* s_kind = reinterpret_cast<int*>(s_dyn + a.stage);
+
+    const int gb = a.group_off[g];
+    const int G = a.group_off[g + 1] - gb;
+    if (threadIdx.x == 0) {
+        int acc = 0, tiles = 0;
+        for (int r = 0; r < G; r++) {
+            int s = a.group_sys[gb + r];
+            s_sys[r] = s;
+            s_apre[r] = acc;
+            s_tpre[r] = tiles;
+            acc += b.sys[s].end - b.sys[s].begin;
+            tiles += b.sys[s].tile_end - b.sys[s].tile_begin;
+        }
+        s_apre[G] = acc;
+        s_tpre[G] = tiles;
+    }
+    __syncthreads();
+    const int A = s_apre[G];
+    const int TT = s_tpre[G];
+    const int ct = rank * PK_THREADS + threadIdx.x;
+    const int CT = C * PK_THREADS;
+    const int wib = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const int wg = rank * PK_WARPS + wib;
+    const int WG = C * PK_WARPS;
+    bool ran = false;
+
+    for (int step = 0; step < a.nsteps; step++) {
+        // ---- 1: [v *= lambda]; v += dt/2 a; x += v dt; fixed-point copy; displacement test
+        const bool apply = a.thermo && step > 0;
+        for (int v = ct; v < A; v += CT) {
+            int r = pk_find(s_apre, G, v);
+            int s = s_sys[r];
+            const SysDev& sd = b.sys[s];
+            int i = sd.begin + (v - s_apre[r]);
+            double4_32a vel = b.vel[i], acc = b.acc[i], p = b.posq[i];
+            if (apply) {
+                double f = a.lambda[s];
+                vel.x *= f;
+                vel.y *= f;
+                vel.z *= f;
+            }
+            vel.x = fma(sd.hdt, acc.x, vel.x);
+            vel.y = fma(sd.hdt, acc.y, vel.y);
+            vel.z = fma(sd.hdt, acc.z, vel.z);
+            p.x = fma(vel.x, sd.dt, p.x);
+            p.y = fma(vel.y, sd.dt, p.y);
+            p.z = fma(vel.z, sd.dt, p.z);
+            b.vel[i] = vel;
+            b.posq[i] = p;
+            uint4 u = fixed_position(sd, p);
+            b.posfx[b.perm[i]] = u;
+            if (fixed_dist2(u, b.pfx_build[i], sd.Lq) > sd.rebuild2_f) b.sys_rebuild[s] = 1u;
+        }
+        pk_sync(cluster);
+
+        // ---- 2: rebuild the lists of the systems that asked for it
+        if (threadIdx.x == 0) {
+            int R = 0, ac = 0, cc = 0;
+            for (int r = 0; r < G; r++) {
+                int s = s_sys[r];
+                if (*(volatile const uint32_t*)&b.sys_rebuild[s]) {
+                    const SysDev& sd = b.sys[s];
+                    s_rsys[R] = s;
+                    s_rapre[R] = ac;
+                    s_rcpre[R] = cc;
+                    ac += sd.end - sd.begin;
+                    cc += sd.ncell[0] * sd.ncell[1] * sd.ncell[2];
+                    R++;
+                }
+            }
+            s_rapre[R] = ac;
+            s_rcpre[R] = cc;
+            s_R = R;
+        }
+        __syncthreads();
+        const int R = s_R;
+        if (R > 0) {
+            const int RA = s_rapre[R], RC = s_rcpre[R];
+            // 2a: cell of each atom from its fixed-point copy (written in phase 1:
+            // u / 2^32 is the wrapped fraction of the cell, so the cell index is
+            // (u * ncell) >> 32, integer arithmetic only), build positions
+            for (int v = ct; v < RA; v += CT) {
+                int r = pk_find(s_rapre, R, v);
+                const SysDev& sd = b.sys[s_rsys[r]];
+                int i = sd.begin + (v - s_rapre[r]);
+                int cell = fixed_cell(sd, b.posfx[b.perm[i]]);
+                b.atom_cell[i] = cell;
+                atomicAdd(&b.cell_count[cell], 1);
+                b.pos_build[i] = b.posq[i];
+            }
+            pk_sync(cluster);
+            // 2b: exclusive scan of each system's cell counts (one block per system)
+            for (int q = rank; q < R; q += C) {
+                int s = s_rsys[q];
+                const SysDev& sd = b.sys[s];
+                int ncells = sd.ncell[0] * sd.ncell[1] * sd.ncell[2];
+                int* count = b.cell_count + sd.cell_begin;
+                int* start = b.cell_start + sd.cell_begin + s;
+                int t = threadIdx.x;
+                int per = (ncells + PK_THREADS - 1) / PK_THREADS;
+                int lo = min(t * per, ncells), hi = min(lo + per, ncells);
+                int sum = 0;
+                for (int c = lo; c < hi; c++) sum += count[c];
+                __syncthreads();
+                s_part[t] = sum;
+                __syncthreads();
+                for (int o = 1; o < PK_THREADS; o <<= 1) {
+                    int x = t >= o ? s_part[t - o] : 0;
+                    __syncthreads();
+                    s_part[t] += x;
+                    __syncthreads();
+                }
+                int run = sd.begin + s_part[t] - sum;
+                for (int c = lo; c < hi; c++) {
+                    start[c] = run;
+                    run += count[c];
+                    count[c] = 0;
+                }
+                if (t == PK_THREADS - 1) start[ncells] = sd.begin + s_part[t];
+            }
+            pk_sync(cluster);
+            // 2c: scatter the atoms into their cells
+            for (int v = ct; v < RA; v += CT) {
+                int r = pk_find(s_rapre, R, v);
+                int s = s_rsys[r];
+                int i = b.sys[s].begin + (v - s_rapre[r]);
+                int c = b.atom_cell[i];
+                int slot = atomicAdd(&b.cell_count[c], 1);
+                b.cell_atoms[b.cell_start[c + s] + slot] = i;
+            }
+            pk_sync(cluster);
+            // 2d: sort each cell by atom index (warp per cell), leave the counts at zero
+            for (int vc = wg; vc < RC; vc += WG) {
+                int r = pk_find(s_rcpre, R, vc);
+                int s = s_rsys[r];
+                int c = b.sys[s].cell_begin + (vc - s_rcpre[r]);
+                int lo = b.cell_start[c + s], hi = b.cell_start[c + s + 1];
+                int m = hi - lo;
+                __syncwarp();
+                if (m <= PK_SORT) {
+                    for (int x = lane; x < m; x += 32) s_buf[wib][x] = b.cell_atoms[lo + x];
+                    __syncwarp();
+                    for (int x = lane; x < m; x += 32) {
+                        int val = s_buf[wib][x], rk = 0;
+                        for (int y = 0; y < m; y++) rk += s_buf[wib][y] < val;
+                        b.cell_atoms[lo + rk] = val;
+                    }
+                } else if (lane == 0) {
+                    for (int x = lo + 1; x < hi; x++) {
+                        int val = b.cell_atoms[x];
+                        int y = x - 1;
+                        while (y >= lo && b.cell_atoms[y] > val) {
+                            b.cell_atoms[y + 1] = b.cell_atoms[y];
+                            y--;
+                        }
+                        b.cell_atoms[y + 1] = val;
+                    }
+                }
+                if (lane == 0) b.cell_count[c] = 0;
+            }
+            pk_sync(cluster);
+            // 2e: sorted position of each atom, sorted (kind, molecule), fixed-point copies
+            for (int v = ct; v < RA; v += CT) {
+                int r = pk_find(s_rapre, R, v);
+                const SysDev& sd = b.sys[s_rsys[r]];
+                int t = sd.begin + (v - s_rapre[r]);
+                int i = b.cell_atoms[t];
+                b.perm[i] = t;
+                b.km[t] = make_int2(b.kind[i], b.mol[i]);
+                uint4 u = fixed_position(sd, b.posq[i]);
+                b.posfx[t] = u;
+                b.pfx_build[i] = u;
+            }
+            pk_sync(cluster);
+            // 2f: Verlet list rows (warp per atom, cell order), as the per-step list build
+            for (int w = wg; w < RA; w += WG) {
+                int r = pk_find(s_rapre, R, w);
+                int si = s_rsys[r];
+                const SysDev& sd = b.sys[si];
+                int t = sd.begin + (w - s_rapre[r]);
+                int i = b.cell_atoms[t];
+                const uint4 ui = b.posfx[t];  // written in 2e, cell order
+                __syncwarp();  // the previous atom's readers of s_lo / s_pre are done
+                int2 nt = stencil_table(sd, si, b.atom_cell[i] - sd.cell_begin, b.cell_start, lane, s_lo[wib],
+                                        s_pre[wib]);
+                const int nruns = nt.x, total = nt.y;
+                __syncwarp();
+                float rl2 = sd.rlist2_f;
+                int count = 0;
+                int* out = b.nbr + (size_t)t * b.maxnb;
+                // candidates by sorted slot, two per lane in flight; the minimum image
+                // is the signed difference of the fixed-point coordinates
+                for (int base = 0; base < total; base += 64) {
+                    int slot[2];
+                    bool keep[2];
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        int q = base + 32 * h + lane;
+                        slot[h] = -1;
+                        if (q < total) slot[h] = stencil_slot(s_lo[wib], s_pre[wib], nruns, q);
+                    }
+                    uint4 uj[2];
+#pragma unroll
+                    for (int h = 0; h < 2; h++) uj[h] = slot[h] >= 0 ? b.posfx[slot[h]] : ui;
+#pragma unroll
+                    for (int h = 0; h < 2; h++)
+                        keep[h] = slot[h] >= 0 && slot[h] != t && fixed_dist2(ui, uj[h], sd.Lq) < rl2;
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {  // candidate order: the first 32, then the next 32
+                        unsigned mask = __ballot_sync(0xffffffffu, keep[h]);
+                        if (keep[h]) {
+                            int pos = count + __popc(mask & ((1u << lane) - 1u));
+                            if (pos < b.maxnb) out[pos] = slot[h];
+                        }
+                        count += __popc(mask);
+                    }
+                }
+                if (lane == 0) {
+                    b.nnb[t] = min(count, b.maxnb);
+                    if (count > b.maxnb) {
+                        atomicOr(b.status, ST_OVERFLOW);
+                        a.group_flag[g] = 1;
+                    }
+                }
+            }
+            pk_sync(cluster);
+            if (rank == 0 && threadIdx.x == 0)
+                for (int q = 0; q < R; q++) b.sys_rebuild[s_rsys[q]] = 0u;
+            // the same value in every block: the caller regrows and replays
+            if (*(volatile const int*)&a.group_flag[g]) break;
+        }
+
+        // ---- 3: forces (compensated FP32 sums) fused with v += dt/2 a, a = F / m, kinetic energy
+        {
+            // every block stages the group's fixed-point positions and kinds in
+            // shared memory (group order: the systems' sorted ranges one after
+            // the other), so the neighbour gathers are shared-memory loads
+            if (a.stage) {
+                for (int v = threadIdx.x; v < A; v += PK_THREADS) {
+                    int r = pk_find(s_apre, G, v);
+                    int t = b.sys[s_sys[r]].begin + (v - s_apre[r]);
+                    s_pos[v] = b.posfx[t];
+                    s_kind[v] = b.km[t].x;
+                }
+                __syncthreads();
+            }
+            constexpr int GPW = 32 / TPA;  // atoms per warp
+            const int sub = lane % TPA;
+            for (int base = wg * GPW; base < A; base += WG * GPW) {
+                int v = base + lane / TPA;
+                bool active = v < A;
+                int vv = active ? v : A - 1;
+                int r = pk_find(s_apre, G, vv);
+                const SysDev& sd = b.sys[s_sys[r]];
+                int tt = sd.begin + (vv - s_apre[r]);  // sorted position
+                int i = b.cell_atoms[tt];
+                uint4 pi = b.posfx[tt];
+                int2 kmi = b.km[tt];
+                const PairDevF* prow = b.ptabf + sd.ptab + kmi.x * sd.nk;
+                MixedAcc acc;
+                const bool single = sd.nk == 1;
+                const int4 ph1 = __ldg(reinterpret_cast<const int4*>(prow));
+                const float4 pq1 = __ldg(reinterpret_cast<const float4*>(prow) + 1);
+                int cnt = active ? b.nnb[tt] : 0;
+                const int* list = b.nbr + (size_t)tt * b.maxnb;
+                int k = sub;
+                const int off = sd.begin - s_apre[r];  // sorted position - group slot
+                for (; k + TPA < cnt; k += 2 * TPA) {
+                    int js0 = list[k], js1 = list[k + TPA];
+                    uint4 pj0, pj1;
+                    int2 km0, km1;
+                    if (a.stage) {
+                        pj0 = s_pos[js0 - off];
+                        pj1 = s_pos[js1 - off];
+                        km0 = make_int2(s_kind[js0 - off], 0);
+                        km1 = make_int2(s_kind[js1 - off], 0);
+                    } else {
+                        pj0 = b.posfx[js0];
+                        pj1 = b.posfx[js1];
+                        km0 = b.km[js0];
+                        km1 = b.km[js1];
+                    }
+                    mixed_entry<false, false>(acc, sd, prow, pi, 0.0f, kmi.y, i, tt, js0, pj0, km0, b.cell_atoms,
+                                              nullptr, nullptr, nullptr, true, false, 0.0f, 0.0f, 0.0f, single, ph1,
+                                              pq1);
+                    mixed_entry<false, false>(acc, sd, prow, pi, 0.0f, kmi.y, i, tt, js1, pj1, km1, b.cell_atoms,
+                                              nullptr, nullptr, nullptr, true, false, 0.0f, 0.0f, 0.0f, single, ph1,
+                                              pq1);
+                }
+                if (k < cnt) {
+                    int js = list[k];
+                    uint4 pj = a.stage ? s_pos[js - off] : b.posfx[js];
+                    int2 kmj = a.stage ? make_int2(s_kind[js - off], 0) : b.km[js];
+                    mixed_entry<false, false>(acc, sd, prow, pi, 0.0f, kmi.y, i, tt, js, pj, kmj, b.cell_atoms,
+                                              nullptr, nullptr, nullptr, true, false, 0.0f, 0.0f, 0.0f, single, ph1,
+                                              pq1);
+                }
+#pragma unroll
+                for (int o = TPA / 2; o > 0; o >>= 1) {
+                    float sx = __shfl_xor_sync(0xffffffffu, acc.fxs, o), cx = __shfl_xor_sync(0xffffffffu, acc.fxc, o);
+                    float sy = __shfl_xor_sync(0xffffffffu, acc.fys, o), cy = __shfl_xor_sync(0xffffffffu, acc.fyc, o);
+                    float sz = __shfl_xor_sync(0xffffffffu, acc.fzs, o), cz = __shfl_xor_sync(0xffffffffu, acc.fzc, o);
+                    two_sum_acc(acc.fxs, acc.fxc, sx);
+                    acc.fxc += cx;
+                    two_sum_acc(acc.fys, acc.fyc, sy);
+                    acc.fyc += cy;
+                    two_sum_acc(acc.fzs, acc.fzc, sz);
+                    acc.fzc += cz;
+                }
+                if (active && sub == 0) {
+                    // as the per-step path: the compensated sum rounded once to FP32, a = F / m in FP32
+                    float im = b.inv_mass[i];
+                    double4_32a vel = b.vel[i];
+                    double4_32a ai = make_double4_32a((double)((acc.fxs + acc.fxc) * im),
+                                                      (double)((acc.fys + acc.fyc) * im),
+                                                      (double)((acc.fzs + acc.fzc) * im), 0.0);
+                    vel.x = fma(sd.hdt, ai.x, vel.x);
+                    vel.y = fma(sd.hdt, ai.y, vel.y);
+                    vel.z = fma(sd.hdt, ai.z, vel.z);
+                    b.acc[i] = ai;
+                    b.vel[i] = vel;
+                    if (a.thermo) a.ke[i] = 0.5 * vel.w * fma(vel.x, vel.x, fma(vel.y, vel.y, vel.z * vel.z));
+                }
+            }
+        }
+        pk_sync(cluster);
+
+        // ---- 4: Berendsen factor of each system: kinetic energy per 256-atom tile
+        // (warp per tile), then per system over its tiles in order (warp per system)
+        if (a.thermo) {
+            for (int vt = wg; vt < TT; vt += WG) {
+                int r = pk_find(s_tpre, G, vt);
+                const SysDev& sd = b.sys[s_sys[r]];
+                int tile = sd.tile_begin + (vt - s_tpre[r]);
+                int lo = b.tiles[tile].y, hi = min(lo + VV_TILE, sd.end);
+                double k = 0.0;
+                for (int i = lo + lane; i < hi; i += 32) k += a.ke[i];
+                for (int o = 16; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
+                if (lane == 0) b.kepart[tile] = k;
+            }
+            pk_sync(cluster);
+            for (int r = wg; r < G; r += WG) {
+                if (lane == 0) {
+                    const SysDev& sd = b.sys[s_sys[r]];
+                    double f = 1.0;
+                    if (sd.thermo_tau > 0.0) {
+                        double k = 0.0;
+                        for (int t = sd.tile_begin; t < sd.tile_end; t++) k += b.kepart[t];
+                        double T = 2.0 * k / (sd.dof * K_BOLTZMANN);
+                        f = sqrt(1.0 + (sd.thermo_T / T - 1.0) / sd.thermo_tau);
+                    }
+                    a.lambda[s_sys[r]] = f;
+                }
+            }
+            pk_sync(cluster);
+        }
+        ran = true;
+    }
+
+    // the last step's Berendsen scaling
+    if (a.thermo && ran && !*(volatile const int*)&a.group_flag[g]) {
+        for (int v = ct; v < A; v += CT) {
+            int r = pk_find(s_apre, G, v);
+            int s = s_sys[r];
+            int i = b.sys[s].begin + (v - s_apre[r]);
+            double f = a.lambda[s];
+            double4_32a vel = b.vel[i];
+            vel.x *= f;
+            vel.y *= f;
+            vel.z *= f;
+            b.vel[i] = vel;
+        }
+    }
+}
+
+size_t persist_smem_bytes(int stage_atoms) { return (size_t)stage_atoms * (sizeof(uint4) + sizeof(int)); }
+
+template <int TPA>
+cudaError_t launch_persist_tpa(const Batch& b, const PkArgs& a, int cluster, cudaStream_t st) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(a.ngroups * cluster), 1, 1);
+    cfg.blockDim = dim3(PK_THREADS, 1, 1);
+    // (the shared-memory limit of the kernel was raised to PK_STAGE_MAX atoms when
+    // the plan queried its occupancy, so a launch needs no attribute call)
+    cfg.dynamicSmemBytes = persist_smem_bytes(a.stage);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, md_persist_kernel<TPA>, b, a);
+}
+
+cudaError_t launch_md_persist(const Batch& b, const PkArgs& a, int cluster, cudaStream_t st) {
+    if (a.ngroups == 0 || a.nsteps == 0) return cudaSuccess;
+    switch (b.tpa) {
+        case 1:
+        case 2: return launch_persist_tpa<2>(b, a, cluster, st);
+        case 4: return launch_persist_tpa<4>(b, a, cluster, st);
+        default: return launch_persist_tpa<8>(b, a, cluster, st);
+    }
+}
+
+template <int TPA>
+int max_clusters_tpa(int cluster, int stage_atoms) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)cluster, 1, 1);
+    cfg.blockDim = dim3(PK_THREADS, 1, 1);
+    cfg.dynamicSmemBytes = persist_smem_bytes(stage_atoms);
+    if (cfg.dynamicSmemBytes > 0 &&
+        cudaFuncSetAttribute(md_persist_kernel<TPA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)cfg.dynamicSmemBytes) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int count = 0;
+    if (cudaOccupancyMaxActiveClusters(&count, md_persist_kernel<TPA>, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return count;
+}
+
+int persist_max_clusters(int tpa, int cluster, int stage_atoms) {
+    switch (tpa) {
+        case 1:
+        case 2: return max_clusters_tpa<2>(cluster, stage_atoms);
+        case 4: return max_clusters_tpa<4>(cluster, stage_atoms);
+        default: return max_clusters_tpa<8>(cluster, stage_atoms);
+    }
+}
+
+}  // namespace lg

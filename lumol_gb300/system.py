@@ -183,10 +183,15 @@ class Engine:
     """Owns one lg_engine handle (a batch of `n_systems` systems)."""
 
     def __init__(self, n_systems: int = 1, precision: str = "fp64", skin: float = 1.0, device: int = 0,
-                 threads_per_atom: int = 0):
+                 threads_per_atom: int = 0, persistent: bool = True, cluster: int = 0, staging: bool = True):
         lib = C.load()
         prec = {"fp64": C.LG_PRECISION_FP64, "mixed": C.LG_PRECISION_MIXED}[precision]
-        opt = C.LgOptions(device, prec, skin, threads_per_atom, 0)
+        flags = 0 if persistent else C.LG_OPT_NO_PERSISTENT
+        if not staging:
+            flags |= C.LG_OPT_NO_STAGING
+        if cluster:  # fixed cluster size of the persistent kernel (1, 2, 4 or 8)
+            flags |= ({1: 1, 2: 2, 4: 3, 8: 4}[cluster]) << C.LG_OPT_CLUSTER_SHIFT
+        opt = C.LgOptions(device, prec, skin, threads_per_atom, flags)
         handle = ctypes.c_void_p()
         C.check(lib.lg_create(ctypes.byref(opt), n_systems, ctypes.byref(handle)))
         self.lib = lib

@@ -1,0 +1,88 @@
+"""Persistent batched MD (one launch per run of steps, one thread-block cluster
+per group of systems) against the per-step kernels of the same mixed path.
+
+The two runs share the force arithmetic and the order of every force sum; the
+Berendsen factor's kinetic energy is summed per system in one and per tile in
+the other; the trajectories agree to rounding (1e-8 A after 80 steps), and
+each path repeats its own trajectory bit for bit.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from lumol_gb300 import workloads
+from lumol_gb300.batch import Batch
+
+pytestmark = pytest.mark.gpu
+
+PARAMS = [(64, 0.4, 120.0), (4096, 0.85, 90.0), (900, 0.3, 280.0), (1500, 0.7, 200.0), (300, 0.9, 150.0),
+          (2500, 0.5, 110.0), (128, 0.6, 250.0)]
+
+
+def replicas():
+    return [workloads.lj_replica(n, rho, t, 700 + k, "mixed") for k, (n, rho, t) in enumerate(PARAMS)]
+
+
+def launches(batch):
+    count = ctypes.c_uint64()
+    batch.engine.call("lg_launch_count", ctypes.byref(count))
+    return count.value
+
+
+def run(persistent, thermostats, calls):
+    """Both paths with 4 threads per atom, so every force sum runs in the same order."""
+    systems = replicas()
+    batch = Batch(systems, precision="mixed", persistent=persistent, threads_per_atom=4)
+    batch.md_setup([1.0] * len(systems), thermostats)
+    for k in calls:
+        before = launches(batch)
+        batch.md_run(k)
+        if persistent and k >= 8:  # one launch per run of up to 32 steps (shorter runs: per-step kernels)
+            assert launches(batch) - before == (k + 31) // 32
+    out = [batch.state(s) for s in range(len(systems))]
+    batch.engine.close()
+    return out
+
+
+@pytest.mark.parametrize("thermo", [False, True])
+def test_persistent_matches_per_step_kernels(thermo):
+    thermostats = [(t, 100.0) if (thermo and k % 2 == 0) else None for k, (n, rho, t) in enumerate(PARAMS)]
+    calls = [1, 40, 7, 32]  # run lengths across and inside the 32-step launches
+    a = run(True, thermostats, calls)
+    b = run(False, thermostats, calls)
+    tol = 1e-8
+    for (pa, va), (pb, vb) in zip(a, b):
+        assert np.abs(pa - pb).max() < tol
+        assert np.abs(va - vb).max() < tol * 10
+
+
+def test_persistent_rebuilds_lists():
+    """Hot, dilute replicas over 200 steps: every system rebuilds its list
+    several times inside the persistent launches.  Rounding differences of the
+    two paths grow along the trajectory (molecular dynamics is chaotic), so
+    the bound after 200 steps is 1e-6 A."""
+    systems = replicas()
+    batch = Batch(systems, precision="mixed", threads_per_atom=4)
+    batch.md_setup([1.0] * len(systems))
+    e0 = [batch.energy(s) for s in range(len(systems))]
+    batch.md_run(200)
+    ref = Batch(replicas(), precision="mixed", persistent=False, threads_per_atom=4)
+    ref.md_setup([1.0] * len(systems))
+    ref.md_run(200)
+    for s in range(len(systems)):
+        pa, _ = batch.state(s)
+        pb, _ = ref.state(s)
+        assert np.abs(pa - pb).max() < 1e-6
+        assert np.isfinite(e0[s])
+
+
+@pytest.mark.parametrize("persistent", [False, True])
+def test_md_paths_are_deterministic(persistent):
+    """The same run twice gives bit-identical positions and velocities: no
+    force, list or reduction depends on the order in which threads finish."""
+    thermostats = [(t, 100.0) if k % 2 == 0 else None for k, (n, rho, t) in enumerate(PARAMS)]
+    a = run(persistent, thermostats, [40, 7])
+    b = run(persistent, thermostats, [40, 7])
+    for (pa, va), (pb, vb) in zip(a, b):
+        assert np.array_equal(pa, pb) and np.array_equal(va, vb)
