@@ -534,13 +534,39 @@ def batch_roofline(args, md, C):
     fp64 = args.precision == "fp64"
     peak = ctypes.c_double()
     C.check(C.load().lg_fma_peak(1 if fp64 else 0, ctypes.byref(peak)))
+    peak_source = (("FP64" if fp64 else "FP32") + " FMA throughput measured live by lg_fma_peak "
+                   "(MEASURED_PEAKS.json has no such figure; no tensor cores on this path)")
+    cluster, groups = ctypes.c_int32(), ctypes.c_int32()
+    md.engine.call("lg_md_plan", ctypes.byref(cluster), ctypes.byref(groups))
+    if cluster.value > 0:
+        # the persistent kernel runs the whole step: time one launch of 32 steps
+        # with CUDA events on the engine's stream (state advances, as in a run)
+        import torch
+        ptr = ctypes.c_void_p()
+        md.engine.call("lg_get_stream", ctypes.byref(ptr))
+        st = torch.cuda.ExternalStream(ptr.value)
+        md.md_run(32)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
+        for e0, e1 in ev:
+            e0.record(st)
+            md.md_run(32)
+            e1.record(st)
+        torch.cuda.synchronize()
+        ms = min(e0.elapsed_time(e1) for e0, e1 in ev)
+        achieved = flops * 32 / (ms * 1e-3) / 1e12
+        return {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
+                "frac": achieved / peak.value, "traffic": traffic_from_profiles("md_persist_kernel_lj_batch256"),
+                "kernel": "md_persist_kernel", "kernel_ms": ms, "steps_per_launch": 32,
+                "cluster": cluster.value, "groups": groups.value,
+                "includes": "whole MD steps: integration, list rebuilds, forces, thermostat",
+                "peak_source": peak_source, "kernel_ms_by_group": times,
+                "work": {"pairs_lj": pairs, "pair_flops_per_step": flops}}
     achieved = flops / (times["pair"] * 1e-3) / 1e12
-    kernel = "pair_fp64_kernel" if fp64 else "pair_mixed_kernel"
+    kernel = "pair_half_kernel" if fp64 else "pair_mixed_kernel"
     return {"bound": "fp64" if fp64 else "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
-            "frac": achieved / peak.value, "traffic": traffic_from_profiles(kernel + "_lj_batch256" + ("_sorted" if not fp64 else "")),
-            "kernel": kernel, "kernel_ms": times["pair"],
-            "peak_source": ("FP64" if fp64 else "FP32") + " FMA throughput measured live by lg_fma_peak "
-                           "(MEASURED_PEAKS.json has no such figure; no tensor cores on this path)",
+            "frac": achieved / peak.value,
+            "traffic": traffic_from_profiles(kernel + "_lj_batch256" + ("_sorted" if not fp64 else "")),
+            "kernel": kernel, "kernel_ms": times["pair"], "peak_source": peak_source,
             "kernel_ms_by_group": times, "work": {"pairs_lj": pairs, "pair_flops": flops}}
 
 
@@ -757,7 +783,7 @@ def measure_roofline(args, eng, C, system):
     candidates = {"pair": work["pair_flops"], "field": work["field_flops"], "rho": work["rho_flops"]}
     dominant = max(candidates, key=lambda k: times.get(k, 0.0))
     achieved = candidates[dominant] / (times[dominant] * 1e-3) / 1e12
-    names = {"pair": "pair_fp64_kernel" if fp64 else "pair_mixed_kernel",
+    names = {"pair": "pair_half_kernel" if fp64 else "pair_mixed_kernel",
              "field": "field_kernel" if fp64 else "field_mixed_kernel",
              "rho": "rho_kernel" if fp64 else "rho_mixed_kernel"}
     pipe = "FP64" if fp64 else "FP32"

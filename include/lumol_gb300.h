@@ -132,9 +132,11 @@ typedef struct {
    lg_md_run chunk, one thread-block cluster per group of systems; this flag
    keeps them on the per-step kernels instead. */
 #define LG_OPT_NO_PERSISTENT 1
-/* The persistent kernel gathers neighbour positions from global memory
-   instead of staging them in shared memory. */
-#define LG_OPT_NO_STAGING 2
+/* Every block of the persistent kernel stages its group's positions in shared
+   memory for the neighbour gathers (by default they go through L1, which
+   keeps more of the neighbour list cached; measured equal on the batched LJ
+   workload). */
+#define LG_OPT_STAGING 2
 /* Bits 4-7 of lg_options.flags fix the cluster size of the persistent kernel
    (the value is log2(size) + 1, so 1, 2, 3, 4 select 1, 2, 4, 8 blocks);
    0 lets the planner choose. */

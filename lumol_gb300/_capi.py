@@ -23,7 +23,7 @@ LG_PAIR_ABSENT, LG_PAIR_NULL, LG_PAIR_LJ, LG_PAIR_BUCKINGHAM, LG_PAIR_HARMONIC =
 LG_COULOMB_NONE, LG_COULOMB_EWALD, LG_COULOMB_WOLF = range(3)
 LG_PRECISION_FP64, LG_PRECISION_MIXED = 0, 1
 LG_OPT_NO_PERSISTENT = 1
-LG_OPT_NO_STAGING = 2
+LG_OPT_STAGING = 2
 LG_OPT_CLUSTER_SHIFT = 4
 
 LG_TERM_PAIRS = 1

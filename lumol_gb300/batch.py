@@ -17,7 +17,7 @@ class Batch:
     and thermostat; atoms are concatenated in system order on the device."""
 
     def __init__(self, systems: list[System], precision: str = "fp64", skin: float = 1.0,
-                 threads_per_atom: int = 0, persistent: bool = True, cluster: int = 0, staging: bool = True):
+                 threads_per_atom: int = 0, persistent: bool = True, cluster: int = 0, staging: bool = False):
         self.systems = systems
         self.engine = Engine(len(systems), precision, skin, threads_per_atom=threads_per_atom,
                              persistent=persistent, cluster=cluster, staging=staging)

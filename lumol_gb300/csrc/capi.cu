@@ -1468,7 +1468,7 @@ int persist_plan(lg_engine* e) {
         for (int k = off[g]; k < off[g + 1]; k++) atoms += (int)e->sys[sys[k]].n;
         stage = std::max(stage, atoms);
     }
-    e->pk_stage = (stage <= PK_STAGE_MAX && !(e->opt.flags & LG_OPT_NO_STAGING)) ? stage : 0;
+    e->pk_stage = (stage <= PK_STAGE_MAX && (e->opt.flags & LG_OPT_STAGING)) ? stage : 0;
     cudaStream_t st = e->stream;
     CUDA_TRY(e, e->pk_group_off.alloc(off.size()));
     CUDA_TRY(e, e->pk_group_sys.alloc(sys.size()));

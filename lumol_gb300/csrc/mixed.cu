@@ -57,21 +57,24 @@ __global__ void __launch_bounds__(256) pair_mixed_kernel(
     const float4 pq1 = __ldg(reinterpret_cast<const float4*>(prow) + 1);
     int cnt = active ? nnb[tt] : 0;
     const int* list = nbr + (size_t)tt * maxnb;
-    // two entries per lane per iteration: their loads are in flight together
-    int k = sub;
-    for (; k + TPA < cnt; k += 2 * TPA) {
-        int js0 = list[k], js1 = list[k + TPA];
-        uint4 pj0 = pfx[js0], pj1 = pfx[js1];
-        int2 km0 = km[js0], km1 = km[js1];
-        mixed_entry<EV, GENERAL>(A, s, prow, pi, qi, kmi.y, i, tt, js0, pj0, km0, order, spec_off, spec_j, spec_path,
-                                 pairs, coul, coul_rc2, alpha, pref, single, ph1, pq1);
-        mixed_entry<EV, GENERAL>(A, s, prow, pi, qi, kmi.y, i, tt, js1, pj1, km1, order, spec_off, spec_j, spec_path,
-                                 pairs, coul, coul_rc2, alpha, pref, single, ph1, pq1);
-    }
-    if (k < cnt) {
-        int js = list[k];
-        mixed_entry<EV, GENERAL>(A, s, prow, pi, qi, kmi.y, i, tt, js, pfx[js], km[js], order, spec_off, spec_j,
-                                 spec_path, pairs, coul, coul_rc2, alpha, pref, single, ph1, pq1);
+    // two adjacent entries per lane per iteration, read as one 8-byte load (a
+    // group of TPA lanes reads 8 * TPA contiguous bytes); both gathers are in
+    // flight together
+    for (int base = 0; base < cnt; base += 2 * TPA) {
+        int k = base + 2 * sub;
+        if (k + 1 < cnt) {
+            int2 js = *reinterpret_cast<const int2*>(list + k);
+            uint4 pj0 = pfx[js.x], pj1 = pfx[js.y];
+            int2 km0 = km[js.x], km1 = km[js.y];
+            mixed_entry<EV, GENERAL>(A, s, prow, pi, qi, kmi.y, i, tt, js.x, pj0, km0, order, spec_off, spec_j,
+                                     spec_path, pairs, coul, coul_rc2, alpha, pref, single, ph1, pq1);
+            mixed_entry<EV, GENERAL>(A, s, prow, pi, qi, kmi.y, i, tt, js.y, pj1, km1, order, spec_off, spec_j,
+                                     spec_path, pairs, coul, coul_rc2, alpha, pref, single, ph1, pq1);
+        } else if (k < cnt) {
+            int js = list[k];
+            mixed_entry<EV, GENERAL>(A, s, prow, pi, qi, kmi.y, i, tt, js, pfx[js], km[js], order, spec_off, spec_j,
+                                     spec_path, pairs, coul, coul_rc2, alpha, pref, single, ph1, pq1);
+        }
     }
     // combine the group's compensated sums (FP32 shuffles); one lane converts to FP64
 #pragma unroll

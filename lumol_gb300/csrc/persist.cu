@@ -337,37 +337,39 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
                 const float4 pq1 = __ldg(reinterpret_cast<const float4*>(prow) + 1);
                 int cnt = active ? b.nnb[tt] : 0;
                 const int* list = b.nbr + (size_t)tt * b.maxnb;
-                int k = sub;
                 const int off = sd.begin - s_apre[r];  // sorted position - group slot
-                for (; k + TPA < cnt; k += 2 * TPA) {
-                    int js0 = list[k], js1 = list[k + TPA];
-                    uint4 pj0, pj1;
-                    int2 km0, km1;
-                    if (a.stage) {
-                        pj0 = s_pos[js0 - off];
-                        pj1 = s_pos[js1 - off];
-                        km0 = make_int2(s_kind[js0 - off], 0);
-                        km1 = make_int2(s_kind[js1 - off], 0);
-                    } else {
-                        pj0 = b.posfx[js0];
-                        pj1 = b.posfx[js1];
-                        km0 = b.km[js0];
-                        km1 = b.km[js1];
+                // as the per-step pair kernel: two adjacent entries per lane per iteration
+                for (int base2 = 0; base2 < cnt; base2 += 2 * TPA) {
+                    int k = base2 + 2 * sub;
+                    if (k + 1 < cnt) {
+                        int2 js = *reinterpret_cast<const int2*>(list + k);
+                        uint4 pj0, pj1;
+                        int2 km0, km1;
+                        if (a.stage) {
+                            pj0 = s_pos[js.x - off];
+                            pj1 = s_pos[js.y - off];
+                            km0 = make_int2(s_kind[js.x - off], 0);
+                            km1 = make_int2(s_kind[js.y - off], 0);
+                        } else {
+                            pj0 = b.posfx[js.x];
+                            pj1 = b.posfx[js.y];
+                            km0 = b.km[js.x];
+                            km1 = b.km[js.y];
+                        }
+                        mixed_entry<false, false>(acc, sd, prow, pi, 0.0f, kmi.y, i, tt, js.x, pj0, km0, b.cell_atoms,
+                                                  nullptr, nullptr, nullptr, true, false, 0.0f, 0.0f, 0.0f, single,
+                                                  ph1, pq1);
+                        mixed_entry<false, false>(acc, sd, prow, pi, 0.0f, kmi.y, i, tt, js.y, pj1, km1, b.cell_atoms,
+                                                  nullptr, nullptr, nullptr, true, false, 0.0f, 0.0f, 0.0f, single,
+                                                  ph1, pq1);
+                    } else if (k < cnt) {
+                        int js = list[k];
+                        uint4 pj = a.stage ? s_pos[js - off] : b.posfx[js];
+                        int2 kmj = a.stage ? make_int2(s_kind[js - off], 0) : b.km[js];
+                        mixed_entry<false, false>(acc, sd, prow, pi, 0.0f, kmi.y, i, tt, js, pj, kmj, b.cell_atoms,
+                                                  nullptr, nullptr, nullptr, true, false, 0.0f, 0.0f, 0.0f, single,
+                                                  ph1, pq1);
                     }
-                    mixed_entry<false, false>(acc, sd, prow, pi, 0.0f, kmi.y, i, tt, js0, pj0, km0, b.cell_atoms,
-                                              nullptr, nullptr, nullptr, true, false, 0.0f, 0.0f, 0.0f, single, ph1,
-                                              pq1);
-                    mixed_entry<false, false>(acc, sd, prow, pi, 0.0f, kmi.y, i, tt, js1, pj1, km1, b.cell_atoms,
-                                              nullptr, nullptr, nullptr, true, false, 0.0f, 0.0f, 0.0f, single, ph1,
-                                              pq1);
-                }
-                if (k < cnt) {
-                    int js = list[k];
-                    uint4 pj = a.stage ? s_pos[js - off] : b.posfx[js];
-                    int2 kmj = a.stage ? make_int2(s_kind[js - off], 0) : b.km[js];
-                    mixed_entry<false, false>(acc, sd, prow, pi, 0.0f, kmi.y, i, tt, js, pj, kmj, b.cell_atoms,
-                                              nullptr, nullptr, nullptr, true, false, 0.0f, 0.0f, 0.0f, single, ph1,
-                                              pq1);
                 }
 #pragma unroll
                 for (int o = TPA / 2; o > 0; o >>= 1) {

@@ -183,12 +183,12 @@ class Engine:
     """Owns one lg_engine handle (a batch of `n_systems` systems)."""
 
     def __init__(self, n_systems: int = 1, precision: str = "fp64", skin: float = 1.0, device: int = 0,
-                 threads_per_atom: int = 0, persistent: bool = True, cluster: int = 0, staging: bool = True):
+                 threads_per_atom: int = 0, persistent: bool = True, cluster: int = 0, staging: bool = False):
         lib = C.load()
         prec = {"fp64": C.LG_PRECISION_FP64, "mixed": C.LG_PRECISION_MIXED}[precision]
         flags = 0 if persistent else C.LG_OPT_NO_PERSISTENT
-        if not staging:
-            flags |= C.LG_OPT_NO_STAGING
+        if staging:
+            flags |= C.LG_OPT_STAGING
         if cluster:  # fixed cluster size of the persistent kernel (1, 2, 4 or 8)
             flags |= ({1: 1, 2: 2, 4: 3, 8: 4}[cluster]) << C.LG_OPT_CLUSTER_SHIFT
         opt = C.LgOptions(device, prec, skin, threads_per_atom, flags)
