@@ -248,7 +248,7 @@ struct lg_engine {
     int pk_groups = 0;
     int pk_stage = 0;    // atoms each block stages in shared memory (0: gathers from global memory)
     DBuf<int> pk_group_off, pk_group_sys, pk_group_flag;
-    DBuf<double> pk_lambda, pk_ke;
+    DBuf<double> pk_ke;
     // one graph per (steps, thermostat): checkpoint copies, flag reset, the launch
     // (a graph replay avoids the per-launch cost of a cluster launch)
     std::map<int, cudaGraphExec_t> pk_graphs;
@@ -1473,7 +1473,6 @@ int persist_plan(lg_engine* e) {
     CUDA_TRY(e, e->pk_group_off.alloc(off.size()));
     CUDA_TRY(e, e->pk_group_sys.alloc(sys.size()));
     CUDA_TRY(e, e->pk_group_flag.alloc(G));
-    CUDA_TRY(e, e->pk_lambda.alloc(nsys));
     CUDA_TRY(e, e->pk_ke.alloc(b.n));
     CUDA_TRY(e, cudaMemcpyAsync(e->pk_group_off.p, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     CUDA_TRY(e, cudaMemcpyAsync(e->pk_group_sys.p, sys.data(), sys.size() * sizeof(int), cudaMemcpyHostToDevice, st));
@@ -1502,8 +1501,8 @@ int md_run_persistent(lg_engine* e, int64_t nsteps, bool thermo) {
             cudaMemcpyAsync(e->cp_vel.p, e->vel.p, bytes, cudaMemcpyDeviceToDevice, st);
             cudaMemcpyAsync(e->cp_acc.p, e->acc.p, bytes, cudaMemcpyDeviceToDevice, st);
             cudaMemsetAsync(e->pk_group_flag.p, 0, e->pk_groups * sizeof(int), st);
-            PkArgs a{e->pk_groups, e->pk_group_off.p, e->pk_group_sys.p, e->pk_group_flag.p, e->pk_lambda.p,
-                     e->pk_ke.p, steps, thermo ? 1 : 0, e->pk_stage};
+            PkArgs a{e->pk_groups, e->pk_group_off.p, e->pk_group_sys.p, e->pk_group_flag.p, e->pk_ke.p, steps,
+                     thermo ? 1 : 0, e->pk_stage};
             cudaError_t le = launch_md_persist(e->b, a, e->pk_cluster, st);
             cudaError_t ce = cudaStreamEndCapture(st, &g);
             if (le != cudaSuccess) return fail(e, LG_ERR_CUDA, std::string("persistent launch: ") + cudaGetErrorString(le));

@@ -92,8 +92,7 @@ struct PkArgs {
     const int* group_off;         // ngroups + 1: each group's range in group_sys
     const int* group_sys;         // system indices, group by group
     int* group_flag;              // ngroups: a list overflow stopped the group (zero before a launch)
-    double* lambda;               // nsys: Berendsen factor of the last step
-    double* ke;                   // n: kinetic energy of each atom after the last step
+    double* ke;                   // n: kinetic energy of each force-phase chunk of a system, at begin + chunk
     int nsteps;
     int thermo;                   // some system has a thermostat
     int stage;                    // > 0: every block stages this many atoms' positions in shared memory

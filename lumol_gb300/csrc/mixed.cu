@@ -65,14 +65,17 @@ __global__ void __launch_bounds__(256) pair_mixed_kernel(
         if (k + 1 < cnt) {
             int2 js = *reinterpret_cast<const int2*>(list + k);
             uint4 pj0 = pfx[js.x], pj1 = pfx[js.y];
-            int2 km0 = km[js.x], km1 = km[js.y];
+            // (kind, molecule) of the neighbour: not needed for one kind without restrictions
+            const bool need_km = GENERAL || !single;
+            int2 km0 = need_km ? km[js.x] : make_int2(0, 0), km1 = need_km ? km[js.y] : make_int2(0, 0);
             mixed_entry<EV, GENERAL>(A, s, prow, pi, qi, kmi.y, i, tt, js.x, pj0, km0, order, spec_off, spec_j,
                                      spec_path, pairs, coul, coul_rc2, alpha, pref, single, ph1, pq1);
             mixed_entry<EV, GENERAL>(A, s, prow, pi, qi, kmi.y, i, tt, js.y, pj1, km1, order, spec_off, spec_j,
                                      spec_path, pairs, coul, coul_rc2, alpha, pref, single, ph1, pq1);
         } else if (k < cnt) {
             int js = list[k];
-            mixed_entry<EV, GENERAL>(A, s, prow, pi, qi, kmi.y, i, tt, js, pfx[js], km[js], order, spec_off, spec_j,
+            int2 kmj = (GENERAL || !single) ? km[js] : make_int2(0, 0);
+            mixed_entry<EV, GENERAL>(A, s, prow, pi, qi, kmi.y, i, tt, js, pfx[js], kmj, order, spec_off, spec_j,
                                      spec_path, pairs, coul, coul_rc2, alpha, pref, single, ph1, pq1);
         }
     }

@@ -8,13 +8,13 @@
 // previous step's Berendsen factor (thermostats.rs:113-120), the neighbour
 // list rebuild of the group's systems that moved more than skin / 2, the
 // forces (the mixed path's compensated FP32 pair sums) fused with the second
-// half (integrators.rs:55-68) and the kinetic energies, then the Berendsen
-// factor of each system.  Groups never wait for one another, so a rebuild in
+// half (integrators.rs:55-68) and the kinetic energy of each chunk of atoms;
+// every block derives the Berendsen factors from those at the next step.  Groups never wait for one another, so a rebuild in
 // one replica delays only its own cluster, and a step costs no kernel launch.
 //
 // The arithmetic is the per-step mixed path's (same list, same order of the
 // force sums, same fixed-point positions); results agree with it to rounding
-// (the thermostat's kinetic energy is summed per system instead of per tile).
+// (the thermostat's kinetic energy is summed per chunk instead of per tile).
 #include <cooperative_groups.h>
 
 #include "kernels.h"
@@ -45,6 +45,30 @@ __device__ __forceinline__ int pk_find(const int* pre, int R, int v) {
 // after it.
 __device__ __forceinline__ void pk_sync(cg::cluster_group& cluster) { cluster.sync(); }
 
+// Berendsen factor sqrt(1 + (T0 / T - 1) / tau) (thermostats.rs:113-120) of
+// each system of the group, T = 2 K / (dof kB) (compute.rs:133-144), K summed
+// over the system's force-phase chunks in a fixed order (lane-strided, then a
+// fixed shuffle tree), so every block of the cluster computes the same factors
+// without another barrier.  Warp w of the block handles systems w, w + 32, ...
+__device__ __forceinline__ void pk_lambdas(const Batch& b, const PkArgs& a, const int* s_sys, int G, int wib,
+                                           int lane, int gpw, double* s_lambda) {
+    for (int r = wib; r < G; r += PK_WARPS) {
+        const SysDev& sd = b.sys[s_sys[r]];
+        int nq = (sd.end - sd.begin + gpw - 1) / gpw;
+        double k = 0.0;
+        for (int q = lane; q < nq; q += 32) k += __ldcg(&a.ke[sd.begin + q]);
+        for (int o = 16; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
+        if (lane == 0) {
+            double f = 1.0;
+            if (sd.thermo_tau > 0.0) {
+                double T = 2.0 * k / (sd.dof * K_BOLTZMANN);
+                f = sqrt(1.0 + (sd.thermo_T / T - 1.0) / sd.thermo_tau);
+            }
+            s_lambda[r] = f;
+        }
+    }
+}
+
 // Every block of a cluster runs the same sequence of cluster barriers: the
 // loop over steps, the rebuild branch (decided from flags that are only
 // written before a barrier and cleared after the rebuild's last barrier) and
@@ -60,7 +84,8 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
 
     __shared__ int s_sys[PK_MAXG];
     __shared__ int s_apre[PK_MAXG + 1];
-    __shared__ int s_tpre[PK_MAXG + 1];  // tile prefix over the group's systems
+    __shared__ int s_qpre[PK_MAXG + 1];  // force-phase chunk prefix over the group's systems
+    __shared__ double s_lambda[PK_MAXG];
     __shared__ int s_rsys[PK_MAXG];      // systems rebuilt at this step
     __shared__ int s_rapre[PK_MAXG + 1];
     __shared__ int s_rcpre[PK_MAXG + 1];
@@ -74,22 +99,24 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
 
     const int gb = a.group_off[g];
     const int G = a.group_off[g + 1] - gb;
+    constexpr int GPW = 32 / TPA;  // atoms of a force-phase chunk (one warp)
     if (threadIdx.x == 0) {
-        int acc = 0, tiles = 0;
+        int acc = 0, chunks = 0;
         for (int r = 0; r < G; r++) {
             int s = a.group_sys[gb + r];
+            int n = b.sys[s].end - b.sys[s].begin;
             s_sys[r] = s;
             s_apre[r] = acc;
-            s_tpre[r] = tiles;
-            acc += b.sys[s].end - b.sys[s].begin;
-            tiles += b.sys[s].tile_end - b.sys[s].tile_begin;
+            s_qpre[r] = chunks;
+            acc += n;
+            chunks += (n + GPW - 1) / GPW;
         }
         s_apre[G] = acc;
-        s_tpre[G] = tiles;
+        s_qpre[G] = chunks;
     }
     __syncthreads();
     const int A = s_apre[G];
-    const int TT = s_tpre[G];
+    const int QQ = s_qpre[G];
     const int ct = rank * PK_THREADS + threadIdx.x;
     const int CT = C * PK_THREADS;
     const int wib = threadIdx.x >> 5;
@@ -101,6 +128,10 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
     for (int step = 0; step < a.nsteps; step++) {
         // ---- 1: [v *= lambda]; v += dt/2 a; x += v dt; fixed-point copy; displacement test
         const bool apply = a.thermo && step > 0;
+        if (apply) {
+            pk_lambdas(b, a, s_sys, G, wib, lane, GPW, s_lambda);
+            __syncthreads();
+        }
         for (int v = ct; v < A; v += CT) {
             int r = pk_find(s_apre, G, v);
             int s = s_sys[r];
@@ -108,7 +139,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
             int i = sd.begin + (v - s_apre[r]);
             double4_32a vel = b.vel[i], acc = b.acc[i], p = b.posq[i];
             if (apply) {
-                double f = a.lambda[s];
+                double f = s_lambda[r];
                 vel.x *= f;
                 vel.y *= f;
                 vel.z *= f;
@@ -318,14 +349,16 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
                 }
                 __syncthreads();
             }
-            constexpr int GPW = 32 / TPA;  // atoms per warp
+            // warp chunks of GPW atoms of one system (chunk q of system r covers its
+            // atoms q * GPW ...), so a chunk's kinetic energy belongs to one system
             const int sub = lane % TPA;
-            for (int base = wg * GPW; base < A; base += WG * GPW) {
-                int v = base + lane / TPA;
-                bool active = v < A;
-                int vv = active ? v : A - 1;
-                int r = pk_find(s_apre, G, vv);
+            for (int q = wg; q < QQ; q += WG) {
+                int r = pk_find(s_qpre, G, q);
                 const SysDev& sd = b.sys[s_sys[r]];
+                int qq = q - s_qpre[r];
+                int local = qq * GPW + lane / TPA;
+                bool active = local < sd.end - sd.begin;
+                int vv = s_apre[r] + (active ? local : 0);
                 int tt = sd.begin + (vv - s_apre[r]);  // sorted position
                 int i = b.cell_atoms[tt];
                 uint4 pi = b.posfx[tt];
@@ -350,11 +383,11 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
                             pj1 = s_pos[js.y - off];
                             km0 = make_int2(s_kind[js.x - off], 0);
                             km1 = make_int2(s_kind[js.y - off], 0);
-                        } else {
+                        } else {  // (the neighbour's kind is not needed for one kind)
                             pj0 = b.posfx[js.x];
                             pj1 = b.posfx[js.y];
-                            km0 = b.km[js.x];
-                            km1 = b.km[js.y];
+                            km0 = single ? make_int2(0, 0) : b.km[js.x];
+                            km1 = single ? make_int2(0, 0) : b.km[js.y];
                         }
                         mixed_entry<false, false>(acc, sd, prow, pi, 0.0f, kmi.y, i, tt, js.x, pj0, km0, b.cell_atoms,
                                                   nullptr, nullptr, nullptr, true, false, 0.0f, 0.0f, 0.0f, single,
@@ -365,7 +398,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
                     } else if (k < cnt) {
                         int js = list[k];
                         uint4 pj = a.stage ? s_pos[js - off] : b.posfx[js];
-                        int2 kmj = a.stage ? make_int2(s_kind[js - off], 0) : b.km[js];
+                        int2 kmj = a.stage ? make_int2(s_kind[js - off], 0) : (single ? make_int2(0, 0) : b.km[js]);
                         mixed_entry<false, false>(acc, sd, prow, pi, 0.0f, kmi.y, i, tt, js, pj, kmj, b.cell_atoms,
                                                   nullptr, nullptr, nullptr, true, false, 0.0f, 0.0f, 0.0f, single,
                                                   ph1, pq1);
@@ -383,6 +416,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
                     two_sum_acc(acc.fzs, acc.fzc, sz);
                     acc.fzc += cz;
                 }
+                double ke = 0.0;
                 if (active && sub == 0) {
                     // as the per-step path: the compensated sum rounded once to FP32, a = F / m in FP32
                     float im = b.inv_mass[i];
@@ -395,51 +429,28 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
                     vel.z = fma(sd.hdt, ai.z, vel.z);
                     b.acc[i] = ai;
                     b.vel[i] = vel;
-                    if (a.thermo) a.ke[i] = 0.5 * vel.w * fma(vel.x, vel.x, fma(vel.y, vel.y, vel.z * vel.z));
+                    if (a.thermo) ke = 0.5 * vel.w * fma(vel.x, vel.x, fma(vel.y, vel.y, vel.z * vel.z));
+                }
+                if (a.thermo) {  // the chunk's kinetic energy, lanes in a fixed order
+                    for (int o = 16; o > 0; o >>= 1) ke += __shfl_xor_sync(0xffffffffu, ke, o);
+                    if (lane == 0) a.ke[sd.begin + qq] = ke;
                 }
             }
         }
         pk_sync(cluster);
 
-        // ---- 4: Berendsen factor of each system: kinetic energy per 256-atom tile
-        // (warp per tile), then per system over its tiles in order (warp per system)
-        if (a.thermo) {
-            for (int vt = wg; vt < TT; vt += WG) {
-                int r = pk_find(s_tpre, G, vt);
-                const SysDev& sd = b.sys[s_sys[r]];
-                int tile = sd.tile_begin + (vt - s_tpre[r]);
-                int lo = b.tiles[tile].y, hi = min(lo + VV_TILE, sd.end);
-                double k = 0.0;
-                for (int i = lo + lane; i < hi; i += 32) k += a.ke[i];
-                for (int o = 16; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
-                if (lane == 0) b.kepart[tile] = k;
-            }
-            pk_sync(cluster);
-            for (int r = wg; r < G; r += WG) {
-                if (lane == 0) {
-                    const SysDev& sd = b.sys[s_sys[r]];
-                    double f = 1.0;
-                    if (sd.thermo_tau > 0.0) {
-                        double k = 0.0;
-                        for (int t = sd.tile_begin; t < sd.tile_end; t++) k += b.kepart[t];
-                        double T = 2.0 * k / (sd.dof * K_BOLTZMANN);
-                        f = sqrt(1.0 + (sd.thermo_T / T - 1.0) / sd.thermo_tau);
-                    }
-                    a.lambda[s_sys[r]] = f;
-                }
-            }
-            pk_sync(cluster);
-        }
         ran = true;
     }
 
     // the last step's Berendsen scaling
     if (a.thermo && ran && !*(volatile const int*)&a.group_flag[g]) {
+        pk_lambdas(b, a, s_sys, G, wib, lane, GPW, s_lambda);
+        __syncthreads();
         for (int v = ct; v < A; v += CT) {
             int r = pk_find(s_apre, G, v);
             int s = s_sys[r];
             int i = b.sys[s].begin + (v - s_apre[r]);
-            double f = a.lambda[s];
+            double f = s_lambda[r];
             double4_32a vel = b.vel[i];
             vel.x *= f;
             vel.y *= f;

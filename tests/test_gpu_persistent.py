@@ -86,3 +86,40 @@ def test_md_paths_are_deterministic(persistent):
     b = run(persistent, thermostats, [40, 7])
     for (pa, va), (pb, vb) in zip(a, b):
         assert np.array_equal(pa, pb) and np.array_equal(va, vb)
+
+
+def clustered_droplet(seed, precision="mixed"):
+    """A solid-density argon crystallite (FCC, a = 5.26 A, 864 atoms, LJ cut at
+    12 A) in one corner of a box four times wider.  The engine sizes the
+    neighbour capacity from each system's mean density, so the crystallite's
+    rows (about 250 neighbours within 13 A) overflow the first list build and
+    the engine regrows the lists and replays the run."""
+    from lumol_gb300 import LennardJones, PairInteraction, System, UnitCell
+    from lumol_gb300.units import from_
+    rng = np.random.default_rng(seed)
+    a, cells = 5.26, 6
+    base = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]])
+    grid = np.array([[i, j, k] for i in range(cells) for j in range(cells) for k in range(cells)], dtype=float)
+    pos = (grid[:, None, :] + base[None, :, :]).reshape(-1, 3) * a + 1.0
+    pos = pos + rng.uniform(-0.05, 0.05, size=pos.shape)
+    s = System(UnitCell.cubic(4 * cells * a), precision=precision)
+    s.add_particles(["Ar"] * len(pos), pos, masses=[39.948] * len(pos))
+    lj = LennardJones(sigma=3.405, epsilon=from_(0.996, "kJ/mol"))
+    s.set_pair_potential(("Ar", "Ar"), PairInteraction.shifted(lj, 12.0))
+    s.velocities = workloads.boltzmann_velocities(s, 40.0, seed + 1)
+    return s
+
+
+def test_persistent_list_overflow_is_regrown_and_replayed():
+    def run_once(persistent):
+        systems = [clustered_droplet(3), workloads.lj_replica(300, 0.3, 120.0, 9, "mixed")]
+        batch = Batch(systems, precision="mixed", persistent=persistent, threads_per_atom=4)
+        batch.md_setup([1.0, 1.0])
+        batch.md_run(40)
+        out = [batch.state(s) for s in range(2)]
+        batch.engine.close()
+        return out
+    a = run_once(True)
+    b = run_once(False)
+    for (pa, va), (pb, vb) in zip(a, b):
+        assert np.all(np.isfinite(pa)) and np.abs(pa - pb).max() < 1e-8
