@@ -1910,10 +1910,15 @@ int lg_mc_run(lg_engine* e, int64_t moves) {
         }
     if (!any) return fail(e, LG_ERR_STATE, "lg_mc_setup was not called for any system");
     CUDA_TRY(e, cudaMemcpyAsync(e->mc_chains.p, e->h_mc.data(), nsys * sizeof(McState), cudaMemcpyHostToDevice, st));
-    // the list must be current for the positions the chains start from
+    // the list must be current for the positions the chains start from, and so
+    // must the fixed-point copies the mixed chains read
     launch_check_displacement(e->b, st);
     launch_nlist_build(e->b, st);
     e->launches += 1 + nlist_launches(e->b);
+    if (!fp64) {
+        launch_split_positions(e->b, st);
+        e->launches += 1;
+    }
     for (int64_t launch = 0; launch < moves + 64; launch++) {
         launch_mc_chains(e->b, e->mc_chains.p, fp64, st);
         e->launches += 1;

@@ -379,11 +379,127 @@ __global__ void __launch_bounds__(128) mc_chain_kernel(Batch b, McState* __restr
     }
 }
 
+// Pair energy in FP32 from r^2 (the mixed path's parameters, shift included).
+__device__ __forceinline__ float mc_pair_energy_r2(int type, float4 pq, float shift, float r2) {
+    if (!(r2 < pq.w)) return 0.0f;
+    float ir2 = 1.0f / r2;
+    float ir6 = ir2 * ir2 * ir2;
+    switch (type) {
+        case 2: return ir6 * (pq.x * ir6 - pq.y) - shift;
+        case 3: {
+            float inv_r = rsqrtf(r2);
+            return pq.x * __expf(-r2 * inv_r * pq.z) - pq.y * ir6 - shift;
+        }
+        case 4: {
+            float dr = r2 * rsqrtf(r2) - pq.y;
+            return 0.5f * pq.x * dr * dr - shift;
+        }
+        default: return 0.0f;
+    }
+}
+
+// Chains of a mixed-precision engine: the same moves and draws as the FP64
+// chains, with the energy change evaluated like the mixed MD path: fixed-point
+// positions in the cell order of the last list build (a neighbour is one
+// gather, its minimum image an integer difference), FP32 pair energies summed
+// per lane in FP32 and across lanes in FP64, the Metropolis test with expf.
+// An accepted move updates the FP64 position and its fixed-point copy.
+__global__ void __launch_bounds__(128) mc_chain_mixed_kernel(Batch b, McState* __restrict__ mc) {
+    int s = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    int lane = threadIdx.x & 31;
+    if (s >= b.nsys) return;
+    McState st = mc[s];
+    if (!st.enabled || st.moves_left <= 0 || st.need_rebuild) return;
+    const SysDev& sd = b.sys[s];
+    int natoms = sd.end - sd.begin;
+    if (natoms <= 0) return;
+    const bool single = sd.nk == 1;  // one kind: the parameters once per chain
+    const PairDevF* ptab = b.ptabf + sd.ptab;
+    int4 ph1 = *reinterpret_cast<const int4*>(ptab);
+    float4 pq1 = *(reinterpret_cast<const float4*>(ptab) + 1);
+    float shift1 = ptab->shift;
+    const float rebuild2 = sd.rebuild2_f;
+    uint64_t rng = st.rng;
+    int64_t left = st.moves_left;
+    double energy = st.energy;
+    long long accepted = st.accepted, attempted = st.attempted;
+    bool rebuild = false;
+    while (left > 0) {
+        // the move: a random atom (select_molecule) and a displacement in [-delta, delta) per axis
+        uint64_t saved = rng;
+        int i = sd.begin + min((int)(uniform01(rng) * natoms), natoms - 1);
+        double ddx = -st.delta + 2.0 * st.delta * uniform01(rng);
+        double ddy = -st.delta + 2.0 * st.delta * uniform01(rng);
+        double ddz = -st.delta + 2.0 * st.delta * uniform01(rng);
+        double u_accept = uniform01(rng);
+        int t = b.perm[i];
+        double4_32a old = b.posq[i];
+        uint4 uo = b.posfx[t];
+        double4_32a np = make_double4_32a(old.x + ddx, old.y + ddy, old.z + ddz, old.w);
+        uint4 un = fixed_position(sd, np);
+        if (fixed_dist2(un, b.pfx_build[i], sd.Lq) > rebuild2) {
+            rng = saved;  // not attempted: retried after the list rebuild
+            rebuild = true;
+            break;
+        }
+        int ki = single ? 0 : b.km[t].x;
+        const PairDevF* prow = ptab + ki * sd.nk;
+        int cnt = b.nnb[t];
+        const int* list = b.nbr + (size_t)t * b.maxnb;
+        float de = 0.0f;
+        for (int k = lane; k < cnt; k += 32) {
+            int js = list[k];
+            uint4 pj = b.posfx[js];
+            int type = ph1.x;
+            float4 pq = pq1;
+            float shift = shift1;
+            int restr = ph1.y;
+            if (!single) {
+                const PairDevF* pp = prow + b.km[js].x;
+                int4 ph = *reinterpret_cast<const int4*>(pp);
+                type = ph.x;
+                restr = ph.y;
+                pq = *(reinterpret_cast<const float4*>(pp) + 1);
+                shift = pp->shift;
+            }
+            if (type == 0 || restriction_excluded(restr, 0)) continue;
+            de += mc_pair_energy_r2(type, pq, shift, fixed_dist2(un, pj, sd.Lq)) -
+                  mc_pair_energy_r2(type, pq, shift, fixed_dist2(uo, pj, sd.Lq));
+        }
+        double ded = (double)de;
+        for (int o = 16; o > 0; o >>= 1) ded += __shfl_xor_sync(0xffffffffu, ded, o);
+        attempted++;
+        double cost = st.beta * ded;
+        bool accept = cost <= 0.0 || (float)u_accept < __expf(-(float)cost);
+        if (accept) {
+            // Translate::apply: new position, then Molecule::wrap (UnitCell::wrap_vector)
+            if (lane == 0) {
+                double w[3] = {np.x, np.y, np.z};
+                for (int d = 0; d < 3; d++) w[d] -= floor(w[d] * sd.invL[d]) * sd.L[d];
+                b.posq[i] = make_double4_32a(w[0], w[1], w[2], old.w);
+                b.posfx[t] = un;  // the fixed-point copy does not change with the wrap
+            }
+            energy += ded;
+            accepted++;
+        }
+        __syncwarp();
+        left--;
+    }
+    if (lane == 0) {
+        mc[s].rng = rng;
+        mc[s].moves_left = left;
+        mc[s].energy = energy;
+        mc[s].accepted = accepted;
+        mc[s].attempted = attempted;
+        mc[s].need_rebuild = rebuild ? 1 : 0;
+    }
+}
+
 void launch_mc_chains(const Batch& b, McState* mc, bool fp64, cudaStream_t st) {
     int warps_per_block = 4;
     int grid = (b.nsys + warps_per_block - 1) / warps_per_block;
     if (fp64) mc_chain_kernel<true><<<grid, 32 * warps_per_block, 0, st>>>(b, mc);
-    else mc_chain_kernel<false><<<grid, 32 * warps_per_block, 0, st>>>(b, mc);
+    else mc_chain_mixed_kernel<<<grid, 32 * warps_per_block, 0, st>>>(b, mc);
 }
 
 }  // namespace lg
