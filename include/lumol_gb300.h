@@ -47,7 +47,11 @@ enum {
     LG_PAIR_NULL = 1,       /* NullPotential (functions.rs:29-50) */
     LG_PAIR_LJ = 2,         /* LennardJones {sigma, epsilon} (functions.rs:71-107) */
     LG_PAIR_BUCKINGHAM = 3, /* Buckingham {a, c, rho} (functions.rs:276-319) */
-    LG_PAIR_HARMONIC = 4    /* Harmonic {k, x0} (functions.rs:127-160) */
+    LG_PAIR_HARMONIC = 4,   /* Harmonic {k, x0} (functions.rs:127-160) */
+    LG_PAIR_BMH = 5,        /* BornMayerHuggins {a, c, d, sigma, rho} (functions.rs:321-386) */
+    LG_PAIR_MORSE = 6,      /* Morse {a, x0, depth} (functions.rs:388-437) */
+    LG_PAIR_GAUSSIAN = 7,   /* Gaussian {a, b}, b > 0 (functions.rs:439-494) */
+    LG_PAIR_MIE = 8         /* Mie {sigma, epsilon, n, m}, m < n (functions.rs:496-592) */
 };
 
 /* PairRestriction (lumol-core/src/energy/restrictions.rs:13-33). */
@@ -93,9 +97,11 @@ typedef struct {
     int32_t shifted;      /* 1: PairInteraction::shifted (energy shifted, force not) */
     int32_t restriction;  /* LG_RESTRICT_* */
     int32_t tail;         /* 1: enable_tail_corrections */
-    double p0, p1, p2;    /* LJ: sigma, epsilon; Buckingham: a, c, rho; Harmonic: k, x0 */
+    double p0, p1, p2;    /* LJ: sigma, epsilon; Buckingham: a, c, rho; Harmonic: k, x0;
+                             Morse: a, x0, depth; Gaussian: a, b; BMH and Mie: see p3, p4 */
     double cutoff;
     double scale14;       /* factor of LG_RESTRICT_SCALE14 */
+    double p3, p4;        /* BMH: {a, c, d, sigma, rho} = p0..p4; Mie: {sigma, epsilon, n, m} = p0..p3 */
 } lg_pair;
 
 /* A bond or angle potential (Harmonic or Null). */

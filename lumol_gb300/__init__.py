@@ -10,13 +10,17 @@ from . import units
 from ._capi import EngineError
 from .system import (
     BerendsenThermostat,
+    BornMayerHuggins,
     Buckingham,
     Engine,
     Ewald,
+    Gaussian,
     Harmonic,
     LennardJones,
+    Mie,
     MolecularDynamics,
     MonteCarlo,
+    Morse,
     NullPotential,
     PairInteraction,
     PairRestriction,

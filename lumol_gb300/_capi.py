@@ -20,6 +20,7 @@ LG_ERR_NONFINITE = 5
 LG_ERR_NO_DEVICE = 6
 
 LG_PAIR_ABSENT, LG_PAIR_NULL, LG_PAIR_LJ, LG_PAIR_BUCKINGHAM, LG_PAIR_HARMONIC = range(5)
+LG_PAIR_BMH, LG_PAIR_MORSE, LG_PAIR_GAUSSIAN, LG_PAIR_MIE = range(5, 9)
 LG_COULOMB_NONE, LG_COULOMB_EWALD, LG_COULOMB_WOLF = range(3)
 LG_PRECISION_FP64, LG_PRECISION_MIXED = 0, 1
 LG_OPT_NO_PERSISTENT = 1
@@ -51,6 +52,8 @@ class LgPair(ctypes.Structure):
         ("p2", ctypes.c_double),
         ("cutoff", ctypes.c_double),
         ("scale14", ctypes.c_double),
+        ("p3", ctypes.c_double),
+        ("p4", ctypes.c_double),
     ]
 
 

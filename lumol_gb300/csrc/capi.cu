@@ -33,7 +33,7 @@ constexpr int MIN_KCHUNK = 8;
 // Tuned launch parameters per workload shape: (device, precision, atoms,
 // list capacity, k-vectors) -> (threads per atom, k-vectors per field chunk).
 std::mutex g_tune_mutex;
-std::map<std::tuple<int, int, int, int, int>, std::pair<int, int>> g_tune_cache;
+std::map<std::tuple<int, int, int, int, int, bool>, std::pair<int, int>> g_tune_cache;
 
 template <class T>
 struct DBuf {
@@ -82,7 +82,12 @@ double powi6(double x) {
     double x4 = x2 * x2;
     return x2 * x4;
 }
-// Potential::energy (functions.rs:85-88, 287-292, 135-139)
+// Mie::new's energy prefactor n / (n - m) (n / m)^(m / (n - m)) epsilon (functions.rs:540-549)
+double mie_prefactor(const lg_pair& p) {
+    double n = p.p2, mm = p.p3;
+    return n / (n - mm) * std::pow(n / mm, mm / (n - mm)) * p.p1;
+}
+// Potential::energy (functions.rs:85-88, 287-292, 135-139, 354-359, 415-418, 475-477, 553-558)
 double pot_energy(const lg_pair& p, double r) {
     switch (p.type) {
         case LG_PAIR_LJ: {
@@ -98,6 +103,22 @@ double pot_energy(const lg_pair& p, double r) {
         case LG_PAIR_HARMONIC: {
             double dx = r - p.p1;
             return 0.5 * p.p0 * dx * dx;
+        }
+        case LG_PAIR_BMH: {  // functions.rs:354-359
+            double r2 = r * r;
+            double r6 = r2 * r2 * r2;
+            double ex = std::exp((p.p3 - r) / p.p4);
+            return p.p0 * ex - p.p1 / r6 + p.p2 / (r6 * r2);
+        }
+        case LG_PAIR_MORSE: {  // functions.rs:415-418
+            double rc = 1.0 - std::exp((p.p1 - r) * p.p0);
+            return p.p2 * rc * rc;
+        }
+        case LG_PAIR_GAUSSIAN:  // functions.rs:475-477
+            return -p.p0 * std::exp(-p.p1 * r * r);
+        case LG_PAIR_MIE: {  // functions.rs:553-558
+            double sr = p.p0 / r;
+            return mie_prefactor(p) * (std::pow(sr, p.p2) - std::pow(sr, p.p3));
         }
         default:
             return 0.0;
@@ -119,6 +140,24 @@ double pot_tail_energy(const lg_pair& p, double rc) {
         double factor = rc2 - 2.0 * rc * p.p2 + 2.0 * p.p2 * p.p2;
         return p.p0 * p.p2 * e * factor - p.p1 / (3.0 * rc3);
     }
+    if (p.type == LG_PAIR_BMH) {  // functions.rs:370-376
+        double rc2 = rc * rc;
+        double rc3 = rc2 * rc;
+        double e = std::exp((p.p3 - rc) / p.p4);
+        double factor = rc2 - 2.0 * rc * p.p4 + 2.0 * p.p4 * p.p4;
+        return p.p0 * p.p4 * e * factor - p.p1 / (3.0 * rc3) + p.p2 / (5.0 * rc2 * rc3);
+    }
+    if (p.type == LG_PAIR_GAUSSIAN) {  // functions.rs:485-488
+        double b = p.p1;
+        return pot_energy(p, rc) * rc / (2.0 * b) -
+               p.p0 * std::sqrt(PI) * std::erfc(std::sqrt(b) * rc) / (4.0 * std::pow(b, 1.5));
+    }
+    if (p.type == LG_PAIR_MIE) {  // functions.rs:569-579
+        if (p.p3 <= 3.0) return 0.0;
+        double src = p.p0 / rc;
+        double n3 = p.p2 - 3.0, m3 = p.p3 - 3.0;
+        return mie_prefactor(p) * (p.p0 * p.p0 * p.p0) * (std::pow(src, n3) / n3 - std::pow(src, m3) / m3);
+    }
     return 0.0;
 }
 double pot_tail_virial(const lg_pair& p, double rc) {
@@ -135,6 +174,25 @@ double pot_tail_virial(const lg_pair& p, double rc) {
         double e = std::exp(-rc / p.p2);
         double factor = rc3 + 3.0 * rc2 * p.p2 + 6.0 * rc * p.p2 * p.p2 + 6.0 * p.p2 * p.p2 * p.p2;
         return p.p0 * e * factor - 20.0 * p.p1 / rc3 + 8.0;
+    }
+    if (p.type == LG_PAIR_BMH) {  // functions.rs:378-385
+        double rc2 = rc * rc;
+        double rc3 = rc2 * rc;
+        double e = std::exp((p.p3 - rc) / p.p4);
+        double factor = rc3 + 3.0 * rc2 * p.p4 + 6.0 * rc * p.p4 * p.p4 + 6.0 * p.p4 * p.p4 * p.p4;
+        return p.p0 * e * factor - 20.0 * p.p1 / rc3 + 8.0 * p.p2 / (5.0 * rc2 * rc3);
+    }
+    if (p.type == LG_PAIR_GAUSSIAN) {  // functions.rs:490-493
+        double b = p.p1;
+        return 3.0 * std::sqrt(PI) * p.p0 * std::erfc(std::sqrt(b) * rc) / (4.0 * std::pow(b, 1.5)) -
+               pot_energy(p, rc) * rc * (2.0 * b * rc * rc + 3.0) / (2.0 * b);
+    }
+    if (p.type == LG_PAIR_MIE) {  // functions.rs:581-591
+        if (p.p3 <= 3.0) return 0.0;
+        double src = p.p0 / rc;
+        double n3 = p.p2 - 3.0, m3 = p.p3 - 3.0;
+        return mie_prefactor(p) * (p.p0 * p.p0 * p.p0) *
+               (std::pow(src, n3) * p.p2 / n3 - std::pow(src, m3) * p.p3 / m3);
     }
     return 0.0;
 }
@@ -434,6 +492,9 @@ int commit(lg_engine* e) {
             q.p0 = p.p0;
             q.p1 = p.p1;
             q.p2 = p.p2;
+            q.p3 = p.p3;
+            q.p4 = p.p4;
+            if (p.type == LG_PAIR_MIE) q.aux = mie_prefactor(p);
             q.cutoff = p.cutoff;
             q.shift = p.shifted ? pot_energy(p, p.cutoff) : 0.0;  // pairs.rs:86-95
             q.scale14 = p.scale14;
@@ -460,6 +521,24 @@ int commit(lg_engine* e) {
             } else if (p.type == LG_PAIR_HARMONIC) {
                 qf.a = (float)p.p0;
                 qf.b = (float)p.p1;
+            } else if (p.type == LG_PAIR_BMH) {  // a exp((sigma - r) / rho) - c / r^6 + d / r^8
+                qf.a = (float)p.p0;
+                qf.b = (float)p.p1;
+                qf.c = (float)(1.0 / p.p4);
+                qf.d = (float)p.p2;
+                qf.e = (float)p.p3;
+            } else if (p.type == LG_PAIR_MORSE) {  // depth (1 - exp(a (x0 - r)))^2
+                qf.a = (float)p.p2;
+                qf.b = (float)p.p0;
+                qf.c = (float)p.p1;
+            } else if (p.type == LG_PAIR_GAUSSIAN) {  // -a exp(-b r^2)
+                qf.a = (float)p.p0;
+                qf.b = (float)p.p1;
+            } else if (p.type == LG_PAIR_MIE) {  // prefactor ((sigma / r)^n - (sigma / r)^m)
+                qf.a = (float)mie_prefactor(p);
+                qf.b = (float)p.p0;
+                qf.c = (float)p.p2;
+                qf.d = (float)p.p3;
             }
             qf.rc2 = (float)(p.cutoff * p.cutoff);
             qf.shift = (float)q.shift;
@@ -610,7 +689,7 @@ int commit(lg_engine* e) {
     CUDA_TRY(e, e->red.alloc((size_t)n * RED_STRIDE));
     CUDA_TRY(e, e->host_const.alloc((size_t)nsys * RED_STRIDE));
     CUDA_TRY(e, e->tiles.alloc(std::max<size_t>(h_tiles.size(), 1)));
-    CUDA_TRY(e, e->kepart.alloc(std::max<size_t>(h_tiles.size(), 1)));
+    CUDA_TRY(e, e->kepart.alloc(std::max<size_t>(n, 1)));  // chunk kinetic energies: at most one per atom
     CUDA_TRY(e, e->cp_pos.alloc(n));
     CUDA_TRY(e, e->cp_vel.alloc(n));
     CUDA_TRY(e, e->cp_acc.alloc(n));
@@ -714,7 +793,7 @@ int commit(lg_engine* e) {
     if (!h_tiles.empty())
         CUDA_TRY(e, cudaMemcpyAsync(e->tiles.p, h_tiles.data(), h_tiles.size() * sizeof(int2), cudaMemcpyHostToDevice,
                                     st));
-    CUDA_TRY(e, cudaMemsetAsync(e->kepart.p, 0, std::max<size_t>(h_tiles.size(), 1) * sizeof(double), st));
+    CUDA_TRY(e, cudaMemsetAsync(e->kepart.p, 0, std::max<size_t>(n, 1) * sizeof(double), st));
     CUDA_TRY(e, cudaMemcpyAsync(e->ptab.p, h_ptab.data(), h_ptab.size() * sizeof(PairDev), cudaMemcpyHostToDevice, st));
     CUDA_TRY(e, cudaMemcpyAsync(e->ptabf.p, h_ptabf.data(), h_ptabf.size() * sizeof(PairDevF), cudaMemcpyHostToDevice,
                                 st));
@@ -1073,10 +1152,17 @@ int lg_set_pairs(lg_engine* e, int32_t s, int32_t nk, const lg_pair* table) {
             const lg_pair& p = table[a * nk + c];
             const lg_pair& q = table[c * nk + a];
             if (p.type != q.type || p.cutoff != q.cutoff || p.p0 != q.p0 || p.p1 != q.p1 || p.p2 != q.p2 ||
-                p.restriction != q.restriction || p.shifted != q.shifted || p.tail != q.tail)
+                p.p3 != q.p3 || p.p4 != q.p4 || p.restriction != q.restriction || p.shifted != q.shifted ||
+                p.tail != q.tail)
                 return fail(e, LG_ERR_ARGUMENT, "the pair table must be symmetric");
-            if (p.type < LG_PAIR_ABSENT || p.type > LG_PAIR_HARMONIC)
+            if (p.type < LG_PAIR_ABSENT || p.type > LG_PAIR_MIE)
                 return fail(e, LG_ERR_ARGUMENT, "unknown pair potential");
+            // the reference's constructors panic on these (functions.rs:468-469, 540-541)
+            if (p.type == LG_PAIR_GAUSSIAN && !(p.p1 > 0.0))
+                return fail(e, LG_ERR_ARGUMENT, "\"b\" has to be positive in Gaussian potential");
+            if (p.type == LG_PAIR_MIE && !(p.p3 < p.p2))
+                return fail(e, LG_ERR_ARGUMENT,
+                            "The repulsive exponent n has to be larger than the attractive exponent m");
             if (p.type != LG_PAIR_ABSENT && !(p.cutoff >= 0.0))
                 return fail(e, LG_ERR_ARGUMENT, "invalid pair cutoff");
         }
@@ -1297,7 +1383,10 @@ int lg_md_get_state(lg_engine* e, int32_t s, double* positions, double* velociti
 
 namespace {
 
-// The autotuner: times the pair kernel at every threads-per-atom width and the
+bool persist_batch(const lg_engine* e);
+
+// The autotuner: times the pair kernel at every threads-per-atom width (2, 4
+// and 8 for a batch the persistent kernel runs) and the
 // Ewald field kernel at several chunk lengths on the current batch and list,
 // keeps the fastest, and caches the choice for this workload shape.
 int autotune(lg_engine* e) {
@@ -1307,7 +1396,7 @@ int autotune(lg_engine* e) {
         return LG_OK;
     }
     Batch& b = e->b;
-    auto key = std::make_tuple(e->opt.device, b.precision, b.n, b.maxnb, b.nkvec);
+    auto key = std::make_tuple(e->opt.device, b.precision, b.n, b.maxnb, b.nkvec, persist_batch(e));
     {
         std::lock_guard<std::mutex> lock(g_tune_mutex);
         auto it = g_tune_cache.find(key);
@@ -1341,10 +1430,15 @@ int autotune(lg_engine* e) {
         }
         return best;
     };
-    const int tpas[6] = {1, 2, 4, 8, 16, 32};
+    // (a batch for the persistent kernel: the group sizes it runs)
+    const int tpas_all[6] = {1, 2, 4, 8, 16, 32}, tpas_persist[3] = {2, 4, 8};
+    const bool pb = std::get<5>(key);
+    const int* tpas = pb ? tpas_persist : tpas_all;
+    const int ntpas = pb ? 3 : 6;
     int best_tpa = b.tpa;
     float best_t = 1e30f;
-    for (int t : tpas) {
+    for (int k = 0; k < ntpas; k++) {
+        int t = tpas[k];
         b.tpa = t;
         float ms = time_it([&] { launch_pair_forces(b, LG_TERM_ALL, false, st); });
         if (ms < best_t) {
@@ -1395,10 +1489,17 @@ void enqueue_md_step(lg_engine* e, bool thermo, bool apply_previous, cudaStream_
 }
 
 // ---- persistent batched MD -------------------------------------------------------
-bool persist_eligible(const lg_engine* e) {
+// A batch the persistent kernel can run: mixed precision, pair potentials
+// only.  It also needs a group size of 2, 4 or 8 threads per atom (the
+// per-step kernel's, so both paths sum every force in the same order).
+bool persist_batch(const lg_engine* e) {
     const Batch& b = e->b;
     return !(e->opt.flags & LG_OPT_NO_PERSISTENT) && b.precision == LG_PRECISION_MIXED && !b.pair_general &&
            !b.bt_off && b.nkvec == 0 && b.n > 0;
+}
+bool persist_eligible(const lg_engine* e) {
+    int t = e->b.tpa;
+    return persist_batch(e) && (t == 2 || t == 4 || t == 8);
 }
 
 // Packs the systems into groups of about equal work (atoms times the expected

@@ -26,6 +26,8 @@ struct PairDev {
     float cutoff2_f;      // mixed path: cutoff^2 in FP32
     float pad_f;
     double c12, c6;       // LJ: 4 eps sigma^12, 4 eps sigma^6 (plain path, interior pairs)
+    double p3, p4;        // BMH: sigma, rho; Mie: m
+    double aux;           // Mie: energy prefactor
 };
 
 // FP32 pair table entry of the mixed path.
@@ -33,7 +35,7 @@ struct PairDev {
 //   Harmonic: a = k, b = x0.  shift: energy shift of a shifted interaction.
 struct alignas(16) PairDevF {
     int32_t type, restriction, pad0, pad1;
-    float a, b, c, rc2, shift, scale14, pad2, pad3;
+    float a, b, c, rc2, shift, scale14, d, e;  // d, e: BMH d and sigma; Mie m
 };
 
 // FP32 k-vector of the mixed Ewald field kernel.
@@ -75,6 +77,36 @@ struct SysDev {
     float rebuild2_f;             // 0.99 (skin / 2)^2: FP32 displacement threshold (errs towards rebuilding)
     float coul_rc2_f;
 };
+
+// Kinetic energy of one system from its chunk sums ke[begin + q] (chunk q:
+// atoms begin + q * gpw ..., each chunk summed by a warp butterfly): a
+// lane-strided sum over the chunks, then a butterfly over the 32 lanes, so
+// every lane gets the same value.  The per-step integrator and the persistent
+// kernel both sum this way (L1 bypassed: the chunks may come from other SMs
+// of the same launch).
+__device__ __forceinline__ double chunk_ke_sum(const SysDev& s, const double* ke, int gpw, int lane) {
+    int nq = (s.end - s.begin + gpw - 1) / gpw;
+    double k = 0.0;
+    for (int q = lane; q < nq; q += 32) k += __ldcg(&ke[s.begin + q]);
+    for (int o = 16; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
+    return k;
+}
+
+// Berendsen factor sqrt(1 + (T0 / T - 1) / tau) (md/thermostats.rs:113-120),
+// T = 2 K / (dof kB) (sys/compute.rs:133-144); 1 without a thermostat.
+__device__ __forceinline__ double berendsen_factor(const SysDev& s, double k) {
+    if (!(s.thermo_tau > 0.0)) return 1.0;
+    double T = 2.0 * k / (s.dof * K_BOLTZMANN);
+    return sqrt(1.0 + (s.thermo_T / T - 1.0) / s.thermo_tau);
+}
+
+// Sum of a chunk of gpw lanes (gpw a power of two dividing 32), as a butterfly
+// inside the chunk: the same tree as a butterfly over a whole warp whose
+// lanes hold one atom's value every 32 / gpw lanes and zeros elsewhere.
+__device__ __forceinline__ double chunk_butterfly(double v, int gpw) {
+    for (int o = gpw / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
 
 // Fixed-point copy of a wrapped position for the mixed path: per axis
 // u = floor(frac(x / L) * 2^32) (UnitCell::wrap_vector, cells.rs:263-282, as a
@@ -320,6 +352,34 @@ __device__ __forceinline__ void pair_energy_force(const PairDev& p, double r, do
             double dx = r - p.p1;
             e = 0.5 * p.p0 * dx * dx;
             f = p.p0 * (p.p1 - r);
+            break;
+        }
+        case 5: {  // BornMayerHuggins (functions.rs:354-366): a, c, d = p0, p1, p2; sigma, rho = p3, p4
+            double r2 = r * r;
+            double r6 = r2 * r2 * r2;
+            double r7 = r6 * r;
+            double ex = exp((p.p3 - r) / p.p4);
+            e = p.p0 * ex - p.p1 / r6 + p.p2 / (r6 * r2);
+            f = p.p0 / p.p4 * ex - 6.0 * p.p1 / r7 + 8.0 * p.p2 / (r7 * r2);
+            break;
+        }
+        case 6: {  // Morse (functions.rs:415-423, the force as written there): a, x0, depth = p0, p1, p2
+            double ex = exp((p.p1 - r) * p.p0);
+            double rc = 1.0 - ex;
+            e = p.p2 * rc * rc;
+            f = 2.0 * p.p2 * (1.0 - ex * ex) * p.p0;
+            break;
+        }
+        case 7: {  // Gaussian (functions.rs:475-481): a, b = p0, p1
+            e = -p.p0 * exp(-p.p1 * r * r);
+            f = 2.0 * p.p1 * r * e;
+            break;
+        }
+        case 8: {  // Mie (functions.rs:553-565): sigma, n, m = p0, p2, p3; prefactor in aux
+            double sr = p.p0 / r;
+            double rep = pow(sr, p.p2), att = pow(sr, p.p3);
+            e = p.aux * (rep - att);
+            f = p.aux * (p.p2 * rep - p.p3 * att) / r;
             break;
         }
         default:

@@ -9,6 +9,7 @@
 // only interact with atoms of OTHER molecules in this cost, so every bond path
 // is BondPath::None (configuration.rs:124-129).
 #include "kernels.h"
+#include "mixed_common.cuh"
 
 namespace lg {
 
@@ -251,40 +252,16 @@ __device__ __forceinline__ double uniform01(uint64_t& state) {
     return (double)(splitmix64(state) >> 11) * (1.0 / 9007199254740992.0);
 }
 
-template <bool FP64>
-__device__ __forceinline__ double mc_pair_energy(const SysDev& s, const PairDev& p, const PairDevF& pf, double dx,
-                                                 double dy, double dz) {
-    if (FP64) {
-        double r = exact_norm(dx, dy, dz);
-        if (r >= p.cutoff) return 0.0;
-        double e, f;
-        pair_energy_force(p, r, 1.0 / r, e, f);
-        return e;
-    } else {
-        float fx = (float)dx, fy = (float)dy, fz = (float)dz;
-        float r2 = fx * fx + fy * fy + fz * fz;
-        if (!(r2 < pf.rc2)) return 0.0;
-        float ir2 = 1.0f / r2;
-        float ir6 = ir2 * ir2 * ir2;
-        if (pf.type == 2) return (double)(ir6 * (pf.a * ir6 - pf.b) - pf.shift);
-        float inv_r = rsqrtf(r2);
-        float fr;
-        float ef;
-        switch (pf.type) {
-            case 3: ef = pf.a * __expf(-r2 * inv_r * pf.c) - pf.b * ir6 - pf.shift; break;
-            case 4: {
-                float dr = r2 * inv_r - pf.b;
-                ef = 0.5f * pf.a * dr * dr - pf.shift;
-                break;
-            }
-            default: ef = 0.0f;
-        }
-        (void)fr;
-        return (double)ef;
-    }
+// PairInteraction::energy of the FP64 chains (pairs.rs:185-196): zero at and
+// beyond the cutoff, on the exact distance.
+__device__ __forceinline__ double mc_pair_energy(const PairDev& p, double dx, double dy, double dz) {
+    double r = exact_norm(dx, dy, dz);
+    if (r >= p.cutoff) return 0.0;
+    double e, f;
+    pair_energy_force(p, r, 1.0 / r, e, f);
+    return e;
 }
 
-template <bool FP64>
 __global__ void __launch_bounds__(128) mc_chain_kernel(Batch b, McState* __restrict__ mc) {
     int s = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
     int lane = threadIdx.x & 31;
@@ -321,7 +298,6 @@ __global__ void __launch_bounds__(128) mc_chain_kernel(Batch b, McState* __restr
         }
         int ki = b.kind[i];
         const PairDev* prow = b.ptab + sd.ptab + ki * sd.nk;
-        const PairDevF* prowf = b.ptabf + sd.ptab + ki * sd.nk;
         double de = 0.0;
         // a cell-sorted list (mixed engines) holds sorted positions: map back to atoms
         int row = b.perm ? b.perm[i] : i;
@@ -333,24 +309,11 @@ __global__ void __launch_bounds__(128) mc_chain_kernel(Batch b, McState* __restr
             int kj = b.kind[j];
             const PairDev& p = prow[kj];
             if (p.type == 0 || restriction_excluded(p.restriction, 0)) continue;
-            if (FP64) {
-                double ox, oy, oz, wx, wy, wz;
-                // Configuration::distance(i, j), UnitCell::distance(r_j, new_i)
-                exact_nearest_image(sd, pj.x, pj.y, pj.z, old.x, old.y, old.z, ox, oy, oz);
-                exact_nearest_image(sd, nx, ny, nz, pj.x, pj.y, pj.z, wx, wy, wz);
-                de += mc_pair_energy<true>(sd, p, prowf[kj], wx, wy, wz) -
-                      mc_pair_energy<true>(sd, p, prowf[kj], ox, oy, oz);
-            } else {
-                // FP32 minimum image of FP64 differences
-                float o3[3] = {(float)(old.x - pj.x), (float)(old.y - pj.y), (float)(old.z - pj.z)};
-                float w3[3] = {(float)(nx - pj.x), (float)(ny - pj.y), (float)(nz - pj.z)};
-                for (int d = 0; d < 3; d++) {
-                    o3[d] -= sd.Lf[d] * rintf(o3[d] * sd.invLf[d]);
-                    w3[d] -= sd.Lf[d] * rintf(w3[d] * sd.invLf[d]);
-                }
-                de += mc_pair_energy<false>(sd, p, prowf[kj], w3[0], w3[1], w3[2]) -
-                      mc_pair_energy<false>(sd, p, prowf[kj], o3[0], o3[1], o3[2]);
-            }
+            double ox, oy, oz, wx, wy, wz;
+            // Configuration::distance(i, j), UnitCell::distance(r_j, new_i)
+            exact_nearest_image(sd, pj.x, pj.y, pj.z, old.x, old.y, old.z, ox, oy, oz);
+            exact_nearest_image(sd, nx, ny, nz, pj.x, pj.y, pj.z, wx, wy, wz);
+            de += mc_pair_energy(p, wx, wy, wz) - mc_pair_energy(p, ox, oy, oz);
         }
         for (int o = 16; o > 0; o >>= 1) de += __shfl_xor_sync(0xffffffffu, de, o);
         attempted++;
@@ -380,22 +343,15 @@ __global__ void __launch_bounds__(128) mc_chain_kernel(Batch b, McState* __restr
 }
 
 // Pair energy in FP32 from r^2 (the mixed path's parameters, shift included).
-__device__ __forceinline__ float mc_pair_energy_r2(int type, float4 pq, float shift, float r2) {
+__device__ __forceinline__ float mc_pair_energy_r2(const PairDevF* pp, int type, float4 pq, float shift, float r2) {
     if (!(r2 < pq.w)) return 0.0f;
-    float ir2 = 1.0f / r2;
-    float ir6 = ir2 * ir2 * ir2;
-    switch (type) {
-        case 2: return ir6 * (pq.x * ir6 - pq.y) - shift;
-        case 3: {
-            float inv_r = rsqrtf(r2);
-            return pq.x * __expf(-r2 * inv_r * pq.z) - pq.y * ir6 - shift;
-        }
-        case 4: {
-            float dr = r2 * rsqrtf(r2) - pq.y;
-            return 0.5f * pq.x * dr * dr - shift;
-        }
-        default: return 0.0f;
+    if (type == 2) {
+        float ir2 = 1.0f / r2;
+        float ir6 = ir2 * ir2 * ir2;
+        return ir6 * (pq.x * ir6 - pq.y) - shift;
     }
+    float inv_r = rsqrtf(r2), fr;
+    return pair_mixed(*pp, r2, inv_r * inv_r, inv_r, fr);
 }
 
 // Chains of a mixed-precision engine: the same moves and draws as the FP64
@@ -463,8 +419,9 @@ __global__ void __launch_bounds__(128) mc_chain_mixed_kernel(Batch b, McState* _
                 shift = pp->shift;
             }
             if (type == 0 || restriction_excluded(restr, 0)) continue;
-            de += mc_pair_energy_r2(type, pq, shift, fixed_dist2(un, pj, sd.Lq)) -
-                  mc_pair_energy_r2(type, pq, shift, fixed_dist2(uo, pj, sd.Lq));
+            const PairDevF* pp = single ? ptab : prow + b.km[js].x;
+            de += mc_pair_energy_r2(pp, type, pq, shift, fixed_dist2(un, pj, sd.Lq)) -
+                  mc_pair_energy_r2(pp, type, pq, shift, fixed_dist2(uo, pj, sd.Lq));
         }
         double ded = (double)de;
         for (int o = 16; o > 0; o >>= 1) ded += __shfl_xor_sync(0xffffffffu, ded, o);
@@ -498,7 +455,7 @@ __global__ void __launch_bounds__(128) mc_chain_mixed_kernel(Batch b, McState* _
 void launch_mc_chains(const Batch& b, McState* mc, bool fp64, cudaStream_t st) {
     int warps_per_block = 4;
     int grid = (b.nsys + warps_per_block - 1) / warps_per_block;
-    if (fp64) mc_chain_kernel<true><<<grid, 32 * warps_per_block, 0, st>>>(b, mc);
+    if (fp64) mc_chain_kernel<<<grid, 32 * warps_per_block, 0, st>>>(b, mc);
     else mc_chain_mixed_kernel<<<grid, 32 * warps_per_block, 0, st>>>(b, mc);
 }
 

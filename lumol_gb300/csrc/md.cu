@@ -85,16 +85,16 @@ __device__ __forceinline__ void flag_rebuild(bool moved, int si, uint32_t* statu
     }
 }
 
-// Berendsen factor sqrt(1 + (T0 / T - 1) / tau) of one system
-// (md/thermostats.rs:113-120), T = 2 K / (dof kB) (compute.rs:133-144) from the
-// tile kinetic energies of the last vv_second, summed in tile order, so every
-// block of the system computes the same factor.
-__device__ __forceinline__ double berendsen_lambda(const SysDev& s, const double* __restrict__ kepart) {
-    if (!(s.thermo_tau > 0.0)) return 1.0;
-    double k = 0.0;
-    for (int t = s.tile_begin; t < s.tile_end; t++) k += kepart[t];
-    double T = 2.0 * k / (s.dof * K_BOLTZMANN);
-    return sqrt(1.0 + (s.thermo_T / T - 1.0) / s.thermo_tau);
+// The Berendsen factor of a tile's system, computed by its first warp from the
+// chunk kinetic energies of the last vv_second (the same sums in every block
+// of the system, and the same as the persistent kernel's).
+__device__ __forceinline__ void tile_lambda(const SysDev& s, const double* __restrict__ ke, int gpw,
+                                            double* s_lambda) {
+    if (threadIdx.x < 32) {
+        double f = berendsen_factor(s, chunk_ke_sum(s, ke, gpw, threadIdx.x));
+        if (threadIdx.x == 0) *s_lambda = f;
+    }
+    __syncthreads();
 }
 
 // The Berendsen scaling of step k is applied at the start of step k + 1 (the
@@ -115,15 +115,12 @@ template <bool MIXED>
 __global__ void __launch_bounds__(VV_TILE) vv_first_kernel(
     const int2* __restrict__ tiles, const SysDev* __restrict__ sys, double4_32a* __restrict__ posq,
     double4_32a* __restrict__ vel, const double4_32a* __restrict__ acc, const double4_32a* __restrict__ pos_build,
-    const uint4* __restrict__ pfx_build, const double* __restrict__ kepart, int apply_thermostat,
+    const uint4* __restrict__ pfx_build, const double* __restrict__ kepart, int gpw, int apply_thermostat,
     const int* __restrict__ perm, uint4* __restrict__ posfx, uint32_t* status, uint32_t* sys_rebuild) {
     int2 tile = tiles[blockIdx.x];
     const SysDev& s = sys[tile.x];
     __shared__ double s_lambda;
-    if (apply_thermostat) {
-        if (threadIdx.x == 0) s_lambda = berendsen_lambda(s, kepart);
-        __syncthreads();
-    }
+    if (apply_thermostat) tile_lambda(s, kepart, gpw, &s_lambda);
     int i = tile.y + threadIdx.x;
     if (i >= s.end) return;
     double hdt = s.hdt, dt = s.dt;
@@ -170,7 +167,9 @@ __global__ void __launch_bounds__(VV_TILE) vv_first_kernel(
 }
 
 // a = F / m; v += 0.5 dt a (integrators.rs:55-68); with a thermostat, the
-// kinetic energy of the tile (fixed-order tree sum) for the next step's factor.
+// kinetic energies of the system's chunks of gpw atoms for the next step's
+// factor (tiles start at their system's first atom in steps of VV_TILE, so a
+// warp holds 32 / gpw whole chunks).
 // Plain path: the reference's division and unfused products; mixed path:
 // a = F * (1 / m) in FP32 (the force is an FP32 value) and fused multiply-adds
 // on the FP64 velocity.
@@ -178,7 +177,7 @@ template <bool MIXED>
 __global__ void __launch_bounds__(VV_TILE) vv_second_kernel(
     const int2* __restrict__ tiles, const SysDev* __restrict__ sys, const double* __restrict__ force,
     const float* __restrict__ inv_mass, double4_32a* __restrict__ vel, double4_32a* __restrict__ acc,
-    double* __restrict__ kepart, int thermostat) {
+    double* __restrict__ kepart, int gpw, int thermostat) {
     int2 tile = tiles[blockIdx.x];
     const SysDev& s = sys[tile.x];
     int i = tile.y + threadIdx.x;
@@ -190,8 +189,9 @@ __global__ void __launch_bounds__(VV_TILE) vv_second_kernel(
         double4_32a a;
         if (MIXED) {  // the force is an FP32 value (the compensated sum, rounded once): a = F / m in FP32
             float im = inv_mass[i];
-            a = make_double4_32a((double)((float)force[3 * i] * im), (double)((float)force[3 * i + 1] * im),
-                                 (double)((float)force[3 * i + 2] * im), 0.0);
+            a = make_double4_32a((double)__fmul_rn((float)force[3 * i], im),
+                                 (double)__fmul_rn((float)force[3 * i + 1], im),
+                                 (double)__fmul_rn((float)force[3 * i + 2], im), 0.0);
             v.x = fma(hdt, a.x, v.x);
             v.y = fma(hdt, a.y, v.y);
             v.z = fma(hdt, a.z, v.z);
@@ -207,27 +207,20 @@ __global__ void __launch_bounds__(VV_TILE) vv_second_kernel(
         vel[i] = v;
     }
     if (thermostat) {
-        __shared__ double sh[VV_TILE];
-        sh[threadIdx.x] = ke;
-        __syncthreads();
-        for (int o = VV_TILE / 2; o > 0; o >>= 1) {
-            if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
-            __syncthreads();
-        }
-        if (threadIdx.x == 0) kepart[blockIdx.x] = sh[0];
+        ke = chunk_butterfly(ke, gpw);
+        if (threadIdx.x % gpw == 0 && i < s.end) kepart[s.begin + (i - s.begin) / gpw] = ke;
     }
 }
 
 // The pending Berendsen scaling at the end of a run.
 __global__ void __launch_bounds__(VV_TILE) thermostat_finalize_kernel(const int2* __restrict__ tiles,
                                                                      const SysDev* __restrict__ sys,
-                                                                     const double* __restrict__ kepart,
+                                                                     const double* __restrict__ kepart, int gpw,
                                                                      double4_32a* __restrict__ vel) {
     int2 tile = tiles[blockIdx.x];
     const SysDev& s = sys[tile.x];
     __shared__ double s_lambda;
-    if (threadIdx.x == 0) s_lambda = berendsen_lambda(s, kepart);
-    __syncthreads();
+    tile_lambda(s, kepart, gpw, &s_lambda);
     int i = tile.y + threadIdx.x;
     if (i >= s.end) return;
     double f = s_lambda;
@@ -271,11 +264,13 @@ void launch_vv_first(const Batch& b, bool apply_thermostat, cudaStream_t st) {
     int th = apply_thermostat ? 1 : 0;
     if (b.precision == 1)
         vv_first_kernel<true><<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.posq, b.vel, b.acc, b.pos_build,
-                                                            b.pfx_build, b.kepart, th, b.perm, b.posfx, b.status,
+                                                            b.pfx_build, b.kepart, 32 / b.tpa, th, b.perm, b.posfx,
+                                                            b.status,
                                                             b.sys_rebuild);
     else
         vv_first_kernel<false><<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.posq, b.vel, b.acc, b.pos_build,
-                                                             nullptr, b.kepart, th, nullptr, b.posfx, b.status,
+                                                             nullptr, b.kepart, 32 / b.tpa, th, nullptr, b.posfx,
+                                                             b.status,
                                                              b.sys_rebuild);
 }
 void launch_vv_second(const Batch& b, bool thermostat, cudaStream_t st) {
@@ -283,13 +278,14 @@ void launch_vv_second(const Batch& b, bool thermostat, cudaStream_t st) {
     int th = thermostat ? 1 : 0;
     if (b.precision == 1)
         vv_second_kernel<true><<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.force, b.inv_mass, b.vel, b.acc,
-                                                             b.kepart, th);
+                                                             b.kepart, 32 / b.tpa, th);
     else
         vv_second_kernel<false><<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.force, nullptr, b.vel, b.acc,
-                                                              b.kepart, th);
+                                                              b.kepart, 32 / b.tpa, th);
 }
 void launch_thermostat_finalize(const Batch& b, cudaStream_t st) {
-    if (b.ntiles) thermostat_finalize_kernel<<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.kepart, b.vel);
+    if (b.ntiles) thermostat_finalize_kernel<<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.kepart, 32 / b.tpa,
+                                                                          b.vel);
 }
 void launch_request_rebuild(const Batch& b, cudaStream_t st) {
     request_rebuild_kernel<<<1, 256, 0, st>>>(b.nsys, b.status, b.sys_rebuild);

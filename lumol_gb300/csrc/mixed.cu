@@ -28,7 +28,7 @@
 namespace lg {
 
 template <int TPA, bool EV, bool GENERAL>
-__global__ void __launch_bounds__(256) pair_mixed_kernel(
+__global__ void __launch_bounds__(256, GENERAL && !EV ? 4 : 1) pair_mixed_kernel(
     int n, const uint4* __restrict__ pfx, const int2* __restrict__ km, const int* __restrict__ order,
     const int* __restrict__ sysid, const SysDev* __restrict__ sys,
     const PairDevF* __restrict__ ptab, const int* __restrict__ nbr, const int* __restrict__ nnb, int maxnb,
@@ -57,41 +57,20 @@ __global__ void __launch_bounds__(256) pair_mixed_kernel(
     const float4 pq1 = __ldg(reinterpret_cast<const float4*>(prow) + 1);
     int cnt = active ? nnb[tt] : 0;
     const int* list = nbr + (size_t)tt * maxnb;
-    // two adjacent entries per lane per iteration, read as one 8-byte load (a
-    // group of TPA lanes reads 8 * TPA contiguous bytes); both gathers are in
-    // flight together
-    for (int base = 0; base < cnt; base += 2 * TPA) {
-        int k = base + 2 * sub;
-        if (k + 1 < cnt) {
-            int2 js = *reinterpret_cast<const int2*>(list + k);
-            uint4 pj0 = pfx[js.x], pj1 = pfx[js.y];
-            // (kind, molecule) of the neighbour: not needed for one kind without restrictions
-            const bool need_km = GENERAL || !single;
-            int2 km0 = need_km ? km[js.x] : make_int2(0, 0), km1 = need_km ? km[js.y] : make_int2(0, 0);
-            mixed_entry<EV, GENERAL>(A, s, prow, pi, qi, kmi.y, i, tt, js.x, pj0, km0, order, spec_off, spec_j,
+    // (kind, molecule) of a neighbour: not needed for one kind without restrictions
+    const bool need_km = GENERAL || !single;
+    walk_row<TPA>(
+        list, cnt, sub,
+        [&](int js, uint4& pj, int2& kmj) {
+            pj = pfx[js];
+            kmj = need_km ? km[js] : make_int2(0, 0);
+        },
+        [&](int js, const uint4& pj, const int2& kmj) {
+            mixed_entry<EV, GENERAL>(A, s, prow, pi, qi, kmi.y, i, tt, js, pj, kmj, order, spec_off, spec_j,
                                      spec_path, pairs, coul, coul_rc2, alpha, pref, single, ph1, pq1);
-            mixed_entry<EV, GENERAL>(A, s, prow, pi, qi, kmi.y, i, tt, js.y, pj1, km1, order, spec_off, spec_j,
-                                     spec_path, pairs, coul, coul_rc2, alpha, pref, single, ph1, pq1);
-        } else if (k < cnt) {
-            int js = list[k];
-            int2 kmj = (GENERAL || !single) ? km[js] : make_int2(0, 0);
-            mixed_entry<EV, GENERAL>(A, s, prow, pi, qi, kmi.y, i, tt, js, pfx[js], kmj, order, spec_off, spec_j,
-                                     spec_path, pairs, coul, coul_rc2, alpha, pref, single, ph1, pq1);
-        }
-    }
-    // combine the group's compensated sums (FP32 shuffles); one lane converts to FP64
-#pragma unroll
-    for (int o = TPA / 2; o > 0; o >>= 1) {
-        float sx = __shfl_xor_sync(0xffffffffu, A.fxs, o), cx = __shfl_xor_sync(0xffffffffu, A.fxc, o);
-        float sy = __shfl_xor_sync(0xffffffffu, A.fys, o), cy = __shfl_xor_sync(0xffffffffu, A.fyc, o);
-        float sz = __shfl_xor_sync(0xffffffffu, A.fzs, o), cz = __shfl_xor_sync(0xffffffffu, A.fzc, o);
-        two_sum_acc(A.fxs, A.fxc, sx);
-        A.fxc += cx;
-        two_sum_acc(A.fys, A.fyc, sy);
-        A.fyc += cy;
-        two_sum_acc(A.fzs, A.fzc, sz);
-        A.fzc += cz;
-    }
+        });
+    // combine the group's compensated sums; one lane converts to FP64
+    group_combine<TPA>(A);
     if (EV) {
         A.ep = group_sum_d<TPA>(A.ep);
         A.ec = group_sum_d<TPA>(A.ec);
@@ -105,9 +84,9 @@ __global__ void __launch_bounds__(256) pair_mixed_kernel(
     if (active && sub == 0) {  // the first force kernel of a step: assigns
         // the compensated sum rounded once to FP32 (one rounding error of the
         // result instead of one per term)
-        force[3 * i] = (double)(A.fxs + A.fxc);
-        force[3 * i + 1] = (double)(A.fys + A.fyc);
-        force[3 * i + 2] = (double)(A.fzs + A.fzc);
+        force[3 * i] = (double)radd(A.fxs, A.fxc);
+        force[3 * i + 1] = (double)radd(A.fys, A.fyc);
+        force[3 * i + 2] = (double)radd(A.fzs, A.fzc);
         if (EV) {
             double ec = A.ec;
             if (GENERAL && (terms & 16u) && s.coul == 2 && qi != 0.0f) {

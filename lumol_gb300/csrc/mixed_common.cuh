@@ -6,12 +6,23 @@
 
 namespace lg {
 
+// FP32 arithmetic with every rounding written out: __fmul_rn / __fadd_rn /
+// __fmaf_rn are never contracted into (or split out of) a fused multiply-add
+// by the compiler, so an expression rounds the same way in every kernel it is
+// inlined into.  The per-step pair kernels, the persistent MD kernel and the
+// energy / no-energy variants therefore give each atom the same force bits.
+__device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float rfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+// Knuth's TwoSum: s + x = t + err exactly; the error joins the compensation c.
 __device__ __forceinline__ void two_sum_acc(float& s, float& c, float x) {
-    float t = s + x;
-    float bp = t - s;
-    float err = (s - (t - bp)) + (x - bp);
+    float t = radd(s, x);
+    float bp = rsub(t, s);
+    float err = radd(rsub(s, rsub(t, bp)), rsub(x, bp));
     s = t;
-    c += err;
+    c = radd(c, err);
 }
 
 template <int TPA>
@@ -23,30 +34,64 @@ __device__ __forceinline__ double group_sum_d(double v) {
 
 // Minimum image of two fixed-point coordinates: signed wrap-around difference.
 __device__ __forceinline__ float fixed_image(uint32_t ui, uint32_t uj, float scale) {
-    return (float)(int32_t)(ui - uj) * scale;
+    return rmul((float)(int32_t)(ui - uj), scale);
+}
+
+// (c12 / r^12 - c6 / r^6): force / r and energy from 1 / r^2 and 1 / r^6.
+__device__ __forceinline__ float lj_force_r(float c12, float c6, float ir6, float inv_r2) {
+    return rmul(rmul(ir6, rfma(rmul(12.0f, c12), ir6, rmul(-6.0f, c6))), inv_r2);
+}
+__device__ __forceinline__ float lj_energy(float c12, float c6, float ir6) {
+    return rmul(ir6, rfma(c12, ir6, -c6));
 }
 
 // Pair potential in FP32: returns energy, writes force / r.
 __device__ __forceinline__ float pair_mixed(const PairDevF& p, float r2, float inv_r2, float inv_r, float& fr) {
     switch (p.type) {
         case 2: {  // LJ: c12 / r^12 - c6 / r^6
-            float ir6 = inv_r2 * inv_r2 * inv_r2;
-            float e = ir6 * (p.a * ir6 - p.b);
-            fr = ir6 * (12.0f * p.a * ir6 - 6.0f * p.b) * inv_r2;
-            return e - p.shift;
+            float ir6 = rmul(rmul(inv_r2, inv_r2), inv_r2);
+            fr = lj_force_r(p.a, p.b, ir6, inv_r2);
+            return rsub(lj_energy(p.a, p.b, ir6), p.shift);
         }
         case 3: {  // Buckingham: A exp(-r / rho) - C / r^6
-            float r = r2 * inv_r;
-            float ex = p.a * __expf(-r * p.c);
-            float ir6 = inv_r2 * inv_r2 * inv_r2;
-            fr = ex * p.c * inv_r - 6.0f * p.b * ir6 * inv_r2;
-            return ex - p.b * ir6 - p.shift;
+            float r = rmul(r2, inv_r);
+            float ex = rmul(p.a, __expf(rmul(-r, p.c)));
+            float ir6 = rmul(rmul(inv_r2, inv_r2), inv_r2);
+            fr = rfma(rmul(ex, p.c), inv_r, -rmul(rmul(rmul(6.0f, p.b), ir6), inv_r2));
+            return rsub(rfma(-p.b, ir6, ex), p.shift);
         }
         case 4: {  // Harmonic k / 2 (r - x0)^2
-            float r = r2 * inv_r;
-            float dx = r - p.b;
-            fr = -p.a * dx * inv_r;
-            return 0.5f * p.a * dx * dx - p.shift;
+            float r = rmul(r2, inv_r);
+            float dx = rsub(r, p.b);
+            fr = rmul(rmul(-p.a, dx), inv_r);
+            return rsub(rmul(rmul(rmul(0.5f, p.a), dx), dx), p.shift);
+        }
+        case 5: {  // BornMayerHuggins: a exp((sigma - r) / rho) - c / r^6 + d / r^8 (c = 1 / rho, e = sigma)
+            float r = rmul(r2, inv_r);
+            float ex = rmul(p.a, __expf(rmul(rsub(p.e, r), p.c)));
+            float ir6 = rmul(rmul(inv_r2, inv_r2), inv_r2);
+            float t6 = rmul(rmul(rmul(6.0f, p.b), ir6), inv_r);
+            float t8 = rmul(rmul(rmul(rmul(8.0f, p.d), ir6), inv_r2), inv_r);
+            fr = rmul(radd(rfma(ex, p.c, -t6), t8), inv_r);
+            return rsub(radd(rfma(-p.b, ir6, ex), rmul(rmul(p.d, ir6), inv_r2)), p.shift);
+        }
+        case 6: {  // Morse: depth (1 - exp(a (x0 - r)))^2, force 2 depth (1 - exp^2) a as the reference
+            float r = rmul(r2, inv_r);
+            float ex = __expf(rmul(rsub(p.c, r), p.b));
+            float rc = rsub(1.0f, ex);
+            fr = rmul(rmul(rmul(rmul(2.0f, p.a), rfma(-ex, ex, 1.0f)), p.b), inv_r);
+            return rsub(rmul(rmul(p.a, rc), rc), p.shift);
+        }
+        case 7: {  // Gaussian: -a exp(-b r^2), force 2 b r E
+            float e = rmul(-p.a, __expf(rmul(-p.b, r2)));
+            fr = rmul(rmul(2.0f, p.b), e);
+            return rsub(e, p.shift);
+        }
+        case 8: {  // Mie: prefactor ((sigma / r)^n - (sigma / r)^m), n = c, m = d
+            float sr = rmul(p.b, inv_r);
+            float rep = powf(sr, p.c), att = powf(sr, p.d);
+            fr = rmul(rmul(p.a, rfma(p.c, rep, -rmul(p.d, att))), inv_r2);
+            return rsub(rmul(p.a, rsub(rep, att)), p.shift);
         }
         default:
             fr = 0.0f;
@@ -73,7 +118,7 @@ __device__ __forceinline__ void mixed_entry(
     float dx = fixed_image(pi.x, pj.x, s.Lq[0]);
     float dy = fixed_image(pi.y, pj.y, s.Lq[1]);
     float dz = fixed_image(pi.z, pj.z, s.Lq[2]);
-    float r2 = dx * dx + dy * dy + dz * dz;
+    float r2 = rfma(dz, dz, rfma(dy, dy, rmul(dx, dx)));
     // the parameters as two 16-byte loads: (type, restriction, -, -) and (a, b, c, rc2);
     // a system with one kind passes them in (loaded once per atom)
     const PairDevF* pp = prow + kmj.x;
@@ -90,15 +135,15 @@ __device__ __forceinline__ void mixed_entry(
     bool cin = GENERAL && coul && qj != 0.0f && r2 <= coul_rc2;
     if (!(pin || cin)) return;
     float inv_r = rsqrtf(r2);
-    float inv_r2 = inv_r * inv_r;
+    float inv_r2 = rmul(inv_r, inv_r);
     float fr = 0.0f;
     float e_pair = 0.0f, e_coul = 0.0f;
     if (!GENERAL) {
         float shift = EV ? __ldg(&pp->shift) : 0.0f;
         if (ph.x == 2) {  // LJ: c12 / r^12 - c6 / r^6
-            float ir6 = inv_r2 * inv_r2 * inv_r2;
-            fr = ir6 * (12.0f * pq.x * ir6 - 6.0f * pq.y) * inv_r2;
-            if (EV) e_pair = ir6 * (pq.x * ir6 - pq.y) - shift;
+            float ir6 = rmul(rmul(inv_r2, inv_r2), inv_r2);
+            fr = lj_force_r(pq.x, pq.y, ir6, inv_r2);
+            if (EV) e_pair = rsub(lj_energy(pq.x, pq.y, ir6), shift);
         } else {
             e_pair = pair_mixed(*pp, r2, inv_r2, inv_r, fr);
         }
@@ -114,8 +159,8 @@ __device__ __forceinline__ void mixed_entry(
         }
         if (pin) {
             float f;
-            e_pair = sc * pair_mixed(p, r2, inv_r2, inv_r, f);
-            fr = sc * f;
+            e_pair = rmul(sc, pair_mixed(p, r2, inv_r2, inv_r, f));
+            fr = rmul(sc, f);
         }
         if (cin) {
             bool excl = false;
@@ -127,41 +172,90 @@ __device__ __forceinline__ void mixed_entry(
                 excl = restriction_excluded(s.coul_restr, path);
                 if (s.coul_restr == 6 && path == 4) csc = (float)s.coul_scale14;
             }
-            float qq = pref * qj;
-            float r = r2 * inv_r;
-            float ar = alpha * r;
+            float qq = rmul(pref, qj);
+            float r = rmul(r2, inv_r);
+            float ar = rmul(alpha, r);
             if (s.coul == 1) {
-                float g = alpha * (float)FRAC_2_SQRT_PI * __expf(-ar * ar);
+                float g = rmul(rmul(alpha, (float)FRAC_2_SQRT_PI), __expf(rmul(-ar, ar)));
                 if (excl) {
                     float ef = erff(ar);
-                    e_coul = -qq * ef * inv_r;
-                    fr += qq * inv_r2 * (g - ef * inv_r);
+                    e_coul = rmul(rmul(-qq, ef), inv_r);
+                    fr = radd(fr, rmul(rmul(qq, inv_r2), rfma(-ef, inv_r, g)));
                 } else {
                     float ec_ = erfcf(ar);
-                    e_coul = qq * ec_ * inv_r;
-                    fr += qq * inv_r2 * (g + ec_ * inv_r);
+                    e_coul = rmul(rmul(qq, ec_), inv_r);
+                    fr = radd(fr, rmul(rmul(qq, inv_r2), rfma(ec_, inv_r, g)));
                 }
             } else if (!excl) {
                 float ec_ = erfcf(ar);
-                e_coul = csc * qq * (ec_ * inv_r - (float)s.wolf_ec);
-                float factor = ec_ * inv_r2 + alpha * (float)FRAC_2_SQRT_PI * __expf(-ar * ar) * inv_r;
-                fr += csc * qq * (factor - (float)s.wolf_fc) * inv_r;
+                float cq = rmul(csc, qq);
+                e_coul = rmul(cq, rfma(ec_, inv_r, -(float)s.wolf_ec));
+                float g = rmul(rmul(alpha, (float)FRAC_2_SQRT_PI), __expf(rmul(-ar, ar)));
+                float factor = rfma(ec_, inv_r2, rmul(g, inv_r));
+                fr = radd(fr, rmul(rmul(cq, rsub(factor, (float)s.wolf_fc)), inv_r));
             }
         }
     }
-    float gx = fr * dx, gy = fr * dy, gz = fr * dz;
+    float gx = rmul(fr, dx), gy = rmul(fr, dy), gz = rmul(fr, dz);
     two_sum_acc(A.fxs, A.fxc, gx);
     two_sum_acc(A.fys, A.fyc, gy);
     two_sum_acc(A.fzs, A.fzc, gz);
     if (EV && js > tt) {  // each unordered pair once (the list is symmetric)
         A.ep += (double)e_pair;
         A.ec += (double)e_coul;
-        A.w0 += (double)(gx * dx);
-        A.w1 += (double)(gx * dy);
-        A.w2 += (double)(gx * dz);
-        A.w3 += (double)(gy * dy);
-        A.w4 += (double)(gy * dz);
-        A.w5 += (double)(gz * dz);
+        A.w0 += (double)rmul(gx, dx);
+        A.w1 += (double)rmul(gx, dy);
+        A.w2 += (double)rmul(gx, dz);
+        A.w3 += (double)rmul(gy, dy);
+        A.w4 += (double)rmul(gy, dz);
+        A.w5 += (double)rmul(gz, dz);
+    }
+}
+
+// Combines the compensated force sums of a TPA-lane group (FP32 shuffles, in
+// a fixed butterfly order); every lane ends with the group's sums.
+template <int TPA>
+__device__ __forceinline__ void group_combine(MixedAcc& A) {
+#pragma unroll
+    for (int o = TPA / 2; o > 0; o >>= 1) {
+        float sx = __shfl_xor_sync(0xffffffffu, A.fxs, o), cx = __shfl_xor_sync(0xffffffffu, A.fxc, o);
+        float sy = __shfl_xor_sync(0xffffffffu, A.fys, o), cy = __shfl_xor_sync(0xffffffffu, A.fyc, o);
+        float sz = __shfl_xor_sync(0xffffffffu, A.fzs, o), cz = __shfl_xor_sync(0xffffffffu, A.fzc, o);
+        two_sum_acc(A.fxs, A.fxc, sx);
+        A.fxc = radd(A.fxc, cx);
+        two_sum_acc(A.fys, A.fyc, sy);
+        A.fyc = radd(A.fyc, cy);
+        two_sum_acc(A.fzs, A.fzc, sz);
+        A.fzc = radd(A.fzc, cz);
+    }
+}
+
+// Walks one atom's neighbour row for lane `sub` of its TPA-lane group: the
+// lane takes pairs of adjacent entries (one 8-byte load of the indices, a
+// group of lanes reading contiguous bytes), issues both gathers, then
+// evaluates the two entries in order; an odd last entry is taken alone.  The
+// per-step pair kernel and the persistent kernel both walk rows this way, so
+// their force sums run in the same order.  (Blocks of four entries measured
+// slower: the extra registers cost occupancy.)
+template <int TPA, typename Gather, typename Eval>
+__device__ __forceinline__ void walk_row(const int* __restrict__ list, int cnt, int sub, Gather gather, Eval eval) {
+    for (int base = 0; base < cnt; base += 2 * TPA) {
+        int k = base + 2 * sub;
+        if (k + 1 < cnt) {
+            int2 js = *reinterpret_cast<const int2*>(list + k);
+            uint4 p0, p1;
+            int2 m0, m1;
+            gather(js.x, p0, m0);
+            gather(js.y, p1, m1);
+            eval(js.x, p0, m0);
+            eval(js.y, p1, m1);
+        } else if (k < cnt) {
+            int j = list[k];
+            uint4 p0;
+            int2 m0;
+            gather(j, p0, m0);
+            eval(j, p0, m0);
+        }
     }
 }
 

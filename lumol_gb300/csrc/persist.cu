@@ -54,18 +54,8 @@ __device__ __forceinline__ void pk_lambdas(const Batch& b, const PkArgs& a, cons
                                            int lane, int gpw, double* s_lambda) {
     for (int r = wib; r < G; r += PK_WARPS) {
         const SysDev& sd = b.sys[s_sys[r]];
-        int nq = (sd.end - sd.begin + gpw - 1) / gpw;
-        double k = 0.0;
-        for (int q = lane; q < nq; q += 32) k += __ldcg(&a.ke[sd.begin + q]);
-        for (int o = 16; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
-        if (lane == 0) {
-            double f = 1.0;
-            if (sd.thermo_tau > 0.0) {
-                double T = 2.0 * k / (sd.dof * K_BOLTZMANN);
-                f = sqrt(1.0 + (sd.thermo_T / T - 1.0) / sd.thermo_tau);
-            }
-            s_lambda[r] = f;
-        }
+        double f = berendsen_factor(sd, chunk_ke_sum(sd, a.ke, gpw, lane));
+        if (lane == 0) s_lambda[r] = f;
     }
 }
 
@@ -371,59 +361,32 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
                 int cnt = active ? b.nnb[tt] : 0;
                 const int* list = b.nbr + (size_t)tt * b.maxnb;
                 const int off = sd.begin - s_apre[r];  // sorted position - group slot
-                // as the per-step pair kernel: two adjacent entries per lane per iteration
-                for (int base2 = 0; base2 < cnt; base2 += 2 * TPA) {
-                    int k = base2 + 2 * sub;
-                    if (k + 1 < cnt) {
-                        int2 js = *reinterpret_cast<const int2*>(list + k);
-                        uint4 pj0, pj1;
-                        int2 km0, km1;
+                // rows walked as the per-step pair kernel walks them
+                walk_row<TPA>(
+                    list, cnt, sub,
+                    [&](int js, uint4& pj, int2& kmj) {
                         if (a.stage) {
-                            pj0 = s_pos[js.x - off];
-                            pj1 = s_pos[js.y - off];
-                            km0 = make_int2(s_kind[js.x - off], 0);
-                            km1 = make_int2(s_kind[js.y - off], 0);
+                            pj = s_pos[js - off];
+                            kmj = make_int2(s_kind[js - off], 0);
                         } else {  // (the neighbour's kind is not needed for one kind)
-                            pj0 = b.posfx[js.x];
-                            pj1 = b.posfx[js.y];
-                            km0 = single ? make_int2(0, 0) : b.km[js.x];
-                            km1 = single ? make_int2(0, 0) : b.km[js.y];
+                            pj = b.posfx[js];
+                            kmj = single ? make_int2(0, 0) : b.km[js];
                         }
-                        mixed_entry<false, false>(acc, sd, prow, pi, 0.0f, kmi.y, i, tt, js.x, pj0, km0, b.cell_atoms,
-                                                  nullptr, nullptr, nullptr, true, false, 0.0f, 0.0f, 0.0f, single,
-                                                  ph1, pq1);
-                        mixed_entry<false, false>(acc, sd, prow, pi, 0.0f, kmi.y, i, tt, js.y, pj1, km1, b.cell_atoms,
-                                                  nullptr, nullptr, nullptr, true, false, 0.0f, 0.0f, 0.0f, single,
-                                                  ph1, pq1);
-                    } else if (k < cnt) {
-                        int js = list[k];
-                        uint4 pj = a.stage ? s_pos[js - off] : b.posfx[js];
-                        int2 kmj = a.stage ? make_int2(s_kind[js - off], 0) : (single ? make_int2(0, 0) : b.km[js]);
+                    },
+                    [&](int js, const uint4& pj, const int2& kmj) {
                         mixed_entry<false, false>(acc, sd, prow, pi, 0.0f, kmi.y, i, tt, js, pj, kmj, b.cell_atoms,
                                                   nullptr, nullptr, nullptr, true, false, 0.0f, 0.0f, 0.0f, single,
                                                   ph1, pq1);
-                    }
-                }
-#pragma unroll
-                for (int o = TPA / 2; o > 0; o >>= 1) {
-                    float sx = __shfl_xor_sync(0xffffffffu, acc.fxs, o), cx = __shfl_xor_sync(0xffffffffu, acc.fxc, o);
-                    float sy = __shfl_xor_sync(0xffffffffu, acc.fys, o), cy = __shfl_xor_sync(0xffffffffu, acc.fyc, o);
-                    float sz = __shfl_xor_sync(0xffffffffu, acc.fzs, o), cz = __shfl_xor_sync(0xffffffffu, acc.fzc, o);
-                    two_sum_acc(acc.fxs, acc.fxc, sx);
-                    acc.fxc += cx;
-                    two_sum_acc(acc.fys, acc.fyc, sy);
-                    acc.fyc += cy;
-                    two_sum_acc(acc.fzs, acc.fzc, sz);
-                    acc.fzc += cz;
-                }
+                    });
+                group_combine<TPA>(acc);
                 double ke = 0.0;
                 if (active && sub == 0) {
                     // as the per-step path: the compensated sum rounded once to FP32, a = F / m in FP32
                     float im = b.inv_mass[i];
                     double4_32a vel = b.vel[i];
-                    double4_32a ai = make_double4_32a((double)((acc.fxs + acc.fxc) * im),
-                                                      (double)((acc.fys + acc.fyc) * im),
-                                                      (double)((acc.fzs + acc.fzc) * im), 0.0);
+                    double4_32a ai = make_double4_32a((double)rmul(radd(acc.fxs, acc.fxc), im),
+                                                      (double)rmul(radd(acc.fys, acc.fyc), im),
+                                                      (double)rmul(radd(acc.fzs, acc.fzc), im), 0.0);
                     vel.x = fma(sd.hdt, ai.x, vel.x);
                     vel.y = fma(sd.hdt, ai.y, vel.y);
                     vel.z = fma(sd.hdt, ai.z, vel.z);
@@ -483,11 +446,11 @@ cudaError_t launch_persist_tpa(const Batch& b, const PkArgs& a, int cluster, cud
 
 cudaError_t launch_md_persist(const Batch& b, const PkArgs& a, int cluster, cudaStream_t st) {
     if (a.ngroups == 0 || a.nsteps == 0) return cudaSuccess;
-    switch (b.tpa) {
-        case 1:
+    switch (b.tpa) {  // (persistent runs need the per-step kernel's group size: 2, 4 or 8)
         case 2: return launch_persist_tpa<2>(b, a, cluster, st);
         case 4: return launch_persist_tpa<4>(b, a, cluster, st);
-        default: return launch_persist_tpa<8>(b, a, cluster, st);
+        case 8: return launch_persist_tpa<8>(b, a, cluster, st);
+        default: return cudaErrorInvalidValue;
     }
 }
 

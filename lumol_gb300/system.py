@@ -80,6 +80,62 @@ class Harmonic:
         return C.LG_PAIR_HARMONIC, (self.k, self.x0, 0.0)
 
 
+@dataclass(frozen=True)
+class BornMayerHuggins:
+    """BornMayerHuggins {a, c, d, sigma, rho}:
+    A exp((sigma - r) / rho) - C / r^6 + D / r^8 (functions.rs:321-386)."""
+    a: float
+    c: float
+    d: float
+    sigma: float
+    rho: float
+
+    def _params(self):
+        return C.LG_PAIR_BMH, (self.a, self.c, self.d, self.sigma, self.rho)
+
+
+@dataclass(frozen=True)
+class Morse:
+    """Morse {a, x0, depth}: depth (1 - exp(a (x0 - r)))^2 (functions.rs:388-437)."""
+    a: float
+    x0: float
+    depth: float
+
+    def _params(self):
+        return C.LG_PAIR_MORSE, (self.a, self.x0, self.depth)
+
+
+@dataclass(frozen=True)
+class Gaussian:
+    """Gaussian::new(a, b): -a exp(-b r^2), b > 0 (functions.rs:439-494)."""
+    a: float
+    b: float
+
+    def __post_init__(self):
+        if not self.b > 0.0:
+            raise ValueError('"b" has to be positive in Gaussian potential')
+
+    def _params(self):
+        return C.LG_PAIR_GAUSSIAN, (self.a, self.b)
+
+
+@dataclass(frozen=True)
+class Mie:
+    """Mie::new(sigma, epsilon, n, m): the LJ form with exponents n > m
+    (functions.rs:496-592)."""
+    sigma: float
+    epsilon: float
+    n: float
+    m: float
+
+    def __post_init__(self):
+        if not self.m < self.n:
+            raise ValueError("The repulsive exponent n has to be larger than the attractive exponent m")
+
+    def _params(self):
+        return C.LG_PAIR_MIE, (self.sigma, self.epsilon, self.n, self.m)
+
+
 class PairInteraction:
     """PairInteraction (lumol-core/src/energy/pairs.rs:22-296)."""
 
@@ -103,9 +159,10 @@ class PairInteraction:
         self.restriction = restriction
 
     def _lower(self) -> C.LgPair:
-        kind, (p0, p1, p2) = self.potential._params()
+        kind, params = self.potential._params()
+        p0, p1, p2, p3, p4 = (list(params) + [0.0] * 5)[:5]
         r, s14 = _restriction(self.restriction)
-        return C.LgPair(kind, int(self.shifted_energy), r, int(self.tail), p0, p1, p2, self.cutoff, s14)
+        return C.LgPair(kind, int(self.shifted_energy), r, int(self.tail), p0, p1, p2, self.cutoff, s14, p3, p4)
 
 
 class Ewald:

@@ -171,9 +171,30 @@ struct PairPot {
                 double dx = r - d.p1;
                 return 0.5 * d.p0 * dx * dx;
             }
+            case ORC_PAIR_BMH: {  // functions.rs:354-359
+                double r2 = r * r;
+                double r6 = r2 * r2 * r2;
+                double e = std::exp((d.p3 - r) / d.p4);
+                return d.p0 * e - d.p1 / r6 + d.p2 / (r6 * r2);
+            }
+            case ORC_PAIR_MORSE: {  // functions.rs:415-418
+                double rc = 1.0 - std::exp((d.p1 - r) * d.p0);
+                return d.p2 * rc * rc;
+            }
+            case ORC_PAIR_GAUSSIAN:  // functions.rs:475-477
+                return -d.p0 * std::exp(-d.p1 * r * r);
+            case ORC_PAIR_MIE: {  // functions.rs:553-558
+                double sr = d.p0 / r;
+                return mie_prefac() * (std::pow(sr, d.p2) - std::pow(sr, d.p3));
+            }
             default:
                 return 0.0;
         }
+    }
+    // Mie::new prefactor (functions.rs:540-549)
+    double mie_prefac() const {
+        double n = d.p2, mm = d.p3;
+        return n / (n - mm) * std::pow(n / mm, mm / (n - mm)) * d.p1;
     }
     // Potential::force
     double pot_force(double r) const {
@@ -190,6 +211,23 @@ struct PairPot {
             }
             case ORC_PAIR_HARMONIC:  // functions.rs:141-143
                 return d.p0 * (d.p1 - r);
+            case ORC_PAIR_BMH: {  // functions.rs:361-366
+                double r2 = r * r;
+                double r7 = r2 * r2 * r2 * r;
+                double e = std::exp((d.p3 - r) / d.p4);
+                return d.p0 / d.p4 * e - 6.0 * d.p1 / r7 + 8.0 * d.p2 / (r7 * r2);
+            }
+            case ORC_PAIR_MORSE: {  // functions.rs:420-423, as written there
+                double e = std::exp((d.p1 - r) * d.p0);
+                return 2.0 * d.p2 * (1.0 - e * e) * d.p0;
+            }
+            case ORC_PAIR_GAUSSIAN:  // functions.rs:479-481
+                return 2.0 * d.p1 * r * pot_energy(r);
+            case ORC_PAIR_MIE: {  // functions.rs:560-565
+                double sr = d.p0 / r;
+                double rep = std::pow(sr, d.p2), att = std::pow(sr, d.p3);
+                return mie_prefac() * (d.p2 * rep - d.p3 * att) / r;
+            }
             default:
                 return 0.0;
         }
@@ -209,6 +247,25 @@ struct PairPot {
                 double e = std::exp(-rc / d.p2);
                 double factor = rc2 - 2.0 * rc * d.p2 + 2.0 * d.p2 * d.p2;
                 return d.p0 * d.p2 * e * factor - d.p1 / (3.0 * rc3);
+            }
+            case ORC_PAIR_BMH: {  // functions.rs:370-376
+                double rc2 = rc * rc;
+                double rc3 = rc2 * rc;
+                double e = std::exp((d.p3 - rc) / d.p4);
+                double factor = rc2 - 2.0 * rc * d.p4 + 2.0 * d.p4 * d.p4;
+                return d.p0 * d.p4 * e * factor - d.p1 / (3.0 * rc3) + d.p2 / (5.0 * rc2 * rc3);
+            }
+            case ORC_PAIR_GAUSSIAN: {  // functions.rs:485-488
+                double b = d.p1;
+                return pot_energy(rc) * rc / (2.0 * b) -
+                       d.p0 * std::sqrt(PI) * std::erfc(std::sqrt(b) * rc) / (4.0 * std::pow(b, 3.0 / 2.0));
+            }
+            case ORC_PAIR_MIE: {  // functions.rs:569-579
+                if (d.p3 <= 3.0) return 0.0;
+                double src = d.p0 / rc;
+                double n3 = d.p2 - 3.0, m3 = d.p3 - 3.0;
+                double s3 = d.p0 * d.p0 * d.p0;  // f64::powi(sigma, 3)
+                return mie_prefac() * s3 * (std::pow(src, n3) / n3 - std::pow(src, m3) / m3);
             }
             default:
                 return 0.0;
@@ -230,6 +287,25 @@ struct PairPot {
                 double factor = rc3 + 3.0 * rc2 * d.p2 + 6.0 * rc * d.p2 * d.p2 +
                                 6.0 * d.p2 * d.p2 * d.p2;
                 return d.p0 * e * factor - 20.0 * d.p1 / rc3 + 8.0;
+            }
+            case ORC_PAIR_BMH: {  // functions.rs:378-385
+                double rc2 = rc * rc;
+                double rc3 = rc2 * rc;
+                double e = std::exp((d.p3 - rc) / d.p4);
+                double factor = rc3 + 3.0 * rc2 * d.p4 + 6.0 * rc * d.p4 * d.p4 + 6.0 * d.p4 * d.p4 * d.p4;
+                return d.p0 * e * factor - 20.0 * d.p1 / rc3 + 8.0 * d.p2 / (5.0 * rc2 * rc3);
+            }
+            case ORC_PAIR_GAUSSIAN: {  // functions.rs:490-493
+                double b = d.p1;
+                return 3.0 * std::sqrt(PI) * d.p0 * std::erfc(std::sqrt(b) * rc) / (4.0 * std::pow(b, 3.0 / 2.0)) -
+                       pot_energy(rc) * rc * (2.0 * b * rc * rc + 3.0) / (2.0 * b);
+            }
+            case ORC_PAIR_MIE: {  // functions.rs:581-591
+                if (d.p3 <= 3.0) return 0.0;
+                double src = d.p0 / rc;
+                double n3 = d.p2 - 3.0, m3 = d.p3 - 3.0;
+                double s3 = d.p0 * d.p0 * d.p0;
+                return mie_prefac() * s3 * (std::pow(src, n3) * d.p2 / n3 - std::pow(src, m3) * d.p3 / m3);
             }
             default:
                 return 0.0;

@@ -30,7 +30,11 @@ enum {
     ORC_PAIR_NULL = 1,       /* NullPotential */
     ORC_PAIR_LJ = 2,         /* LennardJones {sigma, epsilon} */
     ORC_PAIR_BUCKINGHAM = 3, /* Buckingham {a, c, rho} */
-    ORC_PAIR_HARMONIC = 4    /* Harmonic {k, x0} */
+    ORC_PAIR_HARMONIC = 4,   /* Harmonic {k, x0} */
+    ORC_PAIR_BMH = 5,        /* BornMayerHuggins {a, c, d, sigma, rho} */
+    ORC_PAIR_MORSE = 6,      /* Morse {a, x0, depth} */
+    ORC_PAIR_GAUSSIAN = 7,   /* Gaussian {a, b} */
+    ORC_PAIR_MIE = 8         /* Mie {sigma, epsilon, n, m} */
 };
 
 /* PairRestriction (lumol-core/src/energy/restrictions.rs:13-33). */
@@ -67,6 +71,9 @@ typedef struct {
     double p0, p1, p2;   /* LJ: sigma, epsilon; Buckingham: a, c, rho; Harmonic: k, x0 */
     double cutoff;
     double scale14;      /* Scale14 factor */
+    double p3, p4;       /* further parameters: BMH {a, c, d, sigma, rho} = p0..p4;
+                            Morse {a, x0, depth} = p0..p2; Gaussian {a, b} = p0, p1;
+                            Mie {sigma, epsilon, n, m} = p0..p3 */
 } orc_pair;
 
 /* Bond / angle potential (Harmonic or absent). */

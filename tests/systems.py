@@ -78,9 +78,34 @@ def nist_spce(xyz: str, cutoff: float, lammps: tuple | None = None) -> lg.System
     return s
 
 
-def random_lj_fluid(n: int, density: float, seed: int, cutoff: float, buckingham: bool = False,
+def _family_interactions(family: str, cutoff: float):
+    """Three PairInteractions of one potential family for the kinds (Ar, Ar),
+    (Ar, Kr), (Kr, Kr): plain, shifted, and with tail corrections."""
+    eps = units.from_(0.996, "kJ/mol")
+    pots = {
+        "lj": (lg.LennardJones(3.405, eps), lg.LennardJones(3.6, 1.3 * eps), lg.LennardJones(3.8, 1.6 * eps)),
+        "buckingham": (lg.Buckingham(5000.0, 40.0, 0.3), lg.Buckingham(6000.0, 50.0, 0.32),
+                       lg.Buckingham(7000.0, 60.0, 0.35)),
+        "bmh": (lg.BornMayerHuggins(0.2, 40.0, 60.0, 3.0, 0.3), lg.BornMayerHuggins(0.25, 50.0, 70.0, 3.1, 0.32),
+                lg.BornMayerHuggins(0.3, 60.0, 80.0, 3.2, 0.35)),
+        "morse": (lg.Morse(1.5, 3.8, eps), lg.Morse(1.4, 4.0, 1.3 * eps), lg.Morse(1.3, 4.2, 1.6 * eps)),
+        "gaussian": (lg.Gaussian(2.0 * eps, 0.08), lg.Gaussian(2.5 * eps, 0.07), lg.Gaussian(3.0 * eps, 0.06)),
+        "mie": (lg.Mie(3.405, eps, 12.0, 6.0), lg.Mie(3.6, 1.3 * eps, 12.5, 6.5), lg.Mie(3.8, 1.6 * eps, 14.0, 7.0)),
+    }[family]
+    if family == "lj":  # the historical LJ fluid: shifted, tail, plain
+        tail = lg.PairInteraction(pots[1], cutoff)
+        tail.enable_tail_corrections()
+        return lg.PairInteraction.shifted(pots[0], cutoff), tail, lg.PairInteraction(pots[2], cutoff)
+    tail = lg.PairInteraction(pots[2], cutoff)
+    tail.enable_tail_corrections()
+    return lg.PairInteraction(pots[0], cutoff), lg.PairInteraction.shifted(pots[1], cutoff), tail
+
+
+def random_lj_fluid(n: int, density: float, seed: int, cutoff: float, family: str = "lj",
                     precision: str = "fp64") -> lg.System:
-    """Jittered simple-cubic fluid of `n` particles (two kinds) at `density` (1/A^3)."""
+    """Jittered simple-cubic fluid of `n` particles (two kinds) at `density` (1/A^3),
+    with pair potentials of one family ("lj", "buckingham", "bmh", "morse",
+    "gaussian", "mie")."""
     rng = np.random.default_rng(seed)
     side = int(np.ceil(n ** (1.0 / 3.0)))
     length = (n / density) ** (1.0 / 3.0)
@@ -91,19 +116,10 @@ def random_lj_fluid(n: int, density: float, seed: int, cutoff: float, buckingham
     names = ["Ar" if i % 3 else "Kr" for i in range(n)]
     s = lg.System(lg.UnitCell.cubic(length), precision=precision)
     s.add_particles(names, pos)
-    if buckingham:
-        s.set_pair_potential(("Ar", "Ar"), lg.PairInteraction(lg.Buckingham(5000.0, 40.0, 0.3), cutoff))
-        s.set_pair_potential(("Ar", "Kr"), lg.PairInteraction.shifted(lg.Buckingham(6000.0, 50.0, 0.32), cutoff))
-        p = lg.PairInteraction(lg.Buckingham(7000.0, 60.0, 0.35), cutoff)
-        p.enable_tail_corrections()
-        s.set_pair_potential(("Kr", "Kr"), p)
-    else:
-        eps = units.from_(0.996, "kJ/mol")
-        s.set_pair_potential(("Ar", "Ar"), lg.PairInteraction.shifted(lg.LennardJones(3.405, eps), cutoff))
-        p = lg.PairInteraction(lg.LennardJones(3.6, 1.3 * eps), cutoff)
-        p.enable_tail_corrections()
-        s.set_pair_potential(("Ar", "Kr"), p)
-        s.set_pair_potential(("Kr", "Kr"), lg.PairInteraction(lg.LennardJones(3.8, 1.6 * eps), cutoff))
+    aa, ak, kk = _family_interactions(family, cutoff)
+    s.set_pair_potential(("Ar", "Ar"), aa)
+    s.set_pair_potential(("Ar", "Kr"), ak)
+    s.set_pair_potential(("Kr", "Kr"), kk)
     return s
 
 

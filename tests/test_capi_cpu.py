@@ -63,6 +63,11 @@ def test_host_checks_mirror_reference_panics():
         s.set_pair_potential(("A", "A"), lg.PairInteraction(lg.LennardJones(1.0, 1.0), 5.5))
     with pytest.raises(ValueError, match="berendsen"):
         lg.BerendsenThermostat(300.0, 0.5)
+    # functions.rs:774-777 and 803-806 (should_panic tests)
+    with pytest.raises(ValueError, match="positive in Gaussian"):
+        lg.Gaussian(8.0, -2.0)
+    with pytest.raises(ValueError, match="larger than the attractive exponent"):
+        lg.Mie(2.0, 0.8, 6.0, 12.0)
 
 
 def test_units_match_reference_conversions():

@@ -83,3 +83,33 @@ def test_coulomb_systems_are_rejected():
     batch = Batch([s])
     with pytest.raises(lg.EngineError, match="pair potentials only"):
         batch.mc_setup(0, 300.0, 0.3, 1)
+
+
+@pytest.mark.parametrize("family", ["bmh", "morse", "gaussian", "mie"])
+def test_chains_with_other_pair_potentials(family):
+    """FP64 chains follow the oracle move for move; mixed chains keep their
+    running energy within 1e-5 of a fresh evaluation."""
+    import systems as fluids
+    s = fluids.random_lj_fluid(400, 0.02, 9, 9.0, family=family)
+    batch = Batch([s])
+    batch.md_setup([1.0])
+    batch.mc_setup(0, 300.0, 0.3, 55)
+    moves = 300
+    batch.mc_run(moves)
+    pos_ref, e_ref, acc_ref = replay(s, 300.0, 0.3, 55, moves)
+    energy, acc, att = batch.mc_stats(0)
+    pos, _ = batch.state(0)
+    assert att == moves and acc == acc_ref
+    assert np.abs(pos - pos_ref).max() < 1e-9
+    assert abs(energy - e_ref) <= 1e-9 * abs(e_ref)
+    batch.engine.close()
+
+    m = fluids.random_lj_fluid(400, 0.02, 9, 9.0, family=family, precision="mixed")
+    batch = Batch([m], precision="mixed")
+    batch.md_setup([1.0])
+    batch.mc_setup(0, 300.0, 0.3, 56)
+    batch.mc_run(2000)
+    energy, acc, att = batch.mc_stats(0)
+    fresh = batch.energy(0)
+    assert att == 2000 and acc > 0
+    assert abs(energy - fresh) <= 1e-5 * abs(fresh), (energy, fresh)

@@ -56,8 +56,9 @@ def test_mixed_water():
     check(s)
 
 
-def test_mixed_unwrapped_buckingham_fluid():
-    check(systems.random_lj_fluid(700, 0.02, 5, 9.0, buckingham=True, precision="mixed"))
+@pytest.mark.parametrize("family", ["buckingham", "bmh", "morse", "gaussian", "mie"])
+def test_mixed_unwrapped_fluid(family):
+    check(systems.random_lj_fluid(700, 0.02, 5, 9.0, family=family, precision="mixed"))
 
 
 def test_mixed_md_tracks_fp64():

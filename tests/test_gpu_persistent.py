@@ -1,10 +1,10 @@
 """Persistent batched MD (one launch per run of steps, one thread-block cluster
 per group of systems) against the per-step kernels of the same mixed path.
 
-The two runs share the force arithmetic and the order of every force sum; the
-Berendsen factor's kinetic energy is summed per system in one and per tile in
-the other; the trajectories agree to rounding (1e-8 A after 80 steps), and
-each path repeats its own trajectory bit for bit.
+The two paths share the force arithmetic (every FP32 rounding written out),
+the order of every force sum, the neighbour-list builder's entry order and the
+Berendsen factor's kinetic-energy sums, so their trajectories are the same bit
+for bit, list rebuilds and thermostats included.
 """
 import ctypes
 
@@ -51,17 +51,14 @@ def test_persistent_matches_per_step_kernels(thermo):
     calls = [1, 40, 7, 32]  # run lengths across and inside the 32-step launches
     a = run(True, thermostats, calls)
     b = run(False, thermostats, calls)
-    tol = 1e-8
     for (pa, va), (pb, vb) in zip(a, b):
-        assert np.abs(pa - pb).max() < tol
-        assert np.abs(va - vb).max() < tol * 10
+        assert np.array_equal(pa, pb) and np.array_equal(va, vb)
 
 
 def test_persistent_rebuilds_lists():
     """Hot, dilute replicas over 200 steps: every system rebuilds its list
-    several times inside the persistent launches.  Rounding differences of the
-    two paths grow along the trajectory (molecular dynamics is chaotic), so
-    the bound after 200 steps is 1e-6 A."""
+    several times inside the persistent launches, and the trajectories stay
+    the same bit for bit."""
     systems = replicas()
     batch = Batch(systems, precision="mixed", threads_per_atom=4)
     batch.md_setup([1.0] * len(systems))
@@ -71,9 +68,9 @@ def test_persistent_rebuilds_lists():
     ref.md_setup([1.0] * len(systems))
     ref.md_run(200)
     for s in range(len(systems)):
-        pa, _ = batch.state(s)
-        pb, _ = ref.state(s)
-        assert np.abs(pa - pb).max() < 1e-6
+        pa, va = batch.state(s)
+        pb, vb = ref.state(s)
+        assert np.array_equal(pa, pb) and np.array_equal(va, vb)
         assert np.isfinite(e0[s])
 
 
@@ -122,4 +119,29 @@ def test_persistent_list_overflow_is_regrown_and_replayed():
     a = run_once(True)
     b = run_once(False)
     for (pa, va), (pb, vb) in zip(a, b):
-        assert np.all(np.isfinite(pa)) and np.abs(pa - pb).max() < 1e-8
+        assert np.all(np.isfinite(pa)) and np.array_equal(pa, pb) and np.array_equal(va, vb)
+
+
+def test_persistent_other_pair_potentials():
+    """Fluids of the Born-Mayer-Huggins, Morse, Gaussian and Mie potentials
+    (plain, shifted and tail-corrected pairs of two kinds) in one batch with
+    an LJ replica, two of them under a thermostat: the persistent launches
+    give the per-step kernels' trajectories bit for bit."""
+    import systems as fluids
+
+    def make():
+        out = [fluids.random_lj_fluid(400 + 50 * k, 0.02, 30 + k, 9.0, family=f, precision="mixed")
+               for k, f in enumerate(["bmh", "morse", "gaussian", "mie"])]
+        return out + [workloads.lj_replica(500, 0.7, 150.0, 77, "mixed")]
+
+    states = []
+    for persistent in (True, False):
+        systems = make()
+        batch = Batch(systems, precision="mixed", persistent=persistent, threads_per_atom=8)
+        batch.md_setup([1.0] * len(systems), [None, (200.0, 50.0), None, (150.0, 20.0), None])
+        batch.md_run(40)
+        states.append([batch.state(s) for s in range(len(systems))])
+        batch.engine.close()
+    for (pa, va), (pb, vb) in zip(*states):
+        assert np.all(np.isfinite(pa))
+        assert np.array_equal(pa, pb) and np.array_equal(va, vb)

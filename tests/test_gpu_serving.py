@@ -37,6 +37,23 @@ def test_served_results_equal_alone_results():
     assert 0.0 < p50 <= p99
 
 
+def test_served_mixed_results_are_alone_results_bit_for_bit():
+    """Mixed precision, pair-potential requests: the server runs its lanes in
+    chunks of 20 steps through the persistent kernel, a request alone runs in
+    launches of 32 steps; every step's arithmetic is the same in both, so the
+    trajectories are equal bit for bit."""
+    requests = [r for r in workloads.serving_requests(count=16, rate=200.0, seed=6, precision="mixed",
+                                                      scale=0.03) if r.kind == "lj"]
+    assert len(requests) >= 4
+    server = Server(precision="mixed", chunk=20, max_lanes=3, threads_per_atom=8)
+    done = server.run(requests)
+    server.close()
+    assert len(done) == len(requests)
+    for r in done:
+        pos, vel = run_alone(r, "mixed", 8)
+        assert np.array_equal(r.positions, pos) and np.array_equal(r.velocities, vel), r.rid
+
+
 def test_admission_waits_for_memory():
     requests = workloads.serving_requests(count=6, rate=1000.0, seed=9, precision="mixed", scale=0.03)
     for r in requests:

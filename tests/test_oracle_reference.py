@@ -14,7 +14,7 @@ import systems
 from lumol_gb300 import units
 from ulps import relative_eq, rust_round_at, ulps_eq
 
-LJ, BUCK, HARM = 2, 3, 4
+LJ, BUCK, HARM, BMH, MORSE, GAUSS, MIE = 2, 3, 4, 5, 6, 7, 8
 needs_reference = pytest.mark.skipif(not refdata.available(), reason="reference tree not present")
 
 
@@ -55,6 +55,75 @@ def test_buckingham_literals(oracle_lib):
     d = lambda r: oracle.pair_eval(BUCK, (2.0, 1.0, 5.3), 1e9, r)
     assert d(2.2)[0] == 1.3117360696239022
     assert d(2.2)[1] == 0.2251072178835946
+
+
+def test_born_mayer_huggins_literals(oracle_lib):
+    # functions.rs:718-737: BornMayerHuggins {a, c, d, sigma, rho}
+    b = lambda r: oracle.pair_eval(BMH, (2.0, 1.0, 0.5, 2.0, 2.0), 1e9, r)
+    assert b(2.0)[0] == 1.986328125
+    assert b(2.0)[1] == 0.9609375
+    t = oracle.pair_eval(BMH, (2.0, 1.0, 0.5, 2.0, 2.0), 10.0, 1.0, tail=True)
+    assert t[2] == 4.981521444402363
+    assert t[3] == 69.13986044386026
+    eps = 1e-9
+    assert relative_eq((b(4.0)[0] - b(4.0 + eps)[0]) / eps, b(4.0)[1], epsilon=1e-6)
+    # doc test of functions.rs:335-337
+    d = lambda r: oracle.pair_eval(BMH, (2.0, 1.0, 0.5, 1.5, 5.3), 1e9, r)
+    assert d(2.2)[0] == 1.7446409593340713
+    assert d(2.2)[1] == 0.30992873382584607
+
+
+def test_morse_literals(oracle_lib):
+    # functions.rs:739-757 and the doc test of functions.rs:400-402: Morse {a, x0, depth}
+    m = lambda r: oracle.pair_eval(MORSE, (2.0, 1.3, 4.0), 1e9, r)
+    assert m(1.0)[0] == 2.703517287822119
+    assert m(1.0)[1] == -37.12187076378477
+    t = oracle.pair_eval(MORSE, (2.0, 1.3, 4.0), 1.0, 1.0, tail=True)
+    assert t[2] == 0.0 and t[3] == 0.0
+    # the reference's force is 2·depth·(1 - e²)·a, not the derivative of its
+    # energy; its finite-difference check passes at r = x0 where both vanish
+    eps = 1e-9
+    assert relative_eq((m(1.3)[0] - m(1.3 + eps)[0]) / eps, m(1.3)[1], epsilon=1e-6)
+
+
+def test_gaussian_literals(oracle_lib):
+    # functions.rs:759-772: Gaussian::new(a, b)
+    g = lambda r: oracle.pair_eval(GAUSS, (8.0, 2.0), 1e9, r)
+    assert g(0.0)[0] == -8.0
+    assert g(0.0)[1] == 0.0
+    t = oracle.pair_eval(GAUSS, (8.0, 2.0), 2.5, 1.0, tail=True)
+    assert relative_eq(t[2], -1.93518e-5, epsilon=1e-10)
+    assert relative_eq(t[3], 5.23887e-4, epsilon=1e-10)
+    eps = 1e-9
+    assert relative_eq((g(0.5)[0] - g(0.5 + eps)[0]) / eps, g(0.5)[1], epsilon=1e-6)
+    # doc test of functions.rs:454-456
+    assert oracle.pair_eval(GAUSS, (8.0, 0.5), 1e9, 0.0)[:2] == (-8.0, 0.0)
+
+
+def test_mie_literals(oracle_lib):
+    # functions.rs:780-801: Mie::new(sigma, epsilon, n, m)
+    m = lambda r: oracle.pair_eval(MIE, (2.0, 0.8, 12.0, 6.0), 1e9, r)
+    assert m(2.0)[0] == 0.0
+    assert m(2.5)[0] == -0.6189584744448002
+    tail = lambda rc: oracle.pair_eval(MIE, (2.0, 0.8, 12.0, 6.0), rc, 1.0, tail=True)
+    assert relative_eq(tail(1.0)[2], 1388.0888889, epsilon=1e-6)
+    assert relative_eq(tail(2.0)[2], -5.688888888888889, epsilon=1e-6)
+    assert relative_eq(tail(14.42)[2], -0.022767318648783084, epsilon=1e-6)
+    assert relative_eq(tail(1.0)[3], 17066.666666666668, epsilon=1e-6)
+    assert relative_eq(tail(2.0)[3], -17.06666666666667, epsilon=1e-6)
+    assert relative_eq(tail(14.42)[3], -0.1366035877536718, epsilon=1e-6)
+    assert abs(m(2.0 ** (1.0 / 6.0) * 2.0)[1]) < 1e-15
+    assert ulps_eq(m(2.5)[1], -0.95773475733504)
+    eps = 1e-9
+    assert relative_eq((m(4.0)[0] - m(4.0 + eps)[0]) / eps, m(4.0)[1], epsilon=1e-6)
+    # functions.rs:809-815: no tail correction when m <= 3
+    t = oracle.pair_eval(MIE, (2.0, 0.8, 12.0, 2.0), 2.0, 1.0, tail=True)
+    assert t[2] == 0.0 and t[3] == 0.0
+    # doc test of functions.rs:520-524
+    d = lambda r: oracle.pair_eval(MIE, (2.0, 10.0, 12.0, 6.0), 1e9, r)
+    assert d(2.0)[0] == 0.0
+    assert abs(d(3.0)[0] + 3.203365942785746) < 1e-8
+    assert d(2.0)[1] == 120.0
 
 
 # ---- energy/pairs.rs:317-360 ----------------------------------------------------
