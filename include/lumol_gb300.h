@@ -217,6 +217,45 @@ int lg_pairset(lg_engine* e, int32_t s, const double* positions, int32_t family,
  * every step, as MolecularDynamics::propagate does (md/molecular_dynamics.rs:66-76). */
 int lg_md_setup(lg_engine* e, int32_t s, double dt, double thermostat_temperature,
                 double thermostat_tau);
+
+/* Integrators (lumol-sim/src/md/integrators.rs). */
+enum {
+    LG_INTEGRATOR_VELOCITY_VERLET = 0, /* VelocityVerlet (integrators.rs:19-70) */
+    LG_INTEGRATOR_VERLET = 1,          /* Verlet (integrators.rs:72-123): keeps the positions at t - dt */
+    LG_INTEGRATOR_LEAP_FROG = 2        /* LeapFrog (integrators.rs:125-169) */
+};
+/* Thermostats, applied after every step (md/thermostats.rs). */
+enum {
+    LG_THERMOSTAT_NONE = 0,
+    LG_THERMOSTAT_BERENDSEN = 1, /* BerendsenThermostat(temperature, tau) (thermostats.rs:77-121) */
+    LG_THERMOSTAT_RESCALE = 2,   /* RescaleThermostat::with_tolerance(temperature, tolerance) (thermostats.rs:27-73) */
+    LG_THERMOSTAT_CSVR = 3       /* CSVRThermostat(temperature, tau) (thermostats.rs:123-210), noise from `seed` */
+};
+/* Controls, applied after the thermostat at every step (md/controls.rs). */
+#define LG_CONTROL_REMOVE_TRANSLATION 1u /* RemoveTranslation (controls.rs:26-43) */
+#define LG_CONTROL_REWRAP 2u             /* Rewrap (controls.rs:73-89): molecules' centres of mass into the cell */
+
+typedef struct lg_md_params {
+    int32_t integrator;  /* LG_INTEGRATOR_* */
+    int32_t thermostat;  /* LG_THERMOSTAT_* */
+    double timestep;
+    double temperature;  /* thermostat target (K) */
+    double tau;          /* Berendsen / CSVR time scale, in timesteps (>= 1) */
+    double tolerance;    /* RescaleThermostat tolerance (K) */
+    uint64_t seed;       /* CSVR: the noise of step k is drawn from SplitMix64 streams of (seed, k) */
+    uint32_t controls;   /* LG_CONTROL_* bits */
+    uint32_t reserved;   /* 0 */
+} lg_md_params;
+
+/* Molecular dynamics of system `s` with any integrator, thermostat and
+ * controls of the list above, stepped as MolecularDynamics::propagate does
+ * (md/molecular_dynamics.rs:66-76: integrate, thermostat, controls).  The
+ * integrator's setup runs at the next lg_md_run: VelocityVerlet and LeapFrog
+ * zero the accelerations, Verlet takes its positions at t - dt as x - v dt from
+ * the state then on the device (integrators.rs:92-104).  For a Verlet system
+ * the accelerations of lg_md_get/set_state_all hold those previous positions.
+ * Argument checks follow the constructors (thermostats.rs:48-61, 102-109, 151-160). */
+int lg_md_setup_ex(lg_engine* e, int32_t s, const lg_md_params* params);
 /* Uploads / downloads positions and velocities (3n each) of system `s`. */
 int lg_md_set_state(lg_engine* e, int32_t s, const double* positions, const double* velocities);
 int lg_md_get_state(lg_engine* e, int32_t s, double* positions, double* velocities);

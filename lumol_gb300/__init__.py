@@ -2,9 +2,9 @@
 virial / integration path, behind a C ABI (include/lumol_gb300.h).
 
 The Python classes mirror lumol-core / lumol-sim (System, PairInteraction,
-LennardJones, Buckingham, Harmonic, Ewald, Wolf, VelocityVerlet,
-BerendsenThermostat, MolecularDynamics); every computation runs in the CUDA
-library `liblumol_gb300.so` of this package.  There is no CPU fallback.
+the pair potentials, Ewald, Wolf, the integrators, thermostats and controls,
+MolecularDynamics, MonteCarlo); every computation runs in the CUDA library
+`liblumol_gb300.so` of this package.  There is no CPU fallback.
 """
 from . import units
 from ._capi import EngineError
@@ -12,10 +12,12 @@ from .system import (
     BerendsenThermostat,
     BornMayerHuggins,
     Buckingham,
+    CSVRThermostat,
     Engine,
     Ewald,
     Gaussian,
     Harmonic,
+    LeapFrog,
     LennardJones,
     Mie,
     MolecularDynamics,
@@ -24,11 +26,16 @@ from .system import (
     NullPotential,
     PairInteraction,
     PairRestriction,
+    RemoveTranslation,
+    RescaleThermostat,
+    Rewrap,
     System,
     Translate,
     UnitCell,
     VelocityVerlet,
+    Verlet,
     Wolf,
+    md_params,
 )
 from ._capi import (
     LG_TERM_ALL,
@@ -42,9 +49,10 @@ from ._capi import (
 )
 
 __all__ = [
-    "units", "EngineError", "BerendsenThermostat", "Buckingham", "Engine", "Ewald", "Harmonic",
-    "LennardJones", "MolecularDynamics", "MonteCarlo", "Translate", "NullPotential", "PairInteraction", "PairRestriction",
-    "System", "UnitCell", "VelocityVerlet", "Wolf",
+    "units", "EngineError", "BerendsenThermostat", "BornMayerHuggins", "Buckingham", "CSVRThermostat", "Engine",
+    "Ewald", "Gaussian", "Harmonic", "LeapFrog", "LennardJones", "Mie", "MolecularDynamics", "MonteCarlo", "Morse",
+    "Translate", "NullPotential", "PairInteraction", "PairRestriction", "RemoveTranslation", "RescaleThermostat",
+    "Rewrap", "System", "UnitCell", "VelocityVerlet", "Verlet", "Wolf", "md_params",
     "LG_TERM_ALL", "LG_TERM_ANGLES", "LG_TERM_BONDS", "LG_TERM_COUL_KSPACE", "LG_TERM_COUL_REAL",
     "LG_TERM_COUL_SELF", "LG_TERM_PAIRS", "LG_TERM_TAIL",
 ]

@@ -78,6 +78,17 @@ class LgOptions(ctypes.Structure):
                 ("threads_per_atom", ctypes.c_int32), ("flags", ctypes.c_int32)]
 
 
+LG_INTEGRATOR_VELOCITY_VERLET, LG_INTEGRATOR_VERLET, LG_INTEGRATOR_LEAP_FROG = 0, 1, 2
+LG_THERMOSTAT_NONE, LG_THERMOSTAT_BERENDSEN, LG_THERMOSTAT_RESCALE, LG_THERMOSTAT_CSVR = 0, 1, 2, 3
+LG_CONTROL_REMOVE_TRANSLATION, LG_CONTROL_REWRAP = 1, 2
+
+
+class LgMdParams(ctypes.Structure):
+    _fields_ = [("integrator", ctypes.c_int32), ("thermostat", ctypes.c_int32), ("timestep", ctypes.c_double),
+                ("temperature", ctypes.c_double), ("tau", ctypes.c_double), ("tolerance", ctypes.c_double),
+                ("seed", ctypes.c_uint64), ("controls", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
 # name -> (restype, argtypes)
 _P = ctypes.c_void_p
 _D = ctypes.POINTER(ctypes.c_double)
@@ -98,6 +109,7 @@ SIGNATURES = {
     "lg_compute_device": (ctypes.c_int, [_P, _P, ctypes.c_uint32, ctypes.c_uint32, _P, _P, _P, _P]),
     "lg_pairset": (ctypes.c_int, [_P, ctypes.c_int32, _D, ctypes.c_int32, _I32, ctypes.c_int64, _I64]),
     "lg_md_setup": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double]),
+    "lg_md_setup_ex": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(LgMdParams)]),
     "lg_md_set_state": (ctypes.c_int, [_P, ctypes.c_int32, _D, _D]),
     "lg_md_get_state": (ctypes.c_int, [_P, ctypes.c_int32, _D, _D]),
     "lg_md_set_state_all": (ctypes.c_int, [_P, _D, _D, _D]),

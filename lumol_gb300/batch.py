@@ -7,7 +7,7 @@ import ctypes
 import numpy as np
 
 from . import _capi as C
-from .system import Engine, System
+from .system import Engine, System, md_params
 
 
 class Batch:
@@ -29,10 +29,17 @@ class Batch:
     def atoms(self) -> int:
         return int(self.offsets[-1])
 
-    def md_setup(self, timesteps, thermostats=None) -> None:
-        """VelocityVerlet::setup for every system; thermostats[s] is None or a
-        (temperature, tau) Berendsen pair."""
+    def md_setup(self, timesteps=None, thermostats=None, propagators=None) -> None:
+        """The MD setup of every system.  Either `timesteps` (VelocityVerlet)
+        with thermostats[s] None or a (temperature, tau) Berendsen pair, or
+        `propagators`: one MolecularDynamics (integrator, thermostat, controls)
+        per system."""
         for s, system in enumerate(self.systems):
+            if propagators is not None:
+                md = propagators[s]
+                p = md_params(md.integrator, md.thermostat, md.controls)
+                self.engine.call("lg_md_setup_ex", s, ctypes.byref(p))
+                continue
             T0, tau = (thermostats[s] if thermostats and thermostats[s] else (0.0, 0.0))
             self.engine.call("lg_md_setup", s, float(timesteps[s]), float(T0), float(tau))
         for s, system in enumerate(self.systems):

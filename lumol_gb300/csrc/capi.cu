@@ -54,6 +54,15 @@ struct DBuf {
     }
 };
 
+static_assert(MD_VELOCITY_VERLET == LG_INTEGRATOR_VELOCITY_VERLET && MD_VERLET == LG_INTEGRATOR_VERLET &&
+                  MD_LEAP_FROG == LG_INTEGRATOR_LEAP_FROG,
+              "integrator values");
+static_assert(TH_NONE == LG_THERMOSTAT_NONE && TH_BERENDSEN == LG_THERMOSTAT_BERENDSEN &&
+                  TH_RESCALE == LG_THERMOSTAT_RESCALE && TH_CSVR == LG_THERMOSTAT_CSVR,
+              "thermostat values");
+static_assert(CTL_REMOVE_TRANSLATION == LG_CONTROL_REMOVE_TRANSLATION && CTL_REWRAP == LG_CONTROL_REWRAP,
+              "control values");
+
 struct HostSystem {
     bool has_cell = false;
     double L[3] = {0, 0, 0};
@@ -68,13 +77,37 @@ struct HostSystem {
     std::vector<lg_pair> pairs;
     lg_coulomb coul{};
     // molecular dynamics
-    double dt = 0.0, T0 = 0.0, tau = 0.0;
+    double dt = 0.0, T0 = 0.0, tau = 0.0, tol = 0.0;
+    int32_t integrator = LG_INTEGRATOR_VELOCITY_VERLET, thermostat = LG_THERMOSTAT_NONE;
+    uint32_t controls = 0;
+    uint64_t seed = 0;
     bool md_ready = false;
+    bool verlet_setup = false;  // Verlet::setup runs at the next lg_md_run
     // derived
     std::vector<int64_t> mol_begin;  // first atom of each molecule (local index), plus the end
     double tail_energy = 0.0, tail_virial = 0.0, ewald_self = 0.0;
     double alpha = 0.0;
 };
+
+// The MD fields of a system's device record.
+void fill_md(SysDev& d, const HostSystem& h) {
+    d.dt = h.dt;
+    d.hdt = 0.5 * h.dt;
+    d.dt2 = h.dt * h.dt;  // integrators.rs:107, 149
+    d.hdt2 = 0.5 * d.dt2;
+    d.inv_2dt = h.dt > 0.0 ? 1.0 / (2.0 * h.dt) : 0.0;
+    d.thermo_T = h.T0;
+    d.thermo_tau = h.tau;
+    d.thermo_tol = h.tol;
+    d.seed = h.seed;
+    d.integrator = h.integrator;
+    d.thermostat = h.thermostat;
+    d.controls = h.controls;
+    d.dof = (double)(3 * h.n);
+    double total = 0.0;  // RemoveTranslation: masses summed in atom order (controls.rs:31)
+    for (double w : h.masses) total += w;
+    d.total_mass = total;
+}
 
 // ---- host restatement of the reference's scalar functions -----------------
 double powi6(double x) {
@@ -267,7 +300,9 @@ struct lg_engine {
     Batch b;
     // device storage
     DBuf<double4_32a> posq, vel, acc, pos_build;
-    DBuf<double> force, pos3, vel3, red, host_const, kepart, out, fpart, kred, mc_part;
+    DBuf<double> force, pos3, vel3, red, host_const, kepart, mom, out, fpart, kred, mc_part;
+    DBuf<unsigned long long> md_count, cp_count;
+    DBuf<int> mol_start;
     DBuf<int2> tiles;
     DBuf<double4_32a> cp_pos, cp_vel, cp_acc;  // MD checkpoint: a chunk whose list overflowed is replayed
     DBuf<int> kind, mol, sysid, spec_off, spec_j, bt_off, bt_role, nbr, nnb, atom_cell, cell_count, cell_start,
@@ -314,7 +349,7 @@ struct lg_engine {
     // MD graphs, one per chunk length
     std::map<int, cudaGraphExec_t> graphs;
     std::map<int, size_t> graph_nodes;
-    bool graph_thermo = false;
+    int graph_mode = -1;  // md_mode() of the captured graphs
 
     // batched Monte Carlo chains
     DBuf<McState> mc_chains;
@@ -433,6 +468,7 @@ int commit(lg_engine* e) {
     std::vector<double> h_const((size_t)nsys * RED_STRIDE, 0.0);
     int mol_base = 0, cell_total = 0, kdim = 1;
     std::vector<int2> h_tiles;
+    std::vector<int> h_mol_start;  // first atom of each molecule of the batch, then n
     double max_expected = 0.0;
     int64_t max_n = 1;
 
@@ -641,12 +677,14 @@ int commit(lg_engine* e) {
 
         d.begin = (int)base;
         d.end = (int)(base + h.n);
-        d.dt = h.dt;
-        d.hdt = 0.5 * h.dt;
-        d.thermo_T = h.T0;
-        d.thermo_tau = h.tau;
-        d.dof = (double)(3 * h.n);
+        fill_md(d, h);
+        // the system's molecules in the batch molecule table (contiguous atoms each)
+        d.mol_first = (int)(h_mol_start.size());
+        for (size_t k = 0; k + 1 < h.mol_begin.size(); k++)
+            if (h.mol_begin[k + 1] > h.mol_begin[k]) h_mol_start.push_back((int)(base + h.mol_begin[k]));
+        d.mol_end = (int)h_mol_start.size();
     }
+    h_mol_start.push_back((int)n);
 
     // per-atom CSR tables
     std::vector<int> h_spec_off(n + 1, 0), h_spec_j;
@@ -690,6 +728,10 @@ int commit(lg_engine* e) {
     CUDA_TRY(e, e->host_const.alloc((size_t)nsys * RED_STRIDE));
     CUDA_TRY(e, e->tiles.alloc(std::max<size_t>(h_tiles.size(), 1)));
     CUDA_TRY(e, e->kepart.alloc(std::max<size_t>(n, 1)));  // chunk kinetic energies: at most one per atom
+    CUDA_TRY(e, e->mom.alloc(std::max<size_t>(3 * n, 1)));
+    CUDA_TRY(e, e->md_count.alloc(std::max(nsys, 1)));
+    CUDA_TRY(e, e->cp_count.alloc(std::max(nsys, 1)));
+    CUDA_TRY(e, e->mol_start.alloc(h_mol_start.size()));
     CUDA_TRY(e, e->cp_pos.alloc(n));
     CUDA_TRY(e, e->cp_vel.alloc(n));
     CUDA_TRY(e, e->cp_acc.alloc(n));
@@ -794,6 +836,10 @@ int commit(lg_engine* e) {
         CUDA_TRY(e, cudaMemcpyAsync(e->tiles.p, h_tiles.data(), h_tiles.size() * sizeof(int2), cudaMemcpyHostToDevice,
                                     st));
     CUDA_TRY(e, cudaMemsetAsync(e->kepart.p, 0, std::max<size_t>(n, 1) * sizeof(double), st));
+    CUDA_TRY(e, cudaMemsetAsync(e->mom.p, 0, std::max<size_t>(3 * n, 1) * sizeof(double), st));
+    CUDA_TRY(e, cudaMemsetAsync(e->md_count.p, 0, std::max(nsys, 1) * sizeof(unsigned long long), st));
+    CUDA_TRY(e, cudaMemcpyAsync(e->mol_start.p, h_mol_start.data(), h_mol_start.size() * sizeof(int),
+                                cudaMemcpyHostToDevice, st));
     CUDA_TRY(e, cudaMemcpyAsync(e->ptab.p, h_ptab.data(), h_ptab.size() * sizeof(PairDev), cudaMemcpyHostToDevice, st));
     CUDA_TRY(e, cudaMemcpyAsync(e->ptabf.p, h_ptabf.data(), h_ptabf.size() * sizeof(PairDevF), cudaMemcpyHostToDevice,
                                 st));
@@ -865,6 +911,10 @@ int commit(lg_engine* e) {
     b.ntiles = (int)h_tiles.size();
     b.tiles = e->tiles.p;
     b.kepart = e->kepart.p;
+    b.mom = e->mom.p;
+    b.md_count = e->md_count.p;
+    b.nmol = (int)h_mol_start.size() - 1;
+    b.mol_start = e->mol_start.p;
     if (e->h_mc.size() != (size_t)nsys) e->h_mc.assign(nsys, McState{});
     CUDA_TRY(e, e->mc_chains.alloc(nsys));
     CUDA_TRY(e, cudaMemcpy(e->mc_chains.p, e->h_mc.data(), nsys * sizeof(McState), cudaMemcpyHostToDevice));
@@ -1305,27 +1355,53 @@ int lg_pairset(lg_engine* e, int32_t s, const double* positions, int32_t family,
 
 // ---- molecular dynamics -----------------------------------------------------
 int lg_md_setup(lg_engine* e, int32_t s, double dt, double T0, double tau) {
-    if (!valid_sys(e, s) || !(dt > 0.0)) return fail(e, LG_ERR_ARGUMENT, "invalid timestep");
-    if (tau > 0.0) {
-        // BerendsenThermostat::new (thermostats.rs:102-109)
-        if (T0 < 0.0) return fail(e, LG_ERR_ARGUMENT, "The temperature must be positive in thermostats.");
-        if (tau < 1.0) return fail(e, LG_ERR_ARGUMENT, "The timestep must be larger than 1 in berendsen thermostat.");
-    }
+    lg_md_params p{};
+    p.integrator = LG_INTEGRATOR_VELOCITY_VERLET;
+    p.thermostat = tau > 0.0 ? LG_THERMOSTAT_BERENDSEN : LG_THERMOSTAT_NONE;
+    p.timestep = dt;
+    p.temperature = T0;
+    p.tau = tau;
+    return lg_md_setup_ex(e, s, &p);
+}
+
+int lg_md_setup_ex(lg_engine* e, int32_t s, const lg_md_params* p) {
+    if (!valid_sys(e, s) || !p) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    if (!(p->timestep > 0.0)) return fail(e, LG_ERR_ARGUMENT, "invalid timestep");
+    if (p->integrator < LG_INTEGRATOR_VELOCITY_VERLET || p->integrator > LG_INTEGRATOR_LEAP_FROG)
+        return fail(e, LG_ERR_ARGUMENT, "unknown integrator");
+    if (p->thermostat < LG_THERMOSTAT_NONE || p->thermostat > LG_THERMOSTAT_CSVR)
+        return fail(e, LG_ERR_ARGUMENT, "unknown thermostat");
+    if (p->controls & ~(LG_CONTROL_REMOVE_TRANSLATION | LG_CONTROL_REWRAP))
+        return fail(e, LG_ERR_ARGUMENT, "unknown control");
+    // the constructors' checks: RescaleThermostat::new, BerendsenThermostat::new,
+    // CSVRThermostat::from_rng (thermostats.rs:48-53, 102-109, 151-160)
+    if (p->thermostat != LG_THERMOSTAT_NONE && p->temperature < 0.0)
+        return fail(e, LG_ERR_ARGUMENT, "The temperature must be positive in thermostats.");
+    if (p->thermostat == LG_THERMOSTAT_BERENDSEN && !(p->tau >= 1.0))
+        return fail(e, LG_ERR_ARGUMENT, "The timestep must be larger than 1 in berendsen thermostat.");
+    if (p->thermostat == LG_THERMOSTAT_CSVR && !(p->tau >= 1.0))
+        return fail(e, LG_ERR_ARGUMENT, "The timestep must be larger than 1 in CSVR thermostat.");
     HostSystem& h = e->sys[s];
-    h.dt = dt;
-    h.T0 = T0;
-    h.tau = tau > 0.0 ? tau : 0.0;
+    h.dt = p->timestep;
+    h.integrator = p->integrator;
+    h.thermostat = p->thermostat;
+    h.T0 = p->temperature;
+    h.tau = (p->thermostat == LG_THERMOSTAT_BERENDSEN || p->thermostat == LG_THERMOSTAT_CSVR) ? p->tau : 0.0;
+    h.tol = p->tolerance;
+    h.seed = p->seed;
+    h.controls = p->controls;
     h.md_ready = true;
+    h.verlet_setup = p->integrator == LG_INTEGRATOR_VERLET;
     if (!e->dirty) {
         SysDev& d = e->h_sysdev[s];
-        d.dt = h.dt;
-        d.hdt = 0.5 * h.dt;
-        d.thermo_T = h.T0;
-        d.thermo_tau = h.tau;
+        fill_md(d, h);
         CUDA_TRY(e, cudaSetDevice(e->opt.device));
         CUDA_TRY(e, cudaMemcpyAsync(e->sysdev.p + s, &d, sizeof(SysDev), cudaMemcpyHostToDevice, e->stream));
-        // VelocityVerlet::setup: accelerations := 0 (integrators.rs:40-42)
-        CUDA_TRY(e, cudaMemsetAsync(e->acc.p + e->begin[s], 0, h.n * sizeof(double4_32a), e->stream));
+        // VelocityVerlet / LeapFrog::setup: accelerations := 0 (integrators.rs:40-42, 146-148);
+        // Verlet's previous positions are taken at the next run
+        if (p->integrator != LG_INTEGRATOR_VERLET)
+            CUDA_TRY(e, cudaMemsetAsync(e->acc.p + e->begin[s], 0, h.n * sizeof(double4_32a), e->stream));
+        CUDA_TRY(e, cudaMemsetAsync(e->md_count.p + s, 0, sizeof(unsigned long long), e->stream));
         CUDA_TRY(e, cudaStreamSynchronize(e->stream));
         e->drop_graphs();
     }
@@ -1478,24 +1554,64 @@ int autotune(lg_engine* e) {
     return LG_OK;
 }
 
-// One Velocity-Verlet step.  With a thermostat, the Berendsen scaling of the
-// previous step is applied by this step's vv_first (apply_previous), and the
-// last step of a run is followed by launch_thermostat_finalize.
-void enqueue_md_step(lg_engine* e, bool thermo, bool apply_previous, cudaStream_t st) {
-    launch_vv_first(e->b, thermo && apply_previous, st);
-    enqueue_forces(e, LG_TERM_ALL, false, st, true);
-    launch_vv_second(e->b, thermo, st);
+// What the MD steps of a batch need besides the integrators: a thermostat or
+// control (MD_ADJUST), Rewrap (MD_REWRAP), a Verlet system (MD_VERLET_SYS:
+// its positions move after the forces, so the fixed-point copies are taken
+// before each force evaluation).
+constexpr int MD_ADJUST = 1, MD_REWRAP = 2, MD_VERLET_SYS = 4;
+int md_mode(const lg_engine* e) {
+    int mode = 0;
+    for (int s = 0; s < e->nsys; s++) {
+        const HostSystem& h = e->sys[s];
+        if (h.thermostat != LG_THERMOSTAT_NONE || h.controls) mode |= MD_ADJUST;
+        if (h.controls & LG_CONTROL_REWRAP) mode |= MD_REWRAP;
+        if (h.integrator == LG_INTEGRATOR_VERLET) mode |= MD_VERLET_SYS;
+    }
+    return mode;
+}
+
+// One MD step of every system.  The thermostat and controls of the previous
+// step are applied by this step's md_first (apply_previous; Rewrap by a kernel
+// before it), and the last step of a run is followed by launch_md_finalize.
+void enqueue_md_step(lg_engine* e, int mode, bool apply_previous, cudaStream_t st) {
+    bool adjust = (mode & MD_ADJUST) && apply_previous;
+    if (adjust && (mode & MD_REWRAP)) {
+        launch_rewrap(e->b, st);
+        e->launches += e->b.nmol ? 1 : 0;
+    }
+    launch_md_first(e->b, adjust, st);
+    enqueue_forces(e, LG_TERM_ALL, false, st, !(mode & MD_VERLET_SYS));
+    launch_md_second(e->b, st);
     e->launches += e->b.ntiles ? 2 : 0;
+}
+
+// The pending thermostat and controls at the end of a run.
+void enqueue_md_finish(lg_engine* e, int mode, cudaStream_t st) {
+    if (!(mode & MD_ADJUST)) return;
+    launch_md_finalize(e->b, st);
+    e->launches += e->b.ntiles ? 1 : 0;
+    if (mode & MD_REWRAP) {
+        launch_rewrap(e->b, st);
+        e->launches += e->b.nmol ? 1 : 0;
+    }
 }
 
 // ---- persistent batched MD -------------------------------------------------------
 // A batch the persistent kernel can run: mixed precision, pair potentials
-// only.  It also needs a group size of 2, 4 or 8 threads per atom (the
+// only, Velocity-Verlet with at most a Berendsen thermostat.  It also needs a group size of 2, 4 or 8 threads per atom (the
 // per-step kernel's, so both paths sum every force in the same order).
 bool persist_batch(const lg_engine* e) {
     const Batch& b = e->b;
-    return !(e->opt.flags & LG_OPT_NO_PERSISTENT) && b.precision == LG_PRECISION_MIXED && !b.pair_general &&
-           !b.bt_off && b.nkvec == 0 && b.n > 0;
+    if ((e->opt.flags & LG_OPT_NO_PERSISTENT) || b.precision != LG_PRECISION_MIXED || b.pair_general || b.bt_off ||
+        b.nkvec != 0 || b.n == 0)
+        return false;
+    for (int s = 0; s < e->nsys; s++) {  // VelocityVerlet, no thermostat or Berendsen, no control
+        const HostSystem& h = e->sys[s];
+        if (h.integrator != LG_INTEGRATOR_VELOCITY_VERLET || h.controls ||
+            (h.thermostat != LG_THERMOSTAT_NONE && h.thermostat != LG_THERMOSTAT_BERENDSEN))
+            return false;
+    }
+    return true;
 }
 bool persist_eligible(const lg_engine* e) {
     int t = e->b.tpa;
@@ -1636,13 +1752,13 @@ int md_run_persistent(lg_engine* e, int64_t nsteps, bool thermo) {
     return LG_OK;
 }
 
-int build_md_graph(lg_engine* e, int steps, bool thermo) {
-    if (e->graph_thermo != thermo) e->drop_graphs();
+int build_md_graph(lg_engine* e, int steps, int mode) {
+    if (e->graph_mode != mode) e->drop_graphs();
     cudaGraph_t g;
     uint64_t before = e->launches;
     CUDA_TRY(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-    for (int k = 0; k < steps; k++) enqueue_md_step(e, thermo, k > 0, e->stream);
-    if (thermo) launch_thermostat_finalize(e->b, e->stream);
+    for (int k = 0; k < steps; k++) enqueue_md_step(e, mode, k > 0, e->stream);
+    enqueue_md_finish(e, mode, e->stream);
     e->launches = before;  // captured launches run (and are counted) at replay
     CUDA_TRY(e, cudaStreamEndCapture(e->stream, &g));
     size_t nodes = 0;
@@ -1653,7 +1769,7 @@ int build_md_graph(lg_engine* e, int steps, bool thermo) {
     if (ce != cudaSuccess) return fail(e, LG_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ce));
     e->graphs[steps] = exec;
     e->graph_nodes[steps] = nodes;
-    e->graph_thermo = thermo;
+    e->graph_mode = mode;
     return LG_OK;
 }
 
@@ -1665,15 +1781,23 @@ int lg_md_run(lg_engine* e, int64_t nsteps) {
     if (!e || nsteps < 0) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
     CUDA_TRY(e, cudaSetDevice(e->opt.device));
     if (e->dirty) return fail(e, LG_ERR_STATE, "no device state: call lg_md_set_state first");
-    bool thermo = false;
-    for (int s = 0; s < e->nsys; s++) {
+    for (int s = 0; s < e->nsys; s++)
         if (!e->sys[s].md_ready) return fail(e, LG_ERR_STATE, "lg_md_setup was not called for every system");
-        if (e->sys[s].tau > 0.0) thermo = true;
-    }
+    const int mode = md_mode(e);
+    const bool thermo = (mode & MD_ADJUST) != 0;
     const int chunk = 16;
     cudaStream_t st = e->stream;
     int64_t done = 0;
     int retries = 0;
+    // Verlet::setup of the systems set up since the last run, from their current state
+    for (int s = 0; s < e->nsys; s++) {
+        HostSystem& h = e->sys[s];
+        if (!h.verlet_setup) continue;
+        launch_verlet_setup(e->b, s, (int)e->begin[s], (int)e->begin[s + 1], st);
+        e->launches += h.n ? 1 : 0;
+        h.verlet_setup = false;
+    }
+    CUDA_TRY(e, cudaGetLastError());
     if (!e->tuned) {
         int rc = autotune(e);
         if (rc) return rc;
@@ -1692,14 +1816,16 @@ int lg_md_run(lg_engine* e, int64_t nsteps) {
     DBuf<double4_32a>& cp_acc = e->cp_acc;
     while (done < nsteps) {
         int steps = (int)std::min<int64_t>(chunk, nsteps - done);
-        if (e->graph_thermo != thermo || !e->graphs.count(steps)) {
-            int rc = build_md_graph(e, steps, thermo);
+        if (e->graph_mode != mode || !e->graphs.count(steps)) {
+            int rc = build_md_graph(e, steps, mode);
             if (rc) return rc;
         }
         size_t bytes = e->b.n * sizeof(double4_32a);
         CUDA_TRY(e, cudaMemcpyAsync(cp_pos.p, e->posq.p, bytes, cudaMemcpyDeviceToDevice, st));
         CUDA_TRY(e, cudaMemcpyAsync(cp_vel.p, e->vel.p, bytes, cudaMemcpyDeviceToDevice, st));
         CUDA_TRY(e, cudaMemcpyAsync(cp_acc.p, e->acc.p, bytes, cudaMemcpyDeviceToDevice, st));
+        const size_t cbytes = (size_t)e->nsys * sizeof(unsigned long long);  // CSVR noise counters
+        if (thermo) CUDA_TRY(e, cudaMemcpyAsync(e->cp_count.p, e->md_count.p, cbytes, cudaMemcpyDeviceToDevice, st));
         CUDA_TRY(e, cudaGraphLaunch(e->graphs[steps], st));
         e->launches += e->graph_nodes[steps];
         uint32_t status;
@@ -1710,6 +1836,8 @@ int lg_md_run(lg_engine* e, int64_t nsteps) {
             CUDA_TRY(e, cudaMemcpyAsync(e->posq.p, cp_pos.p, bytes, cudaMemcpyDeviceToDevice, st));
             CUDA_TRY(e, cudaMemcpyAsync(e->vel.p, cp_vel.p, bytes, cudaMemcpyDeviceToDevice, st));
             CUDA_TRY(e, cudaMemcpyAsync(e->acc.p, cp_acc.p, bytes, cudaMemcpyDeviceToDevice, st));
+            if (thermo)
+                CUDA_TRY(e, cudaMemcpyAsync(e->md_count.p, e->cp_count.p, cbytes, cudaMemcpyDeviceToDevice, st));
             rc = clear_status_bits(e, ST_OVERFLOW);
             if (rc) return rc;
             rc = regrow(e);
@@ -1815,17 +1943,18 @@ int lg_kernel_times(lg_engine* e, int32_t reps, double* ms) {
     cudaEvent_t e0, e1;
     CUDA_TRY(e, cudaEventCreate(&e0));
     CUDA_TRY(e, cudaEventCreate(&e1));
-    bool thermo = false;
-    for (int s = 0; s < e->nsys; s++) thermo = thermo || e->sys[s].tau > 0.0;
-    // save the state: timing must not advance the trajectory
+    const int mode = md_mode(e);
+    // save the state: timing must not advance the trajectory (nor the CSVR noise counters)
     DBuf<double4_32a> sp, sv, sa;
     CUDA_TRY(e, sp.alloc(b.n));
     CUDA_TRY(e, sv.alloc(b.n));
     CUDA_TRY(e, sa.alloc(b.n));
     size_t bytes = (size_t)b.n * sizeof(double4_32a);
+    const size_t cbytes = (size_t)e->nsys * sizeof(unsigned long long);
     CUDA_TRY(e, cudaMemcpyAsync(sp.p, e->posq.p, bytes, cudaMemcpyDeviceToDevice, st));
     CUDA_TRY(e, cudaMemcpyAsync(sv.p, e->vel.p, bytes, cudaMemcpyDeviceToDevice, st));
     CUDA_TRY(e, cudaMemcpyAsync(sa.p, e->acc.p, bytes, cudaMemcpyDeviceToDevice, st));
+    CUDA_TRY(e, cudaMemcpyAsync(e->cp_count.p, e->md_count.p, cbytes, cudaMemcpyDeviceToDevice, st));
     for (int g = 0; g < LG_KT_COUNT; g++) {
         float total = 0.f;
         for (int r = 0; r < reps; r++) {
@@ -1838,11 +1967,11 @@ int lg_kernel_times(lg_engine* e, int32_t reps, double* ms) {
                 case LG_KT_EIKR: launch_kspace_part(b, 0, false, st); break;
                 case LG_KT_RHO: launch_kspace_part(b, 1, false, st); break;
                 case LG_KT_FIELD: launch_kspace_part(b, 2, false, st); break;
-                case LG_KT_VV:  // (the tile kinetic energies may not be current: no scaling here)
-                    launch_vv_first(b, false, st);
-                    launch_vv_second(b, thermo, st);
+                case LG_KT_VV:  // (the chunk sums may not be current: no thermostat here)
+                    launch_md_first(b, false, st);
+                    launch_md_second(b, st);
                     break;
-                case LG_KT_STEP: enqueue_md_step(e, thermo, false, st); break;
+                case LG_KT_STEP: enqueue_md_step(e, mode, false, st); break;
             }
             CUDA_TRY(e, cudaEventRecord(e1, st));
             CUDA_TRY(e, cudaEventSynchronize(e1));
@@ -1860,6 +1989,7 @@ int lg_kernel_times(lg_engine* e, int32_t reps, double* ms) {
     CUDA_TRY(e, cudaGetLastError());
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    CUDA_TRY(e, cudaMemcpyAsync(e->md_count.p, e->cp_count.p, cbytes, cudaMemcpyDeviceToDevice, st));
     // the forces buffer was overwritten by the timing runs: recompute it at the saved state
     launch_request_rebuild(b, st);
     enqueue_forces(e, LG_TERM_ALL, false, st);

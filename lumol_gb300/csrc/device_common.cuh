@@ -13,6 +13,12 @@ constexpr double FRAC_2_SQRT_PI = 1.12837916709551257390;
 constexpr double K_BOLTZMANN = 8.31446284161522e-7;
 constexpr double FOUR_PI_EPSILON_0 = 7.197589831304046;
 
+// Integrators, thermostats and controls of a system's MD (the values of the
+// C ABI's LG_INTEGRATOR_*, LG_THERMOSTAT_* and LG_CONTROL_*).
+constexpr int MD_VELOCITY_VERLET = 0, MD_VERLET = 1, MD_LEAP_FROG = 2;
+constexpr int TH_NONE = 0, TH_BERENDSEN = 1, TH_RESCALE = 2, TH_CSVR = 3;
+constexpr uint32_t CTL_REMOVE_TRANSLATION = 1u, CTL_REWRAP = 2u;
+
 // Pair potential table entry: one PairInteraction (energy/pairs.rs:57-95).
 struct PairDev {
     int32_t type;         // LG_PAIR_*
@@ -68,7 +74,7 @@ struct SysDev {
     double dt;
     double hdt;                   // 0.5 dt (exact)
     double fxscale[3];            // 2^32 / L: fixed-point units per length (mixed path)
-    double thermo_T, thermo_tau;  // Berendsen (tau <= 0: none)
+    double thermo_T, thermo_tau;  // thermostat target and time scale (timesteps)
     double dof;                   // 3 N (DegreesOfFreedom::Particles)
     int32_t tile_begin, tile_end; // this system's tiles of the per-atom MD kernels
     float Lf[3], invLf[3];        // FP32 copies for the list build and the mixed path
@@ -76,28 +82,124 @@ struct SysDev {
     float rlist2_f;               // (rlist + margin)^2 in FP32
     float rebuild2_f;             // 0.99 (skin / 2)^2: FP32 displacement threshold (errs towards rebuilding)
     float coul_rc2_f;
+    // integrators, thermostats and controls beyond Velocity-Verlet + Berendsen
+    // (after the fields the hot kernels read, which keep their offsets)
+    double dt2;                   // dt * dt (Verlet, LeapFrog)
+    double hdt2;                  // 0.5 dt^2 (mixed LeapFrog)
+    double inv_2dt;               // 1 / (2 dt) (mixed Verlet)
+    double thermo_tol;            // RescaleThermostat tolerance
+    double total_mass;            // sum of the masses in atom order (RemoveTranslation)
+    unsigned long long seed;      // CSVR noise
+    int32_t integrator;           // MD_*
+    int32_t thermostat;           // TH_*
+    uint32_t controls;            // CTL_* bits
+    int32_t mol_first, mol_end;   // the system's molecules in the batch molecule table (Rewrap)
 };
 
-// Kinetic energy of one system from its chunk sums ke[begin + q] (chunk q:
-// atoms begin + q * gpw ..., each chunk summed by a warp butterfly): a
-// lane-strided sum over the chunks, then a butterfly over the 32 lanes, so
+// Sum over one system's chunks of a per-chunk value a[stride * (begin + q)]
+// (chunk q: atoms begin + q * gpw ..., each chunk summed by a warp butterfly):
+// a lane-strided sum over the chunks, then a butterfly over the 32 lanes, so
 // every lane gets the same value.  The per-step integrator and the persistent
-// kernel both sum this way (L1 bypassed: the chunks may come from other SMs
-// of the same launch).
-__device__ __forceinline__ double chunk_ke_sum(const SysDev& s, const double* ke, int gpw, int lane) {
+// kernel both sum kinetic energies this way (L1 bypassed: the chunks may come
+// from other SMs of the same launch).
+__device__ __forceinline__ double chunk_sum(const SysDev& s, const double* a, int stride, int gpw, int lane) {
     int nq = (s.end - s.begin + gpw - 1) / gpw;
     double k = 0.0;
-    for (int q = lane; q < nq; q += 32) k += __ldcg(&ke[s.begin + q]);
+    for (int q = lane; q < nq; q += 32) k += __ldcg(&a[(size_t)stride * (s.begin + q)]);
     for (int o = 16; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
     return k;
 }
+__device__ __forceinline__ double chunk_ke_sum(const SysDev& s, const double* ke, int gpw, int lane) {
+    return chunk_sum(s, ke, 1, gpw, lane);
+}
 
-// Berendsen factor sqrt(1 + (T0 / T - 1) / tau) (md/thermostats.rs:113-120),
-// T = 2 K / (dof kB) (sys/compute.rs:133-144); 1 without a thermostat.
+// SplitMix64 stream of the CSVR noise of one thermostat application: the
+// state starts from (seed, count), so every block of a system draws the same
+// numbers without shared state.
+struct NoiseStream {
+    unsigned long long st;
+    __device__ __host__ NoiseStream(unsigned long long seed, unsigned long long count)
+        : st(seed ^ (count * 0xD1B54A32D192ED03ull)) {}
+    __device__ unsigned long long next() {
+        unsigned long long z = (st += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    }
+    // uniform in (0, 1): the top 53 bits plus one half
+    __device__ double uniform() { return ((double)(next() >> 11) + 0.5) * 0x1.0p-53; }
+    // standard normal, Box-Muller (cosine branch)
+    __device__ double normal() {
+        double u1 = uniform(), u2 = uniform();
+        return sqrt(-2.0 * log(u1)) * cos(2.0 * PI * u2);
+    }
+    // Gamma(a, 1) for a >= 1: Marsaglia and Tsang, ACM TOMS 26 (2000) 363-372.
+    // The rejection loop accepts with probability above 0.95 per round; after
+    // 64 rounds (never reached in practice) it returns the mode d.
+    __device__ double gamma(double a) {
+        double d = a - 1.0 / 3.0;
+        double c = 1.0 / sqrt(9.0 * d);
+        for (int it = 0; it < 64; it++) {
+            double x = normal();
+            double v = 1.0 + c * x;
+            if (v <= 0.0) continue;
+            v = v * v * v;
+            double u = uniform();
+            double x2 = x * x;
+            if (u < 1.0 - 0.0331 * x2 * x2) return d * v;
+            if (log(u) < 0.5 * x2 + d * (1.0 - v + log(v))) return d * v;
+        }
+        return d;
+    }
+};
+
+// CSVRThermostat::apply's factor (thermostats.rs:195-210) with the noise of
+// CSVRThermostat::sum_noises (thermostats.rs:166-192) for dof - 1 degrees:
+// one gaussian rr, and 2 Gamma(n / 2) (n even) or 2 Gamma((n - 1) / 2) + rr^2
+// (n odd, the same rr as the reference).
+// (Not inlined: a call keeps the sampler's code and stack out of the MD kernels.)
+static __device__ __noinline__ double csvr_factor(const SysDev& s, double kinetic, unsigned long long count) {
+    double target = K_BOLTZMANN * s.thermo_T / 2.0;  // target_kinetic_per_dof
+    double kinetic_factor = target / kinetic;
+    double exp_1 = exp(-1.0 / s.thermo_tau);
+    double exp_2 = (1.0 - exp_1) * kinetic_factor;
+    long long n = (long long)s.dof - 1;
+    NoiseStream r(s.seed, count);
+    double gauss = 0.0, wiener = 0.0;
+    if (n == 1) {
+        gauss = r.normal();
+        wiener = gauss * gauss;
+    } else if (n > 1) {
+        gauss = r.normal();
+        if (n % 2 == 0) wiener = 2.0 * r.gamma((double)(n / 2));
+        else wiener = 2.0 * r.gamma((double)((n - 1) / 2)) + gauss * gauss;
+    }
+    double scale = exp_1 + exp_2 * (gauss * gauss + wiener) + 2.0 * gauss * sqrt(exp_1 * exp_2);
+    return sqrt(scale);
+}
+
+// Velocity factor of a system's thermostat at kinetic energy k, with
+// T = 2 K / (dof kB) (sys/compute.rs:133-172):
+//   Berendsen  sqrt(1 + (T0 / T - 1) / tau)         (thermostats.rs:112-121)
+//   Rescale    sqrt(T0 / T) when |T - T0| > tol     (thermostats.rs:66-73, velocities.rs:16-22)
+//   CSVR       csvr_factor                          (count: the system's thermostat applications)
 __device__ __forceinline__ double berendsen_factor(const SysDev& s, double k) {
-    if (!(s.thermo_tau > 0.0)) return 1.0;
     double T = 2.0 * k / (s.dof * K_BOLTZMANN);
     return sqrt(1.0 + (s.thermo_T / T - 1.0) / s.thermo_tau);
+}
+__device__ __forceinline__ double thermostat_factor(const SysDev& s, double k, unsigned long long count) {
+    switch (s.thermostat) {
+        case TH_BERENDSEN:
+            return berendsen_factor(s, k);
+        case TH_RESCALE: {
+            double T = 2.0 * k / (s.dof * K_BOLTZMANN);
+            return fabs(T - s.thermo_T) > s.thermo_tol ? sqrt(s.thermo_T / T) : 1.0;
+        }
+        case TH_CSVR:
+            return csvr_factor(s, k, count);
+        default:
+            return 1.0;
+    }
 }
 
 // Sum of a chunk of gpw lanes (gpw a power of two dividing 32), as a butterfly

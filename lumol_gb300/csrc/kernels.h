@@ -17,7 +17,7 @@ struct Batch {
     // state
     double4_32a* posq = nullptr;      // x, y, z (unwrapped, FP64) and charge
     double4_32a* vel = nullptr;       // vx, vy, vz and mass
-    double4_32a* acc = nullptr;       // accelerations (VelocityVerlet::accelerations)
+    double4_32a* acc = nullptr;       // accelerations (VelocityVerlet / LeapFrog), or Verlet's positions at t - dt
     double* force = nullptr;      // 3n, Vector3D layout
     int* kind = nullptr;          // kind index within the system's pair table
     int* mol = nullptr;           // global molecule index
@@ -66,7 +66,11 @@ struct Batch {
     // per-atom MD kernels run on tiles of VV_TILE atoms that never straddle two systems
     int ntiles = 0;
     int2* tiles = nullptr;        // ntiles: (system, first atom)
-    double* kepart = nullptr;     // ntiles: kinetic energy of each tile after the last vv_second
+    double* kepart = nullptr;     // n: kinetic energy of each chunk of 32 / tpa atoms after md_second, at begin + chunk
+    double* mom = nullptr;        // 3n: momentum of each chunk (RemoveTranslation), at 3 (begin + chunk)
+    unsigned long long* md_count = nullptr;  // nsys: thermostat applications so far (the CSVR noise stream)
+    int nmol = 0;                 // molecules of the batch (Rewrap)
+    int* mol_start = nullptr;     // nmol + 1: first atom of each molecule
     // mixed precision
     int tpa = 32;                 // threads per atom of the pair kernels (autotuned)
     int pair_general = 1;         // 0: pair potentials only, no restriction and no Coulomb in the batch
@@ -125,9 +129,11 @@ void launch_unpack_positions(const Batch& b, double* pos3, cudaStream_t st);
 void launch_pack_velocities(const Batch& b, const double* vel3, cudaStream_t st);
 void launch_unpack_velocities(const Batch& b, double* vel3, cudaStream_t st);
 constexpr int VV_TILE = 256;
-void launch_vv_first(const Batch& b, bool apply_thermostat, cudaStream_t st);
-void launch_vv_second(const Batch& b, bool thermostat, cudaStream_t st);
-void launch_thermostat_finalize(const Batch& b, cudaStream_t st);
+void launch_md_first(const Batch& b, bool adjust, cudaStream_t st);
+void launch_md_second(const Batch& b, cudaStream_t st);
+void launch_md_finalize(const Batch& b, cudaStream_t st);
+void launch_rewrap(const Batch& b, cudaStream_t st);
+void launch_verlet_setup(const Batch& b, int s, int begin, int end, cudaStream_t st);
 void launch_request_rebuild(const Batch& b, cudaStream_t st);
 void launch_check_displacement(const Batch& b, cudaStream_t st);
 

@@ -1,13 +1,17 @@
-// md.cu -- Velocity-Verlet (lumol-sim/src/md/integrators.rs:22-70) and the
-// Berendsen thermostat (md/thermostats.rs:91-121) on device-resident state.
+// md.cu -- molecular dynamics on device-resident state: the integrators of
+// lumol-sim/src/md/integrators.rs (VelocityVerlet, Verlet, LeapFrog), the
+// thermostats of md/thermostats.rs (Berendsen, Rescale, CSVR) and the controls
+// RemoveTranslation and Rewrap of md/controls.rs, in the order of
+// MolecularDynamics::propagate (md/molecular_dynamics.rs:66-76).
 //
-// One step is: vv_first (the previous step's Berendsen scaling, half kick,
-// drift, the mixed path's fixed-point positions, neighbour-list displacement
-// test), the force kernels, vv_second (a = F / m, half kick, per-tile kinetic
-// energy).  The per-atom kernels run on tiles of VV_TILE atoms of one system,
-// so per-system quantities (the thermostat factor) need no atomics and are
-// summed in a fixed order.  All launches have fixed shapes, so a run of steps
-// is captured once in a CUDA graph and replayed.
+// One step is: md_first (the previous step's thermostat and controls, the
+// integrator's update before the forces, the mixed path's fixed-point
+// positions, the neighbour-list displacement test), the force kernels,
+// md_second (the integrator's update after the forces, per-chunk kinetic
+// energies and momenta).  The per-atom kernels run on tiles of VV_TILE atoms of
+// one system, so per-system quantities (the thermostat factor) need no atomics
+// and are summed in a fixed order.  All launches have fixed shapes, so a run
+// of steps is captured once in a CUDA graph and replayed.
 #include "kernels.h"
 
 namespace lg {
@@ -72,9 +76,6 @@ void launch_unpack_velocities(const Batch& b, double* vel3, cudaStream_t st) {
     if (b.n) unpack_velocities_kernel<<<(b.n + 255) / 256, 256, 0, st>>>(b.n, b.vel, vel3);
 }
 
-// v += 0.5 dt a; x += v dt (integrators.rs:48-53), then the displacement
-// since the last list build against skin / 2.  Also clears the force buffer
-// that the force kernels accumulate into.
 // Marks system si for a list rebuild.  The flag store is idempotent; the
 // status word gets one atomic per warp, not one per moved atom.
 __device__ __forceinline__ void flag_rebuild(bool moved, int si, uint32_t* status, uint32_t* sys_rebuild) {
@@ -85,24 +86,68 @@ __device__ __forceinline__ void flag_rebuild(bool moved, int si, uint32_t* statu
     }
 }
 
-// The Berendsen factor of a tile's system, computed by its first warp from the
-// chunk kinetic energies of the last vv_second (the same sums in every block
-// of the system, and the same as the persistent kernel's).
-__device__ __forceinline__ void tile_lambda(const SysDev& s, const double* __restrict__ ke, int gpw,
-                                            double* s_lambda) {
+// Squared displacement since the last list build on the plain path: FP32 on
+// the FP64 differences, minimum image.
+__device__ __forceinline__ float plain_displacement2(const SysDev& s, const double4_32a& p, const double4_32a& b) {
+    float dx = (float)(p.x - b.x);
+    float dy = (float)(p.y - b.y);
+    float dz = (float)(p.z - b.z);
+    dx -= rintf(dx * s.invLf[0]) * s.Lf[0];
+    dy -= rintf(dy * s.invLf[1]) * s.Lf[1];
+    dz -= rintf(dz * s.invLf[2]) * s.Lf[2];
+    return dx * dx + dy * dy + dz * dz;
+}
+
+// The previous step's thermostat factor and controls for a tile's system,
+// computed by its first warp from the chunk sums of the last md_second (the
+// same sums in every block of the system, and the same as the persistent
+// kernel's): adj[0] = the velocity factor, adj[1..3] = the centre-of-mass
+// velocity after scaling (RemoveTranslation, controls.rs:29-43), else zero.
+__device__ __forceinline__ void tile_adjust(const SysDev& s, int si, const double* __restrict__ kepart,
+                                            const double* __restrict__ mom,
+                                            const unsigned long long* __restrict__ md_count, int gpw,
+                                            double* adj) {
     if (threadIdx.x < 32) {
-        double f = berendsen_factor(s, chunk_ke_sum(s, ke, gpw, threadIdx.x));
-        if (threadIdx.x == 0) *s_lambda = f;
+        int lane = threadIdx.x;
+        double k = s.thermostat != TH_NONE ? chunk_ke_sum(s, kepart, gpw, lane) : 0.0;
+        double f = thermostat_factor(s, k, md_count[si]);
+        double c[3] = {0.0, 0.0, 0.0};
+        if (s.controls & CTL_REMOVE_TRANSLATION)
+            for (int d = 0; d < 3; d++) c[d] = f * chunk_sum(s, mom + d, 3, gpw, lane) / s.total_mass;
+        if (lane == 0) {
+            adj[0] = f;
+            adj[1] = c[0];
+            adj[2] = c[1];
+            adj[3] = c[2];
+        }
     }
     __syncthreads();
 }
 
-// The Berendsen scaling of step k is applied at the start of step k + 1 (the
-// same products, in the same order, as scaling right after step k), and by
-// thermostat_finalize at the end of a run, which saves two launches a step.
-// vv_first: [v *= lambda]; v += 0.5 dt a; x += v dt (integrators.rs:45-53);
-// the neighbour-list displacement test.  Zeroing the forces is left to the
-// pair kernel, which assigns.
+// v *= factor (the thermostat), then v -= centre-of-mass velocity (RemoveTranslation)
+__device__ __forceinline__ void apply_adjust(const SysDev& s, const double* adj, double4_32a& v) {
+    double f = adj[0];
+    if (s.controls & CTL_REMOVE_TRANSLATION) {
+        v.x = __dsub_rn(__dmul_rn(v.x, f), adj[1]);
+        v.y = __dsub_rn(__dmul_rn(v.y, f), adj[2]);
+        v.z = __dsub_rn(__dmul_rn(v.z, f), adj[3]);
+    } else {
+        v.x *= f;
+        v.y *= f;
+        v.z *= f;
+    }
+}
+
+// The thermostat and controls of step k are applied at the start of step
+// k + 1 (the same products, in the same order, as right after step k), and by
+// md_finalize at the end of a run, which saves two launches a step.
+//
+// md_first: [v *= lambda; v -= v_com]; then the integrator's update before the forces
+//   VelocityVerlet  v += dt/2 a; x += v dt      (integrators.rs:44-53)
+//   LeapFrog        x += v dt + a dt^2 / 2     (integrators.rs:151-157)
+//   Verlet          nothing (its update follows the forces)
+// and the neighbour-list displacement test.  Zeroing the forces is left to
+// the pair kernel, which assigns.
 //
 // Plain path (MIXED = false): products and sums rounded separately, as the
 // reference (no FMA); the displacement test in FP32 on FP64 differences.
@@ -112,51 +157,57 @@ __device__ __forceinline__ void tile_lambda(const SysDev& s, const double* __res
 // displacement test on fixed-point differences against the copy taken at the
 // last build (no FP64 operation).
 template <bool MIXED>
-__global__ void __launch_bounds__(VV_TILE) vv_first_kernel(
+__global__ void __launch_bounds__(VV_TILE) md_first_kernel(
     const int2* __restrict__ tiles, const SysDev* __restrict__ sys, double4_32a* __restrict__ posq,
     double4_32a* __restrict__ vel, const double4_32a* __restrict__ acc, const double4_32a* __restrict__ pos_build,
-    const uint4* __restrict__ pfx_build, const double* __restrict__ kepart, int gpw, int apply_thermostat,
-    const int* __restrict__ perm, uint4* __restrict__ posfx, uint32_t* status, uint32_t* sys_rebuild) {
+    const uint4* __restrict__ pfx_build, const double* __restrict__ kepart, const double* __restrict__ mom,
+    const unsigned long long* __restrict__ md_count, int gpw, int adjust, const int* __restrict__ perm,
+    uint4* __restrict__ posfx, uint32_t* status, uint32_t* sys_rebuild) {
     int2 tile = tiles[blockIdx.x];
     const SysDev& s = sys[tile.x];
-    __shared__ double s_lambda;
-    if (apply_thermostat) tile_lambda(s, kepart, gpw, &s_lambda);
+    __shared__ double adj[4];
+    if (adjust) tile_adjust(s, tile.x, kepart, mom, md_count, gpw, adj);
     int i = tile.y + threadIdx.x;
     if (i >= s.end) return;
     double hdt = s.hdt, dt = s.dt;
     double4_32a v = vel[i], a = acc[i], p = posq[i];
-    if (apply_thermostat) {
-        double f = s_lambda;
-        v.x *= f;
-        v.y *= f;
-        v.z *= f;
+    if (adjust) apply_adjust(s, adj, v);
+    if (s.integrator == MD_VERLET) {  // positions move after the forces
+        vel[i] = v;
+        return;
     }
+    const bool leap = s.integrator == MD_LEAP_FROG;
     float r2;
     if (MIXED) {
-        v.x = fma(hdt, a.x, v.x);
-        v.y = fma(hdt, a.y, v.y);
-        v.z = fma(hdt, a.z, v.z);
-        p.x = fma(v.x, dt, p.x);
-        p.y = fma(v.y, dt, p.y);
-        p.z = fma(v.z, dt, p.z);
+        if (leap) {
+            p.x = fma(v.x, dt, fma(s.hdt2, a.x, p.x));
+            p.y = fma(v.y, dt, fma(s.hdt2, a.y, p.y));
+            p.z = fma(v.z, dt, fma(s.hdt2, a.z, p.z));
+        } else {
+            v.x = fma(hdt, a.x, v.x);
+            v.y = fma(hdt, a.y, v.y);
+            v.z = fma(hdt, a.z, v.z);
+            p.x = fma(v.x, dt, p.x);
+            p.y = fma(v.y, dt, p.y);
+            p.z = fma(v.z, dt, p.z);
+        }
         uint4 u = fixed_position(s, p);
         posfx[perm[i]] = u;  // a rebuild this step rewrites it in the new order
         r2 = fixed_dist2(u, pfx_build[i], s.Lq);  // as the persistent kernel
     } else {
-        v.x = __dadd_rn(v.x, __dmul_rn(hdt, a.x));
-        v.y = __dadd_rn(v.y, __dmul_rn(hdt, a.y));
-        v.z = __dadd_rn(v.z, __dmul_rn(hdt, a.z));
-        p.x = __dadd_rn(p.x, __dmul_rn(v.x, dt));
-        p.y = __dadd_rn(p.y, __dmul_rn(v.y, dt));
-        p.z = __dadd_rn(p.z, __dmul_rn(v.z, dt));
-        double4_32a b = pos_build[i];
-        float dx = (float)(p.x - b.x);
-        float dy = (float)(p.y - b.y);
-        float dz = (float)(p.z - b.z);
-        dx -= rintf(dx * s.invLf[0]) * s.Lf[0];
-        dy -= rintf(dy * s.invLf[1]) * s.Lf[1];
-        dz -= rintf(dz * s.invLf[2]) * s.Lf[2];
-        r2 = dx * dx + dy * dy + dz * dz;
+        if (leap) {  // (v dt) + ((0.5 a) dt^2)
+            p.x = __dadd_rn(p.x, __dadd_rn(__dmul_rn(v.x, dt), __dmul_rn(__dmul_rn(0.5, a.x), s.dt2)));
+            p.y = __dadd_rn(p.y, __dadd_rn(__dmul_rn(v.y, dt), __dmul_rn(__dmul_rn(0.5, a.y), s.dt2)));
+            p.z = __dadd_rn(p.z, __dadd_rn(__dmul_rn(v.z, dt), __dmul_rn(__dmul_rn(0.5, a.z), s.dt2)));
+        } else {
+            v.x = __dadd_rn(v.x, __dmul_rn(hdt, a.x));
+            v.y = __dadd_rn(v.y, __dmul_rn(hdt, a.y));
+            v.z = __dadd_rn(v.z, __dmul_rn(hdt, a.z));
+            p.x = __dadd_rn(p.x, __dmul_rn(v.x, dt));
+            p.y = __dadd_rn(p.y, __dmul_rn(v.y, dt));
+            p.z = __dadd_rn(p.z, __dmul_rn(v.z, dt));
+        }
+        r2 = plain_displacement2(s, p, pos_build[i]);
         if (posfx) posfx[i] = fixed_position(s, p);  // atom order: the half-list kernel's FP32 classification
     }
     vel[i] = v;
@@ -166,69 +217,197 @@ __global__ void __launch_bounds__(VV_TILE) vv_first_kernel(
     flag_rebuild(r2 > s.rebuild2_f, tile.x, status, sys_rebuild);
 }
 
-// a = F / m; v += 0.5 dt a (integrators.rs:55-68); with a thermostat, the
-// kinetic energies of the system's chunks of gpw atoms for the next step's
-// factor (tiles start at their system's first atom in steps of VV_TILE, so a
-// warp holds 32 / gpw whole chunks).
-// Plain path: the reference's division and unfused products; mixed path:
-// a = F * (1 / m) in FP32 (the force is an FP32 value) and fused multiply-adds
-// on the FP64 velocity.
+// md_second: the integrator's update after the forces
+//   VelocityVerlet  a = F / m; v += dt/2 a                          (integrators.rs:55-68)
+//   LeapFrog        a' = F / m; v += (a + a') dt / 2; a = a'        (integrators.rs:159-167)
+//   Verlet          x' = 2 x - x_prev + dt^2 / m F; v = (x' - x_prev) / (2 dt);
+//                   x_prev = x (held in the acceleration slot)      (integrators.rs:106-122)
+// (a Verlet system then writes its fixed-point copy and runs the displacement
+// test); with a thermostat, the kinetic energies of the system's chunks of gpw
+// atoms, with RemoveTranslation their momenta, for the next step's factors
+// (tiles start at their system's first atom in steps of VV_TILE, so a warp
+// holds 32 / gpw whole chunks).  Plain path: the reference's divisions and
+// unfused products; mixed path: a = F * (1 / m) in FP32 (the force is an FP32
+// value) and fused multiply-adds on the FP64 state.
 template <bool MIXED>
-__global__ void __launch_bounds__(VV_TILE) vv_second_kernel(
+__global__ void __launch_bounds__(VV_TILE) md_second_kernel(
     const int2* __restrict__ tiles, const SysDev* __restrict__ sys, const double* __restrict__ force,
-    const float* __restrict__ inv_mass, double4_32a* __restrict__ vel, double4_32a* __restrict__ acc,
-    double* __restrict__ kepart, int gpw, int thermostat) {
+    const float* __restrict__ inv_mass, double4_32a* __restrict__ posq, double4_32a* __restrict__ vel,
+    double4_32a* __restrict__ acc, const double4_32a* __restrict__ pos_build, const uint4* __restrict__ pfx_build,
+    double* __restrict__ kepart, double* __restrict__ mom, unsigned long long* __restrict__ md_count, int gpw,
+    const int* __restrict__ perm, uint4* __restrict__ posfx, uint32_t* status, uint32_t* sys_rebuild) {
     int2 tile = tiles[blockIdx.x];
     const SysDev& s = sys[tile.x];
     int i = tile.y + threadIdx.x;
-    double ke = 0.0;
+    double ke = 0.0, mx = 0.0, my = 0.0, mz = 0.0;
     if (i < s.end) {
         double hdt = s.hdt;
         double4_32a v = vel[i];
         double m = v.w;
-        double4_32a a;
+        double4_32a an;  // F / m
         if (MIXED) {  // the force is an FP32 value (the compensated sum, rounded once): a = F / m in FP32
             float im = inv_mass[i];
-            a = make_double4_32a((double)__fmul_rn((float)force[3 * i], im),
-                                 (double)__fmul_rn((float)force[3 * i + 1], im),
-                                 (double)__fmul_rn((float)force[3 * i + 2], im), 0.0);
-            v.x = fma(hdt, a.x, v.x);
-            v.y = fma(hdt, a.y, v.y);
-            v.z = fma(hdt, a.z, v.z);
-            if (thermostat) ke = 0.5 * m * fma(v.x, v.x, fma(v.y, v.y, v.z * v.z));
-        } else {  // the reference's force / mass
-            a = make_double4_32a(force[3 * i] / m, force[3 * i + 1] / m, force[3 * i + 2] / m, 0.0);
-            v.x = __dadd_rn(v.x, __dmul_rn(hdt, a.x));
-            v.y = __dadd_rn(v.y, __dmul_rn(hdt, a.y));
-            v.z = __dadd_rn(v.z, __dmul_rn(hdt, a.z));
-            if (thermostat) ke = 0.5 * m * (v.x * v.x + v.y * v.y + v.z * v.z);
+            an = make_double4_32a((double)__fmul_rn((float)force[3 * i], im),
+                                  (double)__fmul_rn((float)force[3 * i + 1], im),
+                                  (double)__fmul_rn((float)force[3 * i + 2], im), 0.0);
+        } else {
+            an = make_double4_32a(force[3 * i] / m, force[3 * i + 1] / m, force[3 * i + 2] / m, 0.0);
         }
-        acc[i] = a;
+        if (s.integrator == MD_VERLET) {
+            double4_32a p = posq[i], prev = acc[i], x = p;
+            if (MIXED) {
+                x.x = fma(s.dt2, an.x, 2.0 * p.x - prev.x);
+                x.y = fma(s.dt2, an.y, 2.0 * p.y - prev.y);
+                x.z = fma(s.dt2, an.z, 2.0 * p.z - prev.z);
+                v.x = (x.x - prev.x) * s.inv_2dt;
+                v.y = (x.y - prev.y) * s.inv_2dt;
+                v.z = (x.z - prev.z) * s.inv_2dt;
+            } else {  // (2 x - x_prev) + (dt^2 / m) F;  (x' - x_prev) / (2 dt)
+                double c = __ddiv_rn(s.dt2, m), two_dt = __dmul_rn(2.0, s.dt);
+                x.x = __dadd_rn(__dsub_rn(__dmul_rn(2.0, p.x), prev.x), __dmul_rn(c, force[3 * i]));
+                x.y = __dadd_rn(__dsub_rn(__dmul_rn(2.0, p.y), prev.y), __dmul_rn(c, force[3 * i + 1]));
+                x.z = __dadd_rn(__dsub_rn(__dmul_rn(2.0, p.z), prev.z), __dmul_rn(c, force[3 * i + 2]));
+                v.x = __ddiv_rn(__dsub_rn(x.x, prev.x), two_dt);
+                v.y = __ddiv_rn(__dsub_rn(x.y, prev.y), two_dt);
+                v.z = __ddiv_rn(__dsub_rn(x.z, prev.z), two_dt);
+            }
+            acc[i] = make_double4_32a(p.x, p.y, p.z, 0.0);
+            posq[i] = x;
+            float r2;
+            if (MIXED) {
+                uint4 u = fixed_position(s, x);
+                posfx[perm[i]] = u;
+                r2 = fixed_dist2(u, pfx_build[i], s.Lq);
+            } else {
+                r2 = plain_displacement2(s, x, pos_build[i]);
+                if (posfx) posfx[i] = fixed_position(s, x);
+            }
+            flag_rebuild(r2 > s.rebuild2_f, tile.x, status, sys_rebuild);
+        } else if (s.integrator == MD_LEAP_FROG) {
+            double4_32a a = acc[i];
+            if (MIXED) {
+                v.x = fma(hdt, a.x + an.x, v.x);
+                v.y = fma(hdt, a.y + an.y, v.y);
+                v.z = fma(hdt, a.z + an.z, v.z);
+            } else {  // v + (0.5 (a + a')) dt
+                v.x = __dadd_rn(v.x, __dmul_rn(__dmul_rn(0.5, __dadd_rn(a.x, an.x)), s.dt));
+                v.y = __dadd_rn(v.y, __dmul_rn(__dmul_rn(0.5, __dadd_rn(a.y, an.y)), s.dt));
+                v.z = __dadd_rn(v.z, __dmul_rn(__dmul_rn(0.5, __dadd_rn(a.z, an.z)), s.dt));
+            }
+            acc[i] = an;
+        } else {
+            if (MIXED) {
+                v.x = fma(hdt, an.x, v.x);
+                v.y = fma(hdt, an.y, v.y);
+                v.z = fma(hdt, an.z, v.z);
+            } else {
+                v.x = __dadd_rn(v.x, __dmul_rn(hdt, an.x));
+                v.y = __dadd_rn(v.y, __dmul_rn(hdt, an.y));
+                v.z = __dadd_rn(v.z, __dmul_rn(hdt, an.z));
+            }
+            acc[i] = an;
+        }
         vel[i] = v;
+        if (s.thermostat != TH_NONE)
+            ke = MIXED ? 0.5 * m * fma(v.x, v.x, fma(v.y, v.y, v.z * v.z))
+                       : 0.5 * m * (v.x * v.x + v.y * v.y + v.z * v.z);
+        if (s.controls & CTL_REMOVE_TRANSLATION) {
+            mx = m * v.x;
+            my = m * v.y;
+            mz = m * v.z;
+        }
     }
-    if (thermostat) {
+    // per-system conditions: every lane of a block belongs to the tile's system
+    const bool head = threadIdx.x % gpw == 0 && i < s.end;
+    const size_t q = (size_t)s.begin + (i - s.begin) / gpw;
+    if (s.thermostat != TH_NONE) {
         ke = chunk_butterfly(ke, gpw);
-        if (threadIdx.x % gpw == 0 && i < s.end) kepart[s.begin + (i - s.begin) / gpw] = ke;
+        if (head) kepart[q] = ke;
+    }
+    if (s.controls & CTL_REMOVE_TRANSLATION) {
+        mx = chunk_butterfly(mx, gpw);
+        my = chunk_butterfly(my, gpw);
+        mz = chunk_butterfly(mz, gpw);
+        if (head) {
+            mom[3 * q] = mx;
+            mom[3 * q + 1] = my;
+            mom[3 * q + 2] = mz;
+        }
+    }
+    // the CSVR noise stream of the next thermostat application
+    if (s.thermostat == TH_CSVR && threadIdx.x == 0 && tile.y == s.begin) md_count[tile.x] += 1ull;
+}
+
+// The pending thermostat and controls at the end of a run.
+__global__ void __launch_bounds__(VV_TILE) md_finalize_kernel(const int2* __restrict__ tiles,
+                                                              const SysDev* __restrict__ sys,
+                                                              const double* __restrict__ kepart,
+                                                              const double* __restrict__ mom,
+                                                              const unsigned long long* __restrict__ md_count,
+                                                              int gpw, double4_32a* __restrict__ vel) {
+    int2 tile = tiles[blockIdx.x];
+    const SysDev& s = sys[tile.x];
+    __shared__ double adj[4];
+    tile_adjust(s, tile.x, kepart, mom, md_count, gpw, adj);
+    int i = tile.y + threadIdx.x;
+    if (i >= s.end) return;
+    double4_32a v = vel[i];
+    apply_adjust(s, adj, v);
+    vel[i] = v;
+}
+
+// Rewrap (controls.rs:80-89): each molecule of a system with the control is
+// moved by the wrapped centre of mass minus the centre of mass
+// (Molecule::wrap, sys/config/molecules.rs:287-296; center_of_mass :256-264;
+// UnitCell::wrap_vector, cells.rs:263-270), one thread per molecule, in the
+// reference's order of operations.  The fixed-point copies follow.
+__global__ void rewrap_kernel(int nmol, const int* __restrict__ mol_start, const int* __restrict__ sysid,
+                              const SysDev* __restrict__ sys, double4_32a* __restrict__ posq,
+                              const double4_32a* __restrict__ vel, const int* __restrict__ perm,
+                              uint4* __restrict__ posfx) {
+    int mi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (mi >= nmol) return;
+    int a0 = mol_start[mi], a1 = mol_start[mi + 1];
+    if (a1 <= a0) return;
+    const SysDev& s = sys[sysid[a0]];
+    if (!(s.controls & CTL_REWRAP)) return;
+    double total = 0.0, c[3] = {0.0, 0.0, 0.0};
+    for (int a = a0; a < a1; a++) {
+        double m = vel[a].w;
+        double4_32a p = posq[a];
+        total = __dadd_rn(total, m);
+        c[0] = __dadd_rn(c[0], __dmul_rn(m, p.x));
+        c[1] = __dadd_rn(c[1], __dmul_rn(m, p.y));
+        c[2] = __dadd_rn(c[2], __dmul_rn(m, p.z));
+    }
+    double delta[3];
+    for (int d = 0; d < 3; d++) {
+        double com = __ddiv_rn(c[d], total);
+        double wrapped = __dsub_rn(com, __dmul_rn(floor(__ddiv_rn(com, s.L[d])), s.L[d]));
+        delta[d] = __dsub_rn(wrapped, com);
+    }
+    if (delta[0] == 0.0 && delta[1] == 0.0 && delta[2] == 0.0) return;
+    for (int a = a0; a < a1; a++) {
+        double4_32a p = posq[a];
+        p.x = __dadd_rn(p.x, delta[0]);
+        p.y = __dadd_rn(p.y, delta[1]);
+        p.z = __dadd_rn(p.z, delta[2]);
+        posq[a] = p;
+        if (perm) posfx[perm[a]] = fixed_position(s, p);
+        else if (posfx) posfx[a] = fixed_position(s, p);
     }
 }
 
-// The pending Berendsen scaling at the end of a run.
-__global__ void __launch_bounds__(VV_TILE) thermostat_finalize_kernel(const int2* __restrict__ tiles,
-                                                                     const SysDev* __restrict__ sys,
-                                                                     const double* __restrict__ kepart, int gpw,
-                                                                     double4_32a* __restrict__ vel) {
-    int2 tile = tiles[blockIdx.x];
-    const SysDev& s = sys[tile.x];
-    __shared__ double s_lambda;
-    tile_lambda(s, kepart, gpw, &s_lambda);
-    int i = tile.y + threadIdx.x;
-    if (i >= s.end) return;
-    double f = s_lambda;
-    double4_32a v = vel[i];
-    v.x *= f;
-    v.y *= f;
-    v.z *= f;
-    vel[i] = v;
+// Verlet::setup (integrators.rs:92-104): x_prev = x - v dt, in the acceleration slot.
+__global__ void verlet_setup_kernel(int begin, int end, const SysDev* __restrict__ sys, int si,
+                                    const double4_32a* __restrict__ posq, const double4_32a* __restrict__ vel,
+                                    double4_32a* __restrict__ acc) {
+    int i = begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= end) return;
+    double dt = sys[si].dt;
+    double4_32a p = posq[i], v = vel[i];
+    acc[i] = make_double4_32a(__dsub_rn(p.x, __dmul_rn(v.x, dt)), __dsub_rn(p.y, __dmul_rn(v.y, dt)),
+                              __dsub_rn(p.z, __dmul_rn(v.z, dt)), 0.0);
 }
 
 // Displacement test alone, for positions set from the host.
@@ -259,33 +438,45 @@ __global__ void request_rebuild_kernel(int nsys, uint32_t* status, uint32_t* sys
     if (threadIdx.x == 0) atomicOr(status, ST_REBUILD);
 }
 
-void launch_vv_first(const Batch& b, bool apply_thermostat, cudaStream_t st) {
+void launch_md_first(const Batch& b, bool adjust, cudaStream_t st) {
     if (!b.ntiles) return;
-    int th = apply_thermostat ? 1 : 0;
+    int aj = adjust ? 1 : 0, gpw = 32 / b.tpa;
     if (b.precision == 1)
-        vv_first_kernel<true><<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.posq, b.vel, b.acc, b.pos_build,
-                                                            b.pfx_build, b.kepart, 32 / b.tpa, th, b.perm, b.posfx,
-                                                            b.status,
-                                                            b.sys_rebuild);
+        md_first_kernel<true><<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.posq, b.vel, b.acc, b.pos_build,
+                                                            b.pfx_build, b.kepart, b.mom, b.md_count, gpw, aj,
+                                                            b.perm, b.posfx, b.status, b.sys_rebuild);
     else
-        vv_first_kernel<false><<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.posq, b.vel, b.acc, b.pos_build,
-                                                             nullptr, b.kepart, 32 / b.tpa, th, nullptr, b.posfx,
-                                                             b.status,
+        md_first_kernel<false><<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.posq, b.vel, b.acc, b.pos_build,
+                                                             nullptr, b.kepart, b.mom, b.md_count, gpw, aj,
+                                                             nullptr, b.posfx, b.status, b.sys_rebuild);
+}
+void launch_md_second(const Batch& b, cudaStream_t st) {
+    if (!b.ntiles) return;
+    int gpw = 32 / b.tpa;
+    if (b.precision == 1)
+        md_second_kernel<true><<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.force, b.inv_mass, b.posq, b.vel,
+                                                             b.acc, b.pos_build, b.pfx_build, b.kepart, b.mom,
+                                                             b.md_count, gpw, b.perm, b.posfx, b.status,
                                                              b.sys_rebuild);
-}
-void launch_vv_second(const Batch& b, bool thermostat, cudaStream_t st) {
-    if (!b.ntiles) return;
-    int th = thermostat ? 1 : 0;
-    if (b.precision == 1)
-        vv_second_kernel<true><<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.force, b.inv_mass, b.vel, b.acc,
-                                                             b.kepart, 32 / b.tpa, th);
     else
-        vv_second_kernel<false><<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.force, nullptr, b.vel, b.acc,
-                                                              b.kepart, 32 / b.tpa, th);
+        md_second_kernel<false><<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.force, nullptr, b.posq, b.vel,
+                                                              b.acc, b.pos_build, nullptr, b.kepart, b.mom,
+                                                              b.md_count, gpw, nullptr, b.posfx, b.status,
+                                                              b.sys_rebuild);
 }
-void launch_thermostat_finalize(const Batch& b, cudaStream_t st) {
-    if (b.ntiles) thermostat_finalize_kernel<<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.kepart, 32 / b.tpa,
-                                                                          b.vel);
+void launch_md_finalize(const Batch& b, cudaStream_t st) {
+    if (b.ntiles)
+        md_finalize_kernel<<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.kepart, b.mom, b.md_count, 32 / b.tpa,
+                                                         b.vel);
+}
+void launch_rewrap(const Batch& b, cudaStream_t st) {
+    if (b.nmol)
+        rewrap_kernel<<<(b.nmol + 127) / 128, 128, 0, st>>>(b.nmol, b.mol_start, b.sysid, b.sys, b.posq, b.vel,
+                                                            b.precision == 1 ? b.perm : nullptr, b.posfx);
+}
+void launch_verlet_setup(const Batch& b, int s, int begin, int end, cudaStream_t st) {
+    if (end > begin)
+        verlet_setup_kernel<<<(end - begin + 255) / 256, 256, 0, st>>>(begin, end, b.sys, s, b.posq, b.vel, b.acc);
 }
 void launch_request_rebuild(const Batch& b, cudaStream_t st) {
     request_rebuild_kernel<<<1, 256, 0, st>>>(b.nsys, b.status, b.sys_rebuild);

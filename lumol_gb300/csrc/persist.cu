@@ -54,7 +54,9 @@ __device__ __forceinline__ void pk_lambdas(const Batch& b, const PkArgs& a, cons
                                            int lane, int gpw, double* s_lambda) {
     for (int r = wib; r < G; r += PK_WARPS) {
         const SysDev& sd = b.sys[s_sys[r]];
-        double f = berendsen_factor(sd, chunk_ke_sum(sd, a.ke, gpw, lane));
+        // (a persistent batch has Berendsen thermostats or none: thermostat_factor's arithmetic)
+        double k = chunk_ke_sum(sd, a.ke, gpw, lane);
+        double f = sd.thermostat == TH_BERENDSEN ? berendsen_factor(sd, k) : 1.0;
         if (lane == 0) s_lambda[r] = f;
     }
 }

@@ -614,36 +614,119 @@ class System:
 # ---------------------------------------------------------------------------
 @dataclass
 class VelocityVerlet:
-    """VelocityVerlet::new(timestep) (md/integrators.rs:22-70)."""
+    """VelocityVerlet::new(timestep) (md/integrators.rs:19-70)."""
     timestep: float
+    _kind = C.LG_INTEGRATOR_VELOCITY_VERLET
+
+
+@dataclass
+class Verlet:
+    """Verlet::new(timestep) (md/integrators.rs:72-123): keeps the positions at
+    t - dt, taken as x - v dt at setup."""
+    timestep: float
+    _kind = C.LG_INTEGRATOR_VERLET
+
+
+@dataclass
+class LeapFrog:
+    """LeapFrog::new(timestep) (md/integrators.rs:125-169)."""
+    timestep: float
+    _kind = C.LG_INTEGRATOR_LEAP_FROG
+
+
+def _check_temperature(temperature: float) -> None:
+    if temperature < 0.0:
+        raise ValueError("The temperature must be positive in thermostats.")
 
 
 @dataclass
 class BerendsenThermostat:
-    """BerendsenThermostat::new(temperature, tau) (md/thermostats.rs:91-121)."""
+    """BerendsenThermostat::new(temperature, tau) (md/thermostats.rs:77-121)."""
     temperature: float
     tau: float
 
     def __post_init__(self):
-        if self.temperature < 0.0:
-            raise ValueError("The temperature must be positive in thermostats.")
+        _check_temperature(self.temperature)
         if self.tau < 1.0:
             raise ValueError("The timestep must be larger than 1 in berendsen thermostat.")
+
+    def _params(self, p) -> None:
+        p.thermostat, p.temperature, p.tau = C.LG_THERMOSTAT_BERENDSEN, self.temperature, self.tau
+
+
+@dataclass
+class RescaleThermostat:
+    """RescaleThermostat::new(temperature) / with_tolerance(temperature, tol)
+    (md/thermostats.rs:27-73): velocities rescaled to `temperature` when the
+    instant temperature is further than `tolerance` from it (default 5 %)."""
+    temperature: float
+    tolerance: float | None = None
+
+    def __post_init__(self):
+        _check_temperature(self.temperature)
+        if self.tolerance is None:
+            self.tolerance = 0.05 * self.temperature
+
+    def _params(self, p) -> None:
+        p.thermostat, p.temperature, p.tolerance = C.LG_THERMOSTAT_RESCALE, self.temperature, self.tolerance
+
+
+@dataclass
+class CSVRThermostat:
+    """CSVRThermostat::new(temperature, tau) (md/thermostats.rs:123-210).  The
+    noise comes from SplitMix64 streams of (seed, application count) instead of
+    the reference's xorshift generator: the same distribution, other numbers."""
+    temperature: float
+    tau: float
+    seed: int = 0
+
+    def __post_init__(self):
+        _check_temperature(self.temperature)
+        if self.tau < 1.0:
+            raise ValueError("The timestep must be larger than 1 in CSVR thermostat.")
+
+    def _params(self, p) -> None:
+        p.thermostat, p.temperature, p.tau = C.LG_THERMOSTAT_CSVR, self.temperature, self.tau
+        p.seed = self.seed & (2 ** 64 - 1)
+
+
+class RemoveTranslation:
+    """RemoveTranslation control (md/controls.rs:26-43)."""
+    _bit = C.LG_CONTROL_REMOVE_TRANSLATION
+
+
+class Rewrap:
+    """Rewrap control (md/controls.rs:73-89): molecules' centres of mass back into the cell."""
+    _bit = C.LG_CONTROL_REWRAP
+
+
+def md_params(integrator, thermostat=None, controls=()) -> "C.LgMdParams":
+    """The C ABI's lg_md_params for an integrator, an optional thermostat and controls."""
+    p = C.LgMdParams()
+    p.integrator = integrator._kind
+    p.timestep = integrator.timestep
+    if thermostat is not None:
+        thermostat._params(p)
+    for c in controls:
+        p.controls |= c._bit
+    return p
 
 
 @dataclass
 class MolecularDynamics:
     """MolecularDynamics propagator (md/molecular_dynamics.rs:11-83): integrate,
-    then thermostat, every step, with the state resident on the GPU."""
-    integrator: VelocityVerlet
-    thermostat: BerendsenThermostat | None = None
+    then thermostat, then controls, every step, with the state resident on the GPU."""
+    integrator: VelocityVerlet | Verlet | LeapFrog
+    thermostat: BerendsenThermostat | RescaleThermostat | CSVRThermostat | None = None
+    controls: tuple = ()
     _ready: bool = field(default=False, repr=False)
 
     def setup(self, system: System) -> None:
-        """Propagator::setup -> VelocityVerlet::setup: accelerations := 0."""
+        """Propagator::setup: the integrator's setup (accelerations := 0, or
+        Verlet's positions at t - dt) at the first run."""
         eng = system.engine()
-        T0, tau = (self.thermostat.temperature, self.thermostat.tau) if self.thermostat else (0.0, 0.0)
-        eng.call("lg_md_setup", 0, self.integrator.timestep, T0, tau)
+        p = md_params(self.integrator, self.thermostat, self.controls)
+        eng.call("lg_md_setup_ex", 0, ctypes.byref(p))
         if system.velocities is None:
             system.velocities = np.zeros((system.size, 3))
         pos = np.ascontiguousarray(system.positions)

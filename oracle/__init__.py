@@ -94,6 +94,10 @@ def load() -> ctypes.CDLL:
         lib.orc_pairset.argtypes = [P, ctypes.c_int, V, ctypes.c_int64]
         lib.orc_velocity_verlet.argtypes = [P, V, V, V, ctypes.c_double, ctypes.c_int64, ctypes.c_double,
                                             ctypes.c_double]
+        lib.orc_md_run.argtypes = [P, V, V, V, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_double,
+                                   ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
+                                   ctypes.POINTER(ctypes.c_uint64), ctypes.c_uint32, ctypes.c_int64]
+        lib.orc_verlet_setup.argtypes = [P, V, V, ctypes.c_double, V]
         lib.orc_temperature.restype = ctypes.c_double
         lib.orc_temperature.argtypes = [P, V]
         lib.orc_kinetic_energy.restype = ctypes.c_double
@@ -230,6 +234,29 @@ class Oracle:
         acc = np.ascontiguousarray(acc, dtype=np.float64).copy()
         self.lib.orc_velocity_verlet(self.h, _ptr(pos), _ptr(vel), _ptr(acc), dt, nsteps, temperature, tau)
         return pos, vel, acc
+
+    def md_run(self, pos, vel, state, nsteps, integrator=0, dt=1.0, thermostat=0, temperature=0.0, tau=0.0,
+               tolerance=0.0, seed=0, count=0, controls=0):
+        """MolecularDynamics::propagate for `nsteps` steps (see orc_md_run);
+        returns (positions, velocities, state, count)."""
+        pos = np.ascontiguousarray(pos, dtype=np.float64).copy()
+        vel = np.ascontiguousarray(vel, dtype=np.float64).copy()
+        state = np.ascontiguousarray(state, dtype=np.float64).copy()
+        c = ctypes.c_uint64(count)
+        self.lib.orc_md_run(self.h, _ptr(pos), _ptr(vel), _ptr(state), integrator, dt, thermostat, temperature,
+                            tau, tolerance, seed & (2 ** 64 - 1), ctypes.byref(c), controls, nsteps)
+        return pos, vel, state, c.value
+
+    def verlet_setup(self, pos, vel, dt) -> np.ndarray:
+        pos = np.ascontiguousarray(pos, dtype=np.float64)
+        vel = np.ascontiguousarray(vel, dtype=np.float64)
+        prev = np.zeros_like(pos)
+        self.lib.orc_verlet_setup(self.h, _ptr(pos), _ptr(vel), dt, _ptr(prev))
+        return prev
+
+    def kinetic_energy(self, vel) -> float:
+        vel = np.ascontiguousarray(vel, dtype=np.float64)
+        return self.lib.orc_kinetic_energy(self.h, _ptr(vel))
 
     def temperature(self, vel) -> float:
         vel = np.ascontiguousarray(vel, dtype=np.float64)

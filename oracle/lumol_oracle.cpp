@@ -1260,6 +1260,160 @@ void orc_velocity_verlet(orc_system* s, double* x, double* v, double* a, double 
     }
 }
 
+// ---- integrators, thermostats and controls ------------------------------------
+
+// The CSVR noise stream of one thermostat application: SplitMix64 from
+// (seed, count), uniforms from the top 53 bits, Box-Muller normals (cosine
+// branch), Gamma(a >= 1) by Marsaglia and Tsang (ACM TOMS 26 (2000) 363-372).
+// The engine draws the same numbers; the reference draws from rand_xorshift /
+// rand_distr (third-party, not restated), so only the distribution matches it.
+struct Noise {
+    uint64_t st;
+    Noise(uint64_t seed, uint64_t count) : st(seed ^ (count * 0xD1B54A32D192ED03ull)) {}
+    uint64_t next() {
+        uint64_t z = (st += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    }
+    double uniform() { return ((double)(next() >> 11) + 0.5) * 0x1.0p-53; }
+    double normal() {
+        double u1 = uniform(), u2 = uniform();
+        return std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * PI * u2);
+    }
+    double gamma(double a) {
+        double d = a - 1.0 / 3.0;
+        double c = 1.0 / std::sqrt(9.0 * d);
+        for (int it = 0; it < 64; it++) {
+            double x = normal();
+            double v = 1.0 + c * x;
+            if (v <= 0.0) continue;
+            v = v * v * v;
+            double u = uniform();
+            double x2 = x * x;
+            if (u < 1.0 - 0.0331 * x2 * x2) return d * v;
+            if (std::log(u) < 0.5 * x2 + d * (1.0 - v + std::log(v))) return d * v;
+        }
+        return d;
+    }
+};
+
+// Verlet::setup (integrators.rs:92-104): x_prev = x - v dt
+void orc_verlet_setup(const orc_system* s, const double* x, const double* v, double dt, double* prev) {
+    for (int64_t i = 0; i < 3 * s->n; i++) prev[i] = x[i] - v[i] * dt;
+}
+
+// MolecularDynamics::propagate (md/molecular_dynamics.rs:66-76): integrate,
+// thermostat, controls, `nsteps` times.
+void orc_md_run(orc_system* s, double* x, double* v, double* state, int integrator, double dt, int thermostat,
+                double T0, double tau, double tol, uint64_t seed, uint64_t* count, uint32_t controls,
+                int64_t nsteps) {
+    int64_t n = s->n;
+    std::vector<double> f(3 * n);
+    const double dt2 = dt * dt;
+    auto forces = [&]() {
+        orc_set_positions(s, x);
+        std::fill(f.begin(), f.end(), 0.0);
+        orc_forces(s, ORC_TERM_ALL, f.data());
+    };
+    for (int64_t step = 0; step < nsteps; step++) {
+        if (integrator == 0) {  // VelocityVerlet::integrate (integrators.rs:44-69)
+            double* a = state;
+            for (int64_t i = 0; i < 3 * n; i++) {
+                v[i] += 0.5 * dt * a[i];
+                x[i] += v[i] * dt;
+            }
+            forces();
+            for (int64_t i = 0; i < n; i++)
+                for (int k = 0; k < 3; k++) a[3 * i + k] = f[3 * i + k] / s->mass[i];
+            for (int64_t i = 0; i < 3 * n; i++) v[i] += 0.5 * dt * a[i];
+        } else if (integrator == 1) {  // Verlet::integrate (integrators.rs:106-122)
+            double* prev = state;
+            forces();
+            for (int64_t i = 0; i < n; i++)
+                for (int k = 0; k < 3; k++) {
+                    int64_t c = 3 * i + k;
+                    double tmp = x[c];
+                    x[c] = 2.0 * x[c] - prev[c] + dt2 / s->mass[i] * f[c];
+                    v[c] = (x[c] - prev[c]) / (2.0 * dt);
+                    prev[c] = tmp;
+                }
+        } else {  // LeapFrog::integrate (integrators.rs:151-168)
+            double* a = state;
+            for (int64_t i = 0; i < 3 * n; i++) x[i] += v[i] * dt + 0.5 * a[i] * dt2;
+            forces();
+            for (int64_t i = 0; i < n; i++)
+                for (int k = 0; k < 3; k++) {
+                    int64_t c = 3 * i + k;
+                    double an = f[c] / s->mass[i];
+                    v[c] += 0.5 * (a[c] + an) * dt;
+                    a[c] = an;
+                }
+        }
+        // Thermostat::apply (thermostats.rs:66-73, 112-121, 195-210)
+        if (thermostat == 1) {
+            double T = orc_temperature(s, v);
+            double factor = std::sqrt(1.0 + (T0 / T - 1.0) / tau);
+            for (int64_t i = 0; i < 3 * n; i++) v[i] *= factor;
+        } else if (thermostat == 2) {
+            double T = orc_temperature(s, v);
+            if (std::fabs(T - T0) > tol) {  // velocities::scale (velocities.rs:16-22)
+                double factor = std::sqrt(T0 / T);
+                for (int64_t i = 0; i < 3 * n; i++) v[i] *= factor;
+            }
+        } else if (thermostat == 3) {
+            *count += 1;
+            double kinetic = orc_kinetic_energy(s, v);
+            double kinetic_factor = (K_BOLTZMANN * T0 / 2.0) / kinetic;
+            double exp_1 = std::exp(-1.0 / tau);
+            double exp_2 = (1.0 - exp_1) * kinetic_factor;
+            int64_t dn = 3 * n - 1;  // sum_noises(dof - 1) (thermostats.rs:166-192)
+            Noise r(seed, *count);
+            double gauss = 0.0, wiener = 0.0;
+            if (dn == 1) {
+                gauss = r.normal();
+                wiener = gauss * gauss;
+            } else if (dn > 1) {
+                gauss = r.normal();
+                if (dn % 2 == 0) wiener = 2.0 * r.gamma((double)(dn / 2));
+                else wiener = 2.0 * r.gamma((double)((dn - 1) / 2)) + gauss * gauss;
+            }
+            double scale = exp_1 + exp_2 * (gauss * gauss + wiener) + 2.0 * gauss * std::sqrt(exp_1 * exp_2);
+            double alpha = std::sqrt(scale);
+            for (int64_t i = 0; i < 3 * n; i++) v[i] *= alpha;
+        }
+        // Control::control (controls.rs:29-43, 80-89)
+        if (controls & 1u) {  // RemoveTranslation
+            double total = 0.0;
+            for (int64_t i = 0; i < n; i++) total += s->mass[i];
+            double com[3] = {0.0, 0.0, 0.0};
+            for (int64_t i = 0; i < n; i++)
+                for (int k = 0; k < 3; k++) com[k] += v[3 * i + k] * s->mass[i] / total;
+            for (int64_t i = 0; i < n; i++)
+                for (int k = 0; k < 3; k++) v[3 * i + k] -= com[k];
+        }
+        if (controls & 2u) {  // Rewrap: Molecule::wrap (sys/config/molecules.rs:256-296)
+            double L[3] = {s->cell.a, s->cell.b, s->cell.c};
+            for (auto& mr : s->mol_range) {
+                double total = 0.0, com[3] = {0.0, 0.0, 0.0};
+                for (int64_t i = mr.first; i < mr.second; i++) {
+                    total += s->mass[i];
+                    for (int k = 0; k < 3; k++) com[k] += s->mass[i] * x[3 * i + k];
+                }
+                double delta[3];
+                for (int k = 0; k < 3; k++) {
+                    double c = com[k] / total;
+                    double w = c - std::floor(c / L[k]) * L[k];  // UnitCell::wrap_vector (cells.rs:263-270)
+                    delta[k] = w - c;
+                }
+                for (int64_t i = mr.first; i < mr.second; i++)
+                    for (int k = 0; k < 3; k++) x[3 * i + k] += delta[k];
+            }
+        }
+    }
+    orc_set_positions(s, x);
+}
+
 void orc_pair_eval(const orc_pair* d, double r, double* energy, double* force, double* tail_energy,
                    double* tail_virial) {
     PairPot p;

@@ -140,6 +140,21 @@ void orc_velocity_verlet(orc_system* s, double* positions, double* velocities,
                          double* accelerations, double dt, int64_t nsteps,
                          double thermostat_temperature, double thermostat_tau);
 double orc_temperature(const orc_system* s, const double* velocities);
+
+/* MolecularDynamics::propagate (lumol-sim/src/md/molecular_dynamics.rs:66-76)
+ * for `nsteps` steps: integrator 0 VelocityVerlet, 1 Verlet, 2 LeapFrog
+ * (md/integrators.rs); thermostat 0 none, 1 Berendsen(T0, tau), 2
+ * Rescale(T0, tol), 3 CSVR(T0, tau) (md/thermostats.rs) with the noise of
+ * SplitMix64 streams of (seed, count) (*count: thermostat applications so far,
+ * in / out); controls bit 1 RemoveTranslation, bit 2 Rewrap (md/controls.rs).
+ * `state` (3n) is the integrator's: accelerations, or Verlet's positions at
+ * t - dt (orc_verlet_setup). */
+void orc_md_run(orc_system* s, double* positions, double* velocities, double* state, int integrator, double dt,
+                int thermostat, double T0, double tau, double tol, uint64_t seed, uint64_t* count,
+                uint32_t controls, int64_t nsteps);
+/* Verlet::setup (md/integrators.rs:92-104): prev = x - v dt. */
+void orc_verlet_setup(const orc_system* s, const double* positions, const double* velocities, double dt,
+                      double* prev);
 double orc_kinetic_energy(const orc_system* s, const double* velocities);
 
 /* One PairInteraction evaluated at distance r: energy, force, tail energy,

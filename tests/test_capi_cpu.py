@@ -68,6 +68,15 @@ def test_host_checks_mirror_reference_panics():
         lg.Gaussian(8.0, -2.0)
     with pytest.raises(ValueError, match="larger than the attractive exponent"):
         lg.Mie(2.0, 0.8, 6.0, 12.0)
+    # thermostats.rs:228-259 (should_panic tests)
+    with pytest.raises(ValueError, match="positive in thermostats"):
+        lg.RescaleThermostat(-56.0)
+    with pytest.raises(ValueError, match="positive in thermostats"):
+        lg.CSVRThermostat(-56.0, 1000.0)
+    with pytest.raises(ValueError, match="larger than 1 in CSVR"):
+        lg.CSVRThermostat(56.0, 0.3)
+    with pytest.raises(ValueError, match="larger than 1 in berendsen"):
+        lg.BerendsenThermostat(56.0, -2.0)
 
 
 def test_units_match_reference_conversions():
