@@ -244,9 +244,11 @@ __device__ __forceinline__ float fixed_dist2(uint4 a, uint4 b, const float* Lq) 
 // Cell of a fixed-point position: u / 2^32 is the wrapped fraction of the
 // cell length, so floor(fraction * ncell) is (u * ncell) >> 32.
 __device__ __forceinline__ int fixed_cell(const SysDev& s, uint4 u) {
-    int cx = (int)(((unsigned long long)u.x * (unsigned)s.ncell[0]) >> 32);
-    int cy = (int)(((unsigned long long)u.y * (unsigned)s.ncell[1]) >> 32);
-    int cz = (int)(((unsigned long long)u.z * (unsigned)s.ncell[2]) >> 32);
+    // the high 32 bits of the 64-bit products u * ncell (__umulhi: the
+    // spelled-out (u64)u * n >> 32 lost its z term in one list-build kernel)
+    int cx = (int)__umulhi(u.x, (unsigned)s.ncell[0]);
+    int cy = (int)__umulhi(u.y, (unsigned)s.ncell[1]);
+    int cz = (int)__umulhi(u.z, (unsigned)s.ncell[2]);
     return s.cell_begin + (cz * s.ncell[1] + cy) * s.ncell[0] + cx;
 }
 

@@ -66,7 +66,7 @@ struct Batch {
     // per-atom MD kernels run on tiles of VV_TILE atoms that never straddle two systems
     int ntiles = 0;
     int2* tiles = nullptr;        // ntiles: (system, first atom)
-    double* kepart = nullptr;     // n: kinetic energy of each chunk of 32 / tpa atoms after md_second, at begin + chunk
+    double* kepart = nullptr;     // n: kinetic energies after md_second (mixed: per atom at its sorted position; plain: per chunk of 32 / tpa atoms, at begin + chunk)
     double* mom = nullptr;        // 3n: momentum of each chunk (RemoveTranslation), at 3 (begin + chunk)
     unsigned long long* md_count = nullptr;  // nsys: thermostat applications so far (the CSVR noise stream)
     int nmol = 0;                 // molecules of the batch (Rewrap)

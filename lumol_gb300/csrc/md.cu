@@ -98,6 +98,48 @@ __device__ __forceinline__ float plain_displacement2(const SysDev& s, const doub
     return dx * dx + dy * dy + dz * dz;
 }
 
+// The sum of the kinetic energies of gpw consecutive sorted positions in the
+// order of a warp butterfly over them (v[j] += v[j + o], o = gpw / 2 ... 1):
+// the tree the persistent kernel's force phase sums a chunk's atoms with.
+template <int G>
+__device__ __forceinline__ double butterfly_tree(const double* a, int cnt) {
+    double v[G];
+#pragma unroll
+    for (int j = 0; j < G; j++) v[j] = j < cnt ? __ldcg(a + j) : 0.0;
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1)
+#pragma unroll
+        for (int j = 0; j < o; j++) v[j] = v[j] + v[j + o];
+    return v[0];
+}
+
+// Kinetic energy of a mixed-path system from its atoms' kinetic energies at
+// their cell-sorted positions: chunks of gpw sorted positions summed as the
+// persistent kernel sums them, then the chunks as chunk_ke_sum adds them, so
+// both MD paths derive the same thermostat factor.  (Not inlined: the tree
+// registers stay out of the integration kernels.)
+static __device__ __noinline__ double sorted_ke_sum(const SysDev& s, const double* ke, int gpw, int lane) {
+    int n = s.end - s.begin;
+    int nq = (n + gpw - 1) / gpw;
+    double k = 0.0;
+    for (int q = lane; q < nq; q += 32) {
+        const double* a = ke + s.begin + (size_t)q * gpw;
+        int cnt = min(gpw, n - q * gpw);
+        double c;
+        switch (gpw) {
+            case 1: c = butterfly_tree<1>(a, cnt); break;
+            case 2: c = butterfly_tree<2>(a, cnt); break;
+            case 4: c = butterfly_tree<4>(a, cnt); break;
+            case 8: c = butterfly_tree<8>(a, cnt); break;
+            case 16: c = butterfly_tree<16>(a, cnt); break;
+            default: c = butterfly_tree<32>(a, cnt); break;
+        }
+        k += c;
+    }
+    for (int o = 16; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
+    return k;
+}
+
 // The previous step's thermostat factor and controls for a tile's system,
 // computed by its first warp from the chunk sums of the last md_second (the
 // same sums in every block of the system, and the same as the persistent
@@ -106,10 +148,12 @@ __device__ __forceinline__ float plain_displacement2(const SysDev& s, const doub
 __device__ __forceinline__ void tile_adjust(const SysDev& s, int si, const double* __restrict__ kepart,
                                             const double* __restrict__ mom,
                                             const unsigned long long* __restrict__ md_count, int gpw,
-                                            double* adj) {
+                                            bool sorted, double* adj) {
     if (threadIdx.x < 32) {
         int lane = threadIdx.x;
-        double k = s.thermostat != TH_NONE ? chunk_ke_sum(s, kepart, gpw, lane) : 0.0;
+        double k = 0.0;
+        if (s.thermostat != TH_NONE)
+            k = sorted ? sorted_ke_sum(s, kepart, gpw, lane) : chunk_ke_sum(s, kepart, gpw, lane);
         double f = thermostat_factor(s, k, md_count[si]);
         double c[3] = {0.0, 0.0, 0.0};
         if (s.controls & CTL_REMOVE_TRANSLATION)
@@ -166,7 +210,7 @@ __global__ void __launch_bounds__(VV_TILE) md_first_kernel(
     int2 tile = tiles[blockIdx.x];
     const SysDev& s = sys[tile.x];
     __shared__ double adj[4];
-    if (adjust) tile_adjust(s, tile.x, kepart, mom, md_count, gpw, adj);
+    if (adjust) tile_adjust(s, tile.x, kepart, mom, md_count, gpw, MIXED, adj);
     int i = tile.y + threadIdx.x;
     if (i >= s.end) return;
     double hdt = s.hdt, dt = s.dt;
@@ -223,10 +267,11 @@ __global__ void __launch_bounds__(VV_TILE) md_first_kernel(
 //   Verlet          x' = 2 x - x_prev + dt^2 / m F; v = (x' - x_prev) / (2 dt);
 //                   x_prev = x (held in the acceleration slot)      (integrators.rs:106-122)
 // (a Verlet system then writes its fixed-point copy and runs the displacement
-// test); with a thermostat, the kinetic energies of the system's chunks of gpw
-// atoms, with RemoveTranslation their momenta, for the next step's factors
-// (tiles start at their system's first atom in steps of VV_TILE, so a warp
-// holds 32 / gpw whole chunks).  Plain path: the reference's divisions and
+// test); with a thermostat, the kinetic energies for the next step's factor
+// (mixed path: each atom's at its cell-sorted position, summed as the
+// persistent kernel sums them; plain path: chunks of gpw atoms), with
+// RemoveTranslation the momenta of chunks of gpw atoms (tiles start at their
+// system's first atom in steps of VV_TILE, so a warp holds 32 / gpw whole chunks).  Plain path: the reference's divisions and
 // unfused products; mixed path: a = F * (1 / m) in FP32 (the force is an FP32
 // value) and fused multiply-adds on the FP64 state.
 template <bool MIXED>
@@ -321,8 +366,12 @@ __global__ void __launch_bounds__(VV_TILE) md_second_kernel(
     const bool head = threadIdx.x % gpw == 0 && i < s.end;
     const size_t q = (size_t)s.begin + (i - s.begin) / gpw;
     if (s.thermostat != TH_NONE) {
-        ke = chunk_butterfly(ke, gpw);
-        if (head) kepart[q] = ke;
+        if (MIXED) {  // each atom's kinetic energy at its sorted position (the persistent kernel's order)
+            if (i < s.end) kepart[perm[i]] = ke;
+        } else {
+            ke = chunk_butterfly(ke, gpw);
+            if (head) kepart[q] = ke;
+        }
     }
     if (s.controls & CTL_REMOVE_TRANSLATION) {
         mx = chunk_butterfly(mx, gpw);
@@ -344,11 +393,11 @@ __global__ void __launch_bounds__(VV_TILE) md_finalize_kernel(const int2* __rest
                                                               const double* __restrict__ kepart,
                                                               const double* __restrict__ mom,
                                                               const unsigned long long* __restrict__ md_count,
-                                                              int gpw, double4_32a* __restrict__ vel) {
+                                                              int gpw, int sorted, double4_32a* __restrict__ vel) {
     int2 tile = tiles[blockIdx.x];
     const SysDev& s = sys[tile.x];
     __shared__ double adj[4];
-    tile_adjust(s, tile.x, kepart, mom, md_count, gpw, adj);
+    tile_adjust(s, tile.x, kepart, mom, md_count, gpw, sorted != 0, adj);
     int i = tile.y + threadIdx.x;
     if (i >= s.end) return;
     double4_32a v = vel[i];
@@ -467,7 +516,7 @@ void launch_md_second(const Batch& b, cudaStream_t st) {
 void launch_md_finalize(const Batch& b, cudaStream_t st) {
     if (b.ntiles)
         md_finalize_kernel<<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.kepart, b.mom, b.md_count, 32 / b.tpa,
-                                                         b.vel);
+                                                         b.precision == 1 ? 1 : 0, b.vel);
 }
 void launch_rewrap(const Batch& b, cudaStream_t st) {
     if (b.nmol)

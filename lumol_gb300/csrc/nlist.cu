@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(1024) nl_plan_kernel(int nsys, const uint32_t*
 __global__ void nl_bin_kernel(int nsys, const int* __restrict__ plan, const double4_32a* __restrict__ posq,
                               const SysDev* __restrict__ sys, const uint32_t* __restrict__ status,
                               int* __restrict__ atom_cell, int* __restrict__ cell_count, float4* __restrict__ wpos,
-                              double4_32a* __restrict__ pos_build, int fixed) {
+                              double4_32a* __restrict__ pos_build) {
     if (!(*status & ST_REBUILD)) return;
     PlanView pv = plan_view(plan, nsys);
     int A = pv.apre[pv.R];
@@ -113,12 +113,6 @@ __global__ void nl_bin_kernel(int nsys, const int* __restrict__ plan, const doub
         int i = s.begin + (v - pv.apre[r]);
         double4_32a p = posq[i];
         pos_build[i] = p;
-        if (fixed) {  // mixed path: cells and the list test from the fixed-point copies
-            int cell = fixed_cell(s, fixed_position(s, p));
-            atom_cell[i] = cell;
-            atomicAdd(&cell_count[cell], 1);
-            continue;
-        }
         double w[3] = {p.x, p.y, p.z};
         int c[3];
         for (int d = 0; d < 3; d++) {
@@ -130,6 +124,30 @@ __global__ void nl_bin_kernel(int nsys, const int* __restrict__ plan, const doub
         atom_cell[i] = cell;
         atomicAdd(&cell_count[cell], 1);
         wpos[i] = make_float4((float)w[0], (float)w[1], (float)w[2], (float)p.w);
+    }
+}
+
+// Atom pass of the mixed path: the cell of each atom from its fixed-point
+// position (integer arithmetic, as the persistent kernel's list build), and
+// the reference position for the displacement test.  (A kernel of its own:
+// with the plain path's pass in the same loop body, the z cell index of this
+// pass came out as 0 on GB300, for every atom.)
+__global__ void nl_bin_fixed_kernel(int nsys, const int* __restrict__ plan, const double4_32a* __restrict__ posq,
+                                    const SysDev* __restrict__ sys, const uint32_t* __restrict__ status,
+                                    int* __restrict__ atom_cell, int* __restrict__ cell_count,
+                                    double4_32a* __restrict__ pos_build) {
+    if (!(*status & ST_REBUILD)) return;
+    PlanView pv = plan_view(plan, nsys);
+    int A = pv.apre[pv.R];
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < A; v += gridDim.x * blockDim.x) {
+        int r = plan_find(pv.apre, pv.R, v);
+        const SysDev& s = sys[pv.sys[r]];
+        int i = s.begin + (v - pv.apre[r]);
+        double4_32a p = posq[i];
+        pos_build[i] = p;
+        int cell = fixed_cell(s, fixed_position(s, p));
+        atom_cell[i] = cell;
+        atomicAdd(&cell_count[cell], 1);
     }
 }
 
@@ -439,8 +457,12 @@ void launch_nlist_build(const Batch& b, cudaStream_t st) {
     unsigned build_grid = (unsigned)std::min((n + NL_WARPS - 1) / NL_WARPS, 8 * b.sms);
     unsigned scan_grid = (unsigned)std::min(b.nsys, 2 * b.sms);
     nl_plan_kernel<<<1, 1024, 0, st>>>(b.nsys, b.status, b.sys_rebuild, b.sys, b.plan);
-    nl_bin_kernel<<<atoms_grid, tb, 0, st>>>(b.nsys, b.plan, b.posq, b.sys, b.status, b.atom_cell, b.cell_count,
-                                             b.wpos, b.pos_build, b.perm ? 1 : 0);
+    if (b.perm)
+        nl_bin_fixed_kernel<<<atoms_grid, tb, 0, st>>>(b.nsys, b.plan, b.posq, b.sys, b.status, b.atom_cell,
+                                                       b.cell_count, b.pos_build);
+    else
+        nl_bin_kernel<<<atoms_grid, tb, 0, st>>>(b.nsys, b.plan, b.posq, b.sys, b.status, b.atom_cell, b.cell_count,
+                                                 b.wpos, b.pos_build);
     nl_scan_kernel<<<scan_grid, 1024, 0, st>>>(b.nsys, b.status, b.plan, b.sys, b.cell_count, b.cell_start);
     nl_scatter_kernel<<<atoms_grid, tb, 0, st>>>(b.nsys, b.plan, b.status, b.sys, b.atom_cell, b.cell_count,
                                                  b.cell_start, b.cell_atoms);
