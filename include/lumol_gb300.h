@@ -209,6 +209,10 @@ int lg_compute_device(lg_engine* e, const double* d_positions, uint32_t terms, u
  * device kernels see it.  Writes up to `capacity` (i, j), i < j, and the count. */
 int lg_pairset(lg_engine* e, int32_t s, const double* positions, int32_t family,
                int32_t* pairs, int64_t capacity, int64_t* count);
+/* Test hook: the cell of each atom of system `s` (n entries, atom order) at the
+ * last neighbour-list build, as (cz * ny + cy) * nx + cx, and the cells per
+ * axis (nx, ny, nz).  Cells are at least half the list radius wide. */
+int lg_list_cells(lg_engine* e, int32_t s, int32_t* cells, int32_t ncell[3]);
 
 /* ---- molecular dynamics ------------------------------------------------------ */
 /* VelocityVerlet::new + setup (lumol-sim/src/md/integrators.rs:22-42): sets the

@@ -110,6 +110,7 @@ SIGNATURES = {
     "lg_pairset": (ctypes.c_int, [_P, ctypes.c_int32, _D, ctypes.c_int32, _I32, ctypes.c_int64, _I64]),
     "lg_md_setup": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double]),
     "lg_md_setup_ex": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(LgMdParams)]),
+    "lg_list_cells": (ctypes.c_int, [_P, ctypes.c_int32, _I32, _I32]),
     "lg_md_set_state": (ctypes.c_int, [_P, ctypes.c_int32, _D, _D]),
     "lg_md_get_state": (ctypes.c_int, [_P, ctypes.c_int32, _D, _D]),
     "lg_md_set_state_all": (ctypes.c_int, [_P, _D, _D, _D]),

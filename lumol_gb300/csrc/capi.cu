@@ -1934,6 +1934,19 @@ int lg_fma_peak(int32_t fp64, double* tflops) {
     return rc ? fail(nullptr, LG_ERR_CUDA, "FMA probe failed") : LG_OK;
 }
 
+int lg_list_cells(lg_engine* e, int32_t s, int32_t* cells, int32_t ncell[3]) {
+    if (!valid_sys(e, s) || !cells || !ncell) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    if (e->dirty) return fail(e, LG_ERR_STATE, "no device state");
+    CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    const SysDev& d = e->h_sysdev[s];
+    size_t n = (size_t)e->sys[s].n;
+    CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+    CUDA_TRY(e, cudaMemcpy(cells, e->atom_cell.p + e->begin[s], n * sizeof(int), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; i++) cells[i] -= d.cell_begin;
+    for (int k = 0; k < 3; k++) ncell[k] = d.ncell[k];
+    return LG_OK;
+}
+
 int lg_kernel_times(lg_engine* e, int32_t reps, double* ms) {
     if (!e || !ms || reps <= 0) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
     if (e->dirty) return fail(e, LG_ERR_STATE, "no device state");

@@ -232,3 +232,33 @@ def test_batch_of_systems_matches_each_alone():
     for s in range(3):
         pos, vel = batch.state(s)
         assert np.array_equal(pos, states[s][0]) and np.array_equal(vel, states[s][1])
+
+
+# ---- cell binning of the list build --------------------------------------------------------
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_list_build_cells_match_positions(precision):
+    """Every atom sits in the cell its position gives: the FP64 path bins the
+    wrapped position (UnitCell::wrap_vector, cells.rs:263-270), the mixed path
+    the fixed-point fraction u = floor(x 2^32 / L) mod 2^32, cell (u n) >> 32."""
+    import ctypes
+    import math
+    s = systems.random_lj_fluid(900, 0.02, 12, 9.0, family="lj", precision=precision)
+    s.compute()  # builds the neighbour lists at these positions
+    cells = np.zeros(s.size, dtype=np.int32)
+    ncell = (ctypes.c_int32 * 3)()
+    s.engine().call("lg_list_cells", 0, cells.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), ncell)
+    n = list(ncell)
+    assert min(n) > 1
+    expect = []
+    for p in s.positions:
+        c = []
+        for d in range(3):
+            L = s.cell.lengths[d]
+            if precision == "mixed":
+                u = math.floor(p[d] * ((1.0 / L) * 4294967296.0)) % 2 ** 32
+                c.append((u * n[d]) >> 32)
+            else:
+                w = p[d] - math.floor(p[d] / L) * L
+                c.append(min(max(int(w * (1.0 / L) * n[d]), 0), n[d] - 1))
+        expect.append((c[2] * n[1] + c[1]) * n[0] + c[0])
+    assert cells.tolist() == expect
