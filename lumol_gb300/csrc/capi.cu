@@ -302,6 +302,7 @@ struct lg_engine {
     DBuf<double4_32a> posq, vel, acc, pos_build;
     DBuf<double> force, pos3, vel3, red, host_const, kepart, mom, out, fpart, kred, mc_part;
     DBuf<unsigned long long> md_count, cp_count;
+    DBuf<double> adj;
     DBuf<int> mol_start;
     DBuf<int2> tiles;
     DBuf<double4_32a> cp_pos, cp_vel, cp_acc;  // MD checkpoint: a chunk whose list overflowed is replayed
@@ -731,6 +732,7 @@ int commit(lg_engine* e) {
     CUDA_TRY(e, e->mom.alloc(std::max<size_t>(3 * n, 1)));
     CUDA_TRY(e, e->md_count.alloc(std::max(nsys, 1)));
     CUDA_TRY(e, e->cp_count.alloc(std::max(nsys, 1)));
+    CUDA_TRY(e, e->adj.alloc(4 * (size_t)std::max(nsys, 1)));
     CUDA_TRY(e, e->mol_start.alloc(h_mol_start.size()));
     CUDA_TRY(e, e->cp_pos.alloc(n));
     CUDA_TRY(e, e->cp_vel.alloc(n));
@@ -913,6 +915,7 @@ int commit(lg_engine* e) {
     b.kepart = e->kepart.p;
     b.mom = e->mom.p;
     b.md_count = e->md_count.p;
+    b.adj = e->adj.p;
     b.nmol = (int)h_mol_start.size() - 1;
     b.mol_start = e->mol_start.p;
     if (e->h_mc.size() != (size_t)nsys) e->h_mc.assign(nsys, McState{});
@@ -1583,6 +1586,10 @@ void enqueue_md_step(lg_engine* e, int mode, bool apply_previous, cudaStream_t s
     enqueue_forces(e, LG_TERM_ALL, false, st, !(mode & MD_VERLET_SYS));
     launch_md_second(e->b, st);
     e->launches += e->b.ntiles ? 2 : 0;
+    if (mode & MD_ADJUST) {  // this step's thermostat factor and controls, per system
+        launch_md_adjust(e->b, st);
+        e->launches += 1;
+    }
 }
 
 // The pending thermostat and controls at the end of a run.

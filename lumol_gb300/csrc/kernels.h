@@ -69,6 +69,7 @@ struct Batch {
     double* kepart = nullptr;     // n: kinetic energies after md_second (mixed: per atom at its sorted position; plain: per chunk of 32 / tpa atoms, at begin + chunk)
     double* mom = nullptr;        // 3n: momentum of each chunk (RemoveTranslation), at 3 (begin + chunk)
     unsigned long long* md_count = nullptr;  // nsys: thermostat applications so far (the CSVR noise stream)
+    double* adj = nullptr;        // 4 nsys: each system's pending thermostat factor and centre-of-mass velocity
     int nmol = 0;                 // molecules of the batch (Rewrap)
     int* mol_start = nullptr;     // nmol + 1: first atom of each molecule
     // mixed precision
@@ -131,6 +132,7 @@ void launch_unpack_velocities(const Batch& b, double* vel3, cudaStream_t st);
 constexpr int VV_TILE = 256;
 void launch_md_first(const Batch& b, bool adjust, cudaStream_t st);
 void launch_md_second(const Batch& b, cudaStream_t st);
+void launch_md_adjust(const Batch& b, cudaStream_t st);
 void launch_md_finalize(const Batch& b, cudaStream_t st);
 void launch_rewrap(const Batch& b, cudaStream_t st);
 void launch_verlet_setup(const Batch& b, int s, int begin, int end, cudaStream_t st);

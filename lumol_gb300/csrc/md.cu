@@ -140,36 +140,39 @@ static __device__ __noinline__ double sorted_ke_sum(const SysDev& s, const doubl
     return k;
 }
 
-// The previous step's thermostat factor and controls for a tile's system,
-// computed by its first warp from the chunk sums of the last md_second (the
-// same sums in every block of the system, and the same as the persistent
-// kernel's): adj[0] = the velocity factor, adj[1..3] = the centre-of-mass
-// velocity after scaling (RemoveTranslation, controls.rs:29-43), else zero.
-__device__ __forceinline__ void tile_adjust(const SysDev& s, int si, const double* __restrict__ kepart,
-                                            const double* __restrict__ mom,
-                                            const unsigned long long* __restrict__ md_count, int gpw,
-                                            bool sorted, double* adj) {
-    if (threadIdx.x < 32) {
-        int lane = threadIdx.x;
-        double k = 0.0;
-        if (s.thermostat != TH_NONE)
-            k = sorted ? sorted_ke_sum(s, kepart, gpw, lane) : chunk_ke_sum(s, kepart, gpw, lane);
-        double f = thermostat_factor(s, k, md_count[si]);
-        double c[3] = {0.0, 0.0, 0.0};
-        if (s.controls & CTL_REMOVE_TRANSLATION)
-            for (int d = 0; d < 3; d++) c[d] = f * chunk_sum(s, mom + d, 3, gpw, lane) / s.total_mass;
-        if (lane == 0) {
-            adj[0] = f;
-            adj[1] = c[0];
-            adj[2] = c[1];
-            adj[3] = c[2];
-        }
+// The thermostat factor and RemoveTranslation's centre-of-mass velocity of
+// every system after a step (adj[4 s] = factor, adj[4 s + 1 .. 3] = the
+// centre-of-mass velocity after scaling, controls.rs:29-43, else zero), one
+// warp per system, from the sums md_second left: the kinetic energies in the
+// persistent kernel's order (mixed path) or per chunk (plain path), the
+// momenta per chunk.  Computed once per system and step; the next md_first (or
+// md_finalize at the end of a run) applies it.
+__global__ void __launch_bounds__(128) md_adjust_kernel(int nsys, const SysDev* __restrict__ sys,
+                                                        const double* __restrict__ kepart,
+                                                        const double* __restrict__ mom,
+                                                        const unsigned long long* __restrict__ md_count, int gpw,
+                                                        int sorted, double* __restrict__ adj) {
+    int si = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    int lane = threadIdx.x & 31;
+    if (si >= nsys) return;
+    const SysDev& s = sys[si];
+    double k = 0.0;
+    if (s.thermostat != TH_NONE)
+        k = sorted ? sorted_ke_sum(s, kepart, gpw, lane) : chunk_ke_sum(s, kepart, gpw, lane);
+    double f = thermostat_factor(s, k, md_count[si]);
+    double c[3] = {0.0, 0.0, 0.0};
+    if (s.controls & CTL_REMOVE_TRANSLATION)
+        for (int d = 0; d < 3; d++) c[d] = f * chunk_sum(s, mom + d, 3, gpw, lane) / s.total_mass;
+    if (lane == 0) {
+        adj[4 * si] = f;
+        adj[4 * si + 1] = c[0];
+        adj[4 * si + 2] = c[1];
+        adj[4 * si + 3] = c[2];
     }
-    __syncthreads();
 }
 
 // v *= factor (the thermostat), then v -= centre-of-mass velocity (RemoveTranslation)
-__device__ __forceinline__ void apply_adjust(const SysDev& s, const double* adj, double4_32a& v) {
+__device__ __forceinline__ void apply_adjust(const SysDev& s, const double* __restrict__ adj, double4_32a& v) {
     double f = adj[0];
     if (s.controls & CTL_REMOVE_TRANSLATION) {
         v.x = __dsub_rn(__dmul_rn(v.x, f), adj[1]);
@@ -182,9 +185,10 @@ __device__ __forceinline__ void apply_adjust(const SysDev& s, const double* adj,
     }
 }
 
-// The thermostat and controls of step k are applied at the start of step
-// k + 1 (the same products, in the same order, as right after step k), and by
-// md_finalize at the end of a run, which saves two launches a step.
+// The thermostat and controls of step k are computed once per system by
+// md_adjust after step k and applied at the start of step k + 1 (the same
+// products, in the same order, as right after step k), or by md_finalize at
+// the end of a run, which saves a pass over the atoms every step.
 //
 // md_first: [v *= lambda; v -= v_com]; then the integrator's update before the forces
 //   VelocityVerlet  v += dt/2 a; x += v dt      (integrators.rs:44-53)
@@ -204,18 +208,15 @@ template <bool MIXED>
 __global__ void __launch_bounds__(VV_TILE) md_first_kernel(
     const int2* __restrict__ tiles, const SysDev* __restrict__ sys, double4_32a* __restrict__ posq,
     double4_32a* __restrict__ vel, const double4_32a* __restrict__ acc, const double4_32a* __restrict__ pos_build,
-    const uint4* __restrict__ pfx_build, const double* __restrict__ kepart, const double* __restrict__ mom,
-    const unsigned long long* __restrict__ md_count, int gpw, int adjust, const int* __restrict__ perm,
+    const uint4* __restrict__ pfx_build, const double* __restrict__ adj, int adjust, const int* __restrict__ perm,
     uint4* __restrict__ posfx, uint32_t* status, uint32_t* sys_rebuild) {
     int2 tile = tiles[blockIdx.x];
     const SysDev& s = sys[tile.x];
-    __shared__ double adj[4];
-    if (adjust) tile_adjust(s, tile.x, kepart, mom, md_count, gpw, MIXED, adj);
     int i = tile.y + threadIdx.x;
     if (i >= s.end) return;
     double hdt = s.hdt, dt = s.dt;
     double4_32a v = vel[i], a = acc[i], p = posq[i];
-    if (adjust) apply_adjust(s, adj, v);
+    if (adjust) apply_adjust(s, adj + 4 * tile.x, v);
     if (s.integrator == MD_VERLET) {  // positions move after the forces
         vel[i] = v;
         return;
@@ -390,18 +391,14 @@ __global__ void __launch_bounds__(VV_TILE) md_second_kernel(
 // The pending thermostat and controls at the end of a run.
 __global__ void __launch_bounds__(VV_TILE) md_finalize_kernel(const int2* __restrict__ tiles,
                                                               const SysDev* __restrict__ sys,
-                                                              const double* __restrict__ kepart,
-                                                              const double* __restrict__ mom,
-                                                              const unsigned long long* __restrict__ md_count,
-                                                              int gpw, int sorted, double4_32a* __restrict__ vel) {
+                                                              const double* __restrict__ adj,
+                                                              double4_32a* __restrict__ vel) {
     int2 tile = tiles[blockIdx.x];
     const SysDev& s = sys[tile.x];
-    __shared__ double adj[4];
-    tile_adjust(s, tile.x, kepart, mom, md_count, gpw, sorted != 0, adj);
     int i = tile.y + threadIdx.x;
     if (i >= s.end) return;
     double4_32a v = vel[i];
-    apply_adjust(s, adj, v);
+    apply_adjust(s, adj + 4 * tile.x, v);
     vel[i] = v;
 }
 
@@ -489,15 +486,15 @@ __global__ void request_rebuild_kernel(int nsys, uint32_t* status, uint32_t* sys
 
 void launch_md_first(const Batch& b, bool adjust, cudaStream_t st) {
     if (!b.ntiles) return;
-    int aj = adjust ? 1 : 0, gpw = 32 / b.tpa;
+    int aj = adjust ? 1 : 0;
     if (b.precision == 1)
         md_first_kernel<true><<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.posq, b.vel, b.acc, b.pos_build,
-                                                            b.pfx_build, b.kepart, b.mom, b.md_count, gpw, aj,
-                                                            b.perm, b.posfx, b.status, b.sys_rebuild);
+                                                            b.pfx_build, b.adj, aj, b.perm, b.posfx, b.status,
+                                                            b.sys_rebuild);
     else
         md_first_kernel<false><<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.posq, b.vel, b.acc, b.pos_build,
-                                                             nullptr, b.kepart, b.mom, b.md_count, gpw, aj,
-                                                             nullptr, b.posfx, b.status, b.sys_rebuild);
+                                                             nullptr, b.adj, aj, nullptr, b.posfx, b.status,
+                                                             b.sys_rebuild);
 }
 void launch_md_second(const Batch& b, cudaStream_t st) {
     if (!b.ntiles) return;
@@ -513,10 +510,13 @@ void launch_md_second(const Batch& b, cudaStream_t st) {
                                                               b.md_count, gpw, nullptr, b.posfx, b.status,
                                                               b.sys_rebuild);
 }
+void launch_md_adjust(const Batch& b, cudaStream_t st) {
+    if (b.nsys)
+        md_adjust_kernel<<<(b.nsys + 3) / 4, 128, 0, st>>>(b.nsys, b.sys, b.kepart, b.mom, b.md_count, 32 / b.tpa,
+                                                          b.precision == 1 ? 1 : 0, b.adj);
+}
 void launch_md_finalize(const Batch& b, cudaStream_t st) {
-    if (b.ntiles)
-        md_finalize_kernel<<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.kepart, b.mom, b.md_count, 32 / b.tpa,
-                                                         b.precision == 1 ? 1 : 0, b.vel);
+    if (b.ntiles) md_finalize_kernel<<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.adj, b.vel);
 }
 void launch_rewrap(const Batch& b, cudaStream_t st) {
     if (b.nmol)
