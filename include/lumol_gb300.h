@@ -238,6 +238,7 @@ enum {
 /* Controls, applied after the thermostat at every step (md/controls.rs). */
 #define LG_CONTROL_REMOVE_TRANSLATION 1u /* RemoveTranslation (controls.rs:26-43) */
 #define LG_CONTROL_REWRAP 2u             /* Rewrap (controls.rs:73-89): molecules' centres of mass into the cell */
+#define LG_CONTROL_REMOVE_ROTATION 4u    /* RemoveRotation (controls.rs:44-71) */
 
 typedef struct lg_md_params {
     int32_t integrator;  /* LG_INTEGRATOR_* */
@@ -247,7 +248,7 @@ typedef struct lg_md_params {
     double tau;          /* Berendsen / CSVR time scale, in timesteps (>= 1) */
     double tolerance;    /* RescaleThermostat tolerance (K) */
     uint64_t seed;       /* CSVR: the noise of step k is drawn from SplitMix64 streams of (seed, k) */
-    uint32_t controls;   /* LG_CONTROL_* bits */
+    uint32_t controls;   /* LG_CONTROL_* bits; applied as RemoveTranslation, RemoveRotation, Rewrap */
     uint32_t reserved;   /* 0 */
 } lg_md_params;
 

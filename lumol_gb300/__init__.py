@@ -26,6 +26,7 @@ from .system import (
     NullPotential,
     PairInteraction,
     PairRestriction,
+    RemoveRotation,
     RemoveTranslation,
     RescaleThermostat,
     Rewrap,
@@ -51,7 +52,7 @@ from ._capi import (
 __all__ = [
     "units", "EngineError", "BerendsenThermostat", "BornMayerHuggins", "Buckingham", "CSVRThermostat", "Engine",
     "Ewald", "Gaussian", "Harmonic", "LeapFrog", "LennardJones", "Mie", "MolecularDynamics", "MonteCarlo", "Morse",
-    "Translate", "NullPotential", "PairInteraction", "PairRestriction", "RemoveTranslation", "RescaleThermostat",
+    "Translate", "NullPotential", "PairInteraction", "PairRestriction", "RemoveRotation", "RemoveTranslation", "RescaleThermostat",
     "Rewrap", "System", "UnitCell", "VelocityVerlet", "Verlet", "Wolf", "md_params",
     "LG_TERM_ALL", "LG_TERM_ANGLES", "LG_TERM_BONDS", "LG_TERM_COUL_KSPACE", "LG_TERM_COUL_REAL",
     "LG_TERM_COUL_SELF", "LG_TERM_PAIRS", "LG_TERM_TAIL",

@@ -80,7 +80,7 @@ class LgOptions(ctypes.Structure):
 
 LG_INTEGRATOR_VELOCITY_VERLET, LG_INTEGRATOR_VERLET, LG_INTEGRATOR_LEAP_FROG = 0, 1, 2
 LG_THERMOSTAT_NONE, LG_THERMOSTAT_BERENDSEN, LG_THERMOSTAT_RESCALE, LG_THERMOSTAT_CSVR = 0, 1, 2, 3
-LG_CONTROL_REMOVE_TRANSLATION, LG_CONTROL_REWRAP = 1, 2
+LG_CONTROL_REMOVE_TRANSLATION, LG_CONTROL_REWRAP, LG_CONTROL_REMOVE_ROTATION = 1, 2, 4
 
 
 class LgMdParams(ctypes.Structure):

@@ -60,7 +60,8 @@ static_assert(MD_VELOCITY_VERLET == LG_INTEGRATOR_VELOCITY_VERLET && MD_VERLET =
 static_assert(TH_NONE == LG_THERMOSTAT_NONE && TH_BERENDSEN == LG_THERMOSTAT_BERENDSEN &&
                   TH_RESCALE == LG_THERMOSTAT_RESCALE && TH_CSVR == LG_THERMOSTAT_CSVR,
               "thermostat values");
-static_assert(CTL_REMOVE_TRANSLATION == LG_CONTROL_REMOVE_TRANSLATION && CTL_REWRAP == LG_CONTROL_REWRAP,
+static_assert(CTL_REMOVE_TRANSLATION == LG_CONTROL_REMOVE_TRANSLATION && CTL_REWRAP == LG_CONTROL_REWRAP &&
+                  CTL_REMOVE_ROTATION == LG_CONTROL_REMOVE_ROTATION,
               "control values");
 
 struct HostSystem {
@@ -1374,7 +1375,7 @@ int lg_md_setup_ex(lg_engine* e, int32_t s, const lg_md_params* p) {
         return fail(e, LG_ERR_ARGUMENT, "unknown integrator");
     if (p->thermostat < LG_THERMOSTAT_NONE || p->thermostat > LG_THERMOSTAT_CSVR)
         return fail(e, LG_ERR_ARGUMENT, "unknown thermostat");
-    if (p->controls & ~(LG_CONTROL_REMOVE_TRANSLATION | LG_CONTROL_REWRAP))
+    if (p->controls & ~(LG_CONTROL_REMOVE_TRANSLATION | LG_CONTROL_REWRAP | LG_CONTROL_REMOVE_ROTATION))
         return fail(e, LG_ERR_ARGUMENT, "unknown control");
     // the constructors' checks: RescaleThermostat::new, BerendsenThermostat::new,
     // CSVRThermostat::from_rng (thermostats.rs:48-53, 102-109, 151-160)

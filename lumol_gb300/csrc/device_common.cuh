@@ -17,7 +17,7 @@ constexpr double FOUR_PI_EPSILON_0 = 7.197589831304046;
 // C ABI's LG_INTEGRATOR_*, LG_THERMOSTAT_* and LG_CONTROL_*).
 constexpr int MD_VELOCITY_VERLET = 0, MD_VERLET = 1, MD_LEAP_FROG = 2;
 constexpr int TH_NONE = 0, TH_BERENDSEN = 1, TH_RESCALE = 2, TH_CSVR = 3;
-constexpr uint32_t CTL_REMOVE_TRANSLATION = 1u, CTL_REWRAP = 2u;
+constexpr uint32_t CTL_REMOVE_TRANSLATION = 1u, CTL_REWRAP = 2u, CTL_REMOVE_ROTATION = 4u;
 
 // Pair potential table entry: one PairInteraction (energy/pairs.rs:57-95).
 struct PairDev {

@@ -147,15 +147,78 @@ static __device__ __noinline__ double sorted_ke_sum(const SysDev& s, const doubl
 // persistent kernel's order (mixed path) or per chunk (plain path), the
 // momenta per chunk.  Computed once per system and step; the next md_first (or
 // md_finalize at the end of a run) applies it.
+// RemoveRotation::control (controls.rs:47-71) on the velocities after a step,
+// before the thermostat's uniform scaling (which scales the angular momentum
+// and so the removed rotation alike): the centre of mass, then the angular
+// momentum and the reference's inertia matrix -sum m d (x) d + trace about it,
+// angular velocity = inverse(inertia) moment (types/matrix.rs:212-249), and
+// v -= (x - com) ^ angular, by one warp over the system's atoms in three passes.
+__device__ void remove_rotation(const SysDev& s, const double4_32a* __restrict__ posq,
+                                double4_32a* __restrict__ vel, int lane) {
+    double c[3] = {0.0, 0.0, 0.0};
+    for (int i = s.begin + lane; i < s.end; i += 32) {
+        double m = vel[i].w;
+        double4_32a p = posq[i];
+        c[0] = __dadd_rn(c[0], __dmul_rn(m, p.x));
+        c[1] = __dadd_rn(c[1], __dmul_rn(m, p.y));
+        c[2] = __dadd_rn(c[2], __dmul_rn(m, p.z));
+    }
+    double com[3];
+    for (int d = 0; d < 3; d++) com[d] = __ddiv_rn(warp_sum(c[d]), s.total_mass);
+    double L[3] = {0.0, 0.0, 0.0}, I[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int i = s.begin + lane; i < s.end; i += 32) {
+        double m = vel[i].w;
+        double4_32a p = posq[i], v = vel[i];
+        double d[3] = {__dsub_rn(p.x, com[0]), __dsub_rn(p.y, com[1]), __dsub_rn(p.z, com[2])};
+        double vv[3] = {v.x, v.y, v.z};
+        for (int k = 0; k < 3; k++) {  // moment += m (d ^ v)
+            int k1 = (k + 1) % 3, k2 = (k + 2) % 3;
+            L[k] = __dadd_rn(L[k], __dmul_rn(m, __dsub_rn(__dmul_rn(d[k1], vv[k2]), __dmul_rn(d[k2], vv[k1]))));
+        }
+        for (int a = 0; a < 3; a++)  // inertia += -m d (x) d
+            for (int b = 0; b < 3; b++) I[3 * a + b] = __dadd_rn(I[3 * a + b], __dmul_rn(-m, __dmul_rn(d[a], d[b])));
+    }
+    for (int k = 0; k < 3; k++) L[k] = warp_sum(L[k]);
+    for (int k = 0; k < 9; k++) I[k] = warp_sum(I[k]);
+    double tr = __dadd_rn(__dadd_rn(I[0], I[4]), I[8]);
+    I[0] = __dadd_rn(I[0], tr);
+    I[4] = __dadd_rn(I[4], tr);
+    I[8] = __dadd_rn(I[8], tr);
+    auto e = [&](int r, int q) { return I[3 * r + q]; };
+    auto dif = [&](int a, int b, int c2, int d2) {  // e(a) * e(b) - e(c) * e(d)
+        return __dsub_rn(__dmul_rn(I[a], I[b]), __dmul_rn(I[c2], I[d2]));
+    };
+    double det = __dadd_rn(__dsub_rn(__dmul_rn(e(0, 0), dif(4, 8, 7, 5)), __dmul_rn(e(0, 1), dif(3, 8, 5, 6))),
+                           __dmul_rn(e(0, 2), dif(3, 7, 4, 6)));
+    double id = __ddiv_rn(1.0, det);
+    double inv[9] = {__dmul_rn(dif(4, 8, 7, 5), id), __dmul_rn(dif(2, 7, 1, 8), id), __dmul_rn(dif(1, 5, 2, 4), id),
+                     __dmul_rn(dif(5, 6, 3, 8), id), __dmul_rn(dif(0, 8, 2, 6), id), __dmul_rn(dif(3, 2, 0, 5), id),
+                     __dmul_rn(dif(3, 7, 6, 4), id), __dmul_rn(dif(6, 1, 0, 7), id), __dmul_rn(dif(0, 4, 3, 1), id)};
+    double w[3];
+    for (int r = 0; r < 3; r++)
+        w[r] = __dadd_rn(__dadd_rn(__dmul_rn(inv[3 * r], L[0]), __dmul_rn(inv[3 * r + 1], L[1])),
+                         __dmul_rn(inv[3 * r + 2], L[2]));
+    for (int i = s.begin + lane; i < s.end; i += 32) {
+        double4_32a p = posq[i], v = vel[i];
+        double d[3] = {__dsub_rn(p.x, com[0]), __dsub_rn(p.y, com[1]), __dsub_rn(p.z, com[2])};
+        v.x = __dsub_rn(v.x, __dsub_rn(__dmul_rn(d[1], w[2]), __dmul_rn(d[2], w[1])));
+        v.y = __dsub_rn(v.y, __dsub_rn(__dmul_rn(d[2], w[0]), __dmul_rn(d[0], w[2])));
+        v.z = __dsub_rn(v.z, __dsub_rn(__dmul_rn(d[0], w[1]), __dmul_rn(d[1], w[0])));
+        vel[i] = v;
+    }
+}
+
 __global__ void __launch_bounds__(128) md_adjust_kernel(int nsys, const SysDev* __restrict__ sys,
                                                         const double* __restrict__ kepart,
                                                         const double* __restrict__ mom,
                                                         const unsigned long long* __restrict__ md_count, int gpw,
-                                                        int sorted, double* __restrict__ adj) {
+                                                        int sorted, const double4_32a* __restrict__ posq,
+                                                        double4_32a* __restrict__ vel, double* __restrict__ adj) {
     int si = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
     int lane = threadIdx.x & 31;
     if (si >= nsys) return;
     const SysDev& s = sys[si];
+    if (s.controls & CTL_REMOVE_ROTATION) remove_rotation(s, posq, vel, lane);
     double k = 0.0;
     if (s.thermostat != TH_NONE)
         k = sorted ? sorted_ke_sum(s, kepart, gpw, lane) : chunk_ke_sum(s, kepart, gpw, lane);
@@ -513,7 +576,7 @@ void launch_md_second(const Batch& b, cudaStream_t st) {
 void launch_md_adjust(const Batch& b, cudaStream_t st) {
     if (b.nsys)
         md_adjust_kernel<<<(b.nsys + 3) / 4, 128, 0, st>>>(b.nsys, b.sys, b.kepart, b.mom, b.md_count, 32 / b.tpa,
-                                                          b.precision == 1 ? 1 : 0, b.adj);
+                                                          b.precision == 1 ? 1 : 0, b.posq, b.vel, b.adj);
 }
 void launch_md_finalize(const Batch& b, cudaStream_t st) {
     if (b.ntiles) md_finalize_kernel<<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.adj, b.vel);

@@ -695,6 +695,11 @@ class RemoveTranslation:
     _bit = C.LG_CONTROL_REMOVE_TRANSLATION
 
 
+class RemoveRotation:
+    """RemoveRotation control (md/controls.rs:44-71)."""
+    _bit = C.LG_CONTROL_REMOVE_ROTATION
+
+
 class Rewrap:
     """Rewrap control (md/controls.rs:73-89): molecules' centres of mass back into the cell."""
     _bit = C.LG_CONTROL_REWRAP

@@ -1392,6 +1392,52 @@ void orc_md_run(orc_system* s, double* x, double* v, double* state, int integrat
             for (int64_t i = 0; i < n; i++)
                 for (int k = 0; k < 3; k++) v[3 * i + k] -= com[k];
         }
+        if (controls & 4u) {  // RemoveRotation (controls.rs:47-71)
+            double total = 0.0, com[3] = {0.0, 0.0, 0.0};  // Configuration::center_of_mass (configuration.rs:270-278)
+            for (int64_t i = 0; i < n; i++) {
+                total += s->mass[i];
+                for (int k = 0; k < 3; k++) com[k] += s->mass[i] * x[3 * i + k];
+            }
+            for (int k = 0; k < 3; k++) com[k] = com[k] / total;
+            double L[3] = {0.0, 0.0, 0.0}, I[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+            for (int64_t i = 0; i < n; i++) {
+                double d[3], vv[3];
+                for (int k = 0; k < 3; k++) {
+                    d[k] = x[3 * i + k] - com[k];
+                    vv[k] = v[3 * i + k];
+                }
+                double cr[3] = {d[1] * vv[2] - d[2] * vv[1], d[2] * vv[0] - d[0] * vv[2], d[0] * vv[1] - d[1] * vv[0]};
+                for (int k = 0; k < 3; k++) L[k] += s->mass[i] * cr[k];
+                for (int a = 0; a < 3; a++)
+                    for (int b = 0; b < 3; b++) I[a][b] += -s->mass[i] * (d[a] * d[b]);
+            }
+            double tr = I[0][0] + I[1][1] + I[2][2];
+            for (int k = 0; k < 3; k++) I[k][k] += tr;
+            // Matrix3::inverse (types/matrix.rs:212-249)
+            double det = I[0][0] * (I[1][1] * I[2][2] - I[2][1] * I[1][2]) -
+                         I[0][1] * (I[1][0] * I[2][2] - I[1][2] * I[2][0]) +
+                         I[0][2] * (I[1][0] * I[2][1] - I[1][1] * I[2][0]);
+            double id = 1.0 / det;
+            double r[3][3];
+            r[0][0] = (I[1][1] * I[2][2] - I[2][1] * I[1][2]) * id;
+            r[0][1] = (I[0][2] * I[2][1] - I[0][1] * I[2][2]) * id;
+            r[0][2] = (I[0][1] * I[1][2] - I[0][2] * I[1][1]) * id;
+            r[1][0] = (I[1][2] * I[2][0] - I[1][0] * I[2][2]) * id;
+            r[1][1] = (I[0][0] * I[2][2] - I[0][2] * I[2][0]) * id;
+            r[1][2] = (I[1][0] * I[0][2] - I[0][0] * I[1][2]) * id;
+            r[2][0] = (I[1][0] * I[2][1] - I[2][0] * I[1][1]) * id;
+            r[2][1] = (I[2][0] * I[0][1] - I[0][0] * I[2][1]) * id;
+            r[2][2] = (I[0][0] * I[1][1] - I[1][0] * I[0][1]) * id;
+            double w[3];
+            for (int a = 0; a < 3; a++) w[a] = r[a][0] * L[0] + r[a][1] * L[1] + r[a][2] * L[2];
+            for (int64_t i = 0; i < n; i++) {
+                double d[3];
+                for (int k = 0; k < 3; k++) d[k] = x[3 * i + k] - com[k];
+                v[3 * i] -= d[1] * w[2] - d[2] * w[1];
+                v[3 * i + 1] -= d[2] * w[0] - d[0] * w[2];
+                v[3 * i + 2] -= d[0] * w[1] - d[1] * w[0];
+            }
+        }
         if (controls & 2u) {  // Rewrap: Molecule::wrap (sys/config/molecules.rs:256-296)
             double L[3] = {s->cell.a, s->cell.b, s->cell.c};
             for (auto& mr : s->mol_range) {

@@ -146,7 +146,8 @@ double orc_temperature(const orc_system* s, const double* velocities);
  * (md/integrators.rs); thermostat 0 none, 1 Berendsen(T0, tau), 2
  * Rescale(T0, tol), 3 CSVR(T0, tau) (md/thermostats.rs) with the noise of
  * SplitMix64 streams of (seed, count) (*count: thermostat applications so far,
- * in / out); controls bit 1 RemoveTranslation, bit 2 Rewrap (md/controls.rs).
+ * in / out); controls bit 1 RemoveTranslation, bit 4 RemoveRotation, bit 2
+ * Rewrap (md/controls.rs), applied in that order.
  * `state` (3n) is the integrator's: accelerations, or Verlet's positions at
  * t - dt (orc_verlet_setup). */
 void orc_md_run(orc_system* s, double* positions, double* velocities, double* state, int integrator, double dt,

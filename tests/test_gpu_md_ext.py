@@ -33,6 +33,8 @@ CASES = [  # integrator, thermostat, controls
     ("leapfrog", "rescale", ("rewrap",)),
     ("leapfrog", "csvr", ()),
     ("vv", "rescale", ("translation", "rewrap")),
+    ("vv", "berendsen", ("translation", "rotation")),
+    ("leapfrog", None, ("rotation", "rewrap")),
 ]
 
 
@@ -44,7 +46,8 @@ def thermostat(name):
 
 
 def controls(names):
-    return tuple({"translation": lg.RemoveTranslation, "rewrap": lg.Rewrap}[c] for c in names)
+    return tuple({"translation": lg.RemoveTranslation, "rewrap": lg.Rewrap, "rotation": lg.RemoveRotation}[c]
+                 for c in names)
 
 
 def fluid(precision="fp64"):
@@ -101,6 +104,11 @@ def test_controls_literals():
     s = two_silver([15.0, 0.0, 0.0], [[0.0, 0.0, 0.0], [0.0, 0.0, 0.0]])
     lg.MolecularDynamics(lg.VelocityVerlet(1.0), None, (lg.Rewrap,)).run(s, 1)
     assert s.positions.tolist() == [[0.0, 0.0, 0.0], [5.0, 0.0, 0.0]]
+    # controls.rs:109-122 (RemoveRotation): a step of 1e-300 fs moves the atoms by
+    # about 1e-300 A, which leaves terms of that size in the result
+    s = two_silver([1.0, 0.0, 0.0], [[0.0, 1.0, 0.0], [0.0, -1.0, 2.0]])
+    lg.MolecularDynamics(lg.VelocityVerlet(1e-300), None, (lg.RemoveRotation,)).run(s, 1)
+    assert np.abs(s.velocities - [[0.0, 0.0, 1.0], [0.0, 0.0, 1.0]]).max() < 1e-12
 
 
 def helium_gas(n_side=10, temperature=300.0, seed=42):

@@ -10,7 +10,7 @@ from lumol_gb300.units import K_BOLTZMANN
 
 VV, VERLET, LEAP = 0, 1, 2
 NONE, BERENDSEN, RESCALE, CSVR = 0, 1, 2, 3
-REMOVE_TRANSLATION, REWRAP = 1, 2
+REMOVE_TRANSLATION, REWRAP, REMOVE_ROTATION = 1, 2, 4
 
 
 def two_silver(x1):
@@ -26,6 +26,15 @@ def test_remove_translation_literals(oracle_lib):
     orc = oracle.Oracle(s)
     _, v1, _, _ = orc.md_run(s.positions, v, np.zeros((2, 3)), 1, dt=1e-3, controls=REMOVE_TRANSLATION)
     assert v1.tolist() == [[0.0, 1.0, 0.0], [0.0, -1.0, 0.0]]
+
+
+def test_remove_rotation_literals(oracle_lib):
+    # controls.rs:109-122 (dt = 0: the step leaves the positions as they are)
+    s = two_silver([1.0, 0.0, 0.0])
+    v = np.array([[0.0, 1.0, 0.0], [0.0, -1.0, 2.0]])
+    orc = oracle.Oracle(s)
+    _, v1, _, _ = orc.md_run(s.positions, v, np.zeros((2, 3)), 1, dt=0.0, controls=REMOVE_ROTATION)
+    assert v1.tolist() == [[0.0, 0.0, 1.0], [0.0, 0.0, 1.0]]
 
 
 def test_rewrap_literals(oracle_lib):
