@@ -102,6 +102,12 @@ typedef struct {
     double cutoff;
     double scale14;       /* factor of LG_RESTRICT_SCALE14 */
     double p3, p4;        /* BMH: {a, c, d, sigma, rho} = p0..p4; Mie: {sigma, epsilon, n, m} = p0..p3 */
+    int32_t table_size;   /* > 0: TableComputation::new(potential, table_size, table_max)
+                             (energy/computations.rs:63-128): energies and forces interpolated
+                             from table_size points on [0, table_max), zero beyond; tail
+                             corrections from the potential itself (computations.rs:151-173) */
+    int32_t table_pad;
+    double table_max;
 } lg_pair;
 
 /* A bond or angle potential (Harmonic or Null). */

@@ -31,6 +31,7 @@ from .system import (
     RescaleThermostat,
     Rewrap,
     System,
+    TableComputation,
     Translate,
     UnitCell,
     VelocityVerlet,
@@ -53,7 +54,7 @@ __all__ = [
     "units", "EngineError", "BerendsenThermostat", "BornMayerHuggins", "Buckingham", "CSVRThermostat", "Engine",
     "Ewald", "Gaussian", "Harmonic", "LeapFrog", "LennardJones", "Mie", "MolecularDynamics", "MonteCarlo", "Morse",
     "Translate", "NullPotential", "PairInteraction", "PairRestriction", "RemoveRotation", "RemoveTranslation", "RescaleThermostat",
-    "Rewrap", "System", "UnitCell", "VelocityVerlet", "Verlet", "Wolf", "md_params",
+    "Rewrap", "System", "TableComputation", "UnitCell", "VelocityVerlet", "Verlet", "Wolf", "md_params",
     "LG_TERM_ALL", "LG_TERM_ANGLES", "LG_TERM_BONDS", "LG_TERM_COUL_KSPACE", "LG_TERM_COUL_REAL",
     "LG_TERM_COUL_SELF", "LG_TERM_PAIRS", "LG_TERM_TAIL",
 ]

@@ -54,6 +54,9 @@ class LgPair(ctypes.Structure):
         ("scale14", ctypes.c_double),
         ("p3", ctypes.c_double),
         ("p4", ctypes.c_double),
+        ("table_size", ctypes.c_int32),
+        ("table_pad", ctypes.c_int32),
+        ("table_max", ctypes.c_double),
     ]
 
 

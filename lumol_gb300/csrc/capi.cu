@@ -158,6 +158,65 @@ double pot_energy(const lg_pair& p, double r) {
             return 0.0;
     }
 }
+// Potential::force (functions.rs:90-93, 294-299, 141-143, 361-366, 420-423, 479-481, 560-565)
+double pot_force(const lg_pair& p, double r) {
+    switch (p.type) {
+        case LG_PAIR_LJ: {
+            double s6 = powi6(p.p0 / r);
+            return -24.0 * p.p1 * (s6 - 2.0 * (s6 * s6)) / r;
+        }
+        case LG_PAIR_BUCKINGHAM: {
+            double r3 = r * r * r;
+            double r7 = r3 * r3 * r;
+            double e = std::exp(-r / p.p2);
+            return p.p0 / p.p2 * e - 6.0 * p.p1 / r7;
+        }
+        case LG_PAIR_HARMONIC:
+            return p.p0 * (p.p1 - r);
+        case LG_PAIR_BMH: {
+            double r2 = r * r;
+            double r7 = r2 * r2 * r2 * r;
+            double e = std::exp((p.p3 - r) / p.p4);
+            return p.p0 / p.p4 * e - 6.0 * p.p1 / r7 + 8.0 * p.p2 / (r7 * r2);
+        }
+        case LG_PAIR_MORSE: {  // as written there: 2 depth (1 - e^2) a
+            double e = std::exp((p.p1 - r) * p.p0);
+            return 2.0 * p.p2 * (1.0 - e * e) * p.p0;
+        }
+        case LG_PAIR_GAUSSIAN:
+            return 2.0 * p.p1 * r * pot_energy(p, r);
+        case LG_PAIR_MIE: {
+            double sr = p.p0 / r;
+            double rep = std::pow(sr, p.p2), att = std::pow(sr, p.p3);
+            return mie_prefactor(p) * (p.p2 * rep - p.p3 * att) / r;
+        }
+        default:
+            return 0.0;
+    }
+}
+
+// TableComputation::new (energy/computations.rs:101-121): (energy, force) at
+// r = i delta, delta = max / size.
+void build_table(const lg_pair& p, std::vector<double2>& out) {
+    double delta = p.table_max / (double)p.table_size;
+    for (int32_t i = 0; i < p.table_size; i++) {
+        double r = (double)i * delta;
+        out.push_back(make_double2(pot_energy(p, r), pot_force(p, r)));
+    }
+}
+// Computation::compute_energy (computations.rs:123-133) on a table built above
+double table_energy(const lg_pair& p, const double2* t, double r) {
+    double delta = p.table_max / (double)p.table_size;
+    double binf = std::floor(r / delta);
+    if (binf < (double)(p.table_size - 1)) {
+        size_t bin = (size_t)binf;
+        double dx = r - (double)bin * delta;
+        double slope = (t[bin + 1].x - t[bin].x) / delta;
+        return t[bin].x + dx * slope;
+    }
+    return 0.0;
+}
+
 // PairPotential::tail_energy / tail_virial (functions.rs:97-111, 303-318)
 double pot_tail_energy(const lg_pair& p, double rc) {
     if (p.type == LG_PAIR_LJ) {
@@ -319,6 +378,8 @@ struct lg_engine {
     DBuf<int> nlo, rev;
     DBuf<double4_32a> pf;
     DBuf<PairDevF> ptabf;
+    DBuf<double2> table;  // TableComputation tables (plain path)
+    DBuf<float2> tablef;  // the same in FP32 (mixed path)
     DBuf<KVecF> kvecf;
     DBuf<float2> eikrf, rhof;
     DBuf<SysDev> sysdev;
@@ -458,6 +519,7 @@ int commit(lg_engine* e) {
     std::vector<int> h_kind(n), h_mol(n), h_sysid(n);
     std::vector<PairDev> h_ptab;
     std::vector<PairDevF> h_ptabf;
+    std::vector<double2> h_table;  // TableComputation tables of the pair entries
     std::vector<KVecDev> h_kvec;
     std::vector<std::vector<std::pair<int, int8_t>>> spec(n);
     struct Term {
@@ -535,6 +597,16 @@ int commit(lg_engine* e) {
             if (p.type == LG_PAIR_MIE) q.aux = mie_prefactor(p);
             q.cutoff = p.cutoff;
             q.shift = p.shifted ? pot_energy(p, p.cutoff) : 0.0;  // pairs.rs:86-95
+            const bool tab = p.type != LG_PAIR_ABSENT && p.table_size > 0;
+            size_t toff = h_table.size();
+            if (tab) {  // the table replaces the potential (its tails stay the potential's)
+                build_table(p, h_table);
+                q.type = PAIR_TABLE;
+                q.tsize = p.table_size;
+                q.tdelta = p.table_max / (double)p.table_size;
+                q.table = reinterpret_cast<const double2*>(toff);  // an offset until the upload
+                q.shift = p.shifted ? table_energy(p, h_table.data() + toff, p.cutoff) : 0.0;
+            }
             q.scale14 = p.scale14;
             q.cutoff2_f = (float)(p.cutoff * p.cutoff);
             if (p.type == LG_PAIR_LJ) {
@@ -577,6 +649,13 @@ int commit(lg_engine* e) {
                 qf.b = (float)p.p0;
                 qf.c = (float)p.p2;
                 qf.d = (float)p.p3;
+            }
+            if (tab) {
+                qf.type = PAIR_TABLE;
+                qf.a = (float)(1.0 / q.tdelta);
+                qf.b = (float)q.tdelta;
+                qf.c = (float)(p.table_size - 1);
+                qf.table = reinterpret_cast<const float2*>(toff);
             }
             qf.rc2 = (float)(p.cutoff * p.cutoff);
             qf.shift = (float)q.shift;
@@ -777,6 +856,16 @@ int commit(lg_engine* e) {
                            (float)v.energy};
     }
     CUDA_TRY(e, e->ptabf.alloc(h_ptabf.size()));
+    // TableComputation tables: FP64 for the plain path, FP32 for the mixed path;
+    // the pair entries get their table's device address
+    CUDA_TRY(e, e->table.alloc(std::max<size_t>(h_table.size(), 1)));
+    CUDA_TRY(e, e->tablef.alloc(std::max<size_t>(h_table.size(), 1)));
+    std::vector<float2> h_tablef(h_table.size());
+    for (size_t k = 0; k < h_table.size(); k++) h_tablef[k] = make_float2((float)h_table[k].x, (float)h_table[k].y);
+    for (PairDev& q : h_ptab)
+        if (q.type == PAIR_TABLE) q.table = e->table.p + reinterpret_cast<size_t>(q.table);
+    for (PairDevF& q : h_ptabf)
+        if (q.type == PAIR_TABLE) q.table = e->tablef.p + reinterpret_cast<size_t>(q.table);
     CUDA_TRY(e, e->posfx.alloc(n));  // fixed-point copy: the mixed path's positions, the plain path's classification
     CUDA_TRY(e, e->nlo.alloc(mixed ? 1 : n));
     CUDA_TRY(e, e->rev.alloc(mixed ? 1 : (size_t)n * maxnb));
@@ -843,6 +932,12 @@ int commit(lg_engine* e) {
     CUDA_TRY(e, cudaMemsetAsync(e->md_count.p, 0, std::max(nsys, 1) * sizeof(unsigned long long), st));
     CUDA_TRY(e, cudaMemcpyAsync(e->mol_start.p, h_mol_start.data(), h_mol_start.size() * sizeof(int),
                                 cudaMemcpyHostToDevice, st));
+    if (!h_table.empty()) {
+        CUDA_TRY(e, cudaMemcpyAsync(e->table.p, h_table.data(), h_table.size() * sizeof(double2),
+                                    cudaMemcpyHostToDevice, st));
+        CUDA_TRY(e, cudaMemcpyAsync(e->tablef.p, h_tablef.data(), h_tablef.size() * sizeof(float2),
+                                    cudaMemcpyHostToDevice, st));
+    }
     CUDA_TRY(e, cudaMemcpyAsync(e->ptab.p, h_ptab.data(), h_ptab.size() * sizeof(PairDev), cudaMemcpyHostToDevice, st));
     CUDA_TRY(e, cudaMemcpyAsync(e->ptabf.p, h_ptabf.data(), h_ptabf.size() * sizeof(PairDevF), cudaMemcpyHostToDevice,
                                 st));
@@ -1207,8 +1302,10 @@ int lg_set_pairs(lg_engine* e, int32_t s, int32_t nk, const lg_pair* table) {
             const lg_pair& q = table[c * nk + a];
             if (p.type != q.type || p.cutoff != q.cutoff || p.p0 != q.p0 || p.p1 != q.p1 || p.p2 != q.p2 ||
                 p.p3 != q.p3 || p.p4 != q.p4 || p.restriction != q.restriction || p.shifted != q.shifted ||
-                p.tail != q.tail)
+                p.tail != q.tail || p.table_size != q.table_size || p.table_max != q.table_max)
                 return fail(e, LG_ERR_ARGUMENT, "the pair table must be symmetric");
+            if (p.type != LG_PAIR_ABSENT && (p.table_size < 0 || (p.table_size > 0 && !(p.table_max > 0.0))))
+                return fail(e, LG_ERR_ARGUMENT, "a TableComputation needs a positive size and maximum");
             if (p.type < LG_PAIR_ABSENT || p.type > LG_PAIR_MIE)
                 return fail(e, LG_ERR_ARGUMENT, "unknown pair potential");
             // the reference's constructors panic on these (functions.rs:468-469, 540-541)

@@ -34,7 +34,14 @@ struct PairDev {
     double c12, c6;       // LJ: 4 eps sigma^12, 4 eps sigma^6 (plain path, interior pairs)
     double p3, p4;        // BMH: sigma, rho; Mie: m
     double aux;           // Mie: energy prefactor
+    // a TableComputation (type PAIR_TABLE): (energy, force) at r = i delta, i < tsize
+    const double2* table;
+    int32_t tsize, tpad;
+    double tdelta;
 };
+
+// Device type of a pair tabulated with TableComputation (any potential kind).
+constexpr int PAIR_TABLE = 9;
 
 // FP32 pair table entry of the mixed path.
 //   LJ: a = 4 eps sigma^12, b = 4 eps sigma^6;  Buckingham: a = A, b = C, c = 1 / rho;
@@ -42,6 +49,7 @@ struct PairDev {
 struct alignas(16) PairDevF {
     int32_t type, restriction, pad0, pad1;
     float a, b, c, rc2, shift, scale14, d, e;  // d, e: BMH d and sigma; Mie m
+    const float2* table;  // PAIR_TABLE: (energy, force) at r = i delta, a = 1 / delta, c = tsize - 1
 };
 
 // FP32 k-vector of the mixed Ewald field kernel.
@@ -484,6 +492,20 @@ __device__ __forceinline__ void pair_energy_force(const PairDev& p, double r, do
             double rep = pow(sr, p.p2), att = pow(sr, p.p3);
             e = p.aux * (rep - att);
             f = p.aux * (p.p2 * rep - p.p3 * att) / r;
+            break;
+        }
+        case PAIR_TABLE: {  // Computation::compute_energy / compute_force (computations.rs:123-144)
+            double binf = floor(__ddiv_rn(r, p.tdelta));
+            if (binf < (double)(p.tsize - 1)) {
+                int bin = (int)binf;
+                double2 t0 = p.table[bin], t1 = p.table[bin + 1];
+                double dx = __dsub_rn(r, __dmul_rn((double)bin, p.tdelta));
+                e = __dadd_rn(t0.x, __dmul_rn(dx, __ddiv_rn(__dsub_rn(t1.x, t0.x), p.tdelta)));
+                f = __dadd_rn(t0.y, __dmul_rn(dx, __ddiv_rn(__dsub_rn(t1.y, t0.y), p.tdelta)));
+            } else {
+                e = 0.0;
+                f = 0.0;
+            }
             break;
         }
         default:

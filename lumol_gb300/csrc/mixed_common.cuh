@@ -93,6 +93,20 @@ __device__ __forceinline__ float pair_mixed(const PairDevF& p, float r2, float i
             fr = rmul(rmul(p.a, rfma(p.c, rep, -rmul(p.d, att))), inv_r2);
             return rsub(rmul(p.a, rsub(rep, att)), p.shift);
         }
+        case PAIR_TABLE: {  // TableComputation (computations.rs:123-144) on FP32 tables
+            float r = rmul(r2, inv_r);
+            float binf = floorf(rmul(r, p.a));
+            if (binf < p.c) {
+                int bin = (int)binf;
+                float2 t0 = __ldg(p.table + bin), t1 = __ldg(p.table + bin + 1);
+                float dx = rfma(-(float)bin, p.b, r);  // r - bin delta (b = delta)
+                float e = rfma(dx, rmul(rsub(t1.x, t0.x), p.a), t0.x);
+                fr = rmul(rfma(dx, rmul(rsub(t1.y, t0.y), p.a), t0.y), inv_r);
+                return rsub(e, p.shift);
+            }
+            fr = 0.0f;
+            return rsub(0.0f, p.shift);
+        }
         default:
             fr = 0.0f;
             return 0.0f;

@@ -136,6 +136,22 @@ class Mie:
         return C.LG_PAIR_MIE, (self.sigma, self.epsilon, self.n, self.m)
 
 
+class TableComputation:
+    """TableComputation::new(potential, size, max) (energy/computations.rs:63-173):
+    the potential's energy and force tabulated at r = i max / size,
+    interpolated linearly, zero from the last point on; the tail corrections
+    are the potential's own."""
+
+    def __init__(self, potential, size: int, max: float):
+        if size <= 0 or not max > 0.0:
+            raise ValueError("TableComputation needs a positive size and maximum")
+        self.potential = potential
+        self._table = (int(size), float(max))
+
+    def _params(self):
+        return self.potential._params()
+
+
 class PairInteraction:
     """PairInteraction (lumol-core/src/energy/pairs.rs:22-296)."""
 
@@ -162,7 +178,9 @@ class PairInteraction:
         kind, params = self.potential._params()
         p0, p1, p2, p3, p4 = (list(params) + [0.0] * 5)[:5]
         r, s14 = _restriction(self.restriction)
-        return C.LgPair(kind, int(self.shifted_energy), r, int(self.tail), p0, p1, p2, self.cutoff, s14, p3, p4)
+        tsize, tmax = getattr(self.potential, "_table", (0, 0.0))
+        return C.LgPair(kind, int(self.shifted_energy), r, int(self.tail), p0, p1, p2, self.cutoff, s14, p3, p4,
+                        tsize, 0, tmax)
 
 
 class Ewald:

@@ -45,7 +45,8 @@ class OrcPair(ctypes.Structure):
     _fields_ = [("type", ctypes.c_int32), ("shifted", ctypes.c_int32), ("restriction", ctypes.c_int32),
                 ("tail", ctypes.c_int32), ("p0", ctypes.c_double), ("p1", ctypes.c_double),
                 ("p2", ctypes.c_double), ("cutoff", ctypes.c_double), ("scale14", ctypes.c_double),
-                ("p3", ctypes.c_double), ("p4", ctypes.c_double)]
+                ("p3", ctypes.c_double), ("p4", ctypes.c_double), ("table_size", ctypes.c_int32),
+                ("table_pad", ctypes.c_int32), ("table_max", ctypes.c_double)]
 
 
 class OrcBonded(ctypes.Structure):
@@ -154,8 +155,9 @@ class Oracle:
                     p0, p1, p2, p3, p4 = (list(params) + [0.0] * 5)[:5]
                     r = inter.restriction
                     rr, s14 = (r[0], r[1]) if isinstance(r, tuple) else (r, 1.0)
+                    tsize, tmax = getattr(inter.potential, "_table", (0, 0.0))
                     pairs[a * nk + b] = OrcPair(kind, int(inter.shifted_energy), rr, int(inter.tail),
-                                                p0, p1, p2, inter.cutoff, s14, p3, p4)
+                                                p0, p1, p2, inter.cutoff, s14, p3, p4, tsize, 0, tmax)
                 bp = spec.bond_potentials.get(tuple(sorted((na, nb))))
                 if bp is not None:
                     kind, (k, x0, _) = bp._params()
@@ -277,10 +279,12 @@ class Oracle:
 
 
 def pair_eval(potential_type: int, params, cutoff: float, r: float, shifted: bool = False,
-              tail: bool = False):
-    """(energy, force, tail_energy, tail_virial) of one PairInteraction at r."""
+              tail: bool = False, table=None):
+    """(energy, force, tail_energy, tail_virial) of one PairInteraction at r;
+    table = (size, max) evaluates TableComputation::new(potential, size, max)."""
     p0, p1, p2, p3, p4 = (list(params) + [0.0] * 5)[:5]
-    pair = OrcPair(potential_type, int(shifted), 0, int(tail), p0, p1, p2, cutoff, 1.0, p3, p4)
+    tsize, tmax = table if table else (0, 0.0)
+    pair = OrcPair(potential_type, int(shifted), 0, int(tail), p0, p1, p2, cutoff, 1.0, p3, p4, tsize, 0, tmax)
     out = [ctypes.c_double() for _ in range(4)]
     load().orc_pair_eval(ctypes.byref(pair), r, *[ctypes.byref(o) for o in out])
     return tuple(o.value for o in out)

@@ -153,6 +153,37 @@ inline double powi6(double x) {
 struct PairPot {
     orc_pair d;
     double shift = 0.0;
+    // TableComputation (energy/computations.rs:63-144): tabulated at r = i delta
+    std::vector<double> te, tf;
+    double tdelta = 0.0;
+
+    // TableComputation::new (computations.rs:101-121); call after d is set
+    void build_table() {
+        te.clear();
+        tf.clear();
+        if (d.table_size <= 0) return;
+        tdelta = d.table_max / (double)d.table_size;
+        for (int32_t i = 0; i < d.table_size; i++) {
+            double r = (double)i * tdelta;
+            te.push_back(pot_energy(r));
+            tf.push_back(pot_force(r));
+        }
+    }
+    // Computation::compute_energy / compute_force (computations.rs:123-144)
+    static double interpolate(const std::vector<double>& t, double delta, double r) {
+        double binf = std::floor(r / delta);
+        if (binf < 0.0 || binf >= (double)t.size()) return 0.0;
+        size_t bin = (size_t)binf;
+        if (bin < t.size() - 1) {
+            double dx = r - (double)bin * delta;
+            double slope = (t[bin + 1] - t[bin]) / delta;
+            return t[bin] + dx * slope;
+        }
+        return 0.0;
+    }
+    // the PairPotential's energy / force: the table when there is one
+    double comp_energy(double r) const { return d.table_size > 0 ? interpolate(te, tdelta, r) : pot_energy(r); }
+    double comp_force(double r) const { return d.table_size > 0 ? interpolate(tf, tdelta, r) : pot_force(r); }
 
     // Potential::energy
     double pot_energy(double r) const {
@@ -315,17 +346,17 @@ struct PairPot {
     // PairInteraction (energy/pairs.rs:185-296)
     double energy(double r) const {
         if (r >= d.cutoff) return 0.0;
-        double e = pot_energy(r);
+        double e = comp_energy(r);
         return d.shifted ? e - shift : e;
     }
     double force(double r) const {
         if (r >= d.cutoff) return 0.0;
-        return pot_force(r);
+        return comp_force(r);
     }
     // PairPotential::virial default (energy/mod.rs:137-142) behind the cutoff test
     M3 virial(const V3& r) const {
         if (vnorm(r) >= d.cutoff) return mzero();
-        double fact = pot_force(vnorm(r));
+        double fact = comp_force(vnorm(r));
         V3 rn = vnormalized(r);
         V3 f = vscale(fact, rn);
         return tensorial(f, r);
@@ -1087,7 +1118,8 @@ orc_system* orc_create(const orc_desc* d) {
     for (size_t p = 0; p < s->pairs.size(); p++) {
         s->pairs[p].d = d->pairs[p];
         // PairInteraction::shifted: shift = potential.energy(cutoff) (pairs.rs:86-95)
-        if (d->pairs[p].shifted) s->pairs[p].shift = s->pairs[p].pot_energy(d->pairs[p].cutoff);
+        s->pairs[p].build_table();
+        if (d->pairs[p].shifted) s->pairs[p].shift = s->pairs[p].comp_energy(d->pairs[p].cutoff);
     }
     s->bond_pots.resize((size_t)s->nk * s->nk);
     for (size_t p = 0; p < s->bond_pots.size(); p++) s->bond_pots[p].d = d->bond_pots ? d->bond_pots[p] : orc_bonded{0, 0, 0, 0};
@@ -1464,7 +1496,8 @@ void orc_pair_eval(const orc_pair* d, double r, double* energy, double* force, d
                    double* tail_virial) {
     PairPot p;
     p.d = *d;
-    if (d->shifted) p.shift = p.pot_energy(d->cutoff);
+    p.build_table();
+    if (d->shifted) p.shift = p.comp_energy(d->cutoff);
     *energy = p.energy(r);
     *force = p.force(r);
     *tail_energy = p.tail_energy();

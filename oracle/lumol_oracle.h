@@ -74,6 +74,9 @@ typedef struct {
     double p3, p4;       /* further parameters: BMH {a, c, d, sigma, rho} = p0..p4;
                             Morse {a, x0, depth} = p0..p2; Gaussian {a, b} = p0, p1;
                             Mie {sigma, epsilon, n, m} = p0..p3 */
+    int32_t table_size;  /* > 0: TableComputation of the potential (energy/computations.rs:63-173) */
+    int32_t table_pad;
+    double table_max;
 } orc_pair;
 
 /* Bond / angle potential (Harmonic or absent). */

@@ -91,6 +91,10 @@ def _family_interactions(family: str, cutoff: float):
         "morse": (lg.Morse(1.5, 3.8, eps), lg.Morse(1.4, 4.0, 1.3 * eps), lg.Morse(1.3, 4.2, 1.6 * eps)),
         "gaussian": (lg.Gaussian(2.0 * eps, 0.08), lg.Gaussian(2.5 * eps, 0.07), lg.Gaussian(3.0 * eps, 0.06)),
         "mie": (lg.Mie(3.405, eps, 12.0, 6.0), lg.Mie(3.6, 1.3 * eps, 12.5, 6.5), lg.Mie(3.8, 1.6 * eps, 14.0, 7.0)),
+        # TableComputation of LJ / Mie / LJ, 4000 points up to 10 A
+        "table": (lg.TableComputation(lg.LennardJones(3.405, eps), 4000, 10.0),
+                  lg.TableComputation(lg.Mie(3.6, 1.3 * eps, 12.5, 6.5), 4000, 10.0),
+                  lg.TableComputation(lg.LennardJones(3.8, 1.6 * eps), 4000, 10.0)),
     }[family]
     if family == "lj":  # the historical LJ fluid: shifted, tail, plain
         tail = lg.PairInteraction(pots[1], cutoff)
@@ -105,7 +109,7 @@ def random_lj_fluid(n: int, density: float, seed: int, cutoff: float, family: st
                     precision: str = "fp64") -> lg.System:
     """Jittered simple-cubic fluid of `n` particles (two kinds) at `density` (1/A^3),
     with pair potentials of one family ("lj", "buckingham", "bmh", "morse",
-    "gaussian", "mie")."""
+    "gaussian", "mie", "table")."""
     rng = np.random.default_rng(seed)
     side = int(np.ceil(n ** (1.0 / 3.0)))
     length = (n / density) ** (1.0 / 3.0)

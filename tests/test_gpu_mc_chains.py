@@ -85,7 +85,7 @@ def test_coulomb_systems_are_rejected():
         batch.mc_setup(0, 300.0, 0.3, 1)
 
 
-@pytest.mark.parametrize("family", ["bmh", "morse", "gaussian", "mie"])
+@pytest.mark.parametrize("family", ["bmh", "morse", "gaussian", "mie", "table"])
 def test_chains_with_other_pair_potentials(family):
     """FP64 chains follow the oracle move for move; mixed chains keep their
     running energy within 1e-5 of a fresh evaluation."""

@@ -56,7 +56,7 @@ def test_mixed_water():
     check(s)
 
 
-@pytest.mark.parametrize("family", ["buckingham", "bmh", "morse", "gaussian", "mie"])
+@pytest.mark.parametrize("family", ["buckingham", "bmh", "morse", "gaussian", "mie", "table"])
 def test_mixed_unwrapped_fluid(family):
     check(systems.random_lj_fluid(700, 0.02, 5, 9.0, family=family, precision="mixed"))
 

@@ -80,7 +80,7 @@ def test_reference_unit_systems():
                                                lg.LG_TERM_ANGLES])
 
 
-@pytest.mark.parametrize("family", ["lj", "buckingham", "bmh", "morse", "gaussian", "mie"])
+@pytest.mark.parametrize("family", ["lj", "buckingham", "bmh", "morse", "gaussian", "mie", "table"])
 def test_two_kind_fluid_unwrapped(family):
     s = systems.random_lj_fluid(700, 0.02, 5, 9.0, family=family)
     assert_parity(s, [lg.LG_TERM_ALL, lg.LG_TERM_PAIRS, lg.LG_TERM_TAIL])

@@ -123,22 +123,22 @@ def test_persistent_list_overflow_is_regrown_and_replayed():
 
 
 def test_persistent_other_pair_potentials():
-    """Fluids of the Born-Mayer-Huggins, Morse, Gaussian and Mie potentials
-    (plain, shifted and tail-corrected pairs of two kinds) in one batch with
+    """Fluids of the Born-Mayer-Huggins, Morse, Gaussian and Mie potentials and
+    of TableComputations (plain, shifted and tail-corrected pairs of two kinds) in one batch with
     an LJ replica, two of them under a thermostat: the persistent launches
     give the per-step kernels' trajectories bit for bit."""
     import systems as fluids
 
     def make():
         out = [fluids.random_lj_fluid(400 + 50 * k, 0.02, 30 + k, 9.0, family=f, precision="mixed")
-               for k, f in enumerate(["bmh", "morse", "gaussian", "mie"])]
+               for k, f in enumerate(["bmh", "morse", "gaussian", "mie", "table"])]
         return out + [workloads.lj_replica(500, 0.7, 150.0, 77, "mixed")]
 
     states = []
     for persistent in (True, False):
         systems = make()
         batch = Batch(systems, precision="mixed", persistent=persistent, threads_per_atom=8)
-        batch.md_setup([1.0] * len(systems), [None, (200.0, 50.0), None, (150.0, 20.0), None])
+        batch.md_setup([1.0] * len(systems), [None, (200.0, 50.0), None, (150.0, 20.0), None, None])
         batch.md_run(40)
         states.append([batch.state(s) for s in range(len(systems))])
         batch.engine.close()

@@ -126,6 +126,24 @@ def test_mie_literals(oracle_lib):
     assert d(2.0)[1] == 120.0
 
 
+def test_table_computation_literals(oracle_lib):
+    # computations.rs:180-205: TableComputation of Harmonic {k 50, x0 2}, 1000 points up to 4
+    t = lambda r: oracle.pair_eval(HARM, (50.0, 2.0), 1e9, r, table=(1000, 4.0))
+    assert t(2.5)[:2] == (6.25, -25.0)
+    delta = 4.0 / 1000.0
+    assert t(4.0 - 2.0 * delta)[:2] == (99.2016, -99.6)
+    for r in (4.0 - delta, 4.0, 4.1):
+        assert t(r)[:2] == (0.0, 0.0)
+    # the tail corrections are the potential's own
+    lj = oracle.pair_eval(LJ, (2.0, 50.0), 5.0, 1.0, tail=True)
+    tab = oracle.pair_eval(LJ, (2.0, 50.0), 5.0, 1.0, tail=True, table=(1000, 4.0))
+    assert tab[2:] == lj[2:]
+    # doc test of computations.rs:92-100: Harmonic {x0 0.5, k 4.2}, 1000 points up to 2
+    d = lambda r: oracle.pair_eval(HARM, (4.2, 0.5), 1e9, r, table=(1000, 2.0))
+    assert d(1.0)[0] == 0.525
+    assert d(3.0)[0] == 0.0
+
+
 # ---- energy/pairs.rs:317-360 ----------------------------------------------------
 def test_pair_interaction_literals(oracle_lib):
     cut = lambda r: oracle.pair_eval(LJ, (1.0, 2.0), 4.0, r)
