@@ -84,7 +84,8 @@ enum {
     LG_TERM_COUL_REAL = 16,     /* Ewald real space, or the whole Wolf sum */
     LG_TERM_COUL_SELF = 32,     /* Ewald self energy (ewald.rs:619-626) */
     LG_TERM_COUL_KSPACE = 64,   /* Ewald k-space (ewald.rs:677-733) */
-    LG_TERM_ALL = 127
+    LG_TERM_DIHEDRALS = 128,    /* dihedral angles (sys/energy.rs:130-141) */
+    LG_TERM_ALL = 255
 };
 
 /* Quantities (bit mask). */
@@ -110,10 +111,17 @@ typedef struct {
     double table_max;
 } lg_pair;
 
-/* A bond or angle potential (Harmonic or Null). */
+/* Bond, angle and dihedral potentials beyond the pair kinds (functions.rs). */
+enum {
+    LG_BONDED_COSINE_HARMONIC = 10, /* CosineHarmonic::new(k, x0): k/2 (cos x - cos x0)^2 (functions.rs:162-210) */
+    LG_BONDED_TORSION = 11          /* Torsion {k, delta, n}: k (1 + cos(n x - delta)) (functions.rs:212-258) */
+};
+/* A bond, angle or dihedral potential: bonds LG_PAIR_NULL / LG_PAIR_HARMONIC;
+ * angles also LG_BONDED_COSINE_HARMONIC; dihedrals also LG_BONDED_TORSION
+ * (x0 = delta, n = multiplicity). */
 typedef struct {
-    int32_t type;  /* LG_PAIR_ABSENT, LG_PAIR_NULL or LG_PAIR_HARMONIC */
-    int32_t pad;
+    int32_t type;  /* LG_PAIR_ABSENT, LG_PAIR_NULL, LG_PAIR_HARMONIC or LG_BONDED_* */
+    int32_t n;     /* Torsion multiplicity */
     double k, x0;
 } lg_bonded;
 
@@ -184,6 +192,11 @@ int lg_set_bonds(lg_engine* e, int32_t s, int64_t n_bonds, const int32_t* bonds,
                  const lg_bonded* potentials);
 int lg_set_angles(lg_engine* e, int32_t s, int64_t n_angles, const int32_t* angles,
                   const lg_bonded* potentials);
+/* The dihedral angles (i, j, k, m) of system `s` (4 per dihedral, particle
+ * indices, in the orientation Bonding::rebuild gives them, bonding.rs:111-157)
+ * with their potential (System::dihedral_potential). */
+int lg_set_dihedrals(lg_engine* e, int32_t s, int64_t n_dihedrals, const int32_t* dihedrals,
+                     const lg_bonded* potentials);
 
 /* Pair table of system `s`: n_kinds^2 entries, symmetric, replacing
  * System::set_pair_potential (sys/system.rs:122-131).  Fails like the

@@ -12,6 +12,7 @@ from .system import (
     BerendsenThermostat,
     BornMayerHuggins,
     Buckingham,
+    CosineHarmonic,
     CSVRThermostat,
     Engine,
     Ewald,
@@ -32,6 +33,7 @@ from .system import (
     Rewrap,
     System,
     TableComputation,
+    Torsion,
     Translate,
     UnitCell,
     VelocityVerlet,
@@ -46,6 +48,7 @@ from ._capi import (
     LG_TERM_COUL_KSPACE,
     LG_TERM_COUL_REAL,
     LG_TERM_COUL_SELF,
+    LG_TERM_DIHEDRALS,
     LG_TERM_PAIRS,
     LG_TERM_TAIL,
 )
@@ -54,7 +57,7 @@ __all__ = [
     "units", "EngineError", "BerendsenThermostat", "BornMayerHuggins", "Buckingham", "CSVRThermostat", "Engine",
     "Ewald", "Gaussian", "Harmonic", "LeapFrog", "LennardJones", "Mie", "MolecularDynamics", "MonteCarlo", "Morse",
     "Translate", "NullPotential", "PairInteraction", "PairRestriction", "RemoveRotation", "RemoveTranslation", "RescaleThermostat",
-    "Rewrap", "System", "TableComputation", "UnitCell", "VelocityVerlet", "Verlet", "Wolf", "md_params",
+    "Rewrap", "System", "TableComputation", "Torsion", "CosineHarmonic", "UnitCell", "VelocityVerlet", "Verlet", "Wolf", "md_params",
     "LG_TERM_ALL", "LG_TERM_ANGLES", "LG_TERM_BONDS", "LG_TERM_COUL_KSPACE", "LG_TERM_COUL_REAL",
-    "LG_TERM_COUL_SELF", "LG_TERM_PAIRS", "LG_TERM_TAIL",
+    "LG_TERM_COUL_SELF", "LG_TERM_DIHEDRALS", "LG_TERM_PAIRS", "LG_TERM_TAIL",
 ]

@@ -34,7 +34,9 @@ LG_TERM_ANGLES = 8
 LG_TERM_COUL_REAL = 16
 LG_TERM_COUL_SELF = 32
 LG_TERM_COUL_KSPACE = 64
-LG_TERM_ALL = 127
+LG_TERM_DIHEDRALS = 128
+LG_TERM_ALL = 255
+LG_BONDED_COSINE_HARMONIC, LG_BONDED_TORSION = 10, 11
 
 LG_WANT_FORCES = 1
 LG_WANT_ENERGY = 2
@@ -61,7 +63,7 @@ class LgPair(ctypes.Structure):
 
 
 class LgBonded(ctypes.Structure):
-    _fields_ = [("type", ctypes.c_int32), ("pad", ctypes.c_int32), ("k", ctypes.c_double), ("x0", ctypes.c_double)]
+    _fields_ = [("type", ctypes.c_int32), ("n", ctypes.c_int32), ("k", ctypes.c_double), ("x0", ctypes.c_double)]
 
 
 class LgCoulomb(ctypes.Structure):
@@ -106,6 +108,7 @@ SIGNATURES = {
     "lg_set_particles": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int64, _I32, _D, _D, _I32]),
     "lg_set_bonds": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int64, _I32, ctypes.POINTER(LgBonded)]),
     "lg_set_angles": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int64, _I32, ctypes.POINTER(LgBonded)]),
+    "lg_set_dihedrals": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int64, _I32, ctypes.POINTER(LgBonded)]),
     "lg_set_pairs": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(LgPair)]),
     "lg_set_coulomb": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(LgCoulomb)]),
     "lg_compute": (ctypes.c_int, [_P, ctypes.c_int32, _D, ctypes.c_uint32, ctypes.c_uint32, _D, _D, _D]),

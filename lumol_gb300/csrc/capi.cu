@@ -74,6 +74,8 @@ struct HostSystem {
     std::vector<lg_bonded> bond_pots;
     std::vector<int32_t> angles;
     std::vector<lg_bonded> angle_pots;
+    std::vector<int32_t> dihedrals;
+    std::vector<lg_bonded> dihedral_pots;
     int32_t nk = 0;
     std::vector<lg_pair> pairs;
     lg_coulomb coul{};
@@ -108,6 +110,16 @@ void fill_md(SysDev& d, const HostSystem& h) {
     double total = 0.0;  // RemoveTranslation: masses summed in atom order (controls.rs:31)
     for (double w : h.masses) total += w;
     d.total_mass = total;
+}
+
+// A bonded potential as the bonded kernel reads it: (k, x0, extra, kind) with
+// k NaN for NullPotential; kind 0 Harmonic, 1 CosineHarmonic (extra = cos x0,
+// CosineHarmonic::new, functions.rs:190-195), 2 Torsion (x0 = delta, extra = n).
+double4_32a bonded_par(const lg_bonded& p) {
+    double k = p.type == LG_PAIR_NULL ? NAN : p.k;
+    if (p.type == LG_BONDED_COSINE_HARMONIC) return make_double4_32a(k, p.x0, std::cos(p.x0), 1.0);
+    if (p.type == LG_BONDED_TORSION) return make_double4_32a(k, p.x0, (double)p.n, 2.0);
+    return make_double4_32a(k, p.x0, 0.0, 0.0);
 }
 
 // ---- host restatement of the reference's scalar functions -----------------
@@ -371,7 +383,8 @@ struct lg_engine {
     DBuf<int2> km;
     DBuf<int8_t> spec_path;
     DBuf<int4> bt;
-    DBuf<double2> bt_par, eikr, rho;
+    DBuf<double4_32a> bt_par;
+    DBuf<double2> eikr, rho;
     DBuf<float4> wpos;
     DBuf<uint4> posfx, pfx_build;
     DBuf<float> inv_mass;
@@ -523,9 +536,9 @@ int commit(lg_engine* e) {
     std::vector<KVecDev> h_kvec;
     std::vector<std::vector<std::pair<int, int8_t>>> spec(n);
     struct Term {
-        int4 t;
+        int4 t;  // (type | fourth atom << 2, atoms...): 0 bond, 1 angle, 2 dihedral
         int role;
-        double2 par;
+        double4_32a par;
     };
     std::vector<std::vector<Term>> terms(n);
     e->h_sysdev.assign(nsys, SysDev{});
@@ -558,24 +571,33 @@ int commit(lg_engine* e) {
         for (size_t b = 0; b * 2 < h.bonds.size(); b++) {
             const lg_bonded& p = h.bond_pots[b];
             if (p.type == LG_PAIR_ABSENT) continue;
-            double k = p.type == LG_PAIR_NULL ? NAN : p.k;
+            double4_32a par = bonded_par(p);
             int i = (int)(base + h.bonds[2 * b]), j = (int)(base + h.bonds[2 * b + 1]);
             int a = std::min(i, j), c = std::max(i, j);  // Bond::new orders i < j (connect.rs:21-26)
             int4 t = make_int4(0, a, c, -1);
-            terms[a].push_back({t, 0, make_double2(k, p.x0)});
-            terms[c].push_back({t, 1, make_double2(k, p.x0)});
+            terms[a].push_back({t, 0, par});
+            terms[c].push_back({t, 1, par});
         }
         for (size_t a = 0; a * 3 < h.angles.size(); a++) {
             const lg_bonded& p = h.angle_pots[a];
             if (p.type == LG_PAIR_ABSENT) continue;
-            double k = p.type == LG_PAIR_NULL ? NAN : p.k;
+            double4_32a par = bonded_par(p);
             int i = (int)(base + h.angles[3 * a]), j = (int)(base + h.angles[3 * a + 1]),
                 m = (int)(base + h.angles[3 * a + 2]);
             int lo = std::min(i, m), hi = std::max(i, m);  // Angle::new (connect.rs:54-65)
             int4 t = make_int4(1, lo, j, hi);
-            terms[lo].push_back({t, 0, make_double2(k, p.x0)});
-            terms[j].push_back({t, 1, make_double2(k, p.x0)});
-            terms[hi].push_back({t, 2, make_double2(k, p.x0)});
+            terms[lo].push_back({t, 0, par});
+            terms[j].push_back({t, 1, par});
+            terms[hi].push_back({t, 2, par});
+        }
+        for (size_t d = 0; d * 4 < h.dihedrals.size(); d++) {
+            const lg_bonded& p = h.dihedral_pots[d];
+            if (p.type == LG_PAIR_ABSENT) continue;
+            double4_32a par = bonded_par(p);
+            int q[4];
+            for (int k = 0; k < 4; k++) q[k] = (int)(base + h.dihedrals[4 * d + k]);
+            int4 t = make_int4(2 | (q[3] << 2), q[0], q[1], q[2]);  // the fourth atom in the type word
+            for (int k = 0; k < 4; k++) terms[q[k]].push_back({t, k, par});
         }
 
         // pair table
@@ -780,7 +802,7 @@ int commit(lg_engine* e) {
     h_spec_off[n] = (int)h_spec_j.size();
     std::vector<int> h_bt_off(n + 1, 0), h_bt_role;
     std::vector<int4> h_bt;
-    std::vector<double2> h_bt_par;
+    std::vector<double4_32a> h_bt_par;
     for (int64_t i = 0; i < n; i++) {
         h_bt_off[i] = (int)h_bt.size();
         for (auto& t : terms[i]) {
@@ -903,7 +925,7 @@ int commit(lg_engine* e) {
         CUDA_TRY(e, cudaMemcpyAsync(e->bt.p, h_bt.data(), h_bt.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
         CUDA_TRY(e, cudaMemcpyAsync(e->bt_role.p, h_bt_role.data(), h_bt_role.size() * sizeof(int),
                                     cudaMemcpyHostToDevice, st));
-        CUDA_TRY(e, cudaMemcpyAsync(e->bt_par.p, h_bt_par.data(), h_bt_par.size() * sizeof(double2),
+        CUDA_TRY(e, cudaMemcpyAsync(e->bt_par.p, h_bt_par.data(), h_bt_par.size() * sizeof(double4_32a),
                                     cudaMemcpyHostToDevice, st));
     }
     CUDA_TRY(e, cudaMemsetAsync(e->cell_count.p, 0, cell_total * sizeof(int), st));
@@ -1093,7 +1115,7 @@ void enqueue_forces(lg_engine* e, uint32_t terms, bool ev, cudaStream_t st, bool
     } else {
         cudaMemsetAsync(e->force.p, 0, 3 * (size_t)b.n * sizeof(double), st);
     }
-    if ((terms & (LG_TERM_BONDS | LG_TERM_ANGLES)) && b.bt_off) {
+    if ((terms & (LG_TERM_BONDS | LG_TERM_ANGLES | LG_TERM_DIHEDRALS)) && b.bt_off) {
         launch_bonded(b, terms, ev, st);
         e->launches += 1;
     }
@@ -1285,8 +1307,31 @@ int lg_set_angles(lg_engine* e, int32_t s, int64_t na, const int32_t* angles, co
     HostSystem& h = e->sys[s];
     for (int64_t a = 0; a < 3 * na; a++)
         if (angles[a] < 0 || angles[a] >= h.n) return fail(e, LG_ERR_ARGUMENT, "angle index out of range");
+    for (int64_t a = 0; a < na; a++)  // AnglePotential: Harmonic, CosineHarmonic, Null
+        if (pots[a].type != LG_PAIR_ABSENT && pots[a].type != LG_PAIR_NULL && pots[a].type != LG_PAIR_HARMONIC &&
+            pots[a].type != LG_BONDED_COSINE_HARMONIC)
+            return fail(e, LG_ERR_ARGUMENT, "unknown angle potential");
     h.angles.assign(angles, angles + 3 * na);
     h.angle_pots.assign(pots, pots + na);
+    invalidate(e);
+    return LG_OK;
+}
+
+int lg_set_dihedrals(lg_engine* e, int32_t s, int64_t nd, const int32_t* dihedrals, const lg_bonded* pots) {
+    if (!valid_sys(e, s) || nd < 0 || (nd > 0 && (!dihedrals || !pots)))
+        return fail(e, LG_ERR_ARGUMENT, "invalid dihedrals");
+    HostSystem& h = e->sys[s];
+    for (int64_t a = 0; a < 4 * nd; a++)
+        if (dihedrals[a] < 0 || dihedrals[a] >= h.n)
+            return fail(e, LG_ERR_ARGUMENT, "dihedral index out of range");
+    for (int64_t a = 0; a < nd; a++) {  // DihedralPotential: Harmonic, CosineHarmonic, Torsion, Null
+        int t = pots[a].type;
+        if (t != LG_PAIR_ABSENT && t != LG_PAIR_NULL && t != LG_PAIR_HARMONIC && t != LG_BONDED_COSINE_HARMONIC &&
+            t != LG_BONDED_TORSION)
+            return fail(e, LG_ERR_ARGUMENT, "unknown dihedral potential");
+    }
+    h.dihedrals.assign(dihedrals, dihedrals + 4 * nd);
+    h.dihedral_pots.assign(pots, pots + nd);
     invalidate(e);
     return LG_OK;
 }

@@ -386,7 +386,7 @@ enum : uint32_t {
 
 // Number of energy slots per system in the reduction output:
 // [pairs, coulomb real (Ewald real or Wolf), bonds, angles, kspace] then virial 9.
-enum { E_PAIRS = 0, E_COUL = 1, E_BONDS = 2, E_ANGLES = 3, E_KSPACE = 4, N_ESLOT = 5 };
+enum { E_PAIRS = 0, E_COUL = 1, E_BONDS = 2, E_ANGLES = 3, E_KSPACE = 4, E_DIHEDRALS = 5, N_ESLOT = 6 };
 enum { RED_STRIDE = N_ESLOT + 9 };
 
 // ---------------------------------------------------------------------------

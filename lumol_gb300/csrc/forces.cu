@@ -312,26 +312,48 @@ void launch_pair_forces(const Batch& b, uint32_t terms, bool ev, cudaStream_t st
 }
 
 // ---------------------------------------------------------------------------
-// Bonds and angles, gathered per atom (compute.rs:62-84, 233-241;
-// energy.rs:90-120; UnitCell::angle_and_derivatives, cells.rs:335-362).
+// Bonds, angles and dihedrals, gathered per atom (compute.rs:62-96, 233-241;
+// energy.rs:90-141; UnitCell::angle_and_derivatives, cells.rs:335-362;
+// UnitCell::dihedral_and_derivatives, cells.rs:364-411).
 // ---------------------------------------------------------------------------
+// Energy and force of an angle or dihedral potential at x (par = (k, x0,
+// extra, kind), k NaN for NullPotential): Harmonic (functions.rs:135-143),
+// CosineHarmonic (functions.rs:198-207), Torsion (functions.rs:244-256).
+__device__ __forceinline__ double bonded_energy(const double4_32a& par, double x) {
+    if (isnan(par.x)) return 0.0;
+    if (par.w == 1.0) {
+        double dr = cos(x) - par.z;
+        return 0.5 * par.x * dr * dr;
+    }
+    if (par.w == 2.0) return par.x * (1.0 + cos(par.z * x - par.y));
+    double dx = x - par.y;
+    return 0.5 * par.x * dx * dx;
+}
+__device__ __forceinline__ double bonded_force(const double4_32a& par, double x) {
+    if (isnan(par.x)) return 0.0;
+    if (par.w == 1.0) return par.x * (cos(x) - par.z) * sin(x);
+    if (par.w == 2.0) return par.x * par.z * sin(par.z * x - par.y);
+    return par.x * (par.y - x);
+}
+
 template <bool EV>
 __global__ void bonded_kernel(int n, const double4_32a* __restrict__ posq, const int* __restrict__ sysid,
                               const SysDev* __restrict__ sys, const int* __restrict__ bt_off,
                               const int4* __restrict__ bt, const int* __restrict__ bt_role,
-                              const double2* __restrict__ bt_par, uint32_t terms,
+                              const double4_32a* __restrict__ bt_par, uint32_t terms,
                               double* __restrict__ force, double* __restrict__ red) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const SysDev& s = sys[sysid[i]];
-    double fx = 0.0, fy = 0.0, fz = 0.0, eb = 0.0, ea = 0.0;
+    double fx = 0.0, fy = 0.0, fz = 0.0, eb = 0.0, ea = 0.0, ed = 0.0;
     double w[6] = {0, 0, 0, 0, 0, 0};
     for (int t = bt_off[i]; t < bt_off[i + 1]; t++) {
         int4 term = bt[t];
         int role = bt_role[t];
-        double2 par = bt_par[t];  // (k, x0); k is NaN for a NullPotential
+        double4_32a par = bt_par[t];  // (k, x0, extra, kind); k is NaN for a NullPotential
         bool null_pot = isnan(par.x);
-        if (term.x == 0) {
+        int type = term.x & 3;
+        if (type == 0) {
             if (!(terms & 4u)) continue;
             double4_32a pa = posq[term.y], pb = posq[term.z];
             double dx, dy, dz;
@@ -349,7 +371,7 @@ __global__ void bonded_kernel(int n, const double4_32a* __restrict__ posq, const
                 w[0] += gx * dx; w[1] += gx * dy; w[2] += gx * dz;
                 w[3] += gy * dy; w[4] += gy * dz; w[5] += gz * dz;
             }
-        } else {
+        } else if (type == 1) {
             if (!(terms & 8u)) continue;
             double4_32a p1 = posq[term.y], p2 = posq[term.z], p3 = posq[term.w];
             double ax, ay, az, bx, by, bz;
@@ -361,7 +383,7 @@ __global__ void bonded_kernel(int n, const double4_32a* __restrict__ posq, const
             double cs = ux * vx + uy * vy + uz * vz;
             double sin_inv = 1.0 / sqrt(1.0 - cs * cs);
             double theta = acos(cs);
-            double f = null_pot ? 0.0 : par.x * (par.y - theta);
+            double f = bonded_force(par, theta);
             double gx, gy, gz;
             double d1x = sin_inv * (cs * ux - vx) / n12, d1y = sin_inv * (cs * uy - vy) / n12,
                    d1z = sin_inv * (cs * uz - vz) / n12;
@@ -380,9 +402,42 @@ __global__ void bonded_kernel(int n, const double4_32a* __restrict__ posq, const
             if (EV && role == 0 && !null_pot) {
                 // EnergyEvaluator::angles uses UnitCell::angle (cells.rs:322-330)
                 double th = acos((ax * bx + ay * by + az * bz) / (n12 * n23));
-                double dt = th - par.y;
-                ea += 0.5 * par.x * dt * dt;
+                ea += bonded_energy(par, th);
             }
+        } else {
+            if (!(terms & 128u)) continue;
+            double4_32a q1 = posq[term.y], q2 = posq[term.z], q3 = posq[term.w], q4 = posq[term.x >> 2];
+            double r12[3], r23[3], r34[3];
+            exact_nearest_image(s, q2.x, q2.y, q2.z, q1.x, q1.y, q1.z, r12[0], r12[1], r12[2]);
+            exact_nearest_image(s, q3.x, q3.y, q3.z, q2.x, q2.y, q2.z, r23[0], r23[1], r23[2]);
+            exact_nearest_image(s, q4.x, q4.y, q4.z, q3.x, q3.y, q3.z, r34[0], r34[1], r34[2]);
+            double u[3] = {r12[1] * r23[2] - r12[2] * r23[1], r12[2] * r23[0] - r12[0] * r23[2],
+                           r12[0] * r23[1] - r12[1] * r23[0]};
+            double v[3] = {r23[1] * r34[2] - r23[2] * r34[1], r23[2] * r34[0] - r23[0] * r34[2],
+                           r23[0] * r34[1] - r23[1] * r34[0]};
+            double u2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+            double v2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+            double r23_2 = r23[0] * r23[0] + r23[1] * r23[1] + r23[2] * r23[2];
+            double r23n = sqrt(r23_2);
+            double r23_r34 = r23[0] * r34[0] + r23[1] * r34[1] + r23[2] * r34[2];
+            double r12_r23 = r12[0] * r23[0] + r12[1] * r23[1] + r12[2] * r23[2];
+            double c1 = -r23n / u2, c4 = r23n / v2;
+            double d[3];
+            for (int k = 0; k < 3; k++) {
+                double d1 = c1 * u[k], d4 = c4 * v[k];
+                if (role == 0) d[k] = d1;
+                else if (role == 3) d[k] = d4;
+                else if (role == 1) d[k] = (-r12_r23 / r23_2 - 1.0) * d1 + (r23_r34 / r23_2) * d4;
+                else d[k] = (-r23_r34 / r23_2 - 1.0) * d4 + (r12_r23 / r23_2) * d1;
+            }
+            double vs[3] = {r23n * v[0], r23n * v[1], r23n * v[2]};
+            double phi = atan2(vs[0] * r12[0] + vs[1] * r12[1] + vs[2] * r12[2],
+                               u[0] * v[0] + u[1] * v[1] + u[2] * v[2]);
+            double f = bonded_force(par, phi);
+            fx += f * d[0];
+            fy += f * d[1];
+            fz += f * d[2];
+            if (EV && role == 0) ed += bonded_energy(par, phi);  // dihedral angles add no virial (compute.rs:241)
         }
     }
     force[3 * i] += fx;
@@ -392,6 +447,7 @@ __global__ void bonded_kernel(int n, const double4_32a* __restrict__ posq, const
         double* rr = red + (size_t)i * RED_STRIDE;
         rr[E_BONDS] += eb;
         rr[E_ANGLES] += ea;
+        rr[E_DIHEDRALS] += ed;
         double* v = rr + N_ESLOT;
         v[0] += w[0]; v[1] += w[1]; v[2] += w[2];
         v[3] += w[1]; v[4] += w[3]; v[5] += w[4];
@@ -634,6 +690,7 @@ __global__ void __launch_bounds__(256) reduce_kernel(const SysDev* __restrict__ 
         if (terms & 2u) e += hc[0];
         if (terms & 4u) e += sh[E_BONDS][0];
         if (terms & 8u) e += sh[E_ANGLES][0];
+        if (terms & 128u) e += sh[E_DIHEDRALS][0];
         if (terms & 16u) e += sh[E_COUL][0];
         if ((terms & 32u) && s.coul == 1) e += hc[2];
         if ((terms & 64u) && s.coul == 1) e += sh[E_KSPACE][0] / FOUR_PI_EPSILON_0;

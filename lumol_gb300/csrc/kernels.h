@@ -30,9 +30,9 @@ struct Batch {
     int8_t* spec_path = nullptr;
     // bonded terms gathered per atom
     int* bt_off = nullptr;        // n + 1
-    int4* bt = nullptr;           // (type: 0 bond 1 angle, a, b, c) ; role implied by position
+    int4* bt = nullptr;           // (type | m << 2, a, b, c): type 0 bond, 1 angle, 2 dihedral (a, b, c, m)
     int* bt_role = nullptr;
-    double2* bt_par = nullptr;    // (k, x0)
+    double4_32a* bt_par = nullptr; // (k, x0, extra, kind): see bonded_par in the engine
     // neighbour list
     int maxnb = 0;
     int ncells = 0;

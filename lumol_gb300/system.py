@@ -81,6 +81,29 @@ class Harmonic:
 
 
 @dataclass(frozen=True)
+class CosineHarmonic:
+    """CosineHarmonic::new(k, x0): k / 2 (cos x - cos x0)^2, for angles and
+    dihedral angles (functions.rs:162-210)."""
+    k: float
+    x0: float
+
+    def _params(self):
+        return C.LG_BONDED_COSINE_HARMONIC, (self.k, self.x0, 0.0)
+
+
+@dataclass(frozen=True)
+class Torsion:
+    """Torsion {k, delta, n}: k (1 + cos(n phi - delta)), for dihedral angles
+    (functions.rs:212-258)."""
+    k: float
+    delta: float
+    n: int
+
+    def _params(self):
+        return C.LG_BONDED_TORSION, (self.k, self.delta, self.n)
+
+
+@dataclass(frozen=True)
 class BornMayerHuggins:
     """BornMayerHuggins {a, c, d, sigma, rho}:
     A exp((sigma - r) / rho) - C / r^6 + D / r^8 (functions.rs:321-386)."""
@@ -314,6 +337,27 @@ def _angles_from_bonds(bonds: list[tuple[int, int]]) -> list[tuple[int, int, int
     return sorted(angles)
 
 
+def _dihedrals_from_bonds(bonds: list[tuple[int, int]]) -> list[tuple[int, int, int, int]]:
+    """Dihedral angles of a bond set as Bonding::rebuild finds them
+    (bonding.rs:111-157): every angle (i, j, k) with one more bond at an end
+    gives a dihedral, oriented as Dihedral::new orders it (the end whose pair
+    holds the smaller largest index first)."""
+    def make(a, b, c, d):
+        return (a, b, c, d) if max(a, b) < max(c, d) else (d, c, b, a)
+    out = set()
+    for i, j, k in _angles_from_bonds(bonds):
+        for p, q in bonds:
+            if k == p and j != q:
+                out.add(make(i, j, k, q))
+            elif k == q and j != p:
+                out.add(make(i, j, k, p))
+            elif i == q and j != p:
+                out.add(make(p, i, j, k))
+            elif i == p and j != q:
+                out.add(make(q, i, j, k))
+    return sorted(out)
+
+
 class System:
     """Configuration + Interactions (lumol-core/src/sys/system.rs), evaluated on
     the GPU.  Particles of a molecule are contiguous, as in Lumol."""
@@ -333,6 +377,7 @@ class System:
         self.pairs: dict[tuple[str, str], PairInteraction] = {}
         self.bond_potentials: dict[tuple[str, str], object] = {}
         self.angle_potentials: dict[tuple[str, str, str], object] = {}
+        self.dihedral_potentials: dict[tuple[str, str, str, str], object] = {}
         self.coulomb = None
         self.step = 0
         self._engine: Engine | None = None
@@ -439,6 +484,13 @@ class System:
             self._angles_key = key
         return self._angles_cache
 
+    def dihedrals(self) -> list[tuple[int, int, int, int]]:
+        key = len(self._bonds)
+        if getattr(self, "_dihedrals_key", None) != key:
+            self._dihedrals_cache = _dihedrals_from_bonds(self.bonds)
+            self._dihedrals_key = key
+        return self._dihedrals_cache
+
     def molecule_range(self, molid: int) -> tuple[int, int]:
         mols = self.molecules
         idx = np.nonzero(mols == molid)[0]
@@ -469,6 +521,15 @@ class System:
         self.angle_potentials[(min(a, c), b, max(a, c))] = potential
         self._touch()
 
+    def set_dihedral_potential(self, dihedral: tuple[str, str, str, str], potential) -> None:
+        """System::set_dihedral_potential: the potential of the dihedral angles
+        whose particles have these names, in either direction."""
+        self.dihedral_potentials[min(tuple(dihedral), tuple(reversed(dihedral)))] = potential
+        self._touch()
+
+    def dihedral_potential(self, names: tuple[str, str, str, str]):
+        return self.dihedral_potentials.get(min(tuple(names), tuple(reversed(names))))
+
     def set_coulomb_potential(self, potential) -> None:
         """System::set_coulomb_potential (sys/system.rs:159-170)."""
         if any(0.5 * d < potential.cutoff for d in self.cell.lengths):
@@ -493,8 +554,8 @@ class System:
     def _bonded(self, pot) -> C.LgBonded:
         if pot is None:
             return C.LgBonded(C.LG_PAIR_ABSENT, 0, 0.0, 0.0)
-        kind, (k, x0, _) = pot._params()
-        return C.LgBonded(kind, 0, k, x0)
+        kind, (k, x0, extra) = pot._params()
+        return C.LgBonded(kind, int(extra) if kind == C.LG_BONDED_TORSION else 0, k, x0)
 
     def _lower_into(self, eng: Engine, s: int) -> None:
         n = self.size
@@ -519,6 +580,12 @@ class System:
             ni, nj, nk_ = self.names[i], self.names[j], self.names[k]
             apots[a] = self._bonded(self.angle_potentials.get((min(ni, nk_), nj, max(ni, nk_))))
         eng.call("lg_set_angles", s, len(angles), C.iptr(aarr), apots)
+        dihedrals = self.dihedrals()
+        darr = np.array(dihedrals, dtype=np.int32).reshape(-1)
+        dpots = (C.LgBonded * max(len(dihedrals), 1))()
+        for d, q in enumerate(dihedrals):
+            dpots[d] = self._bonded(self.dihedral_potential(tuple(self.names[x] for x in q)))
+        eng.call("lg_set_dihedrals", s, len(dihedrals), C.iptr(darr), dpots)
         coul = self.coulomb._lower() if self.coulomb is not None else C.LgCoulomb()
         eng.call("lg_set_coulomb", s, ctypes.byref(coul))
 

@@ -21,7 +21,7 @@ SRC = os.path.join(HERE, "lumol_oracle.cpp")
 LIB = os.path.join(HERE, "_build", "liblumol_oracle.so")
 
 TERM_PAIRS, TERM_TAIL, TERM_BONDS, TERM_ANGLES = 1, 2, 4, 8
-TERM_COUL_REAL, TERM_COUL_SELF, TERM_COUL_KSPACE, TERM_ALL = 16, 32, 64, 127
+TERM_COUL_REAL, TERM_COUL_SELF, TERM_COUL_KSPACE, TERM_DIHEDRALS, TERM_ALL = 16, 32, 64, 128, 255
 
 
 def build(force: bool = False) -> str:
@@ -50,7 +50,7 @@ class OrcPair(ctypes.Structure):
 
 
 class OrcBonded(ctypes.Structure):
-    _fields_ = [("type", ctypes.c_int32), ("pad", ctypes.c_int32), ("k", ctypes.c_double), ("x0", ctypes.c_double)]
+    _fields_ = [("type", ctypes.c_int32), ("n", ctypes.c_int32), ("k", ctypes.c_double), ("x0", ctypes.c_double)]
 
 
 class OrcCoulomb(ctypes.Structure):
@@ -65,7 +65,7 @@ class OrcDesc(ctypes.Structure):
                 ("n_bonds", ctypes.c_int64), ("bonds", ctypes.c_void_p), ("n_kinds", ctypes.c_int32),
                 ("pairs", ctypes.POINTER(OrcPair)), ("bond_pots", ctypes.POINTER(OrcBonded)),
                 ("angle_pots", ctypes.POINTER(OrcBonded)), ("coulomb", OrcCoulomb),
-                ("cell", ctypes.c_double * 3)]
+                ("cell", ctypes.c_double * 3), ("dihedral_pots", ctypes.POINTER(OrcBonded))]
 
 
 _lib = None
@@ -110,6 +110,11 @@ def load() -> ctypes.CDLL:
         lib.orc_move_molecule_cost.argtypes = [P, ctypes.c_int64, V]
         lib.orc_cache_update.argtypes = [P]
         lib.orc_pair_eval.argtypes = [ctypes.POINTER(OrcPair), ctypes.c_double, D, D, D, D]
+        lib.orc_bonded_eval.argtypes = [ctypes.POINTER(OrcBonded), ctypes.c_double, D, D]
+        lib.orc_dihedral_geometry.argtypes = [V, V, V, V, V, D, V]
+        lib.orc_n_dihedrals.restype = ctypes.c_int64
+        lib.orc_n_dihedrals.argtypes = [P]
+        lib.orc_dihedrals.argtypes = [P, V]
         _lib = lib
     return _lib
 
@@ -147,6 +152,7 @@ class Oracle:
         pairs = (OrcPair * (nk * nk))()
         bpots = (OrcBonded * (nk * nk))()
         apots = (OrcBonded * (nk * nk * nk))()
+        dpots = (OrcBonded * (nk * nk * nk * nk))()
         for a, na in enumerate(names):
             for b, nb in enumerate(names):
                 inter = spec.pairs.get(tuple(sorted((na, nb))))
@@ -160,13 +166,15 @@ class Oracle:
                                                 p0, p1, p2, inter.cutoff, s14, p3, p4, tsize, 0, tmax)
                 bp = spec.bond_potentials.get(tuple(sorted((na, nb))))
                 if bp is not None:
-                    kind, (k, x0, _) = bp._params()
-                    bpots[a * nk + b] = OrcBonded(kind, 0, k, x0)
+                    bpots[a * nk + b] = _orc_bonded(bp)
                 for c, nc in enumerate(names):
                     ap = spec.angle_potentials.get((min(na, nc), nb, max(na, nc)))
                     if ap is not None:
-                        kind, (k, x0, _) = ap._params()
-                        apots[(a * nk + b) * nk + c] = OrcBonded(kind, 0, k, x0)
+                        apots[(a * nk + b) * nk + c] = _orc_bonded(ap)
+                    for d, nd in enumerate(names):
+                        dp = spec.dihedral_potential((na, nb, nc, nd))
+                        if dp is not None:
+                            dpots[((a * nk + b) * nk + c) * nk + d] = _orc_bonded(dp)
         coul = OrcCoulomb()
         if spec.coulomb is not None:
             c = spec.coulomb
@@ -189,6 +197,7 @@ class Oracle:
         desc.pairs = pairs
         desc.bond_pots = bpots
         desc.angle_pots = apots
+        desc.dihedral_pots = dpots
         desc.coulomb = coul
         desc.cell = (ctypes.c_double * 3)(*spec.cell.lengths)
         self.h = lib.orc_create(ctypes.byref(desc))
@@ -223,6 +232,12 @@ class Oracle:
         out = np.zeros(2 * max(count, 1), dtype=np.int32)
         self.lib.orc_pairset(self.h, family, _ptr(out), count)
         return out[: 2 * count].reshape(-1, 2)
+
+    def dihedrals(self) -> np.ndarray:
+        n = self.lib.orc_n_dihedrals(self.h)
+        out = np.zeros(4 * max(n, 1), dtype=np.int32)
+        self.lib.orc_dihedrals(self.h, _ptr(out))
+        return out[: 4 * n].reshape(-1, 4)
 
     def angles(self) -> np.ndarray:
         n = self.lib.orc_n_angles(self.h)
@@ -276,6 +291,32 @@ class Oracle:
 
     def cache_update(self) -> None:
         self.lib.orc_cache_update(self.h)
+
+
+def _orc_bonded(pot) -> OrcBonded:
+    kind, (k, x0, extra) = pot._params()
+    return OrcBonded(kind, int(extra) if kind == TORSION else 0, k, x0)
+
+
+NULL, HARMONIC, COSINE_HARMONIC, TORSION = 1, 4, 10, 11
+
+
+def bonded_eval(kind: int, k: float, x0: float, x: float, n: int = 0):
+    """(energy, force) of a bond / angle / dihedral potential at x."""
+    e, f = ctypes.c_double(), ctypes.c_double()
+    p = OrcBonded(kind, n, k, x0)
+    load().orc_bonded_eval(ctypes.byref(p), x, ctypes.byref(e), ctypes.byref(f))
+    return e.value, f.value
+
+
+def dihedral_geometry(r1, r2, r3, r4, cell=(1e9, 1e9, 1e9)):
+    """UnitCell::dihedral_and_derivatives: (phi, [d1, d2, d3, d4])."""
+    arr = [np.ascontiguousarray(r, dtype=np.float64) for r in (r1, r2, r3, r4)]
+    c = np.ascontiguousarray(cell, dtype=np.float64)
+    phi = ctypes.c_double()
+    d = np.zeros(12)
+    load().orc_dihedral_geometry(_ptr(c), *[_ptr(a) for a in arr], ctypes.byref(phi), _ptr(d))
+    return phi.value, d.reshape(4, 3)
 
 
 def pair_eval(potential_type: int, params, cutoff: float, r: float, shifted: bool = False,

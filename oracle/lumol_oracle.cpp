@@ -48,6 +48,10 @@ inline V3 vscale(double s, const V3& a) { return V3{{s * a[0], s * a[1], s * a[2
 inline V3 vdiv(const V3& a, double s) { return V3{{a[0] / s, a[1] / s, a[2] / s}}; }
 // types/vectors.rs: dot = x*x' + y*y' + z*z' evaluated left to right
 inline double vdot(const V3& a, const V3& b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+// cross product, Vector3D ^ Vector3D (types/vectors.rs:221-228)
+inline V3 vcross(const V3& a, const V3& b) {
+    return V3{{a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]}};
+}
 inline double vnorm2(const V3& a) { return vdot(a, a); }
 inline double vnorm(const V3& a) { return std::sqrt(vnorm2(a)); }
 inline V3 vnormalized(const V3& a) { return vdiv(a, vnorm(a)); }
@@ -368,16 +372,59 @@ struct PairPot {
 struct Bonded {
     orc_bonded d;
     bool present() const { return d.type != 0; }
+    // Potential::energy / force of Harmonic (functions.rs:135-143), CosineHarmonic
+    // (functions.rs:190-207, cos x0 taken at construction) and Torsion (functions.rs:244-256)
     double energy(double x) const {
+        if (d.type == ORC_BONDED_COSINE_HARMONIC) {
+            double dr = std::cos(x) - std::cos(d.x0);
+            return 0.5 * d.k * dr * dr;
+        }
+        if (d.type == ORC_BONDED_TORSION) {
+            double n = (double)d.n;
+            double cs = std::cos(n * x - d.x0);
+            return d.k * (1.0 + cs);
+        }
         if (d.type != ORC_PAIR_HARMONIC) return 0.0;
         double dx = x - d.x0;
         return 0.5 * d.k * dx * dx;
     }
     double force(double x) const {
+        if (d.type == ORC_BONDED_COSINE_HARMONIC) return d.k * (std::cos(x) - std::cos(d.x0)) * std::sin(x);
+        if (d.type == ORC_BONDED_TORSION) {
+            double n = (double)d.n;
+            double sn = std::sin(n * x - d.x0);
+            return d.k * n * sn;
+        }
         if (d.type != ORC_PAIR_HARMONIC) return 0.0;
         return d.k * (d.x0 - x);
     }
 };
+
+// UnitCell::dihedral_and_derivatives (cells.rs:379-411); image(v) applies the
+// cell's vector_image
+template <typename Image>
+double dihedral_and_derivatives(const V3& r1, const V3& r2, const V3& r3, const V3& r4, Image image, V3& d1,
+                                V3& d2, V3& d3, V3& d4) {
+    V3 r12 = vsub(r2, r1);
+    image(r12);
+    V3 r23 = vsub(r3, r2);
+    image(r23);
+    V3 r34 = vsub(r4, r3);
+    image(r34);
+    V3 u = vcross(r12, r23);
+    V3 v = vcross(r23, r34);
+    double u_norm2 = vnorm2(u);
+    double v_norm2 = vnorm2(v);
+    double r23_norm2 = vnorm2(r23);
+    double r23_norm = std::sqrt(r23_norm2);
+    d1 = vscale(-r23_norm / u_norm2, u);
+    d4 = vscale(r23_norm / v_norm2, v);
+    double r23_r34 = vdot(r23, r34);
+    double r12_r23 = vdot(r12, r23);
+    d2 = vadd(vscale(-r12_r23 / r23_norm2 - 1.0, d1), vscale(r23_r34 / r23_norm2, d4));
+    d3 = vadd(vscale(-r23_r34 / r23_norm2 - 1.0, d4), vscale(r12_r23 / r23_norm2, d1));
+    return std::atan2(vdot(vscale(r23_norm, v), r12), vdot(u, v));
+}
 
 // BondPath (energy/restrictions.rs:37-50)
 enum BondPath { PATH_NONE, PATH_SAME, PATH_ONE, PATH_TWO, PATH_THREE, PATH_FAR };
@@ -421,7 +468,7 @@ struct orc_system {
     std::vector<std::pair<int64_t, int64_t>> mol_range;  // [start, end) per molecule
     int32_t nk = 0;
     std::vector<PairPot> pairs;
-    std::vector<Bonded> bond_pots, angle_pots;
+    std::vector<Bonded> bond_pots, angle_pots, dihedral_pots;
     std::vector<std::pair<int32_t, int32_t>> bonds;          // i < j
     std::vector<std::tuple<int32_t, int32_t, int32_t>> angles;  // i < k
     std::vector<std::tuple<int32_t, int32_t, int32_t, int32_t>> dihedrals;
@@ -706,6 +753,32 @@ const Bonded* angle_pot(const orc_system* s, int32_t i, int32_t j, int32_t k) {
     return b.present() ? &b : nullptr;
 }
 
+const Bonded* dihedral_pot(const orc_system* s, int32_t i, int32_t j, int32_t k, int32_t l) {
+    size_t nk = s->nk;
+    if (s->dihedral_pots.empty()) return nullptr;
+    const Bonded& b =
+        s->dihedral_pots[(((size_t)s->kind[i] * nk + s->kind[j]) * nk + s->kind[k]) * nk + s->kind[l]];
+    return b.present() ? &b : nullptr;
+}
+double cell_dihedral(const orc_system* s, int32_t i, int32_t j, int32_t k, int32_t l, V3& d1, V3& d2, V3& d3,
+                     V3& d4) {
+    return dihedral_and_derivatives(s->pos[i], s->pos[j], s->pos[k], s->pos[l],
+                                    [&](V3& v) { s->cell.vector_image(v); }, d1, d2, d3, d4);
+}
+// EnergyEvaluator::dihedrals (sys/energy.rs:130-141); UnitCell::dihedral (cells.rs:364-375)
+// is the angle of dihedral_and_derivatives
+double dihedrals_energy(const orc_system* s) {
+    double e = 0.0;
+    for (auto& d : s->dihedrals) {
+        int32_t i = std::get<0>(d), j = std::get<1>(d), k = std::get<2>(d), l = std::get<3>(d);
+        const Bonded* p = dihedral_pot(s, i, j, k, l);
+        if (!p) continue;
+        V3 d1, d2, d3, d4;
+        e += p->energy(cell_dihedral(s, i, j, k, l, d1, d2, d3, d4));
+    }
+    return e;
+}
+
 double bonds_energy(const orc_system* s) {
     double e = 0.0;
     for (auto& b : s->bonds) {
@@ -779,6 +852,20 @@ void bonded_forces(const orc_system* s, int terms, double* out) {
                 }
             }
         }
+    }
+}
+
+// dihedral forces (compute.rs:86-96)
+void dihedral_forces(const orc_system* s, double* out) {
+    for (auto& d : s->dihedrals) {
+        int32_t q[4] = {std::get<0>(d), std::get<1>(d), std::get<2>(d), std::get<3>(d)};
+        const Bonded* p = dihedral_pot(s, q[0], q[1], q[2], q[3]);
+        if (!p) continue;
+        V3 dv[4];
+        double phi = cell_dihedral(s, q[0], q[1], q[2], q[3], dv[0], dv[1], dv[2], dv[3]);
+        double f = p->force(phi);
+        for (int a = 0; a < 4; a++)
+            for (int c = 0; c < 3; c++) out[3 * q[a] + c] += f * dv[a][c];
     }
 }
 
@@ -1125,6 +1212,10 @@ orc_system* orc_create(const orc_desc* d) {
     for (size_t p = 0; p < s->bond_pots.size(); p++) s->bond_pots[p].d = d->bond_pots ? d->bond_pots[p] : orc_bonded{0, 0, 0, 0};
     s->angle_pots.resize((size_t)s->nk * s->nk * s->nk);
     for (size_t p = 0; p < s->angle_pots.size(); p++) s->angle_pots[p].d = d->angle_pots ? d->angle_pots[p] : orc_bonded{0, 0, 0, 0};
+    if (d->dihedral_pots) {
+        s->dihedral_pots.resize((size_t)s->nk * s->nk * s->nk * s->nk);
+        for (size_t p = 0; p < s->dihedral_pots.size(); p++) s->dihedral_pots[p].d = d->dihedral_pots[p];
+    }
     for (int64_t b = 0; b < d->n_bonds; b++) {
         int32_t i = d->bonds[2 * b], j = d->bonds[2 * b + 1];
         s->bonds.push_back({std::min(i, j), std::max(i, j)});
@@ -1186,6 +1277,7 @@ double orc_energy(orc_system* s, int terms) {
     if (terms & ORC_TERM_TAIL) e += pairs_tail(s);
     if (terms & ORC_TERM_BONDS) e += bonds_energy(s);
     if (terms & ORC_TERM_ANGLES) e += angles_energy(s);
+    if (terms & ORC_TERM_DIHEDRALS) e += dihedrals_energy(s);
     e += coulomb_energy_terms(s, terms);
     return e;
 }
@@ -1194,6 +1286,7 @@ double orc_energy(orc_system* s, int terms) {
 void orc_forces(orc_system* s, int terms, double* out) {
     if (terms & ORC_TERM_PAIRS) pairs_forces(s, out);
     bonded_forces(s, terms, out);
+    if (terms & ORC_TERM_DIHEDRALS) dihedral_forces(s, out);
     if (s->coul.kind != ORC_COULOMB_NONE) {
         if (s->coul.kind == ORC_COULOMB_EWALD) ewald_prepare(s);
         if (terms & ORC_TERM_COUL_REAL) coulomb_real_forces(s, out);
@@ -1492,6 +1585,37 @@ void orc_md_run(orc_system* s, double* x, double* v, double* state, int integrat
     orc_set_positions(s, x);
 }
 
+void orc_bonded_eval(const orc_bonded* p, double x, double* energy, double* force) {
+    Bonded b;
+    b.d = *p;
+    *energy = b.energy(x);
+    *force = b.force(x);
+}
+
+void orc_dihedral_geometry(const double cell[3], const double* r1, const double* r2, const double* r3,
+                           const double* r4, double* phi, double* derivatives) {
+    Cell c;
+    c.init(cell[0], cell[1], cell[2]);
+    auto v = [](const double* r) { return V3{{r[0], r[1], r[2]}}; };
+    V3 d[4];
+    *phi = dihedral_and_derivatives(v(r1), v(r2), v(r3), v(r4), [&](V3& x) { c.vector_image(x); }, d[0], d[1],
+                                    d[2], d[3]);
+    for (int a = 0; a < 4; a++)
+        for (int k = 0; k < 3; k++) derivatives[3 * a + k] = d[a][k];
+}
+
+int64_t orc_n_dihedrals(const orc_system* s) { return (int64_t)s->dihedrals.size(); }
+
+void orc_dihedrals(const orc_system* s, int32_t* out) {
+    size_t k = 0;
+    for (auto& d : s->dihedrals) {
+        out[k++] = std::get<0>(d);
+        out[k++] = std::get<1>(d);
+        out[k++] = std::get<2>(d);
+        out[k++] = std::get<3>(d);
+    }
+}
+
 void orc_pair_eval(const orc_pair* d, double r, double* energy, double* force, double* tail_energy,
                    double* tail_virial) {
     PairPot p;
@@ -1519,7 +1643,7 @@ void orc_cache_init(orc_system* s) {
         }
     s->c_tail = pairs_tail(s);
     s->c_bonds = bonds_energy(s);
-    s->c_angles = angles_energy(s);
+    s->c_angles = angles_energy(s) + dihedrals_energy(s);  // intramolecular angular terms
     s->c_coulomb = coulomb_energy_terms(s, ORC_TERM_ALL);
     s->has_pending = false;
 }

@@ -59,7 +59,8 @@ enum {
     ORC_TERM_COUL_REAL = 16,  /* Ewald real space, or the whole Wolf sum */
     ORC_TERM_COUL_SELF = 32,  /* Ewald self energy (Wolf self is part of COUL_REAL) */
     ORC_TERM_COUL_KSPACE = 64,
-    ORC_TERM_ALL = 127
+    ORC_TERM_DIHEDRALS = 128,
+    ORC_TERM_ALL = 255
 };
 
 /* PairInteraction (lumol-core/src/energy/pairs.rs:57-95). */
@@ -80,9 +81,13 @@ typedef struct {
 } orc_pair;
 
 /* Bond / angle potential (Harmonic or absent). */
+/* Bond, angle and dihedral potentials: ORC_PAIR_NULL, ORC_PAIR_HARMONIC {k, x0},
+ * ORC_BONDED_COSINE_HARMONIC {k, x0} (CosineHarmonic::new, functions.rs:162-210),
+ * ORC_BONDED_TORSION {k, delta = x0, n} (functions.rs:212-258). */
+enum { ORC_BONDED_COSINE_HARMONIC = 10, ORC_BONDED_TORSION = 11 };
 typedef struct {
-    int32_t type;        /* 0: absent, ORC_PAIR_HARMONIC, ORC_PAIR_NULL */
-    int32_t pad;
+    int32_t type;        /* 0: absent, ORC_PAIR_NULL, ORC_PAIR_HARMONIC or ORC_BONDED_* */
+    int32_t n;           /* Torsion multiplicity */
     double k, x0;
 } orc_bonded;
 
@@ -111,6 +116,7 @@ typedef struct {
     const orc_bonded* angle_pots;  /* n_kinds^3, symmetric in first/last */
     orc_coulomb coulomb;
     double cell[3];           /* orthorhombic cell lengths */
+    const orc_bonded* dihedral_pots;  /* n_kinds^4, symmetric under reversal; may be NULL */
 } orc_desc;
 
 typedef struct orc_system orc_system;
@@ -160,6 +166,15 @@ void orc_md_run(orc_system* s, double* positions, double* velocities, double* st
 void orc_verlet_setup(const orc_system* s, const double* positions, const double* velocities, double dt,
                       double* prev);
 double orc_kinetic_energy(const orc_system* s, const double* velocities);
+
+/* One bonded potential evaluated at x: energy and force (functions.rs). */
+void orc_bonded_eval(const orc_bonded* p, double x, double* energy, double* force);
+/* UnitCell::dihedral_and_derivatives (cells.rs:379-411) of four points in a cell
+ * of lengths `cell`: the angle and the derivatives d1..d4 (12 doubles). */
+void orc_dihedral_geometry(const double cell[3], const double* r1, const double* r2, const double* r3,
+                           const double* r4, double* phi, double* derivatives);
+int64_t orc_n_dihedrals(const orc_system* s);
+void orc_dihedrals(const orc_system* s, int32_t* out); /* 4 * n_dihedrals, sorted */
 
 /* One PairInteraction evaluated at distance r: energy, force, tail energy,
  * tail virial (energy/pairs.rs:185-296). */

@@ -127,8 +127,10 @@ def random_lj_fluid(n: int, density: float, seed: int, cutoff: float, family: st
     return s
 
 
-def chains(n_mol: int, length: float, seed: int, restriction, coulomb=None) -> lg.System:
-    """Flexible 5-atom chains with charges, for bond-path restrictions."""
+def chains(n_mol: int, length: float, seed: int, restriction, coulomb=None, dihedrals: bool = False) -> lg.System:
+    """Flexible 5-atom chains with charges, for bond-path restrictions; with
+    `dihedrals`, a Torsion on C-C-O-C, a CosineHarmonic on C-O-C-N and a
+    CosineHarmonic O-C-N angle."""
     rng = np.random.default_rng(seed)
     s = lg.System(lg.UnitCell.cubic(length))
     side = int(np.ceil(n_mol ** (1.0 / 3.0)))
@@ -156,6 +158,10 @@ def chains(n_mol: int, length: float, seed: int, restriction, coulomb=None) -> l
     s.set_angle_potential(("C", "C", "O"), lg.Harmonic(k=units.from_(300.0, "kJ/mol/rad^2"), x0=1.9))
     s.set_angle_potential(("C", "O", "C"), lg.Harmonic(k=units.from_(320.0, "kJ/mol/rad^2"), x0=1.95))
     s.set_angle_potential(("O", "C", "N"), lg.Harmonic(k=units.from_(280.0, "kJ/mol/rad^2"), x0=2.0))
+    if dihedrals:
+        s.set_angle_potential(("O", "C", "N"), lg.CosineHarmonic(k=units.from_(250.0, "kJ/mol"), x0=2.0))
+        s.set_dihedral_potential(("C", "C", "O", "C"), lg.Torsion(k=units.from_(5.0, "kJ/mol"), delta=0.4, n=3))
+        s.set_dihedral_potential(("N", "C", "O", "C"), lg.CosineHarmonic(k=units.from_(40.0, "kJ/mol"), x0=1.2))
     if coulomb is not None:
         coulomb.set_restriction(restriction)
         s.set_coulomb_potential(coulomb)

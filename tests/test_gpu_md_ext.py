@@ -89,6 +89,19 @@ def test_mixed_md_tracks_fp64_oracle(integrator, th, ctl):
     assert np.abs(s.positions - xo).max() < 1e-6
 
 
+def test_md_with_dihedrals_matches_oracle():
+    """VelocityVerlet with Berendsen on flexible chains with Torsion and
+    CosineHarmonic dihedral angles: the FP64 trajectory follows the oracle."""
+    s = systems.chains(27, 24.0, 9, lg.PairRestriction.EXCLUDE13, coulomb=lg.Wolf(8.0), dihedrals=True)
+    s.velocities = workloads.boltzmann_velocities(s, 250.0, 4)
+    xo, vo = oracle_run(s, "vv", "berendsen", (), 0.5, 25)
+    md = lg.MolecularDynamics(lg.VelocityVerlet(0.5), thermostat("berendsen"))
+    md.setup(s)
+    md.run(s, 25)
+    assert np.abs(s.positions - xo).max() < 1e-9
+    assert np.abs(s.velocities - vo).max() / np.abs(vo).max() < 1e-8
+
+
 def two_silver(x1, v):
     s = lg.System(lg.UnitCell.cubic(10.0))
     s.add_particles(["Ag", "Ag"], np.array([[0.0, 0.0, 0.0], x1]), masses=[107.8682, 107.8682])

@@ -61,6 +61,12 @@ def test_mixed_unwrapped_fluid(family):
     check(systems.random_lj_fluid(700, 0.02, 5, 9.0, family=family, precision="mixed"))
 
 
+def test_mixed_chains_with_dihedrals():
+    s = systems.chains(27, 24.0, 9, lg.PairRestriction.EXCLUDE13, coulomb=lg.Wolf(8.0), dihedrals=True)
+    s.precision = "mixed"  # (before the engine is created)
+    check(s)
+
+
 def test_mixed_md_tracks_fp64():
     """Short trajectories of the two precisions stay within 1e-6 A."""
     a = workloads.nacl_crystal(cells=3, cutoff=8.0, kmax=5)

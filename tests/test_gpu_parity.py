@@ -15,7 +15,7 @@ pytestmark = pytest.mark.gpu
 
 TOL = 1e-10
 TERMS = [lg.LG_TERM_ALL, lg.LG_TERM_PAIRS, lg.LG_TERM_TAIL, lg.LG_TERM_BONDS, lg.LG_TERM_ANGLES,
-         lg.LG_TERM_COUL_REAL, lg.LG_TERM_COUL_SELF, lg.LG_TERM_COUL_KSPACE]
+         lg.LG_TERM_COUL_REAL, lg.LG_TERM_COUL_SELF, lg.LG_TERM_COUL_KSPACE, lg.LG_TERM_DIHEDRALS]
 
 
 def _rel(a, b, scale):
@@ -97,6 +97,16 @@ def test_chain_restrictions_wolf(restriction):
 @pytest.mark.parametrize("restriction", [lg.PairRestriction.EXCLUDE13, lg.PairRestriction.INTER_MOLECULAR])
 def test_chain_restrictions_ewald(restriction):
     s = systems.chains(27, 24.0, 8, restriction, coulomb=lg.Ewald(8.0, 6, 0.4))
+    assert_parity(s)
+
+
+@pytest.mark.parametrize("coulomb", [None, "wolf"])
+def test_chain_dihedrals_and_cosine_angles(coulomb):
+    """Torsion and CosineHarmonic dihedral angles and a CosineHarmonic angle
+    (functions.rs:162-258; cells.rs:379-411; compute.rs:86-96)."""
+    s = systems.chains(27, 24.0, 9, lg.PairRestriction.EXCLUDE13,
+                       coulomb=lg.Wolf(8.0) if coulomb else None, dihedrals=True)
+    assert len(s.dihedrals()) == 54
     assert_parity(s)
 
 

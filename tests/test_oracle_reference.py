@@ -8,6 +8,7 @@ import math
 import numpy as np
 import pytest
 
+import lumol_gb300 as lg
 import oracle
 import refdata
 import systems
@@ -142,6 +143,49 @@ def test_table_computation_literals(oracle_lib):
     d = lambda r: oracle.pair_eval(HARM, (4.2, 0.5), 1e9, r, table=(1000, 2.0))
     assert d(1.0)[0] == 0.525
     assert d(3.0)[0] == 0.0
+
+
+def test_cosine_harmonic_and_torsion_literals(oracle_lib):
+    # functions.rs:663-697 and the doc tests of functions.rs:173-177, 228-232
+    cos = lambda x: oracle.bonded_eval(oracle.COSINE_HARMONIC, 50.0, 2.0, x)
+    assert cos(2.0) == (0.0, 0.0)
+    dcos = math.cos(2.5) - math.cos(2.0)
+    assert cos(2.5) == (0.5 * 50.0 * dcos * dcos, 50.0 * dcos * math.sin(2.5))
+    eps = 1e-9
+    assert relative_eq((cos(2.3)[0] - cos(2.3 + eps)[0]) / eps, cos(2.3)[1], epsilon=1e-6)
+    assert oracle.bonded_eval(oracle.COSINE_HARMONIC, 100.0, 2.0, 3.0)[0] == 16.464942078100552
+    tor = lambda x: oracle.bonded_eval(oracle.TORSION, 5.0, 3.0, x, n=3)
+    assert tor(1.0) == (10.0, 0.0)
+    assert tor(1.1)[0] == 5.0 * (1.0 + math.cos(3.0 * 1.1 - 3.0))
+    assert relative_eq((tor(4.0)[0] - tor(4.0 + eps)[0]) / eps, tor(4.0)[1], epsilon=1e-6)
+    doc = lambda x: oracle.bonded_eval(oracle.TORSION, 10.0, math.pi / 2.0, x, n=3)
+    assert doc(math.pi / 2.0)[0] == 0.0
+    assert doc(math.pi / 3.0)[0] == 10.0
+    assert abs(doc(math.pi / 2.0)[1]) < 1e-12
+
+
+def test_dihedral_geometry_literals(oracle_lib):
+    # sys/config/cells.rs:746-797
+    phi, _ = oracle.dihedral_geometry([0, 0, 0], [1, 0, 0], [1, 1, 0], [2, 1, 0])
+    assert phi == math.pi
+    pts = [np.array(p) for p in ([1.241, 0.444, 0.349], [-0.011, -0.441, 0.333], [-1.176, 0.296, -0.332],
+                                 [-1.396, 1.211, 0.219])]
+    phi, d = oracle.dihedral_geometry(*pts)
+    assert relative_eq(phi, -1.0453789626063168)
+    eps = 1e-6
+    for a in range(4):
+        for k in range(3):
+            moved = [p.copy() for p in pts]
+            moved[a][k] += eps
+            fd = (oracle.dihedral_geometry(*moved)[0] - phi) / eps
+            assert ulps_eq(fd, d[a][k], epsilon=1e-6)
+
+
+def test_dihedrals_of_the_host_match_the_oracle(oracle_lib):
+    s = systems.chains(8, 30.0, 3, lg.PairRestriction.INTER_MOLECULAR, dihedrals=True)
+    orc = oracle.Oracle(s)
+    assert orc.dihedrals().tolist() == [list(d) for d in s.dihedrals()]
+    assert len(s.dihedrals()) == 16
 
 
 # ---- energy/pairs.rs:317-360 ----------------------------------------------------
