@@ -116,13 +116,16 @@ enum {
     LG_BONDED_COSINE_HARMONIC = 10, /* CosineHarmonic::new(k, x0): k/2 (cos x - cos x0)^2 (functions.rs:162-210) */
     LG_BONDED_TORSION = 11          /* Torsion {k, delta, n}: k (1 + cos(n x - delta)) (functions.rs:212-258) */
 };
-/* A bond, angle or dihedral potential: bonds LG_PAIR_NULL / LG_PAIR_HARMONIC;
- * angles also LG_BONDED_COSINE_HARMONIC; dihedrals also LG_BONDED_TORSION
- * (x0 = delta, n = multiplicity). */
+/* A bond, angle or dihedral potential: bonds LG_PAIR_NULL / LG_PAIR_HARMONIC /
+ * LG_PAIR_MORSE; angles also LG_BONDED_COSINE_HARMONIC; dihedrals also
+ * LG_BONDED_TORSION (x0 = delta, n = multiplicity).  Morse {a, x0, depth}
+ * (functions.rs:405-437, BondPotential / AnglePotential / DihedralPotential)
+ * takes k = depth, x0 and a. */
 typedef struct {
-    int32_t type;  /* LG_PAIR_ABSENT, LG_PAIR_NULL, LG_PAIR_HARMONIC or LG_BONDED_* */
+    int32_t type;  /* LG_PAIR_ABSENT, LG_PAIR_NULL, LG_PAIR_HARMONIC, LG_PAIR_MORSE or LG_BONDED_* */
     int32_t n;     /* Torsion multiplicity */
     double k, x0;
+    double a;      /* Morse width */
 } lg_bonded;
 
 /* Ewald::new(cutoff, kmax, alpha) (ewald.rs:278-305) or Wolf::new(cutoff) (wolf.rs:68-84). */

@@ -8,6 +8,7 @@ MolecularDynamics, MonteCarlo); every computation runs in the CUDA library
 """
 from . import units
 from ._capi import EngineError
+from .input import InputError, InteractionsInput, read_interactions
 from .system import (
     BerendsenThermostat,
     BornMayerHuggins,
@@ -54,7 +55,7 @@ from ._capi import (
 )
 
 __all__ = [
-    "units", "EngineError", "BerendsenThermostat", "BornMayerHuggins", "Buckingham", "CSVRThermostat", "Engine",
+    "units", "EngineError", "InputError", "InteractionsInput", "read_interactions", "BerendsenThermostat", "BornMayerHuggins", "Buckingham", "CSVRThermostat", "Engine",
     "Ewald", "Gaussian", "Harmonic", "LeapFrog", "LennardJones", "Mie", "MolecularDynamics", "MonteCarlo", "Morse",
     "Translate", "NullPotential", "PairInteraction", "PairRestriction", "RemoveRotation", "RemoveTranslation", "RescaleThermostat",
     "Rewrap", "System", "TableComputation", "Torsion", "CosineHarmonic", "UnitCell", "VelocityVerlet", "Verlet", "Wolf", "md_params",

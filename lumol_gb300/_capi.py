@@ -63,7 +63,8 @@ class LgPair(ctypes.Structure):
 
 
 class LgBonded(ctypes.Structure):
-    _fields_ = [("type", ctypes.c_int32), ("n", ctypes.c_int32), ("k", ctypes.c_double), ("x0", ctypes.c_double)]
+    _fields_ = [("type", ctypes.c_int32), ("n", ctypes.c_int32), ("k", ctypes.c_double), ("x0", ctypes.c_double),
+                ("a", ctypes.c_double)]
 
 
 class LgCoulomb(ctypes.Structure):

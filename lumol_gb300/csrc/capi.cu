@@ -119,6 +119,7 @@ double4_32a bonded_par(const lg_bonded& p) {
     double k = p.type == LG_PAIR_NULL ? NAN : p.k;
     if (p.type == LG_BONDED_COSINE_HARMONIC) return make_double4_32a(k, p.x0, std::cos(p.x0), 1.0);
     if (p.type == LG_BONDED_TORSION) return make_double4_32a(k, p.x0, (double)p.n, 2.0);
+    if (p.type == LG_PAIR_MORSE) return make_double4_32a(k, p.x0, p.a, 3.0);
     return make_double4_32a(k, p.x0, 0.0, 0.0);
 }
 
@@ -1290,7 +1291,10 @@ int lg_set_bonds(lg_engine* e, int32_t s, int64_t nb, const int32_t* bonds, cons
     HostSystem& h = e->sys[s];
     for (int64_t b = 0; b < 2 * nb; b++)
         if (bonds[b] < 0 || bonds[b] >= h.n) return fail(e, LG_ERR_ARGUMENT, "bond index out of range");
-    for (int64_t b = 0; b < nb; b++) {
+    for (int64_t b = 0; b < nb; b++) {  // BondPotential: Harmonic, Morse, Null
+        int t = pots[b].type;
+        if (t != LG_PAIR_ABSENT && t != LG_PAIR_NULL && t != LG_PAIR_HARMONIC && t != LG_PAIR_MORSE)
+            return fail(e, LG_ERR_ARGUMENT, "unknown bond potential");
         if (bonds[2 * b] == bonds[2 * b + 1]) return fail(e, LG_ERR_ARGUMENT, "a bond needs two particles");
         if (h.mols[bonds[2 * b]] != h.mols[bonds[2 * b + 1]])
             return fail(e, LG_ERR_ARGUMENT, "bonded particles must be in the same molecule");
@@ -1307,9 +1311,9 @@ int lg_set_angles(lg_engine* e, int32_t s, int64_t na, const int32_t* angles, co
     HostSystem& h = e->sys[s];
     for (int64_t a = 0; a < 3 * na; a++)
         if (angles[a] < 0 || angles[a] >= h.n) return fail(e, LG_ERR_ARGUMENT, "angle index out of range");
-    for (int64_t a = 0; a < na; a++)  // AnglePotential: Harmonic, CosineHarmonic, Null
+    for (int64_t a = 0; a < na; a++)  // AnglePotential: Harmonic, CosineHarmonic, Morse, Null
         if (pots[a].type != LG_PAIR_ABSENT && pots[a].type != LG_PAIR_NULL && pots[a].type != LG_PAIR_HARMONIC &&
-            pots[a].type != LG_BONDED_COSINE_HARMONIC)
+            pots[a].type != LG_BONDED_COSINE_HARMONIC && pots[a].type != LG_PAIR_MORSE)
             return fail(e, LG_ERR_ARGUMENT, "unknown angle potential");
     h.angles.assign(angles, angles + 3 * na);
     h.angle_pots.assign(pots, pots + na);
@@ -1324,10 +1328,10 @@ int lg_set_dihedrals(lg_engine* e, int32_t s, int64_t nd, const int32_t* dihedra
     for (int64_t a = 0; a < 4 * nd; a++)
         if (dihedrals[a] < 0 || dihedrals[a] >= h.n)
             return fail(e, LG_ERR_ARGUMENT, "dihedral index out of range");
-    for (int64_t a = 0; a < nd; a++) {  // DihedralPotential: Harmonic, CosineHarmonic, Torsion, Null
+    for (int64_t a = 0; a < nd; a++) {  // DihedralPotential: Harmonic, CosineHarmonic, Torsion, Morse, Null
         int t = pots[a].type;
         if (t != LG_PAIR_ABSENT && t != LG_PAIR_NULL && t != LG_PAIR_HARMONIC && t != LG_BONDED_COSINE_HARMONIC &&
-            t != LG_BONDED_TORSION)
+            t != LG_BONDED_TORSION && t != LG_PAIR_MORSE)
             return fail(e, LG_ERR_ARGUMENT, "unknown dihedral potential");
     }
     h.dihedrals.assign(dihedrals, dihedrals + 4 * nd);

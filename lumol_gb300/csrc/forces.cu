@@ -326,6 +326,10 @@ __device__ __forceinline__ double bonded_energy(const double4_32a& par, double x
         return 0.5 * par.x * dr * dr;
     }
     if (par.w == 2.0) return par.x * (1.0 + cos(par.z * x - par.y));
+    if (par.w == 3.0) {  // Morse: depth (1 - exp((x0 - x) a))^2 (functions.rs:415-418)
+        double rc = 1.0 - exp((par.y - x) * par.z);
+        return par.x * rc * rc;
+    }
     double dx = x - par.y;
     return 0.5 * par.x * dx * dx;
 }
@@ -333,6 +337,10 @@ __device__ __forceinline__ double bonded_force(const double4_32a& par, double x)
     if (isnan(par.x)) return 0.0;
     if (par.w == 1.0) return par.x * (cos(x) - par.z) * sin(x);
     if (par.w == 2.0) return par.x * par.z * sin(par.z * x - par.y);
+    if (par.w == 3.0) {  // Morse's force as functions.rs:420-423 writes it
+        double ex = exp((par.y - x) * par.z);
+        return 2.0 * par.x * (1.0 - ex * ex) * par.z;
+    }
     return par.x * (par.y - x);
 }
 

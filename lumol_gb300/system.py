@@ -13,7 +13,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _capi as C
-from .units import ATOMIC_MASSES
+from .units import ATOMIC_MASSES, FOUR_PI_EPSILON_0
 
 
 # ---------------------------------------------------------------------------
@@ -223,6 +223,40 @@ class Ewald:
         self.kmax = int(kmax)
         self.alpha = float(a)
         self.restriction = PairRestriction.NONE
+
+    @classmethod
+    def with_accuracy(cls, cutoff: float, accuracy: float, system: "System") -> "Ewald":
+        """Ewald::with_accuracy (ewald.rs:312-351): alpha from the accuracy, the
+        cutoff, the particle count, the cell volume and the charges; kmax the
+        smallest one whose k-space error estimate is within the accuracy."""
+        if cutoff < 0.0:
+            raise ValueError("the cutoff can not be negative in Ewald")
+        if accuracy < 0.0:
+            raise ValueError("accuracy can not be negative in Ewald")
+        f = np.float64
+        with np.errstate(all="ignore"):  # IEEE arithmetic: an empty or neutral system gives inf / NaN
+            q2 = f(0.0)
+            for q in system.charges:
+                q2 += f(q) * f(q)
+            q2 /= f(FOUR_PI_EPSILON_0)
+            natoms = f(system.size)
+            a, b, c = (f(x) for x in system.cell.lengths)
+            alpha = f(accuracy) * np.sqrt(natoms * f(cutoff) * a * b * c) / (f(2.0) * q2)
+            if alpha >= 1.0:
+                alpha = (f(1.35) - f(0.15) * np.log(f(accuracy))) / f(cutoff)
+            else:
+                alpha = np.sqrt(-np.log(alpha)) / f(cutoff)
+            min_length = min(a, b, c)
+
+            def error(kmax: float):
+                arg = f(np.pi) * f(kmax) / (alpha * min_length)
+                return f(1.1283791670955126) * q2 * alpha / min_length / np.sqrt(f(kmax) * natoms) * np.exp(-arg * arg)
+
+            kmax = 1
+            while error(kmax) > accuracy:  # 2 / sqrt(pi) above is f64's FRAC_2_SQRT_PI
+                kmax += 1
+        alpha = float(alpha)
+        return cls(cutoff, kmax, alpha)
 
     def set_restriction(self, restriction) -> None:
         self.restriction = restriction
@@ -553,9 +587,12 @@ class System:
 
     def _bonded(self, pot) -> C.LgBonded:
         if pot is None:
-            return C.LgBonded(C.LG_PAIR_ABSENT, 0, 0.0, 0.0)
-        kind, (k, x0, extra) = pot._params()
-        return C.LgBonded(kind, int(extra) if kind == C.LG_BONDED_TORSION else 0, k, x0)
+            return C.LgBonded(C.LG_PAIR_ABSENT, 0, 0.0, 0.0, 0.0)
+        kind, par = pot._params()
+        if kind == C.LG_PAIR_MORSE:  # Morse {a, x0, depth}
+            return C.LgBonded(kind, 0, par[2], par[1], par[0])
+        k, x0, extra = par
+        return C.LgBonded(kind, int(extra) if kind == C.LG_BONDED_TORSION else 0, k, x0, 0.0)
 
     def _lower_into(self, eng: Engine, s: int) -> None:
         n = self.size

@@ -3,7 +3,7 @@
 Internal units: Angstrom, femtosecond, unified atomic mass, Kelvin, radian;
 energy is 1e-4 kJ/mol.  `from_(value, "kJ/mol/A^2")` mirrors `units::from`.
 Unit expressions are products and quotients of the units below with integer
-powers, evaluated left to right.
+powers and parentheses.
 """
 from __future__ import annotations
 
@@ -32,26 +32,91 @@ CONVERSION_FACTORS = {
     "bar": 1e-35 / U_IN_KG, "atm": 101325.0 * 1e-40 / U_IN_KG,
 }
 
-_TOKEN = re.compile(r"\s*([A-Za-z]+)(?:\^(-?\d+))?\s*([*/]|$)")
+_TOKEN = re.compile(r"\s*(?:([*/^()])|([^*/^()\s]+))")
+
+
+def _tokens(unit: str) -> list[str]:
+    out, pos = [], 0
+    while pos < len(unit):
+        m = _TOKEN.match(unit, pos)
+        if m is None:  # only whitespace is left
+            break
+        out.append(m.group(1) or m.group(2))
+        pos = m.end()
+    return out
 
 
 def _factor(unit: str) -> float:
-    factor = 1.0
-    op = "*"
+    """Evaluates a unit expression as units.rs:183-365 reads it: names,
+    '*' and '/' (left-associative, same precedence), '^' with an integer power
+    (higher precedence), and parentheses."""
+    toks = _tokens(unit)
     pos = 0
-    unit = unit.strip()
-    while pos < len(unit):
-        m = _TOKEN.match(unit, pos)
-        if not m or m.end() == pos:
-            raise ValueError(f"can not parse unit '{unit}'")
-        name, power, nxt = m.group(1), m.group(2), m.group(3)
-        if name not in CONVERSION_FACTORS:
-            raise ValueError(f"unknown unit '{name}'")
-        value = CONVERSION_FACTORS[name] ** (int(power) if power else 1)
-        factor = factor * value if op == "*" else factor / value
-        op = nxt or "*"
-        pos = m.end()
-    return factor
+
+    def peek():
+        return toks[pos] if pos < len(toks) else None
+
+    def atom() -> float:
+        nonlocal pos
+        t = peek()
+        if t is None:
+            raise ValueError(f"malformed unit '{unit}': missing a value")
+        pos += 1
+        if t == "(":
+            v = expr()
+            if peek() != ")":
+                raise ValueError(f"malformed unit '{unit}': unbalanced parenthesis")
+            pos += 1
+            return v
+        if t in "*/^)":
+            raise ValueError(f"malformed unit '{unit}': unexpected '{t}'")
+        if t not in CONVERSION_FACTORS:
+            raise ValueError(f"unknown unit '{t}'")
+        return CONVERSION_FACTORS[t]
+
+    def power() -> float:
+        nonlocal pos
+        v = atom()
+        while peek() == "^":
+            pos += 1
+            t = peek()
+            try:
+                exponent = int(t)
+            except (TypeError, ValueError):
+                raise ValueError(f"malformed unit '{unit}': invalid value after ^: {t}") from None
+            pos += 1
+            v = v ** exponent
+        return v
+
+    def expr() -> float:
+        nonlocal pos
+        v = power()
+        while peek() in ("*", "/"):
+            op = toks[pos]
+            pos += 1
+            rhs = power()
+            v = v * rhs if op == "*" else v / rhs
+        return v
+
+    value = expr()
+    if pos != len(toks):
+        raise ValueError(f"malformed unit '{unit}': remaining values after the end of the unit: "
+                         + " ".join(toks[pos:]))
+    return value
+
+
+def from_str(value: str) -> float:
+    """units::from_str (units.rs:384-394): "<number> <unit>" to internal
+    units; the unit may be omitted."""
+    parts = value.split()
+    if not parts:
+        raise ValueError("can not parse an empty value")
+    factor = _factor(" ".join(parts[1:])) if len(parts) > 1 else 1.0
+    try:
+        number = float(parts[0])
+    except ValueError:
+        raise ValueError(f"can not parse '{parts[0]}' as a number") from None
+    return factor * number
 
 
 def from_(value: float, unit: str) -> float:

@@ -50,7 +50,8 @@ class OrcPair(ctypes.Structure):
 
 
 class OrcBonded(ctypes.Structure):
-    _fields_ = [("type", ctypes.c_int32), ("n", ctypes.c_int32), ("k", ctypes.c_double), ("x0", ctypes.c_double)]
+    _fields_ = [("type", ctypes.c_int32), ("n", ctypes.c_int32), ("k", ctypes.c_double), ("x0", ctypes.c_double),
+                ("a", ctypes.c_double)]
 
 
 class OrcCoulomb(ctypes.Structure):
@@ -294,17 +295,21 @@ class Oracle:
 
 
 def _orc_bonded(pot) -> OrcBonded:
-    kind, (k, x0, extra) = pot._params()
-    return OrcBonded(kind, int(extra) if kind == TORSION else 0, k, x0)
+    kind, par = pot._params()
+    if kind == MORSE:  # Morse {a, x0, depth}
+        return OrcBonded(kind, 0, par[2], par[1], par[0])
+    k, x0, extra = par
+    return OrcBonded(kind, int(extra) if kind == TORSION else 0, k, x0, 0.0)
 
 
-NULL, HARMONIC, COSINE_HARMONIC, TORSION = 1, 4, 10, 11
+NULL, HARMONIC, MORSE, COSINE_HARMONIC, TORSION = 1, 4, 6, 10, 11
 
 
-def bonded_eval(kind: int, k: float, x0: float, x: float, n: int = 0):
-    """(energy, force) of a bond / angle / dihedral potential at x."""
+def bonded_eval(kind: int, k: float, x0: float, x: float, n: int = 0, a: float = 0.0):
+    """(energy, force) of a bond / angle / dihedral potential at x (Morse:
+    k = depth, width a)."""
     e, f = ctypes.c_double(), ctypes.c_double()
-    p = OrcBonded(kind, n, k, x0)
+    p = OrcBonded(kind, n, k, x0, a)
     load().orc_bonded_eval(ctypes.byref(p), x, ctypes.byref(e), ctypes.byref(f))
     return e.value, f.value
 

@@ -373,8 +373,13 @@ struct Bonded {
     orc_bonded d;
     bool present() const { return d.type != 0; }
     // Potential::energy / force of Harmonic (functions.rs:135-143), CosineHarmonic
-    // (functions.rs:190-207, cos x0 taken at construction) and Torsion (functions.rs:244-256)
+    // (functions.rs:190-207, cos x0 taken at construction), Torsion (functions.rs:244-256)
+    // and Morse (functions.rs:414-424, the force as written there)
     double energy(double x) const {
+        if (d.type == ORC_PAIR_MORSE) {
+            double rc = 1.0 - std::exp((d.x0 - x) * d.a);
+            return d.k * rc * rc;
+        }
         if (d.type == ORC_BONDED_COSINE_HARMONIC) {
             double dr = std::cos(x) - std::cos(d.x0);
             return 0.5 * d.k * dr * dr;
@@ -389,6 +394,10 @@ struct Bonded {
         return 0.5 * d.k * dx * dx;
     }
     double force(double x) const {
+        if (d.type == ORC_PAIR_MORSE) {
+            double ex = std::exp((d.x0 - x) * d.a);
+            return 2.0 * d.k * (1.0 - ex * ex) * d.a;
+        }
         if (d.type == ORC_BONDED_COSINE_HARMONIC) return d.k * (std::cos(x) - std::cos(d.x0)) * std::sin(x);
         if (d.type == ORC_BONDED_TORSION) {
             double n = (double)d.n;
@@ -1209,9 +1218,9 @@ orc_system* orc_create(const orc_desc* d) {
         if (d->pairs[p].shifted) s->pairs[p].shift = s->pairs[p].comp_energy(d->pairs[p].cutoff);
     }
     s->bond_pots.resize((size_t)s->nk * s->nk);
-    for (size_t p = 0; p < s->bond_pots.size(); p++) s->bond_pots[p].d = d->bond_pots ? d->bond_pots[p] : orc_bonded{0, 0, 0, 0};
+    for (size_t p = 0; p < s->bond_pots.size(); p++) s->bond_pots[p].d = d->bond_pots ? d->bond_pots[p] : orc_bonded{0, 0, 0, 0, 0};
     s->angle_pots.resize((size_t)s->nk * s->nk * s->nk);
-    for (size_t p = 0; p < s->angle_pots.size(); p++) s->angle_pots[p].d = d->angle_pots ? d->angle_pots[p] : orc_bonded{0, 0, 0, 0};
+    for (size_t p = 0; p < s->angle_pots.size(); p++) s->angle_pots[p].d = d->angle_pots ? d->angle_pots[p] : orc_bonded{0, 0, 0, 0, 0};
     if (d->dihedral_pots) {
         s->dihedral_pots.resize((size_t)s->nk * s->nk * s->nk * s->nk);
         for (size_t p = 0; p < s->dihedral_pots.size(); p++) s->dihedral_pots[p].d = d->dihedral_pots[p];

@@ -80,15 +80,16 @@ typedef struct {
     double table_max;
 } orc_pair;
 
-/* Bond / angle potential (Harmonic or absent). */
 /* Bond, angle and dihedral potentials: ORC_PAIR_NULL, ORC_PAIR_HARMONIC {k, x0},
  * ORC_BONDED_COSINE_HARMONIC {k, x0} (CosineHarmonic::new, functions.rs:162-210),
- * ORC_BONDED_TORSION {k, delta = x0, n} (functions.rs:212-258). */
+ * ORC_BONDED_TORSION {k, delta = x0, n} (functions.rs:212-258),
+ * ORC_PAIR_MORSE {depth = k, x0, a} (functions.rs:405-437). */
 enum { ORC_BONDED_COSINE_HARMONIC = 10, ORC_BONDED_TORSION = 11 };
 typedef struct {
     int32_t type;        /* 0: absent, ORC_PAIR_NULL, ORC_PAIR_HARMONIC or ORC_BONDED_* */
     int32_t n;           /* Torsion multiplicity */
     double k, x0;
+    double a;            /* Morse width */
 } orc_bonded;
 
 typedef struct {
