@@ -219,6 +219,16 @@ int lg_set_coulomb(lg_engine* e, int32_t s, const lg_coulomb* coulomb);
 int lg_compute(lg_engine* e, int32_t s, const double* positions, uint32_t terms, uint32_t want,
                double* forces, double* energy, double virial[9]);
 
+/* MolecularVirial::compute (sys/compute.rs:278-362) of system `s` at
+ * `positions`: pair potentials and real-space Coulomb between molecules with
+ * the molecular definition (w_ab (r_ab . r_ij) / r_ab^2, r_ij the image of the
+ * centres of mass), the tail correction, and the Ewald k-space atomic virial
+ * minus sum_a F_k,a (x) (x_a - com) (ewald.rs:533-571, 736-752; wolf.rs:285-320);
+ * bonds, angles and dihedral angles contribute nothing.  `terms` selects among
+ * LG_TERM_PAIRS, LG_TERM_TAIL, LG_TERM_COUL_REAL and LG_TERM_COUL_KSPACE.
+ * FP64 engines only. */
+int lg_molecular_virial(lg_engine* e, int32_t s, const double* positions, uint32_t terms, double virial[9]);
+
 /* Same for every system of the engine, on device pointers: d_positions and
  * d_forces hold 3*N_total doubles (systems in index order, forces overwritten),
  * d_energy n_systems doubles and d_virial 9*n_systems doubles.  `stream` is a

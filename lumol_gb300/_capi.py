@@ -113,6 +113,7 @@ SIGNATURES = {
     "lg_set_pairs": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(LgPair)]),
     "lg_set_coulomb": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(LgCoulomb)]),
     "lg_compute": (ctypes.c_int, [_P, ctypes.c_int32, _D, ctypes.c_uint32, ctypes.c_uint32, _D, _D, _D]),
+    "lg_molecular_virial": (ctypes.c_int, [_P, ctypes.c_int32, _D, ctypes.c_uint32, _D]),
     "lg_compute_device": (ctypes.c_int, [_P, _P, ctypes.c_uint32, ctypes.c_uint32, _P, _P, _P, _P]),
     "lg_pairset": (ctypes.c_int, [_P, ctypes.c_int32, _D, ctypes.c_int32, _I32, ctypes.c_int64, _I64]),
     "lg_md_setup": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double]),

@@ -391,6 +391,7 @@ struct lg_engine {
     DBuf<float> inv_mass;
     DBuf<int> nlo, rev;
     DBuf<double4_32a> pf;
+    DBuf<double4_32a> molcom;  // per-atom centre of mass of its molecule (molecular virial)
     DBuf<PairDevF> ptabf;
     DBuf<double2> table;  // TableComputation tables (plain path)
     DBuf<float2> tablef;  // the same in FP32 (mixed path)
@@ -1421,6 +1422,35 @@ int lg_compute(lg_engine* e, int32_t s, const double* positions, uint32_t terms,
     if ((want & LG_WANT_ENERGY) && energy) *energy = e->h_out[0];
     if ((want & LG_WANT_VIRIAL) && virial)
         for (int c = 0; c < 9; c++) virial[c] = e->h_out[1 + c];
+    return LG_OK;
+}
+
+int lg_molecular_virial(lg_engine* e, int32_t s, const double* positions, uint32_t terms, double virial[9]) {
+    if (!valid_sys(e, s) || !positions || !virial) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    if (e->opt.precision != LG_PRECISION_FP64)
+        return fail(e, LG_ERR_ARGUMENT, "the molecular virial is computed by fp64 engines");
+    CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    int rc = commit(e);
+    if (rc) return rc;
+    cudaStream_t st = e->stream;
+    rc = upload_positions(e, s, positions);
+    if (rc) return rc;
+    // the k-space forces (and the list for the current positions)
+    bool kspace = (terms & LG_TERM_COUL_KSPACE) && e->b.nkvec;
+    rc = compute_batch(e, terms & LG_TERM_COUL_KSPACE, LG_WANT_FORCES | LG_WANT_VIRIAL, nullptr, nullptr);
+    if (rc) return rc;
+    if (e->molcom.n < (size_t)e->b.n) CUDA_TRY(e, e->molcom.alloc(e->b.n));
+    CUDA_TRY(e, cudaMemsetAsync(e->red.p, 0, (size_t)e->b.n * RED_STRIDE * sizeof(double), st));
+    launch_molecular_virial(e->b, terms & (LG_TERM_PAIRS | LG_TERM_COUL_REAL), e->molcom.p,
+                            kspace ? e->force.p : nullptr, st);
+    launch_reduce(e->b, terms & (LG_TERM_PAIRS | LG_TERM_TAIL | LG_TERM_COUL_REAL | LG_TERM_COUL_KSPACE), kspace,
+                  e->out.p, st);
+    e->launches += 3;
+    CUDA_TRY(e, cudaGetLastError());
+    CUDA_TRY(e, cudaMemcpyAsync(e->h_out, e->out.p + (size_t)s * RED_STRIDE, RED_STRIDE * sizeof(double),
+                                cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(e, cudaStreamSynchronize(st));
+    for (int c = 0; c < 9; c++) virial[c] = e->h_out[1 + c];
     return LG_OK;
 }
 

@@ -367,15 +367,14 @@ __global__ void bonded_kernel(int n, const double4_32a* __restrict__ posq, const
             double dx, dy, dz;
             exact_nearest_image(s, pa.x, pa.y, pa.z, pb.x, pb.y, pb.z, dx, dy, dz);
             double r = exact_norm(dx, dy, dz);
-            double f = null_pot ? 0.0 : par.x * (par.y - r);
+            double f = bonded_force(par, r);  // 0 for a NullPotential
             double gx = f * (dx / r), gy = f * (dy / r), gz = f * (dz / r);
             double sgn = role == 0 ? 1.0 : -1.0;
             fx += sgn * gx;
             fy += sgn * gy;
             fz += sgn * gz;
             if (EV && role == 0) {
-                double dr = r - par.y;
-                eb += null_pot ? 0.0 : 0.5 * par.x * dr * dr;
+                eb += bonded_energy(par, r);
                 w[0] += gx * dx; w[1] += gx * dy; w[2] += gx * dz;
                 w[3] += gy * dy; w[4] += gy * dz; w[5] += gz * dz;
             }
@@ -717,6 +716,105 @@ void launch_reduce(const Batch& b, uint32_t terms, bool kspace, double* out, cud
     if (b.nsys == 0) return;
     reduce_kernel<<<b.nsys, 256, 0, st>>>(b.sys, b.red, b.kred, b.host_const, terms, kspace ? 1 : 0, out,
                                           b.status);
+}
+
+// ---------------------------------------------------------------------------
+// Molecular virial (MolecularVirial, sys/compute.rs:278-362).  The centre of
+// mass of every molecule (molecules.rs:256-264) is written to each of its
+// atoms; then every atom walks the j > i part of its neighbour row and, for
+// pairs of different molecules, adds w_ab (r_ab . r_ij) / r_ab^2 with w_ab the
+// pair and real-space Coulomb virial of the pair (Ewald ewald.rs:533-571, Wolf
+// wolf.rs:285-320) and r_ij the image of the centres' separation; with the
+// k-space forces given, it also subtracts F_k,a (x) (x_a - com) (the Ewald
+// k-space correction, ewald.rs:736-752).  Each atom assigns its nine slots.
+// ---------------------------------------------------------------------------
+__global__ void molecule_com_kernel(int nmol, const int* __restrict__ mol_start,
+                                    const double4_32a* __restrict__ posq, const double4_32a* __restrict__ vel,
+                                    double4_32a* __restrict__ com) {
+    int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nmol) return;
+    int a0 = mol_start[m], a1 = mol_start[m + 1];
+    double total = 0.0, cx = 0.0, cy = 0.0, cz = 0.0;
+    for (int a = a0; a < a1; a++) {
+        double4_32a p = posq[a];
+        double mass = vel[a].w;
+        total += mass;
+        cx += mass * p.x;
+        cy += mass * p.y;
+        cz += mass * p.z;
+    }
+    double4_32a c = make_double4_32a(cx / total, cy / total, cz / total, 0.0);
+    for (int a = a0; a < a1; a++) com[a] = c;
+}
+
+__global__ void __launch_bounds__(128) molecular_virial_kernel(
+    int n, const double4_32a* __restrict__ posq, const int* __restrict__ kind, const int* __restrict__ mol,
+    const int* __restrict__ sysid, const SysDev* __restrict__ sys, const PairDev* __restrict__ ptab,
+    const int* __restrict__ nbr, const int* __restrict__ nnb, const int* __restrict__ nlo, int maxnb,
+    const int* __restrict__ spec_off, const int* __restrict__ spec_j, const int8_t* __restrict__ spec_path,
+    uint32_t terms, const double4_32a* __restrict__ com, const double* __restrict__ kforce,
+    double* __restrict__ red) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const SysDev& s = sys[sysid[i]];
+    double4_32a pi = posq[i], ci = com[i];
+    int ki = kind[i], mi = mol[i];
+    const PairDev* prow = ptab + s.ptab + ki * s.nk;
+    double w[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const int* list = nbr + (size_t)i * maxnb;
+    for (int k = nlo[i]; k < nnb[i]; k++) {
+        int j = list[k];
+        if (mol[j] == mi) continue;
+        double4_32a pj = posq[j];
+        double dx, dy, dz;
+        exact_nearest_image(s, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z, dx, dy, dz);
+        double r = exact_norm(dx, dy, dz);
+        const PairDev& p = prow[kind[j]];
+        PairDecision dec = decide_pair(s, p, terms, i, j, mi, mol[j], pi.w, pj.w, r, spec_off, spec_j, spec_path);
+        if (!dec.pair_in && !dec.coul_in) continue;
+        double inv_r = 1.0 / r;
+        double f_over_r = 0.0;
+        if (dec.pair_in) {
+            double e, f;
+            pair_energy_force(p, r, inv_r, e, f);
+            f_over_r += dec.pair_scale * f * inv_r;
+        }
+        if (dec.coul_in) {
+            double e, fr;
+            if (s.coul == 1) {
+                ewald_real_pair(s.alpha, dec.coul_excl, pi.w * pj.w, r, inv_r, e, fr);
+            } else {
+                wolf_pair(s, pi.w * pj.w, r, inv_r, e, fr);
+                fr *= dec.coul_scale;
+            }
+            f_over_r += fr;
+        }
+        double4_32a cj = com[j];
+        double rx = exact_image(__dsub_rn(ci.x, cj.x), s.L[0], s.invL[0]);
+        double ry = exact_image(__dsub_rn(ci.y, cj.y), s.L[1], s.invL[1]);
+        double rz = exact_image(__dsub_rn(ci.z, cj.z), s.L[2], s.invL[2]);
+        double scale = f_over_r * (dx * rx + dy * ry + dz * rz) / (dx * dx + dy * dy + dz * dz);
+        double gx = scale * dx, gy = scale * dy, gz = scale * dz;
+        w[0] += gx * dx; w[1] += gx * dy; w[2] += gx * dz;
+        w[3] += gy * dx; w[4] += gy * dy; w[5] += gy * dz;
+        w[6] += gz * dx; w[7] += gz * dy; w[8] += gz * dz;
+    }
+    if (kforce != nullptr && s.coul == 1) {
+        double d[3] = {pi.x - ci.x, pi.y - ci.y, pi.z - ci.z};
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) w[3 * a + b] -= kforce[3 * i + a] * d[b];
+    }
+    double* out = red + (size_t)i * RED_STRIDE + N_ESLOT;
+    for (int c = 0; c < 9; c++) out[c] = w[c];
+}
+
+void launch_molecular_virial(const Batch& b, uint32_t terms, double4_32a* com, const double* kforce,
+                             cudaStream_t st) {
+    if (b.n == 0) return;
+    molecule_com_kernel<<<(b.nmol + 127) / 128, 128, 0, st>>>(b.nmol, b.mol_start, b.posq, b.vel, com);
+    molecular_virial_kernel<<<(b.n + 127) / 128, 128, 0, st>>>(
+        b.n, b.posq, b.kind, b.mol, b.sysid, b.sys, b.ptab, b.nbr, b.nnb, b.nlo, b.maxnb, b.spec_off, b.spec_j,
+        b.spec_path, terms, com, kforce, b.red);
 }
 
 // ---------------------------------------------------------------------------

@@ -120,6 +120,10 @@ void launch_pair_mixed(const Batch& b, uint32_t terms, bool ev, cudaStream_t st)
 void launch_split_positions(const Batch& b, cudaStream_t st);
 void launch_kspace_mixed_part(const Batch& b, int part, bool ev, cudaStream_t st);
 void launch_reduce(const Batch& b, uint32_t terms, bool kspace, double* out, cudaStream_t st);
+// MolecularVirial's pair / real-space part minus the Ewald k-space correction
+// (kforce: the k-space forces, or null) into the per-atom virial slots of red.
+void launch_molecular_virial(const Batch& b, uint32_t terms, double4_32a* com, const double* kforce,
+                             cudaStream_t st);
 void launch_pairset(const Batch& b, int family, int s_begin, int s_end, int* out, long long cap,
                     unsigned long long* count, cudaStream_t st);
 // md.cu

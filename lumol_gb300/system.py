@@ -658,6 +658,15 @@ class System:
         """System::virial with the atomic definition (sys/compute.rs:198-254)."""
         return self.compute(C.LG_TERM_ALL, C.LG_WANT_VIRIAL)[2]
 
+    def molecular_virial(self, terms: int = C.LG_TERM_ALL) -> np.ndarray:
+        """MolecularVirial::compute (sys/compute.rs:278-362): the virial with
+        the molecular definition (FP64 systems)."""
+        eng = self.engine()
+        pos = np.ascontiguousarray(self.positions, dtype=np.float64)
+        virial = np.zeros(9)
+        eng.call("lg_molecular_virial", 0, C.dptr(pos), terms, C.dptr(virial))
+        return virial.reshape(3, 3)
+
     def energy_term(self, terms: int) -> float:
         return self.compute(terms, C.LG_WANT_ENERGY)[1]
 

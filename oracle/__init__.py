@@ -92,6 +92,7 @@ def load() -> ctypes.CDLL:
         lib.orc_energy.argtypes = [P, ctypes.c_int]
         lib.orc_forces.argtypes = [P, ctypes.c_int, V]
         lib.orc_virial.argtypes = [P, ctypes.c_int, V]
+        lib.orc_molecular_virial.argtypes = [P, ctypes.c_int, V]
         lib.orc_pairset.restype = ctypes.c_int64
         lib.orc_pairset.argtypes = [P, ctypes.c_int, V, ctypes.c_int64]
         lib.orc_velocity_verlet.argtypes = [P, V, V, V, ctypes.c_double, ctypes.c_int64, ctypes.c_double,
@@ -226,6 +227,12 @@ class Oracle:
     def virial(self, terms: int = TERM_ALL) -> np.ndarray:
         v = np.zeros(9)
         self.lib.orc_virial(self.h, terms, _ptr(v))
+        return v.reshape(3, 3)
+
+    def molecular_virial(self, terms: int = TERM_ALL) -> np.ndarray:
+        """MolecularVirial (sys/compute.rs:278-362)."""
+        v = np.zeros(9)
+        self.lib.orc_molecular_virial(self.h, terms, _ptr(v))
         return v.reshape(3, 3)
 
     def pairset(self, family: int) -> np.ndarray:

@@ -1318,6 +1318,83 @@ void orc_virial(orc_system* s, int terms, double* out) {
         for (int b = 0; b < 3; b++) out[3 * a + b] = v.m[a][b];
 }
 
+// Molecule::center_of_mass (sys/config/molecules.rs:256-264)
+V3 center_of_mass(const orc_system* s, size_t m) {
+    double total = 0.0;
+    V3 com{{0.0, 0.0, 0.0}};
+    for (int64_t i = s->mol_range[m].first; i < s->mol_range[m].second; i++) {
+        total += s->mass[i];
+        com = vadd(com, vscale(s->mass[i], s->pos[i]));
+    }
+    return V3{{com[0] / total, com[1] / total, com[2] / total}};
+}
+
+// MolecularVirial::compute (compute.rs:278-362), per term: the pair potentials
+// between molecules with the molecular definition (Allen & Tildesley 2.54,
+// 2.61, 2.63), the tail correction, bonds ignored; real-space Coulomb with
+// the same definition (Ewald ewald.rs:533-571, Wolf wolf.rs:285-320) and the
+// Ewald k-space atomic virial minus sum_i F_k,i (x) (x_i - com) (ewald.rs:736-752).
+void orc_molecular_virial(orc_system* s, int terms, double* out) {
+    size_t nm = s->mol_range.size();
+    std::vector<V3> com(nm);
+    for (size_t m = 0; m < nm; m++) com[m] = center_of_mass(s, m);
+    bool ewald = s->coul.kind == ORC_COULOMB_EWALD;
+    bool coul = s->coul.kind != ORC_COULOMB_NONE && (terms & ORC_TERM_COUL_REAL);
+    if (ewald) ewald_prepare(s);
+    std::vector<M3> partial(nthreads(), mzero());
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int64_t mi = 0; mi < (int64_t)nm; mi++) {
+        M3 local = mzero();
+        for (size_t mj = (size_t)mi + 1; mj < nm; mj++) {
+            V3 rij = vsub(com[mi], com[mj]);
+            s->cell.vector_image(rij);
+            for (int64_t a = s->mol_range[mi].first; a < s->mol_range[mi].second; a++) {
+                for (int64_t b = s->mol_range[mj].first; b < s->mol_range[mj].second; b++) {
+                    V3 rab = s->nearest_image(a, b);
+                    double dot = vdot(rab, rij), n2 = vdot(rab, rab);
+                    if (terms & ORC_TERM_PAIRS) {
+                        const PairPot* p = s->pair(a, b);
+                        if (p) {
+                            RestrictionInfo info = information(p->d.restriction, p->d.scale14, s->bond_path(a, b));
+                            if (!info.excluded) madd(local, mscale(dot / n2, mscale(info.scaling, p->virial(rab))));
+                        }
+                    }
+                    double qa = s->charge[a], qb = s->charge[b];
+                    if (coul && qa != 0.0 && qb != 0.0) {
+                        RestrictionInfo info = coul_info(s, a, b);
+                        V3 f;
+                        if (ewald) {
+                            f = vscale(ewald_real_force_pair(s, info, qa * qb, vnorm(rab)), rab);
+                        } else {
+                            if (info.excluded) continue;
+                            f = vscale(info.scaling * wolf_force_pair(s, qa * qb, vnorm(rab)), rab);
+                        }
+                        madd(local, mscale(dot / n2, tensorial(f, rab)));
+                    }
+                }
+            }
+        }
+        madd(partial[thread_id()], local);
+    }
+    M3 v = mzero();
+    for (auto& m : partial) madd(v, m);
+    if (terms & ORC_TERM_TAIL) madd(v, pairs_tail_virial(s));
+    if (ewald && (terms & ORC_TERM_COUL_KSPACE)) {
+        madd(v, ewald_kspace_virial(s));
+        std::vector<double> fk(3 * (size_t)s->n, 0.0);
+        ewald_kspace_forces(s, fk.data());
+        M3 correction = mzero();
+        for (size_t m = 0; m < nm; m++)
+            for (int64_t i = s->mol_range[m].first; i < s->mol_range[m].second; i++) {
+                V3 fi{{fk[3 * i], fk[3 * i + 1], fk[3 * i + 2]}};
+                madd(correction, tensorial(fi, vsub(s->pos[i], com[m])));
+            }
+        madd(v, mscale(-1.0, correction));
+    }
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++) out[3 * a + b] = v.m[a][b];
+}
+
 int64_t orc_pairset(orc_system* s, int family, int32_t* out, int64_t cap) {
     int64_t count = 0;
     for (int64_t i = 0; i < s->n; i++) {

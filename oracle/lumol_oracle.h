@@ -137,6 +137,9 @@ double orc_energy(orc_system* s, int terms);
 /* forces (3n) are ACCUMULATED into `forces`. */
 void orc_forces(orc_system* s, int terms, double* forces);
 void orc_virial(orc_system* s, int terms, double* virial9);
+/* MolecularVirial (sys/compute.rs:278-362) with the terms PAIRS, TAIL,
+ * COUL_REAL and COUL_KSPACE (bonds, angles and dihedral angles give none). */
+void orc_molecular_virial(orc_system* s, int terms, double* virial9);
 
 /* Pair set of a family: 0 = pair potentials (r < cutoff and not excluded),
  * 1 = real-space Coulomb (r <= cutoff, q_i q_j != 0).  Returns the count and

@@ -1,0 +1,99 @@
+"""MolecularVirial (lumol-core/src/sys/compute.rs:278-362) on the GPU and in
+the oracle.
+
+The reference has no known-answer test for it (its benches time it,
+benches/{water,nacl,argon,propane}.rs), so the oracle's restatement is pinned
+by two properties of the definition: for one-atom molecules it equals the
+atomic virial term by term, and for rigid molecules its trace is minus the
+derivative of the potential energy when the centres of mass and the cell are
+scaled together (the virial theorem the molecular definition is built for),
+where the image of the centres' separation agrees with the atoms' one.
+The GPU is then held to the oracle at 1e-10 relative."""
+import numpy as np
+import pytest
+
+import lumol_gb300 as lg
+import oracle
+import systems
+from lumol_gb300 import workloads
+
+PAIRS, TAIL, REAL, KSPACE = lg.LG_TERM_PAIRS, lg.LG_TERM_TAIL, lg.LG_TERM_COUL_REAL, lg.LG_TERM_COUL_KSPACE
+TERMS = [PAIRS | TAIL | REAL | KSPACE, PAIRS, TAIL, REAL, KSPACE]
+
+
+def _rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def small_water(coulomb="ewald", scale=1.0, seed=5):
+    """64 water molecules in an 18 A cell, cutoff 6.5 A: every pair of atoms
+    within the cutoff belongs to molecules whose centres are closer than half
+    the cell, so the image of the centres' separation is the one of the atoms'."""
+    s = workloads.water_box(n_side=4, length=18.0, seed=seed, cutoff=6.5, alpha=0.45, kmax=6)
+    if coulomb == "wolf":
+        w = lg.Wolf(6.5)
+        w.set_restriction(lg.PairRestriction.INTER_MOLECULAR)
+        s.set_coulomb_potential(w)
+    if scale != 1.0:
+        x = s.positions.reshape(-1, 3, 3)
+        m = s.masses.reshape(-1, 3, 1)
+        com = (m * x).sum(axis=1, keepdims=True) / m.sum(axis=1, keepdims=True)
+        s.cell = lg.UnitCell.cubic(18.0 * scale)
+        s.positions = (x + (scale - 1.0) * com).reshape(-1, 3)
+    return s
+
+
+def nacl(coulomb="ewald"):
+    return workloads.nacl_crystal(cells=3, a=5.64, jitter=0.1, seed=2, cutoff=8.0, coulomb=coulomb)
+
+
+def test_oracle_one_atom_molecules_equal_atomic_virial():
+    cases = [systems.random_lj_fluid(400, 0.02, 3, 9.0, family="lj"), nacl(), nacl("wolf")]
+    for s in cases:
+        orc = oracle.Oracle(s)
+        for terms in TERMS:
+            atomic, molecular = orc.virial(terms), orc.molecular_virial(terms)
+            if np.abs(atomic).max() == 0.0:
+                assert np.abs(molecular).max() == 0.0
+            else:
+                assert _rel(molecular, atomic) < 1e-12, terms
+
+
+def test_oracle_trace_is_the_centre_of_mass_scaling_derivative():
+    """tr W_mol = -dU/d lambda for x_a -> x_a + (lambda - 1) com(a), L -> lambda L
+    (pairs, Ewald real space, self and k space; rigid molecules)."""
+    terms = PAIRS | REAL | lg.LG_TERM_COUL_SELF | KSPACE
+    eps = 1e-5
+    energy = {}
+    for lam in (1.0 - eps, 1.0 + eps):
+        energy[lam] = oracle.Oracle(small_water(scale=lam)).energy(terms)
+    dudl = (energy[1.0 + eps] - energy[1.0 - eps]) / (2.0 * eps)
+    w = oracle.Oracle(small_water()).molecular_virial(PAIRS | REAL | KSPACE)
+    assert abs(np.trace(w) + dudl) / abs(dudl) < 1e-7
+    # the atomic virial differs for molecules (it holds the intramolecular forces)
+    atomic = oracle.Oracle(small_water()).virial(PAIRS | REAL | KSPACE)
+    assert _rel(w, atomic) > 1e-3
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["water_ewald", "water_wolf", "chains_wolf", "argon", "nacl"])
+def test_molecular_virial_matches_oracle(name):
+    s = {"water_ewald": lambda: small_water(),
+         "water_wolf": lambda: small_water("wolf"),
+         "chains_wolf": lambda: systems.chains(27, 24.0, 9, lg.PairRestriction.EXCLUDE13, coulomb=lg.Wolf(8.0)),
+         "argon": lambda: systems.random_lj_fluid(400, 0.02, 3, 9.0, family="lj"),
+         "nacl": nacl}[name]()
+    orc = oracle.Oracle(s)
+    for terms in TERMS + [lg.LG_TERM_ALL]:
+        gpu, ref = s.molecular_virial(terms), orc.molecular_virial(terms)
+        if np.abs(ref).max() < 1e-14:
+            assert np.abs(gpu).max() < 1e-14, terms
+        else:
+            assert _rel(gpu, ref) <= 1e-10, (terms, gpu, ref)
+
+
+@pytest.mark.gpu
+def test_molecular_virial_needs_fp64():
+    s = systems.random_lj_fluid(200, 0.02, 3, 9.0, family="lj", precision="mixed")
+    with pytest.raises(lg.EngineError, match="fp64"):
+        s.molecular_virial()
