@@ -1163,6 +1163,74 @@ int compute_batch(lg_engine* e, uint32_t terms, uint32_t want, double* d_force_o
     return fail(e, LG_ERR_CAPACITY, "neighbour list overflow persisted after regrowing");
 }
 
+// The device address of a page-locked host buffer (cudaHostAlloc /
+// cudaHostRegister memory is mapped into the device's address space under
+// unified addressing), or null for pageable memory.  The pack / unpack kernels
+// read and write such buffers over the host link directly, which fuses the
+// host <-> device transfer with the change of layout.
+const void* mapped_host(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// Host positions and velocities (3 n doubles each) of atoms [base, base + n)
+// into the packed device state: read in place from page-locked buffers, else
+// staged through pos3 / vel3.
+int put_state(lg_engine* e, int64_t base, int64_t n, const double* positions, const double* velocities) {
+    cudaStream_t st = e->stream;
+    Batch sub = e->b;
+    sub.n = (int)n;
+    sub.posq = e->posq.p + base;
+    sub.vel = e->vel.p + base;
+    const double* dp = (const double*)mapped_host(positions);
+    const double* dv = (const double*)mapped_host(velocities);
+    if (!dp) {
+        CUDA_TRY(e, cudaMemcpyAsync(e->pos3.p + 3 * base, positions, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st));
+        dp = e->pos3.p + 3 * base;
+    }
+    if (!dv) {
+        CUDA_TRY(e, cudaMemcpyAsync(e->vel3.p + 3 * base, velocities, 3 * n * sizeof(double), cudaMemcpyHostToDevice,
+                                    st));
+        dv = e->vel3.p + 3 * base;
+    }
+    launch_pack_positions(sub, dp, st);
+    launch_pack_velocities(sub, dv, st);
+    e->launches += 2;
+    return LG_OK;
+}
+
+// The packed device state of atoms [base, base + n) into host positions and
+// velocities (either may be null): written in place into page-locked buffers,
+// else staged through pos3 / vel3.
+int get_state(lg_engine* e, int64_t base, int64_t n, double* positions, double* velocities) {
+    cudaStream_t st = e->stream;
+    Batch sub = e->b;
+    sub.n = (int)n;
+    sub.posq = e->posq.p + base;
+    sub.vel = e->vel.p + base;
+    if (positions) {
+        double* dp = (double*)mapped_host(positions);
+        launch_unpack_positions(sub, dp ? dp : e->pos3.p + 3 * base, st);
+        e->launches += 1;
+        if (!dp)
+            CUDA_TRY(e, cudaMemcpyAsync(positions, e->pos3.p + 3 * base, 3 * n * sizeof(double),
+                                        cudaMemcpyDeviceToHost, st));
+    }
+    if (velocities) {
+        double* dv = (double*)mapped_host(velocities);
+        launch_unpack_velocities(sub, dv ? dv : e->vel3.p + 3 * base, st);
+        e->launches += 1;
+        if (!dv)
+            CUDA_TRY(e, cudaMemcpyAsync(velocities, e->vel3.p + 3 * base, 3 * n * sizeof(double),
+                                        cudaMemcpyDeviceToHost, st));
+    }
+    return LG_OK;
+}
+
 // Copies the host positions of system s into its slice of the device state;
 // the other systems keep theirs.
 int upload_positions(lg_engine* e, int32_t s, const double* positions) {
@@ -1598,15 +1666,8 @@ int lg_md_set_state(lg_engine* e, int32_t s, const double* positions, const doub
     int64_t base = e->begin[s];
     cudaStream_t st = e->stream;
     if (h.n == 0) return LG_OK;
-    CUDA_TRY(e, cudaMemcpyAsync(e->pos3.p + 3 * base, positions, 3 * h.n * sizeof(double), cudaMemcpyHostToDevice, st));
-    CUDA_TRY(e, cudaMemcpyAsync(e->vel3.p + 3 * base, velocities, 3 * h.n * sizeof(double), cudaMemcpyHostToDevice, st));
-    // pack only this system's atoms: the other systems keep their state
-    Batch sub = e->b;
-    sub.n = (int)h.n;
-    sub.posq = e->posq.p + base;
-    sub.vel = e->vel.p + base;
-    launch_pack_positions(sub, e->pos3.p + 3 * base, st);
-    launch_pack_velocities(sub, e->vel3.p + 3 * base, st);
+    rc = put_state(e, base, h.n, positions, velocities);  // this system's atoms only
+    if (rc) return rc;
     if (was_dirty) CUDA_TRY(e, cudaMemsetAsync(e->acc.p, 0, e->b.n * sizeof(double4_32a), st));
     CUDA_TRY(e, cudaGetLastError());
     CUDA_TRY(e, cudaStreamSynchronize(st));
@@ -1621,16 +1682,9 @@ int lg_md_get_state(lg_engine* e, int32_t s, double* positions, double* velociti
     int64_t base = e->begin[s];
     cudaStream_t st = e->stream;
     if (h.n == 0) return LG_OK;
-    Batch sub = e->b;
-    sub.n = (int)h.n;
-    sub.posq = e->posq.p + base;
-    sub.vel = e->vel.p + base;
-    launch_unpack_positions(sub, e->pos3.p + 3 * base, st);
-    launch_unpack_velocities(sub, e->vel3.p + 3 * base, st);
-    if (positions)
-        CUDA_TRY(e, cudaMemcpyAsync(positions, e->pos3.p + 3 * base, 3 * h.n * sizeof(double), cudaMemcpyDeviceToHost, st));
-    if (velocities)
-        CUDA_TRY(e, cudaMemcpyAsync(velocities, e->vel3.p + 3 * base, 3 * h.n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    int rc = get_state(e, base, h.n, positions, velocities);
+    if (rc) return rc;
+    CUDA_TRY(e, cudaGetLastError());
     CUDA_TRY(e, cudaStreamSynchronize(st));
     return LG_OK;
 }
@@ -1987,7 +2041,9 @@ int lg_md_run(lg_engine* e, int64_t nsteps) {
         if (rc) return rc;
     }
     // the persistent kernel for runs of several steps: a launch pays for the
-    // slowest group's list rebuild, which short runs do not amortize
+    // slowest group's list rebuild, which short runs do not amortize (a
+    // 1-step launch measured 193 us against 178 us for the per-step kernels
+    // on the 128-replica batch)
     if (persist_eligible(e) && nsteps >= 8) {
         if (e->pk_cluster == 0) {
             int rc = persist_plan(e);
@@ -2043,11 +2099,8 @@ int lg_md_set_state_all(lg_engine* e, const double* positions, const double* vel
     cudaStream_t st = e->stream;
     size_t n = (size_t)e->b.n;
     if (n == 0) return LG_OK;
-    CUDA_TRY(e, cudaMemcpyAsync(e->pos3.p, positions, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st));
-    CUDA_TRY(e, cudaMemcpyAsync(e->vel3.p, velocities, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st));
-    launch_pack_positions(e->b, e->pos3.p, st);
-    launch_pack_velocities(e->b, e->vel3.p, st);
-    e->launches += 2;
+    rc = put_state(e, 0, (int64_t)n, positions, velocities);
+    if (rc) return rc;
     if (accelerations) {
         CUDA_TRY(e, cudaMemcpyAsync(e->force.p, accelerations, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st));
         launch_pack_vectors(e->b.n, e->force.p, e->acc.p, st);
@@ -2067,13 +2120,8 @@ int lg_md_get_state_all(lg_engine* e, double* positions, double* velocities, dou
     cudaStream_t st = e->stream;
     size_t n = (size_t)e->b.n;
     if (n == 0) return LG_OK;
-    launch_unpack_positions(e->b, e->pos3.p, st);
-    launch_unpack_velocities(e->b, e->vel3.p, st);
-    e->launches += 2;
-    if (positions)
-        CUDA_TRY(e, cudaMemcpyAsync(positions, e->pos3.p, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, st));
-    if (velocities)
-        CUDA_TRY(e, cudaMemcpyAsync(velocities, e->vel3.p, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    int rc = get_state(e, 0, (int64_t)n, positions, velocities);
+    if (rc) return rc;
     if (accelerations) {
         launch_unpack_vectors(e->b.n, e->acc.p, e->force.p, st);
         e->launches += 1;

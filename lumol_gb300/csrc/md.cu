@@ -16,39 +16,27 @@
 
 namespace lg {
 
-__global__ void pack_positions_kernel(int n, const double* __restrict__ pos3, double4_32a* __restrict__ posq) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    double4_32a p = posq[i];
-    p.x = pos3[3 * i];
-    p.y = pos3[3 * i + 1];
-    p.z = pos3[3 * i + 2];
-    posq[i] = p;
+// Layout changes between 3 n doubles (x, y, z per atom) and the packed
+// double4 state (x, y, z plus the charge or mass, kept): one thread per double
+// of the 3 n array, so the 3 n side is read or written in whole contiguous
+// lines (it may be a page-locked host buffer reached over the host link).
+__global__ void pack3_kernel(int n3, const double* __restrict__ src3, double* __restrict__ dst4) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n3) return;
+    int i = t / 3;
+    dst4[4 * i + (t - 3 * i)] = src3[t];
 }
-__global__ void unpack_positions_kernel(int n, const double4_32a* __restrict__ posq, double* __restrict__ pos3) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    double4_32a p = posq[i];
-    pos3[3 * i] = p.x;
-    pos3[3 * i + 1] = p.y;
-    pos3[3 * i + 2] = p.z;
+__global__ void unpack3_kernel(int n3, const double* __restrict__ src4, double* __restrict__ dst3) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n3) return;
+    int i = t / 3;
+    dst3[t] = src4[4 * i + (t - 3 * i)];
 }
-__global__ void pack_velocities_kernel(int n, const double* __restrict__ vel3, double4_32a* __restrict__ vel) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    double4_32a v = vel[i];
-    v.x = vel3[3 * i];
-    v.y = vel3[3 * i + 1];
-    v.z = vel3[3 * i + 2];
-    vel[i] = v;
+void launch_pack3(int n, const double* src3, double4_32a* dst, cudaStream_t st) {
+    if (n) pack3_kernel<<<(3 * n + 255) / 256, 256, 0, st>>>(3 * n, src3, reinterpret_cast<double*>(dst));
 }
-__global__ void unpack_velocities_kernel(int n, const double4_32a* __restrict__ vel, double* __restrict__ vel3) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    double4_32a v = vel[i];
-    vel3[3 * i] = v.x;
-    vel3[3 * i + 1] = v.y;
-    vel3[3 * i + 2] = v.z;
+void launch_unpack3(int n, const double4_32a* src, double* dst3, cudaStream_t st) {
+    if (n) unpack3_kernel<<<(3 * n + 255) / 256, 256, 0, st>>>(3 * n, reinterpret_cast<const double*>(src), dst3);
 }
 
 __global__ void pack_vectors_kernel(int n, const double* __restrict__ src3, double4_32a* __restrict__ dst) {
@@ -60,20 +48,14 @@ void launch_pack_vectors(int n, const double* src3, double4_32a* dst, cudaStream
     if (n) pack_vectors_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, src3, dst);
 }
 void launch_unpack_vectors(int n, const double4_32a* src, double* dst3, cudaStream_t st) {
-    if (n) unpack_velocities_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, src, dst3);
+    launch_unpack3(n, src, dst3, st);
 }
 
-void launch_pack_positions(const Batch& b, const double* pos3, cudaStream_t st) {
-    if (b.n) pack_positions_kernel<<<(b.n + 255) / 256, 256, 0, st>>>(b.n, pos3, b.posq);
-}
-void launch_unpack_positions(const Batch& b, double* pos3, cudaStream_t st) {
-    if (b.n) unpack_positions_kernel<<<(b.n + 255) / 256, 256, 0, st>>>(b.n, b.posq, pos3);
-}
-void launch_pack_velocities(const Batch& b, const double* vel3, cudaStream_t st) {
-    if (b.n) pack_velocities_kernel<<<(b.n + 255) / 256, 256, 0, st>>>(b.n, vel3, b.vel);
-}
+void launch_pack_positions(const Batch& b, const double* pos3, cudaStream_t st) { launch_pack3(b.n, pos3, b.posq, st); }
+void launch_unpack_positions(const Batch& b, double* pos3, cudaStream_t st) { launch_unpack3(b.n, b.posq, pos3, st); }
+void launch_pack_velocities(const Batch& b, const double* vel3, cudaStream_t st) { launch_pack3(b.n, vel3, b.vel, st); }
 void launch_unpack_velocities(const Batch& b, double* vel3, cudaStream_t st) {
-    if (b.n) unpack_velocities_kernel<<<(b.n + 255) / 256, 256, 0, st>>>(b.n, b.vel, vel3);
+    launch_unpack3(b.n, b.vel, vel3, st);
 }
 
 // Marks system si for a list rebuild.  The flag store is idempotent; the

@@ -145,3 +145,46 @@ def test_persistent_other_pair_potentials():
     for (pa, va), (pb, vb) in zip(*states):
         assert np.all(np.isfinite(pa))
         assert np.array_equal(pa, pb) and np.array_equal(va, vb)
+
+
+def test_pinned_host_buffers_match_pageable():
+    """lg_md_set_state(_all) / lg_md_get_state(_all) read and write page-locked
+    host buffers in place (the pack kernels take their mapped addresses) and
+    stage pageable ones: the trajectories and the returned states are the same
+    bit for bit."""
+    torch = pytest.importorskip("torch")
+    from lumol_gb300 import _capi as C
+
+    def go(pinned):
+        systems = replicas()
+        n = sum(s.size for s in systems)
+        batch = Batch(systems, precision="mixed", threads_per_atom=4)
+        batch.md_setup([1.0] * len(systems))
+        batch.md_run(1)
+
+        def alloc(rows):
+            if pinned:
+                return torch.zeros((rows, 3), dtype=torch.float64, pin_memory=True).numpy()
+            return np.zeros((rows, 3))
+
+        pos, vel = alloc(n), alloc(n)
+        eng = batch.engine
+        eng.call("lg_md_get_state_all", C.dptr(pos), C.dptr(vel), None)
+        for k in (1, 3, 40):
+            eng.call("lg_md_set_state_all", C.dptr(pos), C.dptr(vel), None)
+            eng.call("lg_md_run", k)
+            eng.call("lg_md_get_state_all", C.dptr(pos), C.dptr(vel), None)
+        m = systems[3].size
+        p3, v3 = alloc(m), alloc(m)
+        eng.call("lg_md_get_state", 3, C.dptr(p3), C.dptr(v3))
+        p3 += 0.01
+        eng.call("lg_md_set_state", 3, C.dptr(p3), C.dptr(v3))
+        eng.call("lg_md_run", 5)
+        eng.call("lg_md_get_state", 3, C.dptr(p3), C.dptr(v3))
+        out = (pos.copy(), vel.copy(), p3.copy(), v3.copy())
+        eng.close()
+        return out
+
+    a, b = go(True), go(False)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
