@@ -414,6 +414,10 @@ class System:
         self.dihedral_potentials: dict[tuple[str, str, str, str], object] = {}
         self.coulomb = None
         self.step = 0
+        # DegreesOfFreedom (sys/system.rs:18-26): "particles", "molecules" or
+        # ("frozen", n); the device MD integrates every particle
+        self.simulated_degrees_of_freedom = "particles"
+        self.external_temperature: float | None = None
         self._engine: Engine | None = None
         self._positions = None
         self._version = 0
@@ -654,9 +658,50 @@ class System:
         """System::potential_energy (sys/system.rs:263-265)."""
         return self.compute(C.LG_TERM_ALL, C.LG_WANT_ENERGY)[1]
 
-    def virial(self) -> np.ndarray:
-        """System::virial with the atomic definition (sys/compute.rs:198-254)."""
+    def atomic_virial(self) -> np.ndarray:
+        """AtomicVirial::compute (sys/compute.rs:195-254)."""
         return self.compute(C.LG_TERM_ALL, C.LG_WANT_VIRIAL)[2]
+
+    def virial(self) -> np.ndarray:
+        """System::virial / Virial::compute (sys/compute.rs:372-380): the
+        molecular definition when the simulated degrees of freedom are the
+        molecules', else the atomic one."""
+        if self.simulated_degrees_of_freedom == "molecules":
+            return self.molecular_virial()
+        return self.atomic_virial()
+
+    def degrees_of_freedom(self) -> int:
+        """System::degrees_of_freedom (sys/system.rs:249-255)."""
+        dof = self.simulated_degrees_of_freedom
+        if dof == "particles":
+            return 3 * self.size
+        if dof == "molecules":
+            return 3 * len(set(self._mols))
+        return 3 * self.size - int(dof[1])  # ("frozen", n)
+
+    def pressure_at_temperature(self, temperature: float) -> float:
+        """PressureAtTemperature (sys/compute.rs:383-397)."""
+        from .units import K_BOLTZMANN
+        if not temperature >= 0.0:
+            raise ValueError("the temperature must be positive")
+        virial = float(np.trace(self.virial()))
+        return (self.degrees_of_freedom() * K_BOLTZMANN * temperature + virial) / (3.0 * self.volume())
+
+    def pressure(self) -> float:
+        """Pressure (sys/compute.rs:403-410), at the kinetic temperature."""
+        return self.pressure_at_temperature(self.temperature())
+
+    def stress_at_temperature(self, temperature: float) -> np.ndarray:
+        """StressAtTemperature (sys/compute.rs:418-433)."""
+        from .units import K_BOLTZMANN
+        if not temperature >= 0.0:
+            raise ValueError("the temperature must be positive")
+        kinetic = self.degrees_of_freedom() / 3.0 * K_BOLTZMANN * temperature * np.eye(3)
+        return (kinetic + self.virial()) / self.volume()
+
+    def stress(self) -> np.ndarray:
+        """Stress (sys/compute.rs:436-445), at the kinetic temperature."""
+        return self.stress_at_temperature(self.temperature())
 
     def molecular_virial(self, terms: int = C.LG_TERM_ALL) -> np.ndarray:
         """MolecularVirial::compute (sys/compute.rs:278-362): the virial with
@@ -735,9 +780,21 @@ class System:
         v = self.velocities
         return float(sum(0.5 * m * float(np.dot(vi, vi)) for m, vi in zip(self._masses, v)))
 
+    def simulated_temperature(self, temperature: float | None) -> None:
+        """System::simulated_temperature (sys/system.rs): an external
+        temperature that temperature() returns instead of the kinetic one."""
+        if temperature is not None and not temperature >= 0.0:
+            raise ValueError("the temperature must be positive")
+        self.external_temperature = temperature
+
     def temperature(self) -> float:
+        """System::temperature (sys/system.rs:273-278): the external
+        temperature if one is set, else Temperature (sys/compute.rs:165-172),
+        2 K / (dof k_B)."""
         from .units import K_BOLTZMANN
-        return 2.0 * self.kinetic_energy() / (3 * self.size * K_BOLTZMANN)
+        if self.external_temperature is not None:
+            return self.external_temperature
+        return 2.0 * self.kinetic_energy() / (self.degrees_of_freedom() * K_BOLTZMANN)
 
 
 # ---------------------------------------------------------------------------

@@ -15,7 +15,7 @@ import pytest
 import lumol_gb300 as lg
 import oracle
 import systems
-from lumol_gb300 import workloads
+from lumol_gb300 import units, workloads
 
 PAIRS, TAIL, REAL, KSPACE = lg.LG_TERM_PAIRS, lg.LG_TERM_TAIL, lg.LG_TERM_COUL_REAL, lg.LG_TERM_COUL_KSPACE
 TERMS = [PAIRS | TAIL | REAL | KSPACE, PAIRS, TAIL, REAL, KSPACE]
@@ -97,3 +97,44 @@ def test_molecular_virial_needs_fp64():
     s = systems.random_lj_fluid(200, 0.02, 3, 9.0, family="lj", precision="mixed")
     with pytest.raises(lg.EngineError, match="fp64"):
         s.molecular_virial()
+
+
+def pairs_system():
+    """sys/compute.rs tests, test_pairs_system: two F atoms 1.3 A apart in a
+    10 A cell with velocities, a Harmonic pair (300 kJ/mol/A^2, 1.2 A) with
+    tail corrections at 5 A."""
+    s = lg.System(lg.UnitCell.cubic(10.0))
+    s.add_particles(["F", "F"], [[0.0, 0.0, 0.0], [1.3, 0.0, 0.0]])
+    s.velocities = np.array([[-0.007225222699367925, -0.002405756495275919, 0.0026065109398392215],
+                             [0.001179633958023287, 0.003525262341736351, -0.0004132774783154952]])
+    pair = lg.PairInteraction(lg.Harmonic(k=units.from_(300.0, "kJ/mol/A^2"), x0=1.2), 5.0)
+    pair.enable_tail_corrections()
+    s.set_pair_potential(("F", "F"), pair)
+    return s
+
+
+@pytest.mark.gpu
+def test_pressure_and_stress_literals():
+    """sys/compute.rs tests: temperature 300 K, virial -30 kJ/mol/A * 1.3 A in
+    xx, PressureAtTemperature(550 K), Pressure with an external temperature,
+    and the stress whose trace / 3 is the pressure."""
+    from lumol_gb300.units import K_BOLTZMANN
+    s = pairs_system()
+    assert abs(s.temperature() - 300.0) < 1e-12
+    force = units.from_(30.0, "kJ/mol/A")
+    expected = np.zeros((3, 3))
+    expected[0, 0] = -force * 1.3
+    w = s.virial()
+    assert np.abs(w - expected).max() <= 1e-14 * abs(expected[0, 0])
+    p = s.pressure_at_temperature(550.0)
+    assert abs(p - (2.0 * K_BOLTZMANN * 550.0 / 1000.0 + expected[0, 0] / 3000.0)) <= 1e-14 * abs(p)
+    assert s.pressure() == s.pressure_at_temperature(s.temperature())
+    s.simulated_temperature(550.0)
+    assert s.pressure() == p
+    stress = s.stress_at_temperature(550.0)
+    assert abs(np.trace(stress) / 3.0 - p) <= 1e-14 * abs(p)
+    with pytest.raises(ValueError):
+        s.pressure_at_temperature(-4.0)
+    # molecules as the degrees of freedom: the molecular definition (one-atom molecules: the same)
+    s.simulated_degrees_of_freedom = "molecules"
+    assert np.abs(s.virial() - w).max() <= 1e-14 * abs(expected[0, 0])
