@@ -378,17 +378,18 @@ def _dihedrals_from_bonds(bonds: list[tuple[int, int]]) -> list[tuple[int, int, 
     holds the smaller largest index first)."""
     def make(a, b, c, d):
         return (a, b, c, d) if max(a, b) < max(c, d) else (d, c, b, a)
+    partners: dict[int, list[int]] = {}
+    for a, b in bonds:
+        partners.setdefault(a, []).append(b)
+        partners.setdefault(b, []).append(a)
     out = set()
     for i, j, k in _angles_from_bonds(bonds):
-        for p, q in bonds:
-            if k == p and j != q:
+        for q in partners.get(k, ()):  # a bond (k, q) other than (j, k)
+            if q != j:
                 out.add(make(i, j, k, q))
-            elif k == q and j != p:
-                out.add(make(i, j, k, p))
-            elif i == q and j != p:
+        for p in partners.get(i, ()):  # a bond (p, i) other than (i, j) and, in a 3-ring, (i, k)
+            if p != j and p != k:
                 out.add(make(p, i, j, k))
-            elif i == p and j != q:
-                out.add(make(q, i, j, k))
     return sorted(out)
 
 
