@@ -68,6 +68,18 @@ def test_reference_bad_interaction_files():
         assert err.value.reason == _message(case), name
 
 
+@needs_reference
+def test_reference_bench_interaction_files():
+    """The interactions files of the reference's benches (benches/data/*.toml:
+    argon, NaCl, water, propane) read without error."""
+    files = sorted(glob.glob(refdata.path("benches", "data", "*.toml")))
+    assert len(files) >= 4
+    for path in files:
+        s = empty_system()
+        lg.InteractionsInput.new(path).read(s)
+        assert s.pairs, path
+
+
 def test_unit_strings():
     # units.rs tests: "10 A", kJ/mol, powers and parentheses
     assert units.from_str("10 A") == 10.0
