@@ -918,6 +918,10 @@ class MolecularDynamics:
     def setup(self, system: System) -> None:
         """Propagator::setup: the integrator's setup (accelerations := 0, or
         Verlet's positions at t - dt) at the first run."""
+        # Simulation::run (lumol-sim/src/simulations.rs:70-86): MD takes the
+        # temperature from the velocities and moves every particle
+        system.simulated_temperature(None)
+        system.simulated_degrees_of_freedom = "particles"
         eng = system.engine()
         p = md_params(self.integrator, self.thermostat, self.controls)
         eng.call("lg_md_setup_ex", 0, ctypes.byref(p))
@@ -962,6 +966,7 @@ class MonteCarlo:
 
     def __init__(self, temperature: float, move: Translate, seed: int = 0):
         from .units import K_BOLTZMANN
+        self.temperature = float(temperature)
         self.beta = 1.0 / (K_BOLTZMANN * temperature)
         self.move = move
         self.rng = np.random.default_rng(seed)
@@ -970,6 +975,11 @@ class MonteCarlo:
         self.energy = None
 
     def setup(self, system: System) -> None:
+        # Simulation::run (lumol-sim/src/simulations.rs:70-86) with MonteCarlo's
+        # temperature strategy and degrees of freedom (mc/monte_carlo.rs:243-279):
+        # the external temperature, and rigid molecules for Translate
+        system.simulated_temperature(self.temperature)
+        system.simulated_degrees_of_freedom = "molecules"
         self.energy = system.mc_init()
 
     def propagate(self, system: System) -> None:
