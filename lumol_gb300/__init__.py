@@ -32,6 +32,7 @@ from .system import (
     RemoveTranslation,
     RescaleThermostat,
     Rewrap,
+    Rotate,
     System,
     TableComputation,
     Torsion,
@@ -58,7 +59,7 @@ __all__ = [
     "units", "EngineError", "InputError", "InteractionsInput", "read_interactions", "BerendsenThermostat", "BornMayerHuggins", "Buckingham", "CSVRThermostat", "Engine",
     "Ewald", "Gaussian", "Harmonic", "LeapFrog", "LennardJones", "Mie", "MolecularDynamics", "MonteCarlo", "Morse",
     "Translate", "NullPotential", "PairInteraction", "PairRestriction", "RemoveRotation", "RemoveTranslation", "RescaleThermostat",
-    "Rewrap", "System", "TableComputation", "Torsion", "CosineHarmonic", "UnitCell", "VelocityVerlet", "Verlet", "Wolf", "md_params",
+    "Rewrap", "Rotate", "System", "TableComputation", "Torsion", "CosineHarmonic", "UnitCell", "VelocityVerlet", "Verlet", "Wolf", "md_params",
     "LG_TERM_ALL", "LG_TERM_ANGLES", "LG_TERM_BONDS", "LG_TERM_COUL_KSPACE", "LG_TERM_COUL_REAL",
     "LG_TERM_COUL_SELF", "LG_TERM_DIHEDRALS", "LG_TERM_PAIRS", "LG_TERM_TAIL",
 ]

@@ -959,16 +959,49 @@ class Translate:
         self.delta = delta / np.sqrt(3.0)
 
 
+class Rotate:
+    """Rotate move (mc/moves/rotate.rs:24-125): one random molecule rotated
+    about its centre of mass by an angle uniform in [-theta, theta) around an
+    axis uniform on the unit sphere (Matrix3::rotation, types/matrix.rs:149-176)."""
+
+    def __init__(self, theta: float):
+        if not theta > 0.0:
+            raise ValueError("theta must be positive in Rotate move")
+        self.theta = float(theta)
+
+
+def _rotation(axis: np.ndarray, angle: float) -> np.ndarray:
+    """Matrix3::rotation (types/matrix.rs:149-169) around `axis` (normalised):
+    the matrix with the reference's sign convention, which turns e3 into e2
+    for a quarter turn around e1."""
+    n = axis / np.sqrt(axis @ axis)
+    c, s_ = np.cos(angle), np.sin(angle)
+    t = 1.0 - c
+    xs, ys, zs = n * s_
+    xy, xz, yz = n[0] * n[1] * t, n[0] * n[2] * t, n[1] * n[2] * t
+    return np.array([[n[0] * n[0] * t + c, xy + zs, xz - ys],
+                     [xy - zs, n[1] * n[1] * t + c, yz + xs],
+                     [xz + ys, yz - xs, n[2] * n[2] * t + c]])
+
+
 class MonteCarlo:
-    """Metropolis propagator (mc/monte_carlo.rs:289-329) with Translate moves;
-    the move costs run on the GPU.  The random stream is numpy's, seeded (the
+    """Metropolis propagator (mc/monte_carlo.rs:289-329) with Translate and
+    Rotate moves, each picked with its frequency (MonteCarlo::add); the move
+    costs run on the GPU.  The random stream is numpy's, seeded (the
     reference's xorshift stream is not reproduced)."""
 
-    def __init__(self, temperature: float, move: Translate, seed: int = 0):
+    def __init__(self, temperature: float, move, seed: int = 0):
+        """`move`: a Translate or Rotate, or a list of (move, frequency)."""
         from .units import K_BOLTZMANN
         self.temperature = float(temperature)
         self.beta = 1.0 / (K_BOLTZMANN * temperature)
-        self.move = move
+        moves = [(move, 1.0)] if isinstance(move, (Translate, Rotate)) else [(m, float(f)) for m, f in move]
+        if not moves or any(not f > 0.0 for _, f in moves):
+            raise ValueError("MonteCarlo needs moves with positive frequencies")
+        self.moves = [m for m, _ in moves]
+        freq = np.array([f for _, f in moves])
+        self.frequencies = freq / freq.sum()
+        self.move = self.moves[0]
         self.rng = np.random.default_rng(seed)
         self.accepted = 0
         self.attempted = 0
@@ -986,8 +1019,18 @@ class MonteCarlo:
         nmol = int(system.molecules[-1]) + 1
         molid = int(self.rng.integers(nmol))
         lo, hi = system.molecule_range(molid)
-        delta = self.rng.uniform(-self.move.delta, self.move.delta, size=3)
-        newpos = system.positions[lo:hi] + delta
+        move = self.moves[int(self.rng.choice(len(self.moves), p=self.frequencies))] if len(self.moves) > 1 \
+            else self.moves[0]
+        if isinstance(move, Rotate):
+            pos = system.positions[lo:hi]
+            m = system.masses[lo:hi, None]
+            com = (m * pos).sum(axis=0) / m.sum()
+            axis = self.rng.normal(size=3)
+            rot = _rotation(axis, self.rng.uniform(-move.theta, move.theta))
+            newpos = com + (pos - com) @ rot.T
+        else:
+            delta = self.rng.uniform(-move.delta, move.delta, size=3)
+            newpos = system.positions[lo:hi] + delta
         cost = self.beta * system.move_molecule_cost(molid, newpos)
         self.attempted += 1
         if cost <= 0.0 or self.rng.random() < np.exp(-cost):

@@ -47,6 +47,31 @@ def test_cached_energy_equals_fresh_energy_after_many_moves():
     assert abs(mc.energy - fresh) <= 1e-9 * abs(fresh)
 
 
+def test_rotate_and_translate_moves_on_water():
+    """Rotate (mc/moves/rotate.rs) with Translate on rigid water with Ewald:
+    rotations keep every molecule's geometry, some of each kind are accepted,
+    and the cached energy equals a fresh evaluation after 300 moves."""
+    s = workloads.water_box(n_side=4, length=14.0, seed=2, cutoff=6.5, alpha=0.45, kmax=6)
+    s.set_bond_potential(("H", "O"), lg.NullPotential())
+    s.set_angle_potential(("H", "O", "H"), lg.NullPotential())
+    mc = lg.MonteCarlo(300.0, [(lg.Translate(0.3), 1.0), (lg.Rotate(0.6), 1.0)], seed=4)
+    mc.setup(s)
+    assert s.simulated_degrees_of_freedom == "molecules" and s.temperature() == 300.0
+
+    def geometry(x):
+        x = x.reshape(-1, 3, 3)
+        return np.stack([np.linalg.norm(x[:, 1] - x[:, 0], axis=1), np.linalg.norm(x[:, 2] - x[:, 0], axis=1),
+                         np.linalg.norm(x[:, 2] - x[:, 1], axis=1)])
+
+    g0 = geometry(s.positions)
+    for _ in range(300):
+        mc.propagate(s)
+    assert mc.accepted > 0 and mc.accepted < mc.attempted
+    assert np.abs(geometry(s.positions) - g0).max() < 1e-12
+    fresh = s.potential_energy()
+    assert abs(mc.energy - fresh) <= 1e-9 * abs(fresh)
+
+
 def test_update_without_cost_is_an_error():
     s = workloads.nacl_crystal(cells=3, cutoff=8.0, kmax=5)
     s.mc_init()

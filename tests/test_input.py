@@ -263,3 +263,11 @@ def test_interactions_from_toml_match_oracle():
     assert isinstance(s.bond_potentials[("C", "C")], lg.Morse)
     assert isinstance(s.dihedral_potential(("N", "C", "O", "C")), lg.Morse)
     assert_parity(s)
+
+
+def test_rotation_matrix_literal():
+    """types/matrix.rs:136-148: a quarter turn around 2 e1 takes e3 to e2."""
+    from lumol_gb300.system import _rotation
+    r = _rotation(np.array([2.0, 0.0, 0.0]), np.radians(90.0))
+    assert np.array_equal(np.round(r @ [0.0, 0.0, 1.0] * 1e8) / 1e8, [0.0, 1.0, 0.0])
+    assert np.allclose(r @ r.T, np.eye(3), atol=1e-15)
