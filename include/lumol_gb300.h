@@ -379,7 +379,8 @@ int lg_fma_peak(int32_t fp64, double* tflops);
  * cudaStream_t (NULL: the default stream).  Calls share the scratch array:
  * calls whose work overlaps on the GPU race.  The first call on a device sets
  * the scratch address up for that device and should come before any stream
- * capture. */
+ * capture.  The address it keeps belongs to the device's primary context, so
+ * the entry point must not be used again after cudaDeviceReset. */
 #define LG_NOALLOC_MAX_ATOMS 4096
 #define LG_NOALLOC_MAX_KMAX 8
 int lg_ewald_kspace_noalloc(const double* d_positions, const double* d_charges, int64_t n,

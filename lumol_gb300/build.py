@@ -15,7 +15,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liblumol_gb300.so")
-SOURCES = ["nlist.cu", "forces.cu", "mixed.cu", "persist.cu", "md.cu", "diag.cu", "mc.cu", "noalloc.cu", "capi.cu"]
+SOURCES = ["nlist.cu", "forces.cu", "mixed.cu", "persist.cu", "md.cu", "diag.cu", "mc.cu", "noalloc.cu",
+           "lower.cu", "runtime.cu", "capi.cu", "capi_mc.cu"]
 
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",

@@ -1,0 +1,219 @@
+// capi_mc.cu -- the Monte Carlo entry points of include/lumol_gb300.h: the
+// EnergyCache move cost / update of one molecule, and the batched device
+// Metropolis chains.
+#include "engine.h"
+
+extern "C" {
+
+int lg_mc_init(lg_engine* e, int32_t s, const double* positions, double* energy) {
+    if (!valid_sys(e, s) || !positions) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    int rc = commit(e);
+    if (rc) return rc;
+    cudaStream_t st = e->stream;
+    rc = upload_positions(e, s, positions);
+    if (rc) return rc;
+    rc = compute_batch(e, LG_TERM_ALL, LG_WANT_ENERGY, nullptr, nullptr);
+    if (rc) return rc;
+    // FP64 e^{ik.r} and rho(k) at these positions: the state the move costs update
+    Batch fb = e->b;
+    fb.precision = LG_PRECISION_FP64;
+    launch_kspace_part(fb, 0, false, st);
+    launch_kspace_part(fb, 1, false, st);
+    CUDA_TRY(e, cudaMemcpyAsync(e->h_out, e->out.p + (size_t)s * RED_STRIDE, sizeof(double), cudaMemcpyDeviceToHost,
+                                st));
+    CUDA_TRY(e, cudaStreamSynchronize(st));
+    CUDA_TRY(e, cudaGetLastError());
+    e->mc_energy = e->h_out[0];
+    e->mc_sys = s;
+    e->mc_pending = false;
+    if (energy) *energy = e->mc_energy;
+    return LG_OK;
+}
+
+int lg_mc_move_molecule_cost(lg_engine* e, int32_t s, int64_t molecule, const double* new_positions, double* cost) {
+    if (!valid_sys(e, s) || !new_positions || !cost) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    if (e->dirty || e->mc_sys != s) return fail(e, LG_ERR_STATE, "lg_mc_init was not called for this system");
+    const HostSystem& h = e->sys[s];
+    if (molecule < 0 || molecule + 1 >= (int64_t)h.mol_begin.size())
+        return fail(e, LG_ERR_ARGUMENT, "molecule index out of range");
+    CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    int64_t mb = h.mol_begin[molecule], me = h.mol_begin[molecule + 1];
+    int msize = (int)(me - mb);
+    const SysDev& sd = e->h_sysdev[s];
+    cudaStream_t st = e->stream;
+    size_t need_pos = (size_t)std::max(msize, 1) * 3;
+    if (e->mc_newpos.n < need_pos) CUDA_TRY(e, e->mc_newpos.alloc(need_pos));
+    int nblocks = (int)((h.n + 255) / 256);
+    if (e->mc_partial.n < (size_t)std::max(2 * nblocks, 2)) CUDA_TRY(e, e->mc_partial.alloc(std::max(2 * nblocks, 2)));
+    int nk = sd.coul == LG_COULOMB_EWALD ? sd.kend - sd.kbegin : 0;
+    if (e->mc_dk.n < (size_t)std::max(nk, 1)) CUDA_TRY(e, e->mc_dk.alloc(std::max(nk, 1)));
+    if (e->mc_drho.n < (size_t)std::max(nk, 1)) CUDA_TRY(e, e->mc_drho.alloc(std::max(nk, 1)));
+    size_t need_eikr = (size_t)(sd.kmax + 1) * 3 * std::max(msize, 1);
+    if (e->mc_eikr.n < need_eikr) CUDA_TRY(e, e->mc_eikr.alloc(need_eikr));
+    if (e->mc_out.n < 3) CUDA_TRY(e, e->mc_out.alloc(3));
+    CUDA_TRY(e, cudaMemcpyAsync(e->mc_newpos.p, new_positions, 3 * msize * sizeof(double), cudaMemcpyHostToDevice,
+                                st));
+    launch_mc_cost(e->b, s, sd, (int)(e->begin[s] + mb), msize, e->mc_newpos.p, e->mc_eikr.p, e->mc_drho.p,
+                   e->mc_partial.p, e->mc_dk.p, e->mc_out.p, st);
+    e->launches += 2 + (nk > 0 ? 2 : 0);
+    double out[3];
+    CUDA_TRY(e, cudaMemcpyAsync(out, e->mc_out.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(e, cudaStreamSynchronize(st));
+    CUDA_TRY(e, cudaGetLastError());
+    e->mc_pending_cost = out[0] + out[1] + out[2];
+    e->mc_pending = true;
+    e->mc_mol_begin = e->begin[s] + mb;
+    e->mc_mol_size = msize;
+    *cost = e->mc_pending_cost;
+    return LG_OK;
+}
+
+int lg_mc_update(lg_engine* e, int32_t s, const double* molecule_positions, double* energy) {
+    if (!valid_sys(e, s) || !molecule_positions) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    if (!e->mc_pending || e->mc_sys != s)
+        return fail(e, LG_ERR_STATE, "called EnergyCache::update without call a `*_cost` function first");
+    CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    cudaStream_t st = e->stream;
+    int msize = (int)e->mc_mol_size;
+    const SysDev& sd = e->h_sysdev[s];
+    CUDA_TRY(e, cudaMemcpyAsync(e->mc_newpos.p, molecule_positions, 3 * msize * sizeof(double),
+                                cudaMemcpyHostToDevice, st));
+    const double* d_k1 = (const double*)((const char*)(e->sysdev.p + s) + offsetof(SysDev, k1));
+    launch_mc_accept(e->b, sd, (int)e->mc_mol_begin, msize, e->mc_newpos.p, d_k1, e->mc_drho.p, st);
+    e->launches += 2;
+    CUDA_TRY(e, cudaStreamSynchronize(st));
+    CUDA_TRY(e, cudaGetLastError());
+    e->mc_energy += e->mc_pending_cost;
+    e->mc_pending = false;
+    if (energy) *energy = e->mc_energy;
+    return LG_OK;
+}
+
+int lg_mc_setup(lg_engine* e, int32_t s, double temperature, double delta, uint64_t seed) {
+    if (!valid_sys(e, s)) return fail(e, LG_ERR_ARGUMENT, "invalid system index");
+    // MonteCarlo::new (mc/monte_carlo.rs) and Translate::new (translate.rs:41-52)
+    if (!(temperature > 0.0)) return fail(e, LG_ERR_ARGUMENT, "the temperature must be positive in Monte Carlo");
+    if (!(delta > 0.0)) return fail(e, LG_ERR_ARGUMENT, "delta must be positive in Translate move");
+    const HostSystem& h = e->sys[s];
+    if (h.coul.kind != LG_COULOMB_NONE)
+        return fail(e, LG_ERR_ARGUMENT,
+                    "batched Monte Carlo chains evaluate pair potentials only; use lg_mc_move_molecule_cost "
+                    "for systems with Coulomb interactions");
+    for (size_t i = 1; i < h.mols.size(); i++)
+        if (h.mols[i] == h.mols[i - 1])
+            return fail(e, LG_ERR_ARGUMENT, "batched Monte Carlo chains move single-particle molecules only");
+    double half = delta / std::sqrt(3.0);
+    if (std::sqrt(3.0) * half > 0.5 * e->skin)
+        return fail(e, LG_ERR_ARGUMENT, "the Translate amplitude must not exceed half the neighbour-list skin");
+    if (e->h_mc.size() != (size_t)e->nsys) e->h_mc.assign(e->nsys, McState{});
+    McState& m = e->h_mc[s];
+    m.beta = 1.0 / (K_BOLTZMANN * temperature);
+    m.delta = half;
+    m.rng = seed * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull;
+    m.enabled = 1;
+    m.moves_left = 0;
+    m.need_rebuild = 0;
+    m.accepted = m.attempted = 0;
+    if (!e->dirty) {
+        CUDA_TRY(e, cudaSetDevice(e->opt.device));
+        CUDA_TRY(e, cudaMemcpy(e->mc_chains.p + s, &m, sizeof(McState), cudaMemcpyHostToDevice));
+    }
+    return LG_OK;
+}
+
+int lg_mc_run(lg_engine* e, int64_t moves) {
+    if (!e || moves < 0) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    if (e->dirty) return fail(e, LG_ERR_STATE, "no device state: call lg_md_set_state first");
+    CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    cudaStream_t st = e->stream;
+    int nsys = e->nsys;
+    CUDA_TRY(e, cudaMemcpy(e->h_mc.data(), e->mc_chains.p, nsys * sizeof(McState), cudaMemcpyDeviceToHost));
+    if (!e->mc_energies_ready) {
+        // EnergyCache::init: the chains start from the full energy of every system
+        int rc = compute_batch(e, LG_TERM_ALL, LG_WANT_ENERGY, nullptr, nullptr);
+        if (rc) return rc;
+        std::vector<double> out((size_t)nsys * RED_STRIDE);
+        CUDA_TRY(e, cudaMemcpy(out.data(), e->out.p, out.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        for (int s = 0; s < nsys; s++) e->h_mc[s].energy = out[(size_t)s * RED_STRIDE];
+        e->mc_energies_ready = true;
+    }
+    bool any = false;
+    bool fp64 = e->opt.precision == LG_PRECISION_FP64;
+    for (int s = 0; s < nsys; s++)
+        if (e->h_mc[s].enabled) {
+            e->h_mc[s].moves_left = moves;
+            e->h_mc[s].need_rebuild = 0;
+            any = true;
+        }
+    if (!any) return fail(e, LG_ERR_STATE, "lg_mc_setup was not called for any system");
+    CUDA_TRY(e, cudaMemcpyAsync(e->mc_chains.p, e->h_mc.data(), nsys * sizeof(McState), cudaMemcpyHostToDevice, st));
+    // the list must be current for the positions the chains start from, and so
+    // must the fixed-point copies the mixed chains read
+    launch_check_displacement(e->b, st);
+    launch_nlist_build(e->b, st);
+    e->launches += 1 + nlist_launches(e->b);
+    if (!fp64) {
+        launch_split_positions(e->b, st);
+        e->launches += 1;
+    }
+    for (int64_t launch = 0; launch < moves + 64; launch++) {
+        launch_mc_chains(e->b, e->mc_chains.p, fp64, st);
+        e->launches += 1;
+        CUDA_TRY(e, cudaMemcpyAsync(e->h_mc.data(), e->mc_chains.p, nsys * sizeof(McState), cudaMemcpyDeviceToHost,
+                                    st));
+        CUDA_TRY(e, cudaStreamSynchronize(st));
+        CUDA_TRY(e, cudaGetLastError());
+        bool rebuild = false, pending = false;
+        for (int s = 0; s < nsys; s++) {
+            if (!e->h_mc[s].enabled) continue;
+            rebuild = rebuild || e->h_mc[s].need_rebuild;
+            pending = pending || e->h_mc[s].moves_left > 0;
+        }
+        if (!pending) return LG_OK;
+        if (rebuild) {
+            // rebuild the lists of the stopped chains' systems only
+            std::vector<uint32_t> flags(nsys, 0u);
+            for (int s = 0; s < nsys; s++) {
+                flags[s] = e->h_mc[s].need_rebuild ? 1u : 0u;
+                e->h_mc[s].need_rebuild = 0;
+            }
+            CUDA_TRY(e, cudaMemcpyAsync(e->mc_chains.p, e->h_mc.data(), nsys * sizeof(McState),
+                                        cudaMemcpyHostToDevice, st));
+            CUDA_TRY(e, cudaMemcpyAsync(e->sys_rebuild.p, flags.data(), nsys * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                        st));
+            uint32_t rebuild_bit = ST_REBUILD;
+            CUDA_TRY(e, cudaMemcpyAsync(e->h_status, e->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+            CUDA_TRY(e, cudaStreamSynchronize(st));
+            *e->h_status |= rebuild_bit;
+            CUDA_TRY(e, cudaMemcpyAsync(e->status.p, e->h_status, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+            launch_nlist_build(e->b, st);
+            e->launches += nlist_launches(e->b);
+            uint32_t status;
+            int rc = read_status(e, &status);
+            if (rc) return rc;
+            if (status & ST_OVERFLOW) {
+                rc = clear_status_bits(e, ST_OVERFLOW);
+                if (rc) return rc;
+                rc = regrow(e);
+                if (rc) return rc;
+                launch_nlist_build(e->b, st);
+            }
+        }
+    }
+    return fail(e, LG_ERR_STATE, "Monte Carlo chains did not finish");
+}
+
+int lg_mc_stats(lg_engine* e, int32_t s, double* energy, int64_t* accepted, int64_t* attempted) {
+    if (!valid_sys(e, s)) return fail(e, LG_ERR_ARGUMENT, "invalid system index");
+    if (e->dirty) return fail(e, LG_ERR_STATE, "no device state");
+    CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    McState m;
+    CUDA_TRY(e, cudaMemcpy(&m, e->mc_chains.p + s, sizeof(McState), cudaMemcpyDeviceToHost));
+    if (energy) *energy = m.energy;
+    if (accepted) *accepted = m.accepted;
+    if (attempted) *attempted = m.attempted;
+    return LG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,252 @@
+// engine.h -- the engine object behind the C ABI of include/lumol_gb300.h,
+// shared by the host translation units of the engine:
+//
+//   lower.cu    the description of every system (particles, topology, pair
+//               table, Coulomb potential, cell) lowered into the flat device
+//               layout of kernels.h, and the host restatements of the
+//               reference's scalar arithmetic that feed it;
+//   runtime.cu  status words, list regrowth, force passes, state transfers,
+//               the autotuner, MD step graphs and the persistent-kernel plan;
+//   capi.cu     the C entry points of description, forces, MD, diagnostics;
+//   capi_mc.cu  the C entry points of Monte Carlo.
+//
+// Host arithmetic that feeds results (potential shifts, Ewald k-vector
+// factors, tail corrections, self energy) restates the reference operation by
+// operation; these files are compiled with -ffp-contract=off so the host
+// compiler does not fuse it either.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstddef>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <string>
+#include <vector>
+
+#include "../../include/lumol_gb300.h"
+#include "kernels.h"
+
+namespace lg {
+
+constexpr int MIN_KCHUNK = 8;
+
+// Message of the last failed call that has no engine (lg_create, the
+// allocation-free entry point), per thread.
+extern thread_local std::string g_create_error;
+
+// Tuned launch parameters per workload shape: (device, precision, atoms,
+// list capacity, k-vectors, persistent batch) -> (threads per atom,
+// k-vectors per field chunk).
+extern std::mutex g_tune_mutex;
+extern std::map<std::tuple<int, int, int, int, int, bool>, std::pair<int, int>> g_tune_cache;
+
+template <class T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    ~DBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    cudaError_t alloc(size_t count) {
+        release();
+        if (count == 0) count = 1;
+        cudaError_t e = cudaMalloc((void**)&p, count * sizeof(T));
+        if (e == cudaSuccess) n = count;
+        return e;
+    }
+};
+
+static_assert(MD_VELOCITY_VERLET == LG_INTEGRATOR_VELOCITY_VERLET && MD_VERLET == LG_INTEGRATOR_VERLET &&
+                  MD_LEAP_FROG == LG_INTEGRATOR_LEAP_FROG,
+              "integrator values");
+static_assert(TH_NONE == LG_THERMOSTAT_NONE && TH_BERENDSEN == LG_THERMOSTAT_BERENDSEN &&
+                  TH_RESCALE == LG_THERMOSTAT_RESCALE && TH_CSVR == LG_THERMOSTAT_CSVR,
+              "thermostat values");
+static_assert(CTL_REMOVE_TRANSLATION == LG_CONTROL_REMOVE_TRANSLATION && CTL_REWRAP == LG_CONTROL_REWRAP &&
+                  CTL_REMOVE_ROTATION == LG_CONTROL_REMOVE_ROTATION,
+              "control values");
+
+struct HostSystem {
+    bool has_cell = false;
+    double L[3] = {0, 0, 0};
+    int64_t n = 0;
+    std::vector<int32_t> kinds, mols;
+    std::vector<double> charges, masses;
+    std::vector<int32_t> bonds;
+    std::vector<lg_bonded> bond_pots;
+    std::vector<int32_t> angles;
+    std::vector<lg_bonded> angle_pots;
+    std::vector<int32_t> dihedrals;
+    std::vector<lg_bonded> dihedral_pots;
+    int32_t nk = 0;
+    std::vector<lg_pair> pairs;
+    lg_coulomb coul{};
+    // molecular dynamics
+    double dt = 0.0, T0 = 0.0, tau = 0.0, tol = 0.0;
+    int32_t integrator = LG_INTEGRATOR_VELOCITY_VERLET, thermostat = LG_THERMOSTAT_NONE;
+    uint32_t controls = 0;
+    uint64_t seed = 0;
+    bool md_ready = false;
+    bool verlet_setup = false;  // Verlet::setup runs at the next lg_md_run
+    // derived
+    std::vector<int64_t> mol_begin;  // first atom of each molecule (local index), plus the end
+    double tail_energy = 0.0, tail_virial = 0.0, ewald_self = 0.0;
+    double alpha = 0.0;
+};
+
+}  // namespace lg
+
+using namespace lg;
+
+struct lg_engine {
+    lg_options opt{};
+    int nsys = 0;
+    std::vector<HostSystem> sys;
+    std::string err;
+    cudaStream_t stream = nullptr;
+    bool dirty = true;
+    std::vector<int64_t> begin;  // atom offsets (nsys + 1)
+    double skin = 1.0;
+
+    Batch b;
+    // device storage
+    DBuf<double4_32a> posq, vel, acc, pos_build;
+    DBuf<double> force, pos3, vel3, red, host_const, kepart, mom, out, fpart, kred, mc_part;
+    DBuf<unsigned long long> md_count, cp_count;
+    DBuf<double> adj;
+    DBuf<int> mol_start;
+    DBuf<int2> tiles;
+    DBuf<double4_32a> cp_pos, cp_vel, cp_acc;  // MD checkpoint: a chunk whose list overflowed is replayed
+    DBuf<int> kind, mol, sysid, spec_off, spec_j, bt_off, bt_role, nbr, nnb, atom_cell, cell_count, cell_start,
+        cell_atoms, plan, perm;
+    DBuf<int2> km;
+    DBuf<int8_t> spec_path;
+    DBuf<int4> bt;
+    DBuf<double4_32a> bt_par;
+    DBuf<double2> eikr, rho;
+    DBuf<float4> wpos;
+    DBuf<uint4> posfx, pfx_build;
+    DBuf<float> inv_mass;
+    DBuf<int> nlo, rev;
+    DBuf<double4_32a> pf;
+    DBuf<double4_32a> molcom;  // per-atom centre of mass of its molecule (molecular virial)
+    DBuf<PairDevF> ptabf;
+    DBuf<double2> table;  // TableComputation tables (plain path)
+    DBuf<float2> tablef;  // the same in FP32 (mixed path)
+    DBuf<KVecF> kvecf;
+    DBuf<float2> eikrf, rhof;
+    DBuf<SysDev> sysdev;
+    DBuf<PairDev> ptab;
+    DBuf<KVecDev> kvec;
+    DBuf<uint32_t> status, sys_rebuild;
+    DBuf<int> pairs_out;
+    DBuf<unsigned long long> pairs_count;
+    uint32_t* h_status = nullptr;  // pinned
+    double* h_out = nullptr;       // pinned, nsys * RED_STRIDE
+    std::vector<SysDev> h_sysdev;
+    std::vector<int> h_kvec_sys;
+
+    bool tuned = false;
+    int max_nk = 0;
+    // kernels launched so far (graph replays counted by their kernel nodes)
+    uint64_t launches = 0;
+    size_t graph_kernels = 0;
+
+    // persistent batched MD (mixed batches of pair-potential systems)
+    int pk_cluster = 0;  // cluster size of the plan; 0: not planned, -1: not eligible
+    int pk_groups = 0;
+    int pk_stage = 0;    // atoms each block stages in shared memory (0: gathers from global memory)
+    DBuf<int> pk_group_off, pk_group_sys, pk_group_flag;
+    DBuf<double> pk_ke;
+    // one graph per (steps, thermostat): checkpoint copies, flag reset, the launch
+    // (a graph replay avoids the per-launch cost of a cluster launch)
+    std::map<int, cudaGraphExec_t> pk_graphs;
+
+    // MD graphs, one per chunk length
+    std::map<int, cudaGraphExec_t> graphs;
+    std::map<int, size_t> graph_nodes;
+    int graph_mode = -1;  // md_mode() of the captured graphs
+
+    // batched Monte Carlo chains
+    DBuf<McState> mc_chains;
+    std::vector<McState> h_mc;
+    bool mc_energies_ready = false;
+
+    // MC (single molecule moves)
+    DBuf<double> mc_newpos, mc_partial, mc_dk, mc_out;
+    DBuf<double2> mc_eikr, mc_drho;
+    double mc_energy = 0.0;
+    double mc_pending_cost = 0.0;
+    bool mc_pending = false;
+    int mc_sys = -1;
+    int64_t mc_mol_begin = 0, mc_mol_size = 0;
+
+    void drop_graphs() {
+        for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+        graphs.clear();
+        graph_nodes.clear();
+        for (auto& g : pk_graphs) cudaGraphExecDestroy(g.second);
+        pk_graphs.clear();
+    }
+
+    ~lg_engine() {
+        drop_graphs();
+        if (h_status) cudaFreeHost(h_status);
+        if (h_out) cudaFreeHost(h_out);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace lg {
+
+int fail(lg_engine* e, int code, const std::string& msg);
+
+#define CUDA_TRY(e, call)                                                                          \
+    do {                                                                                           \
+        cudaError_t _err = (call);                                                                 \
+        if (_err != cudaSuccess)                                                                   \
+            return fail((e), LG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_err)); \
+    } while (0)
+
+bool valid_sys(lg_engine* e, int32_t s);
+void invalidate(lg_engine* e);
+
+// ---- lower.cu -------------------------------------------------------------------
+void fill_md(SysDev& d, const HostSystem& h);
+double max_cutoff(const HostSystem& h);
+int check_pair_cutoffs(lg_engine* e, const HostSystem& h);
+// Lowers the description into device memory when it changed (e->dirty).
+int commit(lg_engine* e);
+
+// ---- runtime.cu -----------------------------------------------------------------
+int regrow(lg_engine* e);
+int read_status(lg_engine* e, uint32_t* out);
+int clear_status_bits(lg_engine* e, uint32_t bits);
+int nlist_launches(const Batch& b);
+void enqueue_forces(lg_engine* e, uint32_t terms, bool ev, cudaStream_t st, bool fixed_written = false);
+int compute_batch(lg_engine* e, uint32_t terms, uint32_t want, double* d_force_out, double* d_out);
+const void* mapped_host(const void* p);
+int put_state(lg_engine* e, int64_t base, int64_t n, const double* positions, const double* velocities);
+int get_state(lg_engine* e, int64_t base, int64_t n, double* positions, double* velocities);
+int upload_positions(lg_engine* e, int32_t s, const double* positions);
+int autotune(lg_engine* e);
+// What the MD steps of a batch need besides the integrators (md_mode bits).
+constexpr int MD_ADJUST = 1, MD_REWRAP = 2, MD_VERLET_SYS = 4;
+int md_mode(const lg_engine* e);
+void enqueue_md_step(lg_engine* e, int mode, bool apply_previous, cudaStream_t st);
+void enqueue_md_finish(lg_engine* e, int mode, cudaStream_t st);
+bool persist_batch(const lg_engine* e);
+bool persist_eligible(const lg_engine* e);
+int persist_plan(lg_engine* e);
+int md_run_persistent(lg_engine* e, int64_t nsteps, bool thermo);
+int build_md_graph(lg_engine* e, int steps, int mode);
+
+}  // namespace lg

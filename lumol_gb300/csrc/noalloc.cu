@@ -18,8 +18,11 @@
 // previous call leaks into the next one.
 //
 // The first call on a device looks up the device address of the array
-// (cudaGetSymbolAddress) with that device current; make that first call
-// before any stream capture.
+// (cudaGetSymbolAddress) with that device current and keeps it for the life
+// of the process; make that first call before any stream capture.  The
+// address belongs to the device's primary context: after cudaDeviceReset (or
+// anything else that destroys and re-creates the primary context) the array
+// can move, so the entry point must not be called again in that process.
 #include <algorithm>
 #include <mutex>
 #include <string>

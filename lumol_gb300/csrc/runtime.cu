@@ -1,0 +1,527 @@
+// runtime.cu -- what the engine does with a lowered batch: status words,
+// list regrowth, force passes, host <-> device state transfers, the
+// autotuner, MD step graphs, and the persistent-kernel plan and launches.
+#include "engine.h"
+
+namespace lg {
+
+thread_local std::string g_create_error;
+std::mutex g_tune_mutex;
+std::map<std::tuple<int, int, int, int, int, bool>, std::pair<int, int>> g_tune_cache;
+
+void set_global_error(const std::string& msg) { g_create_error = msg; }
+
+int fail(lg_engine* e, int code, const std::string& msg) {
+    if (e) e->err = msg;
+    else g_create_error = msg;
+    return code;
+}
+
+bool valid_sys(lg_engine* e, int32_t s) { return e && s >= 0 && s < e->nsys; }
+
+void invalidate(lg_engine* e) {
+    e->dirty = true;
+    e->drop_graphs();
+}
+
+// Regrows the neighbour list after an overflow.
+int regrow(lg_engine* e) {
+    int maxnb = e->b.maxnb * 3 / 2;
+    maxnb = (maxnb + 31) / 32 * 32;
+    CUDA_TRY(e, e->nbr.alloc((size_t)e->b.n * maxnb));
+    e->b.maxnb = maxnb;
+    e->b.nbr = e->nbr.p;
+    if (e->b.pf) {
+        CUDA_TRY(e, e->rev.alloc((size_t)e->b.n * maxnb));
+        CUDA_TRY(e, e->pf.alloc((size_t)e->b.n * maxnb));
+        e->b.rev = e->rev.p;
+        e->b.pf = e->pf.p;
+    }
+    launch_request_rebuild(e->b, e->stream);
+    e->drop_graphs();
+    return LG_OK;
+}
+
+int read_status(lg_engine* e, uint32_t* out) {
+    CUDA_TRY(e, cudaMemcpyAsync(e->h_status, e->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->stream));
+    CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+    *out = *e->h_status;
+    return LG_OK;
+}
+
+int clear_status_bits(lg_engine* e, uint32_t bits) {
+    uint32_t v = *e->h_status & ~bits;
+    *e->h_status = v;
+    CUDA_TRY(e, cudaMemcpyAsync(e->status.p, e->h_status, sizeof(uint32_t), cudaMemcpyHostToDevice, e->stream));
+    return LG_OK;
+}
+
+// Kernels launch_nlist_build enqueues.
+int nlist_launches(const Batch& b) { return b.n ? (b.perm ? 8 : 9) : 0; }
+
+// Forces (and energies / virials) of the whole batch at the positions in posq.
+// The pair kernel assigns the forces, the other force kernels add to them.
+// In an MD step vv_first has already written the mixed path's fixed-point
+// positions (fixed_written).
+void enqueue_forces(lg_engine* e, uint32_t terms, bool ev, cudaStream_t st, bool fixed_written) {
+    const Batch& b = e->b;
+    if (b.n == 0) return;
+    launch_nlist_build(b, st);
+    e->launches += nlist_launches(b);
+    if (!fixed_written) {  // fixed-point copy (mixed: in the order of the list)
+        launch_split_positions(b, st);
+        e->launches += 1;
+    }
+    if (terms & (LG_TERM_PAIRS | LG_TERM_COUL_REAL)) {
+        launch_pair_forces(b, terms, ev, st);
+        e->launches += b.precision == LG_PRECISION_MIXED ? 1 : 2;
+    } else {
+        cudaMemsetAsync(e->force.p, 0, 3 * (size_t)b.n * sizeof(double), st);
+    }
+    if ((terms & (LG_TERM_BONDS | LG_TERM_ANGLES | LG_TERM_DIHEDRALS)) && b.bt_off) {
+        launch_bonded(b, terms, ev, st);
+        e->launches += 1;
+    }
+    if ((terms & LG_TERM_COUL_KSPACE) && b.nkvec) {
+        launch_kspace(b, true, ev, st);
+        e->launches += 4;
+    }
+}
+
+int compute_batch(lg_engine* e, uint32_t terms, uint32_t want, double* d_force_out, double* d_out) {
+    bool ev = (want & (LG_WANT_ENERGY | LG_WANT_VIRIAL)) != 0;
+    cudaStream_t st = e->stream;
+    for (int attempt = 0; attempt < 4; attempt++) {
+        launch_check_displacement(e->b, st);
+        e->launches += e->b.n ? 1 : 0;
+        if (ev) CUDA_TRY(e, cudaMemsetAsync(e->red.p, 0, (size_t)e->b.n * RED_STRIDE * sizeof(double), st));
+        enqueue_forces(e, terms, ev, st);
+        if (ev) {
+            launch_reduce(e->b, terms, (terms & LG_TERM_COUL_KSPACE) && e->b.nkvec, e->out.p, st);
+            e->launches += 1;
+        }
+        CUDA_TRY(e, cudaGetLastError());
+        uint32_t status;
+        int rc = read_status(e, &status);
+        if (rc) return rc;
+        if (status & ST_OVERFLOW) {
+            rc = clear_status_bits(e, ST_OVERFLOW);
+            if (rc) return rc;
+            rc = regrow(e);
+            if (rc) return rc;
+            continue;
+        }
+        if (status & ST_NONFINITE) {
+            clear_status_bits(e, ST_NONFINITE);
+            return fail(e, LG_ERR_NONFINITE, "Potential energy is infinite!");
+        }
+        if (d_force_out)
+            CUDA_TRY(e, cudaMemcpyAsync(d_force_out, e->force.p, 3 * (size_t)e->b.n * sizeof(double),
+                                        cudaMemcpyDeviceToDevice, st));
+        (void)d_out;
+        return LG_OK;
+    }
+    return fail(e, LG_ERR_CAPACITY, "neighbour list overflow persisted after regrowing");
+}
+
+// The device address of a page-locked host buffer (cudaHostAlloc /
+// cudaHostRegister memory is mapped into the device's address space under
+// unified addressing), or null for pageable memory.  The pack / unpack kernels
+// read and write such buffers over the host link directly, which fuses the
+// host <-> device transfer with the change of layout.
+const void* mapped_host(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// Host positions and velocities (3 n doubles each) of atoms [base, base + n)
+// into the packed device state: read in place from page-locked buffers, else
+// staged through pos3 / vel3.
+int put_state(lg_engine* e, int64_t base, int64_t n, const double* positions, const double* velocities) {
+    cudaStream_t st = e->stream;
+    Batch sub = e->b;
+    sub.n = (int)n;
+    sub.posq = e->posq.p + base;
+    sub.vel = e->vel.p + base;
+    const double* dp = (const double*)mapped_host(positions);
+    const double* dv = (const double*)mapped_host(velocities);
+    if (!dp) {
+        CUDA_TRY(e, cudaMemcpyAsync(e->pos3.p + 3 * base, positions, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st));
+        dp = e->pos3.p + 3 * base;
+    }
+    if (!dv) {
+        CUDA_TRY(e, cudaMemcpyAsync(e->vel3.p + 3 * base, velocities, 3 * n * sizeof(double), cudaMemcpyHostToDevice,
+                                    st));
+        dv = e->vel3.p + 3 * base;
+    }
+    launch_pack_positions(sub, dp, st);
+    launch_pack_velocities(sub, dv, st);
+    e->launches += 2;
+    return LG_OK;
+}
+
+// The packed device state of atoms [base, base + n) into host positions and
+// velocities (either may be null): written in place into page-locked buffers,
+// else staged through pos3 / vel3.
+int get_state(lg_engine* e, int64_t base, int64_t n, double* positions, double* velocities) {
+    cudaStream_t st = e->stream;
+    Batch sub = e->b;
+    sub.n = (int)n;
+    sub.posq = e->posq.p + base;
+    sub.vel = e->vel.p + base;
+    if (positions) {
+        double* dp = (double*)mapped_host(positions);
+        launch_unpack_positions(sub, dp ? dp : e->pos3.p + 3 * base, st);
+        e->launches += 1;
+        if (!dp)
+            CUDA_TRY(e, cudaMemcpyAsync(positions, e->pos3.p + 3 * base, 3 * n * sizeof(double),
+                                        cudaMemcpyDeviceToHost, st));
+    }
+    if (velocities) {
+        double* dv = (double*)mapped_host(velocities);
+        launch_unpack_velocities(sub, dv ? dv : e->vel3.p + 3 * base, st);
+        e->launches += 1;
+        if (!dv)
+            CUDA_TRY(e, cudaMemcpyAsync(velocities, e->vel3.p + 3 * base, 3 * n * sizeof(double),
+                                        cudaMemcpyDeviceToHost, st));
+    }
+    return LG_OK;
+}
+
+// Copies the host positions of system s into its slice of the device state;
+// the other systems keep theirs.
+int upload_positions(lg_engine* e, int32_t s, const double* positions) {
+    const HostSystem& h = e->sys[s];
+    if (h.n == 0) return LG_OK;
+    int64_t base = e->begin[s];
+    cudaStream_t st = e->stream;
+    CUDA_TRY(e, cudaMemcpyAsync(e->pos3.p + 3 * base, positions, 3 * h.n * sizeof(double), cudaMemcpyHostToDevice,
+                                st));
+    Batch sub = e->b;
+    sub.n = (int)h.n;
+    sub.posq = e->posq.p + base;
+    launch_pack_positions(sub, e->pos3.p + 3 * base, st);
+    e->launches += 1;
+    return LG_OK;
+}
+
+// The autotuner: times the pair kernel at every threads-per-atom width (2, 4
+// and 8 for a batch the persistent kernel runs) and the
+// Ewald field kernel at several chunk lengths on the current batch and list,
+// keeps the fastest, and caches the choice for this workload shape.
+int autotune(lg_engine* e) {
+    if (e->tuned || e->b.n == 0) return LG_OK;
+    if (e->opt.threads_per_atom) {  // fixed by the caller
+        e->tuned = true;
+        return LG_OK;
+    }
+    Batch& b = e->b;
+    auto key = std::make_tuple(e->opt.device, b.precision, b.n, b.maxnb, b.nkvec, persist_batch(e));
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            b.tpa = it->second.first;
+            b.kchunk = it->second.second;
+            b.nkchunks = (e->max_nk + b.kchunk - 1) / b.kchunk;
+            e->tuned = true;
+            return LG_OK;
+        }
+    }
+    cudaStream_t st = e->stream;
+    cudaEvent_t e0, e1;
+    CUDA_TRY(e, cudaEventCreate(&e0));
+    CUDA_TRY(e, cudaEventCreate(&e1));
+    // a current list for the timing
+    launch_check_displacement(b, st);
+    launch_nlist_build(b, st);
+    launch_split_positions(b, st);
+    auto time_it = [&](auto&& launch) -> float {
+        launch();  // warm
+        float best = 1e30f;
+        for (int r = 0; r < 3; r++) {
+            cudaEventRecord(e0, st);
+            launch();
+            cudaEventRecord(e1, st);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            best = std::min(best, ms);
+        }
+        return best;
+    };
+    // (a batch for the persistent kernel: the group sizes it runs)
+    const int tpas_all[6] = {1, 2, 4, 8, 16, 32}, tpas_persist[3] = {2, 4, 8};
+    const bool pb = std::get<5>(key);
+    const int* tpas = pb ? tpas_persist : tpas_all;
+    const int ntpas = pb ? 3 : 6;
+    int best_tpa = b.tpa;
+    float best_t = 1e30f;
+    for (int k = 0; k < ntpas; k++) {
+        int t = tpas[k];
+        b.tpa = t;
+        float ms = time_it([&] { launch_pair_forces(b, LG_TERM_ALL, false, st); });
+        if (ms < best_t) {
+            best_t = ms;
+            best_tpa = t;
+        }
+    }
+    b.tpa = best_tpa;
+    if (b.nkvec) {
+        launch_kspace_part(b, 0, false, st);
+        launch_kspace_part(b, 1, false, st);
+        const int chunks[4] = {MIN_KCHUNK, 16, 32, 64};
+        int best_c = b.kchunk;
+        best_t = 1e30f;
+        for (int kc : chunks) {
+            b.kchunk = kc;
+            b.nkchunks = (e->max_nk + kc - 1) / kc;
+            float ms = time_it([&] { launch_kspace_part(b, 2, false, st); });
+            if (ms < best_t) {
+                best_t = ms;
+                best_c = kc;
+            }
+        }
+        b.kchunk = best_c;
+        b.nkchunks = (e->max_nk + best_c - 1) / best_c;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    CUDA_TRY(e, cudaGetLastError());
+    CUDA_TRY(e, cudaStreamSynchronize(st));
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        g_tune_cache[key] = {b.tpa, b.kchunk};
+    }
+    e->tuned = true;
+    e->drop_graphs();
+    return LG_OK;
+}
+
+// What the MD steps of a batch need besides the integrators: a thermostat or
+// control (MD_ADJUST), Rewrap (MD_REWRAP), a Verlet system (MD_VERLET_SYS:
+// its positions move after the forces, so the fixed-point copies are taken
+// before each force evaluation).
+int md_mode(const lg_engine* e) {
+    int mode = 0;
+    for (int s = 0; s < e->nsys; s++) {
+        const HostSystem& h = e->sys[s];
+        if (h.thermostat != LG_THERMOSTAT_NONE || h.controls) mode |= MD_ADJUST;
+        if (h.controls & LG_CONTROL_REWRAP) mode |= MD_REWRAP;
+        if (h.integrator == LG_INTEGRATOR_VERLET) mode |= MD_VERLET_SYS;
+    }
+    return mode;
+}
+
+// One MD step of every system.  The thermostat and controls of the previous
+// step are applied by this step's md_first (apply_previous; Rewrap by a kernel
+// before it), and the last step of a run is followed by launch_md_finalize.
+void enqueue_md_step(lg_engine* e, int mode, bool apply_previous, cudaStream_t st) {
+    bool adjust = (mode & MD_ADJUST) && apply_previous;
+    if (adjust && (mode & MD_REWRAP)) {
+        launch_rewrap(e->b, st);
+        e->launches += e->b.nmol ? 1 : 0;
+    }
+    launch_md_first(e->b, adjust, st);
+    enqueue_forces(e, LG_TERM_ALL, false, st, !(mode & MD_VERLET_SYS));
+    launch_md_second(e->b, st);
+    e->launches += e->b.ntiles ? 2 : 0;
+    if (mode & MD_ADJUST) {  // this step's thermostat factor and controls, per system
+        launch_md_adjust(e->b, st);
+        e->launches += 1;
+    }
+}
+
+// The pending thermostat and controls at the end of a run.
+void enqueue_md_finish(lg_engine* e, int mode, cudaStream_t st) {
+    if (!(mode & MD_ADJUST)) return;
+    launch_md_finalize(e->b, st);
+    e->launches += e->b.ntiles ? 1 : 0;
+    if (mode & MD_REWRAP) {
+        launch_rewrap(e->b, st);
+        e->launches += e->b.nmol ? 1 : 0;
+    }
+}
+
+// ---- persistent batched MD -------------------------------------------------------
+// A batch the persistent kernel can run: mixed precision, pair potentials
+// only, Velocity-Verlet with at most a Berendsen thermostat.  It also needs a group size of 2, 4 or 8 threads per atom (the
+// per-step kernel's, so both paths sum every force in the same order).
+bool persist_batch(const lg_engine* e) {
+    const Batch& b = e->b;
+    if ((e->opt.flags & LG_OPT_NO_PERSISTENT) || b.precision != LG_PRECISION_MIXED || b.pair_general || b.bt_off ||
+        b.nkvec != 0 || b.n == 0)
+        return false;
+    for (int s = 0; s < e->nsys; s++) {  // VelocityVerlet, no thermostat or Berendsen, no control
+        const HostSystem& h = e->sys[s];
+        if (h.integrator != LG_INTEGRATOR_VELOCITY_VERLET || h.controls ||
+            (h.thermostat != LG_THERMOSTAT_NONE && h.thermostat != LG_THERMOSTAT_BERENDSEN))
+            return false;
+    }
+    return true;
+}
+bool persist_eligible(const lg_engine* e) {
+    int t = e->b.tpa;
+    return persist_batch(e) && (t == 2 || t == 4 || t == 8);
+}
+
+// Packs the systems into groups of about equal work (atoms times the expected
+// neighbour count; longest first, each to the least loaded group) for each
+// cluster size the device can hold, and keeps the size whose largest group
+// per block is smallest.  A system's arithmetic does not depend on its group.
+int persist_plan(lg_engine* e) {
+    e->pk_cluster = -1;
+    const Batch& b = e->b;
+    int nsys = e->nsys;
+    // work of a system: its neighbour-list entries (measured when the lists
+    // exist, else estimated from the density) plus a per-atom share
+    std::vector<int> h_nnb(b.n);
+    CUDA_TRY(e, cudaMemcpy(h_nnb.data(), e->nnb.p, (size_t)b.n * sizeof(int), cudaMemcpyDeviceToHost));
+    std::vector<double> work(nsys);
+    for (int s = 0; s < nsys; s++) {
+        const HostSystem& h = e->sys[s];
+        double V = h.L[0] * h.L[1] * h.L[2];
+        double rl = e->h_sysdev[s].rlist;
+        double entries = 0.0;
+        for (int64_t i = e->begin[s]; i < e->begin[s + 1]; i++) entries += h_nnb[i];
+        if (entries == 0.0) entries = (double)h.n * (double)h.n / V * 4.0 / 3.0 * PI * rl * rl * rl;
+        work[s] = entries + 8.0 * (double)h.n;
+    }
+    std::vector<int> order(nsys);
+    for (int s = 0; s < nsys; s++) order[s] = s;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return work[x] > work[y]; });
+    double best_t = 0.0;
+    int best_c = 0;
+    std::vector<std::vector<int>> best_bins;
+    int forced = (e->opt.flags >> LG_OPT_CLUSTER_SHIFT) & 0xf;
+    for (int C : {1, 2, 4, 8}) {
+        if (forced && C != (1 << (forced - 1))) continue;
+        int gmax = persist_max_clusters(b.tpa, C, PK_STAGE_MAX);
+        if (gmax <= 0) continue;
+        int G = std::max(std::min(gmax, nsys), (nsys + PK_MAXG - 1) / PK_MAXG);
+        std::vector<std::vector<int>> bins(G);
+        std::vector<double> load(G, 0.0);
+        for (int s : order) {
+            int pick = -1;
+            for (int g = 0; g < G; g++)
+                if ((int)bins[g].size() < PK_MAXG && (pick < 0 || load[g] < load[pick])) pick = g;
+            bins[pick].push_back(s);
+            load[pick] += work[s];
+        }
+        double waves = std::ceil((double)G / (double)gmax);
+        double t = *std::max_element(load.begin(), load.end()) / C * waves;
+        if (best_c == 0 || t < 0.97 * best_t) {
+            best_t = t;
+            best_c = C;
+            best_bins = bins;
+        }
+    }
+    if (best_c == 0) return LG_OK;  // no cluster fits: the per-step kernels run
+    std::vector<int> off(1, 0), sys;
+    for (auto& bin : best_bins) {
+        if (bin.empty()) continue;
+        std::sort(bin.begin(), bin.end());
+        sys.insert(sys.end(), bin.begin(), bin.end());
+        off.push_back((int)sys.size());
+    }
+    int G = (int)off.size() - 1;
+    // the largest group's atoms, staged in shared memory when they fit
+    int stage = 0;
+    for (int g = 0; g < G; g++) {
+        int atoms = 0;
+        for (int k = off[g]; k < off[g + 1]; k++) atoms += (int)e->sys[sys[k]].n;
+        stage = std::max(stage, atoms);
+    }
+    e->pk_stage = (stage <= PK_STAGE_MAX && (e->opt.flags & LG_OPT_STAGING)) ? stage : 0;
+    cudaStream_t st = e->stream;
+    CUDA_TRY(e, e->pk_group_off.alloc(off.size()));
+    CUDA_TRY(e, e->pk_group_sys.alloc(sys.size()));
+    CUDA_TRY(e, e->pk_group_flag.alloc(G));
+    CUDA_TRY(e, e->pk_ke.alloc(b.n));
+    CUDA_TRY(e, cudaMemcpyAsync(e->pk_group_off.p, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(e, cudaMemcpyAsync(e->pk_group_sys.p, sys.data(), sys.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(e, cudaStreamSynchronize(st));
+    e->pk_groups = G;
+    e->pk_cluster = best_c;
+    return LG_OK;
+}
+
+// lg_md_run on the persistent kernel: one launch per chunk, with the same
+// checkpoint / regrow / replay on a list overflow as the per-step path.
+int md_run_persistent(lg_engine* e, int64_t nsteps, bool thermo) {
+    const int chunk = 32;
+    cudaStream_t st = e->stream;
+    int64_t done = 0;
+    int retries = 0;
+    size_t bytes = e->b.n * sizeof(double4_32a);
+    while (done < nsteps) {
+        int steps = (int)std::min<int64_t>(chunk, nsteps - done);
+        int key = 2 * steps + (thermo ? 1 : 0);
+        auto it = e->pk_graphs.find(key);
+        if (it == e->pk_graphs.end()) {
+            cudaGraph_t g;
+            CUDA_TRY(e, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            cudaMemcpyAsync(e->cp_pos.p, e->posq.p, bytes, cudaMemcpyDeviceToDevice, st);
+            cudaMemcpyAsync(e->cp_vel.p, e->vel.p, bytes, cudaMemcpyDeviceToDevice, st);
+            cudaMemcpyAsync(e->cp_acc.p, e->acc.p, bytes, cudaMemcpyDeviceToDevice, st);
+            cudaMemsetAsync(e->pk_group_flag.p, 0, e->pk_groups * sizeof(int), st);
+            PkArgs a{e->pk_groups, e->pk_group_off.p, e->pk_group_sys.p, e->pk_group_flag.p, e->pk_ke.p, steps,
+                     thermo ? 1 : 0, e->pk_stage};
+            cudaError_t le = launch_md_persist(e->b, a, e->pk_cluster, st);
+            cudaError_t ce = cudaStreamEndCapture(st, &g);
+            if (le != cudaSuccess) return fail(e, LG_ERR_CUDA, std::string("persistent launch: ") + cudaGetErrorString(le));
+            if (ce != cudaSuccess) return fail(e, LG_ERR_CUDA, std::string("stream capture: ") + cudaGetErrorString(ce));
+            cudaGraphExec_t exec = nullptr;
+            ce = cudaGraphInstantiate(&exec, g, 0);
+            cudaGraphDestroy(g);
+            if (ce != cudaSuccess)
+                return fail(e, LG_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ce));
+            it = e->pk_graphs.emplace(key, exec).first;
+        }
+        CUDA_TRY(e, cudaGraphLaunch(it->second, st));
+        e->launches += 1;
+        uint32_t status;
+        int rc = read_status(e, &status);
+        if (rc) return rc;
+        if (status & ST_OVERFLOW) {
+            if (++retries > 4) return fail(e, LG_ERR_CAPACITY, "neighbour list overflow persisted after regrowing");
+            CUDA_TRY(e, cudaMemcpyAsync(e->posq.p, e->cp_pos.p, bytes, cudaMemcpyDeviceToDevice, st));
+            CUDA_TRY(e, cudaMemcpyAsync(e->vel.p, e->cp_vel.p, bytes, cudaMemcpyDeviceToDevice, st));
+            CUDA_TRY(e, cudaMemcpyAsync(e->acc.p, e->cp_acc.p, bytes, cudaMemcpyDeviceToDevice, st));
+            rc = clear_status_bits(e, ST_OVERFLOW);
+            if (rc) return rc;
+            rc = regrow(e);
+            if (rc) return rc;
+            continue;
+        }
+        done += steps;
+    }
+    return LG_OK;
+}
+
+int build_md_graph(lg_engine* e, int steps, int mode) {
+    if (e->graph_mode != mode) e->drop_graphs();
+    cudaGraph_t g;
+    uint64_t before = e->launches;
+    CUDA_TRY(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < steps; k++) enqueue_md_step(e, mode, k > 0, e->stream);
+    enqueue_md_finish(e, mode, e->stream);
+    e->launches = before;  // captured launches run (and are counted) at replay
+    CUDA_TRY(e, cudaStreamEndCapture(e->stream, &g));
+    size_t nodes = 0;
+    cudaGraphGetNodes(g, nullptr, &nodes);
+    cudaGraphExec_t exec = nullptr;
+    cudaError_t ce = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) return fail(e, LG_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ce));
+    e->graphs[steps] = exec;
+    e->graph_nodes[steps] = nodes;
+    e->graph_mode = mode;
+    return LG_OK;
+}
+
+}  // namespace lg

@@ -1034,5 +1034,10 @@ class MonteCarlo:
         cost = self.beta * system.move_molecule_cost(molid, newpos)
         self.attempted += 1
         if cost <= 0.0 or self.rng.random() < np.exp(-cost):
-            self.energy = system.mc_update(molid, system.wrap_molecule(molid, newpos))
+            # Translate::apply wraps the molecule's centre of mass into the cell
+            # (translate.rs:114-125); Rotate::apply only copies the new positions
+            # (rotate.rs:91-96)
+            if isinstance(move, Translate):
+                newpos = system.wrap_molecule(molid, newpos)
+            self.energy = system.mc_update(molid, newpos)
             self.accepted += 1

@@ -5,6 +5,10 @@ tests (tests/nist-lj.rs, tests/nist-spce.rs) together with the configurations
 they apply to (tests/data/nist-*).  Nothing is copied into this repository:
 these helpers parse the assertions and the data files where they lie, and the
 tests that use them are skipped when the reference tree is not present.
+
+The reference tree is the directory named by the environment variable
+LUMOL_REFERENCE_ROOT; without it, a checkout named `reference` beside this
+repository's root directory is used when one exists.
 """
 from __future__ import annotations
 
@@ -13,7 +17,10 @@ import re
 
 import numpy as np
 
-REFERENCE_ROOT = os.environ.get("LUMOL_REFERENCE_ROOT", "/root/reference")
+_REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REFERENCE_ROOT = os.environ.get("LUMOL_REFERENCE_ROOT") or os.path.join(os.path.dirname(_REPO), "reference")
+SKIP_REASON = ("reference tree not found: set LUMOL_REFERENCE_ROOT to a lumol checkout "
+               "(or place one beside this repository as `reference`)")
 
 
 def available() -> bool:

@@ -77,3 +77,45 @@ def test_update_without_cost_is_an_error():
     s.mc_init()
     with pytest.raises(lg.EngineError, match="without call a"):
         s.mc_update(0, s.positions[0:1])
+
+
+def test_accepted_rotation_is_not_wrapped():
+    """Rotate::apply copies the rotated positions as they are (rotate.rs:91-96),
+    unlike Translate::apply, which wraps the centre of mass into the cell: a
+    molecule whose centre of mass lies outside the cell stays outside after an
+    accepted rotation, at com + R (x - com)."""
+    s = workloads.water_box(n_side=3, length=14.0, seed=3, cutoff=6.5, alpha=0.45, kmax=5)
+    s.set_bond_potential(("H", "O"), lg.NullPotential())
+    s.set_angle_potential(("H", "O", "H"), lg.NullPotential())
+    pos = s.positions.copy()
+    lo, hi = s.molecule_range(4)
+    pos[lo:hi] += np.array([14.0, -14.0, 0.0])  # the same periodic image, centre of mass outside
+    s.positions = pos
+    # a huge temperature accepts every move
+    mc = lg.MonteCarlo(1e12, lg.Rotate(0.5), seed=7)
+    mc.setup(s)
+    rotated_outside = 0
+    for _ in range(400):
+        before = s.positions.copy()
+        mc.propagate(s)
+        after = s.positions
+        moved = np.flatnonzero(np.any(after != before, axis=1))
+        if moved.size == 0:
+            continue
+        mol = int(s.molecules[moved[0]])
+        rotated_outside += mol == 4
+        if rotated_outside >= 3:
+            break
+        a, b = s.molecule_range(mol)
+        m = s.masses[a:b, None]
+        com_before = (m * before[a:b]).sum(axis=0) / m.sum()
+        com_after = (m * after[a:b]).sum(axis=0) / m.sum()
+        assert np.abs(com_after - com_before).max() < 1e-9, (mol, com_before, com_after)
+    lo, hi = s.molecule_range(4)
+    m = s.masses[lo:hi, None]
+    com = (m * s.positions[lo:hi]).sum(axis=0) / m.sum()
+    assert rotated_outside >= 3
+    assert com[0] > 14.0 and com[1] < 0.0
+    assert mc.accepted == mc.attempted
+    fresh = s.potential_energy()
+    assert abs(mc.energy - fresh) <= 1e-9 * abs(fresh)

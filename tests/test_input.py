@@ -20,7 +20,7 @@ import systems
 from lumol_gb300 import units
 
 INTERACTIONS = refdata.path("lumol-input", "tests", "interactions")
-needs_reference = pytest.mark.skipif(not os.path.isdir(INTERACTIONS), reason="reference tree not present")
+needs_reference = pytest.mark.skipif(not os.path.isdir(INTERACTIONS), reason=refdata.SKIP_REASON)
 
 
 def _cases(kind):
@@ -160,7 +160,7 @@ def test_charges_and_ewald_accuracy():
     assert s.angle_potentials[("H", "O", "H")].x0 == units.from_(109.47, "deg")
 
 
-@pytest.mark.skipif(not refdata.available(), reason="reference tree not present")
+@pytest.mark.skipif(not refdata.available(), reason=refdata.SKIP_REASON)
 def test_ewald_with_accuracy_nist_spce():
     # ewald.rs:1446-1462
     for xyz, alpha, kmax in [("spce-1.xyz", 0.2826, 5), ("spce-2.xyz", 0.2900, 5), ("spce-3.xyz", 0.2943, 5),

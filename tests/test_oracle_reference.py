@@ -16,7 +16,7 @@ from lumol_gb300 import units
 from ulps import relative_eq, rust_round_at, ulps_eq
 
 LJ, BUCK, HARM, BMH, MORSE, GAUSS, MIE = 2, 3, 4, 5, 6, 7, 8
-needs_reference = pytest.mark.skipif(not refdata.available(), reason="reference tree not present")
+needs_reference = pytest.mark.skipif(not refdata.available(), reason=refdata.SKIP_REASON)
 
 
 # ---- energy/functions.rs:621-715 ---------------------------------------------
