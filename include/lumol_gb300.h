@@ -305,9 +305,38 @@ int lg_md_set_state_all(lg_engine* e, const double* positions, const double* vel
 int lg_md_get_state_all(lg_engine* e, double* positions, double* velocities, double* accelerations);
 /* Runs `nsteps` steps of every system with device-resident state. */
 int lg_md_run(lg_engine* e, int64_t nsteps);
-/* Integrator::integrate for a single-system engine (integrators.rs:44-69): copies
- * host positions / velocities in, runs `nsteps` steps, copies them back. */
+/* Integrator::integrate for a single-system engine (integrators.rs:44-69): runs
+ * `nsteps` steps from the host positions / velocities and copies them back.
+ * The same as lg_md_propagate(..., LG_SYNC_DOWNLOAD): the host arrays are
+ * uploaded only when they differ from what the engine last exchanged. */
 int lg_md_integrate(lg_engine* e, double* positions, double* velocities, int64_t nsteps);
+
+/* Lazy host synchronisation behind Integrator::integrate and
+ * Propagator::propagate (lumol-sim/src/md/molecular_dynamics.rs:66-76,
+ * lumol-sim/src/simulations.rs:87-92): the engine keeps x and v resident on
+ * the device and a page-locked copy of the host arrays it last exchanged.
+ * A call uploads `positions` / `velocities` only when the device state is not
+ * the one last exchanged (first call, description change, another call wrote
+ * the state) or when the host arrays differ from that copy (a host-side
+ * thermostat, control or user edit); LG_SYNC_TRUST_HOST skips the comparison
+ * (the caller knows the arrays are unchanged).  It then runs `nsteps` steps
+ * and, with LG_SYNC_DOWNLOAD, copies the state back (one device
+ * synchronisation for the steps and the copy); without it the host arrays are
+ * left as they were, e.g. between the steps that outputs read.  Single-system
+ * engines only.  Returns LG_ERR_NONFINITE (after completing the steps) when
+ * the velocities became non-finite (compute.rs:141, "Kinetic energy is
+ * infinite!"). */
+#define LG_SYNC_DOWNLOAD 1u
+#define LG_SYNC_TRUST_HOST 2u
+int lg_md_propagate(lg_engine* e, double* positions, double* velocities, int64_t nsteps, uint32_t flags);
+
+/* Per-system status flags (n_systems entries) of the last runs: LG_SYS_NONFINITE
+ * when a system's velocities or its energy became non-finite (the reference
+ * panics there, sys/compute.rs:125,141).  lg_md_run completes the steps of
+ * every system and returns LG_ERR_NONFINITE; the other systems' results are
+ * unaffected.  `clear` resets the flags after reading them. */
+#define LG_SYS_NONFINITE 1u
+int lg_system_status(lg_engine* e, uint32_t* flags, int32_t clear);
 
 /* ---- Monte Carlo ------------------------------------------------------------- */
 /* EnergyCache::init (sys/cache.rs:75-98) at `positions` for system `s`. */
@@ -360,6 +389,11 @@ int lg_launch_count(lg_engine* e, uint64_t* count);
  * of groups (0 and 0 while MD runs on the per-step kernels or before the first
  * lg_md_run). */
 int lg_md_plan(lg_engine* e, int32_t* cluster, int32_t* groups);
+/* Test hook: leaves system `s` as an interrupted list build would, with
+ * `extra` stale atoms counted in its first cell, and asks for a rebuild.  The
+ * next build finds the counts inconsistent, writes nothing out of range, and
+ * the engine recounts and rebuilds before using the list. */
+int lg_test_stale_cell_counts(lg_engine* e, int32_t s, int32_t extra);
 /* Measured FMA throughput of the FP64 (fp64 = 1) or FP32 pipe of the current
  * device, in TFLOP/s (2 flops per FMA). */
 int lg_fma_peak(int32_t fp64, double* tflops);

@@ -38,6 +38,10 @@ LG_TERM_DIHEDRALS = 128
 LG_TERM_ALL = 255
 LG_BONDED_COSINE_HARMONIC, LG_BONDED_TORSION = 10, 11
 
+LG_SYNC_DOWNLOAD = 1
+LG_SYNC_TRUST_HOST = 2
+LG_SYS_NONFINITE = 1
+
 LG_WANT_FORCES = 1
 LG_WANT_ENERGY = 2
 LG_WANT_VIRIAL = 4
@@ -125,6 +129,8 @@ SIGNATURES = {
     "lg_md_get_state_all": (ctypes.c_int, [_P, _D, _D, _D]),
     "lg_md_run": (ctypes.c_int, [_P, ctypes.c_int64]),
     "lg_md_integrate": (ctypes.c_int, [_P, _D, _D, ctypes.c_int64]),
+    "lg_md_propagate": (ctypes.c_int, [_P, _D, _D, ctypes.c_int64, ctypes.c_uint32]),
+    "lg_system_status": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint32), ctypes.c_int32]),
     "lg_mc_init": (ctypes.c_int, [_P, ctypes.c_int32, _D, _D]),
     "lg_mc_move_molecule_cost": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int64, _D, _D]),
     "lg_mc_update": (ctypes.c_int, [_P, ctypes.c_int32, _D, _D]),
@@ -136,6 +142,7 @@ SIGNATURES = {
     "lg_launch_count": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64)]),
     "lg_md_plan": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
     "lg_fma_peak": (ctypes.c_int, [ctypes.c_int32, _D]),
+    "lg_test_stale_cell_counts": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
     "lg_ewald_kspace_noalloc": (ctypes.c_int, [_P, _P, ctypes.c_int64, _D, ctypes.c_double, ctypes.c_int32,
                                                _P, _P, _P, _P]),
 }

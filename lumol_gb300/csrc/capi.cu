@@ -4,6 +4,8 @@
 // object and its helpers are in engine.h.
 #include "engine.h"
 
+#include <functional>
+
 // ============================================================================
 // C ABI
 // ============================================================================
@@ -276,6 +278,7 @@ int lg_compute_device(lg_engine* e, const double* d_positions, uint32_t terms, u
         cudaStreamWaitEvent(st, ev, 0);
         cudaEventDestroy(ev);
     }
+    e->shadow_valid = false;
     launch_pack_positions(e->b, d_positions, st);
     rc = compute_batch(e, terms, want, (want & LG_WANT_FORCES) ? d_forces : nullptr, nullptr);
     if (rc) return rc;
@@ -430,14 +433,13 @@ int lg_md_get_state(lg_engine* e, int32_t s, double* positions, double* velociti
 
 }  // extern "C"
 
-extern "C" {
+namespace {
 
-int lg_md_run(lg_engine* e, int64_t nsteps) {
-    if (!e || nsteps < 0) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
-    CUDA_TRY(e, cudaSetDevice(e->opt.device));
-    if (e->dirty) return fail(e, LG_ERR_STATE, "no device state: call lg_md_set_state first");
-    for (int s = 0; s < e->nsys; s++)
-        if (!e->sys[s].md_ready) return fail(e, LG_ERR_STATE, "lg_md_setup was not called for every system");
+// The steps of lg_md_run.  `tail` (may be empty) is enqueued after the last
+// chunk, before the status read that ends it, so a caller that copies the state
+// back pays for one synchronisation only; it is enqueued again if that chunk is
+// replayed.
+int md_run_steps(lg_engine* e, int64_t nsteps, const std::function<int()>& tail) {
     const int mode = md_mode(e);
     const bool thermo = (mode & MD_ADJUST) != 0;
     const int chunk = 16;
@@ -466,11 +468,21 @@ int lg_md_run(lg_engine* e, int64_t nsteps) {
             int rc = persist_plan(e);
             if (rc) return rc;
         }
-        if (e->pk_cluster > 0) return md_run_persistent(e, nsteps, thermo);
+        if (e->pk_cluster > 0) {
+            int rc = md_run_persistent(e, nsteps, thermo);
+            if (rc == LG_OK && tail) rc = tail();
+            if (rc == LG_OK && tail) CUDA_TRY(e, cudaStreamSynchronize(st));
+            return rc;
+        }
     }
     DBuf<double4_32a>& cp_pos = e->cp_pos;
     DBuf<double4_32a>& cp_vel = e->cp_vel;
     DBuf<double4_32a>& cp_acc = e->cp_acc;
+    if (nsteps == 0 && tail) {
+        int rc = tail();
+        if (rc) return rc;
+        CUDA_TRY(e, cudaStreamSynchronize(st));
+    }
     while (done < nsteps) {
         int steps = (int)std::min<int64_t>(chunk, nsteps - done);
         if (e->graph_mode != mode || !e->graphs.count(steps)) {
@@ -485,24 +497,75 @@ int lg_md_run(lg_engine* e, int64_t nsteps) {
         if (thermo) CUDA_TRY(e, cudaMemcpyAsync(e->cp_count.p, e->md_count.p, cbytes, cudaMemcpyDeviceToDevice, st));
         CUDA_TRY(e, cudaGraphLaunch(e->graphs[steps], st));
         e->launches += e->graph_nodes[steps];
+        if (done + steps == nsteps && tail) {
+            int rc = tail();
+            if (rc) return rc;
+        }
         uint32_t status;
         int rc = read_status(e, &status);
         if (rc) return rc;
-        if (status & ST_OVERFLOW) {
+        if (status & (ST_OVERFLOW | ST_CELL_OVF)) {
             if (++retries > 4) return fail(e, LG_ERR_CAPACITY, "neighbour list overflow persisted after regrowing");
             CUDA_TRY(e, cudaMemcpyAsync(e->posq.p, cp_pos.p, bytes, cudaMemcpyDeviceToDevice, st));
             CUDA_TRY(e, cudaMemcpyAsync(e->vel.p, cp_vel.p, bytes, cudaMemcpyDeviceToDevice, st));
             CUDA_TRY(e, cudaMemcpyAsync(e->acc.p, cp_acc.p, bytes, cudaMemcpyDeviceToDevice, st));
             if (thermo)
                 CUDA_TRY(e, cudaMemcpyAsync(e->md_count.p, e->cp_count.p, cbytes, cudaMemcpyDeviceToDevice, st));
-            rc = clear_status_bits(e, ST_OVERFLOW);
-            if (rc) return rc;
-            rc = regrow(e);
-            if (rc) return rc;
+            if (status & ST_CELL_OVF) {
+                rc = recount_cells(e);
+                if (rc) return rc;
+            }
+            if (status & ST_OVERFLOW) {
+                rc = clear_status_bits(e, ST_OVERFLOW);
+                if (rc) return rc;
+                rc = regrow(e);
+                if (rc) return rc;
+            }
             continue;
+        }
+        if (status & ST_NONFINITE) {  // reported after the run; the other systems are unaffected
+            e->nonfinite = true;
+            rc = clear_status_bits(e, ST_NONFINITE);
+            if (rc) return rc;
         }
         done += steps;
     }
+    return LG_OK;
+}
+
+int md_run_checked(lg_engine* e, int64_t nsteps, const std::function<int()>& tail) {
+    if (!e || nsteps < 0) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    if (e->dirty) return fail(e, LG_ERR_STATE, "no device state: call lg_md_set_state first");
+    for (int s = 0; s < e->nsys; s++)
+        if (!e->sys[s].md_ready) return fail(e, LG_ERR_STATE, "lg_md_setup was not called for every system");
+    e->nonfinite = false;
+    int rc = md_run_steps(e, nsteps, tail);
+    if (rc) return rc;
+    e->state_gen += 1;
+    if (e->nonfinite)
+        return fail(e, LG_ERR_NONFINITE,
+                    "Kinetic energy is infinite! (non-finite velocities in system " + nonfinite_systems(e) +
+                        "; every other system completed its steps)");
+    return LG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lg_md_run(lg_engine* e, int64_t nsteps) { return md_run_checked(e, nsteps, {}); }
+
+int lg_system_status(lg_engine* e, uint32_t* flags, int32_t clear) {
+    if (!e || !flags) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    if (e->dirty) {
+        for (int s = 0; s < e->nsys; s++) flags[s] = 0u;
+        return LG_OK;
+    }
+    CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+    CUDA_TRY(e, cudaMemcpy(flags, e->sys_status.p, e->nsys * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (clear) CUDA_TRY(e, cudaMemset(e->sys_status.p, 0, e->nsys * sizeof(uint32_t)));
     return LG_OK;
 }
 
@@ -548,13 +611,58 @@ int lg_md_get_state_all(lg_engine* e, double* positions, double* velocities, dou
     return LG_OK;
 }
 
+int lg_md_propagate(lg_engine* e, double* positions, double* velocities, int64_t nsteps, uint32_t flags) {
+    if (!e || e->nsys != 1) return fail(e, LG_ERR_ARGUMENT, "lg_md_propagate needs a single-system engine");
+    if (!positions || !velocities || (flags & ~(LG_SYNC_DOWNLOAD | LG_SYNC_TRUST_HOST)))
+        return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    const bool was_dirty = e->dirty;
+    int rc = commit(e);
+    if (rc) return rc;
+    const int64_t n = e->sys[0].n;
+    const size_t n3 = 3 * (size_t)n;
+    if (e->shadow_n3 != n3 || !e->h_shadow) {
+        if (e->h_shadow) cudaFreeHost(e->h_shadow);
+        e->h_shadow = nullptr;
+        e->shadow_n3 = 0;
+        e->shadow_valid = false;
+        CUDA_TRY(e, cudaMallocHost((void**)&e->h_shadow, std::max<size_t>(2 * n3, 1) * sizeof(double)));
+        e->shadow_n3 = n3;
+    }
+    double* sp = e->h_shadow;
+    double* sv = e->h_shadow + n3;
+    // the host copy changed (or the device state is not the one last exchanged): upload
+    bool upload = !e->shadow_valid;
+    if (!upload && !(flags & LG_SYNC_TRUST_HOST))
+        upload = std::memcmp(positions, sp, n3 * sizeof(double)) != 0 ||
+                 std::memcmp(velocities, sv, n3 * sizeof(double)) != 0;
+    if (upload && n > 0) {
+        std::memcpy(sp, positions, n3 * sizeof(double));
+        std::memcpy(sv, velocities, n3 * sizeof(double));
+        rc = put_state(e, 0, n, sp, sv);  // read in place from the page-locked copy
+        if (rc) return rc;
+        if (was_dirty) CUDA_TRY(e, cudaMemsetAsync(e->acc.p, 0, n * sizeof(double4_32a), e->stream));
+    }
+    e->shadow_valid = true;
+    const bool download = (flags & LG_SYNC_DOWNLOAD) && n > 0;
+    std::function<int()> tail;
+    if (download) tail = [e, n, sp, sv]() { return get_state(e, 0, n, sp, sv); };
+    rc = md_run_checked(e, nsteps, tail);
+    if (rc != LG_OK && rc != LG_ERR_NONFINITE) {
+        e->shadow_valid = false;
+        return rc;
+    }
+    e->shadow_valid = true;
+    if (download) {
+        std::memcpy(positions, sp, n3 * sizeof(double));
+        std::memcpy(velocities, sv, n3 * sizeof(double));
+    }
+    return rc;
+}
+
 int lg_md_integrate(lg_engine* e, double* positions, double* velocities, int64_t nsteps) {
     if (!e || e->nsys != 1) return fail(e, LG_ERR_ARGUMENT, "lg_md_integrate needs a single-system engine");
-    int rc = lg_md_set_state(e, 0, positions, velocities);
-    if (rc) return rc;
-    rc = lg_md_run(e, nsteps);
-    if (rc) return rc;
-    return lg_md_get_state(e, 0, positions, velocities);
+    return lg_md_propagate(e, positions, velocities, nsteps, LG_SYNC_DOWNLOAD);
 }
 
 // ---- diagnostics ---------------------------------------------------------------
@@ -593,6 +701,23 @@ int lg_list_cells(lg_engine* e, int32_t s, int32_t* cells, int32_t ncell[3]) {
     CUDA_TRY(e, cudaMemcpy(cells, e->atom_cell.p + e->begin[s], n * sizeof(int), cudaMemcpyDeviceToHost));
     for (size_t i = 0; i < n; i++) cells[i] -= d.cell_begin;
     for (int k = 0; k < 3; k++) ncell[k] = d.ncell[k];
+    return LG_OK;
+}
+
+int lg_test_stale_cell_counts(lg_engine* e, int32_t s, int32_t extra) {
+    if (!valid_sys(e, s) || extra < 0) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    if (e->dirty) return fail(e, LG_ERR_STATE, "no device state");
+    CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    // what an interrupted build leaves: counts of binned atoms that were never
+    // sorted back to zero, and a rebuild request for the system
+    int* first = e->cell_count.p + e->h_sysdev[s].cell_begin;
+    CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+    int c = 0;
+    CUDA_TRY(e, cudaMemcpy(&c, first, sizeof(int), cudaMemcpyDeviceToHost));
+    c += extra;
+    CUDA_TRY(e, cudaMemcpy(first, &c, sizeof(int), cudaMemcpyHostToDevice));
+    launch_request_rebuild(e->b, e->stream);
+    CUDA_TRY(e, cudaStreamSynchronize(e->stream));
     return LG_OK;
 }
 

@@ -80,6 +80,7 @@ int lg_mc_update(lg_engine* e, int32_t s, const double* molecule_positions, doub
     CUDA_TRY(e, cudaMemcpyAsync(e->mc_newpos.p, molecule_positions, 3 * msize * sizeof(double),
                                 cudaMemcpyHostToDevice, st));
     const double* d_k1 = (const double*)((const char*)(e->sysdev.p + s) + offsetof(SysDev, k1));
+    e->shadow_valid = false;
     launch_mc_accept(e->b, sd, (int)e->mc_mol_begin, msize, e->mc_newpos.p, d_k1, e->mc_drho.p, st);
     e->launches += 2;
     CUDA_TRY(e, cudaStreamSynchronize(st));
@@ -147,6 +148,7 @@ int lg_mc_run(lg_engine* e, int64_t moves) {
             any = true;
         }
     if (!any) return fail(e, LG_ERR_STATE, "lg_mc_setup was not called for any system");
+    e->shadow_valid = false;
     CUDA_TRY(e, cudaMemcpyAsync(e->mc_chains.p, e->h_mc.data(), nsys * sizeof(McState), cudaMemcpyHostToDevice, st));
     // the list must be current for the positions the chains start from, and so
     // must the fixed-point copies the mixed chains read
@@ -192,11 +194,17 @@ int lg_mc_run(lg_engine* e, int64_t moves) {
             uint32_t status;
             int rc = read_status(e, &status);
             if (rc) return rc;
-            if (status & ST_OVERFLOW) {
-                rc = clear_status_bits(e, ST_OVERFLOW);
-                if (rc) return rc;
-                rc = regrow(e);
-                if (rc) return rc;
+            if (status & (ST_OVERFLOW | ST_CELL_OVF)) {
+                if (status & ST_CELL_OVF) {
+                    rc = recount_cells(e);
+                    if (rc) return rc;
+                }
+                if (status & ST_OVERFLOW) {
+                    rc = clear_status_bits(e, ST_OVERFLOW);
+                    if (rc) return rc;
+                    rc = regrow(e);
+                    if (rc) return rc;
+                }
                 launch_nlist_build(e->b, st);
             }
         }

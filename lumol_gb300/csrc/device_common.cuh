@@ -382,7 +382,24 @@ enum : uint32_t {
     ST_OVERFLOW = 2u,       // neighbour list capacity exceeded
     ST_NONFINITE = 4u,      // non-finite energy
     ST_SPECIAL_OVF = 8u,    // bond-path table overflow
+    ST_CELL_OVF = 16u,      // cell counts inconsistent with the atoms binned (a cell build was
+                            // interrupted): the scatter skipped the write; recount and rebuild
 };
+
+// Per-system status bits (Batch::sys_status), read by the host after a run.
+enum : uint32_t {
+    SYS_NONFINITE = 1u,  // a non-finite velocity, acceleration or energy appeared in the system
+};
+
+// A non-finite value in a system's state: the system is flagged (and the
+// batch's status word), the others are not affected.
+__device__ __forceinline__ void flag_nonfinite(double a, double b, double c, int s, uint32_t* sys_status,
+                                               uint32_t* status) {
+    if (!(isfinite(a) && isfinite(b) && isfinite(c)) && sys_status) {
+        atomicOr(sys_status + s, SYS_NONFINITE);
+        atomicOr(status, ST_NONFINITE);
+    }
+}
 
 // Number of energy slots per system in the reduction output:
 // [pairs, coulomb real (Ewald real or Wolf), bonds, angles, kspace] then virial 9.

@@ -70,6 +70,7 @@ static_assert(MD_VELOCITY_VERLET == LG_INTEGRATOR_VELOCITY_VERLET && MD_VERLET =
 static_assert(TH_NONE == LG_THERMOSTAT_NONE && TH_BERENDSEN == LG_THERMOSTAT_BERENDSEN &&
                   TH_RESCALE == LG_THERMOSTAT_RESCALE && TH_CSVR == LG_THERMOSTAT_CSVR,
               "thermostat values");
+static_assert(SYS_NONFINITE == LG_SYS_NONFINITE, "system status values");
 static_assert(CTL_REMOVE_TRANSLATION == LG_CONTROL_REMOVE_TRANSLATION && CTL_REWRAP == LG_CONTROL_REWRAP &&
                   CTL_REMOVE_ROTATION == LG_CONTROL_REMOVE_ROTATION,
               "control values");
@@ -146,7 +147,7 @@ struct lg_engine {
     DBuf<SysDev> sysdev;
     DBuf<PairDev> ptab;
     DBuf<KVecDev> kvec;
-    DBuf<uint32_t> status, sys_rebuild;
+    DBuf<uint32_t> status, sys_rebuild, sys_status;
     DBuf<int> pairs_out;
     DBuf<unsigned long long> pairs_count;
     uint32_t* h_status = nullptr;  // pinned
@@ -155,6 +156,14 @@ struct lg_engine {
     std::vector<int> h_kvec_sys;
 
     bool tuned = false;
+    bool nonfinite = false;  // a system's state became non-finite during the current lg_md_run
+    // Lazy host synchronisation (lg_md_propagate): the positions and velocities
+    // the host and the engine last exchanged (pinned, 3n + 3n doubles), valid
+    // while no other call has written the device state since.
+    double* h_shadow = nullptr;
+    size_t shadow_n3 = 0;
+    bool shadow_valid = false;
+    uint64_t state_gen = 0;  // completed lg_md_run calls (a generation counter of the device state)
     int max_nk = 0;
     // kernels launched so far (graph replays counted by their kernel nodes)
     uint64_t launches = 0;
@@ -199,6 +208,7 @@ struct lg_engine {
 
     ~lg_engine() {
         drop_graphs();
+        if (h_shadow) cudaFreeHost(h_shadow);
         if (h_status) cudaFreeHost(h_status);
         if (h_out) cudaFreeHost(h_out);
         if (stream) cudaStreamDestroy(stream);
@@ -228,6 +238,10 @@ int commit(lg_engine* e);
 
 // ---- runtime.cu -----------------------------------------------------------------
 int regrow(lg_engine* e);
+// After ST_CELL_OVF: zeroes every cell count and asks every system for a rebuild.
+int recount_cells(lg_engine* e);
+// Which systems have SYS_NONFINITE set, as "k, l, ..." (the flags stay set).
+std::string nonfinite_systems(lg_engine* e);
 int read_status(lg_engine* e, uint32_t* out);
 int clear_status_bits(lg_engine* e, uint32_t bits);
 int nlist_launches(const Batch& b);

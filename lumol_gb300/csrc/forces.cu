@@ -657,7 +657,8 @@ __global__ void __launch_bounds__(256) reduce_kernel(const SysDev* __restrict__ 
                                                      const double* __restrict__ kred,
                                                      const double* __restrict__ host_const,
                                                      uint32_t terms, int use_kspace,
-                                                     double* __restrict__ out, uint32_t* status) {
+                                                     double* __restrict__ out, uint32_t* status,
+                                                     uint32_t* sys_status) {
     __shared__ double sh[RED_STRIDE][256];
     int s_idx = blockIdx.x;
     const SysDev& s = sys[s_idx];
@@ -703,6 +704,11 @@ __global__ void __launch_bounds__(256) reduce_kernel(const SysDev* __restrict__ 
         if ((terms & 64u) && s.coul == 1) e += sh[E_KSPACE][0] / FOUR_PI_EPSILON_0;
         double* o = out + (size_t)s_idx * RED_STRIDE;
         o[0] = e;
+        // PotentialEnergy::compute asserts a finite energy (sys/compute.rs:125)
+        if (!isfinite(e)) {
+            atomicOr(status, ST_NONFINITE);
+            if (sys_status) atomicOr(sys_status + s_idx, SYS_NONFINITE);
+        }
         for (int c = 0; c < 9; c++) o[1 + c] = sh[N_ESLOT + c][0];
         if (terms & 2u) {
             o[1] += hc[1];
@@ -715,7 +721,7 @@ __global__ void __launch_bounds__(256) reduce_kernel(const SysDev* __restrict__ 
 void launch_reduce(const Batch& b, uint32_t terms, bool kspace, double* out, cudaStream_t st) {
     if (b.nsys == 0) return;
     reduce_kernel<<<b.nsys, 256, 0, st>>>(b.sys, b.red, b.kred, b.host_const, terms, kspace ? 1 : 0, out,
-                                          b.status);
+                                          b.status, b.sys_status);
 }
 
 // ---------------------------------------------------------------------------

@@ -50,6 +50,7 @@ struct Batch {
     double4_32a* pos_build = nullptr; // positions at the last build
     uint32_t* status = nullptr;   // ST_* bits
     uint32_t* sys_rebuild = nullptr;  // nsys: 1 when that system's list must be rebuilt
+    uint32_t* sys_status = nullptr;   // nsys: SYS_* bits of each system (non-finite state or energy)
     // Ewald k-space
     int nkvec = 0;
     int kdim = 0;                 // max kmax + 1 (eikr stores k = 0..kmax per axis)
@@ -152,7 +153,7 @@ void launch_mc_accept(const Batch& b, const SysDev& sd, int mbeg, int msize, con
 void launch_mc_chains(const Batch& b, McState* mc, bool fp64, cudaStream_t st);
 // diag.cu
 int measure_fma_peak(int fp64, double* tflops);
-// capi.cu: the message lg_last_error(NULL) returns
+// runtime.cu: the message lg_last_error(NULL) returns
 void set_global_error(const std::string& msg);
 
 }  // namespace lg

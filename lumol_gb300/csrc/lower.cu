@@ -325,6 +325,7 @@ int check_pair_cutoffs(lg_engine* e, const HostSystem& h) {
 
 int commit(lg_engine* e) {
     if (!e->dirty) return LG_OK;
+    e->shadow_valid = false;
     int nsys = e->nsys;
     e->begin.assign(nsys + 1, 0);
     for (int s = 0; s < nsys; s++) {
@@ -671,6 +672,7 @@ int commit(lg_engine* e) {
     CUDA_TRY(e, e->ptab.alloc(h_ptab.size()));
     CUDA_TRY(e, e->status.alloc(1));
     CUDA_TRY(e, e->sys_rebuild.alloc(nsys));
+    CUDA_TRY(e, e->sys_status.alloc(nsys));
     int nkv = (int)h_kvec.size();
     int kchunk = 32;
     int nkchunks = 0, max_chunks = 0;
@@ -780,6 +782,7 @@ int commit(lg_engine* e) {
                                 cudaMemcpyHostToDevice, st));
     uint32_t st_init = ST_REBUILD;
     CUDA_TRY(e, cudaMemcpyAsync(e->status.p, &st_init, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(e, cudaMemsetAsync(e->sys_status.p, 0, nsys * sizeof(uint32_t), st));
     std::vector<uint32_t> all_rebuild(nsys, 1u);
     CUDA_TRY(e, cudaMemcpyAsync(e->sys_rebuild.p, all_rebuild.data(), nsys * sizeof(uint32_t), cudaMemcpyHostToDevice,
                                 st));
@@ -826,6 +829,7 @@ int commit(lg_engine* e) {
     b.pos_build = e->pos_build.p;
     b.status = e->status.p;
     b.sys_rebuild = e->sys_rebuild.p;
+    b.sys_status = e->sys_status.p;
     b.nkvec = nkv;
     b.kdim = kdim;
     b.kchunk = kchunk;

@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(VV_TILE) md_first_kernel(
     const int2* __restrict__ tiles, const SysDev* __restrict__ sys, double4_32a* __restrict__ posq,
     double4_32a* __restrict__ vel, const double4_32a* __restrict__ acc, const double4_32a* __restrict__ pos_build,
     const uint4* __restrict__ pfx_build, const double* __restrict__ adj, int adjust, const int* __restrict__ perm,
-    uint4* __restrict__ posfx, uint32_t* status, uint32_t* sys_rebuild) {
+    uint4* __restrict__ posfx, uint32_t* status, uint32_t* sys_rebuild, uint32_t* sys_status) {
     int2 tile = tiles[blockIdx.x];
     const SysDev& s = sys[tile.x];
     int i = tile.y + threadIdx.x;
@@ -302,6 +302,7 @@ __global__ void __launch_bounds__(VV_TILE) md_first_kernel(
     }
     vel[i] = v;
     posq[i] = p;
+    flag_nonfinite(p.x, p.y, p.z, tile.x, sys_status, status);
     // against a threshold 1 % below (skin / 2)^2: the FP32 rounding only ever
     // triggers a rebuild early
     flag_rebuild(r2 > s.rebuild2_f, tile.x, status, sys_rebuild);
@@ -326,7 +327,8 @@ __global__ void __launch_bounds__(VV_TILE) md_second_kernel(
     const float* __restrict__ inv_mass, double4_32a* __restrict__ posq, double4_32a* __restrict__ vel,
     double4_32a* __restrict__ acc, const double4_32a* __restrict__ pos_build, const uint4* __restrict__ pfx_build,
     double* __restrict__ kepart, double* __restrict__ mom, unsigned long long* __restrict__ md_count, int gpw,
-    const int* __restrict__ perm, uint4* __restrict__ posfx, uint32_t* status, uint32_t* sys_rebuild) {
+    const int* __restrict__ perm, uint4* __restrict__ posfx, uint32_t* status, uint32_t* sys_rebuild,
+    uint32_t* sys_status) {
     int2 tile = tiles[blockIdx.x];
     const SysDev& s = sys[tile.x];
     int i = tile.y + threadIdx.x;
@@ -364,6 +366,7 @@ __global__ void __launch_bounds__(VV_TILE) md_second_kernel(
             }
             acc[i] = make_double4_32a(p.x, p.y, p.z, 0.0);
             posq[i] = x;
+            flag_nonfinite(x.x, x.y, x.z, tile.x, sys_status, status);
             float r2;
             if (MIXED) {
                 uint4 u = fixed_position(s, x);
@@ -399,6 +402,7 @@ __global__ void __launch_bounds__(VV_TILE) md_second_kernel(
             acc[i] = an;
         }
         vel[i] = v;
+        flag_nonfinite(v.x, v.y, v.z, tile.x, sys_status, status);
         if (s.thermostat != TH_NONE)
             ke = MIXED ? 0.5 * m * fma(v.x, v.x, fma(v.y, v.y, v.z * v.z))
                        : 0.5 * m * (v.x * v.x + v.y * v.y + v.z * v.z);
@@ -535,11 +539,11 @@ void launch_md_first(const Batch& b, bool adjust, cudaStream_t st) {
     if (b.precision == 1)
         md_first_kernel<true><<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.posq, b.vel, b.acc, b.pos_build,
                                                             b.pfx_build, b.adj, aj, b.perm, b.posfx, b.status,
-                                                            b.sys_rebuild);
+                                                            b.sys_rebuild, b.sys_status);
     else
         md_first_kernel<false><<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.posq, b.vel, b.acc, b.pos_build,
                                                              nullptr, b.adj, aj, nullptr, b.posfx, b.status,
-                                                             b.sys_rebuild);
+                                                             b.sys_rebuild, b.sys_status);
 }
 void launch_md_second(const Batch& b, cudaStream_t st) {
     if (!b.ntiles) return;
@@ -548,12 +552,12 @@ void launch_md_second(const Batch& b, cudaStream_t st) {
         md_second_kernel<true><<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.force, b.inv_mass, b.posq, b.vel,
                                                              b.acc, b.pos_build, b.pfx_build, b.kepart, b.mom,
                                                              b.md_count, gpw, b.perm, b.posfx, b.status,
-                                                             b.sys_rebuild);
+                                                             b.sys_rebuild, b.sys_status);
     else
         md_second_kernel<false><<<b.ntiles, VV_TILE, 0, st>>>(b.tiles, b.sys, b.force, nullptr, b.posq, b.vel,
                                                               b.acc, b.pos_build, nullptr, b.kepart, b.mom,
                                                               b.md_count, gpw, nullptr, b.posfx, b.status,
-                                                              b.sys_rebuild);
+                                                              b.sys_rebuild, b.sys_status);
 }
 void launch_md_adjust(const Batch& b, cudaStream_t st) {
     if (b.nsys)

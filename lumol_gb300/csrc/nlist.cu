@@ -155,7 +155,7 @@ __global__ void nl_bin_fixed_kernel(int nsys, const int* __restrict__ plan, cons
 // system).  A system's cells hold its atoms at [begin, end) of cell_atoms, and
 // its start array has one slot per cell plus an end sentinel, at
 // cell_start[cell + system index].  Also zeroes the counts for the scatter.
-__global__ void __launch_bounds__(1024) nl_scan_kernel(int nsys, const uint32_t* __restrict__ status,
+__global__ void __launch_bounds__(1024) nl_scan_kernel(int nsys, uint32_t* __restrict__ status,
                                                        const int* __restrict__ plan,
                                                        const SysDev* __restrict__ sys, int* __restrict__ cell_count,
                                                        int* __restrict__ cell_start) {
@@ -188,11 +188,20 @@ __global__ void __launch_bounds__(1024) nl_scan_kernel(int nsys, const uint32_t*
             run += count[c];
             count[c] = 0;
         }
-        if (t == (int)blockDim.x - 1) start[ncells] = d.begin + partial[t];
+        if (t == (int)blockDim.x - 1) {
+            start[ncells] = d.begin + partial[t];
+            // the counts must add up to the system's atoms: otherwise a build was
+            // interrupted between binning and sorting, and the scatter below would
+            // overrun the system's slice of cell_atoms
+            if (d.begin + partial[t] != d.end) atomicOr(status, ST_CELL_OVF);
+        }
     }
 }
 
-__global__ void nl_scatter_kernel(int nsys, const int* __restrict__ plan, const uint32_t* __restrict__ status,
+// Scatter of the atoms into their cells.  A slot beyond the cell's range (or
+// the system's slice) is never written: the status word gets ST_CELL_OVF and
+// the host recounts and rebuilds.
+__global__ void nl_scatter_kernel(int nsys, const int* __restrict__ plan, uint32_t* __restrict__ status,
                                   const SysDev* __restrict__ sys, const int* __restrict__ atom_cell,
                                   int* __restrict__ cell_count, const int* __restrict__ cell_start,
                                   int* __restrict__ cell_atoms) {
@@ -202,10 +211,15 @@ __global__ void nl_scatter_kernel(int nsys, const int* __restrict__ plan, const 
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < A; v += gridDim.x * blockDim.x) {
         int r = plan_find(pv.apre, pv.R, v);
         int s = pv.sys[r];
-        int i = sys[s].begin + (v - pv.apre[r]);
+        const SysDev& d = sys[s];
+        int i = d.begin + (v - pv.apre[r]);
         int c = atom_cell[i];
         int slot = atomicAdd(&cell_count[c], 1);
-        cell_atoms[cell_start[c + s] + slot] = i;
+        int at = cell_start[c + s] + slot;
+        if (at < cell_start[c + s + 1] && at >= d.begin && at < d.end)
+            cell_atoms[at] = i;
+        else
+            atomicOr(status, ST_CELL_OVF);
     }
 }
 

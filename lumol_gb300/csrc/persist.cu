@@ -144,6 +144,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
             p.z = fma(vel.z, sd.dt, p.z);
             b.vel[i] = vel;
             b.posq[i] = p;
+            flag_nonfinite(p.x, p.y, p.z, s, b.sys_status, b.status);
             uint4 u = fixed_position(sd, p);
             b.posfx[b.perm[i]] = u;
             if (fixed_dist2(u, b.pfx_build[i], sd.Lq) > sd.rebuild2_f) b.sys_rebuild[s] = 1u;
@@ -213,7 +214,13 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
                     run += count[c];
                     count[c] = 0;
                 }
-                if (t == PK_THREADS - 1) start[ncells] = sd.begin + s_part[t];
+                if (t == PK_THREADS - 1) {
+                    start[ncells] = sd.begin + s_part[t];
+                    if (sd.begin + s_part[t] != sd.end) {  // an interrupted earlier build left counts
+                        atomicOr(b.status, ST_CELL_OVF);
+                        a.group_flag[g] = 1;
+                    }
+                }
             }
             pk_sync(cluster);
             // 2c: scatter the atoms into their cells
@@ -223,7 +230,13 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
                 int i = b.sys[s].begin + (v - s_rapre[r]);
                 int c = b.atom_cell[i];
                 int slot = atomicAdd(&b.cell_count[c], 1);
-                b.cell_atoms[b.cell_start[c + s] + slot] = i;
+                int at = b.cell_start[c + s] + slot;
+                if (at < b.cell_start[c + s + 1] && at >= b.sys[s].begin && at < b.sys[s].end) {
+                    b.cell_atoms[at] = i;
+                } else {  // never written out of range: the host recounts and replays
+                    atomicOr(b.status, ST_CELL_OVF);
+                    a.group_flag[g] = 1;
+                }
             }
             pk_sync(cluster);
             // 2d: sort each cell by atom index (warp per cell), leave the counts at zero
@@ -394,6 +407,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
                     vel.z = fma(sd.hdt, ai.z, vel.z);
                     b.acc[i] = ai;
                     b.vel[i] = vel;
+                    flag_nonfinite(vel.x, vel.y, vel.z, s_sys[r], b.sys_status, b.status);
                     if (a.thermo) ke = 0.5 * vel.w * fma(vel.x, vel.x, fma(vel.y, vel.y, vel.z * vel.z));
                 }
                 if (a.thermo) {  // the chunk's kinetic energy, lanes in a fixed order

@@ -42,6 +42,25 @@ int regrow(lg_engine* e) {
     return LG_OK;
 }
 
+int recount_cells(lg_engine* e) {
+    int rc = clear_status_bits(e, ST_CELL_OVF);
+    if (rc) return rc;
+    CUDA_TRY(e, cudaMemsetAsync(e->cell_count.p, 0, (size_t)e->b.ncells * sizeof(int), e->stream));
+    launch_request_rebuild(e->b, e->stream);
+    return LG_OK;
+}
+
+std::string nonfinite_systems(lg_engine* e) {
+    std::vector<uint32_t> flags(e->nsys, 0u);
+    if (cudaMemcpy(flags.data(), e->sys_status.p, e->nsys * sizeof(uint32_t), cudaMemcpyDeviceToHost) !=
+        cudaSuccess)
+        return "?";
+    std::string out;
+    for (int s = 0; s < e->nsys; s++)
+        if (flags[s] & SYS_NONFINITE) out += (out.empty() ? "" : ", ") + std::to_string(s);
+    return out;
+}
+
 int read_status(lg_engine* e, uint32_t* out) {
     CUDA_TRY(e, cudaMemcpyAsync(e->h_status, e->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->stream));
     CUDA_TRY(e, cudaStreamSynchronize(e->stream));
@@ -104,6 +123,11 @@ int compute_batch(lg_engine* e, uint32_t terms, uint32_t want, double* d_force_o
         uint32_t status;
         int rc = read_status(e, &status);
         if (rc) return rc;
+        if (status & ST_CELL_OVF) {
+            rc = recount_cells(e);
+            if (rc) return rc;
+            continue;
+        }
         if (status & ST_OVERFLOW) {
             rc = clear_status_bits(e, ST_OVERFLOW);
             if (rc) return rc;
@@ -112,8 +136,10 @@ int compute_batch(lg_engine* e, uint32_t terms, uint32_t want, double* d_force_o
             continue;
         }
         if (status & ST_NONFINITE) {
-            clear_status_bits(e, ST_NONFINITE);
-            return fail(e, LG_ERR_NONFINITE, "Potential energy is infinite!");
+            rc = clear_status_bits(e, ST_NONFINITE);
+            if (rc) return rc;
+            if (want & LG_WANT_ENERGY)
+                return fail(e, LG_ERR_NONFINITE, "Potential energy is infinite! (system " + nonfinite_systems(e) + ")");
         }
         if (d_force_out)
             CUDA_TRY(e, cudaMemcpyAsync(d_force_out, e->force.p, 3 * (size_t)e->b.n * sizeof(double),
@@ -142,6 +168,7 @@ const void* mapped_host(const void* p) {
 // into the packed device state: read in place from page-locked buffers, else
 // staged through pos3 / vel3.
 int put_state(lg_engine* e, int64_t base, int64_t n, const double* positions, const double* velocities) {
+    e->shadow_valid = false;
     cudaStream_t st = e->stream;
     Batch sub = e->b;
     sub.n = (int)n;
@@ -195,6 +222,7 @@ int get_state(lg_engine* e, int64_t base, int64_t n, double* positions, double* 
 // Copies the host positions of system s into its slice of the device state;
 // the other systems keep theirs.
 int upload_positions(lg_engine* e, int32_t s, const double* positions) {
+    e->shadow_valid = false;
     const HostSystem& h = e->sys[s];
     if (h.n == 0) return LG_OK;
     int64_t base = e->begin[s];
@@ -487,16 +515,27 @@ int md_run_persistent(lg_engine* e, int64_t nsteps, bool thermo) {
         uint32_t status;
         int rc = read_status(e, &status);
         if (rc) return rc;
-        if (status & ST_OVERFLOW) {
+        if (status & (ST_OVERFLOW | ST_CELL_OVF)) {
             if (++retries > 4) return fail(e, LG_ERR_CAPACITY, "neighbour list overflow persisted after regrowing");
             CUDA_TRY(e, cudaMemcpyAsync(e->posq.p, e->cp_pos.p, bytes, cudaMemcpyDeviceToDevice, st));
             CUDA_TRY(e, cudaMemcpyAsync(e->vel.p, e->cp_vel.p, bytes, cudaMemcpyDeviceToDevice, st));
             CUDA_TRY(e, cudaMemcpyAsync(e->acc.p, e->cp_acc.p, bytes, cudaMemcpyDeviceToDevice, st));
-            rc = clear_status_bits(e, ST_OVERFLOW);
-            if (rc) return rc;
-            rc = regrow(e);
-            if (rc) return rc;
+            if (status & ST_CELL_OVF) {
+                rc = recount_cells(e);
+                if (rc) return rc;
+            }
+            if (status & ST_OVERFLOW) {
+                rc = clear_status_bits(e, ST_OVERFLOW);
+                if (rc) return rc;
+                rc = regrow(e);
+                if (rc) return rc;
+            }
             continue;
+        }
+        if (status & ST_NONFINITE) {  // reported after the run; the other systems are unaffected
+            e->nonfinite = true;
+            rc = clear_status_bits(e, ST_NONFINITE);
+            if (rc) return rc;
         }
         done += steps;
     }
