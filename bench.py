@@ -508,8 +508,9 @@ def main_serving(args, world, rank, local):
                                    f"60% LJ (200-20000 atoms), 25% NaCl+Ewald (216-8000 ions), 15% water "
                                    f"(300-3000 molecules), 500-5000 steps each", "kinds": kinds,
                        "precision": args.precision, "timing": "host wall clock over the stream (latency metric)",
-                       "lanes_max": server.stats.max_lanes, "lane_rebuilds": server.stats.lane_rebuilds,
-                       "rounds": server.stats.rounds},
+                       "lanes_max": server.stats.max_lanes, "lanes_opened": server.stats.lanes_opened,
+                       "joins": server.stats.joins, "leaves": server.stats.leaves,
+                       "chunks": server.stats.chunks},
             "latency_s": {"p50": p50, "p99": p99},
             "clocks": clk,
         }

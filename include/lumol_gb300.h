@@ -303,8 +303,31 @@ int lg_md_get_state(lg_engine* e, int32_t s, double* positions, double* velociti
 int lg_md_set_state_all(lg_engine* e, const double* positions, const double* velocities,
                         const double* accelerations);
 int lg_md_get_state_all(lg_engine* e, double* positions, double* velocities, double* accelerations);
-/* Runs `nsteps` steps of every system with device-resident state. */
+/* The same for system `s` with its accelerations (3n each; VelocityVerlet's
+ * a(t), Verlet's positions at t - dt), for a snapshot of a running system and
+ * its restore; `accelerations` may be NULL (set: zero after a description
+ * change, else kept; get: not read). */
+int lg_md_set_state_ex(lg_engine* e, int32_t s, const double* positions, const double* velocities,
+                       const double* accelerations);
+int lg_md_get_state_ex(lg_engine* e, int32_t s, double* positions, double* velocities, double* accelerations);
+/* Runs `nsteps` steps of every system with device-resident state.  A system
+ * whose positions or velocities became non-finite is flagged (see
+ * lg_system_status); the call still completes every system's steps and then
+ * returns LG_ERR_NONFINITE. */
 int lg_md_run(lg_engine* e, int64_t nsteps);
+
+/* ---- systems joining and leaving a batch -------------------------------------- */
+/* Appends `count` empty systems (indices n_systems .. n_systems + count - 1),
+ * to be described with lg_set_* and given a state with lg_md_set_state.  At
+ * the next use the batch is lowered again; the systems already there keep
+ * their device state (positions, velocities, accelerations, thermostat noise
+ * counters, Monte Carlo chains) and continue their trajectories.  Device
+ * buffers grow only when the batch exceeds the largest size it has had. */
+int lg_add_systems(lg_engine* e, int32_t count);
+/* Removes system `s`; the systems after it move down one index and, with the
+ * others, keep their device state.  Allocates nothing: buffers keep their
+ * capacity.  The last system of an engine cannot be removed (destroy it). */
+int lg_remove_system(lg_engine* e, int32_t s);
 /* Integrator::integrate for a single-system engine (integrators.rs:44-69): runs
  * `nsteps` steps from the host positions / velocities and copies them back.
  * The same as lg_md_propagate(..., LG_SYNC_DOWNLOAD): the host arrays are

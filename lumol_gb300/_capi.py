@@ -128,6 +128,10 @@ SIGNATURES = {
     "lg_md_set_state_all": (ctypes.c_int, [_P, _D, _D, _D]),
     "lg_md_get_state_all": (ctypes.c_int, [_P, _D, _D, _D]),
     "lg_md_run": (ctypes.c_int, [_P, ctypes.c_int64]),
+    "lg_md_set_state_ex": (ctypes.c_int, [_P, ctypes.c_int32, _D, _D, _D]),
+    "lg_md_get_state_ex": (ctypes.c_int, [_P, ctypes.c_int32, _D, _D, _D]),
+    "lg_add_systems": (ctypes.c_int, [_P, ctypes.c_int32]),
+    "lg_remove_system": (ctypes.c_int, [_P, ctypes.c_int32]),
     "lg_md_integrate": (ctypes.c_int, [_P, _D, _D, ctypes.c_int64]),
     "lg_md_propagate": (ctypes.c_int, [_P, _D, _D, ctypes.c_int64, ctypes.c_uint32]),
     "lg_system_status": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint32), ctypes.c_int32]),

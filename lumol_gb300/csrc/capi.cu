@@ -41,6 +41,7 @@ int lg_create(const lg_options* options, int32_t n_systems, lg_engine** out) {
     e->skin = opt.skin;
     e->nsys = n_systems;
     e->sys.resize(n_systems);
+    e->carry_from.assign(n_systems, -1);
     ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
     if (ce == cudaSuccess) ce = cudaMallocHost((void**)&e->h_status, sizeof(uint32_t));
     if (ce != cudaSuccess) {
@@ -92,6 +93,7 @@ int lg_set_particles(lg_engine* e, int32_t s, int64_t n, const int32_t* kinds, c
             return fail(e, LG_ERR_ARGUMENT, "molecules must be numbered contiguously in atom order");
     }
     h.md_ready = false;
+    if (s < (int)e->carry_from.size()) e->carry_from[s] = -1;  // new particles: no state to carry
     invalidate(e);
     return LG_OK;
 }
@@ -382,6 +384,7 @@ int lg_md_setup_ex(lg_engine* e, int32_t s, const lg_md_params* p) {
     h.controls = p->controls;
     h.md_ready = true;
     h.verlet_setup = p->integrator == LG_INTEGRATOR_VERLET;
+    h.reset_acc = e->dirty && p->integrator != LG_INTEGRATOR_VERLET;  // a carried system's, at the commit
     if (!e->dirty) {
         SysDev& d = e->h_sysdev[s];
         fill_md(d, h);
@@ -410,7 +413,9 @@ int lg_md_set_state(lg_engine* e, int32_t s, const double* positions, const doub
     if (h.n == 0) return LG_OK;
     rc = put_state(e, base, h.n, positions, velocities);  // this system's atoms only
     if (rc) return rc;
-    if (was_dirty) CUDA_TRY(e, cudaMemsetAsync(e->acc.p, 0, e->b.n * sizeof(double4_32a), st));
+    // a new state after a description change starts from zero accelerations
+    // (systems carried through the change keep theirs)
+    if (was_dirty) CUDA_TRY(e, cudaMemsetAsync(e->acc.p + base, 0, h.n * sizeof(double4_32a), st));
     CUDA_TRY(e, cudaGetLastError());
     CUDA_TRY(e, cudaStreamSynchronize(st));
     return LG_OK;
@@ -428,6 +433,68 @@ int lg_md_get_state(lg_engine* e, int32_t s, double* positions, double* velociti
     if (rc) return rc;
     CUDA_TRY(e, cudaGetLastError());
     CUDA_TRY(e, cudaStreamSynchronize(st));
+    return LG_OK;
+}
+
+int lg_md_set_state_ex(lg_engine* e, int32_t s, const double* positions, const double* velocities,
+                       const double* accelerations) {
+    int rc = lg_md_set_state(e, s, positions, velocities);
+    if (rc || !accelerations) return rc;
+    const HostSystem& h = e->sys[s];
+    if (h.n == 0) return LG_OK;
+    int64_t base = e->begin[s];
+    cudaStream_t st = e->stream;
+    CUDA_TRY(e, cudaMemcpyAsync(e->pos3.p + 3 * base, accelerations, 3 * h.n * sizeof(double),
+                                cudaMemcpyHostToDevice, st));
+    launch_pack_vectors((int)h.n, e->pos3.p + 3 * base, e->acc.p + base, st);
+    e->launches += 1;
+    CUDA_TRY(e, cudaGetLastError());
+    CUDA_TRY(e, cudaStreamSynchronize(st));
+    return LG_OK;
+}
+
+int lg_md_get_state_ex(lg_engine* e, int32_t s, double* positions, double* velocities, double* accelerations) {
+    int rc = lg_md_get_state(e, s, positions, velocities);
+    if (rc || !accelerations) return rc;
+    const HostSystem& h = e->sys[s];
+    if (h.n == 0) return LG_OK;
+    int64_t base = e->begin[s];
+    cudaStream_t st = e->stream;
+    launch_unpack_vectors((int)h.n, e->acc.p + base, e->pos3.p + 3 * base, st);
+    e->launches += 1;
+    CUDA_TRY(e, cudaMemcpyAsync(accelerations, e->pos3.p + 3 * base, 3 * h.n * sizeof(double),
+                                cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(e, cudaGetLastError());
+    CUDA_TRY(e, cudaStreamSynchronize(st));
+    return LG_OK;
+}
+
+int lg_add_systems(lg_engine* e, int32_t count) {
+    if (!e || count <= 0) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    if (e->carry_from.size() != (size_t)e->nsys) e->carry_from.assign(e->nsys, -1);
+    e->sys.resize(e->nsys + count);
+    e->carry_from.resize(e->nsys + count, -1);
+    if (e->h_mc.size() == (size_t)e->nsys) e->h_mc.resize(e->nsys + count, McState{});
+    e->nsys += count;
+    invalidate(e);
+    return LG_OK;
+}
+
+int lg_remove_system(lg_engine* e, int32_t s) {
+    if (!valid_sys(e, s)) return fail(e, LG_ERR_ARGUMENT, "invalid system index");
+    if (e->nsys == 1) return fail(e, LG_ERR_ARGUMENT, "an engine keeps at least one system");
+    if (e->carry_from.size() != (size_t)e->nsys) e->carry_from.assign(e->nsys, -1);
+    e->sys.erase(e->sys.begin() + s);
+    e->carry_from.erase(e->carry_from.begin() + s);
+    if (e->h_mc.size() == (size_t)e->nsys) e->h_mc.erase(e->h_mc.begin() + s);
+    if (e->mc_sys == s) {
+        e->mc_sys = -1;
+        e->mc_pending = false;
+    } else if (e->mc_sys > s) {
+        e->mc_sys -= 1;
+    }
+    e->nsys -= 1;
+    invalidate(e);
     return LG_OK;
 }
 

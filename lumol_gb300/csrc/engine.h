@@ -45,21 +45,31 @@ extern thread_local std::string g_create_error;
 extern std::mutex g_tune_mutex;
 extern std::map<std::tuple<int, int, int, int, int, bool>, std::pair<int, int>> g_tune_cache;
 
+// A device buffer that keeps its memory when asked for no more than it holds:
+// a batch that shrinks (a system leaves) or is re-lowered at the same size
+// allocates nothing; only growth calls cudaMalloc.  The contents are kept when
+// the memory is kept.
 template <class T>
 struct DBuf {
     T* p = nullptr;
-    size_t n = 0;
+    size_t n = 0;    // elements in use
+    size_t cap = 0;  // elements allocated
     ~DBuf() { release(); }
     void release() {
         if (p) cudaFree(p);
         p = nullptr;
         n = 0;
+        cap = 0;
     }
     cudaError_t alloc(size_t count) {
-        release();
         if (count == 0) count = 1;
+        if (p && count <= cap) {
+            n = count;
+            return cudaSuccess;
+        }
+        release();
         cudaError_t e = cudaMalloc((void**)&p, count * sizeof(T));
-        if (e == cudaSuccess) n = count;
+        if (e == cudaSuccess) n = cap = count;
         return e;
     }
 };
@@ -97,6 +107,7 @@ struct HostSystem {
     uint64_t seed = 0;
     bool md_ready = false;
     bool verlet_setup = false;  // Verlet::setup runs at the next lg_md_run
+    bool reset_acc = false;     // VelocityVerlet / LeapFrog::setup zeroes the accelerations at the next commit
     // derived
     std::vector<int64_t> mol_begin;  // first atom of each molecule (local index), plus the end
     double tail_energy = 0.0, tail_virial = 0.0, ewald_self = 0.0;
@@ -115,6 +126,10 @@ struct lg_engine {
     cudaStream_t stream = nullptr;
     bool dirty = true;
     std::vector<int64_t> begin;  // atom offsets (nsys + 1)
+    // Systems that join or leave keep the others' device state: carry_from[s]
+    // is the index system s had at the last commit (-1: new or re-described
+    // particles, its state comes from the next lg_md_set_state).
+    std::vector<int> carry_from;
     double skin = 1.0;
 
     Batch b;

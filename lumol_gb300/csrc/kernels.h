@@ -142,6 +142,7 @@ void launch_md_finalize(const Batch& b, cudaStream_t st);
 void launch_rewrap(const Batch& b, cudaStream_t st);
 void launch_verlet_setup(const Batch& b, int s, int begin, int end, cudaStream_t st);
 void launch_request_rebuild(const Batch& b, cudaStream_t st);
+void launch_carry_vectors(const double4_32a* src, double4_32a* dst, int n, bool keep_w, cudaStream_t st);
 void launch_check_displacement(const Batch& b, cudaStream_t st);
 
 // mc.cu

@@ -327,16 +327,70 @@ int commit(lg_engine* e) {
     if (!e->dirty) return LG_OK;
     e->shadow_valid = false;
     int nsys = e->nsys;
-    e->begin.assign(nsys + 1, 0);
+    const std::vector<int64_t> old_begin = e->begin;
+    const int old_n = e->b.n, old_nsys = e->b.nsys;
+    std::vector<int64_t> new_begin(nsys + 1, 0);
     for (int s = 0; s < nsys; s++) {
         const HostSystem& h = e->sys[s];
         if (!h.has_cell) return fail(e, LG_ERR_STATE, "system " + std::to_string(s) + " has no cell");
         if (h.nk == 0 && h.n > 0)
             return fail(e, LG_ERR_STATE, "system " + std::to_string(s) + " has no pair table");
-        e->begin[s + 1] = e->begin[s] + h.n;
+        new_begin[s + 1] = new_begin[s] + h.n;
     }
-    int64_t n = e->begin[nsys];
+    int64_t n = new_begin[nsys];
     if (n > (int64_t)0x7fffffff / 64) return fail(e, LG_ERR_ARGUMENT, "too many atoms");
+    cudaStream_t st = e->stream;
+
+    // Systems that stay (carry_from) keep their positions, velocities,
+    // accelerations, thermostat counters, status flags and Monte Carlo chains
+    // through the re-lowering: staged here, put back at their new offsets at
+    // the end.  The staging reuses the checkpoint buffers when the batch does
+    // not grow, so a system leaving allocates nothing.
+    std::vector<int> carry(nsys, -1);
+    bool any_carry = false;
+    if (old_n > 0 && (int)old_begin.size() == old_nsys + 1) {
+        for (int s = 0; s < nsys && s < (int)e->carry_from.size(); s++) {
+            int o = e->carry_from[s];
+            if (o >= 0 && o < old_nsys && old_begin[o + 1] - old_begin[o] == e->sys[s].n) {
+                carry[s] = o;
+                any_carry = true;
+            }
+        }
+    }
+    DBuf<double4_32a> tpos, tvel, tacc;
+    double4_32a *sp = nullptr, *sv = nullptr, *sa = nullptr;
+    std::vector<unsigned long long> old_count;
+    std::vector<uint32_t> old_status;
+    std::vector<McState> old_mc;
+    if (any_carry) {
+        if ((size_t)n <= e->cp_pos.cap && (size_t)n <= e->cp_vel.cap && (size_t)n <= e->cp_acc.cap) {
+            sp = e->cp_pos.p;
+            sv = e->cp_vel.p;
+            sa = e->cp_acc.p;
+        } else {
+            CUDA_TRY(e, tpos.alloc(old_n));
+            CUDA_TRY(e, tvel.alloc(old_n));
+            CUDA_TRY(e, tacc.alloc(old_n));
+            sp = tpos.p;
+            sv = tvel.p;
+            sa = tacc.p;
+        }
+        size_t bytes = (size_t)old_n * sizeof(double4_32a);
+        CUDA_TRY(e, cudaMemcpyAsync(sp, e->posq.p, bytes, cudaMemcpyDeviceToDevice, st));
+        CUDA_TRY(e, cudaMemcpyAsync(sv, e->vel.p, bytes, cudaMemcpyDeviceToDevice, st));
+        CUDA_TRY(e, cudaMemcpyAsync(sa, e->acc.p, bytes, cudaMemcpyDeviceToDevice, st));
+        old_count.resize(old_nsys);
+        old_status.resize(old_nsys);
+        old_mc.resize(old_nsys);
+        CUDA_TRY(e, cudaMemcpyAsync(old_count.data(), e->md_count.p, old_nsys * sizeof(unsigned long long),
+                                    cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(e, cudaMemcpyAsync(old_status.data(), e->sys_status.p, old_nsys * sizeof(uint32_t),
+                                    cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(e, cudaMemcpyAsync(old_mc.data(), e->mc_chains.p, old_nsys * sizeof(McState),
+                                    cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(e, cudaStreamSynchronize(st));
+    }
+    e->begin = new_begin;
 
     std::vector<double4_32a> h_posq(n), h_vel(n);
     std::vector<int> h_kind(n), h_mol(n), h_sysid(n);
@@ -716,7 +770,6 @@ int commit(lg_engine* e) {
     CUDA_TRY(e, e->kred.alloc((size_t)nkv * 7));
     CUDA_TRY(e, e->fpart.alloc(nkv ? (size_t)max_chunks * 3 * n : 1));
 
-    cudaStream_t st = e->stream;
     CUDA_TRY(e, cudaMemcpyAsync(e->posq.p, h_posq.data(), n * sizeof(double4_32a), cudaMemcpyHostToDevice, st));
     CUDA_TRY(e, cudaMemcpyAsync(e->vel.p, h_vel.data(), n * sizeof(double4_32a), cudaMemcpyHostToDevice, st));
     CUDA_TRY(e, cudaMemsetAsync(e->acc.p, 0, n * sizeof(double4_32a), st));
@@ -849,6 +902,11 @@ int commit(lg_engine* e) {
     b.adj = e->adj.p;
     b.nmol = (int)h_mol_start.size() - 1;
     b.mol_start = e->mol_start.p;
+    if (any_carry) {  // the chains of the systems that stay; the others' as lg_mc_setup left them
+        e->h_mc.resize(nsys, McState{});
+        for (int s = 0; s < nsys; s++)
+            if (carry[s] >= 0) e->h_mc[s] = old_mc[carry[s]];
+    }
     if (e->h_mc.size() != (size_t)nsys) e->h_mc.assign(nsys, McState{});
     CUDA_TRY(e, e->mc_chains.alloc(nsys));
     CUDA_TRY(e, cudaMemcpy(e->mc_chains.p, e->h_mc.data(), nsys * sizeof(McState), cudaMemcpyHostToDevice));
@@ -868,6 +926,35 @@ int commit(lg_engine* e) {
     b.kvecf = e->kvecf.p;
     b.eikrf = e->eikrf.p;
     b.rhof = e->rhof.p;
+    if (any_carry) {
+        std::vector<unsigned long long> count(nsys, 0ull);
+        std::vector<uint32_t> status(nsys, 0u);
+        for (int s = 0; s < nsys; s++) {
+            int o = carry[s];
+            if (o < 0) continue;
+            int m = (int)e->sys[s].n;
+            // x, v and a at the new offsets (charges and masses from the new description)
+            launch_carry_vectors(sp + old_begin[o], e->posq.p + new_begin[s], m, true, st);
+            launch_carry_vectors(sv + old_begin[o], e->vel.p + new_begin[s], m, true, st);
+            launch_carry_vectors(sa + old_begin[o], e->acc.p + new_begin[s], m, false, st);
+            count[s] = old_count[o];
+            status[s] = old_status[o];
+        }
+        CUDA_TRY(e, cudaMemcpyAsync(e->md_count.p, count.data(), nsys * sizeof(unsigned long long),
+                                    cudaMemcpyHostToDevice, st));
+        CUDA_TRY(e, cudaMemcpyAsync(e->sys_status.p, status.data(), nsys * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                    st));
+    }
+    for (int s = 0; s < nsys; s++) {  // VelocityVerlet / LeapFrog::setup of a carried system
+        HostSystem& h = e->sys[s];
+        if (h.reset_acc && carry[s] >= 0 && h.n)
+            CUDA_TRY(e, cudaMemsetAsync(e->acc.p + new_begin[s], 0, h.n * sizeof(double4_32a), st));
+        h.reset_acc = false;
+    }
+    CUDA_TRY(e, cudaGetLastError());
+    CUDA_TRY(e, cudaStreamSynchronize(st));  // the staging buffers are released on return
+    e->carry_from.resize(nsys);
+    for (int s = 0; s < nsys; s++) e->carry_from[s] = s;
     e->dirty = false;
     e->tuned = false;
     e->pk_cluster = 0;

@@ -576,6 +576,20 @@ void launch_verlet_setup(const Batch& b, int s, int begin, int end, cudaStream_t
     if (end > begin)
         verlet_setup_kernel<<<(end - begin + 255) / 256, 256, 0, st>>>(begin, end, b.sys, s, b.posq, b.vel, b.acc);
 }
+// A system's x, y, z (and w unless keep_w: the charge or mass of the new
+// description stays) moved to its new offset when the batch changes.
+__global__ void carry_vectors_kernel(int n, const double4_32a* __restrict__ src, double4_32a* __restrict__ dst,
+                                     int keep_w) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double4_32a v = src[i];
+    if (keep_w) v.w = dst[i].w;
+    dst[i] = v;
+}
+void launch_carry_vectors(const double4_32a* src, double4_32a* dst, int n, bool keep_w, cudaStream_t st) {
+    if (n > 0) carry_vectors_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, src, dst, keep_w ? 1 : 0);
+}
+
 void launch_request_rebuild(const Batch& b, cudaStream_t st) {
     request_rebuild_kernel<<<1, 256, 0, st>>>(b.nsys, b.status, b.sys_rebuild);
 }

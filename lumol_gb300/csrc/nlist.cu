@@ -182,17 +182,20 @@ __global__ void __launch_bounds__(1024) nl_scan_kernel(int nsys, uint32_t* __res
             partial[t] += v;
             __syncthreads();
         }
+        // Every start is clamped to the system's slice [begin, end] of cell_atoms.
+        // The counts add up to the system's atoms unless a build was interrupted
+        // between binning and sorting (stale counts, only ever too large): then
+        // the status word gets ST_CELL_OVF and the clamped ranges keep every later
+        // kernel of this build (scatter, sort, sorted order, rows) inside the
+        // slice; the host recounts and rebuilds before the list is used.
         int run = d.begin + partial[t] - sum;
         for (int c = lo; c < hi; c++) {
-            start[c] = run;
+            start[c] = min(run, d.end);
             run += count[c];
             count[c] = 0;
         }
         if (t == (int)blockDim.x - 1) {
-            start[ncells] = d.begin + partial[t];
-            // the counts must add up to the system's atoms: otherwise a build was
-            // interrupted between binning and sorting, and the scatter below would
-            // overrun the system's slice of cell_atoms
+            start[ncells] = min(d.begin + partial[t], d.end);
             if (d.begin + partial[t] != d.end) atomicOr(status, ST_CELL_OVF);
         }
     }

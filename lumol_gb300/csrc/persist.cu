@@ -208,15 +208,18 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
                     s_part[t] += x;
                     __syncthreads();
                 }
+                // starts clamped to the system's slice of cell_atoms: stale counts
+                // (an interrupted earlier build) keep every later pass in bounds,
+                // flag the group, and the host recounts and replays
                 int run = sd.begin + s_part[t] - sum;
                 for (int c = lo; c < hi; c++) {
-                    start[c] = run;
+                    start[c] = min(run, sd.end);
                     run += count[c];
                     count[c] = 0;
                 }
                 if (t == PK_THREADS - 1) {
-                    start[ncells] = sd.begin + s_part[t];
-                    if (sd.begin + s_part[t] != sd.end) {  // an interrupted earlier build left counts
+                    start[ncells] = min(sd.begin + s_part[t], sd.end);
+                    if (sd.begin + s_part[t] != sd.end) {
                         atomicOr(b.status, ST_CELL_OVF);
                         a.group_flag[g] = 1;
                     }

@@ -1,37 +1,44 @@
 """A continuous-batching MD server on one GPU.
 
 Requests (a Lumol system and a number of Velocity-Verlet steps) arrive over
-time.  The server keeps their state resident on the device and advances them
-in rounds:
+time.  The server keeps their state resident on the device:
 
-* every round, each lane (one engine holding a batch of requests, on its own
-  CUDA stream) runs `chunk` steps; lanes run concurrently, so the work of
-  requests admitted at different times overlaps on the device;
-* at a round boundary, finished requests are read back and retired (a lane
-  that lost requests is rebuilt around the remaining ones, carrying positions,
-  velocities and accelerations over exactly), and requests that have arrived
-  are admitted as a new lane, as long as their estimated device footprint fits
-  in the free HBM (cudaMemGetInfo) minus a reserve, and the lane count is below
-  its limit; the rest wait;
-* small lanes are merged when there are too many of them.
+* a lane is one engine holding a batch of requests on its own CUDA stream,
+  stepped by its own host thread in chunks of `chunk` steps; lanes step
+  independently (a lane never waits for another one), so the work of requests
+  admitted at different times overlaps on the device;
+* an arriving request joins the least loaded lane with room (lg_add_systems:
+  the requests already there keep their device state and continue), or opens
+  a new lane while there are fewer than `max_lanes`; it is admitted only when
+  its estimated device footprint fits in the free HBM (cudaMemGetInfo) minus a
+  reserve, and in the optional memory budget; otherwise it waits;
+* between two chunks a lane retires the requests that finished (their state is
+  read back and they leave in place with lg_remove_system, which allocates
+  nothing), takes in the requests that joined, drops cancelled ones and takes
+  snapshots;
+* a request whose state becomes non-finite (the reference panics there,
+  lumol-core/src/sys/compute.rs:125,141) fails alone: the engine flags it
+  (lg_system_status), it leaves its lane with an error, and the other
+  requests of the lane continue from the same chunk.
 
 Each system's arithmetic depends only on its own atoms (per-atom gathers,
-per-system list rebuilds and reductions), so a request gives the same result
-alone and in the mix, within the stated tolerance (tests/test_gpu_serving.py).
+per-system list rebuilds and reductions, a fixed group width per atom), so a
+request gives the same result alone and in the mix, within the stated
+tolerance (tests/test_gpu_serving.py).
 """
 from __future__ import annotations
 
-import concurrent.futures
 import ctypes
 import math
+import queue
+import threading
 import time
 from dataclasses import dataclass, field
 
 import numpy as np
 
 from . import _capi as C
-from .batch import Batch
-from .system import System
+from .system import Engine, System, md_params, VelocityVerlet
 
 
 @dataclass
@@ -42,12 +49,17 @@ class Request:
     timestep: float
     arrival: float = 0.0          # seconds after the server started
     kind: str = ""
+    # a snapshot to resume from: (positions, velocities, accelerations, steps done)
+    restore: tuple | None = None
     # filled by the server
     admitted: float | None = None
     finished: float | None = None
     steps_done: int = 0
     positions: np.ndarray | None = None
     velocities: np.ndarray | None = None
+    error: str | None = None
+    cancelled: bool = False
+    snapshot: tuple | None = None  # (positions, velocities, accelerations, steps done), on request
 
     @property
     def latency(self) -> float:
@@ -75,39 +87,161 @@ def footprint_bytes(system: System, precision: str, skin: float = 1.0) -> int:
 
 
 class Lane:
-    """One engine holding a batch of requests."""
+    """One engine holding a batch of requests, stepped by its own thread."""
 
-    def __init__(self, requests: list[Request], precision: str, threads_per_atom: int, states=None):
-        self.requests = requests
-        self.batch = Batch([r.system for r in requests], precision=precision, threads_per_atom=threads_per_atom)
-        self.batch.md_setup([r.timestep for r in requests])
-        if states is not None:
-            pos = np.ascontiguousarray(np.concatenate([s[0] for s in states]))
-            vel = np.ascontiguousarray(np.concatenate([s[1] for s in states]))
-            acc = np.ascontiguousarray(np.concatenate([s[2] for s in states]))
-            self.batch.engine.call("lg_md_set_state_all", C.dptr(pos), C.dptr(vel), C.dptr(acc))
+    def __init__(self, server: "Server", first: list[Request]):
+        self.server = server
+        self.requests: list[Request] = []
+        self.engine: Engine | None = None
+        self.joining: list[Request] = list(first)
+        self.cancel: set[int] = set()
+        self.snap: set[int] = set()
+        self.lock = threading.Lock()
+        self.open = True           # accepts joins; closed by its thread when it runs empty
+        self.atoms = sum(r.system.size for r in first)
+        self.thread = threading.Thread(target=self._serve, daemon=True)
 
-    def states(self):
-        n = self.batch.atoms
-        pos, vel, acc = np.zeros((n, 3)), np.zeros((n, 3)), np.zeros((n, 3))
-        self.batch.engine.call("lg_md_get_state_all", C.dptr(pos), C.dptr(vel), C.dptr(acc))
-        off = self.batch.offsets
-        return [(pos[off[k]:off[k + 1]], vel[off[k]:off[k + 1]], acc[off[k]:off[k + 1]])
-                for k in range(len(self.requests))]
+    # ---- called by the server thread (under self.lock) ------------------------------
+    def try_join(self, r: Request) -> bool:
+        with self.lock:
+            if not self.open:
+                return False
+            self.joining.append(r)
+            self.atoms += r.system.size
+            return True
 
-    def steps_left(self) -> int:
-        return min(r.nsteps - r.steps_done for r in self.requests)
+    # ---- the lane's own thread ---------------------------------------------------------
+    def _take_joins(self) -> None:
+        with self.lock:
+            joins, self.joining = self.joining, []
+        if not joins:
+            return
+        if self.engine is None:
+            self.engine = Engine(len(joins), self.server.precision, threads_per_atom=self.server.tpa)
+            first = 0
+        else:
+            first = len(self.requests)
+            self.engine.call("lg_add_systems", len(joins))
+        eng = self.engine
+        for k, r in enumerate(joins):
+            s = first + k
+            r.system._lower_into(eng, s)
+            p = md_params(VelocityVerlet(r.timestep))
+            eng.call("lg_md_setup_ex", s, ctypes.byref(p))
+        for k, r in enumerate(joins):
+            s = first + k
+            if r.restore is not None:
+                x, v, a, done = r.restore
+                r.steps_done = int(done)
+                eng.call("lg_md_set_state_ex", s, C.dptr(np.ascontiguousarray(x, dtype=np.float64)),
+                         C.dptr(np.ascontiguousarray(v, dtype=np.float64)),
+                         C.dptr(np.ascontiguousarray(a, dtype=np.float64)))
+            else:
+                v = r.system.velocities if r.system.velocities is not None else np.zeros((r.system.size, 3))
+                eng.call("lg_md_set_state", s, C.dptr(np.ascontiguousarray(r.system.positions)),
+                         C.dptr(np.ascontiguousarray(v, dtype=np.float64)))
+        self.requests += joins
+        self.server.stats.joins += len(joins)
 
-    def close(self) -> None:
-        self.batch.engine.close()
+    def _state(self, s: int, with_acc: bool = False):
+        n = self.requests[s].system.size
+        x, v = np.zeros((n, 3)), np.zeros((n, 3))
+        a = np.zeros((n, 3)) if with_acc else None
+        self.engine.call("lg_md_get_state_ex", s, C.dptr(x), C.dptr(v), C.dptr(a) if with_acc else None)
+        return x, v, a
+
+    def _leave(self, indices: list[int]) -> None:
+        for s in sorted(indices, reverse=True):
+            r = self.requests[s]
+            if len(self.requests) > 1:
+                self.engine.call("lg_remove_system", s)
+                self.server.stats.leaves += 1
+            else:  # the engine keeps at least one system: the lane closes with it
+                self.engine.close()
+                self.engine = None
+            del self.requests[s]
+            with self.lock:
+                self.atoms -= r.system.size
+
+    def _boundary(self) -> None:
+        """Retirement, cancellation and snapshots between two chunks."""
+        now = self.server.now()
+        leave = []
+        with self.lock:
+            cancel, self.cancel = self.cancel, set()
+            snap, self.snap = self.snap, set()
+        for s, r in enumerate(self.requests):
+            if r.rid in snap:
+                x, v, a = self._state(s, with_acc=True)
+                r.snapshot = (x, v, a, r.steps_done)
+            if r.error is not None:
+                leave.append(s)
+            elif r.rid in cancel:
+                r.cancelled = True
+                r.finished = now
+                leave.append(s)
+            elif r.steps_done >= r.nsteps:
+                r.positions, r.velocities, _ = self._state(s)
+                r.finished = now
+                leave.append(s)
+        for s in leave:
+            self.server._complete(self.requests[s])
+        if leave:
+            self._leave(leave)
+
+    def _serve(self) -> None:
+        try:
+            while True:
+                self._take_joins()
+                if not self.requests:
+                    with self.lock:
+                        if not self.joining:
+                            self.open = False
+                            break
+                    continue
+                steps = min(self.server.chunk, min(r.nsteps - r.steps_done for r in self.requests))
+                steps = max(steps, 0)
+                code = self.engine.lib.lg_md_run(self.engine.handle, steps)
+                if code == C.LG_ERR_NONFINITE:
+                    flags = (ctypes.c_uint32 * len(self.requests))()
+                    self.engine.call("lg_system_status", flags, 1)
+                    for s, r in enumerate(self.requests):
+                        if flags[s] & C.LG_SYS_NONFINITE:
+                            r.error = "non-finite positions or velocities (Kinetic energy is infinite!)"
+                            r.finished = self.server.now()
+                    self.server.stats.failed += sum(1 for f in flags if f & C.LG_SYS_NONFINITE)
+                elif code != C.LG_OK:
+                    C.check(code, self.engine.handle)
+                for r in self.requests:
+                    if r.error is None:
+                        r.steps_done += steps
+                        self.server.stats.atom_steps += steps * r.system.size
+                self.server.stats.chunks += 1
+                self._boundary()
+        except BaseException as exc:  # a lane that fails reports every request it holds
+            with self.lock:
+                self.open = False
+                pending = self.requests + self.joining
+                self.requests, self.joining = [], []
+            for r in pending:
+                if r.finished is None:
+                    r.error = f"lane failed: {exc}"
+                    r.finished = self.server.now()
+                    self.server._complete(r)
+            if self.engine is not None:
+                self.engine.close()
+                self.engine = None
 
 
 @dataclass
 class ServerStats:
-    rounds: int = 0
-    lane_rebuilds: int = 0
+    chunks: int = 0
+    lanes_opened: int = 0
     max_lanes: int = 0
+    joins: int = 0
+    leaves: int = 0
     waited_for_memory: int = 0
+    failed: int = 0
     atom_steps: int = 0
 
 
@@ -115,120 +249,139 @@ class Server:
     """Continuous batching of MD requests on one GPU."""
 
     def __init__(self, precision: str = "mixed", chunk: int = 50, max_lanes: int = 4,
-                 memory_budget: int | None = None, reserve_bytes: int = 1 << 30, threads_per_atom: int = 8):
+                 memory_budget: int | None = None, reserve_bytes: int = 1 << 30, threads_per_atom: int = 8,
+                 lane_atoms: int = 400_000):
         self.precision = precision
         self.chunk = chunk
         self.max_lanes = max_lanes
         self.memory_budget = memory_budget
         self.reserve = reserve_bytes
         self.tpa = threads_per_atom
+        self.lane_atoms = lane_atoms
         self.lanes: list[Lane] = []
         self.stats = ServerStats()
-        self.pool = concurrent.futures.ThreadPoolExecutor(max_workers=max(2, max_lanes + 1))
+        self._done: queue.Queue = queue.Queue()
+        self._t0 = time.perf_counter()
+        self._active: dict[int, Request] = {}
+        self._lock = threading.Lock()
 
-    # ---- admission ---------------------------------------------------------------------
+    def now(self) -> float:
+        return time.perf_counter() - self._t0
+
+    def _complete(self, r: Request) -> None:
+        with self._lock:
+            self._active.pop(r.rid, None)
+        self._done.put(r)
+
+    # ---- controls -------------------------------------------------------------------
+    def cancel(self, rid: int) -> None:
+        """Stops request `rid` at its lane's next chunk boundary."""
+        for lane in list(self.lanes):
+            with lane.lock:
+                if any(r.rid == rid for r in lane.requests + lane.joining):
+                    lane.cancel.add(rid)
+
+    def snapshot(self, rid: int) -> None:
+        """Asks for request `rid`'s state at its lane's next chunk boundary
+        (Request.snapshot; resume it with Request(restore=snapshot))."""
+        for lane in list(self.lanes):
+            with lane.lock:
+                if any(r.rid == rid for r in lane.requests + lane.joining):
+                    lane.snap.add(rid)
+
+    # ---- admission --------------------------------------------------------------------
     def _free_bytes(self) -> int:
         import torch
         free, _ = torch.cuda.mem_get_info()
+        free -= self.reserve
         if self.memory_budget is not None:
-            used = sum(footprint_bytes(r.system, self.precision) for lane in self.lanes for r in lane.requests)
+            with self._lock:
+                used = sum(footprint_bytes(r.system, self.precision) for r in self._active.values())
             free = min(free, self.memory_budget - used)
-        return free - self.reserve
+        return free
 
-    def _admit(self, waiting: list[Request], now: float) -> list[Request]:
-        ready = [r for r in waiting if r.arrival <= now]
-        if not ready or len(self.lanes) >= self.max_lanes:
-            return waiting
-        free = self._free_bytes()
-        chosen = []
-        for r in ready:
-            need = footprint_bytes(r.system, self.precision)
-            if need <= free:
-                chosen.append(r)
-                free -= need
-            else:
-                self.stats.waited_for_memory += 1
-        if chosen:
-            for r in chosen:
-                r.admitted = now
-            self.lanes.append(Lane(chosen, self.precision, self.tpa))
-        return [r for r in waiting if r not in chosen]
-
-    # ---- retirement and lane maintenance -------------------------------------------------
-    def _retire(self, now_fn) -> list[Request]:
-        done = []
-        new_lanes = []
-        for lane in self.lanes:
-            finished = [k for k, r in enumerate(lane.requests) if r.steps_done >= r.nsteps]
-            if not finished:
-                new_lanes.append(lane)
+    def _admit(self, waiting: list[Request]) -> list[Request]:
+        now = self.now()
+        self.lanes = [lane for lane in self.lanes if lane.open or lane.thread.is_alive()]
+        rest = []
+        free = None
+        for r in waiting:
+            if r.arrival > now:
+                rest.append(r)
                 continue
-            states = lane.states()
-            t = now_fn()
-            for k in finished:
-                r = lane.requests[k]
-                r.positions, r.velocities = states[k][0].copy(), states[k][1].copy()
-                r.finished = t
-                done.append(r)
-            keep = [k for k in range(len(lane.requests)) if k not in finished]
-            lane.close()
-            if keep:
-                new_lanes.append(Lane([lane.requests[k] for k in keep], self.precision, self.tpa,
-                                      [states[k] for k in keep]))
-                self.stats.lane_rebuilds += 1
-        self.lanes = new_lanes
-        return done
+            if free is None:
+                free = self._free_bytes()
+            need = footprint_bytes(r.system, self.precision)
+            if need > free:
+                self.stats.waited_for_memory += 1
+                rest.append(r)
+                continue
+            placed = False
+            for lane in sorted((l for l in self.lanes if l.open), key=lambda l: l.atoms):
+                if lane.atoms + r.system.size <= self.lane_atoms and lane.try_join(r):
+                    placed = True
+                    break
+            if not placed and len([l for l in self.lanes if l.open]) < self.max_lanes:
+                lane = Lane(self, [r])
+                self.lanes.append(lane)
+                self.stats.lanes_opened += 1
+                lane.thread.start()
+                placed = True
+            if not placed:
+                rest.append(r)
+                continue
+            r.admitted = now
+            with self._lock:
+                self._active[r.rid] = r
+            free -= need
+        self.stats.max_lanes = max(self.stats.max_lanes, len([l for l in self.lanes if l.open]))
+        return rest
 
-    def _merge(self) -> None:
-        while len(self.lanes) > self.max_lanes - 1 and len(self.lanes) >= 2:
-            self.lanes.sort(key=lambda lane: lane.batch.atoms)
-            a, b = self.lanes[0], self.lanes[1]
-            reqs = a.requests + b.requests
-            states = a.states() + b.states()
-            a.close()
-            b.close()
-            self.lanes = self.lanes[2:] + [Lane(reqs, self.precision, self.tpa, states)]
-            self.stats.lane_rebuilds += 1
-
-    # ---- the loop ----------------------------------------------------------------------
-    def run(self, requests: list[Request]) -> list[Request]:
+    # ---- the loop ---------------------------------------------------------------------
+    def run(self, requests: list[Request], on_start=None) -> list[Request]:
         """Serves `requests` (arrival times in seconds from now) and returns
-        them completed, in completion order."""
+        them completed (finished, cancelled or failed), in completion order.
+        `on_start(server)`, if given, runs once the first requests are admitted
+        (tests use it to cancel or snapshot requests while they run)."""
+        self._t0 = time.perf_counter()
         waiting = sorted(requests, key=lambda r: r.arrival)
         completed: list[Request] = []
-        t0 = time.perf_counter()
-        now_fn = lambda: time.perf_counter() - t0
-        while waiting or self.lanes:
-            waiting = self._admit(waiting, now_fn())
-            if not self.lanes:
-                now = now_fn()
-                if all(r.arrival <= now for r in waiting):
-                    # nothing runs and nothing arrived could be admitted: it never will be
-                    raise RuntimeError("a request's device footprint exceeds the memory available to the server")
-                # idle until the next arrival
-                time.sleep(max(0.0, min(r.arrival for r in waiting) - now))
-                continue
-            self.stats.max_lanes = max(self.stats.max_lanes, len(self.lanes))
-            steps = [min(self.chunk, lane.steps_left()) for lane in self.lanes]
-            futures = [self.pool.submit(lane.batch.md_run, k) for lane, k in zip(self.lanes, steps)]
-            for f in futures:
-                f.result()
-            for lane, k in zip(self.lanes, steps):
-                for r in lane.requests:
-                    r.steps_done += k
-                self.stats.atom_steps += k * lane.batch.atoms
-            self.stats.rounds += 1
-            completed += self._retire(now_fn)
-            self._merge()
+        total = len(requests)
+        started = False
+        while len(completed) < total:
+            if waiting:
+                waiting = self._admit(waiting)
+                if waiting and not self._active and not any(l.open for l in self.lanes):
+                    if all(r.arrival <= self.now() for r in waiting):
+                        r0 = waiting[0]
+                        raise RuntimeError(
+                            "a request's device footprint exceeds the memory available to the server "
+                            f"(request {r0.rid}: {footprint_bytes(r0.system, self.precision)} bytes; "
+                            f"free {self._free_bytes()} bytes after a reserve of {self.reserve})")
+            if not started and self._active and on_start is not None:
+                started = True
+                on_start(self)
+            # wait for a completion, or until the next arrival
+            timeout = 0.002
+            if waiting:
+                timeout = max(0.0005, min(0.05, waiting[0].arrival - self.now()))
+            try:
+                completed.append(self._done.get(timeout=timeout))
+                while True:
+                    completed.append(self._done.get_nowait())
+            except queue.Empty:
+                pass
+        for lane in self.lanes:
+            lane.thread.join()
+        self.lanes = []
         return completed
 
     def close(self) -> None:
         for lane in self.lanes:
-            lane.close()
+            lane.thread.join()
         self.lanes = []
-        self.pool.shutdown()
 
 
 def latency_percentiles(requests: list[Request]) -> tuple[float, float]:
-    lat = np.array([r.latency for r in requests])
+    lat = np.array([r.latency for r in requests if r.error is None and not r.cancelled])
     return float(np.percentile(lat, 50)), float(np.percentile(lat, 99))

@@ -67,3 +67,123 @@ def test_admission_waits_for_memory():
     server.close()
     assert len(done) == len(requests)
     assert server.stats.waited_for_memory > 0
+
+
+def test_bad_request_fails_alone_and_others_match_alone_runs():
+    """A request whose positions hold a NaN (injected on the host) fails with an
+    error; the requests served beside it, in the same lanes, finish with their
+    alone results."""
+    requests = [r for r in workloads.serving_requests(count=12, rate=400.0, seed=8, precision="fp64",
+                                                      scale=0.03) if r.kind == "lj"][:5]
+    assert len(requests) >= 4
+    bad = requests[1]
+    pos = bad.system.positions.copy()
+    pos[3] = np.nan
+    bad.system.positions = pos
+    server = Server(precision="fp64", chunk=20, max_lanes=2, threads_per_atom=8)
+    done = server.run(requests)
+    server.close()
+    assert len(done) == len(requests)
+    assert bad.error is not None and "non-finite" in bad.error
+    assert server.stats.failed == 1
+    for r in done:
+        if r is bad:
+            continue
+        assert r.error is None
+        pos, vel = run_alone(r, "fp64", 8)
+        assert np.abs(r.positions - pos).max() < 1e-9, r.rid
+
+
+def test_cancel_and_snapshot_restore():
+    """A cancelled request leaves at its lane's next boundary; a snapshot taken
+    while a request runs, restored as a new request, finishes where the
+    uninterrupted run finishes (FP64, 1e-9 A)."""
+    requests = [r for r in workloads.serving_requests(count=12, rate=1000.0, seed=12, precision="fp64",
+                                                      scale=0.05) if r.kind == "lj"][:3]
+    for r in requests:
+        r.arrival = 0.0
+        r.nsteps = 200
+    victim, traced = requests[0], requests[1]
+
+    def control(server):
+        server.cancel(victim.rid)
+        server.snapshot(traced.rid)
+
+    server = Server(precision="fp64", chunk=20, max_lanes=2, threads_per_atom=8)
+    done = server.run(requests, on_start=control)
+    server.close()
+    assert victim.cancelled and victim.positions is None
+    assert traced.snapshot is not None
+    x, v, a, steps = traced.snapshot
+    assert 0 < steps < traced.nsteps
+    from lumol_gb300.serving import Request
+    resumed = Request(rid=99, system=traced.system, nsteps=traced.nsteps, timestep=traced.timestep,
+                      restore=(x, v, a, steps))
+    server = Server(precision="fp64", chunk=20, max_lanes=1, threads_per_atom=8)
+    again = server.run([resumed])
+    server.close()
+    assert again[0].steps_done == traced.nsteps
+    assert np.abs(again[0].positions - traced.positions).max() < 1e-9
+    assert np.abs(again[0].velocities - traced.velocities).max() < 1e-9
+
+
+def test_joining_and_leaving_in_place_keeps_trajectories():
+    """Systems join and leave a running engine in place (lg_add_systems,
+    lg_remove_system): the systems that stay continue their trajectories
+    (FP64, 1e-9 A against each system run alone), and leaving allocates no
+    device memory."""
+    import ctypes
+    import torch
+    import lumol_gb300 as lg
+    from lumol_gb300 import _capi as C
+    sizes, total_steps = [200, 300, 250], [40, 60, 40]
+
+    def make(k):
+        return workloads.lj_replica(sizes[k], 0.6, 150.0, seed=70 + k)
+
+    ref = []
+    for k in range(3):
+        b = Batch([make(k)], threads_per_atom=8)
+        b.md_setup([1.0])
+        b.md_run(total_steps[k])
+        ref.append(b.state(0))
+        b.engine.close()
+    systems = [make(k) for k in range(3)]
+
+    def join(eng, k, s):
+        systems[k]._lower_into(eng, s)
+        p = lg.md_params(lg.VelocityVerlet(1.0))
+        eng.call("lg_md_setup_ex", s, ctypes.byref(p))
+        eng.call("lg_md_set_state", s, C.dptr(np.ascontiguousarray(systems[k].positions)),
+                 C.dptr(np.ascontiguousarray(systems[k].velocities)))
+
+    def state(eng, s, n):
+        x, v = np.zeros((n, 3)), np.zeros((n, 3))
+        eng.call("lg_md_get_state", s, C.dptr(x), C.dptr(v))
+        return x, v
+
+    eng = lg.Engine(2, "fp64", threads_per_atom=8)
+    join(eng, 0, 0)
+    join(eng, 1, 1)
+    eng.call("lg_md_run", 20)
+    eng.call("lg_add_systems", 1)  # system 2 joins at step 20 of the others
+    join(eng, 2, 2)
+    eng.call("lg_md_run", 20)
+    x0, v0 = state(eng, 0, 200)
+    assert np.abs(x0 - ref[0][0]).max() < 1e-9 and np.abs(v0 - ref[0][1]).max() < 1e-9
+    x1, _ = state(eng, 1, 300)
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
+    eng.call("lg_remove_system", 0)  # system 1 becomes 0, system 2 becomes 1
+    forces, energy, virial = np.zeros((300, 3)), ctypes.c_double(), np.zeros(9)
+    eng.call("lg_compute", 0, C.dptr(x1), C.LG_TERM_ALL, C.LG_WANT_FORCES, C.dptr(forces), ctypes.byref(energy),
+             C.dptr(virial))  # the batch is lowered again here, without the system that left
+    torch.cuda.synchronize()
+    free_after, _ = torch.cuda.mem_get_info()
+    assert free_after >= free_before, (free_before, free_after)
+    eng.call("lg_md_run", 20)
+    x1, v1 = state(eng, 0, 300)
+    assert np.abs(x1 - ref[1][0]).max() < 1e-9 and np.abs(v1 - ref[1][1]).max() < 1e-9
+    x2, v2 = state(eng, 1, 250)
+    assert np.abs(x2 - ref[2][0]).max() < 1e-9 and np.abs(v2 - ref[2][1]).max() < 1e-9
+    eng.close()
