@@ -66,6 +66,8 @@ def parse():
     p.add_argument("--no-roofline", action="store_true")
     p.add_argument("--no-accuracy", action="store_true", help="skip the mixed-vs-FP64 error report")
     p.add_argument("--no-fp64-leg", action="store_true", help="lj_batch: skip timing the plain FP64 path")
+    p.add_argument("--no-configs", action="store_true",
+                   help="lj_batch: skip the single-system (argon, NaCl, water) and serving legs")
     return p.parse_args()
 
 
@@ -249,13 +251,26 @@ def run_reference(args, world, rank):
     oracle.build()
     if args.workload == "lj_batch":
         md_sys, md_p, mc_sys, mc_p, desc = batch_workload(args, "fp64")
-        base = batch_cpu_baseline(md_sys, mc_sys, mc_p, seconds=max(5.0, 0.05 * args.steps))
-        line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": METRIC, "n_gpus": 0,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic (seeded replicas)", "config": {"workload": desc, "precision": "fp64"},
+        ref = reference_batch_steps(md_sys, md_p, mc_sys, mc_p, args.steps, args.warmup)
+        md_atoms = sum(s.size for s in md_sys)
+        mc_atoms = sum(s.size for s in mc_sys)
+        value = ref["value"]
+        base = {"value": value, "unit": METRIC, "cores": ref["threads"], "kind": "port",
+                "sample": f"{args.steps} whole batched steps after {args.warmup} warm-up steps: one "
+                          f"Velocity-Verlet + Berendsen step of each of the {len(md_sys)} MD replicas (O(N^2) "
+                          f"forces) and one Translate move of each of the {len(mc_sys)} Monte Carlo chains "
+                          f"(EnergyCache move cost and update); C++ restatement of lumol-core, OpenMP "
+                          f"{ref['threads']} threads"}
+        line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 0,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ref["ms_per_step"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded replicas, lattice + jitter, Maxwell-Boltzmann velocities)",
+                "config": batch_config(desc, md_atoms, mc_atoms, len(mc_sys)),
+                "run": {"precision": "fp64", "parallelism": f"host, OpenMP {ref['threads']} threads",
+                        "timed_iteration": "1 batched step (every MD replica, then every chain)"},
+                "mc_moves_per_s": ref["mc_moves_per_s"], "md_atom_steps_per_s": ref["md_value"],
                 "cpu_baseline": base,
-                "e2e": {"value": base["value"], "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+                "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
     system, dt, desc = make_system(args.workload, "fp64", args.cells)
@@ -283,6 +298,69 @@ def run_reference(args, world, rank):
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def batch_config(desc, md_atoms, mc_atoms, mc_chains):
+    """The workload of the batched-replica line, the same in both arms."""
+    return {"workload": desc, "atoms": md_atoms + mc_atoms, "md_atoms": md_atoms, "mc_chains": mc_chains}
+
+
+def reference_batch_steps(md_sys, md_p, mc_sys, mc_p, steps: int, warmup: int):
+    """The reference's algorithm on the host cores for whole batched steps of
+    the batched-replica workload: per step, one Velocity-Verlet step with the
+    Berendsen thermostat of every MD replica (O(N^2) forces,
+    lumol-sim/src/md/integrators.rs:44-69, md/thermostats.rs:112-121), then one
+    Translate move of every Monte Carlo chain (a uniform displacement of one
+    random atom, EnergyCache::move_molecule_cost and the Metropolis test,
+    EnergyCache::update on acceptance; sys/cache.rs:118-220,
+    mc/moves/translate.rs:41-125).  The caches are initialised before the
+    timing.  The units counted are the GPU arm's: MD atoms + chains per step."""
+    import numpy as np
+    import oracle
+    from lumol_gb300.units import K_BOLTZMANN
+    threads = oracle.num_threads()
+    md_orc = [oracle.Oracle(s) for s in md_sys]
+    md_state = [(s.positions.copy(), s.velocities.copy(), np.zeros((s.size, 3))) for s in md_sys]
+    md_temp = [t for _, (n, rho, t) in md_p]
+    mc_orc = [oracle.Oracle(s) for s in mc_sys]
+    mc_pos = [s.positions.copy() for s in mc_sys]
+    import concurrent.futures
+    with concurrent.futures.ThreadPoolExecutor(max_workers=max(1, threads)) as pool:
+        list(pool.map(lambda o: o.cache_init(), mc_orc))  # EnergyCache::init, O(N^2) per chain, untimed
+    mc_beta = [1.0 / (K_BOLTZMANN * t) for _, (n, rho, t) in mc_p]
+    rng = np.random.default_rng(99)
+    half = 0.3 / math.sqrt(3.0)
+    md_time = mc_time = 0.0
+
+    def one_step():
+        nonlocal md_time, mc_time
+        t0 = time.perf_counter()
+        for k, o in enumerate(md_orc):
+            x, v, a = md_state[k]
+            md_state[k] = o.velocity_verlet(x, v, a, 1.0, 1, md_temp[k], 100.0)
+        t1 = time.perf_counter()
+        for k, o in enumerate(mc_orc):
+            pos = mc_pos[k]
+            i = int(rng.integers(len(pos)))
+            newpos = pos[i:i + 1] + rng.uniform(-half, half, size=(1, 3))
+            cost = mc_beta[k] * o.move_molecule_cost(i, newpos)
+            if cost <= 0.0 or rng.random() < math.exp(-cost):
+                pos[i] = newpos[0]  # (the wrap of the centre of mass does not change energies)
+                o.set_positions(pos)
+                o.cache_update()
+        t2 = time.perf_counter()
+        md_time += t1 - t0
+        mc_time += t2 - t1
+        return t2 - t0
+
+    for _ in range(warmup):
+        one_step()
+    md_time = mc_time = 0.0
+    total = sum(one_step() for _ in range(steps))
+    md_atoms = sum(s.size for s in md_sys)
+    return {"value": (md_atoms + len(mc_sys)) * steps / total, "ms_per_step": 1e3 * total / steps,
+            "md_value": md_atoms * steps / md_time, "mc_moves_per_s": len(mc_sys) * steps / mc_time,
+            "threads": threads}
 
 
 def batch_workload(args, precision):
@@ -435,6 +513,9 @@ def main_batch(args, world, rank, local):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = batch_cpu_baseline(leg["md_sys"], leg["mc_sys"], leg["mc_p"])
+    configs = None
+    if rank == 0 and world == 1 and not args.no_configs:
+        configs = config_legs(args, local)
     acc = None
     if rank == 0 and args.precision == "mixed" and not args.no_accuracy:
         from lumol_gb300 import workloads
@@ -450,12 +531,13 @@ def main_batch(args, world, rank, local):
             "warmup": args.warmup, "ms_per_step": leg["ms_max"] / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
             "data": "synthetic (seeded replicas, lattice + jitter, Maxwell-Boltzmann velocities)",
-            "config": {"workload": leg["desc"], "atoms": md_atoms + mc.atoms, "md_atoms": md_atoms,
-                       "mc_chains": mc_chains, "precision": args.precision,
-                       "parallelism": f"replicas x{world}" if world > 1 else "one GPU, two engine streams",
-                       "timed_iteration": f"{leg['chunk']} batched steps (lg_md_run || lg_mc_run)",
-                       "l2": "inputs larger than L2 (neighbour lists of all replicas), no flush"},
+            "config": batch_config(leg["desc"], md_atoms, mc.atoms, mc_chains),
+            "run": {"precision": args.precision,
+                    "parallelism": f"replicas x{world}" if world > 1 else "one GPU, two engine streams",
+                    "timed_iteration": f"{leg['chunk']} batched steps (lg_md_run || lg_mc_run)",
+                    "l2": "inputs larger than L2 (neighbour lists of all replicas), no flush"},
             "fp64_plain": fp64_leg,
+            "configs": configs,
             "accuracy": acc,
             "mc_moves_per_s": mc_rate,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
@@ -515,6 +597,121 @@ def main_serving(args, world, rank, local):
             "clocks": clk,
         }
         print(json.dumps(line), flush=True)
+
+
+def time_md_device(system, steps: int, chunk: int = 16):
+    """atom-steps/s of `steps` MD steps of one system with its state resident
+    in HBM (lg_md_run of `chunk` steps per timed iteration, CUDA events on the
+    engine's stream, the L2 flushed before every iteration)."""
+    import ctypes
+
+    import torch
+
+    eng = system.engine()
+    ptr = ctypes.c_void_p()
+    eng.call("lg_get_stream", ctypes.byref(ptr))
+    stream = torch.cuda.ExternalStream(ptr.value)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    for _ in range(3):
+        eng.call("lg_md_run", chunk)
+    torch.cuda.synchronize()
+    ms, done = 0.0, 0
+    while done < steps:
+        k = min(chunk, steps - done)
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        eng.call("lg_md_run", k)
+        e1.record(stream)
+        e1.synchronize()
+        ms += e0.elapsed_time(e1)
+        done += k
+    return system.size * steps / (ms * 1e-3)
+
+
+def time_md_e2e(system, steps: int, every: int):
+    """atom-steps/s through the reference-facing call, one Lumol step per call
+    (Integrator::integrate -> lg_md_propagate on page-locked host arrays),
+    the state copied back to the host every `every` steps (1: every step, as
+    lg_md_integrate); host wall clock."""
+    import torch
+
+    from lumol_gb300 import _capi as C
+    eng = system.engine()
+    pos = torch.empty((system.size, 3), dtype=torch.float64, pin_memory=True)
+    vel = torch.empty((system.size, 3), dtype=torch.float64, pin_memory=True)
+    eng.call("lg_md_get_state", 0, C.dptr(pos.numpy()), C.dptr(vel.numpy()))
+    px, pv = C.dptr(pos.numpy()), C.dptr(vel.numpy())
+    for _ in range(3):
+        eng.call("lg_md_propagate", px, pv, 1, C.LG_SYNC_DOWNLOAD)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(steps):
+        flags = C.LG_SYNC_DOWNLOAD if (k + 1) % every == 0 else 0
+        eng.call("lg_md_propagate", px, pv, 1, flags)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    return system.size * steps / el
+
+
+def config_legs(args, local):
+    """The single-system workloads (argon LJ 500 atoms, NaCl Ewald 1000 ions,
+    water 5184 atoms) and the serving stream, each measured briefly: device
+    atom-steps/s of the plain FP64 and the mixed path, end to end through
+    lg_md_integrate (state copied back every step) and through
+    lg_md_propagate at an output cadence of 10 steps, the mixed path's error
+    against FP64 (force RMS, energy) with the NVE drift of both paths over the
+    workload's stated run length, and the oracle on the host cores."""
+    import torch
+
+    import lumol_gb300 as lg
+    torch.cuda.set_device(local)
+    out = {}
+    specs = {"argon": ("C0", 1000, 64), "nacl_ewald": ("C1", 2000, 64), "water": ("C2", 5000, 32)}
+    for name, (tag, nve, steps) in specs.items():
+        leg = {}
+        for precision in ("fp64", "mixed"):
+            system, dt, desc = make_system(name, precision)
+            md = lg.MolecularDynamics(lg.VelocityVerlet(dt))
+            md.setup(system)
+            leg[f"{precision}_value"] = time_md_device(system, steps)
+            if precision == "mixed":
+                leg["e2e_every_step"] = time_md_e2e(system, 64, 1)
+                leg["e2e_every_10_steps"] = time_md_e2e(system, 64, 10)
+            system.engine().close()
+        leg["mixed_over_fp64"] = leg["mixed_value"] / leg["fp64_value"]
+        leg["workload"] = desc
+        pair = (make_system(name, "fp64")[0], make_system(name, "mixed")[0])
+        acc = accuracy_report([pair], [dt], nve, "starting positions + 0.05 A seeded jitter; NVE")
+        leg.update({k: acc[k] for k in ("force_rms_rel", "energy_rel", "virial_rel", "nve_steps",
+                                        "nve_drift_rel_fp64", "nve_drift_rel_mixed")})
+        cpu = cpu_baseline(make_system(name, "fp64")[0], dt, seconds=3.0)
+        leg["cpu_oracle"] = cpu["value"]
+        leg["cpu_cores"] = cpu["cores"]
+        leg["e2e_every_step_over_cpu"] = leg["e2e_every_step"] / cpu["value"]
+        out[tag] = leg
+    # C4: the seeded serving stream (48 requests at 40/s)
+    from lumol_gb300 import workloads
+    from lumol_gb300.serving import Server, latency_percentiles
+    warm = workloads.serving_requests(count=4, rate=1000.0, seed=1, precision="mixed", scale=0.02)
+    server = Server(precision="mixed", chunk=64, max_lanes=4)
+    server.run(warm)
+    server.close()
+    requests = workloads.serving_requests(count=48, rate=40.0, seed=77, precision="mixed")
+    server = Server(precision="mixed", chunk=64, max_lanes=4)
+    t0 = time.perf_counter()
+    done = server.run(requests)
+    span = time.perf_counter() - t0
+    server.close()
+    p50, p99 = latency_percentiles(done)
+    out["C4"] = {"value": sum(r.system.size * r.nsteps for r in done) / span, "unit": METRIC,
+                 "requests": len(done), "rate_per_s": 40.0, "latency_s": {"p50": p50, "p99": p99},
+                 "span_s": span, "lanes_max": server.stats.max_lanes, "joins": server.stats.joins,
+                 "leaves": server.stats.leaves, "failed": server.stats.failed,
+                 "workload": "seeded Poisson stream: 60% LJ (200-20000 atoms), 25% NaCl+Ewald (216-8000 ions), "
+                             "15% water (300-3000 molecules), 500-5000 steps each, mixed precision"}
+    return out
 
 
 def batch_roofline(args, md, C):

@@ -423,8 +423,11 @@ int lg_md_set_state(lg_engine* e, int32_t s, const double* positions, const doub
 
 int lg_md_get_state(lg_engine* e, int32_t s, double* positions, double* velocities) {
     if (!valid_sys(e, s)) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
-    if (e->dirty) return fail(e, LG_ERR_STATE, "no device state: call lg_md_set_state first");
     CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    {
+        int rc0 = commit_carried(e);
+        if (rc0) return rc0;
+    }
     const HostSystem& h = e->sys[s];
     int64_t base = e->begin[s];
     cudaStream_t st = e->stream;
@@ -603,7 +606,10 @@ int md_run_steps(lg_engine* e, int64_t nsteps, const std::function<int()>& tail)
 int md_run_checked(lg_engine* e, int64_t nsteps, const std::function<int()>& tail) {
     if (!e || nsteps < 0) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
     CUDA_TRY(e, cudaSetDevice(e->opt.device));
-    if (e->dirty) return fail(e, LG_ERR_STATE, "no device state: call lg_md_set_state first");
+    {
+        int rc = commit_carried(e);  // systems that left or were re-described keep their state
+        if (rc) return rc;
+    }
     for (int s = 0; s < e->nsys; s++)
         if (!e->sys[s].md_ready) return fail(e, LG_ERR_STATE, "lg_md_setup was not called for every system");
     e->nonfinite = false;
@@ -662,8 +668,11 @@ int lg_md_set_state_all(lg_engine* e, const double* positions, const double* vel
 
 int lg_md_get_state_all(lg_engine* e, double* positions, double* velocities, double* accelerations) {
     if (!e) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
-    if (e->dirty) return fail(e, LG_ERR_STATE, "no device state: call lg_md_set_state first");
     CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    {
+        int rc0 = commit_carried(e);
+        if (rc0) return rc0;
+    }
     cudaStream_t st = e->stream;
     size_t n = (size_t)e->b.n;
     if (n == 0) return LG_OK;

@@ -125,8 +125,11 @@ int lg_mc_setup(lg_engine* e, int32_t s, double temperature, double delta, uint6
 
 int lg_mc_run(lg_engine* e, int64_t moves) {
     if (!e || moves < 0) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
-    if (e->dirty) return fail(e, LG_ERR_STATE, "no device state: call lg_md_set_state first");
     CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    {
+        int rc0 = commit_carried(e);
+        if (rc0) return rc0;
+    }
     cudaStream_t st = e->stream;
     int nsys = e->nsys;
     CUDA_TRY(e, cudaMemcpy(e->h_mc.data(), e->mc_chains.p, nsys * sizeof(McState), cudaMemcpyDeviceToHost));

@@ -250,6 +250,9 @@ double max_cutoff(const HostSystem& h);
 int check_pair_cutoffs(lg_engine* e, const HostSystem& h);
 // Lowers the description into device memory when it changed (e->dirty).
 int commit(lg_engine* e);
+// commit() for a batch whose systems all keep their device state (systems
+// left, or were re-described without new particles); LG_ERR_STATE otherwise.
+int commit_carried(lg_engine* e);
 
 // ---- runtime.cu -----------------------------------------------------------------
 int regrow(lg_engine* e);

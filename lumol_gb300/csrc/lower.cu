@@ -961,4 +961,12 @@ int commit(lg_engine* e) {
     return LG_OK;
 }
 
+int commit_carried(lg_engine* e) {
+    if (!e->dirty) return LG_OK;
+    bool carried = e->carry_from.size() == (size_t)e->nsys;
+    for (int s = 0; carried && s < e->nsys; s++) carried = e->carry_from[s] >= 0;
+    if (!carried) return fail(e, LG_ERR_STATE, "no device state: call lg_md_set_state first");
+    return commit(e);
+}
+
 }  // namespace lg

@@ -33,7 +33,7 @@ __global__ void __launch_bounds__(256, GENERAL && !EV ? 4 : 1) pair_mixed_kernel
     const int* __restrict__ sysid, const SysDev* __restrict__ sys,
     const PairDevF* __restrict__ ptab, const int* __restrict__ nbr, const int* __restrict__ nnb, int maxnb,
     const int* __restrict__ spec_off, const int* __restrict__ spec_j, const int8_t* __restrict__ spec_path,
-    uint32_t terms, double* __restrict__ force, double* __restrict__ red) {
+    uint32_t terms, double* __restrict__ force, double* __restrict__ red, const double4_32a* __restrict__ posq) {
     // t walks the cell-sorted order; i is the atom's own index (forces, bond paths)
     int gt = blockIdx.x * blockDim.x + threadIdx.x;
     int t = gt / TPA;
@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(256, GENERAL && !EV ? 4 : 1) pair_mixed_kernel
         },
         [&](int js, const uint4& pj, const int2& kmj) {
             mixed_entry<EV, GENERAL>(A, s, prow, pi, qi, kmi.y, i, tt, js, pj, kmj, order, spec_off, spec_j,
-                                     spec_path, pairs, coul, coul_rc2, alpha, pref, single, ph1, pq1);
+                                     spec_path, pairs, coul, coul_rc2, alpha, pref, single, ph1, pq1, posq);
         });
     // combine the group's compensated sums; one lane converts to FP64
     group_combine<TPA>(A);
@@ -112,11 +112,11 @@ void launch_pair_mixed_variant(const Batch& b, uint32_t terms, bool ev, cudaStre
     if (ev)
         pair_mixed_kernel<TPA, true, GENERAL><<<grid, tb, 0, st>>>(
             b.n, b.posfx, b.km, b.cell_atoms, b.sysid, b.sys, b.ptabf, b.nbr, b.nnb, b.maxnb, b.spec_off, b.spec_j,
-            b.spec_path, terms, b.force, b.red);
+            b.spec_path, terms, b.force, b.red, b.posq);
     else
         pair_mixed_kernel<TPA, false, GENERAL><<<grid, tb, 0, st>>>(
             b.n, b.posfx, b.km, b.cell_atoms, b.sysid, b.sys, b.ptabf, b.nbr, b.nnb, b.maxnb, b.spec_off, b.spec_j,
-            b.spec_path, terms, b.force, b.red);
+            b.spec_path, terms, b.force, b.red, b.posq);
 }
 
 template <int TPA>

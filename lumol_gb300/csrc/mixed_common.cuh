@@ -127,7 +127,7 @@ __device__ __forceinline__ void mixed_entry(
     MixedAcc& A, const SysDev& s, const PairDevF* __restrict__ prow, uint4 pi, float qi, int mi, int i, int tt,
     int js, uint4 pj, int2 kmj, const int* __restrict__ order, const int* __restrict__ spec_off,
     const int* __restrict__ spec_j, const int8_t* __restrict__ spec_path, bool pairs, bool coul, float coul_rc2,
-    float alpha, float pref, bool single, int4 ph1, float4 pq1) {
+    float alpha, float pref, bool single, int4 ph1, float4 pq1, const double4_32a* __restrict__ posq) {
     float qj = __uint_as_float(pj.w);
     float dx = fixed_image(pi.x, pj.x, s.Lq[0]);
     float dy = fixed_image(pi.y, pj.y, s.Lq[1]);
@@ -152,6 +152,7 @@ __device__ __forceinline__ void mixed_entry(
     float inv_r2 = rmul(inv_r, inv_r);
     float fr = 0.0f;
     float e_pair = 0.0f, e_coul = 0.0f;
+    double e_coul_d = 0.0;
     if (!GENERAL) {
         float shift = EV ? __ldg(&pp->shift) : 0.0f;
         if (ph.x == 2) {  // LJ: c12 / r^12 - c6 / r^6
@@ -192,9 +193,24 @@ __device__ __forceinline__ void mixed_entry(
             if (s.coul == 1) {
                 float g = rmul(rmul(alpha, (float)FRAC_2_SQRT_PI), __expf(rmul(-ar, ar)));
                 if (excl) {
-                    float ef = erff(ar);
-                    e_coul = rmul(rmul(-qq, ef), inv_r);
-                    fr = radd(fr, rmul(rmul(qq, inv_r2), rfma(-ef, inv_r, g)));
+                    // an excluded (bonded) pair's -erf correction (ewald.rs:394-397,
+                    // 411-427) in FP64, from the FP64 positions and charges: these
+                    // terms (three per water molecule) all have one sign and a
+                    // large sum, so FP32 roundings would not average out in the
+                    // energy.  The force is then rounded to FP32 like the others.
+                    const int j = order[js];
+                    const double4_32a a4 = posq[i], b4 = posq[j];
+                    double d[3] = {a4.x - b4.x, a4.y - b4.y, a4.z - b4.z};
+                    for (int k = 0; k < 3; k++) d[k] = exact_image(d[k], s.L[k], s.invL[k]);
+                    double rd2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+                    double rd = sqrt(rd2);
+                    double ad = s.alpha * rd;
+                    double qqd = a4.w * b4.w / FOUR_PI_EPSILON_0;
+                    double efd = erf(ad);
+                    double gd = s.alpha * FRAC_2_SQRT_PI * exp(-ad * ad);
+                    e_coul_d = -qqd * efd / rd;
+                    fr = radd(fr, (float)(qqd / rd2 * (gd - efd / rd)));
+                    (void)g;
                 } else {
                     float ec_ = erfcf(ar);
                     e_coul = rmul(rmul(qq, ec_), inv_r);
@@ -222,7 +238,7 @@ __device__ __forceinline__ void mixed_entry(
     two_sum_acc(A.fzs, A.fzc, gz);
     if (EV && js > tt) {  // each unordered pair once (the list is symmetric)
         A.ep += (double)e_pair;
-        A.ec += (double)e_coul;
+        A.ec += (double)e_coul + e_coul_d;
         A.w0 += (double)rmul(gx, dx);
         A.w1 += (double)rmul(gx, dy);
         A.w2 += (double)rmul(gx, dz);

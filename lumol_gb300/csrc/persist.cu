@@ -394,7 +394,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
                     [&](int js, const uint4& pj, const int2& kmj) {
                         mixed_entry<false, false>(acc, sd, prow, pi, 0.0f, kmi.y, i, tt, js, pj, kmj, b.cell_atoms,
                                                   nullptr, nullptr, nullptr, true, false, 0.0f, 0.0f, 0.0f, single,
-                                                  ph1, pq1);
+                                                  ph1, pq1, nullptr);
                     });
                 group_combine<TPA>(acc);
                 double ke = 0.0;

@@ -38,7 +38,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _capi as C
-from .system import Engine, System, md_params, VelocityVerlet
+from .system import Engine, System, VelocityVerlet, md_params
 
 
 @dataclass
@@ -87,28 +87,38 @@ def footprint_bytes(system: System, precision: str, skin: float = 1.0) -> int:
 
 
 class Lane:
-    """One engine holding a batch of requests, stepped by its own thread."""
+    """One engine holding a batch of requests, stepped by its own thread.
+
+    The server thread only appends to `joining`, `cancel` and `snap` (under
+    `lock`); everything else, the engine included, belongs to the lane's
+    thread."""
 
     def __init__(self, server: "Server", first: list[Request]):
         self.server = server
         self.requests: list[Request] = []
-        self.engine: Engine | None = None
+        self.engine = None
         self.joining: list[Request] = list(first)
         self.cancel: set[int] = set()
         self.snap: set[int] = set()
         self.lock = threading.Lock()
         self.open = True           # accepts joins; closed by its thread when it runs empty
         self.atoms = sum(r.system.size for r in first)
+        self.members = {r.rid for r in first}  # every request assigned to the lane and not yet gone
         self.thread = threading.Thread(target=self._serve, daemon=True)
 
-    # ---- called by the server thread (under self.lock) ------------------------------
+    # ---- called by the server thread --------------------------------------------------
     def try_join(self, r: Request) -> bool:
         with self.lock:
             if not self.open:
                 return False
             self.joining.append(r)
+            self.members.add(r.rid)
             self.atoms += r.system.size
             return True
+
+    def holds(self, rid: int) -> bool:
+        with self.lock:
+            return rid in self.members
 
     # ---- the lane's own thread ---------------------------------------------------------
     def _take_joins(self) -> None:
@@ -117,19 +127,18 @@ class Lane:
         if not joins:
             return
         if self.engine is None:
-            self.engine = Engine(len(joins), self.server.precision, threads_per_atom=self.server.tpa)
+            self.engine = self.server.make_engine(len(joins))
             first = 0
         else:
             first = len(self.requests)
             self.engine.call("lg_add_systems", len(joins))
         eng = self.engine
+        for k, r in enumerate(joins):  # every new system described before any state is set
+            r.system._lower_into(eng, first + k)
         for k, r in enumerate(joins):
             s = first + k
-            r.system._lower_into(eng, s)
             p = md_params(VelocityVerlet(r.timestep))
             eng.call("lg_md_setup_ex", s, ctypes.byref(p))
-        for k, r in enumerate(joins):
-            s = first + k
             if r.restore is not None:
                 x, v, a, done = r.restore
                 r.steps_done = int(done)
@@ -138,9 +147,10 @@ class Lane:
                          C.dptr(np.ascontiguousarray(a, dtype=np.float64)))
             else:
                 v = r.system.velocities if r.system.velocities is not None else np.zeros((r.system.size, 3))
-                eng.call("lg_md_set_state", s, C.dptr(np.ascontiguousarray(r.system.positions)),
+                eng.call("lg_md_set_state", s, C.dptr(np.ascontiguousarray(r.system.positions, dtype=np.float64)),
                          C.dptr(np.ascontiguousarray(v, dtype=np.float64)))
-        self.requests += joins
+        with self.lock:
+            self.requests += joins
         self.server.stats.joins += len(joins)
 
     def _state(self, s: int, with_acc: bool = False):
@@ -152,26 +162,29 @@ class Lane:
 
     def _leave(self, indices: list[int]) -> None:
         for s in sorted(indices, reverse=True):
-            r = self.requests[s]
-            if len(self.requests) > 1:
+            with self.lock:
+                r = self.requests[s]
+                last = len(self.requests) == 1
+            if not last:
                 self.engine.call("lg_remove_system", s)
                 self.server.stats.leaves += 1
-            else:  # the engine keeps at least one system: the lane closes with it
+            else:  # the engine keeps at least one system: it closes with its last one
                 self.engine.close()
                 self.engine = None
-            del self.requests[s]
             with self.lock:
+                del self.requests[s]
+                self.members.discard(r.rid)
                 self.atoms -= r.system.size
 
     def _boundary(self) -> None:
-        """Retirement, cancellation and snapshots between two chunks."""
+        """Snapshots, cancellation and retirement between two chunks."""
         now = self.server.now()
         leave = []
         with self.lock:
             cancel, self.cancel = self.cancel, set()
             snap, self.snap = self.snap, set()
         for s, r in enumerate(self.requests):
-            if r.rid in snap:
+            if r.rid in snap and r.error is None:
                 x, v, a = self._state(s, with_acc=True)
                 r.snapshot = (x, v, a, r.steps_done)
             if r.error is not None:
@@ -184,10 +197,34 @@ class Lane:
                 r.positions, r.velocities, _ = self._state(s)
                 r.finished = now
                 leave.append(s)
-        for s in leave:
-            self.server._complete(self.requests[s])
+        present = {r.rid for r in self.requests}
+        with self.lock:  # controls of requests still joining wait for their first boundary
+            self.cancel |= {rid for rid in cancel if rid not in present}
+            self.snap |= {rid for rid in snap if rid not in present}
+        done = [self.requests[s] for s in leave]
         if leave:
             self._leave(leave)
+        for r in done:
+            self.server._complete(r)
+
+    def _run_chunk(self) -> None:
+        steps = max(0, min(self.server.chunk, min(r.nsteps - r.steps_done for r in self.requests)))
+        code = self.engine.run_steps(steps)
+        if code == C.LG_ERR_NONFINITE:  # the flagged requests fail; the others completed the chunk
+            flags = (ctypes.c_uint32 * len(self.requests))()
+            self.engine.call("lg_system_status", flags, 1)
+            for s, r in enumerate(self.requests):
+                if flags[s] & C.LG_SYS_NONFINITE:
+                    r.error = "non-finite positions or velocities (Kinetic energy is infinite!)"
+                    r.finished = self.server.now()
+                    self.server.stats.failed += 1
+        elif code != C.LG_OK:
+            self.engine.check(code)
+        for r in self.requests:
+            if r.error is None:
+                r.steps_done += steps
+                self.server.stats.atom_steps += steps * r.system.size
+        self.server.stats.chunks += 1
 
     def _serve(self) -> None:
         try:
@@ -199,25 +236,11 @@ class Lane:
                             self.open = False
                             break
                     continue
-                steps = min(self.server.chunk, min(r.nsteps - r.steps_done for r in self.requests))
-                steps = max(steps, 0)
-                code = self.engine.lib.lg_md_run(self.engine.handle, steps)
-                if code == C.LG_ERR_NONFINITE:
-                    flags = (ctypes.c_uint32 * len(self.requests))()
-                    self.engine.call("lg_system_status", flags, 1)
-                    for s, r in enumerate(self.requests):
-                        if flags[s] & C.LG_SYS_NONFINITE:
-                            r.error = "non-finite positions or velocities (Kinetic energy is infinite!)"
-                            r.finished = self.server.now()
-                    self.server.stats.failed += sum(1 for f in flags if f & C.LG_SYS_NONFINITE)
-                elif code != C.LG_OK:
-                    C.check(code, self.engine.handle)
-                for r in self.requests:
-                    if r.error is None:
-                        r.steps_done += steps
-                        self.server.stats.atom_steps += steps * r.system.size
-                self.server.stats.chunks += 1
+                # requests that joined or were controlled before their first chunk
                 self._boundary()
+                if self.requests:
+                    self._run_chunk()
+                    self._boundary()
         except BaseException as exc:  # a lane that fails reports every request it holds
             with self.lock:
                 self.open = False
@@ -225,7 +248,7 @@ class Lane:
                 self.requests, self.joining = [], []
             for r in pending:
                 if r.finished is None:
-                    r.error = f"lane failed: {exc}"
+                    r.error = f"lane failed: {exc!r}"
                     r.finished = self.server.now()
                     self.server._complete(r)
             if self.engine is not None:
@@ -250,7 +273,12 @@ class Server:
 
     def __init__(self, precision: str = "mixed", chunk: int = 50, max_lanes: int = 4,
                  memory_budget: int | None = None, reserve_bytes: int = 1 << 30, threads_per_atom: int = 8,
-                 lane_atoms: int = 400_000):
+                 lane_atoms: int = 400_000, engine_factory=None, free_bytes=None):
+        """`engine_factory(n_systems, precision, threads_per_atom)` and
+        `free_bytes()` default to the GPU engine and cudaMemGetInfo; the CPU
+        tests of the scheduling logic pass stand-ins."""
+        self.engine_factory = engine_factory or (lambda n, prec, tpa: Engine(n, prec, threads_per_atom=tpa))
+        self.device_free = free_bytes or _device_free_bytes
         self.precision = precision
         self.chunk = chunk
         self.max_lanes = max_lanes
@@ -268,32 +296,37 @@ class Server:
     def now(self) -> float:
         return time.perf_counter() - self._t0
 
+    def make_engine(self, n_systems: int):
+        return self.engine_factory(n_systems, self.precision, self.tpa)
+
     def _complete(self, r: Request) -> None:
         with self._lock:
             self._active.pop(r.rid, None)
         self._done.put(r)
 
     # ---- controls -------------------------------------------------------------------
-    def cancel(self, rid: int) -> None:
+    def cancel(self, rid: int) -> bool:
         """Stops request `rid` at its lane's next chunk boundary."""
         for lane in list(self.lanes):
-            with lane.lock:
-                if any(r.rid == rid for r in lane.requests + lane.joining):
+            if lane.holds(rid):
+                with lane.lock:
                     lane.cancel.add(rid)
+                return True
+        return False
 
-    def snapshot(self, rid: int) -> None:
+    def snapshot(self, rid: int) -> bool:
         """Asks for request `rid`'s state at its lane's next chunk boundary
         (Request.snapshot; resume it with Request(restore=snapshot))."""
         for lane in list(self.lanes):
-            with lane.lock:
-                if any(r.rid == rid for r in lane.requests + lane.joining):
+            if lane.holds(rid):
+                with lane.lock:
                     lane.snap.add(rid)
+                return True
+        return False
 
     # ---- admission --------------------------------------------------------------------
     def _free_bytes(self) -> int:
-        import torch
-        free, _ = torch.cuda.mem_get_info()
-        free -= self.reserve
+        free = self.device_free() - self.reserve
         if self.memory_budget is not None:
             with self._lock:
                 used = sum(footprint_bytes(r.system, self.precision) for r in self._active.values())
@@ -316,17 +349,20 @@ class Server:
                 self.stats.waited_for_memory += 1
                 rest.append(r)
                 continue
+            # a new lane while there are fewer than max_lanes (lanes step
+            # concurrently), else the least loaded lane with room
             placed = False
-            for lane in sorted((l for l in self.lanes if l.open), key=lambda l: l.atoms):
-                if lane.atoms + r.system.size <= self.lane_atoms and lane.try_join(r):
-                    placed = True
-                    break
-            if not placed and len([l for l in self.lanes if l.open]) < self.max_lanes:
+            if len([l for l in self.lanes if l.open]) < self.max_lanes:
                 lane = Lane(self, [r])
                 self.lanes.append(lane)
                 self.stats.lanes_opened += 1
                 lane.thread.start()
                 placed = True
+            else:
+                for lane in sorted((l for l in self.lanes if l.open), key=lambda l: l.atoms):
+                    if lane.atoms + r.system.size <= self.lane_atoms and lane.try_join(r):
+                        placed = True
+                        break
             if not placed:
                 rest.append(r)
                 continue
@@ -380,6 +416,12 @@ class Server:
         for lane in self.lanes:
             lane.thread.join()
         self.lanes = []
+
+
+def _device_free_bytes() -> int:
+    import torch
+    free, _ = torch.cuda.mem_get_info()
+    return free
 
 
 def latency_percentiles(requests: list[Request]) -> tuple[float, float]:

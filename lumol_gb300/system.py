@@ -334,6 +334,14 @@ class Engine:
     def call(self, name: str, *args) -> None:
         C.check(getattr(self.lib, name)(self.handle, *args), self.handle)
 
+    def run_steps(self, nsteps: int) -> int:
+        """lg_md_run; returns the status (LG_ERR_NONFINITE still completes the
+        steps of every system, see lg_system_status)."""
+        return self.lib.lg_md_run(self.handle, int(nsteps))
+
+    def check(self, code: int) -> None:
+        C.check(code, self.handle)
+
     def close(self) -> None:
         if self.handle:
             self.lib.lg_destroy(self.handle)

@@ -54,18 +54,23 @@ class _Buffers:
         self.kmax = system.coulomb.kmax
 
     def call(self, stream=None):
-        """One call; the forces are accumulated into a zeroed buffer."""
+        """One call; the forces are accumulated into a zeroed buffer.  Also
+        returns the device's free memory just before and just after the call
+        (the test's own buffer preparation is outside that window)."""
         import torch
         self.forces.zero_()
         self.energy.fill_(np.nan)
         self.virial.fill_(np.nan)
         torch.cuda.synchronize()
         handle = None if stream is None else ctypes.c_void_p(stream.cuda_stream)
+        free_before, _ = torch.cuda.mem_get_info()
         rc = C.load().lg_ewald_kspace_noalloc(self.pos.data_ptr(), self.charges.data_ptr(), self.n, self.cell,
                                               self.alpha, self.kmax, self.forces.data_ptr(),
                                               self.energy.data_ptr(), self.virial.data_ptr(), handle)
         C.check(rc)
         torch.cuda.synchronize()
+        free_after, _ = torch.cuda.mem_get_info()
+        self.free = (free_before, free_after)
         return (self.forces.cpu().numpy(), float(self.energy.item()), self.virial.cpu().numpy().reshape(3, 3))
 
 
@@ -100,15 +105,15 @@ def test_noalloc_allocates_nothing_and_honours_the_stream():
     system = workloads.nacl_crystal()
     ref = _oracle(system)
     buf = _Buffers(system)
-    buf.call()  # warm-up: loads the module and looks the scratch address up
-    torch.cuda.synchronize()
-    free_before, _ = torch.cuda.mem_get_info()
     side = torch.cuda.Stream()
+    buf.call()  # warm-up on both streams: module loading, the scratch address, torch's own kernels
+    with torch.cuda.stream(side):
+        buf.call(side)
     with torch.cuda.stream(side):
         got_side = buf.call(side)
+    assert buf.free[1] == buf.free[0], ("side stream", buf.free)
     got_default = buf.call()
-    free_after, _ = torch.cuda.mem_get_info()
-    assert free_after == free_before, (free_before, free_after)
+    assert buf.free[1] == buf.free[0], ("default stream", buf.free)
     _assert_close(got_side, ref, "side stream")
     _assert_close(got_default, ref, "default stream after the side stream")
 
