@@ -284,6 +284,27 @@ typedef struct lg_md_params {
     uint32_t reserved;   /* 0 */
 } lg_md_params;
 
+/* Barostats (lumol-sim/src/md/integrators.rs). */
+enum {
+    LG_BAROSTAT_NONE = 0,
+    LG_BAROSTAT_BERENDSEN = 1  /* BerendsenBarostat (integrators.rs:174-250), isotropic */
+};
+/* BerendsenBarostat::new(timestep, pressure, tau): system `s`, set up with
+ * LG_INTEGRATOR_VELOCITY_VERLET by lg_md_setup_ex (whose timestep it uses),
+ * integrates with the Velocity-Verlet based Berendsen barostat instead.  Every
+ * step scales the positions by eta and the cell matrix by eta^3 (the
+ * reference's UnitCell::scale_mut(eta^3 * 1)), evaluates the pressure
+ * (N_f k_B T + Tr W) / (3 V) at the new positions with the half-step
+ * velocities, takes eta^3 = 1 - 7372 / tau (pressure - P) for the next step,
+ * and completes the step with the forces.  The cell change is applied on the
+ * device in place; lg_get_cell returns the current cell.  A cell length at or
+ * below twice the maximum cutoff fails the run with the reference's panic
+ * message.  LG_BAROSTAT_NONE turns it off.  (AnisoBerendsenBarostat turns an
+ * orthorhombic cell triclinic, which the engine does not represent.) */
+int lg_md_set_barostat(lg_engine* e, int32_t s, int32_t kind, double pressure, double tau);
+/* The cell matrix of system `s` (9 doubles, row-major). */
+int lg_get_cell(lg_engine* e, int32_t s, double matrix[9]);
+
 /* Molecular dynamics of system `s` with any integrator, thermostat and
  * controls of the list above, stepped as MolecularDynamics::propagate does
  * (md/molecular_dynamics.rs:66-76: integrate, thermostat, controls).  The

@@ -91,6 +91,7 @@ class LgOptions(ctypes.Structure):
 LG_INTEGRATOR_VELOCITY_VERLET, LG_INTEGRATOR_VERLET, LG_INTEGRATOR_LEAP_FROG = 0, 1, 2
 LG_THERMOSTAT_NONE, LG_THERMOSTAT_BERENDSEN, LG_THERMOSTAT_RESCALE, LG_THERMOSTAT_CSVR = 0, 1, 2, 3
 LG_CONTROL_REMOVE_TRANSLATION, LG_CONTROL_REWRAP, LG_CONTROL_REMOVE_ROTATION = 1, 2, 4
+LG_BAROSTAT_NONE, LG_BAROSTAT_BERENDSEN = 0, 1
 
 
 class LgMdParams(ctypes.Structure):
@@ -123,6 +124,8 @@ SIGNATURES = {
     "lg_md_setup": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double]),
     "lg_md_setup_ex": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(LgMdParams)]),
     "lg_list_cells": (ctypes.c_int, [_P, ctypes.c_int32, _I32, _I32]),
+    "lg_md_set_barostat": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double]),
+    "lg_get_cell": (ctypes.c_int, [_P, ctypes.c_int32, _D]),
     "lg_md_set_state": (ctypes.c_int, [_P, ctypes.c_int32, _D, _D]),
     "lg_md_get_state": (ctypes.c_int, [_P, ctypes.c_int32, _D, _D]),
     "lg_md_set_state_all": (ctypes.c_int, [_P, _D, _D, _D]),

@@ -67,12 +67,20 @@ int lg_set_cell(lg_engine* e, int32_t s, const double m[9]) {
                 return fail(e, LG_ERR_ARGUMENT, "only orthorhombic cells are supported");
     if (!(m[0] > 0.0 && m[4] > 0.0 && m[8] > 0.0)) return fail(e, LG_ERR_ARGUMENT, "Cell lengths must be positive");
     HostSystem& h = e->sys[s];
+    const double L[3] = {m[0], m[4], m[8]};
+    int rc = check_cell_cutoffs(e, h, L);
+    if (rc) return rc;
+    if (!e->dirty && h.has_cell) {  // a lowered batch: change the cell in place, keeping the state
+        CUDA_TRY(e, cudaSetDevice(e->opt.device));
+        rc = set_cell_fast(e, s, L);
+        if (rc != -1) return rc;
+    }
     h.L[0] = m[0];
     h.L[1] = m[4];
     h.L[2] = m[8];
     h.has_cell = true;
     invalidate(e);
-    return check_pair_cutoffs(e, h);
+    return LG_OK;
 }
 
 int lg_set_particles(lg_engine* e, int32_t s, int64_t n, const int32_t* kinds, const double* charges,
@@ -401,6 +409,42 @@ int lg_md_setup_ex(lg_engine* e, int32_t s, const lg_md_params* p) {
     return LG_OK;
 }
 
+int lg_md_set_barostat(lg_engine* e, int32_t s, int32_t kind, double pressure, double tau) {
+    if (!valid_sys(e, s)) return fail(e, LG_ERR_ARGUMENT, "invalid system index");
+    if (kind != LG_BAROSTAT_NONE && kind != LG_BAROSTAT_BERENDSEN) return fail(e, LG_ERR_ARGUMENT, "unknown barostat");
+    HostSystem& h = e->sys[s];
+    if (kind == LG_BAROSTAT_BERENDSEN) {
+        if (!h.md_ready || h.integrator != LG_INTEGRATOR_VELOCITY_VERLET)
+            return fail(e, LG_ERR_STATE,
+                        "the Berendsen barostat needs lg_md_setup_ex with LG_INTEGRATOR_VELOCITY_VERLET first");
+        if (!(tau > 0.0)) return fail(e, LG_ERR_ARGUMENT, "the barostat time scale must be positive");
+    }
+    h.barostat = kind;
+    h.baro_pressure = pressure;
+    h.baro_tau = tau;
+    h.baro_eta = 1.0;  // BerendsenBarostat::new
+    if (!e->dirty) {
+        SysDev& d = e->h_sysdev[s];
+        fill_md(d, h);
+        CUDA_TRY(e, cudaSetDevice(e->opt.device));
+        CUDA_TRY(e, cudaMemcpyAsync(e->sysdev.p + s, &d, sizeof(SysDev), cudaMemcpyHostToDevice, e->stream));
+        CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+        e->drop_graphs();
+        e->pk_cluster = 0;
+    }
+    return LG_OK;
+}
+
+int lg_get_cell(lg_engine* e, int32_t s, double m[9]) {
+    if (!valid_sys(e, s) || !m) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    const HostSystem& h = e->sys[s];
+    for (int k = 0; k < 9; k++) m[k] = 0.0;
+    m[0] = h.L[0];
+    m[4] = h.L[1];
+    m[8] = h.L[2];
+    return LG_OK;
+}
+
 int lg_md_set_state(lg_engine* e, int32_t s, const double* positions, const double* velocities) {
     if (!valid_sys(e, s) || !positions || !velocities) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
     CUDA_TRY(e, cudaSetDevice(e->opt.device));
@@ -532,8 +576,16 @@ int md_run_steps(lg_engine* e, int64_t nsteps, const std::function<int()>& tail)
     // the persistent kernel for runs of several steps: a launch pays for the
     // slowest group's list rebuild, which short runs do not amortize (a
     // 1-step launch measured 193 us against 178 us for the per-step kernels
-    // on the 128-replica batch)
-    if (persist_eligible(e) && nsteps >= 8) {
+    // on the 128-replica batch); a batch of a few systems has no such spread,
+    // and one launch per step beats a graph of a dozen kernels
+    for (int s = 0; s < e->nsys; s++)
+        if (e->sys[s].barostat != LG_BAROSTAT_NONE) {
+            int rc = md_run_barostat(e, nsteps);
+            if (rc == LG_OK && tail) rc = tail();
+            if (rc == LG_OK && tail) CUDA_TRY(e, cudaStreamSynchronize(st));
+            return rc;
+        }
+    if (persist_eligible(e) && (nsteps >= 8 || e->nsys <= 4)) {
         if (e->pk_cluster == 0) {
             int rc = persist_plan(e);
             if (rc) return rc;

@@ -102,6 +102,9 @@ struct SysDev {
     int32_t thermostat;           // TH_*
     uint32_t controls;            // CTL_* bits
     int32_t mol_first, mol_end;   // the system's molecules in the batch molecule table (Rewrap)
+    double baro_eta;              // BerendsenBarostat: the factor this step scales the positions by
+    int32_t barostat;             // 1: BerendsenBarostat (Velocity-Verlet based)
+    int32_t baro_pad;
 };
 
 // Sum over one system's chunks of a per-chunk value a[stride * (begin + q)]

@@ -108,6 +108,9 @@ struct HostSystem {
     bool md_ready = false;
     bool verlet_setup = false;  // Verlet::setup runs at the next lg_md_run
     bool reset_acc = false;     // VelocityVerlet / LeapFrog::setup zeroes the accelerations at the next commit
+    // BerendsenBarostat (lumol-sim/src/md/integrators.rs:174-250)
+    int32_t barostat = LG_BAROSTAT_NONE;
+    double baro_pressure = 0.0, baro_tau = 0.0, baro_eta = 1.0;
     // derived
     std::vector<int64_t> mol_begin;  // first atom of each molecule (local index), plus the end
     double tail_energy = 0.0, tail_virial = 0.0, ewald_self = 0.0;
@@ -135,7 +138,7 @@ struct lg_engine {
     Batch b;
     // device storage
     DBuf<double4_32a> posq, vel, acc, pos_build;
-    DBuf<double> force, pos3, vel3, red, host_const, kepart, mom, out, fpart, kred, mc_part;
+    DBuf<double> force, pos3, vel3, red, host_const, kepart, mom, out, fpart, kred, mc_part, kin;
     DBuf<unsigned long long> md_count, cp_count;
     DBuf<double> adj;
     DBuf<int> mol_start;
@@ -248,8 +251,17 @@ void invalidate(lg_engine* e);
 void fill_md(SysDev& d, const HostSystem& h);
 double max_cutoff(const HostSystem& h);
 int check_pair_cutoffs(lg_engine* e, const HostSystem& h);
+// System::set_pair_potential / set_coulomb_potential's check (sys/system.rs:122-131,
+// 159-170) of the potentials of h against the cell lengths L.
+int check_cell_cutoffs(lg_engine* e, const HostSystem& h, const double L[3]);
 // Lowers the description into device memory when it changed (e->dirty).
 int commit(lg_engine* e);
+// A new orthorhombic cell for system s of a lowered batch, in place: the
+// cell-dependent fields of its device record, Ewald k-vector factors and tail
+// constants, and a list rebuild; the device state is kept.  Returns -1 (and
+// changes nothing) when the cell grid or the k-vector set would change: the
+// caller then lowers the batch again (invalidate); LG_OK or an LG_ERR_* else.
+int set_cell_fast(lg_engine* e, int s, const double L[3]);
 // commit() for a batch whose systems all keep their device state (systems
 // left, or were re-described without new particles); LG_ERR_STATE otherwise.
 int commit_carried(lg_engine* e);
@@ -279,6 +291,10 @@ bool persist_batch(const lg_engine* e);
 bool persist_eligible(const lg_engine* e);
 int persist_plan(lg_engine* e);
 int md_run_persistent(lg_engine* e, int64_t nsteps, bool thermo);
+// lg_md_run of a batch with a barostat system: one step at a time, the cell
+// of every barostat system changed between steps from the pressure of the
+// previous one (one host synchronisation per step).
+int md_run_barostat(lg_engine* e, int64_t nsteps);
 int build_md_graph(lg_engine* e, int steps, int mode);
 
 }  // namespace lg

@@ -142,6 +142,12 @@ void launch_md_finalize(const Batch& b, cudaStream_t st);
 void launch_rewrap(const Batch& b, cudaStream_t st);
 void launch_verlet_setup(const Batch& b, int s, int begin, int end, cudaStream_t st);
 void launch_request_rebuild(const Batch& b, cudaStream_t st);
+// cell_atoms and perm set to the identity order (after an interrupted build).
+void launch_identity_order(const Batch& b, cudaStream_t st);
+// Sets ST_REBUILD only (the systems to rebuild are already flagged in sys_rebuild).
+void launch_request_rebuild_flag(const Batch& b, cudaStream_t st);
+// Kinetic energy of every system (nsys doubles) at the current velocities.
+void launch_kinetic(const Batch& b, double* out, cudaStream_t st);
 void launch_carry_vectors(const double4_32a* src, double4_32a* dst, int n, bool keep_w, cudaStream_t st);
 void launch_check_displacement(const Batch& b, cudaStream_t st);
 

@@ -298,6 +298,8 @@ void fill_md(SysDev& d, const HostSystem& h) {
     double total = 0.0;  // RemoveTranslation: masses summed in atom order (controls.rs:31)
     for (double w : h.masses) total += w;
     d.total_mass = total;
+    d.barostat = h.barostat;
+    d.baro_eta = h.baro_eta;
 }
 
 double max_cutoff(const HostSystem& h) {
@@ -310,7 +312,11 @@ double max_cutoff(const HostSystem& h) {
 
 int check_pair_cutoffs(lg_engine* e, const HostSystem& h) {
     if (!h.has_cell) return LG_OK;
-    double half = 0.5 * std::min(std::min(h.L[0], h.L[1]), h.L[2]);
+    return check_cell_cutoffs(e, h, h.L);
+}
+
+int check_cell_cutoffs(lg_engine* e, const HostSystem& h, const double L[3]) {
+    double half = 0.5 * std::min(std::min(L[0], L[1]), L[2]);
     for (const lg_pair& p : h.pairs)
         if (p.type != LG_PAIR_ABSENT && half < p.cutoff)
             return fail(e, LG_ERR_ARGUMENT,
@@ -320,6 +326,101 @@ int check_pair_cutoffs(lg_engine* e, const HostSystem& h) {
         return fail(e, LG_ERR_ARGUMENT,
                     "Can not add a potential with a cutoff bigger than half of the smallest cell length. "
                     "Try increasing the cell size or decreasing the cutoff.");
+    return LG_OK;
+}
+
+// The fields of a system's device record that follow from its cell: lengths
+// and their inverses in FP64 / FP32, the fixed-point scale, the list radius
+// and rebuild threshold, and the cell grid (cells at least half the list
+// radius wide: the list builds look two cells around).
+void cell_geometry(SysDev& d, const HostSystem& h, const double L[3], double skin) {
+    for (int k = 0; k < 3; k++) {
+        d.L[k] = L[k];
+        d.invL[k] = 1.0 / L[k];
+        d.Lf[k] = (float)L[k];
+        d.invLf[k] = (float)(1.0 / L[k]);
+        d.Lq[k] = (float)(L[k] / 4294967296.0);
+        d.fxscale[k] = d.invL[k] * 4294967296.0;
+    }
+    double rc = max_cutoff(h);
+    d.rlist = rc + skin;
+    d.half_skin2 = 0.25 * skin * skin;
+    d.rebuild2_f = 0.99f * (float)d.half_skin2;
+    double margin = 1e-5 * std::max(std::max(L[0], L[1]), L[2]) + 1e-4;
+    d.rlist2_f = (float)((d.rlist + margin) * (d.rlist + margin));
+    for (int k = 0; k < 3; k++) {
+        int nc = (int)std::floor(L[k] / (0.5 * (d.rlist + margin)));
+        d.ncell[k] = std::max(1, std::min(nc, 128));
+    }
+}
+
+// k_vector([1, 0, 0]) etc. of the cell (cells.rs:224-226): 2 PI times the
+// diagonal of the inverse cell matrix.
+void ewald_k1(SysDev& d, const double L[3]) {
+    double inv[3];
+    ortho_inverse_diag(L, inv);
+    for (int k = 0; k < 3; k++) d.k1[k] = (2.0 * PI) * inv[k];
+}
+
+// Tail corrections (sys/energy.rs:63-79, compute.rs:219-229), kinds in index
+// order, at the current volume.
+void tail_corrections(HostSystem& h) {
+    double volume = h.L[0] * h.L[1] * h.L[2];
+    std::vector<int64_t> counts(h.nk, 0);
+    for (int32_t k : h.kinds) counts[k]++;
+    double te = 0.0, tv = 0.0;
+    for (int a = 0; a < h.nk; a++) {
+        if (!counts[a]) continue;
+        for (int c = 0; c < h.nk; c++) {
+            if (!counts[c]) continue;
+            double two_pi_density = 2.0 * PI * (double)counts[a] * (double)counts[c] / volume;
+            const lg_pair& p = h.pairs[(size_t)a * h.nk + c];
+            if (p.type == LG_PAIR_ABSENT || !p.tail) continue;
+            te += two_pi_density * pot_tail_energy(p, p.cutoff);
+            tv += two_pi_density * (pot_tail_virial(p, p.cutoff) * (1.0 / 3.0));
+        }
+    }
+    h.tail_energy = te;
+    h.tail_virial = tv;
+}
+
+int set_cell_fast(lg_engine* e, int s, const double L[3]) {
+    HostSystem& h = e->sys[s];
+    SysDev d = e->h_sysdev[s];
+    cell_geometry(d, h, L, e->skin);
+    const SysDev& old = e->h_sysdev[s];
+    if (d.ncell[0] != old.ncell[0] || d.ncell[1] != old.ncell[1] || d.ncell[2] != old.ncell[2]) return -1;
+    std::vector<KVecDev> kv;
+    if (h.coul.kind == LG_COULOMB_EWALD) {
+        ewald_k1(d, L);
+        ewald_factors(L, h.alpha, h.coul.kmax, s, kv);
+        if ((int)kv.size() != old.kend - old.kbegin) return -1;  // another k-vector set: lower again
+    }
+    for (int k = 0; k < 3; k++) h.L[k] = L[k];
+    tail_corrections(h);
+    e->h_sysdev[s] = d;
+    cudaStream_t st = e->stream;
+    double hc[3] = {h.tail_energy, h.tail_virial, h.ewald_self};
+    CUDA_TRY(e, cudaMemcpyAsync(e->sysdev.p + s, &e->h_sysdev[s], sizeof(SysDev), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(e, cudaMemcpyAsync(e->host_const.p + (size_t)s * RED_STRIDE, hc, 3 * sizeof(double),
+                                cudaMemcpyHostToDevice, st));
+    if (!kv.empty()) {
+        std::vector<KVecF> kf(kv.size());
+        for (size_t k = 0; k < kv.size(); k++)
+            kf[k] = KVecF{kv[k].ikx, kv[k].iky, kv[k].ikz, kv[k].sys, (float)kv[k].field[0], (float)kv[k].field[1],
+                          (float)kv[k].field[2], (float)kv[k].energy};
+        CUDA_TRY(e, cudaMemcpyAsync(e->kvec.p + d.kbegin, kv.data(), kv.size() * sizeof(KVecDev),
+                                    cudaMemcpyHostToDevice, st));
+        CUDA_TRY(e, cudaMemcpyAsync(e->kvecf.p + d.kbegin, kf.data(), kf.size() * sizeof(KVecF),
+                                    cudaMemcpyHostToDevice, st));
+    }
+    // positions keep their values in Angstrom: every list of the system is rebuilt
+    uint32_t one = 1u;
+    CUDA_TRY(e, cudaMemcpyAsync(e->sys_rebuild.p + s, &one, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    launch_request_rebuild_flag(e->b, st);
+    CUDA_TRY(e, cudaStreamSynchronize(st));  // the host copies above live on this stack
+    e->shadow_valid = false;
+    e->pk_cluster = 0;  // the persistent plan weighs systems by their density
     return LG_OK;
 }
 
@@ -552,28 +653,8 @@ int commit(lg_engine* e) {
         d.needs_path = needs_path;
 
         // cell and neighbour list geometry
-        for (int k = 0; k < 3; k++) {
-            d.L[k] = h.L[k];
-            d.invL[k] = 1.0 / h.L[k];
-            d.Lf[k] = (float)h.L[k];
-            d.invLf[k] = (float)(1.0 / h.L[k]);
-            d.Lq[k] = (float)(h.L[k] / 4294967296.0);
-            d.fxscale[k] = d.invL[k] * 4294967296.0;
-        }
-        double rc = max_cutoff(h);
-        d.rlist = rc + e->skin;
-        d.half_skin2 = 0.25 * e->skin * e->skin;
-        d.rebuild2_f = 0.99f * (float)d.half_skin2;
-        double margin = 1e-5 * std::max(std::max(h.L[0], h.L[1]), h.L[2]) + 1e-4;
-        d.rlist2_f = (float)((d.rlist + margin) * (d.rlist + margin));
-        // cells at least half the list radius wide: the list builds look two cells around
-        int cells = 1;
-        for (int k = 0; k < 3; k++) {
-            int nc = (int)std::floor(h.L[k] / (0.5 * (d.rlist + margin)));
-            nc = std::max(1, std::min(nc, 128));
-            d.ncell[k] = nc;
-            cells *= nc;
-        }
+        cell_geometry(d, h, h.L, e->skin);
+        const int cells = d.ncell[0] * d.ncell[1] * d.ncell[2];
         d.cell_begin = cell_total;
         cell_total += cells;
         d.tile_begin = (int)h_tiles.size();
@@ -597,9 +678,7 @@ int commit(lg_engine* e) {
             d.alpha = h.alpha;
             d.kmax = h.coul.kmax;
             kdim = std::max(kdim, h.coul.kmax + 1);
-            double inv[3];
-            ortho_inverse_diag(h.L, inv);
-            for (int k = 0; k < 3; k++) d.k1[k] = (2.0 * PI) * inv[k];
+            ewald_k1(d, h.L);
             d.kbegin = (int)h_kvec.size();
             ewald_factors(h.L, h.alpha, h.coul.kmax, s, h_kvec);
             d.kend = (int)h_kvec.size();
@@ -620,26 +699,10 @@ int commit(lg_engine* e) {
         d.kbegin = h.coul.kind == LG_COULOMB_EWALD ? d.kbegin : (int)h_kvec.size();
         d.kend = h.coul.kind == LG_COULOMB_EWALD ? d.kend : (int)h_kvec.size();
 
-        // Tail corrections (sys/energy.rs:63-79, compute.rs:219-229), kinds in index order
-        std::vector<int64_t> counts(h.nk, 0);
-        for (int32_t k : h.kinds) counts[k]++;
-        double te = 0.0, tv = 0.0;
-        for (int a = 0; a < h.nk; a++) {
-            if (!counts[a]) continue;
-            for (int c = 0; c < h.nk; c++) {
-                if (!counts[c]) continue;
-                double two_pi_density = 2.0 * PI * (double)counts[a] * (double)counts[c] / volume;
-                const lg_pair& p = h.pairs[(size_t)a * h.nk + c];
-                if (p.type == LG_PAIR_ABSENT || !p.tail) continue;
-                te += two_pi_density * pot_tail_energy(p, p.cutoff);
-                tv += two_pi_density * (pot_tail_virial(p, p.cutoff) * (1.0 / 3.0));
-            }
-        }
-        h.tail_energy = te;
-        h.tail_virial = tv;
+        tail_corrections(h);
         double* hc = &h_const[(size_t)s * RED_STRIDE];
-        hc[0] = te;
-        hc[1] = tv;
+        hc[0] = h.tail_energy;
+        hc[1] = h.tail_virial;
         hc[2] = h.ewald_self;
 
         d.begin = (int)base;

@@ -277,6 +277,11 @@ __global__ void __launch_bounds__(VV_TILE) md_first_kernel(
             v.x = fma(hdt, a.x, v.x);
             v.y = fma(hdt, a.y, v.y);
             v.z = fma(hdt, a.z, v.z);
+            if (s.barostat) {  // BerendsenBarostat: x *= eta, then x += v dt (integrators.rs:219-225)
+                p.x *= s.baro_eta;
+                p.y *= s.baro_eta;
+                p.z *= s.baro_eta;
+            }
             p.x = fma(v.x, dt, p.x);
             p.y = fma(v.y, dt, p.y);
             p.z = fma(v.z, dt, p.z);
@@ -293,6 +298,11 @@ __global__ void __launch_bounds__(VV_TILE) md_first_kernel(
             v.x = __dadd_rn(v.x, __dmul_rn(hdt, a.x));
             v.y = __dadd_rn(v.y, __dmul_rn(hdt, a.y));
             v.z = __dadd_rn(v.z, __dmul_rn(hdt, a.z));
+            if (s.barostat) {  // BerendsenBarostat: x *= eta, then x += v dt (integrators.rs:219-225)
+                p.x = __dmul_rn(p.x, s.baro_eta);
+                p.y = __dmul_rn(p.y, s.baro_eta);
+                p.z = __dmul_rn(p.z, s.baro_eta);
+            }
             p.x = __dadd_rn(p.x, __dmul_rn(v.x, dt));
             p.y = __dadd_rn(p.y, __dmul_rn(v.y, dt));
             p.z = __dadd_rn(p.z, __dmul_rn(v.z, dt));
@@ -576,6 +586,30 @@ void launch_verlet_setup(const Batch& b, int s, int begin, int end, cudaStream_t
     if (end > begin)
         verlet_setup_kernel<<<(end - begin + 255) / 256, 256, 0, st>>>(begin, end, b.sys, s, b.posq, b.vel, b.acc);
 }
+// KineticEnergy::compute (sys/compute.rs:133-144) of every system at the
+// current velocities: one block per system, 0.5 m v.v per atom, a fixed-order
+// tree sum.
+__global__ void __launch_bounds__(256) kinetic_kernel(const SysDev* __restrict__ sys,
+                                                      const double4_32a* __restrict__ vel, double* __restrict__ out) {
+    __shared__ double sh[256];
+    const SysDev& s = sys[blockIdx.x];
+    double k = 0.0;
+    for (int i = s.begin + threadIdx.x; i < s.end; i += blockDim.x) {
+        double4_32a v = vel[i];
+        k += 0.5 * v.w * (v.x * v.x + v.y * v.y + v.z * v.z);
+    }
+    sh[threadIdx.x] = k;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = sh[0];
+}
+void launch_kinetic(const Batch& b, double* out, cudaStream_t st) {
+    if (b.nsys) kinetic_kernel<<<b.nsys, 256, 0, st>>>(b.sys, b.vel, out);
+}
+
 // A system's x, y, z (and w unless keep_w: the charge or mass of the new
 // description stays) moved to its new offset when the batch changes.
 __global__ void carry_vectors_kernel(int n, const double4_32a* __restrict__ src, double4_32a* __restrict__ dst,
@@ -588,6 +622,21 @@ __global__ void carry_vectors_kernel(int n, const double4_32a* __restrict__ src,
 }
 void launch_carry_vectors(const double4_32a* src, double4_32a* dst, int n, bool keep_w, cudaStream_t st) {
     if (n > 0) carry_vectors_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, src, dst, keep_w ? 1 : 0);
+}
+
+__global__ void identity_order_kernel(int n, int* __restrict__ cell_atoms, int* __restrict__ perm) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    cell_atoms[i] = i;
+    if (perm) perm[i] = i;
+}
+void launch_identity_order(const Batch& b, cudaStream_t st) {
+    if (b.n > 0) identity_order_kernel<<<(b.n + 255) / 256, 256, 0, st>>>(b.n, b.cell_atoms, b.perm);
+}
+
+__global__ void request_rebuild_flag_kernel(uint32_t* status) { atomicOr(status, ST_REBUILD); }
+void launch_request_rebuild_flag(const Batch& b, cudaStream_t st) {
+    if (b.status) request_rebuild_flag_kernel<<<1, 1, 0, st>>>(b.status);
 }
 
 void launch_request_rebuild(const Batch& b, cudaStream_t st) {

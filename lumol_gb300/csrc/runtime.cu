@@ -46,6 +46,11 @@ int recount_cells(lg_engine* e) {
     int rc = clear_status_bits(e, ST_CELL_OVF);
     if (rc) return rc;
     CUDA_TRY(e, cudaMemsetAsync(e->cell_count.p, 0, (size_t)e->b.ncells * sizeof(int), e->stream));
+    // The interrupted build may have left the cell order (cell_atoms) and its
+    // inverse (perm) incomplete: both go back to the identity, a consistent
+    // order that the rebuild replaces (the fixed-point copies are written
+    // through perm before the cells are binned from them).
+    launch_identity_order(e->b, e->stream);
     launch_request_rebuild(e->b, e->stream);
     return LG_OK;
 }
@@ -560,6 +565,118 @@ int build_md_graph(lg_engine* e, int steps, int mode) {
     e->graphs[steps] = exec;
     e->graph_nodes[steps] = nodes;
     e->graph_mode = mode;
+    return LG_OK;
+}
+
+// ---- Berendsen barostat -----------------------------------------------------------
+int md_run_barostat(lg_engine* e, int64_t nsteps) {
+    const double WATER_COMPRESSIBILITY = 7372.0;  // integrators.rs:171 (from DL_POLY)
+    const int mode = md_mode(e);
+    const bool thermo = (mode & MD_ADJUST) != 0;
+    cudaStream_t st = e->stream;
+    const int nsys = e->nsys;
+    CUDA_TRY(e, e->kin.alloc(nsys));
+    std::vector<double> kin(nsys), out((size_t)nsys * RED_STRIDE);
+    const size_t bytes = (size_t)e->b.n * sizeof(double4_32a);
+    const size_t cbytes = (size_t)nsys * sizeof(unsigned long long);
+    for (int64_t step = 0; step < nsteps; step++) {
+        // UnitCell::scale_mut(eta^3 * 1) of every barostat system (integrators.rs:227-236)
+        for (int s = 0; s < nsys; s++) {
+            HostSystem& h = e->sys[s];
+            if (h.barostat == LG_BAROSTAT_NONE) continue;
+            double eta = h.baro_eta;
+            double e3 = eta * eta * eta;
+            double L[3] = {h.L[0] * e3, h.L[1] * e3, h.L[2] * e3};
+            double rc = max_cutoff(h);
+            if (0.5 * L[0] <= rc || 0.5 * L[1] <= rc || 0.5 * L[2] <= rc)
+                return fail(e, LG_ERR_ARGUMENT,
+                            "Tried to decrease the cell size in Berendesen barostat but the new size is smaller "
+                            "than the interactions cut off radius. You can try to increase the cell size or the "
+                            "number of particles. (system " + std::to_string(s) + ")");
+            e->h_sysdev[s].baro_eta = eta;
+            int rc2 = set_cell_fast(e, s, L);
+            if (rc2 != LG_OK && rc2 != -1) return rc2;
+            if (rc2 == -1) {  // another cell grid or k-vector set: lower the batch again, keeping the state
+                for (int k = 0; k < 3; k++) h.L[k] = L[k];
+                invalidate(e);
+                int rc3 = commit_carried(e);
+                if (rc3) return rc3;
+                CUDA_TRY(e, e->kin.alloc(nsys));
+            }
+        }
+        CUDA_TRY(e, cudaMemcpyAsync(e->cp_pos.p, e->posq.p, bytes, cudaMemcpyDeviceToDevice, st));
+        CUDA_TRY(e, cudaMemcpyAsync(e->cp_vel.p, e->vel.p, bytes, cudaMemcpyDeviceToDevice, st));
+        CUDA_TRY(e, cudaMemcpyAsync(e->cp_acc.p, e->acc.p, bytes, cudaMemcpyDeviceToDevice, st));
+        if (thermo) CUDA_TRY(e, cudaMemcpyAsync(e->cp_count.p, e->md_count.p, cbytes, cudaMemcpyDeviceToDevice, st));
+        for (int attempt = 0;; attempt++) {
+            // the step: the first half (with the previous step's thermostat and
+            // controls), the forces with the virial, the kinetic energy of the
+            // half-step velocities, the second half
+            bool adjust = thermo && step > 0;
+            if (adjust && (mode & MD_REWRAP)) {
+                launch_rewrap(e->b, st);
+                e->launches += e->b.nmol ? 1 : 0;
+            }
+            launch_md_first(e->b, adjust, st);
+            CUDA_TRY(e, cudaMemsetAsync(e->red.p, 0, (size_t)e->b.n * RED_STRIDE * sizeof(double), st));
+            enqueue_forces(e, LG_TERM_ALL, true, st, !(mode & MD_VERLET_SYS));
+            launch_reduce(e->b, LG_TERM_ALL, e->b.nkvec != 0, e->out.p, st);
+            launch_kinetic(e->b, e->kin.p, st);
+            launch_md_second(e->b, st);
+            e->launches += (e->b.ntiles ? 2 : 0) + 2;
+            if (mode & MD_ADJUST) {
+                launch_md_adjust(e->b, st);
+                e->launches += 1;
+            }
+            CUDA_TRY(e, cudaGetLastError());
+            CUDA_TRY(e, cudaMemcpyAsync(kin.data(), e->kin.p, nsys * sizeof(double), cudaMemcpyDeviceToHost, st));
+            CUDA_TRY(e, cudaMemcpyAsync(out.data(), e->out.p, out.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                        st));
+            uint32_t status;
+            int rc = read_status(e, &status);
+            if (rc) return rc;
+            if (status & (ST_OVERFLOW | ST_CELL_OVF)) {
+                if (attempt >= 4) return fail(e, LG_ERR_CAPACITY, "neighbour list overflow persisted after regrowing");
+                CUDA_TRY(e, cudaMemcpyAsync(e->posq.p, e->cp_pos.p, bytes, cudaMemcpyDeviceToDevice, st));
+                CUDA_TRY(e, cudaMemcpyAsync(e->vel.p, e->cp_vel.p, bytes, cudaMemcpyDeviceToDevice, st));
+                CUDA_TRY(e, cudaMemcpyAsync(e->acc.p, e->cp_acc.p, bytes, cudaMemcpyDeviceToDevice, st));
+                if (thermo)
+                    CUDA_TRY(e, cudaMemcpyAsync(e->md_count.p, e->cp_count.p, cbytes, cudaMemcpyDeviceToDevice, st));
+                if (status & ST_CELL_OVF) {
+                    rc = recount_cells(e);
+                    if (rc) return rc;
+                }
+                if (status & ST_OVERFLOW) {
+                    rc = clear_status_bits(e, ST_OVERFLOW);
+                    if (rc) return rc;
+                    rc = regrow(e);
+                    if (rc) return rc;
+                }
+                continue;
+            }
+            if (status & ST_NONFINITE) {
+                e->nonfinite = true;
+                rc = clear_status_bits(e, ST_NONFINITE);
+                if (rc) return rc;
+            }
+            break;
+        }
+        // System::pressure at the new positions with the half-step velocities
+        // (Pressure, sys/compute.rs:399-431), and the next step's factor
+        for (int s = 0; s < nsys; s++) {
+            HostSystem& h = e->sys[s];
+            if (h.barostat == LG_BAROSTAT_NONE) continue;
+            const double* w = &out[(size_t)s * RED_STRIDE + 1];
+            double dof = (double)(3 * h.n);
+            double T = 2.0 * kin[s] / (dof * K_BOLTZMANN);  // Temperature (compute.rs:164-172)
+            double volume = h.L[0] * h.L[1] * h.L[2];
+            double P = (dof * K_BOLTZMANN * T + (w[0] + w[4] + w[8])) / (3.0 * volume);
+            double eta3 = 1.0 - WATER_COMPRESSIBILITY / h.baro_tau * (h.baro_pressure - P);
+            h.baro_eta = std::cbrt(eta3);
+        }
+    }
+    enqueue_md_finish(e, mode, st);
+    CUDA_TRY(e, cudaGetLastError());
     return LG_OK;
 }
 

@@ -817,6 +817,19 @@ class VelocityVerlet:
 
 
 @dataclass
+class BerendsenBarostat:
+    """BerendsenBarostat::new(timestep, pressure, tau) (md/integrators.rs:174-250):
+    Velocity-Verlet with the positions scaled by eta and the cell by eta^3 at
+    every step, eta^3 = 1 - 7372 / tau (pressure - P) from the pressure of the
+    previous step.  The cell changes on the device; MolecularDynamics.run
+    brings the new cell back into System.cell."""
+    timestep: float
+    pressure: float
+    tau: float
+    _kind = C.LG_INTEGRATOR_VELOCITY_VERLET
+
+
+@dataclass
 class Verlet:
     """Verlet::new(timestep) (md/integrators.rs:72-123): keeps the positions at
     t - dt, taken as x - v dt at setup."""
@@ -933,6 +946,9 @@ class MolecularDynamics:
         eng = system.engine()
         p = md_params(self.integrator, self.thermostat, self.controls)
         eng.call("lg_md_setup_ex", 0, ctypes.byref(p))
+        if isinstance(self.integrator, BerendsenBarostat):
+            eng.call("lg_md_set_barostat", 0, C.LG_BAROSTAT_BERENDSEN, float(self.integrator.pressure),
+                     float(self.integrator.tau))
         if system.velocities is None:
             system.velocities = np.zeros((system.size, 3))
         pos = np.ascontiguousarray(system.positions)
@@ -952,6 +968,11 @@ class MolecularDynamics:
         system.positions = pos
         system.velocities = vel
         system.step += int(nsteps)
+        if isinstance(self.integrator, BerendsenBarostat):  # the cell the barostat left
+            m = np.zeros(9)
+            eng.call("lg_get_cell", 0, C.dptr(m))
+            system.cell = UnitCell.ortho(m[0], m[4], m[8])
+            system._uploaded = system._version  # the engine already holds this cell
 
 
 # ---------------------------------------------------------------------------

@@ -105,6 +105,14 @@ def load() -> ctypes.CDLL:
         lib.orc_temperature.argtypes = [P, V]
         lib.orc_kinetic_energy.restype = ctypes.c_double
         lib.orc_kinetic_energy.argtypes = [P, V]
+        lib.orc_set_cell.argtypes = [P, ctypes.c_double, ctypes.c_double, ctypes.c_double]
+        lib.orc_get_cell.argtypes = [P, V]
+        lib.orc_maximum_cutoff.restype = ctypes.c_double
+        lib.orc_maximum_cutoff.argtypes = [P]
+        lib.orc_berendsen_barostat_run.restype = ctypes.c_int
+        lib.orc_berendsen_barostat_run.argtypes = [P, V, V, V, ctypes.POINTER(ctypes.c_double), ctypes.c_double,
+                                                   ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                                   ctypes.c_double, ctypes.c_int64]
         lib.orc_cache_init.argtypes = [P]
         lib.orc_cache_energy.restype = ctypes.c_double
         lib.orc_cache_energy.argtypes = [P]
@@ -286,6 +294,30 @@ class Oracle:
     def temperature(self, vel) -> float:
         vel = np.ascontiguousarray(vel, dtype=np.float64)
         return self.lib.orc_temperature(self.h, _ptr(vel))
+
+    def set_cell(self, lengths) -> None:
+        self.lib.orc_set_cell(self.h, *[float(x) for x in lengths])
+
+    def cell(self) -> np.ndarray:
+        out = np.zeros(3)
+        self.lib.orc_get_cell(self.h, _ptr(out))
+        return out
+
+    def berendsen_barostat(self, pos, vel, acc, eta, dt, pressure, tau, nsteps, temperature=0.0,
+                           tau_thermostat=0.0):
+        """BerendsenBarostat::integrate (+ an optional Berendsen thermostat) for
+        `nsteps` steps; returns (positions, velocities, accelerations, eta, cell
+        lengths).  Raises where the reference panics."""
+        pos = np.ascontiguousarray(pos, dtype=np.float64).copy()
+        vel = np.ascontiguousarray(vel, dtype=np.float64).copy()
+        acc = np.ascontiguousarray(acc, dtype=np.float64).copy()
+        e = ctypes.c_double(eta)
+        rc = self.lib.orc_berendsen_barostat_run(self.h, _ptr(pos), _ptr(vel), _ptr(acc), ctypes.byref(e), dt,
+                                                 pressure, tau, temperature, tau_thermostat, nsteps)
+        if rc:
+            raise RuntimeError("Tried to decrease the cell size in Berendesen barostat but the new size is "
+                               "smaller than the interactions cut off radius.")
+        return pos, vel, acc, e.value, self.cell()
 
     def cache_init(self) -> None:
         self.lib.orc_cache_init(self.h)

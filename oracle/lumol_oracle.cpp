@@ -1714,6 +1714,71 @@ void orc_pair_eval(const orc_pair* d, double r, double* energy, double* force, d
     *tail_virial = p.tail_virial_scalar();
 }
 
+// UnitCell::scale_mut of the orthorhombic cell (cells.rs:201-207) to new lengths;
+// Ewald::prepare recomputes its k-vectors for the new cell (ewald.rs:353-379).
+void orc_set_cell(orc_system* s, double a, double b, double c) {
+    s->cell.init(a, b, c);
+    s->factors_ready = false;
+}
+void orc_get_cell(const orc_system* s, double* out) {
+    out[0] = s->cell.a;
+    out[1] = s->cell.b;
+    out[2] = s->cell.c;
+}
+
+// Interactions::maximum_cutoff (interactions.rs:173-190): pair and Coulomb cutoffs
+double orc_maximum_cutoff(const orc_system* s) {
+    double rc = 0.0;
+    for (const PairPot& p : s->pairs)
+        if (p.d.type != ORC_PAIR_ABSENT) rc = std::max(rc, p.d.cutoff);
+    if (s->coul.kind != ORC_COULOMB_NONE) rc = std::max(rc, s->coul.cutoff);
+    return rc;
+}
+
+// BerendsenBarostat::integrate (lumol-sim/src/md/integrators.rs:213-250), then
+// the Berendsen thermostat when tau_thermostat > 0 (thermostats.rs:112-121), as
+// MolecularDynamics::propagate does, `nsteps` times.  `eta` (in / out) is the
+// scaling factor the next step applies (1 after setup).  Returns 1 where the
+// reference panics (a cell length at or below twice the maximum cutoff), with
+// the state of that step's first half.
+int orc_berendsen_barostat_run(orc_system* s, double* x, double* v, double* a, double* eta, double dt,
+                               double pressure, double tau, double T0, double tau_thermostat, int64_t nsteps) {
+    const double WATER_COMPRESSIBILITY = 7372.0;  // integrators.rs:171
+    int64_t n = s->n;
+    std::vector<double> f(3 * n);
+    for (int64_t step = 0; step < nsteps; step++) {
+        for (int64_t i = 0; i < 3 * n; i++) {
+            v[i] += 0.5 * dt * a[i];
+            x[i] *= *eta;
+            x[i] += v[i] * dt;
+        }
+        double e3 = *eta * *eta * *eta;
+        orc_set_cell(s, s->cell.a * e3, s->cell.b * e3, s->cell.c * e3);
+        double rc = orc_maximum_cutoff(s);
+        if (0.5 * s->cell.a <= rc || 0.5 * s->cell.b <= rc || 0.5 * s->cell.c <= rc) return 1;
+        // System::pressure (Pressure, compute.rs:399-431): (N_f k_B T + Tr W) / (3 V)
+        orc_set_positions(s, x);
+        double w[9];
+        orc_virial(s, ORC_TERM_ALL, w);
+        double T = orc_temperature(s, v);
+        double dof = (double)(3 * n);
+        double P = (dof * K_BOLTZMANN * T + (w[0] + w[4] + w[8])) / (3.0 * s->cell.volume());
+        double eta3 = 1.0 - WATER_COMPRESSIBILITY / tau * (pressure - P);
+        *eta = std::cbrt(eta3);
+        std::fill(f.begin(), f.end(), 0.0);
+        orc_forces(s, ORC_TERM_ALL, f.data());
+        for (int64_t i = 0; i < n; i++)
+            for (int k = 0; k < 3; k++) a[3 * i + k] = f[3 * i + k] / s->mass[i];
+        for (int64_t i = 0; i < 3 * n; i++) v[i] += 0.5 * dt * a[i];
+        if (tau_thermostat > 0.0) {
+            double Tt = orc_temperature(s, v);
+            double factor = std::sqrt(1.0 + (T0 / Tt - 1.0) / tau_thermostat);
+            for (int64_t i = 0; i < 3 * n; i++) v[i] *= factor;
+        }
+    }
+    return 0;
+}
+
 // EnergyCache::init (cache.rs:75-98)
 void orc_cache_init(orc_system* s) {
     int64_t n = s->n;

@@ -185,6 +185,20 @@ void orc_dihedrals(const orc_system* s, int32_t* out); /* 4 * n_dihedrals, sorte
 void orc_pair_eval(const orc_pair* p, double r, double* energy, double* force,
                    double* tail_energy, double* tail_virial);
 
+/* UnitCell::scale_mut (cells.rs:201-207) to new orthorhombic lengths, and the
+ * current lengths (3 doubles). */
+void orc_set_cell(orc_system* s, double a, double b, double c);
+void orc_get_cell(const orc_system* s, double* lengths);
+/* Interactions::maximum_cutoff (interactions.rs:173-190). */
+double orc_maximum_cutoff(const orc_system* s);
+/* BerendsenBarostat::integrate (lumol-sim/src/md/integrators.rs:213-250) and an
+ * optional Berendsen thermostat (tau_thermostat > 0), nsteps times; `eta` is
+ * the barostat's scaling factor (1 after setup, in / out).  Returns 1 where
+ * the reference panics (a cell length at or below twice the maximum cutoff). */
+int orc_berendsen_barostat_run(orc_system* s, double* positions, double* velocities, double* accelerations,
+                               double* eta, double dt, double pressure, double tau, double T0,
+                               double tau_thermostat, int64_t nsteps);
+
 /* EnergyCache (lumol-core/src/sys/cache.rs). */
 void orc_cache_init(orc_system* s);
 double orc_cache_energy(const orc_system* s);

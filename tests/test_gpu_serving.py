@@ -3,6 +3,9 @@ work overlapping on the device, each result the same alone and in the mix.
 
 Stated tolerance: final positions of a request served in the mix and the same
 request run alone in its own engine agree within 1e-9 A (FP64)."""
+import threading
+import time
+
 import numpy as np
 import pytest
 
@@ -108,7 +111,13 @@ def test_cancel_and_snapshot_restore():
 
     def control(server):
         server.cancel(victim.rid)
-        server.snapshot(traced.rid)
+
+        def later():  # a snapshot once the traced request has run some steps
+            t0 = time.perf_counter()
+            while traced.steps_done < 40 and time.perf_counter() - t0 < 30.0:
+                time.sleep(0.0005)
+            server.snapshot(traced.rid)
+        threading.Thread(target=later, daemon=True).start()
 
     server = Server(precision="fp64", chunk=20, max_lanes=2, threads_per_atom=8)
     done = server.run(requests, on_start=control)

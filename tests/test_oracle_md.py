@@ -109,3 +109,40 @@ def test_integrators_conserve_energy(oracle_lib):
         state = orc.verlet_setup(x0, v0, 1.0) if integrator == VERLET else np.zeros_like(x0)
         x, v, _, _ = orc.md_run(x0, v0, state, 300, integrator=integrator, dt=1.0)
         assert abs((total_energy(orc, x, v) - e0) / e0) < bound, integrator
+
+
+def test_berendsen_barostat_sequence(oracle_lib):
+    """The oracle's BerendsenBarostat follows integrators.rs:213-250 step by step:
+    v += dt/2 a; x *= eta; x += v dt; the cell matrix times eta^3; the pressure
+    (N_f k_B T + Tr W) / (3 V) at the new positions with the half-step
+    velocities (compute.rs:399-431) sets eta^3 = 1 - 7372 / tau (P0 - P) for
+    the next step; then the forces and the second half kick.  Restated here
+    with the oracle's own virial, forces and temperature."""
+    s = workloads.argon_fcc()
+    s.positions = s.positions + np.random.default_rng(3).uniform(-0.2, 0.2, size=(s.size, 3))
+    dt, P0, tau = 1.0, 4e-5, 20.0
+    orc = oracle.Oracle(s)
+    got = orc.berendsen_barostat(s.positions, s.velocities, np.zeros((s.size, 3)), 1.0, dt, P0, tau, 2)
+
+    ref = oracle.Oracle(s)
+    x, v, a, eta = s.positions.copy(), s.velocities.copy(), np.zeros((s.size, 3)), 1.0
+    L = np.array(s.cell.lengths)
+    m = s.masses[:, None]
+    for _ in range(2):
+        v = v + 0.5 * dt * a
+        x = x * eta
+        x = x + v * dt
+        L = L * (eta * eta * eta)
+        ref.set_cell(L)
+        ref.set_positions(x)
+        w = ref.virial()
+        dof = 3 * s.size
+        T = 2.0 * (0.5 * np.sum(m * v * v)) / (dof * K_BOLTZMANN)
+        P = (dof * K_BOLTZMANN * T + np.trace(w)) / (3.0 * np.prod(L))
+        eta = np.cbrt(1.0 - 7372.0 / tau * (P0 - P))
+        a = ref.forces() / m
+        v = v + 0.5 * dt * a
+    xg, vg, ag, etag, cellg = got
+    assert abs(etag - eta) < 1e-14 and np.allclose(cellg, L, rtol=1e-15, atol=0)
+    assert np.abs(xg - x).max() < 1e-12 and np.abs(vg - v).max() < 1e-14
+    assert etag != 1.0 and not np.allclose(L, s.cell.lengths)
