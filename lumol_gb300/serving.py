@@ -86,6 +86,21 @@ def footprint_bytes(system: System, precision: str, skin: float = 1.0) -> int:
     return n * per_atom + kbytes + (1 << 20)
 
 
+def lane_class(system) -> str:
+    """The lanes a request may join: "pairs" for systems with pair potentials
+    only (no Coulomb, bonds or restrictions: a mixed-precision batch of them
+    runs MD in one persistent launch per chunk), "general" for the others, so
+    that one Coulomb request does not move a lane of pair fluids onto the
+    general per-step kernels."""
+    if getattr(system, "coulomb", None) is not None or getattr(system, "bonds", None):
+        return "general"
+    for p in getattr(system, "pairs", {}).values():
+        r = p.restriction
+        if (r[0] if isinstance(r, tuple) else r) != 0:
+            return "general"
+    return "pairs"
+
+
 class Lane:
     """One engine holding a batch of requests, stepped by its own thread.
 
@@ -93,8 +108,9 @@ class Lane:
     `lock`); everything else, the engine included, belongs to the lane's
     thread."""
 
-    def __init__(self, server: "Server", first: list[Request]):
+    def __init__(self, server: "Server", first: list[Request], cls: str = "general"):
         self.server = server
+        self.cls = cls
         self.requests: list[Request] = []
         self.engine = None
         self.joining: list[Request] = list(first)
@@ -349,17 +365,20 @@ class Server:
                 self.stats.waited_for_memory += 1
                 rest.append(r)
                 continue
-            # a new lane while there are fewer than max_lanes (lanes step
-            # concurrently), else the least loaded lane with room
+            # a new lane of the request's class while that class has fewer than
+            # max_lanes (lanes step concurrently), else the least loaded lane of
+            # the class with room
+            cls = lane_class(r.system)
+            mine = [l for l in self.lanes if l.open and l.cls == cls]
             placed = False
-            if len([l for l in self.lanes if l.open]) < self.max_lanes:
-                lane = Lane(self, [r])
+            if len(mine) < self.max_lanes:
+                lane = Lane(self, [r], cls)
                 self.lanes.append(lane)
                 self.stats.lanes_opened += 1
                 lane.thread.start()
                 placed = True
             else:
-                for lane in sorted((l for l in self.lanes if l.open), key=lambda l: l.atoms):
+                for lane in sorted(mine, key=lambda l: l.atoms):
                     if lane.atoms + r.system.size <= self.lane_atoms and lane.try_join(r):
                         placed = True
                         break
