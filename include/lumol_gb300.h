@@ -391,8 +391,26 @@ int lg_mc_move_molecule_cost(lg_engine* e, int32_t s, int64_t molecule,
                              const double* new_positions, double* cost);
 /* EnergyCache::update (sys/cache.rs:118-127) after the move was applied:
  * `positions` are the molecule's positions after Translate::apply's
- * center-of-mass wrap (lumol-sim/src/mc/moves/translate.rs:114-125). */
+ * center-of-mass wrap (lumol-sim/src/mc/moves/translate.rs:114-125), or
+ * Rotate::apply's positions; after lg_mc_move_all_molecules_cost they are
+ * not read (may be NULL). */
 int lg_mc_update(lg_engine* e, int32_t s, const double* molecule_positions, double* energy);
+
+/* EnergyCache::move_all_molecules_cost (sys/cache.rs:238-292) for the
+ * configuration a Resize move prepares (lumol-sim/src/mc/moves/resize.rs:63-107):
+ * the new orthorhombic cell (9 doubles, row-major) and the new positions of
+ * every atom of system `s` (3n) are installed on the device and the change of
+ * the energy against the cache is returned (pairs, tail, Coulomb; the rigid
+ * molecules' bonded energies do not change).  Fails with the reference's
+ * message when a cell length is at most twice the maximum cutoff.  Then
+ * lg_mc_update keeps the new configuration (Resize::apply), or lg_mc_restore
+ * puts the previous cell and positions back (Resize::restore, resize.rs:121-124);
+ * a pending Resize is restored by the next cost call otherwise. */
+int lg_mc_move_all_molecules_cost(lg_engine* e, int32_t s, const double new_cell[9], const double* new_positions,
+                                  double* cost);
+/* Rejection of the pending move of system `s`: a pending Resize's previous
+ * configuration comes back; a single-molecule move has changed nothing. */
+int lg_mc_restore(lg_engine* e, int32_t s);
 
 /* Batched Monte Carlo: every system given lg_mc_setup runs its own Metropolis
  * chain of single-particle Translate moves on the device (MonteCarlo::propagate,

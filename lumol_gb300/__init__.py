@@ -32,6 +32,7 @@ from .system import (
     RemoveRotation,
     RemoveTranslation,
     RescaleThermostat,
+    Resize,
     Rewrap,
     Rotate,
     System,

@@ -3,6 +3,10 @@
 // Metropolis chains.
 #include "engine.h"
 
+namespace {
+int mc_restore_resize(lg_engine* e);
+}  // namespace
+
 extern "C" {
 
 int lg_mc_init(lg_engine* e, int32_t s, const double* positions, double* energy) {
@@ -34,6 +38,11 @@ int lg_mc_init(lg_engine* e, int32_t s, const double* positions, double* energy)
 int lg_mc_move_molecule_cost(lg_engine* e, int32_t s, int64_t molecule, const double* new_positions, double* cost) {
     if (!valid_sys(e, s) || !new_positions || !cost) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
     if (e->dirty || e->mc_sys != s) return fail(e, LG_ERR_STATE, "lg_mc_init was not called for this system");
+    if (e->mc_resize) {  // a Resize that was neither accepted nor restored: restored now
+        CUDA_TRY(e, cudaSetDevice(e->opt.device));
+        int rc0 = mc_restore_resize(e);
+        if (rc0) return rc0;
+    }
     const HostSystem& h = e->sys[s];
     if (molecule < 0 || molecule + 1 >= (int64_t)h.mol_begin.size())
         return fail(e, LG_ERR_ARGUMENT, "molecule index out of range");
@@ -69,12 +78,124 @@ int lg_mc_move_molecule_cost(lg_engine* e, int32_t s, int64_t molecule, const do
     return LG_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// The FP64 e^{ik.r} tables and rho(k) of the Monte Carlo system at the device
+// positions (what lg_mc_init computes; the single-molecule costs update them).
+void mc_refresh_kspace(lg_engine* e) {
+    Batch fb = e->b;
+    fb.precision = LG_PRECISION_FP64;
+    launch_kspace_part(fb, 0, false, e->stream);
+    launch_kspace_part(fb, 1, false, e->stream);
+    e->launches += 2;
+}
+
+// Installs cell lengths L for system s, in place when the cell grid and the
+// k-vector set allow it, else by lowering the batch again (state kept).
+int mc_set_cell(lg_engine* e, int s, const double L[3]) {
+    int rc = set_cell_fast(e, s, L);
+    if (rc != -1) return rc;
+    HostSystem& h = e->sys[s];
+    for (int k = 0; k < 3; k++) h.L[k] = L[k];
+    invalidate(e);
+    return commit_carried(e);
+}
+
+// Resize::restore (mc/moves/resize.rs:121-124) of a pending
+// move_all_molecules_cost: the previous cell and positions come back.
+int mc_restore_resize(lg_engine* e) {
+    if (!e->mc_resize) return LG_OK;
+    int s = e->mc_sys;
+    e->mc_resize = false;
+    e->mc_pending = false;
+    int rc = mc_set_cell(e, s, e->mc_old_L);
+    if (rc) return rc;
+    const HostSystem& h = e->sys[s];
+    CUDA_TRY(e, cudaMemcpyAsync(e->posq.p + e->begin[s], e->mc_saved_pos.p, h.n * sizeof(double4_32a),
+                                cudaMemcpyDeviceToDevice, e->stream));
+    launch_request_rebuild(e->b, e->stream);
+    e->shadow_valid = false;
+    mc_refresh_kspace(e);
+    CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+    CUDA_TRY(e, cudaGetLastError());
+    return LG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lg_mc_move_all_molecules_cost(lg_engine* e, int32_t s, const double new_cell[9], const double* new_positions,
+                                  double* cost) {
+    if (!valid_sys(e, s) || !new_cell || !new_positions || !cost) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    if (e->dirty || e->mc_sys != s) return fail(e, LG_ERR_STATE, "lg_mc_init was not called for this system");
+    for (int a = 0; a < 3; a++)
+        for (int c = 0; c < 3; c++)
+            if (a != c && new_cell[3 * a + c] != 0.0)
+                return fail(e, LG_ERR_ARGUMENT, "only orthorhombic cells are supported");
+    const double L[3] = {new_cell[0], new_cell[4], new_cell[8]};
+    if (!(L[0] > 0.0 && L[1] > 0.0 && L[2] > 0.0)) return fail(e, LG_ERR_ARGUMENT, "Cell lengths must be positive");
+    CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    int rc = mc_restore_resize(e);  // a previous Resize that was neither accepted nor restored
+    if (rc) return rc;
+    HostSystem& h = e->sys[s];
+    double rcut = max_cutoff(h);
+    if (0.5 * L[0] <= rcut || 0.5 * L[1] <= rcut || 0.5 * L[2] <= rcut)  // resize.rs:76-86
+        return fail(e, LG_ERR_ARGUMENT,
+                    "Tried to decrease the cell size in Monte Carlo Resize move but the new size is smaller than "
+                    "the interactions cut off radius. You can try to increase the cell size or the number of "
+                    "particles.");
+    cudaStream_t st = e->stream;
+    CUDA_TRY(e, e->mc_saved_pos.alloc(std::max<int64_t>(h.n, 1)));
+    CUDA_TRY(e, cudaMemcpyAsync(e->mc_saved_pos.p, e->posq.p + e->begin[s], h.n * sizeof(double4_32a),
+                                cudaMemcpyDeviceToDevice, st));
+    for (int k = 0; k < 3; k++) e->mc_old_L[k] = h.L[k];
+    rc = mc_set_cell(e, s, L);
+    if (rc) return rc;
+    rc = upload_positions(e, s, new_positions);
+    if (rc) return rc;
+    rc = compute_batch(e, LG_TERM_ALL, LG_WANT_ENERGY, nullptr, nullptr);
+    if (rc) return rc;
+    CUDA_TRY(e, cudaMemcpyAsync(e->h_out, e->out.p + (size_t)s * RED_STRIDE, sizeof(double), cudaMemcpyDeviceToHost,
+                                st));
+    CUDA_TRY(e, cudaStreamSynchronize(st));
+    // the rigid molecules keep their bonded energies: the change of the total
+    // is the change of the pairs, tails and Coulomb terms
+    e->mc_pending_cost = e->h_out[0] - e->mc_energy;
+    e->mc_pending = true;
+    e->mc_resize = true;
+    *cost = e->mc_pending_cost;
+    return LG_OK;
+}
+
+int lg_mc_restore(lg_engine* e, int32_t s) {
+    if (!valid_sys(e, s)) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    if (e->mc_sys != s) return fail(e, LG_ERR_STATE, "lg_mc_init was not called for this system");
+    CUDA_TRY(e, cudaSetDevice(e->opt.device));
+    int rc = mc_restore_resize(e);
+    e->mc_pending = false;
+    return rc;
+}
+
 int lg_mc_update(lg_engine* e, int32_t s, const double* molecule_positions, double* energy) {
-    if (!valid_sys(e, s) || !molecule_positions) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    if (!valid_sys(e, s)) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
     if (!e->mc_pending || e->mc_sys != s)
         return fail(e, LG_ERR_STATE, "called EnergyCache::update without call a `*_cost` function first");
     CUDA_TRY(e, cudaSetDevice(e->opt.device));
     cudaStream_t st = e->stream;
+    if (e->mc_resize) {  // the new cell and positions stay
+        e->mc_resize = false;
+        mc_refresh_kspace(e);
+        CUDA_TRY(e, cudaStreamSynchronize(st));
+        CUDA_TRY(e, cudaGetLastError());
+        e->mc_energy += e->mc_pending_cost;
+        e->mc_pending = false;
+        if (energy) *energy = e->mc_energy;
+        return LG_OK;
+    }
+    if (!molecule_positions) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
     int msize = (int)e->mc_mol_size;
     const SysDev& sd = e->h_sysdev[s];
     CUDA_TRY(e, cudaMemcpyAsync(e->mc_newpos.p, molecule_positions, 3 * msize * sizeof(double),

@@ -215,6 +215,10 @@ struct lg_engine {
     bool mc_pending = false;
     int mc_sys = -1;
     int64_t mc_mol_begin = 0, mc_mol_size = 0;
+    // a pending move_all_molecules_cost: the configuration before the move
+    bool mc_resize = false;
+    double mc_old_L[3] = {0, 0, 0};
+    DBuf<double4_32a> mc_saved_pos;
 
     void drop_graphs() {
         for (auto& g : graphs) cudaGraphExecDestroy(g.second);

@@ -999,6 +999,29 @@ class Rotate:
         self.theta = float(theta)
 
 
+class Resize:
+    """Resize move (mc/moves/resize.rs:14-128) for NPT Monte Carlo: the volume
+    changes by a uniform delta in [-delta, delta), the cell is scaled by
+    cbrt((V + delta) / V) and every molecule moves with its centre of mass
+    (fractional coordinates kept); the cost is
+    beta (dE + P dV) - N_molecules ln(V' / V), dE from
+    EnergyCache::move_all_molecules_cost on the GPU."""
+
+    def __init__(self, pressure: float, delta: float):
+        if not delta > 0.0:
+            raise ValueError("delta must be positive in Resize move")
+        self.pressure = float(pressure)
+        self.delta = float(delta)
+
+
+def _ortho_inverse(L) -> np.ndarray:
+    """The diagonal of Matrix3::inverse of diag(a, b, c) (types/matrix.rs:212-227)."""
+    a, b, c = (float(x) for x in L)
+    det = a * (b * c - 0.0 * 0.0) - 0.0 * (0.0 * c - 0.0 * 0.0) + 0.0 * (0.0 * 0.0 - b * 0.0)
+    inv = 1.0 / det
+    return np.array([(b * c - 0.0 * 0.0) * inv, (a * c - 0.0 * 0.0) * inv, (a * b - 0.0 * 0.0) * inv])
+
+
 def _rotation(axis: np.ndarray, angle: float) -> np.ndarray:
     """Matrix3::rotation (types/matrix.rs:149-169) around `axis` (normalised):
     the matrix with the reference's sign convention, which turns e3 into e2
@@ -1024,7 +1047,7 @@ class MonteCarlo:
         from .units import K_BOLTZMANN
         self.temperature = float(temperature)
         self.beta = 1.0 / (K_BOLTZMANN * temperature)
-        moves = [(move, 1.0)] if isinstance(move, (Translate, Rotate)) else [(m, float(f)) for m, f in move]
+        moves = [(move, 1.0)] if isinstance(move, (Translate, Rotate, Resize)) else [(m, float(f)) for m, f in move]
         if not moves or any(not f > 0.0 for _, f in moves):
             raise ValueError("MonteCarlo needs moves with positive frequencies")
         self.moves = [m for m, _ in moves]
@@ -1044,12 +1067,56 @@ class MonteCarlo:
         system.simulated_degrees_of_freedom = "molecules"
         self.energy = system.mc_init()
 
+    def _resize(self, system: System, move: Resize) -> None:
+        """Resize::prepare / cost / apply / restore (resize.rs:63-124)."""
+        eng = system.engine()
+        L = np.array(system.cell.lengths, dtype=np.float64)
+        volume = float(L[0] * L[1] * L[2])
+        delta = self.rng.uniform(-move.delta, move.delta)
+        scaling = np.cbrt((volume + delta) / volume)
+        L_new = L * scaling  # UnitCell::scale_mut(Matrix3::one() * scaling)
+        inv = _ortho_inverse(L)
+        pos = system.positions
+        newpos = pos.copy()
+        m = system.masses
+        for mol in range(int(system.molecules[-1]) + 1):
+            lo, hi = system.molecule_range(mol)
+            total, com = 0.0, np.zeros(3)
+            for a in range(lo, hi):  # Molecule::center_of_mass (molecules.rs:256-264)
+                total += m[a]
+                com = com + m[a] * pos[a]
+            com = com / total
+            frac = inv * com            # previous.cell.fractional(com)
+            delta_com = L_new * frac - com  # cell.cartesian(frac) - com
+            newpos[lo:hi] = pos[lo:hi] + delta_com
+        cell = np.diag(L_new).ravel().copy()
+        de = ctypes.c_double(0.0)
+        eng.call("lg_mc_move_all_molecules_cost", 0, C.dptr(cell), C.dptr(np.ascontiguousarray(newpos)),
+                 ctypes.byref(de))
+        new_volume = float(L_new[0] * L_new[1] * L_new[2])
+        nmol = int(system.molecules[-1]) + 1
+        cost = self.beta * (de.value + move.pressure * (new_volume - volume)) - nmol * np.log(new_volume / volume)
+        self.attempted += 1
+        if cost <= 0.0 or self.rng.random() < np.exp(-cost):
+            energy = ctypes.c_double(0.0)
+            eng.call("lg_mc_update", 0, None, ctypes.byref(energy))
+            self.energy = energy.value
+            system.cell = UnitCell.ortho(*L_new)
+            system.positions = newpos
+            system._uploaded = system._version  # the engine holds the new cell and positions
+            self.accepted += 1
+        else:
+            eng.call("lg_mc_restore", 0)
+
     def propagate(self, system: System) -> None:
         nmol = int(system.molecules[-1]) + 1
-        molid = int(self.rng.integers(nmol))
-        lo, hi = system.molecule_range(molid)
         move = self.moves[int(self.rng.choice(len(self.moves), p=self.frequencies))] if len(self.moves) > 1 \
             else self.moves[0]
+        if isinstance(move, Resize):
+            self._resize(system, move)
+            return
+        molid = int(self.rng.integers(nmol))
+        lo, hi = system.molecule_range(molid)
         if isinstance(move, Rotate):
             pos = system.positions[lo:hi]
             m = system.masses[lo:hi, None]

@@ -113,6 +113,9 @@ def load() -> ctypes.CDLL:
         lib.orc_berendsen_barostat_run.argtypes = [P, V, V, V, ctypes.POINTER(ctypes.c_double), ctypes.c_double,
                                                    ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                                    ctypes.c_double, ctypes.c_int64]
+        lib.orc_move_all_molecules_cost.restype = ctypes.c_double
+        lib.orc_move_all_molecules_cost.argtypes = [P, V, V]
+        lib.orc_cache_restore.argtypes = [P]
         lib.orc_cache_init.argtypes = [P]
         lib.orc_cache_energy.restype = ctypes.c_double
         lib.orc_cache_energy.argtypes = [P]
@@ -331,6 +334,14 @@ class Oracle:
 
     def cache_update(self) -> None:
         self.lib.orc_cache_update(self.h)
+
+    def move_all_molecules_cost(self, cell_lengths, newpos) -> float:
+        cell = np.ascontiguousarray(cell_lengths, dtype=np.float64)
+        newpos = np.ascontiguousarray(newpos, dtype=np.float64)
+        return self.lib.orc_move_all_molecules_cost(self.h, _ptr(cell), _ptr(newpos))
+
+    def cache_restore(self) -> None:
+        self.lib.orc_cache_restore(self.h)
 
 
 def _orc_bonded(pot) -> OrcBonded:

@@ -512,6 +512,13 @@ struct orc_system {
     std::vector<double> pending_new_pairs;  // rows of the moved molecule: [local i][j]
     double pending_pairs_delta = 0, pending_coulomb_delta = 0;
     std::vector<Complex> pending_delta_rho;
+    // move_all_molecules_cost (cache.rs:238-292): the pending update, and the
+    // configuration before the move (the Resize move's `previous`)
+    bool pending_all = false;
+    std::vector<double> pending_all_pairs;  // [i * n + j], between molecules
+    double pending_all_tail = 0, pending_all_coulomb = 0;
+    double saved_cell[3] = {0, 0, 0};
+    std::vector<V3> saved_pos;
 
     const PairPot* pair(int64_t i, int64_t j) const {
         const PairPot& p = pairs[(size_t)kind[i] * nk + kind[j]];
@@ -1925,8 +1932,74 @@ double orc_move_molecule_cost(orc_system* s, int64_t molid, const double* newp) 
     return pairs_delta + coulomb_delta;
 }
 
+// EnergyCache::move_all_molecules_cost (cache.rs:238-292) for the configuration
+// a Resize move prepared (resize.rs:70-107): the new cell and positions are
+// installed (the Resize move changed the System before the cost), pairs
+// between different molecules are evaluated again against the cache, the
+// Coulomb energy and the tail correction in full.  orc_cache_update keeps the
+// new configuration, orc_cache_restore puts the previous one back.
+double orc_move_all_molecules_cost(orc_system* s, const double* cell, const double* newp) {
+    int64_t n = s->n;
+    s->saved_cell[0] = s->cell.a;
+    s->saved_cell[1] = s->cell.b;
+    s->saved_cell[2] = s->cell.c;
+    s->saved_pos = s->pos;
+    orc_set_cell(s, cell[0], cell[1], cell[2]);
+    orc_set_positions(s, newp);
+    s->pending_all_pairs.assign((size_t)(n * n), 0.0);
+    double pairs_delta = 0.0;
+    for (size_t mi = 0; mi < s->mol_range.size(); mi++)
+        for (size_t mj = mi + 1; mj < s->mol_range.size(); mj++)
+            for (int64_t i = s->mol_range[mi].first; i < s->mol_range[mi].second; i++)
+                for (int64_t j = s->mol_range[mj].first; j < s->mol_range[mj].second; j++) {
+                    double r = s->distance(i, j);
+                    double e = pair_energy_ij(s, s->bond_path(i, j), r, i, j);
+                    pairs_delta += e;
+                    s->pending_all_pairs[(size_t)(i * n + j)] += e;
+                    s->pending_all_pairs[(size_t)(j * n + i)] += e;
+                    pairs_delta -= s->pairs_cache[(size_t)(i * n + j)];
+                }
+    double new_coulomb = coulomb_energy_terms(s, ORC_TERM_ALL);
+    double tail = pairs_tail(s);
+    double cost = pairs_delta + (tail - s->c_tail) + (new_coulomb - s->c_coulomb);
+    s->pending_pairs_delta = pairs_delta;
+    s->pending_all_tail = tail;
+    s->pending_all_coulomb = new_coulomb;
+    s->pending_all = true;
+    s->has_pending = false;
+    return cost;
+}
+
+// Resize::restore (resize.rs:121-124): the previous configuration back; the
+// pending update is dropped.
+void orc_cache_restore(orc_system* s) {
+    if (s->pending_all) {
+        orc_set_cell(s, s->saved_cell[0], s->saved_cell[1], s->saved_cell[2]);
+        s->pos = s->saved_pos;
+    }
+    s->pending_all = false;
+    s->has_pending = false;
+}
+
 // EnergyCache::update (cache.rs:118-127) running the closure of cache.rs:190-218
+// (or of cache.rs:274-290 after move_all_molecules_cost)
 void orc_cache_update(orc_system* s) {
+    if (s->pending_all) {
+        int64_t n = s->n;
+        s->c_pairs += s->pending_pairs_delta;
+        s->c_tail = s->pending_all_tail;
+        s->c_coulomb = s->pending_all_coulomb;
+        for (size_t mi = 0; mi < s->mol_range.size(); mi++)
+            for (size_t mj = mi + 1; mj < s->mol_range.size(); mj++)
+                for (int64_t i = s->mol_range[mi].first; i < s->mol_range[mi].second; i++)
+                    for (int64_t j = s->mol_range[mj].first; j < s->mol_range[mj].second; j++) {
+                        double e = s->pending_all_pairs[(size_t)(i * n + j)];
+                        s->pairs_cache[(size_t)(i * n + j)] = e;
+                        s->pairs_cache[(size_t)(j * n + i)] = e;
+                    }
+        s->pending_all = false;
+        return;
+    }
     if (!s->has_pending) return;
     int64_t n = s->n;
     int64_t start = s->mol_range[s->pending_mol].first, end = s->mol_range[s->pending_mol].second;

@@ -204,6 +204,12 @@ void orc_cache_init(orc_system* s);
 double orc_cache_energy(const orc_system* s);
 double orc_move_molecule_cost(orc_system* s, int64_t molecule, const double* new_positions);
 void orc_cache_update(orc_system* s);
+/* EnergyCache::move_all_molecules_cost (cache.rs:238-292) of a Resize move's
+ * configuration: new cell lengths (3) and positions (3n), installed in the
+ * system; orc_cache_update keeps them, orc_cache_restore puts the previous
+ * configuration back (Resize::restore, mc/moves/resize.rs:121-124). */
+double orc_move_all_molecules_cost(orc_system* s, const double* cell_lengths, const double* new_positions);
+void orc_cache_restore(orc_system* s);
 
 #ifdef __cplusplus
 }

@@ -345,6 +345,49 @@ def test_cache_cost_is_energy_difference(oracle_lib, coulomb):
     assert abs(orc.cache_energy() - e_after) <= 1e-9 * max(1.0, abs(e_after))
 
 
+# ---- sys/cache.rs:450-484 (move_all_molecules) and a Resize-like cell change --------------
+@pytest.mark.parametrize("coulomb", ["none", "ewald", "wolf"])
+def test_cache_all_molecules_cost_is_energy_difference(oracle_lib, coulomb):
+    """cost == E(new) - E(old) (cache.rs:450-484, epsilon 1e-12 there) for a
+    rigid translation of every molecule, then for a Resize of the cell with
+    the centres of mass scaled (resize.rs:70-107); the update keeps the new
+    configuration, the restore puts the old one back."""
+    import lumol_gb300 as lg
+    mk = lambda: systems.chains(8, 22.0, 3, lg.PairRestriction.INTER_MOLECULAR,
+                                coulomb={"none": None, "ewald": lg.Ewald(9.0, 5, 0.35),
+                                         "wolf": lg.Wolf(9.0)}[coulomb])
+    s = mk()
+    orc = oracle.Oracle(s)
+    orc.cache_init()
+    e0 = orc.energy()
+    L = np.array(s.cell.lengths)
+    pos1 = s.positions + np.array([-0.9, 0.0, 1.8])
+    cost = orc.move_all_molecules_cost(L, pos1)
+    ref = oracle.Oracle(mk())
+    ref.set_positions(pos1)
+    e1 = ref.energy()
+    assert abs(cost - (e1 - e0)) <= 1e-10 * max(1.0, abs(e0))
+    orc.cache_update()
+    assert abs(orc.cache_energy() - e1) <= 1e-10 * max(1.0, abs(e1))
+    # a Resize: cell x 1.02, each molecule moved with its centre of mass
+    L2 = L * 1.02
+    m = s.masses
+    pos2 = pos1.copy()
+    for mol in range(int(s.molecules.max()) + 1):
+        lo, hi = s.molecule_range(mol)
+        com = (m[lo:hi, None] * pos1[lo:hi]).sum(axis=0) / m[lo:hi].sum()
+        pos2[lo:hi] += com / L * L2 - com
+    cost2 = orc.move_all_molecules_cost(L2, pos2)
+    ref2 = oracle.Oracle(mk())
+    ref2.set_cell(L2)
+    ref2.set_positions(pos2)
+    e2 = ref2.energy()
+    assert abs(cost2 - (e2 - e1)) <= 1e-10 * max(1.0, abs(e0))
+    orc.cache_restore()  # rejected: back to the translated configuration
+    assert np.allclose(orc.cell(), L, rtol=0, atol=0)
+    assert abs(orc.energy() - e1) <= 1e-12 * max(1.0, abs(e1))
+
+
 # ---- tests/nist-lj.rs ----------------------------------------------------------------------
 @needs_reference
 @pytest.mark.parametrize("case", range(8))
