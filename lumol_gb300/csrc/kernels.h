@@ -102,6 +102,11 @@ struct PkArgs {
     int nsteps;
     int thermo;                   // some system has a thermostat
     int stage;                    // > 0: every block stages this many atoms' positions in shared memory
+    // the state before the launch, written by its first step (a replay after a
+    // list overflow restores it); the kernel also clears its group flags
+    double4_32a* cp_pos;
+    double4_32a* cp_vel;
+    double4_32a* cp_acc;
 };
 constexpr int PK_STAGE_MAX = 9216;  // atoms a group may stage (20 bytes each)
 cudaError_t launch_md_persist(const Batch& b, const PkArgs& a, int cluster, cudaStream_t st);
@@ -134,6 +139,8 @@ void launch_unpack_vectors(int n, const double4_32a* src, double* dst3, cudaStre
 void launch_unpack_positions(const Batch& b, double* pos3, cudaStream_t st);
 void launch_pack_velocities(const Batch& b, const double* vel3, cudaStream_t st);
 void launch_unpack_velocities(const Batch& b, double* vel3, cudaStream_t st);
+// Positions and velocities of atoms [0, b.n) into 3n arrays, in one launch.
+void launch_unpack_state(const Batch& b, double* pos3, double* vel3, cudaStream_t st);
 constexpr int VV_TILE = 256;
 void launch_md_first(const Batch& b, bool adjust, cudaStream_t st);
 void launch_md_second(const Batch& b, cudaStream_t st);

@@ -58,6 +58,22 @@ void launch_unpack_velocities(const Batch& b, double* vel3, cudaStream_t st) {
     launch_unpack3(b.n, b.vel, vel3, st);
 }
 
+__global__ void unpack_state_kernel(int n3, const double* __restrict__ pos4, const double* __restrict__ vel4,
+                                    double* __restrict__ pos3, double* __restrict__ vel3) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n3) return;
+    int i = t / 3;
+    int c = 4 * i + (t - 3 * i);
+    pos3[t] = pos4[c];
+    vel3[t] = vel4[c];
+}
+void launch_unpack_state(const Batch& b, double* pos3, double* vel3, cudaStream_t st) {
+    if (b.n)
+        unpack_state_kernel<<<(3 * b.n + 255) / 256, 256, 0, st>>>(3 * b.n, reinterpret_cast<const double*>(b.posq),
+                                                                  reinterpret_cast<const double*>(b.vel), pos3,
+                                                                  vel3);
+}
+
 // Marks system si for a list rebuild.  The flag store is idempotent; the
 // status word gets one atomic per warp, not one per moved atom.
 __device__ __forceinline__ void flag_rebuild(bool moved, int si, uint32_t* status, uint32_t* sys_rebuild) {

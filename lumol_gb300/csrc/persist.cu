@@ -106,6 +106,8 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
         s_apre[G] = acc;
         s_qpre[G] = chunks;
     }
+    // the group flag is read only after a cluster barrier: cleared here for this launch
+    if (rank == 0 && threadIdx.x == 0) a.group_flag[g] = 0;
     __syncthreads();
     const int A = s_apre[G];
     const int QQ = s_qpre[G];
@@ -130,6 +132,11 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
             const SysDev& sd = b.sys[s];
             int i = sd.begin + (v - s_apre[r]);
             double4_32a vel = b.vel[i], acc = b.acc[i], p = b.posq[i];
+            if (step == 0 && a.cp_pos) {  // the launch's checkpoint
+                a.cp_pos[i] = p;
+                a.cp_vel[i] = vel;
+                a.cp_acc[i] = acc;
+            }
             if (apply) {
                 double f = s_lambda[r];
                 vel.x *= f;

@@ -205,6 +205,15 @@ int get_state(lg_engine* e, int64_t base, int64_t n, double* positions, double* 
     sub.n = (int)n;
     sub.posq = e->posq.p + base;
     sub.vel = e->vel.p + base;
+    if (positions && velocities) {  // one launch for both when the host arrays are page-locked
+        double* dp = (double*)mapped_host(positions);
+        double* dv = (double*)mapped_host(velocities);
+        if (dp && dv) {
+            launch_unpack_state(sub, dp, dv, st);
+            e->launches += 1;
+            return LG_OK;
+        }
+    }
     if (positions) {
         double* dp = (double*)mapped_host(positions);
         launch_unpack_positions(sub, dp ? dp : e->pos3.p + 3 * base, st);
@@ -498,12 +507,9 @@ int md_run_persistent(lg_engine* e, int64_t nsteps, bool thermo) {
         if (it == e->pk_graphs.end()) {
             cudaGraph_t g;
             CUDA_TRY(e, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-            cudaMemcpyAsync(e->cp_pos.p, e->posq.p, bytes, cudaMemcpyDeviceToDevice, st);
-            cudaMemcpyAsync(e->cp_vel.p, e->vel.p, bytes, cudaMemcpyDeviceToDevice, st);
-            cudaMemcpyAsync(e->cp_acc.p, e->acc.p, bytes, cudaMemcpyDeviceToDevice, st);
-            cudaMemsetAsync(e->pk_group_flag.p, 0, e->pk_groups * sizeof(int), st);
+            // (the kernel's first step writes the checkpoint and clears the group flags)
             PkArgs a{e->pk_groups, e->pk_group_off.p, e->pk_group_sys.p, e->pk_group_flag.p, e->pk_ke.p, steps,
-                     thermo ? 1 : 0, e->pk_stage};
+                     thermo ? 1 : 0, e->pk_stage, e->cp_pos.p, e->cp_vel.p, e->cp_acc.p};
             cudaError_t le = launch_md_persist(e->b, a, e->pk_cluster, st);
             cudaError_t ce = cudaStreamEndCapture(st, &g);
             if (le != cudaSuccess) return fail(e, LG_ERR_CUDA, std::string("persistent launch: ") + cudaGetErrorString(le));

@@ -24,7 +24,7 @@ pytestmark = pytest.mark.gpu
 def _pressure(system):
     """System::pressure at the system's positions and velocities (compute.rs:399-431)."""
     from lumol_gb300.units import K_BOLTZMANN
-    w = system.compute(lg.LG_TERM_ALL, lg.LG_WANT_VIRIAL)[2]
+    w = system.compute(C.LG_TERM_ALL, C.LG_WANT_VIRIAL)[2]
     dof = 3 * system.size
     T = 2.0 * system.kinetic_energy() / (dof * K_BOLTZMANN)
     return (dof * K_BOLTZMANN * T + np.trace(w)) / (3.0 * system.cell.volume())
