@@ -709,6 +709,8 @@ def config_legs(args, local):
                  "requests": len(done), "rate_per_s": 40.0, "latency_s": {"p50": p50, "p99": p99},
                  "span_s": span, "lanes_max": server.stats.max_lanes, "joins": server.stats.joins,
                  "leaves": server.stats.leaves, "failed": server.stats.failed,
+                 "lane_host_s": {"join": server.stats.join_s, "run": server.stats.run_s,
+                                 "boundary": server.stats.boundary_s},
                  "workload": "seeded Poisson stream: 60% LJ (200-20000 atoms), 25% NaCl+Ewald (216-8000 ions), "
                              "15% water (300-3000 molecules), 500-5000 steps each, mixed precision"}
     return out

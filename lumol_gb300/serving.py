@@ -225,7 +225,9 @@ class Lane:
 
     def _run_chunk(self) -> None:
         steps = max(0, min(self.server.chunk, min(r.nsteps - r.steps_done for r in self.requests)))
+        t0 = time.perf_counter()
         code = self.engine.run_steps(steps)
+        self.server.stats.run_s += time.perf_counter() - t0
         if code == C.LG_ERR_NONFINITE:  # the flagged requests fail; the others completed the chunk
             flags = (ctypes.c_uint32 * len(self.requests))()
             self.engine.call("lg_system_status", flags, 1)
@@ -245,7 +247,9 @@ class Lane:
     def _serve(self) -> None:
         try:
             while True:
+                t0 = time.perf_counter()
                 self._take_joins()
+                self.server.stats.join_s += time.perf_counter() - t0
                 if not self.requests:
                     with self.lock:
                         if not self.joining:
@@ -253,10 +257,14 @@ class Lane:
                             break
                     continue
                 # requests that joined or were controlled before their first chunk
+                t0 = time.perf_counter()
                 self._boundary()
+                self.server.stats.boundary_s += time.perf_counter() - t0
                 if self.requests:
                     self._run_chunk()
+                    t0 = time.perf_counter()
                     self._boundary()
+                    self.server.stats.boundary_s += time.perf_counter() - t0
         except BaseException as exc:  # a lane that fails reports every request it holds
             with self.lock:
                 self.open = False
@@ -282,6 +290,12 @@ class ServerStats:
     waited_for_memory: int = 0
     failed: int = 0
     atom_steps: int = 0
+    # host seconds the lane threads spent (summed over lanes): taking in joins
+    # (description lowering), running chunks (device work + the first run's
+    # re-lowering after a change), retiring at boundaries (state reads, leaves)
+    join_s: float = 0.0
+    run_s: float = 0.0
+    boundary_s: float = 0.0
 
 
 class Server:

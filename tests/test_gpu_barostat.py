@@ -45,17 +45,19 @@ def _run(make, precision, pressure, tau, runs):
     return out
 
 
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("mixed", 1e-6)])
-def test_barostat_argon_compression_changes_the_cell_grid(precision, tol):
+@pytest.mark.parametrize("precision,tol,cell_tol", [("fp64", 1e-9, 1e-12), ("mixed", 1e-6, 1e-7)])
+def test_barostat_argon_compression_changes_the_cell_grid(precision, tol, cell_tol):
+    """(The mixed path's pressure carries the FP32 pair virial's ~1e-6 relative
+    error, hence its looser cell tolerance.)"""
     base = workloads.argon_fcc()
-    target = _pressure(base) + units.from_(5000.0, "bar")  # compresses the box by ~1 % per step
-    out = _run(lambda p: workloads.argon_fcc(precision=p), precision, target, 10.0, [1, 2, 3, 5])
-    L0 = base.cell.lengths[0]
+    target = _pressure(base) + units.from_(10000.0, "bar")  # compresses the box by ~5 % in 6 steps
+    out = _run(lambda p: workloads.argon_fcc(precision=p), precision, target, 30.0, [1, 2, 3, 5, 8])
     for x, v, cell, xo, vo, cello in out:
-        assert np.abs(cell - cello).max() <= 1e-12 * cello.max(), (cell, cello)
+        assert np.abs(cell - cello).max() <= cell_tol * cello.max(), (cell, cello)
         assert np.abs(x - xo).max() < tol, np.abs(x - xo).max()
-    # the box shrank through a change of the list's cell grid (5 -> 4 cells per axis at rc + skin = 11 A)
-    assert out[-1][2][0] < L0 * 0.955, (L0, out[-1][2][0])
+    # the box shrank through a change of the list's cell grid (5 -> 4 cells per
+    # axis below 27.5 A, cells at least (rc + skin) / 2 = 5.5 A wide)
+    assert out[-1][2][0] < 27.5, out[-1][2][0]
 
 
 def test_barostat_nacl_ewald_follows_the_oracle():
