@@ -170,6 +170,7 @@ struct lg_engine {
     DBuf<unsigned long long> pairs_count;
     uint32_t* h_status = nullptr;  // pinned
     double* h_out = nullptr;       // pinned, nsys * RED_STRIDE
+    size_t h_out_cap = 0;          // systems h_out holds
     std::vector<SysDev> h_sysdev;
     std::vector<int> h_kvec_sys;
 

@@ -904,9 +904,13 @@ int commit(lg_engine* e) {
                                 st));
     CUDA_TRY(e, cudaStreamSynchronize(st));
 
-    if (e->h_out) cudaFreeHost(e->h_out);
-    e->h_out = nullptr;
-    CUDA_TRY(e, cudaMallocHost((void**)&e->h_out, (size_t)nsys * RED_STRIDE * sizeof(double)));
+    if (e->h_out_cap < (size_t)nsys) {  // page-locked: reallocated only when the batch grows
+        if (e->h_out) cudaFreeHost(e->h_out);
+        e->h_out = nullptr;
+        e->h_out_cap = 0;
+        CUDA_TRY(e, cudaMallocHost((void**)&e->h_out, (size_t)nsys * RED_STRIDE * sizeof(double)));
+        e->h_out_cap = (size_t)nsys;
+    }
 
     Batch& b = e->b;
     b = Batch{};

@@ -463,6 +463,19 @@ int persist_plan(lg_engine* e) {
         }
     }
     if (best_c == 0) return LG_OK;  // no cluster fits: the per-step kernels run
+    // One cluster owns a group for the whole launch, so a group much larger
+    // than an even share of the device (a large system among few) would run
+    // on a few SMs while the per-step kernels spread it over all of them: the
+    // per-step kernels run instead, unless the batch is small enough that
+    // launch latency, not throughput, sets the time.
+    {
+        double total = 0.0;
+        for (double w : work) total += w;
+        int sms = std::max(1, b.sms);
+        double persistent_t = best_t;             // largest group per block (times waves)
+        double spread_t = total / (double)sms;    // an even spread over every SM
+        if (b.n > 32768 && persistent_t > 2.0 * spread_t) return LG_OK;
+    }
     std::vector<int> off(1, 0), sys;
     for (auto& bin : best_bins) {
         if (bin.empty()) continue;
