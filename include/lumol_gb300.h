@@ -11,7 +11,9 @@
  * from different threads.
  *
  * Units are Lumol's internal units (lumol-core/src/units.rs:4-16): Angstrom,
- * femtosecond, unified atomic mass, Kelvin, and 1e-4 kJ/mol for energy.
+ * femtosecond, unified atomic mass, Kelvin; energies in u A^2 / fs^2, which is
+ * 1e4 kJ/mol (units::from(0.544, "kJ/mol") = 5.44e-5; the module comment of
+ * units.rs says 1e-4 kJ/mol, its conversions use 1e4).
  *
  * Arrays of vectors are 3*n doubles, x y z per atom, the layout of
  * `&[Vector3D]` (lumol-core/src/types/vectors.rs:59).  A virial is 9 doubles,
@@ -392,8 +394,9 @@ int lg_mc_move_molecule_cost(lg_engine* e, int32_t s, int64_t molecule,
 /* EnergyCache::update (sys/cache.rs:118-127) after the move was applied:
  * `positions` are the molecule's positions after Translate::apply's
  * center-of-mass wrap (lumol-sim/src/mc/moves/translate.rs:114-125), or
- * Rotate::apply's positions; after lg_mc_move_all_molecules_cost they are
- * not read (may be NULL). */
+ * Rotate::apply's positions; NULL keeps the positions the cost was computed
+ * for (GlobalCache::update has no positions, global/mod.rs:183-188; a wrap
+ * changes no energy); after lg_mc_move_all_molecules_cost they are not read. */
 int lg_mc_update(lg_engine* e, int32_t s, const double* molecule_positions, double* energy);
 
 /* EnergyCache::move_all_molecules_cost (sys/cache.rs:238-292) for the

@@ -195,11 +195,12 @@ int lg_mc_update(lg_engine* e, int32_t s, const double* molecule_positions, doub
         if (energy) *energy = e->mc_energy;
         return LG_OK;
     }
-    if (!molecule_positions) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
     int msize = (int)e->mc_mol_size;
     const SysDev& sd = e->h_sysdev[s];
-    CUDA_TRY(e, cudaMemcpyAsync(e->mc_newpos.p, molecule_positions, 3 * msize * sizeof(double),
-                                cudaMemcpyHostToDevice, st));
+    // NULL: the positions the cost was computed for (already on the device)
+    if (molecule_positions)
+        CUDA_TRY(e, cudaMemcpyAsync(e->mc_newpos.p, molecule_positions, 3 * msize * sizeof(double),
+                                    cudaMemcpyHostToDevice, st));
     const double* d_k1 = (const double*)((const char*)(e->sysdev.p + s) + offsetof(SysDev, k1));
     e->shadow_valid = false;
     launch_mc_accept(e->b, sd, (int)e->mc_mol_begin, msize, e->mc_newpos.p, d_k1, e->mc_drho.p, st);

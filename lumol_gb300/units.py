@@ -1,7 +1,8 @@
 """Conversion to Lumol's internal units (lumol-core/src/units.rs).
 
 Internal units: Angstrom, femtosecond, unified atomic mass, Kelvin, radian;
-energy is 1e-4 kJ/mol.  `from_(value, "kJ/mol/A^2")` mirrors `units::from`.
+energy is u A^2 / fs^2 = 1e4 kJ/mol (the module comment of units.rs says
+1e-4 kJ/mol; its conversion factors give 1e4).  `from_(value, "kJ/mol/A^2")` mirrors `units::from`.
 Unit expressions are products and quotients of the units below with integer
 powers and parentheses.
 """
