@@ -792,12 +792,15 @@ def accuracy_report(pairs, timesteps, nve_steps: int, label: str):
         d = rng.uniform(-0.05, 0.05, size=(sd.size, 3))
         sd.positions = sd.positions + d
         sm.positions = sm.positions + d
+    def worst(a, b):  # max that keeps a NaN visible (Python's max drops it)
+        return b if (b != b or b > a) else a
+
     for sd, sm in pairs:
         fd, ed, wd = sd.compute()
         fm, em, wm = sm.compute()
-        out["force_rms_rel"] = max(out["force_rms_rel"], float(np.sqrt(np.sum((fm - fd) ** 2) / np.sum(fd ** 2))))
-        out["energy_rel"] = max(out["energy_rel"], abs(em - ed) / abs(ed))
-        out["virial_rel"] = max(out["virial_rel"], float(np.max(np.abs(wm - wd)) / np.max(np.abs(wd))))
+        out["force_rms_rel"] = worst(out["force_rms_rel"], float(np.sqrt(np.sum((fm - fd) ** 2) / np.sum(fd ** 2))))
+        out["energy_rel"] = worst(out["energy_rel"], abs(em - ed) / abs(ed))
+        out["virial_rel"] = worst(out["virial_rel"], float(np.max(np.abs(wm - wd)) / np.max(np.abs(wd))))
     for name, idx in (("fp64", 0), ("mixed", 1)):
         systems = [p[idx] for p in pairs]
         b = Batch(systems, precision=name)
@@ -811,8 +814,8 @@ def accuracy_report(pairs, timesteps, nve_steps: int, label: str):
         for s, system in enumerate(systems):
             _, v = b.state(s)
             e1 = b.energy(s) + 0.5 * float(np.sum(system.masses[:, None] * v * v))
-            drift = max(drift, abs(e1 - e0[s]) / abs(e0[s]))
-            per_atom = max(per_atom, units.to(abs(e1 - e0[s]), "kJ/mol") / system.size)
+            drift = worst(drift, abs(e1 - e0[s]) / abs(e0[s]))
+            per_atom = worst(per_atom, units.to(abs(e1 - e0[s]), "kJ/mol") / system.size)
         b.engine.close()
         out[f"nve_drift_rel_{name}"] = drift
         out[f"nve_drift_kJmol_per_atom_{name}"] = per_atom
