@@ -225,10 +225,14 @@ __device__ __forceinline__ double chunk_butterfly(double v, int gpw) {
 // u = floor(frac(x / L) * 2^32) (UnitCell::wrap_vector, cells.rs:263-282, as a
 // fraction of the cell), and the charge's FP32 bits.
 // floor(x 2^32 / L) taken modulo 2^32 is that fraction (two's complement
-// wrap-around does the frac), so each axis costs one FP64 multiply and one
-// conversion.
+// wrap-around does the frac).  One FP64 instruction per axis: the fused
+// x * scale + 1.5 * 2^52 rounded toward -infinity is floor(x * scale) +
+// 1.5 * 2^52 exactly (the unit in the last place there is 1), and the low 32
+// bits of its encoding are floor(x * scale) modulo 2^32; this holds for
+// |x * scale| < 2^51, i.e. positions within 2^19 cell lengths of the origin.
+// (floor of the exact product: no rounding of x * scale first.)
 __device__ __forceinline__ uint32_t fixed_coordinate(double x, double scale) {
-    return (uint32_t)(unsigned long long)__double2ll_rd(x * scale);
+    return (uint32_t)__double2loint(__fma_rd(x, scale, 6755399441055744.0));
 }
 // The charge's FP32 copy is never zero for a non-zero charge (a charge below
 // the FP32 range keeps the smallest normal value), so "q != 0" tests agree
@@ -240,6 +244,18 @@ __device__ __forceinline__ float charge_f32(double q) {
 __device__ __forceinline__ uint4 fixed_position(const SysDev& s, double4_32a p) {
     return make_uint4(fixed_coordinate(p.x, s.fxscale[0]), fixed_coordinate(p.y, s.fxscale[1]),
                       fixed_coordinate(p.z, s.fxscale[2]), __float_as_uint(charge_f32(p.w)));
+}
+// The coordinates alone (w = 0), for the integrators' updates: the charge
+// word of an atom's record never changes between list builds, so they store
+// x, y, z only (store_fixed_xyz) and skip its FP64 conversion.
+__device__ __forceinline__ uint4 fixed_xyz(const SysDev& s, double4_32a p) {
+    return make_uint4(fixed_coordinate(p.x, s.fxscale[0]), fixed_coordinate(p.y, s.fxscale[1]),
+                      fixed_coordinate(p.z, s.fxscale[2]), 0u);
+}
+__device__ __forceinline__ void store_fixed_xyz(uint4* dst, uint4 u) {
+    uint32_t* d = reinterpret_cast<uint32_t*>(dst);
+    *reinterpret_cast<uint2*>(d) = make_uint2(u.x, u.y);
+    d[2] = u.z;
 }
 
 // Squared minimum-image distance of two fixed-point positions in FP32, every
@@ -396,9 +412,14 @@ enum : uint32_t {
 
 // A non-finite value in a system's state: the system is flagged (and the
 // batch's status word), the others are not affected.
+// (the test reads the exponent bits with integer instructions: on GB300 an
+// FP64 comparison would take the FP64 pipe, which the integrators saturate)
+__device__ __forceinline__ bool nonfinite_bits(double x) {
+    return (__double2hiint(x) & 0x7ff00000) == 0x7ff00000;
+}
 __device__ __forceinline__ void flag_nonfinite(double a, double b, double c, int s, uint32_t* sys_status,
                                                uint32_t* status) {
-    if (!(isfinite(a) && isfinite(b) && isfinite(c)) && sys_status) {
+    if ((nonfinite_bits(a) | nonfinite_bits(b) | nonfinite_bits(c)) && sys_status) {
         atomicOr(sys_status + s, SYS_NONFINITE);
         atomicOr(status, ST_NONFINITE);
     }

@@ -302,8 +302,8 @@ __global__ void __launch_bounds__(VV_TILE) md_first_kernel(
             p.y = fma(v.y, dt, p.y);
             p.z = fma(v.z, dt, p.z);
         }
-        uint4 u = fixed_position(s, p);
-        posfx[perm[i]] = u;  // a rebuild this step rewrites it in the new order
+        uint4 u = fixed_xyz(s, p);
+        store_fixed_xyz(posfx + perm[i], u);  // a rebuild this step rewrites it in the new order
         r2 = fixed_dist2(u, pfx_build[i], s.Lq);  // as the persistent kernel
     } else {
         if (leap) {  // (v dt) + ((0.5 a) dt^2)

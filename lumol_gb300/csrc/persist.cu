@@ -39,6 +39,13 @@ __device__ __forceinline__ int pk_find(const int* pre, int R, int v) {
     return a;
 }
 
+// This block's share [lo, hi) of n items split evenly over the C blocks of a
+// cluster: contiguous (coalesced) and within one item of the others, so no
+// block of a phase that ends at a cluster barrier carries more than its share.
+__device__ __forceinline__ int2 pk_share(int n, int rank, int C) {
+    return make_int2((int)((long long)n * rank / C), (int)((long long)n * (rank + 1) / C));
+}
+
 // Cluster-wide barrier.  barrier.cluster.arrive has release and
 // barrier.cluster.wait acquire semantics at cluster scope, so every global
 // write made before the barrier is visible to every block of the cluster
@@ -84,7 +91,15 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
     __shared__ int s_R;
     __shared__ int s_part[PK_THREADS];
     __shared__ int s_lo[PK_WARPS][NL_RUNS], s_pre[PK_WARPS][NL_RUNS + 1];
-    __shared__ int s_buf[PK_WARPS][PK_SORT];
+    __shared__ __align__(16) int s_buf[PK_WARPS][PK_SORT];
+    // the force phase's per-warp epilogue buffers reuse the list build's
+    // (phases are separated by cluster barriers): 32 FP32 accelerations, their
+    // atoms, and the (system slot, chunk) of each buffered chunk
+    static_assert(PK_SORT * sizeof(int) >= 32 * sizeof(float4), "epilogue buffer");
+    static_assert(NL_RUNS >= 32 && NL_RUNS + 1 >= 2 * 8, "epilogue buffer");
+    float4(*s_epa)[32] = reinterpret_cast<float4(*)[32]>(s_buf);
+    int(*s_epi)[NL_RUNS] = s_lo;
+    int(*s_epq)[NL_RUNS + 1] = s_pre;
     extern __shared__ uint4 s_dyn[];  // staged positions (a.stage atoms), then their kinds
     uint4* s_pos = s_dyn;
     int* s_kind = reinterpret_cast<int*>(s_dyn + a.stage);
@@ -111,22 +126,26 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
     __syncthreads();
     const int A = s_apre[G];
     const int QQ = s_qpre[G];
-    const int ct = rank * PK_THREADS + threadIdx.x;
-    const int CT = C * PK_THREADS;
     const int wib = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    const int wg = rank * PK_WARPS + wib;
-    const int WG = C * PK_WARPS;
+    const int2 ash = pk_share(A, rank, C);  // this block's atoms of the group
+    // the force phase hands out chunks from a counter in rank 0's shared
+    // memory (one atomic per chunk and warp), so the blocks of the cluster
+    // reach its closing barrier together whatever the chunks cost
+    __shared__ int s_next;
+    int* next_chunk = cluster.map_shared_rank(&s_next, 0);
     bool ran = false;
 
     for (int step = 0; step < a.nsteps; step++) {
         // ---- 1: [v *= lambda]; v += dt/2 a; x += v dt; fixed-point copy; displacement test
         const bool apply = a.thermo && step > 0;
+        // (the previous step's chunks were all taken before its closing barrier)
+        if (rank == 0 && threadIdx.x == 0) s_next = 0;
         if (apply) {
             pk_lambdas(b, a, s_sys, G, wib, lane, GPW, s_lambda);
             __syncthreads();
         }
-        for (int v = ct; v < A; v += CT) {
+        for (int v = ash.x + threadIdx.x; v < ash.y; v += PK_THREADS) {
             int r = pk_find(s_apre, G, v);
             int s = s_sys[r];
             const SysDev& sd = b.sys[s];
@@ -152,8 +171,8 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
             b.vel[i] = vel;
             b.posq[i] = p;
             flag_nonfinite(p.x, p.y, p.z, s, b.sys_status, b.status);
-            uint4 u = fixed_position(sd, p);
-            b.posfx[b.perm[i]] = u;
+            uint4 u = fixed_xyz(sd, p);
+            store_fixed_xyz(b.posfx + b.perm[i], u);
             if (fixed_dist2(u, b.pfx_build[i], sd.Lq) > sd.rebuild2_f) b.sys_rebuild[s] = 1u;
         }
         pk_sync(cluster);
@@ -181,10 +200,11 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
         const int R = s_R;
         if (R > 0) {
             const int RA = s_rapre[R], RC = s_rcpre[R];
+            const int2 rsh = pk_share(RA, rank, C), csh = pk_share(RC, rank, C);
             // 2a: cell of each atom from its fixed-point copy (written in phase 1:
             // u / 2^32 is the wrapped fraction of the cell, so the cell index is
             // (u * ncell) >> 32, integer arithmetic only), build positions
-            for (int v = ct; v < RA; v += CT) {
+            for (int v = rsh.x + threadIdx.x; v < rsh.y; v += PK_THREADS) {
                 int r = pk_find(s_rapre, R, v);
                 const SysDev& sd = b.sys[s_rsys[r]];
                 int i = sd.begin + (v - s_rapre[r]);
@@ -234,7 +254,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
             }
             pk_sync(cluster);
             // 2c: scatter the atoms into their cells
-            for (int v = ct; v < RA; v += CT) {
+            for (int v = rsh.x + threadIdx.x; v < rsh.y; v += PK_THREADS) {
                 int r = pk_find(s_rapre, R, v);
                 int s = s_rsys[r];
                 int i = b.sys[s].begin + (v - s_rapre[r]);
@@ -250,7 +270,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
             }
             pk_sync(cluster);
             // 2d: sort each cell by atom index (warp per cell), leave the counts at zero
-            for (int vc = wg; vc < RC; vc += WG) {
+            for (int vc = csh.x + wib; vc < csh.y; vc += PK_WARPS) {
                 int r = pk_find(s_rcpre, R, vc);
                 int s = s_rsys[r];
                 int c = b.sys[s].cell_begin + (vc - s_rcpre[r]);
@@ -280,7 +300,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
             }
             pk_sync(cluster);
             // 2e: sorted position of each atom, sorted (kind, molecule), fixed-point copies
-            for (int v = ct; v < RA; v += CT) {
+            for (int v = rsh.x + threadIdx.x; v < rsh.y; v += PK_THREADS) {
                 int r = pk_find(s_rapre, R, v);
                 const SysDev& sd = b.sys[s_rsys[r]];
                 int t = sd.begin + (v - s_rapre[r]);
@@ -293,7 +313,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
             }
             pk_sync(cluster);
             // 2f: Verlet list rows (warp per atom, cell order), as the per-step list build
-            for (int w = wg; w < RA; w += WG) {
+            for (int w = rsh.x + wib; w < rsh.y; w += PK_WARPS) {
                 int r = pk_find(s_rapre, R, w);
                 int si = s_rsys[r];
                 const SysDev& sd = b.sys[si];
@@ -365,9 +385,50 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
                 __syncthreads();
             }
             // warp chunks of GPW atoms of one system (chunk q of system r covers its
-            // atoms q * GPW ...), so a chunk's kinetic energy belongs to one system
+            // atoms q * GPW ...), so a chunk's kinetic energy belongs to one system.
+            // The FP64 epilogue (a = F / m widened, v += dt/2 a, kinetic energy)
+            // runs once every TPA chunks over the 32 buffered atoms, one atom a
+            // lane: GB300 issues one FP64 warp instruction per about 19 cycles and
+            // SM, so an epilogue with one atom per TPA lanes would pay TPA times
+            // over.  The chunk sums of the kinetic energy take the same tree as a
+            // whole-warp butterfly over one atom every TPA lanes (chunk_sum).
             const int sub = lane % TPA;
-            for (int q = wg; q < QQ; q += WG) {
+            int nbuf = 0;  // chunks buffered by this warp (warp-uniform)
+            auto flush = [&]() {
+                __syncwarp();
+                const int c = lane / GPW;  // buffered chunk of this lane
+                double ke = 0.0;
+                int s = -1, qq = 0;
+                if (c < nbuf) {
+                    s = s_sys[s_epq[wib][2 * c]];
+                    qq = s_epq[wib][2 * c + 1];
+                    const int i = s_epi[wib][lane];
+                    if (i >= 0) {
+                        const SysDev& sd = b.sys[s];
+                        const float4 a4 = s_epa[wib][lane];
+                        double4_32a vel = b.vel[i];
+                        double4_32a ai = make_double4_32a((double)a4.x, (double)a4.y, (double)a4.z, 0.0);
+                        vel.x = fma(sd.hdt, ai.x, vel.x);
+                        vel.y = fma(sd.hdt, ai.y, vel.y);
+                        vel.z = fma(sd.hdt, ai.z, vel.z);
+                        b.acc[i] = ai;
+                        b.vel[i] = vel;
+                        flag_nonfinite(vel.x, vel.y, vel.z, s, b.sys_status, b.status);
+                        if (a.thermo) ke = 0.5 * vel.w * fma(vel.x, vel.x, fma(vel.y, vel.y, vel.z * vel.z));
+                    }
+                }
+                if (a.thermo) {  // per chunk, lanes in a fixed order
+#pragma unroll
+                    for (int o = GPW / 2; o > 0; o >>= 1) ke += __shfl_xor_sync(0xffffffffu, ke, o);
+                    if (c < nbuf && lane % GPW == 0) a.ke[b.sys[s].begin + qq] = ke;
+                }
+                nbuf = 0;
+                __syncwarp();
+            };
+            int q = 0;
+            if (lane == 0) q = atomicAdd(next_chunk, 1);
+            q = __shfl_sync(0xffffffffu, q, 0);
+            for (; q < QQ;) {
                 int r = pk_find(s_qpre, G, q);
                 const SysDev& sd = b.sys[s_sys[r]];
                 int qq = q - s_qpre[r];
@@ -404,27 +465,27 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
                                                   ph1, pq1, nullptr);
                     });
                 group_combine<TPA>(acc);
-                double ke = 0.0;
-                if (active && sub == 0) {
+                if (sub == 0) {
                     // as the per-step path: the compensated sum rounded once to FP32, a = F / m in FP32
-                    float im = b.inv_mass[i];
-                    double4_32a vel = b.vel[i];
-                    double4_32a ai = make_double4_32a((double)rmul(radd(acc.fxs, acc.fxc), im),
-                                                      (double)rmul(radd(acc.fys, acc.fyc), im),
-                                                      (double)rmul(radd(acc.fzs, acc.fzc), im), 0.0);
-                    vel.x = fma(sd.hdt, ai.x, vel.x);
-                    vel.y = fma(sd.hdt, ai.y, vel.y);
-                    vel.z = fma(sd.hdt, ai.z, vel.z);
-                    b.acc[i] = ai;
-                    b.vel[i] = vel;
-                    flag_nonfinite(vel.x, vel.y, vel.z, s_sys[r], b.sys_status, b.status);
-                    if (a.thermo) ke = 0.5 * vel.w * fma(vel.x, vel.x, fma(vel.y, vel.y, vel.z * vel.z));
+                    const int slot = nbuf * GPW + lane / TPA;
+                    if (active) {
+                        float im = b.inv_mass[i];
+                        s_epa[wib][slot] = make_float4(rmul(radd(acc.fxs, acc.fxc), im),
+                                                       rmul(radd(acc.fys, acc.fyc), im),
+                                                       rmul(radd(acc.fzs, acc.fzc), im), 0.0f);
+                    }
+                    s_epi[wib][slot] = active ? i : -1;
                 }
-                if (a.thermo) {  // the chunk's kinetic energy, lanes in a fixed order
-                    for (int o = 16; o > 0; o >>= 1) ke += __shfl_xor_sync(0xffffffffu, ke, o);
-                    if (lane == 0) a.ke[sd.begin + qq] = ke;
+                if (lane == 0) {
+                    s_epq[wib][2 * nbuf] = r;
+                    s_epq[wib][2 * nbuf + 1] = qq;
                 }
+                if (++nbuf == TPA) flush();
+                int qn = 0;
+                if (lane == 0) qn = atomicAdd(next_chunk, 1);
+                q = __shfl_sync(0xffffffffu, qn, 0);
             }
+            if (nbuf > 0) flush();
         }
         pk_sync(cluster);
 
@@ -435,7 +496,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
     if (a.thermo && ran && !*(volatile const int*)&a.group_flag[g]) {
         pk_lambdas(b, a, s_sys, G, wib, lane, GPW, s_lambda);
         __syncthreads();
-        for (int v = ct; v < A; v += CT) {
+        for (int v = ash.x + threadIdx.x; v < ash.y; v += PK_THREADS) {
             int r = pk_find(s_apre, G, v);
             int s = s_sys[r];
             int i = b.sys[s].begin + (v - s_apre[r]);

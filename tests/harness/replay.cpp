@@ -16,8 +16,9 @@
 //   System::set_pair_potential a cutoff above half the cell fails with the
 //   (sys/system.rs:122-131)    reference's panic message
 //
-// Usage: replay <input file>.  The input holds "n L cutoff alpha kmax" and
-// then n lines "kind charge mass x y z" (two kinds: LJ pair table below).
+// Usage: replay <input file>.  The input holds "n L cutoff alpha kmax", a line
+// "sigma0 sigma1 epsilon0 epsilon1" (LJ of the two kinds in internal units,
+// Lorentz-Berthelot mixing below), then n lines "kind charge mass x y z".
 // Prints one JSON line; exits 0 when every check passed, 1 on a failed check,
 // 3 when no device is visible (the engine has no CPU fallback).
 #include <cmath>
@@ -40,6 +41,7 @@ struct Input {
     long n = 0;
     double L = 0, cutoff = 0, alpha = 0;
     int kmax = 0;
+    double sigma[2] = {0, 0}, eps[2] = {0, 0};
     std::vector<int> kind, mol;
     std::vector<double> q, m, x;
 };
@@ -48,6 +50,7 @@ static bool read_input(const char* path, Input& in) {
     FILE* f = std::fopen(path, "r");
     if (!f) return false;
     if (std::fscanf(f, "%ld %lf %lf %lf %d", &in.n, &in.L, &in.cutoff, &in.alpha, &in.kmax) != 5) return false;
+    if (std::fscanf(f, "%lf %lf %lf %lf", &in.sigma[0], &in.sigma[1], &in.eps[0], &in.eps[1]) != 4) return false;
     in.kind.resize(in.n);
     in.mol.resize(in.n);
     in.q.resize(in.n);
@@ -64,8 +67,9 @@ static bool read_input(const char* path, Input& in) {
 }
 
 // NaCl-like pair table: LJ with Lorentz-Berthelot parameters between two kinds
-static std::vector<lg_pair> pair_table(double cutoff) {
-    const double sigma[2] = {2.35, 4.40}, eps[2] = {0.544e-4, 0.4184e-4};  // kJ/mol in units of 1e4 kJ/mol
+static std::vector<lg_pair> pair_table(const Input& in) {
+    const double* sigma = in.sigma;
+    const double* eps = in.eps;
     std::vector<lg_pair> t(4);
     for (int a = 0; a < 2; a++)
         for (int b = 0; b < 2; b++) {
@@ -74,7 +78,7 @@ static std::vector<lg_pair> pair_table(double cutoff) {
             p.type = LG_PAIR_LJ;
             p.p0 = 0.5 * (sigma[a] + sigma[b]);
             p.p1 = std::sqrt(eps[a] * eps[b]);
-            p.cutoff = cutoff;
+            p.cutoff = in.cutoff;
             p.scale14 = 1.0;
         }
     return t;
@@ -89,7 +93,7 @@ static lg_engine* make_engine(const Input& in, int* status) {
     check(lg_set_cell(e, 0, cell) == LG_OK, "lg_set_cell");
     check(lg_set_particles(e, 0, in.n, in.kind.data(), in.q.data(), in.m.data(), in.mol.data()) == LG_OK,
           "lg_set_particles");
-    std::vector<lg_pair> table = pair_table(in.cutoff);
+    std::vector<lg_pair> table = pair_table(in);
     check(lg_set_pairs(e, 0, 2, table.data()) == LG_OK, "lg_set_pairs");
     lg_coulomb c;
     std::memset(&c, 0, sizeof(c));
@@ -160,7 +164,9 @@ int main(int argc, char** argv) {
     check(same, "ten integrate calls equal one ten-step run");
 
     // set_pair_potential's check of the cutoff against half the cell
-    std::vector<lg_pair> big = pair_table(0.75 * in.L);
+    Input wide = in;
+    wide.cutoff = 0.75 * in.L;
+    std::vector<lg_pair> big = pair_table(wide);
     int rc = lg_set_pairs(e2, 0, 2, big.data());
     check(rc == LG_ERR_ARGUMENT, "cutoff above half the cell is refused");
     check(std::strstr(lg_last_error(e2), "cutoff bigger than half of the smallest cell length") != nullptr,

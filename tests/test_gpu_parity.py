@@ -252,6 +252,7 @@ def test_list_build_cells_match_positions(precision):
     the fixed-point fraction u = floor(x 2^32 / L) mod 2^32, cell (u n) >> 32."""
     import ctypes
     import math
+    from fractions import Fraction
     s = systems.random_lj_fluid(900, 0.02, 12, 9.0, family="lj", precision=precision)
     s.compute()  # builds the neighbour lists at these positions
     cells = np.zeros(s.size, dtype=np.int32)
@@ -264,8 +265,8 @@ def test_list_build_cells_match_positions(precision):
         c = []
         for d in range(3):
             L = s.cell.lengths[d]
-            if precision == "mixed":
-                u = math.floor(p[d] * ((1.0 / L) * 4294967296.0)) % 2 ** 32
+            if precision == "mixed":  # (floor of the exact product)
+                u = math.floor(Fraction(float(p[d])) * Fraction((1.0 / L) * 4294967296.0)) % 2 ** 32
                 c.append((u * n[d]) >> 32)
             else:
                 w = p[d] - math.floor(p[d] / L) * L
