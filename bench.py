@@ -66,6 +66,8 @@ def parse():
     p.add_argument("--no-roofline", action="store_true")
     p.add_argument("--no-accuracy", action="store_true", help="skip the mixed-vs-FP64 error report")
     p.add_argument("--no-fp64-leg", action="store_true", help="lj_batch: skip timing the plain FP64 path")
+    p.add_argument("--threads-per-atom", type=int, default=0,
+                   help="lj_batch: fixed pair-kernel group size of the MD engine (0: autotuned)")
     p.add_argument("--no-configs", action="store_true",
                    help="lj_batch: skip the single-system (argon, NaCl, water) and serving legs")
     return p.parse_args()
@@ -392,7 +394,7 @@ def timed_batch(args, world, local, precision: str, steps: int, warmup: int):
     from lumol_gb300.batch import Batch
 
     md_sys, md_p, mc_sys, mc_p, desc = batch_workload(args, precision)
-    md = Batch(md_sys, precision=precision)
+    md = Batch(md_sys, precision=precision, threads_per_atom=args.threads_per_atom)
     md.md_setup([1.0] * len(md_sys), [(t, 100.0) for _, (n, rho, t) in md_p])
     # a 2 A skin for the chains: fewer list rebuilds for single-particle moves of up to 0.3 A
     mc = Batch(mc_sys, precision=precision, skin=2.0)

@@ -179,9 +179,23 @@ int lg_create(const lg_options* options, int32_t n_systems, lg_engine** engine);
 void lg_destroy(lg_engine* engine);
 
 /* ---- system description (per system index `s`) ----------------------------- */
-/* UnitCell::ortho / cubic (cells.rs:51-66): `matrix` is the 3x3 cell, row-major;
- * only orthorhombic cells are accepted.  Replaces setting `System::cell`. */
+/* CellShape (cells.rs:12-20) of a cell given to lg_set_cell_ex. */
+#define LG_CELL_ORTHORHOMBIC 0
+#define LG_CELL_TRICLINIC 1
+
+/* UnitCell::ortho / cubic / triclinic (cells.rs:51-94): `matrix` is the 3x3
+ * cell, row-major, its columns the cell vectors (UnitCell::matrix).  The shape
+ * follows from the matrix: any non-zero off-diagonal entry makes it
+ * triclinic (UnitCell::triclinic with any angle; its 90-degree angles leave
+ * cos(pi / 2) terms off the diagonal).  Replaces setting `System::cell`. */
 int lg_set_cell(lg_engine* e, int32_t s, const double matrix[9]);
+/* The same with the shape given: LG_CELL_TRICLINIC for any cell whose
+ * volume is positive (a triclinic cell with a diagonal matrix still takes the
+ * triclinic branches, as in the reference); LG_CELL_ORTHORHOMBIC requires a
+ * diagonal matrix.  (UnitCell::scale_mut keeps the shape, cells.rs:201-207, so
+ * AnisoBerendsenBarostat can leave an orthorhombic cell with off-diagonal
+ * terms; the engine does not represent that state.) */
+int lg_set_cell_ex(lg_engine* e, int32_t s, const double matrix[9], int32_t shape);
 
 /* Particles of system `s` (Configuration, sys/config/configuration.rs:42-51):
  * kinds index the pair table, molecules give each atom's molecule index
@@ -306,6 +320,9 @@ enum {
 int lg_md_set_barostat(lg_engine* e, int32_t s, int32_t kind, double pressure, double tau);
 /* The cell matrix of system `s` (9 doubles, row-major). */
 int lg_get_cell(lg_engine* e, int32_t s, double matrix[9]);
+/* Its CellShape (LG_CELL_*), face distances (UnitCell::lengths, cells.rs:134-146)
+ * and volume (cells.rs:185-200), as the engine computed them. */
+int lg_cell_info(lg_engine* e, int32_t s, int32_t* shape, double lengths[3], double* volume);
 
 /* Molecular dynamics of system `s` with any integrator, thermostat and
  * controls of the list above, stepped as MolecularDynamics::propagate does

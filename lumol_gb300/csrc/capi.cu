@@ -59,28 +59,38 @@ void lg_destroy(lg_engine* e) {
     delete e;
 }
 
-int lg_set_cell(lg_engine* e, int32_t s, const double m[9]) {
+int lg_set_cell_ex(lg_engine* e, int32_t s, const double m[9], int32_t shape) {
     if (!valid_sys(e, s) || !m) return fail(e, LG_ERR_ARGUMENT, "invalid system index or cell");
-    for (int a = 0; a < 3; a++)
-        for (int c = 0; c < 3; c++)
-            if (a != c && m[3 * a + c] != 0.0)
-                return fail(e, LG_ERR_ARGUMENT, "only orthorhombic cells are supported");
-    if (!(m[0] > 0.0 && m[4] > 0.0 && m[8] > 0.0)) return fail(e, LG_ERR_ARGUMENT, "Cell lengths must be positive");
+    if (shape != LG_CELL_ORTHORHOMBIC && shape != LG_CELL_TRICLINIC) return fail(e, LG_ERR_ARGUMENT, "invalid cell shape");
+    for (int k = 0; k < 9; k++)
+        if (!std::isfinite(m[k])) return fail(e, LG_ERR_ARGUMENT, "non-finite cell matrix");
+    if (shape == LG_CELL_ORTHORHOMBIC) {
+        for (int a = 0; a < 3; a++)
+            for (int c = 0; c < 3; c++)
+                if (a != c && m[3 * a + c] != 0.0)
+                    return fail(e, LG_ERR_ARGUMENT, "an orthorhombic cell has a diagonal matrix");
+        if (!(m[0] > 0.0 && m[4] > 0.0 && m[8] > 0.0)) return fail(e, LG_ERR_ARGUMENT, "Cell lengths must be positive");
+    }
+    HostCell cell;
+    if (!cell_init(cell, m, shape)) return fail(e, LG_ERR_ARGUMENT, "the cell matrix is not invertible or its volume is not positive");
     HostSystem& h = e->sys[s];
-    const double L[3] = {m[0], m[4], m[8]};
-    int rc = check_cell_cutoffs(e, h, L);
+    int rc = check_cell_cutoffs(e, h, cell.len);
     if (rc) return rc;
-    if (!e->dirty && h.has_cell) {  // a lowered batch: change the cell in place, keeping the state
+    // a cell's shape decides the list grid and the kernels' branches: lower again when it changes
+    if (!e->dirty && h.has_cell && h.cell.shape == shape) {  // in place, keeping the state
         CUDA_TRY(e, cudaSetDevice(e->opt.device));
-        rc = set_cell_fast(e, s, L);
+        rc = set_cell_fast(e, s, cell);
         if (rc != -1) return rc;
     }
-    h.L[0] = m[0];
-    h.L[1] = m[4];
-    h.L[2] = m[8];
-    h.has_cell = true;
+    set_host_cell(h, cell);
     invalidate(e);
     return LG_OK;
+}
+
+int lg_set_cell(lg_engine* e, int32_t s, const double m[9]) {
+    if (!valid_sys(e, s) || !m) return fail(e, LG_ERR_ARGUMENT, "invalid system index or cell");
+    bool diagonal = m[1] == 0.0 && m[2] == 0.0 && m[3] == 0.0 && m[5] == 0.0 && m[6] == 0.0 && m[7] == 0.0;
+    return lg_set_cell_ex(e, s, m, diagonal ? LG_CELL_ORTHORHOMBIC : LG_CELL_TRICLINIC);
 }
 
 int lg_set_particles(lg_engine* e, int32_t s, int64_t n, const int32_t* kinds, const double* charges,
@@ -438,10 +448,18 @@ int lg_md_set_barostat(lg_engine* e, int32_t s, int32_t kind, double pressure, d
 int lg_get_cell(lg_engine* e, int32_t s, double m[9]) {
     if (!valid_sys(e, s) || !m) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
     const HostSystem& h = e->sys[s];
-    for (int k = 0; k < 9; k++) m[k] = 0.0;
-    m[0] = h.L[0];
-    m[4] = h.L[1];
-    m[8] = h.L[2];
+    for (int k = 0; k < 9; k++) m[k] = h.cell.m[k];
+    return LG_OK;
+}
+
+int lg_cell_info(lg_engine* e, int32_t s, int32_t* shape, double lengths[3], double* volume) {
+    if (!valid_sys(e, s)) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    const HostSystem& h = e->sys[s];
+    if (!h.has_cell) return fail(e, LG_ERR_STATE, "system " + std::to_string(s) + " has no cell");
+    if (shape) *shape = h.cell.shape;
+    if (lengths)
+        for (int k = 0; k < 3; k++) lengths[k] = h.cell.len[k];
+    if (volume) *volume = h.cell.volume;
     return LG_OK;
 }
 

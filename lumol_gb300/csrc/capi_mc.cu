@@ -92,13 +92,12 @@ void mc_refresh_kspace(lg_engine* e) {
     e->launches += 2;
 }
 
-// Installs cell lengths L for system s, in place when the cell grid and the
-// k-vector set allow it, else by lowering the batch again (state kept).
-int mc_set_cell(lg_engine* e, int s, const double L[3]) {
-    int rc = set_cell_fast(e, s, L);
+// Installs a cell for system s, in place when the cell grid and the k-vector
+// set allow it, else by lowering the batch again (state kept).
+int mc_set_cell(lg_engine* e, int s, const HostCell& cell) {
+    int rc = set_cell_fast(e, s, cell);
     if (rc != -1) return rc;
-    HostSystem& h = e->sys[s];
-    for (int k = 0; k < 3; k++) h.L[k] = L[k];
+    set_host_cell(e->sys[s], cell);
     invalidate(e);
     return commit_carried(e);
 }
@@ -110,7 +109,7 @@ int mc_restore_resize(lg_engine* e) {
     int s = e->mc_sys;
     e->mc_resize = false;
     e->mc_pending = false;
-    int rc = mc_set_cell(e, s, e->mc_old_L);
+    int rc = mc_set_cell(e, s, e->mc_old_cell);
     if (rc) return rc;
     const HostSystem& h = e->sys[s];
     CUDA_TRY(e, cudaMemcpyAsync(e->posq.p + e->begin[s], e->mc_saved_pos.p, h.n * sizeof(double4_32a),
@@ -131,12 +130,16 @@ int lg_mc_move_all_molecules_cost(lg_engine* e, int32_t s, const double new_cell
                                   double* cost) {
     if (!valid_sys(e, s) || !new_cell || !new_positions || !cost) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
     if (e->dirty || e->mc_sys != s) return fail(e, LG_ERR_STATE, "lg_mc_init was not called for this system");
-    for (int a = 0; a < 3; a++)
-        for (int c = 0; c < 3; c++)
-            if (a != c && new_cell[3 * a + c] != 0.0)
-                return fail(e, LG_ERR_ARGUMENT, "only orthorhombic cells are supported");
-    const double L[3] = {new_cell[0], new_cell[4], new_cell[8]};
-    if (!(L[0] > 0.0 && L[1] > 0.0 && L[2] > 0.0)) return fail(e, LG_ERR_ARGUMENT, "Cell lengths must be positive");
+    // the shape is kept (UnitCell::scale_mut, cells.rs:201-207)
+    HostCell cell;
+    const int shape = e->sys[s].cell.shape;
+    if (shape == LG_CELL_ORTHORHOMBIC)
+        for (int a = 0; a < 3; a++)
+            for (int c = 0; c < 3; c++)
+                if (a != c && new_cell[3 * a + c] != 0.0)
+                    return fail(e, LG_ERR_ARGUMENT, "an orthorhombic cell has a diagonal matrix");
+    if (!cell_init(cell, new_cell, shape)) return fail(e, LG_ERR_ARGUMENT, "the new cell is singular");
+    const double* L = cell.len;
     CUDA_TRY(e, cudaSetDevice(e->opt.device));
     int rc = mc_restore_resize(e);  // a previous Resize that was neither accepted nor restored
     if (rc) return rc;
@@ -151,8 +154,8 @@ int lg_mc_move_all_molecules_cost(lg_engine* e, int32_t s, const double new_cell
     CUDA_TRY(e, e->mc_saved_pos.alloc(std::max<int64_t>(h.n, 1)));
     CUDA_TRY(e, cudaMemcpyAsync(e->mc_saved_pos.p, e->posq.p + e->begin[s], h.n * sizeof(double4_32a),
                                 cudaMemcpyDeviceToDevice, st));
-    for (int k = 0; k < 3; k++) e->mc_old_L[k] = h.L[k];
-    rc = mc_set_cell(e, s, L);
+    e->mc_old_cell = h.cell;
+    rc = mc_set_cell(e, s, cell);
     if (rc) return rc;
     rc = upload_positions(e, s, new_positions);
     if (rc) return rc;
@@ -201,9 +204,8 @@ int lg_mc_update(lg_engine* e, int32_t s, const double* molecule_positions, doub
     if (molecule_positions)
         CUDA_TRY(e, cudaMemcpyAsync(e->mc_newpos.p, molecule_positions, 3 * msize * sizeof(double),
                                     cudaMemcpyHostToDevice, st));
-    const double* d_k1 = (const double*)((const char*)(e->sysdev.p + s) + offsetof(SysDev, k1));
     e->shadow_valid = false;
-    launch_mc_accept(e->b, sd, (int)e->mc_mol_begin, msize, e->mc_newpos.p, d_k1, e->mc_drho.p, st);
+    launch_mc_accept(e->b, sd, (int)e->mc_mol_begin, msize, e->mc_newpos.p, e->sysdev.p + s, e->mc_drho.p, st);
     e->launches += 2;
     CUDA_TRY(e, cudaStreamSynchronize(st));
     CUDA_TRY(e, cudaGetLastError());
@@ -219,6 +221,10 @@ int lg_mc_setup(lg_engine* e, int32_t s, double temperature, double delta, uint6
     if (!(temperature > 0.0)) return fail(e, LG_ERR_ARGUMENT, "the temperature must be positive in Monte Carlo");
     if (!(delta > 0.0)) return fail(e, LG_ERR_ARGUMENT, "delta must be positive in Translate move");
     const HostSystem& h = e->sys[s];
+    if (h.cell.shape != LG_CELL_ORTHORHOMBIC)
+        return fail(e, LG_ERR_ARGUMENT,
+                    "batched Monte Carlo chains take orthorhombic cells; use lg_mc_move_molecule_cost for a "
+                    "triclinic cell");
     if (h.coul.kind != LG_COULOMB_NONE)
         return fail(e, LG_ERR_ARGUMENT,
                     "batched Monte Carlo chains evaluate pair potentials only; use lg_mc_move_molecule_cost "

@@ -105,7 +105,82 @@ struct SysDev {
     double baro_eta;              // BerendsenBarostat: the factor this step scales the positions by
     int32_t barostat;             // 1: BerendsenBarostat (Velocity-Verlet based)
     int32_t baro_pad;
+    // CellShape::Triclinic (cells.rs:72-94): the general branches of the
+    // geometry.  For an orthorhombic system H and Hi hold the diagonal cell
+    // and its inverse, and L / invL / Lf / Lq stay the only fields read.
+    int32_t tric;                 // 1: triclinic cell
+    int32_t tric_pad;
+    double H[9];                  // UnitCell::matrix, row-major; columns are the cell vectors
+    double Hi[9];                 // its Matrix3::inverse (matrix.rs:212-227)
+    double kax[9];                // k_vector(e_a) = 2 PI Hi e_a (cells.rs:224-226), row a = axis a
+    float Hf[9];                  // H in FP32 (mixed path and list builds)
+    float tric_padf[3];
 };
+
+// Matrix3 * Vector3D (matrix.rs:389-398): each row a left-to-right sum of
+// unfused products.
+__device__ __forceinline__ void mat_vec_exact(const double* m, const double v[3], double out[3]) {
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+        out[a] = __dadd_rn(__dadd_rn(__dmul_rn(m[3 * a], v[0]), __dmul_rn(m[3 * a + 1], v[1])),
+                           __dmul_rn(m[3 * a + 2], v[2]));
+}
+
+// vector_image of a triclinic cell (cells.rs:292-298): fractional = inv * d,
+// each component minus its round (half away from zero), back to Cartesian.
+__device__ __forceinline__ void tric_image(const SysDev& s, double d[3]) {
+    double f[3];
+    mat_vec_exact(s.Hi, d, f);
+#pragma unroll
+    for (int a = 0; a < 3; a++) f[a] = __dsub_rn(f[a], round(f[a]));
+    mat_vec_exact(s.H, f, d);
+}
+
+// wrap_vector of a triclinic cell (cells.rs:271-279): the same with floor.
+__device__ __forceinline__ void tric_wrap(const SysDev& s, double d[3]) {
+    double f[3];
+    mat_vec_exact(s.Hi, d, f);
+#pragma unroll
+    for (int a = 0; a < 3; a++) f[a] = __dsub_rn(f[a], floor(f[a]));
+    mat_vec_exact(s.H, f, d);
+}
+
+// k_vector(e_axis) * r (cells.rs:224-226, ewald.rs:646-649): the phase of
+// e^{i k r} for index 1 along an axis (orthorhombic: the one coordinate).
+__device__ __forceinline__ double axis_phase(const SysDev& s, int axis, double x, double y, double z) {
+    if (!s.tric) return s.k1[axis] * (axis == 0 ? x : (axis == 1 ? y : z));
+    const double* k = s.kax + 3 * axis;
+    return __dadd_rn(__dadd_rn(__dmul_rn(k[0], x), __dmul_rn(k[1], y)), __dmul_rn(k[2], z));
+}
+
+// Squared minimum-image length of a displacement (list-rebuild tests).
+__device__ __forceinline__ double image_norm2(const SysDev& s, double dx, double dy, double dz) {
+    if (s.tric) {
+        double d[3] = {dx, dy, dz};
+        tric_image(s, d);
+        return d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    }
+    dx -= rint(dx * s.invL[0]) * s.L[0];
+    dy -= rint(dy * s.invL[1]) * s.L[1];
+    dz -= rint(dz * s.invL[2]) * s.L[2];
+    return dx * dx + dy * dy + dz * dz;
+}
+
+// Fractional coordinates of a position (fused: for the list builds and the
+// fixed-point copies, which need consistency, not the reference's roundings).
+__device__ __forceinline__ void tric_fractional(const SysDev& s, double x, double y, double z, double f[3]) {
+#pragma unroll
+    for (int a = 0; a < 3; a++) f[a] = fma(s.Hi[3 * a + 2], z, fma(s.Hi[3 * a + 1], y, s.Hi[3 * a] * x));
+}
+
+// Cartesian offset of a fractional offset in FP32 (fractions of the cell
+// vectors), each row a fixed sequence of roundings.
+__device__ __forceinline__ void tric_cartesian_f(const SysDev& s, float fx, float fy, float fz, float& dx,
+                                                 float& dy, float& dz) {
+    dx = __fmaf_rn(s.Hf[2], fz, __fmaf_rn(s.Hf[1], fy, __fmul_rn(s.Hf[0], fx)));
+    dy = __fmaf_rn(s.Hf[5], fz, __fmaf_rn(s.Hf[4], fy, __fmul_rn(s.Hf[3], fx)));
+    dz = __fmaf_rn(s.Hf[8], fz, __fmaf_rn(s.Hf[7], fy, __fmul_rn(s.Hf[6], fx)));
+}
 
 // Sum over one system's chunks of a per-chunk value a[stride * (begin + q)]
 // (chunk q: atoms begin + q * gpw ..., each chunk summed by a warp butterfly):
@@ -241,7 +316,25 @@ __device__ __forceinline__ float charge_f32(double q) {
     float f = (float)q;
     return (f == 0.0f && q != 0.0) ? (q < 0.0 ? -1.17549435e-38f : 1.17549435e-38f) : f;
 }
+// (triclinic: u = floor(frac(f) * 2^32) of the fractional coordinates f, so
+// the signed 32-bit difference of two atoms is the fractional difference
+// minus its nearest integer, as vector_image takes it)
+__device__ __forceinline__ uint3 fixed_coordinates(const SysDev& s, double4_32a p) {
+    if (s.tric) {
+        double f[3];
+        tric_fractional(s, p.x, p.y, p.z, f);
+        return make_uint3(fixed_coordinate(f[0], 4294967296.0), fixed_coordinate(f[1], 4294967296.0),
+                          fixed_coordinate(f[2], 4294967296.0));
+    }
+    return make_uint3(fixed_coordinate(p.x, s.fxscale[0]), fixed_coordinate(p.y, s.fxscale[1]),
+                      fixed_coordinate(p.z, s.fxscale[2]));
+}
 __device__ __forceinline__ uint4 fixed_position(const SysDev& s, double4_32a p) {
+    uint3 u = fixed_coordinates(s, p);
+    return make_uint4(u.x, u.y, u.z, __float_as_uint(charge_f32(p.w)));
+}
+// Orthorhombic only (the persistent kernel, whose batches have no triclinic cell).
+__device__ __forceinline__ uint4 fixed_position_ortho(const SysDev& s, double4_32a p) {
     return make_uint4(fixed_coordinate(p.x, s.fxscale[0]), fixed_coordinate(p.y, s.fxscale[1]),
                       fixed_coordinate(p.z, s.fxscale[2]), __float_as_uint(charge_f32(p.w)));
 }
@@ -249,6 +342,10 @@ __device__ __forceinline__ uint4 fixed_position(const SysDev& s, double4_32a p) 
 // word of an atom's record never changes between list builds, so they store
 // x, y, z only (store_fixed_xyz) and skip its FP64 conversion.
 __device__ __forceinline__ uint4 fixed_xyz(const SysDev& s, double4_32a p) {
+    uint3 u = fixed_coordinates(s, p);
+    return make_uint4(u.x, u.y, u.z, 0u);
+}
+__device__ __forceinline__ uint4 fixed_xyz_ortho(const SysDev& s, double4_32a p) {
     return make_uint4(fixed_coordinate(p.x, s.fxscale[0]), fixed_coordinate(p.y, s.fxscale[1]),
                       fixed_coordinate(p.z, s.fxscale[2]), 0u);
 }
@@ -265,6 +362,26 @@ __device__ __forceinline__ float fixed_dist2(uint4 a, uint4 b, const float* Lq) 
     float dx = __fmul_rn((float)(int32_t)(a.x - b.x), Lq[0]);
     float dy = __fmul_rn((float)(int32_t)(a.y - b.y), Lq[1]);
     float dz = __fmul_rn((float)(int32_t)(a.z - b.z), Lq[2]);
+    return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
+// Cartesian minimum-image offset of two fixed-point positions in FP32
+// (vector_image's image: each fractional difference wrapped into [-1/2, 1/2)).
+__device__ __forceinline__ void fixed_delta(const SysDev& s, uint4 a, uint4 b, float& dx, float& dy, float& dz) {
+    if (s.tric) {
+        const float q = 2.3283064365386963e-10f;  // 2^-32
+        tric_cartesian_f(s, __fmul_rn((float)(int32_t)(a.x - b.x), q), __fmul_rn((float)(int32_t)(a.y - b.y), q),
+                         __fmul_rn((float)(int32_t)(a.z - b.z), q), dx, dy, dz);
+    } else {
+        dx = __fmul_rn((float)(int32_t)(a.x - b.x), s.Lq[0]);
+        dy = __fmul_rn((float)(int32_t)(a.y - b.y), s.Lq[1]);
+        dz = __fmul_rn((float)(int32_t)(a.z - b.z), s.Lq[2]);
+    }
+}
+// fixed_dist2 for any cell shape (the per-step kernels)
+__device__ __forceinline__ float fixed_dist2_s(const SysDev& s, uint4 a, uint4 b) {
+    if (!s.tric) return fixed_dist2(a, b, s.Lq);
+    float dx, dy, dz;
+    fixed_delta(s, a, b, dx, dy, dz);
     return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
 }
 
@@ -455,6 +572,14 @@ __device__ __forceinline__ double exact_norm(double x, double y, double z) {
 __device__ __forceinline__ void exact_nearest_image(const SysDev& s, double xi, double yi, double zi,
                                                     double xj, double yj, double zj, double& dx,
                                                     double& dy, double& dz) {
+    if (s.tric) {
+        double d[3] = {__dsub_rn(xi, xj), __dsub_rn(yi, yj), __dsub_rn(zi, zj)};
+        tric_image(s, d);
+        dx = d[0];
+        dy = d[1];
+        dz = d[2];
+        return;
+    }
     dx = exact_image(__dsub_rn(xi, xj), s.L[0], s.invL[0]);
     dy = exact_image(__dsub_rn(yi, yj), s.L[1], s.invL[1]);
     dz = exact_image(__dsub_rn(zi, zj), s.L[2], s.invL[2]);

@@ -85,9 +85,22 @@ static_assert(CTL_REMOVE_TRANSLATION == LG_CONTROL_REMOVE_TRANSLATION && CTL_REW
                   CTL_REMOVE_ROTATION == LG_CONTROL_REMOVE_ROTATION,
               "control values");
 
+// UnitCell (lumol-core/src/sys/config/cells.rs): its shape and matrix, and
+// what the engine derives from them with the reference's operations.
+struct HostCell {
+    int shape = LG_CELL_ORTHORHOMBIC;
+    double m[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};    // UnitCell::matrix, row-major (columns: cell vectors)
+    double inv[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // Matrix3::inverse (types/matrix.rs:212-227)
+    double len[3] = {0, 0, 0};                    // lengths(): distances between opposite faces (cells.rs:134-146)
+    double volume = 0.0;                          // volume() (cells.rs:185-200)
+};
+// Fills c from a cell matrix and its shape; false for a singular matrix.
+bool cell_init(HostCell& c, const double m[9], int shape);
+
 struct HostSystem {
     bool has_cell = false;
-    double L[3] = {0, 0, 0};
+    HostCell cell;
+    double L[3] = {0, 0, 0};  // cell.len (the orthorhombic lengths a, b, c)
     int64_t n = 0;
     std::vector<int32_t> kinds, mols;
     std::vector<double> charges, masses;
@@ -218,7 +231,7 @@ struct lg_engine {
     int64_t mc_mol_begin = 0, mc_mol_size = 0;
     // a pending move_all_molecules_cost: the configuration before the move
     bool mc_resize = false;
-    double mc_old_L[3] = {0, 0, 0};
+    HostCell mc_old_cell;
     DBuf<double4_32a> mc_saved_pos;
 
     void drop_graphs() {
@@ -258,7 +271,7 @@ double max_cutoff(const HostSystem& h);
 int check_pair_cutoffs(lg_engine* e, const HostSystem& h);
 // System::set_pair_potential / set_coulomb_potential's check (sys/system.rs:122-131,
 // 159-170) of the potentials of h against the cell lengths L.
-int check_cell_cutoffs(lg_engine* e, const HostSystem& h, const double L[3]);
+int check_cell_cutoffs(lg_engine* e, const HostSystem& h, const double len[3]);
 // Lowers the description into device memory when it changed (e->dirty).
 int commit(lg_engine* e);
 // A new orthorhombic cell for system s of a lowered batch, in place: the
@@ -266,7 +279,9 @@ int commit(lg_engine* e);
 // constants, and a list rebuild; the device state is kept.  Returns -1 (and
 // changes nothing) when the cell grid or the k-vector set would change: the
 // caller then lowers the batch again (invalidate); LG_OK or an LG_ERR_* else.
-int set_cell_fast(lg_engine* e, int s, const double L[3]);
+int set_cell_fast(lg_engine* e, int s, const HostCell& cell);
+// Installs `cell` as system s's cell on the host (no device work).
+void set_host_cell(HostSystem& h, const HostCell& cell);
 // commit() for a batch whose systems all keep their device state (systems
 // left, or were re-described without new particles); LG_ERR_STATE otherwise.
 int commit_carried(lg_engine* e);

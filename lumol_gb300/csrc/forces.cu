@@ -133,9 +133,8 @@ __global__ void __launch_bounds__(256) pair_half_kernel(
     for (int k = k0 + sub; k < cnt; k += TPA) {
         int j = list[k];
         uint4 uj = pfx[j];
-        float dxf = (float)(int32_t)(ui.x - uj.x) * s.Lq[0];
-        float dyf = (float)(int32_t)(ui.y - uj.y) * s.Lq[1];
-        float dzf = (float)(int32_t)(ui.z - uj.z) * s.Lq[2];
+        float dxf, dyf, dzf;
+        fixed_delta(s, ui, uj, dxf, dyf, dzf);
         float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
         const PairDev& p = prow[kind[j]];
         bool pc = pairs && p.type != 0;
@@ -149,7 +148,7 @@ __global__ void __launch_bounds__(256) pair_half_kernel(
             double4_32a pj = posq[j];
             double dx, dy, dz, r = 0.0, r2 = 0.0;
             PairDecision dec;
-            if (band) {
+            if (band || s.tric) {  // (a triclinic cell takes the exact geometry for every pair)
                 exact_nearest_image(s, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z, dx, dy, dz);
                 r = exact_norm(dx, dy, dz);
                 dec = decide_pair(s, p, terms, i, j, mi, mol[j], pi.w, pj.w, r, spec_off, spec_j, spec_path);
@@ -493,7 +492,7 @@ __global__ void eikr_kernel(int n, int kdim, const double4_32a* __restrict__ pos
     if (s.coul != 1) return;
     double4_32a p = posq[i];
     double x = axis == 0 ? p.x : (axis == 1 ? p.y : p.z);
-    double phi = s.k1[axis] * x;
+    double phi = axis_phase(s, axis, p.x, p.y, p.z);
     double sn, cs;
     sincos(phi, &sn, &cs);
     double2 e1 = make_double2(cs, sn);
@@ -796,9 +795,8 @@ __global__ void __launch_bounds__(128) molecular_virial_kernel(
             f_over_r += fr;
         }
         double4_32a cj = com[j];
-        double rx = exact_image(__dsub_rn(ci.x, cj.x), s.L[0], s.invL[0]);
-        double ry = exact_image(__dsub_rn(ci.y, cj.y), s.L[1], s.invL[1]);
-        double rz = exact_image(__dsub_rn(ci.z, cj.z), s.L[2], s.invL[2]);
+        double rx, ry, rz;
+        exact_nearest_image(s, ci.x, ci.y, ci.z, cj.x, cj.y, cj.z, rx, ry, rz);
         double scale = f_over_r * (dx * rx + dy * ry + dz * rz) / (dx * dx + dy * dy + dz * dz);
         double gx = scale * dx, gy = scale * dy, gz = scale * dz;
         w[0] += gx * dx; w[1] += gx * dy; w[2] += gx * dz;

@@ -163,7 +163,7 @@ void launch_mc_cost(const Batch& b, int s, const SysDev& sd, int mbeg, int msize
                     double2* d_new_eikr, double2* d_drho, double* d_partial, double* d_dk, double* d_out,
                     cudaStream_t st);
 void launch_mc_accept(const Batch& b, const SysDev& sd, int mbeg, int msize, const double* d_newpos,
-                      const double* d_k1, const double2* d_drho, cudaStream_t st);
+                      const SysDev* d_sys, const double2* d_drho, cudaStream_t st);
 void launch_mc_chains(const Batch& b, McState* mc, bool fp64, cudaStream_t st);
 // diag.cu
 int measure_fma_peak(int fp64, double* tflops);

@@ -200,31 +200,27 @@ double pot_tail_virial(const lg_pair& p, double rc) {
     return 0.0;
 }
 
-// Matrix3::inverse of diag(a, b, c) (types/matrix.rs:212-227), diagonal only
-void ortho_inverse_diag(const double L[3], double out[3]) {
-    double a = L[0], b = L[1], c = L[2];
-    double m[3][3] = {{a, 0.0, 0.0}, {0.0, b, 0.0}, {0.0, 0.0, c}};
-    double det = m[0][0] * (m[1][1] * m[2][2] - m[2][1] * m[1][2]) -
-                 m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) +
-                 m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
-    double id = 1.0 / det;
-    out[0] = (m[1][1] * m[2][2] - m[2][1] * m[1][2]) * id;
-    out[1] = (m[0][0] * m[2][2] - m[0][2] * m[2][0]) * id;
-    out[2] = (m[0][0] * m[1][1] - m[1][0] * m[0][1]) * id;
+// UnitCell::k_vector (cells.rs:224-226): (2 PI * inv) * index, the scaled
+// matrix times the vector row by row (matrix.rs:389-398).
+void k_vector(const HostCell& c, double i0, double i1, double i2, double k[3]) {
+    for (int a = 0; a < 3; a++) {
+        const double* r = c.inv + 3 * a;
+        k[a] = (2.0 * PI) * r[0] * i0 + (2.0 * PI) * r[1] * i1 + (2.0 * PI) * r[2] * i2;
+    }
 }
 
 // Ewald::prepare + compute_ewald_factors_triclinic (ewald.rs:130-183, 353-379)
-void ewald_factors(const double L[3], double alpha, int kmax, int sys, std::vector<KVecDev>& out) {
-    double inv[3];
-    ortho_inverse_diag(L, inv);
-    double s[3] = {(2.0 * PI) * inv[0], (2.0 * PI) * inv[1], (2.0 * PI) * inv[2]};
-    // k_vector([1, 1, 1]).max() * kmax; off-diagonal products are zero
-    double mx = std::max(std::max(s[0], s[1]), s[2]) * (double)kmax;
+void ewald_factors(const HostCell& cell, double alpha, int kmax, int sys, std::vector<KVecDev>& out) {
+    // k_vector([1, 1, 1]).max() * kmax (Vector3D::max: the largest component)
+    double k111[3];
+    k_vector(cell, 1.0, 1.0, 1.0, k111);
+    double mx = std::max(std::max(k111[0], k111[1]), k111[2]) * (double)kmax;
     double kmax2 = 1.0001 * mx * mx;
     double alpha_sq_inv_fourth = 0.25 / (alpha * alpha);
-    double four_pi_v = 4.0 * PI / (L[0] * L[1] * L[2]);
+    double four_pi_v = 4.0 * PI / cell.volume;
     auto push = [&](int ikx, int iky, int ikz) {
-        double k[3] = {s[0] * (double)ikx, s[1] * (double)iky, s[2] * (double)ikz};
+        double k[3];
+        k_vector(cell, (double)ikx, (double)iky, (double)ikz, k);
         double k2 = k[0] * k[0] + k[1] * k[1] + k[2] * k[2];
         if (k2 > kmax2) return;
         KVecDev f;
@@ -280,6 +276,61 @@ void bond_paths(const HostSystem& h, int64_t base, std::vector<std::vector<std::
 
 }  // namespace
 
+// UnitCell's derived values (cells.rs:108-200) with the reference's
+// operations: Matrix3::inverse (matrix.rs:212-249), lengths() from the face
+// normals (b ^ c).normalized() (vectors.rs:102-130, 219-228), volume() as
+// a * b * c (orthorhombic) or the mixed product a * (b ^ c) (triclinic).
+bool cell_init(HostCell& c, const double m[9], int shape) {
+    c.shape = shape;
+    for (int k = 0; k < 9; k++) c.m[k] = m[k];
+    auto M = [&](int i, int j) { return m[3 * i + j]; };
+    double det = M(0, 0) * (M(1, 1) * M(2, 2) - M(2, 1) * M(1, 2)) - M(0, 1) * (M(1, 0) * M(2, 2) - M(1, 2) * M(2, 0)) +
+                 M(0, 2) * (M(1, 0) * M(2, 1) - M(1, 1) * M(2, 0));
+    if (!(std::fabs(det) > 1e-30)) return false;
+    double id = 1.0 / det;
+    double* r = c.inv;
+    r[0] = (M(1, 1) * M(2, 2) - M(2, 1) * M(1, 2)) * id;
+    r[1] = (M(0, 2) * M(2, 1) - M(0, 1) * M(2, 2)) * id;
+    r[2] = (M(0, 1) * M(1, 2) - M(0, 2) * M(1, 1)) * id;
+    r[3] = (M(1, 2) * M(2, 0) - M(1, 0) * M(2, 2)) * id;
+    r[4] = (M(0, 0) * M(2, 2) - M(0, 2) * M(2, 0)) * id;
+    r[5] = (M(1, 0) * M(0, 2) - M(0, 0) * M(1, 2)) * id;
+    r[6] = (M(1, 0) * M(2, 1) - M(2, 0) * M(1, 1)) * id;
+    r[7] = (M(2, 0) * M(0, 1) - M(0, 0) * M(2, 1)) * id;
+    r[8] = (M(0, 0) * M(1, 1) - M(1, 0) * M(0, 1)) * id;
+    double va[3] = {M(0, 0), M(1, 0), M(2, 0)}, vb[3] = {M(0, 1), M(1, 1), M(2, 1)}, vc[3] = {M(0, 2), M(1, 2), M(2, 2)};
+    auto cross = [](const double* x, const double* y, double* z) {
+        z[0] = x[1] * y[2] - x[2] * y[1];
+        z[1] = x[2] * y[0] - x[0] * y[2];
+        z[2] = x[0] * y[1] - x[1] * y[0];
+    };
+    auto dot = [](const double* x, const double* y) { return x[0] * y[0] + x[1] * y[1] + x[2] * y[2]; };
+    auto face = [&](const double* x, const double* y, const double* v) {
+        double n[3];
+        cross(x, y, n);
+        double norm = std::sqrt(dot(n, n));
+        for (int k = 0; k < 3; k++) n[k] = n[k] / norm;
+        return std::fabs(dot(n, v));
+    };
+    c.len[0] = face(vb, vc, va);
+    c.len[1] = face(vc, va, vb);
+    c.len[2] = face(va, vb, vc);
+    if (shape == LG_CELL_ORTHORHOMBIC) {
+        c.volume = M(0, 0) * M(1, 1) * M(2, 2);
+    } else {
+        double bc[3];
+        cross(vb, vc, bc);
+        c.volume = dot(va, bc);
+    }
+    return c.volume > 0.0;
+}
+
+void set_host_cell(HostSystem& h, const HostCell& cell) {
+    h.cell = cell;
+    for (int k = 0; k < 3; k++) h.L[k] = cell.len[k];
+    h.has_cell = true;
+}
+
 // The MD fields of a system's device record.
 void fill_md(SysDev& d, const HostSystem& h) {
     d.dt = h.dt;
@@ -315,8 +366,8 @@ int check_pair_cutoffs(lg_engine* e, const HostSystem& h) {
     return check_cell_cutoffs(e, h, h.L);
 }
 
-int check_cell_cutoffs(lg_engine* e, const HostSystem& h, const double L[3]) {
-    double half = 0.5 * std::min(std::min(L[0], L[1]), L[2]);
+int check_cell_cutoffs(lg_engine* e, const HostSystem& h, const double len[3]) {
+    double half = 0.5 * std::min(std::min(len[0], len[1]), len[2]);
     for (const lg_pair& p : h.pairs)
         if (p.type != LG_PAIR_ABSENT && half < p.cutoff)
             return fail(e, LG_ERR_ARGUMENT,
@@ -332,8 +383,17 @@ int check_cell_cutoffs(lg_engine* e, const HostSystem& h, const double L[3]) {
 // The fields of a system's device record that follow from its cell: lengths
 // and their inverses in FP64 / FP32, the fixed-point scale, the list radius
 // and rebuild threshold, and the cell grid (cells at least half the list
-// radius wide: the list builds look two cells around).
-void cell_geometry(SysDev& d, const HostSystem& h, const double L[3], double skin) {
+// radius wide: the list builds look two cells around).  A triclinic cell's
+// grid divides the fractional coordinates: its cells are at least half the
+// list radius apart across every pair of faces.
+void cell_geometry(SysDev& d, const HostSystem& h, const HostCell& cell, double skin) {
+    const double* L = cell.len;
+    d.tric = cell.shape == LG_CELL_TRICLINIC;
+    for (int k = 0; k < 9; k++) {
+        d.H[k] = cell.m[k];
+        d.Hi[k] = cell.inv[k];
+        d.Hf[k] = (float)cell.m[k];
+    }
     for (int k = 0; k < 3; k++) {
         d.L[k] = L[k];
         d.invL[k] = 1.0 / L[k];
@@ -354,18 +414,23 @@ void cell_geometry(SysDev& d, const HostSystem& h, const double L[3], double ski
     }
 }
 
-// k_vector([1, 0, 0]) etc. of the cell (cells.rs:224-226): 2 PI times the
-// diagonal of the inverse cell matrix.
-void ewald_k1(SysDev& d, const double L[3]) {
-    double inv[3];
-    ortho_inverse_diag(L, inv);
-    for (int k = 0; k < 3; k++) d.k1[k] = (2.0 * PI) * inv[k];
+// k_vector([1, 0, 0]) etc. of the cell (cells.rs:224-226): the columns of
+// 2 PI inv; k1 holds their one non-zero component for an orthorhombic cell.
+void ewald_k1(SysDev& d, const HostCell& cell) {
+    for (int a = 0; a < 3; a++) {
+        double e[3] = {0.0, 0.0, 0.0};
+        e[a] = 1.0;
+        double k[3];
+        k_vector(cell, e[0], e[1], e[2], k);
+        for (int c = 0; c < 3; c++) d.kax[3 * a + c] = k[c];
+        d.k1[a] = k[a];
+    }
 }
 
 // Tail corrections (sys/energy.rs:63-79, compute.rs:219-229), kinds in index
 // order, at the current volume.
 void tail_corrections(HostSystem& h) {
-    double volume = h.L[0] * h.L[1] * h.L[2];
+    double volume = h.cell.volume;
     std::vector<int64_t> counts(h.nk, 0);
     for (int32_t k : h.kinds) counts[k]++;
     double te = 0.0, tv = 0.0;
@@ -384,19 +449,19 @@ void tail_corrections(HostSystem& h) {
     h.tail_virial = tv;
 }
 
-int set_cell_fast(lg_engine* e, int s, const double L[3]) {
+int set_cell_fast(lg_engine* e, int s, const HostCell& cell) {
     HostSystem& h = e->sys[s];
     SysDev d = e->h_sysdev[s];
-    cell_geometry(d, h, L, e->skin);
+    cell_geometry(d, h, cell, e->skin);
     const SysDev& old = e->h_sysdev[s];
     if (d.ncell[0] != old.ncell[0] || d.ncell[1] != old.ncell[1] || d.ncell[2] != old.ncell[2]) return -1;
     std::vector<KVecDev> kv;
     if (h.coul.kind == LG_COULOMB_EWALD) {
-        ewald_k1(d, L);
-        ewald_factors(L, h.alpha, h.coul.kmax, s, kv);
+        ewald_k1(d, cell);
+        ewald_factors(cell, h.alpha, h.coul.kmax, s, kv);
         if ((int)kv.size() != old.kend - old.kbegin) return -1;  // another k-vector set: lower again
     }
-    for (int k = 0; k < 3; k++) h.L[k] = L[k];
+    set_host_cell(h, cell);
     tail_corrections(h);
     e->h_sysdev[s] = d;
     cudaStream_t st = e->stream;
@@ -653,14 +718,14 @@ int commit(lg_engine* e) {
         d.needs_path = needs_path;
 
         // cell and neighbour list geometry
-        cell_geometry(d, h, h.L, e->skin);
+        cell_geometry(d, h, h.cell, e->skin);
         const int cells = d.ncell[0] * d.ncell[1] * d.ncell[2];
         d.cell_begin = cell_total;
         cell_total += cells;
         d.tile_begin = (int)h_tiles.size();
         for (int64_t a = 0; a < h.n; a += VV_TILE) h_tiles.push_back(make_int2(s, (int)(base + a)));
         d.tile_end = (int)h_tiles.size();
-        double volume = h.L[0] * h.L[1] * h.L[2];
+        double volume = h.cell.volume;
         if (h.n > 0) {
             double expected = (double)h.n / volume * 4.0 / 3.0 * PI * d.rlist * d.rlist * d.rlist;
             max_expected = std::max(max_expected, expected);
@@ -678,9 +743,9 @@ int commit(lg_engine* e) {
             d.alpha = h.alpha;
             d.kmax = h.coul.kmax;
             kdim = std::max(kdim, h.coul.kmax + 1);
-            ewald_k1(d, h.L);
+            ewald_k1(d, h.cell);
             d.kbegin = (int)h_kvec.size();
-            ewald_factors(h.L, h.alpha, h.coul.kmax, s, h_kvec);
+            ewald_factors(h.cell, h.alpha, h.coul.kmax, s, h_kvec);
             d.kend = (int)h_kvec.size();
             // Ewald::self_energy (ewald.rs:619-626)
             double q2 = 0.0;
@@ -990,6 +1055,9 @@ int commit(lg_engine* e) {
     b.pair_general = 0;
     for (const PairDevF& q : h_ptabf) b.pair_general |= (q.type != 0 && q.restriction != 0) ? 1 : 0;
     for (int s = 0; s < nsys; s++) b.pair_general |= e->h_sysdev[s].coul != 0 ? 1 : 0;
+    // a triclinic cell's minimum image is in the general kernels only (and
+    // keeps its batch off the persistent kernel)
+    for (int s = 0; s < nsys; s++) b.pair_general |= e->h_sysdev[s].tric ? 1 : 0;
     b.kvecf = e->kvecf.p;
     b.eikrf = e->eikrf.p;
     b.rhof = e->rhof.p;

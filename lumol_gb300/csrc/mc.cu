@@ -97,7 +97,7 @@ __global__ void mc_new_eikr_kernel(int sys_index, int msize, const double* __res
     const SysDev& s = sys[sys_index];
     int axis = t / msize, a = t - axis * msize;
     double sn, cs;
-    sincos(s.k1[axis] * newpos[3 * a + axis], &sn, &cs);
+    sincos(axis_phase(s, axis, newpos[3 * a], newpos[3 * a + 1], newpos[3 * a + 2]), &sn, &cs);
     double2 e1 = make_double2(cs, sn), v = e1;
     out[(size_t)(0 * 3 + axis) * msize + a] = make_double2(1.0, 0.0);
     out[(size_t)(1 * 3 + axis) * msize + a] = e1;
@@ -180,7 +180,7 @@ __global__ void mc_accept_kernel(int kbegin, int nk, const double2* __restrict__
 }
 
 __global__ void mc_set_positions_kernel(int n, int mbeg, int msize, int kmax, const double* __restrict__ newpos,
-                                        const double* __restrict__ k1, double4_32a* __restrict__ posq,
+                                        const SysDev* __restrict__ sysp, double4_32a* __restrict__ posq,
                                         double2* __restrict__ eikr, int update_eikr) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 3 * msize) return;
@@ -192,7 +192,7 @@ __global__ void mc_set_positions_kernel(int n, int mbeg, int msize, int kmax, co
     else posq[i].z = x;
     if (!update_eikr) return;
     double sn, cs;
-    sincos(k1[axis] * x, &sn, &cs);
+    sincos(axis_phase(*sysp, axis, newpos[3 * a], newpos[3 * a + 1], newpos[3 * a + 2]), &sn, &cs);
     double2 e1 = make_double2(cs, sn), v = e1;
     eikr[(size_t)(0 * 3 + axis) * n + i] = make_double2(1.0, 0.0);
     eikr[(size_t)(1 * 3 + axis) * n + i] = e1;
@@ -220,11 +220,11 @@ void launch_mc_cost(const Batch& b, int s, const SysDev& sd, int mbeg, int msize
 }
 
 void launch_mc_accept(const Batch& b, const SysDev& sd, int mbeg, int msize, const double* d_newpos,
-                      const double* d_k1, const double2* d_drho, cudaStream_t st) {
+                      const SysDev* d_sys, const double2* d_drho, cudaStream_t st) {
     int nk = sd.coul == 1 ? sd.kend - sd.kbegin : 0;
     if (nk > 0) mc_accept_kernel<<<(nk + 127) / 128, 128, 0, st>>>(sd.kbegin, nk, d_drho, b.rho);
     if (msize > 0)
-        mc_set_positions_kernel<<<(3 * msize + 127) / 128, 128, 0, st>>>(b.n, mbeg, msize, sd.kmax, d_newpos, d_k1,
+        mc_set_positions_kernel<<<(3 * msize + 127) / 128, 128, 0, st>>>(b.n, mbeg, msize, sd.kmax, d_newpos, d_sys,
                                                                         b.posq, b.eikr, nk > 0 ? 1 : 0);
 }
 

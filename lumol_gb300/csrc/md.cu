@@ -87,6 +87,7 @@ __device__ __forceinline__ void flag_rebuild(bool moved, int si, uint32_t* statu
 // Squared displacement since the last list build on the plain path: FP32 on
 // the FP64 differences, minimum image.
 __device__ __forceinline__ float plain_displacement2(const SysDev& s, const double4_32a& p, const double4_32a& b) {
+    if (s.tric) return (float)image_norm2(s, p.x - b.x, p.y - b.y, p.z - b.z);
     float dx = (float)(p.x - b.x);
     float dy = (float)(p.y - b.y);
     float dz = (float)(p.z - b.z);
@@ -304,7 +305,7 @@ __global__ void __launch_bounds__(VV_TILE) md_first_kernel(
         }
         uint4 u = fixed_xyz(s, p);
         store_fixed_xyz(posfx + perm[i], u);  // a rebuild this step rewrites it in the new order
-        r2 = fixed_dist2(u, pfx_build[i], s.Lq);  // as the persistent kernel
+        r2 = fixed_dist2_s(s, u, pfx_build[i]);  // as the persistent kernel
     } else {
         if (leap) {  // (v dt) + ((0.5 a) dt^2)
             p.x = __dadd_rn(p.x, __dadd_rn(__dmul_rn(v.x, dt), __dmul_rn(__dmul_rn(0.5, a.x), s.dt2)));
@@ -397,7 +398,7 @@ __global__ void __launch_bounds__(VV_TILE) md_second_kernel(
             if (MIXED) {
                 uint4 u = fixed_position(s, x);
                 posfx[perm[i]] = u;
-                r2 = fixed_dist2(u, pfx_build[i], s.Lq);
+                r2 = fixed_dist2_s(s, u, pfx_build[i]);
             } else {
                 r2 = plain_displacement2(s, x, pos_build[i]);
                 if (posfx) posfx[i] = fixed_position(s, x);
@@ -502,10 +503,17 @@ __global__ void rewrap_kernel(int nmol, const int* __restrict__ mol_start, const
         c[2] = __dadd_rn(c[2], __dmul_rn(m, p.z));
     }
     double delta[3];
-    for (int d = 0; d < 3; d++) {
-        double com = __ddiv_rn(c[d], total);
-        double wrapped = __dsub_rn(com, __dmul_rn(floor(__ddiv_rn(com, s.L[d])), s.L[d]));
-        delta[d] = __dsub_rn(wrapped, com);
+    if (s.tric) {  // wrap_vector's triclinic branch (cells.rs:271-279)
+        double com[3], w[3];
+        for (int d = 0; d < 3; d++) com[d] = w[d] = __ddiv_rn(c[d], total);
+        tric_wrap(s, w);
+        for (int d = 0; d < 3; d++) delta[d] = __dsub_rn(w[d], com[d]);
+    } else {
+        for (int d = 0; d < 3; d++) {
+            double com = __ddiv_rn(c[d], total);
+            double wrapped = __dsub_rn(com, __dmul_rn(floor(__ddiv_rn(com, s.L[d])), s.L[d]));
+            delta[d] = __dsub_rn(wrapped, com);
+        }
     }
     if (delta[0] == 0.0 && delta[1] == 0.0 && delta[2] == 0.0) return;
     for (int a = a0; a < a1; a++) {
@@ -541,11 +549,7 @@ __global__ void check_displacement_kernel(int n, const int* __restrict__ sysid, 
     int si = sysid[i];
     const SysDev& s = sys[si];
     double4_32a p = posq[i], b = pos_build[i];
-    double dx = p.x - b.x, dy = p.y - b.y, dz = p.z - b.z;
-    dx -= rint(dx * s.invL[0]) * s.L[0];
-    dy -= rint(dy * s.invL[1]) * s.L[1];
-    dz -= rint(dz * s.invL[2]) * s.L[2];
-    flag_rebuild(!(dx * dx + dy * dy + dz * dz <= s.half_skin2), si, status, sys_rebuild);
+    flag_rebuild(!(image_norm2(s, p.x - b.x, p.y - b.y, p.z - b.z) <= s.half_skin2), si, status, sys_rebuild);
 }
 
 void launch_check_displacement(const Batch& b, cudaStream_t st) {

@@ -129,9 +129,14 @@ __device__ __forceinline__ void mixed_entry(
     const int* __restrict__ spec_j, const int8_t* __restrict__ spec_path, bool pairs, bool coul, float coul_rc2,
     float alpha, float pref, bool single, int4 ph1, float4 pq1, const double4_32a* __restrict__ posq) {
     float qj = __uint_as_float(pj.w);
-    float dx = fixed_image(pi.x, pj.x, s.Lq[0]);
-    float dy = fixed_image(pi.y, pj.y, s.Lq[1]);
-    float dz = fixed_image(pi.z, pj.z, s.Lq[2]);
+    float dx, dy, dz;
+    if (GENERAL && s.tric) {  // (the general kernels only: batches with a triclinic cell take them)
+        fixed_delta(s, pi, pj, dx, dy, dz);
+    } else {
+        dx = fixed_image(pi.x, pj.x, s.Lq[0]);
+        dy = fixed_image(pi.y, pj.y, s.Lq[1]);
+        dz = fixed_image(pi.z, pj.z, s.Lq[2]);
+    }
     float r2 = rfma(dz, dz, rfma(dy, dy, rmul(dx, dx)));
     // the parameters as two 16-byte loads: (type, restriction, -, -) and (a, b, c, rc2);
     // a system with one kind passes them in (loaded once per atom)
@@ -200,8 +205,8 @@ __device__ __forceinline__ void mixed_entry(
                     // energy.  The force is then rounded to FP32 like the others.
                     const int j = order[js];
                     const double4_32a a4 = posq[i], b4 = posq[j];
-                    double d[3] = {a4.x - b4.x, a4.y - b4.y, a4.z - b4.z};
-                    for (int k = 0; k < 3; k++) d[k] = exact_image(d[k], s.L[k], s.invL[k]);
+                    double d[3];
+                    exact_nearest_image(s, a4.x, a4.y, a4.z, b4.x, b4.y, b4.z, d[0], d[1], d[2]);
                     double rd2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
                     double rd = sqrt(rd2);
                     double ad = s.alpha * rd;

@@ -115,10 +115,19 @@ __global__ void nl_bin_kernel(int nsys, const int* __restrict__ plan, const doub
         pos_build[i] = p;
         double w[3] = {p.x, p.y, p.z};
         int c[3];
-        for (int d = 0; d < 3; d++) {
-            w[d] -= floor(w[d] / s.L[d]) * s.L[d];
-            int cd = (int)(w[d] * s.invL[d] * (double)s.ncell[d]);
-            c[d] = min(max(cd, 0), s.ncell[d] - 1);
+        if (s.tric) {  // the wrapped fractional coordinates: cells of the fractional grid
+            tric_fractional(s, p.x, p.y, p.z, w);
+            for (int d = 0; d < 3; d++) {
+                w[d] -= floor(w[d]);
+                int cd = (int)(w[d] * (double)s.ncell[d]);
+                c[d] = min(max(cd, 0), s.ncell[d] - 1);
+            }
+        } else {
+            for (int d = 0; d < 3; d++) {
+                w[d] -= floor(w[d] / s.L[d]) * s.L[d];
+                int cd = (int)(w[d] * s.invL[d] * (double)s.ncell[d]);
+                c[d] = min(max(cd, 0), s.ncell[d] - 1);
+            }
         }
         int cell = s.cell_begin + (c[2] * s.ncell[1] + c[1]) * s.ncell[0] + c[0];
         atom_cell[i] = cell;
@@ -346,15 +355,19 @@ __global__ void __launch_bounds__(32 * NL_WARPS) nl_build_kernel(
                 int slot = stencil_slot(s_lo[wib], s_pre[wib], nruns, t);
                 if (perm) {  // the same test as the persistent kernel's list build
                     jout = slot;
-                    keep = slot != row && fixed_dist2(ui, posfx[slot], s.Lq) < rl2;
+                    keep = slot != row && fixed_dist2_s(s, ui, posfx[slot]) < rl2;
                 } else {
                     j = cell_atoms[slot];
                     jout = j;
                     float4 pj = wpos[j];
                     float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-                    dx -= rintf(dx * ix) * Lx;
-                    dy -= rintf(dy * iy) * Ly;
-                    dz -= rintf(dz * iz) * Lz;
+                    if (s.tric) {  // wpos holds wrapped fractional coordinates
+                        tric_cartesian_f(s, dx - rintf(dx), dy - rintf(dy), dz - rintf(dz), dx, dy, dz);
+                    } else {
+                        dx -= rintf(dx * ix) * Lx;
+                        dy -= rintf(dy * iy) * Ly;
+                        dz -= rintf(dz * iz) * Lz;
+                    }
                     float r2 = dx * dx + dy * dy + dz * dz;
                     keep = (j != i) && (r2 < rl2);
                 }

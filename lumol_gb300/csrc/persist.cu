@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
             b.vel[i] = vel;
             b.posq[i] = p;
             flag_nonfinite(p.x, p.y, p.z, s, b.sys_status, b.status);
-            uint4 u = fixed_xyz(sd, p);
+            uint4 u = fixed_xyz_ortho(sd, p);
             store_fixed_xyz(b.posfx + b.perm[i], u);
             if (fixed_dist2(u, b.pfx_build[i], sd.Lq) > sd.rebuild2_f) b.sys_rebuild[s] = 1u;
         }
@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
                 int i = b.cell_atoms[t];
                 b.perm[i] = t;
                 b.km[t] = make_int2(b.kind[i], b.mol[i]);
-                uint4 u = fixed_position(sd, b.posq[i]);
+                uint4 u = fixed_position_ortho(sd, b.posq[i]);
                 b.posfx[t] = u;
                 b.pfx_build[i] = u;
             }

@@ -426,7 +426,7 @@ int persist_plan(lg_engine* e) {
     std::vector<double> work(nsys);
     for (int s = 0; s < nsys; s++) {
         const HostSystem& h = e->sys[s];
-        double V = h.L[0] * h.L[1] * h.L[2];
+        double V = h.cell.volume;
         double rl = e->h_sysdev[s].rlist;
         double entries = 0.0;
         for (int64_t i = e->begin[s]; i < e->begin[s + 1]; i++) entries += h_nnb[i];
@@ -605,7 +605,15 @@ int md_run_barostat(lg_engine* e, int64_t nsteps) {
             if (h.barostat == LG_BAROSTAT_NONE) continue;
             double eta = h.baro_eta;
             double e3 = eta * eta * eta;
-            double L[3] = {h.L[0] * e3, h.L[1] * e3, h.L[2] * e3};
+            // cell * (e3 * 1) with Matrix3's product (matrix.rs:342-362)
+            const double f[9] = {e3, 0.0 * e3, 0.0 * e3, 0.0 * e3, e3, 0.0 * e3, 0.0 * e3, 0.0 * e3, e3};
+            double m[9];
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++)
+                    m[3 * i + j] = h.cell.m[3 * i] * f[j] + h.cell.m[3 * i + 1] * f[3 + j] + h.cell.m[3 * i + 2] * f[6 + j];
+            HostCell cell;
+            if (!cell_init(cell, m, h.cell.shape)) return fail(e, LG_ERR_ARGUMENT, "the barostat made the cell singular");
+            const double* L = cell.len;
             double rc = max_cutoff(h);
             if (0.5 * L[0] <= rc || 0.5 * L[1] <= rc || 0.5 * L[2] <= rc)
                 return fail(e, LG_ERR_ARGUMENT,
@@ -613,10 +621,10 @@ int md_run_barostat(lg_engine* e, int64_t nsteps) {
                             "than the interactions cut off radius. You can try to increase the cell size or the "
                             "number of particles. (system " + std::to_string(s) + ")");
             e->h_sysdev[s].baro_eta = eta;
-            int rc2 = set_cell_fast(e, s, L);
+            int rc2 = set_cell_fast(e, s, cell);
             if (rc2 != LG_OK && rc2 != -1) return rc2;
             if (rc2 == -1) {  // another cell grid or k-vector set: lower the batch again, keeping the state
-                for (int k = 0; k < 3; k++) h.L[k] = L[k];
+                set_host_cell(h, cell);
                 invalidate(e);
                 int rc3 = commit_carried(e);
                 if (rc3) return rc3;
@@ -688,7 +696,7 @@ int md_run_barostat(lg_engine* e, int64_t nsteps) {
             const double* w = &out[(size_t)s * RED_STRIDE + 1];
             double dof = (double)(3 * h.n);
             double T = 2.0 * kin[s] / (dof * K_BOLTZMANN);  // Temperature (compute.rs:164-172)
-            double volume = h.L[0] * h.L[1] * h.L[2];
+            double volume = h.cell.volume;
             double P = (dof * K_BOLTZMANN * T + (w[0] + w[4] + w[8])) / (3.0 * volume);
             double eta3 = 1.0 - WATER_COMPRESSIBILITY / h.baro_tau * (h.baro_pressure - P);
             h.baro_eta = std::cbrt(eta3);
