@@ -92,6 +92,7 @@ LG_INTEGRATOR_VELOCITY_VERLET, LG_INTEGRATOR_VERLET, LG_INTEGRATOR_LEAP_FROG = 0
 LG_THERMOSTAT_NONE, LG_THERMOSTAT_BERENDSEN, LG_THERMOSTAT_RESCALE, LG_THERMOSTAT_CSVR = 0, 1, 2, 3
 LG_CONTROL_REMOVE_TRANSLATION, LG_CONTROL_REWRAP, LG_CONTROL_REMOVE_ROTATION = 1, 2, 4
 LG_BAROSTAT_NONE, LG_BAROSTAT_BERENDSEN = 0, 1
+LG_CELL_ORTHORHOMBIC, LG_CELL_TRICLINIC = 0, 1
 
 
 class LgMdParams(ctypes.Structure):
@@ -111,6 +112,7 @@ SIGNATURES = {
     "lg_create": (ctypes.c_int, [ctypes.POINTER(LgOptions), ctypes.c_int32, ctypes.POINTER(_P)]),
     "lg_destroy": (None, [_P]),
     "lg_set_cell": (ctypes.c_int, [_P, ctypes.c_int32, _D]),
+    "lg_set_cell_ex": (ctypes.c_int, [_P, ctypes.c_int32, _D, ctypes.c_int32]),
     "lg_set_particles": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int64, _I32, _D, _D, _I32]),
     "lg_set_bonds": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int64, _I32, ctypes.POINTER(LgBonded)]),
     "lg_set_angles": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int64, _I32, ctypes.POINTER(LgBonded)]),
@@ -126,6 +128,7 @@ SIGNATURES = {
     "lg_list_cells": (ctypes.c_int, [_P, ctypes.c_int32, _I32, _I32]),
     "lg_md_set_barostat": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double]),
     "lg_get_cell": (ctypes.c_int, [_P, ctypes.c_int32, _D]),
+    "lg_cell_info": (ctypes.c_int, [_P, ctypes.c_int32, _I32, _D, _D]),
     "lg_md_set_state": (ctypes.c_int, [_P, ctypes.c_int32, _D, _D]),
     "lg_md_get_state": (ctypes.c_int, [_P, ctypes.c_int32, _D, _D]),
     "lg_md_set_state_all": (ctypes.c_int, [_P, _D, _D, _D]),

@@ -70,10 +70,9 @@ def footprint_bytes(system: System, precision: str, skin: float = 1.0) -> int:
     """Device bytes a system needs in an engine (per-atom state, neighbour list
     at the engine's capacity rule, Ewald tables), used for admission."""
     n = system.size
-    L = system.cell.lengths
     rc = max([p.cutoff for p in system.pairs.values()] + [system.coulomb.cutoff if system.coulomb else 0.0])
     rlist = rc + skin
-    density = n / (L[0] * L[1] * L[2])
+    density = n / system.cell.volume()
     maxnb = min(n, int(math.ceil(1.6 * density * 4.0 / 3.0 * math.pi * rlist ** 3 + 64)))
     maxnb = max(32, (maxnb + 31) // 32 * 32)
     per_atom = 4 * 32 + 3 * 24 + 14 * 8 + 16 + 6 * 4 + 4 * maxnb + (32 if precision == "mixed" else 0)

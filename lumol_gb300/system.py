@@ -283,29 +283,134 @@ class Wolf:
         return C.LgCoulomb(C.LG_COULOMB_WOLF, r, 0, 0, self.cutoff, 0.0, s14)
 
 
-@dataclass
+def _cross(x, y):
+    """Vector3D ^ (types/vectors.rs:219-228)."""
+    return (x[1] * y[2] - x[2] * y[1], x[2] * y[0] - x[0] * y[2], x[0] * y[1] - x[1] * y[0])
+
+
+def _dot(x, y):
+    """Vector3D * Vector3D (types/vectors.rs:212-217)."""
+    return x[0] * y[0] + x[1] * y[1] + x[2] * y[2]
+
+
+def _mat_vec(m, v):
+    """Matrix3 * Vector3D (types/matrix.rs:389-398), row by row."""
+    return tuple(m[a][0] * v[0] + m[a][1] * v[1] + m[a][2] * v[2] for a in range(3))
+
+
+def _mat_mul(x, y):
+    """Matrix3 * Matrix3 (types/matrix.rs:342-362)."""
+    return tuple(tuple(x[i][0] * y[0][j] + x[i][1] * y[1][j] + x[i][2] * y[2][j] for j in range(3))
+                 for i in range(3))
+
+
+def _inverse(m):
+    """Matrix3::inverse (types/matrix.rs:212-249)."""
+    det = (m[0][0] * (m[1][1] * m[2][2] - m[2][1] * m[1][2]) - m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0])
+           + m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]))
+    if not abs(det) > 1e-30:
+        raise ValueError("The matrix is not invertible!")
+    i = 1.0 / det
+    return ((((m[1][1] * m[2][2] - m[2][1] * m[1][2]) * i), ((m[0][2] * m[2][1] - m[0][1] * m[2][2]) * i),
+             ((m[0][1] * m[1][2] - m[0][2] * m[1][1]) * i)),
+            (((m[1][2] * m[2][0] - m[1][0] * m[2][2]) * i), ((m[0][0] * m[2][2] - m[0][2] * m[2][0]) * i),
+             ((m[1][0] * m[0][2] - m[0][0] * m[1][2]) * i)),
+            (((m[1][0] * m[2][1] - m[2][0] * m[1][1]) * i), ((m[2][0] * m[0][1] - m[0][0] * m[2][1]) * i),
+             ((m[0][0] * m[1][1] - m[1][0] * m[0][1]) * i)))
+
+
 class UnitCell:
-    """Orthorhombic UnitCell (lumol-core/src/sys/config/cells.rs:51-66)."""
-    lengths: tuple
+    """UnitCell (lumol-core/src/sys/config/cells.rs): an orthorhombic or a
+    triclinic cell, held as its matrix (columns: the cell vectors) and shape.
+    `lengths` are the distances between opposite faces (UnitCell::lengths,
+    cells.rs:134-146: a, b, c for an orthorhombic cell), which the cutoff
+    checks read."""
+
+    ORTHORHOMBIC, TRICLINIC = "orthorhombic", "triclinic"
+
+    def __init__(self, matrix, shape: str = "orthorhombic"):
+        m = tuple(tuple(float(x) for x in row) for row in np.asarray(matrix, dtype=np.float64).reshape(3, 3))
+        if shape not in (self.ORTHORHOMBIC, self.TRICLINIC):
+            raise ValueError(f"unknown cell shape {shape!r}")
+        self._m = m
+        self.shape = shape
+        self._inv = _inverse(m)
+        va, vb, vc = ((m[0][k], m[1][k], m[2][k]) for k in range(3))
+
+        def face(x, y, v):  # (x ^ y).normalized(), then |n * v|
+            n = _cross(x, y)
+            norm = float(np.sqrt(_dot(n, n)))
+            n = (n[0] / norm, n[1] / norm, n[2] / norm)
+            return abs(_dot(n, v))
+        self.lengths = (face(vb, vc, va), face(vc, va, vb), face(va, vb, vc))
 
     @classmethod
     def cubic(cls, length: float) -> "UnitCell":
         if not length > 0.0:
             raise ValueError("Cell lengths must be positive")
-        return cls((float(length),) * 3)
+        return cls(np.diag([float(length)] * 3))
 
     @classmethod
     def ortho(cls, a: float, b: float, c: float) -> "UnitCell":
         if not (a > 0.0 and b > 0.0 and c > 0.0):
             raise ValueError("Cell lengths must be positive")
-        return cls((float(a), float(b), float(c)))
+        return cls(np.diag([float(a), float(b), float(c)]))
 
-    def volume(self) -> float:
-        a, b, c = self.lengths
-        return a * b * c
+    @classmethod
+    def triclinic(cls, a: float, b: float, c: float, alpha: float, beta: float, gamma: float) -> "UnitCell":
+        """UnitCell::triclinic (cells.rs:72-94): angles in degrees."""
+        if not (a > 0.0 and b > 0.0 and c > 0.0):
+            raise ValueError("Cell lengths must be positive")
+        a, b, c = float(a), float(b), float(c)
+        rad = np.pi / 180.0  # f64::to_radians
+        cos_alpha = float(np.cos(float(alpha) * rad))
+        cos_beta = float(np.cos(float(beta) * rad))
+        g = float(gamma) * rad
+        sin_gamma, cos_gamma = float(np.sin(g)), float(np.cos(g))
+        b_x = b * cos_gamma
+        b_y = b * sin_gamma
+        c_x = c * cos_beta
+        c_y = c * (cos_alpha - cos_beta * cos_gamma) / sin_gamma
+        c_z = float(np.sqrt(c * c - c_y * c_y - c_x * c_x))
+        return cls([[a, b_x, c_x], [0.0, b_y, c_y], [0.0, 0.0, c_z]], cls.TRICLINIC)
 
     def matrix(self) -> np.ndarray:
-        return np.diag(np.array(self.lengths, dtype=np.float64))
+        return np.array(self._m, dtype=np.float64)
+
+    def inverse(self) -> np.ndarray:
+        return np.array(self._inv, dtype=np.float64)
+
+    def volume(self) -> float:
+        """cells.rs:185-200."""
+        m = self._m
+        if self.shape == self.ORTHORHOMBIC:
+            return m[0][0] * m[1][1] * m[2][2]
+        va, vb, vc = ((m[0][k], m[1][k], m[2][k]) for k in range(3))
+        return _dot(va, _cross(vb, vc))
+
+    def fractional(self, v):
+        return _mat_vec(self._inv, v)
+
+    def cartesian(self, f):
+        return _mat_vec(self._m, f)
+
+    def scaled(self, factor: float) -> "UnitCell":
+        """UnitCell::scale_mut(Matrix3::one() * factor) (cells.rs:201-207): the shape is kept."""
+        f = float(factor)
+        one = ((f * 1.0, f * 0.0, f * 0.0), (f * 0.0, f * 1.0, f * 0.0), (f * 0.0, f * 0.0, f * 1.0))
+        return UnitCell(_mat_mul(self._m, one), self.shape)
+
+    def wrap_vector(self, v):
+        """cells.rs:263-282."""
+        if self.shape == self.ORTHORHOMBIC:
+            d = (self._m[0][0], self._m[1][1], self._m[2][2])
+            return tuple(float(v[k]) - float(np.floor(float(v[k]) / d[k])) * d[k] for k in range(3))
+        f = self.fractional(v)
+        return self.cartesian(tuple(x - float(np.floor(x)) for x in f))
+
+    def _lower(self):
+        return np.ascontiguousarray(self.matrix().ravel()), (
+            C.LG_CELL_ORTHORHOMBIC if self.shape == self.ORTHORHOMBIC else C.LG_CELL_TRICLINIC)
 
 
 # ---------------------------------------------------------------------------
@@ -609,7 +714,8 @@ class System:
 
     def _lower_into(self, eng: Engine, s: int) -> None:
         n = self.size
-        eng.call("lg_set_cell", s, C.dptr(np.ascontiguousarray(self.cell.matrix().ravel())))
+        m, shape = self.cell._lower()
+        eng.call("lg_set_cell_ex", s, C.dptr(m), shape)
         kinds = self.kinds
         charges = self.charges
         masses = self.masses
@@ -779,10 +885,7 @@ class System:
             total += m[a]
             com = com + m[a] * positions[a]
         com = com / total
-        wrapped = com.copy()
-        for d in range(3):
-            L = self.cell.lengths[d]
-            wrapped[d] -= np.floor(wrapped[d] / L) * L
+        wrapped = np.array(self.cell.wrap_vector(com))
         return positions + (wrapped - com)
 
     def kinetic_energy(self) -> float:
@@ -971,7 +1074,7 @@ class MolecularDynamics:
         if isinstance(self.integrator, BerendsenBarostat):  # the cell the barostat left
             m = np.zeros(9)
             eng.call("lg_get_cell", 0, C.dptr(m))
-            system.cell = UnitCell.ortho(m[0], m[4], m[8])
+            system.cell = UnitCell(m.reshape(3, 3), system.cell.shape)
             system._uploaded = system._version  # the engine already holds this cell
 
 
@@ -1070,12 +1173,11 @@ class MonteCarlo:
     def _resize(self, system: System, move: Resize) -> None:
         """Resize::prepare / cost / apply / restore (resize.rs:63-124)."""
         eng = system.engine()
-        L = np.array(system.cell.lengths, dtype=np.float64)
-        volume = float(L[0] * L[1] * L[2])
+        old = system.cell
+        volume = old.volume()
         delta = self.rng.uniform(-move.delta, move.delta)
-        scaling = np.cbrt((volume + delta) / volume)
-        L_new = L * scaling  # UnitCell::scale_mut(Matrix3::one() * scaling)
-        inv = _ortho_inverse(L)
+        scaling = float(np.cbrt((volume + delta) / volume))
+        new = old.scaled(scaling)  # UnitCell::scale_mut(Matrix3::one() * scaling)
         pos = system.positions
         newpos = pos.copy()
         m = system.masses
@@ -1086,14 +1188,14 @@ class MonteCarlo:
                 total += m[a]
                 com = com + m[a] * pos[a]
             com = com / total
-            frac = inv * com            # previous.cell.fractional(com)
-            delta_com = L_new * frac - com  # cell.cartesian(frac) - com
+            frac = old.fractional(com)  # previous.cell.fractional(com)
+            delta_com = np.array(new.cartesian(frac)) - com  # cell.cartesian(frac) - com
             newpos[lo:hi] = pos[lo:hi] + delta_com
-        cell = np.diag(L_new).ravel().copy()
+        cell = np.ascontiguousarray(new.matrix().ravel())
         de = ctypes.c_double(0.0)
         eng.call("lg_mc_move_all_molecules_cost", 0, C.dptr(cell), C.dptr(np.ascontiguousarray(newpos)),
                  ctypes.byref(de))
-        new_volume = float(L_new[0] * L_new[1] * L_new[2])
+        new_volume = new.volume()
         nmol = int(system.molecules[-1]) + 1
         cost = self.beta * (de.value + move.pressure * (new_volume - volume)) - nmol * np.log(new_volume / volume)
         self.attempted += 1
@@ -1101,7 +1203,7 @@ class MonteCarlo:
             energy = ctypes.c_double(0.0)
             eng.call("lg_mc_update", 0, None, ctypes.byref(energy))
             self.energy = energy.value
-            system.cell = UnitCell.ortho(*L_new)
+            system.cell = new
             system.positions = newpos
             system._uploaded = system._version  # the engine holds the new cell and positions
             self.accepted += 1

@@ -66,7 +66,10 @@ class OrcDesc(ctypes.Structure):
                 ("n_bonds", ctypes.c_int64), ("bonds", ctypes.c_void_p), ("n_kinds", ctypes.c_int32),
                 ("pairs", ctypes.POINTER(OrcPair)), ("bond_pots", ctypes.POINTER(OrcBonded)),
                 ("angle_pots", ctypes.POINTER(OrcBonded)), ("coulomb", OrcCoulomb),
-                ("cell", ctypes.c_double * 3), ("dihedral_pots", ctypes.POINTER(OrcBonded))]
+                ("cell", ctypes.c_double * 3), ("dihedral_pots", ctypes.POINTER(OrcBonded)),
+                ("cell_shape", ctypes.c_int32), ("cell_pad", ctypes.c_int32), ("cell_matrix", ctypes.c_double * 9)]
+
+CELL_ORTHORHOMBIC, CELL_TRICLINIC = 0, 1
 
 
 _lib = None
@@ -107,6 +110,10 @@ def load() -> ctypes.CDLL:
         lib.orc_kinetic_energy.argtypes = [P, V]
         lib.orc_set_cell.argtypes = [P, ctypes.c_double, ctypes.c_double, ctypes.c_double]
         lib.orc_get_cell.argtypes = [P, V]
+        lib.orc_set_cell_matrix.argtypes = [P, V, ctypes.c_int32]
+        lib.orc_get_cell_matrix.argtypes = [P, V]
+        lib.orc_cell_info.argtypes = [P, V, V]
+        lib.orc_cell_apply.argtypes = [P, V, ctypes.c_int32]
         lib.orc_maximum_cutoff.restype = ctypes.c_double
         lib.orc_maximum_cutoff.argtypes = [P]
         lib.orc_berendsen_barostat_run.restype = ctypes.c_int
@@ -213,6 +220,10 @@ class Oracle:
         desc.dihedral_pots = dpots
         desc.coulomb = coul
         desc.cell = (ctypes.c_double * 3)(*spec.cell.lengths)
+        tric = getattr(spec.cell, "shape", "orthorhombic") == "triclinic"
+        desc.cell_shape = CELL_TRICLINIC if tric else CELL_ORTHORHOMBIC
+        if tric:
+            desc.cell_matrix = (ctypes.c_double * 9)(*[float(x) for x in spec.cell.matrix().ravel()])
         self.h = lib.orc_create(ctypes.byref(desc))
         self.masses = masses
 
@@ -301,10 +312,33 @@ class Oracle:
     def set_cell(self, lengths) -> None:
         self.lib.orc_set_cell(self.h, *[float(x) for x in lengths])
 
+    def set_cell_matrix(self, matrix, triclinic: bool) -> None:
+        m = np.ascontiguousarray(np.asarray(matrix, dtype=np.float64).reshape(9))
+        self.lib.orc_set_cell_matrix(self.h, _ptr(m), CELL_TRICLINIC if triclinic else CELL_ORTHORHOMBIC)
+
     def cell(self) -> np.ndarray:
+        """The orthorhombic lengths (the diagonal of the cell matrix)."""
         out = np.zeros(3)
         self.lib.orc_get_cell(self.h, _ptr(out))
         return out
+
+    def cell_matrix(self) -> np.ndarray:
+        out = np.zeros(9)
+        self.lib.orc_get_cell_matrix(self.h, _ptr(out))
+        return out.reshape(3, 3)
+
+    def cell_apply(self, v, mode: str) -> np.ndarray:
+        """UnitCell::vector_image ("image"), wrap_vector ("wrap") or
+        cartesian(fractional(v)) ("roundtrip") of one vector."""
+        x = np.ascontiguousarray(np.asarray(v, dtype=np.float64).copy())
+        self.lib.orc_cell_apply(self.h, _ptr(x), {"image": 0, "wrap": 1, "roundtrip": 2}[mode])
+        return x
+
+    def cell_info(self):
+        """(UnitCell::lengths, UnitCell::volume) of the oracle's cell."""
+        lengths, volume = np.zeros(3), np.zeros(1)
+        self.lib.orc_cell_info(self.h, _ptr(lengths), _ptr(volume))
+        return lengths, float(volume[0])
 
     def berendsen_barostat(self, pos, vel, acc, eta, dt, pressure, tau, nsteps, temperature=0.0,
                            tau_thermostat=0.0):
@@ -335,8 +369,12 @@ class Oracle:
     def cache_update(self) -> None:
         self.lib.orc_cache_update(self.h)
 
-    def move_all_molecules_cost(self, cell_lengths, newpos) -> float:
-        cell = np.ascontiguousarray(cell_lengths, dtype=np.float64)
+    def move_all_molecules_cost(self, cell, newpos) -> float:
+        """`cell`: the new cell's 3 x 3 matrix, or its three orthorhombic lengths."""
+        cell = np.asarray(cell, dtype=np.float64)
+        if cell.size == 3:
+            cell = np.diag(cell)
+        cell = np.ascontiguousarray(cell.reshape(9))
         newpos = np.ascontiguousarray(newpos, dtype=np.float64)
         return self.lib.orc_move_all_molecules_cost(self.h, _ptr(cell), _ptr(newpos))
 

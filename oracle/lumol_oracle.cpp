@@ -89,17 +89,33 @@ inline Complex cconj(const Complex& a) { return Complex{a.re, -a.im}; }
 inline double cnorm2(const Complex& a) { return a.re * a.re + a.im * a.im; }
 
 // ---------------------------------------------------------------------------
-// UnitCell, orthorhombic (lumol-core/src/sys/config/cells.rs)
+// UnitCell (lumol-core/src/sys/config/cells.rs), orthorhombic or triclinic
 // ---------------------------------------------------------------------------
+// Matrix3 * Vector3D (types/matrix.rs:389-398)
+inline V3 mat_vec(const M3& m, const V3& v) {
+    return V3{{m.m[0][0] * v[0] + m.m[0][1] * v[1] + m.m[0][2] * v[2],
+               m.m[1][0] * v[0] + m.m[1][1] * v[1] + m.m[1][2] * v[2],
+               m.m[2][0] * v[0] + m.m[2][1] * v[1] + m.m[2][2] * v[2]}};
+}
+
 struct Cell {
-    double a, b, c;
-    M3 inv;  // Matrix3::inverse of diag(a, b, c), types/matrix.rs:212-227
+    int shape = ORC_CELL_ORTHORHOMBIC;
+    double a, b, c;  // the orthorhombic branches' lengths: the diagonal (cells.rs:108-132)
+    M3 cell;         // UnitCell::matrix
+    M3 inv;          // Matrix3::inverse, types/matrix.rs:212-227
 
     void init(double la, double lb, double lc) {
-        a = la;
-        b = lb;
-        c = lc;
-        double m[3][3] = {{a, 0.0, 0.0}, {0.0, b, 0.0}, {0.0, 0.0, c}};
+        double m[9] = {la, 0.0, 0.0, 0.0, lb, 0.0, 0.0, 0.0, lc};
+        init_matrix(m, ORC_CELL_ORTHORHOMBIC);
+    }
+    void init_matrix(const double* mm, int sh) {
+        shape = sh;
+        double m[3][3];
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) m[i][j] = cell.m[i][j] = mm[3 * i + j];
+        a = m[0][0];
+        b = m[1][1];
+        c = m[2][2];
         double det = m[0][0] * (m[1][1] * m[2][2] - m[2][1] * m[1][2]) -
                      m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) +
                      m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
@@ -114,16 +130,43 @@ struct Cell {
         inv.m[2][1] = (m[2][0] * m[0][1] - m[0][0] * m[2][1]) * id;
         inv.m[2][2] = (m[0][0] * m[1][1] - m[1][0] * m[0][1]) * id;
     }
+    V3 vect(int k) const { return V3{{cell.m[0][k], cell.m[1][k], cell.m[2][k]}}; }
     // cells.rs:185-200
-    double volume() const { return a * b * c; }
-    // cells.rs:284-301, orthorhombic branch
+    double volume() const {
+        if (shape == ORC_CELL_ORTHORHOMBIC) return a * b * c;
+        return vdot(vect(0), vcross(vect(1), vect(2)));
+    }
+    // cells.rs:134-146: distances between opposite faces
+    V3 lengths() const {
+        V3 va = vect(0), vb = vect(1), vc = vect(2);
+        auto face = [](const V3& x, const V3& y, const V3& v) {
+            V3 n = vcross(x, y);
+            double norm = std::sqrt(vdot(n, n));
+            n = V3{{n[0] / norm, n[1] / norm, n[2] / norm}};
+            return std::fabs(vdot(n, v));
+        };
+        return V3{{face(vb, vc, va), face(vc, va, vb), face(va, vb, vc)}};
+    }
+    // cells.rs:284-301
     void vector_image(V3& v) const {
+        if (shape == ORC_CELL_TRICLINIC) {
+            V3 f = mat_vec(inv, v);
+            for (int k = 0; k < 3; k++) f[k] -= std::round(f[k]);
+            v = mat_vec(cell, f);
+            return;
+        }
         v[0] -= std::round(v[0] / a) * a;
         v[1] -= std::round(v[1] / b) * b;
         v[2] -= std::round(v[2] / c) * c;
     }
     // cells.rs:263-282
     void wrap_vector(V3& v) const {
+        if (shape == ORC_CELL_TRICLINIC) {
+            V3 f = mat_vec(inv, v);
+            for (int k = 0; k < 3; k++) f[k] -= std::floor(f[k]);
+            v = mat_vec(cell, f);
+            return;
+        }
         v[0] -= std::floor(v[0] / a) * a;
         v[1] -= std::floor(v[1] / b) * b;
         v[2] -= std::floor(v[2] / c) * c;
@@ -517,7 +560,7 @@ struct orc_system {
     bool pending_all = false;
     std::vector<double> pending_all_pairs;  // [i * n + j], between molecules
     double pending_all_tail = 0, pending_all_coulomb = 0;
-    double saved_cell[3] = {0, 0, 0};
+    Cell saved_cell;
     std::vector<V3> saved_pos;
 
     const PairPot* pair(int64_t i, int64_t j) const {
@@ -1239,7 +1282,8 @@ orc_system* orc_create(const orc_desc* d) {
     std::sort(s->bonds.begin(), s->bonds.end());
     s->bonds.erase(std::unique(s->bonds.begin(), s->bonds.end()), s->bonds.end());
     rebuild_bonding(s);
-    s->cell.init(d->cell[0], d->cell[1], d->cell[2]);
+    if (d->cell_shape == ORC_CELL_TRICLINIC) s->cell.init_matrix(d->cell_matrix, ORC_CELL_TRICLINIC);
+    else s->cell.init(d->cell[0], d->cell[1], d->cell[2]);
     s->coul = d->coulomb;
     s->kmax = d->coulomb.kmax;
     if (s->coul.kind == ORC_COULOMB_EWALD) {
@@ -1657,19 +1701,17 @@ void orc_md_run(orc_system* s, double* x, double* v, double* state, int integrat
             }
         }
         if (controls & 2u) {  // Rewrap: Molecule::wrap (sys/config/molecules.rs:256-296)
-            double L[3] = {s->cell.a, s->cell.b, s->cell.c};
             for (auto& mr : s->mol_range) {
                 double total = 0.0, com[3] = {0.0, 0.0, 0.0};
                 for (int64_t i = mr.first; i < mr.second; i++) {
                     total += s->mass[i];
                     for (int k = 0; k < 3; k++) com[k] += s->mass[i] * x[3 * i + k];
                 }
+                V3 c{{com[0] / total, com[1] / total, com[2] / total}};
+                V3 w = c;
+                s->cell.wrap_vector(w);  // UnitCell::wrap_vector (cells.rs:263-282)
                 double delta[3];
-                for (int k = 0; k < 3; k++) {
-                    double c = com[k] / total;
-                    double w = c - std::floor(c / L[k]) * L[k];  // UnitCell::wrap_vector (cells.rs:263-270)
-                    delta[k] = w - c;
-                }
+                for (int k = 0; k < 3; k++) delta[k] = w[k] - c[k];
                 for (int64_t i = mr.first; i < mr.second; i++)
                     for (int k = 0; k < 3; k++) x[3 * i + k] += delta[k];
             }
@@ -1732,6 +1774,41 @@ void orc_get_cell(const orc_system* s, double* out) {
     out[1] = s->cell.b;
     out[2] = s->cell.c;
 }
+// Any cell: its matrix (row-major) and shape
+void orc_set_cell_matrix(orc_system* s, const double* m, int32_t shape) {
+    s->cell.init_matrix(m, shape);
+    s->factors_ready = false;
+}
+void orc_get_cell_matrix(const orc_system* s, double* out) {
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) out[3 * i + j] = s->cell.cell.m[i][j];
+}
+// UnitCell::lengths and volume (cells.rs:134-146, 185-200)
+void orc_cell_info(const orc_system* s, double* lengths, double* volume) {
+    V3 l = s->cell.lengths();
+    for (int k = 0; k < 3; k++) lengths[k] = l[k];
+    *volume = s->cell.volume();
+}
+// UnitCell::vector_image (wrap == 0) or wrap_vector (wrap != 0) of v, and
+// the fractional / Cartesian round trip (wrap == 2), in place
+void orc_cell_apply(const orc_system* s, double* v, int32_t wrap) {
+    V3 x{{v[0], v[1], v[2]}};
+    if (wrap == 2) x = mat_vec(s->cell.cell, mat_vec(s->cell.inv, x));
+    else if (wrap) s->cell.wrap_vector(x);
+    else s->cell.vector_image(x);
+    for (int k = 0; k < 3; k++) v[k] = x[k];
+}
+
+// UnitCell::scale_mut(f * Matrix3::one()) (cells.rs:201-207): cell * (f 1)
+static void scale_cell(orc_system* s, double f) {
+    M3 one = mscale(f, M3{{{1.0, 0.0, 0.0}, {0.0, 1.0, 0.0}, {0.0, 0.0, 1.0}}});
+    double m[9];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++)
+            m[3 * i + j] = s->cell.cell.m[i][0] * one.m[0][j] + s->cell.cell.m[i][1] * one.m[1][j] +
+                           s->cell.cell.m[i][2] * one.m[2][j];
+    orc_set_cell_matrix(s, m, s->cell.shape);
+}
 
 // Interactions::maximum_cutoff (interactions.rs:173-190): pair and Coulomb cutoffs
 double orc_maximum_cutoff(const orc_system* s) {
@@ -1760,9 +1837,10 @@ int orc_berendsen_barostat_run(orc_system* s, double* x, double* v, double* a, d
             x[i] += v[i] * dt;
         }
         double e3 = *eta * *eta * *eta;
-        orc_set_cell(s, s->cell.a * e3, s->cell.b * e3, s->cell.c * e3);
+        scale_cell(s, e3);
         double rc = orc_maximum_cutoff(s);
-        if (0.5 * s->cell.a <= rc || 0.5 * s->cell.b <= rc || 0.5 * s->cell.c <= rc) return 1;
+        V3 len = s->cell.lengths();
+        if (0.5 * len[0] <= rc || 0.5 * len[1] <= rc || 0.5 * len[2] <= rc) return 1;
         // System::pressure (Pressure, compute.rs:399-431): (N_f k_B T + Tr W) / (3 V)
         orc_set_positions(s, x);
         double w[9];
@@ -1940,11 +2018,9 @@ double orc_move_molecule_cost(orc_system* s, int64_t molid, const double* newp) 
 // new configuration, orc_cache_restore puts the previous one back.
 double orc_move_all_molecules_cost(orc_system* s, const double* cell, const double* newp) {
     int64_t n = s->n;
-    s->saved_cell[0] = s->cell.a;
-    s->saved_cell[1] = s->cell.b;
-    s->saved_cell[2] = s->cell.c;
+    s->saved_cell = s->cell;
     s->saved_pos = s->pos;
-    orc_set_cell(s, cell[0], cell[1], cell[2]);
+    orc_set_cell_matrix(s, cell, s->cell.shape);  // (the shape is kept: cells.rs:201-207)
     orc_set_positions(s, newp);
     s->pending_all_pairs.assign((size_t)(n * n), 0.0);
     double pairs_delta = 0.0;
@@ -1974,7 +2050,8 @@ double orc_move_all_molecules_cost(orc_system* s, const double* cell, const doub
 // pending update is dropped.
 void orc_cache_restore(orc_system* s) {
     if (s->pending_all) {
-        orc_set_cell(s, s->saved_cell[0], s->saved_cell[1], s->saved_cell[2]);
+        s->cell = s->saved_cell;
+        s->factors_ready = false;
         s->pos = s->saved_pos;
     }
     s->pending_all = false;

@@ -49,6 +49,8 @@ enum {
 };
 
 enum { ORC_COULOMB_NONE = 0, ORC_COULOMB_EWALD = 1, ORC_COULOMB_WOLF = 2 };
+/* CellShape (cells.rs:12-20) */
+enum { ORC_CELL_ORTHORHOMBIC = 0, ORC_CELL_TRICLINIC = 1 };
 
 /* Energy / force / virial terms, combinable as a bit mask. */
 enum {
@@ -118,6 +120,9 @@ typedef struct {
     orc_coulomb coulomb;
     double cell[3];           /* orthorhombic cell lengths */
     const orc_bonded* dihedral_pots;  /* n_kinds^4, symmetric under reversal; may be NULL */
+    int32_t cell_shape;       /* ORC_CELL_*; a triclinic cell is given by cell_matrix */
+    int32_t cell_pad;
+    double cell_matrix[9];    /* row-major, columns the cell vectors (UnitCell::matrix) */
 } orc_desc;
 
 typedef struct orc_system orc_system;
@@ -189,6 +194,10 @@ void orc_pair_eval(const orc_pair* p, double r, double* energy, double* force,
  * current lengths (3 doubles). */
 void orc_set_cell(orc_system* s, double a, double b, double c);
 void orc_get_cell(const orc_system* s, double* lengths);
+void orc_set_cell_matrix(orc_system* s, const double* matrix, int32_t shape);
+void orc_get_cell_matrix(const orc_system* s, double* matrix);
+void orc_cell_info(const orc_system* s, double* lengths, double* volume);
+void orc_cell_apply(const orc_system* s, double* v, int32_t wrap);
 /* Interactions::maximum_cutoff (interactions.rs:173-190). */
 double orc_maximum_cutoff(const orc_system* s);
 /* BerendsenBarostat::integrate (lumol-sim/src/md/integrators.rs:213-250) and an
@@ -208,7 +217,7 @@ void orc_cache_update(orc_system* s);
  * configuration: new cell lengths (3) and positions (3n), installed in the
  * system; orc_cache_update keeps them, orc_cache_restore puts the previous
  * configuration back (Resize::restore, mc/moves/resize.rs:121-124). */
-double orc_move_all_molecules_cost(orc_system* s, const double* cell_lengths, const double* new_positions);
+double orc_move_all_molecules_cost(orc_system* s, const double* cell_matrix, const double* new_positions);
 void orc_cache_restore(orc_system* s);
 
 #ifdef __cplusplus
