@@ -148,7 +148,9 @@ __global__ void __launch_bounds__(256) pair_half_kernel(
             double4_32a pj = posq[j];
             double dx, dy, dz, r = 0.0, r2 = 0.0;
             PairDecision dec;
-            if (band || s.tric) {  // (a triclinic cell takes the exact geometry for every pair)
+            // (a triclinic cell takes the exact geometry for every pair)
+            const bool exact = band || s.tric;
+            if (exact) {
                 exact_nearest_image(s, pi.x, pi.y, pi.z, pj.x, pj.y, pj.z, dx, dy, dz);
                 r = exact_norm(dx, dy, dz);
                 dec = decide_pair(s, p, terms, i, j, mi, mol[j], pi.w, pj.w, r, spec_off, spec_j, spec_path);
@@ -161,14 +163,14 @@ __global__ void __launch_bounds__(256) pair_half_kernel(
                 else dec = PairDecision{pin, false, false, 1.0, 1.0};
             }
             double f_over_r = 0.0, e_p = 0.0, e_c = 0.0;
-            if (!band && dec.pair_in && p.type == 2 && !dec.coul_in) {
+            if (!exact && dec.pair_in && p.type == 2 && !dec.coul_in) {
                 // interior LJ: c12 / r^12 - c6 / r^6 from 1 / r^2
                 double inv_r2 = __drcp_rn(r2);
                 double ir6 = inv_r2 * inv_r2 * inv_r2;
                 f_over_r = dec.pair_scale * (ir6 * (12.0 * p.c12 * ir6 - 6.0 * p.c6) * inv_r2);
                 if (EV) e_p = dec.pair_scale * (ir6 * (p.c12 * ir6 - p.c6) - p.shift);
             } else if (dec.pair_in || dec.coul_in) {
-                if (!band) r = sqrt(r2);
+                if (!exact) r = sqrt(r2);
                 double inv_r = 1.0 / r;
                 if (dec.pair_in) {
                     double e, f;
@@ -491,7 +493,6 @@ __global__ void eikr_kernel(int n, int kdim, const double4_32a* __restrict__ pos
     const SysDev& s = sys[sysid[i]];
     if (s.coul != 1) return;
     double4_32a p = posq[i];
-    double x = axis == 0 ? p.x : (axis == 1 ? p.y : p.z);
     double phi = axis_phase(s, axis, p.x, p.y, p.z);
     double sn, cs;
     sincos(phi, &sn, &cs);

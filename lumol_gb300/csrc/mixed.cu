@@ -170,7 +170,6 @@ __global__ void eikr_mixed_kernel(int n, const double4_32a* __restrict__ posq, c
     const SysDev& s = sys[sysid[i]];
     if (s.coul != 1) return;
     double4_32a p = posq[i];
-    double x = axis == 0 ? p.x : (axis == 1 ? p.y : p.z);
     double phase = axis_phase(s, axis, p.x, p.y, p.z);
     phase -= 2.0 * PI * rint(phase * (0.5 / PI));
     float sn, cs;

@@ -612,10 +612,11 @@ int md_run_barostat(lg_engine* e, int64_t nsteps) {
                 for (int j = 0; j < 3; j++)
                     m[3 * i + j] = h.cell.m[3 * i] * f[j] + h.cell.m[3 * i + 1] * f[3 + j] + h.cell.m[3 * i + 2] * f[6 + j];
             HostCell cell;
-            if (!cell_init(cell, m, h.cell.shape)) return fail(e, LG_ERR_ARGUMENT, "the barostat made the cell singular");
+            // (a factor eta <= 0 inverts or collapses the cell: the reference panics as well)
+            bool valid = eta > 0.0 && cell_init(cell, m, h.cell.shape);
             const double* L = cell.len;
             double rc = max_cutoff(h);
-            if (0.5 * L[0] <= rc || 0.5 * L[1] <= rc || 0.5 * L[2] <= rc)
+            if (!valid || 0.5 * L[0] <= rc || 0.5 * L[1] <= rc || 0.5 * L[2] <= rc)
                 return fail(e, LG_ERR_ARGUMENT,
                             "Tried to decrease the cell size in Berendesen barostat but the new size is smaller "
                             "than the interactions cut off radius. You can try to increase the cell size or the "

@@ -143,6 +143,18 @@ def _ptr(a: np.ndarray) -> int:
     return a.ctypes.data
 
 
+def _state_array(a, n: int, copy: bool = False) -> np.ndarray:
+    """An (n, 3) float64 C-contiguous copy or view of a state array; anything
+    else (None, a wrong shape) is an error, since the library reads and writes
+    3 n doubles through the pointer."""
+    if a is None:
+        raise ValueError("state array is None")
+    arr = np.ascontiguousarray(a, dtype=np.float64)
+    if arr.size != 3 * n:
+        raise ValueError(f"state array has {arr.size} values, expected {3 * n}")
+    return arr.copy() if copy else arr
+
+
 class Oracle:
     """Oracle restatement of one Lumol System.
 
@@ -235,7 +247,7 @@ class Oracle:
             pass
 
     def set_positions(self, pos) -> None:
-        pos = np.ascontiguousarray(pos, dtype=np.float64)
+        pos = _state_array(pos, self.n)
         self.lib.orc_set_positions(self.h, _ptr(pos))
 
     def energy(self, terms: int = TERM_ALL) -> float:
@@ -276,9 +288,9 @@ class Oracle:
         return out[: 3 * n].reshape(-1, 3)
 
     def velocity_verlet(self, pos, vel, acc, dt, nsteps, temperature=0.0, tau=0.0):
-        pos = np.ascontiguousarray(pos, dtype=np.float64).copy()
-        vel = np.ascontiguousarray(vel, dtype=np.float64).copy()
-        acc = np.ascontiguousarray(acc, dtype=np.float64).copy()
+        pos = _state_array(pos, self.n, copy=True)
+        vel = _state_array(vel, self.n, copy=True)
+        acc = _state_array(acc, self.n, copy=True)
         self.lib.orc_velocity_verlet(self.h, _ptr(pos), _ptr(vel), _ptr(acc), dt, nsteps, temperature, tau)
         return pos, vel, acc
 
@@ -286,27 +298,27 @@ class Oracle:
                tolerance=0.0, seed=0, count=0, controls=0):
         """MolecularDynamics::propagate for `nsteps` steps (see orc_md_run);
         returns (positions, velocities, state, count)."""
-        pos = np.ascontiguousarray(pos, dtype=np.float64).copy()
-        vel = np.ascontiguousarray(vel, dtype=np.float64).copy()
-        state = np.ascontiguousarray(state, dtype=np.float64).copy()
+        pos = _state_array(pos, self.n, copy=True)
+        vel = _state_array(vel, self.n, copy=True)
+        state = _state_array(state, self.n, copy=True)
         c = ctypes.c_uint64(count)
         self.lib.orc_md_run(self.h, _ptr(pos), _ptr(vel), _ptr(state), integrator, dt, thermostat, temperature,
                             tau, tolerance, seed & (2 ** 64 - 1), ctypes.byref(c), controls, nsteps)
         return pos, vel, state, c.value
 
     def verlet_setup(self, pos, vel, dt) -> np.ndarray:
-        pos = np.ascontiguousarray(pos, dtype=np.float64)
-        vel = np.ascontiguousarray(vel, dtype=np.float64)
+        pos = _state_array(pos, self.n)
+        vel = _state_array(vel, self.n)
         prev = np.zeros_like(pos)
         self.lib.orc_verlet_setup(self.h, _ptr(pos), _ptr(vel), dt, _ptr(prev))
         return prev
 
     def kinetic_energy(self, vel) -> float:
-        vel = np.ascontiguousarray(vel, dtype=np.float64)
+        vel = _state_array(vel, self.n)
         return self.lib.orc_kinetic_energy(self.h, _ptr(vel))
 
     def temperature(self, vel) -> float:
-        vel = np.ascontiguousarray(vel, dtype=np.float64)
+        vel = _state_array(vel, self.n)
         return self.lib.orc_temperature(self.h, _ptr(vel))
 
     def set_cell(self, lengths) -> None:
@@ -345,9 +357,9 @@ class Oracle:
         """BerendsenBarostat::integrate (+ an optional Berendsen thermostat) for
         `nsteps` steps; returns (positions, velocities, accelerations, eta, cell
         lengths).  Raises where the reference panics."""
-        pos = np.ascontiguousarray(pos, dtype=np.float64).copy()
-        vel = np.ascontiguousarray(vel, dtype=np.float64).copy()
-        acc = np.ascontiguousarray(acc, dtype=np.float64).copy()
+        pos = _state_array(pos, self.n, copy=True)
+        vel = _state_array(vel, self.n, copy=True)
+        acc = _state_array(acc, self.n, copy=True)
         e = ctypes.c_double(eta)
         rc = self.lib.orc_berendsen_barostat_run(self.h, _ptr(pos), _ptr(vel), _ptr(acc), ctypes.byref(e), dt,
                                                  pressure, tau, temperature, tau_thermostat, nsteps)
@@ -375,7 +387,7 @@ class Oracle:
         if cell.size == 3:
             cell = np.diag(cell)
         cell = np.ascontiguousarray(cell.reshape(9))
-        newpos = np.ascontiguousarray(newpos, dtype=np.float64)
+        newpos = _state_array(newpos, self.n)
         return self.lib.orc_move_all_molecules_cost(self.h, _ptr(cell), _ptr(newpos))
 
     def cache_restore(self) -> None:

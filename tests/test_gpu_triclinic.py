@@ -19,7 +19,7 @@ import lumol_gb300 as lg
 import oracle
 import systems
 from lumol_gb300 import _capi as C
-from lumol_gb300 import workloads
+from lumol_gb300 import units, workloads
 from test_gpu_mixed import check as mixed_check
 from test_gpu_parity import _pairset_equal, assert_parity, jitter
 
@@ -157,7 +157,8 @@ def test_mixed_md_tracks_fp64_and_stays_off_the_persistent_kernel():
     b.engine.call("lg_md_plan", ctypes.byref(c), ctypes.byref(g))
     assert c.value <= 0  # the per-step kernels: the persistent kernel has no triclinic image
     x, _ = b.state(0)
-    xo, _, _ = oracle.Oracle(ref).velocity_verlet(ref.positions, ref.velocities, np.zeros((ref.size, 3)), 1.0, 20)
+    zeros = np.zeros((ref.size, 3))  # (the fluid starts at rest, as Batch.md_setup sets it up)
+    xo, _, _ = oracle.Oracle(ref).velocity_verlet(ref.positions, zeros, zeros, 1.0, 20)
     assert np.abs(x - xo).max() < 1e-6
     b.engine.close()
 
@@ -166,12 +167,13 @@ def test_berendsen_barostat_scales_the_triclinic_cell():
     s = to_triclinic(workloads.lj_replica(500, 0.6, 200.0, seed=4), stretch=(1.0, 1.0, 1.0))
     ref = to_triclinic(workloads.lj_replica(500, 0.6, 200.0, seed=4), stretch=(1.0, 1.0, 1.0))
     orc = oracle.Oracle(ref)
-    md = lg.MolecularDynamics(lg.BerendsenBarostat(1.0, 5000.0, 30.0))
+    pressure = units.from_(1e4, "bar")
+    md = lg.MolecularDynamics(lg.BerendsenBarostat(1.0, pressure, 30.0))
     md.setup(s)
     x, v, a, eta = ref.positions.copy(), ref.velocities.copy(), np.zeros((ref.size, 3)), 1.0
     for k in (1, 4, 10):
         md.run(s, k)
-        x, v, a, eta, _ = orc.berendsen_barostat(x, v, a, eta, 1.0, 5000.0, 30.0, k)
+        x, v, a, eta, _ = orc.berendsen_barostat(x, v, a, eta, 1.0, pressure, 30.0, k)
         m = orc.cell_matrix()
         assert np.abs(s.positions - x).max() < 1e-9
         assert np.abs(s.cell.matrix() - m).max() <= 1e-12 * np.abs(m).max()
