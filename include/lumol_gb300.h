@@ -191,10 +191,12 @@ void lg_destroy(lg_engine* engine);
 int lg_set_cell(lg_engine* e, int32_t s, const double matrix[9]);
 /* The same with the shape given: LG_CELL_TRICLINIC for any cell whose
  * volume is positive (a triclinic cell with a diagonal matrix still takes the
- * triclinic branches, as in the reference); LG_CELL_ORTHORHOMBIC requires a
- * diagonal matrix.  (UnitCell::scale_mut keeps the shape, cells.rs:201-207, so
- * AnisoBerendsenBarostat can leave an orthorhombic cell with off-diagonal
- * terms; the engine does not represent that state.) */
+ * triclinic branches, as in the reference); LG_CELL_ORTHORHOMBIC for a matrix
+ * with a positive diagonal.  An orthorhombic matrix may have off-diagonal
+ * terms (UnitCell::scale_mut keeps the shape, cells.rs:201-207, so
+ * AnisoBerendsenBarostat leaves them): as in the reference, the minimum
+ * image, wrap and volume read its diagonal, the face distances and the
+ * k-vectors the whole matrix. */
 int lg_set_cell_ex(lg_engine* e, int32_t s, const double matrix[9], int32_t shape);
 
 /* Particles of system `s` (Configuration, sys/config/configuration.rs:42-51):
@@ -242,7 +244,9 @@ int lg_compute(lg_engine* e, int32_t s, const double* positions, uint32_t terms,
  * minus sum_a F_k,a (x) (x_a - com) (ewald.rs:533-571, 736-752; wolf.rs:285-320);
  * bonds, angles and dihedral angles contribute nothing.  `terms` selects among
  * LG_TERM_PAIRS, LG_TERM_TAIL, LG_TERM_COUL_REAL and LG_TERM_COUL_KSPACE.
- * FP64 engines only. */
+ * The pair and real-space terms are FP64 on either precision (a mixed engine
+ * walks its cell-sorted list, each pair once); the k-space correction takes
+ * the engine's own k-space forces. */
 int lg_molecular_virial(lg_engine* e, int32_t s, const double* positions, uint32_t terms, double virial[9]);
 
 /* Same for every system of the engine, on device pointers: d_positions and
@@ -303,7 +307,8 @@ typedef struct lg_md_params {
 /* Barostats (lumol-sim/src/md/integrators.rs). */
 enum {
     LG_BAROSTAT_NONE = 0,
-    LG_BAROSTAT_BERENDSEN = 1  /* BerendsenBarostat (integrators.rs:174-250), isotropic */
+    LG_BAROSTAT_BERENDSEN = 1,        /* BerendsenBarostat (integrators.rs:174-250), isotropic */
+    LG_BAROSTAT_ANISO_BERENDSEN = 2   /* AnisoBerendsenBarostat (integrators.rs:252-342) */
 };
 /* BerendsenBarostat::new(timestep, pressure, tau): system `s`, set up with
  * LG_INTEGRATOR_VELOCITY_VERLET by lg_md_setup_ex (whose timestep it uses),
@@ -315,9 +320,19 @@ enum {
  * and completes the step with the forces.  The cell change is applied on the
  * device in place; lg_get_cell returns the current cell.  A cell length at or
  * below twice the maximum cutoff fails the run with the reference's panic
- * message.  LG_BAROSTAT_NONE turns it off.  (AnisoBerendsenBarostat turns an
- * orthorhombic cell triclinic, which the engine does not represent.) */
+ * message.  LG_BAROSTAT_NONE turns it off. */
 int lg_md_set_barostat(lg_engine* e, int32_t s, int32_t kind, double pressure, double tau);
+/* AnisoBerendsenBarostat::new(timestep, stress, tau) (integrators.rs:268-287;
+ * `hydrostatic(timestep, p, tau)` is stress = p * 1): every step scales the
+ * positions by the matrix eta (x = eta x) and the cell by it (cell * eta, the
+ * shape kept: an orthorhombic cell takes off-diagonal terms that its
+ * orthorhombic branches then ignore, as in the reference), evaluates the stress
+ * (sum_i m v (x) v + W) / V at the new positions with the half-step velocities,
+ * takes eta = 1 - dt 7372 / tau (stress - Stress) made symmetric for the next
+ * step, and completes the step with the forces.  `stress` is 9 doubles,
+ * row-major.  A face distance at or below twice the maximum cutoff fails the
+ * run with the reference's panic message. */
+int lg_md_set_aniso_barostat(lg_engine* e, int32_t s, const double stress[9], double tau);
 /* The cell matrix of system `s` (9 doubles, row-major). */
 int lg_get_cell(lg_engine* e, int32_t s, double matrix[9]);
 /* Its CellShape (LG_CELL_*), face distances (UnitCell::lengths, cells.rs:134-146)

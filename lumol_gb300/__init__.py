@@ -10,6 +10,7 @@ from . import units
 from ._capi import EngineError
 from .input import InputError, InteractionsInput, read_interactions
 from .system import (
+    AnisoBerendsenBarostat,
     BerendsenBarostat,
     BerendsenThermostat,
     BornMayerHuggins,

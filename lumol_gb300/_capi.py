@@ -91,7 +91,7 @@ class LgOptions(ctypes.Structure):
 LG_INTEGRATOR_VELOCITY_VERLET, LG_INTEGRATOR_VERLET, LG_INTEGRATOR_LEAP_FROG = 0, 1, 2
 LG_THERMOSTAT_NONE, LG_THERMOSTAT_BERENDSEN, LG_THERMOSTAT_RESCALE, LG_THERMOSTAT_CSVR = 0, 1, 2, 3
 LG_CONTROL_REMOVE_TRANSLATION, LG_CONTROL_REWRAP, LG_CONTROL_REMOVE_ROTATION = 1, 2, 4
-LG_BAROSTAT_NONE, LG_BAROSTAT_BERENDSEN = 0, 1
+LG_BAROSTAT_NONE, LG_BAROSTAT_BERENDSEN, LG_BAROSTAT_ANISO_BERENDSEN = 0, 1, 2
 LG_CELL_ORTHORHOMBIC, LG_CELL_TRICLINIC = 0, 1
 
 
@@ -128,6 +128,7 @@ SIGNATURES = {
     "lg_list_cells": (ctypes.c_int, [_P, ctypes.c_int32, _I32, _I32]),
     "lg_md_set_barostat": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double]),
     "lg_get_cell": (ctypes.c_int, [_P, ctypes.c_int32, _D]),
+    "lg_md_set_aniso_barostat": (ctypes.c_int, [_P, ctypes.c_int32, _D, ctypes.c_double]),
     "lg_cell_info": (ctypes.c_int, [_P, ctypes.c_int32, _I32, _D, _D]),
     "lg_md_set_state": (ctypes.c_int, [_P, ctypes.c_int32, _D, _D]),
     "lg_md_get_state": (ctypes.c_int, [_P, ctypes.c_int32, _D, _D]),

@@ -64,13 +64,8 @@ int lg_set_cell_ex(lg_engine* e, int32_t s, const double m[9], int32_t shape) {
     if (shape != LG_CELL_ORTHORHOMBIC && shape != LG_CELL_TRICLINIC) return fail(e, LG_ERR_ARGUMENT, "invalid cell shape");
     for (int k = 0; k < 9; k++)
         if (!std::isfinite(m[k])) return fail(e, LG_ERR_ARGUMENT, "non-finite cell matrix");
-    if (shape == LG_CELL_ORTHORHOMBIC) {
-        for (int a = 0; a < 3; a++)
-            for (int c = 0; c < 3; c++)
-                if (a != c && m[3 * a + c] != 0.0)
-                    return fail(e, LG_ERR_ARGUMENT, "an orthorhombic cell has a diagonal matrix");
-        if (!(m[0] > 0.0 && m[4] > 0.0 && m[8] > 0.0)) return fail(e, LG_ERR_ARGUMENT, "Cell lengths must be positive");
-    }
+    if (shape == LG_CELL_ORTHORHOMBIC && !(m[0] > 0.0 && m[4] > 0.0 && m[8] > 0.0))
+        return fail(e, LG_ERR_ARGUMENT, "Cell lengths must be positive");
     HostCell cell;
     if (!cell_init(cell, m, shape)) return fail(e, LG_ERR_ARGUMENT, "the cell matrix is not invertible or its volume is not positive");
     HostSystem& h = e->sys[s];
@@ -256,8 +251,6 @@ int lg_compute(lg_engine* e, int32_t s, const double* positions, uint32_t terms,
 
 int lg_molecular_virial(lg_engine* e, int32_t s, const double* positions, uint32_t terms, double virial[9]) {
     if (!valid_sys(e, s) || !positions || !virial) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
-    if (e->opt.precision != LG_PRECISION_FP64)
-        return fail(e, LG_ERR_ARGUMENT, "the molecular virial is computed by fp64 engines");
     CUDA_TRY(e, cudaSetDevice(e->opt.device));
     int rc = commit(e);
     if (rc) return rc;
@@ -441,6 +434,26 @@ int lg_md_set_barostat(lg_engine* e, int32_t s, int32_t kind, double pressure, d
         CUDA_TRY(e, cudaStreamSynchronize(e->stream));
         e->drop_graphs();
         e->pk_cluster = 0;
+    }
+    return LG_OK;
+}
+
+int lg_md_set_aniso_barostat(lg_engine* e, int32_t s, const double stress[9], double tau) {
+    if (!valid_sys(e, s) || !stress) return fail(e, LG_ERR_ARGUMENT, "invalid arguments");
+    int rc = lg_md_set_barostat(e, s, LG_BAROSTAT_BERENDSEN, 0.0, tau);  // the same checks
+    if (rc) return rc;
+    HostSystem& h = e->sys[s];
+    h.barostat = LG_BAROSTAT_ANISO_BERENDSEN;
+    for (int k = 0; k < 9; k++) {
+        h.baro_stress[k] = stress[k];
+        h.baro_m[k] = (k % 4 == 0) ? 1.0 : 0.0;  // AnisoBerendsenBarostat::new: eta = Matrix3::one()
+    }
+    if (!e->dirty) {
+        SysDev& d = e->h_sysdev[s];
+        fill_md(d, h);
+        CUDA_TRY(e, cudaMemcpyAsync(e->sysdev.p + s, &d, sizeof(SysDev), cudaMemcpyHostToDevice, e->stream));
+        CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+        e->drop_graphs();
     }
     return LG_OK;
 }

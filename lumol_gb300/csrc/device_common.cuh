@@ -109,13 +109,26 @@ struct SysDev {
     // geometry.  For an orthorhombic system H and Hi hold the diagonal cell
     // and its inverse, and L / invL / Lf / Lq stay the only fields read.
     int32_t tric;                 // 1: triclinic cell
-    int32_t tric_pad;
+    int32_t kgen;                 // 1: k-vectors off the axes (an orthorhombic cell with off-diagonal terms)
     double H[9];                  // UnitCell::matrix, row-major; columns are the cell vectors
     double Hi[9];                 // its Matrix3::inverse (matrix.rs:212-227)
     double kax[9];                // k_vector(e_a) = 2 PI Hi e_a (cells.rs:224-226), row a = axis a
     float Hf[9];                  // H in FP32 (mixed path and list builds)
     float tric_padf[3];
+    double baro_m[9];             // AnisoBerendsenBarostat: the matrix this step scales the positions by
 };
+
+// eta * x (Matrix3 * Vector3D, matrix.rs:389-398) of the anisotropic barostat, in place.
+__device__ __forceinline__ void baro_scale(const double* m, double& x, double& y, double& z) {
+    double v[3] = {x, y, z}, o[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+        o[a] = __dadd_rn(__dadd_rn(__dmul_rn(m[3 * a], v[0]), __dmul_rn(m[3 * a + 1], v[1])),
+                         __dmul_rn(m[3 * a + 2], v[2]));
+    x = o[0];
+    y = o[1];
+    z = o[2];
+}
 
 // Matrix3 * Vector3D (matrix.rs:389-398): each row a left-to-right sum of
 // unfused products.
@@ -148,7 +161,7 @@ __device__ __forceinline__ void tric_wrap(const SysDev& s, double d[3]) {
 // k_vector(e_axis) * r (cells.rs:224-226, ewald.rs:646-649): the phase of
 // e^{i k r} for index 1 along an axis (orthorhombic: the one coordinate).
 __device__ __forceinline__ double axis_phase(const SysDev& s, int axis, double x, double y, double z) {
-    if (!s.tric) return s.k1[axis] * (axis == 0 ? x : (axis == 1 ? y : z));
+    if (!s.tric && !s.kgen) return s.k1[axis] * (axis == 0 ? x : (axis == 1 ? y : z));
     const double* k = s.kax + 3 * axis;
     return __dadd_rn(__dadd_rn(__dmul_rn(k[0], x), __dmul_rn(k[1], y)), __dmul_rn(k[2], z));
 }

@@ -124,6 +124,8 @@ struct HostSystem {
     // BerendsenBarostat (lumol-sim/src/md/integrators.rs:174-250)
     int32_t barostat = LG_BAROSTAT_NONE;
     double baro_pressure = 0.0, baro_tau = 0.0, baro_eta = 1.0;
+    double baro_stress[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // AnisoBerendsenBarostat: target stress
+    double baro_m[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};       // and its eta (Matrix3::one() at setup)
     // derived
     std::vector<int64_t> mol_begin;  // first atom of each molecule (local index), plus the end
     double tail_energy = 0.0, tail_virial = 0.0, ewald_self = 0.0;
@@ -151,7 +153,7 @@ struct lg_engine {
     Batch b;
     // device storage
     DBuf<double4_32a> posq, vel, acc, pos_build;
-    DBuf<double> force, pos3, vel3, red, host_const, kepart, mom, out, fpart, kred, mc_part, kin;
+    DBuf<double> force, pos3, vel3, red, host_const, kepart, mom, out, fpart, kred, mc_part, kin, kten;
     DBuf<unsigned long long> md_count, cp_count;
     DBuf<double> adj;
     DBuf<int> mol_start;

@@ -759,7 +759,7 @@ __global__ void __launch_bounds__(128) molecular_virial_kernel(
     const int* __restrict__ nbr, const int* __restrict__ nnb, const int* __restrict__ nlo, int maxnb,
     const int* __restrict__ spec_off, const int* __restrict__ spec_j, const int8_t* __restrict__ spec_path,
     uint32_t terms, const double4_32a* __restrict__ com, const double* __restrict__ kforce,
-    double* __restrict__ red) {
+    const int* __restrict__ perm, const int* __restrict__ cell_atoms, double* __restrict__ red) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const SysDev& s = sys[sysid[i]];
@@ -767,9 +767,17 @@ __global__ void __launch_bounds__(128) molecular_virial_kernel(
     int ki = kind[i], mi = mol[i];
     const PairDev* prow = ptab + s.ptab + ki * s.nk;
     double w[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    const int* list = nbr + (size_t)i * maxnb;
-    for (int k = nlo[i]; k < nnb[i]; k++) {
+    // a mixed engine's cell-sorted full list: row perm[i], entries are sorted
+    // positions, each pair taken once from its lower atom; the plain path's
+    // half list: row i from its first j > i
+    const int row = perm ? perm[i] : i;
+    const int* list = nbr + (size_t)row * maxnb;
+    for (int k = perm ? 0 : nlo[i]; k < nnb[row]; k++) {
         int j = list[k];
+        if (perm) {
+            j = cell_atoms[j];
+            if (j <= i) continue;
+        }
         if (mol[j] == mi) continue;
         double4_32a pj = posq[j];
         double dx, dy, dz;
@@ -819,7 +827,7 @@ void launch_molecular_virial(const Batch& b, uint32_t terms, double4_32a* com, c
     molecule_com_kernel<<<(b.nmol + 127) / 128, 128, 0, st>>>(b.nmol, b.mol_start, b.posq, b.vel, com);
     molecular_virial_kernel<<<(b.n + 127) / 128, 128, 0, st>>>(
         b.n, b.posq, b.kind, b.mol, b.sysid, b.sys, b.ptab, b.nbr, b.nnb, b.nlo, b.maxnb, b.spec_off, b.spec_j,
-        b.spec_path, terms, com, kforce, b.red);
+        b.spec_path, terms, com, kforce, b.perm, b.perm ? b.cell_atoms : nullptr, b.red);
 }
 
 // ---------------------------------------------------------------------------

@@ -155,6 +155,7 @@ void launch_identity_order(const Batch& b, cudaStream_t st);
 void launch_request_rebuild_flag(const Batch& b, cudaStream_t st);
 // Kinetic energy of every system (nsys doubles) at the current velocities.
 void launch_kinetic(const Batch& b, double* out, cudaStream_t st);
+void launch_kinetic_tensor(const Batch& b, double* out, cudaStream_t st);
 void launch_carry_vectors(const double4_32a* src, double4_32a* dst, int n, bool keep_w, cudaStream_t st);
 void launch_check_displacement(const Batch& b, cudaStream_t st);
 

@@ -351,6 +351,7 @@ void fill_md(SysDev& d, const HostSystem& h) {
     d.total_mass = total;
     d.barostat = h.barostat;
     d.baro_eta = h.baro_eta;
+    for (int k = 0; k < 9; k++) d.baro_m[k] = h.baro_m[k];
 }
 
 double max_cutoff(const HostSystem& h) {
@@ -387,8 +388,17 @@ int check_cell_cutoffs(lg_engine* e, const HostSystem& h, const double len[3]) {
 // grid divides the fractional coordinates: its cells are at least half the
 // list radius apart across every pair of faces.
 void cell_geometry(SysDev& d, const HostSystem& h, const HostCell& cell, double skin) {
-    const double* L = cell.len;
-    d.tric = cell.shape == LG_CELL_TRICLINIC;
+    // the orthorhombic branches read the diagonal (cells.rs:108-132), even of a
+    // matrix that UnitCell::scale_mut gave off-diagonal terms; a triclinic
+    // cell's grid spans its face distances
+    const bool ortho = cell.shape == LG_CELL_ORTHORHOMBIC;
+    const double diag[3] = {cell.m[0], cell.m[4], cell.m[8]};
+    const double* L = ortho ? diag : cell.len;
+    d.tric = !ortho;
+    d.kgen = 0;
+    for (int a = 0; a < 3; a++)
+        for (int c = 0; c < 3; c++)
+            if (a != c && cell.inv[3 * a + c] != 0.0) d.kgen = 1;
     for (int k = 0; k < 9; k++) {
         d.H[k] = cell.m[k];
         d.Hi[k] = cell.inv[k];

@@ -294,7 +294,9 @@ __global__ void __launch_bounds__(VV_TILE) md_first_kernel(
             v.x = fma(hdt, a.x, v.x);
             v.y = fma(hdt, a.y, v.y);
             v.z = fma(hdt, a.z, v.z);
-            if (s.barostat) {  // BerendsenBarostat: x *= eta, then x += v dt (integrators.rs:219-225)
+            if (s.barostat == 2) {  // AnisoBerendsenBarostat: x = eta x (integrators.rs:302-306)
+                baro_scale(s.baro_m, p.x, p.y, p.z);
+            } else if (s.barostat) {  // BerendsenBarostat: x *= eta, then x += v dt (integrators.rs:219-225)
                 p.x *= s.baro_eta;
                 p.y *= s.baro_eta;
                 p.z *= s.baro_eta;
@@ -315,7 +317,9 @@ __global__ void __launch_bounds__(VV_TILE) md_first_kernel(
             v.x = __dadd_rn(v.x, __dmul_rn(hdt, a.x));
             v.y = __dadd_rn(v.y, __dmul_rn(hdt, a.y));
             v.z = __dadd_rn(v.z, __dmul_rn(hdt, a.z));
-            if (s.barostat) {  // BerendsenBarostat: x *= eta, then x += v dt (integrators.rs:219-225)
+            if (s.barostat == 2) {  // AnisoBerendsenBarostat: x = eta x (integrators.rs:302-306)
+                baro_scale(s.baro_m, p.x, p.y, p.z);
+            } else if (s.barostat) {  // BerendsenBarostat: x *= eta, then x += v dt (integrators.rs:219-225)
                 p.x = __dmul_rn(p.x, s.baro_eta);
                 p.y = __dmul_rn(p.y, s.baro_eta);
                 p.z = __dmul_rn(p.z, s.baro_eta);
@@ -628,6 +632,42 @@ __global__ void __launch_bounds__(256) kinetic_kernel(const SysDev* __restrict__
 }
 void launch_kinetic(const Batch& b, double* out, cudaStream_t st) {
     if (b.nsys) kinetic_kernel<<<b.nsys, 256, 0, st>>>(b.sys, b.vel, out);
+}
+
+// sum_i m_i v_i (x) v_i of each system (Stress, sys/compute.rs:466-480: the
+// kinetic part, mass * v.tensorial(v)), a fixed-order tree per system, 9 entries.
+__global__ void __launch_bounds__(256) kinetic_tensor_kernel(const SysDev* __restrict__ sys,
+                                                             const double4_32a* __restrict__ vel,
+                                                             double* __restrict__ out) {
+    __shared__ double sh[6][256];
+    const SysDev& s = sys[blockIdx.x];
+    double k[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = s.begin + threadIdx.x; i < s.end; i += blockDim.x) {
+        double4_32a v = vel[i];
+        const double c[3] = {v.x, v.y, v.z};
+        const int ia[6] = {0, 0, 0, 1, 1, 2}, ib[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+        for (int q = 0; q < 6; q++) k[q] += v.w * (c[ia[q]] * c[ib[q]]);
+    }
+    for (int q = 0; q < 6; q++) sh[q][threadIdx.x] = k[q];
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o)
+            for (int q = 0; q < 6; q++) sh[q][threadIdx.x] += sh[q][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double* o9 = out + 9 * blockIdx.x;
+        o9[0] = sh[0][0];
+        o9[1] = o9[3] = sh[1][0];
+        o9[2] = o9[6] = sh[2][0];
+        o9[4] = sh[3][0];
+        o9[5] = o9[7] = sh[4][0];
+        o9[8] = sh[5][0];
+    }
+}
+void launch_kinetic_tensor(const Batch& b, double* out, cudaStream_t st) {
+    if (b.nsys) kinetic_tensor_kernel<<<b.nsys, 256, 0, st>>>(b.sys, b.vel, out);
 }
 
 // A system's x, y, z (and w unless keep_w: the charge or mass of the new

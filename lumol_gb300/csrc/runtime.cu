@@ -595,7 +595,10 @@ int md_run_barostat(lg_engine* e, int64_t nsteps) {
     cudaStream_t st = e->stream;
     const int nsys = e->nsys;
     CUDA_TRY(e, e->kin.alloc(nsys));
-    std::vector<double> kin(nsys), out((size_t)nsys * RED_STRIDE);
+    CUDA_TRY(e, e->kten.alloc(9 * (size_t)nsys));
+    std::vector<double> kin(nsys), kten(9 * (size_t)nsys), out((size_t)nsys * RED_STRIDE);
+    bool aniso = false;
+    for (int s = 0; s < nsys; s++) aniso = aniso || e->sys[s].barostat == LG_BAROSTAT_ANISO_BERENDSEN;
     const size_t bytes = (size_t)e->b.n * sizeof(double4_32a);
     const size_t cbytes = (size_t)nsys * sizeof(unsigned long long);
     for (int64_t step = 0; step < nsteps; step++) {
@@ -603,25 +606,30 @@ int md_run_barostat(lg_engine* e, int64_t nsteps) {
         for (int s = 0; s < nsys; s++) {
             HostSystem& h = e->sys[s];
             if (h.barostat == LG_BAROSTAT_NONE) continue;
+            const bool an = h.barostat == LG_BAROSTAT_ANISO_BERENDSEN;
             double eta = h.baro_eta;
             double e3 = eta * eta * eta;
-            // cell * (e3 * 1) with Matrix3's product (matrix.rs:342-362)
-            const double f[9] = {e3, 0.0 * e3, 0.0 * e3, 0.0 * e3, e3, 0.0 * e3, 0.0 * e3, 0.0 * e3, e3};
+            // cell * (e3 * 1), or cell * eta of the anisotropic barostat
+            // (integrators.rs:309), with Matrix3's product (matrix.rs:342-388)
+            const double fi[9] = {e3, 0.0 * e3, 0.0 * e3, 0.0 * e3, e3, 0.0 * e3, 0.0 * e3, 0.0 * e3, e3};
+            const double* f = an ? h.baro_m : fi;
             double m[9];
             for (int i = 0; i < 3; i++)
                 for (int j = 0; j < 3; j++)
                     m[3 * i + j] = h.cell.m[3 * i] * f[j] + h.cell.m[3 * i + 1] * f[3 + j] + h.cell.m[3 * i + 2] * f[6 + j];
             HostCell cell;
             // (a factor eta <= 0 inverts or collapses the cell: the reference panics as well)
-            bool valid = eta > 0.0 && cell_init(cell, m, h.cell.shape);
+            bool valid = (an || eta > 0.0) && cell_init(cell, m, h.cell.shape);
             const double* L = cell.len;
             double rc = max_cutoff(h);
             if (!valid || 0.5 * L[0] <= rc || 0.5 * L[1] <= rc || 0.5 * L[2] <= rc)
                 return fail(e, LG_ERR_ARGUMENT,
-                            "Tried to decrease the cell size in Berendesen barostat but the new size is smaller "
-                            "than the interactions cut off radius. You can try to increase the cell size or the "
-                            "number of particles. (system " + std::to_string(s) + ")");
+                            std::string(an ? "Tried to decrease the cell size in anisotropic Berendesen barostat "
+                                           : "Tried to decrease the cell size in Berendesen barostat ") +
+                                "but the new size is smaller than the interactions cut off radius. You can try to "
+                                "increase the cell size or the number of particles. (system " + std::to_string(s) + ")");
             e->h_sysdev[s].baro_eta = eta;
+            for (int k = 0; k < 9; k++) e->h_sysdev[s].baro_m[k] = h.baro_m[k];
             int rc2 = set_cell_fast(e, s, cell);
             if (rc2 != LG_OK && rc2 != -1) return rc2;
             if (rc2 == -1) {  // another cell grid or k-vector set: lower the batch again, keeping the state
@@ -630,6 +638,7 @@ int md_run_barostat(lg_engine* e, int64_t nsteps) {
                 int rc3 = commit_carried(e);
                 if (rc3) return rc3;
                 CUDA_TRY(e, e->kin.alloc(nsys));
+                CUDA_TRY(e, e->kten.alloc(9 * (size_t)nsys));
             }
         }
         CUDA_TRY(e, cudaMemcpyAsync(e->cp_pos.p, e->posq.p, bytes, cudaMemcpyDeviceToDevice, st));
@@ -650,6 +659,10 @@ int md_run_barostat(lg_engine* e, int64_t nsteps) {
             enqueue_forces(e, LG_TERM_ALL, true, st, !(mode & MD_VERLET_SYS));
             launch_reduce(e->b, LG_TERM_ALL, e->b.nkvec != 0, e->out.p, st);
             launch_kinetic(e->b, e->kin.p, st);
+            if (aniso) {
+                launch_kinetic_tensor(e->b, e->kten.p, st);
+                e->launches += 1;
+            }
             launch_md_second(e->b, st);
             e->launches += (e->b.ntiles ? 2 : 0) + 2;
             if (mode & MD_ADJUST) {
@@ -658,6 +671,9 @@ int md_run_barostat(lg_engine* e, int64_t nsteps) {
             }
             CUDA_TRY(e, cudaGetLastError());
             CUDA_TRY(e, cudaMemcpyAsync(kin.data(), e->kin.p, nsys * sizeof(double), cudaMemcpyDeviceToHost, st));
+            if (aniso)
+                CUDA_TRY(e, cudaMemcpyAsync(kten.data(), e->kten.p, 9 * nsys * sizeof(double), cudaMemcpyDeviceToHost,
+                                            st));
             CUDA_TRY(e, cudaMemcpyAsync(out.data(), e->out.p, out.size() * sizeof(double), cudaMemcpyDeviceToHost,
                                         st));
             uint32_t status;
@@ -695,6 +711,24 @@ int md_run_barostat(lg_engine* e, int64_t nsteps) {
             HostSystem& h = e->sys[s];
             if (h.barostat == LG_BAROSTAT_NONE) continue;
             const double* w = &out[(size_t)s * RED_STRIDE + 1];
+            if (h.barostat == LG_BAROSTAT_ANISO_BERENDSEN) {
+                // Stress (compute.rs:466-480): (sum m v (x) v + W) / V; then
+                // eta = 1 - dt 7372 / tau (stress0 - stress), made symmetric
+                // (integrators.rs:322-331)
+                const double factor = h.dt * WATER_COMPRESSIBILITY / h.baro_tau;
+                double eta[9];
+                for (int k = 0; k < 9; k++) {
+                    double stress = (kten[9 * (size_t)s + k] + w[k]) / h.cell.volume;
+                    eta[k] = (k % 4 == 0 ? 1.0 : 0.0) - factor * (h.baro_stress[k] - stress);
+                }
+                for (int i = 0; i < 3; i++)
+                    for (int j = 0; j < i; j++) {
+                        eta[3 * i + j] = 0.5 * (eta[3 * i + j] + eta[3 * j + i]);
+                        eta[3 * j + i] = eta[3 * i + j];
+                    }
+                for (int k = 0; k < 9; k++) h.baro_m[k] = eta[k];
+                continue;
+            }
             double dof = (double)(3 * h.n);
             double T = 2.0 * kin[s] / (dof * K_BOLTZMANN);  // Temperature (compute.rs:164-172)
             double volume = h.cell.volume;

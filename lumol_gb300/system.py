@@ -932,6 +932,25 @@ class BerendsenBarostat:
     _kind = C.LG_INTEGRATOR_VELOCITY_VERLET
 
 
+class AnisoBerendsenBarostat:
+    """AnisoBerendsenBarostat::new(timestep, stress, tau) (md/integrators.rs:252-342):
+    Velocity-Verlet with the positions scaled by the matrix eta (x = eta x) and
+    the cell by it (cell * eta, shape kept) at every step, eta = 1 - dt 7372 /
+    tau (stress - Stress) made symmetric, from the stress tensor of the
+    previous step.  `hydrostatic(timestep, pressure, tau)` takes stress =
+    pressure * 1."""
+    _kind = C.LG_INTEGRATOR_VELOCITY_VERLET
+
+    def __init__(self, timestep: float, stress, tau: float):
+        self.timestep = float(timestep)
+        self.stress = np.asarray(stress, dtype=np.float64).reshape(3, 3).copy()
+        self.tau = float(tau)
+
+    @classmethod
+    def hydrostatic(cls, timestep: float, pressure: float, tau: float) -> "AnisoBerendsenBarostat":
+        return cls(timestep, float(pressure) * np.eye(3), tau)
+
+
 @dataclass
 class Verlet:
     """Verlet::new(timestep) (md/integrators.rs:72-123): keeps the positions at
@@ -1052,6 +1071,9 @@ class MolecularDynamics:
         if isinstance(self.integrator, BerendsenBarostat):
             eng.call("lg_md_set_barostat", 0, C.LG_BAROSTAT_BERENDSEN, float(self.integrator.pressure),
                      float(self.integrator.tau))
+        elif isinstance(self.integrator, AnisoBerendsenBarostat):
+            stress = np.ascontiguousarray(self.integrator.stress.ravel())
+            eng.call("lg_md_set_aniso_barostat", 0, C.dptr(stress), float(self.integrator.tau))
         if system.velocities is None:
             system.velocities = np.zeros((system.size, 3))
         pos = np.ascontiguousarray(system.positions)
@@ -1071,7 +1093,7 @@ class MolecularDynamics:
         system.positions = pos
         system.velocities = vel
         system.step += int(nsteps)
-        if isinstance(self.integrator, BerendsenBarostat):  # the cell the barostat left
+        if isinstance(self.integrator, (BerendsenBarostat, AnisoBerendsenBarostat)):  # the cell the barostat left
             m = np.zeros(9)
             eng.call("lg_get_cell", 0, C.dptr(m))
             system.cell = UnitCell(m.reshape(3, 3), system.cell.shape)

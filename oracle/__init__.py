@@ -114,6 +114,8 @@ def load() -> ctypes.CDLL:
         lib.orc_get_cell_matrix.argtypes = [P, V]
         lib.orc_cell_info.argtypes = [P, V, V]
         lib.orc_cell_apply.argtypes = [P, V, ctypes.c_int32]
+        lib.orc_aniso_barostat_run.restype = ctypes.c_int
+        lib.orc_aniso_barostat_run.argtypes = [P, V, V, V, V, ctypes.c_double, V, ctypes.c_double, ctypes.c_int64]
         lib.orc_maximum_cutoff.restype = ctypes.c_double
         lib.orc_maximum_cutoff.argtypes = [P]
         lib.orc_berendsen_barostat_run.restype = ctypes.c_int
@@ -367,6 +369,22 @@ class Oracle:
             raise RuntimeError("Tried to decrease the cell size in Berendesen barostat but the new size is "
                                "smaller than the interactions cut off radius.")
         return pos, vel, acc, e.value, self.cell()
+
+    def aniso_barostat(self, pos, vel, acc, eta, dt, stress, tau, nsteps):
+        """AnisoBerendsenBarostat::integrate for `nsteps` steps; returns
+        (positions, velocities, accelerations, eta (3 x 3), cell matrix).
+        Raises where the reference panics."""
+        pos = _state_array(pos, self.n, copy=True)
+        vel = _state_array(vel, self.n, copy=True)
+        acc = _state_array(acc, self.n, copy=True)
+        e = np.ascontiguousarray(np.asarray(eta, dtype=np.float64).reshape(9).copy())
+        st = np.ascontiguousarray(np.asarray(stress, dtype=np.float64).reshape(9))
+        rc = self.lib.orc_aniso_barostat_run(self.h, _ptr(pos), _ptr(vel), _ptr(acc), _ptr(e), dt, _ptr(st), tau,
+                                             nsteps)
+        if rc:
+            raise RuntimeError("Tried to decrease the cell size in anisotropic Berendesen barostat but the new "
+                               "size is smaller than the interactions cut off radius.")
+        return pos, vel, acc, e.reshape(3, 3), self.cell_matrix()
 
     def cache_init(self) -> None:
         self.lib.orc_cache_init(self.h)

@@ -1864,6 +1864,64 @@ int orc_berendsen_barostat_run(orc_system* s, double* x, double* v, double* a, d
     return 0;
 }
 
+// AnisoBerendsenBarostat::integrate (lumol-sim/src/md/integrators.rs:296-342)
+// `nsteps` times: v += dt/2 a; x = eta x; x += v dt; cell * eta; the panic
+// check on the face distances; eta = 1 - dt 7372 / tau (stress0 - Stress)
+// made symmetric, with Stress = (sum m v (x) v + W) / V (compute.rs:466-480);
+// then the forces.  `eta` (9, in / out) starts at the identity.  Returns 1
+// where the reference panics.
+int orc_aniso_barostat_run(orc_system* s, double* x, double* v, double* a, double* eta, double dt,
+                           const double* stress0, double tau, int64_t nsteps) {
+    const double WATER_COMPRESSIBILITY = 7372.0;  // integrators.rs:171
+    int64_t n = s->n;
+    std::vector<double> f(3 * n);
+    for (int64_t step = 0; step < nsteps; step++) {
+        for (int64_t i = 0; i < n; i++) {
+            for (int k = 0; k < 3; k++) v[3 * i + k] += 0.5 * dt * a[3 * i + k];
+            V3 p{{x[3 * i], x[3 * i + 1], x[3 * i + 2]}};
+            M3 m;
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++) m.m[r][c] = eta[3 * r + c];
+            p = mat_vec(m, p);
+            for (int k = 0; k < 3; k++) x[3 * i + k] = p[k] + v[3 * i + k] * dt;
+        }
+        // self.cell *= factor (matrix.rs:365-388)
+        double cm[9];
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++)
+                cm[3 * r + c] = s->cell.cell.m[r][0] * eta[c] + s->cell.cell.m[r][1] * eta[3 + c] +
+                                s->cell.cell.m[r][2] * eta[6 + c];
+        orc_set_cell_matrix(s, cm, s->cell.shape);
+        double rc = orc_maximum_cutoff(s);
+        V3 len = s->cell.lengths();
+        if (0.5 * len[0] <= rc || 0.5 * len[1] <= rc || 0.5 * len[2] <= rc) return 1;
+        orc_set_positions(s, x);
+        double w[9];
+        orc_virial(s, ORC_TERM_ALL, w);
+        double kin[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        for (int64_t i = 0; i < n; i++)  // kinetic += mass * velocity.tensorial(velocity)
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++) kin[3 * r + c] += s->mass[i] * (v[3 * i + r] * v[3 * i + c]);
+        double volume = s->cell.volume();
+        double factor = dt * WATER_COMPRESSIBILITY / tau;
+        for (int k = 0; k < 9; k++) {
+            double stress = (kin[k] + w[k]) / volume;
+            eta[k] = (k % 4 == 0 ? 1.0 : 0.0) - factor * (stress0[k] - stress);
+        }
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < r; c++) {
+                eta[3 * r + c] = 0.5 * (eta[3 * r + c] + eta[3 * c + r]);
+                eta[3 * c + r] = eta[3 * r + c];
+            }
+        std::fill(f.begin(), f.end(), 0.0);
+        orc_forces(s, ORC_TERM_ALL, f.data());
+        for (int64_t i = 0; i < n; i++)
+            for (int k = 0; k < 3; k++) a[3 * i + k] = f[3 * i + k] / s->mass[i];
+        for (int64_t i = 0; i < 3 * n; i++) v[i] += 0.5 * dt * a[i];
+    }
+    return 0;
+}
+
 // EnergyCache::init (cache.rs:75-98)
 void orc_cache_init(orc_system* s) {
     int64_t n = s->n;

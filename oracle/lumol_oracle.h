@@ -198,6 +198,8 @@ void orc_set_cell_matrix(orc_system* s, const double* matrix, int32_t shape);
 void orc_get_cell_matrix(const orc_system* s, double* matrix);
 void orc_cell_info(const orc_system* s, double* lengths, double* volume);
 void orc_cell_apply(const orc_system* s, double* v, int32_t wrap);
+int orc_aniso_barostat_run(orc_system* s, double* x, double* v, double* a, double* eta, double dt,
+                           const double* stress0, double tau, int64_t nsteps);
 /* Interactions::maximum_cutoff (interactions.rs:173-190). */
 double orc_maximum_cutoff(const orc_system* s);
 /* BerendsenBarostat::integrate (lumol-sim/src/md/integrators.rs:213-250) and an

@@ -1,4 +1,4 @@
-"""The Berendsen barostat (lumol-sim/src/md/integrators.rs:174-250) on the GPU
+"""The Berendsen barostats (lumol-sim/src/md/integrators.rs:174-342) on the GPU
 against the oracle's restatement.
 
 FP64: positions within 1e-9 A and cell lengths within 1e-12 relative of the
@@ -6,7 +6,10 @@ oracle after every run, for LJ argon (cells of the list grid change as the
 box shrinks: the batch is lowered again in place) and for NaCl with Ewald
 (the k-vector factors follow the cell at every step); the mixed path within
 1e-6 A.  A compression below twice the cutoff fails with the reference's
-panic message.
+panic message.  The anisotropic barostat likewise (positions 1e-9 A, the
+cell matrix 1e-12), from an orthorhombic cell (which keeps its shape and
+takes off-diagonal terms) and from a triclinic one with a full stress
+target.
 """
 import ctypes
 
@@ -86,3 +89,69 @@ def test_barostat_needs_velocity_verlet():
     eng.call("lg_md_setup_ex", 0, ctypes.byref(p))
     with pytest.raises(lg.EngineError):
         eng.call("lg_md_set_barostat", 0, C.LG_BAROSTAT_BERENDSEN, 0.0, 10.0)
+
+
+# ---- AnisoBerendsenBarostat (integrators.rs:252-342) ----------------------------------
+def _aniso_run(make, stress, tau, runs, precision="fp64"):
+    s = make(precision)
+    ref = make("fp64")
+    orc = oracle.Oracle(ref)
+    md = lg.MolecularDynamics(lg.AnisoBerendsenBarostat(1.0, stress, tau))
+    md.setup(s)
+    x, v, a, eta = ref.positions.copy(), ref.velocities.copy(), np.zeros((ref.size, 3)), np.eye(3)
+    out = []
+    for k in runs:
+        md.run(s, k)
+        x, v, a, eta, cell = orc.aniso_barostat(x, v, a, eta, 1.0, stress, tau, k)
+        out.append((s.positions.copy(), s.velocities.copy(), s.cell.matrix(), s.cell.shape, x, v, cell))
+    return out
+
+
+def _replica(precision):
+    return workloads.lj_replica(500, 0.6, 200.0, seed=4, precision=precision)
+
+
+def test_aniso_barostat_hydrostatic_follows_the_oracle():
+    """An orthorhombic cell takes off-diagonal terms (cell * eta with a
+    symmetric eta) and keeps its shape; the orthorhombic branches then read
+    its diagonal, the k-vectors and face distances the whole matrix."""
+    stress = units.from_(1e4, "bar") * np.eye(3)
+    for x, v, cell, shape, xo, vo, co in _aniso_run(_replica, stress, 100.0, [1, 3, 8]):
+        assert np.abs(x - xo).max() < 1e-9, np.abs(x - xo).max()
+        assert np.abs(v - vo).max() / np.abs(vo).max() < 1e-8
+        assert np.abs(cell - co).max() <= 1e-12 * np.abs(co).max()
+        assert shape == "orthorhombic"
+    off = np.abs(cell - np.diag(np.diag(cell))).max()
+    assert off > 0.0  # the cell is no longer diagonal
+
+
+def test_aniso_barostat_stress_target_on_a_triclinic_cell():
+    stress = units.from_(1.0, "bar") * np.array([[2e3, 3e2, 0.0], [3e2, 1e3, -2e2], [0.0, -2e2, 5e2]])
+
+    def make(precision):
+        s = _replica(precision)
+        L = np.array(s.cell.lengths)
+        cell = lg.UnitCell.triclinic(L[0], L[1], L[2], 85.0, 95.0, 100.0)
+        frac = s.positions / L
+        s.cell = cell
+        s.positions = frac @ cell.matrix().T
+        return s
+    for x, v, cell, shape, xo, vo, co in _aniso_run(make, stress, 100.0, [2, 6]):
+        assert np.abs(x - xo).max() < 1e-9, np.abs(x - xo).max()
+        assert np.abs(cell - co).max() <= 1e-12 * np.abs(co).max()
+        assert shape == "triclinic"
+
+
+def test_aniso_barostat_mixed_precision_tracks_fp64():
+    stress = units.from_(1e4, "bar") * np.eye(3)
+    for x, v, cell, shape, xo, vo, co in _aniso_run(_replica, stress, 100.0, [1, 3, 8], precision="mixed"):
+        assert np.abs(x - xo).max() < 1e-6, np.abs(x - xo).max()
+        assert np.abs(cell - co).max() <= 1e-7 * np.abs(co).max()
+
+
+def test_aniso_barostat_below_twice_the_cutoff_fails_like_the_reference():
+    s = workloads.argon_fcc()
+    md = lg.MolecularDynamics(lg.AnisoBerendsenBarostat.hydrostatic(1.0, units.from_(1e8, "bar"), 1.0))
+    md.setup(s)
+    with pytest.raises(lg.EngineError, match="Tried to decrease the cell size in anisotropic Berendesen barostat"):
+        md.run(s, 20)

@@ -239,6 +239,7 @@ def test_shape_and_chain_errors():
     s = nacl("ewald")
     eng = s.engine()
     m = s.cell.matrix().ravel().copy()
+    m[0] = -m[0]  # an orthorhombic matrix needs a positive diagonal
     with pytest.raises(lg.EngineError):
         eng.call("lg_set_cell_ex", 0, C.dptr(m), C.LG_CELL_ORTHORHOMBIC)
     with pytest.raises(lg.EngineError):

@@ -93,10 +93,25 @@ def test_molecular_virial_matches_oracle(name):
 
 
 @pytest.mark.gpu
-def test_molecular_virial_needs_fp64():
-    s = systems.random_lj_fluid(200, 0.02, 3, 9.0, family="lj", precision="mixed")
-    with pytest.raises(lg.EngineError, match="fp64"):
-        s.molecular_virial()
+@pytest.mark.parametrize("name", ["water_ewald", "argon", "nacl"])
+def test_molecular_virial_of_mixed_engines(name):
+    """A mixed engine evaluates the pair and real-space terms in FP64 on its
+    cell-sorted list (each pair once), so they match the oracle at 1e-10; the
+    k-space correction takes its FP32-accurate k-space forces (1e-5 of the
+    largest entry, the mixed path's virial tolerance)."""
+    mixed = {"water_ewald": lambda: workloads.water_box(n_side=4, length=18.0, seed=5, cutoff=6.5, alpha=0.45,
+                                                        kmax=6, precision="mixed"),
+             "argon": lambda: systems.random_lj_fluid(400, 0.02, 3, 9.0, family="lj", precision="mixed"),
+             "nacl": lambda: workloads.nacl_crystal(cells=3, a=5.64, jitter=0.1, seed=2, cutoff=8.0,
+                                                    precision="mixed")}[name]()
+    orc = oracle.Oracle(mixed)
+    for terms in TERMS + [lg.LG_TERM_ALL]:
+        gpu, ref = mixed.molecular_virial(terms), orc.molecular_virial(terms)
+        tol = 1e-5 if terms & KSPACE else 1e-10
+        if np.abs(ref).max() < 1e-14:
+            assert np.abs(gpu).max() < 1e-12, terms
+        else:
+            assert _rel(gpu, ref) <= tol, (terms, _rel(gpu, ref))
 
 
 def pairs_system():
