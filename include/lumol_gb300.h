@@ -457,6 +457,20 @@ int lg_mc_restore(lg_engine* e, int32_t s);
  * The random stream is the engine's own (SplitMix64 seeded by `seed`), not the
  * reference's xorshift stream. */
 int lg_mc_setup(lg_engine* e, int32_t s, double temperature, double delta, uint64_t seed);
+/* The chain of system `s` with MonteCarlo::add(Translate::new(delta), f_t) and
+ * MonteCarlo::add(Rotate::new(theta), f_r) (mc/moves/translate.rs,
+ * rotate.rs:34-124): molecules of any size move rigidly, a move picked by its
+ * cumulative frequency (monte_carlo.rs:190-208, 289-298), a molecule uniformly,
+ * then a displacement (as lg_mc_setup) or a rotation about the centre of mass
+ * (an axis uniform on the unit sphere, an angle uniform in [-theta, theta),
+ * Matrix3::rotation); the cost counts the pair potentials between the moved
+ * molecule and the other atoms.  A translated molecule is wrapped by its
+ * centre of mass, a rotated one is not (as the reference applies them).  Pair
+ * potentials only, orthorhombic cells; a frequency of 0 leaves that move out.
+ * lg_mc_run checks that the largest rotated displacement stays within half the
+ * skin. */
+int lg_mc_setup_ex(lg_engine* e, int32_t s, double temperature, double translate_delta, double translate_frequency,
+                   double rotate_theta, double rotate_frequency, uint64_t seed);
 /* Runs `moves` attempted moves in every chain. */
 int lg_mc_run(lg_engine* e, int64_t moves);
 /* Cached energy, accepted and attempted moves of chain `s`. */

@@ -148,6 +148,8 @@ SIGNATURES = {
     "lg_mc_move_all_molecules_cost": (ctypes.c_int, [_P, ctypes.c_int32, _D, _D, _D]),
     "lg_mc_restore": (ctypes.c_int, [_P, ctypes.c_int32]),
     "lg_mc_setup": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_uint64]),
+    "lg_mc_setup_ex": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                      ctypes.c_double, ctypes.c_double, ctypes.c_uint64]),
     "lg_mc_run": (ctypes.c_int, [_P, ctypes.c_int64]),
     "lg_mc_stats": (ctypes.c_int, [_P, ctypes.c_int32, _D, _I64, _I64]),
     "lg_get_stream": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),

@@ -61,6 +61,15 @@ class Batch:
         """MonteCarlo(temperature) with Translate(delta) moves for system `s`."""
         self.engine.call("lg_mc_setup", s, float(temperature), float(delta), int(seed) & (2 ** 64 - 1))
 
+    def mc_setup_moves(self, s: int, temperature: float, translate=(0.3, 1.0), rotate=None, seed: int = 0) -> None:
+        """MonteCarlo(temperature) with Translate(delta) at frequency f_t and
+        Rotate(theta) at f_r (`translate` / `rotate` = (amplitude, frequency) or
+        None) for system `s`: rigid moves of whole molecules."""
+        td, tf = translate if translate else (0.0, 0.0)
+        rt, rf = rotate if rotate else (0.0, 0.0)
+        self.engine.call("lg_mc_setup_ex", s, float(temperature), float(td), float(tf), float(rt), float(rf),
+                         int(seed) & (2 ** 64 - 1))
+
     def mc_run(self, moves: int) -> None:
         """`moves` attempted moves in every chain."""
         self.engine.call("lg_mc_run", int(moves))

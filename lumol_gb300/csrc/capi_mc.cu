@@ -215,7 +215,10 @@ int lg_mc_update(lg_engine* e, int32_t s, const double* molecule_positions, doub
     return LG_OK;
 }
 
-int lg_mc_setup(lg_engine* e, int32_t s, double temperature, double delta, uint64_t seed) {
+// MonteCarlo::new (mc/monte_carlo.rs) with Translate::new (translate.rs:41-52):
+// the chain of system s (molecules: whether molecules of several atoms are allowed)
+static int mc_setup_chain(lg_engine* e, int32_t s, double temperature, double delta, uint64_t seed,
+                          bool molecules) {
     if (!valid_sys(e, s)) return fail(e, LG_ERR_ARGUMENT, "invalid system index");
     // MonteCarlo::new (mc/monte_carlo.rs) and Translate::new (translate.rs:41-52)
     if (!(temperature > 0.0)) return fail(e, LG_ERR_ARGUMENT, "the temperature must be positive in Monte Carlo");
@@ -229,9 +232,12 @@ int lg_mc_setup(lg_engine* e, int32_t s, double temperature, double delta, uint6
         return fail(e, LG_ERR_ARGUMENT,
                     "batched Monte Carlo chains evaluate pair potentials only; use lg_mc_move_molecule_cost "
                     "for systems with Coulomb interactions");
-    for (size_t i = 1; i < h.mols.size(); i++)
-        if (h.mols[i] == h.mols[i - 1])
-            return fail(e, LG_ERR_ARGUMENT, "batched Monte Carlo chains move single-particle molecules only");
+    if (!molecules)
+        for (size_t i = 1; i < h.mols.size(); i++)
+            if (h.mols[i] == h.mols[i - 1])
+                return fail(e, LG_ERR_ARGUMENT,
+                            "batched Monte Carlo chains of lg_mc_setup move single-particle molecules; "
+                            "lg_mc_setup_ex moves whole molecules");
     double half = delta / std::sqrt(3.0);
     if (std::sqrt(3.0) * half > 0.5 * e->skin)
         return fail(e, LG_ERR_ARGUMENT, "the Translate amplitude must not exceed half the neighbour-list skin");
@@ -244,10 +250,52 @@ int lg_mc_setup(lg_engine* e, int32_t s, double temperature, double delta, uint6
     m.moves_left = 0;
     m.need_rebuild = 0;
     m.accepted = m.attempted = 0;
+    m.molecular = 0;  // (lg_mc_setup_ex sets the molecular moves afterwards)
+    m.theta = 0.0;
+    m.cum_translate = 1.0;
     if (!e->dirty) {
         CUDA_TRY(e, cudaSetDevice(e->opt.device));
         CUDA_TRY(e, cudaMemcpy(e->mc_chains.p + s, &m, sizeof(McState), cudaMemcpyHostToDevice));
     }
+    return LG_OK;
+}
+
+int lg_mc_setup(lg_engine* e, int32_t s, double temperature, double delta, uint64_t seed) {
+    return mc_setup_chain(e, s, temperature, delta, seed, false);
+}
+
+int lg_mc_setup_ex(lg_engine* e, int32_t s, double temperature, double translate_delta, double translate_frequency,
+                   double rotate_theta, double rotate_frequency, uint64_t seed) {
+    if (!valid_sys(e, s)) return fail(e, LG_ERR_ARGUMENT, "invalid system index");
+    if (!(temperature > 0.0)) return fail(e, LG_ERR_ARGUMENT, "the temperature must be positive in Monte Carlo");
+    if (!(translate_frequency >= 0.0) || !(rotate_frequency >= 0.0) || !(translate_frequency + rotate_frequency > 0.0))
+        return fail(e, LG_ERR_ARGUMENT, "move frequencies must be non-negative with a positive sum");
+    if (translate_frequency > 0.0 && !(translate_delta > 0.0))
+        return fail(e, LG_ERR_ARGUMENT, "delta must be positive in Translate move");
+    if (rotate_frequency > 0.0 && !(rotate_theta > 0.0))
+        return fail(e, LG_ERR_ARGUMENT, "theta must be positive in Rotate move");
+    const HostSystem& h = e->sys[s];
+    if (h.cell.shape != LG_CELL_ORTHORHOMBIC)
+        return fail(e, LG_ERR_ARGUMENT,
+                    "batched Monte Carlo chains take orthorhombic cells; use lg_mc_move_molecule_cost for a "
+                    "triclinic cell");
+    if (h.coul.kind != LG_COULOMB_NONE)
+        return fail(e, LG_ERR_ARGUMENT,
+                    "batched Monte Carlo chains evaluate pair potentials only; use lg_mc_move_molecule_cost "
+                    "for systems with Coulomb interactions");
+    double half = translate_frequency > 0.0 ? translate_delta / std::sqrt(3.0) : 0.0;
+    if (std::sqrt(3.0) * half > 0.5 * e->skin)
+        return fail(e, LG_ERR_ARGUMENT, "the Translate amplitude must not exceed half the neighbour-list skin");
+    int rc = mc_setup_chain(e, s, temperature, translate_frequency > 0.0 ? translate_delta : 1.0, seed, true);
+    if (rc) return rc;
+    McState& m = e->h_mc[s];
+    m.molecular = 1;
+    m.theta = rotate_theta;
+    // MonteCarlo::normalize_frequencies (monte_carlo.rs:190-208): the last cumulative frequency is 1
+    double sum = translate_frequency + rotate_frequency;
+    m.cum_translate = rotate_frequency > 0.0 ? translate_frequency / sum : 1.0;
+    m.delta = half;
+    if (!e->dirty) CUDA_TRY(e, cudaMemcpy(e->mc_chains.p + s, &m, sizeof(McState), cudaMemcpyHostToDevice));
     return LG_OK;
 }
 
@@ -279,6 +327,39 @@ int lg_mc_run(lg_engine* e, int64_t moves) {
             any = true;
         }
     if (!any) return fail(e, LG_ERR_STATE, "lg_mc_setup was not called for any system");
+    bool molecular = false;  // chains of lg_mc_setup_ex: the molecular chains' kernel runs too
+    for (int s = 0; s < nsys; s++) {
+        const McState& m = e->h_mc[s];
+        if (!m.enabled || !m.molecular) continue;
+        molecular = true;
+        if (m.cum_translate >= 1.0) continue;
+        // a rotated atom moves by at most 2 r sin(theta / 2), r its distance from
+        // the molecule's centre of mass: it must stay within skin / 2, else no
+        // rotation could ever be attempted between two list builds
+        const HostSystem& h = e->sys[s];
+        std::vector<double4_32a> x(h.n), v(h.n);
+        CUDA_TRY(e, cudaMemcpy(x.data(), e->posq.p + e->begin[s], h.n * sizeof(double4_32a), cudaMemcpyDeviceToHost));
+        CUDA_TRY(e, cudaMemcpy(v.data(), e->vel.p + e->begin[s], h.n * sizeof(double4_32a), cudaMemcpyDeviceToHost));
+        double rmax = 0.0;
+        for (size_t mi = 0; mi + 1 < h.mol_begin.size(); mi++) {
+            int64_t lo = h.mol_begin[mi], hi = h.mol_begin[mi + 1];
+            double total = 0.0, c[3] = {0, 0, 0};
+            for (int64_t a = lo; a < hi; a++) {
+                total += v[a].w;
+                c[0] += v[a].w * x[a].x;
+                c[1] += v[a].w * x[a].y;
+                c[2] += v[a].w * x[a].z;
+            }
+            for (int64_t a = lo; a < hi; a++) {
+                double dx = x[a].x - c[0] / total, dy = x[a].y - c[1] / total, dz = x[a].z - c[2] / total;
+                rmax = std::max(rmax, std::sqrt(dx * dx + dy * dy + dz * dz));
+            }
+        }
+        if (2.0 * rmax * std::sin(0.5 * std::min(m.theta, PI)) > 0.5 * e->skin)
+            return fail(e, LG_ERR_ARGUMENT,
+                        "the Rotate amplitude must not move an atom farther than half the neighbour-list skin "
+                        "(system " + std::to_string(s) + ")");
+    }
     e->shadow_valid = false;
     CUDA_TRY(e, cudaMemcpyAsync(e->mc_chains.p, e->h_mc.data(), nsys * sizeof(McState), cudaMemcpyHostToDevice, st));
     // the list must be current for the positions the chains start from, and so
@@ -291,7 +372,7 @@ int lg_mc_run(lg_engine* e, int64_t moves) {
         e->launches += 1;
     }
     for (int64_t launch = 0; launch < moves + 64; launch++) {
-        launch_mc_chains(e->b, e->mc_chains.p, fp64, st);
+        launch_mc_chains(e->b, e->mc_chains.p, fp64, molecular, st);
         e->launches += 1;
         CUDA_TRY(e, cudaMemcpyAsync(e->h_mc.data(), e->mc_chains.p, nsys * sizeof(McState), cudaMemcpyDeviceToHost,
                                     st));

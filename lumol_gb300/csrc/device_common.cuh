@@ -523,6 +523,11 @@ struct McState {
     long long accepted, attempted;
     int32_t enabled;
     int32_t need_rebuild;
+    // molecular chains (lg_mc_setup_ex): Translate and Rotate of whole molecules
+    double theta;          // Rotate: largest angle
+    double cum_translate;  // cumulative frequency of Translate (MonteCarlo::normalize_frequencies); 1 without Rotate
+    int32_t molecular;     // 1: moves pick molecules (any size) and may rotate them
+    int32_t mol_pad;
 };
 
 // Status word bits (device -> host).

@@ -165,7 +165,7 @@ void launch_mc_cost(const Batch& b, int s, const SysDev& sd, int mbeg, int msize
                     cudaStream_t st);
 void launch_mc_accept(const Batch& b, const SysDev& sd, int mbeg, int msize, const double* d_newpos,
                       const SysDev* d_sys, const double2* d_drho, cudaStream_t st);
-void launch_mc_chains(const Batch& b, McState* mc, bool fp64, cudaStream_t st);
+void launch_mc_chains(const Batch& b, McState* mc, bool fp64, bool molecular, cudaStream_t st);
 // diag.cu
 int measure_fma_peak(int fp64, double* tflops);
 // runtime.cu: the message lg_last_error(NULL) returns

@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(128) mc_chain_kernel(Batch b, McState* __restr
     int lane = threadIdx.x & 31;
     if (s >= b.nsys) return;
     McState st = mc[s];
-    if (!st.enabled || st.moves_left <= 0 || st.need_rebuild) return;
+    if (!st.enabled || st.molecular || st.moves_left <= 0 || st.need_rebuild) return;
     const SysDev& sd = b.sys[s];
     int natoms = sd.end - sd.begin;
     if (natoms <= 0) return;
@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(128) mc_chain_mixed_kernel(Batch b, McState* _
     int lane = threadIdx.x & 31;
     if (s >= b.nsys) return;
     McState st = mc[s];
-    if (!st.enabled || st.moves_left <= 0 || st.need_rebuild) return;
+    if (!st.enabled || st.molecular || st.moves_left <= 0 || st.need_rebuild) return;
     const SysDev& sd = b.sys[s];
     int natoms = sd.end - sd.begin;
     if (natoms <= 0) return;
@@ -452,9 +452,196 @@ __global__ void __launch_bounds__(128) mc_chain_mixed_kernel(Batch b, McState* _
     }
 }
 
-void launch_mc_chains(const Batch& b, McState* mc, bool fp64, cudaStream_t st) {
+// ---------------------------------------------------------------------------
+// Molecular chains: MonteCarlo::propagate (mc/monte_carlo.rs:289-330) with
+// Translate (mc/moves/translate.rs:84-125) and Rotate (mc/moves/rotate.rs:
+// 68-124) of whole rigid molecules, one warp per system, in FP64 on either
+// precision.  A move draws, from the chain's SplitMix64 stream: the move
+// (the first whose cumulative frequency reaches a uniform number), the
+// molecule (uniform), then the displacement (three uniforms in
+// [-delta, delta)) or the axis (Marsaglia's 1972 method for a point of the
+// unit sphere: two uniforms in [-1, 1) until x1^2 + x2^2 < 1) and the angle
+// (uniform in [-theta, theta)), then the Metropolis number.  The energy change
+// is EnergyCache::move_molecule_cost (sys/cache.rs:145-220) of the pair
+// potentials: each moved atom against its Verlet-list neighbours outside the
+// molecule (a rigid move keeps the intramolecular terms).  A move that would
+// carry any atom of the molecule past skin / 2 stops the chain before it is
+// attempted, as in the single-atom chains.
+// ---------------------------------------------------------------------------
+struct MolMove {
+    bool rotate;
+    double d[3];    // Translate: the displacement
+    double R[9];    // Rotate: Matrix3::rotation(axis, angle) (matrix.rs:149-168)
+    double com[3];  // Rotate: Molecule::center_of_mass (molecules.rs:256-264)
+};
+
+__device__ __forceinline__ void mol_new_position(const MolMove& mv, const double4_32a& p, double out[3]) {
+    if (!mv.rotate) {
+        out[0] = p.x + mv.d[0];
+        out[1] = p.y + mv.d[1];
+        out[2] = p.z + mv.d[2];
+        return;
+    }
+    // rotate_around_axis (rotate.rs:118-124): com + rotation * (position - com)
+    double v[3] = {p.x - mv.com[0], p.y - mv.com[1], p.z - mv.com[2]}, r[3];
+    for (int a = 0; a < 3; a++)
+        r[a] = __dadd_rn(__dadd_rn(__dmul_rn(mv.R[3 * a], v[0]), __dmul_rn(mv.R[3 * a + 1], v[1])),
+                         __dmul_rn(mv.R[3 * a + 2], v[2]));
+    for (int a = 0; a < 3; a++) out[a] = mv.com[a] + r[a];
+}
+
+__global__ void __launch_bounds__(128) mc_chain_mol_kernel(Batch b, McState* __restrict__ mc) {
+    int s = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    int lane = threadIdx.x & 31;
+    if (s >= b.nsys) return;
+    McState st = mc[s];
+    if (!st.enabled || !st.molecular || st.moves_left <= 0 || st.need_rebuild) return;
+    const SysDev& sd = b.sys[s];
+    const int nmol = sd.mol_end - sd.mol_first;
+    if (nmol <= 0) return;
+    uint64_t rng = st.rng;
+    int64_t left = st.moves_left;
+    double energy = st.energy;
+    long long accepted = st.accepted, attempted = st.attempted;
+    bool rebuild = false;
+    while (left > 0) {
+        uint64_t saved = rng;
+        MolMove mv;
+        mv.rotate = !(uniform01(rng) <= st.cum_translate);
+        const int m = sd.mol_first + min((int)(uniform01(rng) * nmol), nmol - 1);
+        const int a0 = b.mol_start[m], a1 = b.mol_start[m + 1];
+        if (!mv.rotate) {
+            for (int k = 0; k < 3; k++) mv.d[k] = -st.delta + 2.0 * st.delta * uniform01(rng);
+        } else {
+            double x1 = 0.0, x2 = 0.0, sum = 1.0;
+            for (int tries = 0; tries < 64 && !(sum < 1.0); tries++) {
+                x1 = -1.0 + 2.0 * uniform01(rng);
+                x2 = -1.0 + 2.0 * uniform01(rng);
+                sum = x1 * x1 + x2 * x2;
+            }
+            double axis[3] = {0.0, 0.0, 1.0};
+            if (sum < 1.0) {
+                double factor = 2.0 * sqrt(1.0 - sum);
+                axis[0] = x1 * factor;
+                axis[1] = x2 * factor;
+                axis[2] = 1.0 - 2.0 * sum;
+            }
+            double angle = -st.theta + 2.0 * st.theta * uniform01(rng);
+            double norm = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(axis[0], axis[0]), __dmul_rn(axis[1], axis[1])),
+                                               __dmul_rn(axis[2], axis[2])));
+            double n[3] = {__ddiv_rn(axis[0], norm), __ddiv_rn(axis[1], norm), __ddiv_rn(axis[2], norm)};
+            double sn = sin(angle), cs = cos(angle);
+            double xs = n[0] * sn, ys = n[1] * sn, zs = n[2] * sn;
+            double omc = 1.0 - cs;
+            double xy = __dmul_rn(__dmul_rn(n[0], n[1]), omc), xz = __dmul_rn(__dmul_rn(n[0], n[2]), omc),
+                   yz = __dmul_rn(__dmul_rn(n[1], n[2]), omc);
+            mv.R[0] = __dadd_rn(__dmul_rn(__dmul_rn(n[0], n[0]), omc), cs);
+            mv.R[1] = __dadd_rn(xy, zs);
+            mv.R[2] = __dsub_rn(xz, ys);
+            mv.R[3] = __dsub_rn(xy, zs);
+            mv.R[4] = __dadd_rn(__dmul_rn(__dmul_rn(n[1], n[1]), omc), cs);
+            mv.R[5] = __dadd_rn(yz, xs);
+            mv.R[6] = __dadd_rn(xz, ys);
+            mv.R[7] = __dsub_rn(yz, xs);
+            mv.R[8] = __dadd_rn(__dmul_rn(__dmul_rn(n[2], n[2]), omc), cs);
+            double total = 0.0, c[3] = {0.0, 0.0, 0.0};
+            for (int a = a0; a < a1; a++) {
+                double4_32a p = b.posq[a];
+                double w = b.vel[a].w;
+                total = __dadd_rn(total, w);
+                c[0] = __dadd_rn(c[0], __dmul_rn(w, p.x));
+                c[1] = __dadd_rn(c[1], __dmul_rn(w, p.y));
+                c[2] = __dadd_rn(c[2], __dmul_rn(w, p.z));
+            }
+            for (int k = 0; k < 3; k++) mv.com[k] = __ddiv_rn(c[k], total);
+        }
+        double u_accept = uniform01(rng);
+        // every moved atom stays within skin / 2 of its position at the last build
+        bool far = false;
+        for (int a = a0 + lane; a < a1; a += 32) {
+            double np[3];
+            mol_new_position(mv, b.posq[a], np);
+            double4_32a bp = b.pos_build[a];
+            far = far || !(image_norm2(sd, np[0] - bp.x, np[1] - bp.y, np[2] - bp.z) <= sd.half_skin2);
+        }
+        if (__any_sync(0xffffffffu, far)) {
+            rng = saved;  // not attempted: retried after the list rebuild
+            rebuild = true;
+            break;
+        }
+        double de = 0.0;
+        for (int a = a0; a < a1; a++) {
+            double4_32a old = b.posq[a];
+            double np[3];
+            mol_new_position(mv, old, np);
+            const PairDev* prow = b.ptab + sd.ptab + b.kind[a] * sd.nk;
+            int row = b.perm ? b.perm[a] : a;
+            int cnt = b.nnb[row];
+            const int* list = b.nbr + (size_t)row * b.maxnb;
+            for (int k = lane; k < cnt; k += 32) {
+                int j = b.perm ? b.cell_atoms[list[k]] : list[k];
+                if (b.mol[j] == m) continue;  // (intramolecular terms do not change)
+                const PairDev& p = prow[b.kind[j]];
+                if (p.type == 0 || restriction_excluded(p.restriction, 0)) continue;
+                double4_32a pj = b.posq[j];
+                double ox, oy, oz, wx, wy, wz;
+                exact_nearest_image(sd, pj.x, pj.y, pj.z, old.x, old.y, old.z, ox, oy, oz);
+                exact_nearest_image(sd, np[0], np[1], np[2], pj.x, pj.y, pj.z, wx, wy, wz);
+                de += mc_pair_energy(p, wx, wy, wz) - mc_pair_energy(p, ox, oy, oz);
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) de += __shfl_xor_sync(0xffffffffu, de, o);
+        attempted++;
+        double cost = st.beta * de;
+        bool accept = cost <= 0.0 || u_accept < exp(-cost);
+        if (accept) {
+            // apply: the new positions; a translated molecule is wrapped by its
+            // centre of mass (Molecule::wrap, molecules.rs:287-296)
+            double shift[3] = {0.0, 0.0, 0.0};
+            if (!mv.rotate) {
+                double total = 0.0, c[3] = {0.0, 0.0, 0.0};
+                for (int a = a0; a < a1; a++) {
+                    double np[3];
+                    mol_new_position(mv, b.posq[a], np);
+                    double w = b.vel[a].w;
+                    total = __dadd_rn(total, w);
+                    for (int k = 0; k < 3; k++) c[k] = __dadd_rn(c[k], __dmul_rn(w, np[k]));
+                }
+                double com[3], wc[3];
+                for (int k = 0; k < 3; k++) com[k] = wc[k] = __ddiv_rn(c[k], total);
+                for (int k = 0; k < 3; k++) wc[k] = __dsub_rn(wc[k], __dmul_rn(floor(__ddiv_rn(wc[k], sd.L[k])), sd.L[k]));
+                for (int k = 0; k < 3; k++) shift[k] = __dsub_rn(wc[k], com[k]);
+            }
+            __syncwarp();  // every lane has read the old positions
+            for (int a = a0 + lane; a < a1; a += 32) {
+                double4_32a old = b.posq[a];
+                double np[3];
+                mol_new_position(mv, old, np);
+                double4_32a q = make_double4_32a(np[0] + shift[0], np[1] + shift[1], np[2] + shift[2], old.w);
+                b.posq[a] = q;
+                if (b.perm) b.posfx[b.perm[a]] = fixed_position(sd, q);
+            }
+            energy += de;
+            accepted++;
+        }
+        __syncwarp();
+        left--;
+    }
+    if (lane == 0) {
+        mc[s].rng = rng;
+        mc[s].moves_left = left;
+        mc[s].energy = energy;
+        mc[s].accepted = accepted;
+        mc[s].attempted = attempted;
+        mc[s].need_rebuild = rebuild ? 1 : 0;
+    }
+}
+
+void launch_mc_chains(const Batch& b, McState* mc, bool fp64, bool molecular, cudaStream_t st) {
     int warps_per_block = 4;
     int grid = (b.nsys + warps_per_block - 1) / warps_per_block;
+    // (each kernel skips the other kind's chains: a chain's draws do not depend on the batch)
+    if (molecular) mc_chain_mol_kernel<<<grid, 32 * warps_per_block, 0, st>>>(b, mc);
     if (fp64) mc_chain_kernel<<<grid, 32 * warps_per_block, 0, st>>>(b, mc);
     else mc_chain_mixed_kernel<<<grid, 32 * warps_per_block, 0, st>>>(b, mc);
 }

@@ -113,3 +113,103 @@ def test_chains_with_other_pair_potentials(family):
     fresh = batch.energy(0)
     assert att == 2000 and acc > 0
     assert abs(energy - fresh) <= 1e-5 * abs(fresh), (energy, fresh)
+
+
+# ---- molecular chains: Translate and Rotate of whole molecules (lg_mc_setup_ex) ---------
+def replay_molecular(system, temperature, delta, f_t, theta, f_r, seed, moves):
+    """The molecular chain's draws (move by cumulative frequency, molecule,
+    displacement or Marsaglia axis + angle, Metropolis number) replayed through
+    the oracle's EnergyCache, with the moves applied as Translate (then
+    Molecule::wrap) and Rotate (rotate_around_axis) apply them."""
+    orc = oracle.Oracle(system)
+    orc.cache_init()
+    rng = SplitMix64(seed)
+    beta = 1.0 / (K_BOLTZMANN * temperature)
+    half = delta / math.sqrt(3.0)
+    cum_t = f_t / (f_t + f_r) if f_r > 0.0 else 1.0
+    pos = system.positions.copy()
+    masses = system.masses
+    L = np.array(system.cell.lengths)
+    nmol = int(system.molecules[-1]) + 1
+    accepted = 0
+    for _ in range(moves):
+        rotate = not (rng.uniform() <= cum_t)
+        m = min(int(rng.uniform() * nmol), nmol - 1)
+        lo, hi = system.molecule_range(m)
+        if not rotate:
+            d = [-half + 2.0 * half * rng.uniform() for _ in range(3)]
+            new = pos[lo:hi] + np.array(d)
+        else:
+            x1 = x2 = 0.0
+            s = 1.0
+            tries = 0
+            while tries < 64 and not (s < 1.0):
+                x1 = -1.0 + 2.0 * rng.uniform()
+                x2 = -1.0 + 2.0 * rng.uniform()
+                s = x1 * x1 + x2 * x2
+                tries += 1
+            axis = [0.0, 0.0, 1.0]
+            if s < 1.0:
+                f = 2.0 * math.sqrt(1.0 - s)
+                axis = [x1 * f, x2 * f, 1.0 - 2.0 * s]
+            angle = -theta + 2.0 * theta * rng.uniform()
+            norm = math.sqrt(axis[0] * axis[0] + axis[1] * axis[1] + axis[2] * axis[2])
+            n = [axis[0] / norm, axis[1] / norm, axis[2] / norm]
+            sn, cs = math.sin(angle), math.cos(angle)
+            omc = 1.0 - cs
+            xy, xz, yz = n[0] * n[1] * omc, n[0] * n[2] * omc, n[1] * n[2] * omc
+            R = [[n[0] * n[0] * omc + cs, xy + n[2] * sn, xz - n[1] * sn],
+                 [xy - n[2] * sn, n[1] * n[1] * omc + cs, yz + n[0] * sn],
+                 [xz + n[1] * sn, yz - n[0] * sn, n[2] * n[2] * omc + cs]]
+            total, c = 0.0, [0.0, 0.0, 0.0]
+            for a in range(lo, hi):
+                total += masses[a]
+                for k in range(3):
+                    c[k] += masses[a] * pos[a][k]
+            com = [c[k] / total for k in range(3)]
+            new = pos[lo:hi].copy()
+            for r, a in enumerate(range(lo, hi)):
+                v = [pos[a][k] - com[k] for k in range(3)]
+                new[r] = [com[k] + (R[k][0] * v[0] + R[k][1] * v[1] + R[k][2] * v[2]) for k in range(3)]
+        u = rng.uniform()
+        cost = beta * orc.move_molecule_cost(m, new)
+        if cost <= 0.0 or u < math.exp(-cost):
+            if not rotate:  # Molecule::wrap by the centre of mass
+                total, c = 0.0, np.zeros(3)
+                for r, a in enumerate(range(lo, hi)):
+                    total += masses[a]
+                    c = c + masses[a] * new[r]
+                com = c / total
+                new = new + ((com - np.floor(com / L) * L) - com)
+            pos[lo:hi] = new
+            orc.set_positions(pos)
+            orc.cache_update()
+            accepted += 1
+    return pos, orc.cache_energy(), accepted
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_molecular_chains_follow_the_oracle_move_for_move(precision):
+    """Rigid 5-atom chains (LJ between molecules, Exclude13 inside them) with
+    Translate and Rotate at equal frequency, next to a single-atom chain in
+    the same batch, whose moves stay those of its own replay."""
+    import systems as test_systems
+    mol = test_systems.chains(27, 24.0, 3, lg.PairRestriction.EXCLUDE13)
+    atoms = workloads.lj_replica(300, 0.6, 120.0, 11)
+    batch = Batch([mol, atoms], precision=precision)
+    batch.md_setup([1.0, 1.0])
+    batch.mc_setup_moves(0, 300.0, translate=(0.3, 1.0), rotate=(0.15, 1.0), seed=41)
+    batch.mc_setup(1, 120.0, 0.3, 100)
+    moves = 300
+    batch.mc_run(moves)
+    mol_ref = test_systems.chains(27, 24.0, 3, lg.PairRestriction.EXCLUDE13)
+    pos_ref, e_ref, acc_ref = replay_molecular(mol_ref, 300.0, 0.3, 1.0, 0.15, 1.0, 41, moves)
+    energy, acc, att = batch.mc_stats(0)
+    pos, _ = batch.state(0)
+    assert att == moves and acc == acc_ref and 0 < acc < moves
+    assert np.abs(pos - pos_ref).max() < 1e-9
+    assert abs(energy - e_ref) <= 1e-9 * abs(e_ref)
+    pos_a, e_a, acc_a = replay(workloads.lj_replica(300, 0.6, 120.0, 11), 120.0, 0.3, 100, moves)
+    energy, acc, att = batch.mc_stats(1)
+    pos, _ = batch.state(1)
+    assert acc == acc_a and np.abs(pos - pos_a).max() < 1e-9
