@@ -60,7 +60,8 @@ def parse():
     p.add_argument("--replicas", type=int, default=256, help="lj_batch: replicas (half MD, half MC)")
     p.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     p.add_argument("--cells", type=int, default=0, help="lattice cells per side (0: the workload's size)")
-    p.add_argument("--chunk", type=int, default=16, help="MD steps per timed iteration (one lg_md_run call)")
+    p.add_argument("--chunk", type=int, default=32,
+                   help="MD steps per timed iteration (one lg_md_run call; one persistent launch up to 32)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-roofline", action="store_true")
@@ -565,10 +566,10 @@ def main_serving(args, world, rank, local):
     requests = workloads.serving_requests(count=args.requests, rate=args.rate, seed=77 + rank,
                                           precision=args.precision)
     warm = workloads.serving_requests(count=4, rate=1000.0, seed=1, precision=args.precision, scale=0.02)
-    server = Server(precision=args.precision, chunk=args.chunk * 4, max_lanes=4)
+    server = Server(precision=args.precision, chunk=max(16, args.chunk) * 2, max_lanes=4)
     server.run(warm)
     server.close()
-    server = Server(precision=args.precision, chunk=args.chunk * 4, max_lanes=4)
+    server = Server(precision=args.precision, chunk=max(16, args.chunk) * 2, max_lanes=4)
     barrier(world)
     torch.cuda.synchronize()
     clocks = ClockSampler(local)

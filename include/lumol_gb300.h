@@ -466,7 +466,9 @@ int lg_mc_setup(lg_engine* e, int32_t s, double temperature, double delta, uint6
  * Matrix3::rotation); the cost counts the pair potentials between the moved
  * molecule and the other atoms.  A translated molecule is wrapped by its
  * centre of mass, a rotated one is not (as the reference applies them).  Pair
- * potentials only, orthorhombic cells; a frequency of 0 leaves that move out.
+ * potentials only; a frequency of 0 leaves that move out.  (A chain that
+ * lg_mc_setup gives a triclinic system runs this way too: the move draw comes
+ * first, then the molecule, the displacement, the Metropolis number.)
  * lg_mc_run checks that the largest rotated displacement stays within half the
  * skin. */
 int lg_mc_setup_ex(lg_engine* e, int32_t s, double temperature, double translate_delta, double translate_frequency,

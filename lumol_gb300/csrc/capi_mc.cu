@@ -224,10 +224,6 @@ static int mc_setup_chain(lg_engine* e, int32_t s, double temperature, double de
     if (!(temperature > 0.0)) return fail(e, LG_ERR_ARGUMENT, "the temperature must be positive in Monte Carlo");
     if (!(delta > 0.0)) return fail(e, LG_ERR_ARGUMENT, "delta must be positive in Translate move");
     const HostSystem& h = e->sys[s];
-    if (h.cell.shape != LG_CELL_ORTHORHOMBIC)
-        return fail(e, LG_ERR_ARGUMENT,
-                    "batched Monte Carlo chains take orthorhombic cells; use lg_mc_move_molecule_cost for a "
-                    "triclinic cell");
     if (h.coul.kind != LG_COULOMB_NONE)
         return fail(e, LG_ERR_ARGUMENT,
                     "batched Monte Carlo chains evaluate pair potentials only; use lg_mc_move_molecule_cost "
@@ -250,7 +246,9 @@ static int mc_setup_chain(lg_engine* e, int32_t s, double temperature, double de
     m.moves_left = 0;
     m.need_rebuild = 0;
     m.accepted = m.attempted = 0;
-    m.molecular = 0;  // (lg_mc_setup_ex sets the molecular moves afterwards)
+    // (lg_mc_setup_ex sets the molecular moves afterwards; a triclinic cell's
+    // chain runs in the molecular chains' kernel, whose geometry is general)
+    m.molecular = h.cell.shape == LG_CELL_ORTHORHOMBIC ? 0 : 1;
     m.theta = 0.0;
     m.cum_translate = 1.0;
     if (!e->dirty) {
@@ -275,10 +273,6 @@ int lg_mc_setup_ex(lg_engine* e, int32_t s, double temperature, double translate
     if (rotate_frequency > 0.0 && !(rotate_theta > 0.0))
         return fail(e, LG_ERR_ARGUMENT, "theta must be positive in Rotate move");
     const HostSystem& h = e->sys[s];
-    if (h.cell.shape != LG_CELL_ORTHORHOMBIC)
-        return fail(e, LG_ERR_ARGUMENT,
-                    "batched Monte Carlo chains take orthorhombic cells; use lg_mc_move_molecule_cost for a "
-                    "triclinic cell");
     if (h.coul.kind != LG_COULOMB_NONE)
         return fail(e, LG_ERR_ARGUMENT,
                     "batched Monte Carlo chains evaluate pair potentials only; use lg_mc_move_molecule_cost "

@@ -609,7 +609,10 @@ __global__ void __launch_bounds__(128) mc_chain_mol_kernel(Batch b, McState* __r
                 }
                 double com[3], wc[3];
                 for (int k = 0; k < 3; k++) com[k] = wc[k] = __ddiv_rn(c[k], total);
-                for (int k = 0; k < 3; k++) wc[k] = __dsub_rn(wc[k], __dmul_rn(floor(__ddiv_rn(wc[k], sd.L[k])), sd.L[k]));
+                if (sd.tric) tric_wrap(sd, wc);  // UnitCell::wrap_vector (cells.rs:263-282)
+                else
+                    for (int k = 0; k < 3; k++)
+                        wc[k] = __dsub_rn(wc[k], __dmul_rn(floor(__ddiv_rn(wc[k], sd.L[k])), sd.L[k]));
                 for (int k = 0; k < 3; k++) shift[k] = __dsub_rn(wc[k], com[k]);
             }
             __syncwarp();  // every lane has read the old positions

@@ -180,7 +180,7 @@ def replay_molecular(system, temperature, delta, f_t, theta, f_r, seed, moves):
                     total += masses[a]
                     c = c + masses[a] * new[r]
                 com = c / total
-                new = new + ((com - np.floor(com / L) * L) - com)
+                new = new + (np.array(system.cell.wrap_vector(com)) - com)
             pos[lo:hi] = new
             orc.set_positions(pos)
             orc.cache_update()

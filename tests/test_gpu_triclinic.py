@@ -244,6 +244,23 @@ def test_shape_and_chain_errors():
         eng.call("lg_set_cell_ex", 0, C.dptr(m), C.LG_CELL_ORTHORHOMBIC)
     with pytest.raises(lg.EngineError):
         eng.call("lg_set_cell_ex", 0, C.dptr(np.zeros(9)), C.LG_CELL_TRICLINIC)
-    f = fluid(n=300)
-    with pytest.raises(lg.EngineError):
-        f.engine().call("lg_mc_setup", 0, 150.0, 0.3, 1)
+
+
+
+def test_device_chains_in_a_triclinic_cell():
+    """A chain of a triclinic system runs in the molecular chains' kernel
+    (general image and wrap): replayed move for move through the oracle."""
+    from lumol_gb300.batch import Batch
+    from test_gpu_mc_chains import replay_molecular
+    s = fluid(n=300, seed=8)
+    b = Batch([s])
+    b.md_setup([1.0])
+    b.mc_setup(0, 150.0, 0.3, 17)
+    b.mc_run(300)
+    pos_ref, e_ref, acc_ref = replay_molecular(fluid(n=300, seed=8), 150.0, 0.3, 1.0, 0.0, 0.0, 17, 300)
+    energy, acc, att = b.mc_stats(0)
+    pos, _ = b.state(0)
+    assert att == 300 and acc == acc_ref and acc > 0
+    assert np.abs(pos - pos_ref).max() < 1e-9
+    assert abs(energy - e_ref) <= 1e-9 * abs(e_ref)
+    b.engine.close()
