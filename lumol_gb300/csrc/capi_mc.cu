@@ -224,10 +224,6 @@ static int mc_setup_chain(lg_engine* e, int32_t s, double temperature, double de
     if (!(temperature > 0.0)) return fail(e, LG_ERR_ARGUMENT, "the temperature must be positive in Monte Carlo");
     if (!(delta > 0.0)) return fail(e, LG_ERR_ARGUMENT, "delta must be positive in Translate move");
     const HostSystem& h = e->sys[s];
-    if (h.coul.kind != LG_COULOMB_NONE)
-        return fail(e, LG_ERR_ARGUMENT,
-                    "batched Monte Carlo chains evaluate pair potentials only; use lg_mc_move_molecule_cost "
-                    "for systems with Coulomb interactions");
     if (!molecules)
         for (size_t i = 1; i < h.mols.size(); i++)
             if (h.mols[i] == h.mols[i - 1])
@@ -246,9 +242,10 @@ static int mc_setup_chain(lg_engine* e, int32_t s, double temperature, double de
     m.moves_left = 0;
     m.need_rebuild = 0;
     m.accepted = m.attempted = 0;
-    // (lg_mc_setup_ex sets the molecular moves afterwards; a triclinic cell's
-    // chain runs in the molecular chains' kernel, whose geometry is general)
-    m.molecular = h.cell.shape == LG_CELL_ORTHORHOMBIC ? 0 : 1;
+    // (lg_mc_setup_ex sets the molecular moves afterwards; the chain of a
+    // triclinic cell or of a system with Coulomb interactions runs in the
+    // molecular chains' kernel, whose geometry and energy terms are general)
+    m.molecular = (h.cell.shape == LG_CELL_ORTHORHOMBIC && h.coul.kind == LG_COULOMB_NONE) ? 0 : 1;
     m.theta = 0.0;
     m.cum_translate = 1.0;
     if (!e->dirty) {
@@ -272,11 +269,6 @@ int lg_mc_setup_ex(lg_engine* e, int32_t s, double temperature, double translate
         return fail(e, LG_ERR_ARGUMENT, "delta must be positive in Translate move");
     if (rotate_frequency > 0.0 && !(rotate_theta > 0.0))
         return fail(e, LG_ERR_ARGUMENT, "theta must be positive in Rotate move");
-    const HostSystem& h = e->sys[s];
-    if (h.coul.kind != LG_COULOMB_NONE)
-        return fail(e, LG_ERR_ARGUMENT,
-                    "batched Monte Carlo chains evaluate pair potentials only; use lg_mc_move_molecule_cost "
-                    "for systems with Coulomb interactions");
     double half = translate_frequency > 0.0 ? translate_delta / std::sqrt(3.0) : 0.0;
     if (std::sqrt(3.0) * half > 0.5 * e->skin)
         return fail(e, LG_ERR_ARGUMENT, "the Translate amplitude must not exceed half the neighbour-list skin");
@@ -322,10 +314,12 @@ int lg_mc_run(lg_engine* e, int64_t moves) {
         }
     if (!any) return fail(e, LG_ERR_STATE, "lg_mc_setup was not called for any system");
     bool molecular = false;  // chains of lg_mc_setup_ex: the molecular chains' kernel runs too
+    bool kspace = false;     // ... with Ewald: they read and update the FP64 rho(k)
     for (int s = 0; s < nsys; s++) {
         const McState& m = e->h_mc[s];
         if (!m.enabled || !m.molecular) continue;
         molecular = true;
+        kspace = kspace || e->sys[s].coul.kind == LG_COULOMB_EWALD;
         if (m.cum_translate >= 1.0) continue;
         // a rotated atom moves by at most 2 r sin(theta / 2), r its distance from
         // the molecule's centre of mass: it must stay within skin / 2, else no
@@ -365,6 +359,9 @@ int lg_mc_run(lg_engine* e, int64_t moves) {
         launch_split_positions(e->b, st);
         e->launches += 1;
     }
+    if (kspace) {  // the FP64 rho(k) of the current positions
+        mc_refresh_kspace(e);
+    }
     for (int64_t launch = 0; launch < moves + 64; launch++) {
         launch_mc_chains(e->b, e->mc_chains.p, fp64, molecular, st);
         e->launches += 1;
@@ -378,7 +375,15 @@ int lg_mc_run(lg_engine* e, int64_t moves) {
             rebuild = rebuild || e->h_mc[s].need_rebuild;
             pending = pending || e->h_mc[s].moves_left > 0;
         }
-        if (!pending) return LG_OK;
+        if (!pending) {
+            // (the chains updated rho(k) themselves; the e^{ik.r} tables follow the
+            // moved atoms for the single-molecule costs that may come next)
+            if (kspace) {
+                mc_refresh_kspace(e);
+                CUDA_TRY(e, cudaStreamSynchronize(st));
+            }
+            return LG_OK;
+        }
         if (rebuild) {
             // rebuild the lists of the stopped chains' systems only
             std::vector<uint32_t> flags(nsys, 0u);

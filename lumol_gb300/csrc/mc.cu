@@ -490,6 +490,44 @@ __device__ __forceinline__ void mol_new_position(const MolMove& mv, const double
     for (int a = 0; a < 3; a++) out[a] = mv.com[a] + r[a];
 }
 
+// The Ewald k-space energy change of a molecular move (ewald.rs:790-839), this
+// lane's share of the system's k-vectors: delta rho(k) = sum_a q_a
+// (e^{ik.r_new} - e^{ik.r_old}) with k.r = ikx k_x.r + iky k_y.r + ikz k_z.r
+// from the per-axis k-vectors, and sum_k f_k (|rho + delta|^2 - |rho|^2) /
+// (4 pi eps0).  With `apply`, rho(k) += delta rho(k) instead (the accepted move).
+__device__ double mol_kspace_delta(const Batch& b, const SysDev& sd, const MolMove& mv, int a0, int a1, int lane,
+                                   bool apply) {
+    double dk = 0.0;
+    for (int kk = sd.kbegin + lane; kk < sd.kend; kk += 32) {
+        const KVecDev& kv = b.kvec[kk];
+        double re = 0.0, im = 0.0;
+        for (int a = a0; a < a1; a++) {
+            double4_32a p = b.posq[a];
+            if (p.w == 0.0) continue;
+            double np[3];
+            mol_new_position(mv, p, np);
+            double po = kv.ikx * axis_phase(sd, 0, p.x, p.y, p.z) + kv.iky * axis_phase(sd, 1, p.x, p.y, p.z) +
+                        kv.ikz * axis_phase(sd, 2, p.x, p.y, p.z);
+            double pn = kv.ikx * axis_phase(sd, 0, np[0], np[1], np[2]) +
+                        kv.iky * axis_phase(sd, 1, np[0], np[1], np[2]) +
+                        kv.ikz * axis_phase(sd, 2, np[0], np[1], np[2]);
+            double so, co, sn, cn;
+            sincos(po, &so, &co);
+            sincos(pn, &sn, &cn);
+            re += p.w * (cn - co);
+            im += p.w * (sn - so);
+        }
+        double2 r = b.rho[kk];
+        if (apply) {
+            b.rho[kk] = make_double2(r.x + re, r.y + im);
+            continue;
+        }
+        double nx = r.x + re, ny = r.y + im;
+        dk += kv.energy * (nx * nx + ny * ny) - kv.energy * (r.x * r.x + r.y * r.y);
+    }
+    return dk / FOUR_PI_EPSILON_0;
+}
+
 __global__ void __launch_bounds__(128) mc_chain_mol_kernel(Batch b, McState* __restrict__ mc) {
     int s = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
     int lane = threadIdx.x & 31;
@@ -570,6 +608,7 @@ __global__ void __launch_bounds__(128) mc_chain_mol_kernel(Batch b, McState* __r
             break;
         }
         double de = 0.0;
+        const bool coul = sd.coul != 0 && !restriction_excluded(sd.coul_restr, 0);
         for (int a = a0; a < a1; a++) {
             double4_32a old = b.posq[a];
             double np[3];
@@ -582,14 +621,32 @@ __global__ void __launch_bounds__(128) mc_chain_mol_kernel(Batch b, McState* __r
                 int j = b.perm ? b.cell_atoms[list[k]] : list[k];
                 if (b.mol[j] == m) continue;  // (intramolecular terms do not change)
                 const PairDev& p = prow[b.kind[j]];
-                if (p.type == 0 || restriction_excluded(p.restriction, 0)) continue;
+                const bool pair = p.type != 0 && !restriction_excluded(p.restriction, 0);
                 double4_32a pj = b.posq[j];
+                const double qq = old.w * pj.w;
+                if (!pair && !(coul && qq != 0.0)) continue;
                 double ox, oy, oz, wx, wy, wz;
                 exact_nearest_image(sd, pj.x, pj.y, pj.z, old.x, old.y, old.z, ox, oy, oz);
                 exact_nearest_image(sd, np[0], np[1], np[2], pj.x, pj.y, pj.z, wx, wy, wz);
-                de += mc_pair_energy(p, wx, wy, wz) - mc_pair_energy(p, ox, oy, oz);
+                if (pair) de += mc_pair_energy(p, wx, wy, wz) - mc_pair_energy(p, ox, oy, oz);
+                if (coul && qq != 0.0) {  // Ewald real space or Wolf (ewald.rs:387-428, wolf.rs:90-117)
+                    const double r_old = exact_norm(ox, oy, oz), r_new = exact_norm(wx, wy, wz);
+                    double e, fr, e_old = 0.0, e_new = 0.0;
+                    if (!(r_old > sd.coul_rc)) {
+                        if (sd.coul == 1) ewald_real_pair(sd.alpha, false, qq, r_old, 1.0 / r_old, e, fr);
+                        else wolf_pair(sd, qq, r_old, 1.0 / r_old, e, fr);
+                        e_old = e;
+                    }
+                    if (!(r_new > sd.coul_rc)) {
+                        if (sd.coul == 1) ewald_real_pair(sd.alpha, false, qq, r_new, 1.0 / r_new, e, fr);
+                        else wolf_pair(sd, qq, r_new, 1.0 / r_new, e, fr);
+                        e_new = e;
+                    }
+                    de += e_new - e_old;
+                }
             }
         }
+        if (sd.coul == 1) de += mol_kspace_delta(b, sd, mv, a0, a1, lane, false);
         for (int o = 16; o > 0; o >>= 1) de += __shfl_xor_sync(0xffffffffu, de, o);
         attempted++;
         double cost = st.beta * de;
@@ -615,6 +672,9 @@ __global__ void __launch_bounds__(128) mc_chain_mol_kernel(Batch b, McState* __r
                         wc[k] = __dsub_rn(wc[k], __dmul_rn(floor(__ddiv_rn(wc[k], sd.L[k])), sd.L[k]));
                 for (int k = 0; k < 3; k++) shift[k] = __dsub_rn(wc[k], com[k]);
             }
+            // rho(k) += delta rho(k) of the accepted move (ewald.rs:826-830), each
+            // lane its own k-vectors, before the positions change
+            if (sd.coul == 1) (void)mol_kspace_delta(b, sd, mv, a0, a1, lane, true);
             __syncwarp();  // every lane has read the old positions
             for (int a = a0 + lane; a < a1; a += 32) {
                 double4_32a old = b.posq[a];

@@ -78,13 +78,6 @@ def test_chain_energy_tracks_fresh_energy(precision):
         assert abs(energy - fresh) <= tol * abs(fresh), (energy, fresh)
 
 
-def test_coulomb_systems_are_rejected():
-    s = workloads.nacl_crystal(cells=3, cutoff=8.0, kmax=5)
-    batch = Batch([s])
-    with pytest.raises(lg.EngineError, match="pair potentials only"):
-        batch.mc_setup(0, 300.0, 0.3, 1)
-
-
 @pytest.mark.parametrize("family", ["bmh", "morse", "gaussian", "mie", "table"])
 def test_chains_with_other_pair_potentials(family):
     """FP64 chains follow the oracle move for move; mixed chains keep their
@@ -116,11 +109,14 @@ def test_chains_with_other_pair_potentials(family):
 
 
 # ---- molecular chains: Translate and Rotate of whole molecules (lg_mc_setup_ex) ---------
-def replay_molecular(system, temperature, delta, f_t, theta, f_r, seed, moves):
+def replay_molecular(system, temperature, delta, f_t, theta, f_r, seed, moves, refresh=False):
     """The molecular chain's draws (move by cumulative frequency, molecule,
     displacement or Marsaglia axis + angle, Metropolis number) replayed through
     the oracle's EnergyCache, with the moves applied as Translate (then
-    Molecule::wrap) and Rotate (rotate_around_axis) apply them."""
+    Molecule::wrap) and Rotate (rotate_around_axis) apply them.  `refresh`
+    rebuilds the oracle's cache after every accepted move: with Ewald, the
+    reference keeps a moved molecule's e^{ik.r} stale (ewald.rs:826-830),
+    the engine's chains do not."""
     orc = oracle.Oracle(system)
     orc.cache_init()
     rng = SplitMix64(seed)
@@ -183,7 +179,10 @@ def replay_molecular(system, temperature, delta, f_t, theta, f_r, seed, moves):
                 new = new + (np.array(system.cell.wrap_vector(com)) - com)
             pos[lo:hi] = new
             orc.set_positions(pos)
-            orc.cache_update()
+            if refresh:
+                orc.cache_init()
+            else:
+                orc.cache_update()
             accepted += 1
     return pos, orc.cache_energy(), accepted
 
@@ -213,3 +212,45 @@ def test_molecular_chains_follow_the_oracle_move_for_move(precision):
     energy, acc, att = batch.mc_stats(1)
     pos, _ = batch.state(1)
     assert acc == acc_a and np.abs(pos - pos_a).max() < 1e-9
+
+
+@pytest.mark.parametrize("coulomb", ["wolf", "ewald"])
+def test_molecular_chains_with_coulomb_follow_the_oracle(coulomb):
+    """Charged rigid chains with Wolf or Ewald: the chain adds the real-space
+    Coulomb terms of the moved molecule's neighbours and, for Ewald, the
+    k-space change from delta rho(k), which an accepted move adds to rho(k)."""
+    import systems as test_systems
+
+    def make():
+        c = {"wolf": lg.Wolf(8.0), "ewald": lg.Ewald(9.0, 5, 0.35)}[coulomb]
+        return test_systems.chains(27, 24.0, 5, lg.PairRestriction.INTER_MOLECULAR, coulomb=c)
+    s = make()
+    batch = Batch([s])
+    batch.md_setup([1.0])
+    batch.mc_setup_moves(0, 300.0, translate=(0.3, 1.0), rotate=(0.15, 1.0), seed=43)
+    moves = 200
+    batch.mc_run(moves)
+    pos_ref, e_ref, acc_ref = replay_molecular(make(), 300.0, 0.3, 1.0, 0.15, 1.0, 43, moves,
+                                               refresh=coulomb == "ewald")
+    energy, acc, att = batch.mc_stats(0)
+    pos, _ = batch.state(0)
+    assert att == moves and acc == acc_ref and acc > 0
+    assert np.abs(pos - pos_ref).max() < 1e-9
+    assert abs(energy - e_ref) <= 1e-9 * abs(e_ref)
+    assert abs(energy - batch.energy(0)) <= 1e-9 * abs(e_ref)  # the chain's energy is the fresh energy
+
+
+def test_single_atom_chains_with_ewald_run_in_the_molecular_kernel():
+    """lg_mc_setup of a system with Coulomb interactions (NaCl, Ewald): one-ion
+    molecules through the molecular chains' kernel."""
+    s = workloads.nacl_crystal(cells=3, cutoff=8.0, kmax=5)
+    batch = Batch([s])
+    batch.md_setup([1.0])
+    batch.mc_setup(0, 300.0, 0.3, 9)
+    batch.mc_run(200)
+    pos_ref, e_ref, acc_ref = replay_molecular(workloads.nacl_crystal(cells=3, cutoff=8.0, kmax=5), 300.0, 0.3,
+                                               1.0, 0.0, 0.0, 9, 200, refresh=True)
+    energy, acc, att = batch.mc_stats(0)
+    pos, _ = batch.state(0)
+    assert acc == acc_ref and np.abs(pos - pos_ref).max() < 1e-9
+    assert abs(energy - e_ref) <= 1e-9 * abs(e_ref)
