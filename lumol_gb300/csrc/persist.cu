@@ -312,54 +312,67 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
                 b.pfx_build[i] = u;
             }
             pk_sync(cluster);
-            // 2f: Verlet list rows (warp per atom, cell order), as the per-step list build
-            for (int w = rsh.x + wib; w < rsh.y; w += PK_WARPS) {
-                int r = pk_find(s_rapre, R, w);
+            // 2f: Verlet list rows, one warp per cell.  The cell's stencil table and
+            // each 32-candidate chunk of fixed-point positions are gathered once and
+            // tested against every atom of the cell (a cell's atoms share one
+            // stencil); each row keeps the candidate order of the per-step list
+            // build, so the rows are the same
+            for (int vc = csh.x + wib; vc < csh.y; vc += PK_WARPS) {
+                int r = pk_find(s_rcpre, R, vc);
                 int si = s_rsys[r];
                 const SysDev& sd = b.sys[si];
-                int t = sd.begin + (w - s_rapre[r]);
-                int i = b.cell_atoms[t];
-                const uint4 ui = b.posfx[t];  // written in 2e, cell order
-                __syncwarp();  // the previous atom's readers of s_lo / s_pre are done
-                int2 nt = stencil_table(sd, si, b.atom_cell[i] - sd.cell_begin, b.cell_start, lane, s_lo[wib],
-                                        s_pre[wib]);
+                int local = vc - s_rcpre[r];
+                int c = sd.cell_begin + local;
+                int lo = b.cell_start[c + si], hi = b.cell_start[c + si + 1];
+                if (hi <= lo) continue;  // (the same in every lane)
+                __syncwarp();            // the previous cell's readers of s_lo / s_pre are done
+                int2 nt = stencil_table(sd, si, local, b.cell_start, lane, s_lo[wib], s_pre[wib]);
                 const int nruns = nt.x, total = nt.y;
                 __syncwarp();
-                float rl2 = sd.rlist2_f;
-                int count = 0;
-                int* out = b.nbr + (size_t)t * b.maxnb;
-                // candidates by sorted slot, two per lane in flight; the minimum image
-                // is the signed difference of the fixed-point coordinates
-                for (int base = 0; base < total; base += 64) {
-                    int slot[2];
-                    bool keep[2];
+                const float rl2 = sd.rlist2_f;
+                const unsigned below = (1u << lane) - 1u;
+                for (int a0 = lo; a0 < hi; a0 += 32) {  // the cell's atoms, 32 at a time
+                    const int na = min(32, hi - a0);
+                    const uint4 ua = lane < na ? b.posfx[a0 + lane] : make_uint4(0u, 0u, 0u, 0u);
+                    int count = 0;  // row length of atom a0 + lane
+                    // four 32-candidate chunks per pass, their gathers in flight together
+                    for (int base = 0; base < total; base += 128) {
+                        int slot[4];
+                        uint4 uj[4];
 #pragma unroll
-                    for (int h = 0; h < 2; h++) {
-                        int q = base + 32 * h + lane;
-                        slot[h] = -1;
-                        if (q < total) slot[h] = stencil_slot(s_lo[wib], s_pre[wib], nruns, q);
-                    }
-                    uint4 uj[2];
-#pragma unroll
-                    for (int h = 0; h < 2; h++) uj[h] = slot[h] >= 0 ? b.posfx[slot[h]] : ui;
-#pragma unroll
-                    for (int h = 0; h < 2; h++)
-                        keep[h] = slot[h] >= 0 && slot[h] != t && fixed_dist2(ui, uj[h], sd.Lq) < rl2;
-#pragma unroll
-                    for (int h = 0; h < 2; h++) {  // candidate order: the first 32, then the next 32
-                        unsigned mask = __ballot_sync(0xffffffffu, keep[h]);
-                        if (keep[h]) {
-                            int pos = count + __popc(mask & ((1u << lane) - 1u));
-                            if (pos < b.maxnb) out[pos] = slot[h];
+                        for (int h = 0; h < 4; h++) {
+                            int q = base + 32 * h + lane;
+                            slot[h] = q < total ? stencil_slot(s_lo[wib], s_pre[wib], nruns, q) : -1;
                         }
-                        count += __popc(mask);
+#pragma unroll
+                        for (int h = 0; h < 4; h++) uj[h] = slot[h] >= 0 ? b.posfx[slot[h]] : ua;
+                        for (int k = 0; k < na; k++) {
+                            uint4 ui;
+                            ui.x = __shfl_sync(0xffffffffu, ua.x, k);
+                            ui.y = __shfl_sync(0xffffffffu, ua.y, k);
+                            ui.z = __shfl_sync(0xffffffffu, ua.z, k);
+                            const int t = a0 + k;
+                            int at = __shfl_sync(0xffffffffu, count, k);
+#pragma unroll
+                            for (int h = 0; h < 4; h++) {  // candidate order: chunk by chunk
+                                if (base + 32 * h >= total) break;  // (the same in every lane)
+                                bool keep = slot[h] >= 0 && slot[h] != t && fixed_dist2(ui, uj[h], sd.Lq) < rl2;
+                                unsigned mask = __ballot_sync(0xffffffffu, keep);
+                                if (keep) {
+                                    int pos = at + __popc(mask & below);
+                                    if (pos < b.maxnb) b.nbr[(size_t)t * b.maxnb + pos] = slot[h];
+                                }
+                                at += __popc(mask);
+                            }
+                            if (lane == k) count = at;
+                        }
                     }
-                }
-                if (lane == 0) {
-                    b.nnb[t] = min(count, b.maxnb);
-                    if (count > b.maxnb) {
-                        atomicOr(b.status, ST_OVERFLOW);
-                        a.group_flag[g] = 1;
+                    if (lane < na) {
+                        b.nnb[a0 + lane] = min(count, b.maxnb);
+                        if (count > b.maxnb) {
+                            atomicOr(b.status, ST_OVERFLOW);
+                            a.group_flag[g] = 1;
+                        }
                     }
                 }
             }

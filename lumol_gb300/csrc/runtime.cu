@@ -417,6 +417,8 @@ bool persist_eligible(const lg_engine* e) {
 // per block is smallest.  A system's arithmetic does not depend on its group.
 int persist_plan(lg_engine* e) {
     e->pk_cluster = -1;
+    for (auto& g : e->pk_graphs) cudaGraphExecDestroy(g.second);  // (they hold the old groups)
+    e->pk_graphs.clear();
     const Batch& b = e->b;
     int nsys = e->nsys;
     // work of a system: its neighbour-list entries (measured when the lists
@@ -479,7 +481,15 @@ int persist_plan(lg_engine* e) {
     std::vector<int> off(1, 0), sys;
     for (auto& bin : best_bins) {
         if (bin.empty()) continue;
-        std::sort(bin.begin(), bin.end());
+        // the force phase hands out chunks in group order: the systems with the
+        // most work per atom first, so the last chunks, whose length sets the
+        // wait at the closing barrier, are the cheapest (a system's results do
+        // not depend on its place in the group)
+        std::stable_sort(bin.begin(), bin.end(), [&](int x, int y) {
+            double wx = work[x] / (double)std::max<int64_t>(1, e->sys[x].n);
+            double wy = work[y] / (double)std::max<int64_t>(1, e->sys[y].n);
+            return wx > wy;
+        });
         sys.insert(sys.end(), bin.begin(), bin.end());
         off.push_back((int)sys.size());
     }
