@@ -621,12 +621,7 @@ int md_run_steps(lg_engine* e, int64_t nsteps, const std::function<int()>& tail)
             int rc = persist_plan(e);
             if (rc) return rc;
         }
-        if (e->pk_cluster > 0) {
-            int rc = md_run_persistent(e, nsteps, thermo);
-            if (rc == LG_OK && tail) rc = tail();
-            if (rc == LG_OK && tail) CUDA_TRY(e, cudaStreamSynchronize(st));
-            return rc;
-        }
+        if (e->pk_cluster > 0) return md_run_persistent(e, nsteps, thermo, tail);
     }
     DBuf<double4_32a>& cp_pos = e->cp_pos;
     DBuf<double4_32a>& cp_vel = e->cp_vel;

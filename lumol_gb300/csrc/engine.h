@@ -26,6 +26,7 @@
 #include <mutex>
 #include <tuple>
 #include <string>
+#include <functional>
 #include <vector>
 
 #include "../../include/lumol_gb300.h"
@@ -312,7 +313,7 @@ void enqueue_md_finish(lg_engine* e, int mode, cudaStream_t st);
 bool persist_batch(const lg_engine* e);
 bool persist_eligible(const lg_engine* e);
 int persist_plan(lg_engine* e);
-int md_run_persistent(lg_engine* e, int64_t nsteps, bool thermo);
+int md_run_persistent(lg_engine* e, int64_t nsteps, bool thermo, const std::function<int()>& tail);
 // lg_md_run of a batch with a barostat system: one step at a time, the cell
 // of every barostat system changed between steps from the pressure of the
 // previous one (one host synchronisation per step).

@@ -517,12 +517,17 @@ int persist_plan(lg_engine* e) {
 
 // lg_md_run on the persistent kernel: one launch per chunk, with the same
 // checkpoint / regrow / replay on a list overflow as the per-step path.
-int md_run_persistent(lg_engine* e, int64_t nsteps, bool thermo) {
+int md_run_persistent(lg_engine* e, int64_t nsteps, bool thermo, const std::function<int()>& tail) {
     const int chunk = 32;
     cudaStream_t st = e->stream;
     int64_t done = 0;
     int retries = 0;
     size_t bytes = e->b.n * sizeof(double4_32a);
+    if (nsteps == 0 && tail) {
+        int rc = tail();
+        if (rc) return rc;
+        CUDA_TRY(e, cudaStreamSynchronize(st));
+    }
     while (done < nsteps) {
         int steps = (int)std::min<int64_t>(chunk, nsteps - done);
         int key = 2 * steps + (thermo ? 1 : 0);
@@ -546,6 +551,12 @@ int md_run_persistent(lg_engine* e, int64_t nsteps, bool thermo) {
         }
         CUDA_TRY(e, cudaGraphLaunch(it->second, st));
         e->launches += 1;
+        // the caller's download of the last chunk goes before the status read, so
+        // one wait covers both (a replayed chunk enqueues it again)
+        if (done + steps == nsteps && tail) {
+            int rc = tail();
+            if (rc) return rc;
+        }
         uint32_t status;
         int rc = read_status(e, &status);
         if (rc) return rc;
