@@ -60,8 +60,8 @@ def parse():
     p.add_argument("--replicas", type=int, default=256, help="lj_batch: replicas (half MD, half MC)")
     p.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     p.add_argument("--cells", type=int, default=0, help="lattice cells per side (0: the workload's size)")
-    p.add_argument("--chunk", type=int, default=32,
-                   help="MD steps per timed iteration (one lg_md_run call; one persistent launch up to 32)")
+    p.add_argument("--chunk", type=int, default=256,
+                   help="MD steps per timed iteration (one lg_md_run call; one persistent launch up to 256)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-roofline", action="store_true")
@@ -207,6 +207,10 @@ def count_kvectors(lengths, kmax):
                     if k2 <= kmax2:
                         n += 1
     return n
+
+
+# MD steps a serving lane runs between admissions
+SERVING_CHUNK = 64
 
 
 def traffic_from_profiles(kernel: str):
@@ -566,10 +570,10 @@ def main_serving(args, world, rank, local):
     requests = workloads.serving_requests(count=args.requests, rate=args.rate, seed=77 + rank,
                                           precision=args.precision)
     warm = workloads.serving_requests(count=4, rate=1000.0, seed=1, precision=args.precision, scale=0.02)
-    server = Server(precision=args.precision, chunk=max(16, args.chunk) * 2, max_lanes=4)
+    server = Server(precision=args.precision, chunk=SERVING_CHUNK, max_lanes=4)
     server.run(warm)
     server.close()
-    server = Server(precision=args.precision, chunk=max(16, args.chunk) * 2, max_lanes=4)
+    server = Server(precision=args.precision, chunk=SERVING_CHUNK, max_lanes=4)
     barrier(world)
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
@@ -742,24 +746,27 @@ def batch_roofline(args, md, C):
     cluster, groups = ctypes.c_int32(), ctypes.c_int32()
     md.engine.call("lg_md_plan", ctypes.byref(cluster), ctypes.byref(groups))
     if cluster.value > 0:
-        # the persistent kernel runs the whole step: time one launch of 32 steps
-        # with CUDA events on the engine's stream (state advances, as in a run)
+        # the persistent kernel runs the whole step: time launches of the timed
+        # iteration's length (up to 256 steps, one launch) with CUDA events on
+        # the engine's stream (state advances, as in a run)
         import torch
         ptr = ctypes.c_void_p()
         md.engine.call("lg_get_stream", ctypes.byref(ptr))
         st = torch.cuda.ExternalStream(ptr.value)
-        md.md_run(32)
+        nst = max(8, min(args.chunk, args.steps, 256))
+        md.md_run(nst)
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
         for e0, e1 in ev:
             e0.record(st)
-            md.md_run(32)
+            md.md_run(nst)
             e1.record(st)
         torch.cuda.synchronize()
         ms = min(e0.elapsed_time(e1) for e0, e1 in ev)
-        achieved = flops * 32 / (ms * 1e-3) / 1e12
+        achieved = flops * nst / (ms * 1e-3) / 1e12
+        per_step = traffic_from_profiles("md_persist_kernel_lj_batch256_per_step")
         return {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
-                "frac": achieved / peak.value, "traffic": traffic_from_profiles("md_persist_kernel_lj_batch256"),
-                "kernel": "md_persist_kernel", "kernel_ms": ms, "steps_per_launch": 32,
+                "frac": achieved / peak.value, "traffic": per_step * nst if per_step else None,
+                "kernel": "md_persist_kernel", "kernel_ms": ms, "steps_per_launch": nst,
                 "cluster": cluster.value, "groups": groups.value,
                 "includes": "whole MD steps: integration, list rebuilds, forces, thermostat",
                 "peak_source": peak_source, "kernel_ms_by_group": times,

@@ -411,10 +411,53 @@ bool persist_eligible(const lg_engine* e) {
     return persist_batch(e) && (t == 2 || t == 4 || t == 8);
 }
 
-// Packs the systems into groups of about equal work (atoms times the expected
-// neighbour count; longest first, each to the least loaded group) for each
-// cluster size the device can hold, and keeps the size whose largest group
-// per block is smallest.  A system's arithmetic does not depend on its group.
+// Packs the systems into groups of about equal work for each cluster size the
+// device can hold (longest first, each to the least loaded group, then single
+// moves and pairwise swaps out of the most loaded group while they lower it),
+// and keeps the size whose largest group per block is smallest.  A system's
+// arithmetic does not depend on its group.
+// Lowers the most loaded group while a move of one of its systems to another
+// group, or a swap with a lighter system of another group, makes both loads
+// smaller than its load (the best such change first).
+static void refine_bins(std::vector<std::vector<int>>& bins, std::vector<double>& load,
+                        const std::vector<double>& work) {
+    const int G = (int)bins.size();
+    for (int iter = 0; iter < 512; iter++) {
+        int gm = (int)(std::max_element(load.begin(), load.end()) - load.begin());
+        double best = load[gm];
+        int bg = -1, ba = -1, bb = -1;  // group, index in gm, index in group (-1: a move)
+        for (int g = 0; g < G; g++) {
+            if (g == gm) continue;
+            for (int x = 0; x < (int)bins[gm].size(); x++) {
+                double wa = work[bins[gm][x]];
+                if ((int)bins[g].size() < PK_MAXG) {
+                    double m = std::max(load[gm] - wa, load[g] + wa);
+                    if (m < best * (1.0 - 1e-9)) best = m, bg = g, ba = x, bb = -1;
+                }
+                for (int y = 0; y < (int)bins[g].size(); y++) {
+                    double d = wa - work[bins[g][y]];
+                    if (d <= 0.0) continue;
+                    double m = std::max(load[gm] - d, load[g] + d);
+                    if (m < best * (1.0 - 1e-9)) best = m, bg = g, ba = x, bb = y;
+                }
+            }
+        }
+        if (bg < 0) return;
+        int a = bins[gm][ba];
+        bins[gm].erase(bins[gm].begin() + ba);
+        load[gm] -= work[a];
+        if (bb >= 0) {
+            int c = bins[bg][bb];
+            bins[bg].erase(bins[bg].begin() + bb);
+            load[bg] -= work[c];
+            bins[gm].push_back(c);
+            load[gm] += work[c];
+        }
+        bins[bg].push_back(a);
+        load[bg] += work[a];
+    }
+}
+
 int persist_plan(lg_engine* e) {
     e->pk_cluster = -1;
     for (auto& g : e->pk_graphs) cudaGraphExecDestroy(g.second);  // (they hold the old groups)
@@ -422,7 +465,10 @@ int persist_plan(lg_engine* e) {
     const Batch& b = e->b;
     int nsys = e->nsys;
     // work of a system: its neighbour-list entries (measured when the lists
-    // exist, else estimated from the density) plus a per-atom share
+    // exist, else estimated from the density) plus a per-atom share.  The
+    // share is fitted to the per-cluster times of the first-half and force
+    // phases on batched LJ replicas: an atom costs about as much as 32 list
+    // entries (its FP64 integration, its chunk's epilogue and lane padding)
     std::vector<int> h_nnb(b.n);
     CUDA_TRY(e, cudaMemcpy(h_nnb.data(), e->nnb.p, (size_t)b.n * sizeof(int), cudaMemcpyDeviceToHost));
     std::vector<double> work(nsys);
@@ -433,7 +479,7 @@ int persist_plan(lg_engine* e) {
         double entries = 0.0;
         for (int64_t i = e->begin[s]; i < e->begin[s + 1]; i++) entries += h_nnb[i];
         if (entries == 0.0) entries = (double)h.n * (double)h.n / V * 4.0 / 3.0 * PI * rl * rl * rl;
-        work[s] = entries + 8.0 * (double)h.n;
+        work[s] = entries + 32.0 * (double)h.n;
     }
     std::vector<int> order(nsys);
     for (int s = 0; s < nsys; s++) order[s] = s;
@@ -456,6 +502,7 @@ int persist_plan(lg_engine* e) {
             bins[pick].push_back(s);
             load[pick] += work[s];
         }
+        refine_bins(bins, load, work);
         double waves = std::ceil((double)G / (double)gmax);
         double t = *std::max_element(load.begin(), load.end()) / C * waves;
         if (best_c == 0 || t < 0.97 * best_t) {
@@ -517,8 +564,15 @@ int persist_plan(lg_engine* e) {
 
 // lg_md_run on the persistent kernel: one launch per chunk, with the same
 // checkpoint / regrow / replay on a list overflow as the per-step path.
+// Steps per persistent launch at most.  A launch ends when its slowest cluster
+// does, and a cluster's list rebuilds (about 130 us each on the 128-replica
+// batch) fall on random steps, so longer launches average them out: 32, 64,
+// 128 and 256 steps a launch measured 98.5, 94.9, 93.3 and 92.6 us a step.
+// An overflowing list replays the launch from its checkpoint.
+constexpr int PK_MAX_STEPS = 256;
+
 int md_run_persistent(lg_engine* e, int64_t nsteps, bool thermo, const std::function<int()>& tail) {
-    const int chunk = 32;
+    const int chunk = PK_MAX_STEPS;
     cudaStream_t st = e->stream;
     int64_t done = 0;
     int retries = 0;

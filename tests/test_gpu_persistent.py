@@ -38,8 +38,8 @@ def run(persistent, thermostats, calls):
     for k in calls:
         before = launches(batch)
         batch.md_run(k)
-        if persistent and k >= 8:  # one launch per run of up to 32 steps (shorter runs: per-step kernels)
-            assert launches(batch) - before == (k + 31) // 32
+        if persistent and k >= 8:  # one launch per run of up to 256 steps (shorter runs: per-step kernels)
+            assert launches(batch) - before == (k + 255) // 256
     out = [batch.state(s) for s in range(len(systems))]
     batch.engine.close()
     return out
@@ -48,7 +48,7 @@ def run(persistent, thermostats, calls):
 @pytest.mark.parametrize("thermo", [False, True])
 def test_persistent_matches_per_step_kernels(thermo):
     thermostats = [(t, 100.0) if (thermo and k % 2 == 0) else None for k, (n, rho, t) in enumerate(PARAMS)]
-    calls = [1, 40, 7, 32]  # run lengths across and inside the 32-step launches
+    calls = [1, 40, 7, 300]  # run lengths across and inside the 256-step launches
     a = run(True, thermostats, calls)
     b = run(False, thermostats, calls)
     for (pa, va), (pb, vb) in zip(a, b):

@@ -44,7 +44,7 @@ def test_served_results_equal_alone_results():
 def test_served_mixed_results_are_alone_results_bit_for_bit():
     """Mixed precision, pair-potential requests: the server runs its lanes in
     chunks of 20 steps through the persistent kernel, a request alone runs in
-    launches of 32 steps; every step's arithmetic is the same in both, so the
+    launches of up to 256 steps; every step's arithmetic is the same in both, so the
     trajectories are equal bit for bit."""
     requests = [r for r in workloads.serving_requests(count=16, rate=200.0, seed=6, precision="mixed",
                                                       scale=0.03) if r.kind == "lj"]
