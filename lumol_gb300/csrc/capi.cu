@@ -44,6 +44,7 @@ int lg_create(const lg_options* options, int32_t n_systems, lg_engine** out) {
     e->carry_from.assign(n_systems, -1);
     ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
     if (ce == cudaSuccess) ce = cudaMallocHost((void**)&e->h_status, sizeof(uint32_t));
+    if (ce == cudaSuccess) ce = cudaHostGetDevicePointer((void**)&e->d_h_status, e->h_status, 0);
     if (ce != cudaSuccess) {
         delete e;
         return fail(nullptr, LG_ERR_CUDA, cudaGetErrorString(ce));
@@ -781,6 +782,7 @@ int lg_md_propagate(lg_engine* e, double* positions, double* velocities, int64_t
         e->shadow_n3 = 0;
         e->shadow_valid = false;
         CUDA_TRY(e, cudaMallocHost((void**)&e->h_shadow, std::max<size_t>(2 * n3, 1) * sizeof(double)));
+        CUDA_TRY(e, cudaHostGetDevicePointer((void**)&e->d_shadow, e->h_shadow, 0));
         e->shadow_n3 = n3;
     }
     double* sp = e->h_shadow;
@@ -800,7 +802,8 @@ int lg_md_propagate(lg_engine* e, double* positions, double* velocities, int64_t
     e->shadow_valid = true;
     const bool download = (flags & LG_SYNC_DOWNLOAD) && n > 0;
     std::function<int()> tail;
-    if (download) tail = [e, n, sp, sv]() { return get_state(e, 0, n, sp, sv); };
+    double* dsp = e->d_shadow;  // (mapped once: no pointer query per call)
+    if (download) tail = [e, n, dsp, n3]() { return get_state_mapped(e, 0, n, dsp, dsp + n3); };
     rc = md_run_checked(e, nsteps, tail);
     if (rc != LG_OK && rc != LG_ERR_NONFINITE) {
         e->shadow_valid = false;

@@ -185,6 +185,7 @@ struct lg_engine {
     DBuf<int> pairs_out;
     DBuf<unsigned long long> pairs_count;
     uint32_t* h_status = nullptr;  // pinned
+    uint32_t* d_h_status = nullptr;  // h_status as kernels address it
     double* h_out = nullptr;       // pinned, nsys * RED_STRIDE
     size_t h_out_cap = 0;          // systems h_out holds
     std::vector<SysDev> h_sysdev;
@@ -196,6 +197,7 @@ struct lg_engine {
     // the host and the engine last exchanged (pinned, 3n + 3n doubles), valid
     // while no other call has written the device state since.
     double* h_shadow = nullptr;
+    double* d_shadow = nullptr;  // h_shadow as kernels address it
     size_t shadow_n3 = 0;
     bool shadow_valid = false;
     uint64_t state_gen = 0;  // completed lg_md_run calls (a generation counter of the device state)
@@ -303,6 +305,8 @@ int compute_batch(lg_engine* e, uint32_t terms, uint32_t want, double* d_force_o
 const void* mapped_host(const void* p);
 int put_state(lg_engine* e, int64_t base, int64_t n, const double* positions, const double* velocities);
 int get_state(lg_engine* e, int64_t base, int64_t n, double* positions, double* velocities);
+// get_state into page-locked host buffers given by their device addresses
+int get_state_mapped(lg_engine* e, int64_t base, int64_t n, double* dp, double* dv);
 int upload_positions(lg_engine* e, int32_t s, const double* positions);
 int autotune(lg_engine* e);
 // What the MD steps of a batch need besides the integrators (md_mode bits).

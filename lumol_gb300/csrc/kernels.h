@@ -141,6 +141,8 @@ void launch_pack_velocities(const Batch& b, const double* vel3, cudaStream_t st)
 void launch_unpack_velocities(const Batch& b, double* vel3, cudaStream_t st);
 // Positions and velocities of atoms [0, b.n) into 3n arrays, in one launch.
 void launch_unpack_state(const Batch& b, double* pos3, double* vel3, cudaStream_t st);
+// *status into page-locked host memory (dst: its device address)
+void launch_status_copy(const uint32_t* status, uint32_t* dst, cudaStream_t st);
 constexpr int VV_TILE = 256;
 void launch_md_first(const Batch& b, bool adjust, cudaStream_t st);
 void launch_md_second(const Batch& b, cudaStream_t st);

@@ -67,6 +67,11 @@ __global__ void unpack_state_kernel(int n3, const double* __restrict__ pos4, con
     pos3[t] = pos4[c];
     vel3[t] = vel4[c];
 }
+__global__ void status_copy_kernel(const uint32_t* __restrict__ src, uint32_t* dst) { *dst = *src; }
+void launch_status_copy(const uint32_t* status, uint32_t* dst, cudaStream_t st) {
+    status_copy_kernel<<<1, 1, 0, st>>>(status, dst);
+}
+
 void launch_unpack_state(const Batch& b, double* pos3, double* vel3, cudaStream_t st) {
     if (b.n)
         unpack_state_kernel<<<(3 * b.n + 255) / 256, 256, 0, st>>>(3 * b.n, reinterpret_cast<const double*>(b.posq),

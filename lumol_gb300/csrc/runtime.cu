@@ -199,6 +199,16 @@ int put_state(lg_engine* e, int64_t base, int64_t n, const double* positions, co
 // The packed device state of atoms [base, base + n) into host positions and
 // velocities (either may be null): written in place into page-locked buffers,
 // else staged through pos3 / vel3.
+int get_state_mapped(lg_engine* e, int64_t base, int64_t n, double* dp, double* dv) {
+    Batch sub = e->b;
+    sub.n = (int)n;
+    sub.posq = e->posq.p + base;
+    sub.vel = e->vel.p + base;
+    launch_unpack_state(sub, dp, dv, e->stream);
+    e->launches += n ? 1 : 0;
+    return LG_OK;
+}
+
 int get_state(lg_engine* e, int64_t base, int64_t n, double* positions, double* velocities) {
     cudaStream_t st = e->stream;
     Batch sub = e->b;
@@ -593,6 +603,11 @@ int md_run_persistent(lg_engine* e, int64_t nsteps, bool thermo, const std::func
             PkArgs a{e->pk_groups, e->pk_group_off.p, e->pk_group_sys.p, e->pk_group_flag.p, e->pk_ke.p, steps,
                      thermo ? 1 : 0, e->pk_stage, e->cp_pos.p, e->cp_vel.p, e->cp_acc.p};
             cudaError_t le = launch_md_persist(e->b, a, e->pk_cluster, st);
+            // the status word reaches the host inside the graph (no copy call per launch)
+            if (le == cudaSuccess) {
+                launch_status_copy(e->status.p, e->d_h_status, st);
+                le = cudaGetLastError();
+            }
             cudaError_t ce = cudaStreamEndCapture(st, &g);
             if (le != cudaSuccess) return fail(e, LG_ERR_CUDA, std::string("persistent launch: ") + cudaGetErrorString(le));
             if (ce != cudaSuccess) return fail(e, LG_ERR_CUDA, std::string("stream capture: ") + cudaGetErrorString(ce));
@@ -604,16 +619,17 @@ int md_run_persistent(lg_engine* e, int64_t nsteps, bool thermo, const std::func
             it = e->pk_graphs.emplace(key, exec).first;
         }
         CUDA_TRY(e, cudaGraphLaunch(it->second, st));
-        e->launches += 1;
-        // the caller's download of the last chunk goes before the status read, so
-        // one wait covers both (a replayed chunk enqueues it again)
+        e->launches += 2;
+        // the caller's download of the last chunk goes before the wait, so one
+        // wait covers the launch, its status word and the download (a replayed
+        // chunk enqueues the download again)
         if (done + steps == nsteps && tail) {
             int rc = tail();
             if (rc) return rc;
         }
-        uint32_t status;
-        int rc = read_status(e, &status);
-        if (rc) return rc;
+        CUDA_TRY(e, cudaStreamSynchronize(st));
+        uint32_t status = *(volatile const uint32_t*)e->h_status;
+        int rc = LG_OK;
         if (status & (ST_OVERFLOW | ST_CELL_OVF)) {
             if (++retries > 4) return fail(e, LG_ERR_CAPACITY, "neighbour list overflow persisted after regrowing");
             CUDA_TRY(e, cudaMemcpyAsync(e->posq.p, e->cp_pos.p, bytes, cudaMemcpyDeviceToDevice, st));

@@ -38,8 +38,9 @@ def run(persistent, thermostats, calls):
     for k in calls:
         before = launches(batch)
         batch.md_run(k)
-        if persistent and k >= 8:  # one launch per run of up to 256 steps (shorter runs: per-step kernels)
-            assert launches(batch) - before == (k + 255) // 256
+        if persistent and k >= 8:  # one launch per run of up to 256 steps (shorter runs: per-step
+            # kernels), each with the one-thread kernel that hands the status word to the host
+            assert launches(batch) - before == 2 * ((k + 255) // 256)
     out = [batch.state(s) for s in range(len(systems))]
     batch.engine.close()
     return out
