@@ -546,7 +546,8 @@ cudaError_t launch_persist_tpa(const Batch& b, const PkArgs& a, int cluster, cud
 
 cudaError_t launch_md_persist(const Batch& b, const PkArgs& a, int cluster, cudaStream_t st) {
     if (a.ngroups == 0 || a.nsteps == 0) return cudaSuccess;
-    switch (b.tpa) {  // (persistent runs need the per-step kernel's group size: 2, 4 or 8)
+    switch (b.tpa) {  // (persistent runs need the per-step kernel's group size: 1, 2, 4 or 8)
+        case 1: return launch_persist_tpa<1>(b, a, cluster, st);
         case 2: return launch_persist_tpa<2>(b, a, cluster, st);
         case 4: return launch_persist_tpa<4>(b, a, cluster, st);
         case 8: return launch_persist_tpa<8>(b, a, cluster, st);
@@ -583,7 +584,7 @@ int max_clusters_tpa(int cluster, int stage_atoms) {
 
 int persist_max_clusters(int tpa, int cluster, int stage_atoms) {
     switch (tpa) {
-        case 1:
+        case 1: return max_clusters_tpa<1>(cluster, stage_atoms);
         case 2: return max_clusters_tpa<2>(cluster, stage_atoms);
         case 4: return max_clusters_tpa<4>(cluster, stage_atoms);
         default: return max_clusters_tpa<8>(cluster, stage_atoms);

@@ -261,8 +261,54 @@ int upload_positions(lg_engine* e, int32_t s, const double* positions) {
     return LG_OK;
 }
 
-// The autotuner: times the pair kernel at every threads-per-atom width (2, 4
-// and 8 for a batch the persistent kernel runs) and the
+// Threads per atom for a batch the persistent kernel runs, from launches of the
+// persistent kernel itself (the per-step pair kernel ranks the widths
+// differently: the persistent force phase pays a tail of one chunk and an
+// epilogue per chunk, and 2 and 4 threads per atom timed alike there while the
+// persistent kernel ran 16 % faster at 2).  Each width runs a warm-up and a
+// timed launch of 16 steps from the current state, which every launch's own
+// checkpoint restores afterwards; the lists the trials built stay valid for
+// the restored positions (the rebuild test is relative to each list's build
+// positions).
+static int tune_persistent(lg_engine* e, cudaEvent_t e0, cudaEvent_t e1) {
+    cudaStream_t st = e->stream;
+    const bool thermo = (md_mode(e) & MD_ADJUST) != 0;
+    const size_t bytes = (size_t)e->b.n * sizeof(double4_32a);
+    const int tpas[4] = {1, 2, 4, 8};
+    int best_tpa = e->b.tpa;
+    float best_t = 1e30f;
+    for (int t : tpas) {
+        e->b.tpa = t;
+        int rc = persist_plan(e);
+        if (rc) return rc;
+        if (e->pk_cluster <= 0) continue;
+        float ms = 0.f;
+        for (int r = 0; r < 2; r++) {
+            CUDA_TRY(e, cudaEventRecord(e0, st));
+            rc = md_run_persistent(e, 16, thermo, {});
+            CUDA_TRY(e, cudaEventRecord(e1, st));
+            CUDA_TRY(e, cudaEventSynchronize(e1));
+            CUDA_TRY(e, cudaEventElapsedTime(&ms, e0, e1));
+            // (the launch's first step wrote the checkpoint)
+            CUDA_TRY(e, cudaMemcpyAsync(e->posq.p, e->cp_pos.p, bytes, cudaMemcpyDeviceToDevice, st));
+            CUDA_TRY(e, cudaMemcpyAsync(e->vel.p, e->cp_vel.p, bytes, cudaMemcpyDeviceToDevice, st));
+            CUDA_TRY(e, cudaMemcpyAsync(e->acc.p, e->cp_acc.p, bytes, cudaMemcpyDeviceToDevice, st));
+            if (rc) return rc;
+        }
+        if (ms < best_t) {
+            best_t = ms;
+            best_tpa = t;
+        }
+    }
+    CUDA_TRY(e, cudaStreamSynchronize(st));
+    e->nonfinite = false;
+    e->b.tpa = best_tpa;
+    e->pk_cluster = 0;  // planned again for the chosen width at the next run
+    return LG_OK;
+}
+
+// The autotuner: times the pair kernel at every threads-per-atom width (for a
+// batch the persistent kernel runs: the persistent kernel's launches) and the
 // Ewald field kernel at several chunk lengths on the current batch and list,
 // keeps the fastest, and caches the choice for this workload shape.
 int autotune(lg_engine* e) {
@@ -306,23 +352,29 @@ int autotune(lg_engine* e) {
         }
         return best;
     };
-    // (a batch for the persistent kernel: the group sizes it runs)
-    const int tpas_all[6] = {1, 2, 4, 8, 16, 32}, tpas_persist[3] = {2, 4, 8};
     const bool pb = std::get<5>(key);
-    const int* tpas = pb ? tpas_persist : tpas_all;
-    const int ntpas = pb ? 3 : 6;
-    int best_tpa = b.tpa;
-    float best_t = 1e30f;
-    for (int k = 0; k < ntpas; k++) {
-        int t = tpas[k];
-        b.tpa = t;
-        float ms = time_it([&] { launch_pair_forces(b, LG_TERM_ALL, false, st); });
-        if (ms < best_t) {
-            best_t = ms;
-            best_tpa = t;
+    if (pb) {
+        int rc = tune_persistent(e, e0, e1);
+        if (rc) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return rc;
         }
+    } else {
+        const int tpas[6] = {1, 2, 4, 8, 16, 32};
+        int best_tpa = b.tpa;
+        float best_t = 1e30f;
+        for (int t : tpas) {
+            b.tpa = t;
+            float ms = time_it([&] { launch_pair_forces(b, LG_TERM_ALL, false, st); });
+            if (ms < best_t) {
+                best_t = ms;
+                best_tpa = t;
+            }
+        }
+        b.tpa = best_tpa;
     }
-    b.tpa = best_tpa;
+    float best_t = 1e30f;
     if (b.nkvec) {
         launch_kspace_part(b, 0, false, st);
         launch_kspace_part(b, 1, false, st);
@@ -418,14 +470,9 @@ bool persist_batch(const lg_engine* e) {
 }
 bool persist_eligible(const lg_engine* e) {
     int t = e->b.tpa;
-    return persist_batch(e) && (t == 2 || t == 4 || t == 8);
+    return persist_batch(e) && (t == 1 || t == 2 || t == 4 || t == 8);
 }
 
-// Packs the systems into groups of about equal work for each cluster size the
-// device can hold (longest first, each to the least loaded group, then single
-// moves and pairwise swaps out of the most loaded group while they lower it),
-// and keeps the size whose largest group per block is smallest.  A system's
-// arithmetic does not depend on its group.
 // Lowers the most loaded group while a move of one of its systems to another
 // group, or a swap with a lighter system of another group, makes both loads
 // smaller than its load (the best such change first).
@@ -468,6 +515,11 @@ static void refine_bins(std::vector<std::vector<int>>& bins, std::vector<double>
     }
 }
 
+// Packs the systems into groups of about equal work for each cluster size the
+// device can hold (longest first, each to the least loaded group, then single
+// moves and pairwise swaps out of the most loaded group while they lower it),
+// and keeps the size whose largest group per block is smallest.  A system's
+// arithmetic does not depend on its group.
 int persist_plan(lg_engine* e) {
     e->pk_cluster = -1;
     for (auto& g : e->pk_graphs) cudaGraphExecDestroy(g.second);  // (they hold the old groups)

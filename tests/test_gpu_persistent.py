@@ -30,10 +30,10 @@ def launches(batch):
     return count.value
 
 
-def run(persistent, thermostats, calls):
-    """Both paths with 4 threads per atom, so every force sum runs in the same order."""
+def run(persistent, thermostats, calls, tpa=4):
+    """Both paths with the same threads per atom, so every force sum runs in the same order."""
     systems = replicas()
-    batch = Batch(systems, precision="mixed", persistent=persistent, threads_per_atom=4)
+    batch = Batch(systems, precision="mixed", persistent=persistent, threads_per_atom=tpa)
     batch.md_setup([1.0] * len(systems), thermostats)
     for k in calls:
         before = launches(batch)
@@ -46,12 +46,12 @@ def run(persistent, thermostats, calls):
     return out
 
 
-@pytest.mark.parametrize("thermo", [False, True])
-def test_persistent_matches_per_step_kernels(thermo):
+@pytest.mark.parametrize("thermo,tpa", [(False, 4), (True, 4), (True, 1), (True, 2)])
+def test_persistent_matches_per_step_kernels(thermo, tpa):
     thermostats = [(t, 100.0) if (thermo and k % 2 == 0) else None for k, (n, rho, t) in enumerate(PARAMS)]
     calls = [1, 40, 7, 300]  # run lengths across and inside the 256-step launches
-    a = run(True, thermostats, calls)
-    b = run(False, thermostats, calls)
+    a = run(True, thermostats, calls, tpa)
+    b = run(False, thermostats, calls, tpa)
     for (pa, va), (pb, vb) in zip(a, b):
         assert np.array_equal(pa, pb) and np.array_equal(va, vb)
 
@@ -189,3 +189,29 @@ def test_pinned_host_buffers_match_pageable():
     a, b = go(True), go(False)
     for x, y in zip(a, b):
         assert np.array_equal(x, y)
+
+
+def test_autotuned_width_keeps_the_state():
+    """A persistent batch without a fixed group size is tuned on trial launches
+    of the persistent kernel (1, 2, 4 and 8 threads per atom), each undone from
+    the launch's own checkpoint: a zero-step run (which tunes) leaves the
+    positions and velocities bit for bit as they were, and the tuned runs stay
+    finite and planned on the persistent kernel.  (An atom count no other test
+    uses, so the tuning is not taken from the cache.)"""
+    params = [(333, 0.6, 150.0), (1201, 0.8, 110.0), (77, 0.5, 200.0)]
+    systems = [workloads.lj_replica(n, rho, t, 900 + k, "mixed") for k, (n, rho, t) in enumerate(params)]
+    batch = Batch(systems, precision="mixed")
+    batch.md_setup([1.0] * len(systems), [(t, 100.0) for _, _, t in params])
+    before = [batch.state(s) for s in range(len(systems))]
+    batch.md_run(0)
+    after = [batch.state(s) for s in range(len(systems))]
+    for (pa, va), (pb, vb) in zip(before, after):
+        assert np.array_equal(pa, pb) and np.array_equal(va, vb)
+    batch.md_run(40)
+    cluster, groups = ctypes.c_int32(), ctypes.c_int32()
+    batch.engine.call("lg_md_plan", ctypes.byref(cluster), ctypes.byref(groups))
+    assert cluster.value > 0 and groups.value > 0
+    for s in range(len(systems)):
+        p, v = batch.state(s)
+        assert np.all(np.isfinite(p)) and np.all(np.isfinite(v))
+    batch.engine.close()
