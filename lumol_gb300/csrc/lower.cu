@@ -1068,6 +1068,11 @@ int commit(lg_engine* e) {
     // a triclinic cell's minimum image is in the general kernels only (and
     // keeps its batch off the persistent kernel)
     for (int s = 0; s < nsys; s++) b.pair_general |= e->h_sysdev[s].tric ? 1 : 0;
+    b.lj1 = nsys > 0 ? 1 : 0;
+    for (int s = 0; s < nsys; s++) {
+        const SysDev& d = e->h_sysdev[s];
+        if (d.nk != 1 || d.ptab < 0 || (size_t)d.ptab >= h_ptabf.size() || h_ptabf[d.ptab].type != 2) b.lj1 = 0;
+    }
     b.kvecf = e->kvecf.p;
     b.eikrf = e->eikrf.p;
     b.rhof = e->rhof.p;

@@ -122,7 +122,9 @@ struct MixedAcc {
 
 // One neighbour-list entry of atom i (sorted position tt): pair potential and
 // (GENERAL) restrictions and real-space Coulomb, added to the lane's sums.
-template <bool EV, bool GENERAL>
+// LJ1: a system of one kind with a Lennard-Jones pair (the parameters are
+// ph1 / pq1), known when the kernel is compiled; the arithmetic is the same.
+template <bool EV, bool GENERAL, bool LJ1 = false>
 __device__ __forceinline__ void mixed_entry(
     MixedAcc& A, const SysDev& s, const PairDevF* __restrict__ prow, uint4 pi, float qi, int mi, int i, int tt,
     int js, uint4 pj, int2 kmj, const int* __restrict__ order, const int* __restrict__ spec_off,
@@ -143,14 +145,14 @@ __device__ __forceinline__ void mixed_entry(
     const PairDevF* pp = prow + kmj.x;
     int4 ph;
     float4 pq;
-    if (single) {
+    if (LJ1 || single) {
         ph = ph1;
         pq = pq1;
     } else {
         ph = __ldg(reinterpret_cast<const int4*>(pp));
         pq = __ldg(reinterpret_cast<const float4*>(pp) + 1);
     }
-    bool pin = pairs && ph.x != 0 && r2 < pq.w;
+    bool pin = pairs && (LJ1 || ph.x != 0) && r2 < pq.w;
     bool cin = GENERAL && coul && qj != 0.0f && r2 <= coul_rc2;
     if (!(pin || cin)) return;
     float inv_r = rsqrtf(r2);
@@ -160,7 +162,7 @@ __device__ __forceinline__ void mixed_entry(
     double e_coul_d = 0.0;
     if (!GENERAL) {
         float shift = EV ? __ldg(&pp->shift) : 0.0f;
-        if (ph.x == 2) {  // LJ: c12 / r^12 - c6 / r^6
+        if (LJ1 || ph.x == 2) {  // LJ: c12 / r^12 - c6 / r^6
             float ir6 = rmul(rmul(inv_r2, inv_r2), inv_r2);
             fr = lj_force_r(pq.x, pq.y, ir6, inv_r2);
             if (EV) e_pair = rsub(lj_energy(pq.x, pq.y, ir6), shift);

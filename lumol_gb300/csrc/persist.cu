@@ -73,7 +73,9 @@ __device__ __forceinline__ void pk_lambdas(const Batch& b, const PkArgs& a, cons
 // written before a barrier and cleared after the rebuild's last barrier) and
 // the early exit on a list overflow (a per-group flag read after a barrier)
 // are the same in every block.
-template <int TPA>
+// LJ1: every system has one kind and a Lennard-Jones pair and nothing is
+// staged (a force loop with those branches resolved when it is compiled).
+template <int TPA, bool LJ1>
 __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkArgs a) {
     cg::cluster_group cluster = cg::this_cluster();
     const int C = (int)cluster.num_blocks();
@@ -464,16 +466,16 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
                 walk_row<TPA>(
                     list, cnt, sub,
                     [&](int js, uint4& pj, int2& kmj) {
-                        if (a.stage) {
+                        if (!LJ1 && a.stage) {
                             pj = s_pos[js - off];
                             kmj = make_int2(s_kind[js - off], 0);
                         } else {  // (the neighbour's kind is not needed for one kind)
                             pj = b.posfx[js];
-                            kmj = single ? make_int2(0, 0) : b.km[js];
+                            kmj = (LJ1 || single) ? make_int2(0, 0) : b.km[js];
                         }
                     },
                     [&](int js, const uint4& pj, const int2& kmj) {
-                        mixed_entry<false, false>(acc, sd, prow, pi, 0.0f, kmi.y, i, tt, js, pj, kmj, b.cell_atoms,
+                        mixed_entry<false, false, LJ1>(acc, sd, prow, pi, 0.0f, kmi.y, i, tt, js, pj, kmj, b.cell_atoms,
                                                   nullptr, nullptr, nullptr, true, false, 0.0f, 0.0f, 0.0f, single,
                                                   ph1, pq1, nullptr);
                     });
@@ -525,7 +527,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
 
 size_t persist_smem_bytes(int stage_atoms) { return (size_t)stage_atoms * (sizeof(uint4) + sizeof(int)); }
 
-template <int TPA>
+template <int TPA, bool LJ1>
 cudaError_t launch_persist_tpa(const Batch& b, const PkArgs& a, int cluster, cudaStream_t st) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(a.ngroups * cluster), 1, 1);
@@ -541,7 +543,12 @@ cudaError_t launch_persist_tpa(const Batch& b, const PkArgs& a, int cluster, cud
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, md_persist_kernel<TPA>, b, a);
+    return cudaLaunchKernelEx(&cfg, md_persist_kernel<TPA, LJ1>, b, a);
+}
+template <int TPA>
+cudaError_t launch_persist_tpa(const Batch& b, const PkArgs& a, int cluster, cudaStream_t st) {
+    return b.lj1 && a.stage == 0 ? launch_persist_tpa<TPA, true>(b, a, cluster, st)
+                                 : launch_persist_tpa<TPA, false>(b, a, cluster, st);
 }
 
 cudaError_t launch_md_persist(const Batch& b, const PkArgs& a, int cluster, cudaStream_t st) {
@@ -562,7 +569,7 @@ int max_clusters_tpa(int cluster, int stage_atoms) {
     cfg.blockDim = dim3(PK_THREADS, 1, 1);
     cfg.dynamicSmemBytes = persist_smem_bytes(stage_atoms);
     if (cfg.dynamicSmemBytes > 0 &&
-        cudaFuncSetAttribute(md_persist_kernel<TPA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(md_persist_kernel<TPA, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)cfg.dynamicSmemBytes) != cudaSuccess) {
         cudaGetLastError();
         return 0;
@@ -575,7 +582,8 @@ int max_clusters_tpa(int cluster, int stage_atoms) {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     int count = 0;
-    if (cudaOccupancyMaxActiveClusters(&count, md_persist_kernel<TPA>, &cfg) != cudaSuccess) {
+    // (the one-kind LJ variant has the same registers and static shared memory)
+    if (cudaOccupancyMaxActiveClusters(&count, md_persist_kernel<TPA, false>, &cfg) != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
