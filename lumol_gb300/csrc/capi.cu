@@ -606,10 +606,11 @@ int md_run_steps(lg_engine* e, int64_t nsteps, const std::function<int()>& tail)
         if (rc) return rc;
     }
     // the persistent kernel for runs of several steps: a launch pays for the
-    // slowest group's list rebuild, which short runs do not amortize (a
-    // 1-step launch measured 193 us against 178 us for the per-step kernels
-    // on the 128-replica batch); a batch of a few systems has no such spread,
-    // and one launch per step beats a graph of a dozen kernels
+    // slowest group's list rebuild, which short runs do not amortize (on the
+    // 128-replica batch, per step: 218 / 159 / 122 us for runs of 1 / 2 / 4
+    // steps against 176 / 149 / 134 us on the per-step graph); a batch of a
+    // few systems has no such spread, and one launch per step beats a graph
+    // of a dozen kernels
     for (int s = 0; s < e->nsys; s++)
         if (e->sys[s].barostat != LG_BAROSTAT_NONE) {
             int rc = md_run_barostat(e, nsteps);
@@ -617,7 +618,7 @@ int md_run_steps(lg_engine* e, int64_t nsteps, const std::function<int()>& tail)
             if (rc == LG_OK && tail) CUDA_TRY(e, cudaStreamSynchronize(st));
             return rc;
         }
-    if (persist_eligible(e) && (nsteps >= 8 || e->nsys <= 4)) {
+    if (persist_eligible(e) && (nsteps >= 4 || e->nsys <= 4)) {
         if (e->pk_cluster == 0) {
             int rc = persist_plan(e);
             if (rc) return rc;

@@ -38,7 +38,7 @@ def run(persistent, thermostats, calls, tpa=4):
     for k in calls:
         before = launches(batch)
         batch.md_run(k)
-        if persistent and k >= 8:  # one launch per run of up to 256 steps (shorter runs: per-step
+        if persistent and k >= 4:  # one launch per run of up to 256 steps (shorter runs: per-step
             # kernels), each with the one-thread kernel that hands the status word to the host
             assert launches(batch) - before == 2 * ((k + 255) // 256)
     out = [batch.state(s) for s in range(len(systems))]
