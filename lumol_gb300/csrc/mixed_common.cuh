@@ -154,6 +154,19 @@ __device__ __forceinline__ void mixed_entry(
     }
     bool pin = pairs && (LJ1 || ph.x != 0) && r2 < pq.w;
     bool cin = GENERAL && coul && qj != 0.0f && r2 <= coul_rc2;
+    if (LJ1 && !EV && !GENERAL) {
+        // without a branch: an entry beyond the cutoff adds exact zeros, which
+        // leave the compensated sums as they are (r2 >= rc2 > 0 keeps every
+        // intermediate finite), and the lanes of a warp never diverge here
+        const float inv_r = rsqrtf(r2);
+        const float inv_r2 = rmul(inv_r, inv_r);
+        const float ir6 = rmul(rmul(inv_r2, inv_r2), inv_r2);
+        const float fr = lj_force_r(pq.x, pq.y, ir6, inv_r2);
+        two_sum_acc(A.fxs, A.fxc, pin ? rmul(fr, dx) : 0.0f);
+        two_sum_acc(A.fys, A.fyc, pin ? rmul(fr, dy) : 0.0f);
+        two_sum_acc(A.fzs, A.fzc, pin ? rmul(fr, dz) : 0.0f);
+        return;
+    }
     if (!(pin || cin)) return;
     float inv_r = rsqrtf(r2);
     float inv_r2 = rmul(inv_r, inv_r);
