@@ -331,7 +331,11 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
                 int2 nt = stencil_table(sd, si, local, b.cell_start, lane, s_lo[wib], s_pre[wib]);
                 const int nruns = nt.x, total = nt.y;
                 __syncwarp();
+                // (in registers: the row stores below could alias the system record)
                 const float rl2 = sd.rlist2_f;
+                const float Lq[3] = {sd.Lq[0], sd.Lq[1], sd.Lq[2]};
+                const int maxnb = b.maxnb;
+                int* const nbr = b.nbr;
                 const unsigned below = (1u << lane) - 1u;
                 for (int a0 = lo; a0 < hi; a0 += 32) {  // the cell's atoms, 32 at a time
                     const int na = min(32, hi - a0);
@@ -358,11 +362,11 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
 #pragma unroll
                             for (int h = 0; h < 4; h++) {  // candidate order: chunk by chunk
                                 if (base + 32 * h >= total) break;  // (the same in every lane)
-                                bool keep = slot[h] >= 0 && slot[h] != t && fixed_dist2(ui, uj[h], sd.Lq) < rl2;
+                                bool keep = slot[h] >= 0 && slot[h] != t && fixed_dist2(ui, uj[h], Lq) < rl2;
                                 unsigned mask = __ballot_sync(0xffffffffu, keep);
                                 if (keep) {
                                     int pos = at + __popc(mask & below);
-                                    if (pos < b.maxnb) b.nbr[(size_t)t * b.maxnb + pos] = slot[h];
+                                    if (pos < maxnb) nbr[(size_t)t * maxnb + pos] = slot[h];
                                 }
                                 at += __popc(mask);
                             }
@@ -370,8 +374,8 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
                         }
                     }
                     if (lane < na) {
-                        b.nnb[a0 + lane] = min(count, b.maxnb);
-                        if (count > b.maxnb) {
+                        b.nnb[a0 + lane] = min(count, maxnb);
+                        if (count > maxnb) {
                             atomicOr(b.status, ST_OVERFLOW);
                             a.group_flag[g] = 1;
                         }
