@@ -110,6 +110,9 @@ struct PkArgs {
     double4_32a* cp_acc;
 };
 constexpr int PK_STAGE_MAX = 9216;  // atoms a group may stage (20 bytes each)
+// one-kind Lennard-Jones batches stage positions only (16 bytes each) in the
+// same shared-memory limit
+constexpr int PK_STAGE_MAX_LJ1 = 11264;
 cudaError_t launch_md_persist(const Batch& b, const PkArgs& a, int cluster, cudaStream_t st);
 int persist_max_clusters(int tpa, int cluster, int stage_atoms);
 size_t persist_smem_bytes(int stage_atoms);

@@ -399,7 +399,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
                     int r = pk_find(s_apre, G, v);
                     int t = b.sys[s_sys[r]].begin + (v - s_apre[r]);
                     s_pos[v] = b.posfx[t];
-                    s_kind[v] = b.km[t].x;
+                    if (!LJ1) s_kind[v] = b.km[t].x;
                 }
                 __syncthreads();
             }
@@ -470,9 +470,9 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
                 walk_row<TPA>(
                     list, cnt, sub,
                     [&](int js, uint4& pj, int2& kmj) {
-                        if (!LJ1 && a.stage) {
+                        if (a.stage) {
                             pj = s_pos[js - off];
-                            kmj = make_int2(s_kind[js - off], 0);
+                            kmj = make_int2(LJ1 ? 0 : s_kind[js - off], 0);
                         } else {  // (the neighbour's kind is not needed for one kind)
                             pj = b.posfx[js];
                             kmj = (LJ1 || single) ? make_int2(0, 0) : b.km[js];
@@ -538,7 +538,7 @@ cudaError_t launch_persist_tpa(const Batch& b, const PkArgs& a, int cluster, cud
     cfg.blockDim = dim3(PK_THREADS, 1, 1);
     // (the shared-memory limit of the kernel was raised to PK_STAGE_MAX atoms when
     // the plan queried its occupancy, so a launch needs no attribute call)
-    cfg.dynamicSmemBytes = persist_smem_bytes(a.stage);
+    cfg.dynamicSmemBytes = LJ1 ? (size_t)a.stage * sizeof(uint4) : persist_smem_bytes(a.stage);
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -551,8 +551,7 @@ cudaError_t launch_persist_tpa(const Batch& b, const PkArgs& a, int cluster, cud
 }
 template <int TPA>
 cudaError_t launch_persist_tpa(const Batch& b, const PkArgs& a, int cluster, cudaStream_t st) {
-    return b.lj1 && a.stage == 0 ? launch_persist_tpa<TPA, true>(b, a, cluster, st)
-                                 : launch_persist_tpa<TPA, false>(b, a, cluster, st);
+    return b.lj1 ? launch_persist_tpa<TPA, true>(b, a, cluster, st) : launch_persist_tpa<TPA, false>(b, a, cluster, st);
 }
 
 cudaError_t launch_md_persist(const Batch& b, const PkArgs& a, int cluster, cudaStream_t st) {
@@ -573,8 +572,10 @@ int max_clusters_tpa(int cluster, int stage_atoms) {
     cfg.blockDim = dim3(PK_THREADS, 1, 1);
     cfg.dynamicSmemBytes = persist_smem_bytes(stage_atoms);
     if (cfg.dynamicSmemBytes > 0 &&
-        cudaFuncSetAttribute(md_persist_kernel<TPA, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)cfg.dynamicSmemBytes) != cudaSuccess) {
+        (cudaFuncSetAttribute(md_persist_kernel<TPA, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)cfg.dynamicSmemBytes) != cudaSuccess ||
+         cudaFuncSetAttribute(md_persist_kernel<TPA, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)cfg.dynamicSmemBytes) != cudaSuccess)) {
         cudaGetLastError();
         return 0;
     }

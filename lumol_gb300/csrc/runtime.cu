@@ -610,7 +610,8 @@ int persist_plan(lg_engine* e) {
         for (int k = off[g]; k < off[g + 1]; k++) atoms += (int)e->sys[sys[k]].n;
         stage = std::max(stage, atoms);
     }
-    e->pk_stage = (stage <= PK_STAGE_MAX && (e->opt.flags & LG_OPT_STAGING)) ? stage : 0;
+    const int stage_max = e->b.lj1 ? PK_STAGE_MAX_LJ1 : PK_STAGE_MAX;
+    e->pk_stage = (stage <= stage_max && (e->opt.flags & LG_OPT_STAGING)) ? stage : 0;
     cudaStream_t st = e->stream;
     CUDA_TRY(e, e->pk_group_off.alloc(off.size()));
     CUDA_TRY(e, e->pk_group_sys.alloc(sys.size()));

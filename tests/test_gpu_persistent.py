@@ -30,10 +30,10 @@ def launches(batch):
     return count.value
 
 
-def run(persistent, thermostats, calls, tpa=4):
+def run(persistent, thermostats, calls, tpa=4, staging=False):
     """Both paths with the same threads per atom, so every force sum runs in the same order."""
     systems = replicas()
-    batch = Batch(systems, precision="mixed", persistent=persistent, threads_per_atom=tpa)
+    batch = Batch(systems, precision="mixed", persistent=persistent, threads_per_atom=tpa, staging=staging)
     batch.md_setup([1.0] * len(systems), thermostats)
     for k in calls:
         before = launches(batch)
@@ -52,6 +52,18 @@ def test_persistent_matches_per_step_kernels(thermo, tpa):
     calls = [1, 40, 7, 300]  # run lengths across and inside the 256-step launches
     a = run(True, thermostats, calls, tpa)
     b = run(False, thermostats, calls, tpa)
+    for (pa, va), (pb, vb) in zip(a, b):
+        assert np.array_equal(pa, pb) and np.array_equal(va, vb)
+
+
+def test_staged_positions_match_per_step_kernels():
+    """LG_OPT_STAGING: every block copies its group's fixed-point positions into
+    shared memory each step and gathers neighbours from there; the
+    trajectories are the per-step kernels' bit for bit."""
+    thermostats = [(t, 100.0) if k % 2 == 0 else None for k, (n, rho, t) in enumerate(PARAMS)]
+    calls = [40, 300]
+    a = run(True, thermostats, calls, 2, staging=True)
+    b = run(False, thermostats, calls, 2)
     for (pa, va), (pb, vb) in zip(a, b):
         assert np.array_equal(pa, pb) and np.array_equal(va, vb)
 
