@@ -118,30 +118,42 @@ __device__ __forceinline__ double butterfly_tree(const double* a, int cnt) {
 }
 
 // Kinetic energy of a mixed-path system from its atoms' kinetic energies at
-// their cell-sorted positions: chunks of gpw sorted positions summed as the
-// persistent kernel sums them, then the chunks as chunk_ke_sum adds them, so
-// both MD paths derive the same thermostat factor.  (Not inlined: the tree
-// registers stay out of the integration kernels.)
-static __device__ __noinline__ double sorted_ke_sum(const SysDev& s, const double* ke, int gpw, int lane) {
-    int n = s.end - s.begin;
-    int nq = (n + gpw - 1) / gpw;
+// their cell-sorted positions: chunks of G sorted positions summed as the
+// persistent kernel sums them, then the chunks as chunk_ke_sum adds them
+// (lane-strided, in increasing order, then a butterfly), so both MD paths
+// derive the same thermostat factor.  A pass computes 32 / G chunks a lane,
+// their loads issued together, and adds them in order: one L2 round trip a
+// pass instead of one a chunk.
+template <int G>
+__device__ double sorted_ke_sum_g(const SysDev& s, const double* ke, int lane) {
+    constexpr int U = G >= 32 ? 1 : 32 / G;
+    const int n = s.end - s.begin;
+    const int nq = (n + G - 1) / G;
     double k = 0.0;
-    for (int q = lane; q < nq; q += 32) {
-        const double* a = ke + s.begin + (size_t)q * gpw;
-        int cnt = min(gpw, n - q * gpw);
-        double c;
-        switch (gpw) {
-            case 1: c = butterfly_tree<1>(a, cnt); break;
-            case 2: c = butterfly_tree<2>(a, cnt); break;
-            case 4: c = butterfly_tree<4>(a, cnt); break;
-            case 8: c = butterfly_tree<8>(a, cnt); break;
-            case 16: c = butterfly_tree<16>(a, cnt); break;
-            default: c = butterfly_tree<32>(a, cnt); break;
+    for (int q0 = lane; q0 < nq; q0 += 32 * U) {
+        double c[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int q = q0 + 32 * u;
+            c[u] = q < nq ? butterfly_tree<G>(ke + s.begin + (size_t)q * G, min(G, n - q * G)) : 0.0;
         }
-        k += c;
+#pragma unroll
+        for (int u = 0; u < U; u++)
+            if (q0 + 32 * u < nq) k += c[u];
     }
     for (int o = 16; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
     return k;
+}
+// (Not inlined: the tree registers stay out of the integration kernels.)
+static __device__ __noinline__ double sorted_ke_sum(const SysDev& s, const double* ke, int gpw, int lane) {
+    switch (gpw) {
+        case 1: return sorted_ke_sum_g<1>(s, ke, lane);
+        case 2: return sorted_ke_sum_g<2>(s, ke, lane);
+        case 4: return sorted_ke_sum_g<4>(s, ke, lane);
+        case 8: return sorted_ke_sum_g<8>(s, ke, lane);
+        case 16: return sorted_ke_sum_g<16>(s, ke, lane);
+        default: return sorted_ke_sum_g<32>(s, ke, lane);
+    }
 }
 
 // The thermostat factor and RemoveTranslation's centre-of-mass velocity of
