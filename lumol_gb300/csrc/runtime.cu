@@ -270,7 +270,10 @@ int upload_positions(lg_engine* e, int32_t s, const double* positions) {
 // checkpoint restores afterwards; the lists the trials built stay valid for
 // the restored positions (the rebuild test is relative to each list's build
 // positions).
-static int tune_persistent(lg_engine* e, cudaEvent_t e0, cudaEvent_t e1) {
+// *planned: whether some width got a persistent plan (else the batch runs on the
+// per-step kernels, which the caller then tunes).
+static int tune_persistent(lg_engine* e, cudaEvent_t e0, cudaEvent_t e1, bool* planned) {
+    *planned = false;
     cudaStream_t st = e->stream;
     const bool thermo = (md_mode(e) & MD_ADJUST) != 0;
     const size_t bytes = (size_t)e->b.n * sizeof(double4_32a);
@@ -304,6 +307,7 @@ static int tune_persistent(lg_engine* e, cudaEvent_t e0, cudaEvent_t e1) {
     e->nonfinite = false;
     e->b.tpa = best_tpa;
     e->pk_cluster = 0;  // planned again for the chosen width at the next run
+    *planned = best_t < 1e30f;
     return LG_OK;
 }
 
@@ -353,14 +357,16 @@ int autotune(lg_engine* e) {
         return best;
     };
     const bool pb = std::get<5>(key);
+    bool planned = false;
     if (pb) {
-        int rc = tune_persistent(e, e0, e1);
+        int rc = tune_persistent(e, e0, e1, &planned);
         if (rc) {
             cudaEventDestroy(e0);
             cudaEventDestroy(e1);
             return rc;
         }
-    } else {
+    }
+    if (!planned) {
         const int tpas[6] = {1, 2, 4, 8, 16, 32};
         int best_tpa = b.tpa;
         float best_t = 1e30f;
