@@ -459,7 +459,7 @@ void enqueue_md_finish(lg_engine* e, int mode, cudaStream_t st) {
 
 // ---- persistent batched MD -------------------------------------------------------
 // A batch the persistent kernel can run: mixed precision, pair potentials
-// only, Velocity-Verlet with at most a Berendsen thermostat.  It also needs a group size of 2, 4 or 8 threads per atom (the
+// only, Velocity-Verlet with at most a Berendsen thermostat.  It also needs a group size of 1, 2, 4 or 8 threads per atom (the
 // per-step kernel's, so both paths sum every force in the same order).
 bool persist_batch(const lg_engine* e) {
     const Batch& b = e->b;
