@@ -154,13 +154,14 @@ typedef struct {
 
 /* lg_options.flags.  Batches of mixed-precision systems with pair potentials
    only (no bonds, restrictions or Coulomb) run MD in one persistent launch per
-   lg_md_run chunk, one thread-block cluster per group of systems; this flag
-   keeps them on the per-step kernels instead. */
+   lg_md_run chunk of up to 256 steps (runs of 4 or more steps, or any run of
+   a batch of at most four systems), one thread-block cluster per group of
+   systems; this flag keeps them on the per-step kernels instead. */
 #define LG_OPT_NO_PERSISTENT 1
 /* Every block of the persistent kernel stages its group's positions in shared
    memory for the neighbour gathers (by default they go through L1, which
-   keeps more of the neighbour list cached; measured equal on the batched LJ
-   workload). */
+   keeps more of the neighbour list cached; measured 5 % slower on the batched
+   LJ workload, where the copy each step costs more than it saves). */
 #define LG_OPT_STAGING 2
 /* Bits 4-7 of lg_options.flags fix the cluster size of the persistent kernel
    (the value is log2(size) + 1, so 1, 2, 3, 4 select 1, 2, 4, 8 blocks);
