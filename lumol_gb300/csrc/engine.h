@@ -178,6 +178,7 @@ struct lg_engine {
     DBuf<float2> tablef;  // the same in FP32 (mixed path)
     DBuf<KVecF> kvecf;
     DBuf<float2> eikrf, rhof;
+    DBuf<float> qf;
     DBuf<SysDev> sysdev;
     DBuf<PairDev> ptab;
     DBuf<KVecDev> kvec;

@@ -90,6 +90,7 @@ struct Batch {
     KVecF* kvecf = nullptr;
     float2* eikrf = nullptr;
     float2* rhof = nullptr;
+    float* qf = nullptr;          // n: FP32 charges of the Ewald systems (written with e^{ik.r}, mixed path)
 };
 
 // persist.cu: batched MD of pairs-only systems, one persistent launch per run of steps

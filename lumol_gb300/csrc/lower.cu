@@ -902,6 +902,7 @@ int commit(lg_engine* e) {
     CUDA_TRY(e, e->kvecf.alloc(nkv));
     CUDA_TRY(e, e->eikrf.alloc(mixed && nkv ? (size_t)kdim * 3 * n : 1));
     CUDA_TRY(e, e->rhof.alloc(nkv));
+    CUDA_TRY(e, e->qf.alloc(mixed && nkv ? n : 1));
     CUDA_TRY(e, e->kvec.alloc(nkv));
     CUDA_TRY(e, e->eikr.alloc(nkv ? (size_t)kdim * 3 * n : 1));
     CUDA_TRY(e, e->rho.alloc(nkv));
@@ -1076,6 +1077,7 @@ int commit(lg_engine* e) {
     b.kvecf = e->kvecf.p;
     b.eikrf = e->eikrf.p;
     b.rhof = e->rhof.p;
+    b.qf = e->qf.p;
     if (any_carry) {
         std::vector<unsigned long long> count(nsys, 0ull);
         std::vector<uint32_t> status(nsys, 0u);

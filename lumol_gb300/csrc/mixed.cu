@@ -167,13 +167,14 @@ __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
 }
 
 __global__ void eikr_mixed_kernel(int n, const double4_32a* __restrict__ posq, const int* __restrict__ sysid,
-                                  const SysDev* __restrict__ sys, float2* __restrict__ eikr) {
+                                  const SysDev* __restrict__ sys, float2* __restrict__ eikr, float* __restrict__ qf) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 3 * n) return;
     int axis = t / n, i = t - axis * n;
     const SysDev& s = sys[sysid[i]];
     if (s.coul != 1) return;
     double4_32a p = posq[i];
+    if (axis == 0) qf[i] = (float)p.w;  // the charge in FP32, as the real-space pairs use it
     double phase = axis_phase(s, axis, p.x, p.y, p.z);
     phase -= 2.0 * PI * rint(phase * (0.5 / PI));
     float sn, cs;
@@ -195,7 +196,7 @@ __device__ __forceinline__ float2 eikrf_at(const float2* __restrict__ eikr, int 
 }
 
 template <bool EV>
-__global__ void __launch_bounds__(256) rho_mixed_kernel(int n, const double4_32a* __restrict__ posq,
+__global__ void __launch_bounds__(256) rho_mixed_kernel(int n, const float* __restrict__ qf,
                                                         const SysDev* __restrict__ sys,
                                                         const KVecDev* __restrict__ kvec,
                                                         const float2* __restrict__ eikr, double2* __restrict__ rho,
@@ -204,16 +205,24 @@ __global__ void __launch_bounds__(256) rho_mixed_kernel(int n, const double4_32a
     int k = blockIdx.x;
     KVecDev kv = kvec[k];
     const SysDev& s = sys[kv.sys];
-    double re = 0.0, im = 0.0;
+    // each thread's terms q e^{ik.r} summed in FP32 without rounding error to
+    // speak of: the exact product q ph = p + e (e from an FMA), p into a
+    // TwoSum, e into its compensation; the threads' sums then meet in FP64.
+    // (FP64 arithmetic here ran on GB300's narrow FP64 pipe: four FP64
+    // operations a term against about thirty FP32 ones.)
+    float rs = 0.f, rc = 0.f, is = 0.f, ic = 0.f;
     for (int i = s.begin + threadIdx.x; i < s.end; i += blockDim.x) {
         float2 ph = cmulf(cmulf(eikrf_at(eikr, n, kv.ikx, 0, i), eikrf_at(eikr, n, kv.iky, 1, i)),
                           eikrf_at(eikr, n, kv.ikz, 2, i));
-        double q = posq[i].w;
-        re += q * (double)ph.x;
-        im += q * (double)ph.y;
+        const float q = qf[i];
+        const float px = __fmul_rn(q, ph.x), py = __fmul_rn(q, ph.y);
+        two_sum_acc(rs, rc, px);
+        rc = __fadd_rn(rc, __fmaf_rn(q, ph.x, -px));
+        two_sum_acc(is, ic, py);
+        ic = __fadd_rn(ic, __fmaf_rn(q, ph.y, -py));
     }
-    sre[threadIdx.x] = re;
-    sim[threadIdx.x] = im;
+    sre[threadIdx.x] = (double)rs + (double)rc;
+    sim[threadIdx.x] = (double)is + (double)ic;
     __syncthreads();
     for (int o = blockDim.x / 2; o > 0; o >>= 1) {
         if ((int)threadIdx.x < o) {
@@ -269,13 +278,13 @@ __global__ void __launch_bounds__(128) field_mixed_kernel(int n, int kchunk, con
 void launch_kspace_mixed_part(const Batch& b, int part, bool ev, cudaStream_t st) {
     if (b.nkvec == 0 || b.n == 0) return;
     if (part == 0) {
-        eikr_mixed_kernel<<<(3 * b.n + 255) / 256, 256, 0, st>>>(b.n, b.posq, b.sysid, b.sys, b.eikrf);
+        eikr_mixed_kernel<<<(3 * b.n + 255) / 256, 256, 0, st>>>(b.n, b.posq, b.sysid, b.sys, b.eikrf, b.qf);
     } else if (part == 1) {
         if (ev)
-            rho_mixed_kernel<true><<<b.nkvec, 256, 0, st>>>(b.n, b.posq, b.sys, b.kvec, b.eikrf, b.rho, b.rhof,
+            rho_mixed_kernel<true><<<b.nkvec, 256, 0, st>>>(b.n, b.qf, b.sys, b.kvec, b.eikrf, b.rho, b.rhof,
                                                             b.kred);
         else
-            rho_mixed_kernel<false><<<b.nkvec, 256, 0, st>>>(b.n, b.posq, b.sys, b.kvec, b.eikrf, b.rho, b.rhof,
+            rho_mixed_kernel<false><<<b.nkvec, 256, 0, st>>>(b.n, b.qf, b.sys, b.kvec, b.eikrf, b.rho, b.rhof,
                                                              b.kred);
     } else {
         dim3 grid((b.n + 127) / 128, b.nkchunks);
