@@ -73,8 +73,9 @@ __device__ __forceinline__ void pk_lambdas(const Batch& b, const PkArgs& a, cons
 // written before a barrier and cleared after the rebuild's last barrier) and
 // the early exit on a list overflow (a per-group flag read after a barrier)
 // are the same in every block.
-// LJ1: every system has one kind and a Lennard-Jones pair and nothing is
-// staged (a force loop with those branches resolved when it is compiled).
+// LJ1: every system has one kind and a Lennard-Jones pair (a force loop with
+// the pair type and the one-kind parameters resolved when it is compiled, the
+// cutoff a select; staging, if asked for, holds positions only).
 template <int TPA, bool LJ1>
 __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkArgs a) {
     cg::cluster_group cluster = cg::this_cluster();
@@ -102,7 +103,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
     float4(*s_epa)[32] = reinterpret_cast<float4(*)[32]>(s_buf);
     int(*s_epi)[NL_RUNS] = s_lo;
     int(*s_epq)[NL_RUNS + 1] = s_pre;
-    extern __shared__ uint4 s_dyn[];  // staged positions (a.stage atoms), then their kinds
+    extern __shared__ uint4 s_dyn[];  // staged positions (a.stage atoms), then their kinds (not LJ1)
     uint4* s_pos = s_dyn;
     int* s_kind = reinterpret_cast<int*>(s_dyn + a.stage);
 
@@ -391,7 +392,7 @@ __global__ void __launch_bounds__(PK_THREADS, 1) md_persist_kernel(Batch b, PkAr
 
         // ---- 3: forces (compensated FP32 sums) fused with v += dt/2 a, a = F / m, kinetic energy
         {
-            // every block stages the group's fixed-point positions and kinds in
+            // every block stages the group's fixed-point positions (and kinds) in
             // shared memory (group order: the systems' sorted ranges one after
             // the other), so the neighbour gathers are shared-memory loads
             if (a.stage) {
