@@ -227,3 +227,40 @@ def test_autotuned_width_keeps_the_state():
         p, v = batch.state(s)
         assert np.all(np.isfinite(p)) and np.all(np.isfinite(v))
     batch.engine.close()
+
+
+def test_one_kind_lj_variant_matches_the_generic_kernels():
+    """Batches whose systems all have one kind and a Lennard-Jones pair run
+    force loops compiled for that case (per-step and persistent).  The same
+    replicas described with two kinds and the same parameters for every pair
+    take the generic kernels: forces and 60-step trajectories are equal bit
+    for bit."""
+    from lumol_gb300 import LennardJones, PairInteraction, System
+    from lumol_gb300.units import from_
+
+    def two_kinds(one):
+        s = System(one.cell, precision="mixed")
+        names = ["Ar" if k % 2 == 0 else "Xr" for k in range(one.size)]
+        s.add_particles(names, one.positions, masses=[39.948] * one.size)
+        lj = LennardJones(sigma=3.405, epsilon=from_(0.996, "kJ/mol"))
+        for pair in (("Ar", "Ar"), ("Ar", "Xr"), ("Xr", "Xr")):
+            s.set_pair_potential(pair, PairInteraction.shifted(lj, 2.5 * 3.405))
+        s.velocities = one.velocities.copy()
+        return s
+
+    params = [(500, 0.7, 120.0), (1200, 0.5, 200.0), (130, 0.8, 150.0)]
+    ones = [workloads.lj_replica(n, rho, t, 40 + k, "mixed") for k, (n, rho, t) in enumerate(params)]
+    twos = [two_kinds(s) for s in ones]
+    for a, b in zip(ones, twos):
+        fa, ea, wa = a.compute()
+        fb, eb, wb = b.compute()
+        assert np.array_equal(fa, fb) and ea == eb and np.array_equal(wa, wb)
+    states = []
+    for systems in (ones, twos):
+        batch = Batch(systems, precision="mixed", threads_per_atom=2)
+        batch.md_setup([1.0] * len(systems), [(t, 100.0) for _, _, t in params])
+        batch.md_run(60)
+        states.append([batch.state(s) for s in range(len(systems))])
+        batch.engine.close()
+    for (pa, va), (pb, vb) in zip(*states):
+        assert np.array_equal(pa, pb) and np.array_equal(va, vb)
