@@ -77,6 +77,7 @@ struct Batch {
     int tpa = 32;                 // threads per atom of the pair kernels (autotuned)
     int pair_general = 1;         // 0: pair potentials only, no restriction and no Coulomb in the batch
     int lj1 = 0;                  // 1: every system has one kind and a Lennard-Jones pair (a specialised force loop)
+    int norestr = 0;              // 1: no pair or Coulomb restriction in the batch (a specialised general kernel)
     uint4* posfx = nullptr;       // wrapped positions as 32-bit fractions of L, charge bits (cell order)
     uint4* pfx_build = nullptr;   // n: fixed-point positions at the last list build (atom order, mixed path)
     // plain path: half-list evaluation.  Rows are sorted by neighbour index;

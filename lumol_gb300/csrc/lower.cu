@@ -1069,6 +1069,9 @@ int commit(lg_engine* e) {
     // a triclinic cell's minimum image is in the general kernels only (and
     // keeps its batch off the persistent kernel)
     for (int s = 0; s < nsys; s++) b.pair_general |= e->h_sysdev[s].tric ? 1 : 0;
+    b.norestr = 1;
+    for (const PairDevF& q : h_ptabf) b.norestr &= (q.type == 0 || q.restriction == 0) ? 1 : 0;
+    for (int s = 0; s < nsys; s++) b.norestr &= (e->h_sysdev[s].coul_restr == 0 && !e->h_sysdev[s].tric) ? 1 : 0;
     b.lj1 = nsys > 0 ? 1 : 0;
     for (int s = 0; s < nsys; s++) {
         const SysDev& d = e->h_sysdev[s];

@@ -30,7 +30,7 @@ namespace lg {
 // LJ1: every system of the batch has one kind and a Lennard-Jones pair (the
 // pair type and the one-kind parameters resolved when the kernel is compiled;
 // the arithmetic, and so every force bit, is the generic kernel's).
-template <int TPA, bool EV, bool GENERAL, bool LJ1 = false>
+template <int TPA, bool EV, bool GENERAL, bool LJ1 = false, bool NORESTR = false>
 __global__ void __launch_bounds__(256, GENERAL && !EV ? 4 : 1) pair_mixed_kernel(
     int n, const uint4* __restrict__ pfx, const int2* __restrict__ km, const int* __restrict__ order,
     const int* __restrict__ sysid, const SysDev* __restrict__ sys,
@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(256, GENERAL && !EV ? 4 : 1) pair_mixed_kernel
             kmj = need_km ? km[js] : make_int2(0, 0);
         },
         [&](int js, const uint4& pj, const int2& kmj) {
-            mixed_entry<EV, GENERAL, LJ1>(A, s, prow, pi, qi, kmi.y, i, tt, js, pj, kmj, order, spec_off, spec_j,
+            mixed_entry<EV, GENERAL, LJ1, NORESTR>(A, s, prow, pi, qi, kmi.y, i, tt, js, pj, kmj, order, spec_off, spec_j,
                                      spec_path, pairs, coul, coul_rc2, alpha, pref, single, ph1, pq1, posq);
         });
     // combine the group's compensated sums; one lane converts to FP64
@@ -107,24 +107,25 @@ __global__ void __launch_bounds__(256, GENERAL && !EV ? 4 : 1) pair_mixed_kernel
     }
 }
 
-template <int TPA, bool GENERAL, bool LJ1 = false>
+template <int TPA, bool GENERAL, bool LJ1 = false, bool NORESTR = false>
 void launch_pair_mixed_variant(const Batch& b, uint32_t terms, bool ev, cudaStream_t st) {
     int tb = 256;
     long long threads = (long long)b.n * TPA;
     unsigned grid = (unsigned)((threads + tb - 1) / tb);
     if (ev)
-        pair_mixed_kernel<TPA, true, GENERAL, LJ1><<<grid, tb, 0, st>>>(
+        pair_mixed_kernel<TPA, true, GENERAL, LJ1, NORESTR><<<grid, tb, 0, st>>>(
             b.n, b.posfx, b.km, b.cell_atoms, b.sysid, b.sys, b.ptabf, b.nbr, b.nnb, b.maxnb, b.spec_off, b.spec_j,
             b.spec_path, terms, b.force, b.red, b.posq);
     else
-        pair_mixed_kernel<TPA, false, GENERAL, LJ1><<<grid, tb, 0, st>>>(
+        pair_mixed_kernel<TPA, false, GENERAL, LJ1, NORESTR><<<grid, tb, 0, st>>>(
             b.n, b.posfx, b.km, b.cell_atoms, b.sysid, b.sys, b.ptabf, b.nbr, b.nnb, b.maxnb, b.spec_off, b.spec_j,
             b.spec_path, terms, b.force, b.red, b.posq);
 }
 
 template <int TPA>
 void launch_pair_mixed_tpa(const Batch& b, uint32_t terms, bool ev, cudaStream_t st) {
-    if (b.pair_general) launch_pair_mixed_variant<TPA, true>(b, terms, ev, st);
+    if (b.pair_general && b.norestr) launch_pair_mixed_variant<TPA, true, false, true>(b, terms, ev, st);
+    else if (b.pair_general) launch_pair_mixed_variant<TPA, true>(b, terms, ev, st);
     else if (b.lj1) launch_pair_mixed_variant<TPA, false, true>(b, terms, ev, st);
     else launch_pair_mixed_variant<TPA, false>(b, terms, ev, st);
 }

@@ -124,7 +124,9 @@ struct MixedAcc {
 // (GENERAL) restrictions and real-space Coulomb, added to the lane's sums.
 // LJ1: a system of one kind with a Lennard-Jones pair (the parameters are
 // ph1 / pq1), known when the kernel is compiled; the arithmetic is the same.
-template <bool EV, bool GENERAL, bool LJ1 = false>
+// NORESTR: no pair and no Coulomb restriction in the batch (the restriction
+// code compiled out; the arithmetic is the same).
+template <bool EV, bool GENERAL, bool LJ1 = false, bool NORESTR = false>
 __device__ __forceinline__ void mixed_entry(
     MixedAcc& A, const SysDev& s, const PairDevF* __restrict__ prow, uint4 pi, float qi, int mi, int i, int tt,
     int js, uint4 pj, int2 kmj, const int* __restrict__ order, const int* __restrict__ spec_off,
@@ -187,7 +189,7 @@ __device__ __forceinline__ void mixed_entry(
         int mj = kmj.y;
         float sc = 1.0f;
         const PairDevF& p = *pp;
-        if (pin && ph.y != 0) {
+        if (!NORESTR && pin && ph.y != 0) {
             path = ph.y <= 2 ? (mi != mj ? 0 : 5) : bond_path(i, order[js], mi, mj, spec_off, spec_j, spec_path);
             if (restriction_excluded(ph.y, path)) pin = false;
             else sc = ph.y == 6 && path == 4 ? p.scale14 : 1.0f;
@@ -200,7 +202,7 @@ __device__ __forceinline__ void mixed_entry(
         if (cin) {
             bool excl = false;
             float csc = 1.0f;
-            if (s.coul_restr != 0) {
+            if (!NORESTR && s.coul_restr != 0) {
                 if (path < 0 || (s.coul_restr > 2 && path == 5))
                     path = s.coul_restr <= 2 ? (mi != mj ? 0 : 5)
                                              : bond_path(i, order[js], mi, mj, spec_off, spec_j, spec_path);
@@ -212,7 +214,7 @@ __device__ __forceinline__ void mixed_entry(
             float ar = rmul(alpha, r);
             if (s.coul == 1) {
                 float g = rmul(rmul(alpha, (float)FRAC_2_SQRT_PI), __expf(rmul(-ar, ar)));
-                if (excl) {
+                if (!NORESTR && excl) {
                     // an excluded (bonded) pair's -erf correction (ewald.rs:394-397,
                     // 411-427) in FP64, from the FP64 positions and charges: these
                     // terms (three per water molecule) all have one sign and a
